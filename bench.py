@@ -1,0 +1,417 @@
+#!/usr/bin/env python3
+"""Benchmark of the VoxelPathTracer hot path on one GB300 (or N replicas).
+
+Workload (the full-frame configuration): a 256^3 uint8 world from the seeded
+value-noise generator, a 100-block table (5% emissive), 1920x1080 at 1 spp:
+primary ray, sun-shadow ray, one cosine-weighted diffuse bounce with its
+shadow ray, then SVGF (pre-temporal 3x3, temporal, variance, 5 a-trous
+iterations) and the colour pass. One step = one frame; the camera drifts a
+little every frame so the temporal pass reprojects real motion.
+
+`value` is DF-DDA rays per second over the whole denoised frame (trace +
+SVGF + shade inside the timed region, inputs resident in HBM); `frame_ms` is
+the denoised frame time. `e2e` is the same metric through the public C ABI
+call vpt_render_frame with the image copied to pinned host memory every step.
+The L2 is flushed (a 512 MiB write) between timed steps.
+
+--impl reference times the reference's algorithm on the host cores: the CPU
+restatement of the shaders (the reference itself is GLSL and cannot run
+without an OpenGL context), OpenMP over all host threads, on a bounded band
+of rows of the same frame.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+METRIC = "rays/s DF-DDA + denoised 1080p frame ms, batched/learned vs plain at same error"
+WORLD = (256, 256, 256)
+RES = (1920, 1080)
+CAM_POS = (128.0, 90.0, 128.0)
+ALG_BYTES_PER_STEP = 32     # one 32-byte sector per DF gather
+ALG_BYTES_PER_RAY = 16      # ray output
+PEAKS_FILE = REPO / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-reduction over replicas (gloo over TCP; no data-path collective)."""
+
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peak_hbm():
+    try:
+        d = json.loads(PEAKS_FILE.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def workload_inputs(vpt, seed=0):
+    X, Y, Z = WORLD
+    vox = vpt.generate_world(X, Y, Z, seed=seed)
+    blocks = vpt.generate_block_table(100, seed=seed)
+    yaw, pitch = vpt.seeded_pose(seed)
+    return vox, blocks, yaw, pitch
+
+
+def camera_at(vpt, yaw, pitch, step):
+    # a slow pan: 0.25 degree of yaw and 0.05 voxel of travel per frame
+    W, H = RES
+    pos = (CAM_POS[0] + 0.05 * step, CAM_POS[1], CAM_POS[2])
+    return vpt.camera_from_pose(pos, yaw + 0.25 * step, pitch, 90.0, W / H)
+
+
+def frame_at(vpt, step):
+    return vpt.default_frame(frame_index=step, seed=0, time=1.0 + step / 60.0)
+
+
+# ------------------------------------------------------------- our arm --
+def run_ours(args):
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    import voxelpathtracer_gb300 as vpt
+
+    dist = Dist(world)
+    W, H = RES
+    vox, blocks, yaw, pitch = workload_inputs(vpt, seed=rank)
+    ctx = vpt.Context(width=W, height=H, device=local, storage=args.storage)
+    ctx.upload_world(vox)
+    ctx.set_block_table(blocks)
+    ctx.build_df()
+    ctx.synchronize()
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+    total = args.warmup + args.steps
+
+    # 1) counting pass (untimed): rays and DDA steps per frame of the same sequence
+    ctx.set_stats(True)
+    rays, steps = [], []
+    for s in range(total):
+        ctx.render_frame(camera_at(vpt, yaw, pitch, s), frame_at(vpt, s), readback=False)
+        st = ctx.read_stats()
+        rays.append(st["rays"])
+        steps.append(st["steps"])
+    ctx.set_stats(False)
+    ctx.reset_history()
+
+    # 2) device-resident timed run
+    ctx.set_profiling(True)
+    pass_ms = {p: [] for p in vpt.PASSES}
+    times = []
+    with torch.cuda.stream(stream):
+        for s in range(args.warmup):
+            ctx.render_frame(camera_at(vpt, yaw, pitch, s), frame_at(vpt, s), readback=False)
+        torch.cuda.synchronize()
+        dist.barrier()
+        clocks = ClockSampler(local)
+        clocks.start()
+        launches0 = ctx.launch_count()
+        for s in range(args.warmup, total):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.render_frame(camera_at(vpt, yaw, pitch, s), frame_at(vpt, s), readback=False)
+            b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+            for k, v in ctx.pass_times().items():
+                pass_ms[k].append(v)
+        launches = ctx.launch_count() - launches0
+        torch.cuda.synchronize()
+        dist.barrier()
+        clk = clocks.stop()
+    ctx.set_profiling(False)
+
+    timed = slice(args.warmup, total)
+    frame_rays = [sum(r.values()) for r in rays[timed]]
+    t_total = dist.max(sum(times) / 1e3)
+    rays_total = dist.sum(float(sum(frame_rays)))
+    ms_per_step = t_total * 1e3 / args.steps
+    value = rays_total / t_total
+    trace_ms = sum(sum(pass_ms[p]) for p in ("primary", "shadow", "diffuse"))
+    trace_rays_per_s = sum(frame_rays) / (trace_ms / 1e3)
+
+    # dominant kernel: the pass with the largest device time
+    mean_pass = {k: (sum(v) / len(v) if v else 0.0) for k, v in pass_ms.items()}
+    dom = max(mean_pass, key=mean_pass.get)
+    kinds = {"primary": ["primary"], "shadow": ["shadow"], "diffuse": ["diffuse", "bounce_shadow"]}
+    if dom in kinds:
+        per_launch_bytes = np.mean([sum(st[k] for k in kinds[dom]) * ALG_BYTES_PER_STEP +
+                                    sum(r[k] for k in kinds[dom]) * ALG_BYTES_PER_RAY
+                                    for st, r in zip(steps[timed], rays[timed])])
+    else:
+        per_launch_bytes = float("nan")
+    achieved = per_launch_bytes / (mean_pass[dom] / 1e3) / 1e9
+    peak, peak_kind = peak_hbm()
+
+    # 3) end-to-end through the C ABI with host buffers (pinned)
+    ctx.reset_history()
+    out = torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True)
+    out_np = out.numpy()
+    for s in range(args.warmup):
+        ctx.render_frame(camera_at(vpt, yaw, pitch, s), frame_at(vpt, s), out=out_np)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for s in range(args.warmup, total):
+        cam = camera_at(vpt, yaw, pitch, s)
+        fr = frame_at(vpt, s)
+        ctx.render_frame(cam, fr, out=out_np)
+    e2e_t = dist.max(time.perf_counter() - t0)
+    e2e_value = rays_total / e2e_t
+    h2d = len(bytes(memoryview(vpt.Camera()))) + len(bytes(memoryview(vpt.Frame())))
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(vpt, args, vox, blocks, yaw, pitch, sample_rows=args.cpu_rows)
+    ctx.close()
+    dist.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "rays/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "frame_ms": ms_per_step,
+        "trace_rays_per_s": trace_rays_per_s,
+        "rays_per_frame": float(np.mean(frame_rays)),
+        "pass_ms": {k: round(v, 4) for k, v in mean_pass.items()},
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32" if args.storage == 0 else "f16-storage/f32",
+        "data": "synthetic",
+        "config": {"workload": "full frame 1920x1080, 256^3 world (seed 0), 1 spp + sun shadow + 1 bounce "
+                               "(+ bounce shadow), SVGF temporal + variance + 5 a-trous, colour pass",
+                   "world": list(WORLD), "resolution": list(RES), "spp": 1, "bounces": 1,
+                   "storage": "fp32" if args.storage == 0 else "fp16",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "flushed (512 MiB write) between timed steps"},
+        "e2e": {"value": e2e_value, "unit": "rays/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": W * H * 3 * 4, "ms_per_step": e2e_t * 1e3 / args.steps,
+                "api": "vpt_render_frame -> pinned host RGB"},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": f"trace_{dom}" if dom in kinds else dom,
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": args.traffic,
+                     "algorithmic_bytes_per_launch": per_launch_bytes},
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------- CPU (oracle) arm --
+def cpu_band_frame(vpt, oracle, wobj, yaw, pitch, step, rows):
+    """Primary + sun shadow + diffuse traces of rows [r0, r1) of frame `step`
+    on the host cores. Returns (seconds, DF-DDA rays traced)."""
+    W, H = RES
+    cfg = vpt.default_config(width=W, height=H)
+    cam = camera_at(vpt, yaw, pitch, step)
+    fr = frame_at(vpt, step)
+    with oracle.Counting() as cnt:
+        t0 = time.perf_counter()
+        g = oracle.trace_primary(wobj, cam, cfg, rows=rows)
+        oracle.trace_shadow(wobj, cam, cfg, fr, g["t"], g["face"], rows=rows)
+        oracle.trace_diffuse(wobj, cam, cfg, fr, g["t"], g["face"], rows=rows)
+        dt = time.perf_counter() - t0
+    return dt, sum(cnt.rays.values())
+
+
+def band_rows(n):
+    W, H = RES
+    r0 = H // 2 - n // 2
+    return (r0, r0 + n)
+
+
+def cpu_baseline(vpt, args, vox, blocks, yaw, pitch, sample_rows=48):
+    import oracle
+    W, H = RES
+    rows = band_rows(sample_rows)
+    wobj = oracle.World(vox, oracle.build_df(vox), blocks)
+    dt, rays = cpu_band_frame(vpt, oracle, wobj, yaw, pitch, 0, rows)
+    return {"value": rays / dt, "unit": "rays/s", "cores": oracle.omp_threads(), "kind": "port",
+            "sample": f"rows {rows[0]}..{rows[1] - 1} of frame 0 ({sample_rows * W} pixels): primary + sun shadow + "
+                      f"diffuse + bounce-shadow rays of the CPU restatement, {rays} rays in {dt:.2f} s"}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    import voxelpathtracer_gb300 as vpt
+    W, H = RES
+    vox, blocks, yaw, pitch = workload_inputs(vpt, seed=0)
+    rows = band_rows(args.cpu_rows)
+    wobj = oracle.World(vox, oracle.build_df(vox), blocks)
+    times, rays = [], []
+    for s in range(args.warmup + args.steps):
+        dt, n = cpu_band_frame(vpt, oracle, wobj, yaw, pitch, s, rows)
+        if s >= args.warmup:
+            times.append(dt)
+            rays.append(n)
+    value = sum(rays) / sum(times)
+    sample = (f"rows {rows[0]}..{rows[1] - 1} of each 1920x1080 frame ({args.cpu_rows * W} pixels): primary, sun "
+              f"shadow, diffuse and bounce-shadow rays of the CPU restatement")
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "rays/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "full frame 1920x1080, 256^3 world (seed 0), 1 spp + sun shadow + 1 bounce "
+                               "(+ bounce shadow); a bounded band of rows per step",
+                   "world": list(WORLD), "resolution": list(RES)},
+        "cpu_baseline": {"value": value, "unit": "rays/s", "cores": oracle.omp_threads(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference implements this path in GLSL behind OpenGL, which cannot run here; its CPU "
+                "restatement (oracle/) is timed on the host cores instead",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--storage", type=int, default=0, help="0 = fp32 planes, 1 = fp16 planes")
+    ap.add_argument("--cpu-rows", type=int, default=48)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per launch of the dominant kernel from an ncu capture")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,241 @@
+/* libvpt -- GB300-native VoxelPathTracer hot path, C ABI.
+ *
+ * The reference (swr06/VoxelPathTracer) drives its hot path from
+ * Core/Pipeline.cpp through OpenGL objects: a voxel 3-D texture and a block
+ * table SSBO go in, framebuffer colour attachments come out. This header is
+ * the drop-in boundary for those passes: the same contracts over device
+ * buffers owned by a context, plain pointers and sizes, no C++ or torch types.
+ *
+ * Conventions
+ *   - Every call returns vpt_status; nothing throws across the ABI.
+ *   - One context per host thread. Calls are ordered on the context's CUDA
+ *     stream; calls that return data to host memory synchronise it.
+ *   - Voxel volumes are uint8 block ids (0 = air), x fastest:
+ *     index = x + X*(y + Y*z) (Core/World.h:46-49).
+ *   - Image planes are W*H pixels, row 0 at the bottom (OpenGL convention),
+ *     channels interleaved per pixel.
+ *   - Matrices are column-major float[16] (glm layout).
+ */
+#ifndef VPT_H
+#define VPT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VPT_ABI_VERSION 1
+
+typedef enum vpt_status {
+    VPT_OK = 0,
+    VPT_ERR_INVALID_ARG = 1,     /* bad pointer, size or enum value */
+    VPT_ERR_OOM = 2,             /* device or host allocation failed */
+    VPT_ERR_DEVICE_TIMEOUT = 3,  /* a bounded device-side wait gave up */
+    VPT_ERR_CUDA = 4,            /* a CUDA runtime call failed */
+    VPT_ERR_STATE = 5,           /* call out of order (e.g. trace before a world) */
+    VPT_ERR_NO_DEVICE = 6        /* no usable CUDA device */
+} vpt_status;
+
+typedef enum vpt_storage {
+    VPT_STORAGE_F32 = 0,         /* plain path: fp32 planes */
+    VPT_STORAGE_F16 = 1          /* precision variant: fp16 planes, fp32 arithmetic */
+} vpt_storage;
+
+typedef struct vpt_ctx vpt_ctx;
+
+/* Frame-loop settings; the reference keeps these as static globals at the
+ * top of Core/Pipeline.cpp (:17-320). */
+typedef struct vpt_config {
+    int32_t width, height;           /* G-buffer and GI resolution */
+    int32_t primary_max_steps;       /* u_RenderDistance (Core/Pipeline.cpp:55, clamped to 350 at :4824) */
+    int32_t shadow_max_steps;        /* 350 (ShadowRayTraceFrag.glsl:233) */
+    int32_t diffuse_max_steps;       /* u_DiffuseTraceLength = 48 (Core/Pipeline.cpp:75) */
+    int32_t bounce_shadow_max_steps; /* 128 (DiffuseRayTraceFrag.glsl:1220) */
+    int32_t bounces;                 /* MAX_BOUNCE_LIMIT (DiffuseRayTraceFrag.glsl:17) */
+    int32_t spp;                     /* u_SPP */
+    int32_t storage;                 /* vpt_storage */
+    int32_t atrous_iterations;       /* 5 (Core/Pipeline.cpp:2499) */
+    float resolution_scale;          /* u_ResolutionScale (DiffuseIndirectSuperSampleRes, :79) */
+    float color_phi_bias;            /* ColorPhiBias = 3.325 (:85) */
+    int32_t device;                  /* CUDA device ordinal */
+    int32_t reserved[3];
+} vpt_config;
+
+/* Camera uniforms: u_View, u_Projection, u_InverseView, u_InverseProjection
+ * and u_ViewerPosition as Core/Pipeline.cpp sets them per pass. */
+typedef struct vpt_camera {
+    float view[16];
+    float proj[16];
+    float inv_view[16];
+    float inv_proj[16];
+    float position[3];
+    float pad;
+} vpt_camera;
+
+/* One block-table entry. Replaces the BlockDataSSBO texture-layer arrays
+ * (Core/BlockDataSSBO.cpp:9-35) with flat material values. */
+typedef struct vpt_block {
+    uint8_t albedo[3];
+    uint8_t roughness;
+    uint8_t metalness;
+    uint8_t emissive;                /* 0 or 1 */
+} vpt_block;
+
+/* Per-frame uniforms of the trace, filter and colour passes. */
+typedef struct vpt_frame {
+    float sun_dir[3];                /* normalised, towards the sun (u_SunDirection) */
+    float time;                      /* u_Time in seconds (filter jitter noise) */
+    float sun_radiance[3];           /* colour-pass sun colour (SAMPLED_SUN_COLOR) */
+    uint32_t frame_index;            /* per-pixel random stream index */
+    float moon_radiance[3];          /* colour-pass moon colour */
+    uint32_t seed;                   /* random seed */
+    float gi_sun_strength;           /* GISunStrength = 1.0 (Core/Pipeline.cpp:280) */
+    float gi_sky_strength;           /* GISkyStrength = 1.125 (:281) */
+    float diffuse_light_intensity;   /* DiffuseLightIntensity = 1.25 (:74) */
+    int32_t temporal;                /* DO_SVGF_TEMPORAL -> u_BeUseful */
+} vpt_frame;
+
+/* Image planes owned by the context (see vpt_plane_info for sizes). */
+typedef enum vpt_plane {
+    VPT_PLANE_T = 0,          /* hit distance (o_HitDistance), storage type, 1 ch */
+    VPT_PLANE_FACE = 1,       /* face id 0..5 (+Z,-Z,+Y,-Y,-X,+X), 10 = miss; u8 */
+    VPT_PLANE_BLOCK = 2,      /* block id at the hit, 0 = miss; u8 */
+    VPT_PLANE_HIT = 3,        /* ivec3(floor(origin)) at loop exit; i32 x3 */
+    VPT_PLANE_STEPS = 4,      /* DDA iterations; u16 */
+    VPT_PLANE_SHADOW = 5,     /* sun shadow 0/1; u8 */
+    VPT_PLANE_GI_SH = 6,      /* DiffuseRawTraceFBO: SH (4), CoCg (2), luma (1), AO+sky (2) */
+    VPT_PLANE_GI_COCG = 7,
+    VPT_PLANE_GI_LUMA = 8,
+    VPT_PLANE_GI_AOSKY = 9,
+    VPT_PLANE_PRE_SH = 10,    /* DiffusePreTemporal_SpatialFBO */
+    VPT_PLANE_PRE_COCG = 11,
+    VPT_PLANE_PRE_LUMA = 12,
+    VPT_PLANE_PRE_AOSKY = 13,
+    VPT_PLANE_TEMP_SH = 14,   /* DiffuseTemporalFBO of this frame; util = frames, moment, luma, 0 */
+    VPT_PLANE_TEMP_COCG = 15,
+    VPT_PLANE_TEMP_UTIL = 16,
+    VPT_PLANE_TEMP_AOSKY = 17,
+    VPT_PLANE_HIST_SH = 18,   /* PrevDiffuseTemporalFBO (history from the last frame) */
+    VPT_PLANE_HIST_COCG = 19,
+    VPT_PLANE_HIST_UTIL = 20,
+    VPT_PLANE_HIST_AOSKY = 21,
+    VPT_PLANE_PREV_T = 22,    /* InitialTraceFBOPrev */
+    VPT_PLANE_PREV_FACE = 23,
+    VPT_PLANE_PREV_BLOCK = 24,
+    VPT_PLANE_VAR_SH = 25,    /* VarianceFBO */
+    VPT_PLANE_VAR_COCG = 26,
+    VPT_PLANE_VAR_VARIANCE = 27,
+    VPT_PLANE_DEN_SH = 28,    /* output of the last a-trous iteration */
+    VPT_PLANE_DEN_COCG = 29,
+    VPT_PLANE_DEN_VARIANCE = 30,
+    VPT_PLANE_DEN_AOSKY = 31,
+    VPT_PLANE_COLOR = 32,     /* ColoredFBO: RGB radiance */
+    VPT_PLANE_COUNT = 33
+} vpt_plane;
+
+typedef enum vpt_dtype { VPT_DTYPE_F32 = 0, VPT_DTYPE_F16 = 1, VPT_DTYPE_U8 = 2, VPT_DTYPE_U16 = 3, VPT_DTYPE_I32 = 4 } vpt_dtype;
+
+/* Counters filled while statistics are enabled (vpt_set_stats). */
+typedef struct vpt_stats {
+    uint64_t rays[4];                /* primary, sun shadow, diffuse, bounce shadow */
+    uint64_t steps[4];               /* DDA iterations per ray kind */
+} vpt_stats;
+
+/* Per-pass device times of the last frame, from CUDA events on the
+ * context stream (vpt_set_profiling). */
+typedef enum vpt_pass {
+    VPT_PASS_PRIMARY = 0, VPT_PASS_SHADOW = 1, VPT_PASS_DIFFUSE = 2, VPT_PASS_SPATIAL_INITIAL = 3,
+    VPT_PASS_TEMPORAL = 4, VPT_PASS_VARIANCE = 5, VPT_PASS_ATROUS = 6, VPT_PASS_SHADE = 7,
+    VPT_PASS_COUNT = 8
+} vpt_pass;
+
+/* ------------------------------------------------------------- lifetime -- */
+const char* vpt_status_string(vpt_status s);
+int vpt_abi_version(void);
+/* Defaults of the reference's frame loop at BASELINE sizes (1920x1080, 1 spp, 1 bounce). */
+vpt_status vpt_default_config(vpt_config* cfg);
+vpt_status vpt_default_frame(vpt_frame* frame);
+/* Replaces MainPipeline::StartPipeline's FBO creation (Core/Pipeline.cpp:1094-1158, :1690-1735). */
+vpt_status vpt_create(vpt_ctx** out, const vpt_config* cfg);
+vpt_status vpt_destroy(vpt_ctx* ctx);
+const char* vpt_last_error(const vpt_ctx* ctx);
+
+/* ----------------------------------------------------------------- world -- */
+/* World::Buffer -> Texture3D::CreateTexture (Core/World.h:167-171, Core/Texture3D.cpp:19-27):
+ * copies X*Y*Z voxels to the device. Dimensions are runtime values (the
+ * reference fixes them at compile time, Core/Macros.h:3-5). */
+vpt_status vpt_upload_world(vpt_ctx* ctx, const uint8_t* voxels, int32_t X, int32_t Y, int32_t Z);
+/* BlockDataSSBO::CreateBuffers (Core/BlockDataSSBO.cpp:5-37); n <= 256. */
+vpt_status vpt_set_block_table(vpt_ctx* ctx, const vpt_block* table, int32_t n);
+/* World::GenerateDistanceField (Core/World.cpp:69-113). */
+vpt_status vpt_build_df(vpt_ctx* ctx);
+vpt_status vpt_read_df(vpt_ctx* ctx, uint8_t* host_df, size_t bytes);
+/* Context-free form: device pointers in and out, ordered on `stream`
+ * (a cudaStream_t, 0 = legacy default stream). The device must be current. */
+vpt_status vpt_df_build_device(const uint8_t* d_voxels, uint8_t* d_df, int32_t X, int32_t Y, int32_t Z, void* stream);
+
+/* ---------------------------------------------------------------- passes -- */
+/* Initial trace pass, Core/Pipeline.cpp:1959-2016 (InitialRayTraceFrag.glsl):
+ * fills T, FACE, BLOCK, HIT, STEPS. Stores `cam` as this frame's camera. */
+vpt_status vpt_trace_primary(vpt_ctx* ctx, const vpt_camera* cam);
+/* Sun shadow pass, Core/Pipeline.cpp:2790-2850 (ShadowRayTraceFrag.glsl): fills SHADOW. */
+vpt_status vpt_trace_shadow(vpt_ctx* ctx, const vpt_frame* frame);
+/* Diffuse GI pass, Core/Pipeline.cpp:2169-2281 (DiffuseRayTraceFrag.glsl): fills GI_*. */
+vpt_status vpt_trace_diffuse(vpt_ctx* ctx, const vpt_frame* frame);
+/* SVGF, Core/Pipeline.cpp:2284-2615: Spatial3x3Initial, temporal, variance
+ * and the a-trous iterations. `prev_cam` is the previous frame's camera
+ * (u_PrevView / u_PrevProjection); history planes are read and written. */
+vpt_status vpt_svgf(vpt_ctx* ctx, const vpt_camera* prev_cam, const vpt_frame* frame);
+/* Colour pass, Core/Pipeline.cpp:3603-3821 (ColorPassFrag.glsl): fills COLOR. */
+vpt_status vpt_shade(vpt_ctx* ctx, const vpt_frame* frame);
+/* Ping-pong swap of the G-buffer and temporal history (Core/Pipeline.cpp:1775-1788, :1970-1971). */
+vpt_status vpt_end_frame(vpt_ctx* ctx);
+/* Clears the history so the next frame starts without reprojection. */
+vpt_status vpt_reset_history(vpt_ctx* ctx);
+/* One whole frame: primary, shadow, diffuse, SVGF, shade, end_frame. If
+ * rgb_out is not NULL the COLOR plane is copied to it as float32 RGB
+ * (W*H*3 floats) and the call waits for it. prev_cam may be NULL on the
+ * first frame (the camera of the previous call is used otherwise). */
+vpt_status vpt_render_frame(vpt_ctx* ctx, const vpt_camera* cam, const vpt_frame* frame, float* rgb_out);
+
+/* ---------------------------------------------------------------- planes -- */
+vpt_status vpt_plane_info(const vpt_ctx* ctx, int32_t plane, size_t* bytes, int32_t* channels, int32_t* dtype);
+vpt_status vpt_read_plane(vpt_ctx* ctx, int32_t plane, void* host, size_t bytes);
+vpt_status vpt_write_plane(vpt_ctx* ctx, int32_t plane, const void* host, size_t bytes);
+/* Device address of a plane (for callers that keep data on the GPU). */
+vpt_status vpt_plane_device_ptr(vpt_ctx* ctx, int32_t plane, void** dptr);
+
+/* ------------------------------------------------------ instrumentation -- */
+vpt_status vpt_synchronize(vpt_ctx* ctx);
+vpt_status vpt_set_stats(vpt_ctx* ctx, int32_t enabled);
+vpt_status vpt_read_stats(vpt_ctx* ctx, vpt_stats* out);   /* synchronises, then zeroes */
+vpt_status vpt_set_profiling(vpt_ctx* ctx, int32_t enabled);
+vpt_status vpt_read_pass_times(vpt_ctx* ctx, float* ms, int32_t n);   /* synchronises */
+/* Kernels launched by this context since it was created. */
+vpt_status vpt_launch_count(const vpt_ctx* ctx, uint64_t* out);
+/* The context's stream as a cudaStream_t. */
+vpt_status vpt_get_stream(const vpt_ctx* ctx, void** stream);
+
+/* Deterministic math used by every kernel (exp, exp2, log2, pow, sin, cos as
+ * op 0..5), evaluated on the device (on_device = 1) or on the host; lets a
+ * caller check that both give identical bits. y is only read for pow. */
+vpt_status vpt_detmath(int32_t op, const float* x, const float* y, float* out, int32_t n, int32_t on_device);
+
+/* ---------------------------------------------------------- host helpers -- */
+/* Seeded value-noise terrain (heightmap h = 40 + 16*fbm, 4 octaves, base
+ * frequency 1/64, gain 0.5; grass top, three dirt layers, stone below) with
+ * surface blocks 4..n_blocks-1 scattered on 1 column in 16. Host only. */
+vpt_status vpt_generate_world(uint8_t* out, int32_t X, int32_t Y, int32_t Z, uint64_t seed, int32_t n_blocks);
+/* Seeded flat block table: albedo, roughness, metalness uniform, 5% emissive. */
+vpt_status vpt_generate_block_table(vpt_block* out, int32_t n, uint64_t seed);
+/* glm::lookAt / glm::perspective camera as Core/FpsCamera.cpp:14-24 builds it
+ * (front from yaw/pitch in degrees), inverses in double precision. */
+vpt_status vpt_camera_from_pose(vpt_camera* out, const float position[3], float yaw_deg, float pitch_deg,
+                                float fov_deg, float aspect, float znear, float zfar);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VPT_H */

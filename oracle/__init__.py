@@ -1,0 +1,312 @@
+"""CPU oracle for the VoxelPathTracer hot path (ctypes binding).
+
+TEST INFRASTRUCTURE ONLY. The oracle is a C++17 restatement of the reference
+shaders (see vpt_oracle.h for the file list and vpt_oracle.cpp for the
+per-function citations). Only the tests, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py use it, as the checker or as the timed CPU
+baseline; the product (voxelpathtracer_gb300) never imports it.
+
+Parity is unpinned by the reference itself (it has no tests, golden vectors
+or CPU implementation of this path); the oracle is pinned by analytic
+known-answer tests and brute-force cross-checks under tests/.
+
+Struct layouts are byte-compatible with include/vpt.h, so any ctypes
+structure of the same size (e.g. voxelpathtracer_gb300.Camera) is accepted.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libvpt_oracle.so"
+
+
+class OCamera(C.Structure):
+    _fields_ = [("view", C.c_float * 16), ("proj", C.c_float * 16), ("inv_view", C.c_float * 16),
+                ("inv_proj", C.c_float * 16), ("position", C.c_float * 3), ("pad", C.c_float)]
+
+
+class OFrame(C.Structure):
+    _fields_ = [("sun_dir", C.c_float * 3), ("time", C.c_float), ("sun_radiance", C.c_float * 3),
+                ("frame_index", C.c_uint32), ("moon_radiance", C.c_float * 3), ("seed", C.c_uint32),
+                ("gi_sun_strength", C.c_float), ("gi_sky_strength", C.c_float),
+                ("diffuse_light_intensity", C.c_float), ("temporal", C.c_int32)]
+
+
+class OParams(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("primary_max_steps", C.c_int32),
+                ("shadow_max_steps", C.c_int32), ("diffuse_max_steps", C.c_int32),
+                ("bounce_shadow_max_steps", C.c_int32), ("bounces", C.c_int32), ("spp", C.c_int32),
+                ("storage", C.c_int32), ("atrous_iterations", C.c_int32), ("resolution_scale", C.c_float),
+                ("color_phi_bias", C.c_float), ("device", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+class OWorld(C.Structure):
+    _fields_ = [("vox", C.c_void_p), ("df", C.c_void_p), ("X", C.c_int32), ("Y", C.c_int32), ("Z", C.c_int32),
+                ("blocks", C.c_void_p), ("n_blocks", C.c_int32)]
+
+
+class OGBuffer(C.Structure):
+    _fields_ = [("t", C.c_void_p), ("face", C.c_void_p), ("block", C.c_void_p), ("hit", C.c_void_p),
+                ("steps", C.c_void_p)]
+
+
+class OPlanes4(C.Structure):   # vpto_gi / vpto_history / vpto_filtered share this shape
+    _fields_ = [("a", C.c_void_p), ("b", C.c_void_p), ("c", C.c_void_p), ("d", C.c_void_p)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            from voxelpathtracer_gb300 import _build   # build helper only; the oracle code is in this folder
+            _build.build_oracle()
+        L = C.CDLL(str(LIB_PATH))
+        P = C.c_void_p
+        L.vpto_build_df.argtypes = [P, C.c_int, C.c_int, C.c_int, P]
+        L.vpto_trace_primary.argtypes = [P, P, P, C.c_int, C.c_int, P]
+        L.vpto_trace_shadow.argtypes = [P, P, P, P, P, P, C.c_int, C.c_int, P]
+        L.vpto_trace_diffuse.argtypes = [P, P, P, P, P, P, C.c_int, C.c_int, P]
+        L.vpto_spatial_initial.argtypes = [P, P, P, P, P, P]
+        L.vpto_temporal.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, P]
+        L.vpto_variance.argtypes = [P, P, P, P, P, P]
+        L.vpto_atrous.argtypes = [P, P, P, C.c_int, P, P, P, P, P, P]
+        L.vpto_shade.argtypes = [P, P, P, P, P, P, P, P, P, P, P, C.c_int, C.c_int, P]
+        for name in ("vpto_exp", "vpto_exp2", "vpto_log2", "vpto_sin", "vpto_cos", "vpto_half_round"):
+            getattr(L, name).argtypes = [C.c_float]
+            getattr(L, name).restype = C.c_float
+        L.vpto_pow.argtypes = [C.c_float, C.c_float]
+        L.vpto_pow.restype = C.c_float
+        L.vpto_omp_threads.restype = C.c_int
+        L.vpto_set_counters.argtypes = [P]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _as(cls, obj):
+    if isinstance(obj, cls):
+        return obj
+    if C.sizeof(obj) != C.sizeof(cls):
+        raise TypeError(f"{type(obj).__name__} is not layout-compatible with {cls.__name__}")
+    return cls.from_buffer_copy(bytes(memoryview(obj)))
+
+
+def omp_threads() -> int:
+    return lib().vpto_omp_threads()
+
+
+class Counting:
+    """Context manager that counts the oracle's rays and DDA steps."""
+
+    KINDS = ("primary", "shadow", "diffuse", "bounce_shadow")
+
+    def __enter__(self):
+        self.buf = np.zeros(8, dtype=np.uint64)
+        lib().vpto_set_counters(_p(self.buf))
+        return self
+
+    def __exit__(self, *exc):
+        lib().vpto_set_counters(None)
+
+    @property
+    def rays(self) -> dict:
+        return {k: int(v) for k, v in zip(self.KINDS, self.buf[:4])}
+
+    @property
+    def steps(self) -> dict:
+        return {k: int(v) for k, v in zip(self.KINDS, self.buf[4:])}
+
+
+def build_df(vox: np.ndarray) -> np.ndarray:
+    v = np.ascontiguousarray(vox, dtype=np.uint8)
+    Z, Y, X = v.shape
+    df = np.empty_like(v)
+    lib().vpto_build_df(_p(v), X, Y, Z, _p(df))
+    return df
+
+
+class World:
+    """Voxels + distance field + block table, kept alive for the C calls."""
+
+    def __init__(self, vox: np.ndarray, df: np.ndarray, blocks: np.ndarray):
+        self.vox = np.ascontiguousarray(vox, dtype=np.uint8)
+        self.df = np.ascontiguousarray(df, dtype=np.uint8)
+        self.blocks = np.ascontiguousarray(blocks)
+        Z, Y, X = self.vox.shape
+        self.s = OWorld(self.vox.ctypes.data, self.df.ctypes.data, X, Y, Z, self.blocks.ctypes.data,
+                        int(self.blocks.size))
+
+
+def params(config) -> OParams:
+    return _as(OParams, config)
+
+
+def _planes(H, W, spec):
+    return {k: np.zeros((H, W, c) if c > 1 else (H, W), dtype=dt) for k, (c, dt) in spec.items()}
+
+
+def trace_primary(world: World, cam, config, rows=None) -> dict:
+    p = params(config)
+    H, W = p.height, p.width
+    g = _planes(H, W, {"t": (1, np.float32), "face": (1, np.uint8), "block": (1, np.uint8),
+                       "hit": (3, np.int32), "steps": (1, np.uint16)})
+    r0, r1 = rows if rows else (0, H)
+    gb = OGBuffer(_p(g["t"]), _p(g["face"]), _p(g["block"]), _p(g["hit"]), _p(g["steps"]))
+    lib().vpto_trace_primary(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), r0, r1, C.byref(gb))
+    return g
+
+
+def trace_shadow(world: World, cam, config, frame, t, face, rows=None) -> np.ndarray:
+    p = params(config)
+    H, W = p.height, p.width
+    out = np.zeros((H, W), dtype=np.uint8)
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    face = np.ascontiguousarray(face, dtype=np.uint8)
+    r0, r1 = rows if rows else (0, H)
+    lib().vpto_trace_shadow(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)),
+                            _p(t), _p(face), r0, r1, _p(out))
+    return out
+
+
+GI_SPEC = {"sh": (4, np.float32), "cocg": (2, np.float32), "luma": (1, np.float32), "aosky": (2, np.float32)}
+HIST_SPEC = {"sh": (4, np.float32), "cocg": (2, np.float32), "util": (4, np.float32), "aosky": (2, np.float32)}
+FILT_SPEC = {"sh": (4, np.float32), "cocg": (2, np.float32), "variance": (1, np.float32), "aosky": (2, np.float32)}
+
+
+def _struct4(d, keys):
+    return OPlanes4(*[_p(d[k]) if d.get(k) is not None else None for k in keys])
+
+
+def _f32(d, keys):
+    return {k: np.ascontiguousarray(d[k], dtype=np.float32) for k in keys if d.get(k) is not None}
+
+
+def trace_diffuse(world: World, cam, config, frame, t, face, rows=None) -> dict:
+    p = params(config)
+    H, W = p.height, p.width
+    out = _planes(H, W, GI_SPEC)
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    face = np.ascontiguousarray(face, dtype=np.uint8)
+    r0, r1 = rows if rows else (0, H)
+    s = _struct4(out, ["sh", "cocg", "luma", "aosky"])
+    lib().vpto_trace_diffuse(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)),
+                             _p(t), _p(face), r0, r1, C.byref(s))
+    return out
+
+
+def spatial_initial(cam, config, t, face, gi: dict) -> dict:
+    p = params(config)
+    out = _planes(p.height, p.width, GI_SPEC)
+    gi = _f32(gi, ["sh", "cocg", "luma", "aosky"])
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    face = np.ascontiguousarray(face, dtype=np.uint8)
+    sin, sout = _struct4(gi, ["sh", "cocg", "luma", "aosky"]), _struct4(out, ["sh", "cocg", "luma", "aosky"])
+    lib().vpto_spatial_initial(C.byref(_as(OCamera, cam)), C.byref(p), _p(t), _p(face), C.byref(sin), C.byref(sout))
+    return out
+
+
+def temporal(cam, prev_cam, config, frame, t, face, block, prev_t, prev_face, prev_block, cur: dict,
+             hist: dict) -> dict:
+    p = params(config)
+    out = _planes(p.height, p.width, HIST_SPEC)
+    cur = _f32(cur, ["sh", "cocg", "luma", "aosky"])
+    hist = _f32(hist, ["sh", "cocg", "util", "aosky"])
+    arrs = [np.ascontiguousarray(a, dtype=dt) for a, dt in
+            ((t, np.float32), (face, np.uint8), (block, np.uint8), (prev_t, np.float32), (prev_face, np.uint8),
+             (prev_block, np.uint8))]
+    sc, sh_, so = (_struct4(cur, ["sh", "cocg", "luma", "aosky"]), _struct4(hist, ["sh", "cocg", "util", "aosky"]),
+                   _struct4(out, ["sh", "cocg", "util", "aosky"]))
+    lib().vpto_temporal(C.byref(_as(OCamera, cam)), C.byref(_as(OCamera, prev_cam)), C.byref(p),
+                        C.byref(_as(OFrame, frame)), *[_p(a) for a in arrs], C.byref(sc), C.byref(sh_), C.byref(so))
+    return out
+
+
+def variance(cam, config, t, face, temporal_out: dict) -> dict:
+    p = params(config)
+    out = _planes(p.height, p.width, {k: v for k, v in FILT_SPEC.items() if k != "aosky"})
+    h = _f32(temporal_out, ["sh", "cocg", "util", "aosky"])
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    face = np.ascontiguousarray(face, dtype=np.uint8)
+    si, so = _struct4(h, ["sh", "cocg", "util", "aosky"]), _struct4(out, ["sh", "cocg", "variance", "aosky"])
+    lib().vpto_variance(C.byref(_as(OCamera, cam)), C.byref(p), _p(t), _p(face), C.byref(si), C.byref(so))
+    return out
+
+
+def atrous(cam, config, frame, step, t, face, temporal_util, filt_in: dict, aosky_in) -> dict:
+    p = params(config)
+    out = _planes(p.height, p.width, FILT_SPEC)
+    fi = _f32(filt_in, ["sh", "cocg", "variance"])
+    ao = np.ascontiguousarray(aosky_in, dtype=np.float32)
+    tu = np.ascontiguousarray(temporal_util, dtype=np.float32)
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    face = np.ascontiguousarray(face, dtype=np.uint8)
+    si, so = _struct4(fi, ["sh", "cocg", "variance", "aosky"]), _struct4(out, ["sh", "cocg", "variance", "aosky"])
+    lib().vpto_atrous(C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)), int(step), _p(t),
+                      _p(face), _p(tu), C.byref(si), _p(ao), C.byref(so))
+    return out
+
+
+def shade(world: World, cam, config, frame, t, face, block, shadow, sh, cocg, aosky, rows=None) -> np.ndarray:
+    p = params(config)
+    H, W = p.height, p.width
+    out = np.zeros((H, W, 3), dtype=np.float32)
+    arrs = [np.ascontiguousarray(a, dtype=dt) for a, dt in
+            ((t, np.float32), (face, np.uint8), (block, np.uint8), (shadow, np.uint8), (sh, np.float32),
+             (cocg, np.float32), (aosky, np.float32))]
+    r0, r1 = rows if rows else (0, H)
+    lib().vpto_shade(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)),
+                     *[_p(a) for a in arrs], r0, r1, _p(out))
+    return out
+
+
+def svgf(cam, prev_cam, config, frame, g: dict, prev_g: dict, gi: dict, hist: dict) -> dict:
+    """Spatial3x3Initial, temporal, variance and the a-trous iterations, as
+    Core/Pipeline.cpp:2284-2615 sequences them. Returns every intermediate."""
+    p = params(config)
+    pre = spatial_initial(cam, p, g["t"], g["face"], gi)
+    tmp = temporal(cam, prev_cam, p, frame, g["t"], g["face"], g["block"], prev_g["t"], prev_g["face"],
+                   prev_g["block"], pre, hist)
+    var = variance(cam, p, g["t"], g["face"], tmp)
+    cur = {"sh": var["sh"], "cocg": var["cocg"], "variance": var["variance"]}
+    ao = tmp["aosky"]
+    dens = []
+    for it in range(p.atrous_iterations):
+        step = max(16 >> it, 1)
+        den = atrous(cam, p, frame, step, g["t"], g["face"], tmp["util"], cur, ao)
+        dens.append(den)
+        cur, ao = den, den["aosky"]
+    return {"pre": pre, "temporal": tmp, "variance": var, "atrous": dens}
+
+
+def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist: dict) -> dict:
+    """One whole frame in the order of vpt_render_frame."""
+    p = params(config)
+    g = trace_primary(world, cam, p)
+    shadow = trace_shadow(world, cam, p, frame, g["t"], g["face"])
+    gi = trace_diffuse(world, cam, p, frame, g["t"], g["face"])
+    sv = svgf(cam, prev_cam, p, frame, g, prev_g, gi, hist)
+    if sv["atrous"]:
+        last = sv["atrous"][-1]
+        sh, cocg, ao = last["sh"], last["cocg"], last["aosky"]
+    else:
+        sh, cocg, ao = sv["variance"]["sh"], sv["variance"]["cocg"], sv["temporal"]["aosky"]
+    rgb = shade(world, cam, p, frame, g["t"], g["face"], g["block"], shadow, sh, cocg, ao)
+    return {"g": g, "shadow": shadow, "gi": gi, "svgf": sv, "rgb": rgb}
+
+
+def empty_history(H: int, W: int):
+    """The state libvpt starts from: previous G-buffer all misses, zero history."""
+    prev_g = {"t": np.full((H, W), -1.0, np.float32), "face": np.full((H, W), 10, np.uint8),
+              "block": np.zeros((H, W), np.uint8)}
+    hist = {"sh": np.zeros((H, W, 4), np.float32), "cocg": np.zeros((H, W, 2), np.float32),
+            "util": np.zeros((H, W, 4), np.float32), "aosky": np.zeros((H, W, 2), np.float32)}
+    return prev_g, hist

@@ -1,0 +1,1170 @@
+// CPU oracle for the VoxelPathTracer hot path.
+//
+// TEST INFRASTRUCTURE ONLY (see vpt_oracle.h): a C++17 restatement of the
+// reference shaders, used by the parity tests as the checker and by bench.py
+// as the timed CPU baseline. Build: g++ -O2 -fopenmp -ffp-contract=off.
+//
+// Conventions that the reference leaves to the OpenGL implementation are
+// fixed here and in the CUDA kernels alike:
+//   * pixel (i, j) has texture coordinate ((i+0.5)/W, (j+0.5)/H), row 0 at the
+//     bottom, exactly like gl_FragCoord / v_TexCoords of a full-screen quad;
+//   * texture() at a texel centre returns that texel (what the hardware's
+//     fixed-point addressing does); at other coordinates it is bilinear with
+//     REPEAT wrap (Core/GLClasses/Framebuffer.cpp:64-70) and fp32 weights;
+//     the R8 face and block planes are nearest-filtered
+//     (Core/Pipeline.cpp:1094);
+//   * int(NaN) = 0 and out-of-range conversions saturate (omath.h f2i);
+//   * normalize(v) = v / sqrt(dot(v, v)), dot sums left to right;
+//   * transcendental functions come from omath.h.
+// Documented substitutions (the reference's versions need textures):
+//   * block table: flat albedo RGB8, roughness u8, metalness u8, emissive flag;
+//   * sky: an analytic gradient instead of the atmosphere cubemap;
+//   * random numbers: PCG (Jarzynski & Olano 2020, "Hash Functions for GPU
+//     Rendering") seeded per pixel instead of fract(sin()) / blue noise;
+//   * no TAA jitter, no alpha testing, no checkerboard SPP, no player shadow,
+//     no specular/reflection input (its floor 0.0001 is kept).
+#include "vpt_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "omath.h"
+
+using namespace vpto;
+
+namespace {
+
+const float PI = 3.14159265359f;   // DiffuseRayTraceFrag.glsl:11, ColorPassFrag.glsl:6
+
+// Optional ray / DDA-step counters (primary, shadow, diffuse, bounce shadow),
+// same layout as vpt_stats; used by the CPU baseline to count its work.
+uint64_t* g_counters = nullptr;
+struct RowCount {
+    uint64_t rays[4] = {0, 0, 0, 0};
+    uint64_t steps[4] = {0, 0, 0, 0};
+    void add(int kind, int nsteps) { rays[kind] += 1; steps[kind] += (uint64_t)nsteps; }
+    void flush() {
+        if (!g_counters) return;
+        for (int k = 0; k < 4; k++) {
+#pragma omp atomic
+            g_counters[k] += rays[k];
+#pragma omp atomic
+            g_counters[4 + k] += steps[k];
+        }
+    }
+};
+
+inline size_t vidx(const vpto_world* w, int x, int y, int z) {
+    return (size_t)x + (size_t)w->X * ((size_t)y + (size_t)w->Y * (size_t)z);
+}
+
+// IsInVolume (InitialRayTraceFrag.glsl:68-77) on integer coordinates.
+inline bool in_volume(const vpto_world* w, int x, int y, int z) {
+    return !(x < 0 || y < 0 || z < 0 || x > w->X - 1 || y > w->Y - 1 || z > w->Z - 1);
+}
+
+// GetVoxel (InitialRayTraceFrag.glsl:79-87): block id, 0 outside.
+inline int get_voxel(const vpto_world* w, int x, int y, int z) {
+    return in_volume(w, x, y, z) ? (int)w->vox[vidx(w, x, y, z)] : 0;
+}
+
+// int(floor(ToConservativeEuclidean(Dist))) (InitialRayTraceFrag.glsl:89-92, :328-330).
+// texelFetch(R8)*255 returns the stored integer exactly for every byte value.
+inline int euclid_steps(int dist) {
+    float D = (float)dist;
+    float e = (D == 1.0f) ? 1.0f : D * 0.57735026918f;
+    return f2i(std::floor(e));
+}
+
+struct TraceResult {
+    float t;          // distance(origin, initial_origin) or -1
+    v3 normal;        // -RaySign[MinIdx] on MinIdx (valid when hit)
+    int block;        // GetVoxel at the end point (0 on miss)
+    int32_t cell[3];  // ivec3(floor(origin)) at loop exit
+    int steps;        // itr at loop exit
+};
+
+// VoxelTraversalDF: InitialRayTraceFrag.glsl:307-374 (identical copies at
+// ShadowRayTraceFrag.glsl:222-289 and DiffuseRayTraceFrag.glsl:1043-1110, the
+// latter with the step cap as a parameter).
+TraceResult traverse(const vpto_world* w, v3 origin, v3 direction, int max_steps) {
+    const v3 initial = origin;
+    bool intersection = false;
+    int min_idx = 0;
+    const int sgn[3] = {isign(direction.x), isign(direction.y), isign(direction.z)};
+    const int half[3] = {(1 + sgn[0]) >> 1, (1 + sgn[1]) >> 1, (1 + sgn[2]) >> 1};
+    const v3 inv = mk3(1.0f / direction.x, 1.0f / direction.y, 1.0f / direction.z);
+    int itr = 0;
+    for (itr = 0; itr < max_steps; itr++) {
+        int lx = f2i(std::floor(origin.x));
+        int ly = f2i(std::floor(origin.y));
+        int lz = f2i(std::floor(origin.z));
+        if (!in_volume(w, lx, ly, lz)) {
+            intersection = false;
+            break;
+        }
+        int e = euclid_steps((int)w->df[vidx(w, lx, ly, lz)]);
+        if (e == 0) break;
+        if (e == 1) {
+            // one exact DDA face step (:341-356)
+            int g[3] = {f2i(origin.x), f2i(origin.y), f2i(origin.z)};
+            v3 wv = mk3(origin.x - (float)g[0], origin.y - (float)g[1], origin.z - (float)g[2]);
+            v3 df = mk3(((float)half[0] - wv.x) * inv.x, ((float)half[1] - wv.y) * inv.y,
+                        ((float)half[2] - wv.z) * inv.z);
+            min_idx = (df.x < df.y && sgn[0] != 0) ? ((df.x < df.z || sgn[2] == 0) ? 0 : 2)
+                                                   : ((df.y < df.z || sgn[2] == 0) ? 1 : 2);
+            g[min_idx] += sgn[min_idx];
+            float dm = comp(df, min_idx);
+            wv = mk3(wv.x + direction.x * dm, wv.y + direction.y * dm, wv.z + direction.z * dm);
+            set_comp(&wv, min_idx, (float)(1 - half[min_idx]));
+            origin = mk3((float)g[0] + wv.x, (float)g[1] + wv.y, (float)g[2] + wv.z);
+            set_comp(&origin, min_idx, comp(origin, min_idx) + (float)sgn[min_idx] * 0.0001f);
+            intersection = true;
+        } else {
+            // jump by the conservative Euclidean radius (:361)
+            float k = (float)(e - 1);
+            origin = mk3(origin.x + k * direction.x, origin.y + k * direction.y,
+                         origin.z + k * direction.z);
+        }
+    }
+    TraceResult r;
+    r.cell[0] = f2i(std::floor(origin.x));
+    r.cell[1] = f2i(std::floor(origin.y));
+    r.cell[2] = f2i(std::floor(origin.z));
+    r.steps = itr;
+    r.normal = mk3(0.0f, 0.0f, 0.0f);
+    r.block = 0;
+    r.t = -1.0f;
+    if (intersection) {   // :365-371
+        set_comp(&r.normal, min_idx, (float)(-sgn[min_idx]));
+        r.block = get_voxel(w, r.cell[0], r.cell[1], r.cell[2]);
+        r.t = r.block > 0 ? length(sub(origin, initial)) : -1.0f;
+    }
+    return r;
+}
+
+// GetNormalID (InitialRayTraceFrag.glsl:143-185): exact compares, 0 when none match.
+int normal_id(v3 n) {
+    static const v3 N[6] = {{0, 0, 1}, {0, 0, -1}, {0, 1, 0}, {0, -1, 0}, {-1, 0, 0}, {1, 0, 0}};
+    for (int i = 0; i < 6; i++)
+        if (n.x == N[i].x && n.y == N[i].y && n.z == N[i].z) return i;
+    return 0;
+}
+
+// GetNormalFromID (e.g. SVGF/TemporalFilter.glsl:108-119); `miss` is what
+// ids > 5 decode to (vec3(1) in most shaders, vec3(0.5) in the diffuse pass).
+v3 normal_from_id(int id, float miss) {
+    static const v3 N[6] = {{0, 0, 1}, {0, 0, -1}, {0, 1, 0}, {0, -1, 0}, {-1, 0, 0}, {1, 0, 0}};
+    if (id > 5 || id < 0) return mk3(miss, miss, miss);
+    return N[id];
+}
+
+// ------------------------------------------------------------ camera rays --
+inline v2 texcoord(int i, int j, int W, int H) {
+    return v2{((float)i + 0.5f) / (float)W, ((float)j + 0.5f) / (float)H};
+}
+
+// GetRayDirectionAt (e.g. ShadowRayTraceFrag.glsl:303-308) / GetRayStuff
+// (InitialRayTraceFrag.glsl:398-414 without TAA jitter).
+inline v3 ray_dir_at(const vpto_camera* c, v2 uv) {
+    float cx = uv.x * 2.0f - 1.0f;
+    float cy = uv.y * 2.0f - 1.0f;
+    v4 e = mat_mul4(c->inv_proj, cx, cy, -1.0f, 1.0f);
+    v4 d = mat_mul4(c->inv_view, e.x, e.y, -1.0f, 0.0f);
+    return mk3(d.x, d.y, d.z);
+}
+
+inline v3 ray_origin(const vpto_camera* c) { return mk3(c->inv_view[12], c->inv_view[13], c->inv_view[14]); }
+
+// ------------------------------------------------------------- sampling --
+inline int wrapi(int i, int n) {
+    int r = i % n;
+    return r < 0 ? r + n : r;
+}
+
+struct Plane {
+    const float* p;
+    int W, H, C;
+    float at(int i, int j, int c) const {
+        return p[((size_t)wrapi(j, H) * W + wrapi(i, W)) * C + c];
+    }
+    // texture() with GL_LINEAR + GL_REPEAT, fp32 weights.
+    void linear(v2 uv, float* out) const {
+        float x = uv.x * (float)W - 0.5f;
+        float y = uv.y * (float)H - 0.5f;
+        float x0 = std::floor(x), y0 = std::floor(y);
+        float ax = x - x0, ay = y - y0;
+        int i0 = f2i(x0), j0 = f2i(y0);
+        for (int c = 0; c < C; c++) {
+            float v00 = at(i0, j0, c), v10 = at(i0 + 1, j0, c);
+            float v01 = at(i0, j0 + 1, c), v11 = at(i0 + 1, j0 + 1, c);
+            float b = v00 * (1.0f - ax) + v10 * ax;
+            float t = v01 * (1.0f - ax) + v11 * ax;
+            out[c] = b * (1.0f - ay) + t * ay;
+        }
+    }
+};
+
+struct Plane8 {
+    const uint8_t* p;
+    int W, H;
+    int at(int i, int j) const { return p[(size_t)wrapi(j, H) * W + wrapi(i, W)]; }
+    // texture() with GL_NEAREST + GL_REPEAT
+    int nearest(v2 uv) const {
+        return at(f2i(std::floor(uv.x * (float)W)), f2i(std::floor(uv.y * (float)H)));
+    }
+};
+
+inline float storage(float v, int fp16) { return fp16 ? half_round(v) : v; }
+
+// GetPositionAt at a texel centre (fetch) or at an arbitrary coordinate (linear).
+inline v4 position_fetch(const vpto_camera* c, const Plane& t, int i, int j, v2 txc) {
+    float d = t.at(i, j, 0);
+    v3 p = add(ray_origin(c), muls(normalize(ray_dir_at(c, txc)), d));
+    return v4{p.x, p.y, p.z, d};
+}
+inline v4 position_linear(const vpto_camera* c, const Plane& t, v2 txc) {
+    float d;
+    t.linear(txc, &d);
+    v3 p = add(ray_origin(c), muls(normalize(ray_dir_at(c, txc)), d));
+    return v4{p.x, p.y, p.z, d};
+}
+
+// ---------------------------------------------------------------- shading --
+inline float luminance(v3 c) { return dot(c, mk3(0.299f, 0.587f, 0.114f)); }   // GetLuminance
+inline float sh_to_y(const float* sh) { return fmaxg(0.0f, 3.544905f * sh[3]); }  // SHToY
+
+// Analytic sky standing in for the atmosphere cubemap: direction-only like a
+// cubemap lookup, horizon-to-zenith gradient.
+inline v3 sky_radiance(v3 d) {
+    v3 n = normalize(d);
+    float a = clampf(n.y, 0.0f, 1.0f);
+    return vmix(mk3(0.62f, 0.74f, 0.92f), mk3(0.20f, 0.38f, 0.85f), a);
+}
+
+// GetSkyColorAt (DiffuseRayTraceFrag.glsl:984-988)
+inline v3 sky_color_at(v3 rd) {
+    rd.y = clampf(rd.y, 0.125f, 1.5f);
+    return sky_radiance(rd);
+}
+
+// IrridianceToSH (DiffuseRayTraceFrag.glsl:766-784)
+inline void irradiance_to_sh(v3 r, v3 d, float* sh, float* cocg) {
+    float co = r.x - r.z;
+    float t = r.z + co * 0.5f;
+    float cg = r.y - t;
+    float y = fmaxg(t + cg * 0.5f, 0.0f);
+    float l00 = 0.282095f;
+    float l1_1 = 0.488603f * d.y;
+    float l10 = 0.488603f * d.z;
+    float l11 = 0.488603f * d.x;
+    sh[0] = fmaxg(l11 * y, -100.0f);
+    sh[1] = fmaxg(l1_1 * y, -100.0f);
+    sh[2] = fmaxg(l10 * y, -100.0f);
+    sh[3] = fmaxg(l00 * y, -100.0f);
+    cocg[0] = co;
+    cocg[1] = cg;
+}
+
+// SHToIrridiance (ColorPassFrag.glsl:357-368)
+inline v3 sh_to_irradiance(const float* sh, const float* cocg_in, v3 v) {
+    float x = dot(mk3(sh[0], sh[1], sh[2]), v);
+    float y = 2.0f * (1.023326f * x + 0.886226f * sh[3]);
+    y = fmaxg(y, 0.0f);
+    float s = (y * 0.282095f) / (sh[3] + 1e-6f);
+    float co = cocg_in[0] * s, cg = cocg_in[1] * s;
+    float t = y - cg * 0.5f;
+    float g = cg + t;
+    float b = t - co * 0.5f;
+    float r = b + co;
+    return vmax(mk3(r, g, b), 0.0f);
+}
+
+// InverseSchlick (DiffuseRayTraceFrag.glsl:1305-1308)
+inline float inverse_schlick(float f0, float voh) {
+    return 1.0f - clampf(f0 + (1.0f - f0) * dm_pow(1.0f - voh, 5.0f), 0.0f, 1.0f);
+}
+
+// DiffuseHammon (DiffuseRayTraceFrag.glsl:1311-1332); rcp(x) = 1/x.
+inline float diffuse_hammon(v3 n, v3 v, v3 l, float rough) {
+    float ndl = fmaxg(dot(n, l), 0.0f);
+    if (ndl <= 0.0f) return 0.0f;
+    float ndv = fmaxg(dot(n, v), 0.0f);
+    float ldv = fmaxg(dot(l, v), 0.0f);
+    v3 h = normalize(add(v, l));
+    float ndh = fmaxg(dot(n, h), 0.0f);
+    float facing = ldv * 0.5f + 0.5f;
+    float single_rough = facing * (0.9f - 0.4f * facing) * ((0.5f + ndh) * (1.0f / fmaxg(ndh, 0.02f)));
+    float single_smooth = 1.05f * inverse_schlick(0.0f, ndl) * inverse_schlick(0.0f, fmaxg(ndv, 0.0f));
+    float single = clampf(mixf(single_smooth, single_rough, rough) * (1.0f / PI), 0.0f, 1.0f);
+    float multi = 0.1159f * rough;
+    return clampf((multi + single) * ndl, 0.0f, 1.0f);
+}
+
+// ------------------------------------------------------------------- RNG --
+inline uint32_t pcg_step(uint32_t* s) {
+    *s = *s * 747796405u + 2891336453u;
+    uint32_t w = ((*s >> ((*s >> 28u) + 4u)) ^ *s) * 277803737u;
+    return (w >> 22u) ^ w;
+}
+inline uint32_t pcg_hash(uint32_t v) {
+    uint32_t s = v;
+    return pcg_step(&s);
+}
+inline float rand01(uint32_t* s) { return (float)(pcg_step(s) >> 8) * (1.0f / 16777216.0f); }
+inline uint32_t pixel_seed(const vpto_frame* f, uint32_t pixel) {
+    return pcg_hash(pixel + pcg_hash(f->frame_index + pcg_hash(f->seed)));
+}
+
+// cosWeightedRandomHemisphereDirection (DiffuseRayTraceFrag.glsl:945-967)
+inline v3 cos_hemisphere(v3 n, uint32_t* rng) {
+    float rx_ = rand01(rng);
+    float ry_ = rand01(rng);
+    float pi2 = 2.0f * PI;
+    v3 uu = normalize(cross(n, mk3(0.0f, 1.0f, 1.0f)));
+    v3 vv = cross(uu, n);
+    float ra = std::sqrt(ry_);
+    float rx = ra * dm_cos(pi2 * rx_);
+    float ry = ra * dm_sin(pi2 * rx_);
+    float rz = std::sqrt(1.0f - ry_);
+    v3 rr = mk3((rx * uu.x + ry * vv.x) + rz * n.x, (rx * uu.y + ry * vv.y) + rz * n.y,
+                (rx * uu.z + ry * vv.z) + rz * n.z);
+    return normalize(rr);
+}
+
+struct Material {
+    v3 albedo;
+    float rough, metal;
+    int emissive;
+};
+inline Material material(const vpto_world* w, int id) {
+    if (id < 0 || id >= w->n_blocks) id = 0;
+    const vpto_block& b = w->blocks[id];
+    Material m;
+    m.albedo = mk3((float)b.albedo[0] / 255.0f, (float)b.albedo[1] / 255.0f, (float)b.albedo[2] / 255.0f);
+    m.rough = (float)b.roughness / 255.0f;
+    m.metal = (float)b.metalness / 255.0f;
+    m.emissive = b.emissive ? 1 : 0;
+    return m;
+}
+
+struct Lighting {       // per-frame constants of DiffuseRayTraceFrag main (:832-839)
+    v3 light_color, light_dir;
+    bool moon_stronger;
+    float emissivity_multiplier;
+    float sun_visibility;   // Core/Pipeline.cpp:1828
+};
+
+inline v3 moon_dir_of(v3 s) { return normalize(mk3(-s.x, -s.y, s.z)); }   // Core/Pipeline.cpp:1663
+
+Lighting frame_lighting(const vpto_frame* f) {
+    const v3 SUN_COLOR = muls(divs(mk3(192.0f, 216.0f, 255.0f), 255.0f), 16.0f);   // :184
+    const v3 NIGHT_COLOR = muls(divs(mk3(96.0f, 192.0f, 255.0f), 255.0f), 1.5f);   // :185
+    const v3 DUSK_COLOR = muls(divs(mk3(96.0f, 192.0f, 255.0f), 255.0f), 0.9f);    // :186
+    v3 sun = mk3(f->sun_dir[0], f->sun_dir[1], f->sun_dir[2]);
+    Lighting L;
+    bool sun_stronger = -sun.y < 0.01f;
+    float dusk = clampf(dm_pow(std::fabs(sun.y - 1.0f), 2.9f), 0.0f, 1.0f);
+    v3 sun_color = vmix(SUN_COLOR, DUSK_COLOR, dusk);
+    L.light_color = sun_stronger ? sun_color : NIGHT_COLOR;
+    L.light_color = muls(L.light_color, 0.4f * f->gi_sun_strength);
+    L.light_dir = sun_stronger ? sun : moon_dir_of(sun);
+    L.moon_stronger = !sun_stronger;
+    L.emissivity_multiplier = L.moon_stronger ? 13.0f : 12.0f;
+    L.sun_visibility = clampf(dot(sun, mk3(0.0f, 1.0f, 0.0f)) + 0.05f, 0.0f, 0.1f) * 12.0f;
+    return L;
+}
+
+// CalculateDiffuse (DiffuseRayTraceFrag.glsl:535-664) with `bounces` = MAX_BOUNCE_LIMIT.
+v4 calculate_diffuse(const vpto_world* w, const vpto_params* p, const vpto_frame* f, const Lighting& L,
+                     v3 initial_origin, v3 input_normal, uint32_t* rng, v3* odir, bool* skyhit, RowCount* cnt) {
+    *skyhit = false;
+    const float bias = 0.06f;
+    v3 ro = add(initial_origin, muls(input_normal, bias));
+    v3 rd = cos_hemisphere(input_normal, rng);
+    float ao = 1.0f;
+    v3 contribution = mk3(0, 0, 0);
+    v3 throughput = mk3(1, 1, 1);
+    for (int i = 0; i < p->bounces; i++) {
+        if (i == 0) *odir = rd;
+        TraceResult tr = traverse(w, ro, rd, p->diffuse_max_steps);
+        cnt->add(2, tr.steps);
+        float T = tr.t;
+        bool intersect = T > 0.0f;
+        v3 ip = add(ro, muls(rd, T));
+        if (intersect && tr.block > 0) {
+            Material m = material(w, std::min(std::max(tr.block, 0), 127));
+            v3 hn = tr.normal;
+            float emissivity = 0.0f;
+            if (m.emissive) emissivity = 1.0f * L.emissivity_multiplier * f->diffuse_light_intensity;
+            float ndl = fmaxg(dot(hn, L.light_dir), 0.0f);
+            v3 bias_shadow = muls(hn, 0.045f);
+            float shadow_at;
+            if (L.moon_stronger) {
+                shadow_at = 1.0f;
+            } else {
+                // GetShadowAt (:1202-1222)
+                if (ndl < 0.001f) {
+                    shadow_at = 0.0f;
+                } else {
+                    TraceResult sr = traverse(w, add(ip, bias_shadow), L.light_dir, p->bounce_shadow_max_steps);
+                    cnt->add(3, sr.steps);
+                    shadow_at = sr.t > 0.0f ? 1.0f : 0.0f;
+                }
+            }
+            v3 emissive_color = muls(m.albedo, emissivity * mixf(1.0f, 1.0f, L.sun_visibility));
+            // SunBRDF (:499-508)
+            float hs = diffuse_hammon(hn, neg(rd), L.light_dir, m.rough);
+            v3 sun_brdf = muls(muls(mul(muls(m.albedo, hs), muls(L.light_color, 3.5f)), 1.0f - shadow_at), PI);
+            v3 new_dir = cos_hemisphere(hn, rng);
+            float cos_theta = clampf(dot(hn, new_dir), 0.0f, 1.0f);
+            float pdf = fmaxg(cos_theta / PI, 0.00001f);
+            float att = diffuse_hammon(hn, neg(rd), new_dir, m.rough);   // DiffuseRayBRDF (:527-531)
+            contribution = add(contribution, mul(throughput, sun_brdf));
+            contribution = add(contribution, mul(emissive_color, throughput));
+            throughput = mul(throughput, divs(muls(m.albedo, att), pdf));
+            rd = new_dir;
+            ro = add(ip, muls(hn, bias));
+        } else {
+            float x = mixf(1.0f, 1.05f, L.sun_visibility);
+            x = clampf(x * 1.0f * f->gi_sky_strength, 0.0f, 5.0f);
+            v3 sky = muls(sky_color_at(rd), x);
+            contribution = add(contribution, mul(sky, throughput));
+            *skyhit = true;
+            break;
+        }
+        if (i == 0) {
+            const float dao = 2.0f;
+            if (T < dao && T > 0.0f) ao = fmaxg(T / dao, 0.0f);
+        }
+    }
+    return v4{contribution.x, contribution.y, contribution.z, ao};
+}
+
+// CalculateDirectionalLight (ColorPassFrag.glsl:419-451) with
+// FresnelSchlickRoughness (:1205-1209), ndfGGX (:394-400), gaSchlickGGX (:402-412).
+v3 fresnel_schlick_roughness(v3 eye, v3 n, v3 f0, float rough) {
+    float cos_theta = clampf(dot(eye, n), 0.00001f, 1.0f);
+    float k = dm_pow(1.0f - cos_theta, 5.0f);
+    v3 m = mk3(fmaxg(1.0f - rough, f0.x), fmaxg(1.0f - rough, f0.y), fmaxg(1.0f - rough, f0.z));
+    return add(f0, muls(sub(m, f0), k));
+}
+
+v3 directional_light(v3 viewer, v3 wp, v3 light_dir, v3 radiance, v3 radiance_s, v3 albedo, v3 n,
+                     float rough, float metal, float shadow) {
+    const float DIELECTRIC = 0.04f, Epsilon = 0.00001f;
+    float sh = fming(shadow, 1.0f);
+    v3 lo = normalize(sub(viewer, wp));
+    float cos_lo = fmaxg(0.0f, dot(n, lo));
+    v3 f0 = vmix(mk3(DIELECTRIC, DIELECTRIC, DIELECTRIC), albedo, metal);
+    v3 li = light_dir;
+    v3 lh = normalize(add(li, lo));
+    float cos_li = fmaxg(0.0f, dot(n, li));
+    float cos_lh = fmaxg(0.0f, dot(n, lh));
+    v3 F = fresnel_schlick_roughness(lo, n, f0, rough);
+    float alpha = rough * rough;
+    float alpha_sq = alpha * alpha;
+    float denom = (cos_lh * cos_lh) * (alpha_sq - 1.0f) + 1.0f;
+    float D = alpha_sq / ((PI * denom) * denom);
+    float r1 = rough + 1.0f;
+    float k = (r1 * r1) / 8.0f;
+    float G = (cos_li / (cos_li * (1.0f - k) + k)) * (cos_lo / (cos_lo * (1.0f - k) + k));
+    v3 kd = vmix(sub(mk3(1, 1, 1), F), mk3(0, 0, 0), metal);
+    v3 diffuse_brdf = mul(kd, albedo);
+    v3 spec = divs(muls(muls(F, D), G), fmaxg(Epsilon, (4.0f * cos_li) * cos_lo));
+    spec = vclamp(spec, 0.0f, 2.0f);
+    v3 result = add(muls(mul(diffuse_brdf, radiance), cos_li), muls(mul(spec, radiance_s), cos_li));
+    return muls(vclamp(result, 0.0f, 2.5f), clampf(1.0f - sh, 0.0f, 1.0f));
+}
+
+// BasicSaturation (ColorPassFrag.glsl:1227-1232)
+inline v3 basic_saturation(v3 c, float adj) {
+    float l = dot(c, mk3(0.2125f, 0.7154f, 0.0721f));
+    return vmix(mk3(l, l, l), c, adj);
+}
+
+// KarisEnvBRDFApprox (ColorPassFrag.glsl:384-391)
+inline v2 karis_env_brdf(float ndv, float rough) {
+    float rx = rough * -1.0f + 1.0f;
+    float ry = rough * -0.0275f + 0.0425f;
+    float rz = rough * -0.572f + 1.040f;
+    float rw = rough * 0.022f + -0.040f;
+    float a004 = fming(rx * rx, dm_exp2(-9.28f * ndv)) * rx + ry;
+    return v2{-1.04f * a004 + rz, 1.04f * a004 + rw};
+}
+
+}  // namespace
+
+extern "C" {
+
+void vpto_set_counters(uint64_t* counters) { g_counters = counters; }
+
+int vpto_omp_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+float vpto_exp(float x) { return dm_exp(x); }
+float vpto_exp2(float x) { return dm_exp2(x); }
+float vpto_log2(float x) { return dm_log2(x); }
+float vpto_pow(float x, float y) { return dm_pow(x, y); }
+float vpto_sin(float x) { return dm_sin(x); }
+float vpto_cos(float x) { return dm_cos(x); }
+float vpto_half_round(float x) { return half_round(x); }
+
+// World::GenerateDistanceField (Core/World.cpp:69-113): X, Y, Z passes in
+// sequence, each a forward then a backward sweep along one axis.
+void vpto_build_df(const uint8_t* vox, int X, int Y, int Z, uint8_t* df) {
+    const int max_d = std::min(254, X + Y + Z);   // ManhattanDistanceX.comp:51
+    const size_t sx = 1, sy = (size_t)X, sz = (size_t)X * Y;
+    // ManhattanDistanceX.comp:45-68
+#pragma omp parallel for schedule(static)
+    for (int zy = 0; zy < Y * Z; zy++) {
+        int y = zy % Y, z = zy / Y;
+        uint8_t* d = df + y * sy + z * sz;
+        const uint8_t* v = vox + y * sy + z * sz;
+        d[0] = v[0] > 0 ? 0 : (uint8_t)max_d;
+        for (int x = 1; x < X; x++)
+            d[x * sx] = v[x * sx] > 0 ? 0 : (uint8_t)std::min(max_d, 1 + (int)d[(x - 1) * sx]);
+        for (int x = X - 2; x >= 0; x--)
+            if (d[(x + 1) * sx] < d[x * sx]) d[x * sx] = (uint8_t)(1 + d[(x + 1) * sx]);
+    }
+    // ManhattanDistanceY.comp:94-119
+#pragma omp parallel for schedule(static)
+    for (int zx = 0; zx < X * Z; zx++) {
+        int x = zx % X, z = zx / X;
+        uint8_t* d = df + x * sx + z * sz;
+        for (int y = 1; y < Y; y++)
+            if (d[(y - 1) * sy] < d[y * sy]) d[y * sy] = (uint8_t)(1 + d[(y - 1) * sy]);
+        for (int y = Y - 2; y >= 0; y--)
+            if (d[(y + 1) * sy] < d[y * sy]) d[y * sy] = (uint8_t)(1 + d[(y + 1) * sy]);
+    }
+    // ManhattanDistanceZ.comp:142-166
+#pragma omp parallel for schedule(static)
+    for (int yx = 0; yx < X * Y; yx++) {
+        int x = yx % X, y = yx / X;
+        uint8_t* d = df + x * sx + y * sy;
+        for (int z = 1; z < Z; z++)
+            if (d[(z - 1) * sz] < d[z * sz]) d[z * sz] = (uint8_t)(1 + d[(z - 1) * sz]);
+        for (int z = Z - 2; z >= 0; z--)
+            if (d[(z + 1) * sz] < d[z * sz]) d[z * sz] = (uint8_t)(1 + d[(z + 1) * sz]);
+    }
+}
+
+// InitialRayTraceFrag.glsl main (:417-468)
+void vpto_trace_primary(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
+                        int row0, int row1, vpto_gbuffer* out) {
+    const int W = p->width, H = p->height;
+    const v3 r0 = ray_origin(cam);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int j = row0; j < row1; j++) {
+        RowCount cnt;
+        for (int i = 0; i < W; i++) {
+            size_t px = (size_t)j * W + i;
+            v3 dir = normalize(ray_dir_at(cam, texcoord(i, j, W, H)));
+            TraceResult r = traverse(w, r0, dir, p->primary_max_steps);
+            cnt.add(0, r.steps);
+            bool intersect = r.t > 0.0f && r.block > 0;
+            out->t[px] = storage(r.t, p->storage);
+            out->face[px] = (uint8_t)(intersect ? normal_id(r.normal) : 10);
+            out->block[px] = (uint8_t)(intersect ? r.block : 0);
+            out->hit[px * 3 + 0] = r.cell[0];
+            out->hit[px * 3 + 1] = r.cell[1];
+            out->hit[px * 3 + 2] = r.cell[2];
+            out->steps[px] = (uint16_t)r.steps;
+        }
+        cnt.flush();
+    }
+}
+
+// ShadowRayTraceFrag.glsl main (:414-513): hard sun shadow, no cone jitter.
+void vpto_trace_shadow(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
+                       const vpto_frame* f, const float* t, const uint8_t* face,
+                       int row0, int row1, uint8_t* shadow) {
+    const int W = p->width, H = p->height;
+    const v3 r0 = ray_origin(cam);
+    const v3 L = mk3(f->sun_dir[0], f->sun_dir[1], f->sun_dir[2]);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int j = row0; j < row1; j++) {
+        RowCount cnt;
+        for (int i = 0; i < W; i++) {
+            size_t px = (size_t)j * W + i;
+            float d = t[px];
+            if (d < 0.0f) { shadow[px] = 0; continue; }
+            v3 pos = add(r0, muls(normalize(ray_dir_at(cam, texcoord(i, j, W, H))), d));
+            v3 n = normal_from_id(face[px], 1.0f);
+            float ndl = dot(n, L);
+            if (ndl <= 0.01f) { shadow[px] = 1; continue; }
+            v3 o = add(pos, mul(n, mk3(0.06f, 0.06f, 0.06f)));
+            int block_at = get_voxel(w, f2i(std::floor(o.x)), f2i(std::floor(o.y)), f2i(std::floor(o.z)));
+            float T = -1.0f;
+            if (d > 0.0f) {
+                TraceResult r = traverse(w, o, L, p->shadow_max_steps);
+                cnt.add(1, r.steps);
+                T = r.t;
+            }
+            shadow[px] = (uint8_t)((T > 0.0f || block_at > 0) ? 1 : 0);
+        }
+        cnt.flush();
+    }
+}
+
+// DiffuseRayTraceFrag.glsl main (:822-935)
+void vpto_trace_diffuse(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
+                        const vpto_frame* f, const float* t, const uint8_t* face,
+                        int row0, int row1, vpto_gi* out) {
+    const int W = p->width, H = p->height;
+    const v3 r0 = ray_origin(cam);
+    const Lighting L = frame_lighting(f);
+    const int fp16 = p->storage;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int j = row0; j < row1; j++) {
+        RowCount cnt;
+        for (int i = 0; i < W; i++) {
+            size_t px = (size_t)j * W + i;
+            v2 uv = texcoord(i, j, W, H);
+            v3 dir = normalize(ray_dir_at(cam, uv));
+            float d = t[px];
+            v3 pos = add(r0, muls(dir, d));
+            v3 n = normal_from_id(face[px], 0.5f);
+            float sh[4], cocg[2];
+            if (d < 0.0f) {
+                irradiance_to_sh(muls(sky_radiance(dir), 2.66f), n, sh, cocg);
+                for (int c = 0; c < 4; c++) out->sh[px * 4 + c] = storage(sh[c], fp16);
+                out->cocg[px * 2 + 0] = storage(cocg[0], fp16);
+                out->cocg[px * 2 + 1] = storage(cocg[1], fp16);
+                out->luma[px] = storage(luminance(mk3(0, 0, 0)), fp16);
+                out->aosky[px * 2 + 0] = storage(1.0f, fp16);
+                out->aosky[px * 2 + 1] = storage(0.0f, fp16);
+                continue;
+            }
+            uint32_t rng = pixel_seed(f, (uint32_t)px);
+            int spp = std::min(std::max(p->spp, 1), 32);
+            if (L.moon_stronger) spp *= 2;
+            float tot_sh[4] = {0, 0, 0, 0}, tot_cocg[2] = {0, 0};
+            v3 radiance = mk3(0, 0, 0);
+            float acc_ao = 0.0f, skyhits = 0.0f;
+            for (int s = 0; s < spp; s++) {
+                v3 odir = mk3(0, 0, 0);
+                bool ss = false;
+                v4 x = calculate_diffuse(w, p, f, L, pos, n, &rng, &odir, &ss, &cnt);
+                v3 xc = vclamp(mk3(x.x, x.y, x.z), 0.0f, 8.0f);
+                radiance = add(radiance, xc);
+                acc_ao += x.w;
+                irradiance_to_sh(xc, odir, sh, cocg);
+                for (int c = 0; c < 4; c++) tot_sh[c] += sh[c];
+                tot_cocg[0] += cocg[0];
+                tot_cocg[1] += cocg[1];
+                skyhits += ss ? 1.0f : 0.0f;
+            }
+            float fs = (float)spp;
+            acc_ao /= fs;
+            for (int c = 0; c < 4; c++) tot_sh[c] /= fs;
+            tot_cocg[0] /= fs;
+            tot_cocg[1] /= fs;
+            radiance = divs(radiance, fs);
+            skyhits /= fs;
+            for (int c = 0; c < 4; c++) out->sh[px * 4 + c] = storage(clampf(tot_sh[c], -100.0f, 100.0f), fp16);
+            out->cocg[px * 2 + 0] = storage(clampf(tot_cocg[0], -100.0f, 100.0f), fp16);
+            out->cocg[px * 2 + 1] = storage(clampf(tot_cocg[1], -100.0f, 100.0f), fp16);
+            out->luma[px] = storage(clampf(fmaxg(luminance(radiance), 0.01f), 0.001f, 64.0f), fp16);
+            out->aosky[px * 2 + 0] = storage(clampf(acc_ao, 0.0f, 1.0f), fp16);
+            out->aosky[px * 2 + 1] = storage(clampf(skyhits, 0.0f, 1.0f), fp16);
+        }
+        cnt.flush();
+    }
+}
+
+// Spatial3x3Initial.glsl main (:96-176)
+void vpto_spatial_initial(const vpto_camera* cam, const vpto_params* p,
+                          const float* t, const uint8_t* face, const vpto_gi* in, vpto_gi* out) {
+    const int W = p->width, H = p->height;
+    const int fp16 = p->storage;
+    const Plane T{t, W, H, 1}, SH{in->sh, W, H, 4}, CC{in->cocg, W, H, 2}, AO{in->aosky, W, H, 2};
+    const Plane8 F{face, W, H};
+    const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
+    const float atrous_w[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int j = 0; j < H; j++) {
+        for (int i = 0; i < W; i++) {
+            size_t px = (size_t)j * W + i;
+            v2 uv = texcoord(i, j, W, H);
+            v4 bp = position_fetch(cam, T, i, j, uv);
+            v3 bn = normal_from_id(F.at(i, j), 1.0f);
+            float bsh[4], bcc[2], bao[2];
+            for (int c = 0; c < 4; c++) bsh[c] = SH.at(i, j, c);
+            for (int c = 0; c < 2; c++) { bcc[c] = CC.at(i, j, c); bao[c] = AO.at(i, j, c); }
+            float bl = sh_to_y(bsh);
+            float butil = in->luma[px];
+            float tsh[4] = {bsh[0], bsh[1], bsh[2], bsh[3]}, tcc[2] = {bcc[0], bcc[1]};
+            float tao[2] = {bao[0], bao[1]};
+            float tw = 1.0f, taow = 1.0f;
+            const float phi = 4.0f;
+            for (int x = -1; x <= 1; x++) {
+                for (int y = -1; y <= 1; y++) {
+                    if (x == 0 && y == 0) continue;
+                    int si = i + x, sj = j + y;
+                    if (si < 0 || si >= W || sj < 0 || sj >= H) continue;   // InScreenSpace
+                    v2 sc = v2{uv.x + (float)x * texel_x, uv.y + (float)y * texel_y};
+                    v4 sp = position_fetch(cam, T, si, sj, sc);
+                    v3 pd = mk3(std::fabs(sp.x - bp.x), std::fabs(sp.y - bp.y), std::fabs(sp.z - bp.z));
+                    float dist_sqr = dot(pd, pd);
+                    if (dist_sqr < 1.0f) {
+                        float ssh[4], scc[2];
+                        for (int c = 0; c < 4; c++) ssh[c] = SH.at(si, sj, c);
+                        for (int c = 0; c < 2; c++) scc[c] = CC.at(si, sj, c);
+                        v3 sn = normal_from_id(F.at(si, sj), 1.0f);
+                        float sl = sh_to_y(ssh);
+                        float nw = dm_pow(fmaxg(dot(bn, sn), 0.0f), 16.0f);
+                        float lw = std::fabs(sl - bl) / phi;
+                        float wgt = dm_exp(-lw - nw);
+                        wgt = fmaxg(wgt, 0.01f);
+                        wgt = (atrous_w[std::abs(x)] * atrous_w[std::abs(y)]) * wgt;
+                        wgt = fmaxg(wgt, 0.01f);
+                        wgt = clampf(wgt, 0.0f, 1.0f);
+                        for (int c = 0; c < 4; c++) tsh[c] += ssh[c] * wgt;
+                        for (int c = 0; c < 2; c++) tcc[c] += scc[c] * wgt;
+                        tw += wgt;
+                        for (int c = 0; c < 2; c++) tao[c] += AO.at(si, sj, c) * wgt;
+                        taow += wgt;
+                    }
+                }
+            }
+            tw = fmaxg(tw, 0.01f);
+            for (int c = 0; c < 4; c++) out->sh[px * 4 + c] = storage(tsh[c] / tw, fp16);
+            for (int c = 0; c < 2; c++) out->cocg[px * 2 + c] = storage(tcc[c] / tw, fp16);
+            float aw = fmaxg(taow, 0.01f);
+            for (int c = 0; c < 2; c++) out->aosky[px * 2 + c] = storage(tao[c] / aw, fp16);
+            out->luma[px] = storage(butil, fp16);
+        }
+    }
+}
+
+// SVGF/TemporalFilter.glsl main (:132-360)
+void vpto_temporal(const vpto_camera* cam, const vpto_camera* prev_cam, const vpto_params* p,
+                   const vpto_frame* f,
+                   const float* t, const uint8_t* face, const uint8_t* block,
+                   const float* prev_t, const uint8_t* prev_face, const uint8_t* prev_block,
+                   const vpto_gi* cur, const vpto_history* prev, vpto_history* out) {
+    const int W = p->width, H = p->height;
+    const int fp16 = p->storage;
+    const Plane T{t, W, H, 1}, PT{prev_t, W, H, 1};
+    const Plane8 F{face, W, H}, B{block, W, H}, PF{prev_face, W, H}, PB{prev_block, W, H};
+    const Plane PSH{prev->sh, W, H, 4}, PCC{prev->cocg, W, H, 2}, PU{prev->util, W, H, 4}, PAO{prev->aosky, W, H, 2};
+    const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
+    // u_PrevProjection * u_PrevView, a 4x4 product evaluated left to right.
+    float m[16];
+    for (int c = 0; c < 4; c++)
+        for (int r = 0; r < 4; r++)
+            m[c * 4 + r] = ((prev_cam->proj[0 * 4 + r] * prev_cam->view[c * 4 + 0] +
+                             prev_cam->proj[1 * 4 + r] * prev_cam->view[c * 4 + 1]) +
+                            prev_cam->proj[2 * 4 + r] * prev_cam->view[c * 4 + 2]) +
+                           prev_cam->proj[3 * 4 + r] * prev_cam->view[c * 4 + 3];
+    const float weights[5] = {3.0f / 32.0f, 3.0f / 32.0f, 9.0f / 64.0f, 3.0f / 32.0f, 3.0f / 32.0f};
+    const int offs[5][2] = {{1, 0}, {0, 1}, {0, 0}, {-1, 0}, {0, -1}};
+    const bool be_useful = f->temporal != 0;
+    const v3 viewer = ray_origin(cam);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int j = 0; j < H; j++) {
+        for (int i = 0; i < W; i++) {
+            size_t px = (size_t)j * W + i;
+            v2 uv = texcoord(i, j, W, H);
+            v4 bp = position_fetch(cam, T, i, j, uv);
+            v3 bn = normal_from_id(F.at(i, j), 1.0f);
+            float bsh[4], bcc[2], bao[2];
+            for (int c = 0; c < 4; c++) bsh[c] = cur->sh[px * 4 + c];
+            for (int c = 0; c < 2; c++) { bcc[c] = cur->cocg[px * 2 + c]; bao[c] = cur->aosky[px * 2 + c]; }
+            v4 pr = mat_mul4(m, bp.x, bp.y, bp.z, 1.0f);
+            v2 rc = v2{(pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f};
+            float base_lum = cur->luma[px];
+            int base_block = std::min(std::max((int)B.at(i, j), 0), 127);
+            float tol = 0.75f;
+            bool do_block = true, do_normal = true;
+            float dp = length(sub(mk3(bp.x, bp.y, bp.z), viewer));
+            if (dp < 4.0f) { tol = 0.3f; }
+            else if (dp < 6.0f) { tol = 0.65f; }
+            else if (dp < 8.0f) { tol = 0.85f; }
+            else if (dp < 16.0f) { tol = 1.414f; }
+            else if (dp < 32.0f) { tol = 2.4f; }
+            else if (dp < 48.0f) { tol = 3.5f; do_block = false; }
+            else if (dp < 64.0f) { tol = 4.2f; do_block = false; }
+            else if (dp < 96.0f) { tol = 6.25f; do_block = false; do_normal = false; }
+            else if (dp < 128.0f) { tol = 9.0f; do_block = false; do_normal = false; }
+            else if (dp < 200.0f) { tol = 14.0f; do_block = false; do_normal = false; }
+            float tw = 0.0f, ssh[4] = {0, 0, 0, 0}, scc[2] = {0, 0}, sao[2] = {0, 0};
+            float slum = 0.0f, sspp = 0.0f, smom = 0.0f;
+            int successful = 0;
+            for (int k = 0; k < 5; k++) {
+                // Jitter is ivec2((noise - 0.5) * 1.0) == 0 for every pixel (:165)
+                v2 sc = v2{rc.x + ((float)offs[k][0] + 0.0f) * texel_x, rc.y + ((float)offs[k][1] + 0.0f) * texel_y};
+                const float b = 0.0035f;
+                if (!(sc.x < 1.0f - b && sc.x > b && sc.y < 1.0f - b && sc.y > b)) continue;
+                v4 pp = position_linear(cam, PT, sc);
+                v3 pn = normal_from_id(PF.nearest(sc), 1.0f);
+                v3 pd = mk3(std::fabs(bp.x - pp.x), std::fabs(bp.y - pp.y), std::fabs(bp.z - pp.z));
+                float perr = dot(pd, pd);
+                float cw = weights[k];
+                int sblock = std::min(std::max(PB.nearest(sc), 0), 127);
+                bool valid = false;
+                if (perr < tol && ((pp.w < 0.0f) == (bp.w < 0.0f))) {
+                    valid = true;
+                    if (do_normal && !(pn.x == bn.x && pn.y == bn.y && pn.z == bn.z)) valid = false;
+                    if (do_block && base_block != sblock) valid = false;
+                }
+                if (valid) {
+                    float pu[4], psh[4], pcc[2], pao[2];
+                    PU.linear(sc, pu);
+                    PSH.linear(sc, psh);
+                    PCC.linear(sc, pcc);
+                    PAO.linear(sc, pao);
+                    for (int c = 0; c < 4; c++) ssh[c] += psh[c] * cw;
+                    for (int c = 0; c < 2; c++) scc[c] += pcc[c] * cw;
+                    sspp += pu[0] * cw;
+                    smom += pu[1] * cw;
+                    slum += pu[2] * cw;
+                    for (int c = 0; c < 2; c++) sao[c] += pao[c] * cw;
+                    tw += cw;
+                    successful++;
+                }
+            }
+            if (tw > 0.001f) {
+                for (int c = 0; c < 4; c++) ssh[c] /= tw;
+                for (int c = 0; c < 2; c++) scc[c] /= tw;
+                smom /= tw;
+                sspp /= tw;
+                slum /= tw;
+                for (int c = 0; c < 2; c++) sao[c] /= tw;
+            } else {
+                successful = 0;
+            }
+            float inc = be_useful ? 1.0f : 0.0f;
+            float spp_inc = sspp + inc;
+            if (successful <= 0) spp_inc = 0.01f;
+            float blend = fmaxg(1.0f / spp_inc, 0.05f);
+            float mfac = fmaxg(1.0f / spp_inc, 0.05f);
+            if (!be_useful) { blend = 0.99f; sspp = 0.0f; }
+            float util_spp = spp_inc;
+            if (successful <= 0) util_spp = 0.0f;
+            float util_mom = (1.0f - mfac) * smom + mfac * (base_lum * base_lum);
+            float store_luma = mixf(slum, base_lum, blend);
+            float osh[4], occ[2], oao[2];
+            for (int c = 0; c < 4; c++) osh[c] = mixf(ssh[c], bsh[c], blend);
+            for (int c = 0; c < 2; c++) { occ[c] = mixf(scc[c], bcc[c], blend); oao[c] = mixf(sao[c], bao[c], blend); }
+            if (successful <= 0) {
+                for (int c = 0; c < 4; c++) osh[c] = bsh[c];
+                for (int c = 0; c < 2; c++) { occ[c] = bcc[c]; oao[c] = bao[c]; }
+            }
+            for (int c = 0; c < 4; c++) out->sh[px * 4 + c] = storage(clampf(osh[c], -100.0f, 100.0f), fp16);
+            for (int c = 0; c < 2; c++) out->cocg[px * 2 + c] = storage(clampf(occ[c], -10.0f, 100.0f), fp16);
+            for (int c = 0; c < 2; c++) out->aosky[px * 2 + c] = storage(clampf(oao[c], 0.0f, 1.0f), fp16);
+            out->util[px * 4 + 0] = storage(clampf(util_spp, -150.0f, 150.0f), fp16);
+            out->util[px * 4 + 1] = storage(clampf(util_mom, -150.0f, 150.0f), fp16);
+            out->util[px * 4 + 2] = storage(clampf(store_luma, -150.0f, 150.0f), fp16);
+            out->util[px * 4 + 3] = 0.0f;
+        }
+    }
+}
+
+// SVGF/VarianceEstimate.glsl main (:73-193), DO_SPATIAL and
+// AGGRESSIVE_DISOCCLUSION_HANDLING on (Core/Pipeline.cpp:2451-2452).
+void vpto_variance(const vpto_camera* cam, const vpto_params* p,
+                   const float* t, const uint8_t* face, const vpto_history* in, vpto_filtered* out) {
+    const int W = p->width, H = p->height;
+    const int fp16 = p->storage;
+    const Plane T{t, W, H, 1}, SH{in->sh, W, H, 4}, CC{in->cocg, W, H, 2}, U{in->util, W, H, 4};
+    const Plane8 F{face, W, H};
+    const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
+    const float thresh = 4.0f + 4.0f + 4.0f;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int j = 0; j < H; j++) {
+        for (int i = 0; i < W; i++) {
+            size_t px = (size_t)j * W + i;
+            v2 uv = texcoord(i, j, W, H);
+            v4 bp = position_fetch(cam, T, i, j, uv);
+            v3 bn = normal_from_id(F.at(i, j), 1.0f);
+            float bsh[4], bcc[2];
+            for (int c = 0; c < 4; c++) bsh[c] = SH.at(i, j, c);
+            for (int c = 0; c < 2; c++) bcc[c] = CC.at(i, j, c);
+            float bl = sh_to_y(bsh);
+            float acc = U.at(i, j, 0);
+            float bm = U.at(i, j, 1);
+            float osh[4], occ[2], var;
+            if (acc < thresh) {
+                const float phi = 5.0f;
+                float tw = 0.0f, tm = 0.0f, tl = 0.0f, tw2 = 0.0f;
+                float tsh[4] = {0, 0, 0, 0}, tcc[2] = {0, 0};
+                for (int x = -4; x <= 4; x++) {
+                    for (int y = -4; y <= 4; y++) {
+                        int si = i + x, sj = j + y;
+                        if (si < 0 || si >= W || sj < 0 || sj >= H) continue;
+                        v2 sc = v2{uv.x + (float)x * texel_x, uv.y + (float)y * texel_y};
+                        v4 sp = position_fetch(cam, T, si, sj, sc);
+                        v3 sn = normal_from_id(F.at(si, sj), 1.0f);
+                        float smom = U.at(si, sj, 1);
+                        float ssh[4], scc[2];
+                        for (int c = 0; c < 4; c++) ssh[c] = SH.at(si, sj, c);
+                        for (int c = 0; c < 2; c++) scc[c] = CC.at(si, sj, c);
+                        float sl = sh_to_y(ssh);
+                        float nw = dm_pow(fmaxg(dot(bn, sn), 0.0f), 16.0f);
+                        float dw = dm_pow(dm_exp(-std::fabs(sp.w - bp.w)), 2.0f);
+                        float lw = std::fabs(sl - bl) / phi;
+                        float wgt = (dm_exp(-lw) * nw) * dw;
+                        float wgt2 = wgt;
+                        wgt = fmaxg(wgt, 0.000000015f);
+                        wgt2 = fmaxg(wgt2, 0.0000000015f);
+                        tw += wgt;
+                        tm += smom * wgt2;
+                        for (int c = 0; c < 4; c++) tsh[c] += ssh[c] * wgt;
+                        for (int c = 0; c < 2; c++) tcc[c] += scc[c] * wgt;
+                        tl += sl * wgt2;
+                        tw2 += wgt2;
+                    }
+                }
+                if (tw > 0.0f) {
+                    tm /= tw2;
+                    tl /= tw2;
+                    for (int c = 0; c < 2; c++) tcc[c] /= tw;
+                    for (int c = 0; c < 4; c++) tsh[c] /= tw;
+                }
+                for (int c = 0; c < 4; c++) osh[c] = tsh[c];
+                for (int c = 0; c < 2; c++) occ[c] = tcc[c];
+                float al = tl * tl;
+                var = tm - al;
+                var *= 3.0f;
+            } else {
+                for (int c = 0; c < 4; c++) osh[c] = bsh[c];
+                for (int c = 0; c < 2; c++) occ[c] = bcc[c];
+                var = bm - bl * bl;
+            }
+            var *= thresh / acc;
+            for (int c = 0; c < 4; c++) out->sh[px * 4 + c] = storage(clampf(osh[c], -100.0f, 100.0f), fp16);
+            for (int c = 0; c < 2; c++) out->cocg[px * 2 + c] = storage(clampf(occ[c], -10.0f, 100.0f), fp16);
+            out->variance[px] = storage(clampf(var, -1.0f, 50.0f), fp16);
+        }
+    }
+}
+
+// SVGF/SpatialFilter.glsl main (:175-355), u_LargeKernel off, DO_SPATIAL on.
+void vpto_atrous(const vpto_camera* cam, const vpto_params* p, const vpto_frame* f, int step,
+                 const float* t, const uint8_t* face, const float* temporal_util,
+                 const vpto_filtered* in, const float* in_aosky, vpto_filtered* out) {
+    const int W = p->width, H = p->height;
+    const int fp16 = p->storage;
+    const Plane T{t, W, H, 1}, SH{in->sh, W, H, 4}, CC{in->cocg, W, H, 2}, V{in->variance, W, H, 1};
+    const Plane AO{in_aosky, W, H, 2}, U{temporal_util, W, H, 4};
+    const Plane8 F{face, W, H};
+    const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
+    const float atrous_w[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
+    const float gauss[2] = {0.60283f, 0.198585f};
+    const bool filter_ao = step <= 4;
+    const bool filter_sky = (step <= 6) || filter_ao;
+    const float add_scale = mixf(1.0f, 2.4f, p->resolution_scale);
+    const float phi_bias = fmaxg(p->color_phi_bias, 0.1f);
+    const float tmod = f->time * 100.493850275f;
+    const float tmod500 = tmod - 500.0f * std::floor(tmod / 500.0f);   // GLSL mod
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int j = 0; j < H; j++) {
+        for (int i = 0; i < W; i++) {
+            size_t px = (size_t)j * W + i;
+            v2 uv = texcoord(i, j, W, H);
+            // GradientNoise (:160-165)
+            float gx = ((float)i + 0.5f) + tmod500, gy = ((float)j + 0.5f) + tmod500;
+            float noise = fract(52.9829189f * fract(0.06711056f * gx + 0.00583715f * gy));
+            int jit = f2i((noise - 0.5f) * ((float)step * 0.8f));
+            float bd = T.at(i, j, 0);
+            v3 bn = normal_from_id(F.at(i, j), 1.0f);
+            float bsh[4], bcc[2], bao[2];
+            for (int c = 0; c < 4; c++) bsh[c] = SH.at(i, j, c);
+            for (int c = 0; c < 2; c++) { bcc[c] = CC.at(i, j, c); bao[c] = AO.at(i, j, c); }
+            float bl = sh_to_y(bsh);
+            // GaussianVariance (:94-129)
+            float bvar = 0.0f, vsum = 0.0f, tk = 0.0f;
+            for (int x = -1; x <= 1; x++) {
+                for (int y = -1; y <= 1; y++) {
+                    int si = i + x, sj = j + y;
+                    if (si < 0 || si >= W || sj < 0 || sj >= H) continue;
+                    float kv = gauss[std::abs(x)] * gauss[std::abs(y)];
+                    float v = V.at(si, sj, 0);
+                    if (x == 0 && y == 0) bvar = v;
+                    vsum += v * kv;
+                    tk += kv;
+                }
+            }
+            float vest = vsum / fmaxg(tk, 0.01f);
+            float tsh[4] = {bsh[0], bsh[1], bsh[2], bsh[3]}, tcc[2] = {bcc[0], bcc[1]};
+            float tw = 1.0f, tvar = bvar, tao[2] = {bao[0], bao[1]}, taow = 1.0f;
+            float acc_frames = U.at(i, j, 0);
+            bool strong = acc_frames <= 8.0f && step <= 8;
+            float curve = 0.0f;
+            if (vest < 0.01f) curve = 128.0f;
+            else if (vest < 0.025f) curve = 112.0f;
+            else if (vest < 0.05f) curve = 96.0f;
+            else if (vest < 0.075f) curve = 84.0f;
+            else if (vest < 0.1f) curve = 70.0f;
+            float tweaked = vest;
+            if (vest < 0.1f) {   // TweakVariance (:167-173)
+                float fe = clampf(vest, 0.0f, 1.0f);
+                float tt = 1.0f - fe;
+                tweaked = fe * dm_pow(tt, curve + 6.0f);
+            }
+            float phi = std::sqrt(fmaxg(0.0f, 0.000001f + tweaked));
+            phi /= phi_bias;
+            for (int x = -1; x <= 1; x++) {
+                for (int y = -1; y <= 1; y++) {
+                    if (x == 0 && y == 0) continue;
+                    float ox = ((float)x * (float)step) * add_scale + (float)jit * 0.5f;
+                    float oy = ((float)y * (float)step) * add_scale + (float)jit * 0.5f;
+                    v2 sc = v2{uv.x + ox * texel_x, uv.y + oy * texel_y};
+                    if (!(sc.x > 0.0f && sc.x < 1.0f && sc.y > 0.0f && sc.y < 1.0f)) continue;
+                    float sd;
+                    T.linear(sc, &sd);
+                    float dd = std::fabs(sd - bd);
+                    v3 sn = normal_from_id(F.nearest(sc), 1.0f);
+                    if ((bd < 0.0f) == (dd < 0.0f)) {
+                        float ssh[4], scc[2], sv;
+                        SH.linear(sc, ssh);
+                        CC.linear(sc, scc);
+                        float sl = sh_to_y(ssh);
+                        V.linear(sc, &sv);
+                        float nw = clampf(dm_pow(fmaxg(dot(bn, sn), 0.0f), 32.0f), 0.001f, 1.0f);
+                        float lw = std::fabs(sl - bl) / phi;
+                        float dw = clampf(dm_pow(dm_exp(-fmaxg(dd, 0.00001f)), 2.0f), 0.0001f, 1.0f);
+                        float wgt = strong ? nw * dw : (dm_exp(-lw) * nw) * dw;
+                        wgt = clampf(wgt, 0.001f, 1.0f);
+                        float xw = atrous_w[std::abs(x)], yw = atrous_w[std::abs(y)];
+                        wgt = (xw * yw) * wgt;
+                        wgt = fmaxg(wgt, 0.00000001f);
+                        for (int c = 0; c < 4; c++) tsh[c] += ssh[c] * wgt;
+                        for (int c = 0; c < 2; c++) tcc[c] += scc[c] * wgt;
+                        tvar += (wgt * wgt) * sv;
+                        tw += wgt;
+                        if (filter_sky || filter_ao) {
+                            float aw = clampf(((xw * yw) * nw) * dw, 0.000001f, 1.0f);
+                            float sao[2];
+                            AO.linear(sc, sao);
+                            tao[0] += sao[0] * aw;
+                            tao[1] += sao[1] * aw;
+                            taow += aw;
+                        }
+                    }
+                }
+            }
+            for (int c = 0; c < 4; c++) tsh[c] /= tw;
+            for (int c = 0; c < 2; c++) tcc[c] /= tw;
+            tvar /= (tw * tw);
+            tao[0] /= taow;
+            tao[1] /= taow;
+            if (!filter_ao) tao[0] = bao[0];
+            for (int c = 0; c < 4; c++) out->sh[px * 4 + c] = storage(clampf(tsh[c], -100.0f, 100.0f), fp16);
+            for (int c = 0; c < 2; c++) out->cocg[px * 2 + c] = storage(clampf(tcc[c], -10.0f, 100.0f), fp16);
+            out->variance[px] = storage(clampf(tvar, -1.0f, 50.0f), fp16);
+            out->aosky[px * 2 + 0] = storage(clampf(tao[0], 0.0f, 1.0f), fp16);
+            out->aosky[px * 2 + 1] = storage(clampf(tao[1], 0.0f, 1.0f), fp16);
+        }
+    }
+}
+
+// ColorPassFrag.glsl main (:747-1083), u_UseDFG on (Core/Pipeline.cpp:3683),
+// VXAO on with cutoff (:3669, :3679), flat materials, no specular input.
+void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
+                const vpto_frame* f, const float* t, const uint8_t* face, const uint8_t* block,
+                const uint8_t* shadow, const float* sh, const float* cocg, const float* aosky,
+                int row0, int row1, float* rgb) {
+    const int W = p->width, H = p->height;
+    const int fp16 = p->storage;
+    const v3 viewer = mk3(cam->position[0], cam->position[1], cam->position[2]);
+    const v3 r0 = ray_origin(cam);
+    const v3 sun = mk3(f->sun_dir[0], f->sun_dir[1], f->sun_dir[2]);
+    const v3 moon = moon_dir_of(sun);
+    const v3 sun_color = mk3(f->sun_radiance[0], f->sun_radiance[1], f->sun_radiance[2]);
+    const v3 moon_color = mk3(f->moon_radiance[0], f->moon_radiance[1], f->moon_radiance[2]);
+    float sun_vis = clampf(dot(sun, mk3(0.0f, 1.0f, 0.0f)) + 0.05f, 0.0f, 0.1f) * 12.0f;
+    sun_vis = 1.0f - sun_vis;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int j = row0; j < row1; j++) {
+        for (int i = 0; i < W; i++) {
+            size_t px = (size_t)j * W + i;
+            v2 uv = texcoord(i, j, W, H);
+            v3 dir = normalize(ray_dir_at(cam, uv));
+            // SamplePositionAt (:1122-1126) reads 1/t from the R32F depth plane
+            float dist = 1.0f / (1.0f / t[px]);
+            v3 wp = add(r0, muls(dir, dist));
+            v3 n = normal_from_id(face[px], 1.0f);
+            v3 color;
+            if (dist > 0.0f) {
+                int bid = std::min(std::max((int)block[px], 0), 127);
+                Material m = material(w, bid);
+                v3 albedo = basic_saturation(m.albedo, 1.0f - 0.1f);   // u_TextureDesatAmount = 0.1
+                if (m.metal >= 0.1f - 0.01f) albedo = basic_saturation(albedo, 0.9f);
+                float emissivity = (float)m.emissive;
+                float shy[4], cc[2];
+                for (int c = 0; c < 4; c++) shy[c] = sh[px * 4 + c];
+                cc[0] = cocg[px * 2 + 0];
+                cc[1] = cocg[px * 2 + 1];
+                float up_shadow = clampf((float)shadow[px], 0.0f, 1.0f);
+                float up_ao = aosky[px * 2 + 0];
+                float rt_shadow = clampf(clampf(up_shadow + 0.0f, 0.0f, 1.0f), 0.0f, 1.0f);
+                v3 indirect = sh_to_irradiance(shy, cc, n);
+                const float vb = 0.00125f;
+                if (uv.x > vb && uv.x < 1.0f - vb && uv.y > vb && uv.y < 1.0f - vb) {
+                    float ao = up_ao;
+                    float dxz = std::sqrt((wp.x - viewer.x) * (wp.x - viewer.x) + (wp.z - viewer.z) * (wp.z - viewer.z));
+                    float fade = dxz < 256.0f ? 0.0f : 1.0f;
+                    ao = mixf(ao, 1.0f, fade);
+                    ao = dm_pow(ao, 2.2f);
+                    indirect = muls(indirect, clampf(ao, 0.05f, 1.0f));
+                }
+                float sampled_ao = dm_pow(1.0f, 1.25f);
+                v3 sun_direct = directional_light(viewer, wp, sun, sun_color, sun_color, albedo, n, m.rough, m.metal, rt_shadow);
+                v3 moon_direct = directional_light(viewer, wp, moon, moon_color, moon_color, albedo, n, m.rough, m.metal, rt_shadow);
+                v3 direct = vmixv(sun_direct, moon_direct, mk3(sun_vis * 1.0f, sun_vis * 1.0f, sun_vis * 1.0f));
+                direct = muls(direct, (!(emissivity > 0.05f)) ? 1.0f : 0.0f);
+                direct = vmax(direct, 0.000001f);
+                float rough = m.rough;
+                v3 diffuse_indirect = mul(indirect, albedo);
+                v3 I = normalize(sub(wp, viewer));
+                float idn = dot(n, I);
+                v3 R = sub(I, muls(n, 2.0f * idn));
+                v3 spec_ind = vmax(mk3(0, 0, 0), 0.0001f);
+                v3 Lo = normalize(sub(viewer, wp));
+                v3 F0 = vmix(mk3(0.04f, 0.04f, 0.04f), albedo, m.metal);
+                diffuse_indirect = muls(diffuse_indirect, clampf(sampled_ao, 0.2f, 1.01f));
+                float nov = clampf(dot(n, Lo), 0.0000000001f, 1.0f);
+                // ComputeSpecularAO (:742-745), pbr.w (G-buffer AO) = 1 for flat materials
+                float spec_ao = clampf(dm_pow(nov + 1.0f, dm_exp2(-16.0f * rough - 1.0f)) - 1.0f + 1.0f, 0.0f, 1.0f);
+                spec_ao = dm_pow(spec_ao, 1.5f);
+                float horizon = fming(1.0f + dot(R, n), 1.0f);
+                horizon = (horizon * horizon) * horizon;
+                if (m.metal >= 0.1f) spec_ind = muls(spec_ind, 1.3f);
+                spec_ind = muls(spec_ind, spec_ao);
+                spec_ind = muls(spec_ind, horizon);
+                v3 F = vclamp(fresnel_schlick_roughness(Lo, n, F0, rough), 0.0f, 1.0f);
+                v3 kD = sub(mk3(1, 1, 1), F);
+                kD = muls(kD, 1.0f - m.metal);
+                float ex = clampf(fmaxg(dot(neg(I), n), 0.000001f), 0.0f, 1.0f);
+                float ey = clampf(rough, 0.0f, 1.0f);
+                v2 env = karis_env_brdf(ex, ey);
+                v3 ind_spec = mul(spec_ind, mk3(F.x * env.x + env.y, F.y * env.x + env.y, F.z * env.x + env.y));
+                v3 indirect_light = add(mul(kD, diffuse_indirect), ind_spec);
+                color = add(direct, indirect_light);
+            } else {
+                color = sky_radiance(dir);
+            }
+            color = vmax(color, 0.000001f);
+            rgb[px * 3 + 0] = storage(color.x, fp16);
+            rgb[px * 3 + 1] = storage(color.y, fp16);
+            rgb[px * 3 + 2] = storage(color.z, fp16);
+        }
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,168 @@
+/* CPU oracle for the VoxelPathTracer hot path -- C API.
+ *
+ * TEST INFRASTRUCTURE ONLY: a C++17 restatement of the reference shaders
+ * (Core/Shaders/ManhattanDistance{X,Y,Z}.comp, InitialRayTraceFrag.glsl,
+ * ShadowRayTraceFrag.glsl, DiffuseRayTraceFrag.glsl, Spatial3x3Initial.glsl,
+ * SVGF/{TemporalFilter,VarianceEstimate,SpatialFilter}.glsl, ColorPassFrag.glsl).
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it,
+ * as the checker or the timed CPU baseline; the product never does.
+ *
+ * Parity is unpinned by the reference itself: the reference has no tests,
+ * golden vectors or CPU implementation of this path, and its GLSL needs an
+ * OpenGL context. The oracle is pinned instead by analytic known-answer tests
+ * (tests/test_oracle_kat.py) and brute-force cross-checks.
+ *
+ * Struct layouts match include/vpt.h byte for byte so the same host buffers
+ * can be handed to both.
+ */
+#ifndef VPT_ORACLE_H
+#define VPT_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct vpto_camera {
+    float view[16];      /* column-major, m[col*4+row] */
+    float proj[16];
+    float inv_view[16];
+    float inv_proj[16];
+    float position[3];
+    float pad;
+} vpto_camera;
+
+typedef struct vpto_block {
+    uint8_t albedo[3];
+    uint8_t roughness;
+    uint8_t metalness;
+    uint8_t emissive;
+} vpto_block;
+
+typedef struct vpto_frame {
+    float sun_dir[3];
+    float time;
+    float sun_radiance[3];
+    uint32_t frame_index;
+    float moon_radiance[3];
+    uint32_t seed;
+    float gi_sun_strength;
+    float gi_sky_strength;
+    float diffuse_light_intensity;
+    int32_t temporal;
+} vpto_frame;
+
+typedef struct vpto_params {
+    int32_t width, height;
+    int32_t primary_max_steps;
+    int32_t shadow_max_steps;
+    int32_t diffuse_max_steps;
+    int32_t bounce_shadow_max_steps;
+    int32_t bounces;
+    int32_t spp;
+    int32_t storage;            /* 0 = fp32 planes, 1 = fp16 planes */
+    int32_t atrous_iterations;
+    float resolution_scale;
+    float color_phi_bias;
+    int32_t device;
+    int32_t reserved[3];
+} vpto_params;
+
+typedef struct vpto_world {
+    const uint8_t* vox;
+    const uint8_t* df;
+    int32_t X, Y, Z;
+    const vpto_block* blocks;
+    int32_t n_blocks;
+} vpto_world;
+
+/* Planes consumed / produced by the passes (W*H pixels, row 0 = bottom). */
+typedef struct vpto_gbuffer {
+    float* t;          /* hit distance, -1 on miss */
+    uint8_t* face;     /* 0..5 (+Z,-Z,+Y,-Y,-X,+X), 10 on miss */
+    uint8_t* block;    /* block id at the hit, 0 on miss */
+    int32_t* hit;      /* 3 per pixel: ivec3(floor(origin)) at loop exit */
+    uint16_t* steps;   /* DDA iterations executed */
+} vpto_gbuffer;
+
+typedef struct vpto_gi {   /* DiffuseRawTraceFBO-like planes */
+    float* sh;         /* 4 per pixel */
+    float* cocg;       /* 2 per pixel */
+    float* luma;       /* 1 per pixel (o_Utility) */
+    float* aosky;      /* 2 per pixel */
+} vpto_gi;
+
+typedef struct vpto_history {   /* DiffuseTemporalFBO-like planes */
+    float* sh;
+    float* cocg;
+    float* util;       /* 4 per pixel: accumulated frames, moment, luma, 0 */
+    float* aosky;
+} vpto_history;
+
+typedef struct vpto_filtered {  /* VarianceFBO / DiffuseDenoiseFBO-like planes */
+    float* sh;
+    float* cocg;
+    float* variance;
+    float* aosky;      /* unused by the variance pass */
+} vpto_filtered;
+
+int vpto_omp_threads(void);
+/* Counters (8 x uint64: rays then DDA steps for primary, shadow, diffuse,
+ * bounce shadow) that the trace functions add to; NULL disables counting. */
+void vpto_set_counters(uint64_t* counters);
+
+/* ManhattanDistance{X,Y,Z}.comp driven as in World::GenerateDistanceField. */
+void vpto_build_df(const uint8_t* vox, int X, int Y, int Z, uint8_t* df);
+
+/* InitialRayTraceFrag.glsl main, rows [row0, row1). */
+void vpto_trace_primary(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
+                        int row0, int row1, vpto_gbuffer* out);
+
+/* ShadowRayTraceFrag.glsl main (hard sun shadow, one ray per pixel). */
+void vpto_trace_shadow(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
+                       const vpto_frame* f, const float* t, const uint8_t* face,
+                       int row0, int row1, uint8_t* shadow);
+
+/* DiffuseRayTraceFrag.glsl main with CalculateDiffuse. */
+void vpto_trace_diffuse(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
+                        const vpto_frame* f, const float* t, const uint8_t* face,
+                        int row0, int row1, vpto_gi* out);
+
+/* Spatial3x3Initial.glsl */
+void vpto_spatial_initial(const vpto_camera* cam, const vpto_params* p,
+                          const float* t, const uint8_t* face, const vpto_gi* in, vpto_gi* out);
+
+/* SVGF/TemporalFilter.glsl */
+void vpto_temporal(const vpto_camera* cam, const vpto_camera* prev_cam, const vpto_params* p,
+                   const vpto_frame* f,
+                   const float* t, const uint8_t* face, const uint8_t* block,
+                   const float* prev_t, const uint8_t* prev_face, const uint8_t* prev_block,
+                   const vpto_gi* cur, const vpto_history* prev, vpto_history* out);
+
+/* SVGF/VarianceEstimate.glsl */
+void vpto_variance(const vpto_camera* cam, const vpto_params* p,
+                   const float* t, const uint8_t* face, const vpto_history* in, vpto_filtered* out);
+
+/* SVGF/SpatialFilter.glsl, one a-trous iteration with step `step`. */
+void vpto_atrous(const vpto_camera* cam, const vpto_params* p, const vpto_frame* f, int step,
+                 const float* t, const uint8_t* face, const float* temporal_util,
+                 const vpto_filtered* in, const float* in_aosky, vpto_filtered* out);
+
+/* ColorPassFrag.glsl main: direct GGX + indirect-diffuse combine, flat materials. */
+void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
+                const vpto_frame* f, const float* t, const uint8_t* face, const uint8_t* block,
+                const uint8_t* shadow, const float* sh, const float* cocg, const float* aosky,
+                int row0, int row1, float* rgb);
+
+/* Deterministic math, exported so tests can check its error bounds. */
+float vpto_exp(float x);
+float vpto_exp2(float x);
+float vpto_log2(float x);
+float vpto_pow(float x, float y);
+float vpto_sin(float x);
+float vpto_cos(float x);
+float vpto_half_round(float x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,207 @@
+"""Parity of every libvpt pass with the CPU oracle, through the C ABI.
+
+Traversal outputs (distance field, hit distance, face, block, hit voxel, step
+count, shadow) must be bit-identical. The radiance and filter planes are also
+held to bit-identity: libvpt and the oracle evaluate the same IEEE fp32
+operations in the same order (no fused multiply-add, IEEE division and square
+root, the same polynomial exp/log/sin/cos), so any difference is a bug. The
+FP16-storage variant is compared against the oracle emulating half stores.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+W, H = 96, 64
+DIMS = (64, 64, 64)   # X, Y, Z
+
+
+def same_bits(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    if a.dtype == np.float16:
+        a = a.astype(np.float32)
+    if b.dtype == np.float16:
+        b = b.astype(np.float32)
+    if a.dtype.kind == "f":
+        a32, b32 = a.astype(np.float32), b.astype(np.float32)
+        eq = (a32.view(np.uint32) == b32.view(np.uint32)) | (np.isnan(a32) & np.isnan(b32))
+        # +0 and -0 compare equal as values; only their sign bit differs
+        eq |= (a32 == 0) & (b32 == 0)
+        return eq
+    return a == b
+
+
+def assert_same(gpu, ref, what):
+    gpu = np.asarray(gpu).reshape(np.asarray(ref).shape)
+    eq = same_bits(gpu, ref)
+    if not eq.all():
+        bad = np.argwhere(~eq)
+        g = gpu.astype(np.float64)
+        r = np.asarray(ref).astype(np.float64)
+        diff = np.nanmax(np.abs(g - r)[~eq]) if g.dtype.kind == "f" else None
+        first = [tuple(int(v) for v in i) for i in bad[:5]]
+        vals = [(float(g[tuple(i)]), float(r[tuple(i)])) for i in bad[:5]]
+        pytest.fail(f"{what}: {len(bad)} of {eq.size} values differ; max |diff| {diff}; first {first} {vals}")
+
+
+@pytest.fixture(scope="module")
+def scene(vpt, oracle):
+    X, Y, Z = DIMS
+    vox = vpt.generate_world(X, Y, Z, seed=1)
+    blocks = vpt.generate_block_table(100, seed=1)
+    df = oracle.build_df(vox)
+    yaw, pitch = vpt.seeded_pose(1)
+    cam0 = vpt.camera_from_pose((X / 2, 58.0, Z / 2), yaw, pitch, 90.0, W / H)
+    cam1 = vpt.camera_from_pose((X / 2 + 0.7, 58.2, Z / 2 - 0.4), yaw + 2.0, pitch + 1.0, 90.0, W / H)
+    return {"vox": vox, "blocks": blocks, "df": df, "world": oracle.World(vox, df, blocks), "cams": [cam0, cam1]}
+
+
+def make_ctx(vpt, scene, storage):
+    ctx = vpt.Context(width=W, height=H, primary_max_steps=256, storage=storage)
+    ctx.upload_world(scene["vox"])
+    ctx.set_block_table(scene["blocks"])
+    ctx.build_df()
+    return ctx
+
+
+def test_distance_field_bit_exact(vpt, oracle, scene, gpu):
+    with make_ctx(vpt, scene, vpt.STORAGE_F32) as ctx:
+        assert_same(ctx.read_df(), scene["df"], "distance field")
+
+
+@pytest.mark.parametrize("dims", [(16, 16, 16), (37, 21, 50), (200, 40, 9), (1, 1, 1), (64, 1, 3)])
+def test_distance_field_shapes(vpt, oracle, dims, gpu):
+    X, Y, Z = dims
+    rng = np.random.default_rng(sum(dims))
+    vox = (rng.random((Z, Y, X)) < 0.02).astype(np.uint8) * rng.integers(1, 200, (Z, Y, X)).astype(np.uint8)
+    with vpt.Context(width=8, height=8) as ctx:
+        ctx.upload_world(vox)
+        ctx.set_block_table(vpt.generate_block_table(100, 0))
+        ctx.build_df()
+        assert_same(ctx.read_df(), oracle.build_df(vox), f"distance field {dims}")
+
+
+def test_distance_field_empty_and_full(vpt, oracle, gpu):
+    for fill in (0, 7):
+        vox = np.full((20, 30, 40), fill, np.uint8)
+        with vpt.Context(width=8, height=8) as ctx:
+            ctx.upload_world(vox)
+            ctx.set_block_table(vpt.generate_block_table(100, 0))
+            ctx.build_df()
+            got = ctx.read_df()
+        assert_same(got, oracle.build_df(vox), f"distance field fill={fill}")
+        assert (got == (0 if fill else min(254, 90))).all()
+
+
+@pytest.mark.parametrize("storage", [0, 1], ids=["f32", "f16"])
+def test_passes_bit_exact_two_frames(vpt, oracle, scene, storage, gpu):
+    world = scene["world"]
+    ctx = make_ctx(vpt, scene, storage)
+    cfg = ctx.config
+    prev_g, hist = oracle.empty_history(H, W)
+    prev_cam = scene["cams"][0]
+    for fi, cam in enumerate(scene["cams"]):
+        frame = vpt.default_frame(frame_index=fi, seed=11, time=1.3 + 0.37 * fi)
+        ctx.trace_primary(cam)
+        g = oracle.trace_primary(world, cam, cfg)
+        for name, plane in (("t", "T"), ("face", "FACE"), ("block", "BLOCK"), ("hit", "HIT"), ("steps", "STEPS")):
+            assert_same(ctx.read_plane(plane), g[name], f"frame {fi} primary {name}")
+        ctx.trace_shadow(frame)
+        shadow = oracle.trace_shadow(world, cam, cfg, frame, g["t"], g["face"])
+        assert_same(ctx.read_plane("SHADOW"), shadow, f"frame {fi} shadow")
+        ctx.trace_diffuse(frame)
+        gi = oracle.trace_diffuse(world, cam, cfg, frame, g["t"], g["face"])
+        for k in ("sh", "cocg", "luma", "aosky"):
+            assert_same(ctx.read_plane("GI_" + k.upper()), gi[k], f"frame {fi} diffuse {k}")
+        ctx.svgf(prev_cam, frame)
+        sv = oracle.svgf(cam, prev_cam, cfg, frame, g, prev_g, gi, hist)
+        for k in ("sh", "cocg", "luma", "aosky"):
+            assert_same(ctx.read_plane("PRE_" + k.upper()), sv["pre"][k], f"frame {fi} pre-temporal {k}")
+        for k in ("sh", "cocg", "util", "aosky"):
+            assert_same(ctx.read_plane("TEMP_" + k.upper()), sv["temporal"][k], f"frame {fi} temporal {k}")
+        for k in ("sh", "cocg", "variance"):
+            assert_same(ctx.read_plane("VAR_" + k.upper()), sv["variance"][k], f"frame {fi} variance {k}")
+        last = sv["atrous"][-1]
+        for k in ("sh", "cocg", "variance", "aosky"):
+            assert_same(ctx.read_plane("DEN_" + k.upper()), last[k], f"frame {fi} a-trous {k}")
+        ctx.shade(frame)
+        rgb = oracle.shade(world, cam, cfg, frame, g["t"], g["face"], g["block"], shadow, last["sh"], last["cocg"],
+                           last["aosky"])
+        assert_same(ctx.read_plane("COLOR"), rgb, f"frame {fi} colour")
+        ctx.end_frame()
+        prev_g = {"t": g["t"], "face": g["face"], "block": g["block"]}
+        hist = sv["temporal"]
+        prev_cam = cam
+    ctx.close()
+
+
+def test_render_frame_matches_oracle(vpt, oracle, scene, gpu):
+    world = scene["world"]
+    ctx = make_ctx(vpt, scene, vpt.STORAGE_F32)
+    prev_g, hist = oracle.empty_history(H, W)
+    prev_cam = scene["cams"][0]
+    for fi, cam in enumerate(scene["cams"]):
+        frame = vpt.default_frame(frame_index=fi, seed=3, time=0.5 * fi)
+        rgb = ctx.render_frame(cam, frame)
+        ref = oracle.render_frame(world, cam, prev_cam, ctx.config, frame, prev_g, hist)
+        assert_same(rgb, ref["rgb"], f"render_frame {fi}")
+        prev_g = {k: ref["g"][k] for k in ("t", "face", "block")}
+        hist = ref["svgf"]["temporal"]
+        prev_cam = cam
+    ctx.close()
+
+
+def test_primary_steps_cap_and_inside_solid(vpt, oracle, scene, gpu):
+    """A camera buried in stone misses everywhere (InitialRayTraceFrag.glsl:322-335);
+    a tiny step cap truncates every ray at the cap."""
+    world = scene["world"]
+    with make_ctx(vpt, scene, vpt.STORAGE_F32) as ctx:
+        cam = vpt.camera_from_pose((10.5, 5.5, 10.5), 30.0, 10.0, 90.0, W / H)
+        ctx.trace_primary(cam)
+        assert (ctx.read_plane("T") == -1).all()
+        assert (ctx.read_plane("STEPS") == 0).all()
+    with vpt.Context(width=W, height=H, primary_max_steps=3) as ctx:
+        ctx.upload_world(scene["vox"])
+        ctx.set_block_table(scene["blocks"])
+        ctx.build_df()
+        cam = scene["cams"][0]
+        ctx.trace_primary(cam)
+        g = oracle.trace_primary(world, cam, ctx.config)
+        assert_same(ctx.read_plane("STEPS"), g["steps"], "capped steps")
+        assert_same(ctx.read_plane("HIT"), g["hit"], "capped hit voxel")
+        assert ctx.read_plane("STEPS").max() <= 3
+
+
+def test_detmath_device_equals_host(vpt, gpu):
+    rng = np.random.default_rng(5)
+    xs = {
+        0: rng.uniform(-110, 90, 20000).astype(np.float32),
+        1: rng.uniform(-160, 130, 20000).astype(np.float32),
+        2: np.exp(rng.uniform(-100, 80, 20000)).astype(np.float32),
+        3: rng.uniform(0, 3, 20000).astype(np.float32),
+        4: rng.uniform(-50, 50, 20000).astype(np.float32),
+        5: rng.uniform(-50, 50, 20000).astype(np.float32),
+    }
+    y = rng.uniform(-4, 140, 20000).astype(np.float32)
+    for op, x in xs.items():
+        host = vpt.detmath(op, x, y, on_device=False)
+        dev = vpt.detmath(op, x, y, on_device=True)
+        assert_same(dev, host, f"detmath op {op}")
+
+
+def test_stats_count_rays(vpt, oracle, scene, gpu):
+    with make_ctx(vpt, scene, vpt.STORAGE_F32) as ctx:
+        ctx.set_stats(True)
+        cam = scene["cams"][0]
+        frame = vpt.default_frame()
+        ctx.trace_primary(cam)
+        ctx.trace_shadow(frame)
+        ctx.trace_diffuse(frame)
+        s = ctx.read_stats()
+        steps = ctx.read_plane("STEPS")
+        assert s["rays"]["primary"] == W * H
+        assert s["steps"]["primary"] == int(steps.astype(np.int64).sum())
+        hits = int((ctx.read_plane("T") > 0).sum())
+        assert s["rays"]["diffuse"] == hits   # 1 spp, 1 bounce: one GI ray per hit pixel
+        assert 0 < s["rays"]["shadow"] <= hits

@@ -1,0 +1,374 @@
+"""GB300-native VoxelPathTracer hot path: Python host over the libvpt C ABI.
+
+The reference (swr06/VoxelPathTracer) drives its hot path from
+Core/Pipeline.cpp: World::Buffer uploads the voxel volume, World::
+GenerateDistanceField builds the Manhattan distance field, and each frame runs
+the initial (G-buffer) trace, the sun-shadow and diffuse-GI traces, the SVGF
+denoiser and the colour pass, then swaps its history framebuffers. `Context`
+exposes exactly those steps over libvpt (include/vpt.h); every call goes
+through the C ABI into hand-written sm_103a kernels. There is no CPU fallback:
+importing this package without a built libvpt raises.
+
+Arrays: voxel volumes are numpy uint8 of shape (Z, Y, X) (x fastest, as
+Core/World.h:46-49 lays them out); image planes are (H, W, C) with row 0 at
+the bottom (OpenGL convention).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libvpt.so"
+
+# ------------------------------------------------------------------ enums --
+OK, ERR_INVALID_ARG, ERR_OOM, ERR_DEVICE_TIMEOUT, ERR_CUDA, ERR_STATE, ERR_NO_DEVICE = range(7)
+STORAGE_F32, STORAGE_F16 = 0, 1
+DTYPE_F32, DTYPE_F16, DTYPE_U8, DTYPE_U16, DTYPE_I32 = range(5)
+_NP_DTYPE = {DTYPE_F32: np.float32, DTYPE_F16: np.float16, DTYPE_U8: np.uint8, DTYPE_U16: np.uint16,
+             DTYPE_I32: np.int32}
+
+PLANES = [
+    "T", "FACE", "BLOCK", "HIT", "STEPS", "SHADOW",
+    "GI_SH", "GI_COCG", "GI_LUMA", "GI_AOSKY",
+    "PRE_SH", "PRE_COCG", "PRE_LUMA", "PRE_AOSKY",
+    "TEMP_SH", "TEMP_COCG", "TEMP_UTIL", "TEMP_AOSKY",
+    "HIST_SH", "HIST_COCG", "HIST_UTIL", "HIST_AOSKY",
+    "PREV_T", "PREV_FACE", "PREV_BLOCK",
+    "VAR_SH", "VAR_COCG", "VAR_VARIANCE",
+    "DEN_SH", "DEN_COCG", "DEN_VARIANCE", "DEN_AOSKY",
+    "COLOR",
+]
+PLANE = {name: i for i, name in enumerate(PLANES)}
+PASSES = ["primary", "shadow", "diffuse", "spatial_initial", "temporal", "variance", "atrous", "shade"]
+FACE_MISS = 10
+
+
+# ---------------------------------------------------------------- structs --
+class Config(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("primary_max_steps", C.c_int32),
+                ("shadow_max_steps", C.c_int32), ("diffuse_max_steps", C.c_int32),
+                ("bounce_shadow_max_steps", C.c_int32), ("bounces", C.c_int32), ("spp", C.c_int32),
+                ("storage", C.c_int32), ("atrous_iterations", C.c_int32), ("resolution_scale", C.c_float),
+                ("color_phi_bias", C.c_float), ("device", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("view", C.c_float * 16), ("proj", C.c_float * 16), ("inv_view", C.c_float * 16),
+                ("inv_proj", C.c_float * 16), ("position", C.c_float * 3), ("pad", C.c_float)]
+
+
+class Block(C.Structure):
+    _fields_ = [("albedo", C.c_uint8 * 3), ("roughness", C.c_uint8), ("metalness", C.c_uint8),
+                ("emissive", C.c_uint8)]
+
+
+class Frame(C.Structure):
+    _fields_ = [("sun_dir", C.c_float * 3), ("time", C.c_float), ("sun_radiance", C.c_float * 3),
+                ("frame_index", C.c_uint32), ("moon_radiance", C.c_float * 3), ("seed", C.c_uint32),
+                ("gi_sun_strength", C.c_float), ("gi_sky_strength", C.c_float),
+                ("diffuse_light_intensity", C.c_float), ("temporal", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("rays", C.c_uint64 * 4), ("steps", C.c_uint64 * 4)]
+
+
+BLOCK_DTYPE = np.dtype([("albedo", np.uint8, 3), ("roughness", np.uint8), ("metalness", np.uint8),
+                        ("emissive", np.uint8)])
+
+
+class VPTError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        super().__init__(f"{what}: status {status}")
+        self.status = status
+
+
+def _load() -> C.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(f"libvpt is not built ({LIB_PATH} missing); run __graft_entry__.build() or "
+                          "python -m voxelpathtracer_gb300._build")
+    lib = C.CDLL(str(LIB_PATH))
+    P = C.c_void_p
+    i32, u64, f32, sz = C.c_int32, C.c_uint64, C.c_float, C.c_size_t
+    sigs = {
+        "vpt_status_string": ([C.c_int], C.c_char_p),
+        "vpt_abi_version": ([], C.c_int),
+        "vpt_default_config": ([C.POINTER(Config)], C.c_int),
+        "vpt_default_frame": ([C.POINTER(Frame)], C.c_int),
+        "vpt_create": ([C.POINTER(P), C.POINTER(Config)], C.c_int),
+        "vpt_destroy": ([P], C.c_int),
+        "vpt_last_error": ([P], C.c_char_p),
+        "vpt_upload_world": ([P, P, i32, i32, i32], C.c_int),
+        "vpt_set_block_table": ([P, P, i32], C.c_int),
+        "vpt_build_df": ([P], C.c_int),
+        "vpt_read_df": ([P, P, sz], C.c_int),
+        "vpt_df_build_device": ([P, P, i32, i32, i32, P], C.c_int),
+        "vpt_trace_primary": ([P, C.POINTER(Camera)], C.c_int),
+        "vpt_trace_shadow": ([P, C.POINTER(Frame)], C.c_int),
+        "vpt_trace_diffuse": ([P, C.POINTER(Frame)], C.c_int),
+        "vpt_svgf": ([P, C.POINTER(Camera), C.POINTER(Frame)], C.c_int),
+        "vpt_shade": ([P, C.POINTER(Frame)], C.c_int),
+        "vpt_end_frame": ([P], C.c_int),
+        "vpt_reset_history": ([P], C.c_int),
+        "vpt_render_frame": ([P, C.POINTER(Camera), C.POINTER(Frame), P], C.c_int),
+        "vpt_plane_info": ([P, i32, C.POINTER(sz), C.POINTER(i32), C.POINTER(i32)], C.c_int),
+        "vpt_read_plane": ([P, i32, P, sz], C.c_int),
+        "vpt_write_plane": ([P, i32, P, sz], C.c_int),
+        "vpt_plane_device_ptr": ([P, i32, C.POINTER(P)], C.c_int),
+        "vpt_synchronize": ([P], C.c_int),
+        "vpt_set_stats": ([P, i32], C.c_int),
+        "vpt_read_stats": ([P, C.POINTER(Stats)], C.c_int),
+        "vpt_set_profiling": ([P, i32], C.c_int),
+        "vpt_read_pass_times": ([P, C.POINTER(f32), i32], C.c_int),
+        "vpt_launch_count": ([P, C.POINTER(u64)], C.c_int),
+        "vpt_get_stream": ([P, C.POINTER(P)], C.c_int),
+        "vpt_detmath": ([i32, P, P, P, i32, i32], C.c_int),
+        "vpt_generate_world": ([P, i32, i32, i32, u64, i32], C.c_int),
+        "vpt_generate_block_table": ([P, i32, u64], C.c_int),
+        "vpt_camera_from_pose": ([C.POINTER(Camera), C.POINTER(f32), f32, f32, f32, f32, f32, f32], C.c_int),
+    }
+    for name, (argtypes, restype) in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = argtypes
+        fn.restype = restype
+    return lib
+
+
+lib = _load()
+EXPORTED = None  # filled lazily by tests
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _check(status: int, what: str, ctx=None):
+    if status != OK:
+        msg = lib.vpt_status_string(status).decode()
+        if ctx is not None:
+            detail = lib.vpt_last_error(ctx)
+            if detail:
+                msg += f" ({detail.decode()})"
+        raise VPTError(status, f"{what} failed: {msg}")
+
+
+# ------------------------------------------------------------ host helpers --
+def default_config(**kw) -> Config:
+    cfg = Config()
+    _check(lib.vpt_default_config(C.byref(cfg)), "vpt_default_config")
+    for k, v in kw.items():
+        if not hasattr(cfg, k):
+            raise AttributeError(f"unknown config field {k}")
+        setattr(cfg, k, v)
+    return cfg
+
+
+def default_frame(**kw) -> Frame:
+    f = Frame()
+    _check(lib.vpt_default_frame(C.byref(f)), "vpt_default_frame")
+    for k, v in kw.items():
+        if k in ("sun_dir", "sun_radiance", "moon_radiance"):
+            getattr(f, k)[:] = [float(x) for x in v]
+        else:
+            setattr(f, k, v)
+    return f
+
+
+def generate_world(X: int, Y: int, Z: int, seed: int = 0, n_blocks: int = 100) -> np.ndarray:
+    """Seeded value-noise terrain, shape (Z, Y, X) uint8 (vpt_generate_world)."""
+    out = np.empty((Z, Y, X), dtype=np.uint8)
+    _check(lib.vpt_generate_world(_ptr(out), X, Y, Z, seed, n_blocks), "vpt_generate_world")
+    return out
+
+
+def generate_block_table(n: int = 100, seed: int = 0) -> np.ndarray:
+    """Seeded flat block table as a structured array (vpt_generate_block_table)."""
+    out = np.zeros(n, dtype=BLOCK_DTYPE)
+    _check(lib.vpt_generate_block_table(_ptr(out), n, seed), "vpt_generate_block_table")
+    return out
+
+
+def camera_from_pose(position, yaw_deg: float, pitch_deg: float, fov_deg: float = 90.0, aspect: float = 16 / 9,
+                     znear: float = 0.1, zfar: float = 1000.0) -> Camera:
+    cam = Camera()
+    pos = (C.c_float * 3)(*[float(p) for p in position])
+    _check(lib.vpt_camera_from_pose(C.byref(cam), pos, yaw_deg, pitch_deg, fov_deg, aspect, znear, zfar),
+           "vpt_camera_from_pose")
+    return cam
+
+
+def seeded_pose(seed: int, yaw_range=(0.0, 360.0), pitch_range=(-40.0, -10.0)):
+    """Yaw and pitch drawn uniformly from the seed (the bench's camera rule)."""
+    rng = np.random.default_rng(seed)
+    return float(rng.uniform(*yaw_range)), float(rng.uniform(*pitch_range))
+
+
+def detmath(op: int, x: np.ndarray, y: np.ndarray | None = None, on_device: bool = False) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    yy = np.ascontiguousarray(y if y is not None else np.zeros_like(x), dtype=np.float32)
+    out = np.empty_like(x)
+    _check(lib.vpt_detmath(op, _ptr(x), _ptr(yy), _ptr(out), x.size, 1 if on_device else 0), "vpt_detmath")
+    return out
+
+
+# ---------------------------------------------------------------- context --
+class Context:
+    """One libvpt context: device buffers for a world and a W x H frame.
+
+    Method names follow the steps of the reference's frame loop:
+      upload_world     World::Buffer            (Core/World.h:167-171)
+      set_block_table  BlockDataSSBO::CreateBuffers (Core/BlockDataSSBO.cpp:5-37)
+      build_df         World::GenerateDistanceField (Core/World.cpp:69-113)
+      trace_primary    initial trace pass       (Core/Pipeline.cpp:1959-2016)
+      trace_shadow     shadow trace pass        (Core/Pipeline.cpp:2790-2850)
+      trace_diffuse    diffuse GI trace pass    (Core/Pipeline.cpp:2169-2281)
+      svgf             SVGF denoiser            (Core/Pipeline.cpp:2284-2615)
+      shade            colour pass              (Core/Pipeline.cpp:3603-3821)
+      end_frame        history ping-pong        (Core/Pipeline.cpp:1775-1788)
+    """
+
+    def __init__(self, config: Config | None = None, **overrides):
+        cfg = config if config is not None else default_config()
+        for k, v in overrides.items():
+            setattr(cfg, k, v)
+        self.config = cfg
+        self._h = C.c_void_p()
+        _check(lib.vpt_create(C.byref(self._h), C.byref(cfg)), "vpt_create")
+        self.width, self.height = cfg.width, cfg.height
+        self.world_shape = None
+
+    # lifetime
+    def close(self):
+        if self._h:
+            lib.vpt_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, status, what):
+        _check(status, what, self._h)
+
+    # world
+    def upload_world(self, voxels: np.ndarray):
+        v = np.ascontiguousarray(voxels, dtype=np.uint8)
+        if v.ndim != 3:
+            raise ValueError("voxels must have shape (Z, Y, X)")
+        Z, Y, X = v.shape
+        self._ck(lib.vpt_upload_world(self._h, _ptr(v), X, Y, Z), "vpt_upload_world")
+        self.world_shape = (Z, Y, X)
+
+    def set_block_table(self, table: np.ndarray):
+        t = np.ascontiguousarray(table, dtype=BLOCK_DTYPE)
+        self._ck(lib.vpt_set_block_table(self._h, _ptr(t), t.size), "vpt_set_block_table")
+
+    def build_df(self):
+        self._ck(lib.vpt_build_df(self._h), "vpt_build_df")
+
+    def read_df(self) -> np.ndarray:
+        out = np.empty(self.world_shape, dtype=np.uint8)
+        self._ck(lib.vpt_read_df(self._h, _ptr(out), out.nbytes), "vpt_read_df")
+        return out
+
+    # passes
+    def trace_primary(self, cam: Camera):
+        self._ck(lib.vpt_trace_primary(self._h, C.byref(cam)), "vpt_trace_primary")
+
+    def trace_shadow(self, frame: Frame):
+        self._ck(lib.vpt_trace_shadow(self._h, C.byref(frame)), "vpt_trace_shadow")
+
+    def trace_diffuse(self, frame: Frame):
+        self._ck(lib.vpt_trace_diffuse(self._h, C.byref(frame)), "vpt_trace_diffuse")
+
+    def svgf(self, prev_cam: Camera | None, frame: Frame):
+        self._ck(lib.vpt_svgf(self._h, C.byref(prev_cam) if prev_cam is not None else None, C.byref(frame)),
+                 "vpt_svgf")
+
+    def shade(self, frame: Frame):
+        self._ck(lib.vpt_shade(self._h, C.byref(frame)), "vpt_shade")
+
+    def end_frame(self):
+        self._ck(lib.vpt_end_frame(self._h), "vpt_end_frame")
+
+    def reset_history(self):
+        self._ck(lib.vpt_reset_history(self._h), "vpt_reset_history")
+
+    def render_frame(self, cam: Camera, frame: Frame, out: np.ndarray | None = None, readback: bool = True):
+        if readback and out is None:
+            out = np.empty((self.height, self.width, 3), dtype=np.float32)
+        ptr = _ptr(out) if readback else None
+        self._ck(lib.vpt_render_frame(self._h, C.byref(cam), C.byref(frame), ptr), "vpt_render_frame")
+        return out
+
+    # planes
+    def plane_info(self, plane):
+        pid = PLANE[plane] if isinstance(plane, str) else int(plane)
+        nbytes, ch, dt = C.c_size_t(), C.c_int32(), C.c_int32()
+        self._ck(lib.vpt_plane_info(self._h, pid, C.byref(nbytes), C.byref(ch), C.byref(dt)), "vpt_plane_info")
+        return pid, nbytes.value, ch.value, _NP_DTYPE[dt.value]
+
+    def read_plane(self, plane) -> np.ndarray:
+        pid, nbytes, ch, dt = self.plane_info(plane)
+        out = np.empty((self.height, self.width, ch), dtype=dt)
+        self._ck(lib.vpt_read_plane(self._h, pid, _ptr(out), out.nbytes), "vpt_read_plane")
+        return out
+
+    def write_plane(self, plane, data: np.ndarray):
+        pid, nbytes, ch, dt = self.plane_info(plane)
+        a = np.ascontiguousarray(np.asarray(data).reshape(self.height, self.width, ch), dtype=dt)
+        self._ck(lib.vpt_write_plane(self._h, pid, _ptr(a), a.nbytes), "vpt_write_plane")
+
+    # instrumentation
+    def synchronize(self):
+        self._ck(lib.vpt_synchronize(self._h), "vpt_synchronize")
+
+    def set_stats(self, enabled: bool):
+        self._ck(lib.vpt_set_stats(self._h, 1 if enabled else 0), "vpt_set_stats")
+
+    def read_stats(self) -> dict:
+        s = Stats()
+        self._ck(lib.vpt_read_stats(self._h, C.byref(s)), "vpt_read_stats")
+        kinds = ["primary", "shadow", "diffuse", "bounce_shadow"]
+        return {"rays": dict(zip(kinds, list(s.rays))), "steps": dict(zip(kinds, list(s.steps)))}
+
+    def set_profiling(self, enabled: bool):
+        self._ck(lib.vpt_set_profiling(self._h, 1 if enabled else 0), "vpt_set_profiling")
+
+    def pass_times(self) -> dict:
+        arr = (C.c_float * len(PASSES))()
+        self._ck(lib.vpt_read_pass_times(self._h, arr, len(PASSES)), "vpt_read_pass_times")
+        return dict(zip(PASSES, list(arr)))
+
+    def launch_count(self) -> int:
+        v = C.c_uint64()
+        self._ck(lib.vpt_launch_count(self._h, C.byref(v)), "vpt_launch_count")
+        return int(v.value)
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        self._ck(lib.vpt_get_stream(self._h, C.byref(p)), "vpt_get_stream")
+        return p.value or 0
+
+
+def device_available() -> bool:
+    """True when a CUDA device can be opened by libvpt."""
+    h = C.c_void_p()
+    cfg = default_config(width=8, height=8)
+    st = lib.vpt_create(C.byref(h), C.byref(cfg))
+    if st == OK:
+        lib.vpt_destroy(h)
+        return True
+    return False

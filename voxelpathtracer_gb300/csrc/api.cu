@@ -1,0 +1,854 @@
+// libvpt C ABI: context, device buffers, pass sequencing and instrumentation.
+// The per-frame pass order and the ping-pong history follow Core/Pipeline.cpp
+// (initial trace :1959-2016, diffuse :2169-2281, SVGF :2284-2615, shadow
+// :2790-2850, colour :3603-3821, swaps :1775-1788 and :1970-1971).
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "vpt.h"
+
+using namespace vpt;
+
+namespace {
+
+enum GB { GB_T = 0, GB_FACE, GB_BLOCK, GB_HIT, GB_STEPS, GB_N };
+enum GI { GI_SH = 0, GI_COCG, GI_LUMA, GI_AOSKY, GI_N };
+enum HI { HI_SH = 0, HI_COCG, HI_UTIL, HI_AOSKY, HI_N };
+enum FI { FI_SH = 0, FI_COCG, FI_VAR, FI_AOSKY, FI_N };
+
+struct PlaneMeta {
+    int channels;
+    int typed;    // 1: storage type (f32/f16); 0: fixed dtype below
+    int dtype;
+};
+
+PlaneMeta plane_meta(int plane) {
+    switch (plane) {
+        case VPT_PLANE_T: case VPT_PLANE_PREV_T: return {1, 1, 0};
+        case VPT_PLANE_FACE: case VPT_PLANE_BLOCK: case VPT_PLANE_SHADOW:
+        case VPT_PLANE_PREV_FACE: case VPT_PLANE_PREV_BLOCK: return {1, 0, VPT_DTYPE_U8};
+        case VPT_PLANE_HIT: return {3, 0, VPT_DTYPE_I32};
+        case VPT_PLANE_STEPS: return {1, 0, VPT_DTYPE_U16};
+        case VPT_PLANE_GI_SH: case VPT_PLANE_PRE_SH: case VPT_PLANE_TEMP_SH: case VPT_PLANE_HIST_SH:
+        case VPT_PLANE_VAR_SH: case VPT_PLANE_DEN_SH: return {4, 1, 0};
+        case VPT_PLANE_TEMP_UTIL: case VPT_PLANE_HIST_UTIL: return {4, 1, 0};
+        case VPT_PLANE_GI_COCG: case VPT_PLANE_PRE_COCG: case VPT_PLANE_TEMP_COCG: case VPT_PLANE_HIST_COCG:
+        case VPT_PLANE_VAR_COCG: case VPT_PLANE_DEN_COCG: return {2, 1, 0};
+        case VPT_PLANE_GI_AOSKY: case VPT_PLANE_PRE_AOSKY: case VPT_PLANE_TEMP_AOSKY: case VPT_PLANE_HIST_AOSKY:
+        case VPT_PLANE_DEN_AOSKY: return {2, 1, 0};
+        case VPT_PLANE_GI_LUMA: case VPT_PLANE_PRE_LUMA: case VPT_PLANE_VAR_VARIANCE:
+        case VPT_PLANE_DEN_VARIANCE: return {1, 1, 0};
+        case VPT_PLANE_COLOR: return {3, 1, 0};
+        default: return {0, 0, -1};
+    }
+}
+
+size_t dtype_size(int dtype) {
+    switch (dtype) {
+        case VPT_DTYPE_F32: case VPT_DTYPE_I32: return 4;
+        case VPT_DTYPE_F16: case VPT_DTYPE_U16: return 2;
+        case VPT_DTYPE_U8: return 1;
+        default: return 0;
+    }
+}
+
+}  // namespace
+
+struct vpt_ctx {
+    vpt_config cfg{};
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int fp16 = 0;
+    size_t npx = 0;
+    // world
+    uint8_t* vox = nullptr;
+    uint8_t* df = nullptr;
+    int X = 0, Y = 0, Z = 0;
+    bool df_valid = false;
+    vpt_block* blocks = nullptr;
+    int n_blocks = 0;
+    // planes
+    void* gbuf[2][GB_N] = {};
+    uint8_t* shadow = nullptr;
+    void* gi[GI_N] = {};
+    void* pre[GI_N] = {};
+    void* hist[2][HI_N] = {};
+    void* var[FI_N] = {};
+    void* den[2][FI_N] = {};
+    void* color = nullptr;
+    int cur = 0;        // index of this frame's G-buffer / temporal output
+    int den_last = 0;   // den set holding the last a-trous output
+    // cameras
+    vpt_camera cam{};
+    bool have_cam = false;
+    vpt_camera prev_cam{};
+    bool have_prev = false;
+    // instrumentation
+    Counters* counters = nullptr;
+    bool stats = false;
+    bool profiling = false;
+    cudaEvent_t ev[VPT_PASS_COUNT][2] = {};
+    bool ev_used[VPT_PASS_COUNT] = {};
+    uint64_t launches = 0;
+    std::vector<void*> allocs;
+    std::vector<float> host_staging;
+};
+
+namespace {
+
+vpt_status fail(vpt_ctx* c, vpt_status s, const char* fmt, ...) {
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return s;
+}
+
+#define CK(ctx, call)                                                                         \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail((ctx), e_ == cudaErrorMemoryAllocation ? VPT_ERR_OOM : VPT_ERR_CUDA,  \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+vpt_status dalloc(vpt_ctx* c, void** p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(c, e == cudaErrorMemoryAllocation ? VPT_ERR_OOM : VPT_ERR_CUDA, "cudaMalloc(%zu): %s", bytes,
+                    cudaGetErrorString(e));
+    }
+    c->allocs.push_back(*p);
+    return VPT_OK;
+}
+
+CamView cam_view(const vpt_camera& c) {
+    CamView v;
+    memcpy(v.inv_view, c.inv_view, sizeof v.inv_view);
+    memcpy(v.inv_proj, c.inv_proj, sizeof v.inv_proj);
+    v.pos[0] = c.position[0];
+    v.pos[1] = c.position[1];
+    v.pos[2] = c.position[2];
+    return v;
+}
+
+WorldView world_view(const vpt_ctx* c) {
+    WorldView w;
+    w.vox = c->vox;
+    w.df = c->df;
+    w.X = c->X;
+    w.Y = c->Y;
+    w.Z = c->Z;
+    w.blocks = c->blocks;
+    w.n_blocks = c->n_blocks;
+    return w;
+}
+
+void* plane_ptr(vpt_ctx* c, int plane) {
+    int cur = c->cur, prv = 1 - c->cur;
+    switch (plane) {
+        case VPT_PLANE_T: return c->gbuf[cur][GB_T];
+        case VPT_PLANE_FACE: return c->gbuf[cur][GB_FACE];
+        case VPT_PLANE_BLOCK: return c->gbuf[cur][GB_BLOCK];
+        case VPT_PLANE_HIT: return c->gbuf[cur][GB_HIT];
+        case VPT_PLANE_STEPS: return c->gbuf[cur][GB_STEPS];
+        case VPT_PLANE_SHADOW: return c->shadow;
+        case VPT_PLANE_GI_SH: return c->gi[GI_SH];
+        case VPT_PLANE_GI_COCG: return c->gi[GI_COCG];
+        case VPT_PLANE_GI_LUMA: return c->gi[GI_LUMA];
+        case VPT_PLANE_GI_AOSKY: return c->gi[GI_AOSKY];
+        case VPT_PLANE_PRE_SH: return c->pre[GI_SH];
+        case VPT_PLANE_PRE_COCG: return c->pre[GI_COCG];
+        case VPT_PLANE_PRE_LUMA: return c->pre[GI_LUMA];
+        case VPT_PLANE_PRE_AOSKY: return c->pre[GI_AOSKY];
+        case VPT_PLANE_TEMP_SH: return c->hist[cur][HI_SH];
+        case VPT_PLANE_TEMP_COCG: return c->hist[cur][HI_COCG];
+        case VPT_PLANE_TEMP_UTIL: return c->hist[cur][HI_UTIL];
+        case VPT_PLANE_TEMP_AOSKY: return c->hist[cur][HI_AOSKY];
+        case VPT_PLANE_HIST_SH: return c->hist[prv][HI_SH];
+        case VPT_PLANE_HIST_COCG: return c->hist[prv][HI_COCG];
+        case VPT_PLANE_HIST_UTIL: return c->hist[prv][HI_UTIL];
+        case VPT_PLANE_HIST_AOSKY: return c->hist[prv][HI_AOSKY];
+        case VPT_PLANE_PREV_T: return c->gbuf[prv][GB_T];
+        case VPT_PLANE_PREV_FACE: return c->gbuf[prv][GB_FACE];
+        case VPT_PLANE_PREV_BLOCK: return c->gbuf[prv][GB_BLOCK];
+        case VPT_PLANE_VAR_SH: return c->var[FI_SH];
+        case VPT_PLANE_VAR_COCG: return c->var[FI_COCG];
+        case VPT_PLANE_VAR_VARIANCE: return c->var[FI_VAR];
+        case VPT_PLANE_DEN_SH: return c->den[c->den_last][FI_SH];
+        case VPT_PLANE_DEN_COCG: return c->den[c->den_last][FI_COCG];
+        case VPT_PLANE_DEN_VARIANCE: return c->den[c->den_last][FI_VAR];
+        case VPT_PLANE_DEN_AOSKY: return c->den[c->den_last][FI_AOSKY];
+        case VPT_PLANE_COLOR: return c->color;
+        default: return nullptr;
+    }
+}
+
+size_t plane_bytes(const vpt_ctx* c, int plane, int* channels, int* dtype) {
+    PlaneMeta m = plane_meta(plane);
+    if (m.channels == 0) return 0;
+    int dt = m.typed ? (c->fp16 ? VPT_DTYPE_F16 : VPT_DTYPE_F32) : m.dtype;
+    if (channels) *channels = m.channels;
+    if (dtype) *dtype = dt;
+    return c->npx * (size_t)m.channels * dtype_size(dt);
+}
+
+vpt_status alloc_planes(vpt_ctx* c) {
+    const size_t n = c->npx, es = c->fp16 ? 2 : 4;
+    vpt_status s;
+#define A(ptr, bytes) \
+    if ((s = dalloc(c, (void**)&(ptr), (bytes))) != VPT_OK) return s
+    for (int k = 0; k < 2; k++) {
+        A(c->gbuf[k][GB_T], n * es);
+        A(c->gbuf[k][GB_FACE], n);
+        A(c->gbuf[k][GB_BLOCK], n);
+        A(c->gbuf[k][GB_HIT], n * 12);
+        A(c->gbuf[k][GB_STEPS], n * 2);
+        A(c->hist[k][HI_SH], n * 4 * es);
+        A(c->hist[k][HI_COCG], n * 2 * es);
+        A(c->hist[k][HI_UTIL], n * 4 * es);
+        A(c->hist[k][HI_AOSKY], n * 2 * es);
+        A(c->den[k][FI_SH], n * 4 * es);
+        A(c->den[k][FI_COCG], n * 2 * es);
+        A(c->den[k][FI_VAR], n * es);
+        A(c->den[k][FI_AOSKY], n * 2 * es);
+    }
+    A(c->shadow, n);
+    A(c->gi[GI_SH], n * 4 * es);
+    A(c->gi[GI_COCG], n * 2 * es);
+    A(c->gi[GI_LUMA], n * es);
+    A(c->gi[GI_AOSKY], n * 2 * es);
+    A(c->pre[GI_SH], n * 4 * es);
+    A(c->pre[GI_COCG], n * 2 * es);
+    A(c->pre[GI_LUMA], n * es);
+    A(c->pre[GI_AOSKY], n * 2 * es);
+    A(c->var[FI_SH], n * 4 * es);
+    A(c->var[FI_COCG], n * 2 * es);
+    A(c->var[FI_VAR], n * es);
+    c->var[FI_AOSKY] = nullptr;
+    A(c->color, n * 3 * es);
+    A(c->counters, sizeof(Counters));
+#undef A
+    return VPT_OK;
+}
+
+// Fills the previous-frame G-buffer with "miss" and zeroes the history, the
+// state the first frame reprojects from.
+vpt_status clear_history(vpt_ctx* c) {
+    const size_t n = c->npx, es = c->fp16 ? 2 : 4;
+    int prv = 1 - c->cur;
+    std::vector<uint8_t> minus_one(n * es);
+    if (c->fp16) {
+        __half h = __float2half(-1.0f);
+        for (size_t k = 0; k < n; k++) memcpy(&minus_one[k * 2], &h, 2);
+    } else {
+        float f = -1.0f;
+        for (size_t k = 0; k < n; k++) memcpy(&minus_one[k * 4], &f, 4);
+    }
+    CK(c, cudaMemcpyAsync(c->gbuf[prv][GB_T], minus_one.data(), n * es, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemsetAsync(c->gbuf[prv][GB_FACE], kFaceMiss, n, c->stream));
+    CK(c, cudaMemsetAsync(c->gbuf[prv][GB_BLOCK], 0, n, c->stream));
+    CK(c, cudaMemsetAsync(c->hist[prv][HI_SH], 0, n * 4 * es, c->stream));
+    CK(c, cudaMemsetAsync(c->hist[prv][HI_COCG], 0, n * 2 * es, c->stream));
+    CK(c, cudaMemsetAsync(c->hist[prv][HI_UTIL], 0, n * 4 * es, c->stream));
+    CK(c, cudaMemsetAsync(c->hist[prv][HI_AOSKY], 0, n * 2 * es, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    c->have_prev = false;
+    return VPT_OK;
+}
+
+void pass_begin(vpt_ctx* c, int pass) {
+    if (c->profiling) {
+        cudaEventRecord(c->ev[pass][0], c->stream);
+        c->ev_used[pass] = true;
+    }
+}
+void pass_end(vpt_ctx* c, int pass) {
+    if (c->profiling) cudaEventRecord(c->ev[pass][1], c->stream);
+}
+
+// Per-frame constants of DiffuseRayTraceFrag main (:832-839); same operation
+// order as the shader.
+GILighting gi_lighting(const vpt_frame* f) {
+    const v3 SUN_COLOR = muls(divs(mk3(192.0f, 216.0f, 255.0f), 255.0f), 16.0f);
+    const v3 NIGHT_COLOR = muls(divs(mk3(96.0f, 192.0f, 255.0f), 255.0f), 1.5f);
+    const v3 DUSK_COLOR = muls(divs(mk3(96.0f, 192.0f, 255.0f), 255.0f), 0.9f);
+    v3 sun = mk3(f->sun_dir[0], f->sun_dir[1], f->sun_dir[2]);
+    bool sun_stronger = -sun.y < 0.01f;
+    float dusk = clampf(dpow(fabsf(sun.y - 1.0f), 2.9f), 0.0f, 1.0f);
+    v3 sun_color = vmix(SUN_COLOR, DUSK_COLOR, dusk);
+    v3 lc = sun_stronger ? sun_color : NIGHT_COLOR;
+    lc = muls(lc, 0.4f * f->gi_sun_strength);
+    v3 ld = sun_stronger ? sun : normalize(mk3(-sun.x, -sun.y, sun.z));
+    GILighting L;
+    L.light_color[0] = lc.x; L.light_color[1] = lc.y; L.light_color[2] = lc.z;
+    L.light_dir[0] = ld.x; L.light_dir[1] = ld.y; L.light_dir[2] = ld.z;
+    L.moon_stronger = sun_stronger ? 0 : 1;
+    L.emissivity_multiplier = sun_stronger ? 12.0f : 13.0f;
+    L.sun_visibility = clampf(dot(sun, mk3(0.0f, 1.0f, 0.0f)) + 0.05f, 0.0f, 0.1f) * 12.0f;
+    L.gi_sky_strength = f->gi_sky_strength;
+    L.diffuse_light_intensity = f->diffuse_light_intensity;
+    return L;
+}
+
+vpt_status check_world(vpt_ctx* c) {
+    if (!c->vox) return fail(c, VPT_ERR_STATE, "no world uploaded");
+    if (!c->df_valid) return fail(c, VPT_ERR_STATE, "distance field not built (call vpt_build_df)");
+    if (!c->blocks) return fail(c, VPT_ERR_STATE, "no block table set");
+    return VPT_OK;
+}
+
+vpt_status check_frame(vpt_ctx* c, const vpt_frame* f) {
+    if (!f) return fail(c, VPT_ERR_INVALID_ARG, "frame is NULL");
+    if (!c->have_cam) return fail(c, VPT_ERR_STATE, "no primary trace this frame");
+    return VPT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* vpt_status_string(vpt_status s) {
+    switch (s) {
+        case VPT_OK: return "ok";
+        case VPT_ERR_INVALID_ARG: return "invalid argument";
+        case VPT_ERR_OOM: return "out of memory";
+        case VPT_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+        case VPT_ERR_CUDA: return "CUDA error";
+        case VPT_ERR_STATE: return "call out of order";
+        case VPT_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+int vpt_abi_version(void) { return VPT_ABI_VERSION; }
+
+vpt_status vpt_default_config(vpt_config* cfg) {
+    if (!cfg) return VPT_ERR_INVALID_ARG;
+    memset(cfg, 0, sizeof *cfg);
+    cfg->width = 1920;
+    cfg->height = 1080;
+    cfg->primary_max_steps = 350;
+    cfg->shadow_max_steps = 350;
+    cfg->diffuse_max_steps = 48;
+    cfg->bounce_shadow_max_steps = 128;
+    cfg->bounces = 1;
+    cfg->spp = 1;
+    cfg->storage = VPT_STORAGE_F32;
+    cfg->atrous_iterations = 5;
+    cfg->resolution_scale = 1.0f;
+    cfg->color_phi_bias = 3.325f;
+    cfg->device = 0;
+    return VPT_OK;
+}
+
+vpt_status vpt_default_frame(vpt_frame* f) {
+    if (!f) return VPT_ERR_INVALID_ARG;
+    memset(f, 0, sizeof *f);
+    // a morning sun: normalize(0.3, 0.8, 0.5)
+    float sx = 0.3f, sy = 0.8f, sz = 0.5f;
+    float l = sqrtf((sx * sx + sy * sy) + sz * sz);
+    f->sun_dir[0] = sx / l;
+    f->sun_dir[1] = sy / l;
+    f->sun_dir[2] = sz / l;
+    f->time = 1.0f;
+    f->sun_radiance[0] = 5.2f;
+    f->sun_radiance[1] = 4.9f;
+    f->sun_radiance[2] = 4.4f;
+    f->moon_radiance[0] = 0.05f;
+    f->moon_radiance[1] = 0.06f;
+    f->moon_radiance[2] = 0.09f;
+    f->frame_index = 0;
+    f->seed = 0;
+    f->gi_sun_strength = 1.0f;
+    f->gi_sky_strength = 1.125f;
+    f->diffuse_light_intensity = 1.25f;
+    f->temporal = 1;
+    return VPT_OK;
+}
+
+vpt_status vpt_create(vpt_ctx** out, const vpt_config* cfg) {
+    if (!out || !cfg) return VPT_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (cfg->width <= 0 || cfg->height <= 0 || cfg->width > 16384 || cfg->height > 16384) return VPT_ERR_INVALID_ARG;
+    if (cfg->storage != VPT_STORAGE_F32 && cfg->storage != VPT_STORAGE_F16) return VPT_ERR_INVALID_ARG;
+    if (cfg->primary_max_steps < 0 || cfg->shadow_max_steps < 0 || cfg->diffuse_max_steps < 0 ||
+        cfg->bounce_shadow_max_steps < 0 || cfg->bounces < 0 || cfg->bounces > 8 || cfg->spp < 1 ||
+        cfg->spp > 32 || cfg->atrous_iterations < 0 || cfg->atrous_iterations > 8)
+        return VPT_ERR_INVALID_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        return VPT_ERR_NO_DEVICE;
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) return VPT_ERR_INVALID_ARG;
+    vpt_ctx* c = new (std::nothrow) vpt_ctx();
+    if (!c) return VPT_ERR_OOM;
+    c->cfg = *cfg;
+    c->dev = cfg->device;
+    c->fp16 = cfg->storage == VPT_STORAGE_F16;
+    c->npx = (size_t)cfg->width * (size_t)cfg->height;
+    vpt_status s = VPT_OK;
+    if (cudaSetDevice(c->dev) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        s = VPT_ERR_CUDA;
+    }
+    if (s == VPT_OK) s = alloc_planes(c);
+    if (s == VPT_OK) {
+        for (int p = 0; p < VPT_PASS_COUNT && s == VPT_OK; p++)
+            for (int k = 0; k < 2; k++)
+                if (cudaEventCreate(&c->ev[p][k]) != cudaSuccess) s = VPT_ERR_CUDA;
+    }
+    if (s == VPT_OK && cudaMemsetAsync(c->counters, 0, sizeof(Counters), c->stream) != cudaSuccess) s = VPT_ERR_CUDA;
+    if (s == VPT_OK) s = clear_history(c);
+    if (s != VPT_OK) {
+        vpt_destroy(c);
+        return s;
+    }
+    *out = c;
+    return VPT_OK;
+}
+
+vpt_status vpt_destroy(vpt_ctx* c) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    cudaSetDevice(c->dev);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (void* p : c->allocs) cudaFree(p);
+    if (c->vox) cudaFree(c->vox);
+    if (c->df) cudaFree(c->df);
+    for (int p = 0; p < VPT_PASS_COUNT; p++)
+        for (int k = 0; k < 2; k++)
+            if (c->ev[p][k]) cudaEventDestroy(c->ev[p][k]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return VPT_OK;
+}
+
+const char* vpt_last_error(const vpt_ctx* c) { return c ? c->err.c_str() : ""; }
+
+vpt_status vpt_upload_world(vpt_ctx* c, const uint8_t* voxels, int32_t X, int32_t Y, int32_t Z) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (!voxels) return fail(c, VPT_ERR_INVALID_ARG, "voxels is NULL");
+    if (X <= 0 || Y <= 0 || Z <= 0 || X > 2048 || Y > 2048 || Z > 2048 || (size_t)X * Y * Z > ((size_t)1 << 31))
+        return fail(c, VPT_ERR_INVALID_ARG, "bad world dimensions %d x %d x %d", X, Y, Z);
+    cudaSetDevice(c->dev);
+    size_t n = (size_t)X * Y * Z;
+    if (c->vox == nullptr || (size_t)c->X * c->Y * c->Z != n) {
+        if (c->vox) { cudaFree(c->vox); cudaFree(c->df); }
+        c->vox = nullptr;
+        c->df = nullptr;
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaError_t e1 = cudaMalloc(&a, n);
+        cudaError_t e2 = e1 == cudaSuccess ? cudaMalloc(&b, n) : e1;
+        if (e1 != cudaSuccess || e2 != cudaSuccess) {
+            if (a) cudaFree(a);
+            return fail(c, VPT_ERR_OOM, "world allocation of %zu bytes failed", 2 * n);
+        }
+        c->vox = (uint8_t*)a;
+        c->df = (uint8_t*)b;
+    }
+    c->X = X;
+    c->Y = Y;
+    c->Z = Z;
+    c->df_valid = false;
+    CK(c, cudaMemcpyAsync(c->vox, voxels, n, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return VPT_OK;
+}
+
+vpt_status vpt_set_block_table(vpt_ctx* c, const vpt_block* table, int32_t n) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (!table || n <= 0 || n > 256) return fail(c, VPT_ERR_INVALID_ARG, "block table must have 1..256 entries");
+    cudaSetDevice(c->dev);
+    if (!c->blocks) {
+        void* p = nullptr;
+        vpt_status s = dalloc(c, &p, 256 * sizeof(vpt_block));
+        if (s != VPT_OK) return s;
+        c->blocks = (vpt_block*)p;
+    }
+    CK(c, cudaMemcpyAsync(c->blocks, table, (size_t)n * sizeof(vpt_block), cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    c->n_blocks = n;
+    return VPT_OK;
+}
+
+vpt_status vpt_build_df(vpt_ctx* c) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (!c->vox) return fail(c, VPT_ERR_STATE, "no world uploaded");
+    cudaSetDevice(c->dev);
+    int launches = 0;
+    CK(c, df_build(c->vox, c->df, c->X, c->Y, c->Z, c->stream, &launches));
+    c->launches += (uint64_t)launches;
+    c->df_valid = true;
+    return VPT_OK;
+}
+
+vpt_status vpt_read_df(vpt_ctx* c, uint8_t* host, size_t bytes) {
+    if (!c || !host) return VPT_ERR_INVALID_ARG;
+    if (!c->df_valid) return fail(c, VPT_ERR_STATE, "distance field not built");
+    size_t n = (size_t)c->X * c->Y * c->Z;
+    if (bytes < n) return fail(c, VPT_ERR_INVALID_ARG, "buffer too small: %zu < %zu", bytes, n);
+    cudaSetDevice(c->dev);
+    CK(c, cudaMemcpyAsync(host, c->df, n, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return VPT_OK;
+}
+
+vpt_status vpt_df_build_device(const uint8_t* d_voxels, uint8_t* d_df, int32_t X, int32_t Y, int32_t Z, void* stream) {
+    if (!d_voxels || !d_df || X <= 0 || Y <= 0 || Z <= 0 || (size_t)X * Y * Z > ((size_t)1 << 31))
+        return VPT_ERR_INVALID_ARG;
+    int launches = 0;
+    cudaError_t e = df_build(d_voxels, d_df, X, Y, Z, (cudaStream_t)stream, &launches);
+    return e == cudaSuccess ? VPT_OK : VPT_ERR_CUDA;
+}
+
+vpt_status vpt_trace_primary(vpt_ctx* c, const vpt_camera* cam) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (!cam) return fail(c, VPT_ERR_INVALID_ARG, "camera is NULL");
+    vpt_status s = check_world(c);
+    if (s != VPT_OK) return s;
+    cudaSetDevice(c->dev);
+    c->cam = *cam;
+    c->have_cam = true;
+    GBufferOut g;
+    g.t = c->gbuf[c->cur][GB_T];
+    g.face = (uint8_t*)c->gbuf[c->cur][GB_FACE];
+    g.block = (uint8_t*)c->gbuf[c->cur][GB_BLOCK];
+    g.hit = (int32_t*)c->gbuf[c->cur][GB_HIT];
+    g.steps = (uint16_t*)c->gbuf[c->cur][GB_STEPS];
+    pass_begin(c, VPT_PASS_PRIMARY);
+    CK(c, trace_primary(world_view(c), cam_view(*cam), c->cfg.width, c->cfg.height, c->cfg.primary_max_steps, c->fp16,
+                        g, c->stats ? c->counters : nullptr, c->stream));
+    pass_end(c, VPT_PASS_PRIMARY);
+    c->launches += 1;
+    return VPT_OK;
+}
+
+vpt_status vpt_trace_shadow(vpt_ctx* c, const vpt_frame* f) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    vpt_status s = check_world(c);
+    if (s != VPT_OK) return s;
+    if ((s = check_frame(c, f)) != VPT_OK) return s;
+    cudaSetDevice(c->dev);
+    pass_begin(c, VPT_PASS_SHADOW);
+    CK(c, trace_shadow(world_view(c), cam_view(c->cam), c->cfg.width, c->cfg.height, c->cfg.shadow_max_steps,
+                       f->sun_dir, c->fp16, c->gbuf[c->cur][GB_T], (const uint8_t*)c->gbuf[c->cur][GB_FACE],
+                       c->shadow, c->stats ? c->counters : nullptr, c->stream));
+    pass_end(c, VPT_PASS_SHADOW);
+    c->launches += 1;
+    return VPT_OK;
+}
+
+vpt_status vpt_trace_diffuse(vpt_ctx* c, const vpt_frame* f) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    vpt_status s = check_world(c);
+    if (s != VPT_OK) return s;
+    if ((s = check_frame(c, f)) != VPT_OK) return s;
+    cudaSetDevice(c->dev);
+    DiffuseArgs a;
+    a.diffuse_max_steps = c->cfg.diffuse_max_steps;
+    a.bounce_shadow_max_steps = c->cfg.bounce_shadow_max_steps;
+    a.bounces = c->cfg.bounces;
+    a.spp = c->cfg.spp;
+    a.frame_index = f->frame_index;
+    a.seed = f->seed;
+    a.lighting = gi_lighting(f);
+    GIOut o{c->gi[GI_SH], c->gi[GI_COCG], c->gi[GI_LUMA], c->gi[GI_AOSKY]};
+    pass_begin(c, VPT_PASS_DIFFUSE);
+    CK(c, trace_diffuse(world_view(c), cam_view(c->cam), c->cfg.width, c->cfg.height, a, c->fp16,
+                        c->gbuf[c->cur][GB_T], (const uint8_t*)c->gbuf[c->cur][GB_FACE], o,
+                        c->stats ? c->counters : nullptr, c->stream));
+    pass_end(c, VPT_PASS_DIFFUSE);
+    c->launches += 1;
+    return VPT_OK;
+}
+
+vpt_status vpt_svgf(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    vpt_status s = check_frame(c, f);
+    if (s != VPT_OK) return s;
+    cudaSetDevice(c->dev);
+    const int W = c->cfg.width, H = c->cfg.height, cur = c->cur, prv = 1 - c->cur;
+    const CamView cv = cam_view(c->cam);
+    const vpt_camera& pc = prev_cam ? *prev_cam : (c->have_prev ? c->prev_cam : c->cam);
+    const void* t = c->gbuf[cur][GB_T];
+    const uint8_t* face = (const uint8_t*)c->gbuf[cur][GB_FACE];
+    const uint8_t* block = (const uint8_t*)c->gbuf[cur][GB_BLOCK];
+    // Spatial3x3Initial (Core/Pipeline.cpp:2288-2330)
+    pass_begin(c, VPT_PASS_SPATIAL_INITIAL);
+    CK(c, svgf_spatial_initial(cv, W, H, c->fp16, t, face, GIIn{c->gi[GI_SH], c->gi[GI_COCG], c->gi[GI_LUMA], c->gi[GI_AOSKY]},
+                               GIOut{c->pre[GI_SH], c->pre[GI_COCG], c->pre[GI_LUMA], c->pre[GI_AOSKY]}, c->stream));
+    pass_end(c, VPT_PASS_SPATIAL_INITIAL);
+    // temporal (:2334-2436)
+    TemporalArgs ta;
+    for (int col = 0; col < 4; col++)
+        for (int r = 0; r < 4; r++)
+            ta.prev_view_proj[col * 4 + r] = ((pc.proj[0 * 4 + r] * pc.view[col * 4 + 0] +
+                                               pc.proj[1 * 4 + r] * pc.view[col * 4 + 1]) +
+                                              pc.proj[2 * 4 + r] * pc.view[col * 4 + 2]) +
+                                             pc.proj[3 * 4 + r] * pc.view[col * 4 + 3];
+    ta.be_useful = f->temporal ? 1 : 0;
+    HistIO hout{c->hist[cur][HI_SH], c->hist[cur][HI_COCG], c->hist[cur][HI_UTIL], c->hist[cur][HI_AOSKY]};
+    HistIO hprev{c->hist[prv][HI_SH], c->hist[prv][HI_COCG], c->hist[prv][HI_UTIL], c->hist[prv][HI_AOSKY]};
+    pass_begin(c, VPT_PASS_TEMPORAL);
+    CK(c, svgf_temporal(cv, W, H, c->fp16, ta, t, face, block, c->gbuf[prv][GB_T],
+                        (const uint8_t*)c->gbuf[prv][GB_FACE], (const uint8_t*)c->gbuf[prv][GB_BLOCK],
+                        GIIn{c->pre[GI_SH], c->pre[GI_COCG], c->pre[GI_LUMA], c->pre[GI_AOSKY]}, hprev, hout,
+                        c->stream));
+    pass_end(c, VPT_PASS_TEMPORAL);
+    // variance (:2438-2475)
+    pass_begin(c, VPT_PASS_VARIANCE);
+    CK(c, svgf_variance(cv, W, H, c->fp16, t, face, hout, FiltIO{c->var[FI_SH], c->var[FI_COCG], c->var[FI_VAR], nullptr},
+                        c->stream));
+    pass_end(c, VPT_PASS_VARIANCE);
+    c->launches += 3;
+    // a-trous iterations with steps 16, 8, 4, 2, 1 (:2481-2610)
+    const float tmod = f->time * 100.493850275f;
+    pass_begin(c, VPT_PASS_ATROUS);
+    for (int it = 0; it < c->cfg.atrous_iterations; it++) {
+        AtrousArgs aa;
+        aa.step = 16 >> it;
+        if (aa.step < 1) aa.step = 1;
+        aa.add_scale = mixf(1.0f, 2.4f, c->cfg.resolution_scale);
+        aa.phi_bias = fmaxf(c->cfg.color_phi_bias, 0.1f);
+        aa.tmod500 = tmod - 500.0f * floorf(tmod / 500.0f);
+        FiltIO in;
+        const void* in_ao;
+        if (it == 0) {
+            in = FiltIO{c->var[FI_SH], c->var[FI_COCG], c->var[FI_VAR], nullptr};
+            in_ao = c->hist[cur][HI_AOSKY];
+        } else {
+            int k = (it - 1) & 1;
+            in = FiltIO{c->den[k][FI_SH], c->den[k][FI_COCG], c->den[k][FI_VAR], c->den[k][FI_AOSKY]};
+            in_ao = c->den[k][FI_AOSKY];
+        }
+        int k = it & 1;
+        FiltIO out{c->den[k][FI_SH], c->den[k][FI_COCG], c->den[k][FI_VAR], c->den[k][FI_AOSKY]};
+        CK(c, svgf_atrous(cv, W, H, c->fp16, aa, t, face, c->hist[cur][HI_UTIL], in, in_ao, out, c->stream));
+        c->den_last = k;
+        c->launches += 1;
+    }
+    pass_end(c, VPT_PASS_ATROUS);
+    return VPT_OK;
+}
+
+vpt_status vpt_shade(vpt_ctx* c, const vpt_frame* f) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    vpt_status s = check_world(c);
+    if (s != VPT_OK) return s;
+    if ((s = check_frame(c, f)) != VPT_OK) return s;
+    cudaSetDevice(c->dev);
+    ShadeArgs a;
+    v3 sun = mk3(f->sun_dir[0], f->sun_dir[1], f->sun_dir[2]);
+    v3 moon = normalize(mk3(-sun.x, -sun.y, sun.z));
+    a.sun[0] = sun.x; a.sun[1] = sun.y; a.sun[2] = sun.z;
+    a.moon[0] = moon.x; a.moon[1] = moon.y; a.moon[2] = moon.z;
+    for (int k = 0; k < 3; k++) {
+        a.sun_color[k] = f->sun_radiance[k];
+        a.moon_color[k] = f->moon_radiance[k];
+    }
+    float sv = clampf(dot(sun, mk3(0.0f, 1.0f, 0.0f)) + 0.05f, 0.0f, 0.1f) * 12.0f;
+    a.sun_vis = 1.0f - sv;
+    const void* sh = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_SH] : c->var[FI_SH];
+    const void* cocg = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_COCG] : c->var[FI_COCG];
+    const void* ao = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_AOSKY] : c->hist[c->cur][HI_AOSKY];
+    pass_begin(c, VPT_PASS_SHADE);
+    CK(c, shade(world_view(c), cam_view(c->cam), c->cfg.width, c->cfg.height, c->fp16, a, c->gbuf[c->cur][GB_T],
+                (const uint8_t*)c->gbuf[c->cur][GB_FACE], (const uint8_t*)c->gbuf[c->cur][GB_BLOCK], c->shadow, sh, cocg,
+                ao, c->color, c->stream));
+    pass_end(c, VPT_PASS_SHADE);
+    c->launches += 1;
+    return VPT_OK;
+}
+
+vpt_status vpt_end_frame(vpt_ctx* c) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (c->have_cam) {
+        c->prev_cam = c->cam;
+        c->have_prev = true;
+    }
+    c->cur = 1 - c->cur;
+    c->have_cam = false;
+    return VPT_OK;
+}
+
+vpt_status vpt_reset_history(vpt_ctx* c) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    cudaSetDevice(c->dev);
+    return clear_history(c);
+}
+
+vpt_status vpt_render_frame(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f, float* rgb_out) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (!cam || !f) return fail(c, VPT_ERR_INVALID_ARG, "camera and frame are required");
+    vpt_status s;
+    const vpt_camera prev = c->have_prev ? c->prev_cam : *cam;
+    if ((s = vpt_trace_primary(c, cam)) != VPT_OK) return s;
+    if ((s = vpt_trace_shadow(c, f)) != VPT_OK) return s;
+    if ((s = vpt_trace_diffuse(c, f)) != VPT_OK) return s;
+    if ((s = vpt_svgf(c, &prev, f)) != VPT_OK) return s;
+    if ((s = vpt_shade(c, f)) != VPT_OK) return s;
+    if (rgb_out) {
+        size_t n = c->npx * 3;
+        if (c->fp16) {
+            std::vector<__half> tmp(n);
+            CK(c, cudaMemcpyAsync(tmp.data(), c->color, n * 2, cudaMemcpyDeviceToHost, c->stream));
+            CK(c, cudaStreamSynchronize(c->stream));
+            for (size_t k = 0; k < n; k++) rgb_out[k] = __half2float(tmp[k]);
+        } else {
+            CK(c, cudaMemcpyAsync(rgb_out, c->color, n * 4, cudaMemcpyDeviceToHost, c->stream));
+            CK(c, cudaStreamSynchronize(c->stream));
+        }
+    }
+    return vpt_end_frame(c);
+}
+
+vpt_status vpt_plane_info(const vpt_ctx* c, int32_t plane, size_t* bytes, int32_t* channels, int32_t* dtype) {
+    if (!c || plane < 0 || plane >= VPT_PLANE_COUNT) return VPT_ERR_INVALID_ARG;
+    int ch = 0, dt = 0;
+    size_t b = plane_bytes(c, plane, &ch, &dt);
+    if (bytes) *bytes = b;
+    if (channels) *channels = ch;
+    if (dtype) *dtype = dt;
+    return VPT_OK;
+}
+
+vpt_status vpt_read_plane(vpt_ctx* c, int32_t plane, void* host, size_t bytes) {
+    if (!c || !host || plane < 0 || plane >= VPT_PLANE_COUNT) return VPT_ERR_INVALID_ARG;
+    size_t need = plane_bytes(c, plane, nullptr, nullptr);
+    if (bytes < need) return fail(c, VPT_ERR_INVALID_ARG, "buffer too small: %zu < %zu", bytes, need);
+    cudaSetDevice(c->dev);
+    CK(c, cudaMemcpyAsync(host, plane_ptr(c, plane), need, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return VPT_OK;
+}
+
+vpt_status vpt_write_plane(vpt_ctx* c, int32_t plane, const void* host, size_t bytes) {
+    if (!c || !host || plane < 0 || plane >= VPT_PLANE_COUNT) return VPT_ERR_INVALID_ARG;
+    size_t need = plane_bytes(c, plane, nullptr, nullptr);
+    if (bytes != need) return fail(c, VPT_ERR_INVALID_ARG, "size mismatch: %zu != %zu", bytes, need);
+    cudaSetDevice(c->dev);
+    CK(c, cudaMemcpyAsync(plane_ptr(c, plane), host, need, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return VPT_OK;
+}
+
+vpt_status vpt_plane_device_ptr(vpt_ctx* c, int32_t plane, void** dptr) {
+    if (!c || !dptr || plane < 0 || plane >= VPT_PLANE_COUNT) return VPT_ERR_INVALID_ARG;
+    *dptr = plane_ptr(c, plane);
+    return VPT_OK;
+}
+
+vpt_status vpt_synchronize(vpt_ctx* c) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    cudaSetDevice(c->dev);
+    CK(c, cudaStreamSynchronize(c->stream));
+    return VPT_OK;
+}
+
+vpt_status vpt_set_stats(vpt_ctx* c, int32_t enabled) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    c->stats = enabled != 0;
+    return VPT_OK;
+}
+
+vpt_status vpt_read_stats(vpt_ctx* c, vpt_stats* out) {
+    if (!c || !out) return VPT_ERR_INVALID_ARG;
+    cudaSetDevice(c->dev);
+    Counters h;
+    CK(c, cudaMemcpyAsync(&h, c->counters, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemsetAsync(c->counters, 0, sizeof(Counters), c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < 4; k++) {
+        out->rays[k] = h.rays[k];
+        out->steps[k] = h.steps[k];
+    }
+    return VPT_OK;
+}
+
+vpt_status vpt_set_profiling(vpt_ctx* c, int32_t enabled) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    c->profiling = enabled != 0;
+    for (int p = 0; p < VPT_PASS_COUNT; p++) c->ev_used[p] = false;
+    return VPT_OK;
+}
+
+vpt_status vpt_read_pass_times(vpt_ctx* c, float* ms, int32_t n) {
+    if (!c || !ms || n <= 0) return VPT_ERR_INVALID_ARG;
+    cudaSetDevice(c->dev);
+    CK(c, cudaStreamSynchronize(c->stream));
+    for (int p = 0; p < n && p < VPT_PASS_COUNT; p++) {
+        ms[p] = 0.0f;
+        if (c->ev_used[p]) {
+            float v = 0.0f;
+            if (cudaEventElapsedTime(&v, c->ev[p][0], c->ev[p][1]) == cudaSuccess) ms[p] = v;
+            else cudaGetLastError();
+        }
+    }
+    return VPT_OK;
+}
+
+vpt_status vpt_launch_count(const vpt_ctx* c, uint64_t* out) {
+    if (!c || !out) return VPT_ERR_INVALID_ARG;
+    *out = c->launches;
+    return VPT_OK;
+}
+
+vpt_status vpt_get_stream(const vpt_ctx* c, void** stream) {
+    if (!c || !stream) return VPT_ERR_INVALID_ARG;
+    *stream = (void*)c->stream;
+    return VPT_OK;
+}
+
+// Exposed for the parity tests of the deterministic math (not in vpt.h's
+// frame API): evaluates op over n host inputs on the device, or on the host
+// when on_device is 0.
+vpt_status vpt_detmath(int32_t op, const float* x, const float* y, float* out, int32_t n, int32_t on_device) {
+    if (!x || !out || n < 0 || op < 0 || op > 5 || (op == 3 && !y)) return VPT_ERR_INVALID_ARG;
+    if (!on_device) {
+        for (int k = 0; k < n; k++) {
+            float a = x[k], r;
+            switch (op) {
+                case 0: r = dexp(a); break;
+                case 1: r = dexp2(a); break;
+                case 2: r = dlog2(a); break;
+                case 3: r = dpow(a, y[k]); break;
+                case 4: r = dsin(a); break;
+                default: r = dcos(a); break;
+            }
+            out[k] = r;
+        }
+        return VPT_OK;
+    }
+    float *dx = nullptr, *dy = nullptr, *dout = nullptr;
+    size_t b = (size_t)(n > 0 ? n : 1) * 4;
+    if (cudaMalloc(&dx, b) != cudaSuccess || cudaMalloc(&dy, b) != cudaSuccess || cudaMalloc(&dout, b) != cudaSuccess) {
+        cudaFree(dx); cudaFree(dy); cudaFree(dout);
+        return VPT_ERR_OOM;
+    }
+    vpt_status st = VPT_OK;
+    if (cudaMemcpy(dx, x, (size_t)n * 4, cudaMemcpyHostToDevice) != cudaSuccess) st = VPT_ERR_CUDA;
+    if (st == VPT_OK && y && cudaMemcpy(dy, y, (size_t)n * 4, cudaMemcpyHostToDevice) != cudaSuccess) st = VPT_ERR_CUDA;
+    if (st == VPT_OK && detmath_eval(op, dx, dy, dout, n, 0) != cudaSuccess) st = VPT_ERR_CUDA;
+    if (st == VPT_OK && cudaMemcpy(out, dout, (size_t)n * 4, cudaMemcpyDeviceToHost) != cudaSuccess) st = VPT_ERR_CUDA;
+    cudaFree(dx); cudaFree(dy); cudaFree(dout);
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,276 @@
+// Device-side building blocks shared by the trace, filter and colour kernels:
+// camera rays, plane access with the OpenGL sampling rules the reference
+// relies on, material lookup, the BRDF / spherical-harmonic helpers and the
+// per-pixel random stream. Each helper cites the shader function it restates.
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "vmath.cuh"
+#include "vpt.h"
+
+namespace vpt {
+
+constexpr float kPI = 3.14159265359f;   // DiffuseRayTraceFrag.glsl:11, ColorPassFrag.glsl:6
+constexpr int kFaceMiss = 10;           // round(1.0 * 10) decoded from a miss (InitialRayTraceFrag.glsl:454)
+
+// ------------------------------------------------------------------ world --
+struct WorldView {
+    const uint8_t* vox;       // block ids, x fastest
+    const uint8_t* df;        // Manhattan distance field, same layout
+    int X, Y, Z;
+    const vpt_block* blocks;  // block table
+    int n_blocks;
+};
+
+struct CamView {
+    float inv_view[16];
+    float inv_proj[16];
+    float pos[3];             // u_ViewerPosition
+};
+
+__device__ __forceinline__ int vox_index(const WorldView& w, int x, int y, int z) {
+    return x + w.X * (y + w.Y * z);
+}
+__device__ __forceinline__ bool in_volume(const WorldView& w, int x, int y, int z) {
+    // IsInVolume (InitialRayTraceFrag.glsl:68-77)
+    return !(x < 0 || y < 0 || z < 0 || x > w.X - 1 || y > w.Y - 1 || z > w.Z - 1);
+}
+__device__ __forceinline__ int get_voxel(const WorldView& w, int x, int y, int z) {
+    // GetVoxel (InitialRayTraceFrag.glsl:79-87)
+    return in_volume(w, x, y, z) ? (int)__ldg(w.vox + vox_index(w, x, y, z)) : 0;
+}
+
+// --------------------------------------------------------------- camera --
+__device__ __forceinline__ v2 texcoord(int i, int j, int W, int H) {
+    return mk2(((float)i + 0.5f) / (float)W, ((float)j + 0.5f) / (float)H);
+}
+// GetRayDirectionAt (ShadowRayTraceFrag.glsl:303-308), GetRayStuff (InitialRayTraceFrag.glsl:398-414)
+__device__ __forceinline__ v3 ray_dir_at(const CamView& c, v2 uv) {
+    float cx = uv.x * 2.0f - 1.0f;
+    float cy = uv.y * 2.0f - 1.0f;
+    v4 e = mat_mul4(c.inv_proj, cx, cy, -1.0f, 1.0f);
+    v4 d = mat_mul4(c.inv_view, e.x, e.y, -1.0f, 0.0f);
+    return mk3(d.x, d.y, d.z);
+}
+__device__ __forceinline__ v3 ray_origin(const CamView& c) {
+    return mk3(c.inv_view[12], c.inv_view[13], c.inv_view[14]);
+}
+
+// GetNormalFromID (SVGF/TemporalFilter.glsl:108-119); `miss` is the value
+// ids above 5 decode to (1.0, or 0.5 in DiffuseRayTraceFrag.glsl:790-801).
+__device__ __forceinline__ v3 normal_from_id(int id, float miss) {
+    switch (id) {
+        case 0: return mk3(0.0f, 0.0f, 1.0f);
+        case 1: return mk3(0.0f, 0.0f, -1.0f);
+        case 2: return mk3(0.0f, 1.0f, 0.0f);
+        case 3: return mk3(0.0f, -1.0f, 0.0f);
+        case 4: return mk3(-1.0f, 0.0f, 0.0f);
+        case 5: return mk3(1.0f, 0.0f, 0.0f);
+        default: return mk3(miss, miss, miss);
+    }
+}
+
+// ------------------------------------------------------------ storage --
+__device__ __forceinline__ float ld(const float* p) { return __ldg(p); }
+__device__ __forceinline__ float ld(const __half* p) { return __half2float(__ldg(p)); }
+__device__ __forceinline__ void st(float* p, float v) { *p = v; }
+__device__ __forceinline__ void st(__half* p, float v) { *p = __float2half_rn(v); }
+
+__device__ __forceinline__ int wrapi(int i, int n) {
+    int r = i % n;
+    return r < 0 ? r + n : r;
+}
+
+// A W x H plane with C interleaved channels of storage type S.
+template <typename S, int C>
+struct Plane {
+    const S* p;
+    int W, H;
+    __device__ __forceinline__ float at(int i, int j, int c) const {
+        return ld(p + ((size_t)wrapi(j, H) * W + wrapi(i, W)) * C + c);
+    }
+    __device__ __forceinline__ float at_in(int i, int j, int c) const {   // i, j known in range
+        return ld(p + ((size_t)j * W + i) * C + c);
+    }
+    // texture() with GL_LINEAR and GL_REPEAT (Core/GLClasses/Framebuffer.cpp:64-70), fp32 weights
+    __device__ __forceinline__ void linear(v2 uv, float* out) const {
+        float x = uv.x * (float)W - 0.5f;
+        float y = uv.y * (float)H - 0.5f;
+        float x0 = floorf(x), y0 = floorf(y);
+        float ax = x - x0, ay = y - y0;
+        int i0 = wrapi(f2i(x0), W), j0 = wrapi(f2i(y0), H);
+        int i1 = i0 + 1 == W ? 0 : i0 + 1;
+        int j1 = j0 + 1 == H ? 0 : j0 + 1;
+        const S* r0 = p + (size_t)j0 * W * C;
+        const S* r1 = p + (size_t)j1 * W * C;
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+            float v00 = ld(r0 + i0 * C + c), v10 = ld(r0 + i1 * C + c);
+            float v01 = ld(r1 + i0 * C + c), v11 = ld(r1 + i1 * C + c);
+            float b = v00 * (1.0f - ax) + v10 * ax;
+            float t = v01 * (1.0f - ax) + v11 * ax;
+            out[c] = b * (1.0f - ay) + t * ay;
+        }
+    }
+};
+
+struct Plane8 {
+    const uint8_t* p;
+    int W, H;
+    __device__ __forceinline__ int at(int i, int j) const { return __ldg(p + (size_t)wrapi(j, H) * W + wrapi(i, W)); }
+    __device__ __forceinline__ int at_in(int i, int j) const { return __ldg(p + (size_t)j * W + i); }
+    // texture() with GL_NEAREST and GL_REPEAT
+    __device__ __forceinline__ int nearest(v2 uv) const {
+        return at(f2i(floorf(uv.x * (float)W)), f2i(floorf(uv.y * (float)H)));
+    }
+};
+
+// GetPositionAt (SVGF/TemporalFilter.glsl:82-86) at a texel centre or anywhere.
+template <typename S>
+__device__ __forceinline__ v4 position_fetch(const CamView& c, const Plane<S, 1>& t, int i, int j, v2 txc) {
+    float d = t.at_in(i, j, 0);
+    v3 p = add(ray_origin(c), muls(normalize(ray_dir_at(c, txc)), d));
+    v4 r; r.x = p.x; r.y = p.y; r.z = p.z; r.w = d;
+    return r;
+}
+template <typename S>
+__device__ __forceinline__ v4 position_linear(const CamView& c, const Plane<S, 1>& t, v2 txc) {
+    float d;
+    t.linear(txc, &d);
+    v3 p = add(ray_origin(c), muls(normalize(ray_dir_at(c, txc)), d));
+    v4 r; r.x = p.x; r.y = p.y; r.z = p.z; r.w = d;
+    return r;
+}
+
+// ------------------------------------------------------------- shading --
+__device__ __forceinline__ float luminance(v3 c) { return dot(c, mk3(0.299f, 0.587f, 0.114f)); }
+__device__ __forceinline__ float sh_to_y(const float* sh) { return fmaxf(0.0f, 3.544905f * sh[3]); }
+
+// Analytic horizon-to-zenith sky standing in for the atmosphere cubemap.
+__device__ __forceinline__ v3 sky_radiance(v3 d) {
+    v3 n = normalize(d);
+    float a = clampf(n.y, 0.0f, 1.0f);
+    return vmix(mk3(0.62f, 0.74f, 0.92f), mk3(0.20f, 0.38f, 0.85f), a);
+}
+// GetSkyColorAt (DiffuseRayTraceFrag.glsl:984-988)
+__device__ __forceinline__ v3 sky_color_at(v3 rd) {
+    rd.y = clampf(rd.y, 0.125f, 1.5f);
+    return sky_radiance(rd);
+}
+
+// IrridianceToSH (DiffuseRayTraceFrag.glsl:766-784)
+__device__ __forceinline__ void irradiance_to_sh(v3 r, v3 d, float* sh, float* cocg) {
+    float co = r.x - r.z;
+    float t = r.z + co * 0.5f;
+    float cg = r.y - t;
+    float y = fmaxf(t + cg * 0.5f, 0.0f);
+    float l00 = 0.282095f;
+    float l1_1 = 0.488603f * d.y;
+    float l10 = 0.488603f * d.z;
+    float l11 = 0.488603f * d.x;
+    sh[0] = fmaxf(l11 * y, -100.0f);
+    sh[1] = fmaxf(l1_1 * y, -100.0f);
+    sh[2] = fmaxf(l10 * y, -100.0f);
+    sh[3] = fmaxf(l00 * y, -100.0f);
+    cocg[0] = co;
+    cocg[1] = cg;
+}
+
+// SHToIrridiance (ColorPassFrag.glsl:357-368)
+__device__ __forceinline__ v3 sh_to_irradiance(const float* sh, const float* cocg_in, v3 v) {
+    float x = dot(mk3(sh[0], sh[1], sh[2]), v);
+    float y = 2.0f * (1.023326f * x + 0.886226f * sh[3]);
+    y = fmaxf(y, 0.0f);
+    float s = (y * 0.282095f) / (sh[3] + 1e-6f);
+    float co = cocg_in[0] * s, cg = cocg_in[1] * s;
+    float t = y - cg * 0.5f;
+    float g = cg + t;
+    float b = t - co * 0.5f;
+    float r = b + co;
+    return vmax(mk3(r, g, b), 0.0f);
+}
+
+// InverseSchlick (DiffuseRayTraceFrag.glsl:1305-1308)
+__device__ __forceinline__ float inverse_schlick(float f0, float voh) {
+    return 1.0f - clampf(f0 + (1.0f - f0) * dpow(1.0f - voh, 5.0f), 0.0f, 1.0f);
+}
+
+// DiffuseHammon (DiffuseRayTraceFrag.glsl:1311-1332), rcp(x) = 1/x
+__device__ __forceinline__ float diffuse_hammon(v3 n, v3 v, v3 l, float rough) {
+    float ndl = fmaxf(dot(n, l), 0.0f);
+    if (ndl <= 0.0f) return 0.0f;
+    float ndv = fmaxf(dot(n, v), 0.0f);
+    float ldv = fmaxf(dot(l, v), 0.0f);
+    v3 h = normalize(add(v, l));
+    float ndh = fmaxf(dot(n, h), 0.0f);
+    float facing = ldv * 0.5f + 0.5f;
+    float single_rough = facing * (0.9f - 0.4f * facing) * ((0.5f + ndh) * (1.0f / fmaxf(ndh, 0.02f)));
+    float single_smooth = 1.05f * inverse_schlick(0.0f, ndl) * inverse_schlick(0.0f, fmaxf(ndv, 0.0f));
+    float single = clampf(mixf(single_smooth, single_rough, rough) * (1.0f / kPI), 0.0f, 1.0f);
+    float multi = 0.1159f * rough;
+    return clampf((multi + single) * ndl, 0.0f, 1.0f);
+}
+
+// ---------------------------------------------------------------- random --
+// PCG-RXS-M-XS 32 (Jarzynski & Olano 2020), seeded per pixel; stands in for
+// the reference's fract(sin()) / blue-noise sequences.
+__host__ __device__ __forceinline__ uint32_t pcg_step(uint32_t* s) {
+    *s = *s * 747796405u + 2891336453u;
+    uint32_t w = ((*s >> ((*s >> 28u) + 4u)) ^ *s) * 277803737u;
+    return (w >> 22u) ^ w;
+}
+__host__ __device__ __forceinline__ uint32_t pcg_hash(uint32_t v) {
+    uint32_t s = v;
+    return pcg_step(&s);
+}
+__device__ __forceinline__ float rand01(uint32_t* s) { return (float)(pcg_step(s) >> 8) * (1.0f / 16777216.0f); }
+
+// cosWeightedRandomHemisphereDirection (DiffuseRayTraceFrag.glsl:945-967)
+__device__ __forceinline__ v3 cos_hemisphere(v3 n, uint32_t* rng) {
+    float rx_ = rand01(rng);
+    float ry_ = rand01(rng);
+    float pi2 = 2.0f * kPI;
+    v3 uu = normalize(cross(n, mk3(0.0f, 1.0f, 1.0f)));
+    v3 vv = cross(uu, n);
+    float ra = sqrtf(ry_);
+    float sn, cs;
+    dsincos(pi2 * rx_, &sn, &cs);
+    float rx = ra * cs;
+    float ry = ra * sn;
+    float rz = sqrtf(1.0f - ry_);
+    v3 rr = mk3((rx * uu.x + ry * vv.x) + rz * n.x, (rx * uu.y + ry * vv.y) + rz * n.y,
+                (rx * uu.z + ry * vv.z) + rz * n.z);
+    return normalize(rr);
+}
+
+// ------------------------------------------------------------- materials --
+struct Material {
+    v3 albedo;
+    float rough, metal;
+    int emissive;
+};
+__device__ __forceinline__ Material material(const WorldView& w, int id) {
+    if (id < 0 || id >= w.n_blocks) id = 0;
+    const uint8_t* b = reinterpret_cast<const uint8_t*>(w.blocks + id);
+    Material m;
+    m.albedo = mk3((float)__ldg(b + 0) / 255.0f, (float)__ldg(b + 1) / 255.0f, (float)__ldg(b + 2) / 255.0f);
+    m.rough = (float)__ldg(b + 3) / 255.0f;
+    m.metal = (float)__ldg(b + 4) / 255.0f;
+    m.emissive = __ldg(b + 5) ? 1 : 0;
+    return m;
+}
+
+// Per-frame constants of DiffuseRayTraceFrag main (:832-839), computed once on the host.
+struct GILighting {
+    float light_color[3];
+    float light_dir[3];
+    int moon_stronger;
+    float emissivity_multiplier;
+    float sun_visibility;          // Core/Pipeline.cpp:1828
+    float gi_sky_strength;
+    float diffuse_light_intensity;
+};
+
+}  // namespace vpt

@@ -1,0 +1,110 @@
+// Launch interfaces of the libvpt kernels (one translation unit per group).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace vpt {
+
+// Device counters filled when statistics are on (layout of vpt_stats).
+struct Counters {
+    unsigned long long rays[4];
+    unsigned long long steps[4];
+};
+enum RayKind { kRayPrimary = 0, kRayShadow = 1, kRayDiffuse = 2, kRayBounceShadow = 3 };
+
+// ---------------------------------------------------------------- df.cu --
+// Manhattan distance field, min(min(254, X+Y+Z), L1 distance to the nearest
+// solid voxel): three sweeps along x, y and z. `launches` counts kernels.
+cudaError_t df_build(const uint8_t* vox, uint8_t* df, int X, int Y, int Z, cudaStream_t s, int* launches);
+
+// ------------------------------------------------------------- trace.cu --
+struct GBufferOut {
+    void* t;            // storage type
+    uint8_t* face;
+    uint8_t* block;
+    int32_t* hit;       // 3 per pixel
+    uint16_t* steps;
+};
+struct DiffuseArgs {
+    int diffuse_max_steps;
+    int bounce_shadow_max_steps;
+    int bounces;
+    int spp;
+    uint32_t frame_index;
+    uint32_t seed;
+    GILighting lighting;
+};
+struct GIOut {
+    void* sh;           // 4 ch
+    void* cocg;         // 2 ch
+    void* luma;         // 1 ch
+    void* aosky;        // 2 ch
+};
+
+cudaError_t trace_primary(const WorldView& w, const CamView& cam, int W, int H, int max_steps, int fp16,
+                          GBufferOut out, Counters* stats, cudaStream_t s);
+cudaError_t trace_shadow(const WorldView& w, const CamView& cam, int W, int H, int max_steps, const float sun[3],
+                         int fp16, const void* t, const uint8_t* face, uint8_t* shadow, Counters* stats,
+                         cudaStream_t s);
+cudaError_t trace_diffuse(const WorldView& w, const CamView& cam, int W, int H, const DiffuseArgs& a, int fp16,
+                          const void* t, const uint8_t* face, GIOut out, Counters* stats, cudaStream_t s);
+
+// -------------------------------------------------------------- svgf.cu --
+struct GIIn {
+    const void* sh;
+    const void* cocg;
+    const void* luma;
+    const void* aosky;
+};
+struct HistIO {          // util has 4 channels: frames, moment, luma, 0
+    void* sh;
+    void* cocg;
+    void* util;
+    void* aosky;
+};
+struct FiltIO {
+    void* sh;
+    void* cocg;
+    void* variance;
+    void* aosky;
+};
+struct TemporalArgs {
+    float prev_view_proj[16];   // u_PrevProjection * u_PrevView, evaluated on the host
+    int be_useful;
+};
+struct AtrousArgs {
+    int step;
+    float add_scale;            // mix(1, 2.4, u_ResolutionScale)
+    float phi_bias;             // max(u_ColorPhiBias, 0.1)
+    float tmod500;              // mod(u_Time * 100.493850275, 500)
+};
+
+cudaError_t svgf_spatial_initial(const CamView& cam, int W, int H, int fp16, const void* t, const uint8_t* face,
+                                 GIIn in, GIOut out, cudaStream_t s);
+cudaError_t svgf_temporal(const CamView& cam, int W, int H, int fp16, const TemporalArgs& a,
+                          const void* t, const uint8_t* face, const uint8_t* block,
+                          const void* prev_t, const uint8_t* prev_face, const uint8_t* prev_block,
+                          GIIn cur, HistIO prev, HistIO out, cudaStream_t s);
+cudaError_t svgf_variance(const CamView& cam, int W, int H, int fp16, const void* t, const uint8_t* face,
+                          HistIO in, FiltIO out, cudaStream_t s);
+cudaError_t svgf_atrous(const CamView& cam, int W, int H, int fp16, const AtrousArgs& a,
+                        const void* t, const uint8_t* face, const void* temporal_util,
+                        FiltIO in, const void* in_aosky, FiltIO out, cudaStream_t s);
+
+// ------------------------------------------------------------- shade.cu --
+struct ShadeArgs {
+    float sun[3], moon[3];
+    float sun_color[3], moon_color[3];
+    float sun_vis;             // 1 - clamp(dot(sun, up) + 0.05, 0, 0.1) * 12
+};
+cudaError_t shade(const WorldView& w, const CamView& cam, int W, int H, int fp16, const ShadeArgs& a,
+                  const void* t, const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
+                  const void* sh, const void* cocg, const void* aosky, void* rgb, cudaStream_t s);
+
+// Deterministic-math probe: evaluates op `op` (0 exp, 1 exp2, 2 log2, 3 pow,
+// 4 sin, 5 cos) over n inputs on the device.
+cudaError_t detmath_eval(int op, const float* x, const float* y, float* out, int n, cudaStream_t s);
+
+}  // namespace vpt

@@ -1,0 +1,192 @@
+// Colour pass (ColorPassFrag.glsl main, :747-1083) for flat materials:
+// Cook-Torrance direct sun/moon light with the traced shadow, SH irradiance
+// decode of the denoised GI, VXAO and the DFG (Karis) indirect combine
+// (u_UseDFG on, Core/Pipeline.cpp:3683). One thread per pixel, a streaming
+// pass over the G-buffer and the denoised planes.
+#include "kernels.cuh"
+
+namespace vpt {
+
+namespace {
+
+// FresnelSchlickRoughness (ColorPassFrag.glsl:1205-1209)
+__device__ __forceinline__ v3 fresnel_schlick_roughness(v3 eye, v3 n, v3 f0, float rough) {
+    float cos_theta = clampf(dot(eye, n), 0.00001f, 1.0f);
+    float k = dpow(1.0f - cos_theta, 5.0f);
+    v3 m = mk3(fmaxf(1.0f - rough, f0.x), fmaxf(1.0f - rough, f0.y), fmaxf(1.0f - rough, f0.z));
+    return add(f0, muls(sub(m, f0), k));
+}
+
+// CalculateDirectionalLight (ColorPassFrag.glsl:419-451) with ndfGGX (:394-400)
+// and gaSchlickGGX (:402-412)
+__device__ __forceinline__ v3 directional_light(v3 viewer, v3 wp, v3 light_dir, v3 radiance, v3 radiance_s,
+                                                v3 albedo, v3 n, float rough, float metal, float shadow) {
+    const float DIELECTRIC = 0.04f, Epsilon = 0.00001f;
+    float sh = fminf(shadow, 1.0f);
+    v3 lo = normalize(sub(viewer, wp));
+    float cos_lo = fmaxf(0.0f, dot(n, lo));
+    v3 f0 = vmix(mk3(DIELECTRIC, DIELECTRIC, DIELECTRIC), albedo, metal);
+    v3 li = light_dir;
+    v3 lh = normalize(add(li, lo));
+    float cos_li = fmaxf(0.0f, dot(n, li));
+    float cos_lh = fmaxf(0.0f, dot(n, lh));
+    v3 F = fresnel_schlick_roughness(lo, n, f0, rough);
+    float alpha = rough * rough;
+    float alpha_sq = alpha * alpha;
+    float denom = (cos_lh * cos_lh) * (alpha_sq - 1.0f) + 1.0f;
+    float D = alpha_sq / ((kPI * denom) * denom);
+    float r1 = rough + 1.0f;
+    float k = (r1 * r1) / 8.0f;
+    float G = (cos_li / (cos_li * (1.0f - k) + k)) * (cos_lo / (cos_lo * (1.0f - k) + k));
+    v3 kd = vmix(sub(mk3(1.0f, 1.0f, 1.0f), F), mk3(0.0f, 0.0f, 0.0f), metal);
+    v3 diffuse_brdf = mul(kd, albedo);
+    v3 spec = divs(muls(muls(F, D), G), fmaxf(Epsilon, (4.0f * cos_li) * cos_lo));
+    spec = vclamp(spec, 0.0f, 2.0f);
+    v3 result = add(muls(mul(diffuse_brdf, radiance), cos_li), muls(mul(spec, radiance_s), cos_li));
+    return muls(vclamp(result, 0.0f, 2.5f), clampf(1.0f - sh, 0.0f, 1.0f));
+}
+
+// BasicSaturation (ColorPassFrag.glsl:1227-1232)
+__device__ __forceinline__ v3 basic_saturation(v3 c, float adj) {
+    float l = dot(c, mk3(0.2125f, 0.7154f, 0.0721f));
+    return vmix(mk3(l, l, l), c, adj);
+}
+
+// KarisEnvBRDFApprox (ColorPassFrag.glsl:384-391)
+__device__ __forceinline__ v2 karis_env_brdf(float ndv, float rough) {
+    float rx = rough * -1.0f + 1.0f;
+    float ry = rough * -0.0275f + 0.0425f;
+    float rz = rough * -0.572f + 1.040f;
+    float rw = rough * 0.022f + -0.040f;
+    float a004 = fminf(rx * rx, dexp2(-9.28f * ndv)) * rx + ry;
+    return mk2(-1.04f * a004 + rz, 1.04f * a004 + rw);
+}
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_shade(WorldView w, CamView cam, int W, int H, ShadeArgs a, const S* t,
+                                               const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
+                                               const S* sh_p, const S* cocg_p, const S* ao_p, S* rgb) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= W || j >= H) return;
+    size_t px = (size_t)j * W + i;
+    const v3 viewer = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
+    v2 uv = texcoord(i, j, W, H);
+    v3 dir = normalize(ray_dir_at(cam, uv));
+    // SamplePositionAt (:1122-1126) reads 1/t from the R32F depth plane
+    float dist = 1.0f / (1.0f / ld(t + px));
+    v3 wp = add(ray_origin(cam), muls(dir, dist));
+    v3 n = normal_from_id(__ldg(face + px), 1.0f);
+    v3 color;
+    if (dist > 0.0f) {
+        int bid = min(max((int)__ldg(block + px), 0), 127);
+        Material m = material(w, bid);
+        v3 albedo = basic_saturation(m.albedo, 1.0f - 0.1f);
+        if (m.metal >= 0.1f - 0.01f) albedo = basic_saturation(albedo, 0.9f);
+        float emissivity = (float)m.emissive;
+        float shy[4], cc[2];
+        for (int c = 0; c < 4; c++) shy[c] = ld(sh_p + px * 4 + c);
+        cc[0] = ld(cocg_p + px * 2 + 0);
+        cc[1] = ld(cocg_p + px * 2 + 1);
+        float up_shadow = clampf((float)__ldg(shadow + px), 0.0f, 1.0f);
+        float up_ao = ld(ao_p + px * 2 + 0);
+        float rt_shadow = clampf(clampf(up_shadow + 0.0f, 0.0f, 1.0f), 0.0f, 1.0f);
+        v3 indirect = sh_to_irradiance(shy, cc, n);
+        const float vb = 0.00125f;
+        if (uv.x > vb && uv.x < 1.0f - vb && uv.y > vb && uv.y < 1.0f - vb) {
+            float ao = up_ao;
+            float dxz = sqrtf((wp.x - viewer.x) * (wp.x - viewer.x) + (wp.z - viewer.z) * (wp.z - viewer.z));
+            float fade = dxz < 256.0f ? 0.0f : 1.0f;
+            ao = mixf(ao, 1.0f, fade);
+            ao = dpow(ao, 2.2f);
+            indirect = muls(indirect, clampf(ao, 0.05f, 1.0f));
+        }
+        float sampled_ao = dpow(1.0f, 1.25f);
+        v3 sun = mk3(a.sun[0], a.sun[1], a.sun[2]);
+        v3 moon = mk3(a.moon[0], a.moon[1], a.moon[2]);
+        v3 sun_color = mk3(a.sun_color[0], a.sun_color[1], a.sun_color[2]);
+        v3 moon_color = mk3(a.moon_color[0], a.moon_color[1], a.moon_color[2]);
+        v3 sun_direct = directional_light(viewer, wp, sun, sun_color, sun_color, albedo, n, m.rough, m.metal, rt_shadow);
+        v3 moon_direct = directional_light(viewer, wp, moon, moon_color, moon_color, albedo, n, m.rough, m.metal, rt_shadow);
+        v3 direct = vmixv(sun_direct, moon_direct, mk3(a.sun_vis * 1.0f, a.sun_vis * 1.0f, a.sun_vis * 1.0f));
+        direct = muls(direct, (!(emissivity > 0.05f)) ? 1.0f : 0.0f);
+        direct = vmax(direct, 0.000001f);
+        float rough = m.rough;
+        v3 diffuse_indirect = mul(indirect, albedo);
+        v3 I = normalize(sub(wp, viewer));
+        float idn = dot(n, I);
+        v3 R = sub(I, muls(n, 2.0f * idn));
+        v3 spec_ind = vmax(mk3(0.0f, 0.0f, 0.0f), 0.0001f);
+        v3 Lo = normalize(sub(viewer, wp));
+        v3 F0 = vmix(mk3(0.04f, 0.04f, 0.04f), albedo, m.metal);
+        diffuse_indirect = muls(diffuse_indirect, clampf(sampled_ao, 0.2f, 1.01f));
+        float nov = clampf(dot(n, Lo), 0.0000000001f, 1.0f);
+        // ComputeSpecularAO (:742-745) with the flat G-buffer AO of 1
+        float spec_ao = clampf(dpow(nov + 1.0f, dexp2(-16.0f * rough - 1.0f)) - 1.0f + 1.0f, 0.0f, 1.0f);
+        spec_ao = dpow(spec_ao, 1.5f);
+        float horizon = fminf(1.0f + dot(R, n), 1.0f);
+        horizon = (horizon * horizon) * horizon;
+        if (m.metal >= 0.1f) spec_ind = muls(spec_ind, 1.3f);
+        spec_ind = muls(spec_ind, spec_ao);
+        spec_ind = muls(spec_ind, horizon);
+        v3 F = vclamp(fresnel_schlick_roughness(Lo, n, F0, rough), 0.0f, 1.0f);
+        v3 kD = sub(mk3(1.0f, 1.0f, 1.0f), F);
+        kD = muls(kD, 1.0f - m.metal);
+        float ex = clampf(fmaxf(dot(neg(I), n), 0.000001f), 0.0f, 1.0f);
+        float ey = clampf(rough, 0.0f, 1.0f);
+        v2 env = karis_env_brdf(ex, ey);
+        v3 ind_spec = mul(spec_ind, mk3(F.x * env.x + env.y, F.y * env.x + env.y, F.z * env.x + env.y));
+        v3 indirect_light = add(mul(kD, diffuse_indirect), ind_spec);
+        color = add(direct, indirect_light);
+    } else {
+        color = sky_radiance(dir);
+    }
+    color = vmax(color, 0.000001f);
+    st(rgb + px * 3 + 0, color.x);
+    st(rgb + px * 3 + 1, color.y);
+    st(rgb + px * 3 + 2, color.z);
+}
+
+}  // namespace
+
+cudaError_t shade(const WorldView& w, const CamView& cam, int W, int H, int fp16, const ShadeArgs& a,
+                  const void* t, const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
+                  const void* sh, const void* cocg, const void* aosky, void* rgb, cudaStream_t s) {
+    dim3 grid((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8));
+    dim3 blk(32, 8);
+    if (fp16)
+        k_shade<__half><<<grid, blk, 0, s>>>(w, cam, W, H, a, (const __half*)t, face, block, shadow,
+                                             (const __half*)sh, (const __half*)cocg, (const __half*)aosky,
+                                             (__half*)rgb);
+    else
+        k_shade<float><<<grid, blk, 0, s>>>(w, cam, W, H, a, (const float*)t, face, block, shadow,
+                                            (const float*)sh, (const float*)cocg, (const float*)aosky,
+                                            (float*)rgb);
+    return cudaGetLastError();
+}
+
+namespace {
+__global__ void k_detmath(int op, const float* x, const float* y, float* out, int n) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    float a = x[k];
+    float r;
+    switch (op) {
+        case 0: r = dexp(a); break;
+        case 1: r = dexp2(a); break;
+        case 2: r = dlog2(a); break;
+        case 3: r = dpow(a, y[k]); break;
+        case 4: r = dsin(a); break;
+        default: r = dcos(a); break;
+    }
+    out[k] = r;
+}
+}  // namespace
+
+cudaError_t detmath_eval(int op, const float* x, const float* y, float* out, int n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_detmath<<<(n + 255) / 256, 256, 0, s>>>(op, x, y, out, n);
+    return cudaGetLastError();
+}
+
+}  // namespace vpt

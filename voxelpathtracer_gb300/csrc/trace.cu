@@ -1,0 +1,370 @@
+// DF-accelerated voxel DDA and the three trace passes: primary (G-buffer),
+// sun shadow and diffuse GI.
+//
+// The traversal restates VoxelTraversalDF (InitialRayTraceFrag.glsl:307-374;
+// the same loop appears at ShadowRayTraceFrag.glsl:222-289 and
+// DiffuseRayTraceFrag.glsl:1043-1110) in IEEE fp32 without fused
+// multiply-adds, so hit voxel, face and step count are bit-identical to the
+// CPU restatement. Each step is one dependent 1-byte gather from the distance
+// field; the kernels are bound by L2 latency/bandwidth of those gathers.
+#include "kernels.cuh"
+
+namespace vpt {
+
+namespace {
+
+// int(floor(ToConservativeEuclidean(Dist))) (InitialRayTraceFrag.glsl:89-92, :328-330)
+__device__ __forceinline__ int euclid_steps(int dist) {
+    float D = (float)dist;
+    float e = (D == 1.0f) ? 1.0f : D * 0.57735026918f;
+    return f2i(floorf(e));
+}
+
+struct TraceResult {
+    float t;
+    v3 normal;
+    int block;
+    int cell[3];
+    int steps;
+};
+
+__device__ __forceinline__ TraceResult traverse(const WorldView& w, v3 origin, v3 direction, int max_steps) {
+    const v3 initial = origin;
+    bool intersection = false;
+    int min_idx = 0;
+    const int sx = isign(direction.x), sy = isign(direction.y), sz = isign(direction.z);
+    const int hx = (1 + sx) >> 1, hy = (1 + sy) >> 1, hz = (1 + sz) >> 1;
+    const float ix = 1.0f / direction.x, iy = 1.0f / direction.y, iz = 1.0f / direction.z;
+    int itr = 0;
+    for (itr = 0; itr < max_steps; itr++) {
+        int lx = f2i(floorf(origin.x));
+        int ly = f2i(floorf(origin.y));
+        int lz = f2i(floorf(origin.z));
+        if (!in_volume(w, lx, ly, lz)) {
+            intersection = false;
+            break;
+        }
+        int e = euclid_steps((int)__ldg(w.df + vox_index(w, lx, ly, lz)));
+        if (e == 0) break;
+        if (e == 1) {
+            int gx = f2i(origin.x), gy = f2i(origin.y), gz = f2i(origin.z);
+            float wx = origin.x - (float)gx, wy = origin.y - (float)gy, wz = origin.z - (float)gz;
+            float dfx = ((float)hx - wx) * ix;
+            float dfy = ((float)hy - wy) * iy;
+            float dfz = ((float)hz - wz) * iz;
+            min_idx = (dfx < dfy && sx != 0) ? ((dfx < dfz || sz == 0) ? 0 : 2)
+                                             : ((dfy < dfz || sz == 0) ? 1 : 2);
+            float dm = min_idx == 0 ? dfx : (min_idx == 1 ? dfy : dfz);
+            wx = wx + direction.x * dm;
+            wy = wy + direction.y * dm;
+            wz = wz + direction.z * dm;
+            if (min_idx == 0) { gx += sx; wx = (float)(1 - hx); }
+            else if (min_idx == 1) { gy += sy; wy = (float)(1 - hy); }
+            else { gz += sz; wz = (float)(1 - hz); }
+            origin.x = (float)gx + wx;
+            origin.y = (float)gy + wy;
+            origin.z = (float)gz + wz;
+            if (min_idx == 0) origin.x = origin.x + (float)sx * 0.0001f;
+            else if (min_idx == 1) origin.y = origin.y + (float)sy * 0.0001f;
+            else origin.z = origin.z + (float)sz * 0.0001f;
+            intersection = true;
+        } else {
+            float k = (float)(e - 1);
+            origin.x = origin.x + k * direction.x;
+            origin.y = origin.y + k * direction.y;
+            origin.z = origin.z + k * direction.z;
+        }
+    }
+    TraceResult r;
+    r.cell[0] = f2i(floorf(origin.x));
+    r.cell[1] = f2i(floorf(origin.y));
+    r.cell[2] = f2i(floorf(origin.z));
+    r.steps = itr;
+    r.normal = mk3(0.0f, 0.0f, 0.0f);
+    r.block = 0;
+    r.t = -1.0f;
+    if (intersection) {
+        int s = min_idx == 0 ? sx : (min_idx == 1 ? sy : sz);
+        float nv = (float)(-s);
+        if (min_idx == 0) r.normal.x = nv; else if (min_idx == 1) r.normal.y = nv; else r.normal.z = nv;
+        r.block = get_voxel(w, r.cell[0], r.cell[1], r.cell[2]);
+        r.t = r.block > 0 ? length(sub(origin, initial)) : -1.0f;
+    }
+    return r;
+}
+
+// GetNormalID (InitialRayTraceFrag.glsl:143-185)
+__device__ __forceinline__ int normal_id(v3 n) {
+    if (n.x == 0.0f && n.y == 0.0f && n.z == 1.0f) return 0;
+    if (n.x == 0.0f && n.y == 0.0f && n.z == -1.0f) return 1;
+    if (n.x == 0.0f && n.y == 1.0f && n.z == 0.0f) return 2;
+    if (n.x == 0.0f && n.y == -1.0f && n.z == 0.0f) return 3;
+    if (n.x == -1.0f && n.y == 0.0f && n.z == 0.0f) return 4;
+    if (n.x == 1.0f && n.y == 0.0f && n.z == 0.0f) return 5;
+    return 0;
+}
+
+// Pixel of thread `tid` in a 16x16 tile: each warp covers an 8x4 patch so its
+// rays stay spatially coherent.
+__device__ __forceinline__ void tile_pixel(int* i, int* j) {
+    int tid = threadIdx.x;
+    int warp = tid >> 5, lane = tid & 31;
+    *i = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+    *j = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
+}
+
+__device__ __forceinline__ void count_rays(Counters* c, int kind, unsigned rays, unsigned steps) {
+    unsigned r = __reduce_add_sync(0xffffffffu, rays);
+    unsigned s = __reduce_add_sync(0xffffffffu, steps);
+    if ((threadIdx.x & 31) == 0 && (r | s)) {
+        atomicAdd(&c->rays[kind], (unsigned long long)r);
+        atomicAdd(&c->steps[kind], (unsigned long long)s);
+    }
+}
+
+// InitialRayTraceFrag.glsl main (:417-468)
+template <typename S>
+__global__ void __launch_bounds__(256) k_trace_primary(WorldView w, CamView cam, int W, int H, int max_steps,
+                                                       S* out_t, uint8_t* out_face, uint8_t* out_block,
+                                                       int32_t* out_hit, uint16_t* out_steps, Counters* stats) {
+    int i, j;
+    tile_pixel(&i, &j);
+    bool valid = i < W && j < H;
+    unsigned nsteps = 0;
+    if (valid) {
+        size_t px = (size_t)j * W + i;
+        v3 r0 = ray_origin(cam);
+        v3 dir = normalize(ray_dir_at(cam, texcoord(i, j, W, H)));
+        TraceResult r = traverse(w, r0, dir, max_steps);
+        bool intersect = r.t > 0.0f && r.block > 0;
+        st(out_t + px, r.t);
+        out_face[px] = (uint8_t)(intersect ? normal_id(r.normal) : kFaceMiss);
+        out_block[px] = (uint8_t)(intersect ? r.block : 0);
+        out_hit[px * 3 + 0] = r.cell[0];
+        out_hit[px * 3 + 1] = r.cell[1];
+        out_hit[px * 3 + 2] = r.cell[2];
+        out_steps[px] = (uint16_t)r.steps;
+        nsteps = (unsigned)r.steps;
+    }
+    if (stats) count_rays(stats, kRayPrimary, valid ? 1u : 0u, nsteps);
+}
+
+// ShadowRayTraceFrag.glsl main (:414-513): one hard shadow ray towards the sun.
+template <typename S>
+__global__ void __launch_bounds__(256) k_trace_shadow(WorldView w, CamView cam, int W, int H, int max_steps,
+                                                      float lx, float ly, float lz, const S* t,
+                                                      const uint8_t* face, uint8_t* shadow, Counters* stats) {
+    int i, j;
+    tile_pixel(&i, &j);
+    unsigned nrays = 0, nsteps = 0;
+    if (i < W && j < H) {
+        size_t px = (size_t)j * W + i;
+        float d = ld(t + px);
+        uint8_t out;
+        if (d < 0.0f) {
+            out = 0;
+        } else {
+            v3 L = mk3(lx, ly, lz);
+            v3 pos = add(ray_origin(cam), muls(normalize(ray_dir_at(cam, texcoord(i, j, W, H))), d));
+            v3 n = normal_from_id(__ldg(face + px), 1.0f);
+            float ndl = dot(n, L);
+            if (ndl <= 0.01f) {
+                out = 1;
+            } else {
+                v3 o = add(pos, mul(n, mk3(0.06f, 0.06f, 0.06f)));
+                int block_at = get_voxel(w, f2i(floorf(o.x)), f2i(floorf(o.y)), f2i(floorf(o.z)));
+                float T = -1.0f;
+                if (d > 0.0f) {
+                    TraceResult r = traverse(w, o, L, max_steps);
+                    T = r.t;
+                    nrays = 1;
+                    nsteps = (unsigned)r.steps;
+                }
+                out = (T > 0.0f || block_at > 0) ? 1 : 0;
+            }
+        }
+        shadow[px] = out;
+    }
+    if (stats) count_rays(stats, kRayShadow, nrays, nsteps);
+}
+
+struct GICount {
+    unsigned diffuse_rays, diffuse_steps, shadow_rays, shadow_steps;
+};
+
+// CalculateDiffuse (DiffuseRayTraceFrag.glsl:535-664)
+__device__ __forceinline__ v4 calculate_diffuse(const WorldView& w, const DiffuseArgs& a, v3 initial_origin,
+                                                v3 input_normal, uint32_t* rng, v3* odir, bool* skyhit,
+                                                GICount* cnt) {
+    const GILighting& L = a.lighting;
+    const v3 light_dir = mk3(L.light_dir[0], L.light_dir[1], L.light_dir[2]);
+    const v3 light_color = mk3(L.light_color[0], L.light_color[1], L.light_color[2]);
+    *skyhit = false;
+    const float bias = 0.06f;
+    v3 ro = add(initial_origin, muls(input_normal, bias));
+    v3 rd = cos_hemisphere(input_normal, rng);
+    float ao = 1.0f;
+    v3 contribution = mk3(0.0f, 0.0f, 0.0f);
+    v3 throughput = mk3(1.0f, 1.0f, 1.0f);
+    for (int i = 0; i < a.bounces; i++) {
+        if (i == 0) *odir = rd;
+        TraceResult tr = traverse(w, ro, rd, a.diffuse_max_steps);
+        cnt->diffuse_rays += 1;
+        cnt->diffuse_steps += (unsigned)tr.steps;
+        float T = tr.t;
+        bool intersect = T > 0.0f;
+        v3 ip = add(ro, muls(rd, T));
+        if (intersect && tr.block > 0) {
+            Material m = material(w, min(max(tr.block, 0), 127));
+            v3 hn = tr.normal;
+            float emissivity = 0.0f;
+            if (m.emissive) emissivity = 1.0f * L.emissivity_multiplier * L.diffuse_light_intensity;
+            float ndl = fmaxf(dot(hn, light_dir), 0.0f);
+            v3 bias_shadow = muls(hn, 0.045f);
+            float shadow_at;
+            if (L.moon_stronger) {
+                shadow_at = 1.0f;
+            } else if (ndl < 0.001f) {
+                shadow_at = 0.0f;
+            } else {
+                // GetShadowAt (:1202-1222)
+                TraceResult sr = traverse(w, add(ip, bias_shadow), light_dir, a.bounce_shadow_max_steps);
+                cnt->shadow_rays += 1;
+                cnt->shadow_steps += (unsigned)sr.steps;
+                shadow_at = sr.t > 0.0f ? 1.0f : 0.0f;
+            }
+            v3 emissive_color = muls(m.albedo, emissivity * mixf(1.0f, 1.0f, L.sun_visibility));
+            float hs = diffuse_hammon(hn, neg(rd), light_dir, m.rough);
+            v3 sun_brdf = muls(muls(mul(muls(m.albedo, hs), muls(light_color, 3.5f)), 1.0f - shadow_at), kPI);
+            v3 new_dir = cos_hemisphere(hn, rng);
+            float cos_theta = clampf(dot(hn, new_dir), 0.0f, 1.0f);
+            float pdf = fmaxf(cos_theta / kPI, 0.00001f);
+            float att = diffuse_hammon(hn, neg(rd), new_dir, m.rough);
+            contribution = add(contribution, mul(throughput, sun_brdf));
+            contribution = add(contribution, mul(emissive_color, throughput));
+            throughput = mul(throughput, divs(muls(m.albedo, att), pdf));
+            rd = new_dir;
+            ro = add(ip, muls(hn, bias));
+        } else {
+            float x = mixf(1.0f, 1.05f, L.sun_visibility);
+            x = clampf(x * 1.0f * L.gi_sky_strength, 0.0f, 5.0f);
+            v3 sky = muls(sky_color_at(rd), x);
+            contribution = add(contribution, mul(sky, throughput));
+            *skyhit = true;
+            break;
+        }
+        if (i == 0) {
+            const float dao = 2.0f;
+            if (T < dao && T > 0.0f) ao = fmaxf(T / dao, 0.0f);
+        }
+    }
+    v4 r;
+    r.x = contribution.x; r.y = contribution.y; r.z = contribution.z; r.w = ao;
+    return r;
+}
+
+// DiffuseRayTraceFrag.glsl main (:822-935)
+template <typename S>
+__global__ void __launch_bounds__(256) k_trace_diffuse(WorldView w, CamView cam, int W, int H, DiffuseArgs a,
+                                                       const S* t, const uint8_t* face, S* o_sh, S* o_cocg,
+                                                       S* o_luma, S* o_aosky, Counters* stats) {
+    int i, j;
+    tile_pixel(&i, &j);
+    GICount cnt = {0u, 0u, 0u, 0u};
+    if (i < W && j < H) {
+        size_t px = (size_t)j * W + i;
+        v3 dir = normalize(ray_dir_at(cam, texcoord(i, j, W, H)));
+        float d = ld(t + px);
+        v3 pos = add(ray_origin(cam), muls(dir, d));
+        v3 n = normal_from_id(__ldg(face + px), 0.5f);
+        float sh[4], cocg[2];
+        if (d < 0.0f) {
+            irradiance_to_sh(muls(sky_radiance(dir), 2.66f), n, sh, cocg);
+            for (int c = 0; c < 4; c++) st(o_sh + px * 4 + c, sh[c]);
+            st(o_cocg + px * 2 + 0, cocg[0]);
+            st(o_cocg + px * 2 + 1, cocg[1]);
+            st(o_luma + px, luminance(mk3(0.0f, 0.0f, 0.0f)));
+            st(o_aosky + px * 2 + 0, 1.0f);
+            st(o_aosky + px * 2 + 1, 0.0f);
+        } else {
+            uint32_t rng = pcg_hash((uint32_t)px + pcg_hash(a.frame_index + pcg_hash(a.seed)));
+            int spp = min(max(a.spp, 1), 32);
+            if (a.lighting.moon_stronger) spp *= 2;
+            float tsh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, tcc[2] = {0.0f, 0.0f};
+            v3 radiance = mk3(0.0f, 0.0f, 0.0f);
+            float acc_ao = 0.0f, skyhits = 0.0f;
+            for (int s = 0; s < spp; s++) {
+                v3 odir = mk3(0.0f, 0.0f, 0.0f);
+                bool ss = false;
+                v4 x = calculate_diffuse(w, a, pos, n, &rng, &odir, &ss, &cnt);
+                v3 xc = vclamp(mk3(x.x, x.y, x.z), 0.0f, 8.0f);
+                radiance = add(radiance, xc);
+                acc_ao += x.w;
+                irradiance_to_sh(xc, odir, sh, cocg);
+                for (int c = 0; c < 4; c++) tsh[c] += sh[c];
+                tcc[0] += cocg[0];
+                tcc[1] += cocg[1];
+                skyhits += ss ? 1.0f : 0.0f;
+            }
+            float fs = (float)spp;
+            acc_ao /= fs;
+            for (int c = 0; c < 4; c++) tsh[c] /= fs;
+            tcc[0] /= fs;
+            tcc[1] /= fs;
+            radiance = divs(radiance, fs);
+            skyhits /= fs;
+            for (int c = 0; c < 4; c++) st(o_sh + px * 4 + c, clampf(tsh[c], -100.0f, 100.0f));
+            st(o_cocg + px * 2 + 0, clampf(tcc[0], -100.0f, 100.0f));
+            st(o_cocg + px * 2 + 1, clampf(tcc[1], -100.0f, 100.0f));
+            st(o_luma + px, clampf(fmaxf(luminance(radiance), 0.01f), 0.001f, 64.0f));
+            st(o_aosky + px * 2 + 0, clampf(acc_ao, 0.0f, 1.0f));
+            st(o_aosky + px * 2 + 1, clampf(skyhits, 0.0f, 1.0f));
+        }
+    }
+    if (stats) {
+        count_rays(stats, kRayDiffuse, cnt.diffuse_rays, cnt.diffuse_steps);
+        count_rays(stats, kRayBounceShadow, cnt.shadow_rays, cnt.shadow_steps);
+    }
+}
+
+inline dim3 tile_grid(int W, int H) { return dim3((unsigned)((W + 15) / 16), (unsigned)((H + 15) / 16)); }
+
+}  // namespace
+
+cudaError_t trace_primary(const WorldView& w, const CamView& cam, int W, int H, int max_steps, int fp16,
+                          GBufferOut out, Counters* stats, cudaStream_t s) {
+    if (fp16)
+        k_trace_primary<__half><<<tile_grid(W, H), 256, 0, s>>>(w, cam, W, H, max_steps, (__half*)out.t, out.face,
+                                                                out.block, out.hit, out.steps, stats);
+    else
+        k_trace_primary<float><<<tile_grid(W, H), 256, 0, s>>>(w, cam, W, H, max_steps, (float*)out.t, out.face,
+                                                               out.block, out.hit, out.steps, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t trace_shadow(const WorldView& w, const CamView& cam, int W, int H, int max_steps, const float sun[3],
+                         int fp16, const void* t, const uint8_t* face, uint8_t* shadow, Counters* stats,
+                         cudaStream_t s) {
+    if (fp16)
+        k_trace_shadow<__half><<<tile_grid(W, H), 256, 0, s>>>(w, cam, W, H, max_steps, sun[0], sun[1], sun[2],
+                                                               (const __half*)t, face, shadow, stats);
+    else
+        k_trace_shadow<float><<<tile_grid(W, H), 256, 0, s>>>(w, cam, W, H, max_steps, sun[0], sun[1], sun[2],
+                                                              (const float*)t, face, shadow, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t trace_diffuse(const WorldView& w, const CamView& cam, int W, int H, const DiffuseArgs& a, int fp16,
+                          const void* t, const uint8_t* face, GIOut out, Counters* stats, cudaStream_t s) {
+    if (fp16)
+        k_trace_diffuse<__half><<<tile_grid(W, H), 256, 0, s>>>(w, cam, W, H, a, (const __half*)t, face,
+                                                                (__half*)out.sh, (__half*)out.cocg,
+                                                                (__half*)out.luma, (__half*)out.aosky, stats);
+    else
+        k_trace_diffuse<float><<<tile_grid(W, H), 256, 0, s>>>(w, cam, W, H, a, (const float*)t, face,
+                                                               (float*)out.sh, (float*)out.cocg, (float*)out.luma,
+                                                               (float*)out.aosky, stats);
+    return cudaGetLastError();
+}
+
+}  // namespace vpt
