@@ -64,8 +64,12 @@ def lib() -> C.CDLL:
     global _lib
     if _lib is None:
         if not LIB_PATH.exists():
-            from voxelpathtracer_gb300 import _build   # build helper only; the oracle code is in this folder
-            _build.build_oracle()
+            import importlib.util
+            build_py = LIB_PATH.parent.parent.parent / "voxelpathtracer_gb300" / "_build.py"
+            spec = importlib.util.spec_from_file_location("vpt_build", build_py)
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            mod.build_oracle()
         L = C.CDLL(str(LIB_PATH))
         P = C.c_void_p
         L.vpto_build_df.argtypes = [P, C.c_int, C.c_int, C.c_int, P]

@@ -15,8 +15,8 @@ def pytest_configure(config):
 
 def pytest_sessionstart(session):
     # Build libvpt and the oracle once per session (incremental, seconds).
-    from voxelpathtracer_gb300 import _build
-    _build.build_all()
+    import __graft_entry__
+    __graft_entry__.build()
 
 
 @pytest.fixture(scope="session")
