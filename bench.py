@@ -44,6 +44,19 @@ ALG_BYTES_PER_STEP = 32     # one 32-byte sector per DF gather
 ALG_BYTES_PER_RAY = 16      # ray output
 PEAKS_FILE = REPO / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
+TRACE_KINDS = {"primary": ["primary"], "shadow": ["shadow"], "diffuse": ["diffuse", "bounce_shadow"]}
+# Algorithmic bytes per pixel of the filter and colour kernels (planes read +
+# planes written once), fp32 / fp16 storage.
+FILTER_BYTES_PER_PX = {
+    "spatial_initial": (77, 39),   # t, face, SH, CoCg, luma, AO in; SH, CoCg, luma, AO out
+    "temporal": (144, 74),         # current G-buffer + pre-temporal planes, previous G-buffer + history; history out
+    "variance": (65, 33),          # t, face, SH, CoCg, util.xy in; SH, CoCg, variance out
+    "atrous": (81, 41),            # t, face, util.x, SH, CoCg, variance, AO in; SH, CoCg, variance, AO out
+    "shade": (47, 25),             # t, face, block, shadow, SH, CoCg, AO.x in; RGB out
+}
+KERNEL_NAMES = {"primary": "k_trace_primary", "shadow": "k_trace_shadow", "diffuse": "k_trace_diffuse",
+                "spatial_initial": "k_spatial_initial", "temporal": "k_temporal", "variance": "k_variance",
+                "atrous": "k_atrous", "shade": "k_shade"}
 
 
 def log(*a):
@@ -241,18 +254,26 @@ def run_ours(args):
     trace_ms = sum(sum(pass_ms[p]) for p in ("primary", "shadow", "diffuse"))
     trace_rays_per_s = sum(frame_rays) / (trace_ms / 1e3)
 
-    # dominant kernel: the pass with the largest device time
+    # roofline of every kernel; the dominant one has the largest share of the frame
     mean_pass = {k: (sum(v) / len(v) if v else 0.0) for k, v in pass_ms.items()}
-    dom = max(mean_pass, key=mean_pass.get)
-    kinds = {"primary": ["primary"], "shadow": ["shadow"], "diffuse": ["diffuse", "bounce_shadow"]}
-    if dom in kinds:
-        per_launch_bytes = np.mean([sum(st[k] for k in kinds[dom]) * ALG_BYTES_PER_STEP +
-                                    sum(r[k] for k in kinds[dom]) * ALG_BYTES_PER_RAY
-                                    for st, r in zip(steps[timed], rays[timed])])
-    else:
-        per_launch_bytes = float("nan")
-    achieved = per_launch_bytes / (mean_pass[dom] / 1e3) / 1e9
     peak, peak_kind = peak_hbm()
+    iters = ctx.config.atrous_iterations
+    kernels = {}
+    for p, ms in mean_pass.items():
+        launches_per_frame = iters if p == "atrous" else 1
+        if p in TRACE_KINDS:
+            b = float(np.mean([sum(st[k] for k in TRACE_KINDS[p]) * ALG_BYTES_PER_STEP +
+                               sum(r[k] for k in TRACE_KINDS[p]) * ALG_BYTES_PER_RAY
+                               for st, r in zip(steps[timed], rays[timed])]))
+        else:
+            b = float(FILTER_BYTES_PER_PX[p][args.storage] * W * H)
+        per_launch_ms = ms / launches_per_frame
+        gbs = b / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
+        kernels[p] = {"launches_per_frame": launches_per_frame, "ms_per_launch": per_launch_ms,
+                      "algorithmic_bytes_per_launch": b, "achieved_gbs": gbs, "frac": gbs / peak}
+    dom = max(mean_pass, key=mean_pass.get)
+    per_launch_bytes = kernels[dom]["algorithmic_bytes_per_launch"]
+    achieved = kernels[dom]["achieved_gbs"]
 
     # 3) end-to-end through the C ABI with host buffers (pinned)
     ctx.reset_history()
@@ -288,6 +309,8 @@ def run_ours(args):
         "frame_ms": ms_per_step,
         "trace_rays_per_s": trace_rays_per_s,
         "rays_per_frame": float(np.mean(frame_rays)),
+        "rays_per_frame_by_kind": {k: float(np.mean([r[k] for r in rays[timed]])) for k in rays[0]},
+        "dda_steps_per_frame_by_kind": {k: float(np.mean([s_[k] for s_ in steps[timed]])) for k in steps[0]},
         "pass_ms": {k: round(v, 4) for k, v in mean_pass.items()},
         "higher_is_better": True,
         "scaling": "weak",
@@ -304,10 +327,12 @@ def run_ours(args):
                 "d2h_bytes_per_step": W * H * 3 * 4, "ms_per_step": e2e_t * 1e3 / args.steps,
                 "api": "vpt_render_frame -> pinned host RGB"},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": f"trace_{dom}" if dom in kinds else dom,
+        "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom],
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": args.traffic,
-                     "algorithmic_bytes_per_launch": per_launch_bytes},
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                     else "fallback", "traffic": args.traffic,
+                     "algorithmic_bytes_per_launch": per_launch_bytes,
+                     "kernels": {KERNEL_NAMES[k]: v for k, v in kernels.items()}},
         "clocks": clk,
         "cpu_baseline": cpu,
     }
@@ -337,15 +362,24 @@ def band_rows(n):
     return (r0, r0 + n)
 
 
-def cpu_baseline(vpt, args, vox, blocks, yaw, pitch, sample_rows=48):
+def cpu_baseline(vpt, args, vox, blocks, yaw, pitch, sample_rows=None):
+    """Whole frames of the workload traced by the CPU restatement on all host
+    threads, repeated until args.cpu_seconds of CPU work have accumulated."""
     import oracle
     W, H = RES
-    rows = band_rows(sample_rows)
+    rows = band_rows(sample_rows) if sample_rows else (0, H)
     wobj = oracle.World(vox, oracle.build_df(vox), blocks)
-    dt, rays = cpu_band_frame(vpt, oracle, wobj, yaw, pitch, 0, rows)
-    return {"value": rays / dt, "unit": "rays/s", "cores": oracle.omp_threads(), "kind": "port",
-            "sample": f"rows {rows[0]}..{rows[1] - 1} of frame 0 ({sample_rows * W} pixels): primary + sun shadow + "
-                      f"diffuse + bounce-shadow rays of the CPU restatement, {rays} rays in {dt:.2f} s"}
+    cpu_band_frame(vpt, oracle, wobj, yaw, pitch, 0, (H // 2, H // 2 + 4))   # thread pool warm-up
+    t_sum, rays_sum, frames = 0.0, 0, 0
+    while t_sum < args.cpu_seconds:
+        dt, rays = cpu_band_frame(vpt, oracle, wobj, yaw, pitch, frames, rows)
+        t_sum += dt
+        rays_sum += rays
+        frames += 1
+    what = "whole frames" if rows == (0, H) else f"rows {rows[0]}..{rows[1] - 1} of frames"
+    return {"value": rays_sum / t_sum, "unit": "rays/s", "cores": oracle.omp_threads(), "kind": "port",
+            "sample": f"{what} 0..{frames - 1} of the workload (primary, sun-shadow, diffuse and bounce-shadow "
+                      f"rays of the CPU restatement): {rays_sum} rays in {t_sum:.1f} s"}
 
 
 def run_reference(args):
@@ -356,7 +390,7 @@ def run_reference(args):
     import voxelpathtracer_gb300 as vpt
     W, H = RES
     vox, blocks, yaw, pitch = workload_inputs(vpt, seed=0)
-    rows = band_rows(args.cpu_rows)
+    rows = band_rows(args.cpu_rows) if args.cpu_rows else (0, H)
     wobj = oracle.World(vox, oracle.build_df(vox), blocks)
     times, rays = [], []
     for s in range(args.warmup + args.steps):
@@ -365,8 +399,8 @@ def run_reference(args):
             times.append(dt)
             rays.append(n)
     value = sum(rays) / sum(times)
-    sample = (f"rows {rows[0]}..{rows[1] - 1} of each 1920x1080 frame ({args.cpu_rows * W} pixels): primary, sun "
-              f"shadow, diffuse and bounce-shadow rays of the CPU restatement")
+    what = "each whole 1920x1080 frame" if rows == (0, H) else f"rows {rows[0]}..{rows[1] - 1} of each frame"
+    sample = f"{what}: primary, sun-shadow, diffuse and bounce-shadow rays of the CPU restatement"
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -400,7 +434,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--storage", type=int, default=0, help="0 = fp32 planes, 1 = fp16 planes")
-    ap.add_argument("--cpu-rows", type=int, default=48)
+    ap.add_argument("--cpu-rows", type=int, default=0,
+                    help="trace only a band of this many rows on the CPU (0 = whole frames)")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="CPU work accumulated by the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the dominant kernel from an ncu capture")

@@ -7,8 +7,9 @@
 //
 // Every operation here is a single IEEE-754 binary32 operation or a fixed
 // sequence of them. The oracle is compiled with -ffp-contract=off and without
-// fast-math, so no multiply-add is fused and the results are reproducible on
-// any IEEE host (x86-64 and aarch64 alike).
+// fast-math, so no multiply-add is fused implicitly; the polynomial steps of
+// the functions below call fmaf explicitly, which is a single correctly
+// rounded operation on every IEEE host (x86-64 and aarch64 alike).
 //
 // Transcendental functions: GLSL leaves exp/pow/sin/cos precision to the
 // driver, so the oracle defines its own. They are written from the textbook
@@ -20,13 +21,17 @@
 //     s = (m-1)/(m+1), odd series to s^11;
 //   * sin / cos: reduction by pi/2 with a three-part Cody-Waite constant,
 //     Taylor series on |r| <= pi/4 (sin to r^9, cos to r^10), quadrant table;
-//   * pow(x, y) = exp2(y * log2(x)) with GLSL's defined cases.
+//   * pow(x, y): binary powering for integer y in 1..1024 (what GPU compilers
+//     emit for pow(x, 2.0) and the like), else exp2(y * log2(x)), with
+//     GLSL's defined cases.
 // Worst-case errors are a few ulp; tests/test_oracle_math.py checks them
 // against numpy float64.
 #pragma once
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+
+using std::fmaf;
 
 namespace vpto {
 
@@ -59,14 +64,14 @@ static inline float dm_exp(float x) {
     int k = (int)kf;
     float r = (x - kf * 0.693145751953125f) - kf * 1.428606765330187e-06f;
     float p = 1.0f / 40320.0f;
-    p = p * r + 1.0f / 5040.0f;
-    p = p * r + 1.0f / 720.0f;
-    p = p * r + 1.0f / 120.0f;
-    p = p * r + 1.0f / 24.0f;
-    p = p * r + 1.0f / 6.0f;
-    p = p * r + 0.5f;
-    p = p * r + 1.0f;
-    p = p * r + 1.0f;
+    p = fmaf(p, r, 1.0f / 5040.0f);
+    p = fmaf(p, r, 1.0f / 720.0f);
+    p = fmaf(p, r, 1.0f / 120.0f);
+    p = fmaf(p, r, 1.0f / 24.0f);
+    p = fmaf(p, r, 1.0f / 6.0f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
     return scale2(p, k);
 }
 
@@ -78,14 +83,14 @@ static inline float dm_exp2(float x) {
     int k = (int)kf;
     float r = (x - kf) * 0.693147182464599609f;
     float p = 1.0f / 40320.0f;
-    p = p * r + 1.0f / 5040.0f;
-    p = p * r + 1.0f / 720.0f;
-    p = p * r + 1.0f / 120.0f;
-    p = p * r + 1.0f / 24.0f;
-    p = p * r + 1.0f / 6.0f;
-    p = p * r + 0.5f;
-    p = p * r + 1.0f;
-    p = p * r + 1.0f;
+    p = fmaf(p, r, 1.0f / 5040.0f);
+    p = fmaf(p, r, 1.0f / 720.0f);
+    p = fmaf(p, r, 1.0f / 120.0f);
+    p = fmaf(p, r, 1.0f / 24.0f);
+    p = fmaf(p, r, 1.0f / 6.0f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
     return scale2(p, k);
 }
 
@@ -107,41 +112,54 @@ static inline float dm_log2(float x) {
     float s = (m - 1.0f) / (m + 1.0f);
     float s2 = s * s;
     float p = 1.0f / 11.0f;
-    p = p * s2 + 1.0f / 9.0f;
-    p = p * s2 + 1.0f / 7.0f;
-    p = p * s2 + 1.0f / 5.0f;
-    p = p * s2 + 1.0f / 3.0f;
-    p = p * s2 + 1.0f;
+    p = fmaf(p, s2, 1.0f / 9.0f);
+    p = fmaf(p, s2, 1.0f / 7.0f);
+    p = fmaf(p, s2, 1.0f / 5.0f);
+    p = fmaf(p, s2, 1.0f / 3.0f);
+    p = fmaf(p, s2, 1.0f);
     float ln_m = 2.0f * (s * p);
     return (float)e + ln_m * 1.44269502162933350f;
 }
 
-// GLSL pow: undefined for x < 0 (NaN here) and for x == 0, y <= 0.
+// GLSL pow: undefined for x < 0 (NaN here) and for x == 0, y <= 0. Integer
+// exponents 1..1024 use binary powering (square-and-multiply from the lowest
+// bit), the rest exp2(y * log2(x)).
 static inline float dm_pow(float x, float y) {
     if (y == 0.0f) return 1.0f;
     if (x == 1.0f) return 1.0f;
     if (x == 0.0f) return y > 0.0f ? 0.0f : INFINITY;
     if (x < 0.0f || x != x || y != y) return NAN;
+    if (y >= 1.0f && y <= 1024.0f && y == std::floor(y)) {
+        int n = (int)y;
+        float r = 1.0f, b = x;
+        for (;;) {
+            if (n & 1) r = r * b;
+            n >>= 1;
+            if (!n) break;
+            b = b * b;
+        }
+        return r;
+    }
     return dm_exp2(y * dm_log2(x));
 }
 
 static inline float sin_poly(float r) {
     float r2 = r * r;
     float p = 1.0f / 362880.0f;
-    p = p * r2 - 1.0f / 5040.0f;
-    p = p * r2 + 1.0f / 120.0f;
-    p = p * r2 - 1.0f / 6.0f;
-    return r + (r * r2) * p;
+    p = fmaf(p, r2, -(1.0f / 5040.0f));
+    p = fmaf(p, r2, 1.0f / 120.0f);
+    p = fmaf(p, r2, -(1.0f / 6.0f));
+    return fmaf(r * r2, p, r);
 }
 
 static inline float cos_poly(float r) {
     float r2 = r * r;
     float p = -1.0f / 3628800.0f;
-    p = p * r2 + 1.0f / 40320.0f;
-    p = p * r2 - 1.0f / 720.0f;
-    p = p * r2 + 1.0f / 24.0f;
-    p = p * r2 - 0.5f;
-    return 1.0f + r2 * p;
+    p = fmaf(p, r2, 1.0f / 40320.0f);
+    p = fmaf(p, r2, -(1.0f / 720.0f));
+    p = fmaf(p, r2, 1.0f / 24.0f);
+    p = fmaf(p, r2, -(0.5f));
+    return fmaf(r2, p, 1.0f);
 }
 
 static inline float reduce_pio2(float x, int* q) {
@@ -200,8 +218,9 @@ static inline v3 cross(v3 a, v3 b) {
     return v3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 static inline float length(v3 a) { return std::sqrt(dot(a, a)); }
-// GLSL normalize(x) = x / length(x)
-static inline v3 normalize(v3 a) { return divs(a, length(a)); }
+// GLSL normalize(x): x scaled by 1/length(x) (one division, as GPU compilers
+// emit it), every operation IEEE-rounded.
+static inline v3 normalize(v3 a) { return muls(a, 1.0f / length(a)); }
 static inline v3 vmax(v3 a, float s) { return v3{fmaxg(a.x, s), fmaxg(a.y, s), fmaxg(a.z, s)}; }
 static inline v3 vclamp(v3 a, float lo, float hi) {
     return v3{clampf(a.x, lo, hi), clampf(a.y, lo, hi), clampf(a.z, lo, hi)};

@@ -14,7 +14,7 @@
 //     the R8 face and block planes are nearest-filtered
 //     (Core/Pipeline.cpp:1094);
 //   * int(NaN) = 0 and out-of-range conversions saturate (omath.h f2i);
-//   * normalize(v) = v / sqrt(dot(v, v)), dot sums left to right;
+//   * normalize(v) = v * (1 / sqrt(dot(v, v))), dot sums left to right;
 //   * transcendental functions come from omath.h.
 // Documented substitutions (the reference's versions need textures):
 //   * block table: flat albedo RGB8, roughness u8, metalness u8, emissive flag;

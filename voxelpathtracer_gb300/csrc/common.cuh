@@ -83,6 +83,84 @@ __device__ __forceinline__ int wrapi(int i, int n) {
     return r < 0 ? r + n : r;
 }
 
+// Vector loads of 4 / 2 interleaved channels (planes are cudaMalloc'd, so a
+// pixel's channels are 16 / 8 byte aligned in fp32 and 8 / 4 in fp16).
+__device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ float4 ld4(const __half* p) {
+    uint2 u = __ldg(reinterpret_cast<const uint2*>(p));
+    __half2 a = *reinterpret_cast<__half2*>(&u.x), b = *reinterpret_cast<__half2*>(&u.y);
+    float2 fa = __half22float2(a), fb = __half22float2(b);
+    return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+__device__ __forceinline__ float2 ld2(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
+__device__ __forceinline__ float2 ld2(const __half* p) {
+    unsigned u = __ldg(reinterpret_cast<const unsigned*>(p));
+    return __half22float2(*reinterpret_cast<__half2*>(&u));
+}
+__device__ __forceinline__ void st4(float* p, float a, float b, float c, float d) {
+    *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void st4(__half* p, float a, float b, float c, float d) {
+    __half2 x = __floats2half2_rn(a, b), y = __floats2half2_rn(c, d);
+    uint2 u;
+    u.x = *reinterpret_cast<unsigned*>(&x);
+    u.y = *reinterpret_cast<unsigned*>(&y);
+    *reinterpret_cast<uint2*>(p) = u;
+}
+__device__ __forceinline__ void st2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
+__device__ __forceinline__ void st2(__half* p, float a, float b) {
+    __half2 x = __floats2half2_rn(a, b);
+    *reinterpret_cast<unsigned*>(p) = *reinterpret_cast<unsigned*>(&x);
+}
+
+// Bilinear footprint of texture() with GL_LINEAR + GL_REPEAT at uv on a W x H
+// plane: texel offsets and fp32 weights, shared by every plane sampled there.
+struct Bilin {
+    int o00, o10, o01, o11;   // pixel indices
+    float ax, ay, bx, by;     // weights: bx = 1 - ax, by = 1 - ay
+};
+__device__ __forceinline__ Bilin bilin(v2 uv, int W, int H) {
+    float x = uv.x * (float)W - 0.5f;
+    float y = uv.y * (float)H - 0.5f;
+    float x0 = floorf(x), y0 = floorf(y);
+    Bilin b;
+    b.ax = x - x0;
+    b.ay = y - y0;
+    b.bx = 1.0f - b.ax;
+    b.by = 1.0f - b.ay;
+    int i0 = wrapi(f2i(x0), W), j0 = wrapi(f2i(y0), H);
+    int i1 = i0 + 1 == W ? 0 : i0 + 1;
+    int j1 = j0 + 1 == H ? 0 : j0 + 1;
+    b.o00 = j0 * W + i0;
+    b.o10 = j0 * W + i1;
+    b.o01 = j1 * W + i0;
+    b.o11 = j1 * W + i1;
+    return b;
+}
+// (v00*(1-ax) + v10*ax)*(1-ay) + (v01*(1-ax) + v11*ax)*ay, per channel
+__device__ __forceinline__ float blend(const Bilin& b, float v00, float v10, float v01, float v11) {
+    float lo = v00 * b.bx + v10 * b.ax;
+    float hi = v01 * b.bx + v11 * b.ax;
+    return lo * b.by + hi * b.ay;
+}
+template <typename S>
+__device__ __forceinline__ float bl1(const S* p, const Bilin& b) {
+    return blend(b, ld(p + b.o00), ld(p + b.o10), ld(p + b.o01), ld(p + b.o11));
+}
+template <typename S>
+__device__ __forceinline__ float2 bl2(const S* p, const Bilin& b) {
+    float2 a = ld2(p + 2 * (size_t)b.o00), c = ld2(p + 2 * (size_t)b.o10);
+    float2 d = ld2(p + 2 * (size_t)b.o01), e = ld2(p + 2 * (size_t)b.o11);
+    return make_float2(blend(b, a.x, c.x, d.x, e.x), blend(b, a.y, c.y, d.y, e.y));
+}
+template <typename S>
+__device__ __forceinline__ float4 bl4(const S* p, const Bilin& b) {
+    float4 a = ld4(p + 4 * (size_t)b.o00), c = ld4(p + 4 * (size_t)b.o10);
+    float4 d = ld4(p + 4 * (size_t)b.o01), e = ld4(p + 4 * (size_t)b.o11);
+    return make_float4(blend(b, a.x, c.x, d.x, e.x), blend(b, a.y, c.y, d.y, e.y), blend(b, a.z, c.z, d.z, e.z),
+                       blend(b, a.w, c.w, d.w, e.w));
+}
+
 // A W x H plane with C interleaved channels of storage type S.
 template <typename S, int C>
 struct Plane {

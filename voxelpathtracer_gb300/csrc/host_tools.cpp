@@ -163,7 +163,7 @@ vpt_status vpt_camera_from_pose(vpt_camera* out, const float position[3], float 
     // glm::lookAt (right-handed)
     double s[3] = {f[1] * up[2] - f[2] * up[1], f[2] * up[0] - f[0] * up[2], f[0] * up[1] - f[1] * up[0]};
     double sl = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
-    if (sl == 0.0) return VPT_ERR_INVALID_ARG;   // looking straight up or down
+    if (sl < 1e-9) return VPT_ERR_INVALID_ARG;   // looking straight up or down
     for (double& v : s) v /= sl;
     double u[3] = {s[1] * f[2] - s[2] * f[1], s[2] * f[0] - s[0] * f[2], s[0] * f[1] - s[1] * f[0]};
     double view[16];

@@ -1,9 +1,13 @@
 // SVGF denoiser kernels: pre-temporal 3x3 spatial pass, temporal
 // reprojection/accumulation, variance estimate and the a-trous iterations
-// (Core/Pipeline.cpp:2284-2615). One thread per pixel; neighbourhood taps at
-// integer offsets are direct fetches (what texture() returns at a texel
-// centre), taps at fractional coordinates are fp32 bilinear with REPEAT wrap.
-// Planes are bandwidth-bound streams read through the L1/L2 caches.
+// (Core/Pipeline.cpp:2284-2615). One thread per pixel, 32x8 blocks so a warp
+// reads 32 consecutive pixels of a row.
+//
+// Taps at integer offsets are direct fetches (what texture() returns at a
+// texel centre); taps at fractional coordinates are fp32 bilinear with REPEAT
+// wrap, the footprint computed once per tap and shared by every plane read
+// there. Multi-channel planes are read with one vector load per texel. The
+// kernels are bound by L1 load throughput and the per-tap weight arithmetic.
 #include "kernels.cuh"
 
 namespace vpt {
@@ -24,58 +28,64 @@ __global__ void __launch_bounds__(256) k_spatial_initial(CamView cam, int W, int
     int i, j;
     if (!pixel_of(W, H, &i, &j)) return;
     const Plane<S, 1> T{t, W, H};
-    const Plane<S, 4> SH{sh, W, H};
-    const Plane<S, 2> CC{cocg, W, H}, AO{aosky, W, H};
-    const Plane8 F{face, W, H};
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
     const float aw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
-    size_t px = (size_t)j * W + i;
-    v2 uv = texcoord(i, j, W, H);
-    v4 bp = position_fetch(cam, T, i, j, uv);
-    v3 bn = normal_from_id(F.at_in(i, j), 1.0f);
-    float bsh[4], bcc[2], bao[2];
-    for (int c = 0; c < 4; c++) bsh[c] = SH.at_in(i, j, c);
-    for (int c = 0; c < 2; c++) { bcc[c] = CC.at_in(i, j, c); bao[c] = AO.at_in(i, j, c); }
-    float bl = sh_to_y(bsh);
-    float butil = ld(luma + px);
-    float tsh[4] = {bsh[0], bsh[1], bsh[2], bsh[3]}, tcc[2] = {bcc[0], bcc[1]}, tao[2] = {bao[0], bao[1]};
+    const size_t px = (size_t)j * W + i;
+    const v2 uv = texcoord(i, j, W, H);
+    const v4 bp = position_fetch(cam, T, i, j, uv);
+    const v3 bn = normal_from_id(__ldg(face + px), 1.0f);
+    const float4 bsh = ld4(sh + 4 * px);
+    const float2 bcc = ld2(cocg + 2 * px), bao = ld2(aosky + 2 * px);
+    float bshv[4] = {bsh.x, bsh.y, bsh.z, bsh.w};
+    const float bl = sh_to_y(bshv);
+    const float butil = ld(luma + px);
+    float tsh[4] = {bsh.x, bsh.y, bsh.z, bsh.w}, tcc[2] = {bcc.x, bcc.y}, tao[2] = {bao.x, bao.y};
     float tw = 1.0f, taow = 1.0f;
     const float phi = 4.0f;
+#pragma unroll
     for (int x = -1; x <= 1; x++) {
+#pragma unroll
         for (int y = -1; y <= 1; y++) {
             if (x == 0 && y == 0) continue;
-            int si = i + x, sj = j + y;
+            const int si = i + x, sj = j + y;
             if (si < 0 || si >= W || sj < 0 || sj >= H) continue;
+            const size_t sp_ = (size_t)sj * W + si;
             v2 sc = mk2(uv.x + (float)x * texel_x, uv.y + (float)y * texel_y);
             v4 sp = position_fetch(cam, T, si, sj, sc);
             v3 pd = mk3(fabsf(sp.x - bp.x), fabsf(sp.y - bp.y), fabsf(sp.z - bp.z));
             float dist_sqr = dot(pd, pd);
             if (dist_sqr < 1.0f) {
-                float ssh[4], scc[2];
-                for (int c = 0; c < 4; c++) ssh[c] = SH.at_in(si, sj, c);
-                for (int c = 0; c < 2; c++) scc[c] = CC.at_in(si, sj, c);
-                v3 sn = normal_from_id(F.at_in(si, sj), 1.0f);
+                float4 s4 = ld4(sh + 4 * sp_);
+                float2 s2 = ld2(cocg + 2 * sp_);
+                float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
+                v3 sn = normal_from_id(__ldg(face + sp_), 1.0f);
                 float sl = sh_to_y(ssh);
                 float nw = dpow(fmaxf(dot(bn, sn), 0.0f), 16.0f);
                 float lw = fabsf(sl - bl) / phi;
                 float wgt = dexp(-lw - nw);
                 wgt = fmaxf(wgt, 0.01f);
-                wgt = (aw[abs(x)] * aw[abs(y)]) * wgt;
+                wgt = (aw[x < 0 ? -x : x] * aw[y < 0 ? -y : y]) * wgt;
                 wgt = fmaxf(wgt, 0.01f);
                 wgt = clampf(wgt, 0.0f, 1.0f);
-                for (int c = 0; c < 4; c++) tsh[c] += ssh[c] * wgt;
-                for (int c = 0; c < 2; c++) tcc[c] += scc[c] * wgt;
+                tsh[0] += ssh[0] * wgt;
+                tsh[1] += ssh[1] * wgt;
+                tsh[2] += ssh[2] * wgt;
+                tsh[3] += ssh[3] * wgt;
+                tcc[0] += s2.x * wgt;
+                tcc[1] += s2.y * wgt;
                 tw += wgt;
-                for (int c = 0; c < 2; c++) tao[c] += AO.at_in(si, sj, c) * wgt;
+                float2 a2 = ld2(aosky + 2 * sp_);
+                tao[0] += a2.x * wgt;
+                tao[1] += a2.y * wgt;
                 taow += wgt;
             }
         }
     }
     tw = fmaxf(tw, 0.01f);
-    for (int c = 0; c < 4; c++) st(o_sh + px * 4 + c, tsh[c] / tw);
-    for (int c = 0; c < 2; c++) st(o_cocg + px * 2 + c, tcc[c] / tw);
-    float awt = fmaxf(taow, 0.01f);
-    for (int c = 0; c < 2; c++) st(o_aosky + px * 2 + c, tao[c] / awt);
+    st4(o_sh + 4 * px, tsh[0] / tw, tsh[1] / tw, tsh[2] / tw, tsh[3] / tw);
+    st2(o_cocg + 2 * px, tcc[0] / tw, tcc[1] / tw);
+    const float awt = fmaxf(taow, 0.01f);
+    st2(o_aosky + 2 * px, tao[0] / awt, tao[1] / awt);
     st(o_luma + px, butil);
 }
 
@@ -89,28 +99,25 @@ __global__ void __launch_bounds__(256) k_temporal(CamView cam, int W, int H, Tem
                                                   S* o_sh, S* o_cocg, S* o_util, S* o_aosky) {
     int i, j;
     if (!pixel_of(W, H, &i, &j)) return;
-    const Plane<S, 1> T{t, W, H}, PT{prev_t, W, H};
-    const Plane8 F{face, W, H}, B{block, W, H}, PF{prev_face, W, H}, PB{prev_block, W, H};
-    const Plane<S, 4> PSH{p_sh, W, H}, PU{p_util, W, H};
-    const Plane<S, 2> PCC{p_cocg, W, H}, PAO{p_aosky, W, H};
+    const Plane<S, 1> T{t, W, H};
+    const Plane8 PF{prev_face, W, H}, PB{prev_block, W, H};
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
     const float weights[5] = {3.0f / 32.0f, 3.0f / 32.0f, 9.0f / 64.0f, 3.0f / 32.0f, 3.0f / 32.0f};
     const int offx[5] = {1, 0, 0, -1, 0};
     const int offy[5] = {0, 1, 0, 0, -1};
-    size_t px = (size_t)j * W + i;
-    v2 uv = texcoord(i, j, W, H);
-    v4 bp = position_fetch(cam, T, i, j, uv);
-    v3 bn = normal_from_id(F.at_in(i, j), 1.0f);
-    float bsh[4], bcc[2], bao[2];
-    for (int c = 0; c < 4; c++) bsh[c] = ld(c_sh + px * 4 + c);
-    for (int c = 0; c < 2; c++) { bcc[c] = ld(c_cocg + px * 2 + c); bao[c] = ld(c_aosky + px * 2 + c); }
-    v4 pr = mat_mul4(a.prev_view_proj, bp.x, bp.y, bp.z, 1.0f);
-    v2 rc = mk2((pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f);
-    float base_lum = ld(c_luma + px);
-    int base_block = min(max((int)B.at_in(i, j), 0), 127);
+    const size_t px = (size_t)j * W + i;
+    const v2 uv = texcoord(i, j, W, H);
+    const v4 bp = position_fetch(cam, T, i, j, uv);
+    const v3 bn = normal_from_id(__ldg(face + px), 1.0f);
+    const float4 bsh = ld4(c_sh + 4 * px);
+    const float2 bcc = ld2(c_cocg + 2 * px), bao = ld2(c_aosky + 2 * px);
+    const v4 pr = mat_mul4(a.prev_view_proj, bp.x, bp.y, bp.z, 1.0f);
+    const v2 rc = mk2((pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f);
+    const float base_lum = ld(c_luma + px);
+    const int base_block = min(max((int)__ldg(block + px), 0), 127);
     float tol = 0.75f;
     bool do_block = true, do_normal = true;
-    float dp = length(sub(mk3(bp.x, bp.y, bp.z), ray_origin(cam)));
+    const float dp = length(sub(mk3(bp.x, bp.y, bp.z), ray_origin(cam)));
     if (dp < 4.0f) { tol = 0.3f; }
     else if (dp < 6.0f) { tol = 0.65f; }
     else if (dp < 8.0f) { tol = 0.85f; }
@@ -124,126 +131,141 @@ __global__ void __launch_bounds__(256) k_temporal(CamView cam, int W, int H, Tem
     float tw = 0.0f, ssh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, scc[2] = {0.0f, 0.0f}, sao[2] = {0.0f, 0.0f};
     float slum = 0.0f, sspp = 0.0f, smom = 0.0f;
     int successful = 0;
+#pragma unroll
     for (int k = 0; k < 5; k++) {
+        // Jitter is ivec2((noise - 0.5) * 1.0) == 0 for every pixel (:165)
         v2 sc = mk2(rc.x + ((float)offx[k] + 0.0f) * texel_x, rc.y + ((float)offy[k] + 0.0f) * texel_y);
         const float b = 0.0035f;
         if (!(sc.x < 1.0f - b && sc.x > b && sc.y < 1.0f - b && sc.y > b)) continue;
-        v4 pp = position_linear(cam, PT, sc);
+        const Bilin fp = bilin(sc, W, H);
+        const float pt = bl1(prev_t, fp);
+        const v3 pdir = normalize(ray_dir_at(cam, sc));
+        const v3 pp = add(ray_origin(cam), muls(pdir, pt));
         v3 pn = normal_from_id(PF.nearest(sc), 1.0f);
         v3 pd = mk3(fabsf(bp.x - pp.x), fabsf(bp.y - pp.y), fabsf(bp.z - pp.z));
         float perr = dot(pd, pd);
         float cw = weights[k];
         int sblock = min(max(PB.nearest(sc), 0), 127);
         bool valid = false;
-        if (perr < tol && ((pp.w < 0.0f) == (bp.w < 0.0f))) {
+        if (perr < tol && ((pt < 0.0f) == (bp.w < 0.0f))) {
             valid = true;
             if (do_normal && !(pn.x == bn.x && pn.y == bn.y && pn.z == bn.z)) valid = false;
             if (do_block && base_block != sblock) valid = false;
         }
         if (valid) {
-            float pu[4], psh[4], pcc[2], pao[2];
-            PU.linear(sc, pu);
-            PSH.linear(sc, psh);
-            PCC.linear(sc, pcc);
-            PAO.linear(sc, pao);
-            for (int c = 0; c < 4; c++) ssh[c] += psh[c] * cw;
-            for (int c = 0; c < 2; c++) scc[c] += pcc[c] * cw;
-            sspp += pu[0] * cw;
-            smom += pu[1] * cw;
-            slum += pu[2] * cw;
-            for (int c = 0; c < 2; c++) sao[c] += pao[c] * cw;
+            float4 pu = bl4(p_util, fp), psh = bl4(p_sh, fp);
+            float2 pcc = bl2(p_cocg, fp), pao = bl2(p_aosky, fp);
+            ssh[0] += psh.x * cw;
+            ssh[1] += psh.y * cw;
+            ssh[2] += psh.z * cw;
+            ssh[3] += psh.w * cw;
+            scc[0] += pcc.x * cw;
+            scc[1] += pcc.y * cw;
+            sspp += pu.x * cw;
+            smom += pu.y * cw;
+            slum += pu.z * cw;
+            sao[0] += pao.x * cw;
+            sao[1] += pao.y * cw;
             tw += cw;
             successful++;
         }
     }
     if (tw > 0.001f) {
         for (int c = 0; c < 4; c++) ssh[c] /= tw;
-        for (int c = 0; c < 2; c++) scc[c] /= tw;
+        scc[0] /= tw;
+        scc[1] /= tw;
         smom /= tw;
         sspp /= tw;
         slum /= tw;
-        for (int c = 0; c < 2; c++) sao[c] /= tw;
+        sao[0] /= tw;
+        sao[1] /= tw;
     } else {
         successful = 0;
     }
-    float inc = a.be_useful ? 1.0f : 0.0f;
+    const float inc = a.be_useful ? 1.0f : 0.0f;
     float spp_inc = sspp + inc;
     if (successful <= 0) spp_inc = 0.01f;
-    float blend = fmaxf(1.0f / spp_inc, 0.05f);
-    float mfac = fmaxf(1.0f / spp_inc, 0.05f);
-    if (!a.be_useful) { blend = 0.99f; sspp = 0.0f; }
+    float blend_f = fmaxf(1.0f / spp_inc, 0.05f);
+    const float mfac = fmaxf(1.0f / spp_inc, 0.05f);
+    if (!a.be_useful) { blend_f = 0.99f; sspp = 0.0f; }
     float util_spp = spp_inc;
     if (successful <= 0) util_spp = 0.0f;
-    float util_mom = (1.0f - mfac) * smom + mfac * (base_lum * base_lum);
-    float store_luma = mixf(slum, base_lum, blend);
+    const float util_mom = (1.0f - mfac) * smom + mfac * (base_lum * base_lum);
+    const float store_luma = mixf(slum, base_lum, blend_f);
     float osh[4], occ[2], oao[2];
-    for (int c = 0; c < 4; c++) osh[c] = mixf(ssh[c], bsh[c], blend);
-    for (int c = 0; c < 2; c++) { occ[c] = mixf(scc[c], bcc[c], blend); oao[c] = mixf(sao[c], bao[c], blend); }
+    const float bshv[4] = {bsh.x, bsh.y, bsh.z, bsh.w};
+    for (int c = 0; c < 4; c++) osh[c] = mixf(ssh[c], bshv[c], blend_f);
+    occ[0] = mixf(scc[0], bcc.x, blend_f);
+    occ[1] = mixf(scc[1], bcc.y, blend_f);
+    oao[0] = mixf(sao[0], bao.x, blend_f);
+    oao[1] = mixf(sao[1], bao.y, blend_f);
     if (successful <= 0) {
-        for (int c = 0; c < 4; c++) osh[c] = bsh[c];
-        for (int c = 0; c < 2; c++) { occ[c] = bcc[c]; oao[c] = bao[c]; }
+        for (int c = 0; c < 4; c++) osh[c] = bshv[c];
+        occ[0] = bcc.x; occ[1] = bcc.y;
+        oao[0] = bao.x; oao[1] = bao.y;
     }
-    for (int c = 0; c < 4; c++) st(o_sh + px * 4 + c, clampf(osh[c], -100.0f, 100.0f));
-    for (int c = 0; c < 2; c++) st(o_cocg + px * 2 + c, clampf(occ[c], -10.0f, 100.0f));
-    for (int c = 0; c < 2; c++) st(o_aosky + px * 2 + c, clampf(oao[c], 0.0f, 1.0f));
-    st(o_util + px * 4 + 0, clampf(util_spp, -150.0f, 150.0f));
-    st(o_util + px * 4 + 1, clampf(util_mom, -150.0f, 150.0f));
-    st(o_util + px * 4 + 2, clampf(store_luma, -150.0f, 150.0f));
-    st(o_util + px * 4 + 3, 0.0f);
+    st4(o_sh + 4 * px, clampf(osh[0], -100.0f, 100.0f), clampf(osh[1], -100.0f, 100.0f),
+        clampf(osh[2], -100.0f, 100.0f), clampf(osh[3], -100.0f, 100.0f));
+    st2(o_cocg + 2 * px, clampf(occ[0], -10.0f, 100.0f), clampf(occ[1], -10.0f, 100.0f));
+    st2(o_aosky + 2 * px, clampf(oao[0], 0.0f, 1.0f), clampf(oao[1], 0.0f, 1.0f));
+    st4(o_util + 4 * px, clampf(util_spp, -150.0f, 150.0f), clampf(util_mom, -150.0f, 150.0f),
+        clampf(store_luma, -150.0f, 150.0f), 0.0f);
 }
 
 // SVGF/VarianceEstimate.glsl main (:73-193) with DO_SPATIAL and
-// AGGRESSIVE_DISOCCLUSION_HANDLING on.
+// AGGRESSIVE_DISOCCLUSION_HANDLING on. Only the hit distance of the taps'
+// reconstructed positions is used (the depth weight), so no ray is rebuilt.
 template <typename S>
-__global__ void __launch_bounds__(256) k_variance(CamView cam, int W, int H, const S* t, const uint8_t* face,
-                                                  const S* i_sh, const S* i_cocg, const S* i_util, S* o_sh,
-                                                  S* o_cocg, S* o_var) {
+__global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, const uint8_t* face, const S* i_sh,
+                                                  const S* i_cocg, const S* i_util, S* o_sh, S* o_cocg, S* o_var) {
     int i, j;
     if (!pixel_of(W, H, &i, &j)) return;
-    const Plane<S, 1> T{t, W, H};
-    const Plane<S, 4> SH{i_sh, W, H}, U{i_util, W, H};
-    const Plane<S, 2> CC{i_cocg, W, H};
-    const Plane8 F{face, W, H};
-    const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
     const float thresh = 4.0f + 4.0f + 4.0f;
-    size_t px = (size_t)j * W + i;
-    v2 uv = texcoord(i, j, W, H);
-    float bsh[4], bcc[2];
-    for (int c = 0; c < 4; c++) bsh[c] = SH.at_in(i, j, c);
-    for (int c = 0; c < 2; c++) bcc[c] = CC.at_in(i, j, c);
-    float bl = sh_to_y(bsh);
-    float acc = U.at_in(i, j, 0);
-    float bm = U.at_in(i, j, 1);
+    const size_t px = (size_t)j * W + i;
+    const float4 bsh = ld4(i_sh + 4 * px);
+    const float2 bcc = ld2(i_cocg + 2 * px);
+    const float bshv[4] = {bsh.x, bsh.y, bsh.z, bsh.w};
+    const float bl = sh_to_y(bshv);
+    const float4 bu = ld4(i_util + 4 * px);
+    const float acc = bu.x;
+    const float bm = bu.y;
     float osh[4], occ[2], var;
     if (acc < thresh) {
-        v4 bp = position_fetch(cam, T, i, j, uv);
-        v3 bn = normal_from_id(F.at_in(i, j), 1.0f);
+        const float bd = ld(t + px);
+        const v3 bn = normal_from_id(__ldg(face + px), 1.0f);
         const float phi = 5.0f;
         float tw = 0.0f, tm = 0.0f, tl = 0.0f, tw2 = 0.0f;
         float tsh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, tcc[2] = {0.0f, 0.0f};
         for (int x = -4; x <= 4; x++) {
+            const int si = i + x;
+            if (si < 0 || si >= W) continue;
+#pragma unroll 3
             for (int y = -4; y <= 4; y++) {
-                int si = i + x, sj = j + y;
-                if (si < 0 || si >= W || sj < 0 || sj >= H) continue;
-                v2 sc = mk2(uv.x + (float)x * texel_x, uv.y + (float)y * texel_y);
-                v4 sp = position_fetch(cam, T, si, sj, sc);
-                v3 sn = normal_from_id(F.at_in(si, sj), 1.0f);
-                float smom = U.at_in(si, sj, 1);
-                float ssh[4], scc[2];
-                for (int c = 0; c < 4; c++) ssh[c] = SH.at_in(si, sj, c);
-                for (int c = 0; c < 2; c++) scc[c] = CC.at_in(si, sj, c);
-                float sl = sh_to_y(ssh);
-                float nw = dpow(fmaxf(dot(bn, sn), 0.0f), 16.0f);
-                float dw = dpow(dexp(-fabsf(sp.w - bp.w)), 2.0f);
-                float lw = fabsf(sl - bl) / phi;
+                const int sj = j + y;
+                if (sj < 0 || sj >= H) continue;
+                const size_t sp_ = (size_t)sj * W + si;
+                const float sd = ld(t + sp_);
+                const v3 sn = normal_from_id(__ldg(face + sp_), 1.0f);
+                const float smom = ld(i_util + 4 * sp_ + 1);
+                const float4 s4 = ld4(i_sh + 4 * sp_);
+                const float2 s2 = ld2(i_cocg + 2 * sp_);
+                const float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
+                const float sl = sh_to_y(ssh);
+                const float nw = dpow(fmaxf(dot(bn, sn), 0.0f), 16.0f);
+                const float dw = dpow(dexp(-fabsf(sd - bd)), 2.0f);
+                const float lw = fabsf(sl - bl) / phi;
                 float wgt = (dexp(-lw) * nw) * dw;
                 float wgt2 = wgt;
                 wgt = fmaxf(wgt, 0.000000015f);
                 wgt2 = fmaxf(wgt2, 0.0000000015f);
                 tw += wgt;
                 tm += smom * wgt2;
-                for (int c = 0; c < 4; c++) tsh[c] += ssh[c] * wgt;
-                for (int c = 0; c < 2; c++) tcc[c] += scc[c] * wgt;
+                tsh[0] += ssh[0] * wgt;
+                tsh[1] += ssh[1] * wgt;
+                tsh[2] += ssh[2] * wgt;
+                tsh[3] += ssh[3] * wgt;
+                tcc[0] += s2.x * wgt;
+                tcc[1] += s2.y * wgt;
                 tl += sl * wgt2;
                 tw2 += wgt2;
             }
@@ -251,36 +273,39 @@ __global__ void __launch_bounds__(256) k_variance(CamView cam, int W, int H, con
         if (tw > 0.0f) {
             tm /= tw2;
             tl /= tw2;
-            for (int c = 0; c < 2; c++) tcc[c] /= tw;
+            tcc[0] /= tw;
+            tcc[1] /= tw;
             for (int c = 0; c < 4; c++) tsh[c] /= tw;
         }
         for (int c = 0; c < 4; c++) osh[c] = tsh[c];
-        for (int c = 0; c < 2; c++) occ[c] = tcc[c];
-        float al = tl * tl;
+        occ[0] = tcc[0];
+        occ[1] = tcc[1];
+        const float al = tl * tl;
         var = tm - al;
         var *= 3.0f;
     } else {
-        for (int c = 0; c < 4; c++) osh[c] = bsh[c];
-        for (int c = 0; c < 2; c++) occ[c] = bcc[c];
+        for (int c = 0; c < 4; c++) osh[c] = bshv[c];
+        occ[0] = bcc.x;
+        occ[1] = bcc.y;
         var = bm - bl * bl;
     }
     var *= thresh / acc;
-    for (int c = 0; c < 4; c++) st(o_sh + px * 4 + c, clampf(osh[c], -100.0f, 100.0f));
-    for (int c = 0; c < 2; c++) st(o_cocg + px * 2 + c, clampf(occ[c], -10.0f, 100.0f));
+    st4(o_sh + 4 * px, clampf(osh[0], -100.0f, 100.0f), clampf(osh[1], -100.0f, 100.0f),
+        clampf(osh[2], -100.0f, 100.0f), clampf(osh[3], -100.0f, 100.0f));
+    st2(o_cocg + 2 * px, clampf(occ[0], -10.0f, 100.0f), clampf(occ[1], -10.0f, 100.0f));
     st(o_var + px, clampf(var, -1.0f, 50.0f));
 }
 
 // SVGF/SpatialFilter.glsl main (:175-355), 3x3 taps (u_LargeKernel off).
+// A tap contributes only when (BaseDepth < 0) == (DepthDiff < 0), i.e. when
+// the centre is not sky (DepthDiff = abs(...) >= 0); sky centres keep their
+// own values, so their tap loop is skipped.
 template <typename S>
-__global__ void __launch_bounds__(256) k_atrous(CamView cam, int W, int H, AtrousArgs a, const S* t,
-                                                const uint8_t* face, const S* t_util, const S* i_sh,
-                                                const S* i_cocg, const S* i_var, const S* i_aosky, S* o_sh,
-                                                S* o_cocg, S* o_var, S* o_aosky) {
+__global__ void __launch_bounds__(256) k_atrous(int W, int H, AtrousArgs a, const S* t, const uint8_t* face,
+                                                const S* t_util, const S* i_sh, const S* i_cocg, const S* i_var,
+                                                const S* i_aosky, S* o_sh, S* o_cocg, S* o_var, S* o_aosky) {
     int i, j;
     if (!pixel_of(W, H, &i, &j)) return;
-    const Plane<S, 1> T{t, W, H}, V{i_var, W, H};
-    const Plane<S, 4> SH{i_sh, W, H}, U{t_util, W, H};
-    const Plane<S, 2> CC{i_cocg, W, H}, AO{i_aosky, W, H};
     const Plane8 F{face, W, H};
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
     const float aw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
@@ -288,167 +313,179 @@ __global__ void __launch_bounds__(256) k_atrous(CamView cam, int W, int H, Atrou
     const int step = a.step;
     const bool filter_ao = step <= 4;
     const bool filter_sky = (step <= 6) || filter_ao;
-    size_t px = (size_t)j * W + i;
-    v2 uv = texcoord(i, j, W, H);
-    // GradientNoise (:160-165)
-    float gx = ((float)i + 0.5f) + a.tmod500, gy = ((float)j + 0.5f) + a.tmod500;
-    float noise = fract(52.9829189f * fract(0.06711056f * gx + 0.00583715f * gy));
-    int jit = f2i((noise - 0.5f) * ((float)step * 0.8f));
-    float bd = T.at_in(i, j, 0);
-    v3 bn = normal_from_id(F.at_in(i, j), 1.0f);
-    float bsh[4], bcc[2], bao[2];
-    for (int c = 0; c < 4; c++) bsh[c] = SH.at_in(i, j, c);
-    for (int c = 0; c < 2; c++) { bcc[c] = CC.at_in(i, j, c); bao[c] = AO.at_in(i, j, c); }
-    float bl = sh_to_y(bsh);
+    const size_t px = (size_t)j * W + i;
+    const float bd = ld(t + px);
+    const float4 bsh = ld4(i_sh + 4 * px);
+    const float2 bcc = ld2(i_cocg + 2 * px), bao = ld2(i_aosky + 2 * px);
     // GaussianVariance (:94-129)
     float bvar = 0.0f, vsum = 0.0f, tk = 0.0f;
+#pragma unroll
     for (int x = -1; x <= 1; x++) {
+#pragma unroll
         for (int y = -1; y <= 1; y++) {
-            int si = i + x, sj = j + y;
+            const int si = i + x, sj = j + y;
             if (si < 0 || si >= W || sj < 0 || sj >= H) continue;
-            float kv = gauss[abs(x)] * gauss[abs(y)];
-            float v = V.at_in(si, sj, 0);
+            const float kv = gauss[x < 0 ? -x : x] * gauss[y < 0 ? -y : y];
+            const float v = ld(i_var + (size_t)sj * W + si);
             if (x == 0 && y == 0) bvar = v;
             vsum += v * kv;
             tk += kv;
         }
     }
-    float vest = vsum / fmaxf(tk, 0.01f);
-    float tsh[4] = {bsh[0], bsh[1], bsh[2], bsh[3]}, tcc[2] = {bcc[0], bcc[1]};
-    float tw = 1.0f, tvar = bvar, tao[2] = {bao[0], bao[1]}, taow = 1.0f;
-    float acc_frames = U.at_in(i, j, 0);
-    bool strong = acc_frames <= 8.0f && step <= 8;
-    float curve = 0.0f;
-    if (vest < 0.01f) curve = 128.0f;
-    else if (vest < 0.025f) curve = 112.0f;
-    else if (vest < 0.05f) curve = 96.0f;
-    else if (vest < 0.075f) curve = 84.0f;
-    else if (vest < 0.1f) curve = 70.0f;
-    float tweaked = vest;
-    if (vest < 0.1f) {   // TweakVariance (:167-173)
-        float fe = clampf(vest, 0.0f, 1.0f);
-        float tt = 1.0f - fe;
-        tweaked = fe * dpow(tt, curve + 6.0f);
-    }
-    float phi = sqrtf(fmaxf(0.0f, 0.000001f + tweaked));
-    phi /= a.phi_bias;
-    for (int x = -1; x <= 1; x++) {
-        for (int y = -1; y <= 1; y++) {
-            if (x == 0 && y == 0) continue;
-            float ox = ((float)x * (float)step) * a.add_scale + (float)jit * 0.5f;
-            float oy = ((float)y * (float)step) * a.add_scale + (float)jit * 0.5f;
-            v2 sc = mk2(uv.x + ox * texel_x, uv.y + oy * texel_y);
-            if (!(sc.x > 0.0f && sc.x < 1.0f && sc.y > 0.0f && sc.y < 1.0f)) continue;
-            float sd;
-            T.linear(sc, &sd);
-            float dd = fabsf(sd - bd);
-            v3 sn = normal_from_id(F.nearest(sc), 1.0f);
-            if ((bd < 0.0f) == (dd < 0.0f)) {
-                float ssh[4], scc[2], sv;
-                SH.linear(sc, ssh);
-                CC.linear(sc, scc);
-                float sl = sh_to_y(ssh);
-                V.linear(sc, &sv);
-                float nw = clampf(dpow(fmaxf(dot(bn, sn), 0.0f), 32.0f), 0.001f, 1.0f);
-                float lw = fabsf(sl - bl) / phi;
-                float dw = clampf(dpow(dexp(-fmaxf(dd, 0.00001f)), 2.0f), 0.0001f, 1.0f);
+    float tsh[4] = {bsh.x, bsh.y, bsh.z, bsh.w}, tcc[2] = {bcc.x, bcc.y};
+    float tw = 1.0f, tvar = bvar, tao[2] = {bao.x, bao.y}, taow = 1.0f;
+    if (!(bd < 0.0f)) {
+        const v2 uv = texcoord(i, j, W, H);
+        // GradientNoise (:160-165)
+        const float gx = ((float)i + 0.5f) + a.tmod500, gy = ((float)j + 0.5f) + a.tmod500;
+        const float noise = fract(52.9829189f * fract(0.06711056f * gx + 0.00583715f * gy));
+        const int jit = f2i((noise - 0.5f) * ((float)step * 0.8f));
+        const v3 bn = normal_from_id(__ldg(face + px), 1.0f);
+        const float bshv[4] = {bsh.x, bsh.y, bsh.z, bsh.w};
+        const float bl = sh_to_y(bshv);
+        const float vest = vsum / fmaxf(tk, 0.01f);
+        const float acc_frames = ld(t_util + 4 * px);
+        const bool strong = acc_frames <= 8.0f && step <= 8;
+        float curve = 0.0f;
+        if (vest < 0.01f) curve = 128.0f;
+        else if (vest < 0.025f) curve = 112.0f;
+        else if (vest < 0.05f) curve = 96.0f;
+        else if (vest < 0.075f) curve = 84.0f;
+        else if (vest < 0.1f) curve = 70.0f;
+        float tweaked = vest;
+        if (vest < 0.1f) {   // TweakVariance (:167-173)
+            const float fe = clampf(vest, 0.0f, 1.0f);
+            const float tt = 1.0f - fe;
+            tweaked = fe * dpow(tt, curve + 6.0f);
+        }
+        float phi = sqrtf(fmaxf(0.0f, 0.000001f + tweaked));
+        phi /= a.phi_bias;
+        const float jo = (float)jit * 0.5f;
+#pragma unroll
+        for (int x = -1; x <= 1; x++) {
+#pragma unroll
+            for (int y = -1; y <= 1; y++) {
+                if (x == 0 && y == 0) continue;
+                const float ox = ((float)x * (float)step) * a.add_scale + jo;
+                const float oy = ((float)y * (float)step) * a.add_scale + jo;
+                const v2 sc = mk2(uv.x + ox * texel_x, uv.y + oy * texel_y);
+                if (!(sc.x > 0.0f && sc.x < 1.0f && sc.y > 0.0f && sc.y < 1.0f)) continue;
+                const Bilin fp = bilin(sc, W, H);
+                const float sd = bl1(t, fp);
+                const float dd = fabsf(sd - bd);
+                const v3 sn = normal_from_id(F.nearest(sc), 1.0f);
+                const float4 s4 = bl4(i_sh, fp);
+                const float2 s2 = bl2(i_cocg, fp);
+                const float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
+                const float sl = sh_to_y(ssh);
+                const float sv = bl1(i_var, fp);
+                const float nw = clampf(dpow(fmaxf(dot(bn, sn), 0.0f), 32.0f), 0.001f, 1.0f);
+                const float lw = fabsf(sl - bl) / phi;
+                const float dw = clampf(dpow(dexp(-fmaxf(dd, 0.00001f)), 2.0f), 0.0001f, 1.0f);
                 float wgt = strong ? nw * dw : (dexp(-lw) * nw) * dw;
                 wgt = clampf(wgt, 0.001f, 1.0f);
-                float xw = aw[abs(x)], yw = aw[abs(y)];
+                const float xw = aw[x < 0 ? -x : x], yw = aw[y < 0 ? -y : y];
                 wgt = (xw * yw) * wgt;
                 wgt = fmaxf(wgt, 0.00000001f);
-                for (int c = 0; c < 4; c++) tsh[c] += ssh[c] * wgt;
-                for (int c = 0; c < 2; c++) tcc[c] += scc[c] * wgt;
+                tsh[0] += ssh[0] * wgt;
+                tsh[1] += ssh[1] * wgt;
+                tsh[2] += ssh[2] * wgt;
+                tsh[3] += ssh[3] * wgt;
+                tcc[0] += s2.x * wgt;
+                tcc[1] += s2.y * wgt;
                 tvar += (wgt * wgt) * sv;
                 tw += wgt;
                 if (filter_sky || filter_ao) {
-                    float awt = clampf(((xw * yw) * nw) * dw, 0.000001f, 1.0f);
-                    float sao[2];
-                    AO.linear(sc, sao);
-                    tao[0] += sao[0] * awt;
-                    tao[1] += sao[1] * awt;
+                    const float awt = clampf(((xw * yw) * nw) * dw, 0.000001f, 1.0f);
+                    const float2 sao = bl2(i_aosky, fp);
+                    tao[0] += sao.x * awt;
+                    tao[1] += sao.y * awt;
                     taow += awt;
                 }
             }
         }
     }
     for (int c = 0; c < 4; c++) tsh[c] /= tw;
-    for (int c = 0; c < 2; c++) tcc[c] /= tw;
+    tcc[0] /= tw;
+    tcc[1] /= tw;
     tvar /= (tw * tw);
     tao[0] /= taow;
     tao[1] /= taow;
-    if (!filter_ao) tao[0] = bao[0];
-    for (int c = 0; c < 4; c++) st(o_sh + px * 4 + c, clampf(tsh[c], -100.0f, 100.0f));
-    for (int c = 0; c < 2; c++) st(o_cocg + px * 2 + c, clampf(tcc[c], -10.0f, 100.0f));
+    if (!filter_ao) tao[0] = bao.x;
+    st4(o_sh + 4 * px, clampf(tsh[0], -100.0f, 100.0f), clampf(tsh[1], -100.0f, 100.0f),
+        clampf(tsh[2], -100.0f, 100.0f), clampf(tsh[3], -100.0f, 100.0f));
+    st2(o_cocg + 2 * px, clampf(tcc[0], -10.0f, 100.0f), clampf(tcc[1], -10.0f, 100.0f));
     st(o_var + px, clampf(tvar, -1.0f, 50.0f));
-    st(o_aosky + px * 2 + 0, clampf(tao[0], 0.0f, 1.0f));
-    st(o_aosky + px * 2 + 1, clampf(tao[1], 0.0f, 1.0f));
+    st2(o_aosky + 2 * px, clampf(tao[0], 0.0f, 1.0f), clampf(tao[1], 0.0f, 1.0f));
 }
 
 inline dim3 grid2(int W, int H) { return dim3((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8)); }
 const dim3 kBlock2(32, 8);
 
+template <typename S>
+cudaError_t launch_all_spatial_initial(const CamView& cam, int W, int H, const void* t, const uint8_t* face, GIIn in,
+                                       GIOut out, cudaStream_t s) {
+    k_spatial_initial<S><<<grid2(W, H), kBlock2, 0, s>>>(cam, W, H, (const S*)t, face, (const S*)in.sh,
+                                                         (const S*)in.cocg, (const S*)in.luma, (const S*)in.aosky,
+                                                         (S*)out.sh, (S*)out.cocg, (S*)out.luma, (S*)out.aosky);
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_temporal(const CamView& cam, int W, int H, const TemporalArgs& a, const void* t,
+                            const uint8_t* face, const uint8_t* block, const void* prev_t, const uint8_t* prev_face,
+                            const uint8_t* prev_block, GIIn cur, HistIO prev, HistIO out, cudaStream_t s) {
+    k_temporal<S><<<grid2(W, H), kBlock2, 0, s>>>(
+        cam, W, H, a, (const S*)t, face, block, (const S*)prev_t, prev_face, prev_block, (const S*)cur.sh,
+        (const S*)cur.cocg, (const S*)cur.luma, (const S*)cur.aosky, (const S*)prev.sh, (const S*)prev.cocg,
+        (const S*)prev.util, (const S*)prev.aosky, (S*)out.sh, (S*)out.cocg, (S*)out.util, (S*)out.aosky);
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_variance(int W, int H, const void* t, const uint8_t* face, HistIO in, FiltIO out, cudaStream_t s) {
+    k_variance<S><<<grid2(W, H), kBlock2, 0, s>>>(W, H, (const S*)t, face, (const S*)in.sh, (const S*)in.cocg,
+                                                  (const S*)in.util, (S*)out.sh, (S*)out.cocg, (S*)out.variance);
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_atrous(int W, int H, const AtrousArgs& a, const void* t, const uint8_t* face,
+                          const void* temporal_util, FiltIO in, const void* in_aosky, FiltIO out, cudaStream_t s) {
+    k_atrous<S><<<grid2(W, H), kBlock2, 0, s>>>(W, H, a, (const S*)t, face, (const S*)temporal_util, (const S*)in.sh,
+                                                (const S*)in.cocg, (const S*)in.variance, (const S*)in_aosky,
+                                                (S*)out.sh, (S*)out.cocg, (S*)out.variance, (S*)out.aosky);
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t svgf_spatial_initial(const CamView& cam, int W, int H, int fp16, const void* t, const uint8_t* face,
                                  GIIn in, GIOut out, cudaStream_t s) {
-    if (fp16)
-        k_spatial_initial<__half><<<grid2(W, H), kBlock2, 0, s>>>(
-            cam, W, H, (const __half*)t, face, (const __half*)in.sh, (const __half*)in.cocg, (const __half*)in.luma,
-            (const __half*)in.aosky, (__half*)out.sh, (__half*)out.cocg, (__half*)out.luma, (__half*)out.aosky);
-    else
-        k_spatial_initial<float><<<grid2(W, H), kBlock2, 0, s>>>(
-            cam, W, H, (const float*)t, face, (const float*)in.sh, (const float*)in.cocg, (const float*)in.luma,
-            (const float*)in.aosky, (float*)out.sh, (float*)out.cocg, (float*)out.luma, (float*)out.aosky);
-    return cudaGetLastError();
+    return fp16 ? launch_all_spatial_initial<__half>(cam, W, H, t, face, in, out, s)
+                : launch_all_spatial_initial<float>(cam, W, H, t, face, in, out, s);
 }
 
 cudaError_t svgf_temporal(const CamView& cam, int W, int H, int fp16, const TemporalArgs& a,
                           const void* t, const uint8_t* face, const uint8_t* block,
                           const void* prev_t, const uint8_t* prev_face, const uint8_t* prev_block,
                           GIIn cur, HistIO prev, HistIO out, cudaStream_t s) {
-    if (fp16)
-        k_temporal<__half><<<grid2(W, H), kBlock2, 0, s>>>(
-            cam, W, H, a, (const __half*)t, face, block, (const __half*)prev_t, prev_face, prev_block,
-            (const __half*)cur.sh, (const __half*)cur.cocg, (const __half*)cur.luma, (const __half*)cur.aosky,
-            (const __half*)prev.sh, (const __half*)prev.cocg, (const __half*)prev.util, (const __half*)prev.aosky,
-            (__half*)out.sh, (__half*)out.cocg, (__half*)out.util, (__half*)out.aosky);
-    else
-        k_temporal<float><<<grid2(W, H), kBlock2, 0, s>>>(
-            cam, W, H, a, (const float*)t, face, block, (const float*)prev_t, prev_face, prev_block,
-            (const float*)cur.sh, (const float*)cur.cocg, (const float*)cur.luma, (const float*)cur.aosky,
-            (const float*)prev.sh, (const float*)prev.cocg, (const float*)prev.util, (const float*)prev.aosky,
-            (float*)out.sh, (float*)out.cocg, (float*)out.util, (float*)out.aosky);
-    return cudaGetLastError();
+    return fp16 ? launch_temporal<__half>(cam, W, H, a, t, face, block, prev_t, prev_face, prev_block, cur, prev, out, s)
+                : launch_temporal<float>(cam, W, H, a, t, face, block, prev_t, prev_face, prev_block, cur, prev, out, s);
 }
 
 cudaError_t svgf_variance(const CamView& cam, int W, int H, int fp16, const void* t, const uint8_t* face,
                           HistIO in, FiltIO out, cudaStream_t s) {
-    if (fp16)
-        k_variance<__half><<<grid2(W, H), kBlock2, 0, s>>>(cam, W, H, (const __half*)t, face, (const __half*)in.sh,
-                                                           (const __half*)in.cocg, (const __half*)in.util,
-                                                           (__half*)out.sh, (__half*)out.cocg, (__half*)out.variance);
-    else
-        k_variance<float><<<grid2(W, H), kBlock2, 0, s>>>(cam, W, H, (const float*)t, face, (const float*)in.sh,
-                                                          (const float*)in.cocg, (const float*)in.util,
-                                                          (float*)out.sh, (float*)out.cocg, (float*)out.variance);
-    return cudaGetLastError();
+    (void)cam;
+    return fp16 ? launch_variance<__half>(W, H, t, face, in, out, s) : launch_variance<float>(W, H, t, face, in, out, s);
 }
 
 cudaError_t svgf_atrous(const CamView& cam, int W, int H, int fp16, const AtrousArgs& a,
                         const void* t, const uint8_t* face, const void* temporal_util,
                         FiltIO in, const void* in_aosky, FiltIO out, cudaStream_t s) {
-    if (fp16)
-        k_atrous<__half><<<grid2(W, H), kBlock2, 0, s>>>(
-            cam, W, H, a, (const __half*)t, face, (const __half*)temporal_util, (const __half*)in.sh,
-            (const __half*)in.cocg, (const __half*)in.variance, (const __half*)in_aosky, (__half*)out.sh,
-            (__half*)out.cocg, (__half*)out.variance, (__half*)out.aosky);
-    else
-        k_atrous<float><<<grid2(W, H), kBlock2, 0, s>>>(
-            cam, W, H, a, (const float*)t, face, (const float*)temporal_util, (const float*)in.sh,
-            (const float*)in.cocg, (const float*)in.variance, (const float*)in_aosky, (float*)out.sh,
-            (float*)out.cocg, (float*)out.variance, (float*)out.aosky);
-    return cudaGetLastError();
+    (void)cam;
+    return fp16 ? launch_atrous<__half>(W, H, a, t, face, temporal_util, in, in_aosky, out, s)
+                : launch_atrous<float>(W, H, a, t, face, temporal_util, in, in_aosky, out, s);
 }
 
 }  // namespace vpt

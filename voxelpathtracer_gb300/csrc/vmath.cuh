@@ -2,7 +2,9 @@
 //
 // Every function is a fixed sequence of IEEE-754 binary32 operations. The
 // library is compiled with -fmad=false (device) and -ffp-contract=off (host),
-// with IEEE division and square root, so the same inputs give the same bits
+// with IEEE division and square root; the only fused multiply-adds are the
+// explicit fmaf calls of the polynomial steps below (one correctly rounded
+// operation on both sides). So the same inputs give the same bits
 // on the GPU and on any host. That is what lets the traversal outputs (hit
 // voxel, face, step count) and the radiance planes match the CPU restatement
 // of the reference shaders bit for bit.
@@ -16,7 +18,8 @@
 //             s = (m-1)/(m+1), odd series to s^11;
 //   sin/cos:  reduction by pi/2 with a three-part constant, Taylor series on
 //             |r| <= pi/4, quadrant selection;
-//   pow:      exp2(y * log2(x)) with GLSL's defined special cases.
+//   pow:      binary powering for integer exponents 1..1024, otherwise
+//             exp2(y * log2(x)), with GLSL's defined special cases.
 #pragma once
 #include <cmath>
 #include <cstdint>
@@ -62,14 +65,14 @@ VPT_HD float scale2(float p, int k) {
 
 VPT_HD float exp_poly(float r) {
     float p = 1.0f / 40320.0f;
-    p = p * r + 1.0f / 5040.0f;
-    p = p * r + 1.0f / 720.0f;
-    p = p * r + 1.0f / 120.0f;
-    p = p * r + 1.0f / 24.0f;
-    p = p * r + 1.0f / 6.0f;
-    p = p * r + 0.5f;
-    p = p * r + 1.0f;
-    p = p * r + 1.0f;
+    p = fmaf(p, r, 1.0f / 5040.0f);
+    p = fmaf(p, r, 1.0f / 720.0f);
+    p = fmaf(p, r, 1.0f / 120.0f);
+    p = fmaf(p, r, 1.0f / 24.0f);
+    p = fmaf(p, r, 1.0f / 6.0f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
     return p;
 }
 
@@ -111,39 +114,51 @@ VPT_HD float dlog2(float x) {
     float s = (m - 1.0f) / (m + 1.0f);
     float s2 = s * s;
     float p = 1.0f / 11.0f;
-    p = p * s2 + 1.0f / 9.0f;
-    p = p * s2 + 1.0f / 7.0f;
-    p = p * s2 + 1.0f / 5.0f;
-    p = p * s2 + 1.0f / 3.0f;
-    p = p * s2 + 1.0f;
+    p = fmaf(p, s2, 1.0f / 9.0f);
+    p = fmaf(p, s2, 1.0f / 7.0f);
+    p = fmaf(p, s2, 1.0f / 5.0f);
+    p = fmaf(p, s2, 1.0f / 3.0f);
+    p = fmaf(p, s2, 1.0f);
     float ln_m = 2.0f * (s * p);
     return (float)e + ln_m * 1.44269502162933350f;
 }
 
+// Integer exponents 1..1024: binary powering from the lowest bit.
 VPT_HD float dpow(float x, float y) {
     if (y == 0.0f) return 1.0f;
     if (x == 1.0f) return 1.0f;
     if (x == 0.0f) return y > 0.0f ? 0.0f : inf_f();
     if (x < 0.0f || x != x || y != y) return nan_f();
+    if (y >= 1.0f && y <= 1024.0f && y == floorf(y)) {
+        int n = (int)y;
+        float r = 1.0f, b = x;
+        for (;;) {
+            if (n & 1) r = r * b;
+            n >>= 1;
+            if (!n) break;
+            b = b * b;
+        }
+        return r;
+    }
     return dexp2(y * dlog2(x));
 }
 
 VPT_HD float sin_poly(float r) {
     float r2 = r * r;
     float p = 1.0f / 362880.0f;
-    p = p * r2 - 1.0f / 5040.0f;
-    p = p * r2 + 1.0f / 120.0f;
-    p = p * r2 - 1.0f / 6.0f;
-    return r + (r * r2) * p;
+    p = fmaf(p, r2, -(1.0f / 5040.0f));
+    p = fmaf(p, r2, 1.0f / 120.0f);
+    p = fmaf(p, r2, -(1.0f / 6.0f));
+    return fmaf(r * r2, p, r);
 }
 VPT_HD float cos_poly(float r) {
     float r2 = r * r;
     float p = -1.0f / 3628800.0f;
-    p = p * r2 + 1.0f / 40320.0f;
-    p = p * r2 - 1.0f / 720.0f;
-    p = p * r2 + 1.0f / 24.0f;
-    p = p * r2 - 0.5f;
-    return 1.0f + r2 * p;
+    p = fmaf(p, r2, 1.0f / 40320.0f);
+    p = fmaf(p, r2, -(1.0f / 720.0f));
+    p = fmaf(p, r2, 1.0f / 24.0f);
+    p = fmaf(p, r2, -(0.5f));
+    return fmaf(r2, p, 1.0f);
 }
 VPT_HD float reduce_pio2(float x, int* q) {
     float kf = floorf(x * 0.636619746685028076f + 0.5f);
@@ -204,7 +219,8 @@ VPT_HD v3 cross(v3 a, v3 b) {
     return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 VPT_HD float length(v3 a) { return sqrtf(dot(a, a)); }
-VPT_HD v3 normalize(v3 a) { return divs(a, length(a)); }
+// x * (1/length(x)): one IEEE division, as GPU compilers emit normalize()
+VPT_HD v3 normalize(v3 a) { return muls(a, 1.0f / length(a)); }
 VPT_HD v3 vmax(v3 a, float s) { return mk3(fmaxf(a.x, s), fmaxf(a.y, s), fmaxf(a.z, s)); }
 VPT_HD v3 vclamp(v3 a, float lo, float hi) {
     return mk3(clampf(a.x, lo, hi), clampf(a.y, lo, hi), clampf(a.z, lo, hi));
