@@ -44,7 +44,8 @@ ALG_BYTES_PER_STEP = 32     # one 32-byte sector per DF gather
 ALG_BYTES_PER_RAY = 16      # ray output
 PEAKS_FILE = REPO / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
-TRACE_KINDS = {"primary": ["primary"], "shadow": ["shadow"], "diffuse": ["diffuse", "bounce_shadow"]}
+TRACE_KINDS = {"primary": ["primary"], "shadow": ["shadow"], "diffuse": ["diffuse", "bounce_shadow"],
+               "trace_frame": ["primary", "shadow", "diffuse", "bounce_shadow"]}
 # Algorithmic bytes per pixel of the filter and colour kernels (planes read +
 # planes written once), fp32 / fp16 storage.
 FILTER_BYTES_PER_PX = {
@@ -55,6 +56,7 @@ FILTER_BYTES_PER_PX = {
     "shade": (47, 25),             # t, face, block, shadow, SH, CoCg, AO.x in; RGB out
 }
 KERNEL_NAMES = {"primary": "k_trace_primary", "shadow": "k_trace_shadow", "diffuse": "k_trace_diffuse",
+                "trace_frame": "k_trace_frame",
                 "spatial_initial": "k_spatial_initial", "temporal": "k_temporal", "variance": "k_variance",
                 "atrous": "k_atrous", "shade": "k_shade"}
 
@@ -251,7 +253,7 @@ def run_ours(args):
     rays_total = dist.sum(float(sum(frame_rays)))
     ms_per_step = t_total * 1e3 / args.steps
     value = rays_total / t_total
-    trace_ms = sum(sum(pass_ms[p]) for p in ("primary", "shadow", "diffuse"))
+    trace_ms = sum(sum(pass_ms[p]) for p in ("primary", "shadow", "diffuse", "trace_frame"))
     trace_rays_per_s = sum(frame_rays) / (trace_ms / 1e3)
 
     # roofline of every kernel; the dominant one has the largest share of the frame
@@ -259,6 +261,7 @@ def run_ours(args):
     peak, peak_kind = peak_hbm()
     iters = ctx.config.atrous_iterations
     kernels = {}
+    mean_pass = {p: ms for p, ms in mean_pass.items() if ms > 0}   # passes this frame path ran
     for p, ms in mean_pass.items():
         launches_per_frame = iters if p == "atrous" else 1
         if p in TRACE_KINDS:

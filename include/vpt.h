@@ -148,8 +148,17 @@ typedef struct vpt_stats {
 typedef enum vpt_pass {
     VPT_PASS_PRIMARY = 0, VPT_PASS_SHADOW = 1, VPT_PASS_DIFFUSE = 2, VPT_PASS_SPATIAL_INITIAL = 3,
     VPT_PASS_TEMPORAL = 4, VPT_PASS_VARIANCE = 5, VPT_PASS_ATROUS = 6, VPT_PASS_SHADE = 7,
-    VPT_PASS_COUNT = 8
+    VPT_PASS_TRACE_FRAME = 8,        /* fused primary + shadow + diffuse (vpt_trace_frame) */
+    VPT_PASS_COUNT = 9
 } vpt_pass;
+
+/* Launch-shape knobs of the fused trace kernel, picked by the autotuner. */
+typedef struct vpt_tuning {
+    int32_t refill_threshold;        /* waiting lanes that trigger a warp refill, 1..32 (default 16) */
+    int32_t trace_blocks;            /* persistent blocks of 128 threads; 0 = fill every SM once */
+    int32_t fused_trace;             /* vpt_render_frame traces with vpt_trace_frame (1) or the three passes (0, default) */
+    int32_t reserved[5];
+} vpt_tuning;
 
 /* ------------------------------------------------------------- lifetime -- */
 const char* vpt_status_string(vpt_status s);
@@ -190,11 +199,18 @@ vpt_status vpt_trace_diffuse(vpt_ctx* ctx, const vpt_frame* frame);
 vpt_status vpt_svgf(vpt_ctx* ctx, const vpt_camera* prev_cam, const vpt_frame* frame);
 /* Colour pass, Core/Pipeline.cpp:3603-3821 (ColorPassFrag.glsl): fills COLOR. */
 vpt_status vpt_shade(vpt_ctx* ctx, const vpt_frame* frame);
+/* The three trace passes of a frame in one persistent kernel: fills T, FACE,
+ * BLOCK, HIT, STEPS, SHADOW and GI_* exactly as vpt_trace_primary,
+ * vpt_trace_shadow and vpt_trace_diffuse would. Stores `cam` as this frame's
+ * camera. */
+vpt_status vpt_trace_frame(vpt_ctx* ctx, const vpt_camera* cam, const vpt_frame* frame);
+vpt_status vpt_set_tuning(vpt_ctx* ctx, const vpt_tuning* tuning);
+vpt_status vpt_get_tuning(const vpt_ctx* ctx, vpt_tuning* tuning);
 /* Ping-pong swap of the G-buffer and temporal history (Core/Pipeline.cpp:1775-1788, :1970-1971). */
 vpt_status vpt_end_frame(vpt_ctx* ctx);
 /* Clears the history so the next frame starts without reprojection. */
 vpt_status vpt_reset_history(vpt_ctx* ctx);
-/* One whole frame: primary, shadow, diffuse, SVGF, shade, end_frame. If
+/* One whole frame: trace_frame, SVGF, shade, end_frame. If
  * rgb_out is not NULL the COLOR plane is copied to it as float32 RGB
  * (W*H*3 floats) and the call waits for it. prev_cam may be NULL on the
  * first frame (the camera of the previous call is used otherwise). */

@@ -136,9 +136,45 @@ def test_passes_bit_exact_two_frames(vpt, oracle, scene, storage, gpu):
     ctx.close()
 
 
-def test_render_frame_matches_oracle(vpt, oracle, scene, gpu):
+TRACE_PLANES = [("t", "T"), ("face", "FACE"), ("block", "BLOCK"), ("hit", "HIT"), ("steps", "STEPS")]
+GI_PLANES = ["sh", "cocg", "luma", "aosky"]
+
+
+@pytest.mark.parametrize("storage,threshold,blocks,spp,bounces", [
+    (0, 16, 0, 1, 1), (0, 1, 0, 1, 1), (0, 32, 3, 1, 1), (1, 16, 0, 1, 1), (0, 8, 0, 2, 2), (1, 24, 7, 2, 2)])
+def test_fused_trace_frame_bit_exact(vpt, oracle, scene, storage, threshold, blocks, spp, bounces, gpu):
+    """The persistent fused kernel writes the same G-buffer, shadow and GI
+    planes as the oracle's three passes, for any refill threshold and grid size."""
+    world = scene["world"]
+    with vpt.Context(width=W, height=H, primary_max_steps=256, storage=storage, spp=spp, bounces=bounces) as ctx:
+        ctx.upload_world(scene["vox"])
+        ctx.set_block_table(scene["blocks"])
+        ctx.build_df()
+        ctx.set_tuning(refill_threshold=threshold, trace_blocks=blocks)
+        for fi, cam in enumerate(scene["cams"]):
+            frame = vpt.default_frame(frame_index=fi, seed=21)
+            ctx.set_stats(True)
+            ctx.trace_frame(cam, frame)
+            stats = ctx.read_stats()
+            cfg = ctx.config
+            with oracle.Counting() as cnt:
+                g = oracle.trace_primary(world, cam, cfg)
+                shadow = oracle.trace_shadow(world, cam, cfg, frame, g["t"], g["face"])
+                gi = oracle.trace_diffuse(world, cam, cfg, frame, g["t"], g["face"])
+            for name, plane in TRACE_PLANES:
+                assert_same(ctx.read_plane(plane), g[name], f"fused {name} frame {fi}")
+            assert_same(ctx.read_plane("SHADOW"), shadow, f"fused shadow frame {fi}")
+            for k in GI_PLANES:
+                assert_same(ctx.read_plane("GI_" + k.upper()), gi[k], f"fused GI {k} frame {fi}")
+            assert stats["rays"] == cnt.rays and stats["steps"] == cnt.steps
+            ctx.end_frame()
+
+
+@pytest.mark.parametrize("fused", [False, True], ids=["passes", "fused"])
+def test_render_frame_matches_oracle(vpt, oracle, scene, fused, gpu):
     world = scene["world"]
     ctx = make_ctx(vpt, scene, vpt.STORAGE_F32)
+    ctx.set_tuning(fused_trace=fused)
     prev_g, hist = oracle.empty_history(H, W)
     prev_cam = scene["cams"][0]
     for fi, cam in enumerate(scene["cams"]):

@@ -43,7 +43,7 @@ PLANES = [
     "COLOR",
 ]
 PLANE = {name: i for i, name in enumerate(PLANES)}
-PASSES = ["primary", "shadow", "diffuse", "spatial_initial", "temporal", "variance", "atrous", "shade"]
+PASSES = ["primary", "shadow", "diffuse", "spatial_initial", "temporal", "variance", "atrous", "shade", "trace_frame"]
 FACE_MISS = 10
 
 
@@ -75,6 +75,11 @@ class Frame(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("rays", C.c_uint64 * 4), ("steps", C.c_uint64 * 4)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("refill_threshold", C.c_int32), ("trace_blocks", C.c_int32), ("fused_trace", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 BLOCK_DTYPE = np.dtype([("albedo", np.uint8, 3), ("roughness", np.uint8), ("metalness", np.uint8),
@@ -112,6 +117,9 @@ def _load() -> C.CDLL:
         "vpt_trace_diffuse": ([P, C.POINTER(Frame)], C.c_int),
         "vpt_svgf": ([P, C.POINTER(Camera), C.POINTER(Frame)], C.c_int),
         "vpt_shade": ([P, C.POINTER(Frame)], C.c_int),
+        "vpt_trace_frame": ([P, C.POINTER(Camera), C.POINTER(Frame)], C.c_int),
+        "vpt_set_tuning": ([P, C.POINTER(Tuning)], C.c_int),
+        "vpt_get_tuning": ([P, C.POINTER(Tuning)], C.c_int),
         "vpt_end_frame": ([P], C.c_int),
         "vpt_reset_history": ([P], C.c_int),
         "vpt_render_frame": ([P, C.POINTER(Camera), C.POINTER(Frame), P], C.c_int),
@@ -299,6 +307,26 @@ class Context:
 
     def shade(self, frame: Frame):
         self._ck(lib.vpt_shade(self._h, C.byref(frame)), "vpt_shade")
+
+    def trace_frame(self, cam: Camera, frame: Frame):
+        """Primary, sun-shadow and diffuse traces in one persistent kernel."""
+        self._ck(lib.vpt_trace_frame(self._h, C.byref(cam), C.byref(frame)), "vpt_trace_frame")
+
+    def set_tuning(self, refill_threshold: int | None = None, trace_blocks: int | None = None,
+                   fused_trace: bool | None = None):
+        t = self.tuning()
+        if refill_threshold is not None:
+            t.refill_threshold = refill_threshold
+        if trace_blocks is not None:
+            t.trace_blocks = trace_blocks
+        if fused_trace is not None:
+            t.fused_trace = 1 if fused_trace else 0
+        self._ck(lib.vpt_set_tuning(self._h, C.byref(t)), "vpt_set_tuning")
+
+    def tuning(self) -> Tuning:
+        t = Tuning()
+        self._ck(lib.vpt_get_tuning(self._h, C.byref(t)), "vpt_get_tuning")
+        return t
 
     def end_frame(self):
         self._ck(lib.vpt_end_frame(self._h), "vpt_end_frame")

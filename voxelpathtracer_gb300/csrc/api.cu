@@ -92,6 +92,9 @@ struct vpt_ctx {
     bool have_cam = false;
     vpt_camera prev_cam{};
     bool have_prev = false;
+    // fused trace: work queue counter and launch-shape knobs
+    int* queue = nullptr;
+    vpt_tuning tuning{};
     // instrumentation
     Counters* counters = nullptr;
     bool stats = false;
@@ -244,6 +247,7 @@ vpt_status alloc_planes(vpt_ctx* c) {
     c->var[FI_AOSKY] = nullptr;
     A(c->color, n * 3 * es);
     A(c->counters, sizeof(Counters));
+    A(c->queue, 256);
 #undef A
     return VPT_OK;
 }
@@ -402,6 +406,8 @@ vpt_status vpt_create(vpt_ctx** out, const vpt_config* cfg) {
     if (!c) return VPT_ERR_OOM;
     c->cfg = *cfg;
     c->dev = cfg->device;
+    c->tuning.refill_threshold = 16;
+    c->tuning.trace_blocks = 0;
     c->fp16 = cfg->storage == VPT_STORAGE_F16;
     c->npx = (size_t)cfg->width * (size_t)cfg->height;
     vpt_status s = VPT_OK;
@@ -579,6 +585,68 @@ vpt_status vpt_trace_diffuse(vpt_ctx* c, const vpt_frame* f) {
     return VPT_OK;
 }
 
+vpt_status vpt_trace_frame(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (!cam || !f) return fail(c, VPT_ERR_INVALID_ARG, "camera and frame are required");
+    vpt_status s = check_world(c);
+    if (s != VPT_OK) return s;
+    cudaSetDevice(c->dev);
+    c->cam = *cam;
+    c->have_cam = true;
+    const int W = c->cfg.width, H = c->cfg.height;
+    FrameTraceArgs a;
+    a.w = world_view(c);
+    a.cam = cam_view(*cam);
+    a.W = W;
+    a.H = H;
+    a.tiles_x = (W + 7) / 8;
+    a.n_items = a.tiles_x * ((H + 3) / 4) * 32;
+    a.primary_max_steps = c->cfg.primary_max_steps;
+    a.shadow_max_steps = c->cfg.shadow_max_steps;
+    for (int k = 0; k < 3; k++) a.sun[k] = f->sun_dir[k];
+    a.refill_threshold = c->tuning.refill_threshold;
+    a.d.diffuse_max_steps = c->cfg.diffuse_max_steps;
+    a.d.bounce_shadow_max_steps = c->cfg.bounce_shadow_max_steps;
+    a.d.bounces = c->cfg.bounces;
+    a.d.spp = c->cfg.spp;
+    a.d.frame_index = f->frame_index;
+    a.d.seed = f->seed;
+    a.d.lighting = gi_lighting(f);
+    a.t = c->gbuf[c->cur][GB_T];
+    a.face = (uint8_t*)c->gbuf[c->cur][GB_FACE];
+    a.block = (uint8_t*)c->gbuf[c->cur][GB_BLOCK];
+    a.hit = (int32_t*)c->gbuf[c->cur][GB_HIT];
+    a.steps = (uint16_t*)c->gbuf[c->cur][GB_STEPS];
+    a.shadow = c->shadow;
+    a.sh = c->gi[GI_SH];
+    a.cocg = c->gi[GI_COCG];
+    a.luma = c->gi[GI_LUMA];
+    a.aosky = c->gi[GI_AOSKY];
+    a.queue = c->queue;
+    a.stats = c->stats ? c->counters : nullptr;
+    pass_begin(c, VPT_PASS_TRACE_FRAME);
+    CK(c, cudaMemsetAsync(c->queue, 0, sizeof(int), c->stream));
+    CK(c, trace_frame(a, c->fp16, c->tuning.trace_blocks, c->stream));
+    pass_end(c, VPT_PASS_TRACE_FRAME);
+    c->launches += 1;
+    return VPT_OK;
+}
+
+vpt_status vpt_set_tuning(vpt_ctx* c, const vpt_tuning* t) {
+    if (!c || !t) return VPT_ERR_INVALID_ARG;
+    if (t->refill_threshold < 1 || t->refill_threshold > 32 || t->trace_blocks < 0 || t->trace_blocks > 65535 ||
+        t->fused_trace < 0 || t->fused_trace > 1)
+        return fail(c, VPT_ERR_INVALID_ARG, "refill_threshold must be 1..32, trace_blocks 0..65535, fused_trace 0/1");
+    c->tuning = *t;
+    return VPT_OK;
+}
+
+vpt_status vpt_get_tuning(const vpt_ctx* c, vpt_tuning* t) {
+    if (!c || !t) return VPT_ERR_INVALID_ARG;
+    *t = c->tuning;
+    return VPT_OK;
+}
+
 vpt_status vpt_svgf(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f) {
     if (!c) return VPT_ERR_INVALID_ARG;
     vpt_status s = check_frame(c, f);
@@ -699,9 +767,13 @@ vpt_status vpt_render_frame(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* 
     if (!cam || !f) return fail(c, VPT_ERR_INVALID_ARG, "camera and frame are required");
     vpt_status s;
     const vpt_camera prev = c->have_prev ? c->prev_cam : *cam;
-    if ((s = vpt_trace_primary(c, cam)) != VPT_OK) return s;
-    if ((s = vpt_trace_shadow(c, f)) != VPT_OK) return s;
-    if ((s = vpt_trace_diffuse(c, f)) != VPT_OK) return s;
+    if (c->tuning.fused_trace) {
+        if ((s = vpt_trace_frame(c, cam, f)) != VPT_OK) return s;
+    } else {
+        if ((s = vpt_trace_primary(c, cam)) != VPT_OK) return s;
+        if ((s = vpt_trace_shadow(c, f)) != VPT_OK) return s;
+        if ((s = vpt_trace_diffuse(c, f)) != VPT_OK) return s;
+    }
     if ((s = vpt_svgf(c, &prev, f)) != VPT_OK) return s;
     if ((s = vpt_shade(c, f)) != VPT_OK) return s;
     if (rgb_out) {

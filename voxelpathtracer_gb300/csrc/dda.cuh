@@ -1,0 +1,141 @@
+// DF-accelerated voxel DDA (VoxelTraversalDF, InitialRayTraceFrag.glsl:307-374;
+// identical loops at ShadowRayTraceFrag.glsl:222-289 and
+// DiffuseRayTraceFrag.glsl:1043-1110) written as a resumable state machine:
+// ray_start sets up the loop, dda_step runs one iteration of the loop body,
+// ray_finish evaluates the code after the loop. `traverse` runs it to the end.
+// All arithmetic is IEEE fp32 without fused multiply-adds, so hit voxel, face
+// and step count are bit-identical to the CPU restatement.
+#pragma once
+#include "common.cuh"
+
+namespace vpt {
+
+// int(floor(ToConservativeEuclidean(Dist))) (InitialRayTraceFrag.glsl:89-92, :328-330);
+// texelFetch(R8)*255 gives back the stored integer exactly.
+__device__ __forceinline__ int euclid_steps(int dist) {
+    float D = (float)dist;
+    float e = (D == 1.0f) ? 1.0f : D * 0.57735026918f;
+    return f2i(floorf(e));
+}
+
+struct RayState {
+    v3 o;            // current origin
+    v3 d;            // direction
+    v3 init;         // initial origin
+    float ix, iy, iz;  // 1 / direction
+    int itr;         // loop counter
+    int max_steps;
+    int min_idx;
+    int inter;       // Intersection flag
+};
+
+struct TraceResult {
+    float t;
+    v3 normal;
+    int block;
+    int cell[3];
+    int steps;
+};
+
+__device__ __forceinline__ void ray_start(RayState& r, v3 origin, v3 dir, int max_steps) {
+    r.o = origin;
+    r.d = dir;
+    r.init = origin;
+    r.ix = 1.0f / dir.x;
+    r.iy = 1.0f / dir.y;
+    r.iz = 1.0f / dir.z;
+    r.itr = 0;
+    r.max_steps = max_steps;
+    r.min_idx = 0;
+    r.inter = 0;
+}
+
+// One iteration of the traversal loop; returns true once the loop is over.
+__device__ __forceinline__ bool dda_step(const WorldView& w, RayState& r) {
+    if (r.itr >= r.max_steps) return true;
+    const int lx = f2i(floorf(r.o.x));
+    const int ly = f2i(floorf(r.o.y));
+    const int lz = f2i(floorf(r.o.z));
+    if (!in_volume(w, lx, ly, lz)) {
+        r.inter = 0;
+        return true;
+    }
+    const int e = euclid_steps((int)__ldg(w.df + vox_index(w, lx, ly, lz)));
+    if (e == 0) return true;
+    if (e == 1) {
+        // one exact DDA face step (:341-356)
+        const int sx = isign(r.d.x), sy = isign(r.d.y), sz = isign(r.d.z);
+        const int hx = (1 + sx) >> 1, hy = (1 + sy) >> 1, hz = (1 + sz) >> 1;
+        int gx = f2i(r.o.x), gy = f2i(r.o.y), gz = f2i(r.o.z);
+        float wx = r.o.x - (float)gx, wy = r.o.y - (float)gy, wz = r.o.z - (float)gz;
+        const float dfx = ((float)hx - wx) * r.ix;
+        const float dfy = ((float)hy - wy) * r.iy;
+        const float dfz = ((float)hz - wz) * r.iz;
+        const int m = (dfx < dfy && sx != 0) ? ((dfx < dfz || sz == 0) ? 0 : 2) : ((dfy < dfz || sz == 0) ? 1 : 2);
+        const float dm = m == 0 ? dfx : (m == 1 ? dfy : dfz);
+        wx = wx + r.d.x * dm;
+        wy = wy + r.d.y * dm;
+        wz = wz + r.d.z * dm;
+        if (m == 0) { gx += sx; wx = (float)(1 - hx); }
+        else if (m == 1) { gy += sy; wy = (float)(1 - hy); }
+        else { gz += sz; wz = (float)(1 - hz); }
+        r.o.x = (float)gx + wx;
+        r.o.y = (float)gy + wy;
+        r.o.z = (float)gz + wz;
+        if (m == 0) r.o.x = r.o.x + (float)sx * 0.0001f;
+        else if (m == 1) r.o.y = r.o.y + (float)sy * 0.0001f;
+        else r.o.z = r.o.z + (float)sz * 0.0001f;
+        r.min_idx = m;
+        r.inter = 1;
+    } else {
+        // jump by the conservative Euclidean radius (:361)
+        const float k = (float)(e - 1);
+        r.o.x = r.o.x + k * r.d.x;
+        r.o.y = r.o.y + k * r.d.y;
+        r.o.z = r.o.z + k * r.d.z;
+    }
+    r.itr++;
+    return r.itr >= r.max_steps;
+}
+
+// The code after the loop (:365-373).
+__device__ __forceinline__ TraceResult ray_finish(const WorldView& w, const RayState& r) {
+    TraceResult t;
+    t.cell[0] = f2i(floorf(r.o.x));
+    t.cell[1] = f2i(floorf(r.o.y));
+    t.cell[2] = f2i(floorf(r.o.z));
+    t.steps = r.itr;
+    t.normal = mk3(0.0f, 0.0f, 0.0f);
+    t.block = 0;
+    t.t = -1.0f;
+    if (r.inter) {
+        const int m = r.min_idx;
+        const int s = m == 0 ? isign(r.d.x) : (m == 1 ? isign(r.d.y) : isign(r.d.z));
+        const float nv = (float)(-s);
+        if (m == 0) t.normal.x = nv; else if (m == 1) t.normal.y = nv; else t.normal.z = nv;
+        t.block = get_voxel(w, t.cell[0], t.cell[1], t.cell[2]);
+        t.t = t.block > 0 ? length(sub(r.o, r.init)) : -1.0f;
+    }
+    return t;
+}
+
+__device__ __forceinline__ TraceResult traverse(const WorldView& w, v3 origin, v3 direction, int max_steps) {
+    RayState r;
+    ray_start(r, origin, direction, max_steps);
+    while (!dda_step(w, r)) {
+    }
+    return ray_finish(w, r);
+}
+
+// GetNormalID (InitialRayTraceFrag.glsl:143-185): exact compares, 0 if none match.
+__device__ __forceinline__ int normal_id(v3 n) {
+    if (n.x == 0.0f && n.y == 0.0f && n.z == 1.0f) return 0;
+    if (n.x == 0.0f && n.y == 0.0f && n.z == -1.0f) return 1;
+    if (n.x == 0.0f && n.y == 1.0f && n.z == 0.0f) return 2;
+    if (n.x == 0.0f && n.y == -1.0f && n.z == 0.0f) return 3;
+    if (n.x == -1.0f && n.y == 0.0f && n.z == 0.0f) return 4;
+    if (n.x == 1.0f && n.y == 0.0f && n.z == 0.0f) return 5;
+    return 0;
+}
+
+}  // namespace vpt

@@ -51,6 +51,36 @@ cudaError_t trace_shadow(const WorldView& w, const CamView& cam, int W, int H, i
 cudaError_t trace_diffuse(const WorldView& w, const CamView& cam, int W, int H, const DiffuseArgs& a, int fp16,
                           const void* t, const uint8_t* face, GIOut out, Counters* stats, cudaStream_t s);
 
+// -------------------------------------------------------- trace_frame.cu --
+// Every ray of a frame (primary, sun shadow, diffuse bounces and their
+// shadow rays) in one persistent kernel; same outputs as the three passes.
+struct FrameTraceArgs {
+    WorldView w;
+    CamView cam;
+    int W, H;
+    int tiles_x;             // 8x4 pixel tiles per row
+    int n_items;             // tiles * 32 queue entries
+    int primary_max_steps;
+    int shadow_max_steps;
+    float sun[3];
+    int refill_threshold;    // waiting lanes that trigger a warp-wide refill (1..32)
+    DiffuseArgs d;
+    void* t;
+    uint8_t* face;
+    uint8_t* block;
+    int32_t* hit;
+    uint16_t* steps;
+    uint8_t* shadow;
+    void* sh;
+    void* cocg;
+    void* luma;
+    void* aosky;
+    int* queue;              // work counter, zero at launch
+    Counters* stats;
+};
+// blocks_hint <= 0 sizes the grid to fill every SM once.
+cudaError_t trace_frame(const FrameTraceArgs& a, int fp16, int blocks_hint, cudaStream_t s);
+
 // -------------------------------------------------------------- svgf.cu --
 struct GIIn {
     const void* sh;

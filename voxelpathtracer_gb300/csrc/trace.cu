@@ -1,108 +1,13 @@
-// DF-accelerated voxel DDA and the three trace passes: primary (G-buffer),
-// sun shadow and diffuse GI.
-//
-// The traversal restates VoxelTraversalDF (InitialRayTraceFrag.glsl:307-374;
-// the same loop appears at ShadowRayTraceFrag.glsl:222-289 and
-// DiffuseRayTraceFrag.glsl:1043-1110) in IEEE fp32 without fused
-// multiply-adds, so hit voxel, face and step count are bit-identical to the
-// CPU restatement. Each step is one dependent 1-byte gather from the distance
-// field; the kernels are bound by L2 latency/bandwidth of those gathers.
+// The three trace passes as separate kernels, one thread per pixel: primary
+// (G-buffer), sun shadow and diffuse GI. They back the pass-by-pass entry
+// points of the C ABI; the frame path uses the fused persistent kernel in
+// trace_frame.cu. The traversal is dda.cuh.
+#include "dda.cuh"
 #include "kernels.cuh"
 
 namespace vpt {
 
 namespace {
-
-// int(floor(ToConservativeEuclidean(Dist))) (InitialRayTraceFrag.glsl:89-92, :328-330)
-__device__ __forceinline__ int euclid_steps(int dist) {
-    float D = (float)dist;
-    float e = (D == 1.0f) ? 1.0f : D * 0.57735026918f;
-    return f2i(floorf(e));
-}
-
-struct TraceResult {
-    float t;
-    v3 normal;
-    int block;
-    int cell[3];
-    int steps;
-};
-
-__device__ __forceinline__ TraceResult traverse(const WorldView& w, v3 origin, v3 direction, int max_steps) {
-    const v3 initial = origin;
-    bool intersection = false;
-    int min_idx = 0;
-    const int sx = isign(direction.x), sy = isign(direction.y), sz = isign(direction.z);
-    const int hx = (1 + sx) >> 1, hy = (1 + sy) >> 1, hz = (1 + sz) >> 1;
-    const float ix = 1.0f / direction.x, iy = 1.0f / direction.y, iz = 1.0f / direction.z;
-    int itr = 0;
-    for (itr = 0; itr < max_steps; itr++) {
-        int lx = f2i(floorf(origin.x));
-        int ly = f2i(floorf(origin.y));
-        int lz = f2i(floorf(origin.z));
-        if (!in_volume(w, lx, ly, lz)) {
-            intersection = false;
-            break;
-        }
-        int e = euclid_steps((int)__ldg(w.df + vox_index(w, lx, ly, lz)));
-        if (e == 0) break;
-        if (e == 1) {
-            int gx = f2i(origin.x), gy = f2i(origin.y), gz = f2i(origin.z);
-            float wx = origin.x - (float)gx, wy = origin.y - (float)gy, wz = origin.z - (float)gz;
-            float dfx = ((float)hx - wx) * ix;
-            float dfy = ((float)hy - wy) * iy;
-            float dfz = ((float)hz - wz) * iz;
-            min_idx = (dfx < dfy && sx != 0) ? ((dfx < dfz || sz == 0) ? 0 : 2)
-                                             : ((dfy < dfz || sz == 0) ? 1 : 2);
-            float dm = min_idx == 0 ? dfx : (min_idx == 1 ? dfy : dfz);
-            wx = wx + direction.x * dm;
-            wy = wy + direction.y * dm;
-            wz = wz + direction.z * dm;
-            if (min_idx == 0) { gx += sx; wx = (float)(1 - hx); }
-            else if (min_idx == 1) { gy += sy; wy = (float)(1 - hy); }
-            else { gz += sz; wz = (float)(1 - hz); }
-            origin.x = (float)gx + wx;
-            origin.y = (float)gy + wy;
-            origin.z = (float)gz + wz;
-            if (min_idx == 0) origin.x = origin.x + (float)sx * 0.0001f;
-            else if (min_idx == 1) origin.y = origin.y + (float)sy * 0.0001f;
-            else origin.z = origin.z + (float)sz * 0.0001f;
-            intersection = true;
-        } else {
-            float k = (float)(e - 1);
-            origin.x = origin.x + k * direction.x;
-            origin.y = origin.y + k * direction.y;
-            origin.z = origin.z + k * direction.z;
-        }
-    }
-    TraceResult r;
-    r.cell[0] = f2i(floorf(origin.x));
-    r.cell[1] = f2i(floorf(origin.y));
-    r.cell[2] = f2i(floorf(origin.z));
-    r.steps = itr;
-    r.normal = mk3(0.0f, 0.0f, 0.0f);
-    r.block = 0;
-    r.t = -1.0f;
-    if (intersection) {
-        int s = min_idx == 0 ? sx : (min_idx == 1 ? sy : sz);
-        float nv = (float)(-s);
-        if (min_idx == 0) r.normal.x = nv; else if (min_idx == 1) r.normal.y = nv; else r.normal.z = nv;
-        r.block = get_voxel(w, r.cell[0], r.cell[1], r.cell[2]);
-        r.t = r.block > 0 ? length(sub(origin, initial)) : -1.0f;
-    }
-    return r;
-}
-
-// GetNormalID (InitialRayTraceFrag.glsl:143-185)
-__device__ __forceinline__ int normal_id(v3 n) {
-    if (n.x == 0.0f && n.y == 0.0f && n.z == 1.0f) return 0;
-    if (n.x == 0.0f && n.y == 0.0f && n.z == -1.0f) return 1;
-    if (n.x == 0.0f && n.y == 1.0f && n.z == 0.0f) return 2;
-    if (n.x == 0.0f && n.y == -1.0f && n.z == 0.0f) return 3;
-    if (n.x == -1.0f && n.y == 0.0f && n.z == 0.0f) return 4;
-    if (n.x == 1.0f && n.y == 0.0f && n.z == 0.0f) return 5;
-    return 0;
-}
 
 // Pixel of thread `tid` in a 16x16 tile: each warp covers an 8x4 patch so its
 // rays stay spatially coherent.
