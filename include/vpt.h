@@ -204,6 +204,42 @@ vpt_status vpt_shade(vpt_ctx* ctx, const vpt_frame* frame);
  * vpt_trace_shadow and vpt_trace_diffuse would. Stores `cam` as this frame's
  * camera. */
 vpt_status vpt_trace_frame(vpt_ctx* ctx, const vpt_camera* cam, const vpt_frame* frame);
+/* Device buffers of one frame trace, owned by the caller. Layouts as the
+ * planes of vpt_plane_info: t and gi_* in cfg->storage's type (fp32 or fp16),
+ * hit 3 x int32 per pixel, gi_sh 4, gi_cocg 2, gi_luma 1, gi_aosky 2 channels. */
+typedef struct vpt_trace_buffers {
+    const uint8_t* voxels;           /* X*Y*Z block ids, x fastest */
+    const uint8_t* df;               /* their distance field (vpt_df_build_device) */
+    int32_t X, Y, Z;
+    const vpt_block* blocks;
+    int32_t n_blocks;
+    void* t;
+    uint8_t* face;
+    uint8_t* block;
+    int32_t* hit;
+    uint16_t* steps;
+    uint8_t* shadow;
+    void* gi_sh;
+    void* gi_cocg;
+    void* gi_luma;
+    void* gi_aosky;
+} vpt_trace_buffers;
+
+/* No counterpart in the reference: vpt_trace_frame for callers that cannot
+ * allocate device memory while rendering (engines that carve all GPU memory
+ * out of a fixed start-up budget, or frame loops that cannot absorb
+ * cudaMalloc's implicit device synchronisation). It allocates nothing: the
+ * caller passes every input and output as device pointers, and the kernel's
+ * only scratch, its work-queue counter, sits in a 256-byte static device
+ * array of libvpt that every GPU using the library holds until the process
+ * exits. The first call on a device looks that array's address up (with the
+ * device current). Images are limited to 16384 x 16384. All calls share the
+ * array, which is reset at the start of each call: calls that overlap on the
+ * GPU race, so issue them on one stream (or otherwise order them). The
+ * current device and `stream` (a cudaStream_t, 0 = legacy default) are the
+ * caller's; refill threshold 16 and a grid that fills every SM once. */
+vpt_status vpt_trace_frame_noalloc(const vpt_trace_buffers* buffers, const vpt_config* cfg, const vpt_camera* cam,
+                                   const vpt_frame* frame, void* stream);
 vpt_status vpt_set_tuning(vpt_ctx* ctx, const vpt_tuning* tuning);
 vpt_status vpt_get_tuning(const vpt_ctx* ctx, vpt_tuning* tuning);
 /* Ping-pong swap of the G-buffer and temporal history (Core/Pipeline.cpp:1775-1788, :1970-1971). */

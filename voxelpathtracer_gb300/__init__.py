@@ -77,6 +77,14 @@ class Stats(C.Structure):
     _fields_ = [("rays", C.c_uint64 * 4), ("steps", C.c_uint64 * 4)]
 
 
+class TraceBuffers(C.Structure):
+    """vpt_trace_buffers: caller-owned device buffers of vpt_trace_frame_noalloc."""
+    _fields_ = [("voxels", C.c_void_p), ("df", C.c_void_p), ("X", C.c_int32), ("Y", C.c_int32), ("Z", C.c_int32),
+                ("blocks", C.c_void_p), ("n_blocks", C.c_int32), ("t", C.c_void_p), ("face", C.c_void_p),
+                ("block", C.c_void_p), ("hit", C.c_void_p), ("steps", C.c_void_p), ("shadow", C.c_void_p),
+                ("gi_sh", C.c_void_p), ("gi_cocg", C.c_void_p), ("gi_luma", C.c_void_p), ("gi_aosky", C.c_void_p)]
+
+
 class Tuning(C.Structure):
     _fields_ = [("refill_threshold", C.c_int32), ("trace_blocks", C.c_int32), ("fused_trace", C.c_int32),
                 ("reserved", C.c_int32 * 5)]
@@ -118,6 +126,8 @@ def _load() -> C.CDLL:
         "vpt_svgf": ([P, C.POINTER(Camera), C.POINTER(Frame)], C.c_int),
         "vpt_shade": ([P, C.POINTER(Frame)], C.c_int),
         "vpt_trace_frame": ([P, C.POINTER(Camera), C.POINTER(Frame)], C.c_int),
+        "vpt_trace_frame_noalloc": ([C.POINTER(TraceBuffers), C.POINTER(Config), C.POINTER(Camera),
+                                     C.POINTER(Frame), P], C.c_int),
         "vpt_set_tuning": ([P, C.POINTER(Tuning)], C.c_int),
         "vpt_get_tuning": ([P, C.POINTER(Tuning)], C.c_int),
         "vpt_end_frame": ([P], C.c_int),

@@ -19,6 +19,30 @@ enum RayKind { kRayPrimary = 0, kRayShadow = 1, kRayDiffuse = 2, kRayBounceShado
 // solid voxel): three sweeps along x, y and z. `launches` counts kernels.
 cudaError_t df_build(const uint8_t* vox, uint8_t* df, int X, int Y, int Z, cudaStream_t s, int* launches);
 
+// Per-frame constants of DiffuseRayTraceFrag main (:832-839), evaluated on
+// the host with the shader's operation order.
+inline GILighting gi_lighting(const vpt_frame* f) {
+    const v3 SUN_COLOR = muls(divs(mk3(192.0f, 216.0f, 255.0f), 255.0f), 16.0f);
+    const v3 NIGHT_COLOR = muls(divs(mk3(96.0f, 192.0f, 255.0f), 255.0f), 1.5f);
+    const v3 DUSK_COLOR = muls(divs(mk3(96.0f, 192.0f, 255.0f), 255.0f), 0.9f);
+    v3 sun = mk3(f->sun_dir[0], f->sun_dir[1], f->sun_dir[2]);
+    bool sun_stronger = -sun.y < 0.01f;
+    float dusk = clampf(dpow(fabsf(sun.y - 1.0f), 2.9f), 0.0f, 1.0f);
+    v3 sun_color = vmix(SUN_COLOR, DUSK_COLOR, dusk);
+    v3 lc = sun_stronger ? sun_color : NIGHT_COLOR;
+    lc = muls(lc, 0.4f * f->gi_sun_strength);
+    v3 ld = sun_stronger ? sun : normalize(mk3(-sun.x, -sun.y, sun.z));
+    GILighting L;
+    L.light_color[0] = lc.x; L.light_color[1] = lc.y; L.light_color[2] = lc.z;
+    L.light_dir[0] = ld.x; L.light_dir[1] = ld.y; L.light_dir[2] = ld.z;
+    L.moon_stronger = sun_stronger ? 0 : 1;
+    L.emissivity_multiplier = sun_stronger ? 12.0f : 13.0f;
+    L.sun_visibility = clampf(dot(sun, mk3(0.0f, 1.0f, 0.0f)) + 0.05f, 0.0f, 0.1f) * 12.0f;
+    L.gi_sky_strength = f->gi_sky_strength;
+    L.diffuse_light_intensity = f->diffuse_light_intensity;
+    return L;
+}
+
 // ------------------------------------------------------------- trace.cu --
 struct GBufferOut {
     void* t;            // storage type

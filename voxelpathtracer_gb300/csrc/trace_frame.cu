@@ -16,6 +16,8 @@
 //   * pixels are handed out in 8x4 tiles so the rays a warp starts together
 //     are coherent.
 // The grid is sized to fill every SM once (persistent blocks).
+#include <mutex>
+
 #include "dda.cuh"
 #include "kernels.cuh"
 
@@ -373,3 +375,114 @@ cudaError_t trace_frame(const FrameTraceArgs& a, int fp16, int blocks_hint, cuda
 }
 
 }  // namespace vpt
+
+// ------------------------------------------------- allocation-free variant --
+// For callers that cannot allocate device memory on the frame path: engines
+// that hand every byte of GPU memory out from a budget fixed at start-up, or
+// frame loops that cannot afford cudaMalloc's implicit device-wide
+// synchronisation. They pass all inputs and outputs; the only scratch the
+// kernel needs, its work-queue counter, lives in this fixed array instead of a
+// cudaMalloc'd buffer. Every process that loads libvpt holds these 256 bytes
+// on each GPU it uses until it exits.
+static constexpr int kNoAllocScratchInts = 64;   // 256 bytes; [0] is the work-queue counter
+static __device__ __align__(256) int g_noalloc_scratch[kNoAllocScratchInts];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+int* g_noalloc_ptr[kMaxDevices];   // device address of g_noalloc_scratch, per device
+std::mutex g_noalloc_mu;
+
+// Device address of the scratch array on the current device. Host code may
+// not use &g_noalloc_scratch (that is a host-side stand-in), so the address is
+// looked up once per device, with that device current.
+vpt_status noalloc_scratch(int** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return VPT_ERR_NO_DEVICE;
+    }
+    if (dev < 0 || dev >= kMaxDevices) return VPT_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return VPT_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = static_cast<int*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return VPT_OK;
+}
+
+}  // namespace
+
+extern "C" vpt_status vpt_trace_frame_noalloc(const vpt_trace_buffers* b, const vpt_config* cfg, const vpt_camera* cam,
+                                              const vpt_frame* f, void* stream) {
+    using namespace vpt;
+    if (!b || !cfg || !cam || !f) return VPT_ERR_INVALID_ARG;
+    if (!b->voxels || !b->df || !b->blocks || !b->t || !b->face || !b->block || !b->hit || !b->steps || !b->shadow ||
+        !b->gi_sh || !b->gi_cocg || !b->gi_luma || !b->gi_aosky)
+        return VPT_ERR_INVALID_ARG;
+    if (b->X <= 0 || b->Y <= 0 || b->Z <= 0 || (size_t)b->X * b->Y * b->Z > ((size_t)1 << 31) || b->n_blocks <= 0 ||
+        b->n_blocks > 256)
+        return VPT_ERR_INVALID_ARG;
+    // the work-queue counter indexes 8x4-pixel tiles * 32 entries in an int
+    if (cfg->width <= 0 || cfg->height <= 0 || cfg->width > 16384 || cfg->height > 16384) return VPT_ERR_INVALID_ARG;
+    if ((cfg->storage != VPT_STORAGE_F32 && cfg->storage != VPT_STORAGE_F16) || cfg->spp < 1 || cfg->spp > 32 ||
+        cfg->bounces < 0 || cfg->bounces > 8 || cfg->primary_max_steps < 0 || cfg->shadow_max_steps < 0 ||
+        cfg->diffuse_max_steps < 0 || cfg->bounce_shadow_max_steps < 0)
+        return VPT_ERR_INVALID_ARG;
+    int* scratch = nullptr;
+    vpt_status st = noalloc_scratch(&scratch);
+    if (st != VPT_OK) return st;
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    FrameTraceArgs a;
+    a.w.vox = b->voxels;
+    a.w.df = b->df;
+    a.w.X = b->X;
+    a.w.Y = b->Y;
+    a.w.Z = b->Z;
+    a.w.blocks = b->blocks;
+    a.w.n_blocks = b->n_blocks;
+    for (int k = 0; k < 16; k++) {
+        a.cam.inv_view[k] = cam->inv_view[k];
+        a.cam.inv_proj[k] = cam->inv_proj[k];
+    }
+    for (int k = 0; k < 3; k++) a.cam.pos[k] = cam->position[k];
+    a.W = cfg->width;
+    a.H = cfg->height;
+    a.tiles_x = (cfg->width + 7) / 8;
+    a.n_items = a.tiles_x * ((cfg->height + 3) / 4) * 32;
+    a.primary_max_steps = cfg->primary_max_steps;
+    a.shadow_max_steps = cfg->shadow_max_steps;
+    for (int k = 0; k < 3; k++) a.sun[k] = f->sun_dir[k];
+    a.refill_threshold = 16;
+    a.d.diffuse_max_steps = cfg->diffuse_max_steps;
+    a.d.bounce_shadow_max_steps = cfg->bounce_shadow_max_steps;
+    a.d.bounces = cfg->bounces;
+    a.d.spp = cfg->spp;
+    a.d.frame_index = f->frame_index;
+    a.d.seed = f->seed;
+    a.d.lighting = gi_lighting(f);
+    a.t = b->t;
+    a.face = b->face;
+    a.block = b->block;
+    a.hit = b->hit;
+    a.steps = b->steps;
+    a.shadow = b->shadow;
+    a.sh = b->gi_sh;
+    a.cocg = b->gi_cocg;
+    a.luma = b->gi_luma;
+    a.aosky = b->gi_aosky;
+    a.queue = scratch;
+    a.stats = nullptr;
+    // the array keeps the previous call's count: the counter must start at zero
+    if (cudaMemsetAsync(scratch, 0, sizeof(int), s) != cudaSuccess) {
+        cudaGetLastError();
+        return VPT_ERR_CUDA;
+    }
+    return trace_frame(a, cfg->storage == VPT_STORAGE_F16, 0, s) == cudaSuccess ? VPT_OK : VPT_ERR_CUDA;
+}
