@@ -293,6 +293,51 @@ def run_ours(args):
     e2e_t = dist.max(time.perf_counter() - t0)
     e2e_value = rays_total / e2e_t
     h2d = len(bytes(memoryview(vpt.Camera()))) + len(bytes(memoryview(vpt.Frame())))
+    last_rgb = {"fp32": out_np.copy()}
+
+    # 4) the FP16-storage variant on the same frames (device-resident timing)
+    variant = None
+    if not args.no_variants:
+        ctx16 = vpt.Context(width=W, height=H, device=local, storage=1)
+        ctx16.upload_world(vox)
+        ctx16.set_block_table(blocks)
+        ctx16.build_df()
+        s16 = torch.cuda.ExternalStream(ctx16.stream(), device=local)
+        t16 = []
+        with torch.cuda.stream(s16):
+            for s in range(total):
+                if s >= args.warmup:
+                    flush.zero_()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(s16)
+                rgb16 = ctx16.render_frame(camera_at(vpt, yaw, pitch, s), frame_at(vpt, s),
+                                           readback=(s == total - 1))
+                b.record(s16)
+                b.synchronize()
+                if s >= args.warmup:
+                    t16.append(a.elapsed_time(b))
+        last_rgb["fp16"] = rgb16
+        ctx16.close()
+        ms16 = dist.max(sum(t16) / 1e3) * 1e3 / args.steps
+        variant = {"fp16_storage": {"frame_ms": ms16, "value": rays_total / (ms16 * args.steps / 1e3),
+                                    "unit": "rays/s"}}
+
+    # 5) error against the FP64 ground truth of the last frame on the centre crop
+    quality_out = None
+    if not args.no_quality and rank == 0:
+        from voxelpathtracer_gb300 import quality
+        crop = quality.DEFAULT_CROP_1080P
+        t0 = time.perf_counter()
+        gt, se = quality.ground_truth_color(ctx, camera_at(vpt, yaw, pitch, total - 1), frame_at(vpt, total - 1),
+                                            crop, spp=args.gt_spp, chunk=256)
+        gt_s = time.perf_counter() - t0
+        x0, y0, cw, ch = crop
+        quality_out = {"crop": list(crop), "gt_spp": args.gt_spp, "gt_accumulation": "fp64 Welford",
+                       "gt_seconds": gt_s, "gt_luma_sh_stderr_mean": float(np.mean(se)),
+                       "frame": total - 1, "rmse": {}}
+        for k, img in last_rgb.items():
+            quality_out["rmse"][f"{k}_svgf"] = quality.rmse(img[y0:y0 + ch, x0:x0 + cw], gt)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -337,6 +382,8 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": per_launch_bytes,
                      "kernels": {KERNEL_NAMES[k]: v for k, v in kernels.items()}},
         "clocks": clk,
+        "variants": variant,
+        "quality": quality_out,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
@@ -442,6 +489,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="CPU work accumulated by the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true", help="skip the FP16-storage variant")
+    ap.add_argument("--no-quality", action="store_true", help="skip the ground-truth error measurement")
+    ap.add_argument("--gt-spp", type=int, default=4096, help="samples per pixel of the FP64 ground truth")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the dominant kernel from an ncu capture")
     args = ap.parse_args()

@@ -252,6 +252,17 @@ vpt_status vpt_reset_history(vpt_ctx* ctx);
  * first frame (the camera of the previous call is used otherwise). */
 vpt_status vpt_render_frame(vpt_ctx* ctx, const vpt_camera* cam, const vpt_frame* frame, float* rgb_out);
 
+/* High-spp ground truth of the diffuse GI over the crop [x0, x0+w) x [y0, y0+h)
+ * of the frame whose primary rays were traced last (fp32 contexts only): spp
+ * samples of the diffuse path per pixel (DiffuseRayTraceFrag.glsl:535-664),
+ * each on its own random stream derived from `seed`, accumulated per pixel
+ * with an FP64 Welford mean and M2 of SH (4), CoCg (2) and AO (1) in that
+ * channel order, in chunks of `chunk` samples merged in a fixed order.
+ * mean_out and m2_out receive w*h*7 doubles each (row-major crop). No
+ * counterpart in the reference (its quality reference is the screen). */
+vpt_status vpt_ground_truth(vpt_ctx* ctx, const vpt_frame* frame, int32_t x0, int32_t y0, int32_t w, int32_t h,
+                            int32_t spp, int32_t chunk, uint32_t seed, double* mean_out, double* m2_out);
+
 /* ---------------------------------------------------------------- planes -- */
 vpt_status vpt_plane_info(const vpt_ctx* ctx, int32_t plane, size_t* bytes, int32_t* channels, int32_t* dtype);
 vpt_status vpt_read_plane(vpt_ctx* ctx, int32_t plane, void* host, size_t bytes);

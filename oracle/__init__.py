@@ -88,6 +88,8 @@ def lib() -> C.CDLL:
         L.vpto_pow.restype = C.c_float
         L.vpto_omp_threads.restype = C.c_int
         L.vpto_set_counters.argtypes = [P]
+        L.vpto_ground_truth.argtypes = [P, P, P, P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        C.c_uint32, P, P]
         _lib = L
     return _lib
 
@@ -270,6 +272,19 @@ def shade(world: World, cam, config, frame, t, face, block, shadow, sh, cocg, ao
     lib().vpto_shade(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)),
                      *[_p(a) for a in arrs], r0, r1, _p(out))
     return out
+
+
+def ground_truth(world: World, cam, config, frame, t, face, crop, spp, chunk, seed=0x5eed):
+    """FP64 Welford mean and M2 (h, w, 7) of the diffuse GI over crop = (x0, y0, w, h)."""
+    p = params(config)
+    x0, y0, w, h = crop
+    mean = np.empty((h, w, 7), np.float64)
+    m2 = np.empty((h, w, 7), np.float64)
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    face = np.ascontiguousarray(face, dtype=np.uint8)
+    lib().vpto_ground_truth(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)),
+                            _p(t), _p(face), x0, y0, w, h, spp, chunk, seed, _p(mean), _p(m2))
+    return mean, m2
 
 
 def svgf(cam, prev_cam, config, frame, g: dict, prev_g: dict, gi: dict, hist: dict) -> dict:

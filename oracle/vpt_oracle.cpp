@@ -1167,4 +1167,76 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
     }
 }
 
+// High-spp ground truth of the diffuse GI over a crop: per pixel, `spp`
+// samples of CalculateDiffuse (DiffuseRayTraceFrag.glsl:535-664), each on its
+// own PCG stream, accumulated in float64 with Welford's update per chunk of
+// `chunk` samples, chunks merged in order with Chan et al.'s pairwise update.
+// Channels: SH (4), CoCg (2), AO.
+void vpto_ground_truth(const vpto_world* w, const vpto_camera* cam, const vpto_params* p, const vpto_frame* f,
+                       const float* t, const uint8_t* face, int x0, int y0, int cw, int ch, int spp, int chunk,
+                       uint32_t seed, double* mean_out, double* m2_out) {
+    const int W = p->width, H = p->height;
+    const v3 r0 = ray_origin(cam);
+    const Lighting L = frame_lighting(f);
+    const int nchunks = (spp + chunk - 1) / chunk;
+    const int CH = 7;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int q = 0; q < cw * ch; q++) {
+        const int i = x0 + q % cw, j = y0 + q / cw;
+        const size_t px = (size_t)j * W + i;
+        const v3 dir = normalize(ray_dir_at(cam, texcoord(i, j, W, H)));
+        const float d = t[px];
+        const v3 pos = add(r0, muls(dir, d));
+        const v3 nrm = normal_from_id(face[px], 0.5f);
+        RowCount cnt;
+        double n = 0.0, mean[7], m2[7];
+        for (int k = 0; k < CH; k++) mean[k] = m2[k] = 0.0;
+        for (int c = 0; c < nchunks; c++) {
+            double cn = 0.0, cmean[7], cm2[7];
+            for (int k = 0; k < CH; k++) cmean[k] = cm2[k] = 0.0;
+            const int k0 = c * chunk, k1 = std::min(spp, k0 + chunk);
+            for (int s = k0; s < k1; s++) {
+                float v[7], sh[4], cocg[2];
+                if (d < 0.0f) {
+                    irradiance_to_sh(muls(sky_radiance(dir), 2.66f), nrm, sh, cocg);
+                    v[6] = 1.0f;
+                } else {
+                    uint32_t rng = pcg_hash((uint32_t)px + pcg_hash((uint32_t)s + pcg_hash(seed ^ 0x9E3779B9u)));
+                    v3 odir = mk3(0, 0, 0);
+                    bool sky = false;
+                    v4 x = calculate_diffuse(w, p, f, L, pos, nrm, &rng, &odir, &sky, &cnt);
+                    irradiance_to_sh(vclamp(mk3(x.x, x.y, x.z), 0.0f, 8.0f), odir, sh, cocg);
+                    v[6] = x.w;
+                }
+                v[0] = sh[0]; v[1] = sh[1]; v[2] = sh[2]; v[3] = sh[3];
+                v[4] = cocg[0]; v[5] = cocg[1];
+                cn += 1.0;
+                for (int k = 0; k < CH; k++) {
+                    const double x = (double)v[k];
+                    const double delta = x - cmean[k];
+                    cmean[k] = cmean[k] + delta / cn;
+                    cm2[k] = cm2[k] + delta * (x - cmean[k]);
+                }
+            }
+            if (cn == 0.0) continue;
+            if (n == 0.0) {
+                n = cn;
+                for (int k = 0; k < CH; k++) { mean[k] = cmean[k]; m2[k] = cm2[k]; }
+                continue;
+            }
+            const double tot = n + cn;
+            for (int k = 0; k < CH; k++) {
+                const double delta = cmean[k] - mean[k];
+                mean[k] = mean[k] + delta * (cn / tot);
+                m2[k] = (m2[k] + cm2[k]) + (delta * delta) * ((n * cn) / tot);
+            }
+            n = tot;
+        }
+        for (int k = 0; k < CH; k++) {
+            mean_out[(size_t)q * CH + k] = mean[k];
+            m2_out[(size_t)q * CH + k] = m2[k];
+        }
+    }
+}
+
 }  // extern "C"

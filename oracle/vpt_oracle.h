@@ -153,6 +153,12 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
                 const uint8_t* shadow, const float* sh, const float* cocg, const float* aosky,
                 int row0, int row1, float* rgb);
 
+/* High-spp FP64 Welford ground truth of the diffuse GI over a crop
+ * (channels SH 4, CoCg 2, AO), as vpt_ground_truth computes it. */
+void vpto_ground_truth(const vpto_world* w, const vpto_camera* cam, const vpto_params* p, const vpto_frame* f,
+                       const float* t, const uint8_t* face, int x0, int y0, int cw, int ch, int spp, int chunk,
+                       uint32_t seed, double* mean_out, double* m2_out);
+
 /* Deterministic math, exported so tests can check its error bounds. */
 float vpto_exp(float x);
 float vpto_exp2(float x);

@@ -129,6 +129,7 @@ def _load() -> C.CDLL:
         "vpt_trace_frame_noalloc": ([C.POINTER(TraceBuffers), C.POINTER(Config), C.POINTER(Camera),
                                      C.POINTER(Frame), P], C.c_int),
         "vpt_set_tuning": ([P, C.POINTER(Tuning)], C.c_int),
+        "vpt_ground_truth": ([P, C.POINTER(Frame), i32, i32, i32, i32, i32, i32, C.c_uint32, P, P], C.c_int),
         "vpt_get_tuning": ([P, C.POINTER(Tuning)], C.c_int),
         "vpt_end_frame": ([P], C.c_int),
         "vpt_reset_history": ([P], C.c_int),
@@ -337,6 +338,17 @@ class Context:
         t = Tuning()
         self._ck(lib.vpt_get_tuning(self._h, C.byref(t)), "vpt_get_tuning")
         return t
+
+    def ground_truth(self, frame: Frame, crop, spp: int = 4096, chunk: int = 256, seed: int = 0x5eed):
+        """FP64 Welford mean and M2 of the diffuse GI (SH 4, CoCg 2, AO) over
+        crop = (x0, y0, w, h) of the frame whose primary rays were traced last.
+        Returns two (h, w, 7) float64 arrays."""
+        x0, y0, w, h = crop
+        mean = np.empty((h, w, 7), np.float64)
+        m2 = np.empty((h, w, 7), np.float64)
+        self._ck(lib.vpt_ground_truth(self._h, C.byref(frame), x0, y0, w, h, spp, chunk, seed, _ptr(mean),
+                                      _ptr(m2)), "vpt_ground_truth")
+        return mean, m2
 
     def end_frame(self):
         self._ck(lib.vpt_end_frame(self._h), "vpt_end_frame")

@@ -608,6 +608,66 @@ vpt_status vpt_trace_frame(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f
     return VPT_OK;
 }
 
+vpt_status vpt_ground_truth(vpt_ctx* c, const vpt_frame* f, int32_t x0, int32_t y0, int32_t w, int32_t h,
+                            int32_t spp, int32_t chunk, uint32_t seed, double* mean_out, double* m2_out) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (!f || !mean_out || !m2_out) return fail(c, VPT_ERR_INVALID_ARG, "frame and output buffers are required");
+    const int W = c->cfg.width, H = c->cfg.height;
+    if (x0 < 0 || y0 < 0 || w <= 0 || h <= 0 || x0 + w > W || y0 + h > H || spp < 1 || chunk < 1)
+        return fail(c, VPT_ERR_INVALID_ARG, "crop must lie inside the image, spp and chunk >= 1");
+    if (c->fp16) return fail(c, VPT_ERR_STATE, "the ground truth needs an fp32-storage context");
+    vpt_status s = check_world(c);
+    if (s != VPT_OK) return s;
+    if (!c->have_cam) return fail(c, VPT_ERR_STATE, "trace the primary rays of this frame first");
+    cudaSetDevice(c->dev);
+    const int nchunks = (spp + chunk - 1) / chunk;
+    const size_t npx = (size_t)w * h;
+    GroundTruthArgs a;
+    a.w = world_view(c);
+    a.cam = cam_view(c->cam);
+    a.W = W;
+    a.H = H;
+    a.d.diffuse_max_steps = c->cfg.diffuse_max_steps;
+    a.d.bounce_shadow_max_steps = c->cfg.bounce_shadow_max_steps;
+    a.d.bounces = c->cfg.bounces;
+    a.d.spp = 1;
+    a.d.frame_index = f->frame_index;
+    a.d.seed = f->seed;
+    a.d.lighting = gi_lighting(f);
+    a.t = (const float*)c->gbuf[c->cur][GB_T];
+    a.face = (const uint8_t*)c->gbuf[c->cur][GB_FACE];
+    a.x0 = x0;
+    a.y0 = y0;
+    a.cw = w;
+    a.ch = h;
+    a.spp = spp;
+    a.chunk = chunk;
+    a.nchunks = nchunks;
+    a.seed = seed;
+    void *part = nullptr, *mean = nullptr, *m2 = nullptr;
+    cudaError_t e = cudaMalloc(&part, npx * nchunks * 15 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&mean, npx * 7 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&m2, npx * 7 * sizeof(double));
+    if (e == cudaSuccess) {
+        a.part = (double*)part;
+        a.mean = (double*)mean;
+        a.m2 = (double*)m2;
+        e = ground_truth(a, c->stream);
+        c->launches += 2;
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(mean_out, mean, npx * 7 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(m2_out, m2, npx * 7 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(part);
+    cudaFree(mean);
+    cudaFree(m2);
+    if (e != cudaSuccess) {
+        return fail(c, e == cudaErrorMemoryAllocation ? VPT_ERR_OOM : VPT_ERR_CUDA, "ground truth: %s",
+                    cudaGetErrorString(e));
+    }
+    return VPT_OK;
+}
+
 vpt_status vpt_set_tuning(vpt_ctx* c, const vpt_tuning* t) {
     if (!c || !t) return VPT_ERR_INVALID_ARG;
     if (t->refill_threshold < 1 || t->refill_threshold > 32 || t->trace_blocks < 0 || t->trace_blocks > 65535 ||

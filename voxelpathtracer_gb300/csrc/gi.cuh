@@ -1,0 +1,85 @@
+// The diffuse GI path of one sample (CalculateDiffuse,
+// DiffuseRayTraceFrag.glsl:535-664), shared by the diffuse trace pass and the
+// ground-truth accumulator.
+#pragma once
+#include "dda.cuh"
+#include "kernels.cuh"
+
+namespace vpt {
+
+struct GICount {
+    unsigned diffuse_rays, diffuse_steps, shadow_rays, shadow_steps;
+};
+
+// CalculateDiffuse (DiffuseRayTraceFrag.glsl:535-664)
+__device__ __forceinline__ v4 calculate_diffuse(const WorldView& w, const DiffuseArgs& a, v3 initial_origin,
+                                                v3 input_normal, uint32_t* rng, v3* odir, bool* skyhit,
+                                                GICount* cnt) {
+    const GILighting& L = a.lighting;
+    const v3 light_dir = mk3(L.light_dir[0], L.light_dir[1], L.light_dir[2]);
+    const v3 light_color = mk3(L.light_color[0], L.light_color[1], L.light_color[2]);
+    *skyhit = false;
+    const float bias = 0.06f;
+    v3 ro = add(initial_origin, muls(input_normal, bias));
+    v3 rd = cos_hemisphere(input_normal, rng);
+    float ao = 1.0f;
+    v3 contribution = mk3(0.0f, 0.0f, 0.0f);
+    v3 throughput = mk3(1.0f, 1.0f, 1.0f);
+    for (int i = 0; i < a.bounces; i++) {
+        if (i == 0) *odir = rd;
+        TraceResult tr = traverse(w, ro, rd, a.diffuse_max_steps);
+        cnt->diffuse_rays += 1;
+        cnt->diffuse_steps += (unsigned)tr.steps;
+        float T = tr.t;
+        bool intersect = T > 0.0f;
+        v3 ip = add(ro, muls(rd, T));
+        if (intersect && tr.block > 0) {
+            Material m = material(w, min(max(tr.block, 0), 127));
+            v3 hn = tr.normal;
+            float emissivity = 0.0f;
+            if (m.emissive) emissivity = 1.0f * L.emissivity_multiplier * L.diffuse_light_intensity;
+            float ndl = fmaxf(dot(hn, light_dir), 0.0f);
+            v3 bias_shadow = muls(hn, 0.045f);
+            float shadow_at;
+            if (L.moon_stronger) {
+                shadow_at = 1.0f;
+            } else if (ndl < 0.001f) {
+                shadow_at = 0.0f;
+            } else {
+                // GetShadowAt (:1202-1222)
+                TraceResult sr = traverse(w, add(ip, bias_shadow), light_dir, a.bounce_shadow_max_steps);
+                cnt->shadow_rays += 1;
+                cnt->shadow_steps += (unsigned)sr.steps;
+                shadow_at = sr.t > 0.0f ? 1.0f : 0.0f;
+            }
+            v3 emissive_color = muls(m.albedo, emissivity * mixf(1.0f, 1.0f, L.sun_visibility));
+            float hs = diffuse_hammon(hn, neg(rd), light_dir, m.rough);
+            v3 sun_brdf = muls(muls(mul(muls(m.albedo, hs), muls(light_color, 3.5f)), 1.0f - shadow_at), kPI);
+            v3 new_dir = cos_hemisphere(hn, rng);
+            float cos_theta = clampf(dot(hn, new_dir), 0.0f, 1.0f);
+            float pdf = fmaxf(cos_theta / kPI, 0.00001f);
+            float att = diffuse_hammon(hn, neg(rd), new_dir, m.rough);
+            contribution = add(contribution, mul(throughput, sun_brdf));
+            contribution = add(contribution, mul(emissive_color, throughput));
+            throughput = mul(throughput, divs(muls(m.albedo, att), pdf));
+            rd = new_dir;
+            ro = add(ip, muls(hn, bias));
+        } else {
+            float x = mixf(1.0f, 1.05f, L.sun_visibility);
+            x = clampf(x * 1.0f * L.gi_sky_strength, 0.0f, 5.0f);
+            v3 sky = muls(sky_color_at(rd), x);
+            contribution = add(contribution, mul(sky, throughput));
+            *skyhit = true;
+            break;
+        }
+        if (i == 0) {
+            const float dao = 2.0f;
+            if (T < dao && T > 0.0f) ao = fmaxf(T / dao, 0.0f);
+        }
+    }
+    v4 r;
+    r.x = contribution.x; r.y = contribution.y; r.z = contribution.z; r.w = ao;
+    return r;
+}
+
+}  // namespace vpt

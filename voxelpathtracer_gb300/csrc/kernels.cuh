@@ -105,6 +105,24 @@ struct FrameTraceArgs {
 // blocks_hint <= 0 sizes the grid to fill every SM once.
 cudaError_t trace_frame(const FrameTraceArgs& a, int fp16, int blocks_hint, cudaStream_t s);
 
+// ------------------------------------------------------- groundtruth.cu --
+// FP64 Welford accumulation of `spp` diffuse samples over a crop (fp32 G-buffer).
+struct GroundTruthArgs {
+    WorldView w;
+    CamView cam;
+    int W, H;
+    DiffuseArgs d;
+    const float* t;
+    const uint8_t* face;
+    int x0, y0, cw, ch;      // crop
+    int spp, chunk, nchunks;
+    uint32_t seed;
+    double* part;            // cw*ch*nchunks records of (n, mean[7], m2[7])
+    double* mean;            // cw*ch*7
+    double* m2;              // cw*ch*7
+};
+cudaError_t ground_truth(const GroundTruthArgs& a, cudaStream_t s);
+
 // -------------------------------------------------------------- svgf.cu --
 struct GIIn {
     const void* sh;

@@ -1,0 +1,58 @@
+"""Image error against the FP64 ground truth.
+
+The ground truth of a frame is the converged output of this renderer: the
+primary and sun-shadow rays are deterministic, and the diffuse GI (SH, CoCg,
+AO) is replaced by its FP64 Welford mean over many samples
+(vpt_ground_truth); that mean goes through the same colour pass as a
+denoised frame. The error of a pipeline variant (plain fp32 SVGF, fp16
+storage, learned denoiser, ...) is the RMSE of its colour against that image
+on a crop, evaluated in float64.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import Context, Camera, Frame, default_config
+
+DEFAULT_CROP_1080P = (800, 450, 320, 180)   # centre 320x180 of a 1920x1080 frame
+
+
+def ground_truth_color(ctx: Context, cam: Camera, frame: Frame, crop, spp: int = 4096, chunk: int = 256,
+                       seed: int = 0x5eed):
+    """Colour of the converged frame on `crop`, with the per-pixel standard
+    error of the GI luminance channel. `ctx` must be an fp32 context with at
+    least one a-trous iteration and the world loaded."""
+    x0, y0, w, h = crop
+    ctx.trace_primary(cam)
+    ctx.trace_shadow(frame)
+    mean, m2 = ctx.ground_truth(frame, crop, spp=spp, chunk=chunk, seed=seed)
+    H, W = ctx.height, ctx.width
+    sh = np.zeros((H, W, 4), np.float32)
+    cocg = np.zeros((H, W, 2), np.float32)
+    ao = np.zeros((H, W, 2), np.float32)
+    sh[y0:y0 + h, x0:x0 + w] = mean[..., 0:4]
+    cocg[y0:y0 + h, x0:x0 + w] = mean[..., 4:6]
+    ao[y0:y0 + h, x0:x0 + w, 0] = mean[..., 6]
+    ctx.write_plane("DEN_SH", sh)
+    ctx.write_plane("DEN_COCG", cocg)
+    ctx.write_plane("DEN_AOSKY", ao)
+    ctx.shade(frame)
+    rgb = ctx.read_plane("COLOR")[y0:y0 + h, x0:x0 + w].astype(np.float64)
+    stderr = np.sqrt(m2[..., 3] / max(spp - 1, 1) / spp)
+    ctx.end_frame()
+    return rgb, stderr
+
+
+def rmse(a: np.ndarray, b: np.ndarray) -> float:
+    d = np.asarray(a, np.float64) - np.asarray(b, np.float64)
+    return float(np.sqrt(np.mean(d * d)))
+
+
+def make_gt_context(width: int, height: int, vox, blocks, **cfg) -> Context:
+    c = default_config(width=width, height=height, **cfg)
+    c.storage = 0
+    ctx = Context(c)
+    ctx.upload_world(vox)
+    ctx.set_block_table(blocks)
+    ctx.build_df()
+    return ctx
