@@ -60,8 +60,14 @@ typedef struct vpt_config {
     float resolution_scale;          /* u_ResolutionScale (DiffuseIndirectSuperSampleRes, :79) */
     float color_phi_bias;            /* ColorPhiBias = 3.325 (:85) */
     int32_t device;                  /* CUDA device ordinal */
-    int32_t reserved[3];
+    int32_t denoiser;                /* vpt_denoiser: USE_SVGF (Core/Pipeline.cpp:84) true or false */
+    int32_t reserved[2];
 } vpt_config;
+
+typedef enum vpt_denoiser {
+    VPT_DENOISER_SVGF = 0,           /* Core/Pipeline.cpp:2284-2615 (default) */
+    VPT_DENOISER_ATROUS = 1          /* temporal + 5x5 a-trous path, Core/Pipeline.cpp:2618-2786 */
+} vpt_denoiser;
 
 /* Camera uniforms: u_View, u_Projection, u_InverseView, u_InverseProjection
  * and u_ViewerPosition as Core/Pipeline.cpp sets them per pass. */

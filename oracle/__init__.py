@@ -40,7 +40,8 @@ class OParams(C.Structure):
                 ("shadow_max_steps", C.c_int32), ("diffuse_max_steps", C.c_int32),
                 ("bounce_shadow_max_steps", C.c_int32), ("bounces", C.c_int32), ("spp", C.c_int32),
                 ("storage", C.c_int32), ("atrous_iterations", C.c_int32), ("resolution_scale", C.c_float),
-                ("color_phi_bias", C.c_float), ("device", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class OWorld(C.Structure):
@@ -88,6 +89,9 @@ def lib() -> C.CDLL:
         L.vpto_pow.restype = C.c_float
         L.vpto_omp_threads.restype = C.c_int
         L.vpto_set_counters.argtypes = [P]
+        L.vpto_plain_temporal.argtypes = [P, P, P, P, P, P, P, P]
+        L.vpto_plain_variance.argtypes = [P, P, P]
+        L.vpto_plain_atrous.argtypes = [P, P, C.c_int, P, P, P, P, P, P, P, P, P]
         L.vpto_ground_truth.argtypes = [P, P, P, P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                         C.c_uint32, P, P]
         _lib = L
@@ -287,6 +291,36 @@ def ground_truth(world: World, cam, config, frame, t, face, crop, spp, chunk, se
     return mean, m2
 
 
+def plain_denoise(cam, prev_cam, config, g: dict, prev_g: dict, gi: dict, hist: dict) -> dict:
+    """The non-SVGF path (Core/Pipeline.cpp:2618-2786): temporal, variance and
+    5 a-trous iterations with steps 12, 8, 4, 2, 1."""
+    p = params(config)
+    H, W = p.height, p.width
+    f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)  # noqa: E731
+    cur = _f32(gi, ["sh", "cocg", "luma", "aosky"])
+    prev = _f32(hist, ["sh", "cocg", "util", "aosky"])
+    tmp = _planes(H, W, HIST_SPEC)
+    t, pt = f32(g["t"]), f32(prev_g["t"])
+    lib().vpto_plain_temporal(C.byref(_as(OCamera, cam)), C.byref(_as(OCamera, prev_cam)), C.byref(p), _p(t), _p(pt),
+                              C.byref(_struct4(cur, ["sh", "cocg", "luma", "aosky"])),
+                              C.byref(_struct4(prev, ["sh", "cocg", "util", "aosky"])),
+                              C.byref(_struct4(tmp, ["sh", "cocg", "util", "aosky"])))
+    var = np.zeros((H, W), np.float32)
+    lib().vpto_plain_variance(C.byref(p), _p(tmp["sh"]), _p(var))
+    face = np.ascontiguousarray(g["face"], np.uint8)
+    block = np.ascontiguousarray(g["block"], np.uint8)
+    sh, cocg, ao = tmp["sh"], tmp["cocg"], tmp["aosky"]
+    dens = []
+    for it in range(p.atrous_iterations):
+        step = (12, 8, 4, 2, 1)[it] if it < 5 else 1
+        o = _planes(H, W, {"sh": (4, np.float32), "cocg": (2, np.float32), "aosky": (2, np.float32)})
+        lib().vpto_plain_atrous(C.byref(_as(OCamera, cam)), C.byref(p), step, _p(t), _p(face), _p(block), _p(sh),
+                                _p(cocg), _p(ao), _p(o["sh"]), _p(o["cocg"]), _p(o["aosky"]))
+        dens.append(o)
+        sh, cocg, ao = o["sh"], o["cocg"], o["aosky"]
+    return {"temporal": tmp, "variance": var, "atrous": dens}
+
+
 def svgf(cam, prev_cam, config, frame, g: dict, prev_g: dict, gi: dict, hist: dict) -> dict:
     """Spatial3x3Initial, temporal, variance and the a-trous iterations, as
     Core/Pipeline.cpp:2284-2615 sequences them. Returns every intermediate."""
@@ -312,12 +346,17 @@ def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist:
     g = trace_primary(world, cam, p)
     shadow = trace_shadow(world, cam, p, frame, g["t"], g["face"])
     gi = trace_diffuse(world, cam, p, frame, g["t"], g["face"])
-    sv = svgf(cam, prev_cam, p, frame, g, prev_g, gi, hist)
-    if sv["atrous"]:
-        last = sv["atrous"][-1]
+    if p.denoiser == 1:
+        sv = plain_denoise(cam, prev_cam, p, g, prev_g, gi, hist)
+        last = sv["atrous"][-1] if sv["atrous"] else sv["temporal"]
         sh, cocg, ao = last["sh"], last["cocg"], last["aosky"]
     else:
-        sh, cocg, ao = sv["variance"]["sh"], sv["variance"]["cocg"], sv["temporal"]["aosky"]
+        sv = svgf(cam, prev_cam, p, frame, g, prev_g, gi, hist)
+        if sv["atrous"]:
+            last = sv["atrous"][-1]
+            sh, cocg, ao = last["sh"], last["cocg"], last["aosky"]
+        else:
+            sh, cocg, ao = sv["variance"]["sh"], sv["variance"]["cocg"], sv["temporal"]["aosky"]
     rgb = shade(world, cam, p, frame, g["t"], g["face"], g["block"], shadow, sh, cocg, ao)
     return {"g": g, "shadow": shadow, "gi": gi, "svgf": sv, "rgb": rgb}
 

@@ -1167,6 +1167,138 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
     }
 }
 
+// TemporalFilter.glsl main (:369-487) with u_DiffuseTemporal on and
+// u_ShadowTemporal off, u_MinimumMix 0 and u_MaximumMix 0.96 (the non-SVGF
+// path, Core/Pipeline.cpp:2618-2680). The shader writes colour (SH) and CoCg;
+// AO passes through and the utility plane is zero.
+void vpto_plain_temporal(const vpto_camera* cam, const vpto_camera* prev_cam, const vpto_params* p,
+                         const float* t, const float* prev_t, const vpto_gi* cur, const vpto_history* prev,
+                         vpto_history* out) {
+    const int W = p->width, H = p->height;
+    const int fp16 = p->storage;
+    const Plane T{t, W, H, 1}, PT{prev_t, W, H, 1}, PSH{prev->sh, W, H, 4}, PCC{prev->cocg, W, H, 2};
+    float m[16];
+    for (int c = 0; c < 4; c++)
+        for (int r = 0; r < 4; r++)
+            m[c * 4 + r] = ((prev_cam->proj[0 * 4 + r] * prev_cam->view[c * 4 + 0] +
+                             prev_cam->proj[1 * 4 + r] * prev_cam->view[c * 4 + 1]) +
+                            prev_cam->proj[2 * 4 + r] * prev_cam->view[c * 4 + 2]) +
+                           prev_cam->proj[3 * 4 + r] * prev_cam->view[c * 4 + 3];
+    const float min_mix = clampf(0.0f, 0.01f, 0.9f), max_mix = clampf(0.96f, 0.1f, 0.98f);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int j = 0; j < H; j++) {
+        for (int i = 0; i < W; i++) {
+            const size_t px = (size_t)j * W + i;
+            const v2 uv = texcoord(i, j, W, H);
+            const v4 bp = position_fetch(cam, T, i, j, uv);
+            float osh[4], occ[2];
+            for (int c = 0; c < 4; c++) osh[c] = cur->sh[px * 4 + c];
+            for (int c = 0; c < 2; c++) occ[c] = cur->cocg[px * 2 + c];
+            if (bp.w > 0.0f) {
+                const v4 pr = mat_mul4(m, bp.x, bp.y, bp.z, 1.0f);
+                const v2 rc = v2{(pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f};
+                float psh[4];
+                PSH.linear(rc, psh);
+                const v4 pp = position_linear(cam, PT, rc);
+                const float bias = 0.01f;
+                if (rc.x > 0.0f + bias && rc.x < 1.0f - bias && rc.y > 0.0f + bias && rc.y < 1.0f - bias) {
+                    const float d = std::fabs(length(sub(mk3(pp.x, pp.y, pp.z), mk3(bp.x, bp.y, bp.z))));
+                    if (!(d > 1.1f)) {
+                        float bf = dm_exp(-d);
+                        bf = clampf(bf, min_mix, max_mix);
+                        const float bfc = clampf(bf, 0.0f, 0.96f);
+                        float pcc[2];
+                        PCC.linear(rc, pcc);
+                        for (int c = 0; c < 4; c++) osh[c] = mixf(osh[c], psh[c], bfc);
+                        for (int c = 0; c < 2; c++) occ[c] = mixf(occ[c], pcc[c], bf);
+                    }
+                }
+            }
+            for (int c = 0; c < 4; c++) out->sh[px * 4 + c] = storage(osh[c], fp16);
+            for (int c = 0; c < 2; c++) out->cocg[px * 2 + c] = storage(occ[c], fp16);
+            for (int c = 0; c < 2; c++) out->aosky[px * 2 + c] = storage(cur->aosky[px * 2 + c], fp16);
+            for (int c = 0; c < 4; c++) out->util[px * 4 + c] = 0.0f;
+        }
+    }
+}
+
+// SampleVarianceCompute.glsl: 5x5 luminance variance of the temporal colour
+// (REPEAT wrap at the borders).
+void vpto_plain_variance(const vpto_params* p, const float* sh, float* variance) {
+    const int W = p->width, H = p->height;
+    const Plane SH{sh, W, H, 4};
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < H; j++) {
+        for (int i = 0; i < W; i++) {
+            float tx = 0.0f, ty = 0.0f;
+            int n = 0;
+            for (int a = -2; a <= 2; a++) {
+                for (int b = -2; b <= 2; b++) {
+                    const float l = luminance(mk3(SH.at(i + a, j + b, 0), SH.at(i + a, j + b, 1), SH.at(i + a, j + b, 2)));
+                    tx += l;
+                    ty += l * l;
+                    n++;
+                }
+            }
+            const float nn = fmaxg((float)n, 1.0f);
+            tx /= nn;
+            ty /= nn;
+            variance[(size_t)j * W + i] = storage(fmaxg(0.0f, ty - tx * tx), p->storage);
+        }
+    }
+}
+
+// AtrousSpatialFilter.glsl main (:96-220), one iteration with step `step`
+// (5x5 B3-spline taps). Its saturation / luminance / edge weights are computed
+// and then discarded by the shader (AdditionalWeight is reset to 1), so only
+// the position, normal, block and sky gates and the distance weight remain.
+void vpto_plain_atrous(const vpto_camera* cam, const vpto_params* p, int step, const float* t, const uint8_t* face,
+                       const uint8_t* block, const float* sh, const float* cocg, const float* aosky, float* out_sh,
+                       float* out_cocg, float* out_aosky) {
+    const int W = p->width, H = p->height;
+    const int fp16 = p->storage;
+    const Plane T{t, W, H, 1};
+    const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
+    const float weights[5] = {0.0625f, 0.25f, 0.375f, 0.25f, 0.0625f};
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int j = 0; j < H; j++) {
+        for (int i = 0; i < W; i++) {
+            const size_t px = (size_t)j * W + i;
+            const v2 uv = texcoord(i, j, W, H);
+            const v4 bp = position_fetch(cam, T, i, j, uv);
+            const v3 bn = normal_from_id(face[px], 1.0f);
+            const int bblock = std::min(std::max((int)block[px], 0), 127);
+            const bool bsky = bp.w < 0.0f;
+            float tc[4] = {0, 0, 0, 0}, t2[2] = {0, 0}, tw = 0.0f;
+            for (int tx = -2; tx <= 2; tx++) {
+                for (int ty = -2; ty <= 2; ty++) {
+                    const int ox = step * tx, oy = step * ty;
+                    const int si = i + ox, sj = j + oy;
+                    if (si < 0 || si >= W || sj < 0 || sj >= H) continue;
+                    const size_t sp_ = (size_t)sj * W + si;
+                    const v2 sc = v2{uv.x + (float)ox * texel_x, uv.y + (float)oy * texel_y};
+                    const v4 pa = position_fetch(cam, T, si, sj, sc);
+                    const v3 na = normal_from_id(face[sp_], 1.0f);
+                    const int ba = std::min(std::max((int)block[sp_], 0), 127);
+                    const float err = (std::fabs(pa.x - bp.x) + std::fabs(pa.y - bp.y)) + std::fabs(pa.z - bp.z);
+                    if (err < 4.25f && na.x == bn.x && na.y == bn.y && na.z == bn.z && ba == bblock &&
+                        (pa.w < 0.0f) == bsky) {
+                        const float dw = dm_pow(std::fabs(4.25f - err), 6.9f);
+                        const float wgt = (weights[tx + 2] * weights[ty + 2]) * dw;
+                        for (int c = 0; c < 4; c++) tc[c] += sh[sp_ * 4 + c] * wgt;
+                        for (int c = 0; c < 2; c++) t2[c] += cocg[sp_ * 2 + c] * wgt;
+                        tw += wgt;
+                    }
+                }
+            }
+            const float d = fmaxg(tw, 0.01f);
+            for (int c = 0; c < 4; c++) out_sh[px * 4 + c] = storage(tc[c] / d, fp16);
+            for (int c = 0; c < 2; c++) out_cocg[px * 2 + c] = storage(t2[c] / d, fp16);
+            for (int c = 0; c < 2; c++) out_aosky[px * 2 + c] = aosky[px * 2 + c];
+        }
+    }
+}
+
 // High-spp ground truth of the diffuse GI over a crop: per pixel, `spp`
 // samples of CalculateDiffuse (DiffuseRayTraceFrag.glsl:535-664), each on its
 // own PCG stream, accumulated in float64 with Welford's update per chunk of

@@ -64,7 +64,8 @@ typedef struct vpto_params {
     float resolution_scale;
     float color_phi_bias;
     int32_t device;
-    int32_t reserved[3];
+    int32_t denoiser;           /* 0 = SVGF, 1 = temporal + 5x5 a-trous */
+    int32_t reserved[2];
 } vpto_params;
 
 typedef struct vpto_world {
@@ -152,6 +153,17 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
                 const vpto_frame* f, const float* t, const uint8_t* face, const uint8_t* block,
                 const uint8_t* shadow, const float* sh, const float* cocg, const float* aosky,
                 int row0, int row1, float* rgb);
+
+/* The non-SVGF denoiser path (USE_SVGF off, Core/Pipeline.cpp:2618-2786):
+ * TemporalFilter.glsl (diffuse mode), SampleVarianceCompute.glsl and one
+ * AtrousSpatialFilter.glsl iteration. */
+void vpto_plain_temporal(const vpto_camera* cam, const vpto_camera* prev_cam, const vpto_params* p,
+                         const float* t, const float* prev_t, const vpto_gi* cur, const vpto_history* prev,
+                         vpto_history* out);
+void vpto_plain_variance(const vpto_params* p, const float* sh, float* variance);
+void vpto_plain_atrous(const vpto_camera* cam, const vpto_params* p, int step, const float* t, const uint8_t* face,
+                       const uint8_t* block, const float* sh, const float* cocg, const float* aosky, float* out_sh,
+                       float* out_cocg, float* out_aosky);
 
 /* High-spp FP64 Welford ground truth of the diffuse GI over a crop
  * (channels SH 4, CoCg 2, AO), as vpt_ground_truth computes it. */

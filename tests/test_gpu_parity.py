@@ -188,6 +188,31 @@ def test_render_frame_matches_oracle(vpt, oracle, scene, fused, gpu):
     ctx.close()
 
 
+@pytest.mark.parametrize("storage", [0, 1], ids=["f32", "f16"])
+def test_plain_atrous_path_bit_exact(vpt, oracle, scene, storage, gpu):
+    """The non-SVGF denoiser (temporal + 5x5 a-trous) over two frames."""
+    world = scene["world"]
+    ctx = vpt.Context(width=W, height=H, primary_max_steps=256, storage=storage, denoiser=vpt.DENOISER_ATROUS)
+    ctx.upload_world(scene["vox"])
+    ctx.set_block_table(scene["blocks"])
+    ctx.build_df()
+    cfg = ctx.config
+    prev_g, hist = oracle.empty_history(H, W)
+    prev_cam = scene["cams"][0]
+    for fi, cam in enumerate(scene["cams"]):
+        frame = vpt.default_frame(frame_index=fi, seed=5)
+        rgb = ctx.render_frame(cam, frame)
+        ref = oracle.render_frame(world, cam, prev_cam, cfg, frame, prev_g, hist)
+        tmp = ref["svgf"]["temporal"]
+        assert_same(ctx.read_plane("HIST_SH"), tmp["sh"], f"frame {fi} plain temporal sh")   # swapped by end_frame
+        assert_same(ctx.read_plane("HIST_COCG"), tmp["cocg"], f"frame {fi} plain temporal cocg")
+        assert_same(rgb, ref["rgb"], f"frame {fi} plain colour")
+        prev_g = {k: ref["g"][k] for k in ("t", "face", "block")}
+        hist = tmp
+        prev_cam = cam
+    ctx.close()
+
+
 def test_primary_steps_cap_and_inside_solid(vpt, oracle, scene, gpu):
     """A camera buried in stone misses everywhere (InitialRayTraceFrag.glsl:322-335);
     a tiny step cap truncates every ray at the cap."""

@@ -27,6 +27,7 @@ LIB_PATH = _PKG / "libvpt.so"
 # ------------------------------------------------------------------ enums --
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_DEVICE_TIMEOUT, ERR_CUDA, ERR_STATE, ERR_NO_DEVICE = range(7)
 STORAGE_F32, STORAGE_F16 = 0, 1
+DENOISER_SVGF, DENOISER_ATROUS = 0, 1
 DTYPE_F32, DTYPE_F16, DTYPE_U8, DTYPE_U16, DTYPE_I32 = range(5)
 _NP_DTYPE = {DTYPE_F32: np.float32, DTYPE_F16: np.float16, DTYPE_U8: np.uint8, DTYPE_U16: np.uint16,
              DTYPE_I32: np.int32}
@@ -53,7 +54,8 @@ class Config(C.Structure):
                 ("shadow_max_steps", C.c_int32), ("diffuse_max_steps", C.c_int32),
                 ("bounce_shadow_max_steps", C.c_int32), ("bounces", C.c_int32), ("spp", C.c_int32),
                 ("storage", C.c_int32), ("atrous_iterations", C.c_int32), ("resolution_scale", C.c_float),
-                ("color_phi_bias", C.c_float), ("device", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class Camera(C.Structure):

@@ -370,7 +370,8 @@ vpt_status vpt_create(vpt_ctx** out, const vpt_config* cfg) {
     if (cfg->storage != VPT_STORAGE_F32 && cfg->storage != VPT_STORAGE_F16) return VPT_ERR_INVALID_ARG;
     if (cfg->primary_max_steps < 0 || cfg->shadow_max_steps < 0 || cfg->diffuse_max_steps < 0 ||
         cfg->bounce_shadow_max_steps < 0 || cfg->bounces < 0 || cfg->bounces > 8 || cfg->spp < 1 ||
-        cfg->spp > 32 || cfg->atrous_iterations < 0 || cfg->atrous_iterations > 8)
+        cfg->spp > 32 || cfg->atrous_iterations < 0 || cfg->atrous_iterations > 8 ||
+        (cfg->denoiser != VPT_DENOISER_SVGF && cfg->denoiser != VPT_DENOISER_ATROUS))
         return VPT_ERR_INVALID_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
@@ -694,6 +695,35 @@ vpt_status vpt_svgf(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f) 
     const void* t = c->gbuf[cur][GB_T];
     const uint8_t* face = (const uint8_t*)c->gbuf[cur][GB_FACE];
     const uint8_t* block = (const uint8_t*)c->gbuf[cur][GB_BLOCK];
+    if (c->cfg.denoiser == VPT_DENOISER_ATROUS) {
+        // the non-SVGF path (Core/Pipeline.cpp:2618-2786)
+        TemporalArgs ta;
+        for (int col = 0; col < 4; col++)
+            for (int r = 0; r < 4; r++)
+                ta.prev_view_proj[col * 4 + r] = ((pc.proj[0 * 4 + r] * pc.view[col * 4 + 0] +
+                                                   pc.proj[1 * 4 + r] * pc.view[col * 4 + 1]) +
+                                                  pc.proj[2 * 4 + r] * pc.view[col * 4 + 2]) +
+                                                 pc.proj[3 * 4 + r] * pc.view[col * 4 + 3];
+        ta.be_useful = f->temporal ? 1 : 0;
+        PlainDenoiseIO io;
+        io.t = t;
+        io.prev_t = c->gbuf[prv][GB_T];
+        io.face = face;
+        io.block = block;
+        io.cur = GIIn{c->gi[GI_SH], c->gi[GI_COCG], c->gi[GI_LUMA], c->gi[GI_AOSKY]};
+        io.prev = HistIO{c->hist[prv][HI_SH], c->hist[prv][HI_COCG], c->hist[prv][HI_UTIL], c->hist[prv][HI_AOSKY]};
+        io.temporal = HistIO{c->hist[cur][HI_SH], c->hist[cur][HI_COCG], c->hist[cur][HI_UTIL], c->hist[cur][HI_AOSKY]};
+        io.variance = c->var[FI_VAR];
+        for (int k = 0; k < 2; k++)
+            io.out[k] = FiltIO{c->den[k][FI_SH], c->den[k][FI_COCG], c->den[k][FI_VAR], c->den[k][FI_AOSKY]};
+        io.iterations = c->cfg.atrous_iterations;
+        pass_begin(c, VPT_PASS_ATROUS);
+        CK(c, plain_denoise(cv, W, H, c->fp16, ta, io, c->stream));
+        pass_end(c, VPT_PASS_ATROUS);
+        if (io.iterations > 0) c->den_last = (io.iterations - 1) & 1;
+        c->launches += 2 + (uint64_t)io.iterations;
+        return VPT_OK;
+    }
     // Spatial3x3Initial (Core/Pipeline.cpp:2288-2330)
     pass_begin(c, VPT_PASS_SPATIAL_INITIAL);
     CK(c, svgf_spatial_initial(cv, W, H, c->fp16, t, face, GIIn{c->gi[GI_SH], c->gi[GI_COCG], c->gi[GI_LUMA], c->gi[GI_AOSKY]},
@@ -769,8 +799,11 @@ vpt_status vpt_shade(vpt_ctx* c, const vpt_frame* f) {
     }
     float sv = clampf(dot(sun, mk3(0.0f, 1.0f, 0.0f)) + 0.05f, 0.0f, 0.1f) * 12.0f;
     a.sun_vis = 1.0f - sv;
-    const void* sh = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_SH] : c->var[FI_SH];
-    const void* cocg = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_COCG] : c->var[FI_COCG];
+    const bool plain = c->cfg.denoiser == VPT_DENOISER_ATROUS;
+    const void* sh = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_SH]
+                                                  : (plain ? c->hist[c->cur][HI_SH] : c->var[FI_SH]);
+    const void* cocg = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_COCG]
+                                                    : (plain ? c->hist[c->cur][HI_COCG] : c->var[FI_COCG]);
     const void* ao = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_AOSKY] : c->hist[c->cur][HI_AOSKY];
     pass_begin(c, VPT_PASS_SHADE);
     CK(c, shade(world_view(c), cam_view(c->cam), c->cfg.width, c->cfg.height, c->fp16, a, c->gbuf[c->cur][GB_T],

@@ -34,8 +34,8 @@ __device__ __forceinline__ int vox_index(const WorldView& w, int x, int y, int z
     return x + w.X * (y + w.Y * z);
 }
 __device__ __forceinline__ bool in_volume(const WorldView& w, int x, int y, int z) {
-    // IsInVolume (InitialRayTraceFrag.glsl:68-77)
-    return !(x < 0 || y < 0 || z < 0 || x > w.X - 1 || y > w.Y - 1 || z > w.Z - 1);
+    // IsInVolume (InitialRayTraceFrag.glsl:68-77): 0 <= x <= X-1, ... as unsigned compares
+    return (unsigned)x < (unsigned)w.X && (unsigned)y < (unsigned)w.Y && (unsigned)z < (unsigned)w.Z;
 }
 __device__ __forceinline__ int get_voxel(const WorldView& w, int x, int y, int z) {
     // GetVoxel (InitialRayTraceFrag.glsl:79-87)
@@ -201,7 +201,7 @@ struct Plane8 {
     __device__ __forceinline__ int at_in(int i, int j) const { return __ldg(p + (size_t)j * W + i); }
     // texture() with GL_NEAREST and GL_REPEAT
     __device__ __forceinline__ int nearest(v2 uv) const {
-        return at(f2i(floorf(uv.x * (float)W)), f2i(floorf(uv.y * (float)H)));
+        return at(f2i_floor(uv.x * (float)W), f2i_floor(uv.y * (float)H));
     }
 };
 

@@ -15,7 +15,7 @@ namespace vpt {
 __device__ __forceinline__ int euclid_steps(int dist) {
     float D = (float)dist;
     float e = (D == 1.0f) ? 1.0f : D * 0.57735026918f;
-    return f2i(floorf(e));
+    return f2i_floor(e);
 }
 
 struct RayState {
@@ -53,9 +53,9 @@ __device__ __forceinline__ void ray_start(RayState& r, v3 origin, v3 dir, int ma
 // One iteration of the traversal loop; returns true once the loop is over.
 __device__ __forceinline__ bool dda_step(const WorldView& w, RayState& r) {
     if (r.itr >= r.max_steps) return true;
-    const int lx = f2i(floorf(r.o.x));
-    const int ly = f2i(floorf(r.o.y));
-    const int lz = f2i(floorf(r.o.z));
+    const int lx = f2i_floor(r.o.x);
+    const int ly = f2i_floor(r.o.y);
+    const int lz = f2i_floor(r.o.z);
     if (!in_volume(w, lx, ly, lz)) {
         r.inter = 0;
         return true;
@@ -101,9 +101,9 @@ __device__ __forceinline__ bool dda_step(const WorldView& w, RayState& r) {
 // The code after the loop (:365-373).
 __device__ __forceinline__ TraceResult ray_finish(const WorldView& w, const RayState& r) {
     TraceResult t;
-    t.cell[0] = f2i(floorf(r.o.x));
-    t.cell[1] = f2i(floorf(r.o.y));
-    t.cell[2] = f2i(floorf(r.o.z));
+    t.cell[0] = f2i_floor(r.o.x);
+    t.cell[1] = f2i_floor(r.o.y);
+    t.cell[2] = f2i_floor(r.o.z);
     t.steps = r.itr;
     t.normal = mk3(0.0f, 0.0f, 0.0f);
     t.block = 0;

@@ -165,6 +165,25 @@ cudaError_t svgf_atrous(const CamView& cam, int W, int H, int fp16, const Atrous
                         const void* t, const uint8_t* face, const void* temporal_util,
                         FiltIO in, const void* in_aosky, FiltIO out, cudaStream_t s);
 
+// ------------------------------------------------------ plain_filter.cu --
+// The non-SVGF path: temporal -> variance -> `iterations` a-trous passes
+// ping-ponging between out[0] and out[1] (the last one lands in
+// out[(iterations - 1) & 1]).
+struct PlainDenoiseIO {
+    const void* t;
+    const void* prev_t;
+    const uint8_t* face;
+    const uint8_t* block;
+    GIIn cur;          // raw GI planes
+    HistIO prev;       // last frame's temporal output (sh, cocg used)
+    HistIO temporal;   // this frame's temporal output
+    void* variance;
+    FiltIO out[2];
+    int iterations;
+};
+cudaError_t plain_denoise(const CamView& cam, int W, int H, int fp16, const TemporalArgs& ta,
+                          const PlainDenoiseIO& io, cudaStream_t s);
+
 // ------------------------------------------------------------- shade.cu --
 struct ShadeArgs {
     float sun[3], moon[3];

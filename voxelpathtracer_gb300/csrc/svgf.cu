@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, cons
 // the centre is not sky (DepthDiff = abs(...) >= 0); sky centres keep their
 // own values, so their tap loop is skipped.
 template <typename S>
-__global__ void __launch_bounds__(256) k_atrous(int W, int H, AtrousArgs a, const S* t, const uint8_t* face,
+__global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, AtrousArgs a, const S* t, const uint8_t* face,
                                                 const S* t_util, const S* i_sh, const S* i_cocg, const S* i_var,
                                                 const S* i_aosky, S* o_sh, S* o_cocg, S* o_var, S* o_aosky) {
     int i, j;

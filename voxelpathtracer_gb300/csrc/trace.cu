@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(256) k_trace_shadow(WorldView w, CamView cam, 
                 out = 1;
             } else {
                 v3 o = add(pos, mul(n, mk3(0.06f, 0.06f, 0.06f)));
-                int block_at = get_voxel(w, f2i(floorf(o.x)), f2i(floorf(o.y)), f2i(floorf(o.z)));
+                int block_at = get_voxel(w, f2i_floor(o.x), f2i_floor(o.y), f2i_floor(o.z));
                 float T = -1.0f;
                 if (d > 0.0f) {
                     TraceResult r = traverse(w, o, L, max_steps);

@@ -256,7 +256,7 @@ struct Engine {
                 return;
             }
             const v3 o = add(ln.pos, mul(n, mk3(0.06f, 0.06f, 0.06f)));
-            ln.block_at = get_voxel(a.w, f2i(floorf(o.x)), f2i(floorf(o.y)), f2i(floorf(o.z)));
+            ln.block_at = get_voxel(a.w, f2i_floor(o.x), f2i_floor(o.y), f2i_floor(o.z));
             if (d > 0.0f) {
                 ray_start(ray, o, L, a.shadow_max_steps);
                 ln.phase = PH_SUN;

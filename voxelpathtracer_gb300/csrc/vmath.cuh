@@ -48,12 +48,26 @@ VPT_HD bool is_nan(float x) { return x != x; }
 VPT_HD float inf_f() { return f_from_bits(0x7f800000u); }
 VPT_HD float nan_f() { return f_from_bits(0x7fc00000u); }
 
-// float -> int32, round toward zero, NaN -> 0, saturating.
+// float -> int32, round toward zero, NaN -> 0, saturating. On the device this
+// is exactly the cvt.rzi.s32.f32 conversion (PTX float-to-integer conversions
+// saturate and map NaN to 0), on the host it is spelled out.
 VPT_HD int32_t f2i(float x) {
+#ifdef __CUDA_ARCH__
+    return __float2int_rz(x);
+#else
     if (x != x) return 0;
     if (x >= 2147483648.0f) return 2147483647;
     if (x < -2147483648.0f) return (-2147483647 - 1);
     return (int32_t)x;
+#endif
+}
+// f2i(floor(x)) in one conversion (round toward minus infinity).
+VPT_HD int32_t f2i_floor(float x) {
+#ifdef __CUDA_ARCH__
+    return __float2int_rd(x);
+#else
+    return f2i(floorf(x));
+#endif
 }
 
 VPT_HD float pow2i(int n) { return f_from_bits((uint32_t)(n + 127) << 23); }
