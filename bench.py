@@ -66,47 +66,11 @@ def log(*a):
 
 
 def dist_env():
+    """RANK / WORLD_SIZE / LOCAL_RANK (read here too, so the reference arm needs no import of the package)."""
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", str(rank)))
     return rank, world, local
-
-
-class Dist:
-    """Barrier and max-reduction over replicas (gloo over TCP; no data-path collective)."""
-
-    def __init__(self, world):
-        self.world = world
-        self.pg = None
-        if world > 1:
-            import torch.distributed as td
-            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-            td.init_process_group("gloo")
-            self.td = td
-
-    def barrier(self):
-        if self.world > 1:
-            self.td.barrier()
-
-    def max(self, v: float) -> float:
-        if self.world == 1:
-            return v
-        import torch
-        t = torch.tensor([v], dtype=torch.float64)
-        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
-        return float(t.item())
-
-    def sum(self, v: float) -> float:
-        if self.world == 1:
-            return v
-        import torch
-        t = torch.tensor([v], dtype=torch.float64)
-        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
-        return float(t.item())
-
-    def close(self):
-        if self.world > 1:
-            self.td.destroy_process_group()
 
 
 class ClockSampler:
@@ -195,7 +159,8 @@ def run_ours(args):
     torch.cuda.set_device(local)
     import voxelpathtracer_gb300 as vpt
 
-    dist = Dist(world)
+    from voxelpathtracer_gb300.replicas import Replicas
+    dist = Replicas(world)
     W, H = RES
     vox, blocks, yaw, pitch = workload_inputs(vpt, seed=rank)
     ctx = vpt.Context(width=W, height=H, device=local, storage=args.storage)

@@ -369,16 +369,20 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, AtrousArgs a, c
                 const float ox = ((float)x * (float)step) * a.add_scale + jo;
                 const float oy = ((float)y * (float)step) * a.add_scale + jo;
                 const v2 sc = mk2(uv.x + ox * texel_x, uv.y + oy * texel_y);
-                if (!(sc.x > 0.0f && sc.x < 1.0f && sc.y > 0.0f && sc.y < 1.0f)) continue;
+                // loads first (the wrapped footprint is always a valid address),
+                // so the unrolled taps' loads can all be in flight together
                 const Bilin fp = bilin(sc, W, H);
                 const float sd = bl1(t, fp);
-                const float dd = fabsf(sd - bd);
-                const v3 sn = normal_from_id(F.nearest(sc), 1.0f);
+                const int sface = F.nearest(sc);
                 const float4 s4 = bl4(i_sh, fp);
                 const float2 s2 = bl2(i_cocg, fp);
+                const float sv = bl1(i_var, fp);
+                const float2 sao = (filter_sky || filter_ao) ? bl2(i_aosky, fp) : make_float2(0.0f, 0.0f);
+                if (!(sc.x > 0.0f && sc.x < 1.0f && sc.y > 0.0f && sc.y < 1.0f)) continue;
+                const float dd = fabsf(sd - bd);
+                const v3 sn = normal_from_id(sface, 1.0f);
                 const float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
                 const float sl = sh_to_y(ssh);
-                const float sv = bl1(i_var, fp);
                 const float nw = clampf(dpow(fmaxf(dot(bn, sn), 0.0f), 32.0f), 0.001f, 1.0f);
                 const float lw = fabsf(sl - bl) / phi;
                 const float dw = clampf(dpow(dexp(-fmaxf(dd, 0.00001f)), 2.0f), 0.0001f, 1.0f);
@@ -397,7 +401,6 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, AtrousArgs a, c
                 tw += wgt;
                 if (filter_sky || filter_ao) {
                     const float awt = clampf(((xw * yw) * nw) * dw, 0.000001f, 1.0f);
-                    const float2 sao = bl2(i_aosky, fp);
                     tao[0] += sao.x * awt;
                     tao[1] += sao.y * awt;
                     taow += awt;
