@@ -304,6 +304,10 @@ def run_ours(args):
         for k, img in last_rgb.items():
             quality_out["rmse"][f"{k}_svgf"] = quality.rmse(img[y0:y0 + ch, x0:x0 + cw], gt)
 
+    batched = None
+    if not args.no_batch:
+        batched = batched_section(vpt, torch, args, local, flush)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(vpt, args, vox, blocks, yaw, pitch, sample_rows=args.cpu_rows)
@@ -349,9 +353,92 @@ def run_ours(args):
         "clocks": clk,
         "variants": variant,
         "quality": quality_out,
+        "batched": batched,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------- batched worlds --
+BATCH_EDGES = (64, 96, 128, 192, 256)
+
+
+def batch_worlds(n=64, seed=0):
+    """n worlds, each edge uniform in BATCH_EDGES, each ray tile uniform between
+    256x256 and 1024x576, cameras above the terrain with seeded yaw/pitch."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        X, Y, Z = (int(e) for e in rng.choice(BATCH_EDGES, 3))
+        W, H = int(rng.integers(256, 1025)), int(rng.integers(256, 577))
+        out.append({"dims": (X, Y, Z), "tile": (W, H), "seed": 1000 + k})
+    return out
+
+
+def batched_section(vpt, torch, args, local, flush):
+    """One persistent launch over 64 uneven worlds (graph replay and direct)
+    against the plain path's three pass kernels per world, same rays."""
+    specs = batch_worlds(64, seed=0)
+    b = vpt.Batch(max_worlds=len(specs), device=local)
+    for k, sp in enumerate(specs):
+        X, Y, Z = sp["dims"]
+        W, H = sp["tile"]
+        vox = vpt.generate_world(X, Y, Z, seed=sp["seed"])
+        blocks = vpt.generate_block_table(100, seed=sp["seed"])
+        yaw, pitch = vpt.seeded_pose(sp["seed"])
+        b.add_world(vox, blocks, W, H)
+        b.set_camera(k, vpt.camera_from_pose((X / 2, min(Y - 3.0, 90.0), Z / 2), yaw, pitch, 90.0, W / H))
+    b.build_df()
+    frame = vpt.default_frame(frame_index=1, seed=0)
+    b.set_stats(True)
+    b.trace(frame, vpt.BATCH_PER_WORLD)
+    st = b.read_stats()
+    b.set_stats(False)
+    rays = sum(st["rays"].values())
+    t0 = time.perf_counter()
+    recs = b.autotune(frame, reps=3)
+    tune_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(b.stream(), device=local)
+    steps = max(3, min(args.steps, 10))
+    out = {}
+    with torch.cuda.stream(stream):
+        for name, mode in (("graph", vpt.BATCH_GRAPH), ("persistent", vpt.BATCH_PERSISTENT),
+                           ("per_world", vpt.BATCH_PER_WORLD)):
+            for _ in range(3):
+                b.trace(frame, mode)
+            torch.cuda.synchronize()
+            l0 = b.launch_count()
+            ms = []
+            for _ in range(steps):
+                flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                b.trace(frame, mode)
+                e1.record(stream)
+                e1.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            host_launches = (b.launch_count() - l0) / steps
+            med = float(statistics.median(ms))
+            out[name] = {"ms": med, "rays_per_s": rays / (med * 1e-3), "host_launch_calls_per_step": host_launches}
+    tiles = [sp["tile"] for sp in specs]
+    res = {
+        "worlds": len(specs),
+        "world_edges": BATCH_EDGES,
+        "rays_per_step": rays,
+        "rays_by_kind": st["rays"],
+        "pixels": int(sum(w * h for w, h in tiles)),
+        "modes": out,
+        "speedup_graph_vs_per_world": out["per_world"]["ms"] / out["graph"]["ms"],
+        "autotuned": b.tuning().as_dict(),
+        "autotune_candidates": len(recs),
+        "autotune_seconds": tune_s,
+        "autotune_worst_ms": max(r["ms"] for r in recs),
+        "per_world_kernels_per_step": 3 * len(specs),
+        "timing": f"median of {steps} steps, L2 flushed between steps",
+    }
+    b.close()
+    return res
 
 
 # ------------------------------------------------------- CPU (oracle) arm --
@@ -456,6 +543,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the FP16-storage variant")
     ap.add_argument("--no-quality", action="store_true", help="skip the ground-truth error measurement")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-world batched comparison")
     ap.add_argument("--gt-spp", type=int, default=4096, help="samples per pixel of the FP64 ground truth")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the dominant kernel from an ncu capture")

@@ -292,6 +292,88 @@ vpt_status vpt_get_stream(const vpt_ctx* ctx, void** stream);
  * caller check that both give identical bits. y is only read for pow. */
 vpt_status vpt_detmath(int32_t op, const float* x, const float* y, float* out, int32_t n, int32_t on_device);
 
+/* -------------------------------------------------------- batched worlds --
+ * Many independent worlds traced together. The reference renders one World
+ * per process (Core/Pipeline.cpp's frame loop over one World, Core/World.h:193-199);
+ * a batch holds many such worlds, each with its own volume, distance field,
+ * block table, camera and ray tile, and traces the primary, sun-shadow and
+ * one diffuse bounce (with its shadow ray) of every world in one persistent
+ * launch. Per world, the planes are bit-identical to vpt_trace_primary /
+ * vpt_trace_shadow / vpt_trace_diffuse of a context holding that world alone.
+ * All planes are float32 (no FP16 storage in a batch). */
+typedef struct vpt_batch vpt_batch;
+
+typedef struct vpt_batch_config {
+    int32_t device;
+    int32_t max_worlds;              /* 1..1024 */
+    int32_t primary_max_steps;       /* same meaning as in vpt_config */
+    int32_t shadow_max_steps;
+    int32_t diffuse_max_steps;
+    int32_t bounce_shadow_max_steps;
+    int32_t bounces;                 /* 0..8 */
+    int32_t spp;                     /* 1..32 */
+    int32_t reserved[4];
+} vpt_batch_config;
+
+/* Launch shape of the persistent batch kernel (vpt_batch_autotune picks it). */
+typedef struct vpt_batch_tuning {
+    int32_t block_threads;           /* 64..512, a multiple of 32 */
+    int32_t tiles_per_grab;          /* 8x4-pixel tiles a warp takes per queue access, 1..16 (rays per warp = 32 x this) */
+    int32_t df_brick;                /* distance-field layout traced: 0 x-fastest, 4 or 8 = B^3-voxel bricks */
+    int32_t blocks;                  /* persistent blocks; 0 = every SM filled to its occupancy limit */
+    int32_t reserved[4];
+} vpt_batch_tuning;
+
+typedef struct vpt_batch_tune_record {
+    vpt_batch_tuning tuning;
+    float ms;                        /* median device time of one persistent launch */
+    float pad;
+} vpt_batch_tune_record;
+
+typedef enum vpt_batch_mode {
+    VPT_BATCH_GRAPH = 0,             /* the persistent launch, replayed from a captured CUDA graph */
+    VPT_BATCH_PERSISTENT = 1,        /* the persistent launch, launched directly */
+    VPT_BATCH_PER_WORLD = 2          /* three pass kernels per world (the plain path), for comparison */
+} vpt_batch_mode;
+
+/* Batch planes (vpt_batch_read_plane) reuse the vpt_plane ids T, FACE, BLOCK,
+ * HIT, STEPS, SHADOW, GI_SH, GI_COCG, GI_LUMA and GI_AOSKY. */
+vpt_status vpt_batch_default_config(vpt_batch_config* cfg);
+vpt_status vpt_batch_create(vpt_batch** out, const vpt_batch_config* cfg);
+vpt_status vpt_batch_destroy(vpt_batch* batch);
+const char* vpt_batch_last_error(const vpt_batch* batch);
+/* Adds a world (x-fastest voxels, each edge 1..1024) with its block table
+ * (1..256 entries) and a width x height ray tile (each 1..4096); returns its
+ * index in *world_id. Invalidates the distance fields of the batch. */
+vpt_status vpt_batch_add_world(vpt_batch* batch, const uint8_t* voxels, int32_t X, int32_t Y, int32_t Z,
+                               const vpt_block* table, int32_t n_blocks, int32_t width, int32_t height,
+                               int32_t* world_id);
+vpt_status vpt_batch_set_camera(vpt_batch* batch, int32_t world, const vpt_camera* cam);
+/* Distance fields of every world (World::GenerateDistanceField per world), in
+ * the x-fastest layout and in the brick layout the tuning selects. */
+vpt_status vpt_batch_build_df(vpt_batch* batch);
+/* Copies world `world`'s x-fastest distance field out (X*Y*Z bytes). */
+vpt_status vpt_batch_read_df(vpt_batch* batch, int32_t world, uint8_t* host, size_t bytes);
+vpt_status vpt_batch_set_tuning(vpt_batch* batch, const vpt_batch_tuning* tuning);
+vpt_status vpt_batch_get_tuning(const vpt_batch* batch, vpt_batch_tuning* tuning);
+/* Traces every world with its camera. Stream-ordered; returns without waiting. */
+vpt_status vpt_batch_trace(vpt_batch* batch, const vpt_frame* frame, int32_t mode);
+/* Times every candidate launch shape (block_threads 128/256/512 x
+ * tiles_per_grab 1/2/4 x df_brick 0/4/8) on the batch as it stands, `reps`
+ * timed launches each after one warm-up, keeps the fastest as the batch's
+ * tuning and writes up to max_records records (all candidates, in the order
+ * tried). Synchronises. */
+vpt_status vpt_batch_autotune(vpt_batch* batch, const vpt_frame* frame, int32_t reps, vpt_batch_tune_record* records,
+                              int32_t max_records, int32_t* n_records);
+vpt_status vpt_batch_read_plane(vpt_batch* batch, int32_t world, int32_t plane, void* host, size_t bytes);
+vpt_status vpt_batch_world_info(const vpt_batch* batch, int32_t world, int32_t dims[3], int32_t tile[2]);
+vpt_status vpt_batch_count(const vpt_batch* batch, int32_t* n_worlds);
+vpt_status vpt_batch_synchronize(vpt_batch* batch);
+vpt_status vpt_batch_set_stats(vpt_batch* batch, int32_t enabled);
+vpt_status vpt_batch_read_stats(vpt_batch* batch, vpt_stats* out);   /* synchronises, then zeroes */
+vpt_status vpt_batch_launch_count(const vpt_batch* batch, uint64_t* out);
+vpt_status vpt_batch_get_stream(const vpt_batch* batch, void** stream);
+
 /* ---------------------------------------------------------- host helpers -- */
 /* Seeded value-noise terrain (heightmap h = 40 + 16*fbm, 4 octaves, base
  * frequency 1/64, gain 0.5; grass top, three dirt layers, stone below) with

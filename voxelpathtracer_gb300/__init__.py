@@ -92,6 +92,30 @@ class Tuning(C.Structure):
                 ("reserved", C.c_int32 * 5)]
 
 
+class BatchConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_worlds", C.c_int32), ("primary_max_steps", C.c_int32),
+                ("shadow_max_steps", C.c_int32), ("diffuse_max_steps", C.c_int32),
+                ("bounce_shadow_max_steps", C.c_int32), ("bounces", C.c_int32), ("spp", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("block_threads", C.c_int32), ("tiles_per_grab", C.c_int32), ("df_brick", C.c_int32),
+                ("blocks", C.c_int32), ("reserved", C.c_int32 * 4)]
+
+    def as_dict(self) -> dict:
+        return {"block_threads": self.block_threads, "tiles_per_grab": self.tiles_per_grab,
+                "rays_per_warp": 32 * self.tiles_per_grab, "df_brick": self.df_brick, "blocks": self.blocks}
+
+
+class BatchTuneRecord(C.Structure):
+    _fields_ = [("tuning", BatchTuning), ("ms", C.c_float), ("pad", C.c_float)]
+
+
+BATCH_GRAPH, BATCH_PERSISTENT, BATCH_PER_WORLD = 0, 1, 2
+BATCH_PLANES = ["T", "FACE", "BLOCK", "HIT", "STEPS", "SHADOW", "GI_SH", "GI_COCG", "GI_LUMA", "GI_AOSKY"]
+
+
 BLOCK_DTYPE = np.dtype([("albedo", np.uint8, 3), ("roughness", np.uint8), ("metalness", np.uint8),
                         ("emissive", np.uint8)])
 
@@ -148,6 +172,27 @@ def _load() -> C.CDLL:
         "vpt_launch_count": ([P, C.POINTER(u64)], C.c_int),
         "vpt_get_stream": ([P, C.POINTER(P)], C.c_int),
         "vpt_detmath": ([i32, P, P, P, i32, i32], C.c_int),
+        "vpt_batch_default_config": ([C.POINTER(BatchConfig)], C.c_int),
+        "vpt_batch_create": ([C.POINTER(P), C.POINTER(BatchConfig)], C.c_int),
+        "vpt_batch_destroy": ([P], C.c_int),
+        "vpt_batch_last_error": ([P], C.c_char_p),
+        "vpt_batch_add_world": ([P, P, i32, i32, i32, P, i32, i32, i32, C.POINTER(i32)], C.c_int),
+        "vpt_batch_set_camera": ([P, i32, C.POINTER(Camera)], C.c_int),
+        "vpt_batch_build_df": ([P], C.c_int),
+        "vpt_batch_read_df": ([P, i32, P, sz], C.c_int),
+        "vpt_batch_set_tuning": ([P, C.POINTER(BatchTuning)], C.c_int),
+        "vpt_batch_get_tuning": ([P, C.POINTER(BatchTuning)], C.c_int),
+        "vpt_batch_trace": ([P, C.POINTER(Frame), i32], C.c_int),
+        "vpt_batch_autotune": ([P, C.POINTER(Frame), i32, C.POINTER(BatchTuneRecord), i32, C.POINTER(i32)],
+                               C.c_int),
+        "vpt_batch_read_plane": ([P, i32, i32, P, sz], C.c_int),
+        "vpt_batch_world_info": ([P, i32, C.POINTER(i32), C.POINTER(i32)], C.c_int),
+        "vpt_batch_count": ([P, C.POINTER(i32)], C.c_int),
+        "vpt_batch_synchronize": ([P], C.c_int),
+        "vpt_batch_set_stats": ([P, i32], C.c_int),
+        "vpt_batch_read_stats": ([P, C.POINTER(Stats)], C.c_int),
+        "vpt_batch_launch_count": ([P, C.POINTER(u64)], C.c_int),
+        "vpt_batch_get_stream": ([P, C.POINTER(P)], C.c_int),
         "vpt_generate_world": ([P, i32, i32, i32, u64, i32], C.c_int),
         "vpt_generate_block_table": ([P, i32, u64], C.c_int),
         "vpt_camera_from_pose": ([C.POINTER(Camera), C.POINTER(f32), f32, f32, f32, f32, f32, f32], C.c_int),
@@ -412,6 +457,138 @@ class Context:
     def stream(self) -> int:
         p = C.c_void_p()
         self._ck(lib.vpt_get_stream(self._h, C.byref(p)), "vpt_get_stream")
+        return p.value or 0
+
+
+class Batch:
+    """Many worlds traced together (vpt_batch_*): each world has its own
+    volume, block table, camera and ray tile; `trace` runs the primary,
+    sun-shadow and diffuse passes of every world in one persistent launch
+    (replayed from a CUDA graph by default) or, for comparison, as three pass
+    kernels per world."""
+
+    def __init__(self, max_worlds: int = 64, device: int = 0, **overrides):
+        cfg = BatchConfig()
+        _check(lib.vpt_batch_default_config(C.byref(cfg)), "vpt_batch_default_config")
+        cfg.max_worlds = max_worlds
+        cfg.device = device
+        for k, v in overrides.items():
+            if not hasattr(cfg, k):
+                raise AttributeError(f"unknown batch config field {k}")
+            setattr(cfg, k, v)
+        self.config = cfg
+        self._h = C.c_void_p()
+        _check(lib.vpt_batch_create(C.byref(self._h), C.byref(cfg)), "vpt_batch_create")
+        self.tiles = []
+
+    def close(self):
+        if self._h:
+            lib.vpt_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, status, what):
+        if status != OK:
+            msg = lib.vpt_status_string(status).decode()
+            detail = lib.vpt_batch_last_error(self._h) if self._h else b""
+            if detail:
+                msg += f" ({detail.decode()})"
+            raise VPTError(status, f"{what} failed: {msg}")
+
+    def add_world(self, voxels: np.ndarray, table: np.ndarray, width: int, height: int) -> int:
+        v = np.ascontiguousarray(voxels, dtype=np.uint8)
+        if v.ndim != 3:
+            raise ValueError("voxels must have shape (Z, Y, X)")
+        t = np.ascontiguousarray(table, dtype=BLOCK_DTYPE)
+        Z, Y, X = v.shape
+        wid = C.c_int32()
+        self._ck(lib.vpt_batch_add_world(self._h, _ptr(v), X, Y, Z, _ptr(t), t.size, width, height, C.byref(wid)),
+                 "vpt_batch_add_world")
+        self.tiles.append((height, width))
+        return int(wid.value)
+
+    def set_camera(self, world: int, cam: Camera):
+        self._ck(lib.vpt_batch_set_camera(self._h, world, C.byref(cam)), "vpt_batch_set_camera")
+
+    def build_df(self):
+        self._ck(lib.vpt_batch_build_df(self._h), "vpt_batch_build_df")
+
+    def read_df(self, world: int) -> np.ndarray:
+        dims = (C.c_int32 * 3)()
+        self._ck(lib.vpt_batch_world_info(self._h, world, dims, None), "vpt_batch_world_info")
+        out = np.empty((dims[2], dims[1], dims[0]), np.uint8)
+        self._ck(lib.vpt_batch_read_df(self._h, world, _ptr(out), out.nbytes), "vpt_batch_read_df")
+        return out
+
+    def set_tuning(self, block_threads=None, tiles_per_grab=None, df_brick=None, blocks=None):
+        t = self.tuning()
+        for k, v in (("block_threads", block_threads), ("tiles_per_grab", tiles_per_grab), ("df_brick", df_brick),
+                     ("blocks", blocks)):
+            if v is not None:
+                setattr(t, k, int(v))
+        self._ck(lib.vpt_batch_set_tuning(self._h, C.byref(t)), "vpt_batch_set_tuning")
+
+    def tuning(self) -> BatchTuning:
+        t = BatchTuning()
+        self._ck(lib.vpt_batch_get_tuning(self._h, C.byref(t)), "vpt_batch_get_tuning")
+        return t
+
+    def trace(self, frame: Frame, mode: int = BATCH_GRAPH):
+        self._ck(lib.vpt_batch_trace(self._h, C.byref(frame), mode), "vpt_batch_trace")
+
+    def autotune(self, frame: Frame, reps: int = 3) -> list:
+        recs = (BatchTuneRecord * 64)()
+        n = C.c_int32()
+        self._ck(lib.vpt_batch_autotune(self._h, C.byref(frame), reps, recs, 64, C.byref(n)), "vpt_batch_autotune")
+        return [dict(recs[k].tuning.as_dict(), ms=float(recs[k].ms)) for k in range(n.value)]
+
+    def read_plane(self, world: int, plane) -> np.ndarray:
+        pid = PLANE[plane] if isinstance(plane, str) else int(plane)
+        name = PLANES[pid]
+        H, W = self.tiles[world]
+        ch = {"HIT": 3, "GI_SH": 4, "GI_COCG": 2, "GI_AOSKY": 2}.get(name, 1)
+        dt = {"FACE": np.uint8, "BLOCK": np.uint8, "SHADOW": np.uint8, "HIT": np.int32, "STEPS": np.uint16}.get(
+            name, np.float32)
+        out = np.empty((H, W, ch) if ch > 1 else (H, W), dt)
+        self._ck(lib.vpt_batch_read_plane(self._h, world, pid, _ptr(out), out.nbytes), "vpt_batch_read_plane")
+        return out
+
+    def count(self) -> int:
+        n = C.c_int32()
+        self._ck(lib.vpt_batch_count(self._h, C.byref(n)), "vpt_batch_count")
+        return int(n.value)
+
+    def synchronize(self):
+        self._ck(lib.vpt_batch_synchronize(self._h), "vpt_batch_synchronize")
+
+    def set_stats(self, enabled: bool):
+        self._ck(lib.vpt_batch_set_stats(self._h, 1 if enabled else 0), "vpt_batch_set_stats")
+
+    def read_stats(self) -> dict:
+        s = Stats()
+        self._ck(lib.vpt_batch_read_stats(self._h, C.byref(s)), "vpt_batch_read_stats")
+        kinds = ["primary", "shadow", "diffuse", "bounce_shadow"]
+        return {"rays": dict(zip(kinds, list(s.rays))), "steps": dict(zip(kinds, list(s.steps)))}
+
+    def launch_count(self) -> int:
+        v = C.c_uint64()
+        self._ck(lib.vpt_batch_launch_count(self._h, C.byref(v)), "vpt_batch_launch_count")
+        return int(v.value)
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        self._ck(lib.vpt_batch_get_stream(self._h, C.byref(p)), "vpt_batch_get_stream")
         return p.value or 0
 
 

@@ -1,0 +1,133 @@
+// Batched multi-world tracing: one persistent launch over the ray tiles of
+// many worlds of different sizes, and the brick re-layout of the distance
+// field that the launch can trace through.
+//
+// The reference renders one world per process (Core/Pipeline.cpp drives one
+// World's passes a frame); here each batch entry is one such world with its
+// own voxel volume, distance field, block table, camera and ray tile. Work is
+// split into 8x4-pixel tiles; a warp takes `tiles_per_grab` consecutive queue
+// entries with one atomic, finds each tile's world by binary search over the
+// tile prefix sums (in shared memory) and runs the primary, sun-shadow and
+// diffuse passes of pixel_passes.cuh for its 32 pixels. Results are the same
+// bits as the per-world pass kernels. The queue is one counter the host zeroes
+// before the launch; no thread waits on another, so the kernel cannot stall.
+#include "pixel_passes.cuh"
+
+namespace vpt {
+
+namespace {
+
+template <int B>
+__global__ void __launch_bounds__(512) k_batch_trace(BatchLaunch a) {
+    __shared__ int s_begin[kBatchMaxWorlds + 1];
+    for (int k = threadIdx.x; k <= a.n_worlds; k += blockDim.x) s_begin[k] = a.tile_begin[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const BatchFrame& fr = *a.frame;
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(a.queue, a.tiles_per_grab);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= a.n_tiles) break;
+        const int end = min(base + a.tiles_per_grab, a.n_tiles);
+        for (int tile = base; tile < end; tile++) {
+            // last world whose first tile is <= tile (worlds with no tiles are skipped over)
+            int lo = 0, hi = a.n_worlds - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_begin[mid] <= tile) lo = mid; else hi = mid - 1;
+            }
+            const BatchWorld& bw = a.worlds[lo];
+            const int local = tile - s_begin[lo];
+            const int i = (local % bw.tiles_x) * 8 + (lane & 7);
+            const int j = (local / bw.tiles_x) * 4 + (lane >> 3);
+            const bool valid = i < bw.W && j < bw.H;
+            unsigned psteps = 0, srays = 0, ssteps = 0;
+            GICount cnt = {0u, 0u, 0u, 0u};
+            if (valid) {
+                const WorldView w = bw.w;
+                const CamView& cam = bw.cam;
+                const size_t px = (size_t)j * bw.W + i;
+                float d;
+                int face;
+                psteps = primary_pixel<B>(w, cam, bw.W, bw.H, i, j, fr.primary_max_steps, px, bw.t, bw.face,
+                                          bw.block, bw.hit, bw.steps, &d, &face);
+                bw.shadow[px] = shadow_pixel<B>(w, cam, bw.W, bw.H, i, j, fr.shadow_max_steps,
+                                                mk3(fr.sun[0], fr.sun[1], fr.sun[2]), d, face, &srays, &ssteps);
+                diffuse_pixel<B>(w, cam, bw.W, bw.H, i, j, fr.d, px, d, face, bw.sh, bw.cocg, bw.luma, bw.aosky,
+                                 &cnt);
+            }
+            if (a.stats) {
+                count_rays(a.stats, kRayPrimary, valid ? 1u : 0u, psteps);
+                count_rays(a.stats, kRayShadow, srays, ssteps);
+                count_rays(a.stats, kRayDiffuse, cnt.diffuse_rays, cnt.diffuse_steps);
+                count_rays(a.stats, kRayBounceShadow, cnt.shadow_rays, cnt.shadow_steps);
+            }
+        }
+    }
+}
+
+template <int B>
+__global__ void __launch_bounds__(256) k_df_bricks(const uint8_t* __restrict__ df, uint8_t* __restrict__ out, int X,
+                                                   int Y, int Z, int bx, int by, size_t total) {
+    const size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= total) return;
+    constexpr int L = B == 4 ? 2 : 3;
+    const size_t brick = o >> (3 * L);
+    const int r = (int)(o & ((size_t)B * B * B - 1));
+    const int x = (int)(brick % (size_t)bx) * B + (r & (B - 1));
+    const int y = (int)((brick / (size_t)bx) % (size_t)by) * B + ((r >> L) & (B - 1));
+    const int z = (int)(brick / ((size_t)bx * by)) * B + (r >> (2 * L));
+    // padding outside the volume is never read (the traversal tests the volume first)
+    out[o] = (x < X && y < Y && z < Z) ? df[(size_t)x + (size_t)X * ((size_t)y + (size_t)Y * z)] : 0;
+}
+
+template <int B>
+int max_blocks_for(int block_threads) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_trace<B>, block_threads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+}  // namespace
+
+int batch_max_blocks(int df_brick, int block_threads, int device) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+    const int per_sm = df_brick == 4 ? max_blocks_for<4>(block_threads)
+                       : df_brick == 8 ? max_blocks_for<8>(block_threads)
+                                       : max_blocks_for<0>(block_threads);
+    return per_sm * sms;
+}
+
+cudaError_t batch_trace(const BatchLaunch& a, int df_brick, int block_threads, int blocks, cudaStream_t s) {
+    if (a.n_worlds < 1 || a.n_worlds > kBatchMaxWorlds || block_threads < 32 || block_threads > 512 ||
+        (block_threads & 31) || a.tiles_per_grab < 1)
+        return cudaErrorInvalidValue;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (blocks <= 0) blocks = batch_max_blocks(df_brick, block_threads, dev);
+    if (blocks <= 0) return cudaErrorInvalidConfiguration;
+    switch (df_brick) {
+        case 0: k_batch_trace<0><<<blocks, block_threads, 0, s>>>(a); break;
+        case 4: k_batch_trace<4><<<blocks, block_threads, 0, s>>>(a); break;
+        case 8: k_batch_trace<8><<<blocks, block_threads, 0, s>>>(a); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t df_to_bricks(const uint8_t* df, uint8_t* out, int X, int Y, int Z, int brick, cudaStream_t s) {
+    if (brick != 4 && brick != 8) return cudaErrorInvalidValue;
+    const int bx = (X + brick - 1) / brick, by = (Y + brick - 1) / brick, bz = (Z + brick - 1) / brick;
+    const size_t total = (size_t)bx * by * bz * brick * brick * brick;
+    const unsigned grid = (unsigned)((total + 255) / 256);
+    if (brick == 4) k_df_bricks<4><<<grid, 256, 0, s>>>(df, out, X, Y, Z, bx, by, total);
+    else k_df_bricks<8><<<grid, 256, 0, s>>>(df, out, X, Y, Z, bx, by, total);
+    return cudaGetLastError();
+}
+
+}  // namespace vpt

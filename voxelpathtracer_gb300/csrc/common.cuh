@@ -18,10 +18,11 @@ constexpr int kFaceMiss = 10;           // round(1.0 * 10) decoded from a miss (
 // ------------------------------------------------------------------ world --
 struct WorldView {
     const uint8_t* vox;       // block ids, x fastest
-    const uint8_t* df;        // Manhattan distance field, same layout
+    const uint8_t* df;        // Manhattan distance field: x fastest, or in BxBxB bricks (df_index)
     int X, Y, Z;
     const vpt_block* blocks;  // block table
     int n_blocks;
+    int bx, by;               // bricks along x and y (brick layouts only)
 };
 
 struct CamView {
@@ -32,6 +33,22 @@ struct CamView {
 
 __device__ __forceinline__ int vox_index(const WorldView& w, int x, int y, int z) {
     return x + w.X * (y + w.Y * z);
+}
+// Distance-field address of voxel (x, y, z). B == 0: the x-fastest layout of
+// the voxel volume. B == 4 or 8: the volume padded to whole BxBxB bricks,
+// bricks in x-fastest order, each brick's B^3 bytes x-fastest, so the
+// neighbourhood a ray probes in a few steps shares a few 32-byte sectors
+// whichever way the ray goes.
+template <int B>
+__host__ __device__ __forceinline__ int df_index(const WorldView& w, int x, int y, int z) {
+    if constexpr (B == 0) {
+        return x + w.X * (y + w.Y * z);
+    } else {
+        static_assert(B == 4 || B == 8, "brick edge 4 or 8");
+        constexpr int L = B == 4 ? 2 : 3;
+        const int brick = ((z >> L) * w.by + (y >> L)) * w.bx + (x >> L);
+        return (brick << (3 * L)) + ((((z & (B - 1)) << L) + (y & (B - 1))) << L) + (x & (B - 1));
+    }
 }
 __device__ __forceinline__ bool in_volume(const WorldView& w, int x, int y, int z) {
     // IsInVolume (InitialRayTraceFrag.glsl:68-77): 0 <= x <= X-1, ... as unsigned compares

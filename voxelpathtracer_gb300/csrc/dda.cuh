@@ -51,6 +51,8 @@ __device__ __forceinline__ void ray_start(RayState& r, v3 origin, v3 dir, int ma
 }
 
 // One iteration of the traversal loop; returns true once the loop is over.
+// B is the distance-field layout (df_index).
+template <int B = 0>
 __device__ __forceinline__ bool dda_step(const WorldView& w, RayState& r) {
     if (r.itr >= r.max_steps) return true;
     const int lx = f2i_floor(r.o.x);
@@ -60,7 +62,7 @@ __device__ __forceinline__ bool dda_step(const WorldView& w, RayState& r) {
         r.inter = 0;
         return true;
     }
-    const int e = euclid_steps((int)__ldg(w.df + vox_index(w, lx, ly, lz)));
+    const int e = euclid_steps((int)__ldg(w.df + df_index<B>(w, lx, ly, lz)));
     if (e == 0) return true;
     if (e == 1) {
         // one exact DDA face step (:341-356)
@@ -119,10 +121,11 @@ __device__ __forceinline__ TraceResult ray_finish(const WorldView& w, const RayS
     return t;
 }
 
+template <int B = 0>
 __device__ __forceinline__ TraceResult traverse(const WorldView& w, v3 origin, v3 direction, int max_steps) {
     RayState r;
     ray_start(r, origin, direction, max_steps);
-    while (!dda_step(w, r)) {
+    while (!dda_step<B>(w, r)) {
     }
     return ray_finish(w, r);
 }

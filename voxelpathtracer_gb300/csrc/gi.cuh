@@ -11,7 +11,8 @@ struct GICount {
     unsigned diffuse_rays, diffuse_steps, shadow_rays, shadow_steps;
 };
 
-// CalculateDiffuse (DiffuseRayTraceFrag.glsl:535-664)
+// CalculateDiffuse (DiffuseRayTraceFrag.glsl:535-664); B is the distance-field layout.
+template <int B = 0>
 __device__ __forceinline__ v4 calculate_diffuse(const WorldView& w, const DiffuseArgs& a, v3 initial_origin,
                                                 v3 input_normal, uint32_t* rng, v3* odir, bool* skyhit,
                                                 GICount* cnt) {
@@ -27,7 +28,7 @@ __device__ __forceinline__ v4 calculate_diffuse(const WorldView& w, const Diffus
     v3 throughput = mk3(1.0f, 1.0f, 1.0f);
     for (int i = 0; i < a.bounces; i++) {
         if (i == 0) *odir = rd;
-        TraceResult tr = traverse(w, ro, rd, a.diffuse_max_steps);
+        TraceResult tr = traverse<B>(w, ro, rd, a.diffuse_max_steps);
         cnt->diffuse_rays += 1;
         cnt->diffuse_steps += (unsigned)tr.steps;
         float T = tr.t;
@@ -47,7 +48,7 @@ __device__ __forceinline__ v4 calculate_diffuse(const WorldView& w, const Diffus
                 shadow_at = 0.0f;
             } else {
                 // GetShadowAt (:1202-1222)
-                TraceResult sr = traverse(w, add(ip, bias_shadow), light_dir, a.bounce_shadow_max_steps);
+                TraceResult sr = traverse<B>(w, add(ip, bias_shadow), light_dir, a.bounce_shadow_max_steps);
                 cnt->shadow_rays += 1;
                 cnt->shadow_steps += (unsigned)sr.steps;
                 shadow_at = sr.t > 0.0f ? 1.0f : 0.0f;

@@ -105,6 +105,50 @@ struct FrameTraceArgs {
 // blocks_hint <= 0 sizes the grid to fill every SM once.
 cudaError_t trace_frame(const FrameTraceArgs& a, int fp16, int blocks_hint, cudaStream_t s);
 
+// -------------------------------------------------------------- batch.cu --
+// Many worlds, each with its own camera and ray tile, traced in one
+// persistent launch: warps take 8x4-pixel tiles of all worlds from one queue
+// and run primary, sun-shadow and diffuse GI for their 32 pixels.
+struct BatchWorld {
+    WorldView w;              // df points at the layout the launch is built for
+    CamView cam;
+    int W, H;
+    int tiles_x;              // 8x4 tiles per row
+    int tile_begin;           // first queue entry of this world
+    float* t;
+    uint8_t* face;
+    uint8_t* block;
+    int32_t* hit;
+    uint16_t* steps;
+    uint8_t* shadow;
+    float* sh;
+    float* cocg;
+    float* luma;
+    float* aosky;
+};
+struct BatchFrame {           // per-frame constants, read from device memory
+    int primary_max_steps;
+    int shadow_max_steps;
+    float sun[3];
+    DiffuseArgs d;
+};
+struct BatchLaunch {
+    const BatchWorld* worlds;
+    const int* tile_begin;    // n_worlds + 1 prefix sums (tile_begin[n] = n_tiles)
+    const BatchFrame* frame;
+    int n_worlds;
+    int n_tiles;
+    int tiles_per_grab;       // queue entries a warp takes at once
+    int* queue;               // zero at launch
+    Counters* stats;
+};
+constexpr int kBatchMaxWorlds = 1024;
+// df_brick: 0, 4 or 8; blocks <= 0 fills every SM to its occupancy limit.
+cudaError_t batch_trace(const BatchLaunch& a, int df_brick, int block_threads, int blocks, cudaStream_t s);
+int batch_max_blocks(int df_brick, int block_threads, int device);
+// Copies an x-fastest distance field into the BxBxB brick layout of df_index.
+cudaError_t df_to_bricks(const uint8_t* df, uint8_t* out, int X, int Y, int Z, int brick, cudaStream_t s);
+
 // ------------------------------------------------------- groundtruth.cu --
 // FP64 Welford accumulation of `spp` diffuse samples over a crop (fp32 G-buffer).
 struct GroundTruthArgs {

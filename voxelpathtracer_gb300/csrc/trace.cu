@@ -1,9 +1,7 @@
 // The three trace passes as separate kernels, one thread per pixel: primary
-// (G-buffer), sun shadow and diffuse GI. They back the pass-by-pass entry
-// points of the C ABI; the frame path uses the fused persistent kernel in
-// trace_frame.cu. The traversal is dda.cuh.
-#include "gi.cuh"
-#include "kernels.cuh"
+// (G-buffer), sun shadow and diffuse GI. The per-pixel work is
+// pixel_passes.cuh; the traversal is dda.cuh.
+#include "pixel_passes.cuh"
 
 namespace vpt {
 
@@ -18,15 +16,6 @@ __device__ __forceinline__ void tile_pixel(int* i, int* j) {
     *j = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
 }
 
-__device__ __forceinline__ void count_rays(Counters* c, int kind, unsigned rays, unsigned steps) {
-    unsigned r = __reduce_add_sync(0xffffffffu, rays);
-    unsigned s = __reduce_add_sync(0xffffffffu, steps);
-    if ((threadIdx.x & 31) == 0 && (r | s)) {
-        atomicAdd(&c->rays[kind], (unsigned long long)r);
-        atomicAdd(&c->steps[kind], (unsigned long long)s);
-    }
-}
-
 // InitialRayTraceFrag.glsl main (:417-468)
 template <typename S>
 __global__ void __launch_bounds__(256) k_trace_primary(WorldView w, CamView cam, int W, int H, int max_steps,
@@ -34,22 +23,13 @@ __global__ void __launch_bounds__(256) k_trace_primary(WorldView w, CamView cam,
                                                        int32_t* out_hit, uint16_t* out_steps, Counters* stats) {
     int i, j;
     tile_pixel(&i, &j);
-    bool valid = i < W && j < H;
+    const bool valid = i < W && j < H;
     unsigned nsteps = 0;
     if (valid) {
-        size_t px = (size_t)j * W + i;
-        v3 r0 = ray_origin(cam);
-        v3 dir = normalize(ray_dir_at(cam, texcoord(i, j, W, H)));
-        TraceResult r = traverse(w, r0, dir, max_steps);
-        bool intersect = r.t > 0.0f && r.block > 0;
-        st(out_t + px, r.t);
-        out_face[px] = (uint8_t)(intersect ? normal_id(r.normal) : kFaceMiss);
-        out_block[px] = (uint8_t)(intersect ? r.block : 0);
-        out_hit[px * 3 + 0] = r.cell[0];
-        out_hit[px * 3 + 1] = r.cell[1];
-        out_hit[px * 3 + 2] = r.cell[2];
-        out_steps[px] = (uint16_t)r.steps;
-        nsteps = (unsigned)r.steps;
+        float d;
+        int face;
+        nsteps = primary_pixel<0>(w, cam, W, H, i, j, max_steps, (size_t)j * W + i, out_t, out_face, out_block,
+                                  out_hit, out_steps, &d, &face);
     }
     if (stats) count_rays(stats, kRayPrimary, valid ? 1u : 0u, nsteps);
 }
@@ -63,32 +43,9 @@ __global__ void __launch_bounds__(256) k_trace_shadow(WorldView w, CamView cam, 
     tile_pixel(&i, &j);
     unsigned nrays = 0, nsteps = 0;
     if (i < W && j < H) {
-        size_t px = (size_t)j * W + i;
-        float d = ld(t + px);
-        uint8_t out;
-        if (d < 0.0f) {
-            out = 0;
-        } else {
-            v3 L = mk3(lx, ly, lz);
-            v3 pos = add(ray_origin(cam), muls(normalize(ray_dir_at(cam, texcoord(i, j, W, H))), d));
-            v3 n = normal_from_id(__ldg(face + px), 1.0f);
-            float ndl = dot(n, L);
-            if (ndl <= 0.01f) {
-                out = 1;
-            } else {
-                v3 o = add(pos, mul(n, mk3(0.06f, 0.06f, 0.06f)));
-                int block_at = get_voxel(w, f2i_floor(o.x), f2i_floor(o.y), f2i_floor(o.z));
-                float T = -1.0f;
-                if (d > 0.0f) {
-                    TraceResult r = traverse(w, o, L, max_steps);
-                    T = r.t;
-                    nrays = 1;
-                    nsteps = (unsigned)r.steps;
-                }
-                out = (T > 0.0f || block_at > 0) ? 1 : 0;
-            }
-        }
-        shadow[px] = out;
+        const size_t px = (size_t)j * W + i;
+        shadow[px] = shadow_pixel<0>(w, cam, W, H, i, j, max_steps, mk3(lx, ly, lz), ld(t + px), __ldg(face + px),
+                                     &nrays, &nsteps);
     }
     if (stats) count_rays(stats, kRayShadow, nrays, nsteps);
 }
@@ -102,54 +59,9 @@ __global__ void __launch_bounds__(256) k_trace_diffuse(WorldView w, CamView cam,
     tile_pixel(&i, &j);
     GICount cnt = {0u, 0u, 0u, 0u};
     if (i < W && j < H) {
-        size_t px = (size_t)j * W + i;
-        v3 dir = normalize(ray_dir_at(cam, texcoord(i, j, W, H)));
-        float d = ld(t + px);
-        v3 pos = add(ray_origin(cam), muls(dir, d));
-        v3 n = normal_from_id(__ldg(face + px), 0.5f);
-        float sh[4], cocg[2];
-        if (d < 0.0f) {
-            irradiance_to_sh(muls(sky_radiance(dir), 2.66f), n, sh, cocg);
-            for (int c = 0; c < 4; c++) st(o_sh + px * 4 + c, sh[c]);
-            st(o_cocg + px * 2 + 0, cocg[0]);
-            st(o_cocg + px * 2 + 1, cocg[1]);
-            st(o_luma + px, luminance(mk3(0.0f, 0.0f, 0.0f)));
-            st(o_aosky + px * 2 + 0, 1.0f);
-            st(o_aosky + px * 2 + 1, 0.0f);
-        } else {
-            uint32_t rng = pcg_hash((uint32_t)px + pcg_hash(a.frame_index + pcg_hash(a.seed)));
-            int spp = min(max(a.spp, 1), 32);
-            if (a.lighting.moon_stronger) spp *= 2;
-            float tsh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, tcc[2] = {0.0f, 0.0f};
-            v3 radiance = mk3(0.0f, 0.0f, 0.0f);
-            float acc_ao = 0.0f, skyhits = 0.0f;
-            for (int s = 0; s < spp; s++) {
-                v3 odir = mk3(0.0f, 0.0f, 0.0f);
-                bool ss = false;
-                v4 x = calculate_diffuse(w, a, pos, n, &rng, &odir, &ss, &cnt);
-                v3 xc = vclamp(mk3(x.x, x.y, x.z), 0.0f, 8.0f);
-                radiance = add(radiance, xc);
-                acc_ao += x.w;
-                irradiance_to_sh(xc, odir, sh, cocg);
-                for (int c = 0; c < 4; c++) tsh[c] += sh[c];
-                tcc[0] += cocg[0];
-                tcc[1] += cocg[1];
-                skyhits += ss ? 1.0f : 0.0f;
-            }
-            float fs = (float)spp;
-            acc_ao /= fs;
-            for (int c = 0; c < 4; c++) tsh[c] /= fs;
-            tcc[0] /= fs;
-            tcc[1] /= fs;
-            radiance = divs(radiance, fs);
-            skyhits /= fs;
-            for (int c = 0; c < 4; c++) st(o_sh + px * 4 + c, clampf(tsh[c], -100.0f, 100.0f));
-            st(o_cocg + px * 2 + 0, clampf(tcc[0], -100.0f, 100.0f));
-            st(o_cocg + px * 2 + 1, clampf(tcc[1], -100.0f, 100.0f));
-            st(o_luma + px, clampf(fmaxf(luminance(radiance), 0.01f), 0.001f, 64.0f));
-            st(o_aosky + px * 2 + 0, clampf(acc_ao, 0.0f, 1.0f));
-            st(o_aosky + px * 2 + 1, clampf(skyhits, 0.0f, 1.0f));
-        }
+        const size_t px = (size_t)j * W + i;
+        diffuse_pixel<0>(w, cam, W, H, i, j, a, px, ld(t + px), __ldg(face + px), o_sh, o_cocg, o_luma, o_aosky,
+                         &cnt);
     }
     if (stats) {
         count_rays(stats, kRayDiffuse, cnt.diffuse_rays, cnt.diffuse_steps);
