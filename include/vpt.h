@@ -374,6 +374,59 @@ vpt_status vpt_batch_read_stats(vpt_batch* batch, vpt_stats* out);   /* synchron
 vpt_status vpt_batch_launch_count(const vpt_batch* batch, uint64_t* out);
 vpt_status vpt_batch_get_stream(const vpt_batch* batch, void** stream);
 
+/* ----------------------------------------------------- learned denoiser --
+ * No counterpart in the reference (its denoisers are the SVGF and a-trous
+ * passes of Core/Pipeline.cpp:2284-2786). A 3-level U-Net (32/64/96
+ * channels, 3x3 convolutions, ReLU, 2x2 average pooling, nearest upsampling
+ * with skip concatenation) on the tcgen05 tensor cores: BF16 weights and
+ * activations (NHWC, channels padded to multiples of 16), FP32 accumulation.
+ * Input: 16 channels (11 features + 5 zero); output: 16 FP32 channels of
+ * which 0..2 are the prediction. Image sizes must be multiples of 4. */
+typedef struct vpt_unet vpt_unet;
+
+/* Raw operators over caller device pointers, enqueued on `stream` (a
+ * cudaStream_t) on the current device. conv3x3: out = act(conv(in) + bias),
+ * in = channels [0,c0) of in0 (nearest-upsampled from half size when up0 = 1)
+ * followed by channels [0,c1) of in1; weight [cout][9][c0+c1] BF16, tap =
+ * (dy+1)*3 + (dx+1); relu 0/1; out zeroed where mask <= 0 if mask is given;
+ * BF16 and/or FP32 output [n*h*w][cout]. conv3x3_dw adds
+ * dW[co][tap][ci] = sum_p dy[p][co] in[p+tap][ci] to the FP32 dw.
+ * vpt_nn_status synchronises `stream` and reports a timed-out tensor-core
+ * wait as VPT_ERR_DEVICE_TIMEOUT. */
+vpt_status vpt_nn_conv3x3(const void* in0, int32_t c0, int32_t up0, const void* in1, int32_t c1, int32_t n, int32_t h,
+                          int32_t w, const void* weight, const float* bias, int32_t cout, int32_t relu,
+                          const void* mask, void* out_bf16, float* out_f32, void* stream);
+vpt_status vpt_nn_conv3x3_dw(const void* in0, int32_t c0, int32_t up0, const void* in1, int32_t c1, int32_t n,
+                             int32_t h, int32_t w, const void* dy, int32_t cout, float* dw, void* stream);
+vpt_status vpt_nn_status(void* stream);
+
+/* Layer `layer` (0..10) of the network: padded input/output channels, real
+ * ones, and the offset of its weights [cout][9][cin] (then bias [cout]) in
+ * the flat FP32 parameter vector. */
+vpt_status vpt_unet_layer_info(int32_t layer, int32_t* cin, int32_t* cout, int32_t* cin_real, int32_t* cout_real,
+                               int64_t* offset);
+/* Capacity: up to max_images images of max_height x max_width pixels. */
+vpt_status vpt_unet_create(vpt_unet** out, int32_t device, int32_t max_images, int32_t max_height, int32_t max_width);
+vpt_status vpt_unet_destroy(vpt_unet* unet);
+const char* vpt_unet_last_error(const vpt_unet* unet);
+vpt_status vpt_unet_param_count(const vpt_unet* unet, int64_t* n);
+vpt_status vpt_unet_set_params(vpt_unet* unet, const float* host, int64_t n);   /* also resets Adam */
+vpt_status vpt_unet_get_params(vpt_unet* unet, float* host, int64_t n);
+vpt_status vpt_unet_get_grads(vpt_unet* unet, float* host, int64_t n);
+/* Inference of n images (device input [n][h][w][16] BF16); the output stays
+ * in the network's buffer (vpt_unet_output) and is copied to `out` (device,
+ * [n][h][w][16] FP32) when not NULL. Stream-ordered on the network's stream. */
+vpt_status vpt_unet_forward(vpt_unet* unet, const void* input, int32_t n, int32_t h, int32_t w, float* out);
+vpt_status vpt_unet_output(vpt_unet* unet, const float** out);
+/* Forward + backward of the mean squared error of output channels 0..2
+ * against `target` (device [n][h][w][3] FP32); the parameter gradient is kept
+ * for vpt_unet_adam / vpt_unet_get_grads. Synchronises when loss is not NULL. */
+vpt_status vpt_unet_backward(vpt_unet* unet, const void* input, const float* target, int32_t n, int32_t h, int32_t w,
+                             double* loss);
+vpt_status vpt_unet_adam(vpt_unet* unet, float lr, float beta1, float beta2, float eps);
+vpt_status vpt_unet_synchronize(vpt_unet* unet);   /* also reports timed-out waits */
+vpt_status vpt_unet_get_stream(const vpt_unet* unet, void** stream);
+
 /* ---------------------------------------------------------- host helpers -- */
 /* Seeded value-noise terrain (heightmap h = 40 + 16*fbm, 4 octaves, base
  * frequency 1/64, gain 0.5; grass top, three dirt layers, stone below) with

@@ -193,6 +193,24 @@ def _load() -> C.CDLL:
         "vpt_batch_read_stats": ([P, C.POINTER(Stats)], C.c_int),
         "vpt_batch_launch_count": ([P, C.POINTER(u64)], C.c_int),
         "vpt_batch_get_stream": ([P, C.POINTER(P)], C.c_int),
+        "vpt_nn_conv3x3": ([P, i32, i32, P, i32, i32, i32, i32, P, P, i32, i32, P, P, P, P], C.c_int),
+        "vpt_nn_conv3x3_dw": ([P, i32, i32, P, i32, i32, i32, i32, P, i32, P, P], C.c_int),
+        "vpt_nn_status": ([P], C.c_int),
+        "vpt_unet_layer_info": ([i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32),
+                                 C.POINTER(C.c_int64)], C.c_int),
+        "vpt_unet_create": ([C.POINTER(P), i32, i32, i32, i32], C.c_int),
+        "vpt_unet_destroy": ([P], C.c_int),
+        "vpt_unet_last_error": ([P], C.c_char_p),
+        "vpt_unet_param_count": ([P, C.POINTER(C.c_int64)], C.c_int),
+        "vpt_unet_set_params": ([P, P, C.c_int64], C.c_int),
+        "vpt_unet_get_params": ([P, P, C.c_int64], C.c_int),
+        "vpt_unet_get_grads": ([P, P, C.c_int64], C.c_int),
+        "vpt_unet_forward": ([P, P, i32, i32, i32, P], C.c_int),
+        "vpt_unet_output": ([P, C.POINTER(P)], C.c_int),
+        "vpt_unet_backward": ([P, P, P, i32, i32, i32, C.POINTER(C.c_double)], C.c_int),
+        "vpt_unet_adam": ([P, f32, f32, f32, f32], C.c_int),
+        "vpt_unet_synchronize": ([P], C.c_int),
+        "vpt_unet_get_stream": ([P, C.POINTER(P)], C.c_int),
         "vpt_generate_world": ([P, i32, i32, i32, u64, i32], C.c_int),
         "vpt_generate_block_table": ([P, i32, u64], C.c_int),
         "vpt_camera_from_pose": ([C.POINTER(Camera), C.POINTER(f32), f32, f32, f32, f32, f32, f32], C.c_int),
@@ -589,6 +607,119 @@ class Batch:
     def stream(self) -> int:
         p = C.c_void_p()
         self._ck(lib.vpt_batch_get_stream(self._h, C.byref(p)), "vpt_batch_get_stream")
+        return p.value or 0
+
+
+# --------------------------------------------------------- learned denoiser --
+UNET_LAYERS = 11
+
+
+def unet_layers() -> list:
+    """(cin, cout, cin_real, cout_real, param offset) of each layer (vpt_unet_layer_info)."""
+    out = []
+    for l in range(UNET_LAYERS):
+        a, b, c, d = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        o = C.c_int64()
+        _check(lib.vpt_unet_layer_info(l, C.byref(a), C.byref(b), C.byref(c), C.byref(d), C.byref(o)),
+               "vpt_unet_layer_info")
+        out.append((a.value, b.value, c.value, d.value, o.value))
+    return out
+
+
+def _dptr(t) -> int | None:
+    """Device address of a torch tensor (None passes NULL)."""
+    return None if t is None else int(t.data_ptr())
+
+
+def nn_conv3x3(in0, c0, in1, c1, n, h, w, weight, bias, cout, relu=False, mask=None, out=None, out_f32=None,
+               up0=False, stream=0):
+    """vpt_nn_conv3x3 over torch device tensors (BF16 NHWC; see include/vpt.h)."""
+    _check(lib.vpt_nn_conv3x3(_dptr(in0), c0, 1 if up0 else 0, _dptr(in1), c1, n, h, w, _dptr(weight), _dptr(bias),
+                              cout, 1 if relu else 0, _dptr(mask), _dptr(out), _dptr(out_f32), stream or None),
+           "vpt_nn_conv3x3")
+
+
+def nn_conv3x3_dw(in0, c0, in1, c1, n, h, w, dy, cout, dw, up0=False, stream=0):
+    _check(lib.vpt_nn_conv3x3_dw(_dptr(in0), c0, 1 if up0 else 0, _dptr(in1), c1, n, h, w, _dptr(dy), cout,
+                                 _dptr(dw), stream or None), "vpt_nn_conv3x3_dw")
+
+
+def nn_status(stream=0):
+    _check(lib.vpt_nn_status(stream or None), "vpt_nn_status")
+
+
+class UNet:
+    """The learned denoiser (vpt_unet_*). Inputs and targets are torch CUDA
+    tensors: input [n, h, w, 16] bfloat16, target [n, h, w, 3] float32."""
+
+    def __init__(self, max_images: int, max_height: int, max_width: int, device: int = 0):
+        self._h = C.c_void_p()
+        _check(lib.vpt_unet_create(C.byref(self._h), device, max_images, max_height, max_width), "vpt_unet_create")
+        n = C.c_int64()
+        self._ck(lib.vpt_unet_param_count(self._h, C.byref(n)), "vpt_unet_param_count")
+        self.n_params = int(n.value)
+        self.device = device
+
+    def close(self):
+        if self._h:
+            lib.vpt_unet_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, status, what):
+        if status != OK:
+            msg = lib.vpt_status_string(status).decode()
+            detail = lib.vpt_unet_last_error(self._h) if self._h else b""
+            if detail:
+                msg += f" ({detail.decode()})"
+            raise VPTError(status, f"{what} failed: {msg}")
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._ck(lib.vpt_unet_set_params(self._h, _ptr(p), p.size), "vpt_unet_set_params")
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        self._ck(lib.vpt_unet_get_params(self._h, _ptr(out), out.size), "vpt_unet_get_params")
+        return out
+
+    def grads(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        self._ck(lib.vpt_unet_get_grads(self._h, _ptr(out), out.size), "vpt_unet_get_grads")
+        return out
+
+    def forward(self, x, out=None):
+        n, h, w, _ = x.shape
+        self._ck(lib.vpt_unet_forward(self._h, _dptr(x), n, h, w, _dptr(out)), "vpt_unet_forward")
+        return out
+
+    def backward(self, x, target) -> float:
+        n, h, w, _ = x.shape
+        loss = C.c_double()
+        self._ck(lib.vpt_unet_backward(self._h, _dptr(x), _dptr(target), n, h, w, C.byref(loss)),
+                 "vpt_unet_backward")
+        return float(loss.value)
+
+    def adam(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+        self._ck(lib.vpt_unet_adam(self._h, lr, beta1, beta2, eps), "vpt_unet_adam")
+
+    def synchronize(self):
+        self._ck(lib.vpt_unet_synchronize(self._h), "vpt_unet_synchronize")
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        self._ck(lib.vpt_unet_get_stream(self._h, C.byref(p)), "vpt_unet_get_stream")
         return p.value or 0
 
 
