@@ -307,6 +307,16 @@ def run_ours(args):
     batched = None
     if not args.no_batch:
         batched = batched_section(vpt, torch, args, local, flush)
+    learned_out = None
+    if not args.no_learned:
+        try:
+            peaks = json.loads(PEAKS_FILE.read_text())
+        except Exception:
+            peaks = {}
+        learned_out = learned_section(vpt, torch, args, local, flush, vox, blocks, yaw, pitch, peaks)
+    large = None
+    if not args.no_large:
+        large = large_section(vpt, torch, args, local)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -354,6 +364,8 @@ def run_ours(args):
         "variants": variant,
         "quality": quality_out,
         "batched": batched,
+        "learned": learned_out,
+        "large": large,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
@@ -439,6 +451,167 @@ def batched_section(vpt, torch, args, local, flush):
     }
     b.close()
     return res
+
+
+# ------------------------------------------------------ learned denoiser --
+def unet_flops(vpt, H, W, real=True):
+    """Multiply-add FLOPs of one U-Net inference on an H x W image (2 per MAC)."""
+    levels = [1, 1, 2, 2, 4, 4, 2, 2, 1, 1, 1]   # resolution divisor of each layer, in layer order
+    f = 0
+    for (cin, cout, cin_r, cout_r, _off), d in zip(vpt.unet_layers(), levels):
+        f += 2 * 9 * (cin_r * cout_r if real else cin * cout) * (H // d) * (W // d)
+    return f
+
+
+def learned_section(vpt, torch, args, local, flush, vox, blocks, yaw, pitch, peaks):
+    """The learned denoiser on the full-frame workload: frame ms of the learned
+    path, U-Net inference time and tensor throughput, and the error of the
+    noisy input, SVGF and the network against the FP64 ground truth."""
+    from voxelpathtracer_gb300 import learned
+    if not learned.WEIGHTS.exists():
+        return {"unavailable": "no trained weights in the package; frames fall back to SVGF"}
+    params, meta = learned.load()
+    W, H = RES
+    out = {"weights": {k: meta[k] for k in ("pairs", "crop", "spp", "steps", "holdout_rmse_noisy",
+                                             "holdout_rmse_net") if k in meta}}
+    with vpt.UNet(1, H, W, device=local) as net, vpt.Context(width=W, height=H, device=local) as ctx:
+        net.set_params(params)
+        ctx.upload_world(vox)
+        ctx.set_block_table(blocks)
+        ctx.build_df()
+        stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
+        ms = []
+        with torch.cuda.stream(stream):
+            for s in range(args.warmup + args.steps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                _, used = ctx.render_frame_learned(camera_at(vpt, yaw, pitch, s), frame_at(vpt, s), net,
+                                                   readback=False)
+                e1.record(stream)
+                e1.synchronize()
+                if s >= args.warmup:
+                    ms.append(e0.elapsed_time(e1))
+        out["frame_ms"] = float(statistics.median(ms))
+        out["used_net"] = bool(used)
+        # inference alone, on the features of the last frame
+        feat = torch.empty((1, H, W, 16), dtype=torch.bfloat16, device=f"cuda:{local}")
+        ctx.learned_input(camera_at(vpt, yaw, pitch, 0), frame_at(vpt, 0))
+        ctx.learned_features((0, 0, W, H), feat[0])
+        ctx.synchronize()
+        ctx.end_frame()
+        ns = torch.cuda.ExternalStream(net.stream(), device=local)
+        inf = []
+        with torch.cuda.stream(ns):
+            for k in range(8):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(ns)
+                net.forward(feat)
+                e1.record(ns)
+                e1.synchronize()
+                if k >= 3:
+                    inf.append(e0.elapsed_time(e1))
+        net.synchronize()
+        inf_ms = float(statistics.median(inf))
+        flops = unet_flops(vpt, H, W)
+        peak = float(peaks.get("bf16_tflops", 1900.0))
+        out["unet_ms"] = inf_ms
+        out["unet_tflop_per_inference"] = flops / 1e12
+        out["unet_tflops"] = flops / (inf_ms * 1e-3) / 1e12
+        out["tensor_roofline"] = {"bound": "tensor", "achieved": out["unet_tflops"], "peak": peak,
+                                  "unit": "TFLOP/s", "frac": out["unet_tflops"] / peak,
+                                  "peak_source": "measured (MEASURED_PEAKS.json bf16_tflops)"}
+        if not args.no_quality:
+            frames = args.warmup + args.steps
+            r = learned.evaluate_frame(net, vox, blocks, CAM_POS, yaw, pitch, frames, gt_spp=args.gt_spp,
+                                       device=local)
+            out["quality"] = dict(r, frames=frames, crop=list(quality_crop()), gt_spp=args.gt_spp)
+    return out
+
+
+def quality_crop():
+    from voxelpathtracer_gb300 import quality
+    return quality.DEFAULT_CROP_1080P
+
+
+# ------------------------------------------------------ large combined --
+LARGE_WORLD = (512, 512, 512)
+LARGE_RES = (3840, 2160)
+
+
+def orbit_camera(vpt, k, theta0, W, H, step_deg=1.0):
+    """Frame k of an orbit of radius 200 at height 150 around the world's
+    centre column, looking at the terrain there."""
+    X, Y, Z = LARGE_WORLD
+    th = np.radians(theta0 + step_deg * k)
+    pos = (X / 2 + 200.0 * np.cos(th), 150.0, Z / 2 + 200.0 * np.sin(th))
+    # yaw faces the centre; the terrain sits near y = 40
+    yaw = float(np.degrees(np.arctan2(Z / 2 - pos[2], X / 2 - pos[0])))
+    pitch = float(-np.degrees(np.arctan2(150.0 - 40.0, 200.0)))
+    return vpt.camera_from_pose(pos, yaw, pitch, 90.0, W / H)
+
+
+def large_section(vpt, torch, args, local):
+    """512^3 world, 3840x2160, 1 spp with 2 diffuse bounces, a seeded 64-frame
+    orbit with temporal reprojection, FP16 planes, the learned denoiser with
+    SVGF fallback: per-frame device ms (p50, p99) and the error against the
+    FP64 ground truth on 4 sampled frames."""
+    from voxelpathtracer_gb300 import learned, quality
+    X, Y, Z = LARGE_WORLD
+    W, H = LARGE_RES
+    rng = np.random.default_rng(0)
+    theta0 = float(rng.uniform(0.0, 360.0))
+    t0 = time.perf_counter()
+    vox = vpt.generate_world(X, Y, Z, seed=0)
+    blocks = vpt.generate_block_table(100, seed=0)
+    gen_s = time.perf_counter() - t0
+    net = None
+    if learned.WEIGHTS.exists():
+        net = vpt.UNet(1, H, W, device=local)
+        net.set_params(learned.load()[0])
+    sampled = (15, 31, 47, 63)
+    crop = (W // 2 - 320, H // 2 - 180, 640, 360)
+    x0, y0, cw, ch = crop
+    ms, crops, used_all = [], {}, []
+    with vpt.Context(width=W, height=H, device=local, storage=1, bounces=2) as ctx:
+        ctx.upload_world(vox)
+        ctx.set_block_table(blocks)
+        ctx.build_df()
+        ctx.synchronize()
+        stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
+        with torch.cuda.stream(stream):
+            for k in range(3):   # warm-up on the first camera, then a fresh history
+                ctx.render_frame_learned(orbit_camera(vpt, 0, theta0, W, H), frame_at(vpt, 0), net, readback=False)
+            torch.cuda.synchronize()
+            ctx.reset_history()
+            for k in range(64):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                _, used = ctx.render_frame_learned(orbit_camera(vpt, k, theta0, W, H), frame_at(vpt, k), net,
+                                                   readback=False)
+                e1.record(stream)
+                e1.synchronize()
+                ms.append(e0.elapsed_time(e1))
+                used_all.append(used)
+                if k in sampled:
+                    # the colour plane is not part of the swapped history: it still holds this frame
+                    crops[k] = ctx.read_plane("COLOR")[y0:y0 + ch, x0:x0 + cw].astype(np.float64)
+    if net is not None:
+        net.close()
+    errs = {}
+    if not args.no_quality:
+        with quality.make_gt_context(W, H, vox, blocks, device=local, bounces=2) as g:
+            for k in sampled:
+                gt, _ = quality.ground_truth_color(g, orbit_camera(vpt, k, theta0, W, H), frame_at(vpt, k), crop,
+                                                   spp=1024)
+                errs[str(k)] = quality.rmse(crops[k], gt)
+    return {"world": list(LARGE_WORLD), "resolution": list(LARGE_RES), "spp": 1, "bounces": 2, "storage": "fp16",
+            "frames": 64, "orbit": {"radius": 200.0, "height": 150.0, "deg_per_frame": 1.0, "theta0_deg": theta0},
+            "denoiser": "learned" if all(used_all) else ("svgf fallback" if not any(used_all) else "mixed"),
+            "frame_ms_p50": float(np.percentile(ms, 50)), "frame_ms_p99": float(np.percentile(ms, 99)),
+            "frame_ms_max": float(max(ms)), "world_generate_s": gen_s,
+            "error_vs_fp64_gt": {"crop": list(crop), "gt_spp": 1024, "rmse_by_frame": errs}}
 
 
 # ------------------------------------------------------- CPU (oracle) arm --
@@ -544,6 +717,8 @@ def main():
     ap.add_argument("--no-variants", action="store_true", help="skip the FP16-storage variant")
     ap.add_argument("--no-quality", action="store_true", help="skip the ground-truth error measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-world batched comparison")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-denoiser measurements")
+    ap.add_argument("--no-large", action="store_true", help="skip the 512^3 / 3840x2160 combined run")
     ap.add_argument("--gt-spp", type=int, default=4096, help="samples per pixel of the FP64 ground truth")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the dominant kernel from an ncu capture")

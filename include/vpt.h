@@ -155,7 +155,8 @@ typedef enum vpt_pass {
     VPT_PASS_PRIMARY = 0, VPT_PASS_SHADOW = 1, VPT_PASS_DIFFUSE = 2, VPT_PASS_SPATIAL_INITIAL = 3,
     VPT_PASS_TEMPORAL = 4, VPT_PASS_VARIANCE = 5, VPT_PASS_ATROUS = 6, VPT_PASS_SHADE = 7,
     VPT_PASS_TRACE_FRAME = 8,        /* fused primary + shadow + diffuse (vpt_trace_frame) */
-    VPT_PASS_COUNT = 9
+    VPT_PASS_LEARNED = 9,            /* features + U-Net + colour write-back (vpt_render_frame_learned) */
+    VPT_PASS_COUNT = 10
 } vpt_pass;
 
 /* Launch-shape knobs of the fused trace kernel, picked by the autotuner. */
@@ -257,6 +258,11 @@ vpt_status vpt_reset_history(vpt_ctx* ctx);
  * (W*H*3 floats) and the call waits for it. prev_cam may be NULL on the
  * first frame (the camera of the previous call is used otherwise). */
 vpt_status vpt_render_frame(vpt_ctx* ctx, const vpt_camera* cam, const vpt_frame* frame, float* rgb_out);
+
+/* The colour pass from the denoised GI (source 0, as vpt_shade), from the
+ * temporally accumulated GI before any spatial filter (source 1) or from
+ * this frame's raw GI (source 2). */
+vpt_status vpt_shade_from(vpt_ctx* ctx, const vpt_frame* frame, int32_t source);
 
 /* High-spp ground truth of the diffuse GI over the crop [x0, x0+w) x [y0, y0+h)
  * of the frame whose primary rays were traced last (fp32 contexts only): spp
@@ -426,6 +432,24 @@ vpt_status vpt_unet_backward(vpt_unet* unet, const void* input, const float* tar
 vpt_status vpt_unet_adam(vpt_unet* unet, float lr, float beta1, float beta2, float eps);
 vpt_status vpt_unet_synchronize(vpt_unet* unet);   /* also reports timed-out waits */
 vpt_status vpt_unet_get_stream(const vpt_unet* unet, void** stream);
+
+/* The learned frame path on a context (SVGF denoiser configured):
+ * vpt_learned_input traces the frame, runs the SVGF pre-filter, temporal and
+ * variance passes and shades from the temporal GI (COLOR then holds the
+ * network's noisy input); the frame stays open until vpt_end_frame.
+ * vpt_learned_features writes the 16-channel BF16 features of a crop
+ * ([h][w][16], device dst): log(1 + noisy RGB), block albedo, face normal,
+ * min(hit distance, 512) / 128, log(1 + SVGF variance), log(1 + RGB shaded
+ * from this frame's raw 1-spp GI), two zeros.
+ * vpt_render_frame_learned renders a whole frame with the network as the
+ * spatial denoiser, which predicts a log-space correction of the noisy colour
+ * (COLOR = exp(log(1 + noisy) + out) - 1), and falls back to the SVGF path
+ * (5 a-trous iterations) when net is NULL or the image size is not a
+ * multiple of 4; *used_net tells which ran. rgb_out as in vpt_render_frame. */
+vpt_status vpt_learned_input(vpt_ctx* ctx, const vpt_camera* cam, const vpt_frame* frame);
+vpt_status vpt_learned_features(vpt_ctx* ctx, int32_t x0, int32_t y0, int32_t w, int32_t h, void* dst);
+vpt_status vpt_render_frame_learned(vpt_ctx* ctx, vpt_unet* net, const vpt_camera* cam, const vpt_frame* frame,
+                                    float* rgb_out, int32_t* used_net);
 
 /* ---------------------------------------------------------- host helpers -- */
 /* Seeded value-noise terrain (heightmap h = 40 + 16*fbm, 4 octaves, base

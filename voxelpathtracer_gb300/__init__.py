@@ -44,7 +44,8 @@ PLANES = [
     "COLOR",
 ]
 PLANE = {name: i for i, name in enumerate(PLANES)}
-PASSES = ["primary", "shadow", "diffuse", "spatial_initial", "temporal", "variance", "atrous", "shade", "trace_frame"]
+PASSES = ["primary", "shadow", "diffuse", "spatial_initial", "temporal", "variance", "atrous", "shade", "trace_frame",
+          "learned"]
 FACE_MISS = 10
 
 
@@ -193,6 +194,10 @@ def _load() -> C.CDLL:
         "vpt_batch_read_stats": ([P, C.POINTER(Stats)], C.c_int),
         "vpt_batch_launch_count": ([P, C.POINTER(u64)], C.c_int),
         "vpt_batch_get_stream": ([P, C.POINTER(P)], C.c_int),
+        "vpt_shade_from": ([P, C.POINTER(Frame), i32], C.c_int),
+        "vpt_learned_input": ([P, C.POINTER(Camera), C.POINTER(Frame)], C.c_int),
+        "vpt_learned_features": ([P, i32, i32, i32, i32, P], C.c_int),
+        "vpt_render_frame_learned": ([P, P, C.POINTER(Camera), C.POINTER(Frame), P, C.POINTER(i32)], C.c_int),
         "vpt_nn_conv3x3": ([P, i32, i32, P, i32, i32, i32, i32, P, P, i32, i32, P, P, P, P], C.c_int),
         "vpt_nn_conv3x3_dw": ([P, i32, i32, P, i32, i32, i32, i32, P, i32, P, P], C.c_int),
         "vpt_nn_status": ([P], C.c_int),
@@ -434,6 +439,31 @@ class Context:
         nbytes, ch, dt = C.c_size_t(), C.c_int32(), C.c_int32()
         self._ck(lib.vpt_plane_info(self._h, pid, C.byref(nbytes), C.byref(ch), C.byref(dt)), "vpt_plane_info")
         return pid, nbytes.value, ch.value, _NP_DTYPE[dt.value]
+
+    def shade_from(self, frame: Frame, source: int):
+        """Colour pass from the denoised GI (0) or the temporal GI before spatial filtering (1)."""
+        self._ck(lib.vpt_shade_from(self._h, C.byref(frame), source), "vpt_shade_from")
+
+    def learned_input(self, cam: Camera, frame: Frame):
+        self._ck(lib.vpt_learned_input(self._h, C.byref(cam), C.byref(frame)), "vpt_learned_input")
+
+    def learned_features(self, crop, out):
+        """16-channel BF16 features of crop (x0, y0, w, h) into the torch tensor `out` [h, w, 16]."""
+        x0, y0, w, h = crop
+        if tuple(out.shape[-3:]) != (h, w, 16) or not out.is_contiguous():
+            raise ValueError("out must be a contiguous [h, w, 16] bfloat16 tensor")
+        self._ck(lib.vpt_learned_features(self._h, x0, y0, w, h, out.data_ptr()), "vpt_learned_features")
+
+    def render_frame_learned(self, cam: Camera, frame: Frame, net=None, out: np.ndarray | None = None,
+                             readback: bool = True):
+        """A frame with the U-Net as spatial denoiser (SVGF fallback when net is None); returns (rgb, used_net)."""
+        if readback and out is None:
+            out = np.empty((self.height, self.width, 3), dtype=np.float32)
+        used = C.c_int32()
+        self._ck(lib.vpt_render_frame_learned(self._h, net._h if net is not None else None, C.byref(cam),
+                                              C.byref(frame), _ptr(out) if readback else None, C.byref(used)),
+                 "vpt_render_frame_learned")
+        return out, bool(used.value)
 
     def read_plane(self, plane) -> np.ndarray:
         pid, nbytes, ch, dt = self.plane_info(plane)

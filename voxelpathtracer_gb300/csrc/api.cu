@@ -104,6 +104,11 @@ struct vpt_ctx {
     uint64_t launches = 0;
     std::vector<void*> allocs;
     std::vector<float> host_staging;
+    // learned denoiser: full-frame feature tensor, the colour shaded from the
+    // raw 1-spp GI, and the cross-stream events
+    void* feat = nullptr;
+    void* color_raw = nullptr;
+    cudaEvent_t ev_net[2] = {};
 };
 
 namespace {
@@ -417,6 +422,8 @@ vpt_status vpt_destroy(vpt_ctx* c) {
     for (int p = 0; p < VPT_PASS_COUNT; p++)
         for (int k = 0; k < 2; k++)
             if (c->ev[p][k]) cudaEventDestroy(c->ev[p][k]);
+    for (int k = 0; k < 2; k++)
+        if (c->ev_net[k]) cudaEventDestroy(c->ev_net[k]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return VPT_OK;
@@ -684,8 +691,13 @@ vpt_status vpt_get_tuning(const vpt_ctx* c, vpt_tuning* t) {
     return VPT_OK;
 }
 
-vpt_status vpt_svgf(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f) {
-    if (!c) return VPT_ERR_INVALID_ARG;
+}  // extern "C"
+
+namespace {
+
+// The denoiser passes of one frame; `atrous` false stops after the SVGF
+// variance pass (the learned path reads the temporal output instead).
+vpt_status svgf_run(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f, bool atrous) {
     vpt_status s = check_frame(c, f);
     if (s != VPT_OK) return s;
     cudaSetDevice(c->dev);
@@ -752,6 +764,7 @@ vpt_status vpt_svgf(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f) 
                         c->stream));
     pass_end(c, VPT_PASS_VARIANCE);
     c->launches += 3;
+    if (!atrous) return VPT_OK;
     // a-trous iterations with steps 16, 8, 4, 2, 1 (:2481-2610)
     const float tmod = f->time * 100.493850275f;
     pass_begin(c, VPT_PASS_ATROUS);
@@ -782,8 +795,11 @@ vpt_status vpt_svgf(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f) 
     return VPT_OK;
 }
 
-vpt_status vpt_shade(vpt_ctx* c, const vpt_frame* f) {
-    if (!c) return VPT_ERR_INVALID_ARG;
+// The colour pass. source 0: the denoised GI (last a-trous output, or the
+// variance / temporal output without a-trous iterations); 1: the temporally
+// accumulated GI before any spatial filter; 2: the raw GI of this frame.
+// Writes `out` (the COLOR plane when NULL).
+vpt_status shade_run(vpt_ctx* c, const vpt_frame* f, int source, void* out = nullptr) {
     vpt_status s = check_world(c);
     if (s != VPT_OK) return s;
     if ((s = check_frame(c, f)) != VPT_OK) return s;
@@ -805,13 +821,136 @@ vpt_status vpt_shade(vpt_ctx* c, const vpt_frame* f) {
     const void* cocg = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_COCG]
                                                     : (plain ? c->hist[c->cur][HI_COCG] : c->var[FI_COCG]);
     const void* ao = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_AOSKY] : c->hist[c->cur][HI_AOSKY];
+    if (source == 1) {
+        sh = c->hist[c->cur][HI_SH];
+        cocg = c->hist[c->cur][HI_COCG];
+        ao = c->hist[c->cur][HI_AOSKY];
+    } else if (source == 2) {
+        sh = c->gi[GI_SH];
+        cocg = c->gi[GI_COCG];
+        ao = c->gi[GI_AOSKY];
+    }
     pass_begin(c, VPT_PASS_SHADE);
     CK(c, shade(world_view(c), cam_view(c->cam), c->cfg.width, c->cfg.height, c->fp16, a, c->gbuf[c->cur][GB_T],
                 (const uint8_t*)c->gbuf[c->cur][GB_FACE], (const uint8_t*)c->gbuf[c->cur][GB_BLOCK], c->shadow, sh, cocg,
-                ao, c->color, c->stream));
+                ao, out ? out : c->color, c->stream));
     pass_end(c, VPT_PASS_SHADE);
     c->launches += 1;
     return VPT_OK;
+}
+
+vpt_status trace_all(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f) {
+    vpt_status s;
+    if (c->tuning.fused_trace) return vpt_trace_frame(c, cam, f);
+    if ((s = vpt_trace_primary(c, cam)) != VPT_OK) return s;
+    if ((s = vpt_trace_shadow(c, f)) != VPT_OK) return s;
+    return vpt_trace_diffuse(c, f);
+}
+
+vpt_status read_color(vpt_ctx* c, float* rgb_out) {
+    const size_t n = c->npx * 3;
+    if (c->fp16) {
+        std::vector<__half> tmp(n);
+        CK(c, cudaMemcpyAsync(tmp.data(), c->color, n * 2, cudaMemcpyDeviceToHost, c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));
+        for (size_t k = 0; k < n; k++) rgb_out[k] = __half2float(tmp[k]);
+    } else {
+        CK(c, cudaMemcpyAsync(rgb_out, c->color, n * 4, cudaMemcpyDeviceToHost, c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));
+    }
+    return VPT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+vpt_status vpt_svgf(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    return svgf_run(c, prev_cam, f, true);
+}
+
+vpt_status vpt_shade(vpt_ctx* c, const vpt_frame* f) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    return shade_run(c, f, 0);
+}
+
+vpt_status vpt_shade_from(vpt_ctx* c, const vpt_frame* f, int32_t source) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (source < 0 || source > 2) return fail(c, VPT_ERR_INVALID_ARG, "shade source must be 0, 1 or 2");
+    return shade_run(c, f, source);
+}
+
+vpt_status vpt_learned_input(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (!cam || !f) return fail(c, VPT_ERR_INVALID_ARG, "camera and frame are required");
+    if (c->cfg.denoiser != VPT_DENOISER_SVGF) return fail(c, VPT_ERR_STATE, "the learned path needs the SVGF denoiser");
+    const vpt_camera prev = c->have_prev ? c->prev_cam : *cam;
+    vpt_status s;
+    if ((s = trace_all(c, cam, f)) != VPT_OK) return s;
+    if ((s = svgf_run(c, &prev, f, false)) != VPT_OK) return s;
+    if (!c->color_raw && (s = dalloc(c, &c->color_raw, c->npx * 3 * (c->fp16 ? 2 : 4))) != VPT_OK) return s;
+    if ((s = shade_run(c, f, 2, c->color_raw)) != VPT_OK) return s;
+    return shade_run(c, f, 1);
+}
+
+vpt_status vpt_learned_features(vpt_ctx* c, int32_t x0, int32_t y0, int32_t w, int32_t h, void* dst) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (!dst || w < 1 || h < 1 || w > 16384 || h > 16384) return fail(c, VPT_ERR_INVALID_ARG, "bad crop or NULL dst");
+    if (!c->blocks) return fail(c, VPT_ERR_STATE, "no block table set");
+    cudaSetDevice(c->dev);
+    if (!c->color_raw) return fail(c, VPT_ERR_STATE, "call vpt_learned_input first");
+    CK(c, learned_features(c->cfg.width, c->cfg.height, x0, y0, w, h, c->fp16, c->color, c->color_raw,
+                           c->gbuf[c->cur][GB_T],
+                           (const uint8_t*)c->gbuf[c->cur][GB_FACE], (const uint8_t*)c->gbuf[c->cur][GB_BLOCK],
+                           c->blocks, c->n_blocks, c->var[FI_VAR], dst, c->stream));
+    c->launches += 1;
+    return VPT_OK;
+}
+
+vpt_status vpt_render_frame_learned(vpt_ctx* c, vpt_unet* net, const vpt_camera* cam, const vpt_frame* f,
+                                    float* rgb_out, int32_t* used_net) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (!cam || !f) return fail(c, VPT_ERR_INVALID_ARG, "camera and frame are required");
+    if (used_net) *used_net = 0;
+    const int W = c->cfg.width, H = c->cfg.height;
+    const bool fits = net && c->cfg.denoiser == VPT_DENOISER_SVGF && (W % 4) == 0 && (H % 4) == 0;
+    vpt_status s;
+    if (!fits) {
+        // SVGF fallback: the plain frame
+        const vpt_camera prev = c->have_prev ? c->prev_cam : *cam;
+        if ((s = trace_all(c, cam, f)) != VPT_OK) return s;
+        if ((s = svgf_run(c, &prev, f, true)) != VPT_OK) return s;
+        if ((s = shade_run(c, f, 0)) != VPT_OK) return s;
+    } else {
+        if ((s = vpt_learned_input(c, cam, f)) != VPT_OK) return s;
+        cudaSetDevice(c->dev);
+        if (!c->feat) {
+            if ((s = dalloc(c, &c->feat, c->npx * 16 * 2)) != VPT_OK) return s;
+            for (int k = 0; k < 2; k++)
+                if (!c->ev_net[k]) CK(c, cudaEventCreateWithFlags(&c->ev_net[k], cudaEventDisableTiming));
+        }
+        void* ns = nullptr;
+        if ((s = vpt_unet_get_stream(net, &ns)) != VPT_OK) return fail(c, s, "learned denoiser: bad network");
+        pass_begin(c, VPT_PASS_LEARNED);
+        CK(c, learned_features(W, H, 0, 0, W, H, c->fp16, c->color, c->color_raw, c->gbuf[c->cur][GB_T],
+                               (const uint8_t*)c->gbuf[c->cur][GB_FACE], (const uint8_t*)c->gbuf[c->cur][GB_BLOCK],
+                               c->blocks, c->n_blocks, c->var[FI_VAR], c->feat, c->stream));
+        CK(c, cudaEventRecord(c->ev_net[0], c->stream));
+        CK(c, cudaStreamWaitEvent((cudaStream_t)ns, c->ev_net[0], 0));
+        s = vpt_unet_forward(net, c->feat, 1, H, W, nullptr);
+        if (s != VPT_OK) return fail(c, s, "learned denoiser: %s", vpt_unet_last_error(net));
+        const float* out = nullptr;
+        vpt_unet_output(net, &out);
+        CK(c, cudaEventRecord(c->ev_net[1], (cudaStream_t)ns));
+        CK(c, cudaStreamWaitEvent(c->stream, c->ev_net[1], 0));
+        CK(c, learned_unpack(W, H, c->fp16, out, c->color, c->stream));
+        pass_end(c, VPT_PASS_LEARNED);
+        c->launches += 2;
+        if (used_net) *used_net = 1;
+    }
+    if (rgb_out && (s = read_color(c, rgb_out)) != VPT_OK) return s;
+    return vpt_end_frame(c);
 }
 
 vpt_status vpt_end_frame(vpt_ctx* c) {
@@ -836,27 +975,10 @@ vpt_status vpt_render_frame(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* 
     if (!cam || !f) return fail(c, VPT_ERR_INVALID_ARG, "camera and frame are required");
     vpt_status s;
     const vpt_camera prev = c->have_prev ? c->prev_cam : *cam;
-    if (c->tuning.fused_trace) {
-        if ((s = vpt_trace_frame(c, cam, f)) != VPT_OK) return s;
-    } else {
-        if ((s = vpt_trace_primary(c, cam)) != VPT_OK) return s;
-        if ((s = vpt_trace_shadow(c, f)) != VPT_OK) return s;
-        if ((s = vpt_trace_diffuse(c, f)) != VPT_OK) return s;
-    }
+    if ((s = trace_all(c, cam, f)) != VPT_OK) return s;
     if ((s = vpt_svgf(c, &prev, f)) != VPT_OK) return s;
     if ((s = vpt_shade(c, f)) != VPT_OK) return s;
-    if (rgb_out) {
-        size_t n = c->npx * 3;
-        if (c->fp16) {
-            std::vector<__half> tmp(n);
-            CK(c, cudaMemcpyAsync(tmp.data(), c->color, n * 2, cudaMemcpyDeviceToHost, c->stream));
-            CK(c, cudaStreamSynchronize(c->stream));
-            for (size_t k = 0; k < n; k++) rgb_out[k] = __half2float(tmp[k]);
-        } else {
-            CK(c, cudaMemcpyAsync(rgb_out, c->color, n * 4, cudaMemcpyDeviceToHost, c->stream));
-            CK(c, cudaStreamSynchronize(c->stream));
-        }
-    }
+    if (rgb_out && (s = read_color(c, rgb_out)) != VPT_OK) return s;
     return vpt_end_frame(c);
 }
 

@@ -238,6 +238,15 @@ cudaError_t shade(const WorldView& w, const CamView& cam, int W, int H, int fp16
                   const void* t, const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
                   const void* sh, const void* cocg, const void* aosky, void* rgb, cudaStream_t s);
 
+// ----------------------------------------------------------- learned.cu --
+// 16-channel BF16 features of the crop [x0, x0+w) x [y0, y0+h) into out
+// (w*h*16), and the network's FP32 output [W*H][16] back into the colour plane.
+cudaError_t learned_features(int W, int H, int x0, int y0, int w, int h, int fp16, const void* color,
+                             const void* color_raw, const void* t,
+                             const uint8_t* face, const uint8_t* block, const vpt_block* blocks, int n_blocks,
+                             const void* var, void* out, cudaStream_t s);
+cudaError_t learned_unpack(int W, int H, int fp16, const float* net_out, void* color, cudaStream_t s);
+
 // Deterministic-math probe: evaluates op `op` (0 exp, 1 exp2, 2 log2, 3 pow,
 // 4 sin, 5 cos) over n inputs on the device.
 cudaError_t detmath_eval(int op, const float* x, const float* y, float* out, int n, cudaStream_t s);
