@@ -35,6 +35,20 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
     return d;
 }
 
+// Descriptor of a swizzled K-major tile: rows of `row_bytes` (32 or 64; the
+// TMA box's inner extent) written with the matching TMA swizzle, 8-row
+// atoms SBO = 8 * row_bytes apart; layout type 6 = 32-byte swizzle, 4 =
+// 64-byte swizzle (bits 61-63). A K step inside the row advances the start
+// address by its byte offset.
+__device__ __forceinline__ uint64_t smem_desc_sw(uint32_t saddr, uint32_t row_bytes) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;                                   // LBO (unused for these layouts)
+    d |= (uint64_t)(((8u * row_bytes) >> 4) & 0x3FFFu) << 32;  // SBO
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)(row_bytes == 64u ? 4u : 6u) << 61;
+    return d;
+}
+
 // Instruction descriptor of kind::f16: FP32 D (bits 4-5 = 1), BF16 A and B
 // (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
@@ -113,6 +127,50 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* er
     }
     if (err) atomicCAS(err, 0, where);
     return false;
+}
+
+// As mbar_wait, for warp-specialised kernels: gives up at once when another
+// role has already set *abort, and sets it on its own timeout, so one stuck
+// wait ends every role's waits instead of each running out its limit.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, int* err, int where,
+                                                   volatile int* abort) {
+    for (int i = 0; i < 2000000; i++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*abort) return false;
+        if (i > 16) __nanosleep(64);
+    }
+    *abort = 1;
+    if (err) atomicCAS(err, 0, where);
+    return false;
+}
+
+// Arrival that also announces `bytes` of asynchronous (TMA) writes the
+// current phase must wait for.
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// TMA tiled loads (cp.async.bulk.tensor) into shared memory, completing on
+// the mbarrier's transaction count; coordinates innermost first. Elements
+// outside the tensor read as zero.
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const void* map, int c0, int c1, int c2, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+            dst),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const void* map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(dst),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 }  // namespace tc

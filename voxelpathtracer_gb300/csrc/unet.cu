@@ -9,16 +9,15 @@
 // `p1` at full resolution, which fuses the U-Net's upsample-and-concatenate
 // into the operand staging.
 //
-// Forward and backward-data convolution (k_conv3x3): one CTA of 128 threads
-// computes 128 consecutive pixels of one image row for all Np output
-// channels: GEMM M = 128 pixels, N = Np, K = 9 taps x Cin. For each tap the
-// 128 x Cin input rows and the Np x Cin weights are staged into shared memory
-// (two stages, so the loads of tap t+1 overlap the MMAs of tap t), one
-// thread issues Cin / 16 MMAs into the TMEM accumulator and commits them to
-// the stage's mbarrier, and the epilogue reads TMEM (warp w: pixels
-// 32w..32w+31), adds the bias, applies ReLU or a ReLU-derivative mask and
-// stores BF16 (or FP32). Backward-data is the same kernel with the weights
-// transposed and the taps flipped.
+// Forward and backward-data convolution (k_conv3x3): GEMM M = 128 pixels of
+// one image row, N = Np output channels, K = 9 taps x Cin, in persistent
+// warp-specialised CTAs: a TMA producer fills a ring of shared-memory stages
+// (one (tap, channel chunk) each; TMA's zero fill is the convolution's
+// padding), one thread issues the tcgen05 MMAs into double-buffered TMEM
+// accumulators, and four epilogue warps add the bias, apply ReLU or a
+// ReLU-derivative mask and store BF16 (or FP32) while the next tile's MMAs
+// run. Backward-data is the same kernel with the weights transposed and the
+// taps flipped. A two-source input is assembled into a scratch tensor first.
 //
 // Weight gradient (k_conv3x3_dw): dW[co][tap][ci] = sum_p dY[p][co] X[p+tap][ci].
 // One CTA handles one tap and a range of pixels: GEMM M = 128 (co, zero
@@ -31,7 +30,10 @@
 // TMEM before returning.
 #include <cuda_bf16.h>
 
+#include <cuda.h>
+
 #include <algorithm>
+#include <mutex>
 
 #include "tc.cuh"
 #include "unet.cuh"
@@ -80,102 +82,219 @@ __device__ __forceinline__ uint4 pack8(const float* f) {
     return u;
 }
 
-__global__ void __launch_bounds__(128, 1) k_conv3x3(ConvArgs a) {
+
+constexpr int kConvStages = 8;   // most shared-memory stages of (tap, channel chunk) operand tiles
+
+// Persistent, warp-specialised forward / backward-data convolution with TMA.
+// Operands sit in shared memory as TMA writes them: a box of (KC channels,
+// R rows) is R rows of KC * 2 bytes (64 or 32) with the 64- or 32-byte
+// swizzle, which the tensor core reads through a swizzled K-major descriptor
+// (8-row atoms 8 * KC * 2 bytes apart; a K step of 16 channels advances the
+// start by 32 bytes).
+//   warp 0      one lane: loads the weights of all 9 taps once (when they fit,
+//               `w_resident`), then for each (tap, channel chunk) stage of each
+//               tile issues the TMA box of the 128 input pixels x + dx of row
+//               y + dy (zero outside the image) - and the chunk's weights when
+//               they are not resident - into a ring of S <= kConvStages, announcing
+//               the bytes on the stage's `full` barrier.
+//   warp 1      one lane issues the stage's tcgen05 MMAs into one of two TMEM
+//               accumulators and releases the stage with a commit to `empty`;
+//               after a tile's last stage it commits `acc_full`.
+//   warps 2-5   epilogue: wait `acc_full`, read their 32 TMEM lanes, add bias,
+//               apply ReLU / mask, store, arrive on `acc_empty`, overlapping the
+//               next tile's MMAs in the other accumulator.
+// CTAs loop over 128-pixel row tiles (x fastest, so neighbouring CTAs share
+// input rows in L2).
+constexpr int kConvThreads = 192;
+__global__ void __launch_bounds__(kConvThreads, 1)
+    k_conv3x3(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_w, ConvArgs a, int KC,
+              int ntiles, int tiles_x, int w_resident, int box_w, int S) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ __align__(8) uint64_t full[kConvStages], empty[kConvStages], acc_full[2], acc_empty[2], wbar;
     __shared__ uint32_t s_taddr;
+    __shared__ volatile int s_abort;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int n = blockIdx.z, y = blockIdx.y, x0 = blockIdx.x * 128;
-    const int K = a.Cin, Np = a.Np, kch = K >> 3;
-    const uint32_t abytes = 128u * K * 2u, bbytes = (uint32_t)Np * K * 2u, stage = abytes + bbytes;
-    const uint32_t ncols = tmem_columns(Np);
-    const uint32_t bar0 = tc::smem_addr(&bars[0]), bar1 = tc::smem_addr(&bars[1]);
+    const int K = a.Cin, Np = a.Np, H = a.in.H, W = a.in.W;
+    const int nkc = K / KC, nit = 9 * nkc;
+    const uint32_t wbytes = w_resident ? 9u * K * Np * 2u : 0u;
+    const uint32_t abytes = 128u * KC * 2u, bbytes = w_resident ? 0u : (uint32_t)Np * KC * 2u;
+    const uint32_t stage = abytes + bbytes;
+    const uint32_t rb = (uint32_t)KC * 2u;          // bytes of one operand row
+    const uint32_t nblk = (uint32_t)Np * rb;        // bytes of one Np x KC weight block
+    // bytes one stage's boxes deliver (a box is box_w <= 128 pixels wide; rows
+    // past it hold stale data that only feeds accumulator rows the epilogue skips)
+    const uint32_t stage_tx = (uint32_t)box_w * rb + bbytes;
+    const uint32_t ncols = tmem_columns(2 * Np);
     if (warp == 0) tc::tmem_alloc(tc::smem_addr(&s_taddr), ncols);
     if (tid == 0) {
-        tc::mbar_init(bar0, 1);
-        tc::mbar_init(bar1, 1);
+        for (int k = 0; k < kConvStages; k++) {
+            tc::mbar_init(tc::smem_addr(&full[k]), 1);
+            tc::mbar_init(tc::smem_addr(&empty[k]), 1);
+        }
+        for (int k = 0; k < 2; k++) {
+            tc::mbar_init(tc::smem_addr(&acc_full[k]), 1);
+            tc::mbar_init(tc::smem_addr(&acc_empty[k]), 128);
+        }
+        tc::mbar_init(tc::smem_addr(&wbar), 1);
+        s_abort = 0;
         tc::mbar_init_fence();
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t taddr = s_taddr;
-    const uint32_t idesc = tc::idesc_bf16(128, Np);
-    bool ok = true;
-    for (int tap = 0; tap < 9; tap++) {
-        const int st = tap & 1;
-        const uint32_t bar = st ? bar1 : bar0;
-        if (tap >= 2) ok = tc::mbar_wait(bar, (uint32_t)(((tap >> 1) - 1) & 1), a.err, 1);
-        if (!__syncthreads_and(ok)) {
-            ok = false;
-            break;
+    const uint32_t wbase = tc::smem_addr(smem), ring = wbase + wbytes;
+
+    if (warp == 0) {
+        // ---------------------------------------------------------- producer
+        if (lane == 0) {
+            if (w_resident) {
+                // block (tap, chunk c) of Np rows x KC channels at (tap * nkc + c) * nblk
+                tc::mbar_expect_tx(tc::smem_addr(&wbar), wbytes);
+                for (int tap = 0; tap < 9; tap++)
+                    for (int c = 0; c < nkc; c++)
+                        tc::tma_load_3d(wbase + (uint32_t)(tap * nkc + c) * nblk, &tm_w, c * KC, tap, 0,
+                                        tc::smem_addr(&wbar));
+            }
+            int j = 0;
+            for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+                const int xb = tile % tiles_x, ry = tile / tiles_x;
+                const int y = ry % H, n = ry / H, x0 = xb * 128;
+                bool ok = true;
+                for (int it = 0; it < nit; it++, j++) {
+                    const int st = j % S;
+                    if (j >= S &&
+                        !tc::mbar_wait_or_abort(tc::smem_addr(&empty[st]), (uint32_t)(((j / S) - 1) & 1),
+                                                a.err, 1, &s_abort)) {
+                        ok = false;
+                        break;
+                    }
+                    const int tap = it / nkc, c0 = (it - tap * nkc) * KC;
+                    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+                    const uint32_t sa = ring + st * stage, sb = sa + abytes;
+                    const uint32_t bar = tc::smem_addr(&full[st]);
+                    tc::mbar_expect_tx(bar, stage_tx);
+                    tc::tma_load_4d(sa, &tm_in, c0, x0 + dx, y + dy, n, bar);
+                    if (!w_resident) tc::tma_load_3d(sb, &tm_w, c0, tap, 0, bar);
+                }
+                if (!ok) break;
+            }
         }
-        uint8_t* sa = smem + st * stage;
-        uint8_t* sb = sa + abytes;
-        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-        for (int idx = tid; idx < 128 * kch; idx += 128) {
-            const int m = idx / kch, c8 = idx - m * kch;
-            *reinterpret_cast<uint4*>(sa + tc::tile_offset(m, c8 * 8, K)) =
-                load8(a.in, n, y + dy, x0 + m + dx, c8 * 8);
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---------------------------------------------------------- MMA issue
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16(128, Np);
+            int j = 0, tcount = 0;
+            bool ok = !w_resident || tc::mbar_wait_or_abort(tc::smem_addr(&wbar), 0u, a.err, 5, &s_abort);
+            for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, tcount++) {
+                const int buf = tcount & 1;
+                if (tcount >= 2 &&
+                    !tc::mbar_wait_or_abort(tc::smem_addr(&acc_empty[buf]), (uint32_t)(((tcount >> 1) - 1) & 1),
+                                            a.err, 2, &s_abort))
+                    break;
+                tc::fence_after_sync();
+                const uint32_t d = taddr + (uint32_t)(buf * Np);
+                for (int it = 0; it < nit; it++, j++) {
+                    const int st = j % S;
+                    if (!tc::mbar_wait_or_abort(tc::smem_addr(&full[st]), (uint32_t)((j / S) & 1), a.err, 3,
+                                                &s_abort)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::fence_after_sync();
+                    const int tap = it / nkc, c = it - tap * nkc;
+                    const uint32_t a0 = ring + st * stage;
+                    const uint32_t b0 = w_resident ? wbase + (uint32_t)(tap * nkc + c) * nblk : a0 + abytes;
+                    for (int k = 0; k < KC / 16; k++)
+                        tc::mma_bf16(d, tc::smem_desc_sw(a0 + 32u * k, rb), tc::smem_desc_sw(b0 + 32u * k, rb), idesc,
+                                     (it | k) != 0 ? 1u : 0u);
+                    tc::mma_commit(tc::smem_addr(&empty[st]));
+                }
+                if (ok) tc::mma_commit(tc::smem_addr(&acc_full[buf]));
+            }
         }
-        for (int idx = tid; idx < Np * kch; idx += 128) {
-            const int r = idx / kch, c8 = idx - r * kch;
-            *reinterpret_cast<uint4*>(sb + tc::tile_offset(r, c8 * 8, K)) =
-                ldg16(a.w + ((size_t)r * 9 + tap) * K + c8 * 8);
-        }
-        tc::fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
+        __syncwarp();
+    } else {
+        // ---------------------------------------------------------- epilogue
+        const int q = warp & 3;                 // TMEM lane quarter of this warp
+        const int m = q * 32 + lane;
+        int tcount = 0;
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, tcount++) {
+            const int buf = tcount & 1;
+            if (!tc::mbar_wait_or_abort(tc::smem_addr(&acc_full[buf]), (uint32_t)((tcount >> 1) & 1), a.err, 4,
+                                        &s_abort))
+                break;
             tc::fence_after_sync();
-            const uint32_t a0 = tc::smem_addr(sa), b0 = tc::smem_addr(sb);
-            const uint32_t sbo = (uint32_t)K * 16u;
-            for (int k = 0; k < K / 16; k++)
-                tc::mma_bf16(taddr, tc::smem_desc(a0 + 256u * k, 128u, sbo), tc::smem_desc(b0 + 256u * k, 128u, sbo),
-                             idesc, (tap | k) != 0 ? 1u : 0u);
-            tc::mma_commit(bar);
+            const int xb = tile % tiles_x, ry = tile / tiles_x;
+            const int y = ry % H, n = ry / H, x = xb * 128 + m;
+            const bool valid = x < W;
+            const size_t p = ((size_t)n * H + y) * W + x;
+            for (int c0 = 0; c0 < Np; c0 += 16) {
+                float v[16];
+                tc::tmem_ld16(taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * Np + c0), v);
+                if (!valid) continue;
+                if (a.bias) {
+                    const float4* bb = reinterpret_cast<const float4*>(a.bias + c0);
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        const float4 b4 = __ldg(bb + k);
+                        v[4 * k] += b4.x;
+                        v[4 * k + 1] += b4.y;
+                        v[4 * k + 2] += b4.z;
+                        v[4 * k + 3] += b4.w;
+                    }
+                }
+                if (a.relu) {
+#pragma unroll
+                    for (int k = 0; k < 16; k++) v[k] = fmaxf(v[k], 0.0f);
+                }
+                if (a.mask) {
+                    float mk[16];
+                    unpack8(ldg16(a.mask + p * Np + c0), mk);
+                    unpack8(ldg16(a.mask + p * Np + c0 + 8), mk + 8);
+#pragma unroll
+                    for (int k = 0; k < 16; k++) v[k] = mk[k] > 0.0f ? v[k] : 0.0f;
+                }
+                if (a.out) {
+                    uint4* o = reinterpret_cast<uint4*>(a.out + p * Np + c0);
+                    o[0] = pack8(v);
+                    o[1] = pack8(v + 8);
+                }
+                if (a.out_f32) {
+                    float4* o = reinterpret_cast<float4*>(a.out_f32 + p * Np + c0);
+#pragma unroll
+                    for (int k = 0; k < 4; k++) o[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+                }
+            }
+            tc::fence_before_sync();
+            tc::mbar_arrive(tc::smem_addr(&acc_empty[buf]));
         }
     }
-    // the commit of tap 8 (stage 0, its fifth phase) covers every MMA issued
-    if (ok) ok = tc::mbar_wait(bar0, 0u, a.err, 2);
-    else tc::mbar_wait(bar0, 0u, nullptr, 0);
-    ok = __syncthreads_and(ok);
-    tc::fence_after_sync();
-    const int m = warp * 32 + lane, x = x0 + m;
-    const bool valid = ok && x < a.in.W;
-    const size_t p = ((size_t)n * a.in.H + y) * a.in.W + x;
-    for (int c0 = 0; c0 < Np; c0 += 16) {
-        float v[16];
-        tc::tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-        if (!valid) continue;
-        if (a.bias) {
-#pragma unroll
-            for (int k = 0; k < 16; k++) v[k] += __ldg(a.bias + c0 + k);
-        }
-        if (a.relu) {
-#pragma unroll
-            for (int k = 0; k < 16; k++) v[k] = fmaxf(v[k], 0.0f);
-        }
-        if (a.mask) {
-            float mk[16];
-            unpack8(ldg16(a.mask + p * Np + c0), mk);
-            unpack8(ldg16(a.mask + p * Np + c0 + 8), mk + 8);
-#pragma unroll
-            for (int k = 0; k < 16; k++) v[k] = mk[k] > 0.0f ? v[k] : 0.0f;
-        }
-        if (a.out) {
-            uint4* o = reinterpret_cast<uint4*>(a.out + p * Np + c0);
-            o[0] = pack8(v);
-            o[1] = pack8(v + 8);
-        }
-        if (a.out_f32) {
-            float4* o = reinterpret_cast<float4*>(a.out_f32 + p * Np + c0);
-#pragma unroll
-            for (int k = 0; k < 4; k++) o[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    // on an abort, give copies and MMAs still in flight a bounded moment before TMEM is freed
+    if (s_abort && warp == 1 && lane == 0) {
+        for (int k = 0; k < kConvStages; k++) {
+            tc::mbar_wait(tc::smem_addr(&full[k]), 0u, nullptr, 0);
+            tc::mbar_wait(tc::smem_addr(&empty[k]), 0u, nullptr, 0);
         }
     }
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_free(taddr, ncols);
+}
+
+// The two-source input of a decoder convolution, assembled: channels [0, C0)
+// nearest-upsampled from the half-size p0, channels [C0, C0 + C1) from p1.
+__global__ void k_upcat(ConvSrc s, bf16* out) {
+    const int C = s.C0 + s.C1, c8n = C >> 3;
+    const long long total = (long long)s.N * s.H * s.W * c8n;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c8 = (int)(i % c8n);
+        const long long q = i / c8n;
+        const int x = (int)(q % s.W), y = (int)((q / s.W) % s.H), n = (int)(q / ((long long)s.W * s.H));
+        *reinterpret_cast<uint4*>(out + (size_t)q * C + c8 * 8) = load8(s, n, y, x, c8 * 8);
+    }
 }
 
 __global__ void __launch_bounds__(128, 1) k_conv3x3_dw(DwArgs a) {
@@ -413,19 +532,114 @@ __global__ void k_weights_bf16(const float* w, bf16* wf, bf16* wb, int Np, int C
 
 }  // namespace
 
-size_t conv3x3_smem(int Cin, int Np) { return 2u * (128u * Cin * 2u + (size_t)Np * Cin * 2u); }
+static unsigned ew_grid(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 152LL * 16); }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+// BF16 tensor map of `rank` dims (innermost first), boxes of `box`, zero fill,
+// with the shared-memory swizzle `swz`.
+static bool make_map(CUtensorMap* m, const void* base, int rank, const cuuint64_t* dims, const cuuint64_t* strides,
+                     const cuuint32_t* box, CUtensorMapSwizzle swz) {
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return false;
+    cuuint32_t es[5] = {1, 1, 1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, const_cast<void*>(base), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Channel chunk of one pipeline stage and whether all 9 taps of weights stay
+// in shared memory, within the shared-memory budget.
+// The ring has as many stages (3..kConvStages) as leave room for two CTAs per SM.
+struct ConvPlan {
+    int kc, resident, stages;
+    size_t smem;
+};
+static ConvPlan conv_plan(int Cin, int Np) {
+    ConvPlan p;
+    p.kc = Cin % 32 == 0 ? 32 : 16;
+    const size_t wbytes = 9u * (size_t)Cin * Np * 2u;
+    p.resident = wbytes <= 80u * 1024u;
+    const size_t stage = 128u * p.kc * 2u + (p.resident ? 0u : (size_t)Np * p.kc * 2u);
+    const size_t fixed = p.resident ? wbytes : 0u, budget = 108u * 1024u;
+    long long s = budget > fixed ? (long long)((budget - fixed) / stage) : 0;
+    p.stages = (int)std::max(3LL, std::min((long long)kConvStages, s));
+    p.smem = fixed + (size_t)p.stages * stage;
+    return p;
+}
+
+size_t conv3x3_smem(int Cin, int Np) { return conv_plan(Cin, Np).smem; }
+
+// Persistent CTAs per SM for a conv: limited by shared memory and by TMEM
+// (two accumulators of Np columns each, 512 columns per SM).
+static int conv_ctas_per_sm(int Np, size_t smem) {
+    const int by_tmem = 512 / (int)tmem_columns(2 * Np);
+    const int by_smem = (int)((220u * 1024u) / (smem + 2048u));
+    return std::max(1, std::min(std::min(by_tmem, by_smem), 2));
+}
+
 size_t conv3x3_dw_smem(int Cin) { return 2u * (128u * 128u * 2u + (size_t)Cin * 128u * 2u); }
 
 cudaError_t conv3x3(const ConvArgs& a, cudaStream_t s) {
     if (a.Cin != a.in.C0 + a.in.C1 || a.Cin % 16 || a.Cin < 16 || a.Cin > 256 || a.Np % 16 || a.Np < 16 ||
-        a.Np > 256 || (a.in.up0 && ((a.in.H | a.in.W) & 1)) || (a.in.C0 % 8) || (a.in.C1 % 8))
+        a.Np > 256 || (a.in.up0 && ((a.in.H | a.in.W) & 1)) || (a.in.C0 % 8) || (a.in.C1 % 8) || !a.w)
         return cudaErrorInvalidValue;
-    const size_t sm = conv3x3_smem(a.Cin, a.Np);
-    if (sm > 200 * 1024) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const long long P = (long long)a.in.N * a.in.H * a.in.W;
+    // a single-source input is read in place; a two-source one is assembled first
+    const bf16* src = a.in.p0;
+    if (a.in.up0 || a.in.C1 > 0) {
+        if (!a.scratch) return cudaErrorInvalidValue;
+        k_upcat<<<ew_grid(P * (a.Cin / 8)), 256, 0, s>>>(a.in, a.scratch);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        src = a.scratch;
+    }
+    const ConvPlan plan = conv_plan(a.Cin, a.Np);
+    if (plan.smem > 200u * 1024u) return cudaErrorInvalidValue;
+    CUtensorMap tm_in, tm_w;
+    const cuuint64_t din[4] = {(cuuint64_t)a.Cin, (cuuint64_t)a.in.W, (cuuint64_t)a.in.H, (cuuint64_t)a.in.N};
+    const cuuint64_t sin[3] = {(cuuint64_t)a.Cin * 2u, (cuuint64_t)a.Cin * 2u * a.in.W,
+                               (cuuint64_t)a.Cin * 2u * a.in.W * a.in.H};
+    const int box_w = a.in.W < 128 ? a.in.W : 128;
+    const cuuint32_t kc = (cuuint32_t)plan.kc;
+    const CUtensorMapSwizzle swz = plan.kc == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
+    const cuuint32_t bin[4] = {kc, (cuuint32_t)box_w, 1u, 1u};
+    const cuuint64_t dw[3] = {(cuuint64_t)a.Cin, 9u, (cuuint64_t)a.Np};
+    const cuuint64_t sw[2] = {(cuuint64_t)a.Cin * 2u, (cuuint64_t)a.Cin * 2u * 9u};
+    const cuuint32_t bw[3] = {kc, 1u, (cuuint32_t)a.Np};
+    if (!make_map(&tm_in, src, 4, din, sin, bin, swz) || !make_map(&tm_w, a.w, 3, dw, sw, bw, swz))
+        return cudaErrorInvalidValue;
+    ConvArgs b = a;
+    b.in = ConvSrc{src, a.Cin, 0, nullptr, 0, a.in.N, a.in.H, a.in.W};
+    cudaError_t e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem);
     if (e != cudaSuccess) return e;
-    dim3 grid((unsigned)((a.in.W + 127) / 128), (unsigned)a.in.H, (unsigned)a.in.N);
-    k_conv3x3<<<grid, 128, sm, s>>>(a);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    const int tiles_x = (a.in.W + 127) / 128;
+    const long long ntiles = (long long)tiles_x * a.in.H * a.in.N;
+    if (ntiles > (1LL << 30)) return cudaErrorInvalidValue;
+    const int grid = (int)std::min<long long>(ntiles, (long long)sms * conv_ctas_per_sm(a.Np, plan.smem));
+    k_conv3x3<<<grid, kConvThreads, plan.smem, s>>>(tm_in, tm_w, b, plan.kc, (int)ntiles, tiles_x, plan.resident,
+                                                     box_w, plan.stages);
     return cudaGetLastError();
 }
 
@@ -442,7 +656,6 @@ cudaError_t conv3x3_dw(const DwArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-static unsigned ew_grid(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 152LL * 16); }
 
 cudaError_t pool2(const bf16* in, bf16* out, int N, int H, int W, int C, cudaStream_t s) {
     k_pool2<<<ew_grid((long long)N * (H / 2) * (W / 2) * (C / 8)), 256, 0, s>>>(in, out, N, H, W, C);

@@ -31,6 +31,7 @@ struct ConvArgs {
     __nv_bfloat16* out;        // [P][Np] BF16 or null
     float* out_f32;            // [P][Np] FP32 or null
     int* err;                  // nonzero after a timed-out wait (which wait), or null
+    __nv_bfloat16* scratch;    // [P][Cin]: the concatenated input is assembled here when it has two sources
 };
 
 struct DwArgs {

@@ -95,6 +95,7 @@ struct vpt_unet {
     bf16* wb[kLayers] = {};    // backward-data weights
     // activations
     bf16 *e1a, *e1, *p1, *e2a, *e2, *p2, *e3a, *e3, *d2a, *d2, *d1a, *d1;
+    bf16 *cat2, *cat1;         // assembled decoder inputs [up(e3), e2] and [up(d2), e1]
     float* out = nullptr;
     // gradients
     bf16 *g_out, *g_d1, *g_d1a, *g_cat1, *g_d2, *g_d2a, *g_cat2, *g_e3, *g_e3a, *g_p2, *g_e2, *g_e2a, *g_p1, *g_e1,
@@ -150,6 +151,7 @@ ConvSrc src_cat(const bf16* low, int C0, const bf16* skip, int C1, int N, int H,
 
 vpt_status run_conv(vpt_unet* u, int l, const ConvSrc& in, const bf16* mask, bf16* out, float* out_f32) {
     ConvArgs a;
+    a.scratch = l == 6 ? u->cat2 : (l == 8 ? u->cat1 : nullptr);
     a.in = in;
     a.w = u->wf[l];
     a.bias = u->params + layer_offset(l) + (long long)kNet[l].cout * 9 * kNet[l].cin;
@@ -168,6 +170,7 @@ vpt_status run_conv(vpt_unet* u, int l, const ConvSrc& in, const bf16* mask, bf1
 // gradient `g` of its pre-activation output, times (mask > 0) when given.
 vpt_status run_conv_bwd(vpt_unet* u, int l, const bf16* g, int N, int H, int W, const bf16* mask, bf16* out) {
     ConvArgs a;
+    a.scratch = nullptr;
     a.in = src1(g, kNet[l].cout, N, H, W);
     a.w = u->wb[l];
     a.bias = nullptr;
@@ -298,6 +301,17 @@ vpt_status vpt_nn_conv3x3(const void* in0, int32_t c0, int32_t up0, const void* 
     cudaGetDevice(&dev);
     ConvArgs a;
     a.in = ConvSrc{(const bf16*)in0, c0, up0, (const bf16*)in1, c1, n, h, w};
+    a.scratch = nullptr;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (up0 || c1 > 0) {
+        // the assembled two-source input lives for this call, stream-ordered
+        void* tmp = nullptr;
+        if (cudaMallocAsync(&tmp, (size_t)n * h * w * (c0 + c1) * 2, st) != cudaSuccess) {
+            cudaGetLastError();
+            return VPT_ERR_OOM;
+        }
+        a.scratch = (bf16*)tmp;
+    }
     a.w = (const bf16*)weight;
     a.bias = bias;
     a.Cin = c0 + c1;
@@ -307,7 +321,9 @@ vpt_status vpt_nn_conv3x3(const void* in0, int32_t c0, int32_t up0, const void* 
     a.out = (bf16*)out_bf16;
     a.out_f32 = out_f32;
     a.err = err_word(dev);
-    return from_cuda(conv3x3(a, (cudaStream_t)stream));
+    const vpt_status r = from_cuda(conv3x3(a, st));
+    if (a.scratch) cudaFreeAsync(a.scratch, st);
+    return r;
 }
 
 vpt_status vpt_nn_conv3x3_dw(const void* in0, int32_t c0, int32_t up0, const void* in1, int32_t c1, int32_t n,
@@ -391,6 +407,7 @@ vpt_status vpt_unet_create(vpt_unet** out, int32_t device, int32_t max_images, i
     A(u->e2a, P2 * 64); A(u->e2, P2 * 64); A(u->p2, P4 * 64);
     A(u->e3a, P4 * 96); A(u->e3, P4 * 96);
     A(u->d2a, P2 * 64); A(u->d2, P2 * 64); A(u->d1a, P * 32); A(u->d1, P * 32);
+    A(u->cat2, P2 * 160); A(u->cat1, P * 96);
     A(u->out, P * 16);
     A(u->g_out, P * 16); A(u->g_d1, P * 32); A(u->g_d1a, P * 32); A(u->g_cat1, P * 96);
     A(u->g_d2, P2 * 64); A(u->g_d2a, P2 * 64); A(u->g_cat2, P2 * 160);
