@@ -185,6 +185,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
         // ---------------------------------------------------------- MMA issue
         if (lane == 0) {
             const uint32_t idesc = tc::idesc_bf16(128, Np);
+            const uint64_t adesc0 = tc::smem_desc_sw(ring, rb), wdesc0 = tc::smem_desc_sw(wbase, rb);
             int j = 0, tcount = 0;
             bool ok = !w_resident || tc::mbar_wait_or_abort(tc::smem_addr(&wbar), 0u, a.err, 5, &s_abort);
             for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, tcount++) {
@@ -204,11 +205,12 @@ __global__ void __launch_bounds__(kConvThreads, 1)
                     }
                     tc::fence_after_sync();
                     const int tap = it / nkc, c = it - tap * nkc;
-                    const uint32_t a0 = ring + st * stage;
-                    const uint32_t b0 = w_resident ? wbase + (uint32_t)(tap * nkc + c) * nblk : a0 + abytes;
+                    // descriptors differ only in the start-address field (address >> 4)
+                    const uint64_t ad = adesc0 + ((st * stage) >> 4);
+                    const uint64_t bd = w_resident ? wdesc0 + (((uint32_t)(tap * nkc + c) * nblk) >> 4)
+                                                   : adesc0 + ((st * stage + abytes) >> 4);
                     for (int k = 0; k < KC / 16; k++)
-                        tc::mma_bf16(d, tc::smem_desc_sw(a0 + 32u * k, rb), tc::smem_desc_sw(b0 + 32u * k, rb), idesc,
-                                     (it | k) != 0 ? 1u : 0u);
+                        tc::mma_bf16(d, ad + (uint64_t)(2u * k), bd + (uint64_t)(2u * k), idesc, (it | k) != 0 ? 1u : 0u);
                     tc::mma_commit(tc::smem_addr(&empty[st]));
                 }
                 if (ok) tc::mma_commit(tc::smem_addr(&acc_full[buf]));
@@ -276,6 +278,237 @@ __global__ void __launch_bounds__(kConvThreads, 1)
         for (int k = 0; k < kConvStages; k++) {
             tc::mbar_wait(tc::smem_addr(&full[k]), 0u, nullptr, 0);
             tc::mbar_wait(tc::smem_addr(&empty[k]), 0u, nullptr, 0);
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_free(taddr, ncols);
+}
+
+// 16-byte global -> shared copy; src_bytes 0 writes zeros.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+// One arrival on the mbarrier (not counted in its expected arrivals) once
+// every cp.async this thread issued before has landed.
+__device__ __forceinline__ void cp_async_arrive(uint32_t bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+constexpr int kRowBufs = 6;       // most resident input rows per CTA
+constexpr int kRowThreads = 288;  // 4 loader warps, 1 MMA warp, 4 epilogue warps
+
+// Row-resident convolution for layers whose weights fit in shared memory.
+// A CTA walks down vertical strips (a 128-pixel column tile, R output rows);
+// every input row segment x0-1 .. x0+128 is fetched once into a ring of
+// `nb` row buffers and serves three output rows and all three dx taps: the
+// tap (dy, dx) operand of output row y is row buffer (y + dy) read through a
+// descriptor that starts dx + 1 pixels in. A row buffer holds the segment as
+// K/8 blocks of 130 pixels x 8 channels (16 bytes a pixel), i.e. the
+// canonical K-major layout without swizzle (SBO = 128, LBO = 2080), in which a
+// one-pixel shift is a 16-byte start offset.
+//   warps 0-3   loaders: coalesced 16-byte cp.async of the row segment (zero
+//               outside the image), arriving on the buffer's `row_full`
+//               barrier as their copies land.
+//   warp 4      one lane: 9 taps x K/16 MMAs per output row into one of two
+//               TMEM accumulators, commits `acc_full`, and releases input row
+//               y - 1 (its last use) with a commit to `row_empty`.
+//   warps 5-8   epilogue, as in k_conv3x3.
+__global__ void __launch_bounds__(kRowThreads, 1)
+    k_conv3x3_rows(const __grid_constant__ CUtensorMap tm_w, ConvArgs a, int R, int nstrips, int tiles_x, int nb) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t row_full[kRowBufs], row_empty[kRowBufs], acc_full[2], acc_empty[2], wbar;
+    __shared__ uint32_t s_taddr;
+    __shared__ volatile int s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int K = a.Cin, Np = a.Np, H = a.in.H, W = a.in.W, G = K / 8;
+    const int strips_y = (H + R - 1) / R;
+    const uint32_t wbytes = 9u * K * Np * 2u;
+    const uint32_t nblk = (uint32_t)Np * 16u;        // one Np x 8-channel weight block
+    const uint32_t rowb = (uint32_t)G * 2080u;       // one row buffer
+    const uint32_t ncols = tmem_columns(2 * Np);
+    if (warp == 0) tc::tmem_alloc(tc::smem_addr(&s_taddr), ncols);
+    if (tid == 0) {
+        for (int k = 0; k < kRowBufs; k++) {
+            tc::mbar_init(tc::smem_addr(&row_full[k]), 128);
+            tc::mbar_init(tc::smem_addr(&row_empty[k]), 1);
+        }
+        for (int k = 0; k < 2; k++) {
+            tc::mbar_init(tc::smem_addr(&acc_full[k]), 1);
+            tc::mbar_init(tc::smem_addr(&acc_empty[k]), 128);
+        }
+        tc::mbar_init(tc::smem_addr(&wbar), 1);
+        s_abort = 0;
+        tc::mbar_init_fence();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t taddr = s_taddr;
+    const uint32_t wbase = tc::smem_addr(smem), rbase = wbase + wbytes;
+    const bf16* in = a.in.p0;
+
+    if (warp < 4) {
+        // ---------------------------------------------------------- loaders
+        if (tid == 0) {
+            tc::mbar_expect_tx(tc::smem_addr(&wbar), wbytes);
+            for (int tap = 0; tap < 9; tap++)
+                for (int g = 0; g < G; g++)
+                    tc::tma_load_3d(wbase + (uint32_t)(tap * G + g) * nblk, &tm_w, g * 8, tap, 0, tc::smem_addr(&wbar));
+        }
+        int L = 0;
+        bool ok = true;
+        for (int strip = blockIdx.x; strip < nstrips && ok; strip += gridDim.x) {
+            const int xb = strip % tiles_x, rest = strip / tiles_x;
+            const int ys = (rest % strips_y) * R, n = rest / strips_y;
+            const int ye = min(ys + R, H);
+            const int x0 = xb * 128;
+            for (int yy = ys - 1; yy <= ye; yy++, L++) {
+                const int b = L % nb;
+                if (L >= nb &&
+                    !tc::mbar_wait_or_abort(tc::smem_addr(&row_empty[b]), (uint32_t)(((L / nb) - 1) & 1), a.err, 6,
+                                            &s_abort)) {
+                    ok = false;
+                    break;
+                }
+                const uint32_t dst = rbase + (uint32_t)b * rowb;
+                const bool yin = yy >= 0 && yy < H;
+                const bf16* row = in + (((size_t)n * H + (yin ? yy : 0)) * W) * K;
+                // 16-byte chunk q = pixel p (x0 - 1 + p) x group g, consecutive in memory
+                for (int q = tid; q < 130 * G; q += 128) {
+                    const int pp = q / G, g = q - pp * G;
+                    const int x = x0 - 1 + pp;
+                    const bool inside = yin && x >= 0 && x < W;
+                    cp_async16(dst + (uint32_t)g * 2080u + (uint32_t)pp * 16u,
+                               inside ? (const void*)(row + (size_t)x * K + g * 8) : (const void*)in, inside ? 16u : 0u);
+                }
+                cp_async_arrive(tc::smem_addr(&row_full[b]));
+            }
+        }
+        cp_async_wait_all();
+    } else if (warp == 4) {
+        // ---------------------------------------------------------- MMA issue
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16(128, Np);
+            const uint64_t adesc0 = tc::smem_desc(rbase, 2080u, 128u), bdesc0 = tc::smem_desc(wbase, nblk, 128u);
+            const uint32_t bstep = (2u * nblk) >> 4;           // 16 channels of weights
+            const int ksteps = K / 16;
+            bool ok = tc::mbar_wait_or_abort(tc::smem_addr(&wbar), 0u, a.err, 7, &s_abort);
+            int L = 0, tcount = 0;
+            for (int strip = blockIdx.x; strip < nstrips && ok; strip += gridDim.x) {
+                const int rest = strip / tiles_x;
+                const int ys = (rest % strips_y) * R;
+                const int ye = min(ys + R, H);
+                const int rows = ye - ys;
+                for (int k = 0; k < rows && ok; k++, tcount++) {
+                    // input rows y-1, y, y+1 are loads L+k, L+k+1, L+k+2
+                    for (int d = 0; d < 3 && ok; d++) {
+                        const int Ld = L + k + d;
+                        ok = tc::mbar_wait_or_abort(tc::smem_addr(&row_full[Ld % nb]), (uint32_t)((Ld / nb) & 1), a.err,
+                                                    8, &s_abort);
+                    }
+                    const int buf = tcount & 1;
+                    if (ok && tcount >= 2)
+                        ok = tc::mbar_wait_or_abort(tc::smem_addr(&acc_empty[buf]), (uint32_t)(((tcount >> 1) - 1) & 1),
+                                                    a.err, 9, &s_abort);
+                    if (!ok) break;
+                    tc::fence_proxy_async();
+                    tc::fence_after_sync();
+                    const uint32_t d = taddr + (uint32_t)(buf * Np);
+                    // descriptors differ only in their start-address field (bits 0-13,
+                    // address >> 4): step them by integer offsets, no rebuilding per MMA
+                    uint32_t acc = 0u;
+                    for (int dy = 0; dy < 3; dy++) {
+                        const uint64_t arow = adesc0 + (((uint32_t)((L + k + dy) % nb) * rowb) >> 4);
+                        for (int dx = 0; dx < 3; dx++) {
+                            const uint64_t ad = arow + (uint32_t)dx;             // one pixel = 16 bytes
+                            const uint64_t bd = bdesc0 + (((uint32_t)((dy * 3 + dx) * G) * nblk) >> 4);
+                            for (int kk = 0; kk < ksteps; kk++) {
+                                tc::mma_bf16(d, ad + (uint64_t)(260u * kk), bd + (uint64_t)(bstep * kk), idesc, acc);
+                                acc = 1u;
+                            }
+                        }
+                    }
+                    tc::mma_commit(tc::smem_addr(&acc_full[buf]));
+                    tc::mma_commit(tc::smem_addr(&row_empty[(L + k) % nb]));   // input row y-1 is done
+                }
+                if (!ok) break;
+                // the strip's last two input rows
+                tc::mma_commit(tc::smem_addr(&row_empty[(L + rows) % nb]));
+                tc::mma_commit(tc::smem_addr(&row_empty[(L + rows + 1) % nb]));
+                L += rows + 2;
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------------------------------------------------- epilogue
+        const int q = warp & 3;
+        const int m = q * 32 + lane;
+        int tcount = 0;
+        bool ok = true;
+        for (int strip = blockIdx.x; strip < nstrips && ok; strip += gridDim.x) {
+            const int xb = strip % tiles_x, rest = strip / tiles_x;
+            const int ys = (rest % strips_y) * R, n = rest / strips_y;
+            const int ye = min(ys + R, H);
+            const int x = xb * 128 + m;
+            const bool valid = x < W;
+            for (int y = ys; y < ye; y++, tcount++) {
+                const int buf = tcount & 1;
+                if (!tc::mbar_wait_or_abort(tc::smem_addr(&acc_full[buf]), (uint32_t)((tcount >> 1) & 1), a.err, 10,
+                                            &s_abort)) {
+                    ok = false;
+                    break;
+                }
+                tc::fence_after_sync();
+                const size_t p = ((size_t)n * H + y) * W + x;
+                for (int c0 = 0; c0 < Np; c0 += 16) {
+                    float v[16];
+                    tc::tmem_ld16(taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * Np + c0), v);
+                    if (!valid) continue;
+                    if (a.bias) {
+                        const float4* bb = reinterpret_cast<const float4*>(a.bias + c0);
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            const float4 b4 = __ldg(bb + k);
+                            v[4 * k] += b4.x;
+                            v[4 * k + 1] += b4.y;
+                            v[4 * k + 2] += b4.z;
+                            v[4 * k + 3] += b4.w;
+                        }
+                    }
+                    if (a.relu) {
+#pragma unroll
+                        for (int k = 0; k < 16; k++) v[k] = fmaxf(v[k], 0.0f);
+                    }
+                    if (a.mask) {
+                        float mk[16];
+                        unpack8(ldg16(a.mask + p * Np + c0), mk);
+                        unpack8(ldg16(a.mask + p * Np + c0 + 8), mk + 8);
+#pragma unroll
+                        for (int k = 0; k < 16; k++) v[k] = mk[k] > 0.0f ? v[k] : 0.0f;
+                    }
+                    if (a.out) {
+                        uint4* o = reinterpret_cast<uint4*>(a.out + p * Np + c0);
+                        o[0] = pack8(v);
+                        o[1] = pack8(v + 8);
+                    }
+                    if (a.out_f32) {
+                        float4* o = reinterpret_cast<float4*>(a.out_f32 + p * Np + c0);
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            o[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+                    }
+                }
+                tc::fence_before_sync();
+                tc::mbar_arrive(tc::smem_addr(&acc_empty[buf]));
+            }
+        }
+    }
+    if (s_abort && warp == 4 && lane == 0) {
+        for (int k = 0; k < kRowBufs; k++) {
+            tc::mbar_wait(tc::smem_addr(&row_full[k]), 0u, nullptr, 0);
+            tc::mbar_wait(tc::smem_addr(&row_empty[k]), 0u, nullptr, 0);
         }
     }
     tc::fence_before_sync();
@@ -612,6 +845,42 @@ cudaError_t conv3x3(const ConvArgs& a, cudaStream_t s) {
         if (e != cudaSuccess) return e;
         src = a.scratch;
     }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int tiles_x = (a.in.W + 127) / 128;
+    // row-resident kernel when the weights and at least four input rows fit
+    {
+        const size_t wbytes = 9u * (size_t)a.Cin * a.Np * 2u, rowb = (size_t)(a.Cin / 8) * 2080u;
+        const size_t budget = 200u * 1024u;
+        if (wbytes <= 80u * 1024u && wbytes + 4u * rowb <= budget) {
+            const int nb = (int)std::min<size_t>(kRowBufs, (budget - wbytes) / rowb);
+            const size_t sm = wbytes + (size_t)nb * rowb;
+            const int per_sm = std::max(1, std::min(std::min(512 / (int)tmem_columns(2 * a.Np),
+                                                             (int)((220u * 1024u) / (sm + 2048u))), 2));
+            const int ctas = sms * per_sm;
+            const long long cols = (long long)tiles_x * a.in.N;
+            // strips of R rows: about four per CTA, at least 4 rows each
+            int R = (int)std::max<long long>(4, ((long long)a.in.H * cols + 4LL * ctas - 1) / (4LL * ctas));
+            R = std::min(R, a.in.H);
+            const long long nstrips = cols * ((a.in.H + R - 1) / R);
+            if (nstrips > (1LL << 30)) return cudaErrorInvalidValue;
+            CUtensorMap tm_w8;
+            const cuuint64_t dw8[3] = {(cuuint64_t)a.Cin, 9u, (cuuint64_t)a.Np};
+            const cuuint64_t sw8[2] = {(cuuint64_t)a.Cin * 2u, (cuuint64_t)a.Cin * 2u * 9u};
+            const cuuint32_t bw8[3] = {8u, 1u, (cuuint32_t)a.Np};
+            if (!make_map(&tm_w8, a.w, 3, dw8, sw8, bw8, CU_TENSOR_MAP_SWIZZLE_NONE)) return cudaErrorInvalidValue;
+            ConvArgs b = a;
+            b.in = ConvSrc{src, a.Cin, 0, nullptr, 0, a.in.N, a.in.H, a.in.W};
+            if ((e = cudaFuncSetAttribute(k_conv3x3_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) !=
+                cudaSuccess)
+                return e;
+            const int grid = (int)std::min<long long>(nstrips, ctas);
+            k_conv3x3_rows<<<grid, kRowThreads, sm, s>>>(tm_w8, b, R, (int)nstrips, tiles_x, nb);
+            return cudaGetLastError();
+        }
+    }
     const ConvPlan plan = conv_plan(a.Cin, a.Np);
     if (plan.smem > 200u * 1024u) return cudaErrorInvalidValue;
     CUtensorMap tm_in, tm_w;
@@ -629,12 +898,9 @@ cudaError_t conv3x3(const ConvArgs& a, cudaStream_t s) {
         return cudaErrorInvalidValue;
     ConvArgs b = a;
     b.in = ConvSrc{src, a.Cin, 0, nullptr, 0, a.in.N, a.in.H, a.in.W};
-    cudaError_t e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem);
-    if (e != cudaSuccess) return e;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    const int tiles_x = (a.in.W + 127) / 128;
+    if ((e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem)) !=
+        cudaSuccess)
+        return e;
     const long long ntiles = (long long)tiles_x * a.in.H * a.in.N;
     if (ntiles > (1LL << 30)) return cudaErrorInvalidValue;
     const int grid = (int)std::min<long long>(ntiles, (long long)sms * conv_ctas_per_sm(a.Np, plan.smem));
