@@ -599,19 +599,31 @@ def large_section(vpt, torch, args, local):
                     crops[k] = ctx.read_plane("COLOR")[y0:y0 + ch, x0:x0 + cw].astype(np.float64)
     if net is not None:
         net.close()
-    errs = {}
+    errs, errs_svgf = {}, {}
     if not args.no_quality:
+        # the SVGF path on the same orbit: the fallback, and the yardstick of the error
+        svgf_crops = {}
+        with vpt.Context(width=W, height=H, device=local, storage=1, bounces=2) as ctx:
+            ctx.upload_world(vox)
+            ctx.set_block_table(blocks)
+            ctx.build_df()
+            for k in range(64):
+                ctx.render_frame(orbit_camera(vpt, k, theta0, W, H), frame_at(vpt, k), readback=False)
+                if k in sampled:
+                    svgf_crops[k] = ctx.read_plane("COLOR")[y0:y0 + ch, x0:x0 + cw].astype(np.float64)
         with quality.make_gt_context(W, H, vox, blocks, device=local, bounces=2) as g:
             for k in sampled:
                 gt, _ = quality.ground_truth_color(g, orbit_camera(vpt, k, theta0, W, H), frame_at(vpt, k), crop,
                                                    spp=1024)
                 errs[str(k)] = quality.rmse(crops[k], gt)
+                errs_svgf[str(k)] = quality.rmse(svgf_crops[k], gt)
     return {"world": list(LARGE_WORLD), "resolution": list(LARGE_RES), "spp": 1, "bounces": 2, "storage": "fp16",
             "frames": 64, "orbit": {"radius": 200.0, "height": 150.0, "deg_per_frame": 1.0, "theta0_deg": theta0},
             "denoiser": "learned" if all(used_all) else ("svgf fallback" if not any(used_all) else "mixed"),
             "frame_ms_p50": float(np.percentile(ms, 50)), "frame_ms_p99": float(np.percentile(ms, 99)),
             "frame_ms_max": float(max(ms)), "world_generate_s": gen_s,
-            "error_vs_fp64_gt": {"crop": list(crop), "gt_spp": 1024, "rmse_by_frame": errs}}
+            "error_vs_fp64_gt": {"crop": list(crop), "gt_spp": 1024, "rmse_by_frame": errs,
+                                 "svgf_rmse_by_frame": errs_svgf}}
 
 
 # ------------------------------------------------------- CPU (oracle) arm --

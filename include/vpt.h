@@ -187,6 +187,13 @@ vpt_status vpt_upload_world(vpt_ctx* ctx, const uint8_t* voxels, int32_t X, int3
 vpt_status vpt_set_block_table(vpt_ctx* ctx, const vpt_block* table, int32_t n);
 /* World::GenerateDistanceField (Core/World.cpp:69-113). */
 vpt_status vpt_build_df(vpt_ctx* ctx);
+/* Block edit (World::SetBlock followed by the distance-field rebuild it
+ * triggers, Core/World.cpp:372-374, :458-460): writes the x-fastest voxels of
+ * the box [x0,x0+w) x [y0,y0+h) x [z0,z0+d) (w*h*d bytes) into the world and,
+ * when the field is built, recomputes it only within L1 distance 254 of the
+ * box; the result is bit-identical to vpt_build_df of the edited world. */
+vpt_status vpt_edit_world(vpt_ctx* ctx, const uint8_t* voxels, int32_t x0, int32_t y0, int32_t z0, int32_t w,
+                          int32_t h, int32_t d);
 vpt_status vpt_read_df(vpt_ctx* ctx, uint8_t* host_df, size_t bytes);
 /* Context-free form: device pointers in and out, ordered on `stream`
  * (a cudaStream_t, 0 = legacy default stream). The device must be current. */
@@ -458,6 +465,20 @@ vpt_status vpt_render_frame_learned(vpt_ctx* ctx, vpt_unet* net, const vpt_camer
 vpt_status vpt_generate_world(uint8_t* out, int32_t X, int32_t Y, int32_t Z, uint64_t seed, int32_t n_blocks);
 /* Seeded flat block table: albedo, roughness, metalness uniform, 5% emissive. */
 vpt_status vpt_generate_block_table(vpt_block* out, int32_t n, uint64_t seed);
+/* World files (Core/WorldFileHandler.cpp:10-83). The reference's .sav is the
+ * raw x-fastest volume, X*Y*Z bytes, no header (dimensions fixed at compile
+ * time): header = 0 writes exactly that; header = 1 prefixes a 32-byte header
+ * ("VPTWORLD", version 1, X, Y, Z, seed; little endian). vpt_load_world reads
+ * either: with a header `dims` (and `seed`) are filled from it, a raw file
+ * needs `dims` from the caller. Truncated, oversized or malformed files give
+ * VPT_ERR_INVALID_ARG. out = NULL only checks the file and reports dims. */
+vpt_status vpt_save_world(const char* path, const uint8_t* voxels, int32_t X, int32_t Y, int32_t Z, uint64_t seed,
+                          int32_t header);
+vpt_status vpt_load_world(const char* path, uint8_t* out, size_t out_bytes, int32_t dims[3], uint64_t* seed);
+/* Emissive voxels of a world, as LoadWorld's light list (:50-66): x, y, z per
+ * voxel in x-fastest order, at most max_out written, *count = all of them. */
+vpt_status vpt_emissive_voxels(const uint8_t* voxels, int32_t X, int32_t Y, int32_t Z, const vpt_block* table,
+                               int32_t n_blocks, int32_t* xyz_out, int64_t max_out, int64_t* count);
 /* glm::lookAt / glm::perspective camera as Core/FpsCamera.cpp:14-24 builds it
  * (front from yaw/pitch in degrees), inverses in double precision. */
 vpt_status vpt_camera_from_pose(vpt_camera* out, const float position[3], float yaw_deg, float pitch_deg,

@@ -195,6 +195,10 @@ def _load() -> C.CDLL:
         "vpt_batch_launch_count": ([P, C.POINTER(u64)], C.c_int),
         "vpt_batch_get_stream": ([P, C.POINTER(P)], C.c_int),
         "vpt_shade_from": ([P, C.POINTER(Frame), i32], C.c_int),
+        "vpt_edit_world": ([P, P, i32, i32, i32, i32, i32, i32], C.c_int),
+        "vpt_save_world": ([C.c_char_p, P, i32, i32, i32, u64, i32], C.c_int),
+        "vpt_load_world": ([C.c_char_p, P, sz, C.POINTER(i32), C.POINTER(u64)], C.c_int),
+        "vpt_emissive_voxels": ([P, i32, i32, i32, P, i32, P, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
         "vpt_learned_input": ([P, C.POINTER(Camera), C.POINTER(Frame)], C.c_int),
         "vpt_learned_features": ([P, i32, i32, i32, i32, P], C.c_int),
         "vpt_render_frame_learned": ([P, P, C.POINTER(Camera), C.POINTER(Frame), P, C.POINTER(i32)], C.c_int),
@@ -290,6 +294,37 @@ def camera_from_pose(position, yaw_deg: float, pitch_deg: float, fov_deg: float 
     return cam
 
 
+def save_world(path, voxels: np.ndarray, seed: int = 0, header: bool = True):
+    """Writes a world file (vpt_save_world): header=False is the reference's raw .sav layout."""
+    v = np.ascontiguousarray(voxels, dtype=np.uint8)
+    Z, Y, X = v.shape
+    _check(lib.vpt_save_world(str(path).encode(), _ptr(v), X, Y, Z, seed, 1 if header else 0), "vpt_save_world")
+
+
+def load_world(path, dims=None):
+    """Reads a world file; `dims` (X, Y, Z) is required for a raw .sav. Returns (voxels (Z, Y, X), seed)."""
+    d = (C.c_int32 * 3)(*(dims if dims is not None else (0, 0, 0)))
+    seed = C.c_uint64()
+    _check(lib.vpt_load_world(str(path).encode(), None, 0, d, C.byref(seed)), "vpt_load_world")
+    out = np.empty((d[2], d[1], d[0]), np.uint8)
+    _check(lib.vpt_load_world(str(path).encode(), _ptr(out), out.nbytes, d, C.byref(seed)), "vpt_load_world")
+    return out, int(seed.value)
+
+
+def emissive_voxels(voxels: np.ndarray, table: np.ndarray) -> np.ndarray:
+    """(n, 3) int32 x, y, z of the emissive voxels (the reference's light list)."""
+    v = np.ascontiguousarray(voxels, dtype=np.uint8)
+    t = np.ascontiguousarray(table, dtype=BLOCK_DTYPE)
+    Z, Y, X = v.shape
+    cnt = C.c_int64()
+    _check(lib.vpt_emissive_voxels(_ptr(v), X, Y, Z, _ptr(t), t.size, None, 0, C.byref(cnt)), "vpt_emissive_voxels")
+    out = np.zeros((cnt.value, 3), np.int32)
+    if cnt.value:
+        _check(lib.vpt_emissive_voxels(_ptr(v), X, Y, Z, _ptr(t), t.size, _ptr(out), cnt.value, C.byref(cnt)),
+               "vpt_emissive_voxels")
+    return out
+
+
 def seeded_pose(seed: int, yaw_range=(0.0, 360.0), pitch_range=(-40.0, -10.0)):
     """Yaw and pitch drawn uniformly from the seed (the bench's camera rule)."""
     rng = np.random.default_rng(seed)
@@ -366,6 +401,13 @@ class Context:
 
     def build_df(self):
         self._ck(lib.vpt_build_df(self._h), "vpt_build_df")
+
+    def edit_world(self, origin, voxels: np.ndarray):
+        """Writes the (d, h, w) block of voxels at origin (x0, y0, z0) and updates the distance field locally."""
+        v = np.ascontiguousarray(voxels, dtype=np.uint8)
+        d, h, w = v.shape
+        x0, y0, z0 = origin
+        self._ck(lib.vpt_edit_world(self._h, _ptr(v), x0, y0, z0, w, h, d), "vpt_edit_world")
 
     def read_df(self) -> np.ndarray:
         out = np.empty(self.world_shape, dtype=np.uint8)

@@ -489,6 +489,29 @@ vpt_status vpt_build_df(vpt_ctx* c) {
     return VPT_OK;
 }
 
+vpt_status vpt_edit_world(vpt_ctx* c, const uint8_t* voxels, int32_t x0, int32_t y0, int32_t z0, int32_t w,
+                          int32_t h, int32_t d) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (!c->vox) return fail(c, VPT_ERR_STATE, "no world uploaded");
+    if (!voxels || w < 1 || h < 1 || d < 1 || x0 < 0 || y0 < 0 || z0 < 0 || x0 + (int64_t)w > c->X ||
+        y0 + (int64_t)h > c->Y || z0 + (int64_t)d > c->Z)
+        return fail(c, VPT_ERR_INVALID_ARG, "edit box [%d,%d)x[%d,%d)x[%d,%d) outside the %dx%dx%d world", x0, x0 + w, y0,
+                    y0 + h, z0, z0 + d, c->X, c->Y, c->Z);
+    cudaSetDevice(c->dev);
+    for (int k = 0; k < d; k++) {
+        uint8_t* dst = c->vox + (size_t)x0 + (size_t)c->X * ((size_t)y0 + (size_t)c->Y * (size_t)(z0 + k));
+        CK(c, cudaMemcpy2DAsync(dst, (size_t)c->X, voxels + (size_t)k * w * h, (size_t)w, (size_t)w, (size_t)h,
+                                cudaMemcpyHostToDevice, c->stream));
+    }
+    if (c->df_valid) {
+        int launches = 0;
+        CK(c, df_update(c->vox, c->df, c->X, c->Y, c->Z, x0, y0, z0, x0 + w, y0 + h, z0 + d, c->stream, &launches));
+        c->launches += (uint64_t)launches;
+    }
+    CK(c, cudaStreamSynchronize(c->stream));   // the host voxels may be reused
+    return VPT_OK;
+}
+
 vpt_status vpt_read_df(vpt_ctx* c, uint8_t* host, size_t bytes) {
     if (!c || !host) return VPT_ERR_INVALID_ARG;
     if (!c->df_valid) return fail(c, VPT_ERR_STATE, "distance field not built");

@@ -4,6 +4,7 @@
 // (built with -ffp-contract=off).
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <utility>
 #include <vector>
@@ -195,6 +196,106 @@ vpt_status vpt_camera_from_pose(vpt_camera* out, const float position[3], float 
     out->position[1] = position[1];
     out->position[2] = position[2];
     out->pad = 0.0f;
+    return VPT_OK;
+}
+
+// ------------------------------------------------------------ world files --
+// The reference's .sav (Core/WorldFileHandler.cpp:10-83) is the raw x-fastest
+// volume of uint8 block ids, X*Y*Z bytes, no header (its dimensions are the
+// compile-time WORLD_SIZE_*). With `header` the same bytes follow a 32-byte
+// header: "VPTWORLD", uint32 version 1, uint32 X, Y, Z, uint64 seed (little
+// endian).
+static const char kMagic[8] = {'V', 'P', 'T', 'W', 'O', 'R', 'L', 'D'};
+
+static void put32(unsigned char* p, uint32_t v) {
+    for (int k = 0; k < 4; k++) p[k] = (unsigned char)(v >> (8 * k));
+}
+static uint32_t get32(const unsigned char* p) {
+    uint32_t v = 0;
+    for (int k = 0; k < 4; k++) v |= (uint32_t)p[k] << (8 * k);
+    return v;
+}
+
+vpt_status vpt_save_world(const char* path, const uint8_t* voxels, int32_t X, int32_t Y, int32_t Z, uint64_t seed,
+                          int32_t header) {
+    if (!path || !voxels || X <= 0 || Y <= 0 || Z <= 0 || X > 4096 || Y > 4096 || Z > 4096) return VPT_ERR_INVALID_ARG;
+    FILE* f = fopen(path, "wb");
+    if (!f) return VPT_ERR_INVALID_ARG;
+    bool ok = true;
+    if (header) {
+        unsigned char h[32] = {0};
+        memcpy(h, kMagic, 8);
+        put32(h + 8, 1u);
+        put32(h + 12, (uint32_t)X);
+        put32(h + 16, (uint32_t)Y);
+        put32(h + 20, (uint32_t)Z);
+        put32(h + 24, (uint32_t)(seed & 0xffffffffu));
+        put32(h + 28, (uint32_t)(seed >> 32));
+        ok = fwrite(h, 1, 32, f) == 32;
+    }
+    const size_t n = (size_t)X * Y * Z;
+    ok = ok && fwrite(voxels, 1, n, f) == n;
+    ok = (fclose(f) == 0) && ok;
+    return ok ? VPT_OK : VPT_ERR_INVALID_ARG;
+}
+
+vpt_status vpt_load_world(const char* path, uint8_t* out, size_t out_bytes, int32_t dims[3], uint64_t* seed) {
+    if (!path || !dims) return VPT_ERR_INVALID_ARG;
+    FILE* f = fopen(path, "rb");
+    if (!f) return VPT_ERR_INVALID_ARG;
+    vpt_status st = VPT_OK;
+    long size = -1;
+    if (fseek(f, 0, SEEK_END) == 0) size = ftell(f);
+    if (size < 0 || fseek(f, 0, SEEK_SET) != 0) st = VPT_ERR_INVALID_ARG;
+    unsigned char h[32] = {0};
+    size_t off = 0;
+    if (st == VPT_OK && size >= 32 && fread(h, 1, 32, f) == 32 && memcmp(h, kMagic, 8) == 0) {
+        const uint32_t X = get32(h + 12), Y = get32(h + 16), Z = get32(h + 20);
+        if (get32(h + 8) != 1u || X == 0 || Y == 0 || Z == 0 || X > 4096 || Y > 4096 || Z > 4096) {
+            st = VPT_ERR_INVALID_ARG;
+        } else {
+            dims[0] = (int32_t)X;
+            dims[1] = (int32_t)Y;
+            dims[2] = (int32_t)Z;
+            if (seed) *seed = (uint64_t)get32(h + 24) | ((uint64_t)get32(h + 28) << 32);
+            off = 32;
+        }
+    } else if (st == VPT_OK) {
+        // raw: the caller names the dimensions
+        if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) st = VPT_ERR_INVALID_ARG;
+        if (seed) *seed = 0;
+    }
+    const size_t n = st == VPT_OK ? (size_t)dims[0] * dims[1] * dims[2] : 0;
+    if (st == VPT_OK && (size_t)size != off + n) st = VPT_ERR_INVALID_ARG;   // truncated or oversized
+    if (st == VPT_OK && out) {
+        if (out_bytes < n || fseek(f, (long)off, SEEK_SET) != 0 || fread(out, 1, n, f) != n) st = VPT_ERR_INVALID_ARG;
+    }
+    fclose(f);
+    return st;
+}
+
+// Positions of voxels whose block is emissive (the light list LoadWorld
+// collects, Core/WorldFileHandler.cpp:50-66), in x-fastest order.
+vpt_status vpt_emissive_voxels(const uint8_t* voxels, int32_t X, int32_t Y, int32_t Z, const vpt_block* table,
+                               int32_t n_blocks, int32_t* xyz_out, int64_t max_out, int64_t* count) {
+    if (!voxels || !table || !count || X <= 0 || Y <= 0 || Z <= 0 || n_blocks < 1 || n_blocks > 256 ||
+        (max_out > 0 && !xyz_out))
+        return VPT_ERR_INVALID_ARG;
+    int64_t c = 0;
+    for (int32_t z = 0; z < Z; z++)
+        for (int32_t y = 0; y < Y; y++)
+            for (int32_t x = 0; x < X; x++) {
+                const uint8_t b = voxels[(size_t)x + (size_t)X * ((size_t)y + (size_t)Y * z)];
+                if (b && b < n_blocks && table[b].emissive) {
+                    if (c < max_out) {
+                        xyz_out[3 * c] = x;
+                        xyz_out[3 * c + 1] = y;
+                        xyz_out[3 * c + 2] = z;
+                    }
+                    c++;
+                }
+            }
+    *count = c;
     return VPT_OK;
 }
 

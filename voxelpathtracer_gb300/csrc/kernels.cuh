@@ -18,6 +18,10 @@ enum RayKind { kRayPrimary = 0, kRayShadow = 1, kRayDiffuse = 2, kRayBounceShado
 // Manhattan distance field, min(min(254, X+Y+Z), L1 distance to the nearest
 // solid voxel): three sweeps along x, y and z. `launches` counts kernels.
 cudaError_t df_build(const uint8_t* vox, uint8_t* df, int X, int Y, int Z, cudaStream_t s, int* launches);
+// After the voxels of [ex0, ex1) x [ey0, ey1) x [ez0, ez1) changed: recompute
+// the field where the edit can change it, bit-identical to df_build.
+cudaError_t df_update(const uint8_t* vox, uint8_t* df, int X, int Y, int Z, int ex0, int ey0, int ez0, int ex1,
+                      int ey1, int ez1, cudaStream_t s, int* launches);
 
 // Per-frame constants of DiffuseRayTraceFrag main (:832-839), evaluated on
 // the host with the shader's operation order.
