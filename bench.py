@@ -541,15 +541,9 @@ LARGE_RES = (3840, 2160)
 
 
 def orbit_camera(vpt, k, theta0, W, H, step_deg=1.0):
-    """Frame k of an orbit of radius 200 at height 150 around the world's
-    centre column, looking at the terrain there."""
-    X, Y, Z = LARGE_WORLD
-    th = np.radians(theta0 + step_deg * k)
-    pos = (X / 2 + 200.0 * np.cos(th), 150.0, Z / 2 + 200.0 * np.sin(th))
-    # yaw faces the centre; the terrain sits near y = 40
-    yaw = float(np.degrees(np.arctan2(Z / 2 - pos[2], X / 2 - pos[0])))
-    pitch = float(-np.degrees(np.arctan2(150.0 - 40.0, 200.0)))
-    return vpt.camera_from_pose(pos, yaw, pitch, 90.0, W / H)
+    """Frame k of the orbit (radius 200, height 150) around the world's centre column."""
+    from voxelpathtracer_gb300 import learned
+    return learned.orbit_camera(LARGE_WORLD, theta0 + step_deg * k, W / H)
 
 
 def large_section(vpt, torch, args, local):
@@ -567,9 +561,10 @@ def large_section(vpt, torch, args, local):
     blocks = vpt.generate_block_table(100, seed=0)
     gen_s = time.perf_counter() - t0
     net = None
-    if learned.WEIGHTS.exists():
+    weights = learned.WEIGHTS_LARGE if learned.WEIGHTS_LARGE.exists() else learned.WEIGHTS
+    if weights.exists():
         net = vpt.UNet(1, H, W, device=local)
-        net.set_params(learned.load()[0])
+        net.set_params(learned.load(weights)[0])
     sampled = (15, 31, 47, 63)
     crop = (W // 2 - 320, H // 2 - 180, 640, 360)
     x0, y0, cw, ch = crop
@@ -620,6 +615,7 @@ def large_section(vpt, torch, args, local):
     return {"world": list(LARGE_WORLD), "resolution": list(LARGE_RES), "spp": 1, "bounces": 2, "storage": "fp16",
             "frames": 64, "orbit": {"radius": 200.0, "height": 150.0, "deg_per_frame": 1.0, "theta0_deg": theta0},
             "denoiser": "learned" if all(used_all) else ("svgf fallback" if not any(used_all) else "mixed"),
+            "weights": weights.name if net is not None else None,
             "frame_ms_p50": float(np.percentile(ms, 50)), "frame_ms_p99": float(np.percentile(ms, 99)),
             "frame_ms_max": float(max(ms)), "world_generate_s": gen_s,
             "error_vs_fp64_gt": {"crop": list(crop), "gt_spp": 1024, "rmse_by_frame": errs,

@@ -104,3 +104,15 @@ def test_learned_frame_with_a_network(vpt, world, gpu):
             assert used
             assert np.isfinite(rgb).all() and (rgb >= 0).all()
         assert c.pass_times()["learned"] > 0
+
+
+def test_pair_generation_fp16_two_bounces(vpt, gpu):
+    """Pairs for the large configuration: FP16 input planes, 2 bounces, the
+    ground truth from a second (FP32) context."""
+    from voxelpathtracer_gb300 import learned
+    X, T = learned.generate_pairs(6, crop=(32, 32), spp=64, n_worlds=1, dims=(64, 64, 64), frame_size=(128, 64),
+                                  history=(1, 6), seed=2, bounces=2, storage=1)
+    x, t = X.float().cpu().numpy(), T.cpu().numpy()
+    assert np.isfinite(x).all() and np.isfinite(t).all()
+    assert (x[..., :3] > 0).any() and (t > 0).any()
+    assert np.all(x[..., 14:] == 0)

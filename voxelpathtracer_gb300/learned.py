@@ -27,6 +27,8 @@ import numpy as np
 from . import (Context, UNet, camera_from_pose, default_frame, generate_block_table, generate_world, quality)
 
 WEIGHTS = pathlib.Path(__file__).resolve().parent / "weights" / "unet_denoiser.npz"
+# trained for the large combined configuration (512^3, 3840x2160, 2 bounces, FP16 planes, orbit camera)
+WEIGHTS_LARGE = pathlib.Path(__file__).resolve().parent / "weights" / "unet_denoiser_large.npz"
 
 
 def he_init(seed: int = 0) -> np.ndarray:
@@ -56,14 +58,40 @@ def drift_camera(pos, yaw, pitch, k, aspect):
     return camera_from_pose((pos[0] - 0.05 * k, pos[1], pos[2]), yaw - 0.25 * k, pitch, 90.0, aspect)
 
 
+def orbit_camera(dims, theta_deg, aspect, radius=200.0, height=150.0, ground=40.0):
+    """On a circle of `radius` at `height` around the world's centre column,
+    looking at the terrain (near y = `ground`) below the centre."""
+    X, Y, Z = dims
+    th = np.radians(theta_deg)
+    pos = (X / 2 + radius * np.cos(th), height, Z / 2 + radius * np.sin(th))
+    yaw = float(np.degrees(np.arctan2(Z / 2 - pos[2], X / 2 - pos[0])))
+    pitch = float(-np.degrees(np.arctan2(height - ground, radius)))
+    return camera_from_pose(pos, yaw, pitch, 90.0, aspect)
+
+
+def pan_sequence(rng, dims, W, H, history):
+    """A random pan: (length, camera of frame k), ending at a random pose."""
+    pos, yaw, pitch = random_pose(rng, dims)
+    length = int(rng.integers(*history))
+    return length, (lambda k: drift_camera(pos, yaw, pitch, length - 1 - k, W / H))
+
+
+def orbit_sequence(rng, dims, W, H, history, deg_per_frame=1.0):
+    """A stretch of the orbit at a random start angle: (length, camera of frame k)."""
+    theta0 = float(rng.uniform(0.0, 360.0))
+    length = int(rng.integers(*history))
+    return length, (lambda k: orbit_camera(dims, theta0 + deg_per_frame * k, W / H))
+
+
 def generate_pairs(n_pairs: int, crop=(256, 256), spp: int = 1024, n_worlds: int = 8, dims=(256, 256, 256),
                    frame_size=(1920, 1080), history=(1, 65), per_sequence: int = 4, seed: int = 0, device: int = 0,
-                   log=None):
+                   log=None, bounces: int = 1, storage: int = 0, camera: str = "pan"):
     """(X [n, h, w, 16] bfloat16, T [n, h, w, 3] float32) on the GPU.
 
-    Each camera sequence is a pan of a random length in `history` (frames of
-    temporal accumulation); at up to `per_sequence` random frames of it a
-    random crop is sampled: its features (vpt_learned_features) and
+    Each camera sequence (a pan, or a stretch of the orbit) has a random
+    length in `history` (frames of temporal accumulation); at up to
+    `per_sequence` random frames of it a random crop is sampled: its features
+    (vpt_learned_features) from a context with `storage` planes, and
     log(1 + colour) of the same frame shaded from the FP64 ground-truth GI."""
     import torch
     cw, ch = crop
@@ -73,6 +101,7 @@ def generate_pairs(n_pairs: int, crop=(256, 256), spp: int = 1024, n_worlds: int
     T = torch.zeros((n_pairs, ch, cw, 3), dtype=torch.float32, device=dev)
     rng = np.random.default_rng(seed)
     per_world = -(-n_pairs // n_worlds)
+    make_seq = orbit_sequence if camera == "orbit" else pan_sequence
     i = 0
     t0 = time.perf_counter()
     for wi in range(n_worlds):
@@ -82,28 +111,39 @@ def generate_pairs(n_pairs: int, crop=(256, 256), spp: int = 1024, n_worlds: int
         vox = generate_world(*dims, seed=wseed)
         blocks = generate_block_table(100, seed=wseed)
         stop = min(n_pairs, i + per_world)
-        with quality.make_gt_context(W, H, vox, blocks, device=device) as ctx:
+        ctx = Context(width=W, height=H, device=device, storage=storage, bounces=bounces)
+        ctx.upload_world(vox)
+        ctx.set_block_table(blocks)
+        ctx.build_df()
+        # the ground truth needs FP32 planes: a second context when the input is FP16
+        gt = ctx if storage == 0 else quality.make_gt_context(W, H, vox, blocks, device=device, bounces=bounces)
+        try:
             while i < stop:
-                pos, yaw, pitch = random_pose(rng, dims)
-                length = int(rng.integers(*history))
+                length, cam_at = make_seq(rng, dims, W, H, history)
                 picks = set(int(v) for v in rng.choice(length, size=min(per_sequence, length), replace=False))
                 fseed = int(rng.integers(0, 2**31))
                 ctx.reset_history()
                 for f in range(length):
-                    cam = drift_camera(pos, yaw, pitch, length - 1 - f, W / H)
+                    cam = cam_at(f)
                     fr = default_frame(seed=fseed, frame_index=f, time=1.0 + f / 60.0)
                     if f in picks and i < stop:
                         ctx.learned_input(cam, fr)
                         x0 = int(rng.integers(0, W - cw + 1))
                         y0 = int(rng.integers(0, H - ch + 1))
                         ctx.learned_features((x0, y0, cw, ch), X[i])
-                        rgb, _ = quality.ground_truth_color(ctx, cam, fr, (x0, y0, cw, ch), spp=spp)   # ends the frame
+                        if gt is not ctx:
+                            ctx.end_frame()
+                        rgb, _ = quality.ground_truth_color(gt, cam, fr, (x0, y0, cw, ch), spp=spp)   # ends gt's frame
                         T[i] = torch.from_numpy(np.log1p(np.maximum(rgb, 0.0)).astype(np.float32)).to(dev)
                         i += 1
                         if log and i % 100 == 0:
                             log(f"pairs {i}/{n_pairs} ({time.perf_counter() - t0:.1f} s)")
                     else:
                         ctx.render_frame(cam, fr, readback=False)
+        finally:
+            if gt is not ctx:
+                gt.close()
+            ctx.close()
     torch.cuda.synchronize()
     return X, T
 
@@ -214,7 +254,10 @@ def main():
     t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--holdout", type=int, default=100)
     t.add_argument("--seed", type=int, default=0)
-    t.add_argument("--out", default=str(WEIGHTS))
+    t.add_argument("--out", default=None)
+    t.add_argument("--profile", choices=["frame", "large"], default="frame",
+                   help="frame: 256^3 worlds, 1920x1080 pans, 1 bounce, FP32 planes; large: 512^3 worlds, "
+                        "3840x2160 orbits, 2 bounces, FP16 planes")
     e = sub.add_parser("evaluate")
     e.add_argument("--weights", default=str(WEIGHTS))
     e.add_argument("--world-seed", type=int, default=0)
@@ -233,8 +276,14 @@ def main():
     import torch
     log = lambda m: print(m, flush=True)  # noqa: E731
     t0 = time.perf_counter()
+    if a.profile == "large":
+        gen = dict(dims=(512, 512, 512), frame_size=(3840, 2160), bounces=2, storage=1, camera="orbit")
+        out = a.out or str(WEIGHTS_LARGE)
+    else:
+        gen = {}
+        out = a.out or str(WEIGHTS)
     X, T = generate_pairs(a.pairs + a.holdout, crop=(a.crop, a.crop), spp=a.spp, n_worlds=a.worlds, seed=a.seed,
-                          log=log)
+                          log=log, **gen)
     gen_s = time.perf_counter() - t0
     Xtr, Ttr, Xva, Tva = X[:a.pairs], T[:a.pairs], X[a.pairs:], T[a.pairs:]
     with UNet(a.batch, a.crop, a.crop) as net:
@@ -244,12 +293,12 @@ def main():
         train_s = time.perf_counter() - t1
         pred = predict_crops(net, Xva, batch=a.batch)
         noisy = Xva[..., :3].float()
-        res = {"pairs": a.pairs, "holdout": a.holdout, "crop": a.crop, "spp": a.spp, "worlds": a.worlds,
+        res = {"profile": a.profile, "pairs": a.pairs, "holdout": a.holdout, "crop": a.crop, "spp": a.spp, "worlds": a.worlds,
                "steps": a.steps, "batch": a.batch, "lr": a.lr, "generate_seconds": gen_s, "train_seconds": train_s,
                "final_loss": float(np.mean(losses[-100:])), "first_loss": float(np.mean(losses[:20])),
                "holdout_rmse_noisy": crop_rmse(noisy, Tva), "holdout_rmse_net": crop_rmse(pred, Tva),
                "loss_curve": [float(np.mean(losses[k:k + 50])) for k in range(0, len(losses), 50)]}
-        save(a.out, net.params(), res)
+        save(out, net.params(), res)
     log(json.dumps({k: v for k, v in res.items() if k != "loss_curve"}))
     del torch
 
