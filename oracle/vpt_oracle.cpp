@@ -1073,8 +1073,61 @@ void vpto_atrous(const vpto_camera* cam, const vpto_params* p, const vpto_frame*
     }
 }
 
+// SpatiallyUpscaleBuffers (ColorPassFrag.glsl:535-653), which the colour pass
+// always runs (:828): a 3x3 joint-bilateral gather of the GI planes with the
+// a-trous kernel, depth weight exp(-2|dd|)^5.25 and normal weight
+// max(n.n', 1e-6)^16; beyond 128 units the sun shadow is filtered over the
+// centre and its four immediate neighbours, otherwise read at the pixel
+// (BetterTexture at a texel centre); then +0.05 shadow bias (:641-643). The GI
+// planes have the G-buffer's resolution, so every tap is a texel centre, REPEAT
+// wrapped (the shader has no screen-space test here).
+struct UpscaledGI {
+    float sh[4], cocg[2], ao, shadow;
+};
+inline UpscaledGI upscale_gi(const Plane& T, const Plane8& F, const Plane8& S, const Plane& SH, const Plane& CC,
+                             const Plane& AO, int i, int j, v3 base_n, float base_d) {
+    static const float kw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
+    UpscaledGI u{};
+    float tsh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, tcc[2] = {0.0f, 0.0f};
+    float tao = 0.0f, tw = 0.0f, tshadow = 0.0f, tsw = 0.0f;
+    const bool filter_shadows = base_d > 128.0f;
+    if (!filter_shadows) tshadow = (float)S.at(i, j);
+    for (int x = -1; x <= 1; x++) {
+        for (int y = -1; y <= 1; y++) {
+            const int si = i + x, sj = j + y;
+            const float lda = 1.0f / (1.0f / T.at(si, sj, 0));
+            const float ed = dm_exp(-(std::fabs(lda - base_d) * 2.0f));
+            const float dw = dm_pow(ed, 5.25f);
+            const v3 na = normal_from_id(F.at(si, sj), 1.0f);
+            float nw = dm_pow(fmaxg(dot(na, base_n), 0.000001f), 16.0f);
+            nw = fmaxg(nw, 0.0001f);
+            const float kwt = kw[std::abs(x)] * kw[std::abs(y)];
+            float wgt = clampf((nw * dw) * kwt, 0.0f, 1.0f);
+            wgt = fmaxg(wgt, 0.00000001f);
+            for (int c = 0; c < 4; c++) tsh[c] += SH.at(si, sj, c) * wgt;
+            for (int c = 0; c < 2; c++) tcc[c] += CC.at(si, sj, c) * wgt;
+            tao += AO.at(si, sj, 0) * wgt;
+            tw += wgt;
+            if (filter_shadows && (x == 0 || y == 0)) {   // IsImmediateNeighbour (:524-530)
+                const float sw = (kwt * clampf(dm_pow(ed, 32.0f), 0.00001f, 1.0f)) * (nw * nw);
+                tshadow += (float)S.at(si, sj) * sw;
+                tsw += sw;
+            }
+        }
+    }
+    tw = fmaxg(tw, 0.0000001f);
+    for (int c = 0; c < 4; c++) u.sh[c] = tsh[c] / tw;
+    for (int c = 0; c < 2; c++) u.cocg[c] = tcc[c] / tw;
+    u.ao = tao / tw;
+    if (filter_shadows) tshadow = tshadow / tsw;
+    tshadow += 0.05f;
+    u.shadow = clampf(tshadow, 0.00000000000001f, 1.0f);
+    return u;
+}
+
 // ColorPassFrag.glsl main (:747-1083), u_UseDFG on (Core/Pipeline.cpp:3683),
-// VXAO on with cutoff (:3669, :3679), flat materials, no specular input.
+// VXAO with cutoff (:3669, :3679) only under SVGF (u_SVGFEnabled, :3680),
+// flat materials, no specular input.
 void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
                 const vpto_frame* f, const float* t, const uint8_t* face, const uint8_t* block,
                 const uint8_t* shadow, const float* sh, const float* cocg, const float* aosky,
@@ -1089,6 +1142,9 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
     const v3 moon_color = mk3(f->moon_radiance[0], f->moon_radiance[1], f->moon_radiance[2]);
     float sun_vis = clampf(dot(sun, mk3(0.0f, 1.0f, 0.0f)) + 0.05f, 0.0f, 0.1f) * 12.0f;
     sun_vis = 1.0f - sun_vis;
+    const bool vxao = p->denoiser == 0;
+    const Plane T{t, W, H, 1}, SH{sh, W, H, 4}, CC{cocg, W, H, 2}, AO{aosky, W, H, 2};
+    const Plane8 F{face, W, H}, S{shadow, W, H};
 #pragma omp parallel for schedule(dynamic, 4)
     for (int j = row0; j < row1; j++) {
         for (int i = 0; i < W; i++) {
@@ -1106,17 +1162,13 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
                 v3 albedo = basic_saturation(m.albedo, 1.0f - 0.1f);   // u_TextureDesatAmount = 0.1
                 if (m.metal >= 0.1f - 0.01f) albedo = basic_saturation(albedo, 0.9f);
                 float emissivity = (float)m.emissive;
-                float shy[4], cc[2];
-                for (int c = 0; c < 4; c++) shy[c] = sh[px * 4 + c];
-                cc[0] = cocg[px * 2 + 0];
-                cc[1] = cocg[px * 2 + 1];
-                float up_shadow = clampf((float)shadow[px], 0.0f, 1.0f);
-                float up_ao = aosky[px * 2 + 0];
+                const UpscaledGI up = upscale_gi(T, F, S, SH, CC, AO, i, j, n, dist);
+                float up_shadow = clampf(up.shadow, 0.0f, 1.0f);
                 float rt_shadow = clampf(clampf(up_shadow + 0.0f, 0.0f, 1.0f), 0.0f, 1.0f);
-                v3 indirect = sh_to_irradiance(shy, cc, n);
+                v3 indirect = sh_to_irradiance(up.sh, up.cocg, n);
                 const float vb = 0.00125f;
-                if (uv.x > vb && uv.x < 1.0f - vb && uv.y > vb && uv.y < 1.0f - vb) {
-                    float ao = up_ao;
+                if (vxao && uv.x > vb && uv.x < 1.0f - vb && uv.y > vb && uv.y < 1.0f - vb) {
+                    float ao = up.ao;
                     float dxz = std::sqrt((wp.x - viewer.x) * (wp.x - viewer.x) + (wp.z - viewer.z) * (wp.z - viewer.z));
                     float fade = dxz < 256.0f ? 0.0f : 1.0f;
                     ao = mixf(ao, 1.0f, fade);

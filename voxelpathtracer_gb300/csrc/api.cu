@@ -839,6 +839,7 @@ vpt_status shade_run(vpt_ctx* c, const vpt_frame* f, int source, void* out = nul
     float sv = clampf(dot(sun, mk3(0.0f, 1.0f, 0.0f)) + 0.05f, 0.0f, 0.1f) * 12.0f;
     a.sun_vis = 1.0f - sv;
     const bool plain = c->cfg.denoiser == VPT_DENOISER_ATROUS;
+    a.vxao = plain ? 0 : 1;
     const void* sh = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_SH]
                                                   : (plain ? c->hist[c->cur][HI_SH] : c->var[FI_SH]);
     const void* cocg = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_COCG]

@@ -237,6 +237,7 @@ struct ShadeArgs {
     float sun[3], moon[3];
     float sun_color[3], moon_color[3];
     float sun_vis;             // 1 - clamp(dot(sun, up) + 0.05, 0, 0.1) * 12
+    int vxao;                  // u_DoVXAO && u_SVGFEnabled: the GI AO darkens the indirect term
 };
 cudaError_t shade(const WorldView& w, const CamView& cam, int W, int H, int fp16, const ShadeArgs& a,
                   const void* t, const uint8_t* face, const uint8_t* block, const uint8_t* shadow,

@@ -1,4 +1,5 @@
-// Colour pass (ColorPassFrag.glsl main, :747-1083) for flat materials:
+// Colour pass (ColorPassFrag.glsl main, :747-1083) for flat materials: the
+// 3x3 joint-bilateral GI gather and shadow filter (SpatiallyUpscaleBuffers),
 // Cook-Torrance direct sun/moon light with the traced shadow, SH irradiance
 // decode of the denoised GI, VXAO and the DFG (Karis) indirect combine
 // (u_UseDFG on, Core/Pipeline.cpp:3683). One thread per pixel, a streaming
@@ -62,6 +63,81 @@ __device__ __forceinline__ v2 karis_env_brdf(float ndv, float rough) {
     return mk2(-1.04f * a004 + rz, 1.04f * a004 + rw);
 }
 
+struct UpscaledGI {
+    float sh[4], cocg[2], ao, shadow;
+};
+
+// SpatiallyUpscaleBuffers (ColorPassFrag.glsl:535-653), which the colour pass
+// always runs (:828): a 3x3 joint-bilateral gather of the GI planes with the
+// a-trous kernel, depth weight exp(-2|dd|)^5.25 and normal weight
+// max(n.n', 1e-6)^16; beyond 128 units the sun shadow is filtered over the
+// centre and its four immediate neighbours, otherwise read at the pixel; then
+// +0.05 shadow bias (:641-643). The GI planes have the G-buffer's resolution,
+// so every tap is a texel centre, REPEAT wrapped. All loads of a tap are
+// issued before its weights are formed; taps in x-outer, y-inner order keep
+// the sums' rounding identical to the shader's loop.
+template <typename S>
+__device__ __forceinline__ UpscaledGI upscale_gi(int W, int H, int i, int j, const S* t, const uint8_t* face,
+                                                 const uint8_t* shadow, const S* sh_p, const S* cocg_p,
+                                                 const S* ao_p, v3 base_n, float base_d) {
+    UpscaledGI u;
+    float4 tsh = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float tcc0 = 0.0f, tcc1 = 0.0f, tao = 0.0f, tw = 0.0f, tsw = 0.0f;
+    const bool filter_shadows = base_d > 128.0f;
+    float tshadow = filter_shadows ? 0.0f : (float)__ldg(shadow + (size_t)j * W + i);
+    const bool inner = i > 0 && j > 0 && i < W - 1 && j < H - 1;
+#pragma unroll
+    for (int x = -1; x <= 1; x++) {
+        const int si = inner ? i + x : wrapi(i + x, W);
+#pragma unroll
+        for (int y = -1; y <= 1; y++) {
+            const int sj = inner ? j + y : wrapi(j + y, H);
+            const size_t q = (size_t)sj * W + si;
+            const float tt = ld(t + q);
+            const int fid = __ldg(face + q);
+            const float4 s4 = ld4(sh_p + q * 4);
+            const float2 c2 = ld2(cocg_p + q * 2);
+            const float a0 = ld(ao_p + q * 2);
+            const bool cross = x == 0 || y == 0;
+            const float sv = (filter_shadows && cross) ? (float)__ldg(shadow + q) : 0.0f;
+            const float lda = 1.0f / (1.0f / tt);
+            const float ed = dexp(-(fabsf(lda - base_d) * 2.0f));
+            const float dw = dpow(ed, 5.25f);
+            const v3 na = normal_from_id(fid, 1.0f);
+            float nw = dpow(fmaxf(dot(na, base_n), 0.000001f), 16.0f);
+            nw = fmaxf(nw, 0.0001f);
+            const float kwt = (x == 0 ? 1.0f : 2.0f / 3.0f) * (y == 0 ? 1.0f : 2.0f / 3.0f);   // AtrousWeights
+            float wgt = clampf((nw * dw) * kwt, 0.0f, 1.0f);
+            wgt = fmaxf(wgt, 0.00000001f);
+            tsh.x += s4.x * wgt;
+            tsh.y += s4.y * wgt;
+            tsh.z += s4.z * wgt;
+            tsh.w += s4.w * wgt;
+            tcc0 += c2.x * wgt;
+            tcc1 += c2.y * wgt;
+            tao += a0 * wgt;
+            tw += wgt;
+            if (filter_shadows && cross) {   // IsImmediateNeighbour (:524-530)
+                const float swt = (kwt * clampf(dpow(ed, 32.0f), 0.00001f, 1.0f)) * (nw * nw);
+                tshadow += sv * swt;
+                tsw += swt;
+            }
+        }
+    }
+    tw = fmaxf(tw, 0.0000001f);
+    u.sh[0] = tsh.x / tw;
+    u.sh[1] = tsh.y / tw;
+    u.sh[2] = tsh.z / tw;
+    u.sh[3] = tsh.w / tw;
+    u.cocg[0] = tcc0 / tw;
+    u.cocg[1] = tcc1 / tw;
+    u.ao = tao / tw;
+    if (filter_shadows) tshadow = tshadow / tsw;
+    tshadow += 0.05f;
+    u.shadow = clampf(tshadow, 0.00000000000001f, 1.0f);
+    return u;
+}
+
 template <typename S>
 __global__ void __launch_bounds__(256) k_shade(WorldView w, CamView cam, int W, int H, ShadeArgs a, const S* t,
                                                const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
@@ -84,17 +160,13 @@ __global__ void __launch_bounds__(256) k_shade(WorldView w, CamView cam, int W, 
         v3 albedo = basic_saturation(m.albedo, 1.0f - 0.1f);
         if (m.metal >= 0.1f - 0.01f) albedo = basic_saturation(albedo, 0.9f);
         float emissivity = (float)m.emissive;
-        float shy[4], cc[2];
-        for (int c = 0; c < 4; c++) shy[c] = ld(sh_p + px * 4 + c);
-        cc[0] = ld(cocg_p + px * 2 + 0);
-        cc[1] = ld(cocg_p + px * 2 + 1);
-        float up_shadow = clampf((float)__ldg(shadow + px), 0.0f, 1.0f);
-        float up_ao = ld(ao_p + px * 2 + 0);
+        const UpscaledGI up = upscale_gi(W, H, i, j, t, face, shadow, sh_p, cocg_p, ao_p, n, dist);
+        float up_shadow = clampf(up.shadow, 0.0f, 1.0f);
         float rt_shadow = clampf(clampf(up_shadow + 0.0f, 0.0f, 1.0f), 0.0f, 1.0f);
-        v3 indirect = sh_to_irradiance(shy, cc, n);
+        v3 indirect = sh_to_irradiance(up.sh, up.cocg, n);
         const float vb = 0.00125f;
-        if (uv.x > vb && uv.x < 1.0f - vb && uv.y > vb && uv.y < 1.0f - vb) {
-            float ao = up_ao;
+        if (a.vxao && uv.x > vb && uv.x < 1.0f - vb && uv.y > vb && uv.y < 1.0f - vb) {
+            float ao = up.ao;
             float dxz = sqrtf((wp.x - viewer.x) * (wp.x - viewer.x) + (wp.z - viewer.z) * (wp.z - viewer.z));
             float fade = dxz < 256.0f ? 0.0f : 1.0f;
             ao = mixf(ao, 1.0f, fade);
