@@ -48,7 +48,7 @@ typedef struct vpt_ctx vpt_ctx;
 /* Frame-loop settings; the reference keeps these as static globals at the
  * top of Core/Pipeline.cpp (:17-320). */
 typedef struct vpt_config {
-    int32_t width, height;           /* G-buffer and GI resolution */
+    int32_t width, height;           /* G-buffer resolution (GI: over gi_divisor) */
     int32_t primary_max_steps;       /* u_RenderDistance (Core/Pipeline.cpp:55, clamped to 350 at :4824) */
     int32_t shadow_max_steps;        /* 350 (ShadowRayTraceFrag.glsl:233) */
     int32_t diffuse_max_steps;       /* u_DiffuseTraceLength = 48 (Core/Pipeline.cpp:75) */
@@ -61,7 +61,10 @@ typedef struct vpt_config {
     float color_phi_bias;            /* ColorPhiBias = 3.325 (:85) */
     int32_t device;                  /* CUDA device ordinal */
     int32_t denoiser;                /* vpt_denoiser: USE_SVGF (Core/Pipeline.cpp:84) true or false */
-    int32_t reserved[2];
+    int32_t gi_divisor;              /* 1 (or 0), 2, 4 ...: DiffuseTraceResolution = DiffuseIndirectSuperSampleRes
+                                        = 1 / gi_divisor (Core/Pipeline.cpp:72, :79; 4 by default, 2 in the
+                                        higher presets :1256-1282); width and height must be multiples */
+    int32_t reserved[1];
 } vpt_config;
 
 typedef enum vpt_denoiser {
@@ -284,6 +287,10 @@ vpt_status vpt_ground_truth(vpt_ctx* ctx, const vpt_frame* frame, int32_t x0, in
 
 /* ---------------------------------------------------------------- planes -- */
 vpt_status vpt_plane_info(const vpt_ctx* ctx, int32_t plane, size_t* bytes, int32_t* channels, int32_t* dtype);
+/* Width and height of a plane: the G-buffer's for the G-buffer, shadow and
+ * colour planes, the GI grid's (width / gi_divisor x height / gi_divisor)
+ * for the GI, temporal, variance and a-trous planes. */
+vpt_status vpt_plane_dims(const vpt_ctx* ctx, int32_t plane, int32_t* width, int32_t* height);
 vpt_status vpt_read_plane(vpt_ctx* ctx, int32_t plane, void* host, size_t bytes);
 vpt_status vpt_write_plane(vpt_ctx* ctx, int32_t plane, const void* host, size_t bytes);
 /* Device address of a plane (for callers that keep data on the GPU). */

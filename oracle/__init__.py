@@ -41,7 +41,7 @@ class OParams(C.Structure):
                 ("bounce_shadow_max_steps", C.c_int32), ("bounces", C.c_int32), ("spp", C.c_int32),
                 ("storage", C.c_int32), ("atrous_iterations", C.c_int32), ("resolution_scale", C.c_float),
                 ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
-                ("reserved", C.c_int32 * 2)]
+                ("gi_divisor", C.c_int32), ("reserved", C.c_int32 * 1)]
 
 
 class OWorld(C.Structure):
@@ -80,7 +80,8 @@ def lib() -> C.CDLL:
         L.vpto_spatial_initial.argtypes = [P, P, P, P, P, P]
         L.vpto_temporal.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, P]
         L.vpto_variance.argtypes = [P, P, P, P, P, P]
-        L.vpto_atrous.argtypes = [P, P, P, C.c_int, P, P, P, P, P, P]
+        L.vpto_atrous.argtypes = [P, P, P, C.c_int, P, P, P, P, P, P, P, P]
+        L.vpto_gi_view.argtypes = [P, P, P, P, P, P, P]
         L.vpto_shade.argtypes = [P, P, P, P, P, P, P, P, P, P, P, C.c_int, C.c_int, P]
         for name in ("vpto_exp", "vpto_exp2", "vpto_log2", "vpto_sin", "vpto_cos", "vpto_half_round"):
             getattr(L, name).argtypes = [C.c_float]
@@ -160,6 +161,24 @@ def params(config) -> OParams:
     return _as(OParams, config)
 
 
+def gi_dims(config) -> tuple:
+    """(height, width) of the GI planes: the G-buffer's over gi_divisor."""
+    p = params(config)
+    d = max(int(p.gi_divisor), 1)
+    return p.height // d, p.width // d
+
+
+def gi_view(config, t, face, block) -> dict:
+    """The G-buffer read at the GI grid's texel centres (vpto_gi_view)."""
+    p = params(config)
+    Hg, Wg = gi_dims(p)
+    out = {"t": np.zeros((Hg, Wg), np.float32), "face": np.zeros((Hg, Wg), np.uint8),
+           "block": np.zeros((Hg, Wg), np.uint8)}
+    arrs = [np.ascontiguousarray(a, dtype=dt) for a, dt in ((t, np.float32), (face, np.uint8), (block, np.uint8))]
+    lib().vpto_gi_view(C.byref(p), *[_p(a) for a in arrs], _p(out["t"]), _p(out["face"]), _p(out["block"]))
+    return out
+
+
 def _planes(H, W, spec):
     return {k: np.zeros((H, W, c) if c > 1 else (H, W), dtype=dt) for k, (c, dt) in spec.items()}
 
@@ -201,8 +220,9 @@ def _f32(d, keys):
 
 
 def trace_diffuse(world: World, cam, config, frame, t, face, rows=None) -> dict:
+    """Diffuse GI on the GI grid; t and face are the G-buffer's GI-grid view."""
     p = params(config)
-    H, W = p.height, p.width
+    H, W = gi_dims(p)
     out = _planes(H, W, GI_SPEC)
     t = np.ascontiguousarray(t, dtype=np.float32)
     face = np.ascontiguousarray(face, dtype=np.uint8)
@@ -215,7 +235,7 @@ def trace_diffuse(world: World, cam, config, frame, t, face, rows=None) -> dict:
 
 def spatial_initial(cam, config, t, face, gi: dict) -> dict:
     p = params(config)
-    out = _planes(p.height, p.width, GI_SPEC)
+    out = _planes(*gi_dims(p), GI_SPEC)
     gi = _f32(gi, ["sh", "cocg", "luma", "aosky"])
     t = np.ascontiguousarray(t, dtype=np.float32)
     face = np.ascontiguousarray(face, dtype=np.uint8)
@@ -227,7 +247,7 @@ def spatial_initial(cam, config, t, face, gi: dict) -> dict:
 def temporal(cam, prev_cam, config, frame, t, face, block, prev_t, prev_face, prev_block, cur: dict,
              hist: dict) -> dict:
     p = params(config)
-    out = _planes(p.height, p.width, HIST_SPEC)
+    out = _planes(*gi_dims(p), HIST_SPEC)
     cur = _f32(cur, ["sh", "cocg", "luma", "aosky"])
     hist = _f32(hist, ["sh", "cocg", "util", "aosky"])
     arrs = [np.ascontiguousarray(a, dtype=dt) for a, dt in
@@ -242,7 +262,7 @@ def temporal(cam, prev_cam, config, frame, t, face, block, prev_t, prev_face, pr
 
 def variance(cam, config, t, face, temporal_out: dict) -> dict:
     p = params(config)
-    out = _planes(p.height, p.width, {k: v for k, v in FILT_SPEC.items() if k != "aosky"})
+    out = _planes(*gi_dims(p), {k: v for k, v in FILT_SPEC.items() if k != "aosky"})
     h = _f32(temporal_out, ["sh", "cocg", "util", "aosky"])
     t = np.ascontiguousarray(t, dtype=np.float32)
     face = np.ascontiguousarray(face, dtype=np.uint8)
@@ -251,17 +271,22 @@ def variance(cam, config, t, face, temporal_out: dict) -> dict:
     return out
 
 
-def atrous(cam, config, frame, step, t, face, temporal_util, filt_in: dict, aosky_in) -> dict:
+def atrous(cam, config, frame, step, t, face, temporal_util, filt_in: dict, aosky_in, t_view=None,
+           face_view=None) -> dict:
+    """t / face: the full-resolution G-buffer; t_view / face_view: its GI-grid
+    view (the same planes when the grids coincide)."""
     p = params(config)
-    out = _planes(p.height, p.width, FILT_SPEC)
+    out = _planes(*gi_dims(p), FILT_SPEC)
     fi = _f32(filt_in, ["sh", "cocg", "variance"])
     ao = np.ascontiguousarray(aosky_in, dtype=np.float32)
     tu = np.ascontiguousarray(temporal_util, dtype=np.float32)
     t = np.ascontiguousarray(t, dtype=np.float32)
     face = np.ascontiguousarray(face, dtype=np.uint8)
+    tv = t if t_view is None else np.ascontiguousarray(t_view, dtype=np.float32)
+    fv = face if face_view is None else np.ascontiguousarray(face_view, dtype=np.uint8)
     si, so = _struct4(fi, ["sh", "cocg", "variance", "aosky"]), _struct4(out, ["sh", "cocg", "variance", "aosky"])
     lib().vpto_atrous(C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)), int(step), _p(t),
-                      _p(face), _p(tu), C.byref(si), _p(ao), C.byref(so))
+                      _p(face), _p(tv), _p(fv), _p(tu), C.byref(si), _p(ao), C.byref(so))
     return out
 
 
@@ -295,20 +320,20 @@ def plain_denoise(cam, prev_cam, config, g: dict, prev_g: dict, gi: dict, hist: 
     """The non-SVGF path (Core/Pipeline.cpp:2618-2786): temporal, variance and
     5 a-trous iterations with steps 12, 8, 4, 2, 1."""
     p = params(config)
-    H, W = p.height, p.width
+    H, W = gi_dims(p)
     f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)  # noqa: E731
     cur = _f32(gi, ["sh", "cocg", "luma", "aosky"])
     prev = _f32(hist, ["sh", "cocg", "util", "aosky"])
     tmp = _planes(H, W, HIST_SPEC)
-    t, pt = f32(g["t"]), f32(prev_g["t"])
+    view = gi_view(p, g["t"], g["face"], g["block"])
+    t, pt = f32(view["t"]), f32(prev_g["t"])
     lib().vpto_plain_temporal(C.byref(_as(OCamera, cam)), C.byref(_as(OCamera, prev_cam)), C.byref(p), _p(t), _p(pt),
                               C.byref(_struct4(cur, ["sh", "cocg", "luma", "aosky"])),
                               C.byref(_struct4(prev, ["sh", "cocg", "util", "aosky"])),
                               C.byref(_struct4(tmp, ["sh", "cocg", "util", "aosky"])))
     var = np.zeros((H, W), np.float32)
     lib().vpto_plain_variance(C.byref(p), _p(tmp["sh"]), _p(var))
-    face = np.ascontiguousarray(g["face"], np.uint8)
-    block = np.ascontiguousarray(g["block"], np.uint8)
+    face, block = view["face"], view["block"]
     sh, cocg, ao = tmp["sh"], tmp["cocg"], tmp["aosky"]
     dens = []
     for it in range(p.atrous_iterations):
@@ -325,16 +350,17 @@ def svgf(cam, prev_cam, config, frame, g: dict, prev_g: dict, gi: dict, hist: di
     """Spatial3x3Initial, temporal, variance and the a-trous iterations, as
     Core/Pipeline.cpp:2284-2615 sequences them. Returns every intermediate."""
     p = params(config)
-    pre = spatial_initial(cam, p, g["t"], g["face"], gi)
-    tmp = temporal(cam, prev_cam, p, frame, g["t"], g["face"], g["block"], prev_g["t"], prev_g["face"],
+    v = gi_view(p, g["t"], g["face"], g["block"])
+    pre = spatial_initial(cam, p, v["t"], v["face"], gi)
+    tmp = temporal(cam, prev_cam, p, frame, v["t"], v["face"], v["block"], prev_g["t"], prev_g["face"],
                    prev_g["block"], pre, hist)
-    var = variance(cam, p, g["t"], g["face"], tmp)
+    var = variance(cam, p, v["t"], v["face"], tmp)
     cur = {"sh": var["sh"], "cocg": var["cocg"], "variance": var["variance"]}
     ao = tmp["aosky"]
     dens = []
     for it in range(p.atrous_iterations):
         step = max(16 >> it, 1)
-        den = atrous(cam, p, frame, step, g["t"], g["face"], tmp["util"], cur, ao)
+        den = atrous(cam, p, frame, step, g["t"], g["face"], tmp["util"], cur, ao, v["t"], v["face"])
         dens.append(den)
         cur, ao = den, den["aosky"]
     return {"pre": pre, "temporal": tmp, "variance": var, "atrous": dens}
@@ -345,7 +371,8 @@ def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist:
     p = params(config)
     g = trace_primary(world, cam, p)
     shadow = trace_shadow(world, cam, p, frame, g["t"], g["face"])
-    gi = trace_diffuse(world, cam, p, frame, g["t"], g["face"])
+    v = gi_view(p, g["t"], g["face"], g["block"])
+    gi = trace_diffuse(world, cam, p, frame, v["t"], v["face"])
     if p.denoiser == 1:
         sv = plain_denoise(cam, prev_cam, p, g, prev_g, gi, hist)
         last = sv["atrous"][-1] if sv["atrous"] else sv["temporal"]
@@ -361,10 +388,13 @@ def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist:
     return {"g": g, "shadow": shadow, "gi": gi, "svgf": sv, "rgb": rgb}
 
 
-def empty_history(H: int, W: int):
-    """The state libvpt starts from: previous G-buffer all misses, zero history."""
+def empty_history(H: int, W: int, gi_divisor: int = 1):
+    """The state libvpt starts from: previous G-buffer all misses, zero history
+    (on the GI grid)."""
     prev_g = {"t": np.full((H, W), -1.0, np.float32), "face": np.full((H, W), 10, np.uint8),
               "block": np.zeros((H, W), np.uint8)}
-    hist = {"sh": np.zeros((H, W, 4), np.float32), "cocg": np.zeros((H, W, 2), np.float32),
-            "util": np.zeros((H, W, 4), np.float32), "aosky": np.zeros((H, W, 2), np.float32)}
+    d = max(int(gi_divisor), 1)
+    Hg, Wg = H // d, W // d
+    hist = {"sh": np.zeros((Hg, Wg, 4), np.float32), "cocg": np.zeros((Hg, Wg, 2), np.float32),
+            "util": np.zeros((Hg, Wg, 4), np.float32), "aosky": np.zeros((Hg, Wg, 2), np.float32)}
     return prev_g, hist

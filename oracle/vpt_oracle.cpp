@@ -619,10 +619,42 @@ void vpto_trace_shadow(const vpto_world* w, const vpto_camera* cam, const vpto_p
 }
 
 // DiffuseRayTraceFrag.glsl main (:822-935)
+// The diffuse GI and its filters run on a grid gi_divisor times coarser than
+// the G-buffer: DiffuseTraceResolution = DiffuseIndirectSuperSampleRes = 1/d
+// (Core/Pipeline.cpp:72, :79, :1702-1710; 1/4 by default, 1/2 in the higher
+// presets :1256-1282). Every such pass sets its offsets in GI texels
+// (u_Dimensions / textureSize of a GI plane, e.g. :2303, :2568).
+inline int gi_div(const vpto_params* p) { return p->gi_divisor > 1 ? p->gi_divisor : 1; }
+
+void vpto_gi_view(const vpto_params* p, const float* t, const uint8_t* face, const uint8_t* block,
+                  float* t_view, uint8_t* face_view, uint8_t* block_view) {
+    const int d = gi_div(p), W = p->width, H = p->height, Wg = W / d, Hg = H / d;
+    const Plane T{t, W, H, 1};
+    const Plane8 F{face, W, H}, B{block, W, H};
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < Hg; j++) {
+        for (int i = 0; i < Wg; i++) {
+            const size_t q = (size_t)j * Wg + i;
+            if (d == 1) {
+                t_view[q] = t[q];
+                face_view[q] = face[q];
+                block_view[q] = block[q];
+                continue;
+            }
+            const v2 uv = texcoord(i, j, Wg, Hg);
+            float v;
+            T.linear(uv, &v);
+            t_view[q] = storage(v, p->storage);
+            face_view[q] = (uint8_t)F.nearest(uv);
+            block_view[q] = (uint8_t)B.nearest(uv);
+        }
+    }
+}
+
 void vpto_trace_diffuse(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
                         const vpto_frame* f, const float* t, const uint8_t* face,
                         int row0, int row1, vpto_gi* out) {
-    const int W = p->width, H = p->height;
+    const int W = p->width / gi_div(p), H = p->height / gi_div(p);
     const v3 r0 = ray_origin(cam);
     const Lighting L = frame_lighting(f);
     const int fp16 = p->storage;
@@ -687,7 +719,7 @@ void vpto_trace_diffuse(const vpto_world* w, const vpto_camera* cam, const vpto_
 // Spatial3x3Initial.glsl main (:96-176)
 void vpto_spatial_initial(const vpto_camera* cam, const vpto_params* p,
                           const float* t, const uint8_t* face, const vpto_gi* in, vpto_gi* out) {
-    const int W = p->width, H = p->height;
+    const int W = p->width / gi_div(p), H = p->height / gi_div(p);
     const int fp16 = p->storage;
     const Plane T{t, W, H, 1}, SH{in->sh, W, H, 4}, CC{in->cocg, W, H, 2}, AO{in->aosky, W, H, 2};
     const Plane8 F{face, W, H};
@@ -755,10 +787,10 @@ void vpto_temporal(const vpto_camera* cam, const vpto_camera* prev_cam, const vp
                    const float* t, const uint8_t* face, const uint8_t* block,
                    const float* prev_t, const uint8_t* prev_face, const uint8_t* prev_block,
                    const vpto_gi* cur, const vpto_history* prev, vpto_history* out) {
-    const int W = p->width, H = p->height;
+    const int W = p->width / gi_div(p), H = p->height / gi_div(p);
     const int fp16 = p->storage;
-    const Plane T{t, W, H, 1}, PT{prev_t, W, H, 1};
-    const Plane8 F{face, W, H}, B{block, W, H}, PF{prev_face, W, H}, PB{prev_block, W, H};
+    const Plane T{t, W, H, 1}, PT{prev_t, p->width, p->height, 1};
+    const Plane8 F{face, W, H}, B{block, W, H}, PF{prev_face, p->width, p->height}, PB{prev_block, p->width, p->height};
     const Plane PSH{prev->sh, W, H, 4}, PCC{prev->cocg, W, H, 2}, PU{prev->util, W, H, 4}, PAO{prev->aosky, W, H, 2};
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
     // u_PrevProjection * u_PrevView, a 4x4 product evaluated left to right.
@@ -878,7 +910,7 @@ void vpto_temporal(const vpto_camera* cam, const vpto_camera* prev_cam, const vp
 // AGGRESSIVE_DISOCCLUSION_HANDLING on (Core/Pipeline.cpp:2451-2452).
 void vpto_variance(const vpto_camera* cam, const vpto_params* p,
                    const float* t, const uint8_t* face, const vpto_history* in, vpto_filtered* out) {
-    const int W = p->width, H = p->height;
+    const int W = p->width / gi_div(p), H = p->height / gi_div(p);
     const int fp16 = p->storage;
     const Plane T{t, W, H, 1}, SH{in->sh, W, H, 4}, CC{in->cocg, W, H, 2}, U{in->util, W, H, 4};
     const Plane8 F{face, W, H};
@@ -955,13 +987,16 @@ void vpto_variance(const vpto_camera* cam, const vpto_params* p,
 
 // SVGF/SpatialFilter.glsl main (:175-355), u_LargeKernel off, DO_SPATIAL on.
 void vpto_atrous(const vpto_camera* cam, const vpto_params* p, const vpto_frame* f, int step,
-                 const float* t, const uint8_t* face, const float* temporal_util,
-                 const vpto_filtered* in, const float* in_aosky, vpto_filtered* out) {
-    const int W = p->width, H = p->height;
+                 const float* t, const uint8_t* face, const float* t_view, const uint8_t* face_view,
+                 const float* temporal_util, const vpto_filtered* in, const float* in_aosky, vpto_filtered* out) {
+    const int W = p->width / gi_div(p), H = p->height / gi_div(p);
     const int fp16 = p->storage;
-    const Plane T{t, W, H, 1}, SH{in->sh, W, H, 4}, CC{in->cocg, W, H, 2}, V{in->variance, W, H, 1};
+    // taps sample the full-resolution depth and face planes at arbitrary
+    // points; the centre reads them at its own GI texel centre (the views)
+    const Plane T{t, p->width, p->height, 1}, TV{t_view, W, H, 1};
+    const Plane SH{in->sh, W, H, 4}, CC{in->cocg, W, H, 2}, V{in->variance, W, H, 1};
     const Plane AO{in_aosky, W, H, 2}, U{temporal_util, W, H, 4};
-    const Plane8 F{face, W, H};
+    const Plane8 F{face, p->width, p->height}, FV{face_view, W, H};
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
     const float atrous_w[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
     const float gauss[2] = {0.60283f, 0.198585f};
@@ -980,8 +1015,8 @@ void vpto_atrous(const vpto_camera* cam, const vpto_params* p, const vpto_frame*
             float gx = ((float)i + 0.5f) + tmod500, gy = ((float)j + 0.5f) + tmod500;
             float noise = fract(52.9829189f * fract(0.06711056f * gx + 0.00583715f * gy));
             int jit = f2i((noise - 0.5f) * ((float)step * 0.8f));
-            float bd = T.at(i, j, 0);
-            v3 bn = normal_from_id(F.at(i, j), 1.0f);
+            float bd = TV.at(i, j, 0);
+            v3 bn = normal_from_id(FV.at(i, j), 1.0f);
             float bsh[4], bcc[2], bao[2];
             for (int c = 0; c < 4; c++) bsh[c] = SH.at(i, j, c);
             for (int c = 0; c < 2; c++) { bcc[c] = CC.at(i, j, c); bao[c] = AO.at(i, j, c); }
@@ -1078,14 +1113,17 @@ void vpto_atrous(const vpto_camera* cam, const vpto_params* p, const vpto_frame*
 // a-trous kernel, depth weight exp(-2|dd|)^5.25 and normal weight
 // max(n.n', 1e-6)^16; beyond 128 units the sun shadow is filtered over the
 // centre and its four immediate neighbours, otherwise read at the pixel
-// (BetterTexture at a texel centre); then +0.05 shadow bias (:641-643). The GI
-// planes have the G-buffer's resolution, so every tap is a texel centre, REPEAT
-// wrapped (the shader has no screen-space test here).
+// (BetterTexture at a texel centre); then +0.05 shadow bias (:641-643). Taps
+// are one GI texel apart (TexelSize of u_DiffuseSHy, :565), so on a GI grid d
+// times coarser they land on the G-buffer texel centres d texels apart (read
+// there, REPEAT wrapped: the shader has no screen-space test here) and between
+// GI texels (bilinear); with d = 1 every tap is a texel centre of both.
 struct UpscaledGI {
     float sh[4], cocg[2], ao, shadow;
 };
 inline UpscaledGI upscale_gi(const Plane& T, const Plane8& F, const Plane8& S, const Plane& SH, const Plane& CC,
-                             const Plane& AO, int i, int j, v3 base_n, float base_d) {
+                             const Plane& AO, int d, int i, int j, v2 uv, v3 base_n, float base_d) {
+    const float texel_x = 1.0f / (float)SH.W, texel_y = 1.0f / (float)SH.H;
     static const float kw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
     UpscaledGI u{};
     float tsh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, tcc[2] = {0.0f, 0.0f};
@@ -1094,7 +1132,17 @@ inline UpscaledGI upscale_gi(const Plane& T, const Plane8& F, const Plane8& S, c
     if (!filter_shadows) tshadow = (float)S.at(i, j);
     for (int x = -1; x <= 1; x++) {
         for (int y = -1; y <= 1; y++) {
-            const int si = i + x, sj = j + y;
+            const int si = i + d * x, sj = j + d * y;
+            float ssh[4], scc[2], sao[2];
+            if (d == 1) {
+                for (int c = 0; c < 4; c++) ssh[c] = SH.at(si, sj, c);
+                for (int c = 0; c < 2; c++) { scc[c] = CC.at(si, sj, c); sao[c] = AO.at(si, sj, c); }
+            } else {
+                const v2 sc = v2{uv.x + (float)x * texel_x, uv.y + (float)y * texel_y};
+                SH.linear(sc, ssh);
+                CC.linear(sc, scc);
+                AO.linear(sc, sao);
+            }
             const float lda = 1.0f / (1.0f / T.at(si, sj, 0));
             const float ed = dm_exp(-(std::fabs(lda - base_d) * 2.0f));
             const float dw = dm_pow(ed, 5.25f);
@@ -1104,9 +1152,9 @@ inline UpscaledGI upscale_gi(const Plane& T, const Plane8& F, const Plane8& S, c
             const float kwt = kw[std::abs(x)] * kw[std::abs(y)];
             float wgt = clampf((nw * dw) * kwt, 0.0f, 1.0f);
             wgt = fmaxg(wgt, 0.00000001f);
-            for (int c = 0; c < 4; c++) tsh[c] += SH.at(si, sj, c) * wgt;
-            for (int c = 0; c < 2; c++) tcc[c] += CC.at(si, sj, c) * wgt;
-            tao += AO.at(si, sj, 0) * wgt;
+            for (int c = 0; c < 4; c++) tsh[c] += ssh[c] * wgt;
+            for (int c = 0; c < 2; c++) tcc[c] += scc[c] * wgt;
+            tao += sao[0] * wgt;
             tw += wgt;
             if (filter_shadows && (x == 0 || y == 0)) {   // IsImmediateNeighbour (:524-530)
                 const float sw = (kwt * clampf(dm_pow(ed, 32.0f), 0.00001f, 1.0f)) * (nw * nw);
@@ -1143,7 +1191,8 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
     float sun_vis = clampf(dot(sun, mk3(0.0f, 1.0f, 0.0f)) + 0.05f, 0.0f, 0.1f) * 12.0f;
     sun_vis = 1.0f - sun_vis;
     const bool vxao = p->denoiser == 0;
-    const Plane T{t, W, H, 1}, SH{sh, W, H, 4}, CC{cocg, W, H, 2}, AO{aosky, W, H, 2};
+    const int d = gi_div(p), Wg = W / d, Hg = H / d;
+    const Plane T{t, W, H, 1}, SH{sh, Wg, Hg, 4}, CC{cocg, Wg, Hg, 2}, AO{aosky, Wg, Hg, 2};
     const Plane8 F{face, W, H}, S{shadow, W, H};
 #pragma omp parallel for schedule(dynamic, 4)
     for (int j = row0; j < row1; j++) {
@@ -1162,7 +1211,7 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
                 v3 albedo = basic_saturation(m.albedo, 1.0f - 0.1f);   // u_TextureDesatAmount = 0.1
                 if (m.metal >= 0.1f - 0.01f) albedo = basic_saturation(albedo, 0.9f);
                 float emissivity = (float)m.emissive;
-                const UpscaledGI up = upscale_gi(T, F, S, SH, CC, AO, i, j, n, dist);
+                const UpscaledGI up = upscale_gi(T, F, S, SH, CC, AO, d, i, j, uv, n, dist);
                 float up_shadow = clampf(up.shadow, 0.0f, 1.0f);
                 float rt_shadow = clampf(clampf(up_shadow + 0.0f, 0.0f, 1.0f), 0.0f, 1.0f);
                 v3 indirect = sh_to_irradiance(up.sh, up.cocg, n);
@@ -1226,9 +1275,9 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
 void vpto_plain_temporal(const vpto_camera* cam, const vpto_camera* prev_cam, const vpto_params* p,
                          const float* t, const float* prev_t, const vpto_gi* cur, const vpto_history* prev,
                          vpto_history* out) {
-    const int W = p->width, H = p->height;
+    const int W = p->width / gi_div(p), H = p->height / gi_div(p);
     const int fp16 = p->storage;
-    const Plane T{t, W, H, 1}, PT{prev_t, W, H, 1}, PSH{prev->sh, W, H, 4}, PCC{prev->cocg, W, H, 2};
+    const Plane T{t, W, H, 1}, PT{prev_t, p->width, p->height, 1}, PSH{prev->sh, W, H, 4}, PCC{prev->cocg, W, H, 2};
     float m[16];
     for (int c = 0; c < 4; c++)
         for (int r = 0; r < 4; r++)
@@ -1277,7 +1326,7 @@ void vpto_plain_temporal(const vpto_camera* cam, const vpto_camera* prev_cam, co
 // SampleVarianceCompute.glsl: 5x5 luminance variance of the temporal colour
 // (REPEAT wrap at the borders).
 void vpto_plain_variance(const vpto_params* p, const float* sh, float* variance) {
-    const int W = p->width, H = p->height;
+    const int W = p->width / gi_div(p), H = p->height / gi_div(p);
     const Plane SH{sh, W, H, 4};
 #pragma omp parallel for schedule(static)
     for (int j = 0; j < H; j++) {
@@ -1307,7 +1356,7 @@ void vpto_plain_variance(const vpto_params* p, const float* sh, float* variance)
 void vpto_plain_atrous(const vpto_camera* cam, const vpto_params* p, int step, const float* t, const uint8_t* face,
                        const uint8_t* block, const float* sh, const float* cocg, const float* aosky, float* out_sh,
                        float* out_cocg, float* out_aosky) {
-    const int W = p->width, H = p->height;
+    const int W = p->width / gi_div(p), H = p->height / gi_div(p);
     const int fp16 = p->storage;
     const Plane T{t, W, H, 1};
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;

@@ -65,7 +65,8 @@ typedef struct vpto_params {
     float color_phi_bias;
     int32_t device;
     int32_t denoiser;           /* 0 = SVGF, 1 = temporal + 5x5 a-trous */
-    int32_t reserved[2];
+    int32_t gi_divisor;         /* GI grid = G-buffer / gi_divisor (0 or 1: same grid) */
+    int32_t reserved[1];
 } vpto_params;
 
 typedef struct vpto_world {
@@ -123,7 +124,20 @@ void vpto_trace_shadow(const vpto_world* w, const vpto_camera* cam, const vpto_p
                        const vpto_frame* f, const float* t, const uint8_t* face,
                        int row0, int row1, uint8_t* shadow);
 
-/* DiffuseRayTraceFrag.glsl main with CalculateDiffuse. */
+/* The G-buffer as the GI passes read it at their own texel centres when the
+ * GI grid is gi_divisor times coarser: texture() of the depth (bilinear) and
+ * nearest face and block at each GI texel centre, the depth stored in the
+ * storage type. With gi_divisor 1 this is the G-buffer itself. */
+void vpto_gi_view(const vpto_params* p, const float* t, const uint8_t* face, const uint8_t* block,
+                  float* t_view, uint8_t* face_view, uint8_t* block_view);
+
+/* Passes below that take t / face / block "views" read them on the GI grid
+ * (vpto_gi_view); prev_t / prev_face / prev_block and the a-trous pass's
+ * t / face are the full-resolution G-buffer, sampled at arbitrary points.
+ * GI planes are (width / gi_divisor) x (height / gi_divisor). */
+
+/* DiffuseRayTraceFrag.glsl main with CalculateDiffuse, on the GI grid
+ * (rows of the GI grid). */
 void vpto_trace_diffuse(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
                         const vpto_frame* f, const float* t, const uint8_t* face,
                         int row0, int row1, vpto_gi* out);
@@ -145,10 +159,13 @@ void vpto_variance(const vpto_camera* cam, const vpto_params* p,
 
 /* SVGF/SpatialFilter.glsl, one a-trous iteration with step `step`. */
 void vpto_atrous(const vpto_camera* cam, const vpto_params* p, const vpto_frame* f, int step,
-                 const float* t, const uint8_t* face, const float* temporal_util,
+                 const float* t, const uint8_t* face, const float* t_view, const uint8_t* face_view,
+                 const float* temporal_util,
                  const vpto_filtered* in, const float* in_aosky, vpto_filtered* out);
 
-/* ColorPassFrag.glsl main: direct GGX + indirect-diffuse combine, flat materials. */
+/* ColorPassFrag.glsl main: joint-bilateral GI upscale, direct GGX +
+ * indirect-diffuse combine, flat materials. t / face / block / shadow at the
+ * G-buffer's resolution, sh / cocg / aosky on the GI grid. */
 void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
                 const vpto_frame* f, const float* t, const uint8_t* face, const uint8_t* block,
                 const uint8_t* shadow, const float* sh, const float* cocg, const float* aosky,

@@ -56,7 +56,7 @@ class Config(C.Structure):
                 ("bounce_shadow_max_steps", C.c_int32), ("bounces", C.c_int32), ("spp", C.c_int32),
                 ("storage", C.c_int32), ("atrous_iterations", C.c_int32), ("resolution_scale", C.c_float),
                 ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
-                ("reserved", C.c_int32 * 2)]
+                ("gi_divisor", C.c_int32), ("reserved", C.c_int32 * 1)]
 
 
 class Camera(C.Structure):
@@ -162,6 +162,7 @@ def _load() -> C.CDLL:
         "vpt_reset_history": ([P], C.c_int),
         "vpt_render_frame": ([P, C.POINTER(Camera), C.POINTER(Frame), P], C.c_int),
         "vpt_plane_info": ([P, i32, C.POINTER(sz), C.POINTER(i32), C.POINTER(i32)], C.c_int),
+        "vpt_plane_dims": ([P, i32, C.POINTER(i32), C.POINTER(i32)], C.c_int),
         "vpt_read_plane": ([P, i32, P, sz], C.c_int),
         "vpt_write_plane": ([P, i32, P, sz], C.c_int),
         "vpt_plane_device_ptr": ([P, i32, C.POINTER(P)], C.c_int),
@@ -507,15 +508,22 @@ class Context:
                  "vpt_render_frame_learned")
         return out, bool(used.value)
 
+    def plane_dims(self, plane) -> tuple:
+        """(height, width) of a plane: the GI grid's for the GI-side planes."""
+        pid = PLANE[plane] if isinstance(plane, str) else int(plane)
+        w, h = C.c_int32(), C.c_int32()
+        self._ck(lib.vpt_plane_dims(self._h, pid, C.byref(w), C.byref(h)), "vpt_plane_dims")
+        return h.value, w.value
+
     def read_plane(self, plane) -> np.ndarray:
         pid, nbytes, ch, dt = self.plane_info(plane)
-        out = np.empty((self.height, self.width, ch), dtype=dt)
+        out = np.empty((*self.plane_dims(pid), ch), dtype=dt)
         self._ck(lib.vpt_read_plane(self._h, pid, _ptr(out), out.nbytes), "vpt_read_plane")
         return out
 
     def write_plane(self, plane, data: np.ndarray):
         pid, nbytes, ch, dt = self.plane_info(plane)
-        a = np.ascontiguousarray(np.asarray(data).reshape(self.height, self.width, ch), dtype=dt)
+        a = np.ascontiguousarray(np.asarray(data).reshape(*self.plane_dims(pid), ch), dtype=dt)
         self._ck(lib.vpt_write_plane(self._h, pid, _ptr(a), a.nbytes), "vpt_write_plane")
 
     # instrumentation

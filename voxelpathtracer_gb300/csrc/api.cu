@@ -28,26 +28,27 @@ struct PlaneMeta {
     int channels;
     int typed;    // 1: storage type (f32/f16); 0: fixed dtype below
     int dtype;
+    int gi;       // 1: on the GI grid; 0: at the G-buffer's resolution
 };
 
 PlaneMeta plane_meta(int plane) {
     switch (plane) {
-        case VPT_PLANE_T: case VPT_PLANE_PREV_T: return {1, 1, 0};
+        case VPT_PLANE_T: case VPT_PLANE_PREV_T: return {1, 1, 0, 0};
         case VPT_PLANE_FACE: case VPT_PLANE_BLOCK: case VPT_PLANE_SHADOW:
-        case VPT_PLANE_PREV_FACE: case VPT_PLANE_PREV_BLOCK: return {1, 0, VPT_DTYPE_U8};
-        case VPT_PLANE_HIT: return {3, 0, VPT_DTYPE_I32};
-        case VPT_PLANE_STEPS: return {1, 0, VPT_DTYPE_U16};
+        case VPT_PLANE_PREV_FACE: case VPT_PLANE_PREV_BLOCK: return {1, 0, VPT_DTYPE_U8, 0};
+        case VPT_PLANE_HIT: return {3, 0, VPT_DTYPE_I32, 0};
+        case VPT_PLANE_STEPS: return {1, 0, VPT_DTYPE_U16, 0};
         case VPT_PLANE_GI_SH: case VPT_PLANE_PRE_SH: case VPT_PLANE_TEMP_SH: case VPT_PLANE_HIST_SH:
-        case VPT_PLANE_VAR_SH: case VPT_PLANE_DEN_SH: return {4, 1, 0};
-        case VPT_PLANE_TEMP_UTIL: case VPT_PLANE_HIST_UTIL: return {4, 1, 0};
+        case VPT_PLANE_VAR_SH: case VPT_PLANE_DEN_SH: return {4, 1, 0, 1};
+        case VPT_PLANE_TEMP_UTIL: case VPT_PLANE_HIST_UTIL: return {4, 1, 0, 1};
         case VPT_PLANE_GI_COCG: case VPT_PLANE_PRE_COCG: case VPT_PLANE_TEMP_COCG: case VPT_PLANE_HIST_COCG:
-        case VPT_PLANE_VAR_COCG: case VPT_PLANE_DEN_COCG: return {2, 1, 0};
+        case VPT_PLANE_VAR_COCG: case VPT_PLANE_DEN_COCG: return {2, 1, 0, 1};
         case VPT_PLANE_GI_AOSKY: case VPT_PLANE_PRE_AOSKY: case VPT_PLANE_TEMP_AOSKY: case VPT_PLANE_HIST_AOSKY:
-        case VPT_PLANE_DEN_AOSKY: return {2, 1, 0};
+        case VPT_PLANE_DEN_AOSKY: return {2, 1, 0, 1};
         case VPT_PLANE_GI_LUMA: case VPT_PLANE_PRE_LUMA: case VPT_PLANE_VAR_VARIANCE:
-        case VPT_PLANE_DEN_VARIANCE: return {1, 1, 0};
-        case VPT_PLANE_COLOR: return {3, 1, 0};
-        default: return {0, 0, -1};
+        case VPT_PLANE_DEN_VARIANCE: return {1, 1, 0, 1};
+        case VPT_PLANE_COLOR: return {3, 1, 0, 0};
+        default: return {0, 0, -1, 0};
     }
 }
 
@@ -69,6 +70,12 @@ struct vpt_ctx {
     std::string err;
     int fp16 = 0;
     size_t npx = 0;
+    // GI grid: gd times coarser than the G-buffer, gw x gh = ngi texels; the
+    // G-buffer read at its texel centres (t, face, block), refreshed before
+    // the GI passes; with gd == 1 these point at the G-buffer itself
+    int gd = 1, gw = 0, gh = 0;
+    size_t ngi = 0;
+    void* view[3] = {};
     // world
     uint8_t* vox = nullptr;
     uint8_t* df = nullptr;
@@ -214,20 +221,20 @@ size_t plane_bytes(const vpt_ctx* c, int plane, int* channels, int* dtype) {
     int dt = m.typed ? (c->fp16 ? VPT_DTYPE_F16 : VPT_DTYPE_F32) : m.dtype;
     if (channels) *channels = m.channels;
     if (dtype) *dtype = dt;
-    return c->npx * (size_t)m.channels * dtype_size(dt);
+    return (m.gi ? c->ngi : c->npx) * (size_t)m.channels * dtype_size(dt);
 }
 
 vpt_status alloc_planes(vpt_ctx* c) {
-    const size_t n = c->npx, es = c->fp16 ? 2 : 4;
+    const size_t nf = c->npx, n = c->ngi, es = c->fp16 ? 2 : 4;
     vpt_status s;
 #define A(ptr, bytes) \
     if ((s = dalloc(c, (void**)&(ptr), (bytes))) != VPT_OK) return s
     for (int k = 0; k < 2; k++) {
-        A(c->gbuf[k][GB_T], n * es);
-        A(c->gbuf[k][GB_FACE], n);
-        A(c->gbuf[k][GB_BLOCK], n);
-        A(c->gbuf[k][GB_HIT], n * 12);
-        A(c->gbuf[k][GB_STEPS], n * 2);
+        A(c->gbuf[k][GB_T], nf * es);
+        A(c->gbuf[k][GB_FACE], nf);
+        A(c->gbuf[k][GB_BLOCK], nf);
+        A(c->gbuf[k][GB_HIT], nf * 12);
+        A(c->gbuf[k][GB_STEPS], nf * 2);
         A(c->hist[k][HI_SH], n * 4 * es);
         A(c->hist[k][HI_COCG], n * 2 * es);
         A(c->hist[k][HI_UTIL], n * 4 * es);
@@ -237,7 +244,12 @@ vpt_status alloc_planes(vpt_ctx* c) {
         A(c->den[k][FI_VAR], n * es);
         A(c->den[k][FI_AOSKY], n * 2 * es);
     }
-    A(c->shadow, n);
+    A(c->shadow, nf);
+    if (c->gd > 1) {
+        A(c->view[0], n * es);
+        A(c->view[1], n);
+        A(c->view[2], n);
+    }
     A(c->gi[GI_SH], n * 4 * es);
     A(c->gi[GI_COCG], n * 2 * es);
     A(c->gi[GI_LUMA], n * es);
@@ -250,7 +262,7 @@ vpt_status alloc_planes(vpt_ctx* c) {
     A(c->var[FI_COCG], n * 2 * es);
     A(c->var[FI_VAR], n * es);
     c->var[FI_AOSKY] = nullptr;
-    A(c->color, n * 3 * es);
+    A(c->color, nf * 3 * es);
     A(c->counters, sizeof(Counters));
     A(c->queue, 256);
 #undef A
@@ -260,7 +272,7 @@ vpt_status alloc_planes(vpt_ctx* c) {
 // Fills the previous-frame G-buffer with "miss" and zeroes the history, the
 // state the first frame reprojects from.
 vpt_status clear_history(vpt_ctx* c) {
-    const size_t n = c->npx, es = c->fp16 ? 2 : 4;
+    const size_t n = c->npx, ng = c->ngi, es = c->fp16 ? 2 : 4;
     int prv = 1 - c->cur;
     std::vector<uint8_t> minus_one(n * es);
     if (c->fp16) {
@@ -273,10 +285,10 @@ vpt_status clear_history(vpt_ctx* c) {
     CK(c, cudaMemcpyAsync(c->gbuf[prv][GB_T], minus_one.data(), n * es, cudaMemcpyHostToDevice, c->stream));
     CK(c, cudaMemsetAsync(c->gbuf[prv][GB_FACE], kFaceMiss, n, c->stream));
     CK(c, cudaMemsetAsync(c->gbuf[prv][GB_BLOCK], 0, n, c->stream));
-    CK(c, cudaMemsetAsync(c->hist[prv][HI_SH], 0, n * 4 * es, c->stream));
-    CK(c, cudaMemsetAsync(c->hist[prv][HI_COCG], 0, n * 2 * es, c->stream));
-    CK(c, cudaMemsetAsync(c->hist[prv][HI_UTIL], 0, n * 4 * es, c->stream));
-    CK(c, cudaMemsetAsync(c->hist[prv][HI_AOSKY], 0, n * 2 * es, c->stream));
+    CK(c, cudaMemsetAsync(c->hist[prv][HI_SH], 0, ng * 4 * es, c->stream));
+    CK(c, cudaMemsetAsync(c->hist[prv][HI_COCG], 0, ng * 2 * es, c->stream));
+    CK(c, cudaMemsetAsync(c->hist[prv][HI_UTIL], 0, ng * 4 * es, c->stream));
+    CK(c, cudaMemsetAsync(c->hist[prv][HI_AOSKY], 0, ng * 2 * es, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     c->have_prev = false;
     return VPT_OK;
@@ -302,6 +314,24 @@ vpt_status check_world(vpt_ctx* c) {
 vpt_status check_frame(vpt_ctx* c, const vpt_frame* f) {
     if (!f) return fail(c, VPT_ERR_INVALID_ARG, "frame is NULL");
     if (!c->have_cam) return fail(c, VPT_ERR_STATE, "no primary trace this frame");
+    return VPT_OK;
+}
+
+// Refreshes the GI-grid reading of this frame's G-buffer (a no-op when the
+// grids coincide). Called by every pass that reads it, so planes written by
+// the caller between passes are picked up.
+vpt_status refresh_view(vpt_ctx* c) {
+    const int cur = c->cur;
+    if (c->gd == 1) {
+        c->view[0] = c->gbuf[cur][GB_T];
+        c->view[1] = c->gbuf[cur][GB_FACE];
+        c->view[2] = c->gbuf[cur][GB_BLOCK];
+        return VPT_OK;
+    }
+    CK(c, gi_view(c->cfg.width, c->cfg.height, c->gw, c->gh, c->fp16, c->gbuf[cur][GB_T],
+                  (const uint8_t*)c->gbuf[cur][GB_FACE], (const uint8_t*)c->gbuf[cur][GB_BLOCK], c->view[0],
+                  (uint8_t*)c->view[1], (uint8_t*)c->view[2], c->stream));
+    c->launches += 1;
     return VPT_OK;
 }
 
@@ -338,6 +368,7 @@ vpt_status vpt_default_config(vpt_config* cfg) {
     cfg->storage = VPT_STORAGE_F32;
     cfg->atrous_iterations = 5;
     cfg->resolution_scale = 1.0f;
+    cfg->gi_divisor = 1;
     cfg->color_phi_bias = 3.325f;
     cfg->device = 0;
     return VPT_OK;
@@ -378,6 +409,8 @@ vpt_status vpt_create(vpt_ctx** out, const vpt_config* cfg) {
         cfg->spp > 32 || cfg->atrous_iterations < 0 || cfg->atrous_iterations > 8 ||
         (cfg->denoiser != VPT_DENOISER_SVGF && cfg->denoiser != VPT_DENOISER_ATROUS))
         return VPT_ERR_INVALID_ARG;
+    const int gd = cfg->gi_divisor <= 1 ? 1 : cfg->gi_divisor;
+    if (cfg->gi_divisor < 0 || gd > 16 || cfg->width % gd != 0 || cfg->height % gd != 0) return VPT_ERR_INVALID_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
         cudaGetLastError();
@@ -392,6 +425,10 @@ vpt_status vpt_create(vpt_ctx** out, const vpt_config* cfg) {
     c->tuning.trace_blocks = 0;
     c->fp16 = cfg->storage == VPT_STORAGE_F16;
     c->npx = (size_t)cfg->width * (size_t)cfg->height;
+    c->gd = gd;
+    c->gw = cfg->width / gd;
+    c->gh = cfg->height / gd;
+    c->ngi = (size_t)c->gw * (size_t)c->gh;
     vpt_status s = VPT_OK;
     if (cudaSetDevice(c->dev) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         s = VPT_ERR_CUDA;
@@ -584,9 +621,9 @@ vpt_status vpt_trace_diffuse(vpt_ctx* c, const vpt_frame* f) {
     a.lighting = gi_lighting(f);
     GIOut o{c->gi[GI_SH], c->gi[GI_COCG], c->gi[GI_LUMA], c->gi[GI_AOSKY]};
     pass_begin(c, VPT_PASS_DIFFUSE);
-    CK(c, trace_diffuse(world_view(c), cam_view(c->cam), c->cfg.width, c->cfg.height, a, c->fp16,
-                        c->gbuf[c->cur][GB_T], (const uint8_t*)c->gbuf[c->cur][GB_FACE], o,
-                        c->stats ? c->counters : nullptr, c->stream));
+    if ((s = refresh_view(c)) != VPT_OK) return s;
+    CK(c, trace_diffuse(world_view(c), cam_view(c->cam), c->gw, c->gh, a, c->fp16, c->view[0],
+                        (const uint8_t*)c->view[1], o, c->stats ? c->counters : nullptr, c->stream));
     pass_end(c, VPT_PASS_DIFFUSE);
     c->launches += 1;
     return VPT_OK;
@@ -597,6 +634,7 @@ vpt_status vpt_trace_frame(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f
     if (!cam || !f) return fail(c, VPT_ERR_INVALID_ARG, "camera and frame are required");
     vpt_status s = check_world(c);
     if (s != VPT_OK) return s;
+    if (c->gd != 1) return fail(c, VPT_ERR_STATE, "the fused trace needs the GI on the G-buffer's grid");
     cudaSetDevice(c->dev);
     c->cam = *cam;
     c->have_cam = true;
@@ -724,12 +762,15 @@ vpt_status svgf_run(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f, 
     vpt_status s = check_frame(c, f);
     if (s != VPT_OK) return s;
     cudaSetDevice(c->dev);
-    const int W = c->cfg.width, H = c->cfg.height, cur = c->cur, prv = 1 - c->cur;
+    // the passes run on the GI grid (W x H); the previous G-buffer and the
+    // a-trous taps sample the G-buffer at its own Wf x Hf
+    const int W = c->gw, H = c->gh, Wf = c->cfg.width, Hf = c->cfg.height, cur = c->cur, prv = 1 - c->cur;
     const CamView cv = cam_view(c->cam);
     const vpt_camera& pc = prev_cam ? *prev_cam : (c->have_prev ? c->prev_cam : c->cam);
-    const void* t = c->gbuf[cur][GB_T];
-    const uint8_t* face = (const uint8_t*)c->gbuf[cur][GB_FACE];
-    const uint8_t* block = (const uint8_t*)c->gbuf[cur][GB_BLOCK];
+    if ((s = refresh_view(c)) != VPT_OK) return s;
+    const void* t = c->view[0];
+    const uint8_t* face = (const uint8_t*)c->view[1];
+    const uint8_t* block = (const uint8_t*)c->view[2];
     if (c->cfg.denoiser == VPT_DENOISER_ATROUS) {
         // the non-SVGF path (Core/Pipeline.cpp:2618-2786)
         TemporalArgs ta;
@@ -743,6 +784,8 @@ vpt_status svgf_run(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f, 
         PlainDenoiseIO io;
         io.t = t;
         io.prev_t = c->gbuf[prv][GB_T];
+        io.Wf = Wf;
+        io.Hf = Hf;
         io.face = face;
         io.block = block;
         io.cur = GIIn{c->gi[GI_SH], c->gi[GI_COCG], c->gi[GI_LUMA], c->gi[GI_AOSKY]};
@@ -776,7 +819,7 @@ vpt_status svgf_run(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f, 
     HistIO hout{c->hist[cur][HI_SH], c->hist[cur][HI_COCG], c->hist[cur][HI_UTIL], c->hist[cur][HI_AOSKY]};
     HistIO hprev{c->hist[prv][HI_SH], c->hist[prv][HI_COCG], c->hist[prv][HI_UTIL], c->hist[prv][HI_AOSKY]};
     pass_begin(c, VPT_PASS_TEMPORAL);
-    CK(c, svgf_temporal(cv, W, H, c->fp16, ta, t, face, block, c->gbuf[prv][GB_T],
+    CK(c, svgf_temporal(cv, W, H, Wf, Hf, c->fp16, ta, t, face, block, c->gbuf[prv][GB_T],
                         (const uint8_t*)c->gbuf[prv][GB_FACE], (const uint8_t*)c->gbuf[prv][GB_BLOCK],
                         GIIn{c->pre[GI_SH], c->pre[GI_COCG], c->pre[GI_LUMA], c->pre[GI_AOSKY]}, hprev, hout,
                         c->stream));
@@ -810,7 +853,8 @@ vpt_status svgf_run(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f, 
         }
         int k = it & 1;
         FiltIO out{c->den[k][FI_SH], c->den[k][FI_COCG], c->den[k][FI_VAR], c->den[k][FI_AOSKY]};
-        CK(c, svgf_atrous(cv, W, H, c->fp16, aa, t, face, c->hist[cur][HI_UTIL], in, in_ao, out, c->stream));
+        CK(c, svgf_atrous(cv, W, H, Wf, Hf, c->fp16, aa, t, face, c->gbuf[cur][GB_T],
+                          (const uint8_t*)c->gbuf[cur][GB_FACE], c->hist[cur][HI_UTIL], in, in_ao, out, c->stream));
         c->den_last = k;
         c->launches += 1;
     }
@@ -840,6 +884,7 @@ vpt_status shade_run(vpt_ctx* c, const vpt_frame* f, int source, void* out = nul
     a.sun_vis = 1.0f - sv;
     const bool plain = c->cfg.denoiser == VPT_DENOISER_ATROUS;
     a.vxao = plain ? 0 : 1;
+    a.gi_div = c->gd;
     const void* sh = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_SH]
                                                   : (plain ? c->hist[c->cur][HI_SH] : c->var[FI_SH]);
     const void* cocg = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_COCG]
@@ -865,7 +910,7 @@ vpt_status shade_run(vpt_ctx* c, const vpt_frame* f, int source, void* out = nul
 
 vpt_status trace_all(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f) {
     vpt_status s;
-    if (c->tuning.fused_trace) return vpt_trace_frame(c, cam, f);
+    if (c->tuning.fused_trace && c->gd == 1) return vpt_trace_frame(c, cam, f);
     if ((s = vpt_trace_primary(c, cam)) != VPT_OK) return s;
     if ((s = vpt_trace_shadow(c, f)) != VPT_OK) return s;
     return vpt_trace_diffuse(c, f);
@@ -909,6 +954,7 @@ vpt_status vpt_learned_input(vpt_ctx* c, const vpt_camera* cam, const vpt_frame*
     if (!c) return VPT_ERR_INVALID_ARG;
     if (!cam || !f) return fail(c, VPT_ERR_INVALID_ARG, "camera and frame are required");
     if (c->cfg.denoiser != VPT_DENOISER_SVGF) return fail(c, VPT_ERR_STATE, "the learned path needs the SVGF denoiser");
+    if (c->gd != 1) return fail(c, VPT_ERR_STATE, "the learned path needs the GI on the G-buffer's grid");
     const vpt_camera prev = c->have_prev ? c->prev_cam : *cam;
     vpt_status s;
     if ((s = trace_all(c, cam, f)) != VPT_OK) return s;
@@ -938,7 +984,7 @@ vpt_status vpt_render_frame_learned(vpt_ctx* c, vpt_unet* net, const vpt_camera*
     if (!cam || !f) return fail(c, VPT_ERR_INVALID_ARG, "camera and frame are required");
     if (used_net) *used_net = 0;
     const int W = c->cfg.width, H = c->cfg.height;
-    const bool fits = net && c->cfg.denoiser == VPT_DENOISER_SVGF && (W % 4) == 0 && (H % 4) == 0;
+    const bool fits = net && c->cfg.denoiser == VPT_DENOISER_SVGF && c->gd == 1 && (W % 4) == 0 && (H % 4) == 0;
     vpt_status s;
     if (!fits) {
         // SVGF fallback: the plain frame
@@ -1013,6 +1059,14 @@ vpt_status vpt_plane_info(const vpt_ctx* c, int32_t plane, size_t* bytes, int32_
     if (bytes) *bytes = b;
     if (channels) *channels = ch;
     if (dtype) *dtype = dt;
+    return VPT_OK;
+}
+
+vpt_status vpt_plane_dims(const vpt_ctx* c, int32_t plane, int32_t* width, int32_t* height) {
+    if (!c || plane < 0 || plane >= VPT_PLANE_COUNT) return VPT_ERR_INVALID_ARG;
+    const bool gi = plane_meta(plane).gi != 0;
+    if (width) *width = gi ? c->gw : c->cfg.width;
+    if (height) *height = gi ? c->gh : c->cfg.height;
     return VPT_OK;
 }
 

@@ -203,23 +203,28 @@ struct AtrousArgs {
 
 cudaError_t svgf_spatial_initial(const CamView& cam, int W, int H, int fp16, const void* t, const uint8_t* face,
                                  GIIn in, GIOut out, cudaStream_t s);
-cudaError_t svgf_temporal(const CamView& cam, int W, int H, int fp16, const TemporalArgs& a,
+// W x H: the GI grid; Wf x Hf: the G-buffer (equal unless the GI grid is coarser).
+cudaError_t svgf_temporal(const CamView& cam, int W, int H, int Wf, int Hf, int fp16, const TemporalArgs& a,
                           const void* t, const uint8_t* face, const uint8_t* block,
                           const void* prev_t, const uint8_t* prev_face, const uint8_t* prev_block,
                           GIIn cur, HistIO prev, HistIO out, cudaStream_t s);
 cudaError_t svgf_variance(const CamView& cam, int W, int H, int fp16, const void* t, const uint8_t* face,
                           HistIO in, FiltIO out, cudaStream_t s);
-cudaError_t svgf_atrous(const CamView& cam, int W, int H, int fp16, const AtrousArgs& a,
-                        const void* t, const uint8_t* face, const void* temporal_util,
-                        FiltIO in, const void* in_aosky, FiltIO out, cudaStream_t s);
+cudaError_t svgf_atrous(const CamView& cam, int W, int H, int Wf, int Hf, int fp16, const AtrousArgs& a,
+                        const void* t, const uint8_t* face, const void* tf, const uint8_t* ff,
+                        const void* temporal_util, FiltIO in, const void* in_aosky, FiltIO out, cudaStream_t s);
+// The G-buffer (W x H) read at the texel centres of the Wg x Hg GI grid.
+cudaError_t gi_view(int W, int H, int Wg, int Hg, int fp16, const void* t, const uint8_t* face, const uint8_t* block,
+                    void* tv, uint8_t* fv, uint8_t* bv, cudaStream_t s);
 
 // ------------------------------------------------------ plain_filter.cu --
 // The non-SVGF path: temporal -> variance -> `iterations` a-trous passes
 // ping-ponging between out[0] and out[1] (the last one lands in
 // out[(iterations - 1) & 1]).
 struct PlainDenoiseIO {
-    const void* t;
-    const void* prev_t;
+    const void* t;         // this frame's depth on the GI grid
+    const void* prev_t;    // the previous frame's depth at the G-buffer's Wf x Hf
+    int Wf, Hf;
     const uint8_t* face;
     const uint8_t* block;
     GIIn cur;          // raw GI planes
@@ -238,6 +243,7 @@ struct ShadeArgs {
     float sun_color[3], moon_color[3];
     float sun_vis;             // 1 - clamp(dot(sun, up) + 0.05, 0, 0.1) * 12
     int vxao;                  // u_DoVXAO && u_SVGFEnabled: the GI AO darkens the indirect term
+    int gi_div;                // the GI planes are (W / gi_div) x (H / gi_div)
 };
 cudaError_t shade(const WorldView& w, const CamView& cam, int W, int H, int fp16, const ShadeArgs& a,
                   const void* t, const uint8_t* face, const uint8_t* block, const uint8_t* shadow,

@@ -17,8 +17,9 @@ __device__ __forceinline__ bool pixel_of(int W, int H, int* i, int* j) {
 
 // TemporalFilter.glsl main (:369-487), u_DiffuseTemporal on, u_MinimumMix 0,
 // u_MaximumMix 0.96. AO passes through, the utility plane is zeroed.
-template <typename S>
-__global__ void __launch_bounds__(256) k_plain_temporal(CamView cam, int W, int H, TemporalArgs a, const S* t,
+template <typename S, bool kScaled>
+__global__ void __launch_bounds__(256) k_plain_temporal(CamView cam, int W, int H, int Wf, int Hf, TemporalArgs a,
+                                                        const S* t,
                                                         const S* prev_t, const S* c_sh, const S* c_cocg,
                                                         const S* c_aosky, const S* p_sh, const S* p_cocg, S* o_sh,
                                                         S* o_cocg, S* o_util, S* o_aosky) {
@@ -35,8 +36,9 @@ __global__ void __launch_bounds__(256) k_plain_temporal(CamView cam, int W, int 
         const v4 pr = mat_mul4(a.prev_view_proj, bp.x, bp.y, bp.z, 1.0f);
         const v2 rc = mk2((pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f);
         const Bilin fp = bilin(rc, W, H);
+        const Bilin fq = kScaled ? bilin(rc, Wf, Hf) : fp;
         const float4 psh = bl4(p_sh, fp);
-        const float pt = bl1(prev_t, fp);
+        const float pt = bl1(prev_t, fq);
         const v3 pp = add(ray_origin(cam), muls(normalize(ray_dir_at(cam, rc)), pt));
         const float bias = 0.01f;
         if (rc.x > 0.0f + bias && rc.x < 1.0f - bias && rc.y > 0.0f + bias && rc.y < 1.0f - bias) {
@@ -145,10 +147,16 @@ const dim3 kBlock2(32, 8);
 template <typename S>
 cudaError_t run_plain(const CamView& cam, int W, int H, const TemporalArgs& ta, const PlainDenoiseIO& io,
                       cudaStream_t s) {
-    k_plain_temporal<S><<<grid2(W, H), kBlock2, 0, s>>>(
-        cam, W, H, ta, (const S*)io.t, (const S*)io.prev_t, (const S*)io.cur.sh, (const S*)io.cur.cocg,
-        (const S*)io.cur.aosky, (const S*)io.prev.sh, (const S*)io.prev.cocg, (S*)io.temporal.sh,
-        (S*)io.temporal.cocg, (S*)io.temporal.util, (S*)io.temporal.aosky);
+    if (io.Wf != W || io.Hf != H)
+        k_plain_temporal<S, true><<<grid2(W, H), kBlock2, 0, s>>>(
+            cam, W, H, io.Wf, io.Hf, ta, (const S*)io.t, (const S*)io.prev_t, (const S*)io.cur.sh,
+            (const S*)io.cur.cocg, (const S*)io.cur.aosky, (const S*)io.prev.sh, (const S*)io.prev.cocg,
+            (S*)io.temporal.sh, (S*)io.temporal.cocg, (S*)io.temporal.util, (S*)io.temporal.aosky);
+    else
+        k_plain_temporal<S, false><<<grid2(W, H), kBlock2, 0, s>>>(
+            cam, W, H, io.Wf, io.Hf, ta, (const S*)io.t, (const S*)io.prev_t, (const S*)io.cur.sh,
+            (const S*)io.cur.cocg, (const S*)io.cur.aosky, (const S*)io.prev.sh, (const S*)io.prev.cocg,
+            (S*)io.temporal.sh, (S*)io.temporal.cocg, (S*)io.temporal.util, (S*)io.temporal.aosky);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_plain_variance<S><<<grid2(W, H), kBlock2, 0, s>>>(W, H, (const S*)io.temporal.sh, (S*)io.variance);

@@ -72,32 +72,47 @@ struct UpscaledGI {
 // a-trous kernel, depth weight exp(-2|dd|)^5.25 and normal weight
 // max(n.n', 1e-6)^16; beyond 128 units the sun shadow is filtered over the
 // centre and its four immediate neighbours, otherwise read at the pixel; then
-// +0.05 shadow bias (:641-643). The GI planes have the G-buffer's resolution,
-// so every tap is a texel centre, REPEAT wrapped. All loads of a tap are
-// issued before its weights are formed; taps in x-outer, y-inner order keep
-// the sums' rounding identical to the shader's loop.
-template <typename S>
-__device__ __forceinline__ UpscaledGI upscale_gi(int W, int H, int i, int j, const S* t, const uint8_t* face,
-                                                 const uint8_t* shadow, const S* sh_p, const S* cocg_p,
-                                                 const S* ao_p, v3 base_n, float base_d) {
+// +0.05 shadow bias (:641-643). Taps are one GI texel apart (TexelSize of
+// u_DiffuseSHy, :565): on a GI grid d times coarser (kScaled) they land on
+// G-buffer texel centres d texels apart (fetched, REPEAT wrapped: the shader
+// has no screen-space test here) and between GI texels (bilinear); with d = 1
+// every tap is a texel centre of both. All loads of a tap are issued before
+// its weights are formed; taps in x-outer, y-inner order keep the sums'
+// rounding identical to the shader's loop.
+template <typename S, bool kScaled>
+__device__ __forceinline__ UpscaledGI upscale_gi(int W, int H, int d, int i, int j, v2 uv, const S* t,
+                                                 const uint8_t* face, const uint8_t* shadow, const S* sh_p,
+                                                 const S* cocg_p, const S* ao_p, v3 base_n, float base_d) {
     UpscaledGI u;
     float4 tsh = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     float tcc0 = 0.0f, tcc1 = 0.0f, tao = 0.0f, tw = 0.0f, tsw = 0.0f;
     const bool filter_shadows = base_d > 128.0f;
     float tshadow = filter_shadows ? 0.0f : (float)__ldg(shadow + (size_t)j * W + i);
-    const bool inner = i > 0 && j > 0 && i < W - 1 && j < H - 1;
+    const int Wg = W / d, Hg = H / d;
+    const float texel_x = 1.0f / (float)Wg, texel_y = 1.0f / (float)Hg;
+    const bool inner = i >= d && j >= d && i < W - d && j < H - d;
 #pragma unroll
     for (int x = -1; x <= 1; x++) {
-        const int si = inner ? i + x : wrapi(i + x, W);
+        const int si = inner ? i + d * x : wrapi(i + d * x, W);
 #pragma unroll
         for (int y = -1; y <= 1; y++) {
-            const int sj = inner ? j + y : wrapi(j + y, H);
+            const int sj = inner ? j + d * y : wrapi(j + d * y, H);
             const size_t q = (size_t)sj * W + si;
             const float tt = ld(t + q);
             const int fid = __ldg(face + q);
-            const float4 s4 = ld4(sh_p + q * 4);
-            const float2 c2 = ld2(cocg_p + q * 2);
-            const float a0 = ld(ao_p + q * 2);
+            float4 s4;
+            float2 c2;
+            float a0;
+            if (kScaled) {
+                const Bilin fg = bilin(mk2(uv.x + (float)x * texel_x, uv.y + (float)y * texel_y), Wg, Hg);
+                s4 = bl4(sh_p, fg);
+                c2 = bl2(cocg_p, fg);
+                a0 = bl2(ao_p, fg).x;
+            } else {
+                s4 = ld4(sh_p + q * 4);
+                c2 = ld2(cocg_p + q * 2);
+                a0 = ld(ao_p + q * 2);
+            }
             const bool cross = x == 0 || y == 0;
             const float sv = (filter_shadows && cross) ? (float)__ldg(shadow + q) : 0.0f;
             const float lda = 1.0f / (1.0f / tt);
@@ -138,7 +153,7 @@ __device__ __forceinline__ UpscaledGI upscale_gi(int W, int H, int i, int j, con
     return u;
 }
 
-template <typename S>
+template <typename S, bool kScaled>
 __global__ void __launch_bounds__(256) k_shade(WorldView w, CamView cam, int W, int H, ShadeArgs a, const S* t,
                                                const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
                                                const S* sh_p, const S* cocg_p, const S* ao_p, S* rgb) {
@@ -160,7 +175,8 @@ __global__ void __launch_bounds__(256) k_shade(WorldView w, CamView cam, int W, 
         v3 albedo = basic_saturation(m.albedo, 1.0f - 0.1f);
         if (m.metal >= 0.1f - 0.01f) albedo = basic_saturation(albedo, 0.9f);
         float emissivity = (float)m.emissive;
-        const UpscaledGI up = upscale_gi(W, H, i, j, t, face, shadow, sh_p, cocg_p, ao_p, n, dist);
+        const UpscaledGI up =
+            upscale_gi<S, kScaled>(W, H, a.gi_div, i, j, uv, t, face, shadow, sh_p, cocg_p, ao_p, n, dist);
         float up_shadow = clampf(up.shadow, 0.0f, 1.0f);
         float rt_shadow = clampf(clampf(up_shadow + 0.0f, 0.0f, 1.0f), 0.0f, 1.0f);
         v3 indirect = sh_to_irradiance(up.sh, up.cocg, n);
@@ -226,14 +242,16 @@ cudaError_t shade(const WorldView& w, const CamView& cam, int W, int H, int fp16
                   const void* sh, const void* cocg, const void* aosky, void* rgb, cudaStream_t s) {
     dim3 grid((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8));
     dim3 blk(32, 8);
-    if (fp16)
-        k_shade<__half><<<grid, blk, 0, s>>>(w, cam, W, H, a, (const __half*)t, face, block, shadow,
-                                             (const __half*)sh, (const __half*)cocg, (const __half*)aosky,
-                                             (__half*)rgb);
-    else
-        k_shade<float><<<grid, blk, 0, s>>>(w, cam, W, H, a, (const float*)t, face, block, shadow,
-                                            (const float*)sh, (const float*)cocg, (const float*)aosky,
-                                            (float*)rgb);
+    const bool scaled = a.gi_div > 1;
+    if (fp16) {
+        auto k = scaled ? k_shade<__half, true> : k_shade<__half, false>;
+        k<<<grid, blk, 0, s>>>(w, cam, W, H, a, (const __half*)t, face, block, shadow, (const __half*)sh,
+                               (const __half*)cocg, (const __half*)aosky, (__half*)rgb);
+    } else {
+        auto k = scaled ? k_shade<float, true> : k_shade<float, false>;
+        k<<<grid, blk, 0, s>>>(w, cam, W, H, a, (const float*)t, face, block, shadow, (const float*)sh,
+                               (const float*)cocg, (const float*)aosky, (float*)rgb);
+    }
     return cudaGetLastError();
 }
 

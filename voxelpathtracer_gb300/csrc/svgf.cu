@@ -89,9 +89,13 @@ __global__ void __launch_bounds__(256) k_spatial_initial(CamView cam, int W, int
     st(o_luma + px, butil);
 }
 
-// SVGF/TemporalFilter.glsl main (:132-360)
-template <typename S>
-__global__ void __launch_bounds__(256) k_temporal(CamView cam, int W, int H, TemporalArgs a, const S* t,
+// SVGF/TemporalFilter.glsl main (:132-360). t / face / block: this frame's
+// G-buffer on the GI grid; prev_t / prev_face / prev_block: the previous
+// G-buffer at its own Wf x Hf, sampled at the reprojected points (kScaled
+// when that grid is finer than the GI grid, so the two need separate
+// bilinear footprints).
+template <typename S, bool kScaled>
+__global__ void __launch_bounds__(256) k_temporal(CamView cam, int W, int H, int Wf, int Hf, TemporalArgs a, const S* t,
                                                   const uint8_t* face, const uint8_t* block, const S* prev_t,
                                                   const uint8_t* prev_face, const uint8_t* prev_block,
                                                   const S* c_sh, const S* c_cocg, const S* c_luma, const S* c_aosky,
@@ -100,7 +104,7 @@ __global__ void __launch_bounds__(256) k_temporal(CamView cam, int W, int H, Tem
     int i, j;
     if (!pixel_of(W, H, &i, &j)) return;
     const Plane<S, 1> T{t, W, H};
-    const Plane8 PF{prev_face, W, H}, PB{prev_block, W, H};
+    const Plane8 PF{prev_face, Wf, Hf}, PB{prev_block, Wf, Hf};
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
     const float weights[5] = {3.0f / 32.0f, 3.0f / 32.0f, 9.0f / 64.0f, 3.0f / 32.0f, 3.0f / 32.0f};
     const int offx[5] = {1, 0, 0, -1, 0};
@@ -138,7 +142,8 @@ __global__ void __launch_bounds__(256) k_temporal(CamView cam, int W, int H, Tem
         const float b = 0.0035f;
         if (!(sc.x < 1.0f - b && sc.x > b && sc.y < 1.0f - b && sc.y > b)) continue;
         const Bilin fp = bilin(sc, W, H);
-        const float pt = bl1(prev_t, fp);
+        const Bilin fq = kScaled ? bilin(sc, Wf, Hf) : fp;
+        const float pt = bl1(prev_t, fq);
         const v3 pdir = normalize(ray_dir_at(cam, sc));
         const v3 pp = add(ray_origin(cam), muls(pdir, pt));
         v3 pn = normal_from_id(PF.nearest(sc), 1.0f);
@@ -299,14 +304,17 @@ __global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, cons
 // SVGF/SpatialFilter.glsl main (:175-355), 3x3 taps (u_LargeKernel off).
 // A tap contributes only when (BaseDepth < 0) == (DepthDiff < 0), i.e. when
 // the centre is not sky (DepthDiff = abs(...) >= 0); sky centres keep their
-// own values, so their tap loop is skipped.
-template <typename S>
-__global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, AtrousArgs a, const S* t, const uint8_t* face,
+// own values, so their tap loop is skipped. t / face: the G-buffer on the GI
+// grid (the centre); tf / ff: the G-buffer at its own Wf x Hf, sampled at the
+// taps (kScaled when that grid is finer than the GI grid).
+template <typename S, bool kScaled>
+__global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf, AtrousArgs a, const S* t,
+                                                const uint8_t* face, const S* tf, const uint8_t* ff,
                                                 const S* t_util, const S* i_sh, const S* i_cocg, const S* i_var,
                                                 const S* i_aosky, S* o_sh, S* o_cocg, S* o_var, S* o_aosky) {
     int i, j;
     if (!pixel_of(W, H, &i, &j)) return;
-    const Plane8 F{face, W, H};
+    const Plane8 F{ff, Wf, Hf};
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
     const float aw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
     const float gauss[2] = {0.60283f, 0.198585f};
@@ -372,7 +380,8 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, AtrousArgs a, c
                 // loads first (the wrapped footprint is always a valid address),
                 // so the unrolled taps' loads can all be in flight together
                 const Bilin fp = bilin(sc, W, H);
-                const float sd = bl1(t, fp);
+                const Bilin fq = kScaled ? bilin(sc, Wf, Hf) : fp;
+                const float sd = bl1(tf, fq);
                 const int sface = F.nearest(sc);
                 const float4 s4 = bl4(i_sh, fp);
                 const float2 s2 = bl2(i_cocg, fp);
@@ -434,12 +443,12 @@ cudaError_t launch_all_spatial_initial(const CamView& cam, int W, int H, const v
     return cudaGetLastError();
 }
 
-template <typename S>
-cudaError_t launch_temporal(const CamView& cam, int W, int H, const TemporalArgs& a, const void* t,
+template <typename S, bool kScaled>
+cudaError_t launch_temporal(const CamView& cam, int W, int H, int Wf, int Hf, const TemporalArgs& a, const void* t,
                             const uint8_t* face, const uint8_t* block, const void* prev_t, const uint8_t* prev_face,
                             const uint8_t* prev_block, GIIn cur, HistIO prev, HistIO out, cudaStream_t s) {
-    k_temporal<S><<<grid2(W, H), kBlock2, 0, s>>>(
-        cam, W, H, a, (const S*)t, face, block, (const S*)prev_t, prev_face, prev_block, (const S*)cur.sh,
+    k_temporal<S, kScaled><<<grid2(W, H), kBlock2, 0, s>>>(
+        cam, W, H, Wf, Hf, a, (const S*)t, face, block, (const S*)prev_t, prev_face, prev_block, (const S*)cur.sh,
         (const S*)cur.cocg, (const S*)cur.luma, (const S*)cur.aosky, (const S*)prev.sh, (const S*)prev.cocg,
         (const S*)prev.util, (const S*)prev.aosky, (S*)out.sh, (S*)out.cocg, (S*)out.util, (S*)out.aosky);
     return cudaGetLastError();
@@ -452,10 +461,12 @@ cudaError_t launch_variance(int W, int H, const void* t, const uint8_t* face, Hi
     return cudaGetLastError();
 }
 
-template <typename S>
-cudaError_t launch_atrous(int W, int H, const AtrousArgs& a, const void* t, const uint8_t* face,
-                          const void* temporal_util, FiltIO in, const void* in_aosky, FiltIO out, cudaStream_t s) {
-    k_atrous<S><<<grid2(W, H), kBlock2, 0, s>>>(W, H, a, (const S*)t, face, (const S*)temporal_util, (const S*)in.sh,
+template <typename S, bool kScaled>
+cudaError_t launch_atrous(int W, int H, int Wf, int Hf, const AtrousArgs& a, const void* t, const uint8_t* face,
+                          const void* tf, const uint8_t* ff, const void* temporal_util, FiltIO in,
+                          const void* in_aosky, FiltIO out, cudaStream_t s) {
+    k_atrous<S, kScaled><<<grid2(W, H), kBlock2, 0, s>>>(W, H, Wf, Hf, a, (const S*)t, face, (const S*)tf, ff,
+                                                         (const S*)temporal_util, (const S*)in.sh,
                                                 (const S*)in.cocg, (const S*)in.variance, (const S*)in_aosky,
                                                 (S*)out.sh, (S*)out.cocg, (S*)out.variance, (S*)out.aosky);
     return cudaGetLastError();
@@ -469,12 +480,20 @@ cudaError_t svgf_spatial_initial(const CamView& cam, int W, int H, int fp16, con
                 : launch_all_spatial_initial<float>(cam, W, H, t, face, in, out, s);
 }
 
-cudaError_t svgf_temporal(const CamView& cam, int W, int H, int fp16, const TemporalArgs& a,
+cudaError_t svgf_temporal(const CamView& cam, int W, int H, int Wf, int Hf, int fp16, const TemporalArgs& a,
                           const void* t, const uint8_t* face, const uint8_t* block,
                           const void* prev_t, const uint8_t* prev_face, const uint8_t* prev_block,
                           GIIn cur, HistIO prev, HistIO out, cudaStream_t s) {
-    return fp16 ? launch_temporal<__half>(cam, W, H, a, t, face, block, prev_t, prev_face, prev_block, cur, prev, out, s)
-                : launch_temporal<float>(cam, W, H, a, t, face, block, prev_t, prev_face, prev_block, cur, prev, out, s);
+    const bool scaled = Wf != W || Hf != H;
+    if (fp16)
+        return scaled ? launch_temporal<__half, true>(cam, W, H, Wf, Hf, a, t, face, block, prev_t, prev_face,
+                                                      prev_block, cur, prev, out, s)
+                      : launch_temporal<__half, false>(cam, W, H, Wf, Hf, a, t, face, block, prev_t, prev_face,
+                                                       prev_block, cur, prev, out, s);
+    return scaled ? launch_temporal<float, true>(cam, W, H, Wf, Hf, a, t, face, block, prev_t, prev_face, prev_block,
+                                                 cur, prev, out, s)
+                  : launch_temporal<float, false>(cam, W, H, Wf, Hf, a, t, face, block, prev_t, prev_face, prev_block,
+                                                  cur, prev, out, s);
 }
 
 cudaError_t svgf_variance(const CamView& cam, int W, int H, int fp16, const void* t, const uint8_t* face,
@@ -483,12 +502,48 @@ cudaError_t svgf_variance(const CamView& cam, int W, int H, int fp16, const void
     return fp16 ? launch_variance<__half>(W, H, t, face, in, out, s) : launch_variance<float>(W, H, t, face, in, out, s);
 }
 
-cudaError_t svgf_atrous(const CamView& cam, int W, int H, int fp16, const AtrousArgs& a,
-                        const void* t, const uint8_t* face, const void* temporal_util,
-                        FiltIO in, const void* in_aosky, FiltIO out, cudaStream_t s) {
+cudaError_t svgf_atrous(const CamView& cam, int W, int H, int Wf, int Hf, int fp16, const AtrousArgs& a,
+                        const void* t, const uint8_t* face, const void* tf, const uint8_t* ff,
+                        const void* temporal_util, FiltIO in, const void* in_aosky, FiltIO out, cudaStream_t s) {
     (void)cam;
-    return fp16 ? launch_atrous<__half>(W, H, a, t, face, temporal_util, in, in_aosky, out, s)
-                : launch_atrous<float>(W, H, a, t, face, temporal_util, in, in_aosky, out, s);
+    const bool scaled = Wf != W || Hf != H;
+    if (fp16)
+        return scaled ? launch_atrous<__half, true>(W, H, Wf, Hf, a, t, face, tf, ff, temporal_util, in, in_aosky, out, s)
+                      : launch_atrous<__half, false>(W, H, Wf, Hf, a, t, face, tf, ff, temporal_util, in, in_aosky, out, s);
+    return scaled ? launch_atrous<float, true>(W, H, Wf, Hf, a, t, face, tf, ff, temporal_util, in, in_aosky, out, s)
+                  : launch_atrous<float, false>(W, H, Wf, Hf, a, t, face, tf, ff, temporal_util, in, in_aosky, out, s);
+}
+
+namespace {
+// The G-buffer read at the texel centres of a GI grid Wg x Hg coarser than
+// its own W x H: texture() of the depth (bilinear, REPEAT wrap) and nearest
+// face and block, which is what the GI passes' GetPositionAt and normal /
+// block fetches at their own texel centres return; the depth is stored in
+// the storage type.
+template <typename S>
+__global__ void __launch_bounds__(256) k_gi_view(int W, int H, int Wg, int Hg, const S* t, const uint8_t* face,
+                                                 const uint8_t* block, S* tv, uint8_t* fv, uint8_t* bv) {
+    int i, j;
+    if (!pixel_of(Wg, Hg, &i, &j)) return;
+    const v2 uv = texcoord(i, j, Wg, Hg);
+    const Bilin fp = bilin(uv, W, H);
+    const Plane8 F{face, W, H}, B{block, W, H};
+    const size_t q = (size_t)j * Wg + i;
+    st(tv + q, bl1(t, fp));
+    fv[q] = (uint8_t)F.nearest(uv);
+    bv[q] = (uint8_t)B.nearest(uv);
+}
+}  // namespace
+
+cudaError_t gi_view(int W, int H, int Wg, int Hg, int fp16, const void* t, const uint8_t* face, const uint8_t* block,
+                    void* tv, uint8_t* fv, uint8_t* bv, cudaStream_t s) {
+    if (fp16)
+        k_gi_view<__half><<<grid2(Wg, Hg), kBlock2, 0, s>>>(W, H, Wg, Hg, (const __half*)t, face, block, (__half*)tv,
+                                                            fv, bv);
+    else
+        k_gi_view<float><<<grid2(Wg, Hg), kBlock2, 0, s>>>(W, H, Wg, Hg, (const float*)t, face, block, (float*)tv, fv,
+                                                           bv);
+    return cudaGetLastError();
 }
 
 }  // namespace vpt
