@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define VPT_ABI_VERSION 1
+#define VPT_ABI_VERSION 2
 
 typedef enum vpt_status {
     VPT_OK = 0,
@@ -64,7 +64,13 @@ typedef struct vpt_config {
     int32_t gi_divisor;              /* 1 (or 0), 2, 4 ...: DiffuseTraceResolution = DiffuseIndirectSuperSampleRes
                                         = 1 / gi_divisor (Core/Pipeline.cpp:72, :79; 4 by default, 2 in the
                                         higher presets :1256-1282); width and height must be multiples */
-    int32_t reserved[1];
+    int32_t reflection_spp;          /* 0: no reflection pass (no specular indirect in the colour pass);
+                                        else ReflectionSPP (Core/Pipeline.cpp:103, 2), 1..16. The
+                                        reflections run on the GI grid (ReflectionTraceResolution = 1/4
+                                        = DiffuseTraceResolution by default, :101) */
+    int32_t reflection_max_steps;    /* u_ReflectionTraceLength = 64 (:100) */
+    int32_t reflection_shadow_max_steps; /* 150 (ReflectionTraceFrag.glsl:1098) */
+    int32_t reserved[5];
 } vpt_config;
 
 typedef enum vpt_denoiser {
@@ -141,15 +147,20 @@ typedef enum vpt_plane {
     VPT_PLANE_DEN_VARIANCE = 30,
     VPT_PLANE_DEN_AOSKY = 31,
     VPT_PLANE_COLOR = 32,     /* ColoredFBO: RGB radiance */
-    VPT_PLANE_COUNT = 33
+    VPT_PLANE_SPEC = 33,      /* ReflectionTraceFBO: reflected radiance RGB + 1 (4 ch), GI grid */
+    VPT_PLANE_SPEC_HIT = 34,  /* its mean hit distance, -1 when every sample missed */
+    VPT_PLANE_SPEC_MASK = 35, /* 1 where a sample hit an emissive block */
+    VPT_PLANE_SPEC_OUT = 36,  /* ReflectionTemporalFBO: the specular indirect the colour pass reads */
+    VPT_PLANE_COUNT = 37
 } vpt_plane;
 
 typedef enum vpt_dtype { VPT_DTYPE_F32 = 0, VPT_DTYPE_F16 = 1, VPT_DTYPE_U8 = 2, VPT_DTYPE_U16 = 3, VPT_DTYPE_I32 = 4 } vpt_dtype;
 
 /* Counters filled while statistics are enabled (vpt_set_stats). */
 typedef struct vpt_stats {
-    uint64_t rays[4];                /* primary, sun shadow, diffuse, bounce shadow */
-    uint64_t steps[4];               /* DDA iterations per ray kind */
+    uint64_t rays[6];                /* primary, sun shadow, diffuse, bounce shadow, reflection,
+                                        reflection-hit shadow */
+    uint64_t steps[6];               /* DDA iterations per ray kind */
 } vpt_stats;
 
 /* Per-pass device times of the last frame, from CUDA events on the
@@ -159,7 +170,8 @@ typedef enum vpt_pass {
     VPT_PASS_TEMPORAL = 4, VPT_PASS_VARIANCE = 5, VPT_PASS_ATROUS = 6, VPT_PASS_SHADE = 7,
     VPT_PASS_TRACE_FRAME = 8,        /* fused primary + shadow + diffuse (vpt_trace_frame) */
     VPT_PASS_LEARNED = 9,            /* features + U-Net + colour write-back (vpt_render_frame_learned) */
-    VPT_PASS_COUNT = 10
+    VPT_PASS_REFLECTION = 10,        /* reflection trace + firefly rejection (vpt_trace_reflections) */
+    VPT_PASS_COUNT = 11
 } vpt_pass;
 
 /* Launch-shape knobs of the fused trace kernel, picked by the autotuner. */
@@ -214,7 +226,14 @@ vpt_status vpt_trace_diffuse(vpt_ctx* ctx, const vpt_frame* frame);
  * and the a-trous iterations. `prev_cam` is the previous frame's camera
  * (u_PrevView / u_PrevProjection); history planes are read and written. */
 vpt_status vpt_svgf(vpt_ctx* ctx, const vpt_camera* prev_cam, const vpt_frame* frame);
-/* Colour pass, Core/Pipeline.cpp:3603-3821 (ColorPassFrag.glsl): fills COLOR. */
+/* Reflection pass, Core/Pipeline.cpp:2998-3260 (ReflectionTraceFrag.glsl,
+ * then the firefly rejection of SpecularTemporalFilter.glsl with TEMPORAL_SPEC
+ * and DenoiseReflections off), on the GI grid, after vpt_svgf (it reads the
+ * denoised GI): fills SPEC, SPEC_HIT, SPEC_MASK and SPEC_OUT. Needs
+ * reflection_spp > 0; vpt_render_frame runs it when that is set. */
+vpt_status vpt_trace_reflections(vpt_ctx* ctx, const vpt_frame* frame);
+/* Colour pass, Core/Pipeline.cpp:3603-3821 (ColorPassFrag.glsl): fills COLOR;
+ * with reflection_spp > 0 it adds the specular indirect from SPEC_OUT. */
 vpt_status vpt_shade(vpt_ctx* ctx, const vpt_frame* frame);
 /* The three trace passes of a frame in one persistent kernel: fills T, FACE,
  * BLOCK, HIT, STEPS, SHADOW and GI_* exactly as vpt_trace_primary,
@@ -287,6 +306,8 @@ vpt_status vpt_ground_truth(vpt_ctx* ctx, const vpt_frame* frame, int32_t x0, in
 
 /* ---------------------------------------------------------------- planes -- */
 vpt_status vpt_plane_info(const vpt_ctx* ctx, int32_t plane, size_t* bytes, int32_t* channels, int32_t* dtype);
+/* vpt_read_plane / vpt_write_plane of the SPEC_* planes need reflection_spp > 0
+ * (VPT_ERR_STATE otherwise: they are not allocated). */
 /* Width and height of a plane: the G-buffer's for the G-buffer, shadow and
  * colour planes, the GI grid's (width / gi_divisor x height / gi_divisor)
  * for the GI, temporal, variance and a-trous planes. */

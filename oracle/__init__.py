@@ -41,7 +41,8 @@ class OParams(C.Structure):
                 ("bounce_shadow_max_steps", C.c_int32), ("bounces", C.c_int32), ("spp", C.c_int32),
                 ("storage", C.c_int32), ("atrous_iterations", C.c_int32), ("resolution_scale", C.c_float),
                 ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
-                ("gi_divisor", C.c_int32), ("reserved", C.c_int32 * 1)]
+                ("gi_divisor", C.c_int32), ("reflection_spp", C.c_int32), ("reflection_max_steps", C.c_int32),
+                ("reflection_shadow_max_steps", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 class OWorld(C.Structure):
@@ -82,7 +83,9 @@ def lib() -> C.CDLL:
         L.vpto_variance.argtypes = [P, P, P, P, P, P]
         L.vpto_atrous.argtypes = [P, P, P, C.c_int, P, P, P, P, P, P, P, P]
         L.vpto_gi_view.argtypes = [P, P, P, P, P, P, P]
-        L.vpto_shade.argtypes = [P, P, P, P, P, P, P, P, P, P, P, C.c_int, C.c_int, P]
+        L.vpto_shade.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, C.c_int, C.c_int, P]
+        L.vpto_trace_reflection.argtypes = [P] * 13 + [C.c_int, C.c_int, P, P, P]
+        L.vpto_spec_resolve.argtypes = [P, P, P, P]
         for name in ("vpto_exp", "vpto_exp2", "vpto_log2", "vpto_sin", "vpto_cos", "vpto_half_round"):
             getattr(L, name).argtypes = [C.c_float]
             getattr(L, name).restype = C.c_float
@@ -118,10 +121,10 @@ def omp_threads() -> int:
 class Counting:
     """Context manager that counts the oracle's rays and DDA steps."""
 
-    KINDS = ("primary", "shadow", "diffuse", "bounce_shadow")
+    KINDS = ("primary", "shadow", "diffuse", "bounce_shadow", "reflection", "reflection_shadow")
 
     def __enter__(self):
-        self.buf = np.zeros(8, dtype=np.uint64)
+        self.buf = np.zeros(12, dtype=np.uint64)
         lib().vpto_set_counters(_p(self.buf))
         return self
 
@@ -130,11 +133,11 @@ class Counting:
 
     @property
     def rays(self) -> dict:
-        return {k: int(v) for k, v in zip(self.KINDS, self.buf[:4])}
+        return {k: int(v) for k, v in zip(self.KINDS, self.buf[:6])}
 
     @property
     def steps(self) -> dict:
-        return {k: int(v) for k, v in zip(self.KINDS, self.buf[4:])}
+        return {k: int(v) for k, v in zip(self.KINDS, self.buf[6:])}
 
 
 def build_df(vox: np.ndarray) -> np.ndarray:
@@ -290,16 +293,49 @@ def atrous(cam, config, frame, step, t, face, temporal_util, filt_in: dict, aosk
     return out
 
 
-def shade(world: World, cam, config, frame, t, face, block, shadow, sh, cocg, aosky, rows=None) -> np.ndarray:
+def shade(world: World, cam, config, frame, t, face, block, shadow, sh, cocg, aosky, rows=None,
+          spec=None) -> np.ndarray:
+    """The colour pass; spec is the resolved reflection (GI grid, 4 ch) or None."""
     p = params(config)
     H, W = p.height, p.width
     out = np.zeros((H, W, 3), dtype=np.float32)
     arrs = [np.ascontiguousarray(a, dtype=dt) for a, dt in
             ((t, np.float32), (face, np.uint8), (block, np.uint8), (shadow, np.uint8), (sh, np.float32),
              (cocg, np.float32), (aosky, np.float32))]
+    sp = None if spec is None else np.ascontiguousarray(spec, dtype=np.float32)
     r0, r1 = rows if rows else (0, H)
     lib().vpto_shade(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)),
-                     *[_p(a) for a in arrs], r0, r1, _p(out))
+                     *[_p(a) for a in arrs], None if sp is None else _p(sp), r0, r1, _p(out))
+    return out
+
+
+def trace_reflection(world: World, cam, config, frame, g: dict, shadow, den: dict, rows=None) -> dict:
+    """The reflection trace on the GI grid from the full G-buffer g, the sun
+    shadow and the denoised diffuse GI den (sh, cocg, aosky); returns spec
+    (4 ch), hit and mask."""
+    p = params(config)
+    H, W = gi_dims(p)
+    v = gi_view(p, g["t"], g["face"], g["block"])
+    out = {"spec": np.zeros((H, W, 4), np.float32), "hit": np.zeros((H, W), np.float32),
+           "mask": np.zeros((H, W), np.float32)}
+    arrs = [np.ascontiguousarray(a, dtype=dt) for a, dt in
+            ((g["t"], np.float32), (g["face"], np.uint8), (shadow, np.uint8), (v["t"], np.float32),
+             (v["face"], np.uint8), (v["block"], np.uint8), (den["sh"], np.float32), (den["cocg"], np.float32),
+             (den["aosky"], np.float32))]
+    r0, r1 = rows if rows else (0, H)
+    lib().vpto_trace_reflection(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p),
+                                C.byref(_as(OFrame, frame)), *[_p(a) for a in arrs], r0, r1, _p(out["spec"]),
+                                _p(out["hit"]), _p(out["mask"]))
+    return out
+
+
+def spec_resolve(config, spec, mask) -> np.ndarray:
+    """The firefly rejection of the reflection (what the colour pass reads)."""
+    p = params(config)
+    spec = np.ascontiguousarray(spec, dtype=np.float32)
+    mask = np.ascontiguousarray(mask, dtype=np.float32)
+    out = np.zeros_like(spec)
+    lib().vpto_spec_resolve(C.byref(p), _p(spec), _p(mask), _p(out))
     return out
 
 
@@ -384,8 +420,13 @@ def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist:
             sh, cocg, ao = last["sh"], last["cocg"], last["aosky"]
         else:
             sh, cocg, ao = sv["variance"]["sh"], sv["variance"]["cocg"], sv["temporal"]["aosky"]
-    rgb = shade(world, cam, p, frame, g["t"], g["face"], g["block"], shadow, sh, cocg, ao)
-    return {"g": g, "shadow": shadow, "gi": gi, "svgf": sv, "rgb": rgb}
+    refl = None
+    if p.reflection_spp > 0:
+        refl = trace_reflection(world, cam, p, frame, g, shadow, {"sh": sh, "cocg": cocg, "aosky": ao})
+        refl["out"] = spec_resolve(p, refl["spec"], refl["mask"])
+    rgb = shade(world, cam, p, frame, g["t"], g["face"], g["block"], shadow, sh, cocg, ao,
+                spec=None if refl is None else refl["out"])
+    return {"g": g, "shadow": shadow, "gi": gi, "svgf": sv, "refl": refl, "rgb": rgb}
 
 
 def empty_history(H: int, W: int, gi_divisor: int = 1):

@@ -46,16 +46,16 @@ const float PI = 3.14159265359f;   // DiffuseRayTraceFrag.glsl:11, ColorPassFrag
 // same layout as vpt_stats; used by the CPU baseline to count its work.
 uint64_t* g_counters = nullptr;
 struct RowCount {
-    uint64_t rays[4] = {0, 0, 0, 0};
-    uint64_t steps[4] = {0, 0, 0, 0};
+    uint64_t rays[6] = {0, 0, 0, 0, 0, 0};
+    uint64_t steps[6] = {0, 0, 0, 0, 0, 0};
     void add(int kind, int nsteps) { rays[kind] += 1; steps[kind] += (uint64_t)nsteps; }
     void flush() {
         if (!g_counters) return;
-        for (int k = 0; k < 4; k++) {
+        for (int k = 0; k < 6; k++) {
 #pragma omp atomic
             g_counters[k] += rays[k];
 #pragma omp atomic
-            g_counters[4 + k] += steps[k];
+            g_counters[6 + k] += steps[k];
         }
     }
 };
@@ -218,6 +218,20 @@ struct Plane8 {
     // texture() with GL_NEAREST + GL_REPEAT
     int nearest(v2 uv) const {
         return at(f2i(std::floor(uv.x * (float)W)), f2i(std::floor(uv.y * (float)H)));
+    }
+    // texture() with GL_LINEAR + GL_REPEAT of a 0/1 plane read as UNORM8
+    // (the sun-shadow FBO, Core/Pipeline.cpp:1152), fp32 weights.
+    float linearf(v2 uv) const {
+        float x = uv.x * (float)W - 0.5f;
+        float y = uv.y * (float)H - 0.5f;
+        float x0 = std::floor(x), y0 = std::floor(y);
+        float ax = x - x0, ay = y - y0;
+        int i0 = f2i(x0), j0 = f2i(y0);
+        float v00 = (float)at(i0, j0), v10 = (float)at(i0 + 1, j0);
+        float v01 = (float)at(i0, j0 + 1), v11 = (float)at(i0 + 1, j0 + 1);
+        float b = v00 * (1.0f - ax) + v10 * ax;
+        float t = v01 * (1.0f - ax) + v11 * ax;
+        return b * (1.0f - ay) + t * ay;
     }
 };
 
@@ -1118,30 +1132,38 @@ void vpto_atrous(const vpto_camera* cam, const vpto_params* p, const vpto_frame*
 // times coarser they land on the G-buffer texel centres d texels apart (read
 // there, REPEAT wrapped: the shader has no screen-space test here) and between
 // GI texels (bilinear); with d = 1 every tap is a texel centre of both.
+// With a reflection pass the specular indirect is gathered too, weighted by
+// the GI weight / (12 |roughness - base roughness| + 1) * max(n.n', 0)^8
+// (:595-603, the G-buffer's roughness and normal being the block's and the
+// face's for flat materials).
 struct UpscaledGI {
-    float sh[4], cocg[2], ao, shadow;
+    float sh[4], cocg[2], ao, shadow, spec[4];
 };
-inline UpscaledGI upscale_gi(const Plane& T, const Plane8& F, const Plane8& S, const Plane& SH, const Plane& CC,
-                             const Plane& AO, int d, int i, int j, v2 uv, v3 base_n, float base_d) {
+inline UpscaledGI upscale_gi(const vpto_world* w, const Plane& T, const Plane8& F, const Plane8& B, const Plane8& S,
+                             const Plane& SH, const Plane& CC, const Plane& AO, const Plane* SP, int d, int i, int j,
+                             v2 uv, v3 base_n, float base_d, float base_rough) {
     const float texel_x = 1.0f / (float)SH.W, texel_y = 1.0f / (float)SH.H;
     static const float kw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
     UpscaledGI u{};
-    float tsh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, tcc[2] = {0.0f, 0.0f};
-    float tao = 0.0f, tw = 0.0f, tshadow = 0.0f, tsw = 0.0f;
+    float tsh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, tcc[2] = {0.0f, 0.0f}, tsp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    float tao = 0.0f, tw = 0.0f, tshadow = 0.0f, tsw = 0.0f, tspw = 0.0f;
     const bool filter_shadows = base_d > 128.0f;
     if (!filter_shadows) tshadow = (float)S.at(i, j);
     for (int x = -1; x <= 1; x++) {
         for (int y = -1; y <= 1; y++) {
             const int si = i + d * x, sj = j + d * y;
-            float ssh[4], scc[2], sao[2];
+            float ssh[4], scc[2], sao[2], ssp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
             if (d == 1) {
                 for (int c = 0; c < 4; c++) ssh[c] = SH.at(si, sj, c);
                 for (int c = 0; c < 2; c++) { scc[c] = CC.at(si, sj, c); sao[c] = AO.at(si, sj, c); }
+                if (SP)
+                    for (int c = 0; c < 4; c++) ssp[c] = SP->at(si, sj, c);
             } else {
                 const v2 sc = v2{uv.x + (float)x * texel_x, uv.y + (float)y * texel_y};
                 SH.linear(sc, ssh);
                 CC.linear(sc, scc);
                 AO.linear(sc, sao);
+                if (SP) SP->linear(sc, ssp);
             }
             const float lda = 1.0f / (1.0f / T.at(si, sj, 0));
             const float ed = dm_exp(-(std::fabs(lda - base_d) * 2.0f));
@@ -1151,6 +1173,14 @@ inline UpscaledGI upscale_gi(const Plane& T, const Plane8& F, const Plane8& S, c
             nw = fmaxg(nw, 0.0001f);
             const float kwt = kw[std::abs(x)] * kw[std::abs(y)];
             float wgt = clampf((nw * dw) * kwt, 0.0f, 1.0f);
+            if (SP) {
+                const float ra = material(w, std::min(std::max(B.at(si, sj), 0), 127)).rough;
+                float spw = (wgt / ((std::fabs(ra - base_rough) * 12.0f) + 1.0f)) *
+                            dm_pow(fmaxg(dot(na, base_n), 0.0f), 8.0f);
+                spw = fmaxg(spw, 0.00000001f);
+                for (int c = 0; c < 4; c++) tsp[c] += ssp[c] * spw;
+                tspw += spw;
+            }
             wgt = fmaxg(wgt, 0.00000001f);
             for (int c = 0; c < 4; c++) tsh[c] += ssh[c] * wgt;
             for (int c = 0; c < 2; c++) tcc[c] += scc[c] * wgt;
@@ -1167,6 +1197,8 @@ inline UpscaledGI upscale_gi(const Plane& T, const Plane8& F, const Plane8& S, c
     for (int c = 0; c < 4; c++) u.sh[c] = tsh[c] / tw;
     for (int c = 0; c < 2; c++) u.cocg[c] = tcc[c] / tw;
     u.ao = tao / tw;
+    tspw = fmaxg(tspw, 0.0000001f);
+    for (int c = 0; c < 4; c++) u.spec[c] = tsp[c] / tspw;
     if (filter_shadows) tshadow = tshadow / tsw;
     tshadow += 0.05f;
     u.shadow = clampf(tshadow, 0.00000000000001f, 1.0f);
@@ -1179,7 +1211,7 @@ inline UpscaledGI upscale_gi(const Plane& T, const Plane8& F, const Plane8& S, c
 void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
                 const vpto_frame* f, const float* t, const uint8_t* face, const uint8_t* block,
                 const uint8_t* shadow, const float* sh, const float* cocg, const float* aosky,
-                int row0, int row1, float* rgb) {
+                const float* spec, int row0, int row1, float* rgb) {
     const int W = p->width, H = p->height;
     const int fp16 = p->storage;
     const v3 viewer = mk3(cam->position[0], cam->position[1], cam->position[2]);
@@ -1192,8 +1224,8 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
     sun_vis = 1.0f - sun_vis;
     const bool vxao = p->denoiser == 0;
     const int d = gi_div(p), Wg = W / d, Hg = H / d;
-    const Plane T{t, W, H, 1}, SH{sh, Wg, Hg, 4}, CC{cocg, Wg, Hg, 2}, AO{aosky, Wg, Hg, 2};
-    const Plane8 F{face, W, H}, S{shadow, W, H};
+    const Plane T{t, W, H, 1}, SH{sh, Wg, Hg, 4}, CC{cocg, Wg, Hg, 2}, AO{aosky, Wg, Hg, 2}, SP{spec, Wg, Hg, 4};
+    const Plane8 F{face, W, H}, B{block, W, H}, S{shadow, W, H};
 #pragma omp parallel for schedule(dynamic, 4)
     for (int j = row0; j < row1; j++) {
         for (int i = 0; i < W; i++) {
@@ -1211,7 +1243,8 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
                 v3 albedo = basic_saturation(m.albedo, 1.0f - 0.1f);   // u_TextureDesatAmount = 0.1
                 if (m.metal >= 0.1f - 0.01f) albedo = basic_saturation(albedo, 0.9f);
                 float emissivity = (float)m.emissive;
-                const UpscaledGI up = upscale_gi(T, F, S, SH, CC, AO, d, i, j, uv, n, dist);
+                const UpscaledGI up = upscale_gi(w, T, F, B, S, SH, CC, AO, spec ? &SP : nullptr, d, i, j, uv, n, dist,
+                                                 m.rough);
                 float up_shadow = clampf(up.shadow, 0.0f, 1.0f);
                 float rt_shadow = clampf(clampf(up_shadow + 0.0f, 0.0f, 1.0f), 0.0f, 1.0f);
                 v3 indirect = sh_to_irradiance(up.sh, up.cocg, n);
@@ -1235,7 +1268,15 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
                 v3 I = normalize(sub(wp, viewer));
                 float idn = dot(n, I);
                 v3 R = sub(I, muls(n, 2.0f * idn));
-                v3 spec_ind = vmax(mk3(0, 0, 0), 0.0001f);
+                // SpecularIndirect (:901-909): the upscaled reflection times
+                // clamp(max(n.n, 1e-8)^2 * 1.5, 0.1, 1) inside the 0.0035 border
+                v3 spec_ind = mk3(0, 0, 0);
+                const float sb = 0.0035f;
+                if (spec && uv.x > sb && uv.x < 1.0f - sb && uv.y > sb && uv.y < 1.0f - sb) {
+                    const float att = clampf(dm_pow(fmaxg(dot(n, n), 0.00000001f), 2.0f) * 1.5f, 0.1f, 1.0f);
+                    spec_ind = muls(mk3(up.spec[0], up.spec[1], up.spec[2]), att);
+                }
+                spec_ind = vmax(spec_ind, 0.0001f);
                 v3 Lo = normalize(sub(viewer, wp));
                 v3 F0 = vmix(mk3(0.04f, 0.04f, 0.04f), albedo, m.metal);
                 diffuse_indirect = muls(diffuse_indirect, clampf(sampled_ao, 0.2f, 1.01f));
@@ -1264,6 +1305,289 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
             rgb[px * 3 + 0] = storage(color.x, fp16);
             rgb[px * 3 + 1] = storage(color.y, fp16);
             rgb[px * 3 + 2] = storage(color.z, fp16);
+        }
+    }
+}
+
+// ------------------------------------------------------------ reflections --
+// SHToIrradianceA (ReflectionTraceFrag.glsl:466-476): the stored irradiance
+// of an SH texel, independent of direction.
+inline v3 sh_to_irradiance_a(const float* sh, const float* cocg_in) {
+    const float Y = fmaxg(0.0f, 3.544905f * sh[3]);
+    const float k = (Y * 0.282095f) / (sh[3] + 1e-6f);
+    const float co = cocg_in[0] * k, cg = cocg_in[1] * k;
+    const float T = Y - cg * 0.5f;
+    const float G = cg + T;
+    const float B = T - co * 0.5f;
+    const float R = B + co;
+    return mk3(fmaxg(R, 0.0f), fmaxg(G, 0.0f), fmaxg(B, 0.0f));
+}
+
+// ImportanceSampleGGX (ReflectionTraceFrag.glsl:345-365)
+inline v3 importance_sample_ggx(v3 N, float roughness, float xi_x, float xi_y) {
+    const float alpha = roughness * roughness;
+    const float alpha2 = alpha * alpha;
+    const float phi = (2.0f * PI) * xi_x;
+    const float cos_t = std::sqrt((1.0f - xi_y) / (1.0f + (alpha2 - 1.0f) * xi_y));
+    const float sin_t = std::sqrt(1.0f - cos_t * cos_t);
+    const v3 H = mk3(dm_cos(phi) * sin_t, dm_sin(phi) * sin_t, cos_t);
+    const v3 up = std::fabs(N.z) < 0.999f ? mk3(0.0f, 0.0f, 1.0f) : mk3(1.0f, 0.0f, 0.0f);
+    const v3 tangent = normalize(cross(up, N));
+    const v3 bitangent = cross(N, tangent);
+    const v3 s = mk3((tangent.x * H.x + bitangent.x * H.y) + N.x * H.z, (tangent.y * H.x + bitangent.y * H.y) + N.y * H.z,
+                     (tangent.z * H.x + bitangent.z * H.y) + N.z * H.z);
+    return normalize(s);
+}
+
+// GetReflectionDirection (ReflectionTraceFrag.glsl:621-646): of three GGX
+// microfacet normals, the one closest to N; the random pairs come from the
+// pixel's PCG stream instead of hash2 / blue noise.
+inline v3 reflection_normal(v3 N, float R, uint32_t* rng) {
+    R = fmaxg(R, 0.05f);
+    float nearest = -100.0f;
+    v3 best = N;
+    for (int i = 0; i < 3; i++) {
+        const float xi_x = rand01(rng) * 0.9f;
+        const float xi_y = rand01(rng) * 0.65f;
+        const v3 h = importance_sample_ggx(N, R, xi_x, xi_y);
+        const float d = dot(h, N);
+        if (d > nearest) {
+            best = h;
+            nearest = d;
+        }
+    }
+    return best;
+}
+
+// GLSL reflect(I, N) = I - 2 * dot(N, I) * N
+inline v3 reflect3(v3 I, v3 N) { return sub(I, muls(N, 2.0f * dot(N, I))); }
+
+// CalculateDirectionalLight of the reflection trace (ReflectionTraceFrag.glsl:
+// 313-336): its specular radiance is scaled by 0, so only the diffuse lobe
+// remains; ndfGGX (:282-289), gaSchlickGGX (:300-305), fresnelSchlick (:307-310).
+inline v3 reflection_directional_light(v3 viewer, v3 wp, v3 light_dir, v3 radiance, v3 albedo, v3 n, float rough,
+                                       float metal, float shadow) {
+    const float Epsilon = 0.00001f;
+    const float sh = fming(shadow, 1.0f);
+    const v3 Lo = normalize(sub(viewer, wp));
+    const float cos_lo = fmaxg(0.0f, dot(n, Lo));
+    const v3 F0 = vmix(mk3(0.04f, 0.04f, 0.04f), albedo, metal);
+    const v3 Li = light_dir;
+    const v3 Lh = normalize(add(Li, Lo));
+    const float cos_li = fmaxg(0.0f, dot(n, Li));
+    const float cos_lh = fmaxg(0.0f, dot(n, Lh));
+    const float fk = dm_pow(1.0f - fmaxg(0.0f, dot(Lh, Lo)), 5.0f);
+    const v3 F = add(F0, muls(sub(mk3(1.0f, 1.0f, 1.0f), F0), fk));
+    const float alpha = rough * rough;
+    const float alpha_sq = alpha * alpha;
+    const float denom = (cos_lh * cos_lh) * (alpha_sq - 1.0f) + 1.0f;
+    const float D = alpha_sq / ((PI * denom) * denom);
+    const float r1 = rough + 1.0f;
+    const float k = (r1 * r1) / 8.0f;
+    const float G = (cos_li / (cos_li * (1.0f - k) + k)) * (cos_lo / (cos_lo * (1.0f - k) + k));
+    const v3 kd = vmix(sub(mk3(1.0f, 1.0f, 1.0f), F), mk3(0.0f, 0.0f, 0.0f), metal);
+    const v3 diffuse_brdf = mul(kd, albedo);
+    const v3 spec_brdf = divs(muls(muls(F, D), G), fmaxg(Epsilon, (4.0f * cos_li) * cos_lo));
+    const v3 radiance_s = muls(muls(radiance, 0.05f), 0.0f);
+    const v3 result = add(muls(mul(diffuse_brdf, radiance), cos_li), muls(mul(spec_brdf, radiance_s), cos_li));
+    return muls(vmax(result, 0.0f), clampf(1.0f - sh, 0.0f, 1.0f));
+}
+
+// The face UV of CalculateVectors (ReflectionTraceFrag.glsl:1388-1446) with
+// the shader's UV.y = 1 - UV.y (:848).
+inline v2 face_uv(v3 p, v3 n) {
+    v2 uv;
+    if (n.z != 0.0f) uv = v2{fract(p.x), fract(p.y)};
+    else if (n.y != 0.0f) uv = v2{fract(p.x), fract(p.z)};
+    else uv = v2{fract(p.z), fract(p.y)};
+    uv.y = 1.0f - uv.y;
+    return uv;
+}
+
+struct ReflectionInputs {
+    Plane T;             // full-resolution depth (GetPositionAt at the reprojected point)
+    Plane8 F;            // full-resolution face ids
+    Plane8 S;            // full-resolution sun shadow (R8, bilinear)
+    Plane TV;            // the depth on the reflection (GI) grid
+    Plane8 FV, BV;       // face and block ids on that grid
+    Plane SH, CC, AO;    // denoised diffuse GI on that grid (DiffuseDenoiseFBO 0, 1, 3)
+};
+
+// ReflectionTraceFrag.glsl main (:717-1084) for one texel of the reflection
+// grid, with u_RoughReflections on, u_ReprojectToScreenSpace on, LPV and cloud
+// reflections off, no player and flat materials (albedo, roughness,
+// metalness, emissive flag of the block; AO 1; the face normal as the
+// normal map); PCG random numbers; no jitter.
+void reflection_texel(const vpto_world* w, const vpto_camera* cam, const vpto_params* p, const vpto_frame* f,
+                      const float* view_proj, const ReflectionInputs& in, int i, int j, int Wg, int Hg, size_t q,
+                      float* spec4, float* hit, float* mask, RowCount* cnt) {
+    const v2 uv = texcoord(i, j, Wg, Hg);
+    v4 P = position_fetch(cam, in.TV, i, j, uv);
+    if (P.w < 0.0f) {
+        for (int c = 0; c < 4; c++) spec4[c] = 0.0f;
+        *hit = -1.0f;
+        *mask = 0.0f;
+        return;
+    }
+    const v3 viewer = mk3(cam->position[0], cam->position[1], cam->position[2]);
+    const v3 cam_pos = ray_origin(cam);
+    const v3 N = normal_from_id(in.FV.at(i, j), 1.0f);
+    const Material base = material(w, std::min(std::max(in.BV.at(i, j), 0), 127));
+    const v3 I = normalize(sub(mk3(P.x, P.y, P.z), viewer));
+    P.x += N.x * 0.035f;
+    P.y += N.y * 0.035f;
+    P.z += N.z * 0.035f;
+    const v3 pos = mk3(P.x, P.y, P.z);
+    float dsh[4], dcc[2];
+    for (int c = 0; c < 4; c++) dsh[c] = in.SH.at(i, j, c);
+    for (int c = 0; c < 2; c++) dcc[c] = in.CC.at(i, j, c);
+    const v3 base_indirect = sh_to_irradiance_a(dsh, dcc);
+    const Lighting L = frame_lighting(f);
+    const v3 sun_color = mk3(f->sun_radiance[0], f->sun_radiance[1], f->sun_radiance[2]);
+    const v3 moon_color = mk3(f->moon_radiance[0], f->moon_radiance[1], f->moon_radiance[2]);
+    const float sun_vis = 1.0f - L.sun_visibility;
+    const v3 mixed = vmix(sun_color, moon_color, sun_vis);   // SAMPLED_COLOR_MIXED (:727-730)
+    uint32_t rng = pcg_hash(pixel_seed(f, (uint32_t)q) ^ 0x5245464Cu);
+    const int spp = std::min(std::max(p->reflection_spp, 1), 16);
+    const float rbias = 0.85f;   // u_RoughnessBias (ReflectionRoughnessBias && DenoiseReflections)
+    float total[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    float avg_hit = 0.001f, meaningful = 0.0f, emask = 0.0f, computed_shadow = 0.0f;
+    int shadow_itr = 0, total_hits = 0;
+    for (int s = 0; s < spp; s++) {
+        const v3 rn = reflection_normal(N, clampf(base.rough * rbias, 0.01f, 1.0f), &rng);
+        const v3 R = reflect3(I, rn);
+        const TraceResult tr = traverse(w, pos, R, p->reflection_max_steps);
+        cnt->add(4, tr.steps);
+        const float T = tr.t;
+        const v3 hp = add(pos, muls(R, T));
+        v3 computed;
+        if (T > 0.0f) {
+            const v3 hn = tr.normal;
+            const int rid = std::min(std::max(tr.block, 0), 127);
+            // ReprojectReflectionToScreenSpace (:582-594)
+            const v4 pr = mat_mul4(view_proj, hp.x, hp.y, hp.z, 1.0f);
+            const v2 rc = v2{(pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f};
+            const v4 pa = position_linear(cam, in.T, rc);
+            const v3 na = normal_from_id(in.F.nearest(rc), 1.0f);
+            const v3 pd = mk3(std::fabs(pa.x - hp.x), std::fabs(pa.y - hp.y), std::fabs(pa.z - hp.z));
+            const float err = dot(pd, pd);
+            const float tb = 0.032593f;   // InThresholdedScreenSpace (:217-221)
+            const bool in_ss = rc.x > tb && rc.x < 1.0f - tb && rc.y > tb && rc.y < 1.0f - tb;
+            const bool success = err < 0.095f && na.x == hn.x && na.y == hn.y && na.z == hn.z && in_ss;
+            v3 ambient = base_indirect;
+            if (success) {
+                float rsh[4], rcc[2], rao[2];
+                in.SH.linear(rc, rsh);
+                in.CC.linear(rc, rcc);
+                in.AO.linear(rc, rao);
+                ambient = sh_to_irradiance_a(rsh, rcc);
+                const float vxao = dm_pow(rao[0], 0.75f);
+                if (pa.w > 0.0f && length(sub(mk3(pa.x, pa.y, pa.z), cam_pos)) < 40.0f) ambient = muls(ambient, vxao);
+            }
+            const Material m = material(w, rid);
+            const v3 radiance = muls(mixed, 0.6f);
+            const float ao = dm_pow(1.0f, 2.0f);
+            if (shadow_itr < std::max(spp / 4, 1)) {   // (:929-953)
+                if (success && in_ss) {
+                    computed_shadow = in.S.linearf(rc);
+                } else {
+                    const TraceResult sr = traverse(w, add(hp, muls(hn, 0.055f)), L.light_dir,
+                                                    p->reflection_shadow_max_steps);
+                    cnt->add(5, sr.steps);
+                    computed_shadow = sr.t > 0.0f ? 1.0f : 0.0f;
+                }
+                shadow_itr++;
+            }
+            ambient = mul(muls(muls(ambient, 1.0f), clampf(ao, 0.1f, 1.0f)), m.albedo);
+            v3 direct = add(ambient, reflection_directional_light(viewer, hp, L.light_dir, radiance, m.albedo, hn,
+                                                                  m.rough, m.metal, computed_shadow));
+            if (m.emissive) {   // (:988-1007), Emissivity = 1 for a flat emissive block
+                float emissivity = 1.0f;
+                const v2 fuv = face_uv(hp, hn);
+                const float bx = 0.02501f, by = 0.03001f;
+                emissivity *= (fuv.x > bx && fuv.x < 1.0f - bx && fuv.y > by && fuv.y < 1.0f - by) ? 1.0f : 0.0f;
+                direct = muls(m.albedo, fmaxg(emissivity * 19.0f * 1.0f, 2.0f));
+                emask = 1.0f;
+            }
+            computed = direct;
+            avg_hit += T;
+            meaningful += 1.0f;
+        } else {
+            computed = muls(sky_radiance(normalize(R)), mixf(1.0f, 1.175f, base.metal > 0.05f ? 1.0f : 0.0f));
+        }
+        total[0] += computed.x;
+        total[1] += computed.y;
+        total[2] += computed.z;
+        total[3] += 1.0f;
+        total_hits++;
+    }
+    avg_hit /= fmaxg(meaningful, 0.01f);
+    for (int c = 0; c < 4; c++) spec4[c] = clampf(total[c] / (float)total_hits, 0.0000001f, 100.0f);
+    *hit = clampf(meaningful > 0.01f ? avg_hit : -1.0f, -10.0f, 200.0f);
+    *mask = clampf(emask, 0.0f, 1.0f);
+}
+
+void vpto_trace_reflection(const vpto_world* w, const vpto_camera* cam, const vpto_params* p, const vpto_frame* f,
+                           const float* t, const uint8_t* face, const uint8_t* shadow, const float* t_view,
+                           const uint8_t* face_view, const uint8_t* block_view, const float* den_sh,
+                           const float* den_cocg, const float* den_aosky, int row0, int row1, float* spec,
+                           float* hit, float* mask) {
+    const int W = p->width, H = p->height, Wg = W / gi_div(p), Hg = H / gi_div(p);
+    const int fp16 = p->storage;
+    const ReflectionInputs in{Plane{t, W, H, 1},          Plane8{face, W, H},        Plane8{shadow, W, H},
+                              Plane{t_view, Wg, Hg, 1},   Plane8{face_view, Wg, Hg}, Plane8{block_view, Wg, Hg},
+                              Plane{den_sh, Wg, Hg, 4},   Plane{den_cocg, Wg, Hg, 2}, Plane{den_aosky, Wg, Hg, 2}};
+    // u_Projection * u_View, evaluated left to right
+    float m[16];
+    for (int c = 0; c < 4; c++)
+        for (int r = 0; r < 4; r++)
+            m[c * 4 + r] = ((cam->proj[0 * 4 + r] * cam->view[c * 4 + 0] + cam->proj[1 * 4 + r] * cam->view[c * 4 + 1]) +
+                            cam->proj[2 * 4 + r] * cam->view[c * 4 + 2]) +
+                           cam->proj[3 * 4 + r] * cam->view[c * 4 + 3];
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int j = row0; j < row1; j++) {
+        RowCount cnt;
+        for (int i = 0; i < Wg; i++) {
+            const size_t q = (size_t)j * Wg + i;
+            float s4[4], h, mk;
+            reflection_texel(w, cam, p, f, m, in, i, j, Wg, Hg, q, s4, &h, &mk, &cnt);
+            for (int c = 0; c < 4; c++) spec[q * 4 + c] = storage(s4[c], fp16);
+            hit[q] = storage(h, fp16);
+            mask[q] = storage(mk, fp16);
+        }
+        cnt.flush();
+    }
+}
+
+// The firefly rejection at the head of SpecularTemporalFilter.glsl main
+// (:316-340, FireflyReject :267-305, u_AggressiveFireflyRejection on: 3 of the
+// 4 neighbours), which runs whether or not the temporal filter is on: a texel
+// whose reflection hit an emissive block takes the mean of its non-emissive
+// 4-neighbours when at least three are. With TEMPORAL_SPEC off the result is
+// the temporal pass's output as it stands (:493-505).
+void vpto_spec_resolve(const vpto_params* p, const float* spec, const float* mask, float* out) {
+    const int Wg = p->width / gi_div(p), Hg = p->height / gi_div(p);
+    const Plane C{spec, Wg, Hg, 4}, M{mask, Wg, Hg, 1};
+    const int ox[4] = {1, 0, -1, 0}, oy[4] = {0, 1, 0, -1};
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < Hg; j++) {
+        for (int i = 0; i < Wg; i++) {
+            const size_t q = (size_t)j * Wg + i;
+            float col[4];
+            for (int c = 0; c < 4; c++) col[c] = spec[q * 4 + c];
+            if (mask[q] > 0.05f) {
+                float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                int unlit = 0;
+                for (int k = 0; k < 4; k++) {
+                    if (M.at(i + ox[k], j + oy[k], 0) < 0.01f) {
+                        for (int c = 0; c < 4; c++) acc[c] += C.at(i + ox[k], j + oy[k], c);
+                        unlit++;
+                    }
+                }
+                if (unlit >= 3)
+                    for (int c = 0; c < 4; c++) col[c] = acc[c] / (float)unlit;
+            }
+            for (int c = 0; c < 4; c++) out[q * 4 + c] = storage(col[c], p->storage);
         }
     }
 }

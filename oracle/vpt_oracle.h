@@ -66,7 +66,10 @@ typedef struct vpto_params {
     int32_t device;
     int32_t denoiser;           /* 0 = SVGF, 1 = temporal + 5x5 a-trous */
     int32_t gi_divisor;         /* GI grid = G-buffer / gi_divisor (0 or 1: same grid) */
-    int32_t reserved[1];
+    int32_t reflection_spp;     /* reflection samples per texel (0: no reflection pass) */
+    int32_t reflection_max_steps;
+    int32_t reflection_shadow_max_steps;
+    int32_t reserved[5];
 } vpto_params;
 
 typedef struct vpto_world {
@@ -108,8 +111,9 @@ typedef struct vpto_filtered {  /* VarianceFBO / DiffuseDenoiseFBO-like planes *
 } vpto_filtered;
 
 int vpto_omp_threads(void);
-/* Counters (8 x uint64: rays then DDA steps for primary, shadow, diffuse,
- * bounce shadow) that the trace functions add to; NULL disables counting. */
+/* Counters (12 x uint64: rays then DDA steps for primary, shadow, diffuse,
+ * bounce shadow, reflection, reflection shadow) that the trace functions add
+ * to; NULL disables counting. */
 void vpto_set_counters(uint64_t* counters);
 
 /* ManhattanDistance{X,Y,Z}.comp driven as in World::GenerateDistanceField. */
@@ -163,13 +167,25 @@ void vpto_atrous(const vpto_camera* cam, const vpto_params* p, const vpto_frame*
                  const float* temporal_util,
                  const vpto_filtered* in, const float* in_aosky, vpto_filtered* out);
 
+/* ReflectionTraceFrag.glsl main on the GI grid: t / face / shadow are the
+ * full-resolution G-buffer and sun shadow, the views the GI-grid reading of
+ * the G-buffer, den_* the denoised diffuse GI. Writes spec (4 ch), hit and
+ * mask on the GI grid, rows [row0, row1) of it. */
+void vpto_trace_reflection(const vpto_world* w, const vpto_camera* cam, const vpto_params* p, const vpto_frame* f,
+                           const float* t, const uint8_t* face, const uint8_t* shadow, const float* t_view,
+                           const uint8_t* face_view, const uint8_t* block_view, const float* den_sh,
+                           const float* den_cocg, const float* den_aosky, int row0, int row1, float* spec,
+                           float* hit, float* mask);
+/* Firefly rejection of SpecularTemporalFilter.glsl (TEMPORAL_SPEC off). */
+void vpto_spec_resolve(const vpto_params* p, const float* spec, const float* mask, float* out);
+
 /* ColorPassFrag.glsl main: joint-bilateral GI upscale, direct GGX +
  * indirect-diffuse combine, flat materials. t / face / block / shadow at the
  * G-buffer's resolution, sh / cocg / aosky on the GI grid. */
 void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
                 const vpto_frame* f, const float* t, const uint8_t* face, const uint8_t* block,
                 const uint8_t* shadow, const float* sh, const float* cocg, const float* aosky,
-                int row0, int row1, float* rgb);
+                const float* spec, int row0, int row1, float* rgb);
 
 /* The non-SVGF denoiser path (USE_SVGF off, Core/Pipeline.cpp:2618-2786):
  * TemporalFilter.glsl (diffuse mode), SampleVarianceCompute.glsl and one

@@ -24,7 +24,7 @@ def test_every_declared_symbol_is_exported(vpt):
 
 
 def test_abi_version_and_status_strings(vpt):
-    assert vpt.lib.vpt_abi_version() == 1
+    assert vpt.lib.vpt_abi_version() == 2
     for s in range(7):
         assert vpt.lib.vpt_status_string(s)
 
@@ -40,6 +40,9 @@ def test_defaults(vpt):
     cfg = vpt.default_config()
     assert (cfg.width, cfg.height, cfg.spp, cfg.bounces, cfg.atrous_iterations) == (1920, 1080, 1, 1, 5)
     assert cfg.diffuse_max_steps == 48 and cfg.bounce_shadow_max_steps == 128 and cfg.shadow_max_steps == 350
+    assert cfg.gi_divisor == 1 and cfg.reflection_spp == 0
+    assert (cfg.reflection_max_steps, cfg.reflection_shadow_max_steps) == (64, 150)
+    assert C.sizeof(vpt.Stats) == 12 * 8
     f = vpt.default_frame()
     assert abs(np.linalg.norm(list(f.sun_dir)) - 1) < 1e-6 and f.temporal == 1
 
@@ -52,6 +55,9 @@ def test_invalid_arguments_are_rejected(vpt):
     assert vpt.lib.vpt_create(C.byref(h), C.byref(bad)) == vpt.ERR_INVALID_ARG
     bad = vpt.default_config(storage=7)
     assert vpt.lib.vpt_create(C.byref(h), C.byref(bad)) == vpt.ERR_INVALID_ARG
+    for field, value in (("reflection_spp", 17), ("reflection_spp", -1), ("reflection_max_steps", -1)):
+        bad = vpt.default_config(**{field: value})
+        assert vpt.lib.vpt_create(C.byref(h), C.byref(bad)) == vpt.ERR_INVALID_ARG, field
     assert vpt.lib.vpt_create(None, None) == vpt.ERR_INVALID_ARG
     assert vpt.lib.vpt_destroy(None) == vpt.ERR_INVALID_ARG
     assert vpt.lib.vpt_upload_world(None, None, 1, 1, 1) == vpt.ERR_INVALID_ARG

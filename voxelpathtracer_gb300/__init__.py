@@ -41,11 +41,12 @@ PLANES = [
     "PREV_T", "PREV_FACE", "PREV_BLOCK",
     "VAR_SH", "VAR_COCG", "VAR_VARIANCE",
     "DEN_SH", "DEN_COCG", "DEN_VARIANCE", "DEN_AOSKY",
-    "COLOR",
+    "COLOR", "SPEC", "SPEC_HIT", "SPEC_MASK", "SPEC_OUT",
 ]
 PLANE = {name: i for i, name in enumerate(PLANES)}
 PASSES = ["primary", "shadow", "diffuse", "spatial_initial", "temporal", "variance", "atrous", "shade", "trace_frame",
-          "learned"]
+          "learned", "reflection"]
+RAY_KINDS = ["primary", "shadow", "diffuse", "bounce_shadow", "reflection", "reflection_shadow"]
 FACE_MISS = 10
 
 
@@ -56,7 +57,8 @@ class Config(C.Structure):
                 ("bounce_shadow_max_steps", C.c_int32), ("bounces", C.c_int32), ("spp", C.c_int32),
                 ("storage", C.c_int32), ("atrous_iterations", C.c_int32), ("resolution_scale", C.c_float),
                 ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
-                ("gi_divisor", C.c_int32), ("reserved", C.c_int32 * 1)]
+                ("gi_divisor", C.c_int32), ("reflection_spp", C.c_int32), ("reflection_max_steps", C.c_int32),
+                ("reflection_shadow_max_steps", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 class Camera(C.Structure):
@@ -77,7 +79,7 @@ class Frame(C.Structure):
 
 
 class Stats(C.Structure):
-    _fields_ = [("rays", C.c_uint64 * 4), ("steps", C.c_uint64 * 4)]
+    _fields_ = [("rays", C.c_uint64 * 6), ("steps", C.c_uint64 * 6)]
 
 
 class TraceBuffers(C.Structure):
@@ -151,6 +153,7 @@ def _load() -> C.CDLL:
         "vpt_trace_shadow": ([P, C.POINTER(Frame)], C.c_int),
         "vpt_trace_diffuse": ([P, C.POINTER(Frame)], C.c_int),
         "vpt_svgf": ([P, C.POINTER(Camera), C.POINTER(Frame)], C.c_int),
+        "vpt_trace_reflections": ([P, C.POINTER(Frame)], C.c_int),
         "vpt_shade": ([P, C.POINTER(Frame)], C.c_int),
         "vpt_trace_frame": ([P, C.POINTER(Camera), C.POINTER(Frame)], C.c_int),
         "vpt_trace_frame_noalloc": ([C.POINTER(TraceBuffers), C.POINTER(Config), C.POINTER(Camera),
@@ -429,6 +432,9 @@ class Context:
         self._ck(lib.vpt_svgf(self._h, C.byref(prev_cam) if prev_cam is not None else None, C.byref(frame)),
                  "vpt_svgf")
 
+    def trace_reflections(self, frame: Frame):
+        self._ck(lib.vpt_trace_reflections(self._h, C.byref(frame)), "vpt_trace_reflections")
+
     def shade(self, frame: Frame):
         self._ck(lib.vpt_shade(self._h, C.byref(frame)), "vpt_shade")
 
@@ -536,7 +542,7 @@ class Context:
     def read_stats(self) -> dict:
         s = Stats()
         self._ck(lib.vpt_read_stats(self._h, C.byref(s)), "vpt_read_stats")
-        kinds = ["primary", "shadow", "diffuse", "bounce_shadow"]
+        kinds = RAY_KINDS
         return {"rays": dict(zip(kinds, list(s.rays))), "steps": dict(zip(kinds, list(s.steps)))}
 
     def set_profiling(self, enabled: bool):
@@ -676,7 +682,7 @@ class Batch:
     def read_stats(self) -> dict:
         s = Stats()
         self._ck(lib.vpt_batch_read_stats(self._h, C.byref(s)), "vpt_batch_read_stats")
-        kinds = ["primary", "shadow", "diffuse", "bounce_shadow"]
+        kinds = RAY_KINDS
         return {"rays": dict(zip(kinds, list(s.rays))), "steps": dict(zip(kinds, list(s.steps)))}
 
     def launch_count(self) -> int:

@@ -48,6 +48,8 @@ PlaneMeta plane_meta(int plane) {
         case VPT_PLANE_GI_LUMA: case VPT_PLANE_PRE_LUMA: case VPT_PLANE_VAR_VARIANCE:
         case VPT_PLANE_DEN_VARIANCE: return {1, 1, 0, 1};
         case VPT_PLANE_COLOR: return {3, 1, 0, 0};
+        case VPT_PLANE_SPEC: case VPT_PLANE_SPEC_OUT: return {4, 1, 0, 1};
+        case VPT_PLANE_SPEC_HIT: case VPT_PLANE_SPEC_MASK: return {1, 1, 0, 1};
         default: return {0, 0, -1, 0};
     }
 }
@@ -92,6 +94,7 @@ struct vpt_ctx {
     void* var[FI_N] = {};
     void* den[2][FI_N] = {};
     void* color = nullptr;
+    void* refl[4] = {};   // reflection: radiance (4 ch), hit distance, emissive mask, resolved (4 ch)
     int cur = 0;        // index of this frame's G-buffer / temporal output
     int den_last = 0;   // den set holding the last a-trous output
     // cameras
@@ -211,6 +214,10 @@ void* plane_ptr(vpt_ctx* c, int plane) {
         case VPT_PLANE_DEN_VARIANCE: return c->den[c->den_last][FI_VAR];
         case VPT_PLANE_DEN_AOSKY: return c->den[c->den_last][FI_AOSKY];
         case VPT_PLANE_COLOR: return c->color;
+        case VPT_PLANE_SPEC: return c->refl[0];
+        case VPT_PLANE_SPEC_HIT: return c->refl[1];
+        case VPT_PLANE_SPEC_MASK: return c->refl[2];
+        case VPT_PLANE_SPEC_OUT: return c->refl[3];
         default: return nullptr;
     }
 }
@@ -263,6 +270,12 @@ vpt_status alloc_planes(vpt_ctx* c) {
     A(c->var[FI_VAR], n * es);
     c->var[FI_AOSKY] = nullptr;
     A(c->color, nf * 3 * es);
+    if (c->cfg.reflection_spp > 0) {
+        A(c->refl[0], n * 4 * es);
+        A(c->refl[1], n * es);
+        A(c->refl[2], n * es);
+        A(c->refl[3], n * 4 * es);
+    }
     A(c->counters, sizeof(Counters));
     A(c->queue, 256);
 #undef A
@@ -369,6 +382,9 @@ vpt_status vpt_default_config(vpt_config* cfg) {
     cfg->atrous_iterations = 5;
     cfg->resolution_scale = 1.0f;
     cfg->gi_divisor = 1;
+    cfg->reflection_spp = 0;
+    cfg->reflection_max_steps = 64;
+    cfg->reflection_shadow_max_steps = 150;
     cfg->color_phi_bias = 3.325f;
     cfg->device = 0;
     return VPT_OK;
@@ -411,6 +427,9 @@ vpt_status vpt_create(vpt_ctx** out, const vpt_config* cfg) {
         return VPT_ERR_INVALID_ARG;
     const int gd = cfg->gi_divisor <= 1 ? 1 : cfg->gi_divisor;
     if (cfg->gi_divisor < 0 || gd > 16 || cfg->width % gd != 0 || cfg->height % gd != 0) return VPT_ERR_INVALID_ARG;
+    if (cfg->reflection_spp < 0 || cfg->reflection_spp > 16 || cfg->reflection_max_steps < 0 ||
+        cfg->reflection_shadow_max_steps < 0)
+        return VPT_ERR_INVALID_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
         cudaGetLastError();
@@ -862,6 +881,61 @@ vpt_status svgf_run(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f, 
     return VPT_OK;
 }
 
+// The denoised diffuse GI (DiffuseDenoiseFBO): the last a-trous output, or
+// the variance / temporal output without a-trous iterations.
+void denoised_gi(vpt_ctx* c, const void** sh, const void** cocg, const void** ao) {
+    const bool plain = c->cfg.denoiser == VPT_DENOISER_ATROUS;
+    const bool den = c->cfg.atrous_iterations > 0;
+    *sh = den ? c->den[c->den_last][FI_SH] : (plain ? c->hist[c->cur][HI_SH] : c->var[FI_SH]);
+    *cocg = den ? c->den[c->den_last][FI_COCG] : (plain ? c->hist[c->cur][HI_COCG] : c->var[FI_COCG]);
+    *ao = den ? c->den[c->den_last][FI_AOSKY] : c->hist[c->cur][HI_AOSKY];
+}
+
+// The reflection pass of this frame (ReflectionTraceFrag.glsl, then the
+// firefly rejection of SpecularTemporalFilter.glsl); runs after the diffuse
+// denoiser, whose output it reads (Core/Pipeline.cpp:2998-3130).
+vpt_status reflection_run(vpt_ctx* c, const vpt_frame* f) {
+    vpt_status s = check_world(c);
+    if (s != VPT_OK) return s;
+    if ((s = check_frame(c, f)) != VPT_OK) return s;
+    if (c->cfg.reflection_spp <= 0) return fail(c, VPT_ERR_STATE, "reflections are off (reflection_spp = 0)");
+    cudaSetDevice(c->dev);
+    if ((s = refresh_view(c)) != VPT_OK) return s;
+    ReflectionArgs a;
+    a.spp = c->cfg.reflection_spp;
+    a.max_steps = c->cfg.reflection_max_steps;
+    a.shadow_max_steps = c->cfg.reflection_shadow_max_steps;
+    a.frame_index = f->frame_index;
+    a.seed = f->seed;
+    const vpt_camera& cm = c->cam;
+    for (int col = 0; col < 4; col++)
+        for (int r = 0; r < 4; r++)
+            a.view_proj[col * 4 + r] = ((cm.proj[0 * 4 + r] * cm.view[col * 4 + 0] + cm.proj[1 * 4 + r] * cm.view[col * 4 + 1]) +
+                                        cm.proj[2 * 4 + r] * cm.view[col * 4 + 2]) +
+                                       cm.proj[3 * 4 + r] * cm.view[col * 4 + 3];
+    const GILighting L = gi_lighting(f);
+    const v3 mixed = vmix(mk3(f->sun_radiance[0], f->sun_radiance[1], f->sun_radiance[2]),
+                          mk3(f->moon_radiance[0], f->moon_radiance[1], f->moon_radiance[2]), 1.0f - L.sun_visibility);
+    for (int k = 0; k < 3; k++) {
+        a.light_dir[k] = L.light_dir[k];
+        a.viewer[k] = cm.position[k];
+    }
+    a.mixed[0] = mixed.x;
+    a.mixed[1] = mixed.y;
+    a.mixed[2] = mixed.z;
+    const void *sh, *cocg, *ao;
+    denoised_gi(c, &sh, &cocg, &ao);
+    pass_begin(c, VPT_PASS_REFLECTION);
+    CK(c, trace_reflection(world_view(c), cam_view(cm), c->cfg.width, c->cfg.height, c->gw, c->gh, c->fp16, a,
+                           c->gbuf[c->cur][GB_T], (const uint8_t*)c->gbuf[c->cur][GB_FACE], c->shadow, c->view[0],
+                           (const uint8_t*)c->view[1], (const uint8_t*)c->view[2], sh, cocg, ao, c->refl[0], c->refl[1],
+                           c->refl[2], c->stats ? c->counters : nullptr, c->stream));
+    CK(c, spec_resolve(c->gw, c->gh, c->fp16, c->refl[0], c->refl[2], c->refl[3], c->stream));
+    pass_end(c, VPT_PASS_REFLECTION);
+    c->launches += 2;
+    return VPT_OK;
+}
+
 // The colour pass. source 0: the denoised GI (last a-trous output, or the
 // variance / temporal output without a-trous iterations); 1: the temporally
 // accumulated GI before any spatial filter; 2: the raw GI of this frame.
@@ -885,11 +959,11 @@ vpt_status shade_run(vpt_ctx* c, const vpt_frame* f, int source, void* out = nul
     const bool plain = c->cfg.denoiser == VPT_DENOISER_ATROUS;
     a.vxao = plain ? 0 : 1;
     a.gi_div = c->gd;
-    const void* sh = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_SH]
-                                                  : (plain ? c->hist[c->cur][HI_SH] : c->var[FI_SH]);
-    const void* cocg = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_COCG]
-                                                    : (plain ? c->hist[c->cur][HI_COCG] : c->var[FI_COCG]);
-    const void* ao = c->cfg.atrous_iterations > 0 ? c->den[c->den_last][FI_AOSKY] : c->hist[c->cur][HI_AOSKY];
+    const void *sh, *cocg, *ao;
+    denoised_gi(c, &sh, &cocg, &ao);
+    // the specular indirect of this frame's reflection pass (the learned
+    // path's inputs, sources 1 and 2, are shaded without it)
+    const void* spec = (c->cfg.reflection_spp > 0 && source == 0) ? c->refl[3] : nullptr;
     if (source == 1) {
         sh = c->hist[c->cur][HI_SH];
         cocg = c->hist[c->cur][HI_COCG];
@@ -902,7 +976,7 @@ vpt_status shade_run(vpt_ctx* c, const vpt_frame* f, int source, void* out = nul
     pass_begin(c, VPT_PASS_SHADE);
     CK(c, shade(world_view(c), cam_view(c->cam), c->cfg.width, c->cfg.height, c->fp16, a, c->gbuf[c->cur][GB_T],
                 (const uint8_t*)c->gbuf[c->cur][GB_FACE], (const uint8_t*)c->gbuf[c->cur][GB_BLOCK], c->shadow, sh, cocg,
-                ao, out ? out : c->color, c->stream));
+                ao, spec, out ? out : c->color, c->stream));
     pass_end(c, VPT_PASS_SHADE);
     c->launches += 1;
     return VPT_OK;
@@ -937,6 +1011,11 @@ extern "C" {
 vpt_status vpt_svgf(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f) {
     if (!c) return VPT_ERR_INVALID_ARG;
     return svgf_run(c, prev_cam, f, true);
+}
+
+vpt_status vpt_trace_reflections(vpt_ctx* c, const vpt_frame* f) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    return reflection_run(c, f);
 }
 
 vpt_status vpt_shade(vpt_ctx* c, const vpt_frame* f) {
@@ -991,6 +1070,7 @@ vpt_status vpt_render_frame_learned(vpt_ctx* c, vpt_unet* net, const vpt_camera*
         const vpt_camera prev = c->have_prev ? c->prev_cam : *cam;
         if ((s = trace_all(c, cam, f)) != VPT_OK) return s;
         if ((s = svgf_run(c, &prev, f, true)) != VPT_OK) return s;
+        if (c->cfg.reflection_spp > 0 && (s = reflection_run(c, f)) != VPT_OK) return s;
         if ((s = shade_run(c, f, 0)) != VPT_OK) return s;
     } else {
         if ((s = vpt_learned_input(c, cam, f)) != VPT_OK) return s;
@@ -1047,6 +1127,7 @@ vpt_status vpt_render_frame(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* 
     const vpt_camera prev = c->have_prev ? c->prev_cam : *cam;
     if ((s = trace_all(c, cam, f)) != VPT_OK) return s;
     if ((s = vpt_svgf(c, &prev, f)) != VPT_OK) return s;
+    if (c->cfg.reflection_spp > 0 && (s = reflection_run(c, f)) != VPT_OK) return s;
     if ((s = vpt_shade(c, f)) != VPT_OK) return s;
     if (rgb_out && (s = read_color(c, rgb_out)) != VPT_OK) return s;
     return vpt_end_frame(c);
@@ -1074,6 +1155,7 @@ vpt_status vpt_read_plane(vpt_ctx* c, int32_t plane, void* host, size_t bytes) {
     if (!c || !host || plane < 0 || plane >= VPT_PLANE_COUNT) return VPT_ERR_INVALID_ARG;
     size_t need = plane_bytes(c, plane, nullptr, nullptr);
     if (bytes < need) return fail(c, VPT_ERR_INVALID_ARG, "buffer too small: %zu < %zu", bytes, need);
+    if (!plane_ptr(c, plane)) return fail(c, VPT_ERR_STATE, "plane %d is not allocated (reflections off)", plane);
     cudaSetDevice(c->dev);
     CK(c, cudaMemcpyAsync(host, plane_ptr(c, plane), need, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
@@ -1084,6 +1166,7 @@ vpt_status vpt_write_plane(vpt_ctx* c, int32_t plane, const void* host, size_t b
     if (!c || !host || plane < 0 || plane >= VPT_PLANE_COUNT) return VPT_ERR_INVALID_ARG;
     size_t need = plane_bytes(c, plane, nullptr, nullptr);
     if (bytes != need) return fail(c, VPT_ERR_INVALID_ARG, "size mismatch: %zu != %zu", bytes, need);
+    if (!plane_ptr(c, plane)) return fail(c, VPT_ERR_STATE, "plane %d is not allocated (reflections off)", plane);
     cudaSetDevice(c->dev);
     CK(c, cudaMemcpyAsync(plane_ptr(c, plane), host, need, cudaMemcpyHostToDevice, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
@@ -1116,7 +1199,7 @@ vpt_status vpt_read_stats(vpt_ctx* c, vpt_stats* out) {
     CK(c, cudaMemcpyAsync(&h, c->counters, sizeof h, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaMemsetAsync(c->counters, 0, sizeof(Counters), c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < 6; k++) {
         out->rays[k] = h.rays[k];
         out->steps[k] = h.steps[k];
     }

@@ -626,7 +626,7 @@ vpt_status vpt_batch_read_stats(vpt_batch* b, vpt_stats* out) {
     BCK(b, cudaMemcpyAsync(&c, b->counters, sizeof c, cudaMemcpyDeviceToHost, b->stream));
     BCK(b, cudaMemsetAsync(b->counters, 0, sizeof(Counters), b->stream));
     BCK(b, cudaStreamSynchronize(b->stream));
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < 6; k++) {
         out->rays[k] = c.rays[k];
         out->steps[k] = c.steps[k];
     }

@@ -9,10 +9,13 @@ namespace vpt {
 
 // Device counters filled when statistics are on (layout of vpt_stats).
 struct Counters {
-    unsigned long long rays[4];
-    unsigned long long steps[4];
+    unsigned long long rays[6];
+    unsigned long long steps[6];
 };
-enum RayKind { kRayPrimary = 0, kRayShadow = 1, kRayDiffuse = 2, kRayBounceShadow = 3 };
+enum RayKind {
+    kRayPrimary = 0, kRayShadow = 1, kRayDiffuse = 2, kRayBounceShadow = 3, kRayReflection = 4,
+    kRayReflectionShadow = 5
+};
 
 // ---------------------------------------------------------------- df.cu --
 // Manhattan distance field, min(min(254, X+Y+Z), L1 distance to the nearest
@@ -237,6 +240,26 @@ struct PlainDenoiseIO {
 cudaError_t plain_denoise(const CamView& cam, int W, int H, int fp16, const TemporalArgs& ta,
                           const PlainDenoiseIO& io, cudaStream_t s);
 
+// ----------------------------------------------------------- reflect.cu --
+struct ReflectionArgs {
+    int spp;                    // ReflectionSPP, 1..16
+    int max_steps;              // u_ReflectionTraceLength
+    int shadow_max_steps;       // 150
+    uint32_t frame_index, seed;
+    float view_proj[16];        // u_Projection * u_View
+    float light_dir[3];         // u_StrongerLightDirection
+    float mixed[3];             // SAMPLED_COLOR_MIXED: sun / moon radiance by sun visibility
+    float viewer[3];            // u_ViewerPosition
+};
+// W x H: the G-buffer (t, face, shadow); Wg x Hg: the GI grid (views, denoised
+// GI, outputs spec 4 ch, hit, mask).
+cudaError_t trace_reflection(const WorldView& w, const CamView& cam, int W, int H, int Wg, int Hg, int fp16,
+                             const ReflectionArgs& a, const void* t, const uint8_t* face, const uint8_t* shadow,
+                             const void* tv, const uint8_t* fv, const uint8_t* bv, const void* den_sh,
+                             const void* den_cocg, const void* den_ao, void* spec, void* hit, void* mask,
+                             Counters* stats, cudaStream_t s);
+cudaError_t spec_resolve(int Wg, int Hg, int fp16, const void* spec, const void* mask, void* out, cudaStream_t s);
+
 // ------------------------------------------------------------- shade.cu --
 struct ShadeArgs {
     float sun[3], moon[3];
@@ -245,9 +268,11 @@ struct ShadeArgs {
     int vxao;                  // u_DoVXAO && u_SVGFEnabled: the GI AO darkens the indirect term
     int gi_div;                // the GI planes are (W / gi_div) x (H / gi_div)
 };
+// spec: the resolved reflection on the GI grid (4 ch), or NULL without a
+// reflection pass.
 cudaError_t shade(const WorldView& w, const CamView& cam, int W, int H, int fp16, const ShadeArgs& a,
                   const void* t, const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
-                  const void* sh, const void* cocg, const void* aosky, void* rgb, cudaStream_t s);
+                  const void* sh, const void* cocg, const void* aosky, const void* spec, void* rgb, cudaStream_t s);
 
 // ----------------------------------------------------------- learned.cu --
 // 16-channel BF16 features of the crop [x0, x0+w) x [y0, y0+h) into out

@@ -1,0 +1,303 @@
+// Reflections: ReflectionTraceFrag.glsl main (:717-1084) and the firefly
+// rejection at the head of SpecularTemporalFilter.glsl (:316-340), on the GI
+// grid, one thread per texel, each warp on an 8x4 patch so its rays stay
+// coherent. Substitutions as in the diffuse trace: flat materials (albedo,
+// roughness, metalness, emissive flag of the block; AO 1; the face normal as
+// the normal map), PCG random numbers instead of hash2 / blue noise, the
+// analytic sky, no LPV, cloud reflections or player, no jitter. The
+// temporal filter and the spatial reflection denoiser are off
+// (TEMPORAL_SPEC / DenoiseReflections false), so the resolved reflection is
+// what the colour pass reads.
+#include "pixel_passes.cuh"
+
+namespace vpt {
+
+namespace {
+
+__device__ __forceinline__ void tile_pixel(int* i, int* j) {
+    int tid = threadIdx.x;
+    int warp = tid >> 5, lane = tid & 31;
+    *i = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+    *j = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
+}
+
+// SHToIrradianceA (ReflectionTraceFrag.glsl:466-476)
+__device__ __forceinline__ v3 sh_to_irradiance_a(float4 sh, float2 cc) {
+    const float Y = fmaxf(0.0f, 3.544905f * sh.w);
+    const float k = (Y * 0.282095f) / (sh.w + 1e-6f);
+    const float co = cc.x * k, cg = cc.y * k;
+    const float T = Y - cg * 0.5f;
+    const float G = cg + T;
+    const float B = T - co * 0.5f;
+    const float R = B + co;
+    return mk3(fmaxf(R, 0.0f), fmaxf(G, 0.0f), fmaxf(B, 0.0f));
+}
+
+// ImportanceSampleGGX (ReflectionTraceFrag.glsl:345-365)
+__device__ __forceinline__ v3 importance_sample_ggx(v3 N, float roughness, float xi_x, float xi_y) {
+    const float alpha = roughness * roughness;
+    const float alpha2 = alpha * alpha;
+    const float phi = (2.0f * kPI) * xi_x;
+    const float cos_t = sqrtf((1.0f - xi_y) / (1.0f + (alpha2 - 1.0f) * xi_y));
+    const float sin_t = sqrtf(1.0f - cos_t * cos_t);
+    const v3 H = mk3(dcos(phi) * sin_t, dsin(phi) * sin_t, cos_t);
+    const v3 up = fabsf(N.z) < 0.999f ? mk3(0.0f, 0.0f, 1.0f) : mk3(1.0f, 0.0f, 0.0f);
+    const v3 tangent = normalize(cross(up, N));
+    const v3 bitangent = cross(N, tangent);
+    const v3 s = mk3((tangent.x * H.x + bitangent.x * H.y) + N.x * H.z, (tangent.y * H.x + bitangent.y * H.y) + N.y * H.z,
+                     (tangent.z * H.x + bitangent.z * H.y) + N.z * H.z);
+    return normalize(s);
+}
+
+// GetReflectionDirection (ReflectionTraceFrag.glsl:621-646)
+__device__ __forceinline__ v3 reflection_normal(v3 N, float R, uint32_t* rng) {
+    R = fmaxf(R, 0.05f);
+    float nearest = -100.0f;
+    v3 best = N;
+#pragma unroll 1
+    for (int i = 0; i < 3; i++) {
+        const float xi_x = rand01(rng) * 0.9f;
+        const float xi_y = rand01(rng) * 0.65f;
+        const v3 h = importance_sample_ggx(N, R, xi_x, xi_y);
+        const float d = dot(h, N);
+        if (d > nearest) {
+            best = h;
+            nearest = d;
+        }
+    }
+    return best;
+}
+
+__device__ __forceinline__ v3 reflect3(v3 I, v3 N) { return sub(I, muls(N, 2.0f * dot(N, I))); }
+
+// CalculateDirectionalLight of the reflection trace (:313-336): the specular
+// radiance is scaled by 0, only the diffuse lobe remains.
+__device__ __forceinline__ v3 reflection_directional_light(v3 viewer, v3 wp, v3 light_dir, v3 radiance, v3 albedo,
+                                                           v3 n, float rough, float metal, float shadow) {
+    const float Epsilon = 0.00001f;
+    const float sh = fminf(shadow, 1.0f);
+    const v3 Lo = normalize(sub(viewer, wp));
+    const float cos_lo = fmaxf(0.0f, dot(n, Lo));
+    const v3 F0 = vmix(mk3(0.04f, 0.04f, 0.04f), albedo, metal);
+    const v3 Li = light_dir;
+    const v3 Lh = normalize(add(Li, Lo));
+    const float cos_li = fmaxf(0.0f, dot(n, Li));
+    const float cos_lh = fmaxf(0.0f, dot(n, Lh));
+    const float fk = dpow(1.0f - fmaxf(0.0f, dot(Lh, Lo)), 5.0f);
+    const v3 F = add(F0, muls(sub(mk3(1.0f, 1.0f, 1.0f), F0), fk));
+    const float alpha = rough * rough;
+    const float alpha_sq = alpha * alpha;
+    const float denom = (cos_lh * cos_lh) * (alpha_sq - 1.0f) + 1.0f;
+    const float D = alpha_sq / ((kPI * denom) * denom);
+    const float r1 = rough + 1.0f;
+    const float k = (r1 * r1) / 8.0f;
+    const float G = (cos_li / (cos_li * (1.0f - k) + k)) * (cos_lo / (cos_lo * (1.0f - k) + k));
+    const v3 kd = vmix(sub(mk3(1.0f, 1.0f, 1.0f), F), mk3(0.0f, 0.0f, 0.0f), metal);
+    const v3 diffuse_brdf = mul(kd, albedo);
+    const v3 spec_brdf = divs(muls(muls(F, D), G), fmaxf(Epsilon, (4.0f * cos_li) * cos_lo));
+    const v3 radiance_s = muls(muls(radiance, 0.05f), 0.0f);
+    const v3 result = add(muls(mul(diffuse_brdf, radiance), cos_li), muls(mul(spec_brdf, radiance_s), cos_li));
+    return muls(vmax(result, 0.0f), clampf(1.0f - sh, 0.0f, 1.0f));
+}
+
+// The face UV of CalculateVectors (:1388-1446), UV.y = 1 - UV.y (:848).
+__device__ __forceinline__ v2 face_uv(v3 p, v3 n) {
+    v2 uv;
+    if (n.z != 0.0f) uv = mk2(fract(p.x), fract(p.y));
+    else if (n.y != 0.0f) uv = mk2(fract(p.x), fract(p.z));
+    else uv = mk2(fract(p.z), fract(p.y));
+    uv.y = 1.0f - uv.y;
+    return uv;
+}
+
+// texture() of the 0/1 sun-shadow plane as UNORM8 with GL_LINEAR + GL_REPEAT.
+__device__ __forceinline__ float bl_u8(const uint8_t* p, const Bilin& b) {
+    return blend(b, (float)__ldg(p + b.o00), (float)__ldg(p + b.o10), (float)__ldg(p + b.o01),
+                 (float)__ldg(p + b.o11));
+}
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_trace_reflection(WorldView w, CamView cam, int W, int H, int Wg, int Hg,
+                                                          ReflectionArgs a, const S* t, const uint8_t* face,
+                                                          const uint8_t* shadow, const S* tv, const uint8_t* fv,
+                                                          const uint8_t* bv, const S* den_sh, const S* den_cocg,
+                                                          const S* den_ao, S* o_spec, S* o_hit, S* o_mask,
+                                                          Counters* stats) {
+    int i, j;
+    tile_pixel(&i, &j);
+    unsigned nr = 0, ns = 0, nsr = 0, nss = 0;
+    if (i < Wg && j < Hg) {
+        const size_t q = (size_t)j * Wg + i;
+        const v2 uv = texcoord(i, j, Wg, Hg);
+        const Plane<S, 1> TV{tv, Wg, Hg};
+        v4 P = position_fetch(cam, TV, i, j, uv);
+        if (P.w < 0.0f) {
+            st4(o_spec + 4 * q, 0.0f, 0.0f, 0.0f, 0.0f);
+            st(o_hit + q, -1.0f);
+            st(o_mask + q, 0.0f);
+        } else {
+            const v3 viewer = mk3(a.viewer[0], a.viewer[1], a.viewer[2]);
+            const v3 cam_pos = ray_origin(cam);
+            const v3 N = normal_from_id(__ldg(fv + q), 1.0f);
+            const Material base = material(w, min(max((int)__ldg(bv + q), 0), 127));
+            const v3 I = normalize(sub(mk3(P.x, P.y, P.z), viewer));
+            P.x += N.x * 0.035f;
+            P.y += N.y * 0.035f;
+            P.z += N.z * 0.035f;
+            const v3 pos = mk3(P.x, P.y, P.z);
+            const v3 base_indirect = sh_to_irradiance_a(ld4(den_sh + 4 * q), ld2(den_cocg + 2 * q));
+            const v3 light_dir = mk3(a.light_dir[0], a.light_dir[1], a.light_dir[2]);
+            const v3 radiance = muls(mk3(a.mixed[0], a.mixed[1], a.mixed[2]), 0.6f);
+            const Plane<S, 1> T{t, W, H};
+            const Plane8 F{face, W, H};
+            uint32_t rng = pcg_hash(pcg_hash((uint32_t)q + pcg_hash(a.frame_index + pcg_hash(a.seed))) ^ 0x5245464Cu);
+            const int spp = min(max(a.spp, 1), 16);
+            const float rbias = 0.85f;
+            float total[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            float avg_hit = 0.001f, meaningful = 0.0f, emask = 0.0f, computed_shadow = 0.0f;
+            int shadow_itr = 0, total_hits = 0;
+#pragma unroll 1
+            for (int s = 0; s < spp; s++) {
+                const v3 rn = reflection_normal(N, clampf(base.rough * rbias, 0.01f, 1.0f), &rng);
+                const v3 R = reflect3(I, rn);
+                const TraceResult tr = traverse<0>(w, pos, R, a.max_steps);
+                nr += 1;
+                ns += (unsigned)tr.steps;
+                const float Tt = tr.t;
+                const v3 hp = add(pos, muls(R, Tt));
+                v3 computed;
+                if (Tt > 0.0f) {
+                    const v3 hn = tr.normal;
+                    const int rid = min(max(tr.block, 0), 127);
+                    const v4 pr = mat_mul4(a.view_proj, hp.x, hp.y, hp.z, 1.0f);
+                    const v2 rc = mk2((pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f);
+                    const v4 pa = position_linear(cam, T, rc);
+                    const v3 na = normal_from_id(F.nearest(rc), 1.0f);
+                    const v3 pd = mk3(fabsf(pa.x - hp.x), fabsf(pa.y - hp.y), fabsf(pa.z - hp.z));
+                    const float err = dot(pd, pd);
+                    const float tb = 0.032593f;
+                    const bool in_ss = rc.x > tb && rc.x < 1.0f - tb && rc.y > tb && rc.y < 1.0f - tb;
+                    const bool success = err < 0.095f && na.x == hn.x && na.y == hn.y && na.z == hn.z && in_ss;
+                    v3 ambient = base_indirect;
+                    if (success) {
+                        const Bilin fg = bilin(rc, Wg, Hg);
+                        ambient = sh_to_irradiance_a(bl4(den_sh, fg), bl2(den_cocg, fg));
+                        const float vxao = dpow(bl2(den_ao, fg).x, 0.75f);
+                        if (pa.w > 0.0f && length(sub(mk3(pa.x, pa.y, pa.z), cam_pos)) < 40.0f)
+                            ambient = muls(ambient, vxao);
+                    }
+                    const Material m = material(w, rid);
+                    const float ao = dpow(1.0f, 2.0f);
+                    if (shadow_itr < max(spp / 4, 1)) {
+                        if (success && in_ss) {
+                            computed_shadow = bl_u8(shadow, bilin(rc, W, H));
+                        } else {
+                            const TraceResult sr = traverse<0>(w, add(hp, muls(hn, 0.055f)), light_dir,
+                                                               a.shadow_max_steps);
+                            nsr += 1;
+                            nss += (unsigned)sr.steps;
+                            computed_shadow = sr.t > 0.0f ? 1.0f : 0.0f;
+                        }
+                        shadow_itr++;
+                    }
+                    ambient = mul(muls(muls(ambient, 1.0f), clampf(ao, 0.1f, 1.0f)), m.albedo);
+                    v3 direct = add(ambient, reflection_directional_light(viewer, hp, light_dir, radiance, m.albedo,
+                                                                          hn, m.rough, m.metal, computed_shadow));
+                    if (m.emissive) {
+                        float emissivity = 1.0f;
+                        const v2 fuv = face_uv(hp, hn);
+                        const float bx = 0.02501f, by = 0.03001f;
+                        emissivity *= (fuv.x > bx && fuv.x < 1.0f - bx && fuv.y > by && fuv.y < 1.0f - by) ? 1.0f
+                                                                                                          : 0.0f;
+                        direct = muls(m.albedo, fmaxf(emissivity * 19.0f * 1.0f, 2.0f));
+                        emask = 1.0f;
+                    }
+                    computed = direct;
+                    avg_hit += Tt;
+                    meaningful += 1.0f;
+                } else {
+                    computed = muls(sky_radiance(normalize(R)), mixf(1.0f, 1.175f, base.metal > 0.05f ? 1.0f : 0.0f));
+                }
+                total[0] += computed.x;
+                total[1] += computed.y;
+                total[2] += computed.z;
+                total[3] += 1.0f;
+                total_hits++;
+            }
+            avg_hit /= fmaxf(meaningful, 0.01f);
+            const float nh = (float)total_hits;
+            st4(o_spec + 4 * q, clampf(total[0] / nh, 0.0000001f, 100.0f), clampf(total[1] / nh, 0.0000001f, 100.0f),
+                clampf(total[2] / nh, 0.0000001f, 100.0f), clampf(total[3] / nh, 0.0000001f, 100.0f));
+            st(o_hit + q, clampf(meaningful > 0.01f ? avg_hit : -1.0f, -10.0f, 200.0f));
+            st(o_mask + q, clampf(emask, 0.0f, 1.0f));
+        }
+    }
+    if (stats) {
+        count_rays(stats, kRayReflection, nr, ns);
+        count_rays(stats, kRayReflectionShadow, nsr, nss);
+    }
+}
+
+// FireflyReject (SpecularTemporalFilter.glsl:267-305) with
+// u_AggressiveFireflyRejection on (3 of 4 non-emissive neighbours), applied
+// where the texel's mask is above 0.05 (:330-337).
+template <typename S>
+__global__ void __launch_bounds__(256) k_spec_resolve(int Wg, int Hg, const S* spec, const S* mask, S* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= Wg || j >= Hg) return;
+    const size_t q = (size_t)j * Wg + i;
+    float4 col = ld4(spec + 4 * q);
+    if (ld(mask + q) > 0.05f) {
+        const int ox[4] = {1, 0, -1, 0}, oy[4] = {0, 1, 0, -1};
+        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        int unlit = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const size_t n = (size_t)wrapi(j + oy[k], Hg) * Wg + wrapi(i + ox[k], Wg);
+            if (ld(mask + n) < 0.01f) {
+                const float4 c = ld4(spec + 4 * n);
+                acc.x += c.x;
+                acc.y += c.y;
+                acc.z += c.z;
+                acc.w += c.w;
+                unlit++;
+            }
+        }
+        if (unlit >= 3) {
+            const float u = (float)unlit;
+            col = make_float4(acc.x / u, acc.y / u, acc.z / u, acc.w / u);
+        }
+    }
+    st4(out + 4 * q, col.x, col.y, col.z, col.w);
+}
+
+}  // namespace
+
+cudaError_t trace_reflection(const WorldView& w, const CamView& cam, int W, int H, int Wg, int Hg, int fp16,
+                             const ReflectionArgs& a, const void* t, const uint8_t* face, const uint8_t* shadow,
+                             const void* tv, const uint8_t* fv, const uint8_t* bv, const void* den_sh,
+                             const void* den_cocg, const void* den_ao, void* spec, void* hit, void* mask,
+                             Counters* stats, cudaStream_t s) {
+    const dim3 grid((unsigned)((Wg + 15) / 16), (unsigned)((Hg + 15) / 16));
+    if (fp16)
+        k_trace_reflection<__half><<<grid, 256, 0, s>>>(
+            w, cam, W, H, Wg, Hg, a, (const __half*)t, face, shadow, (const __half*)tv, fv, bv, (const __half*)den_sh,
+            (const __half*)den_cocg, (const __half*)den_ao, (__half*)spec, (__half*)hit, (__half*)mask, stats);
+    else
+        k_trace_reflection<float><<<grid, 256, 0, s>>>(
+            w, cam, W, H, Wg, Hg, a, (const float*)t, face, shadow, (const float*)tv, fv, bv, (const float*)den_sh,
+            (const float*)den_cocg, (const float*)den_ao, (float*)spec, (float*)hit, (float*)mask, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t spec_resolve(int Wg, int Hg, int fp16, const void* spec, const void* mask, void* out, cudaStream_t s) {
+    const dim3 grid((unsigned)((Wg + 31) / 32), (unsigned)((Hg + 7) / 8)), blk(32, 8);
+    if (fp16)
+        k_spec_resolve<__half><<<grid, blk, 0, s>>>(Wg, Hg, (const __half*)spec, (const __half*)mask, (__half*)out);
+    else
+        k_spec_resolve<float><<<grid, blk, 0, s>>>(Wg, Hg, (const float*)spec, (const float*)mask, (float*)out);
+    return cudaGetLastError();
+}
+
+}  // namespace vpt

@@ -64,7 +64,7 @@ __device__ __forceinline__ v2 karis_env_brdf(float ndv, float rough) {
 }
 
 struct UpscaledGI {
-    float sh[4], cocg[2], ao, shadow;
+    float sh[4], cocg[2], ao, shadow, spec[4];
 };
 
 // SpatiallyUpscaleBuffers (ColorPassFrag.glsl:535-653), which the colour pass
@@ -76,16 +76,21 @@ struct UpscaledGI {
 // u_DiffuseSHy, :565): on a GI grid d times coarser (kScaled) they land on
 // G-buffer texel centres d texels apart (fetched, REPEAT wrapped: the shader
 // has no screen-space test here) and between GI texels (bilinear); with d = 1
-// every tap is a texel centre of both. All loads of a tap are issued before
-// its weights are formed; taps in x-outer, y-inner order keep the sums'
-// rounding identical to the shader's loop.
-template <typename S, bool kScaled>
-__device__ __forceinline__ UpscaledGI upscale_gi(int W, int H, int d, int i, int j, v2 uv, const S* t,
-                                                 const uint8_t* face, const uint8_t* shadow, const S* sh_p,
-                                                 const S* cocg_p, const S* ao_p, v3 base_n, float base_d) {
+// every tap is a texel centre of both. With a reflection pass (kSpec) the
+// specular indirect is gathered too, weighted by the GI weight /
+// (12 |roughness - base roughness| + 1) * max(n.n', 0)^8 (:595-603; the
+// G-buffer roughness and normal are the block's and the face's). All loads of
+// a tap are issued before its weights are formed; taps in x-outer, y-inner
+// order keep the sums' rounding identical to the shader's loop.
+template <typename S, bool kScaled, bool kSpec>
+__device__ __forceinline__ UpscaledGI upscale_gi(const WorldView& w, int W, int H, int d, int i, int j, v2 uv,
+                                                 const S* t, const uint8_t* face, const uint8_t* block,
+                                                 const uint8_t* shadow, const S* sh_p, const S* cocg_p,
+                                                 const S* ao_p, const S* spec_p, v3 base_n, float base_d,
+                                                 float base_rough) {
     UpscaledGI u;
-    float4 tsh = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    float tcc0 = 0.0f, tcc1 = 0.0f, tao = 0.0f, tw = 0.0f, tsw = 0.0f;
+    float4 tsh = make_float4(0.0f, 0.0f, 0.0f, 0.0f), tsp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float tcc0 = 0.0f, tcc1 = 0.0f, tao = 0.0f, tw = 0.0f, tsw = 0.0f, tspw = 0.0f;
     const bool filter_shadows = base_d > 128.0f;
     float tshadow = filter_shadows ? 0.0f : (float)__ldg(shadow + (size_t)j * W + i);
     const int Wg = W / d, Hg = H / d;
@@ -100,7 +105,7 @@ __device__ __forceinline__ UpscaledGI upscale_gi(int W, int H, int d, int i, int
             const size_t q = (size_t)sj * W + si;
             const float tt = ld(t + q);
             const int fid = __ldg(face + q);
-            float4 s4;
+            float4 s4, sp4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             float2 c2;
             float a0;
             if (kScaled) {
@@ -108,11 +113,14 @@ __device__ __forceinline__ UpscaledGI upscale_gi(int W, int H, int d, int i, int
                 s4 = bl4(sh_p, fg);
                 c2 = bl2(cocg_p, fg);
                 a0 = bl2(ao_p, fg).x;
+                if (kSpec) sp4 = bl4(spec_p, fg);
             } else {
                 s4 = ld4(sh_p + q * 4);
                 c2 = ld2(cocg_p + q * 2);
                 a0 = ld(ao_p + q * 2);
+                if (kSpec) sp4 = ld4(spec_p + q * 4);
             }
+            const int tap_block = kSpec ? (int)__ldg(block + q) : 0;
             const bool cross = x == 0 || y == 0;
             const float sv = (filter_shadows && cross) ? (float)__ldg(shadow + q) : 0.0f;
             const float lda = 1.0f / (1.0f / tt);
@@ -123,6 +131,16 @@ __device__ __forceinline__ UpscaledGI upscale_gi(int W, int H, int d, int i, int
             nw = fmaxf(nw, 0.0001f);
             const float kwt = (x == 0 ? 1.0f : 2.0f / 3.0f) * (y == 0 ? 1.0f : 2.0f / 3.0f);   // AtrousWeights
             float wgt = clampf((nw * dw) * kwt, 0.0f, 1.0f);
+            if (kSpec) {
+                const float ra = material(w, min(max(tap_block, 0), 127)).rough;
+                float spw = (wgt / ((fabsf(ra - base_rough) * 12.0f) + 1.0f)) * dpow(fmaxf(dot(na, base_n), 0.0f), 8.0f);
+                spw = fmaxf(spw, 0.00000001f);
+                tsp.x += sp4.x * spw;
+                tsp.y += sp4.y * spw;
+                tsp.z += sp4.z * spw;
+                tsp.w += sp4.w * spw;
+                tspw += spw;
+            }
             wgt = fmaxf(wgt, 0.00000001f);
             tsh.x += s4.x * wgt;
             tsh.y += s4.y * wgt;
@@ -147,16 +165,22 @@ __device__ __forceinline__ UpscaledGI upscale_gi(int W, int H, int d, int i, int
     u.cocg[0] = tcc0 / tw;
     u.cocg[1] = tcc1 / tw;
     u.ao = tao / tw;
+    tspw = fmaxf(tspw, 0.0000001f);
+    u.spec[0] = tsp.x / tspw;
+    u.spec[1] = tsp.y / tspw;
+    u.spec[2] = tsp.z / tspw;
+    u.spec[3] = tsp.w / tspw;
     if (filter_shadows) tshadow = tshadow / tsw;
     tshadow += 0.05f;
     u.shadow = clampf(tshadow, 0.00000000000001f, 1.0f);
     return u;
 }
 
-template <typename S, bool kScaled>
+template <typename S, bool kScaled, bool kSpec>
 __global__ void __launch_bounds__(256) k_shade(WorldView w, CamView cam, int W, int H, ShadeArgs a, const S* t,
                                                const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
-                                               const S* sh_p, const S* cocg_p, const S* ao_p, S* rgb) {
+                                               const S* sh_p, const S* cocg_p, const S* ao_p, const S* spec_p,
+                                               S* rgb) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= W || j >= H) return;
@@ -175,8 +199,8 @@ __global__ void __launch_bounds__(256) k_shade(WorldView w, CamView cam, int W, 
         v3 albedo = basic_saturation(m.albedo, 1.0f - 0.1f);
         if (m.metal >= 0.1f - 0.01f) albedo = basic_saturation(albedo, 0.9f);
         float emissivity = (float)m.emissive;
-        const UpscaledGI up =
-            upscale_gi<S, kScaled>(W, H, a.gi_div, i, j, uv, t, face, shadow, sh_p, cocg_p, ao_p, n, dist);
+        const UpscaledGI up = upscale_gi<S, kScaled, kSpec>(w, W, H, a.gi_div, i, j, uv, t, face, block, shadow,
+                                                            sh_p, cocg_p, ao_p, spec_p, n, dist, m.rough);
         float up_shadow = clampf(up.shadow, 0.0f, 1.0f);
         float rt_shadow = clampf(clampf(up_shadow + 0.0f, 0.0f, 1.0f), 0.0f, 1.0f);
         v3 indirect = sh_to_irradiance(up.sh, up.cocg, n);
@@ -204,7 +228,15 @@ __global__ void __launch_bounds__(256) k_shade(WorldView w, CamView cam, int W, 
         v3 I = normalize(sub(wp, viewer));
         float idn = dot(n, I);
         v3 R = sub(I, muls(n, 2.0f * idn));
-        v3 spec_ind = vmax(mk3(0.0f, 0.0f, 0.0f), 0.0001f);
+        // SpecularIndirect (:901-909): the upscaled reflection times
+        // clamp(max(n.n, 1e-8)^2 * 1.5, 0.1, 1) inside the 0.0035 border
+        v3 spec_ind = mk3(0.0f, 0.0f, 0.0f);
+        const float sb = 0.0035f;
+        if (kSpec && uv.x > sb && uv.x < 1.0f - sb && uv.y > sb && uv.y < 1.0f - sb) {
+            const float att = clampf(dpow(fmaxf(dot(n, n), 0.00000001f), 2.0f) * 1.5f, 0.1f, 1.0f);
+            spec_ind = muls(mk3(up.spec[0], up.spec[1], up.spec[2]), att);
+        }
+        spec_ind = vmax(spec_ind, 0.0001f);
         v3 Lo = normalize(sub(viewer, wp));
         v3 F0 = vmix(mk3(0.04f, 0.04f, 0.04f), albedo, m.metal);
         diffuse_indirect = muls(diffuse_indirect, clampf(sampled_ao, 0.2f, 1.01f));
@@ -239,18 +271,20 @@ __global__ void __launch_bounds__(256) k_shade(WorldView w, CamView cam, int W, 
 
 cudaError_t shade(const WorldView& w, const CamView& cam, int W, int H, int fp16, const ShadeArgs& a,
                   const void* t, const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
-                  const void* sh, const void* cocg, const void* aosky, void* rgb, cudaStream_t s) {
+                  const void* sh, const void* cocg, const void* aosky, const void* spec, void* rgb, cudaStream_t s) {
     dim3 grid((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8));
     dim3 blk(32, 8);
-    const bool scaled = a.gi_div > 1;
+    const bool scaled = a.gi_div > 1, sp = spec != nullptr;
     if (fp16) {
-        auto k = scaled ? k_shade<__half, true> : k_shade<__half, false>;
+        auto k = scaled ? (sp ? k_shade<__half, true, true> : k_shade<__half, true, false>)
+                        : (sp ? k_shade<__half, false, true> : k_shade<__half, false, false>);
         k<<<grid, blk, 0, s>>>(w, cam, W, H, a, (const __half*)t, face, block, shadow, (const __half*)sh,
-                               (const __half*)cocg, (const __half*)aosky, (__half*)rgb);
+                               (const __half*)cocg, (const __half*)aosky, (const __half*)spec, (__half*)rgb);
     } else {
-        auto k = scaled ? k_shade<float, true> : k_shade<float, false>;
+        auto k = scaled ? (sp ? k_shade<float, true, true> : k_shade<float, true, false>)
+                        : (sp ? k_shade<float, false, true> : k_shade<float, false, false>);
         k<<<grid, blk, 0, s>>>(w, cam, W, H, a, (const float*)t, face, block, shadow, (const float*)sh,
-                               (const float*)cocg, (const float*)aosky, (float*)rgb);
+                               (const float*)cocg, (const float*)aosky, (const float*)spec, (float*)rgb);
     }
     return cudaGetLastError();
 }
