@@ -70,7 +70,9 @@ typedef struct vpt_config {
                                         = DiffuseTraceResolution by default, :101) */
     int32_t reflection_max_steps;    /* u_ReflectionTraceLength = 64 (:100) */
     int32_t reflection_shadow_max_steps; /* 150 (ReflectionTraceFrag.glsl:1098) */
-    int32_t reserved[5];
+    int32_t reflection_temporal;     /* TEMPORAL_SPEC (Core/Pipeline.cpp:124): 1 (default) runs
+                                        SpecularTemporalFilter's reprojection and accumulation */
+    int32_t reserved[4];
 } vpt_config;
 
 typedef enum vpt_denoiser {
@@ -151,7 +153,9 @@ typedef enum vpt_plane {
     VPT_PLANE_SPEC_HIT = 34,  /* its mean hit distance, -1 when every sample missed */
     VPT_PLANE_SPEC_MASK = 35, /* 1 where a sample hit an emissive block */
     VPT_PLANE_SPEC_OUT = 36,  /* ReflectionTemporalFBO: the specular indirect the colour pass reads */
-    VPT_PLANE_COUNT = 37
+    VPT_PLANE_SPEC_ACC = 37,  /* its accumulation factor (-1 with the temporal filter off) */
+    VPT_PLANE_SPEC_STABLE_HIT = 38, /* its temporally stabilised hit distance */
+    VPT_PLANE_COUNT = 39
 } vpt_plane;
 
 typedef enum vpt_dtype { VPT_DTYPE_F32 = 0, VPT_DTYPE_F16 = 1, VPT_DTYPE_U8 = 2, VPT_DTYPE_U16 = 3, VPT_DTYPE_I32 = 4 } vpt_dtype;
@@ -226,11 +230,13 @@ vpt_status vpt_trace_diffuse(vpt_ctx* ctx, const vpt_frame* frame);
  * and the a-trous iterations. `prev_cam` is the previous frame's camera
  * (u_PrevView / u_PrevProjection); history planes are read and written. */
 vpt_status vpt_svgf(vpt_ctx* ctx, const vpt_camera* prev_cam, const vpt_frame* frame);
-/* Reflection pass, Core/Pipeline.cpp:2998-3260 (ReflectionTraceFrag.glsl,
- * then the firefly rejection of SpecularTemporalFilter.glsl with TEMPORAL_SPEC
- * and DenoiseReflections off), on the GI grid, after vpt_svgf (it reads the
- * denoised GI): fills SPEC, SPEC_HIT, SPEC_MASK and SPEC_OUT. Needs
- * reflection_spp > 0; vpt_render_frame runs it when that is set. */
+/* Reflection pass, Core/Pipeline.cpp:2998-3262: ReflectionTraceFrag.glsl,
+ * the two bilateral passes over its hit distance and SpecularTemporalFilter
+ * (firefly rejection; reprojection and accumulation when reflection_temporal),
+ * on the GI grid, after vpt_svgf (it reads the denoised GI): fills SPEC,
+ * SPEC_HIT, SPEC_MASK, SPEC_OUT, SPEC_ACC and SPEC_STABLE_HIT. Needs
+ * reflection_spp > 0; vpt_render_frame runs it when that is set. The
+ * reflection planes are swapped with last frame's by vpt_end_frame. */
 vpt_status vpt_trace_reflections(vpt_ctx* ctx, const vpt_frame* frame);
 /* Colour pass, Core/Pipeline.cpp:3603-3821 (ColorPassFrag.glsl): fills COLOR;
  * with reflection_spp > 0 it adds the specular indirect from SPEC_OUT. */

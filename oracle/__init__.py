@@ -42,7 +42,8 @@ class OParams(C.Structure):
                 ("storage", C.c_int32), ("atrous_iterations", C.c_int32), ("resolution_scale", C.c_float),
                 ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
                 ("gi_divisor", C.c_int32), ("reflection_spp", C.c_int32), ("reflection_max_steps", C.c_int32),
-                ("reflection_shadow_max_steps", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("reflection_shadow_max_steps", C.c_int32), ("reflection_temporal", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class OWorld(C.Structure):
@@ -85,7 +86,8 @@ def lib() -> C.CDLL:
         L.vpto_gi_view.argtypes = [P, P, P, P, P, P, P]
         L.vpto_shade.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, C.c_int, C.c_int, P]
         L.vpto_trace_reflection.argtypes = [P] * 13 + [C.c_int, C.c_int, P, P, P]
-        L.vpto_spec_resolve.argtypes = [P, P, P, P]
+        L.vpto_spec_hit_blur.argtypes = [P, C.c_int, P, P, P, P]
+        L.vpto_spec_temporal.argtypes = [P] * 18
         for name in ("vpto_exp", "vpto_exp2", "vpto_log2", "vpto_sin", "vpto_cos", "vpto_half_round"):
             getattr(L, name).argtypes = [C.c_float]
             getattr(L, name).restype = C.c_float
@@ -329,13 +331,39 @@ def trace_reflection(world: World, cam, config, frame, g: dict, shadow, den: dic
     return out
 
 
-def spec_resolve(config, spec, mask) -> np.ndarray:
-    """The firefly rejection of the reflection (what the colour pass reads)."""
+def spec_hit_blur(config, g: dict, hit) -> np.ndarray:
+    """The two bilateral passes over the reflection hit distance."""
     p = params(config)
-    spec = np.ascontiguousarray(spec, dtype=np.float32)
-    mask = np.ascontiguousarray(mask, dtype=np.float32)
-    out = np.zeros_like(spec)
-    lib().vpto_spec_resolve(C.byref(p), _p(spec), _p(mask), _p(out))
+    v = gi_view(p, g["t"], g["face"], g["block"])
+    h0 = np.ascontiguousarray(hit, dtype=np.float32)
+    h1, h2 = np.zeros_like(h0), np.zeros_like(h0)
+    lib().vpto_spec_hit_blur(C.byref(p), 1, _p(v["t"]), _p(v["face"]), _p(h0), _p(h1))
+    lib().vpto_spec_hit_blur(C.byref(p), 2, _p(v["t"]), _p(v["face"]), _p(h1), _p(h2))
+    return h2
+
+
+def empty_reflection_history(config) -> dict:
+    """The reflection state libvpt starts from: zero planes on the GI grid."""
+    H, W = gi_dims(config)
+    return {"out": np.zeros((H, W, 4), np.float32), "hit": np.zeros((H, W), np.float32),
+            "stable": np.zeros((H, W), np.float32)}
+
+
+def spec_temporal(world: World, cam, prev_cam, config, g: dict, prev_g: dict, refl: dict, prev_refl: dict) -> dict:
+    """SpecularTemporalFilter: refl holds this frame's spec, (blurred) hit and
+    mask, prev_refl last frame's out, hit and stable; returns out, acc, stable."""
+    p = params(config)
+    H, W = gi_dims(p)
+    v = gi_view(p, g["t"], g["face"], g["block"])
+    out = {"out": np.zeros((H, W, 4), np.float32), "acc": np.zeros((H, W), np.float32),
+           "stable": np.zeros((H, W), np.float32)}
+    arrs = [np.ascontiguousarray(a, dtype=dt) for a, dt in
+            ((v["t"], np.float32), (v["face"], np.uint8), (v["block"], np.uint8), (prev_g["t"], np.float32),
+             (prev_g["face"], np.uint8), (refl["spec"], np.float32), (refl["hit"], np.float32),
+             (refl["mask"], np.float32), (prev_refl["out"], np.float32), (prev_refl["hit"], np.float32),
+             (prev_refl["stable"], np.float32))]
+    lib().vpto_spec_temporal(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(_as(OCamera, prev_cam)),
+                             C.byref(p), *[_p(a) for a in arrs], _p(out["out"]), _p(out["acc"]), _p(out["stable"]))
     return out
 
 
@@ -402,8 +430,9 @@ def svgf(cam, prev_cam, config, frame, g: dict, prev_g: dict, gi: dict, hist: di
     return {"pre": pre, "temporal": tmp, "variance": var, "atrous": dens}
 
 
-def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist: dict) -> dict:
-    """One whole frame in the order of vpt_render_frame."""
+def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist: dict, prev_refl=None) -> dict:
+    """One whole frame in the order of vpt_render_frame; prev_refl is last
+    frame's "refl" (zero planes when None)."""
     p = params(config)
     g = trace_primary(world, cam, p)
     shadow = trace_shadow(world, cam, p, frame, g["t"], g["face"])
@@ -423,7 +452,10 @@ def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist:
     refl = None
     if p.reflection_spp > 0:
         refl = trace_reflection(world, cam, p, frame, g, shadow, {"sh": sh, "cocg": cocg, "aosky": ao})
-        refl["out"] = spec_resolve(p, refl["spec"], refl["mask"])
+        refl["raw_hit"] = refl["hit"]
+        refl["hit"] = spec_hit_blur(p, g, refl["raw_hit"])
+        prev_refl = prev_refl if prev_refl is not None else empty_reflection_history(p)
+        refl.update(spec_temporal(world, cam, prev_cam, p, g, prev_g, refl, prev_refl))
     rgb = shade(world, cam, p, frame, g["t"], g["face"], g["block"], shadow, sh, cocg, ao,
                 spec=None if refl is None else refl["out"])
     return {"g": g, "shadow": shadow, "gi": gi, "svgf": sv, "refl": refl, "rgb": rgb}

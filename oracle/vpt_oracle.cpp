@@ -1559,35 +1559,228 @@ void vpto_trace_reflection(const vpto_world* w, const vpto_camera* cam, const vp
     }
 }
 
-// The firefly rejection at the head of SpecularTemporalFilter.glsl main
-// (:316-340, FireflyReject :267-305, u_AggressiveFireflyRejection on: 3 of the
-// 4 neighbours), which runs whether or not the temporal filter is on: a texel
-// whose reflection hit an emissive block takes the mean of its non-emissive
-// 4-neighbours when at least three are. With TEMPORAL_SPEC off the result is
-// the temporal pass's output as it stands (:493-505).
-void vpto_spec_resolve(const vpto_params* p, const float* spec, const float* mask, float* out) {
+// BlurHitDistance_Bilateral.glsl (pass 1: 3x3) and
+// BlurHitDistancePass2_Bilateral.glsl (pass 2: 3 x 5 taps, y in -2..2), both
+// two GI texels apart (Scale 2), run on the reflection hit distance before the
+// temporal filter (DENOISE_REFLECTION_HIT_DATA, Core/Pipeline.cpp:126,
+// :3141-3215). Taps with a depth difference above 1, a miss, or another face
+// are skipped; REPEAT wrap. The depth and face are the GI-grid views.
+void vpto_spec_hit_blur(const vpto_params* p, int pass, const float* t_view, const uint8_t* face_view,
+                        const float* hit_in, float* hit_out) {
     const int Wg = p->width / gi_div(p), Hg = p->height / gi_div(p);
-    const Plane C{spec, Wg, Hg, 4}, M{mask, Wg, Hg, 1};
-    const int ox[4] = {1, 0, -1, 0}, oy[4] = {0, 1, 0, -1};
+    const Plane TV{t_view, Wg, Hg, 1}, HI{hit_in, Wg, Hg, 1};
+    const Plane8 FV{face_view, Wg, Hg};
+    static const float kw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
+    const int ry = pass == 2 ? 2 : 1;
 #pragma omp parallel for schedule(static)
     for (int j = 0; j < Hg; j++) {
         for (int i = 0; i < Wg; i++) {
+            const float bd = TV.at(i, j, 0), bh = HI.at(i, j, 0);
+            const int bf = FV.at(i, j);
+            float tw = 1.0f, td = bh;
+            for (int x = -1; x <= 1; x++) {
+                for (int y = -ry; y <= ry; y++) {
+                    if (x == 0 && y == 0) continue;
+                    const int si = i + 2 * x, sj = j + 2 * y;
+                    const float e = std::fabs(TV.at(si, sj, 0) - bd);
+                    const float ha = HI.at(si, sj, 0);
+                    if (e > 1.0f || ha < 0.0f || FV.at(si, sj) != bf) continue;
+                    const float wgt = kw[std::abs(x)] * kw[std::abs(y)];
+                    td += ha * wgt;
+                    tw += wgt;
+                }
+            }
+            hit_out[(size_t)j * Wg + i] = storage(td / fmaxg(tw, 0.001f), p->storage);
+        }
+    }
+}
+
+// ClipToAABB (SpecularTemporalFilter.glsl:146-156)
+inline v3 clip_to_aabb(v3 prev, v3 mn, v3 mx) {
+    const v3 pc = muls(add(mx, mn), 0.5f);
+    const v3 ec = muls(sub(mx, mn), 0.5f);
+    const v3 vc = sub(prev, pc);
+    const v3 vu = mk3(vc.x / ec.x, vc.y / ec.y, vc.z / ec.z);
+    const v3 au = mk3(std::fabs(vu.x), std::fabs(vu.y), std::fabs(vu.z));
+    const float denom = fmaxg(au.x, fmaxg(au.y, au.z));
+    return denom > 1.0f ? add(pc, divs(vc, denom)) : prev;
+}
+
+inline float dist_sq(v3 a, v3 b) {
+    const v3 c = sub(a, b);
+    return dot(c, c);
+}
+
+// SpecularTemporalFilter.glsl main (:316-510) with USE_NEW_REPROJECTION,
+// u_SmartClip, u_RoughnessWeight, u_TemporallyStabializeHitDistance,
+// u_FireflyRejection and u_AggressiveFireflyRejection on
+// (Core/Pipeline.cpp:3226-3262). TEMPORAL_SPEC is p->reflection_temporal;
+// off, the output is the firefly-rejected current colour.
+void vpto_spec_temporal(const vpto_world* w, const vpto_camera* cam, const vpto_camera* prev_cam,
+                        const vpto_params* p, const float* t_view, const uint8_t* face_view,
+                        const uint8_t* block_view, const float* prev_t, const uint8_t* prev_face,
+                        const float* spec, const float* hit, const float* mask, const float* prev_out,
+                        const float* prev_hit, const float* prev_stable, float* out, float* acc, float* stable) {
+    const int W = p->width, H = p->height, Wg = W / gi_div(p), Hg = H / gi_div(p);
+    const int fp16 = p->storage;
+    const bool temporal = p->reflection_temporal != 0;
+    const Plane TV{t_view, Wg, Hg, 1}, C{spec, Wg, Hg, 4}, M{mask, Wg, Hg, 1}, PC{prev_out, Wg, Hg, 4};
+    const Plane PH{prev_hit, Wg, Hg, 1}, PS{prev_stable, Wg, Hg, 1}, PT{prev_t, W, H, 1};
+    const Plane8 FV{face_view, Wg, Hg}, BV{block_view, Wg, Hg}, PF{prev_face, W, H};
+    float m[16];   // u_PrevProjection * u_PrevView, left to right
+    for (int c = 0; c < 4; c++)
+        for (int r = 0; r < 4; r++)
+            m[c * 4 + r] = ((prev_cam->proj[0 * 4 + r] * prev_cam->view[c * 4 + 0] +
+                             prev_cam->proj[1 * 4 + r] * prev_cam->view[c * 4 + 1]) +
+                            prev_cam->proj[2 * 4 + r] * prev_cam->view[c * 4 + 2]) +
+                           prev_cam->proj[3 * 4 + r] * prev_cam->view[c * 4 + 3];
+    const v3 cur_pos = mk3(cam->position[0], cam->position[1], cam->position[2]);
+    const v3 prev_pos = mk3(prev_cam->position[0], prev_cam->position[1], prev_cam->position[2]);
+    const v3 ro = ray_origin(cam);
+    const int ox[4] = {1, 0, -1, 0}, oy[4] = {0, 1, 0, -1};
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int j = 0; j < Hg; j++) {
+        for (int i = 0; i < Wg; i++) {
             const size_t q = (size_t)j * Wg + i;
-            float col[4];
-            for (int c = 0; c < 4; c++) col[c] = spec[q * 4 + c];
+            const v2 uv = texcoord(i, j, Wg, Hg);
+            const v4 P = position_fetch(cam, TV, i, j, uv);
+            const v3 n0 = normal_from_id(FV.at(i, j), 1.0f);
+            float cc[4];
+            for (int c = 0; c < 4; c++) cc[c] = C.at(i, j, c);
+            float o_acc = 0.0f;
+            const float hc = hit[q];
+            float o_col[4], o_stable;
+            // firefly rejection (:330-337, FireflyReject :267-305)
             if (mask[q] > 0.05f) {
-                float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                float a4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
                 int unlit = 0;
                 for (int k = 0; k < 4; k++) {
                     if (M.at(i + ox[k], j + oy[k], 0) < 0.01f) {
-                        for (int c = 0; c < 4; c++) acc[c] += C.at(i + ox[k], j + oy[k], c);
+                        for (int c = 0; c < 4; c++) a4[c] += C.at(i + ox[k], j + oy[k], c);
                         unlit++;
                     }
                 }
                 if (unlit >= 3)
-                    for (int c = 0; c < 4; c++) col[c] = acc[c] / (float)unlit;
+                    for (int c = 0; c < 4; c++) cc[c] = a4[c] / (float)unlit;
             }
-            for (int c = 0; c < 4; c++) out[q * 4 + c] = storage(col[c], p->storage);
+            if (P.w > 0.0f && temporal) {
+                const bool sky = hc < 0.0f;
+                const Material mt = material(w, std::min(std::max(BV.at(i, j), 0), 127));
+                const float rough = mixf(0.095f, mt.rough, 1.0f), metal = mt.metal;
+                bool less_valid = false;
+                v2 rep = v2{0.0f, 0.0f};
+                if (hc > 0.0f && !sky && rough <= 0.875f + 0.01f) {
+                    const v3 I = normalize(sub(ro, mk3(P.x, P.y, P.z)));
+                    const v3 rp = sub(mk3(P.x, P.y, P.z), muls(I, hc));
+                    const v4 pr = mat_mul4(m, rp.x, rp.y, rp.z, 1.0f);
+                    rep = v2{(pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f};
+                    float pt;
+                    PH.linear(rep, &pt);
+                    if (std::fabs(pt - hc) >= 3.8f) less_valid = true;
+                } else if (!sky) {
+                    const v3 off = muls(sub(cur_pos, prev_pos), 0.6f);
+                    const v3 wp = sub(mk3(P.x, P.y, P.z), off);
+                    const v4 pr = mat_mul4(m, wp.x, wp.y, wp.z, 1.0f);
+                    rep = v2{(pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f};
+                }
+                if (sky) {
+                    const v3 I = normalize(sub(ro, mk3(P.x, P.y, P.z)));
+                    const v3 rp = sub(mk3(P.x, P.y, P.z), muls(I, 64.0f));
+                    const v4 pr = mat_mul4(m, rp.x, rp.y, rp.z, 1.0f);
+                    rep = v2{(pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f};
+                }
+                const v4 pp = position_linear(cam, PT, rep);
+                const float d = std::fabs(length(sub(mk3(pp.x, pp.y, pp.z), mk3(P.x, P.y, P.z))));
+                const float rb = 0.01f;
+                const v3 pn = normal_from_id(PF.nearest(rep), 1.0f);
+                if (rep.x > 0.0f + rb && rep.x < 1.0f - rb && rep.y > 0.0f + rb && rep.y < 1.0f - rb && d < 1.0f &&
+                    pn.x == n0.x && pn.y == n0.y && pn.z == n0.z) {
+                    float pc[4];
+                    PC.linear(rep, pc);
+                    const v3 base_prev = mk3(pc[0], pc[1], pc[2]);
+                    const bool moved = dist_sq(cur_pos, prev_pos) > 0.0001f;
+                    if (rough < 0.5f + 0.01f && moved) {
+                        // ReflectionClipping (:163-243) around this texel
+                        float mn[4] = {1000.0f, 1000.0f, 1000.0f, 1000.0f}, mx[4] = {-1000.0f, -1000.0f, -1000.0f, -1000.0f};
+                        const float texel_x = 1.0f / (float)Wg, texel_y = 1.0f / (float)Hg;
+                        (void)texel_x;
+                        (void)texel_y;
+                        float add_max = 0.0f;
+                        for (int x = -1; x <= 1; x++) {
+                            for (int y = -1; y <= 1; y++) {
+                                if (!(M.at(i + x, j + y, 0) < 0.01f)) add_max += 0.1f;
+                                for (int c = 0; c < 4; c++) {
+                                    const float sv = C.at(i + x, j + y, c);
+                                    mn[c] = fming(sv, mn[c]);
+                                    mx[c] = fmaxg(sv, mx[c]);
+                                }
+                            }
+                        }
+                        const v3 omn = mk3(mn[0], mn[1], mn[2]), omx = mk3(mx[0], mx[1], mx[2]);
+                        const float rt = 0.275f + 0.01f;
+                        const bool smoothish = rough < rt;
+                        const bool roughish = rough > rt && rough < 0.50f + 0.01f;
+                        if (smoothish) {
+                            const float pr2 = rough * rough;
+                            const float rt2 = rt * rt;
+                            const float rr = 0.0f + (clampf((pr2 - 0.0f) / (rt2 - 0.0f), 0.0f, 1.0f) * (1.0f - 0.0f));
+                            float bias = mixf(0.01f, 0.085f, rr);
+                            if (rough > 0.235f) bias *= 1.55f;
+                            for (int c = 0; c < 4; c++) {
+                                mn[c] -= bias * 0.95f;
+                                mx[c] += (bias * 0.95f) + add_max;
+                            }
+                        } else if (roughish) {
+                            for (int c = 0; c < 4; c++) {
+                                mn[c] -= 0.37f;
+                                mx[c] += 0.37f + (add_max * 1.1f);
+                            }
+                        }
+                        const float imp = mixf(0.05f, 0.25f, metal > 0.05f ? 1.0f : 0.0f);
+                        v3 mn3 = vmix(mk3(mn[0], mn[1], mn[2]), omn, imp);
+                        v3 mx3 = vmix(mk3(mx[0], mx[1], mx[2]), omx, imp);
+                        const float bm = less_valid ? 0.5f : 0.0f;
+                        mn3 = vmix(mn3, omn, bm);
+                        mx3 = vmix(mx3, omx, bm);
+                        mn[0] = mn3.x; mn[1] = mn3.y; mn[2] = mn3.z;
+                        mx[0] = mx3.x; mx[1] = mx3.y; mx[2] = mx3.z;
+                        const v3 prev3 = mk3(pc[0], pc[1], pc[2]);
+                        const v3 cl = clip_to_aabb(prev3, mn3, mx3);
+                        if (!(cl.x == prev3.x && cl.y == prev3.y && cl.z == prev3.z)) {
+                            if (dist_sq(cl, mn3) > dist_sq(cl, mx3))
+                                for (int c = 0; c < 4; c++) pc[c] = mx[c];
+                            else
+                                for (int c = 0; c < 4; c++) pc[c] = mn[c];
+                        }
+                    }
+                    // GetAccumulationFactor (:308-313)
+                    const float vx = (uv.x - rep.x) * (float)Wg, vy = (uv.y - rep.y) * (float)Hg;
+                    float af = clampf(dm_exp(-std::sqrt(vx * vx + vy * vy)) * 0.9f + 0.750f, 0.00000001f, 0.96f);
+                    af = clampf(af, 0.001f, 0.95f);
+                    for (int c = 0; c < 4; c++) {
+                        const float cv = fmaxg(cc[c], 0.0f), pv = fmaxg(pc[c], 0.0f);
+                        o_col[c] = mixf(cv, pv, af);
+                    }
+                    o_acc = af;
+                    o_stable = hc;
+                    if (dist_sq(base_prev, mk3(fmaxg(pc[0], 0.0f), fmaxg(pc[1], 0.0f), fmaxg(pc[2], 0.0f))) < 0.2f) {
+                        float ps;
+                        PS.linear(rep, &ps);
+                        o_stable = mixf(hc, ps, clampf(af * 1.1f, 0.0f, 0.9f));
+                    }
+                } else {
+                    for (int c = 0; c < 4; c++) o_col[c] = cc[c];
+                    o_acc = 0.0f;
+                    o_stable = hc;
+                }
+            } else {
+                for (int c = 0; c < 4; c++) o_col[c] = cc[c];
+                o_stable = hc;
+            }
+            if (!temporal) o_acc = -1.0f;
+            for (int c = 0; c < 4; c++) out[q * 4 + c] = storage(o_col[c], fp16);
+            acc[q] = storage(o_acc, fp16);
+            stable[q] = storage(o_stable, fp16);
         }
     }
 }

@@ -69,7 +69,8 @@ typedef struct vpto_params {
     int32_t reflection_spp;     /* reflection samples per texel (0: no reflection pass) */
     int32_t reflection_max_steps;
     int32_t reflection_shadow_max_steps;
-    int32_t reserved[5];
+    int32_t reflection_temporal;  /* TEMPORAL_SPEC */
+    int32_t reserved[4];
 } vpto_params;
 
 typedef struct vpto_world {
@@ -176,8 +177,17 @@ void vpto_trace_reflection(const vpto_world* w, const vpto_camera* cam, const vp
                            const uint8_t* face_view, const uint8_t* block_view, const float* den_sh,
                            const float* den_cocg, const float* den_aosky, int row0, int row1, float* spec,
                            float* hit, float* mask);
-/* Firefly rejection of SpecularTemporalFilter.glsl (TEMPORAL_SPEC off). */
-void vpto_spec_resolve(const vpto_params* p, const float* spec, const float* mask, float* out);
+/* The two bilateral passes over the reflection hit distance (pass 1 or 2). */
+void vpto_spec_hit_blur(const vpto_params* p, int pass, const float* t_view, const uint8_t* face_view,
+                        const float* hit_in, float* hit_out);
+/* SpecularTemporalFilter.glsl (firefly rejection, reprojection by the hit
+ * distance, clipping, accumulation; TEMPORAL_SPEC = reflection_temporal). prev_*
+ * are last frame's full-resolution G-buffer and its reflection planes. */
+void vpto_spec_temporal(const vpto_world* w, const vpto_camera* cam, const vpto_camera* prev_cam,
+                        const vpto_params* p, const float* t_view, const uint8_t* face_view,
+                        const uint8_t* block_view, const float* prev_t, const uint8_t* prev_face,
+                        const float* spec, const float* hit, const float* mask, const float* prev_out,
+                        const float* prev_hit, const float* prev_stable, float* out, float* acc, float* stable);
 
 /* ColorPassFrag.glsl main: joint-bilateral GI upscale, direct GGX +
  * indirect-diffuse combine, flat materials. t / face / block / shadow at the

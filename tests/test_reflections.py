@@ -1,7 +1,8 @@
-"""The reflection pass (ReflectionTraceFrag.glsl and the firefly rejection
-of SpecularTemporalFilter.glsl, TEMPORAL_SPEC and DenoiseReflections off) and
-the specular indirect it feeds into the colour pass (ColorPassFrag.glsl
-:595-603, :901-909). Every plane is bit-identical to the oracle.
+"""The reflection pass (ReflectionTraceFrag.glsl, the two bilateral passes
+over its hit distance and SpecularTemporalFilter.glsl with TEMPORAL_SPEC on
+or off; DenoiseReflections off) and the specular indirect it feeds into the
+colour pass (ColorPassFrag.glsl :595-603, :901-909). Every plane is
+bit-identical to the oracle.
 """
 import numpy as np
 import pytest
@@ -30,7 +31,7 @@ def test_oracle_reflection_properties(vpt, oracle):
     differs from the raw one only where an emissive block was hit, and the
     colour pass with reflections adds light on average."""
     sc = scene_inputs(vpt, oracle)
-    cfg = vpt.default_config(width=W, height=H, primary_max_steps=256, reflection_spp=2)
+    cfg = vpt.default_config(width=W, height=H, primary_max_steps=256, reflection_spp=2, reflection_temporal=0)
     cam = sc["cams"][0]
     frame = vpt.default_frame(frame_index=0, seed=9)
     prev_g, hist = oracle.empty_history(H, W)
@@ -41,6 +42,7 @@ def test_oracle_reflection_properties(vpt, oracle):
     assert np.isfinite(r["spec"]).all() and (r["spec"][~sky] > 0).all()
     assert ((r["hit"] >= -10) & (r["hit"] <= 200)).all() and (r["hit"][~sky] > 0).any()
     assert set(np.unique(r["mask"])) <= {0.0, 1.0}
+    assert (r["acc"] == -1).all()
     changed = (r["out"] != r["spec"]).any(axis=-1)
     assert not (changed & (r["mask"] <= 0.05)).any()
     cfg0 = vpt.default_config(width=W, height=H, primary_max_steps=256)
@@ -48,6 +50,28 @@ def test_oracle_reflection_properties(vpt, oracle):
     hit = ~sky
     assert (ref["rgb"][sky] == base["rgb"][sky]).all()
     assert ref["rgb"][hit].mean() > base["rgb"][hit].mean() and (ref["rgb"][hit] != base["rgb"][hit]).any()
+
+
+def test_oracle_reflection_temporal_accumulates(vpt, oracle):
+    """With TEMPORAL_SPEC the second frame of a still camera reprojects onto
+    itself: accumulation factors in (0, 0.95] where history was valid, and
+    the output moves towards last frame's."""
+    sc = scene_inputs(vpt, oracle)
+    cfg = vpt.default_config(width=W, height=H, primary_max_steps=256, reflection_spp=2)
+    cam = sc["cams"][0]
+    prev_g, hist = oracle.empty_history(H, W)
+    f0 = oracle.render_frame(sc["world"], cam, cam, cfg, vpt.default_frame(frame_index=0, seed=9), prev_g, hist)
+    assert (f0["refl"]["acc"] == 0).all()          # nothing to reproject from
+    g0 = {k: f0["g"][k] for k in ("t", "face", "block")}
+    f1 = oracle.render_frame(sc["world"], cam, cam, cfg, vpt.default_frame(frame_index=1, seed=9), g0,
+                             f0["svgf"]["temporal"], f0["refl"])
+    acc = f1["refl"]["acc"]
+    hits = f1["g"]["t"] > 0
+    assert ((acc == 0) | ((acc >= 0.001) & (acc <= 0.95))).all() and (acc[hits] > 0.5).mean() > 0.5
+    hist_ok = acc > 0
+    d_new = np.abs(f1["refl"]["out"] - f1["refl"]["spec"])[hist_ok].mean()
+    d_old = np.abs(f1["refl"]["out"] - f0["refl"]["out"])[hist_ok].mean()
+    assert d_old < d_new
 
 
 def test_oracle_reflection_counts_rays(vpt, oracle):
@@ -65,36 +89,52 @@ def test_oracle_reflection_counts_rays(vpt, oracle):
 
 # ------------------------------------------------------------------ GPU --
 @pytest.mark.gpu
-@pytest.mark.parametrize("d,storage,denoiser", [(1, 0, 0), (2, 0, 0), (1, 1, 0), (4, 1, 0), (1, 0, 1)],
-                         ids=["d1-f32", "d2-f32", "d1-f16", "d4-f16", "d1-plain"])
-def test_reflection_planes_bit_exact(vpt, oracle, d, storage, denoiser, gpu):
+@pytest.mark.parametrize("d,storage,denoiser,temporal", [(1, 0, 0, 1), (2, 0, 0, 1), (1, 1, 0, 1), (4, 1, 0, 1),
+                                                          (1, 0, 1, 1), (1, 0, 0, 0)],
+                         ids=["d1-f32", "d2-f32", "d1-f16", "d4-f16", "d1-plain", "d1-no-temporal"])
+def test_reflection_planes_bit_exact(vpt, oracle, d, storage, denoiser, temporal, gpu):
     sc = scene_inputs(vpt, oracle)
     world = sc["world"]
+    X, Z = DIMS[0], DIMS[2]
+    yaw, pitch = vpt.seeded_pose(1)
+    cams = sc["cams"] + [vpt.camera_from_pose((X / 2 + 1.1, 58.1, Z / 2 - 0.9), yaw + 3.5, pitch + 1.5, 90.0, W / H)]
     ctx = vpt.Context(width=W, height=H, primary_max_steps=256, storage=storage, gi_divisor=d, reflection_spp=2,
-                      denoiser=denoiser)
+                      denoiser=denoiser, reflection_temporal=temporal)
     ctx.upload_world(sc["vox"])
     ctx.set_block_table(sc["blocks"])
     ctx.build_df()
     cfg = ctx.config
     prev_g, hist = oracle.empty_history(H, W, d)
-    prev_cam = sc["cams"][0]
-    for fi, cam in enumerate(sc["cams"]):
+    prev_refl = None
+    prev_cam = cams[0]
+    for fi, cam in enumerate(cams):
         frame = vpt.default_frame(frame_index=fi, seed=13, time=0.7 + 0.2 * fi)
         ctx.set_stats(True)
-        rgb = ctx.render_frame(cam, frame)
+        ctx.trace_primary(cam)
+        ctx.trace_shadow(frame)
+        ctx.trace_diffuse(frame)
+        ctx.svgf(prev_cam, frame)
+        ctx.trace_reflections(frame)
+        ctx.shade(frame)
+        rgb = ctx.read_plane("COLOR")
         stats = ctx.read_stats()
         with oracle.Counting() as cnt:
-            ref = oracle.render_frame(world, cam, prev_cam, cfg, frame, prev_g, hist)
+            ref = oracle.render_frame(world, cam, prev_cam, cfg, frame, prev_g, hist, prev_refl)
         r = ref["refl"]
-        # render_frame has swapped the history, not the reflection planes
         assert_same(ctx.read_plane("SPEC"), r["spec"], f"{d} frame {fi} spec")
-        assert_same(ctx.read_plane("SPEC_HIT")[..., 0], r["hit"], f"{d} frame {fi} hit")
         assert_same(ctx.read_plane("SPEC_MASK")[..., 0], r["mask"], f"{d} frame {fi} mask")
-        assert_same(ctx.read_plane("SPEC_OUT"), r["out"], f"{d} frame {fi} resolved")
+        assert_same(ctx.read_plane("SPEC_HIT")[..., 0], r["hit"], f"{d} frame {fi} blurred hit")
+        assert_same(ctx.read_plane("SPEC_OUT"), r["out"], f"{d} frame {fi} temporal colour")
+        assert_same(ctx.read_plane("SPEC_ACC")[..., 0], r["acc"], f"{d} frame {fi} accumulation")
+        assert_same(ctx.read_plane("SPEC_STABLE_HIT")[..., 0], r["stable"], f"{d} frame {fi} stable hit")
         assert_same(rgb, ref["rgb"], f"{d} frame {fi} colour")
         assert stats["rays"] == cnt.rays and stats["steps"] == cnt.steps
+        if temporal and fi > 0:
+            assert (r["acc"] > 0).any()
+        ctx.end_frame()
         prev_g = {k: ref["g"][k] for k in ("t", "face", "block")}
         hist = ref["svgf"]["temporal"]
+        prev_refl = r
         prev_cam = cam
     ctx.close()
 

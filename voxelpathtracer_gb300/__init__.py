@@ -41,7 +41,7 @@ PLANES = [
     "PREV_T", "PREV_FACE", "PREV_BLOCK",
     "VAR_SH", "VAR_COCG", "VAR_VARIANCE",
     "DEN_SH", "DEN_COCG", "DEN_VARIANCE", "DEN_AOSKY",
-    "COLOR", "SPEC", "SPEC_HIT", "SPEC_MASK", "SPEC_OUT",
+    "COLOR", "SPEC", "SPEC_HIT", "SPEC_MASK", "SPEC_OUT", "SPEC_ACC", "SPEC_STABLE_HIT",
 ]
 PLANE = {name: i for i, name in enumerate(PLANES)}
 PASSES = ["primary", "shadow", "diffuse", "spatial_initial", "temporal", "variance", "atrous", "shade", "trace_frame",
@@ -58,7 +58,8 @@ class Config(C.Structure):
                 ("storage", C.c_int32), ("atrous_iterations", C.c_int32), ("resolution_scale", C.c_float),
                 ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
                 ("gi_divisor", C.c_int32), ("reflection_spp", C.c_int32), ("reflection_max_steps", C.c_int32),
-                ("reflection_shadow_max_steps", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("reflection_shadow_max_steps", C.c_int32), ("reflection_temporal", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class Camera(C.Structure):

@@ -49,7 +49,8 @@ PlaneMeta plane_meta(int plane) {
         case VPT_PLANE_DEN_VARIANCE: return {1, 1, 0, 1};
         case VPT_PLANE_COLOR: return {3, 1, 0, 0};
         case VPT_PLANE_SPEC: case VPT_PLANE_SPEC_OUT: return {4, 1, 0, 1};
-        case VPT_PLANE_SPEC_HIT: case VPT_PLANE_SPEC_MASK: return {1, 1, 0, 1};
+        case VPT_PLANE_SPEC_HIT: case VPT_PLANE_SPEC_MASK: case VPT_PLANE_SPEC_ACC:
+        case VPT_PLANE_SPEC_STABLE_HIT: return {1, 1, 0, 1};
         default: return {0, 0, -1, 0};
     }
 }
@@ -94,7 +95,17 @@ struct vpt_ctx {
     void* var[FI_N] = {};
     void* den[2][FI_N] = {};
     void* color = nullptr;
-    void* refl[4] = {};   // reflection: radiance (4 ch), hit distance, emissive mask, resolved (4 ch)
+    // reflection planes on the GI grid: traced radiance (4 ch) and emissive
+    // mask, hit distance (this / last frame), the temporal output (4 ch) and
+    // stabilised hit distance (this / last frame), accumulation factor, and
+    // the first hit-distance blur pass's output
+    void* rspec = nullptr;
+    void* rmask = nullptr;
+    void* rhit[2] = {};
+    void* rout[2] = {};
+    void* rstable[2] = {};
+    void* racc = nullptr;
+    void* rhit_tmp = nullptr;
     int cur = 0;        // index of this frame's G-buffer / temporal output
     int den_last = 0;   // den set holding the last a-trous output
     // cameras
@@ -214,10 +225,12 @@ void* plane_ptr(vpt_ctx* c, int plane) {
         case VPT_PLANE_DEN_VARIANCE: return c->den[c->den_last][FI_VAR];
         case VPT_PLANE_DEN_AOSKY: return c->den[c->den_last][FI_AOSKY];
         case VPT_PLANE_COLOR: return c->color;
-        case VPT_PLANE_SPEC: return c->refl[0];
-        case VPT_PLANE_SPEC_HIT: return c->refl[1];
-        case VPT_PLANE_SPEC_MASK: return c->refl[2];
-        case VPT_PLANE_SPEC_OUT: return c->refl[3];
+        case VPT_PLANE_SPEC: return c->rspec;
+        case VPT_PLANE_SPEC_HIT: return c->rhit[cur];
+        case VPT_PLANE_SPEC_MASK: return c->rmask;
+        case VPT_PLANE_SPEC_OUT: return c->rout[cur];
+        case VPT_PLANE_SPEC_ACC: return c->racc;
+        case VPT_PLANE_SPEC_STABLE_HIT: return c->rstable[cur];
         default: return nullptr;
     }
 }
@@ -271,10 +284,15 @@ vpt_status alloc_planes(vpt_ctx* c) {
     c->var[FI_AOSKY] = nullptr;
     A(c->color, nf * 3 * es);
     if (c->cfg.reflection_spp > 0) {
-        A(c->refl[0], n * 4 * es);
-        A(c->refl[1], n * es);
-        A(c->refl[2], n * es);
-        A(c->refl[3], n * 4 * es);
+        A(c->rspec, n * 4 * es);
+        A(c->rmask, n * es);
+        A(c->racc, n * es);
+        A(c->rhit_tmp, n * es);
+        for (int k = 0; k < 2; k++) {
+            A(c->rhit[k], n * es);
+            A(c->rout[k], n * 4 * es);
+            A(c->rstable[k], n * es);
+        }
     }
     A(c->counters, sizeof(Counters));
     A(c->queue, 256);
@@ -302,6 +320,11 @@ vpt_status clear_history(vpt_ctx* c) {
     CK(c, cudaMemsetAsync(c->hist[prv][HI_COCG], 0, ng * 2 * es, c->stream));
     CK(c, cudaMemsetAsync(c->hist[prv][HI_UTIL], 0, ng * 4 * es, c->stream));
     CK(c, cudaMemsetAsync(c->hist[prv][HI_AOSKY], 0, ng * 2 * es, c->stream));
+    if (c->cfg.reflection_spp > 0) {
+        CK(c, cudaMemsetAsync(c->rhit[prv], 0, ng * es, c->stream));
+        CK(c, cudaMemsetAsync(c->rout[prv], 0, ng * 4 * es, c->stream));
+        CK(c, cudaMemsetAsync(c->rstable[prv], 0, ng * es, c->stream));
+    }
     CK(c, cudaStreamSynchronize(c->stream));
     c->have_prev = false;
     return VPT_OK;
@@ -385,6 +408,7 @@ vpt_status vpt_default_config(vpt_config* cfg) {
     cfg->reflection_spp = 0;
     cfg->reflection_max_steps = 64;
     cfg->reflection_shadow_max_steps = 150;
+    cfg->reflection_temporal = 1;
     cfg->color_phi_bias = 3.325f;
     cfg->device = 0;
     return VPT_OK;
@@ -925,14 +949,37 @@ vpt_status reflection_run(vpt_ctx* c, const vpt_frame* f) {
     a.mixed[2] = mixed.z;
     const void *sh, *cocg, *ao;
     denoised_gi(c, &sh, &cocg, &ao);
+    const int cur = c->cur, prv = 1 - c->cur;
+    const vpt_camera& pc = c->have_prev ? c->prev_cam : c->cam;
+    SpecTemporalArgs ta;
+    for (int col = 0; col < 4; col++)
+        for (int r = 0; r < 4; r++)
+            ta.prev_view_proj[col * 4 + r] = ((pc.proj[0 * 4 + r] * pc.view[col * 4 + 0] +
+                                               pc.proj[1 * 4 + r] * pc.view[col * 4 + 1]) +
+                                              pc.proj[2 * 4 + r] * pc.view[col * 4 + 2]) +
+                                             pc.proj[3 * 4 + r] * pc.view[col * 4 + 3];
+    for (int k = 0; k < 3; k++) {
+        ta.cur_pos[k] = cm.position[k];
+        ta.prev_pos[k] = pc.position[k];
+    }
+    ta.temporal = c->cfg.reflection_temporal ? 1 : 0;
     pass_begin(c, VPT_PASS_REFLECTION);
     CK(c, trace_reflection(world_view(c), cam_view(cm), c->cfg.width, c->cfg.height, c->gw, c->gh, c->fp16, a,
-                           c->gbuf[c->cur][GB_T], (const uint8_t*)c->gbuf[c->cur][GB_FACE], c->shadow, c->view[0],
-                           (const uint8_t*)c->view[1], (const uint8_t*)c->view[2], sh, cocg, ao, c->refl[0], c->refl[1],
-                           c->refl[2], c->stats ? c->counters : nullptr, c->stream));
-    CK(c, spec_resolve(c->gw, c->gh, c->fp16, c->refl[0], c->refl[2], c->refl[3], c->stream));
+                           c->gbuf[cur][GB_T], (const uint8_t*)c->gbuf[cur][GB_FACE], c->shadow, c->view[0],
+                           (const uint8_t*)c->view[1], (const uint8_t*)c->view[2], sh, cocg, ao, c->rspec, c->rhit[cur],
+                           c->rmask, c->stats ? c->counters : nullptr, c->stream));
+    // the two bilateral passes over the hit distance (Core/Pipeline.cpp:3141-3215)
+    CK(c, spec_hit_blur(c->gw, c->gh, c->fp16, 1, c->view[0], (const uint8_t*)c->view[1], c->rhit[cur], c->rhit_tmp,
+                        c->stream));
+    CK(c, spec_hit_blur(c->gw, c->gh, c->fp16, 2, c->view[0], (const uint8_t*)c->view[1], c->rhit_tmp, c->rhit[cur],
+                        c->stream));
+    // SpecularTemporalFilter (:3217-3262)
+    CK(c, spec_temporal(world_view(c), cam_view(cm), ta, c->cfg.width, c->cfg.height, c->gw, c->gh, c->fp16,
+                        c->view[0], (const uint8_t*)c->view[1], (const uint8_t*)c->view[2], c->gbuf[prv][GB_T],
+                        (const uint8_t*)c->gbuf[prv][GB_FACE], c->rspec, c->rhit[cur], c->rmask, c->rout[prv],
+                        c->rhit[prv], c->rstable[prv], c->rout[cur], c->racc, c->rstable[cur], c->stream));
     pass_end(c, VPT_PASS_REFLECTION);
-    c->launches += 2;
+    c->launches += 4;
     return VPT_OK;
 }
 
@@ -963,7 +1010,7 @@ vpt_status shade_run(vpt_ctx* c, const vpt_frame* f, int source, void* out = nul
     denoised_gi(c, &sh, &cocg, &ao);
     // the specular indirect of this frame's reflection pass (the learned
     // path's inputs, sources 1 and 2, are shaded without it)
-    const void* spec = (c->cfg.reflection_spp > 0 && source == 0) ? c->refl[3] : nullptr;
+    const void* spec = (c->cfg.reflection_spp > 0 && source == 0) ? c->rout[c->cur] : nullptr;
     if (source == 1) {
         sh = c->hist[c->cur][HI_SH];
         cocg = c->hist[c->cur][HI_COCG];

@@ -258,7 +258,18 @@ cudaError_t trace_reflection(const WorldView& w, const CamView& cam, int W, int 
                              const void* tv, const uint8_t* fv, const uint8_t* bv, const void* den_sh,
                              const void* den_cocg, const void* den_ao, void* spec, void* hit, void* mask,
                              Counters* stats, cudaStream_t s);
-cudaError_t spec_resolve(int Wg, int Hg, int fp16, const void* spec, const void* mask, void* out, cudaStream_t s);
+cudaError_t spec_hit_blur(int Wg, int Hg, int fp16, int pass, const void* tv, const uint8_t* fv, const void* hin,
+                          void* hout, cudaStream_t s);
+struct SpecTemporalArgs {
+    float prev_view_proj[16];   // u_PrevProjection * u_PrevView
+    float cur_pos[3], prev_pos[3];
+    int temporal;               // TEMPORAL_SPEC
+};
+cudaError_t spec_temporal(const WorldView& w, const CamView& cam, const SpecTemporalArgs& a, int W, int H, int Wg,
+                          int Hg, int fp16, const void* tv, const uint8_t* fv, const uint8_t* bv, const void* prev_t,
+                          const uint8_t* prev_face, const void* spec, const void* hit, const void* mask,
+                          const void* prev_out, const void* prev_hit, const void* prev_stable, void* out, void* acc,
+                          void* stable, cudaStream_t s);
 
 // ------------------------------------------------------------- shade.cu --
 struct ShadeArgs {

@@ -1,13 +1,13 @@
-// Reflections: ReflectionTraceFrag.glsl main (:717-1084) and the firefly
-// rejection at the head of SpecularTemporalFilter.glsl (:316-340), on the GI
-// grid, one thread per texel, each warp on an 8x4 patch so its rays stay
-// coherent. Substitutions as in the diffuse trace: flat materials (albedo,
-// roughness, metalness, emissive flag of the block; AO 1; the face normal as
-// the normal map), PCG random numbers instead of hash2 / blue noise, the
-// analytic sky, no LPV, cloud reflections or player, no jitter. The
-// temporal filter and the spatial reflection denoiser are off
-// (TEMPORAL_SPEC / DenoiseReflections false), so the resolved reflection is
-// what the colour pass reads.
+// Reflections: ReflectionTraceFrag.glsl main (:717-1084) on the GI grid, one
+// thread per texel, each warp on an 8x4 patch so its rays stay coherent;
+// then the two bilateral passes over its hit distance and
+// SpecularTemporalFilter.glsl (firefly rejection, reprojection, clipping,
+// accumulation). Substitutions as in the diffuse trace: flat materials
+// (albedo, roughness, metalness, emissive flag of the block; AO 1; the face
+// normal as the normal map), PCG random numbers instead of hash2 / blue
+// noise, the analytic sky, no LPV, cloud reflections or player, no jitter.
+// The spatial reflection denoiser is off (DenoiseReflections false), so the
+// temporal output is what the colour pass reads.
 #include "pixel_passes.cuh"
 
 namespace vpt {
@@ -238,38 +238,214 @@ __global__ void __launch_bounds__(256) k_trace_reflection(WorldView w, CamView c
     }
 }
 
-// FireflyReject (SpecularTemporalFilter.glsl:267-305) with
-// u_AggressiveFireflyRejection on (3 of 4 non-emissive neighbours), applied
-// where the texel's mask is above 0.05 (:330-337).
+// BlurHitDistance_Bilateral.glsl (pass 1, 3x3) and
+// BlurHitDistancePass2_Bilateral.glsl (pass 2, 3 x 5 taps), two GI texels
+// apart, REPEAT wrap; depth and face from the GI-grid views.
 template <typename S>
-__global__ void __launch_bounds__(256) k_spec_resolve(int Wg, int Hg, const S* spec, const S* mask, S* out) {
+__global__ void __launch_bounds__(256) k_spec_hit_blur(int Wg, int Hg, int pass, const S* tv, const uint8_t* fv,
+                                                       const S* hin, S* hout) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= Wg || j >= Hg) return;
     const size_t q = (size_t)j * Wg + i;
-    float4 col = ld4(spec + 4 * q);
+    const float bd = ld(tv + q), bh = ld(hin + q);
+    const int bf = __ldg(fv + q);
+    const int ry = pass == 2 ? 2 : 1;
+    float tw = 1.0f, td = bh;
+    for (int x = -1; x <= 1; x++) {
+        const int si = wrapi(i + 2 * x, Wg);
+        for (int y = -ry; y <= ry; y++) {
+            if (x == 0 && y == 0) continue;
+            const size_t n = (size_t)wrapi(j + 2 * y, Hg) * Wg + si;
+            const float e = fabsf(ld(tv + n) - bd);
+            const float ha = ld(hin + n);
+            if (e > 1.0f || ha < 0.0f || (int)__ldg(fv + n) != bf) continue;
+            const float wx = x == 0 ? 1.0f : 2.0f / 3.0f;
+            const float wy = y == 0 ? 1.0f : ((y == 1 || y == -1) ? 2.0f / 3.0f : 1.0f / 6.0f);
+            const float wgt = wx * wy;
+            td += ha * wgt;
+            tw += wgt;
+        }
+    }
+    st(hout + q, td / fmaxf(tw, 0.001f));
+}
+
+// ClipToAABB (SpecularTemporalFilter.glsl:146-156)
+__device__ __forceinline__ v3 clip_to_aabb(v3 prev, v3 mn, v3 mx) {
+    const v3 pc = muls(add(mx, mn), 0.5f);
+    const v3 ec = muls(sub(mx, mn), 0.5f);
+    const v3 vc = sub(prev, pc);
+    const v3 vu = mk3(vc.x / ec.x, vc.y / ec.y, vc.z / ec.z);
+    const float denom = fmaxf(fabsf(vu.x), fmaxf(fabsf(vu.y), fabsf(vu.z)));
+    return denom > 1.0f ? add(pc, divs(vc, denom)) : prev;
+}
+
+__device__ __forceinline__ float dist_sq(v3 a, v3 b) {
+    const v3 c = sub(a, b);
+    return dot(c, c);
+}
+
+// SpecularTemporalFilter.glsl main (:316-510) with USE_NEW_REPROJECTION,
+// u_SmartClip, u_RoughnessWeight, u_TemporallyStabializeHitDistance and
+// aggressive firefly rejection on (Core/Pipeline.cpp:3226-3262); with
+// TEMPORAL_SPEC off the output is the firefly-rejected current colour.
+template <typename S>
+__global__ void __launch_bounds__(256) k_spec_temporal(WorldView w, CamView cam, SpecTemporalArgs a, int W, int H,
+                                                       int Wg, int Hg, const S* tv, const uint8_t* fv,
+                                                       const uint8_t* bv, const S* prev_t, const uint8_t* prev_face,
+                                                       const S* spec, const S* hit, const S* mask, const S* prev_out,
+                                                       const S* prev_hit, const S* prev_stable, S* out, S* acc,
+                                                       S* stable) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= Wg || j >= Hg) return;
+    const size_t q = (size_t)j * Wg + i;
+    const v2 uv = texcoord(i, j, Wg, Hg);
+    const Plane<S, 1> TV{tv, Wg, Hg};
+    const v4 P = position_fetch(cam, TV, i, j, uv);
+    const v3 n0 = normal_from_id(__ldg(fv + q), 1.0f);
+    const float4 c0 = ld4(spec + 4 * q);
+    float cc[4] = {c0.x, c0.y, c0.z, c0.w};
+    float o_acc = 0.0f;
+    const float hc = ld(hit + q);
+    float o_col[4], o_stable;
     if (ld(mask + q) > 0.05f) {
         const int ox[4] = {1, 0, -1, 0}, oy[4] = {0, 1, 0, -1};
-        float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float a4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         int unlit = 0;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
             const size_t n = (size_t)wrapi(j + oy[k], Hg) * Wg + wrapi(i + ox[k], Wg);
             if (ld(mask + n) < 0.01f) {
                 const float4 c = ld4(spec + 4 * n);
-                acc.x += c.x;
-                acc.y += c.y;
-                acc.z += c.z;
-                acc.w += c.w;
+                a4[0] += c.x;
+                a4[1] += c.y;
+                a4[2] += c.z;
+                a4[3] += c.w;
                 unlit++;
             }
         }
-        if (unlit >= 3) {
-            const float u = (float)unlit;
-            col = make_float4(acc.x / u, acc.y / u, acc.z / u, acc.w / u);
-        }
+        if (unlit >= 3)
+            for (int c = 0; c < 4; c++) cc[c] = a4[c] / (float)unlit;
     }
-    st4(out + 4 * q, col.x, col.y, col.z, col.w);
+    if (P.w > 0.0f && a.temporal) {
+        const bool sky = hc < 0.0f;
+        const Material mt = material(w, min(max((int)__ldg(bv + q), 0), 127));
+        const float rough = mixf(0.095f, mt.rough, 1.0f), metal = mt.metal;
+        const v3 cur_pos = mk3(a.cur_pos[0], a.cur_pos[1], a.cur_pos[2]);
+        const v3 prev_pos = mk3(a.prev_pos[0], a.prev_pos[1], a.prev_pos[2]);
+        const v3 ro = ray_origin(cam);
+        const v3 p3 = mk3(P.x, P.y, P.z);
+        bool less_valid = false;
+        v2 rep = mk2(0.0f, 0.0f);
+        if (hc > 0.0f && !sky && rough <= 0.875f + 0.01f) {
+            const v3 I = normalize(sub(ro, p3));
+            const v3 rp = sub(p3, muls(I, hc));
+            const v4 pr = mat_mul4(a.prev_view_proj, rp.x, rp.y, rp.z, 1.0f);
+            rep = mk2((pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f);
+            const float pt = bl1(prev_hit, bilin(rep, Wg, Hg));
+            if (fabsf(pt - hc) >= 3.8f) less_valid = true;
+        } else if (!sky) {
+            const v3 off = muls(sub(cur_pos, prev_pos), 0.6f);
+            const v3 wp = sub(p3, off);
+            const v4 pr = mat_mul4(a.prev_view_proj, wp.x, wp.y, wp.z, 1.0f);
+            rep = mk2((pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f);
+        }
+        if (sky) {
+            const v3 I = normalize(sub(ro, p3));
+            const v3 rp = sub(p3, muls(I, 64.0f));
+            const v4 pr = mat_mul4(a.prev_view_proj, rp.x, rp.y, rp.z, 1.0f);
+            rep = mk2((pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f);
+        }
+        const Plane<S, 1> PT{prev_t, W, H};
+        const Plane8 PF{prev_face, W, H};
+        const v4 pp = position_linear(cam, PT, rep);
+        const float d = fabsf(length(sub(mk3(pp.x, pp.y, pp.z), p3)));
+        const float rb = 0.01f;
+        const v3 pn = normal_from_id(PF.nearest(rep), 1.0f);
+        if (rep.x > 0.0f + rb && rep.x < 1.0f - rb && rep.y > 0.0f + rb && rep.y < 1.0f - rb && d < 1.0f &&
+            pn.x == n0.x && pn.y == n0.y && pn.z == n0.z) {
+            const Bilin fg = bilin(rep, Wg, Hg);
+            const float4 p4 = bl4(prev_out, fg);
+            float pc[4] = {p4.x, p4.y, p4.z, p4.w};
+            const v3 base_prev = mk3(pc[0], pc[1], pc[2]);
+            const bool moved = dist_sq(cur_pos, prev_pos) > 0.0001f;
+            if (rough < 0.5f + 0.01f && moved) {
+                // ReflectionClipping (:163-243) around this texel
+                float mn[4] = {1000.0f, 1000.0f, 1000.0f, 1000.0f}, mx[4] = {-1000.0f, -1000.0f, -1000.0f, -1000.0f};
+                float add_max = 0.0f;
+                for (int x = -1; x <= 1; x++) {
+                    const int si = wrapi(i + x, Wg);
+                    for (int y = -1; y <= 1; y++) {
+                        const size_t n = (size_t)wrapi(j + y, Hg) * Wg + si;
+                        if (!(ld(mask + n) < 0.01f)) add_max += 0.1f;
+                        const float4 sv = ld4(spec + 4 * n);
+                        const float s4[4] = {sv.x, sv.y, sv.z, sv.w};
+                        for (int c = 0; c < 4; c++) {
+                            mn[c] = fminf(s4[c], mn[c]);
+                            mx[c] = fmaxf(s4[c], mx[c]);
+                        }
+                    }
+                }
+                const v3 omn = mk3(mn[0], mn[1], mn[2]), omx = mk3(mx[0], mx[1], mx[2]);
+                const float rt = 0.275f + 0.01f;
+                const bool smoothish = rough < rt;
+                const bool roughish = rough > rt && rough < 0.50f + 0.01f;
+                if (smoothish) {
+                    const float pr2 = rough * rough;
+                    const float rt2 = rt * rt;
+                    const float rr = 0.0f + (clampf((pr2 - 0.0f) / (rt2 - 0.0f), 0.0f, 1.0f) * (1.0f - 0.0f));
+                    float bias = mixf(0.01f, 0.085f, rr);
+                    if (rough > 0.235f) bias *= 1.55f;
+                    for (int c = 0; c < 4; c++) {
+                        mn[c] -= bias * 0.95f;
+                        mx[c] += (bias * 0.95f) + add_max;
+                    }
+                } else if (roughish) {
+                    for (int c = 0; c < 4; c++) {
+                        mn[c] -= 0.37f;
+                        mx[c] += 0.37f + (add_max * 1.1f);
+                    }
+                }
+                const float imp = mixf(0.05f, 0.25f, metal > 0.05f ? 1.0f : 0.0f);
+                v3 mn3 = vmix(mk3(mn[0], mn[1], mn[2]), omn, imp);
+                v3 mx3 = vmix(mk3(mx[0], mx[1], mx[2]), omx, imp);
+                const float bm = less_valid ? 0.5f : 0.0f;
+                mn3 = vmix(mn3, omn, bm);
+                mx3 = vmix(mx3, omx, bm);
+                mn[0] = mn3.x; mn[1] = mn3.y; mn[2] = mn3.z;
+                mx[0] = mx3.x; mx[1] = mx3.y; mx[2] = mx3.z;
+                const v3 prev3 = mk3(pc[0], pc[1], pc[2]);
+                const v3 cl = clip_to_aabb(prev3, mn3, mx3);
+                if (!(cl.x == prev3.x && cl.y == prev3.y && cl.z == prev3.z)) {
+                    if (dist_sq(cl, mn3) > dist_sq(cl, mx3))
+                        for (int c = 0; c < 4; c++) pc[c] = mx[c];
+                    else
+                        for (int c = 0; c < 4; c++) pc[c] = mn[c];
+                }
+            }
+            // GetAccumulationFactor (:308-313)
+            const float vx = (uv.x - rep.x) * (float)Wg, vy = (uv.y - rep.y) * (float)Hg;
+            float af = clampf(dexp(-sqrtf(vx * vx + vy * vy)) * 0.9f + 0.750f, 0.00000001f, 0.96f);
+            af = clampf(af, 0.001f, 0.95f);
+            for (int c = 0; c < 4; c++) o_col[c] = mixf(fmaxf(cc[c], 0.0f), fmaxf(pc[c], 0.0f), af);
+            o_acc = af;
+            o_stable = hc;
+            if (dist_sq(base_prev, mk3(fmaxf(pc[0], 0.0f), fmaxf(pc[1], 0.0f), fmaxf(pc[2], 0.0f))) < 0.2f)
+                o_stable = mixf(hc, bl1(prev_stable, fg), clampf(af * 1.1f, 0.0f, 0.9f));
+        } else {
+            for (int c = 0; c < 4; c++) o_col[c] = cc[c];
+            o_acc = 0.0f;
+            o_stable = hc;
+        }
+    } else {
+        for (int c = 0; c < 4; c++) o_col[c] = cc[c];
+        o_stable = hc;
+    }
+    if (!a.temporal) o_acc = -1.0f;
+    st4(out + 4 * q, o_col[0], o_col[1], o_col[2], o_col[3]);
+    st(acc + q, o_acc);
+    st(stable + q, o_stable);
 }
 
 }  // namespace
@@ -291,12 +467,34 @@ cudaError_t trace_reflection(const WorldView& w, const CamView& cam, int W, int 
     return cudaGetLastError();
 }
 
-cudaError_t spec_resolve(int Wg, int Hg, int fp16, const void* spec, const void* mask, void* out, cudaStream_t s) {
+cudaError_t spec_hit_blur(int Wg, int Hg, int fp16, int pass, const void* tv, const uint8_t* fv, const void* hin,
+                          void* hout, cudaStream_t s) {
     const dim3 grid((unsigned)((Wg + 31) / 32), (unsigned)((Hg + 7) / 8)), blk(32, 8);
     if (fp16)
-        k_spec_resolve<__half><<<grid, blk, 0, s>>>(Wg, Hg, (const __half*)spec, (const __half*)mask, (__half*)out);
+        k_spec_hit_blur<__half><<<grid, blk, 0, s>>>(Wg, Hg, pass, (const __half*)tv, fv, (const __half*)hin,
+                                                     (__half*)hout);
     else
-        k_spec_resolve<float><<<grid, blk, 0, s>>>(Wg, Hg, (const float*)spec, (const float*)mask, (float*)out);
+        k_spec_hit_blur<float><<<grid, blk, 0, s>>>(Wg, Hg, pass, (const float*)tv, fv, (const float*)hin,
+                                                    (float*)hout);
+    return cudaGetLastError();
+}
+
+cudaError_t spec_temporal(const WorldView& w, const CamView& cam, const SpecTemporalArgs& a, int W, int H, int Wg,
+                          int Hg, int fp16, const void* tv, const uint8_t* fv, const uint8_t* bv, const void* prev_t,
+                          const uint8_t* prev_face, const void* spec, const void* hit, const void* mask,
+                          const void* prev_out, const void* prev_hit, const void* prev_stable, void* out, void* acc,
+                          void* stable, cudaStream_t s) {
+    const dim3 grid((unsigned)((Wg + 31) / 32), (unsigned)((Hg + 7) / 8)), blk(32, 8);
+    if (fp16)
+        k_spec_temporal<__half><<<grid, blk, 0, s>>>(
+            w, cam, a, W, H, Wg, Hg, (const __half*)tv, fv, bv, (const __half*)prev_t, prev_face, (const __half*)spec,
+            (const __half*)hit, (const __half*)mask, (const __half*)prev_out, (const __half*)prev_hit,
+            (const __half*)prev_stable, (__half*)out, (__half*)acc, (__half*)stable);
+    else
+        k_spec_temporal<float><<<grid, blk, 0, s>>>(
+            w, cam, a, W, H, Wg, Hg, (const float*)tv, fv, bv, (const float*)prev_t, prev_face, (const float*)spec,
+            (const float*)hit, (const float*)mask, (const float*)prev_out, (const float*)prev_hit,
+            (const float*)prev_stable, (float*)out, (float*)acc, (float*)stable);
     return cudaGetLastError();
 }
 
