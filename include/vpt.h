@@ -72,7 +72,9 @@ typedef struct vpt_config {
     int32_t reflection_shadow_max_steps; /* 150 (ReflectionTraceFrag.glsl:1098) */
     int32_t reflection_temporal;     /* TEMPORAL_SPEC (Core/Pipeline.cpp:124): 1 (default) runs
                                         SpecularTemporalFilter's reprojection and accumulation */
-    int32_t reserved[4];
+    int32_t reflection_denoise;      /* DenoiseReflections (:105): 1 (default) runs the two separable
+                                        passes of ReflectionDenoiserNew.glsl before the colour pass */
+    int32_t reserved[3];
 } vpt_config;
 
 typedef enum vpt_denoiser {
@@ -155,7 +157,8 @@ typedef enum vpt_plane {
     VPT_PLANE_SPEC_OUT = 36,  /* ReflectionTemporalFBO: the specular indirect the colour pass reads */
     VPT_PLANE_SPEC_ACC = 37,  /* its accumulation factor (-1 with the temporal filter off) */
     VPT_PLANE_SPEC_STABLE_HIT = 38, /* its temporally stabilised hit distance */
-    VPT_PLANE_COUNT = 39
+    VPT_PLANE_SPEC_DEN = 39,  /* ReflectionDenoised_2: the spatially denoised reflection (4 ch) */
+    VPT_PLANE_COUNT = 40
 } vpt_plane;
 
 typedef enum vpt_dtype { VPT_DTYPE_F32 = 0, VPT_DTYPE_F16 = 1, VPT_DTYPE_U8 = 2, VPT_DTYPE_U16 = 3, VPT_DTYPE_I32 = 4 } vpt_dtype;
@@ -230,11 +233,12 @@ vpt_status vpt_trace_diffuse(vpt_ctx* ctx, const vpt_frame* frame);
  * and the a-trous iterations. `prev_cam` is the previous frame's camera
  * (u_PrevView / u_PrevProjection); history planes are read and written. */
 vpt_status vpt_svgf(vpt_ctx* ctx, const vpt_camera* prev_cam, const vpt_frame* frame);
-/* Reflection pass, Core/Pipeline.cpp:2998-3262: ReflectionTraceFrag.glsl,
- * the two bilateral passes over its hit distance and SpecularTemporalFilter
- * (firefly rejection; reprojection and accumulation when reflection_temporal),
+/* Reflection pass, Core/Pipeline.cpp:2998-3440: ReflectionTraceFrag.glsl,
+ * the two bilateral passes over its hit distance, SpecularTemporalFilter
+ * (firefly rejection; reprojection and accumulation when reflection_temporal)
+ * and, with reflection_denoise, the x and y passes of ReflectionDenoiserNew,
  * on the GI grid, after vpt_svgf (it reads the denoised GI): fills SPEC,
- * SPEC_HIT, SPEC_MASK, SPEC_OUT, SPEC_ACC and SPEC_STABLE_HIT. Needs
+ * SPEC_HIT, SPEC_MASK, SPEC_OUT, SPEC_ACC, SPEC_STABLE_HIT and SPEC_DEN. Needs
  * reflection_spp > 0; vpt_render_frame runs it when that is set. The
  * reflection planes are swapped with last frame's by vpt_end_frame. */
 vpt_status vpt_trace_reflections(vpt_ctx* ctx, const vpt_frame* frame);

@@ -43,7 +43,7 @@ class OParams(C.Structure):
                 ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
                 ("gi_divisor", C.c_int32), ("reflection_spp", C.c_int32), ("reflection_max_steps", C.c_int32),
                 ("reflection_shadow_max_steps", C.c_int32), ("reflection_temporal", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("reflection_denoise", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class OWorld(C.Structure):
@@ -88,6 +88,7 @@ def lib() -> C.CDLL:
         L.vpto_trace_reflection.argtypes = [P] * 13 + [C.c_int, C.c_int, P, P, P]
         L.vpto_spec_hit_blur.argtypes = [P, C.c_int, P, P, P, P]
         L.vpto_spec_temporal.argtypes = [P] * 18
+        L.vpto_spec_denoise.argtypes = [P, P, P, C.c_int] + [P] * 10
         for name in ("vpto_exp", "vpto_exp2", "vpto_log2", "vpto_sin", "vpto_cos", "vpto_half_round"):
             getattr(L, name).argtypes = [C.c_float]
             getattr(L, name).restype = C.c_float
@@ -430,6 +431,20 @@ def svgf(cam, prev_cam, config, frame, g: dict, prev_g: dict, gi: dict, hist: di
     return {"pre": pre, "temporal": tmp, "variance": var, "atrous": dens}
 
 
+def spec_denoise(world: World, cam, config, g: dict, spec_in, hit_data, frames, direction: int) -> np.ndarray:
+    """One separable pass of the reflection denoiser (direction 1: x, 0: y)."""
+    p = params(config)
+    v = gi_view(p, g["t"], g["face"], g["block"])
+    arrs = [np.ascontiguousarray(a, dtype=dt) for a, dt in
+            ((g["t"], np.float32), (g["face"], np.uint8), (g["block"], np.uint8), (v["t"], np.float32),
+             (v["face"], np.uint8), (v["block"], np.uint8), (spec_in, np.float32), (hit_data, np.float32),
+             (frames, np.float32))]
+    out = np.zeros_like(arrs[6])
+    lib().vpto_spec_denoise(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), int(direction),
+                            *[_p(a) for a in arrs], _p(out))
+    return out
+
+
 def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist: dict, prev_refl=None) -> dict:
     """One whole frame in the order of vpt_render_frame; prev_refl is last
     frame's "refl" (zero planes when None)."""
@@ -456,8 +471,12 @@ def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist:
         refl["hit"] = spec_hit_blur(p, g, refl["raw_hit"])
         prev_refl = prev_refl if prev_refl is not None else empty_reflection_history(p)
         refl.update(spec_temporal(world, cam, prev_cam, p, g, prev_g, refl, prev_refl))
-    rgb = shade(world, cam, p, frame, g["t"], g["face"], g["block"], shadow, sh, cocg, ao,
-                spec=None if refl is None else refl["out"])
+        if p.reflection_denoise:
+            hd = refl["stable"] if p.reflection_temporal else refl["hit"]
+            refl["den1"] = spec_denoise(world, cam, p, g, refl["out"], hd, refl["acc"], 1)
+            refl["den"] = spec_denoise(world, cam, p, g, refl["den1"], hd, refl["acc"], 0)
+    spec = None if refl is None else (refl["den"] if p.reflection_denoise else refl["out"])
+    rgb = shade(world, cam, p, frame, g["t"], g["face"], g["block"], shadow, sh, cocg, ao, spec=spec)
     return {"g": g, "shadow": shadow, "gi": gi, "svgf": sv, "refl": refl, "rgb": rgb}
 
 

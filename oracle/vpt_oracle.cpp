@@ -1122,6 +1122,32 @@ void vpto_atrous(const vpto_camera* cam, const vpto_params* p, const vpto_frame*
     }
 }
 
+// The PBR G-buffer's roughness / metalness (GenerateGBuffer.glsl: nearest
+// filtered, 0 for the sky, :362-363) for flat materials.
+inline float pbr_rough(const vpto_world* w, int block) {
+    return block > 0 ? material(w, std::min(block, 127)).rough : 0.0f;
+}
+inline float pbr_metal(const vpto_world* w, int block) {
+    return block > 0 ? material(w, std::min(block, 127)).metal : 0.0f;
+}
+
+// texture(u_GBufferNormals, uv): the RGB16F normal G-buffer with GL_LINEAR,
+// i.e. the face normals ((1, 1, 1) for the sky, :362) blended bilinearly.
+inline v3 gnormal_linear(const Plane8& F, v2 uv) {
+    const float x = uv.x * (float)F.W - 0.5f, y = uv.y * (float)F.H - 0.5f;
+    const float x0 = std::floor(x), y0 = std::floor(y);
+    const float ax = x - x0, ay = y - y0;
+    const int i0 = f2i(x0), j0 = f2i(y0);
+    const v3 n00 = normal_from_id(F.at(i0, j0), 1.0f), n10 = normal_from_id(F.at(i0 + 1, j0), 1.0f);
+    const v3 n01 = normal_from_id(F.at(i0, j0 + 1), 1.0f), n11 = normal_from_id(F.at(i0 + 1, j0 + 1), 1.0f);
+    auto bl = [&](float a, float b, float c, float d) {
+        const float lo = a * (1.0f - ax) + b * ax;
+        const float hi = c * (1.0f - ax) + d * ax;
+        return lo * (1.0f - ay) + hi * ay;
+    };
+    return mk3(bl(n00.x, n10.x, n01.x, n11.x), bl(n00.y, n10.y, n01.y, n11.y), bl(n00.z, n10.z, n01.z, n11.z));
+}
+
 // SpatiallyUpscaleBuffers (ColorPassFrag.glsl:535-653), which the colour pass
 // always runs (:828): a 3x3 joint-bilateral gather of the GI planes with the
 // a-trous kernel, depth weight exp(-2|dd|)^5.25 and normal weight
@@ -1174,7 +1200,7 @@ inline UpscaledGI upscale_gi(const vpto_world* w, const Plane& T, const Plane8& 
             const float kwt = kw[std::abs(x)] * kw[std::abs(y)];
             float wgt = clampf((nw * dw) * kwt, 0.0f, 1.0f);
             if (SP) {
-                const float ra = material(w, std::min(std::max(B.at(si, sj), 0), 127)).rough;
+                const float ra = pbr_rough(w, B.at(si, sj));
                 float spw = (wgt / ((std::fabs(ra - base_rough) * 12.0f) + 1.0f)) *
                             dm_pow(fmaxg(dot(na, base_n), 0.0f), 8.0f);
                 spw = fmaxg(spw, 0.00000001f);
@@ -1432,6 +1458,9 @@ void reflection_texel(const vpto_world* w, const vpto_camera* cam, const vpto_pa
     const v3 viewer = mk3(cam->position[0], cam->position[1], cam->position[2]);
     const v3 cam_pos = ray_origin(cam);
     const v3 N = normal_from_id(in.FV.at(i, j), 1.0f);
+    // NormalMappedInitial (:794): the linear normal G-buffer at the texel
+    // centre, the face normal itself on the G-buffer's grid
+    const v3 NM = gi_div(p) == 1 ? N : gnormal_linear(in.F, uv);
     const Material base = material(w, std::min(std::max(in.BV.at(i, j), 0), 127));
     const v3 I = normalize(sub(mk3(P.x, P.y, P.z), viewer));
     P.x += N.x * 0.035f;
@@ -1454,7 +1483,7 @@ void reflection_texel(const vpto_world* w, const vpto_camera* cam, const vpto_pa
     float avg_hit = 0.001f, meaningful = 0.0f, emask = 0.0f, computed_shadow = 0.0f;
     int shadow_itr = 0, total_hits = 0;
     for (int s = 0; s < spp; s++) {
-        const v3 rn = reflection_normal(N, clampf(base.rough * rbias, 0.01f, 1.0f), &rng);
+        const v3 rn = reflection_normal(NM, clampf(base.rough * rbias, 0.01f, 1.0f), &rng);
         const v3 R = reflect3(I, rn);
         const TraceResult tr = traverse(w, pos, R, p->reflection_max_steps);
         cnt->add(4, tr.steps);
@@ -1781,6 +1810,188 @@ void vpto_spec_temporal(const vpto_world* w, const vpto_camera* cam, const vpto_
             for (int c = 0; c < 4; c++) out[q * 4 + c] = storage(o_col[c], fp16);
             acc[q] = storage(o_acc, fp16);
             stable[q] = storage(o_stable, fp16);
+        }
+    }
+}
+
+// ReflectionDenoiserNew.glsl main (:140-473), one separable pass (dir 1: x,
+// 0: y) of the 33-tap Gaussian with depth, normal, luminance, normal-map and
+// roughness weights, u_RoughnessBias, u_NormalMapAware, u_HandleLobeDeviation
+// and u_AmplifyReflectionTransversalWeight on, u_DeriveFromDiffuseSH off,
+// NormalMapWeightStrength 0.75, RoughnessNormalWeightBiasStrength 1.075,
+// radius bias 0, scale 1 (Core/Pipeline.cpp:3314-3440); u_ResolutionScale
+// (ReflectionSuperSampleResolution) = 1 / gi_divisor and u_TemporalWeight =
+// TEMPORAL_SPEC. The jitter int((noise - 0.5) * 0.75) is 0 for every noise in
+// [0, 1). Taps at fractional offsets sample the full-resolution depth, face,
+// block and normal planes; the centre reads the GI-grid views.
+void vpto_spec_denoise(const vpto_world* w, const vpto_camera* cam, const vpto_params* p, int dir, const float* t,
+                       const uint8_t* face, const uint8_t* block, const float* t_view, const uint8_t* face_view,
+                       const uint8_t* block_view, const float* in, const float* hit_data, const float* frames,
+                       float* out) {
+    static const float gauss[33] = {0.004013f, 0.005554f, 0.007527f, 0.00999f,  0.012984f, 0.016524f, 0.020594f,
+                                    0.025133f, 0.030036f, 0.035151f, 0.040283f, 0.045207f, 0.049681f, 0.053463f,
+                                    0.056341f, 0.058141f, 0.058754f, 0.058141f, 0.056341f, 0.053463f, 0.049681f,
+                                    0.045207f, 0.040283f, 0.035151f, 0.030036f, 0.025133f, 0.020594f, 0.016524f,
+                                    0.012984f, 0.00999f,  0.007527f, 0.005554f, 0.004013f};
+    const int d = gi_div(p), W = p->width, H = p->height, Wg = W / d, Hg = H / d;
+    const int fp16 = p->storage;
+    const bool temporal_weight = p->reflection_temporal != 0;
+    const Plane T{t, W, H, 1}, TV{t_view, Wg, Hg, 1}, IN{in, Wg, Hg, 4};
+    const Plane8 F{face, W, H}, B{block, W, H}, FV{face_view, Wg, Hg}, BV{block_view, Wg, Hg};
+    const float texel = dir ? 1.0f / (float)Wg : 1.0f / (float)Hg;
+    const float res_scale = 1.0f / (float)d;
+    const float EPS = 0.001f;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int j = 0; j < Hg; j++) {
+        for (int i = 0; i < Wg; i++) {
+            const size_t q = (size_t)j * Wg + i;
+            const v2 uv = texcoord(i, j, Wg, Hg);
+            const v4 bp = position_fetch(cam, TV, i, j, uv);
+            const v3 bn = normal_from_id(FV.at(i, j), 1.0f);
+            const bool base_sky = bp.w < 0.0f;
+            float bc[4];
+            for (int c = 0; c < 4; c++) bc[c] = IN.at(i, j, c);
+            const float base_lum = dot(mk3(bc[0], bc[1], bc[2]), mk3(0.299f, 0.587f, 0.114f));
+            const int bblock = BV.at(i, j);
+            const float pbr_x = pbr_rough(w, bblock), pbr_y = pbr_metal(w, bblock);
+            float br = pbr_x + 0.001f;
+            const float raw_rough = br;
+            br *= mixf(1.0f, 0.91f, 1.0f);
+            const v3 nm_base = d == 1 ? bn : gnormal_linear(F, uv);
+            float hd = hit_data[q] + 0.0001f;
+            if (hd < 0.001f) hd = 1.75f;
+            else hd = dm_pow(hd, 1.0f / 1.3f);
+            if (br <= 0.25f + 0.05f) hd = clampf(hd, 0.0f, 8.0f);
+            if (br <= 0.2f) hd = clampf(hd, 0.0f, 5.5f);
+            const float shd = fmaxg(hd, 0.01f) * (raw_rough < 0.51f ? 0.5f : 0.85f);
+            const v4 vs = mat_mul4(cam->view, bp.x, bp.y, bp.z, 1.0f);
+            const float vlen = length(mk3(vs.x, vs.y, vs.z));
+            float vlw = 0.001f + vlen;
+            if (br > 0.135f) vlw = fmaxg(vlw, 0.750f);
+            else vlw = fmaxg(vlw, 3.0f);
+            if (br < 0.125f) vlw = clampf(vlw, 0.000001f, 6.0f);
+            else if (br < 0.25f) vlw = clampf(vlw, 0.000001f, 8.0f + 1.0f);
+            else if (br < 0.5f) vlw = clampf(vlw, 0.000001f, 16.0f);
+            else if (br < 0.75f) vlw = clampf(vlw, 0.000001f, 24.0f);
+            else vlw = clampf(vlw, 0.000001f, 32.0f);
+            float tc = shd / fmaxg(shd + vlw, 0.00001f);
+            if (raw_rough < 0.535f && bp.w < 50.0f) {
+                const float rr = (((raw_rough - 0.0f) / (0.535f - 0.0f)) * (1.0f - 0.0f)) + 0.0f;
+                const float te = mixf(3.5f, 2.0f, dm_pow(rr, 4.0f));
+                tc = dm_pow(tc, te + 0.8125f);
+            }
+            const float rad_e = dm_pow(1.0f - br, 1.0f / 1.4f) * 5.0f;
+            const float radius = clampf(dm_pow(mixf(1.0f * br, 1.0f, tc), rad_e), 0.0f, 1.0f);
+            const float nm_radius = 1.0f - clampf(dm_pow(mixf(1.0f * br, 1.0f, tc), rad_e), 0.0f, 1.0f);
+            int er = f2i(std::floor(radius * 15.0f));
+            er = std::min(std::max(er, 1), 15);
+            if (br > 0.897511f) er = 15;
+            const int jitter = 0;
+            float scale = mixf(1.0f, 2.0f, clampf(res_scale, 0.0000001f, 1.0f)) + 0.5f;
+            int rbias = 0;
+            if (pbr_y > 0.1f - EPS && br > 0.4f - EPS) rbias += 2;
+            er = std::min(std::max(er + rbias + 0, 1), 15);
+            if (raw_rough >= 0.5f - 0.01f) er += 1;
+            scale *= 1.0f;
+            float tw_t = 0.0f, afc = 0.01f;
+            if (temporal_weight) {
+                const float af = frames[q];
+                afc = af < -0.1f ? 0.0f : (1.0f - af);
+                afc = clampf(afc, 0.000001f, 1.0f);
+                tw_t = clampf(afc * 0.85f, 0.0f, 1.0f);
+                float flt = (float)er;
+                flt = mixf(flt, flt + 2.0f, afc * 1.05f);
+                er = f2i(flt);
+            }
+            float hf_e = (64.0f * 0.750f) * 1.350f;
+            hf_e *= dm_pow(nm_radius, 1.0f / 1.33f);
+            float hf_add = mixf(0.0f, 0.005f, br > 0.45f ? 1.0f : 0.0f);
+            hf_add += mixf(0.0f, 0.0125f, br > 0.525f ? 1.0f : 0.0f);
+            hf_add += mixf(0.0f, 0.022f, br > 0.625f ? 1.0f : 0.0f);
+            hf_add += mixf(0.0f, 0.026f, br > 0.725f ? 1.0f : 0.0f);
+            hf_add += mixf(0.0f, 0.031f, br > 0.75f ? 1.0f : 0.0f);
+            er = std::min(std::max(er, 1), 15);
+            float fc[4] = {0.0f, 0.0f, 0.0f, 0.0f}, tw = 0.0f;
+            for (int s = -er; s <= er; s++) {
+                const float so = (float)s;
+                v2 sc = dir ? v2{uv.x + ((so * scale) * texel), uv.y} : v2{uv.x, uv.y + ((so * scale) * texel)};
+                sc.x += ((float)jitter * texel) * 0.75f;
+                sc.y += ((float)jitter * texel) * 0.75f;
+                const float bias = 0.01f;
+                if (!(sc.x > 0.0f + bias && sc.x < 1.0f - bias && sc.y > 0.0f + bias && sc.y < 1.0f - bias)) continue;
+                // the centre tap is the texel itself; the others fall between texels
+                float sdepth, sd[4];
+                int sface, sblock;
+                v3 nm_at;
+                if (s == 0) {
+                    sdepth = TV.at(i, j, 0);
+                    sface = FV.at(i, j);
+                    sblock = bblock;
+                    for (int c = 0; c < 4; c++) sd[c] = bc[c];
+                    nm_at = nm_base;
+                } else {
+                    T.linear(sc, &sdepth);
+                    sface = F.nearest(sc);
+                    sblock = B.nearest(sc);
+                    IN.linear(sc, sd);
+                    nm_at = gnormal_linear(F, sc);
+                }
+                const bool sample_sky = sdepth < 0.0f;
+                if (sample_sky != base_sky) continue;
+                const float dd = std::fabs(sdepth - bp.w) * 1.5f;
+                const float dw = dm_pow(dm_exp(-dd), 2.0f);
+                const v3 sn = normal_from_id(sface, 1.0f);
+                const float nw = dm_pow(fmaxg(dot(bn, sn), 0.00000000001f), 32.0f);
+                float lw = 1.0f;
+                const float srough = pbr_rough(w, sblock);
+                const bool too_rough = srough >= 0.89f;
+                if (!too_rough) {
+                    const float luma = dot(mk3(sd[0], sd[1], sd[2]), mk3(0.299f, 0.587f, 0.114f));
+                    float le = 1.0f / std::fabs(luma - base_lum);
+                    le = dm_pow(le, 1.7f);
+                    const float lwe = mixf(0.001f, 8.0f, dm_pow(srough, 16.0f));
+                    lw = dm_pow(le, lwe + 0.8f);
+                    lw = clampf(lw, 0.0000000001f, 1.0f);
+                    lw = mixf(lw, 1.0f, tw_t);
+                    lw = clampf(lw, 0.0000000001f, 1.0f);
+                }
+                float hfw = 1.0f;
+                if (!too_rough && br < 0.8f && afc <= ((0.185f + 0.001f) + 0.001f) + 0.0001f) {
+                    const float angle = dot(nm_at, nm_base);
+                    hfw = dm_pow(clampf(angle, 0.00000001f, 1.0f), hf_e);
+                    hfw = clampf(hfw + ((hf_add * 1.075f) * 1.4f), 0.00000000001f, 1.0f);
+                }
+                const float re = std::fabs(srough - br);
+                float rtw = 1.0f / re;
+                rtw = dm_pow(rtw, 12.0f);
+                rtw = clampf(rtw, 0.00000000001f, 1.0f);
+                const float kw = gauss[std::min(std::max(16 + s, 0), 32)];
+                float cw = 1.0f;
+                cw *= dw;
+                cw *= nw;
+                cw *= hfw;
+                cw *= lw;
+                cw *= rtw;
+                cw *= kw;
+                cw = clampf(cw, 0.000000001f, 1.0f);
+                for (int c = 0; c < 4; c++) fc[c] += sd[c] * cw;
+                tw += cw;
+            }
+            float o[4];
+            if (tw > 0.001f) {
+                for (int c = 0; c < 4; c++) fc[c] = fc[c] / tw;
+                float smf = 1.0f;
+                if (br <= 0.1f + 0.007f) {
+                    smf = br * 16.0f;
+                    smf = 1.0f - smf;
+                    smf = dm_pow(smf, 4.0f);
+                    smf = clampf(smf, 0.1f, 0.999f);
+                }
+                for (int c = 0; c < 4; c++) o[c] = mixf(bc[c], fc[c], smf);
+            } else {
+                for (int c = 0; c < 4; c++) o[c] = bc[c];
+            }
+            for (int c = 0; c < 4; c++) out[q * 4 + c] = storage(o[c], fp16);
         }
     }
 }

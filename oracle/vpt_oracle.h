@@ -70,7 +70,8 @@ typedef struct vpto_params {
     int32_t reflection_max_steps;
     int32_t reflection_shadow_max_steps;
     int32_t reflection_temporal;  /* TEMPORAL_SPEC */
-    int32_t reserved[4];
+    int32_t reflection_denoise;   /* DenoiseReflections */
+    int32_t reserved[3];
 } vpto_params;
 
 typedef struct vpto_world {
@@ -188,6 +189,15 @@ void vpto_spec_temporal(const vpto_world* w, const vpto_camera* cam, const vpto_
                         const uint8_t* block_view, const float* prev_t, const uint8_t* prev_face,
                         const float* spec, const float* hit, const float* mask, const float* prev_out,
                         const float* prev_hit, const float* prev_stable, float* out, float* acc, float* stable);
+
+/* ReflectionDenoiserNew.glsl, one separable pass (dir 1: x, 0: y): t / face
+ * / block the full-resolution G-buffer, the views its GI-grid reading, in the
+ * reflection (4 ch), hit_data the (stabilised) hit distance, frames the
+ * temporal accumulation factor; all but the G-buffer on the GI grid. */
+void vpto_spec_denoise(const vpto_world* w, const vpto_camera* cam, const vpto_params* p, int dir, const float* t,
+                       const uint8_t* face, const uint8_t* block, const float* t_view, const uint8_t* face_view,
+                       const uint8_t* block_view, const float* in, const float* hit_data, const float* frames,
+                       float* out);
 
 /* ColorPassFrag.glsl main: joint-bilateral GI upscale, direct GGX +
  * indirect-diffuse combine, flat materials. t / face / block / shadow at the

@@ -1,6 +1,7 @@
 """The reflection pass (ReflectionTraceFrag.glsl, the two bilateral passes
-over its hit distance and SpecularTemporalFilter.glsl with TEMPORAL_SPEC on
-or off; DenoiseReflections off) and the specular indirect it feeds into the
+over its hit distance, SpecularTemporalFilter.glsl with TEMPORAL_SPEC on or
+off, the two separable passes of ReflectionDenoiserNew.glsl with
+DenoiseReflections on or off) and the specular indirect it feeds into the
 colour pass (ColorPassFrag.glsl :595-603, :901-909). Every plane is
 bit-identical to the oracle.
 """
@@ -74,6 +75,22 @@ def test_oracle_reflection_temporal_accumulates(vpt, oracle):
     assert d_old < d_new
 
 
+def test_oracle_reflection_denoiser_smooths(vpt, oracle):
+    """The separable denoiser keeps sky texels and the mean of the hit
+    texels' radiance (within 10%) and lowers its local variation."""
+    sc = scene_inputs(vpt, oracle)
+    cfg = vpt.default_config(width=W, height=H, primary_max_steps=256, reflection_spp=1, reflection_temporal=0)
+    cam = sc["cams"][0]
+    prev_g, hist = oracle.empty_history(H, W)
+    ref = oracle.render_frame(sc["world"], cam, cam, cfg, vpt.default_frame(frame_index=0, seed=3), prev_g, hist)
+    r, hit = ref["refl"], ref["g"]["t"] > 0
+    assert (r["den"][~hit] == r["out"][~hit]).all()
+    a, b = r["out"][..., :3], r["den"][..., :3]
+    assert abs(b[hit].mean() - a[hit].mean()) < 0.1 * a[hit].mean()
+    both = hit[:, 1:] & hit[:, :-1]
+    assert np.abs(np.diff(b, axis=1))[both].mean() < np.abs(np.diff(a, axis=1))[both].mean()
+
+
 def test_oracle_reflection_counts_rays(vpt, oracle):
     sc = scene_inputs(vpt, oracle)
     cfg = vpt.default_config(width=W, height=H, primary_max_steps=256, reflection_spp=3)
@@ -89,17 +106,17 @@ def test_oracle_reflection_counts_rays(vpt, oracle):
 
 # ------------------------------------------------------------------ GPU --
 @pytest.mark.gpu
-@pytest.mark.parametrize("d,storage,denoiser,temporal", [(1, 0, 0, 1), (2, 0, 0, 1), (1, 1, 0, 1), (4, 1, 0, 1),
-                                                          (1, 0, 1, 1), (1, 0, 0, 0)],
-                         ids=["d1-f32", "d2-f32", "d1-f16", "d4-f16", "d1-plain", "d1-no-temporal"])
-def test_reflection_planes_bit_exact(vpt, oracle, d, storage, denoiser, temporal, gpu):
+@pytest.mark.parametrize("d,storage,denoiser,temporal,rden", [
+    (1, 0, 0, 1, 1), (2, 0, 0, 1, 1), (1, 1, 0, 1, 1), (4, 1, 0, 1, 1), (1, 0, 1, 1, 1), (1, 0, 0, 0, 1),
+    (2, 0, 0, 1, 0)], ids=["d1-f32", "d2-f32", "d1-f16", "d4-f16", "d1-plain", "d1-no-temporal", "d2-no-denoise"])
+def test_reflection_planes_bit_exact(vpt, oracle, d, storage, denoiser, temporal, rden, gpu):
     sc = scene_inputs(vpt, oracle)
     world = sc["world"]
     X, Z = DIMS[0], DIMS[2]
     yaw, pitch = vpt.seeded_pose(1)
     cams = sc["cams"] + [vpt.camera_from_pose((X / 2 + 1.1, 58.1, Z / 2 - 0.9), yaw + 3.5, pitch + 1.5, 90.0, W / H)]
     ctx = vpt.Context(width=W, height=H, primary_max_steps=256, storage=storage, gi_divisor=d, reflection_spp=2,
-                      denoiser=denoiser, reflection_temporal=temporal)
+                      denoiser=denoiser, reflection_temporal=temporal, reflection_denoise=rden)
     ctx.upload_world(sc["vox"])
     ctx.set_block_table(sc["blocks"])
     ctx.build_df()
@@ -127,6 +144,8 @@ def test_reflection_planes_bit_exact(vpt, oracle, d, storage, denoiser, temporal
         assert_same(ctx.read_plane("SPEC_OUT"), r["out"], f"{d} frame {fi} temporal colour")
         assert_same(ctx.read_plane("SPEC_ACC")[..., 0], r["acc"], f"{d} frame {fi} accumulation")
         assert_same(ctx.read_plane("SPEC_STABLE_HIT")[..., 0], r["stable"], f"{d} frame {fi} stable hit")
+        if rden:
+            assert_same(ctx.read_plane("SPEC_DEN"), r["den"], f"{d} frame {fi} denoised")
         assert_same(rgb, ref["rgb"], f"{d} frame {fi} colour")
         assert stats["rays"] == cnt.rays and stats["steps"] == cnt.steps
         if temporal and fi > 0:

@@ -41,7 +41,7 @@ PLANES = [
     "PREV_T", "PREV_FACE", "PREV_BLOCK",
     "VAR_SH", "VAR_COCG", "VAR_VARIANCE",
     "DEN_SH", "DEN_COCG", "DEN_VARIANCE", "DEN_AOSKY",
-    "COLOR", "SPEC", "SPEC_HIT", "SPEC_MASK", "SPEC_OUT", "SPEC_ACC", "SPEC_STABLE_HIT",
+    "COLOR", "SPEC", "SPEC_HIT", "SPEC_MASK", "SPEC_OUT", "SPEC_ACC", "SPEC_STABLE_HIT", "SPEC_DEN",
 ]
 PLANE = {name: i for i, name in enumerate(PLANES)}
 PASSES = ["primary", "shadow", "diffuse", "spatial_initial", "temporal", "variance", "atrous", "shade", "trace_frame",
@@ -59,7 +59,7 @@ class Config(C.Structure):
                 ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
                 ("gi_divisor", C.c_int32), ("reflection_spp", C.c_int32), ("reflection_max_steps", C.c_int32),
                 ("reflection_shadow_max_steps", C.c_int32), ("reflection_temporal", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("reflection_denoise", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class Camera(C.Structure):

@@ -48,7 +48,7 @@ PlaneMeta plane_meta(int plane) {
         case VPT_PLANE_GI_LUMA: case VPT_PLANE_PRE_LUMA: case VPT_PLANE_VAR_VARIANCE:
         case VPT_PLANE_DEN_VARIANCE: return {1, 1, 0, 1};
         case VPT_PLANE_COLOR: return {3, 1, 0, 0};
-        case VPT_PLANE_SPEC: case VPT_PLANE_SPEC_OUT: return {4, 1, 0, 1};
+        case VPT_PLANE_SPEC: case VPT_PLANE_SPEC_OUT: case VPT_PLANE_SPEC_DEN: return {4, 1, 0, 1};
         case VPT_PLANE_SPEC_HIT: case VPT_PLANE_SPEC_MASK: case VPT_PLANE_SPEC_ACC:
         case VPT_PLANE_SPEC_STABLE_HIT: return {1, 1, 0, 1};
         default: return {0, 0, -1, 0};
@@ -106,6 +106,8 @@ struct vpt_ctx {
     void* rstable[2] = {};
     void* racc = nullptr;
     void* rhit_tmp = nullptr;
+    void* rden1 = nullptr;   // x pass of the reflection denoiser
+    void* rden = nullptr;    // y pass: what the colour pass reads with reflection_denoise
     int cur = 0;        // index of this frame's G-buffer / temporal output
     int den_last = 0;   // den set holding the last a-trous output
     // cameras
@@ -231,6 +233,7 @@ void* plane_ptr(vpt_ctx* c, int plane) {
         case VPT_PLANE_SPEC_OUT: return c->rout[cur];
         case VPT_PLANE_SPEC_ACC: return c->racc;
         case VPT_PLANE_SPEC_STABLE_HIT: return c->rstable[cur];
+        case VPT_PLANE_SPEC_DEN: return c->rden;
         default: return nullptr;
     }
 }
@@ -288,6 +291,8 @@ vpt_status alloc_planes(vpt_ctx* c) {
         A(c->rmask, n * es);
         A(c->racc, n * es);
         A(c->rhit_tmp, n * es);
+        A(c->rden1, n * 4 * es);
+        A(c->rden, n * 4 * es);
         for (int k = 0; k < 2; k++) {
             A(c->rhit[k], n * es);
             A(c->rout[k], n * 4 * es);
@@ -409,6 +414,7 @@ vpt_status vpt_default_config(vpt_config* cfg) {
     cfg->reflection_max_steps = 64;
     cfg->reflection_shadow_max_steps = 150;
     cfg->reflection_temporal = 1;
+    cfg->reflection_denoise = 1;
     cfg->color_phi_bias = 3.325f;
     cfg->device = 0;
     return VPT_OK;
@@ -978,8 +984,27 @@ vpt_status reflection_run(vpt_ctx* c, const vpt_frame* f) {
                         c->view[0], (const uint8_t*)c->view[1], (const uint8_t*)c->view[2], c->gbuf[prv][GB_T],
                         (const uint8_t*)c->gbuf[prv][GB_FACE], c->rspec, c->rhit[cur], c->rmask, c->rout[prv],
                         c->rhit[prv], c->rstable[prv], c->rout[cur], c->racc, c->rstable[cur], c->stream));
-    pass_end(c, VPT_PASS_REFLECTION);
     c->launches += 4;
+    if (c->cfg.reflection_denoise) {
+        // ReflectionDenoiserNew, x then y (:3312-3440); the hit distance is the
+        // stabilised one with the temporal filter on, else the blurred trace's
+        SpecDenoiseArgs da;
+        memcpy(da.view, cm.view, sizeof da.view);
+        da.res_scale = 1.0f / (float)c->gd;
+        da.temporal_weight = ta.temporal;
+        const void* hd = ta.temporal ? c->rstable[cur] : c->rhit[cur];
+        const uint8_t* gface = (const uint8_t*)c->gbuf[cur][GB_FACE];
+        const uint8_t* gblock = (const uint8_t*)c->gbuf[cur][GB_BLOCK];
+        for (int pass = 0; pass < 2; pass++) {
+            da.dir = pass == 0 ? 1 : 0;
+            CK(c, spec_denoise(world_view(c), cam_view(cm), da, c->cfg.width, c->cfg.height, c->gw, c->gh, c->fp16,
+                               c->gbuf[cur][GB_T], gface, gblock, c->view[0], (const uint8_t*)c->view[1],
+                               (const uint8_t*)c->view[2], pass == 0 ? c->rout[cur] : c->rden1, hd, c->racc,
+                               pass == 0 ? c->rden1 : c->rden, c->stream));
+        }
+        c->launches += 2;
+    }
+    pass_end(c, VPT_PASS_REFLECTION);
     return VPT_OK;
 }
 
@@ -1010,7 +1035,9 @@ vpt_status shade_run(vpt_ctx* c, const vpt_frame* f, int source, void* out = nul
     denoised_gi(c, &sh, &cocg, &ao);
     // the specular indirect of this frame's reflection pass (the learned
     // path's inputs, sources 1 and 2, are shaded without it)
-    const void* spec = (c->cfg.reflection_spp > 0 && source == 0) ? c->rout[c->cur] : nullptr;
+    const void* spec = (c->cfg.reflection_spp > 0 && source == 0)
+                           ? (c->cfg.reflection_denoise ? c->rden : c->rout[c->cur])
+                           : nullptr;
     if (source == 1) {
         sh = c->hist[c->cur][HI_SH];
         cocg = c->hist[c->cur][HI_COCG];

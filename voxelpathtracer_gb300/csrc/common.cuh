@@ -357,6 +357,25 @@ __device__ __forceinline__ Material material(const WorldView& w, int id) {
     return m;
 }
 
+// The PBR G-buffer's roughness / metalness for flat materials
+// (GenerateGBuffer.glsl: nearest filtered, 0 for the sky, :362-363).
+__device__ __forceinline__ float pbr_rough(const WorldView& w, int block) {
+    return block > 0 ? material(w, min(block, 127)).rough : 0.0f;
+}
+__device__ __forceinline__ float pbr_metal(const WorldView& w, int block) {
+    return block > 0 ? material(w, min(block, 127)).metal : 0.0f;
+}
+
+// texture(u_GBufferNormals, uv): the RGB16F normal G-buffer with GL_LINEAR,
+// i.e. the face normals ((1, 1, 1) for the sky) blended bilinearly.
+__device__ __forceinline__ v3 gnormal_linear(const uint8_t* face, int W, int H, v2 uv) {
+    const Bilin b = bilin(uv, W, H);
+    const v3 n00 = normal_from_id(__ldg(face + b.o00), 1.0f), n10 = normal_from_id(__ldg(face + b.o10), 1.0f);
+    const v3 n01 = normal_from_id(__ldg(face + b.o01), 1.0f), n11 = normal_from_id(__ldg(face + b.o11), 1.0f);
+    return mk3(blend(b, n00.x, n10.x, n01.x, n11.x), blend(b, n00.y, n10.y, n01.y, n11.y),
+               blend(b, n00.z, n10.z, n01.z, n11.z));
+}
+
 // Per-frame constants of DiffuseRayTraceFrag main (:832-839), computed once on the host.
 struct GILighting {
     float light_color[3];

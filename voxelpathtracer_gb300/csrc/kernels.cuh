@@ -265,6 +265,16 @@ struct SpecTemporalArgs {
     float cur_pos[3], prev_pos[3];
     int temporal;               // TEMPORAL_SPEC
 };
+struct SpecDenoiseArgs {
+    float view[16];             // u_View
+    float res_scale;            // u_ResolutionScale (ReflectionSuperSampleResolution) = 1 / gi_divisor
+    int dir;                    // u_Dir: 1 = x, 0 = y
+    int temporal_weight;        // u_TemporalWeight && TEMPORAL_SPEC
+};
+cudaError_t spec_denoise(const WorldView& w, const CamView& cam, const SpecDenoiseArgs& a, int W, int H, int Wg,
+                         int Hg, int fp16, const void* t, const uint8_t* face, const uint8_t* block, const void* tv,
+                         const uint8_t* fv, const uint8_t* bv, const void* in, const void* hit_data,
+                         const void* frames, void* out, cudaStream_t s);
 cudaError_t spec_temporal(const WorldView& w, const CamView& cam, const SpecTemporalArgs& a, int W, int H, int Wg,
                           int Hg, int fp16, const void* tv, const uint8_t* fv, const uint8_t* bv, const void* prev_t,
                           const uint8_t* prev_face, const void* spec, const void* hit, const void* mask,

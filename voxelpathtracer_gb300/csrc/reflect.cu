@@ -6,8 +6,8 @@
 // (albedo, roughness, metalness, emissive flag of the block; AO 1; the face
 // normal as the normal map), PCG random numbers instead of hash2 / blue
 // noise, the analytic sky, no LPV, cloud reflections or player, no jitter.
-// The spatial reflection denoiser is off (DenoiseReflections false), so the
-// temporal output is what the colour pass reads.
+// With DenoiseReflections the x and y passes of ReflectionDenoiserNew.glsl
+// follow; the colour pass reads their output (or the temporal output).
 #include "pixel_passes.cuh"
 
 namespace vpt {
@@ -139,6 +139,9 @@ __global__ void __launch_bounds__(256) k_trace_reflection(WorldView w, CamView c
             const v3 viewer = mk3(a.viewer[0], a.viewer[1], a.viewer[2]);
             const v3 cam_pos = ray_origin(cam);
             const v3 N = normal_from_id(__ldg(fv + q), 1.0f);
+            // NormalMappedInitial (:794): the linear normal G-buffer at the
+            // texel centre, the face normal itself on the G-buffer's grid
+            const v3 NM = (W == Wg && H == Hg) ? N : gnormal_linear(face, W, H, uv);
             const Material base = material(w, min(max((int)__ldg(bv + q), 0), 127));
             const v3 I = normalize(sub(mk3(P.x, P.y, P.z), viewer));
             P.x += N.x * 0.035f;
@@ -158,7 +161,7 @@ __global__ void __launch_bounds__(256) k_trace_reflection(WorldView w, CamView c
             int shadow_itr = 0, total_hits = 0;
 #pragma unroll 1
             for (int s = 0; s < spp; s++) {
-                const v3 rn = reflection_normal(N, clampf(base.rough * rbias, 0.01f, 1.0f), &rng);
+                const v3 rn = reflection_normal(NM, clampf(base.rough * rbias, 0.01f, 1.0f), &rng);
                 const v3 R = reflect3(I, rn);
                 const TraceResult tr = traverse<0>(w, pos, R, a.max_steps);
                 nr += 1;
@@ -448,6 +451,188 @@ __global__ void __launch_bounds__(256) k_spec_temporal(WorldView w, CamView cam,
     st(stable + q, o_stable);
 }
 
+__constant__ float kGauss33[33] = {0.004013f, 0.005554f, 0.007527f, 0.00999f,  0.012984f, 0.016524f, 0.020594f,
+                                   0.025133f, 0.030036f, 0.035151f, 0.040283f, 0.045207f, 0.049681f, 0.053463f,
+                                   0.056341f, 0.058141f, 0.058754f, 0.058141f, 0.056341f, 0.053463f, 0.049681f,
+                                   0.045207f, 0.040283f, 0.035151f, 0.030036f, 0.025133f, 0.020594f, 0.016524f,
+                                   0.012984f, 0.00999f,  0.007527f, 0.005554f, 0.004013f};
+
+// ReflectionDenoiserNew.glsl main (:140-473), one separable pass (dir 1: x,
+// 0: y) of the 33-tap Gaussian with depth, normal, luminance, normal-map and
+// roughness weights and the settings of Core/Pipeline.cpp:3314-3440
+// (u_ResolutionScale = 1 / gi_divisor, u_TemporalWeight = TEMPORAL_SPEC; the
+// jitter int((noise - 0.5) * 0.75) is 0). Taps at fractional offsets sample
+// the full-resolution depth, face, block and normal planes; the centre tap
+// reads the GI-grid views.
+template <typename S>
+__global__ void __launch_bounds__(256) k_spec_denoise(WorldView w, CamView cam, SpecDenoiseArgs a, int W, int H,
+                                                      int Wg, int Hg, const S* t, const uint8_t* face,
+                                                      const uint8_t* block, const S* tv, const uint8_t* fv,
+                                                      const uint8_t* bv, const S* in, const S* hit_data,
+                                                      const S* frames, S* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= Wg || j >= Hg) return;
+    const size_t q = (size_t)j * Wg + i;
+    const v2 uv = texcoord(i, j, Wg, Hg);
+    const Plane<S, 1> TV{tv, Wg, Hg}, T{t, W, H};
+    const Plane8 F{face, W, H}, B{block, W, H};
+    const v4 bp = position_fetch(cam, TV, i, j, uv);
+    const v3 bn = normal_from_id(__ldg(fv + q), 1.0f);
+    const bool base_sky = bp.w < 0.0f;
+    const float4 bc = ld4(in + 4 * q);
+    const float base_lum = dot(mk3(bc.x, bc.y, bc.z), mk3(0.299f, 0.587f, 0.114f));
+    const int bblock = __ldg(bv + q);
+    const float pbr_x = pbr_rough(w, bblock), pbr_y = pbr_metal(w, bblock);
+    float br = pbr_x + 0.001f;
+    const float raw_rough = br;
+    br *= mixf(1.0f, 0.91f, 1.0f);
+    const bool same_grid = W == Wg && H == Hg;
+    const v3 nm_base = same_grid ? bn : gnormal_linear(face, W, H, uv);
+    float hd = ld(hit_data + q) + 0.0001f;
+    if (hd < 0.001f) hd = 1.75f;
+    else hd = dpow(hd, 1.0f / 1.3f);
+    if (br <= 0.25f + 0.05f) hd = clampf(hd, 0.0f, 8.0f);
+    if (br <= 0.2f) hd = clampf(hd, 0.0f, 5.5f);
+    const float shd = fmaxf(hd, 0.01f) * (raw_rough < 0.51f ? 0.5f : 0.85f);
+    const v4 vs = mat_mul4(a.view, bp.x, bp.y, bp.z, 1.0f);
+    const float vlen = length(mk3(vs.x, vs.y, vs.z));
+    float vlw = 0.001f + vlen;
+    if (br > 0.135f) vlw = fmaxf(vlw, 0.750f);
+    else vlw = fmaxf(vlw, 3.0f);
+    if (br < 0.125f) vlw = clampf(vlw, 0.000001f, 6.0f);
+    else if (br < 0.25f) vlw = clampf(vlw, 0.000001f, 8.0f + 1.0f);
+    else if (br < 0.5f) vlw = clampf(vlw, 0.000001f, 16.0f);
+    else if (br < 0.75f) vlw = clampf(vlw, 0.000001f, 24.0f);
+    else vlw = clampf(vlw, 0.000001f, 32.0f);
+    float tc = shd / fmaxf(shd + vlw, 0.00001f);
+    if (raw_rough < 0.535f && bp.w < 50.0f) {
+        const float rr = (((raw_rough - 0.0f) / (0.535f - 0.0f)) * (1.0f - 0.0f)) + 0.0f;
+        const float te = mixf(3.5f, 2.0f, dpow(rr, 4.0f));
+        tc = dpow(tc, te + 0.8125f);
+    }
+    const float rad_e = dpow(1.0f - br, 1.0f / 1.4f) * 5.0f;
+    const float radius = clampf(dpow(mixf(1.0f * br, 1.0f, tc), rad_e), 0.0f, 1.0f);
+    const float nm_radius = 1.0f - clampf(dpow(mixf(1.0f * br, 1.0f, tc), rad_e), 0.0f, 1.0f);
+    int er = f2i_floor(radius * 15.0f);
+    er = min(max(er, 1), 15);
+    if (br > 0.897511f) er = 15;
+    const int jitter = 0;
+    float scale = mixf(1.0f, 2.0f, clampf(a.res_scale, 0.0000001f, 1.0f)) + 0.5f;
+    const float EPS = 0.001f;
+    int rbias = 0;
+    if (pbr_y > 0.1f - EPS && br > 0.4f - EPS) rbias += 2;
+    er = min(max(er + rbias + 0, 1), 15);
+    if (raw_rough >= 0.5f - 0.01f) er += 1;
+    scale *= 1.0f;
+    float tw_t = 0.0f, afc = 0.01f;
+    if (a.temporal_weight) {
+        const float af = ld(frames + q);
+        afc = af < -0.1f ? 0.0f : (1.0f - af);
+        afc = clampf(afc, 0.000001f, 1.0f);
+        tw_t = clampf(afc * 0.85f, 0.0f, 1.0f);
+        float flt = (float)er;
+        flt = mixf(flt, flt + 2.0f, afc * 1.05f);
+        er = f2i(flt);
+    }
+    float hf_e = (64.0f * 0.750f) * 1.350f;
+    hf_e *= dpow(nm_radius, 1.0f / 1.33f);
+    float hf_add = mixf(0.0f, 0.005f, br > 0.45f ? 1.0f : 0.0f);
+    hf_add += mixf(0.0f, 0.0125f, br > 0.525f ? 1.0f : 0.0f);
+    hf_add += mixf(0.0f, 0.022f, br > 0.625f ? 1.0f : 0.0f);
+    hf_add += mixf(0.0f, 0.026f, br > 0.725f ? 1.0f : 0.0f);
+    hf_add += mixf(0.0f, 0.031f, br > 0.75f ? 1.0f : 0.0f);
+    er = min(max(er, 1), 15);
+    const float texel = a.dir ? 1.0f / (float)Wg : 1.0f / (float)Hg;
+    const float hf_gate = ((0.185f + 0.001f) + 0.001f) + 0.0001f;
+    float fc[4] = {0.0f, 0.0f, 0.0f, 0.0f}, tw = 0.0f;
+#pragma unroll 1
+    for (int s = -er; s <= er; s++) {
+        const float so = (float)s;
+        v2 sc = a.dir ? mk2(uv.x + ((so * scale) * texel), uv.y) : mk2(uv.x, uv.y + ((so * scale) * texel));
+        sc.x += ((float)jitter * texel) * 0.75f;
+        sc.y += ((float)jitter * texel) * 0.75f;
+        const float bias = 0.01f;
+        if (!(sc.x > 0.0f + bias && sc.x < 1.0f - bias && sc.y > 0.0f + bias && sc.y < 1.0f - bias)) continue;
+        float sdepth;
+        float4 sd;
+        int sface, sblock;
+        v3 nm_at;
+        if (s == 0) {
+            sdepth = TV.at_in(i, j, 0);
+            sface = __ldg(fv + q);
+            sblock = bblock;
+            sd = bc;
+            nm_at = nm_base;
+        } else {
+            sdepth = bl1(t, bilin(sc, W, H));
+            sface = F.nearest(sc);
+            sblock = B.nearest(sc);
+            sd = bl4(in, bilin(sc, Wg, Hg));
+            nm_at = gnormal_linear(face, W, H, sc);
+        }
+        const bool sample_sky = sdepth < 0.0f;
+        if (sample_sky != base_sky) continue;
+        const float dd = fabsf(sdepth - bp.w) * 1.5f;
+        const float dw = dpow(dexp(-dd), 2.0f);
+        const v3 sn = normal_from_id(sface, 1.0f);
+        const float nw = dpow(fmaxf(dot(bn, sn), 0.00000000001f), 32.0f);
+        float lw = 1.0f;
+        const float srough = pbr_rough(w, sblock);
+        const bool too_rough = srough >= 0.89f;
+        if (!too_rough) {
+            const float luma = dot(mk3(sd.x, sd.y, sd.z), mk3(0.299f, 0.587f, 0.114f));
+            float le = 1.0f / fabsf(luma - base_lum);
+            le = dpow(le, 1.7f);
+            const float lwe = mixf(0.001f, 8.0f, dpow(srough, 16.0f));
+            lw = dpow(le, lwe + 0.8f);
+            lw = clampf(lw, 0.0000000001f, 1.0f);
+            lw = mixf(lw, 1.0f, tw_t);
+            lw = clampf(lw, 0.0000000001f, 1.0f);
+        }
+        float hfw = 1.0f;
+        if (!too_rough && br < 0.8f && afc <= hf_gate) {
+            const float angle = dot(nm_at, nm_base);
+            hfw = dpow(clampf(angle, 0.00000001f, 1.0f), hf_e);
+            hfw = clampf(hfw + ((hf_add * 1.075f) * 1.4f), 0.00000000001f, 1.0f);
+        }
+        const float re = fabsf(srough - br);
+        float rtw = 1.0f / re;
+        rtw = dpow(rtw, 12.0f);
+        rtw = clampf(rtw, 0.00000000001f, 1.0f);
+        const float kw = kGauss33[min(max(16 + s, 0), 32)];
+        float cw = 1.0f;
+        cw *= dw;
+        cw *= nw;
+        cw *= hfw;
+        cw *= lw;
+        cw *= rtw;
+        cw *= kw;
+        cw = clampf(cw, 0.000000001f, 1.0f);
+        fc[0] += sd.x * cw;
+        fc[1] += sd.y * cw;
+        fc[2] += sd.z * cw;
+        fc[3] += sd.w * cw;
+        tw += cw;
+    }
+    const float bcv[4] = {bc.x, bc.y, bc.z, bc.w};
+    float o[4];
+    if (tw > 0.001f) {
+        for (int c = 0; c < 4; c++) fc[c] = fc[c] / tw;
+        float smf = 1.0f;
+        if (br <= 0.1f + 0.007f) {
+            smf = br * 16.0f;
+            smf = 1.0f - smf;
+            smf = dpow(smf, 4.0f);
+            smf = clampf(smf, 0.1f, 0.999f);
+        }
+        for (int c = 0; c < 4; c++) o[c] = mixf(bcv[c], fc[c], smf);
+    } else {
+        for (int c = 0; c < 4; c++) o[c] = bcv[c];
+    }
+    st4(out + 4 * q, o[0], o[1], o[2], o[3]);
+}
+
 }  // namespace
 
 cudaError_t trace_reflection(const WorldView& w, const CamView& cam, int W, int H, int Wg, int Hg, int fp16,
@@ -495,6 +680,22 @@ cudaError_t spec_temporal(const WorldView& w, const CamView& cam, const SpecTemp
             w, cam, a, W, H, Wg, Hg, (const float*)tv, fv, bv, (const float*)prev_t, prev_face, (const float*)spec,
             (const float*)hit, (const float*)mask, (const float*)prev_out, (const float*)prev_hit,
             (const float*)prev_stable, (float*)out, (float*)acc, (float*)stable);
+    return cudaGetLastError();
+}
+
+cudaError_t spec_denoise(const WorldView& w, const CamView& cam, const SpecDenoiseArgs& a, int W, int H, int Wg,
+                         int Hg, int fp16, const void* t, const uint8_t* face, const uint8_t* block, const void* tv,
+                         const uint8_t* fv, const uint8_t* bv, const void* in, const void* hit_data,
+                         const void* frames, void* out, cudaStream_t s) {
+    const dim3 grid((unsigned)((Wg + 31) / 32), (unsigned)((Hg + 7) / 8)), blk(32, 8);
+    if (fp16)
+        k_spec_denoise<__half><<<grid, blk, 0, s>>>(w, cam, a, W, H, Wg, Hg, (const __half*)t, face, block,
+                                                    (const __half*)tv, fv, bv, (const __half*)in,
+                                                    (const __half*)hit_data, (const __half*)frames, (__half*)out);
+    else
+        k_spec_denoise<float><<<grid, blk, 0, s>>>(w, cam, a, W, H, Wg, Hg, (const float*)t, face, block,
+                                                   (const float*)tv, fv, bv, (const float*)in,
+                                                   (const float*)hit_data, (const float*)frames, (float*)out);
     return cudaGetLastError();
 }
 

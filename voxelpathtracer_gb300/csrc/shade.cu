@@ -132,7 +132,7 @@ __device__ __forceinline__ UpscaledGI upscale_gi(const WorldView& w, int W, int 
             const float kwt = (x == 0 ? 1.0f : 2.0f / 3.0f) * (y == 0 ? 1.0f : 2.0f / 3.0f);   // AtrousWeights
             float wgt = clampf((nw * dw) * kwt, 0.0f, 1.0f);
             if (kSpec) {
-                const float ra = material(w, min(max(tap_block, 0), 127)).rough;
+                const float ra = pbr_rough(w, tap_block);
                 float spw = (wgt / ((fabsf(ra - base_rough) * 12.0f) + 1.0f)) * dpow(fmaxf(dot(na, base_n), 0.0f), 8.0f);
                 spw = fmaxf(spw, 0.00000001f);
                 tsp.x += sp4.x * spw;
