@@ -300,7 +300,12 @@ def run_ours(args):
         v16, last_rgb["fp16"] = run_variant(storage=1)
         vq, _ = run_variant(gi_divisor=4)
         vq["gi_grid"] = [W // 4, H // 4]
-        variant = {"fp16_storage": v16, "gi_quarter": vq}
+        # with the reflection pass (ReflectionSPP 2, temporal filter and
+        # denoiser on, as the reference runs it), on the full and the 1/4 grid
+        vr, _ = run_variant(reflection_spp=2)
+        vrq, _ = run_variant(gi_divisor=4, reflection_spp=2)
+        vrq["gi_grid"] = [W // 4, H // 4]
+        variant = {"fp16_storage": v16, "gi_quarter": vq, "reflections": vr, "gi_quarter_reflections": vrq}
 
     # 5) error against the FP64 ground truth of the last frame on the centre crop
     quality_out = None
