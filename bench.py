@@ -45,7 +45,9 @@ ALG_BYTES_PER_RAY = 16      # ray output
 PEAKS_FILE = REPO / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 TRACE_KINDS = {"primary": ["primary"], "shadow": ["shadow"], "diffuse": ["diffuse", "bounce_shadow"],
-               "trace_frame": ["primary", "shadow", "diffuse", "bounce_shadow"]}
+               "trace_frame": ["primary", "shadow", "diffuse", "bounce_shadow"],
+               # the reflection pass's bytes are its rays' (its filters are small beside them)
+               "reflection": ["reflection", "reflection_shadow"]}
 # Algorithmic bytes per pixel of the filter and colour kernels (planes read +
 # planes written once), fp32 / fp16 storage.
 FILTER_BYTES_PER_PX = {
@@ -58,7 +60,8 @@ FILTER_BYTES_PER_PX = {
 KERNEL_NAMES = {"primary": "k_trace_primary", "shadow": "k_trace_shadow", "diffuse": "k_trace_diffuse",
                 "trace_frame": "k_trace_frame",
                 "spatial_initial": "k_spatial_initial", "temporal": "k_temporal", "variance": "k_variance",
-                "atrous": "k_atrous", "shade": "k_shade"}
+                "atrous": "k_atrous", "shade": "k_shade",
+                "reflection": "k_trace_reflection (+ hit blur, temporal and denoiser kernels)"}
 
 
 def log(*a):
@@ -163,7 +166,8 @@ def run_ours(args):
     dist = Replicas(world)
     W, H = RES
     vox, blocks, yaw, pitch = workload_inputs(vpt, seed=rank)
-    ctx = vpt.Context(width=W, height=H, device=local, storage=args.storage)
+    ctx = vpt.Context(width=W, height=H, device=local, storage=args.storage, gi_divisor=args.gi_divisor,
+                      reflection_spp=args.reflection_spp)
     ctx.upload_world(vox)
     ctx.set_block_table(blocks)
     ctx.build_df()
@@ -235,6 +239,8 @@ def run_ours(args):
                                for st, r in zip(steps[timed], rays[timed])]))
         else:
             b = float(FILTER_BYTES_PER_PX[p][args.storage] * W * H)
+            if p != "shade":   # the GI-side filters run on the GI grid
+                b /= float(args.gi_divisor * args.gi_divisor)
         per_launch_ms = ms / launches_per_frame
         gbs = b / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
         kernels[p] = {"launches_per_frame": launches_per_frame, "ms_per_launch": per_launch_ms,
@@ -367,6 +373,7 @@ def run_ours(args):
                                "(+ bounce shadow), SVGF temporal + variance + 5 a-trous, colour pass",
                    "world": list(WORLD), "resolution": list(RES), "spp": 1, "bounces": 1,
                    "storage": "fp32" if args.storage == 0 else "fp16",
+                   "gi_divisor": args.gi_divisor, "reflection_spp": args.reflection_spp,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "flushed (512 MiB write) between timed steps"},
         "e2e": {"value": e2e_value, "unit": "rays/s", "h2d_bytes_per_step": h2d,
@@ -736,6 +743,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--storage", type=int, default=0, help="0 = fp32 planes, 1 = fp16 planes")
+    ap.add_argument("--gi-divisor", type=int, default=1,
+                    help="GI grid = frame / this (the reference's DiffuseTraceResolution is 1/4)")
+    ap.add_argument("--reflection-spp", type=int, default=0,
+                    help="reflection rays per GI texel in the timed frame (0: no reflection pass)")
     ap.add_argument("--cpu-rows", type=int, default=0,
                     help="trace only a band of this many rows on the CPU (0 = whole frames)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
