@@ -314,6 +314,17 @@ vpt_status vpt_shade_from(vpt_ctx* ctx, const vpt_frame* frame, int32_t source);
 vpt_status vpt_ground_truth(vpt_ctx* ctx, const vpt_frame* frame, int32_t x0, int32_t y0, int32_t w, int32_t h,
                             int32_t spp, int32_t chunk, uint32_t seed, double* mean_out, double* m2_out);
 
+/* Minecraft Anvil import, Core/NBT/Importer.cpp ImportWorld: every .mca region
+ * file in `directory`, pre-flattening chunks (Level / xPos, zPos / Sections
+ * with Y, Blocks, Data), a voxel stored only where its data value is 0,
+ * mapped through mcid_to_block (the reference's BlockDatabase MinecraftIDLUT:
+ * 0 must map to 0), placed at (x, y, z) - origin + (192, 0, 192) in the
+ * reference's 384 x 128 x 384 world (x fastest, out_bytes >= 384*128*384).
+ * Chunks in the 1.13+ palette layout are skipped. *chunks_read (optional)
+ * counts the decoded chunks. No device needed. */
+vpt_status vpt_import_mca_world(const char* directory, const uint8_t mcid_to_block[256], const float origin[3],
+                                uint8_t* out, size_t out_bytes, int32_t* chunks_read);
+
 /* ---------------------------------------------------------------- planes -- */
 vpt_status vpt_plane_info(const vpt_ctx* ctx, int32_t plane, size_t* bytes, int32_t* channels, int32_t* dtype);
 /* vpt_read_plane / vpt_write_plane of the SPEC_* planes need reflection_spp > 0

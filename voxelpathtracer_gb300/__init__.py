@@ -202,6 +202,7 @@ def _load() -> C.CDLL:
         "vpt_shade_from": ([P, C.POINTER(Frame), i32], C.c_int),
         "vpt_edit_world": ([P, P, i32, i32, i32, i32, i32, i32], C.c_int),
         "vpt_save_world": ([C.c_char_p, P, i32, i32, i32, u64, i32], C.c_int),
+        "vpt_import_mca_world": ([C.c_char_p, P, P, P, sz, C.POINTER(i32)], C.c_int),
         "vpt_load_world": ([C.c_char_p, P, sz, C.POINTER(i32), C.POINTER(u64)], C.c_int),
         "vpt_emissive_voxels": ([P, i32, i32, i32, P, i32, P, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
         "vpt_learned_input": ([P, C.POINTER(Camera), C.POINTER(Frame)], C.c_int),
@@ -314,6 +315,25 @@ def load_world(path, dims=None):
     out = np.empty((d[2], d[1], d[0]), np.uint8)
     _check(lib.vpt_load_world(str(path).encode(), _ptr(out), out.nbytes, d, C.byref(seed)), "vpt_load_world")
     return out, int(seed.value)
+
+
+MCA_WORLD = (384, 128, 384)   # X, Y, Z of the reference's imported world (Core/Macros.h)
+
+
+def import_mca_world(directory, mcid_to_block=None, origin=(0.0, 0.0, 0.0)):
+    """Imports every .mca region file of `directory` (vpt_import_mca_world) into
+    the reference's 384 x 128 x 384 world; mcid_to_block maps Minecraft ids to
+    block ids (identity when None). Returns (voxels (Z, Y, X), chunks read)."""
+    lut = np.arange(256, dtype=np.uint8) if mcid_to_block is None else np.ascontiguousarray(mcid_to_block, np.uint8)
+    if lut.shape != (256,):
+        raise ValueError("mcid_to_block must have 256 entries")
+    org = (C.c_float * 3)(*[float(v) for v in origin])
+    X, Y, Z = MCA_WORLD
+    out = np.empty((Z, Y, X), np.uint8)
+    n = C.c_int32()
+    _check(lib.vpt_import_mca_world(str(directory).encode(), _ptr(lut), org, _ptr(out), out.nbytes, C.byref(n)),
+           "vpt_import_mca_world")
+    return out, int(n.value)
 
 
 def emissive_voxels(voxels: np.ndarray, table: np.ndarray) -> np.ndarray:
