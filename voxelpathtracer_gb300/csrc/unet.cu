@@ -33,6 +33,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 
 #include "tc.cuh"
@@ -308,15 +309,19 @@ constexpr int kRowThreads = 288;  // 4 loader warps, 1 MMA warp, 4 epilogue warp
 // K/8 blocks of 130 pixels x 8 channels (16 bytes a pixel), i.e. the
 // canonical K-major layout without swizzle (SBO = 128, LBO = 2080), in which a
 // one-pixel shift is a 16-byte start offset.
-//   warps 0-3   loaders: coalesced 16-byte cp.async of the row segment (zero
-//               outside the image), arriving on the buffer's `row_full`
-//               barrier as their copies land.
+//   warps 0-3   loaders: one thread issues a TMA box per input row (a 5-D
+//               map of the NHWC input ordered channel-in-group, pixel, group,
+//               row, image, so the box arrives in the row buffer's layout;
+//               zero outside the image) on the buffer's `row_full` barrier;
+//               for images narrower than the box, the four warps issue
+//               coalesced 16-byte cp.async copies instead.
 //   warp 4      one lane: 9 taps x K/16 MMAs per output row into one of two
 //               TMEM accumulators, commits `acc_full`, and releases input row
 //               y - 1 (its last use) with a commit to `row_empty`.
 //   warps 5-8   epilogue, as in k_conv3x3.
 __global__ void __launch_bounds__(kRowThreads, 1)
-    k_conv3x3_rows(const __grid_constant__ CUtensorMap tm_w, ConvArgs a, int R, int nstrips, int tiles_x, int nb) {
+    k_conv3x3_rows(const __grid_constant__ CUtensorMap tm_w, const __grid_constant__ CUtensorMap tm_in, ConvArgs a,
+                   int R, int nstrips, int tiles_x, int nb, int tma_rows) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t row_full[kRowBufs], row_empty[kRowBufs], acc_full[2], acc_empty[2], wbar;
     __shared__ uint32_t s_taddr;
@@ -326,12 +331,12 @@ __global__ void __launch_bounds__(kRowThreads, 1)
     const int strips_y = (H + R - 1) / R;
     const uint32_t wbytes = 9u * K * Np * 2u;
     const uint32_t nblk = (uint32_t)Np * 16u;        // one Np x 8-channel weight block
-    const uint32_t rowb = (uint32_t)G * 2080u;       // one row buffer
+    const uint32_t rowb = ((uint32_t)G * 2080u + 127u) & ~127u;   // one row buffer, 128-byte aligned
     const uint32_t ncols = tmem_columns(2 * Np);
     if (warp == 0) tc::tmem_alloc(tc::smem_addr(&s_taddr), ncols);
     if (tid == 0) {
         for (int k = 0; k < kRowBufs; k++) {
-            tc::mbar_init(tc::smem_addr(&row_full[k]), 128);
+            tc::mbar_init(tc::smem_addr(&row_full[k]), tma_rows ? 1 : 128);
             tc::mbar_init(tc::smem_addr(&row_empty[k]), 1);
         }
         for (int k = 0; k < 2; k++) {
@@ -359,7 +364,11 @@ __global__ void __launch_bounds__(kRowThreads, 1)
         }
         int L = 0;
         bool ok = true;
-        for (int strip = blockIdx.x; strip < nstrips && ok; strip += gridDim.x) {
+        // one TMA box per input row (8 channels x 130 pixels x K/8 groups, zero
+        // outside the image), issued by one thread; else 16-byte cp.async by
+        // the four loader warps
+        const bool loader = !tma_rows || tid == 0;
+        for (int strip = blockIdx.x; strip < nstrips && ok && loader; strip += gridDim.x) {
             const int xb = strip % tiles_x, rest = strip / tiles_x;
             const int ys = (rest % strips_y) * R, n = rest / strips_y;
             const int ye = min(ys + R, H);
@@ -373,6 +382,11 @@ __global__ void __launch_bounds__(kRowThreads, 1)
                     break;
                 }
                 const uint32_t dst = rbase + (uint32_t)b * rowb;
+                if (tma_rows) {
+                    tc::mbar_expect_tx(tc::smem_addr(&row_full[b]), (uint32_t)G * 2080u);
+                    tc::tma_load_5d(dst, &tm_in, 0, x0 - 1, 0, yy, n, tc::smem_addr(&row_full[b]));
+                    continue;
+                }
                 const bool yin = yy >= 0 && yy < H;
                 const bf16* row = in + (((size_t)n * H + (yin ? yy : 0)) * W) * K;
                 // 16-byte chunk q = pixel p (x0 - 1 + p) x group g, consecutive in memory
@@ -386,7 +400,7 @@ __global__ void __launch_bounds__(kRowThreads, 1)
                 cp_async_arrive(tc::smem_addr(&row_full[b]));
             }
         }
-        cp_async_wait_all();
+        if (!tma_rows) cp_async_wait_all();
     } else if (warp == 4) {
         // ---------------------------------------------------------- MMA issue
         if (lane == 0) {
@@ -852,7 +866,7 @@ cudaError_t conv3x3(const ConvArgs& a, cudaStream_t s) {
     const int tiles_x = (a.in.W + 127) / 128;
     // row-resident kernel when the weights and at least four input rows fit
     {
-        const size_t wbytes = 9u * (size_t)a.Cin * a.Np * 2u, rowb = (size_t)(a.Cin / 8) * 2080u;
+        const size_t wbytes = 9u * (size_t)a.Cin * a.Np * 2u, rowb = ((size_t)(a.Cin / 8) * 2080u + 127u) & ~(size_t)127u;
         const size_t budget = 200u * 1024u;
         if (wbytes <= 80u * 1024u && wbytes + 4u * rowb <= budget) {
             const int nb = (int)std::min<size_t>(kRowBufs, (budget - wbytes) / rowb);
@@ -873,11 +887,24 @@ cudaError_t conv3x3(const ConvArgs& a, cudaStream_t s) {
             if (!make_map(&tm_w8, a.w, 3, dw8, sw8, bw8, CU_TENSOR_MAP_SWIZZLE_NONE)) return cudaErrorInvalidValue;
             ConvArgs b = a;
             b.in = ConvSrc{src, a.Cin, 0, nullptr, 0, a.in.N, a.in.H, a.in.W};
+            // input rows as a 5-D map ordered (channel in group, pixel, group,
+            // row, image) so that one box lands in the row buffer's K-major
+            // layout: K/8 blocks of 130 pixels x 16 bytes
+            CUtensorMap tm_rows;
+            const int G = a.Cin / 8;
+            const cuuint64_t dr[5] = {8u, (cuuint64_t)a.in.W, (cuuint64_t)G, (cuuint64_t)a.in.H, (cuuint64_t)a.in.N};
+            const cuuint64_t sr[4] = {(cuuint64_t)a.Cin * 2u, 16u, (cuuint64_t)a.Cin * 2u * a.in.W,
+                                      (cuuint64_t)a.Cin * 2u * a.in.W * a.in.H};
+            const cuuint32_t br[5] = {8u, 130u, (cuuint32_t)G, 1u, 1u};
+            // (images narrower than the box keep the cp.async loaders)
+            const bool tma_rows = a.in.W >= 130 && make_map(&tm_rows, src, 5, dr, sr, br, CU_TENSOR_MAP_SWIZZLE_NONE);
+            if (!tma_rows) std::memset(&tm_rows, 0, sizeof tm_rows);
             if ((e = cudaFuncSetAttribute(k_conv3x3_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) !=
                 cudaSuccess)
                 return e;
             const int grid = (int)std::min<long long>(nstrips, ctas);
-            k_conv3x3_rows<<<grid, kRowThreads, sm, s>>>(tm_w8, b, R, (int)nstrips, tiles_x, nb);
+            k_conv3x3_rows<<<grid, kRowThreads, sm, s>>>(tm_w8, tm_rows, b, R, (int)nstrips, tiles_x, nb,
+                                                         tma_rows ? 1 : 0);
             return cudaGetLastError();
         }
     }
