@@ -18,7 +18,7 @@ namespace vpt {
 namespace {
 
 template <int B>
-__global__ void __launch_bounds__(512) k_batch_trace(BatchLaunch a) {
+__global__ void __launch_bounds__(512, 3) k_batch_trace(BatchLaunch a) {
     __shared__ int s_begin[kBatchMaxWorlds + 1];
     for (int k = threadIdx.x; k <= a.n_worlds; k += blockDim.x) s_begin[k] = a.tile_begin[k];
     __syncthreads();

@@ -117,7 +117,7 @@ __device__ __forceinline__ float bl_u8(const uint8_t* p, const Bilin& b) {
 }
 
 template <typename S>
-__global__ void __launch_bounds__(256) k_trace_reflection(WorldView w, CamView cam, int W, int H, int Wg, int Hg,
+__global__ void __launch_bounds__(256, 8) k_trace_reflection(WorldView w, CamView cam, int W, int H, int Wg, int Hg,
                                                           ReflectionArgs a, const S* t, const uint8_t* face,
                                                           const uint8_t* shadow, const S* tv, const uint8_t* fv,
                                                           const uint8_t* bv, const S* den_sh, const S* den_cocg,
@@ -293,7 +293,7 @@ __device__ __forceinline__ float dist_sq(v3 a, v3 b) {
 // aggressive firefly rejection on (Core/Pipeline.cpp:3226-3262); with
 // TEMPORAL_SPEC off the output is the firefly-rejected current colour.
 template <typename S>
-__global__ void __launch_bounds__(256) k_spec_temporal(WorldView w, CamView cam, SpecTemporalArgs a, int W, int H,
+__global__ void __launch_bounds__(256, 6) k_spec_temporal(WorldView w, CamView cam, SpecTemporalArgs a, int W, int H,
                                                        int Wg, int Hg, const S* tv, const uint8_t* fv,
                                                        const uint8_t* bv, const S* prev_t, const uint8_t* prev_face,
                                                        const S* spec, const S* hit, const S* mask, const S* prev_out,
@@ -465,7 +465,7 @@ __constant__ float kGauss33[33] = {0.004013f, 0.005554f, 0.007527f, 0.00999f,  0
 // the full-resolution depth, face, block and normal planes; the centre tap
 // reads the GI-grid views.
 template <typename S>
-__global__ void __launch_bounds__(256) k_spec_denoise(WorldView w, CamView cam, SpecDenoiseArgs a, int W, int H,
+__global__ void __launch_bounds__(256, 6) k_spec_denoise(WorldView w, CamView cam, SpecDenoiseArgs a, int W, int H,
                                                       int Wg, int Hg, const S* t, const uint8_t* face,
                                                       const uint8_t* block, const S* tv, const uint8_t* fv,
                                                       const uint8_t* bv, const S* in, const S* hit_data,

@@ -177,7 +177,7 @@ __device__ __forceinline__ UpscaledGI upscale_gi(const WorldView& w, int W, int 
 }
 
 template <typename S, bool kScaled, bool kSpec>
-__global__ void __launch_bounds__(256) k_shade(WorldView w, CamView cam, int W, int H, ShadeArgs a, const S* t,
+__global__ void __launch_bounds__(256, 4) k_shade(WorldView w, CamView cam, int W, int H, ShadeArgs a, const S* t,
                                                const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
                                                const S* sh_p, const S* cocg_p, const S* ao_p, const S* spec_p,
                                                S* rgb) {

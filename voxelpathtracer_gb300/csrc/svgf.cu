@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) k_spatial_initial(CamView cam, int W, int
 // when that grid is finer than the GI grid, so the two need separate
 // bilinear footprints).
 template <typename S, bool kScaled>
-__global__ void __launch_bounds__(256) k_temporal(CamView cam, int W, int H, int Wf, int Hf, TemporalArgs a, const S* t,
+__global__ void __launch_bounds__(256, 4) k_temporal(CamView cam, int W, int H, int Wf, int Hf, TemporalArgs a, const S* t,
                                                   const uint8_t* face, const uint8_t* block, const S* prev_t,
                                                   const uint8_t* prev_face, const uint8_t* prev_block,
                                                   const S* c_sh, const S* c_cocg, const S* c_luma, const S* c_aosky,

@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(256) k_trace_shadow(WorldView w, CamView cam, 
 
 // DiffuseRayTraceFrag.glsl main (:822-935)
 template <typename S>
-__global__ void __launch_bounds__(256) k_trace_diffuse(WorldView w, CamView cam, int W, int H, DiffuseArgs a,
+__global__ void __launch_bounds__(256, 8) k_trace_diffuse(WorldView w, CamView cam, int W, int H, DiffuseArgs a,
                                                        const S* t, const uint8_t* face, S* o_sh, S* o_cocg,
                                                        S* o_luma, S* o_aosky, Counters* stats) {
     int i, j;
