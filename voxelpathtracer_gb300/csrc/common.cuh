@@ -89,6 +89,18 @@ __device__ __forceinline__ v3 normal_from_id(int id, float miss) {
     }
 }
 
+// max(dot(normal_from_id(a, 1), normal_from_id(b, 1)), 0) as an integer: the
+// normals are axis vectors or (1, 1, 1) for a miss, so the clamped dot product
+// is exactly 0, 1 or 3 (both misses). Checked against the dot product for all
+// 256 x 256 id pairs.
+__device__ __forceinline__ int face_cos(int a, int b) {
+    const unsigned pos = 0x25u;   // ids whose normal is +z (0), +y (2) or +x (5)
+    const bool ma = (unsigned)a > 5u, mb = (unsigned)b > 5u;
+    if (ma) return mb ? 3 : (int)((pos >> b) & 1u);
+    if (mb) return (int)((pos >> a) & 1u);
+    return a == b ? 1 : 0;
+}
+
 // ------------------------------------------------------------ storage --
 __device__ __forceinline__ float ld(const float* p) { return __ldg(p); }
 __device__ __forceinline__ float ld(const __half* p) { return __half2float(__ldg(p)); }

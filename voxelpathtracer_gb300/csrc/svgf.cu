@@ -33,7 +33,8 @@ __global__ void __launch_bounds__(256) k_spatial_initial(CamView cam, int W, int
     const size_t px = (size_t)j * W + i;
     const v2 uv = texcoord(i, j, W, H);
     const v4 bp = position_fetch(cam, T, i, j, uv);
-    const v3 bn = normal_from_id(__ldg(face + px), 1.0f);
+    const int bf = __ldg(face + px);
+    const float nw3 = dpow(3.0f, 16.0f);   // the normal weight of two misses
     const float4 bsh = ld4(sh + 4 * px);
     const float2 bcc = ld2(cocg + 2 * px), bao = ld2(aosky + 2 * px);
     float bshv[4] = {bsh.x, bsh.y, bsh.z, bsh.w};
@@ -58,9 +59,10 @@ __global__ void __launch_bounds__(256) k_spatial_initial(CamView cam, int W, int
                 float4 s4 = ld4(sh + 4 * sp_);
                 float2 s2 = ld2(cocg + 2 * sp_);
                 float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
-                v3 sn = normal_from_id(__ldg(face + sp_), 1.0f);
+                const int fc = face_cos(bf, __ldg(face + sp_));
                 float sl = sh_to_y(ssh);
-                float nw = dpow(fmaxf(dot(bn, sn), 0.0f), 16.0f);
+                // pow(max(dot(n, n'), 0), 16) for a clamped dot of 0, 1 or 3
+                float nw = fc == 0 ? 0.0f : (fc == 1 ? 1.0f : nw3);
                 float lw = fabsf(sl - bl) / phi;
                 float wgt = dexp(-lw - nw);
                 wgt = fmaxf(wgt, 0.01f);
@@ -237,7 +239,9 @@ __global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, cons
     float osh[4], occ[2], var;
     if (acc < thresh) {
         const float bd = ld(t + px);
-        const v3 bn = normal_from_id(__ldg(face + px), 1.0f);
+        const int bf = __ldg(face + px);
+        // normal weight pow(max(dot(n, n'), 0), 16) for a clamped dot of 0, 1, 3
+        const float nw3 = dpow(3.0f, 16.0f);
         const float phi = 5.0f;
         float tw = 0.0f, tm = 0.0f, tl = 0.0f, tw2 = 0.0f;
         float tsh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, tcc[2] = {0.0f, 0.0f};
@@ -250,14 +254,15 @@ __global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, cons
                 if (sj < 0 || sj >= H) continue;
                 const size_t sp_ = (size_t)sj * W + si;
                 const float sd = ld(t + sp_);
-                const v3 sn = normal_from_id(__ldg(face + sp_), 1.0f);
+                const int fc = face_cos(bf, __ldg(face + sp_));
                 const float smom = ld(i_util + 4 * sp_ + 1);
                 const float4 s4 = ld4(i_sh + 4 * sp_);
                 const float2 s2 = ld2(i_cocg + 2 * sp_);
                 const float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
                 const float sl = sh_to_y(ssh);
-                const float nw = dpow(fmaxf(dot(bn, sn), 0.0f), 16.0f);
-                const float dw = dpow(dexp(-fabsf(sd - bd)), 2.0f);
+                const float nw = fc == 0 ? 0.0f : (fc == 1 ? 1.0f : nw3);
+                const float de = dexp(-fabsf(sd - bd));
+                const float dw = de * de;   // pow(e, 2) for e in [0, 1]
                 const float lw = fabsf(sl - bl) / phi;
                 float wgt = (dexp(-lw) * nw) * dw;
                 float wgt2 = wgt;
@@ -348,7 +353,7 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf,
         const float gx = ((float)i + 0.5f) + a.tmod500, gy = ((float)j + 0.5f) + a.tmod500;
         const float noise = fract(52.9829189f * fract(0.06711056f * gx + 0.00583715f * gy));
         const int jit = f2i((noise - 0.5f) * ((float)step * 0.8f));
-        const v3 bn = normal_from_id(__ldg(face + px), 1.0f);
+        const int bf = __ldg(face + px);
         const float bshv[4] = {bsh.x, bsh.y, bsh.z, bsh.w};
         const float bl = sh_to_y(bshv);
         const float vest = vsum / fmaxf(tk, 0.01f);
@@ -389,12 +394,13 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf,
                 const float2 sao = (filter_sky || filter_ao) ? bl2(i_aosky, fp) : make_float2(0.0f, 0.0f);
                 if (!(sc.x > 0.0f && sc.x < 1.0f && sc.y > 0.0f && sc.y < 1.0f)) continue;
                 const float dd = fabsf(sd - bd);
-                const v3 sn = normal_from_id(sface, 1.0f);
                 const float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
                 const float sl = sh_to_y(ssh);
-                const float nw = clampf(dpow(fmaxf(dot(bn, sn), 0.0f), 32.0f), 0.001f, 1.0f);
+                // clamp(pow(max(dot(n, n'), 0), 32), 0.001, 1) for a clamped dot of 0, 1 or 3
+                const float nw = face_cos(bf, sface) > 0 ? 1.0f : 0.001f;
                 const float lw = fabsf(sl - bl) / phi;
-                const float dw = clampf(dpow(dexp(-fmaxf(dd, 0.00001f)), 2.0f), 0.0001f, 1.0f);
+                const float de = dexp(-fmaxf(dd, 0.00001f));
+                const float dw = clampf(de * de, 0.0001f, 1.0f);   // pow(e, 2) for e in [0, 1)
                 float wgt = strong ? nw * dw : (dexp(-lw) * nw) * dw;
                 wgt = clampf(wgt, 0.001f, 1.0f);
                 const float xw = aw[x < 0 ? -x : x], yw = aw[y < 0 ? -y : y];
