@@ -61,7 +61,10 @@ __device__ __forceinline__ uint8_t shadow_pixel(const WorldView& w, const CamVie
 }
 
 // DiffuseRayTraceFrag.glsl main (:822-935): `spp` GI samples of the texel.
-template <int B, typename S>
+// kOneSample: the caller guarantees one sample (spp <= 1, sun stronger than
+// the moon), so nothing of the per-texel sums stays live across the traversal;
+// the arithmetic is the same.
+template <int B, typename S, bool kOneSample = false>
 __device__ __forceinline__ void diffuse_pixel(const WorldView& w, const CamView& cam, int W, int H, int i, int j,
                                               const DiffuseArgs& a, size_t px, float d, int face, S* o_sh,
                                               S* o_cocg, S* o_luma, S* o_aosky, GICount* cnt) {
@@ -80,8 +83,8 @@ __device__ __forceinline__ void diffuse_pixel(const WorldView& w, const CamView&
         return;
     }
     uint32_t rng = pcg_hash((uint32_t)px + pcg_hash(a.frame_index + pcg_hash(a.seed)));
-    int spp = min(max(a.spp, 1), 32);
-    if (a.lighting.moon_stronger) spp *= 2;
+    int spp = kOneSample ? 1 : min(max(a.spp, 1), 32);
+    if (!kOneSample && a.lighting.moon_stronger) spp *= 2;
     float tsh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, tcc[2] = {0.0f, 0.0f};
     v3 radiance = mk3(0.0f, 0.0f, 0.0f);
     float acc_ao = 0.0f, skyhits = 0.0f;

@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(256) k_trace_shadow(WorldView w, CamView cam, 
 }
 
 // DiffuseRayTraceFrag.glsl main (:822-935)
-template <typename S>
+template <typename S, bool kOneSample>
 __global__ void __launch_bounds__(256, 8) k_trace_diffuse(WorldView w, CamView cam, int W, int H, DiffuseArgs a,
                                                        const S* t, const uint8_t* face, S* o_sh, S* o_cocg,
                                                        S* o_luma, S* o_aosky, Counters* stats) {
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(256, 8) k_trace_diffuse(WorldView w, CamView c
     GICount cnt = {0u, 0u, 0u, 0u};
     if (i < W && j < H) {
         const size_t px = (size_t)j * W + i;
-        diffuse_pixel<0>(w, cam, W, H, i, j, a, px, ld(t + px), __ldg(face + px), o_sh, o_cocg, o_luma, o_aosky,
+        diffuse_pixel<0, S, kOneSample>(w, cam, W, H, i, j, a, px, ld(t + px), __ldg(face + px), o_sh, o_cocg, o_luma, o_aosky,
                          &cnt);
     }
     if (stats) {
@@ -98,14 +98,15 @@ cudaError_t trace_shadow(const WorldView& w, const CamView& cam, int W, int H, i
 
 cudaError_t trace_diffuse(const WorldView& w, const CamView& cam, int W, int H, const DiffuseArgs& a, int fp16,
                           const void* t, const uint8_t* face, GIOut out, Counters* stats, cudaStream_t s) {
+    const bool one = a.spp <= 1 && !a.lighting.moon_stronger;
     if (fp16)
-        k_trace_diffuse<__half><<<tile_grid(W, H), 256, 0, s>>>(w, cam, W, H, a, (const __half*)t, face,
-                                                                (__half*)out.sh, (__half*)out.cocg,
-                                                                (__half*)out.luma, (__half*)out.aosky, stats);
+        (one ? k_trace_diffuse<__half, true> : k_trace_diffuse<__half, false>)<<<tile_grid(W, H), 256, 0, s>>>(
+            w, cam, W, H, a, (const __half*)t, face, (__half*)out.sh, (__half*)out.cocg, (__half*)out.luma,
+            (__half*)out.aosky, stats);
     else
-        k_trace_diffuse<float><<<tile_grid(W, H), 256, 0, s>>>(w, cam, W, H, a, (const float*)t, face,
-                                                               (float*)out.sh, (float*)out.cocg, (float*)out.luma,
-                                                               (float*)out.aosky, stats);
+        (one ? k_trace_diffuse<float, true> : k_trace_diffuse<float, false>)<<<tile_grid(W, H), 256, 0, s>>>(
+            w, cam, W, H, a, (const float*)t, face, (float*)out.sh, (float*)out.cocg, (float*)out.luma,
+            (float*)out.aosky, stats);
     return cudaGetLastError();
 }
 
