@@ -71,8 +71,10 @@ VPT_HD int32_t f2i_floor(float x) {
 }
 
 VPT_HD float pow2i(int n) { return f_from_bits((uint32_t)(n + 127) << 23); }
+// p * 2^k in two exact steps, so a subnormal result is rounded once (either
+// split of k gives the same bits while p * 2^k1 stays normal)
 VPT_HD float scale2(float p, int k) {
-    int k1 = k / 2;
+    int k1 = k >> 1;
     int k2 = k - k1;
     return (p * pow2i(k1)) * pow2i(k2);
 }
@@ -91,9 +93,10 @@ VPT_HD float exp_poly(float r) {
 }
 
 VPT_HD float dexp(float x) {
-    if (x != x) return x;
-    if (x > 88.72283935546875f) return inf_f();
-    if (x < -103.97208404541016f) return 0.0f;
+    if (!(x >= -103.97208404541016f && x <= 88.72283935546875f)) {   // NaN, overflow, underflow
+        if (x != x) return x;
+        return x > 0.0f ? inf_f() : 0.0f;
+    }
     float kf = floorf(x * 1.44269502162933350f + 0.5f);
     int k = (int)kf;
     float r = (x - kf * 0.693145751953125f) - kf * 1.428606765330187e-06f;
