@@ -313,8 +313,10 @@ constexpr int kRowThreads = 288;  // 4 loader warps, 1 MMA warp, 4 epilogue warp
 //               map of the NHWC input ordered channel-in-group, pixel, group,
 //               row, image, so the box arrives in the row buffer's layout;
 //               zero outside the image) on the buffer's `row_full` barrier;
-//               for images narrower than the box, the four warps issue
-//               coalesced 16-byte cp.async copies instead.
+//               for images narrower than the box and for two-source inputs
+//               (the decoder's upsample-and-concatenate, whose half-resolution
+//               pixels appear twice in a row) the four warps issue 16-byte
+//               cp.async copies from the sources instead.
 //   warp 4      one lane: 9 taps x K/16 MMAs per output row into one of two
 //               TMEM accumulators, commits `acc_full`, and releases input row
 //               y - 1 (its last use) with a commit to `row_empty`.
@@ -388,14 +390,20 @@ __global__ void __launch_bounds__(kRowThreads, 1)
                     continue;
                 }
                 const bool yin = yy >= 0 && yy < H;
-                const bf16* row = in + (((size_t)n * H + (yin ? yy : 0)) * W) * K;
-                // 16-byte chunk q = pixel p (x0 - 1 + p) x group g, consecutive in memory
+                const int C0 = a.in.C0, C1 = a.in.C1, up = a.in.up0;
+                const int W0 = W >> up, yc = yin ? yy : 0;
+                const bf16* row0 = in + ((size_t)n * (H >> up) + (yc >> up)) * W0 * C0;
+                const bf16* row1 = C1 > 0 ? a.in.p1 + ((size_t)n * H + yc) * W * C1 : in;
+                // 16-byte chunk q = pixel p (x0 - 1 + p) x group g: channels [0, C0)
+                // from the first source (at x >> up), the rest from the second
                 for (int q = tid; q < 130 * G; q += 128) {
                     const int pp = q / G, g = q - pp * G;
-                    const int x = x0 - 1 + pp;
+                    const int x = x0 - 1 + pp, c = g * 8;
                     const bool inside = yin && x >= 0 && x < W;
-                    cp_async16(dst + (uint32_t)g * 2080u + (uint32_t)pp * 16u,
-                               inside ? (const void*)(row + (size_t)x * K + g * 8) : (const void*)in, inside ? 16u : 0u);
+                    const void* src = c < C0 ? (const void*)(row0 + (size_t)(x >> up) * C0 + c)
+                                             : (const void*)(row1 + (size_t)x * C1 + (c - C0));
+                    cp_async16(dst + (uint32_t)g * 2080u + (uint32_t)pp * 16u, inside ? src : (const void*)in,
+                               inside ? 16u : 0u);
                 }
                 cp_async_arrive(tc::smem_addr(&row_full[b]));
             }
@@ -853,15 +861,8 @@ cudaError_t conv3x3(const ConvArgs& a, cudaStream_t s) {
         a.Np > 256 || (a.in.up0 && ((a.in.H | a.in.W) & 1)) || (a.in.C0 % 8) || (a.in.C1 % 8) || !a.w)
         return cudaErrorInvalidValue;
     const long long P = (long long)a.in.N * a.in.H * a.in.W;
-    // a single-source input is read in place; a two-source one is assembled first
+    const bool two = a.in.up0 || a.in.C1 > 0;
     const bf16* src = a.in.p0;
-    if (a.in.up0 || a.in.C1 > 0) {
-        if (!a.scratch) return cudaErrorInvalidValue;
-        k_upcat<<<ew_grid(P * (a.Cin / 8)), 256, 0, s>>>(a.in, a.scratch);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-        src = a.scratch;
-    }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -897,8 +898,9 @@ cudaError_t conv3x3(const ConvArgs& a, cudaStream_t s) {
             const cuuint64_t sw8[2] = {(cuuint64_t)a.Cin * 2u, (cuuint64_t)a.Cin * 2u * 9u};
             const cuuint32_t bw8[3] = {8u, 1u, (cuuint32_t)a.Np};
             if (!make_map(&tm_w8, a.w, 3, dw8, sw8, bw8, CU_TENSOR_MAP_SWIZZLE_NONE)) return cudaErrorInvalidValue;
+            // a two-source input is read from its sources by the cp.async loaders
             ConvArgs b = a;
-            b.in = ConvSrc{src, a.Cin, 0, nullptr, 0, a.in.N, a.in.H, a.in.W};
+            if (!two) b.in = ConvSrc{src, a.Cin, 0, nullptr, 0, a.in.N, a.in.H, a.in.W};
             // input rows as a 5-D map ordered (channel in group, pixel, group,
             // row, image) so that one box lands in the row buffer's K-major
             // layout: K/8 blocks of 130 pixels x 16 bytes
@@ -909,7 +911,8 @@ cudaError_t conv3x3(const ConvArgs& a, cudaStream_t s) {
                                       (cuuint64_t)a.Cin * 2u * a.in.W * a.in.H};
             const cuuint32_t br[5] = {8u, 130u, (cuuint32_t)G, 1u, 1u};
             // (images narrower than the box keep the cp.async loaders)
-            const bool tma_rows = a.in.W >= 130 && make_map(&tm_rows, src, 5, dr, sr, br, CU_TENSOR_MAP_SWIZZLE_NONE);
+            const bool tma_rows =
+                !two && a.in.W >= 130 && make_map(&tm_rows, src, 5, dr, sr, br, CU_TENSOR_MAP_SWIZZLE_NONE);
             if (!tma_rows) std::memset(&tm_rows, 0, sizeof tm_rows);
             if ((e = cudaFuncSetAttribute(k_conv3x3_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) !=
                 cudaSuccess)
@@ -919,6 +922,13 @@ cudaError_t conv3x3(const ConvArgs& a, cudaStream_t s) {
                                                          tma_rows ? 1 : 0);
             return cudaGetLastError();
         }
+    }
+    // the staged kernel reads one tensor: a two-source input is assembled first
+    if (two) {
+        if (!a.scratch) return cudaErrorInvalidValue;
+        k_upcat<<<ew_grid(P * (a.Cin / 8)), 256, 0, s>>>(a.in, a.scratch);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        src = a.scratch;
     }
     const ConvPlan plan = conv_plan(a.Cin, a.Np);
     if (plan.smem > 200u * 1024u) return cudaErrorInvalidValue;
