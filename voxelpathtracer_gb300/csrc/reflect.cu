@@ -479,6 +479,9 @@ __global__ void __launch_bounds__(256, 6) k_spec_denoise(WorldView w, CamView ca
     const Plane8 F{face, W, H}, B{block, W, H};
     const v4 bp = position_fetch(cam, TV, i, j, uv);
     const v3 bn = normal_from_id(__ldg(fv + q), 1.0f);
+    const int bf = __ldg(fv + q);
+    // pow(max(n.n', 1e-11), 32) for a clamped dot product of 0, 1 or 3 (face_cos)
+    const float nw0 = dpow(0.00000000001f, 32.0f), nw3 = dpow(3.0f, 32.0f);
     const bool base_sky = bp.w < 0.0f;
     const float4 bc = ld4(in + 4 * q);
     const float base_lum = dot(mk3(bc.x, bc.y, bc.z), mk3(0.299f, 0.587f, 0.114f));
@@ -574,9 +577,10 @@ __global__ void __launch_bounds__(256, 6) k_spec_denoise(WorldView w, CamView ca
         const bool sample_sky = sdepth < 0.0f;
         if (sample_sky != base_sky) continue;
         const float dd = fabsf(sdepth - bp.w) * 1.5f;
-        const float dw = dpow(dexp(-dd), 2.0f);
-        const v3 sn = normal_from_id(sface, 1.0f);
-        const float nw = dpow(fmaxf(dot(bn, sn), 0.00000000001f), 32.0f);
+        const float de = dexp(-dd);
+        const float dw = de * de;   // pow(e, 2) for e in [0, 1]
+        const int ncls = face_cos(bf, sface);
+        const float nw = ncls == 0 ? nw0 : (ncls == 1 ? dpow(1.0f, 32.0f) : nw3);
         float lw = 1.0f;
         const float srough = pbr_rough(w, sblock);
         const bool too_rough = srough >= 0.89f;

@@ -86,9 +86,15 @@ template <typename S, bool kScaled, bool kSpec>
 __device__ __forceinline__ UpscaledGI upscale_gi(const WorldView& w, int W, int H, int d, int i, int j, v2 uv,
                                                  const S* t, const uint8_t* face, const uint8_t* block,
                                                  const uint8_t* shadow, const S* sh_p, const S* cocg_p,
-                                                 const S* ao_p, const S* spec_p, v3 base_n, float base_d,
+                                                 const S* ao_p, const S* spec_p, int base_face, float base_d,
                                                  float base_rough) {
     UpscaledGI u;
+    // the normal weights for a clamped dot product of the decoded face
+    // normals of 0, 1 or 3 (face_cos): max(n.n', 1e-6)^16 floored at 1e-4,
+    // and max(n.n', 0)^8 for the specular gather
+    const float nw0 = fmaxf(dpow(0.000001f, 16.0f), 0.0001f), nw1 = fmaxf(dpow(1.0f, 16.0f), 0.0001f),
+                nw3 = fmaxf(dpow(3.0f, 16.0f), 0.0001f);
+    const float sw1 = dpow(1.0f, 8.0f), sw3 = dpow(3.0f, 8.0f);
     float4 tsh = make_float4(0.0f, 0.0f, 0.0f, 0.0f), tsp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     float tcc0 = 0.0f, tcc1 = 0.0f, tao = 0.0f, tw = 0.0f, tsw = 0.0f, tspw = 0.0f;
     const bool filter_shadows = base_d > 128.0f;
@@ -126,14 +132,13 @@ __device__ __forceinline__ UpscaledGI upscale_gi(const WorldView& w, int W, int 
             const float lda = 1.0f / (1.0f / tt);
             const float ed = dexp(-(fabsf(lda - base_d) * 2.0f));
             const float dw = dpow(ed, 5.25f);
-            const v3 na = normal_from_id(fid, 1.0f);
-            float nw = dpow(fmaxf(dot(na, base_n), 0.000001f), 16.0f);
-            nw = fmaxf(nw, 0.0001f);
+            const int fc = face_cos(base_face, fid);
+            const float nw = fc == 0 ? nw0 : (fc == 1 ? nw1 : nw3);
             const float kwt = (x == 0 ? 1.0f : 2.0f / 3.0f) * (y == 0 ? 1.0f : 2.0f / 3.0f);   // AtrousWeights
             float wgt = clampf((nw * dw) * kwt, 0.0f, 1.0f);
             if (kSpec) {
                 const float ra = pbr_rough(w, tap_block);
-                float spw = (wgt / ((fabsf(ra - base_rough) * 12.0f) + 1.0f)) * dpow(fmaxf(dot(na, base_n), 0.0f), 8.0f);
+                float spw = (wgt / ((fabsf(ra - base_rough) * 12.0f) + 1.0f)) * (fc == 0 ? 0.0f : (fc == 1 ? sw1 : sw3));
                 spw = fmaxf(spw, 0.00000001f);
                 tsp.x += sp4.x * spw;
                 tsp.y += sp4.y * spw;
@@ -200,7 +205,8 @@ __global__ void __launch_bounds__(256, 4) k_shade(WorldView w, CamView cam, int 
         if (m.metal >= 0.1f - 0.01f) albedo = basic_saturation(albedo, 0.9f);
         float emissivity = (float)m.emissive;
         const UpscaledGI up = upscale_gi<S, kScaled, kSpec>(w, W, H, a.gi_div, i, j, uv, t, face, block, shadow,
-                                                            sh_p, cocg_p, ao_p, spec_p, n, dist, m.rough);
+                                                            sh_p, cocg_p, ao_p, spec_p, (int)__ldg(face + px), dist,
+                                                            m.rough);
         float up_shadow = clampf(up.shadow, 0.0f, 1.0f);
         float rt_shadow = clampf(clampf(up_shadow + 0.0f, 0.0f, 1.0f), 0.0f, 1.0f);
         v3 indirect = sh_to_irradiance(up.sh, up.cocg, n);
