@@ -248,6 +248,9 @@ def run_ours(args):
     dom = max(mean_pass, key=mean_pass.get)
     per_launch_bytes = kernels[dom]["algorithmic_bytes_per_launch"]
     achieved = kernels[dom]["achieved_gbs"]
+    traffic, traffic_source = args.traffic, "--traffic" if args.traffic is not None else None
+    if traffic is None and args.storage == 0 and args.gi_divisor == 1 and args.reflection_spp == 0:
+        traffic, traffic_source = profile_traffic(KERNEL_NAMES[dom])
 
     # 3) end-to-end through the C ABI with host buffers (pinned)
     ctx.reset_history()
@@ -383,7 +386,7 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom],
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
-                     else "fallback", "traffic": args.traffic,
+                     else "fallback", "traffic": traffic, "traffic_source": traffic_source,
                      "algorithmic_bytes_per_launch": per_launch_bytes,
                      "kernels": {KERNEL_NAMES[k]: v for k, v in kernels.items()}},
         "clocks": clk,
@@ -559,6 +562,24 @@ def learned_section(vpt, torch, args, local, flush, vox, blocks, yaw, pitch, pea
 def quality_crop():
     from voxelpathtracer_gb300 import quality
     return quality.DEFAULT_CROP_1080P
+
+
+def profile_traffic(kernel):
+    """DRAM bytes (read + write) of one launch of `kernel` on this workload,
+    from its committed ncu summary (profiles/<kernel>_1080p.md); (None, None)
+    when there is none."""
+    import re
+    path = Path(__file__).resolve().parent / "profiles" / f"{kernel}_1080p.md"
+    if not path.exists():
+        return None, None
+    units = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
+    total = 0.0
+    for what in ("DRAM read", "DRAM write"):
+        m = re.search(rf"^\| {what} \| ([0-9.]+) \| (\w+) \|$", path.read_text(), re.M)
+        if not m or m.group(2) not in units:
+            return None, None
+        total += float(m.group(1)) * units[m.group(2)]
+    return total, f"profiles/{path.name} (ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch)"
 
 
 # ------------------------------------------------------ large combined --
