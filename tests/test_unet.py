@@ -75,20 +75,27 @@ def test_conv_forward(vpt, gpu, cin, cout, h, w, relu):
 
 
 @pytest.mark.gpu
-def test_conv_upsample_concat_and_mask(vpt, gpu):
-    """Channels [0, 64) nearest-upsampled from half size, [64, 96) full size, masked output."""
+@pytest.mark.parametrize("c0,c1,cout,h,w", [(64, 32, 32, 8, 136), (96, 64, 64, 6, 200), (96, 64, 64, 4, 48),
+                                            (64, 64, 96, 4, 256)],
+                         ids=["rows", "staged-split", "staged-assembled", "staged-split-wide"])
+def test_conv_upsample_concat_and_mask(vpt, gpu, c0, c1, cout, h, w):
+    """Channels [0, c0) nearest-upsampled from half size, [c0, c0 + c1) full
+    size, masked output: through the row-resident kernel's two-source loads,
+    the staged kernel's even / odd half boxes (rows of at least 128 pixels,
+    one ragged tile) and its assembled fallback (narrower rows)."""
     import torch
-    rng = np.random.default_rng(5)
-    n, h, w = 2, 8, 136
-    low = U.bf16(rng.normal(size=(n, h // 2, w // 2, 64)))
-    skip = U.bf16(rng.normal(size=(n, h, w, 32)))
-    wt = U.bf16(rng.normal(size=(32, 9, 96)) / 30.0)
-    mask = U.bf16(rng.normal(size=(n, h, w, 32)))
+    rng = np.random.default_rng(5 + c0 + w)
+    n = 2
+    cin = c0 + c1
+    low = U.bf16(rng.normal(size=(n, h // 2, w // 2, c0)))
+    skip = U.bf16(rng.normal(size=(n, h, w, c1)))
+    wt = U.bf16(rng.normal(size=(cout, 9, cin)) / np.sqrt(9 * cin))
+    mask = U.bf16(rng.normal(size=(n, h, w, cout)))
     ref = U.conv(np.concatenate([U.up(low), skip], axis=3), wt)
     ref = np.where(mask > 0, ref, 0.0)
-    o32 = torch.empty((n, h, w, 32), dtype=torch.float32, device="cuda")
-    vpt.nn_conv3x3(bf16_tensor(torch, low), 64, bf16_tensor(torch, skip), 32, n, h, w, bf16_tensor(torch, wt), None,
-                   32, mask=bf16_tensor(torch, mask), out_f32=o32, up0=True)
+    o32 = torch.empty((n, h, w, cout), dtype=torch.float32, device="cuda")
+    vpt.nn_conv3x3(bf16_tensor(torch, low), c0, bf16_tensor(torch, skip), c1, n, h, w, bf16_tensor(torch, wt), None,
+                   cout, mask=bf16_tensor(torch, mask), out_f32=o32, up0=True)
     vpt.nn_status()
     assert rel_l2(o32.cpu().numpy(), ref) < 1e-5
 

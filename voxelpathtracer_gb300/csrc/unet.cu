@@ -106,10 +106,21 @@ constexpr int kConvStages = 8;   // most shared-memory stages of (tap, channel c
 //               next tile's MMAs in the other accumulator.
 // CTAs loop over 128-pixel row tiles (x fastest, so neighbouring CTAs share
 // input rows in L2).
+// Two-source inputs (`split` > 0: channels [0, split) from a half-resolution
+// tensor upsampled by nearest neighbour, the rest from a full-resolution one)
+// are staged without assembling the concatenation: a tile's 128 accumulator
+// rows are its 64 even pixels, then its 64 odd ones. For tap dx the even
+// pixels x0 + 2m read input column x0 + 2m + dx, i.e. half-resolution column
+// m0 + m + floor(dx / 2) and full-resolution pixel (m0 + m + floor(dx / 2),
+// parity dx & 1); the odd ones the same with dx + 1. So each half is one
+// 64-pixel box: from `tm_in` (the half-resolution tensor) or from `tm_in2`
+// (the full-resolution tensor as (channel, parity, x / 2, y, image)), and the
+// epilogue stores row r to pixel x0 + 2 (r % 64) + r / 64.
 constexpr int kConvThreads = 192;
 __global__ void __launch_bounds__(kConvThreads, 1)
-    k_conv3x3(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_w, ConvArgs a, int KC,
-              int ntiles, int tiles_x, int w_resident, int box_w, int S) {
+    k_conv3x3(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_w,
+              const __grid_constant__ CUtensorMap tm_in2, ConvArgs a, int KC, int ntiles, int tiles_x, int w_resident,
+              int box_w, int S, int split) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t full[kConvStages], empty[kConvStages], acc_full[2], acc_empty[2], wbar;
     __shared__ uint32_t s_taddr;
@@ -124,7 +135,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
     const uint32_t nblk = (uint32_t)Np * rb;        // bytes of one Np x KC weight block
     // bytes one stage's boxes deliver (a box is box_w <= 128 pixels wide; rows
     // past it hold stale data that only feeds accumulator rows the epilogue skips)
-    const uint32_t stage_tx = (uint32_t)box_w * rb + bbytes;
+    const uint32_t stage_tx = (split > 0 ? 128u : (uint32_t)box_w) * rb + bbytes;
     const uint32_t ncols = tmem_columns(2 * Np);
     if (warp == 0) tc::tmem_alloc(tc::smem_addr(&s_taddr), ncols);
     if (tid == 0) {
@@ -175,7 +186,18 @@ __global__ void __launch_bounds__(kConvThreads, 1)
                     const uint32_t sa = ring + st * stage, sb = sa + abytes;
                     const uint32_t bar = tc::smem_addr(&full[st]);
                     tc::mbar_expect_tx(bar, stage_tx);
-                    tc::tma_load_4d(sa, &tm_in, c0, x0 + dx, y + dy, n, bar);
+                    if (split > 0) {
+                        const int m0 = x0 >> 1, e = dx >> 1, o = (dx + 1) >> 1;   // floor(dx / 2), floor((dx + 1) / 2)
+                        if (c0 < split) {
+                            tc::tma_load_4d(sa, &tm_in, c0, m0 + e, (y + dy) >> 1, n, bar);
+                            tc::tma_load_4d(sa + 64u * rb, &tm_in, c0, m0 + o, (y + dy) >> 1, n, bar);
+                        } else {
+                            tc::tma_load_5d(sa, &tm_in2, c0 - split, dx & 1, m0 + e, y + dy, n, bar);
+                            tc::tma_load_5d(sa + 64u * rb, &tm_in2, c0 - split, (dx + 1) & 1, m0 + o, y + dy, n, bar);
+                        }
+                    } else {
+                        tc::tma_load_4d(sa, &tm_in, c0, x0 + dx, y + dy, n, bar);
+                    }
                     if (!w_resident) tc::tma_load_3d(sb, &tm_w, c0, tap, 0, bar);
                 }
                 if (!ok) break;
@@ -230,7 +252,7 @@ __global__ void __launch_bounds__(kConvThreads, 1)
                 break;
             tc::fence_after_sync();
             const int xb = tile % tiles_x, ry = tile / tiles_x;
-            const int y = ry % H, n = ry / H, x = xb * 128 + m;
+            const int y = ry % H, n = ry / H, x = xb * 128 + (split > 0 ? 2 * (m & 63) + (m >> 6) : m);
             const bool valid = x < W;
             const size_t p = ((size_t)n * H + y) * W + x;
             for (int c0 = 0; c0 < Np; c0 += 16) {
@@ -923,16 +945,22 @@ cudaError_t conv3x3(const ConvArgs& a, cudaStream_t s) {
             return cudaGetLastError();
         }
     }
-    // the staged kernel reads one tensor: a two-source input is assembled first
-    if (two) {
+    const ConvPlan plan = conv_plan(a.Cin, a.Np);
+    if (plan.smem > 200u * 1024u) return cudaErrorInvalidValue;
+    // a decoder input (half-resolution source first, then a full-resolution
+    // one) is staged from its sources in even / odd pixel order when both
+    // split at chunk boundaries and a row holds a whole 64-pixel half box;
+    // otherwise it is assembled into a scratch tensor first
+    const bool split = two && a.in.up0 && a.in.C1 > 0 && a.in.C0 % plan.kc == 0 && a.in.C1 % plan.kc == 0 &&
+                       a.in.W >= 128;
+    if (two && !split) {
         if (!a.scratch) return cudaErrorInvalidValue;
         k_upcat<<<ew_grid(P * (a.Cin / 8)), 256, 0, s>>>(a.in, a.scratch);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         src = a.scratch;
     }
-    const ConvPlan plan = conv_plan(a.Cin, a.Np);
-    if (plan.smem > 200u * 1024u) return cudaErrorInvalidValue;
-    CUtensorMap tm_in, tm_w;
+    CUtensorMap tm_in, tm_w, tm_in2;
+    std::memset(&tm_in2, 0, sizeof tm_in2);
     const cuuint64_t din[4] = {(cuuint64_t)a.Cin, (cuuint64_t)a.in.W, (cuuint64_t)a.in.H, (cuuint64_t)a.in.N};
     const cuuint64_t sin[3] = {(cuuint64_t)a.Cin * 2u, (cuuint64_t)a.Cin * 2u * a.in.W,
                                (cuuint64_t)a.Cin * 2u * a.in.W * a.in.H};
@@ -943,18 +971,31 @@ cudaError_t conv3x3(const ConvArgs& a, cudaStream_t s) {
     const cuuint64_t dw[3] = {(cuuint64_t)a.Cin, 9u, (cuuint64_t)a.Np};
     const cuuint64_t sw[2] = {(cuuint64_t)a.Cin * 2u, (cuuint64_t)a.Cin * 2u * 9u};
     const cuuint32_t bw[3] = {kc, 1u, (cuuint32_t)a.Np};
-    if (!make_map(&tm_in, src, 4, din, sin, bin, swz) || !make_map(&tm_w, a.w, 3, dw, sw, bw, swz))
-        return cudaErrorInvalidValue;
+    if (!make_map(&tm_w, a.w, 3, dw, sw, bw, swz)) return cudaErrorInvalidValue;
     ConvArgs b = a;
-    b.in = ConvSrc{src, a.Cin, 0, nullptr, 0, a.in.N, a.in.H, a.in.W};
+    if (split) {
+        const int C0 = a.in.C0, C1 = a.in.C1, W2 = a.in.W / 2, H2 = a.in.H / 2;
+        const cuuint64_t dl[4] = {(cuuint64_t)C0, (cuuint64_t)W2, (cuuint64_t)H2, (cuuint64_t)a.in.N};
+        const cuuint64_t sl[3] = {(cuuint64_t)C0 * 2u, (cuuint64_t)C0 * 2u * W2, (cuuint64_t)C0 * 2u * W2 * H2};
+        const cuuint32_t bl[4] = {kc, 64u, 1u, 1u};
+        const cuuint64_t dp[5] = {(cuuint64_t)C1, 2u, (cuuint64_t)W2, (cuuint64_t)a.in.H, (cuuint64_t)a.in.N};
+        const cuuint64_t sp[4] = {(cuuint64_t)C1 * 2u, (cuuint64_t)C1 * 4u, (cuuint64_t)C1 * 2u * a.in.W,
+                                  (cuuint64_t)C1 * 2u * a.in.W * a.in.H};
+        const cuuint32_t bp[5] = {kc, 1u, 64u, 1u, 1u};
+        if (!make_map(&tm_in, a.in.p0, 4, dl, sl, bl, swz) || !make_map(&tm_in2, a.in.p1, 5, dp, sp, bp, swz))
+            return cudaErrorInvalidValue;
+    } else {
+        if (!make_map(&tm_in, src, 4, din, sin, bin, swz)) return cudaErrorInvalidValue;
+        b.in = ConvSrc{src, a.Cin, 0, nullptr, 0, a.in.N, a.in.H, a.in.W};
+    }
     if ((e = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plan.smem)) !=
         cudaSuccess)
         return e;
     const long long ntiles = (long long)tiles_x * a.in.H * a.in.N;
     if (ntiles > (1LL << 30)) return cudaErrorInvalidValue;
     const int grid = (int)std::min<long long>(ntiles, (long long)sms * conv_ctas_per_sm(a.Np, plan.smem));
-    k_conv3x3<<<grid, kConvThreads, plan.smem, s>>>(tm_in, tm_w, b, plan.kc, (int)ntiles, tiles_x, plan.resident,
-                                                     box_w, plan.stages);
+    k_conv3x3<<<grid, kConvThreads, plan.smem, s>>>(tm_in, tm_w, tm_in2, b, plan.kc, (int)ntiles, tiles_x,
+                                                     plan.resident, box_w, plan.stages, split ? a.in.C0 : 0);
     return cudaGetLastError();
 }
 
