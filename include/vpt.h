@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define VPT_ABI_VERSION 2
+#define VPT_ABI_VERSION 3
 
 typedef enum vpt_status {
     VPT_OK = 0,
@@ -158,7 +158,11 @@ typedef enum vpt_plane {
     VPT_PLANE_SPEC_ACC = 37,  /* its accumulation factor (-1 with the temporal filter off) */
     VPT_PLANE_SPEC_STABLE_HIT = 38, /* its temporally stabilised hit distance */
     VPT_PLANE_SPEC_DEN = 39,  /* ReflectionDenoised_2: the spatially denoised reflection (4 ch) */
-    VPT_PLANE_COUNT = 40
+    VPT_PLANE_GB_ALBEDO = 40, /* GBuffer (GenerateGBuffer.glsl): albedo RGB (3 ch), with block textures */
+    VPT_PLANE_GB_NORMAL = 41, /* normal-mapped normal (3 ch) */
+    VPT_PLANE_GB_PBR = 42,    /* roughness, metalness, displacement, emissivity (4 ch) */
+    VPT_PLANE_GB_AO = 43,     /* texture ambient occlusion (1 ch) */
+    VPT_PLANE_COUNT = 44
 } vpt_plane;
 
 typedef enum vpt_dtype { VPT_DTYPE_F32 = 0, VPT_DTYPE_F16 = 1, VPT_DTYPE_U8 = 2, VPT_DTYPE_U16 = 3, VPT_DTYPE_I32 = 4 } vpt_dtype;
@@ -178,7 +182,8 @@ typedef enum vpt_pass {
     VPT_PASS_TRACE_FRAME = 8,        /* fused primary + shadow + diffuse (vpt_trace_frame) */
     VPT_PASS_LEARNED = 9,            /* features + U-Net + colour write-back (vpt_render_frame_learned) */
     VPT_PASS_REFLECTION = 10,        /* reflection trace + firefly rejection (vpt_trace_reflections) */
-    VPT_PASS_COUNT = 11
+    VPT_PASS_GBUFFER = 11,           /* textured G-buffer (vpt_generate_gbuffer) */
+    VPT_PASS_COUNT = 12
 } vpt_pass;
 
 /* Launch-shape knobs of the fused trace kernel, picked by the autotuner. */
@@ -209,6 +214,41 @@ vpt_status vpt_upload_world(vpt_ctx* ctx, const uint8_t* voxels, int32_t X, int3
 vpt_status vpt_set_block_table(vpt_ctx* ctx, const vpt_block* table, int32_t n);
 /* World::GenerateDistanceField (Core/World.cpp:69-113). */
 vpt_status vpt_build_df(vpt_ctx* ctx);
+
+/* Block texture arrays: the four GL_TEXTURE_2D_ARRAYs of BlockDatabase
+ * (Core/BlockDatabase.cpp:60-90, Core/GLClasses/TextureArray.cpp:10-78) and
+ * the per-block layer indices of BlockDataSSBO (Core/BlockDataSSBO.cpp:9-35)
+ * with GenerateGBuffer's grass override (u_GrassBlockProps,
+ * Core/Pipeline.cpp:2086-2095). Every array is `layers` square layers of
+ * `size` x `size` texels (size a power of two, 1..1024), row-major, row 0 at
+ * t = 0. Mip levels are built on the device (each texel the rounded mean of
+ * the 2 x 2 texels above it, per 8-bit channel). */
+typedef struct vpt_block_textures {
+    int32_t size;
+    const uint8_t* albedo;           /* RGBA8, sRGB-encoded colour (an sRGB_ALPHA array) */
+    int32_t albedo_layers;
+    const uint8_t* normal;           /* RGBA8: tangent-space normal * 0.5 + 0.5 */
+    int32_t normal_layers;
+    const uint8_t* pbr;              /* RGBA8: roughness, metalness, displacement, AO */
+    int32_t pbr_layers;
+    const uint8_t* emissive;         /* R8, or NULL (no block emits through a texture) */
+    int32_t emissive_layers;
+    int32_t albedo_id[128];          /* layer of each block id's texture (BlockAlbedoData) */
+    int32_t normal_id[128];          /* BlockNormalData */
+    int32_t pbr_id[128];             /* BlockPBRData */
+    int32_t emissive_id[128];        /* BlockEmissiveData; -1 = none */
+    int32_t grass[10];               /* grass block id, then albedo / normal / PBR layers of
+                                        its top (1-3), sides (4-6) and bottom (7-9); id -1 = none */
+} vpt_block_textures;
+/* Uploads the arrays and builds their mip chains; NULL removes them (flat
+ * materials from the block table). Allocates the G-buffer texture planes. */
+vpt_status vpt_set_block_textures(vpt_ctx* ctx, const vpt_block_textures* textures);
+/* GenerateGBuffer.glsl main (:347-419; parallax mapping off, its default
+ * Core/Pipeline.cpp:264, no lava block): albedo, normal-mapped normal, PBR and
+ * texture AO of this frame's G-buffer hits, from the block textures sampled
+ * with textureGrad at the face UV (trilinear, the LOD from the quad
+ * derivatives of the UV). Needs vpt_set_block_textures and vpt_trace_primary. */
+vpt_status vpt_generate_gbuffer(vpt_ctx* ctx);
 /* Block edit (World::SetBlock followed by the distance-field rebuild it
  * triggers, Core/World.cpp:372-374, :458-460): writes the x-fastest voxels of
  * the box [x0,x0+w) x [y0,y0+h) x [z0,z0+d) (w*h*d bytes) into the world and,

@@ -101,6 +101,7 @@ def lib() -> C.CDLL:
         L.vpto_plain_atrous.argtypes = [P, P, C.c_int, P, P, P, P, P, P, P, P, P]
         L.vpto_ground_truth.argtypes = [P, P, P, P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                         C.c_uint32, P, P]
+        L.vpto_generate_gbuffer.argtypes = [P, P, P, P, P, P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -293,6 +294,40 @@ def atrous(cam, config, frame, step, t, face, temporal_util, filt_in: dict, aosk
     si, so = _struct4(fi, ["sh", "cocg", "variance", "aosky"]), _struct4(out, ["sh", "cocg", "variance", "aosky"])
     lib().vpto_atrous(C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)), int(step), _p(t),
                       _p(face), _p(tv), _p(fv), _p(tu), C.byref(si), _p(ao), C.byref(so))
+    return out
+
+
+class OBlockTextures(C.Structure):   # vpto_block_textures
+    _fields_ = [("size", C.c_int32), ("albedo", C.c_void_p), ("albedo_layers", C.c_int32),
+                ("normal", C.c_void_p), ("normal_layers", C.c_int32), ("pbr", C.c_void_p),
+                ("pbr_layers", C.c_int32), ("emissive", C.c_void_p), ("emissive_layers", C.c_int32),
+                ("albedo_id", C.c_int32 * 128), ("normal_id", C.c_int32 * 128), ("pbr_id", C.c_int32 * 128),
+                ("emissive_id", C.c_int32 * 128), ("grass", C.c_int32 * 10)]
+
+
+def generate_gbuffer(cam, config, textures: dict, t, face, block) -> dict:
+    """The textured G-buffer pass (GenerateGBuffer.glsl main) over the
+    G-buffer t / face / block with the block textures (a dict as
+    generate_block_textures makes): albedo (3), normal (3), pbr (4), ao."""
+    p = params(config)
+    H, W = p.height, p.width
+    keep = {k: np.ascontiguousarray(textures[k], np.uint8) for k in ("albedo", "normal", "pbr")}
+    if textures.get("emissive") is not None:
+        keep["emissive"] = np.ascontiguousarray(textures["emissive"], np.uint8)
+    bt = OBlockTextures()
+    bt.size = int(textures["size"])
+    for k, arr in keep.items():
+        setattr(bt, k, arr.ctypes.data)
+        setattr(bt, f"{k}_layers", int(arr.shape[0]))
+    for k in ("albedo_id", "normal_id", "pbr_id", "emissive_id"):
+        getattr(bt, k)[:] = [int(v) for v in np.asarray(textures[k], np.int64)[:128]]
+    bt.grass[:] = [int(v) for v in np.asarray(textures["grass"], np.int64)[:10]]
+    out = {"albedo": np.zeros((H, W, 3), np.float32), "normal": np.zeros((H, W, 3), np.float32),
+           "pbr": np.zeros((H, W, 4), np.float32), "ao": np.zeros((H, W), np.float32)}
+    ts, fs, bs = (np.ascontiguousarray(a, dtype=dt) for a, dt in ((t, np.float32), (face, np.uint8),
+                                                                  (block, np.uint8)))
+    lib().vpto_generate_gbuffer(C.byref(_as(OCamera, cam)), C.byref(p), C.byref(bt), _p(ts), _p(fs), _p(bs),
+                                _p(out["albedo"]), _p(out["normal"]), _p(out["pbr"]), _p(out["ao"]))
     return out
 
 

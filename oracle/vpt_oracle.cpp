@@ -2201,3 +2201,220 @@ void vpto_ground_truth(const vpto_world* w, const vpto_camera* cam, const vpto_p
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Textured G-buffer: GenerateGBuffer.glsl main (:347-419) with parallax off
+// (u_POM, Core/Pipeline.cpp:264) and no lava block, sampling the block
+// texture arrays (Core/BlockDatabase.cpp:60-90) as the CUDA path defines
+// GL's texture fetches: REPEAT wrap, LINEAR / LINEAR_MIPMAP_LINEAR with an
+// isotropic level of detail log2(max(|dP/dx|, |dP/dy|) * size), fp32 bilinear
+// weights, texel = byte / 255 (sRGB-decoded for albedo), mip levels the
+// rounded 2 x 2 mean per 8-bit channel, and dFdx / dFdy the fine differences
+// inside the 2 x 2 pixel quad with the partner's position projected onto this
+// pixel's face axes (zero for a partner outside the image).
+namespace {
+
+struct OTexArray {
+    std::vector<uint8_t> texels;
+    std::vector<long long> level_off;
+    int layers = 0, channels = 0, size = 0, levels = 0;
+};
+
+OTexArray build_tex_array(const uint8_t* src, int layers, int channels, int size) {
+    OTexArray a;
+    a.layers = layers;
+    a.channels = channels;
+    a.size = size;
+    int levels = 1;
+    while ((size >> (levels - 1)) > 1) levels++;
+    a.levels = levels;
+    long long off = 0;
+    for (int l = 0; l < levels; l++) {
+        a.level_off.push_back(off);
+        off += (long long)layers * (size >> l) * (size >> l);
+    }
+    a.texels.assign((size_t)off * channels, 0);
+    std::memcpy(a.texels.data(), src, (size_t)layers * size * size * channels);
+    for (int l = 0; l + 1 < levels; l++) {
+        const int s1 = size >> l, s2 = size >> (l + 1);
+        const uint8_t* in = a.texels.data() + a.level_off[l] * channels;
+        uint8_t* out = a.texels.data() + a.level_off[l + 1] * channels;
+        for (int layer = 0; layer < layers; layer++)
+            for (int y = 0; y < s2; y++)
+                for (int x = 0; x < s2; x++)
+                    for (int c = 0; c < channels; c++) {
+                        const uint8_t* r0 = in + (((size_t)layer * s1 + 2 * y) * s1 + 2 * x) * channels;
+                        const uint8_t* r1 = r0 + (size_t)s1 * channels;
+                        out[(((size_t)layer * s2 + y) * s2 + x) * channels + c] =
+                            (uint8_t)(((int)r0[c] + (int)r0[channels + c] + (int)r1[c] + (int)r1[channels + c] + 2) >> 2);
+                    }
+    }
+    return a;
+}
+
+float tex_value(uint8_t v, const float* srgb) { return srgb ? srgb[v] : (float)v / 255.0f; }
+
+void tex_bilinear(const OTexArray& a, int level, int layer, float u, float v, int nch, const float* srgb, float* out) {
+    const int sl = a.size >> level;
+    const float x = u * (float)sl - 0.5f, y = v * (float)sl - 0.5f;
+    const float x0 = std::floor(x), y0 = std::floor(y);
+    const float ax = x - x0, ay = y - y0, bx = 1.0f - ax, by = 1.0f - ay;
+    const int i0 = wrapi(f2i(x0), sl), j0 = wrapi(f2i(y0), sl);
+    const int i1 = i0 + 1 == sl ? 0 : i0 + 1, j1 = j0 + 1 == sl ? 0 : j0 + 1;
+    const uint8_t* base = a.texels.data() + (a.level_off[level] + (long long)layer * sl * sl) * a.channels;
+    const uint8_t* p00 = base + ((size_t)j0 * sl + i0) * a.channels;
+    const uint8_t* p10 = base + ((size_t)j0 * sl + i1) * a.channels;
+    const uint8_t* p01 = base + ((size_t)j1 * sl + i0) * a.channels;
+    const uint8_t* p11 = base + ((size_t)j1 * sl + i1) * a.channels;
+    for (int c = 0; c < nch; c++) {
+        const float v00 = tex_value(p00[c], srgb), v10 = tex_value(p10[c], srgb);
+        const float v01 = tex_value(p01[c], srgb), v11 = tex_value(p11[c], srgb);
+        const float lo = v00 * bx + v10 * ax;
+        const float hi = v01 * bx + v11 * ax;
+        out[c] = lo * by + hi * ay;
+    }
+}
+
+float tex_lod(int size, float dxu, float dxv, float dyu, float dyv) {
+    const float s = (float)size;
+    const float ax = dxu * s, ay = dxv * s, bx = dyu * s, by = dyv * s;
+    const float rx = std::sqrt(ax * ax + ay * ay), ry = std::sqrt(bx * bx + by * by);
+    return dm_log2(fmaxg(rx, ry));
+}
+
+void tex_sample(const OTexArray& a, int layer_id, float u, float v, float lam, int nch, const float* srgb, float* out) {
+    const int layer = std::min(std::max(layer_id, 0), a.layers - 1);
+    const int q = a.levels - 1;
+    if (!(lam > 0.0f)) {
+        tex_bilinear(a, 0, layer, u, v, nch, srgb, out);
+        return;
+    }
+    if (lam >= (float)q) {
+        tex_bilinear(a, q, layer, u, v, nch, srgb, out);
+        return;
+    }
+    const float d1f = std::floor(lam);
+    const int d1 = (int)d1f;
+    const float f = lam - d1f;
+    float t1[4], t2[4];
+    tex_bilinear(a, d1, layer, u, v, nch, srgb, t1);
+    tex_bilinear(a, d1 + 1, layer, u, v, nch, srgb, t2);
+    for (int c = 0; c < nch; c++) out[c] = (1.0f - f) * t1[c] + f * t2[c];
+}
+
+// CalculateVectors' face coordinates: (x, y) for +-Z, (x, z) for +-Y, (z, y) for +-X
+v2 face_coords(v3 p, int f) {
+    const int axis = f >> 1;
+    return axis == 0 ? v2{p.x, p.y} : (axis == 1 ? v2{p.x, p.z} : v2{p.z, p.y});
+}
+
+v3 gbuffer_position(const vpto_camera* cam, int W, int H, const float* t, int i, int j, float* dist) {
+    const float d = 1.0f / (1.0f / t[(size_t)j * W + i]);
+    *dist = d;
+    return add(ray_origin(cam), muls(normalize(ray_dir_at(cam, texcoord(i, j, W, H))), d));
+}
+
+float quad_diff(bool odd, float self, float partner) { return odd ? self - partner : partner - self; }
+float dot2(v2 a) { return a.x * a.x + a.y * a.y; }
+
+}  // namespace
+
+extern "C" void vpto_generate_gbuffer(const vpto_camera* cam, const vpto_params* p, const vpto_block_textures* tx,
+                                      const float* t, const uint8_t* face, const uint8_t* block, float* albedo,
+                                      float* normal, float* pbr, float* ao) {
+    const int W = p->width, H = p->height, fp16 = p->storage, S = tx->size;
+    const OTexArray A = build_tex_array(tx->albedo, tx->albedo_layers, 4, S);
+    const OTexArray N_ = build_tex_array(tx->normal, tx->normal_layers, 4, S);
+    const OTexArray P_ = build_tex_array(tx->pbr, tx->pbr_layers, 4, S);
+    OTexArray E;
+    if (tx->emissive) E = build_tex_array(tx->emissive, tx->emissive_layers, 1, S);
+    // sRGB decode of a byte (IEC 61966-2-1)
+    float srgb[256];
+    for (int v = 0; v < 256; v++) {
+        const float x = (float)v / 255.0f;
+        srgb[v] = x <= 0.04045f ? x / 12.92f : dm_pow((x + 0.055f) / 1.055f, 2.4f);
+    }
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int j = 0; j < H; j++) {
+        for (int i = 0; i < W; i++) {
+            const size_t px = (size_t)j * W + i;
+            float dist;
+            const v3 pos = gbuffer_position(cam, W, H, t, i, j, &dist);
+            if (dist < 0.0f) {
+                for (int c = 0; c < 3; c++) {
+                    albedo[px * 3 + c] = storage(0.0f, fp16);
+                    normal[px * 3 + c] = storage(1.0f, fp16);
+                }
+                for (int c = 0; c < 4; c++) pbr[px * 4 + c] = storage(0.0f, fp16);
+                ao[px] = storage(0.0f, fp16);
+                continue;
+            }
+            const int f = std::min((int)face[px], 5);
+            const int bid = std::min(std::max((int)block[px], 0), 127);
+            const v2 P = face_coords(pos, f);
+            const v2 F{fract(P.x), fract(P.y)};
+            const v2 O{fract(F.x + 0.25f), fract(F.y + 0.25f)};
+            const int ix = i ^ 1, jy = j ^ 1;
+            v2 Fx = F, Ox = O, Fy = F, Oy = O;
+            if (ix < W) {
+                float dn;
+                const v2 Pn = face_coords(gbuffer_position(cam, W, H, t, ix, j, &dn), f);
+                Fx = v2{fract(Pn.x), fract(Pn.y)};
+                Ox = v2{fract(Fx.x + 0.25f), fract(Fx.y + 0.25f)};
+            }
+            if (jy < H) {
+                float dn;
+                const v2 Pn = face_coords(gbuffer_position(cam, W, H, t, i, jy, &dn), f);
+                Fy = v2{fract(Pn.x), fract(Pn.y)};
+                Oy = v2{fract(Fy.x + 0.25f), fract(Fy.y + 0.25f)};
+            }
+            const bool ox = i & 1, oy = j & 1;
+            v2 dx{quad_diff(ox, F.x, Fx.x), quad_diff(ox, F.y, Fx.y)};
+            v2 dy{quad_diff(oy, F.x, Fy.x), quad_diff(oy, F.y, Fy.y)};
+            const v2 dx2{quad_diff(ox, O.x, Ox.x), quad_diff(ox, O.y, Ox.y)};
+            const v2 dy2{quad_diff(oy, O.x, Oy.x), quad_diff(oy, O.y, Oy.y)};
+            if (dot2(dx) + dot2(dy) > dot2(dx2) + dot2(dy2)) {
+                dx = dx2;
+                dy = dy2;
+            }
+            int ia = tx->albedo_id[bid], in_ = tx->normal_id[bid], ip = tx->pbr_id[bid];
+            const int ie = tx->emissive ? tx->emissive_id[bid] : -1;
+            if (bid == tx->grass[0]) {
+                const int k = f == 2 ? 1 : (f == 3 ? 7 : 4);
+                ia = tx->grass[k];
+                in_ = tx->grass[k + 1];
+                ip = tx->grass[k + 2];
+            }
+            const v2 uv{1.0f - F.x, 1.0f - F.y};
+            const float lam = tex_lod(S, dx.x, dx.y, dy.x, dy.y);
+            const v3 T = f < 4 ? mk3(1.0f, 0.0f, 0.0f) : mk3(0.0f, 0.0f, -1.0f);
+            const v3 B = f < 2 ? mk3(0.0f, 1.0f, 0.0f) : (f < 4 ? mk3(0.0f, 0.0f, 1.0f) : mk3(0.0f, -1.0f, 0.0f));
+            const v3 Nf = normal_from_id(f, 1.0f);
+            float nm[4], pb[4], al[4];
+            tex_sample(N_, in_, uv.x, uv.y, lam, 3, nullptr, nm);
+            for (int c = 0; c < 3; c++) nm[c] = nm[c] * 2.0f - 1.0f;
+            const v3 nmap = mk3((T.x * nm[0] + B.x * nm[1]) + Nf.x * nm[2], (T.y * nm[0] + B.y * nm[1]) + Nf.y * nm[2],
+                                (T.z * nm[0] + B.z * nm[1]) + Nf.z * nm[2]);
+            tex_sample(P_, ip, uv.x, uv.y, lam, 4, nullptr, pb);
+            float emis = 0.0f;
+            if (ie > -1) {
+                const v2 ux{1.0f - Fx.x, 1.0f - Fx.y}, uy{1.0f - Fy.x, 1.0f - Fy.y};
+                const float lam_e = tex_lod(S, quad_diff(ox, uv.x, ux.x), quad_diff(ox, uv.y, ux.y),
+                                            quad_diff(oy, uv.x, uy.x), quad_diff(oy, uv.y, uy.y));
+                float e[4];
+                tex_sample(E, ie, uv.x, uv.y, lam_e, 1, nullptr, e);
+                emis = e[0];
+            }
+            tex_sample(A, ia, uv.x, uv.y, lam, 3, srgb, al);
+            const float lb = 0.02f;
+            const float inside = (uv.x > lb && uv.x < 1.0f - lb && uv.y > lb && uv.y < 1.0f - lb) ? 1.0f : 0.0f;
+            for (int c = 0; c < 3; c++) albedo[px * 3 + c] = storage(al[c], fp16);
+            normal[px * 3 + 0] = storage(nmap.x, fp16);
+            normal[px * 3 + 1] = storage(nmap.y, fp16);
+            normal[px * 3 + 2] = storage(nmap.z, fp16);
+            for (int c = 0; c < 3; c++) pbr[px * 4 + c] = storage(clampf(pb[c], 0.0f, 1.0f), fp16);
+            pbr[px * 4 + 3] = storage(clampf(emis, 0.0f, 1.0f) * inside, fp16);
+            ao[px] = storage(clampf(pb[3], 0.00000001f, 1.0f), fp16);
+        }
+    }
+}

@@ -224,6 +224,31 @@ void vpto_ground_truth(const vpto_world* w, const vpto_camera* cam, const vpto_p
                        const float* t, const uint8_t* face, int x0, int y0, int cw, int ch, int spp, int chunk,
                        uint32_t seed, double* mean_out, double* m2_out);
 
+/* Block texture arrays, laid out as vpt_block_textures (level-0 texels;
+ * the oracle builds the mip levels itself). */
+typedef struct vpto_block_textures {
+    int32_t size;
+    const uint8_t* albedo;
+    int32_t albedo_layers;
+    const uint8_t* normal;
+    int32_t normal_layers;
+    const uint8_t* pbr;
+    int32_t pbr_layers;
+    const uint8_t* emissive;
+    int32_t emissive_layers;
+    int32_t albedo_id[128];
+    int32_t normal_id[128];
+    int32_t pbr_id[128];
+    int32_t emissive_id[128];
+    int32_t grass[10];
+} vpto_block_textures;
+
+/* GenerateGBuffer.glsl main (parallax off, no lava): albedo (3), normal (3),
+ * PBR (4) and texture AO (1) per pixel of the W x H G-buffer. */
+void vpto_generate_gbuffer(const vpto_camera* cam, const vpto_params* p, const vpto_block_textures* tx,
+                           const float* t, const uint8_t* face, const uint8_t* block, float* albedo, float* normal,
+                           float* pbr, float* ao);
+
 /* Deterministic math, exported so tests can check its error bounds. */
 float vpto_exp(float x);
 float vpto_exp2(float x);

@@ -24,7 +24,7 @@ def test_every_declared_symbol_is_exported(vpt):
 
 
 def test_abi_version_and_status_strings(vpt):
-    assert vpt.lib.vpt_abi_version() == 2
+    assert vpt.lib.vpt_abi_version() == 3
     for s in range(7):
         assert vpt.lib.vpt_status_string(s)
 

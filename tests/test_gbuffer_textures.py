@@ -1,0 +1,164 @@
+"""The textured G-buffer pass (GenerateGBuffer.glsl main with parallax off):
+block texture arrays sampled with textureGrad at the face UV. The CPU half
+checks the oracle's restatement against properties the shader fixes (sky
+texels, constant textures, the tangent basis, the grass override, the light
+leak fix, mip-level selection); the GPU half holds the CUDA pass to the
+oracle's bits through the C ABI."""
+import numpy as np
+import pytest
+
+from test_gpu_parity import assert_same
+
+W, H = 96, 64
+DIMS = (64, 64, 64)
+
+
+def scene(vpt, oracle, seed=1):
+    X, Y, Z = DIMS
+    vox = vpt.generate_world(X, Y, Z, seed=seed)
+    blocks = vpt.generate_block_table(100, seed=seed)
+    world = oracle.World(vox, oracle.build_df(vox), blocks)
+    yaw, pitch = vpt.seeded_pose(seed)
+    cams = [vpt.camera_from_pose((X / 2, 58.0, Z / 2), yaw, pitch, 90.0, W / H),
+            vpt.camera_from_pose((8.5, 42.0, 8.5), 30.0, -20.0, 90.0, W / H)]
+    return vox, blocks, world, cams
+
+
+def constant_textures(vpt, layers=4, size=8):
+    """Every layer one constant value per channel: layer l albedo (40 l + 20, 100, 200 - 30 l)."""
+    t = vpt.generate_block_textures(size, layers, seed=3)
+    for l in range(layers):
+        t["albedo"][l, ..., :3] = (40 * l + 20, 100, 200 - 30 * l)
+        t["normal"][l, ..., :3] = (128, 128, 255)
+        t["pbr"][l] = (30 + 40 * l, 0, 128, 200)
+        t["emissive"][l] = 255
+    return t
+
+
+def srgb(b):
+    x = np.float32(b) / np.float32(255.0)
+    return x / np.float32(12.92) if x <= 0.04045 else ((x + 0.055) / 1.055) ** 2.4
+
+
+# ------------------------------------------------------------------ CPU --
+def test_oracle_gbuffer_sky_and_constant_textures(vpt, oracle):
+    vox, blocks, world, cams = scene(vpt, oracle)
+    cfg = vpt.default_config(width=W, height=H, primary_max_steps=256)
+    tex = constant_textures(vpt)
+    g = oracle.trace_primary(world, cams[0], cfg)
+    gb = oracle.generate_gbuffer(cams[0], cfg, tex, g["t"], g["face"], g["block"])
+    sky, hit = g["t"] < 0, g["t"] > 0
+    assert sky.any() and hit.any()
+    assert (gb["albedo"][sky] == 0).all() and (gb["normal"][sky] == 1).all()
+    assert (gb["pbr"][sky] == 0).all() and (gb["ao"][sky] == 0).all()
+    # constant layers: every level and every filter weight gives the layer's value
+    ids = tex["albedo_id"][g["block"][hit]]
+    grass = g["block"][hit] == tex["grass"][0]
+    face = g["face"][hit]
+    layer = np.where(grass, np.where(face == 2, tex["grass"][1], np.where(face == 3, tex["grass"][7],
+                                                                           tex["grass"][4])), ids)
+    want = np.array([[srgb(40 * l + 20), srgb(100), srgb(200 - 30 * l)] for l in range(4)], np.float32)
+    np.testing.assert_allclose(gb["albedo"][hit], want[np.clip(layer, 0, 3)], rtol=2e-6)
+    # the flat normal map gives the face normal plus the (1/255) tangent and bitangent tilt
+    n_face = np.array([[0, 0, 1], [0, 0, -1], [0, 1, 0], [0, -1, 0], [-1, 0, 0], [1, 0, 0]], np.float32)
+    tang = np.array([[1, 0, 0]] * 4 + [[0, 0, -1]] * 2, np.float32)
+    bitang = np.array([[0, 1, 0]] * 2 + [[0, 0, 1]] * 2 + [[0, -1, 0]] * 2, np.float32)
+    e = np.float32(128) / np.float32(255) * 2 - 1
+    np.testing.assert_allclose(gb["normal"][hit], n_face[face] + e * (tang[face] + bitang[face]), atol=1e-6)
+    pl = np.where(grass, np.where(face == 2, tex["grass"][3], np.where(face == 3, tex["grass"][9],
+                                                                        tex["grass"][6])), tex["pbr_id"][g["block"][hit]])
+    np.testing.assert_allclose(gb["pbr"][hit][:, 0], (30 + 40 * np.clip(pl, 0, 3)) / 255.0, rtol=2e-6)
+    np.testing.assert_allclose(gb["ao"][hit], 200 / 255.0, rtol=2e-6)
+    # emissive texture of 1: 1 inside the face, 0 in its 2% border band (BloomLightLeakFix)
+    em = gb["pbr"][hit][:, 3]
+    has = tex["emissive_id"][g["block"][hit]] > -1
+    assert set(np.unique(em[has])) <= {0.0, 1.0} and (em[has] == 1).mean() > 0.8
+    assert (em[~has] == 0).all()
+
+
+def test_oracle_gbuffer_grass_override(vpt, oracle):
+    """A grass block's top, side and bottom faces read their own layers."""
+    vox, blocks, world, cams = scene(vpt, oracle)
+    cfg = vpt.default_config(width=W, height=H, primary_max_steps=256)
+    tex = constant_textures(vpt)
+    g = oracle.trace_primary(world, cams[0], cfg)
+    common = np.bincount(g["block"][g["t"] > 0]).argmax()
+    tex["grass"][:] = (common, 0, 0, 0, 1, 1, 1, 2, 2, 2)
+    tex["albedo_id"][:] = 3
+    gb = oracle.generate_gbuffer(cams[0], cfg, tex, g["t"], g["face"], g["block"])
+    sel = (g["block"] == common) & (g["t"] > 0)
+    want = {2: 0, 3: 2, 0: 1, 1: 1, 4: 1, 5: 1}
+    for f, l in want.items():
+        m = sel & (g["face"] == f)
+        if m.any():
+            np.testing.assert_allclose(gb["albedo"][m][:, 0], srgb(40 * l + 20), rtol=2e-6)
+    other = (g["block"] != common) & (g["t"] > 0)
+    np.testing.assert_allclose(gb["albedo"][other][:, 0], srgb(40 * 3 + 20), rtol=2e-6)
+
+
+def test_oracle_gbuffer_filters_towards_the_mean_with_distance(vpt, oracle):
+    """A texel checkerboard: near faces resolve it, far faces read the coarse
+    mip levels, whose texels are all the mean."""
+    vox, blocks, world, cams = scene(vpt, oracle)
+    cfg = vpt.default_config(width=W, height=H, primary_max_steps=256)
+    tex = constant_textures(vpt, size=32)
+    yy, xx = np.meshgrid(np.arange(32), np.arange(32), indexing="ij")
+    tex["pbr"][..., 0] = np.where((xx + yy) % 2 == 0, 0, 254).astype(np.uint8)[None]
+    g = oracle.trace_primary(world, cams[1], cfg)
+    gb = oracle.generate_gbuffer(cams[1], cfg, tex, g["t"], g["face"], g["block"])
+    hit = g["t"] > 0
+    r = gb["pbr"][..., 0]
+    near, far = hit & (g["t"] < 6), hit & (g["t"] > 30)
+    assert near.sum() > 20 and far.sum() > 20
+    assert np.abs(r[far] - 127 / 255.0).mean() < np.abs(r[near] - 127 / 255.0).mean()
+
+
+# ------------------------------------------------------------------ GPU --
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage,size,emissive", [(0, 16, True), (1, 16, True), (0, 64, False), (1, 8, True)],
+                         ids=["f32-16", "f16-16", "f32-64-no-emissive", "f16-8"])
+def test_gbuffer_planes_bit_exact(vpt, oracle, storage, size, emissive, gpu):
+    vox, blocks, world, cams = scene(vpt, oracle, seed=2)
+    solid = vox[vox > 0]
+    tex = vpt.generate_block_textures(size, 7, seed=size, emissive=emissive,
+                                      grass_block=int(np.bincount(solid).argmax()))   # the most common block
+    with vpt.Context(width=W, height=H, primary_max_steps=256, storage=storage) as ctx:
+        ctx.upload_world(vox)
+        ctx.set_block_table(blocks)
+        ctx.build_df()
+        ctx.set_block_textures(tex)
+        cfg = ctx.config
+        for k, cam in enumerate(cams):
+            ctx.trace_primary(cam)
+            ctx.generate_gbuffer()
+            g = oracle.trace_primary(world, cam, cfg)
+            ref = oracle.generate_gbuffer(cam, cfg, tex, g["t"], g["face"], g["block"])
+            assert_same(ctx.read_plane("GB_ALBEDO"), ref["albedo"], f"cam {k} albedo")
+            assert_same(ctx.read_plane("GB_NORMAL"), ref["normal"], f"cam {k} normal")
+            assert_same(ctx.read_plane("GB_PBR"), ref["pbr"], f"cam {k} pbr")
+            assert_same(ctx.read_plane("GB_AO")[..., 0], ref["ao"], f"cam {k} ao")
+            ctx.end_frame()
+
+
+@pytest.mark.gpu
+def test_gbuffer_needs_textures_and_a_gbuffer(vpt, oracle, gpu):
+    vox, blocks, world, cams = scene(vpt, oracle)
+    with vpt.Context(width=W, height=H) as ctx:
+        ctx.upload_world(vox)
+        ctx.set_block_table(blocks)
+        ctx.build_df()
+        with pytest.raises(vpt.VPTError):
+            ctx.read_plane("GB_ALBEDO")
+        ctx.trace_primary(cams[0])
+        with pytest.raises(vpt.VPTError):
+            ctx.generate_gbuffer()
+        bad = vpt.generate_block_textures(8, 2)
+        bad["size"] = 12
+        with pytest.raises(vpt.VPTError):
+            ctx.set_block_textures(bad)
+        ctx.set_block_textures(vpt.generate_block_textures(8, 2))
+        ctx.generate_gbuffer()
+        assert ctx.read_plane("GB_PBR").shape == (H, W, 4)
+        ctx.set_block_textures(None)
+        with pytest.raises(vpt.VPTError):
+            ctx.generate_gbuffer()

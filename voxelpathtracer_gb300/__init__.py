@@ -42,10 +42,11 @@ PLANES = [
     "VAR_SH", "VAR_COCG", "VAR_VARIANCE",
     "DEN_SH", "DEN_COCG", "DEN_VARIANCE", "DEN_AOSKY",
     "COLOR", "SPEC", "SPEC_HIT", "SPEC_MASK", "SPEC_OUT", "SPEC_ACC", "SPEC_STABLE_HIT", "SPEC_DEN",
+    "GB_ALBEDO", "GB_NORMAL", "GB_PBR", "GB_AO",
 ]
 PLANE = {name: i for i, name in enumerate(PLANES)}
 PASSES = ["primary", "shadow", "diffuse", "spatial_initial", "temporal", "variance", "atrous", "shade", "trace_frame",
-          "learned", "reflection"]
+          "learned", "reflection", "gbuffer"]
 RAY_KINDS = ["primary", "shadow", "diffuse", "bounce_shadow", "reflection", "reflection_shadow"]
 FACE_MISS = 10
 
@@ -65,6 +66,15 @@ class Config(C.Structure):
 class Camera(C.Structure):
     _fields_ = [("view", C.c_float * 16), ("proj", C.c_float * 16), ("inv_view", C.c_float * 16),
                 ("inv_proj", C.c_float * 16), ("position", C.c_float * 3), ("pad", C.c_float)]
+
+
+class BlockTextures(C.Structure):
+    """vpt_block_textures: the four block texture arrays and their per-block layer ids."""
+    _fields_ = [("size", C.c_int32), ("albedo", C.c_void_p), ("albedo_layers", C.c_int32),
+                ("normal", C.c_void_p), ("normal_layers", C.c_int32), ("pbr", C.c_void_p),
+                ("pbr_layers", C.c_int32), ("emissive", C.c_void_p), ("emissive_layers", C.c_int32),
+                ("albedo_id", C.c_int32 * 128), ("normal_id", C.c_int32 * 128), ("pbr_id", C.c_int32 * 128),
+                ("emissive_id", C.c_int32 * 128), ("grass", C.c_int32 * 10)]
 
 
 class Block(C.Structure):
@@ -147,6 +157,8 @@ def _load() -> C.CDLL:
         "vpt_last_error": ([P], C.c_char_p),
         "vpt_upload_world": ([P, P, i32, i32, i32], C.c_int),
         "vpt_set_block_table": ([P, P, i32], C.c_int),
+        "vpt_set_block_textures": ([P, C.POINTER(BlockTextures)], C.c_int),
+        "vpt_generate_gbuffer": ([P], C.c_int),
         "vpt_build_df": ([P], C.c_int),
         "vpt_read_df": ([P, P, sz], C.c_int),
         "vpt_df_build_device": ([P, P, i32, i32, i32, P], C.c_int),
@@ -291,6 +303,79 @@ def generate_block_table(n: int = 100, seed: int = 0) -> np.ndarray:
     return out
 
 
+def generate_block_textures(size: int = 32, layers: int = 12, n_blocks: int = 100, seed: int = 0,
+                            emissive: bool = True, grass_block: int = 1) -> dict:
+    """Seeded synthetic block texture arrays standing in for the reference's
+    block PNGs: per layer a base colour with a two-scale noise pattern
+    (albedo, sRGB-encoded), a normal map tilted around (0.5, 0.5, 1), PBR maps
+    (roughness, metalness, displacement, AO) and sparse emissive masks; every
+    block gets a layer in each array (emissive for about one block in five)
+    and block `grass_block` (-1: none) gets separate top / side / bottom layers."""
+    if size < 1 or size & (size - 1):
+        raise ValueError("size must be a power of two")
+    rng = np.random.default_rng(seed)
+    yy, xx = np.meshgrid(np.arange(size), np.arange(size), indexing="ij")
+
+    def pattern(k):
+        f1, f2 = rng.integers(1, 4, size=2)
+        ph = rng.uniform(0, 2 * np.pi, size=2)
+        coarse = np.sin(2 * np.pi * f1 * xx / size + ph[0]) * np.cos(2 * np.pi * f2 * yy / size + ph[1])
+        return 0.5 + 0.25 * coarse + 0.25 * (rng.random((size, size)) - 0.5)
+
+    def u8(a):
+        return np.clip(np.round(a * 255.0), 0, 255).astype(np.uint8)
+
+    alb = np.empty((layers, size, size, 4), np.uint8)
+    nrm = np.empty((layers, size, size, 4), np.uint8)
+    pbr = np.empty((layers, size, size, 4), np.uint8)
+    for l in range(layers):
+        base = rng.uniform(0.15, 0.9, size=3)
+        p = pattern(l)
+        alb[l, ..., :3] = u8(base[None, None, :] * (0.6 + 0.8 * p[..., None] * 0.5))
+        alb[l, ..., 3] = 255
+        tilt = 0.35 * (pattern(l) - 0.5)
+        tilt2 = 0.35 * (pattern(l) - 0.5)
+        n = np.stack([tilt, tilt2, np.ones_like(tilt)], axis=-1)
+        n /= np.linalg.norm(n, axis=-1, keepdims=True)
+        nrm[l, ..., :3] = u8(n * 0.5 + 0.5)
+        nrm[l, ..., 3] = 255
+        pbr[l, ..., 0] = u8(np.clip(rng.uniform(0.2, 0.9) + 0.3 * (pattern(l) - 0.5), 0, 1))
+        pbr[l, ..., 1] = u8(np.full((size, size), 1.0 if rng.random() < 0.15 else 0.0))
+        pbr[l, ..., 2] = u8(pattern(l))
+        pbr[l, ..., 3] = u8(np.clip(0.75 + 0.5 * (pattern(l) - 0.5), 0, 1))
+    emi = None
+    if emissive:
+        emi = u8((rng.random((layers, size, size)) < 0.3) * rng.uniform(0.3, 1.0, size=(layers, 1, 1)))
+    ids = rng.integers(0, layers, size=(4, 128)).astype(np.int32)
+    if emissive:
+        ids[3] = np.where(rng.random(128) < 0.2, ids[3], -1)
+    else:
+        ids[3] = -1
+    grass = np.full(10, -1, np.int32)
+    if grass_block >= 0:
+        grass[0] = grass_block
+        grass[1:] = rng.integers(0, layers, size=9)
+    return {"size": size, "albedo": alb, "normal": nrm, "pbr": pbr, "emissive": emi, "albedo_id": ids[0],
+            "normal_id": ids[1], "pbr_id": ids[2], "emissive_id": ids[3], "grass": grass}
+
+
+def block_textures_struct(t: dict):
+    """(vpt_block_textures, the arrays it points into) for a texture dict."""
+    keep = {k: np.ascontiguousarray(t[k], np.uint8) for k in ("albedo", "normal", "pbr")}
+    if t.get("emissive") is not None:
+        keep["emissive"] = np.ascontiguousarray(t["emissive"], np.uint8)
+    bt = BlockTextures()
+    bt.size = int(t["size"])
+    for k in ("albedo", "normal", "pbr", "emissive"):
+        if k in keep:
+            setattr(bt, k, keep[k].ctypes.data)
+            setattr(bt, f"{k}_layers", int(keep[k].shape[0]))
+    for k in ("albedo_id", "normal_id", "pbr_id", "emissive_id"):
+        getattr(bt, k)[:] = [int(v) for v in np.asarray(t[k], np.int64)[:128]]
+    bt.grass[:] = [int(v) for v in np.asarray(t["grass"], np.int64)[:10]]
+    return bt, keep
+
+
 def camera_from_pose(position, yaw_deg: float, pitch_deg: float, fov_deg: float = 90.0, aspect: float = 16 / 9,
                      znear: float = 0.1, zfar: float = 1000.0) -> Camera:
     cam = Camera()
@@ -426,6 +511,20 @@ class Context:
 
     def build_df(self):
         self._ck(lib.vpt_build_df(self._h), "vpt_build_df")
+
+    def set_block_textures(self, textures):
+        """Uploads block texture arrays (a dict as generate_block_textures makes; None removes them)."""
+        if textures is None:
+            self._ck(lib.vpt_set_block_textures(self._h, None), "vpt_set_block_textures")
+            self._textures = None
+            return
+        bt, keep = block_textures_struct(textures)
+        self._ck(lib.vpt_set_block_textures(self._h, C.byref(bt)), "vpt_set_block_textures")
+        self._textures = keep
+
+    def generate_gbuffer(self):
+        """GenerateGBuffer: the GB_ALBEDO / GB_NORMAL / GB_PBR / GB_AO planes of this frame."""
+        self._ck(lib.vpt_generate_gbuffer(self._h), "vpt_generate_gbuffer")
 
     def edit_world(self, origin, voxels: np.ndarray):
         """Writes the (d, h, w) block of voxels at origin (x0, y0, z0) and updates the distance field locally."""

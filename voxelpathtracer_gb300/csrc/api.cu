@@ -51,6 +51,9 @@ PlaneMeta plane_meta(int plane) {
         case VPT_PLANE_SPEC: case VPT_PLANE_SPEC_OUT: case VPT_PLANE_SPEC_DEN: return {4, 1, 0, 1};
         case VPT_PLANE_SPEC_HIT: case VPT_PLANE_SPEC_MASK: case VPT_PLANE_SPEC_ACC:
         case VPT_PLANE_SPEC_STABLE_HIT: return {1, 1, 0, 1};
+        case VPT_PLANE_GB_ALBEDO: case VPT_PLANE_GB_NORMAL: return {3, 1, 0, 0};
+        case VPT_PLANE_GB_PBR: return {4, 1, 0, 0};
+        case VPT_PLANE_GB_AO: return {1, 1, 0, 0};
         default: return {0, 0, -1, 0};
     }
 }
@@ -132,6 +135,16 @@ struct vpt_ctx {
     void* feat = nullptr;
     void* color_raw = nullptr;
     cudaEvent_t ev_net[2] = {};
+    // block textures: each array's texels with all mip levels, the per-block
+    // layer ids, the sRGB decode table, and the textured G-buffer planes
+    // (albedo 3, normal 3, PBR 4, AO 1 channels)
+    uint8_t* tex[4] = {};
+    TexArray tex_arr[4] = {};
+    int* tex_ids = nullptr;
+    float* srgb = nullptr;
+    int tex_grass[10] = {};
+    bool textured = false;
+    void* gbt[4] = {};
 };
 
 namespace {
@@ -234,6 +247,10 @@ void* plane_ptr(vpt_ctx* c, int plane) {
         case VPT_PLANE_SPEC_ACC: return c->racc;
         case VPT_PLANE_SPEC_STABLE_HIT: return c->rstable[cur];
         case VPT_PLANE_SPEC_DEN: return c->rden;
+        case VPT_PLANE_GB_ALBEDO: return c->gbt[0];
+        case VPT_PLANE_GB_NORMAL: return c->gbt[1];
+        case VPT_PLANE_GB_PBR: return c->gbt[2];
+        case VPT_PLANE_GB_AO: return c->gbt[3];
         default: return nullptr;
     }
 }
@@ -561,6 +578,112 @@ vpt_status vpt_set_block_table(vpt_ctx* c, const vpt_block* table, int32_t n) {
     CK(c, cudaMemcpyAsync(c->blocks, table, (size_t)n * sizeof(vpt_block), cudaMemcpyHostToDevice, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
     c->n_blocks = n;
+    return VPT_OK;
+}
+
+namespace {
+void dfree(vpt_ctx* c, void** p) {
+    if (!*p) return;
+    for (size_t k = 0; k < c->allocs.size(); k++)
+        if (c->allocs[k] == *p) {
+            c->allocs.erase(c->allocs.begin() + (long)k);
+            break;
+        }
+    cudaFree(*p);
+    *p = nullptr;
+}
+}  // namespace
+
+vpt_status vpt_set_block_textures(vpt_ctx* c, const vpt_block_textures* t) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    cudaSetDevice(c->dev);
+    CK(c, cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < 4; k++) dfree(c, (void**)&c->tex[k]);
+    dfree(c, (void**)&c->tex_ids);
+    dfree(c, (void**)&c->srgb);
+    c->textured = false;
+    if (!t) return VPT_OK;
+    const int S = t->size;
+    if (S < 1 || S > 1024 || (S & (S - 1)))
+        return fail(c, VPT_ERR_INVALID_ARG, "texture size must be a power of two in 1..1024");
+    const uint8_t* src[4] = {t->albedo, t->normal, t->pbr, t->emissive};
+    const int layers[4] = {t->albedo_layers, t->normal_layers, t->pbr_layers, t->emissive ? t->emissive_layers : 0};
+    const int chans[4] = {4, 4, 4, 1};
+    for (int k = 0; k < 3; k++)
+        if (!src[k] || layers[k] < 1 || layers[k] > 4096)
+            return fail(c, VPT_ERR_INVALID_ARG, "albedo, normal and PBR arrays need 1..4096 layers");
+    if (t->emissive && (layers[3] < 1 || layers[3] > 4096))
+        return fail(c, VPT_ERR_INVALID_ARG, "the emissive array needs 1..4096 layers");
+    int levels = 1;
+    while ((S >> (levels - 1)) > 1) levels++;
+    vpt_status st;
+    for (int k = 0; k < 4; k++) {
+        TexArray& a = c->tex_arr[k];
+        a = TexArray{};
+        if (!src[k]) continue;
+        a.layers = layers[k];
+        a.channels = chans[k];
+        a.size = S;
+        a.levels = levels;
+        long long off = 0;
+        for (int l = 0; l < levels; l++) {
+            a.level_off[l] = off;
+            off += (long long)a.layers * (S >> l) * (S >> l);
+        }
+        if ((st = dalloc(c, (void**)&c->tex[k], (size_t)off * a.channels)) != VPT_OK) return st;
+        a.texels = c->tex[k];
+        CK(c, cudaMemcpyAsync(c->tex[k], src[k], (size_t)a.layers * S * S * a.channels, cudaMemcpyHostToDevice,
+                              c->stream));
+        for (int l = 0; l + 1 < levels; l++) CK(c, tex_build_mip(a, l, c->tex[k], c->stream));
+        c->launches += (uint64_t)(levels - 1);
+    }
+    // layer ids [albedo | normal | PBR | emissive] and the sRGB decode of a byte
+    // (IEC 61966-2-1: c / 12.92 up to 0.04045, else ((c + 0.055) / 1.055)^2.4)
+    std::vector<int> ids(512);
+    for (int b = 0; b < 128; b++) {
+        ids[b] = t->albedo_id[b];
+        ids[128 + b] = t->normal_id[b];
+        ids[256 + b] = t->pbr_id[b];
+        ids[384 + b] = t->emissive_id[b];
+    }
+    std::vector<float> lut(256);
+    for (int v = 0; v < 256; v++) {
+        const float x = (float)v / 255.0f;
+        lut[v] = x <= 0.04045f ? x / 12.92f : dpow((x + 0.055f) / 1.055f, 2.4f);
+    }
+    if ((st = dalloc(c, (void**)&c->tex_ids, ids.size() * sizeof(int))) != VPT_OK) return st;
+    if ((st = dalloc(c, (void**)&c->srgb, lut.size() * sizeof(float))) != VPT_OK) return st;
+    CK(c, cudaMemcpyAsync(c->tex_ids, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemcpyAsync(c->srgb, lut.data(), lut.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    for (int k = 0; k < 10; k++) c->tex_grass[k] = t->grass[k];
+    const size_t es = c->fp16 ? 2 : 4;
+    const size_t ch[4] = {3, 3, 4, 1};
+    for (int k = 0; k < 4; k++)
+        if (!c->gbt[k] && (st = dalloc(c, &c->gbt[k], c->npx * ch[k] * es)) != VPT_OK) return st;
+    CK(c, cudaStreamSynchronize(c->stream));
+    c->textured = true;
+    return VPT_OK;
+}
+
+vpt_status vpt_generate_gbuffer(vpt_ctx* c) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (!c->textured) return fail(c, VPT_ERR_STATE, "no block textures set (vpt_set_block_textures)");
+    if (!c->have_cam) return fail(c, VPT_ERR_STATE, "no G-buffer yet (call vpt_trace_primary)");
+    cudaSetDevice(c->dev);
+    BlockTexView tv;
+    tv.albedo = c->tex_arr[0];
+    tv.normal = c->tex_arr[1];
+    tv.pbr = c->tex_arr[2];
+    tv.emissive = c->tex_arr[3];
+    tv.ids = c->tex_ids;
+    for (int k = 0; k < 10; k++) tv.grass[k] = c->tex_grass[k];
+    tv.srgb = c->srgb;
+    pass_begin(c, VPT_PASS_GBUFFER);
+    CK(c, gbuffer_textured(cam_view(c->cam), c->cfg.width, c->cfg.height, c->fp16, c->gbuf[c->cur][GB_T],
+                           (const uint8_t*)c->gbuf[c->cur][GB_FACE], (const uint8_t*)c->gbuf[c->cur][GB_BLOCK], tv,
+                           c->gbt[0], c->gbt[1], c->gbt[2], c->gbt[3], c->stream));
+    pass_end(c, VPT_PASS_GBUFFER);
+    c->launches += 1;
     return VPT_OK;
 }
 
@@ -1229,7 +1352,7 @@ vpt_status vpt_read_plane(vpt_ctx* c, int32_t plane, void* host, size_t bytes) {
     if (!c || !host || plane < 0 || plane >= VPT_PLANE_COUNT) return VPT_ERR_INVALID_ARG;
     size_t need = plane_bytes(c, plane, nullptr, nullptr);
     if (bytes < need) return fail(c, VPT_ERR_INVALID_ARG, "buffer too small: %zu < %zu", bytes, need);
-    if (!plane_ptr(c, plane)) return fail(c, VPT_ERR_STATE, "plane %d is not allocated (reflections off)", plane);
+    if (!plane_ptr(c, plane)) return fail(c, VPT_ERR_STATE, "plane %d is not allocated (reflections or block textures off)", plane);
     cudaSetDevice(c->dev);
     CK(c, cudaMemcpyAsync(host, plane_ptr(c, plane), need, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
@@ -1240,7 +1363,7 @@ vpt_status vpt_write_plane(vpt_ctx* c, int32_t plane, const void* host, size_t b
     if (!c || !host || plane < 0 || plane >= VPT_PLANE_COUNT) return VPT_ERR_INVALID_ARG;
     size_t need = plane_bytes(c, plane, nullptr, nullptr);
     if (bytes != need) return fail(c, VPT_ERR_INVALID_ARG, "size mismatch: %zu != %zu", bytes, need);
-    if (!plane_ptr(c, plane)) return fail(c, VPT_ERR_STATE, "plane %d is not allocated (reflections off)", plane);
+    if (!plane_ptr(c, plane)) return fail(c, VPT_ERR_STATE, "plane %d is not allocated (reflections or block textures off)", plane);
     cudaSetDevice(c->dev);
     CK(c, cudaMemcpyAsync(plane_ptr(c, plane), host, need, cudaMemcpyHostToDevice, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));

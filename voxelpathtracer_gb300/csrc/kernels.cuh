@@ -304,6 +304,32 @@ cudaError_t learned_features(int W, int H, int x0, int y0, int w, int h, int fp1
                              const void* var, void* out, cudaStream_t s);
 cudaError_t learned_unpack(int W, int H, int fp16, const float* net_out, void* color, cudaStream_t s);
 
+// ---------------------------------------------------------- textures.cu --
+// One block texture array on the device: `layers` layers of `size`^2 texels
+// of `channels` 8-bit channels per mip level, levels stored one after the
+// other (level l: layers x (size >> l)^2 texels from element offset
+// level_off[l] * channels).
+struct TexArray {
+    const uint8_t* texels;
+    int layers, channels, size, levels;
+    long long level_off[11];
+};
+// The arrays, the per-block layer ids [albedo 128 | normal 128 | PBR 128 |
+// emissive 128], the grass override and the sRGB decode table (256 entries).
+struct BlockTexView {
+    TexArray albedo, normal, pbr, emissive;   // emissive.texels NULL: none
+    const int* ids;
+    int grass[10];
+    const float* srgb;
+};
+// Level l + 1 of every layer from level l (rounded 2 x 2 mean per channel).
+cudaError_t tex_build_mip(const TexArray& a, int level, uint8_t* texels, cudaStream_t s);
+// GenerateGBuffer.glsl main over the W x H G-buffer: albedo (3), normal (3),
+// PBR (4) and AO (1) planes in the storage type.
+cudaError_t gbuffer_textured(const CamView& cam, int W, int H, int fp16, const void* t, const uint8_t* face,
+                             const uint8_t* block, const BlockTexView& tv, void* albedo, void* normal, void* pbr,
+                             void* ao, cudaStream_t s);
+
 // Deterministic-math probe: evaluates op `op` (0 exp, 1 exp2, 2 log2, 3 pow,
 // 4 sin, 5 cos) over n inputs on the device.
 cudaError_t detmath_eval(int op, const float* x, const float* y, float* out, int n, cudaStream_t s);

@@ -1,0 +1,248 @@
+// Block texture arrays and the textured G-buffer pass (GenerateGBuffer.glsl).
+//
+// Sampling restates what the shader asks of OpenGL, with the choices the GL
+// specification leaves to the implementation fixed here:
+//   * textureGrad / texture on a GL_TEXTURE_2D_ARRAY with REPEAT wrap,
+//     LINEAR magnification and LINEAR_MIPMAP_LINEAR minification
+//     (BlockDatabase::SetTextureArraysFilteringLinear,
+//     Core/BlockDatabase.cpp:507-517): the level of detail is
+//     log2(max(|dP/dx|, |dP/dy|) * size) (isotropic; the 4x anisotropic
+//     filtering of Core/GLClasses/TextureArray.cpp:71-77 is not restated),
+//     lambda <= 0 samples level 0 bilinearly, otherwise levels floor(lambda)
+//     and floor(lambda) + 1 (the last level from lambda >= q on) are sampled
+//     bilinearly and mixed by fract(lambda); bilinear weights are fp32 and a
+//     texel value is byte / 255, through the sRGB decode table for the albedo
+//     array (GL_SRGB_ALPHA, TextureArray.cpp:29);
+//   * mip levels (glGenerateMipmap) are the rounded mean of the 2 x 2 texels
+//     above, per stored 8-bit channel;
+//   * the screen-space derivatives dFdx / dFdy are the fine differences inside
+//     the 2 x 2 pixel quad (pixel x | 1 minus pixel x & ~1, likewise in y),
+//     with the quad partner's world position reconstructed from its own depth
+//     and projected onto this pixel's face axes; a partner outside the image
+//     gives a zero derivative.
+#include "kernels.cuh"
+
+namespace vpt {
+
+namespace {
+
+__global__ void k_mip(const uint8_t* src, uint8_t* dst, int layers, int s2, int ch) {
+    // dst: layers x s2 x s2 texels; src: layers x (2 s2) x (2 s2)
+    const long long n = (long long)layers * s2 * s2;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(q % s2), y = (int)((q / s2) % s2), l = (int)(q / ((long long)s2 * s2));
+        const int s1 = 2 * s2;
+        const uint8_t* r0 = src + (((long long)l * s1 + 2 * y) * s1 + 2 * x) * ch;
+        const uint8_t* r1 = r0 + (long long)s1 * ch;
+        for (int c = 0; c < ch; c++)
+            dst[q * ch + c] = (uint8_t)(((int)r0[c] + (int)r0[ch + c] + (int)r1[c] + (int)r1[ch + c] + 2) >> 2);
+    }
+}
+
+__device__ __forceinline__ float fract_f(float x) { return x - floorf(x); }
+
+// texel channel value: byte / 255, or the sRGB decode of the byte
+__device__ __forceinline__ float texel_value(uint8_t v, const float* srgb) {
+    return srgb ? __ldg(srgb + v) : (float)v / 255.0f;
+}
+
+// texture() at one mip level: bilinear with REPEAT wrap and fp32 weights,
+// channels [0, nch)
+__device__ void bilinear_level(const TexArray& a, int level, int layer, float u, float v, int nch, const float* srgb,
+                               float* out) {
+    const int sl = a.size >> level;
+    const float x = u * (float)sl - 0.5f, y = v * (float)sl - 0.5f;
+    const float x0 = floorf(x), y0 = floorf(y);
+    const float ax = x - x0, ay = y - y0, bx = 1.0f - ax, by = 1.0f - ay;
+    const int i0 = wrapi(f2i(x0), sl), j0 = wrapi(f2i(y0), sl);
+    const int i1 = i0 + 1 == sl ? 0 : i0 + 1, j1 = j0 + 1 == sl ? 0 : j0 + 1;
+    const uint8_t* base = a.texels + (a.level_off[level] + (long long)layer * sl * sl) * a.channels;
+    const uint8_t* p00 = base + ((long long)j0 * sl + i0) * a.channels;
+    const uint8_t* p10 = base + ((long long)j0 * sl + i1) * a.channels;
+    const uint8_t* p01 = base + ((long long)j1 * sl + i0) * a.channels;
+    const uint8_t* p11 = base + ((long long)j1 * sl + i1) * a.channels;
+    for (int c = 0; c < nch; c++) {
+        const float v00 = texel_value(__ldg(p00 + c), srgb), v10 = texel_value(__ldg(p10 + c), srgb);
+        const float v01 = texel_value(__ldg(p01 + c), srgb), v11 = texel_value(__ldg(p11 + c), srgb);
+        const float lo = v00 * bx + v10 * ax;
+        const float hi = v01 * bx + v11 * ax;
+        out[c] = lo * by + hi * ay;
+    }
+}
+
+// level of detail of textureGrad(dPdx, dPdy) on a size x size array
+__device__ __forceinline__ float lod_of(int size, float dxu, float dxv, float dyu, float dyv) {
+    const float s = (float)size;
+    const float ax = dxu * s, ay = dxv * s, bx = dyu * s, by = dyv * s;
+    const float rx = sqrtf(ax * ax + ay * ay), ry = sqrtf(bx * bx + by * by);
+    return dlog2(fmaxf(rx, ry));
+}
+
+// LINEAR magnification / LINEAR_MIPMAP_LINEAR minification at level of detail lam
+__device__ void sample_lod(const TexArray& a, int layer_id, float u, float v, float lam, int nch, const float* srgb,
+                           float* out) {
+    const int layer = min(max(layer_id, 0), a.layers - 1);
+    const int q = a.levels - 1;
+    if (!(lam > 0.0f)) {
+        bilinear_level(a, 0, layer, u, v, nch, srgb, out);
+        return;
+    }
+    if (lam >= (float)q) {
+        bilinear_level(a, q, layer, u, v, nch, srgb, out);
+        return;
+    }
+    const float d1f = floorf(lam);
+    const int d1 = (int)d1f;
+    const float f = lam - d1f;
+    float t1[4], t2[4];
+    bilinear_level(a, d1, layer, u, v, nch, srgb, t1);
+    bilinear_level(a, d1 + 1, layer, u, v, nch, srgb, t2);
+    for (int c = 0; c < nch; c++) out[c] = (1.0f - f) * t1[c] + f * t2[c];
+}
+
+// the two face coordinates CalculateVectors takes for face id f: (x, y) for
+// +-Z, (x, z) for +-Y, (z, y) for +-X
+__device__ __forceinline__ v2 face_coords(v3 p, int f) {
+    const int axis = f >> 1;
+    return axis == 0 ? mk2(p.x, p.y) : (axis == 1 ? mk2(p.x, p.z) : mk2(p.z, p.y));
+}
+
+// world position of G-buffer texel (i, j): GetPositionAt (GenerateGBuffer.glsl:114-119)
+template <typename S>
+__device__ __forceinline__ v3 gbuffer_position(const CamView& cam, int W, int H, const S* t, int i, int j, float* dist) {
+    const float d = 1.0f / (1.0f / ld(t + (size_t)j * W + i));
+    *dist = d;
+    return add(ray_origin(cam), muls(normalize(ray_dir_at(cam, texcoord(i, j, W, H))), d));
+}
+
+__device__ __forceinline__ float dot2(v2 a) { return a.x * a.x + a.y * a.y; }
+
+// quad difference: value at the odd pixel minus value at the even one
+__device__ __forceinline__ float quad_diff(bool odd, float self, float partner) { return odd ? self - partner : partner - self; }
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_gbuffer_tex(CamView cam, int W, int H, const S* t, const uint8_t* face,
+                                                     const uint8_t* block, BlockTexView tv, S* o_albedo, S* o_normal,
+                                                     S* o_pbr, S* o_ao) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= W || j >= H) return;
+    const size_t px = (size_t)j * W + i;
+    float dist;
+    const v3 pos = gbuffer_position(cam, W, H, t, i, j, &dist);
+    if (dist < 0.0f) {   // sky (GenerateGBuffer.glsl main, :360-366)
+        for (int c = 0; c < 3; c++) {
+            st(o_albedo + px * 3 + c, 0.0f);
+            st(o_normal + px * 3 + c, 1.0f);
+        }
+        for (int c = 0; c < 4; c++) st(o_pbr + px * 4 + c, 0.0f);
+        st(o_ao + px, 0.0f);
+        return;
+    }
+    const int f = min((int)__ldg(face + px), 5);
+    const int bid = min(max((int)__ldg(block + px), 0), 127);
+    // CalculateVectors (:440-509): UV = fract of the face coordinates, and
+    // GetUVDerivative (:421-438) from the quad partners
+    const v2 P = face_coords(pos, f);
+    const v2 F = mk2(fract_f(P.x), fract_f(P.y));
+    const v2 O = mk2(fract_f(F.x + 0.25f), fract_f(F.y + 0.25f));
+    const int ix = i ^ 1, jy = j ^ 1;
+    v2 Fx = F, Ox = O, Fy = F, Oy = O;
+    if (ix < W) {
+        float dn;
+        const v2 Pn = face_coords(gbuffer_position(cam, W, H, t, ix, j, &dn), f);
+        Fx = mk2(fract_f(Pn.x), fract_f(Pn.y));
+        Ox = mk2(fract_f(Fx.x + 0.25f), fract_f(Fx.y + 0.25f));
+    }
+    if (jy < H) {
+        float dn;
+        const v2 Pn = face_coords(gbuffer_position(cam, W, H, t, i, jy, &dn), f);
+        Fy = mk2(fract_f(Pn.x), fract_f(Pn.y));
+        Oy = mk2(fract_f(Fy.x + 0.25f), fract_f(Fy.y + 0.25f));
+    }
+    const bool ox = i & 1, oy = j & 1;
+    v2 dx = mk2(quad_diff(ox, F.x, Fx.x), quad_diff(ox, F.y, Fx.y));
+    v2 dy = mk2(quad_diff(oy, F.x, Fy.x), quad_diff(oy, F.y, Fy.y));
+    const v2 dx2 = mk2(quad_diff(ox, O.x, Ox.x), quad_diff(ox, O.y, Ox.y));
+    const v2 dy2 = mk2(quad_diff(oy, O.x, Oy.x), quad_diff(oy, O.y, Oy.y));
+    if (dot2(dx) + dot2(dy) > dot2(dx2) + dot2(dy2)) {
+        dx = dx2;
+        dy = dy2;
+    }
+    // GetTextureIDs (:518-550) with the grass override
+    int ia = __ldg(tv.ids + bid), in_ = __ldg(tv.ids + 128 + bid), ip = __ldg(tv.ids + 256 + bid);
+    const int ie = tv.emissive.texels ? __ldg(tv.ids + 384 + bid) : -1;
+    if (bid == tv.grass[0]) {
+        const int k = f == 2 ? 1 : (f == 3 ? 7 : 4);   // top, bottom, sides
+        ia = tv.grass[k];
+        in_ = tv.grass[k + 1];
+        ip = tv.grass[k + 2];
+    }
+    // parallax off: UV = 1 - the flat UV (:388-390)
+    const v2 uv = mk2(1.0f - F.x, 1.0f - F.y);
+    const float lam = lod_of(tv.normal.size, dx.x, dx.y, dy.x, dy.y);
+    // tangent basis of the face (:449-458)
+    const v3 T = f < 4 ? mk3(1.0f, 0.0f, 0.0f) : mk3(0.0f, 0.0f, -1.0f);
+    const v3 B = f < 2 ? mk3(0.0f, 1.0f, 0.0f) : (f < 4 ? mk3(0.0f, 0.0f, 1.0f) : mk3(0.0f, -1.0f, 0.0f));
+    const v3 N = normal_from_id(f, 1.0f);
+    float nm[4], pbr[4], alb[4];
+    sample_lod(tv.normal, in_, uv.x, uv.y, lam, 3, nullptr, nm);
+    for (int c = 0; c < 3; c++) nm[c] = nm[c] * 2.0f - 1.0f;
+    // tbn * NormalMapped, columns tangent, bitangent, normal
+    const v3 nmap = mk3((T.x * nm[0] + B.x * nm[1]) + N.x * nm[2], (T.y * nm[0] + B.y * nm[1]) + N.y * nm[2],
+                        (T.z * nm[0] + B.z * nm[1]) + N.z * nm[2]);
+    sample_lod(tv.pbr, ip, uv.x, uv.y, lam, 4, nullptr, pbr);
+    float emis = 0.0f;
+    if (ie > -1) {
+        // texture() with the implicit derivatives of UV itself
+        const v2 ux = mk2(1.0f - Fx.x, 1.0f - Fx.y), uy = mk2(1.0f - Fy.x, 1.0f - Fy.y);
+        const float lam_e = lod_of(tv.emissive.size, quad_diff(ox, uv.x, ux.x), quad_diff(ox, uv.y, ux.y),
+                                   quad_diff(oy, uv.x, uy.x), quad_diff(oy, uv.y, uy.y));
+        float e[4];
+        sample_lod(tv.emissive, ie, uv.x, uv.y, lam_e, 1, nullptr, e);
+        emis = e[0];
+    }
+    sample_lod(tv.albedo, ia, uv.x, uv.y, lam, 3, tv.srgb, alb);
+    // BloomLightLeakFix (:412-418)
+    const float lb = 0.02f;
+    const float inside = (uv.x > lb && uv.x < 1.0f - lb && uv.y > lb && uv.y < 1.0f - lb) ? 1.0f : 0.0f;
+    st(o_albedo + px * 3 + 0, alb[0]);
+    st(o_albedo + px * 3 + 1, alb[1]);
+    st(o_albedo + px * 3 + 2, alb[2]);
+    st(o_normal + px * 3 + 0, nmap.x);
+    st(o_normal + px * 3 + 1, nmap.y);
+    st(o_normal + px * 3 + 2, nmap.z);
+    st(o_pbr + px * 4 + 0, clampf(pbr[0], 0.0f, 1.0f));
+    st(o_pbr + px * 4 + 1, clampf(pbr[1], 0.0f, 1.0f));
+    st(o_pbr + px * 4 + 2, clampf(pbr[2], 0.0f, 1.0f));
+    st(o_pbr + px * 4 + 3, clampf(emis, 0.0f, 1.0f) * inside);
+    st(o_ao + px, clampf(pbr[3], 0.00000001f, 1.0f));
+}
+
+}  // namespace
+
+cudaError_t tex_build_mip(const TexArray& a, int level, uint8_t* texels, cudaStream_t s) {
+    if (level < 0 || level + 1 >= a.levels) return cudaErrorInvalidValue;
+    const int s2 = a.size >> (level + 1);
+    const long long n = (long long)a.layers * s2 * s2;
+    const int grid = (int)((n + 255) / 256 < 65535 ? (n + 255) / 256 : 65535);
+    k_mip<<<grid, 256, 0, s>>>(texels + a.level_off[level] * a.channels, texels + a.level_off[level + 1] * a.channels,
+                               a.layers, s2, a.channels);
+    return cudaGetLastError();
+}
+
+cudaError_t gbuffer_textured(const CamView& cam, int W, int H, int fp16, const void* t, const uint8_t* face,
+                             const uint8_t* block, const BlockTexView& tv, void* albedo, void* normal, void* pbr,
+                             void* ao, cudaStream_t s) {
+    dim3 grid((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8));
+    dim3 blk(32, 8);
+    if (fp16)
+        k_gbuffer_tex<__half><<<grid, blk, 0, s>>>(cam, W, H, (const __half*)t, face, block, tv, (__half*)albedo,
+                                                   (__half*)normal, (__half*)pbr, (__half*)ao);
+    else
+        k_gbuffer_tex<float><<<grid, blk, 0, s>>>(cam, W, H, (const float*)t, face, block, tv, (float*)albedo,
+                                                  (float*)normal, (float*)pbr, (float*)ao);
+    return cudaGetLastError();
+}
+
+}  // namespace vpt
