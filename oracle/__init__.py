@@ -102,6 +102,7 @@ def lib() -> C.CDLL:
         L.vpto_ground_truth.argtypes = [P, P, P, P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                         C.c_uint32, P, P]
         L.vpto_generate_gbuffer.argtypes = [P, P, P, P, P, P, P, P, P, P]
+        L.vpto_shade_textured.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, C.c_int, C.c_int, P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -332,8 +333,9 @@ def generate_gbuffer(cam, config, textures: dict, t, face, block) -> dict:
 
 
 def shade(world: World, cam, config, frame, t, face, block, shadow, sh, cocg, aosky, rows=None,
-          spec=None) -> np.ndarray:
-    """The colour pass; spec is the resolved reflection (GI grid, 4 ch) or None."""
+          spec=None, gbt=None) -> np.ndarray:
+    """The colour pass; spec is the resolved reflection (GI grid, 4 ch) or None;
+    gbt the textured G-buffer (generate_gbuffer's planes) or None for flat materials."""
     p = params(config)
     H, W = p.height, p.width
     out = np.zeros((H, W, 3), dtype=np.float32)
@@ -342,8 +344,14 @@ def shade(world: World, cam, config, frame, t, face, block, shadow, sh, cocg, ao
              (cocg, np.float32), (aosky, np.float32))]
     sp = None if spec is None else np.ascontiguousarray(spec, dtype=np.float32)
     r0, r1 = rows if rows else (0, H)
-    lib().vpto_shade(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)),
-                     *[_p(a) for a in arrs], None if sp is None else _p(sp), r0, r1, _p(out))
+    if gbt is None:
+        lib().vpto_shade(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)),
+                         *[_p(a) for a in arrs], None if sp is None else _p(sp), r0, r1, _p(out))
+    else:
+        gb = [np.ascontiguousarray(gbt[k], dtype=np.float32) for k in ("albedo", "normal", "pbr", "ao")]
+        lib().vpto_shade_textured(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p),
+                                  C.byref(_as(OFrame, frame)), *[_p(a) for a in arrs], None if sp is None else _p(sp),
+                                  r0, r1, _p(out), *[_p(a) for a in gb])
     return out
 
 
@@ -480,7 +488,8 @@ def spec_denoise(world: World, cam, config, g: dict, spec_in, hit_data, frames, 
     return out
 
 
-def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist: dict, prev_refl=None) -> dict:
+def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist: dict, prev_refl=None,
+                 textures=None) -> dict:
     """One whole frame in the order of vpt_render_frame; prev_refl is last
     frame's "refl" (zero planes when None)."""
     p = params(config)
@@ -511,8 +520,9 @@ def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist:
             refl["den1"] = spec_denoise(world, cam, p, g, refl["out"], hd, refl["acc"], 1)
             refl["den"] = spec_denoise(world, cam, p, g, refl["den1"], hd, refl["acc"], 0)
     spec = None if refl is None else (refl["den"] if p.reflection_denoise else refl["out"])
-    rgb = shade(world, cam, p, frame, g["t"], g["face"], g["block"], shadow, sh, cocg, ao, spec=spec)
-    return {"g": g, "shadow": shadow, "gi": gi, "svgf": sv, "refl": refl, "rgb": rgb}
+    gbt = None if textures is None else generate_gbuffer(cam, p, textures, g["t"], g["face"], g["block"])
+    rgb = shade(world, cam, p, frame, g["t"], g["face"], g["block"], shadow, sh, cocg, ao, spec=spec, gbt=gbt)
+    return {"g": g, "shadow": shadow, "gi": gi, "svgf": sv, "refl": refl, "rgb": rgb, "gbt": gbt}
 
 
 def empty_history(H: int, W: int, gi_divisor: int = 1):

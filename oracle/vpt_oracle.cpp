@@ -1165,9 +1165,13 @@ inline v3 gnormal_linear(const Plane8& F, v2 uv) {
 struct UpscaledGI {
     float sh[4], cocg[2], ao, shadow, spec[4];
 };
+// With block textures (GN, GP non-null) the specular gather reads the tap's
+// roughness and normal-mapped normal from the textured G-buffer
+// (u_GBufferPBR, u_GBufferNormals, :596-599) against the base pixel's base_hf.
 inline UpscaledGI upscale_gi(const vpto_world* w, const Plane& T, const Plane8& F, const Plane8& B, const Plane8& S,
                              const Plane& SH, const Plane& CC, const Plane& AO, const Plane* SP, int d, int i, int j,
-                             v2 uv, v3 base_n, float base_d, float base_rough) {
+                             v2 uv, v3 base_n, float base_d, float base_rough, const Plane* GN, const Plane* GP,
+                             v3 base_hf) {
     const float texel_x = 1.0f / (float)SH.W, texel_y = 1.0f / (float)SH.H;
     static const float kw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
     UpscaledGI u{};
@@ -1200,9 +1204,16 @@ inline UpscaledGI upscale_gi(const vpto_world* w, const Plane& T, const Plane8& 
             const float kwt = kw[std::abs(x)] * kw[std::abs(y)];
             float wgt = clampf((nw * dw) * kwt, 0.0f, 1.0f);
             if (SP) {
-                const float ra = pbr_rough(w, B.at(si, sj));
-                float spw = (wgt / ((std::fabs(ra - base_rough) * 12.0f) + 1.0f)) *
-                            dm_pow(fmaxg(dot(na, base_n), 0.0f), 8.0f);
+                float ra, nsp;
+                if (GN) {
+                    ra = GP->at(si, sj, 0);
+                    const v3 hf = mk3(GN->at(si, sj, 0), GN->at(si, sj, 1), GN->at(si, sj, 2));
+                    nsp = dm_pow(fmaxg(dot(hf, base_hf), 0.0f), 8.0f);
+                } else {
+                    ra = pbr_rough(w, B.at(si, sj));
+                    nsp = dm_pow(fmaxg(dot(na, base_n), 0.0f), 8.0f);
+                }
+                float spw = (wgt / ((std::fabs(ra - base_rough) * 12.0f) + 1.0f)) * nsp;
                 spw = fmaxg(spw, 0.00000001f);
                 for (int c = 0; c < 4; c++) tsp[c] += ssp[c] * spw;
                 tspw += spw;
@@ -1232,12 +1243,17 @@ inline UpscaledGI upscale_gi(const vpto_world* w, const Plane& T, const Plane8& 
 }
 
 // ColorPassFrag.glsl main (:747-1083), u_UseDFG on (Core/Pipeline.cpp:3683),
-// VXAO with cutoff (:3669, :3679) only under SVGF (u_SVGFEnabled, :3680),
-// flat materials, no specular input.
-void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
-                const vpto_frame* f, const float* t, const uint8_t* face, const uint8_t* block,
-                const uint8_t* shadow, const float* sh, const float* cocg, const float* aosky,
-                const float* spec, int row0, int row1, float* rgb) {
+// VXAO with cutoff (:3669, :3679) only under SVGF (u_SVGFEnabled, :3680).
+// Flat materials (gb_* NULL): the block table's albedo, roughness,
+// metalness and emission, the face normal and a texture AO of 1; with block
+// textures the textured G-buffer's albedo, normal-mapped normal, PBR and AO
+// (u_GBufferAlbedos, u_GBufferNormals, u_GBufferPBR, u_GBufferAO, :797-803),
+// the face normal staying where the shader reads u_NormalTexture.
+static void shade_impl(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
+                       const vpto_frame* f, const float* t, const uint8_t* face, const uint8_t* block,
+                       const uint8_t* shadow, const float* sh, const float* cocg, const float* aosky,
+                       const float* spec, int row0, int row1, float* rgb, const float* gb_albedo,
+                       const float* gb_normal, const float* gb_pbr, const float* gb_ao) {
     const int W = p->width, H = p->height;
     const int fp16 = p->storage;
     const v3 viewer = mk3(cam->position[0], cam->position[1], cam->position[2]);
@@ -1265,15 +1281,26 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
             v3 color;
             if (dist > 0.0f) {
                 int bid = std::min(std::max((int)block[px], 0), 127);
-                Material m = material(w, bid);
-                v3 albedo = basic_saturation(m.albedo, 1.0f - 0.1f);   // u_TextureDesatAmount = 0.1
-                if (m.metal >= 0.1f - 0.01f) albedo = basic_saturation(albedo, 0.9f);
-                float emissivity = (float)m.emissive;
+                const Material m = material(w, bid);
+                v3 base_albedo = m.albedo, nh = n;
+                float rough = m.rough, metal = m.metal, emissivity = (float)m.emissive, tex_ao = 1.0f;
+                const bool tex = gb_albedo != nullptr;
+                if (tex) {
+                    base_albedo = mk3(gb_albedo[px * 3], gb_albedo[px * 3 + 1], gb_albedo[px * 3 + 2]);
+                    nh = mk3(gb_normal[px * 3], gb_normal[px * 3 + 1], gb_normal[px * 3 + 2]);
+                    rough = gb_pbr[px * 4];
+                    metal = gb_pbr[px * 4 + 1];
+                    emissivity = gb_pbr[px * 4 + 3];
+                    tex_ao = gb_ao[px];
+                }
+                v3 albedo = basic_saturation(base_albedo, 1.0f - 0.1f);   // u_TextureDesatAmount = 0.1
+                if (metal >= 0.1f - 0.01f) albedo = basic_saturation(albedo, 0.9f);
+                const Plane GN{gb_normal, W, H, 3}, GP{gb_pbr, W, H, 4};
                 const UpscaledGI up = upscale_gi(w, T, F, B, S, SH, CC, AO, spec ? &SP : nullptr, d, i, j, uv, n, dist,
-                                                 m.rough);
+                                                 rough, tex ? &GN : nullptr, tex ? &GP : nullptr, nh);
                 float up_shadow = clampf(up.shadow, 0.0f, 1.0f);
                 float rt_shadow = clampf(clampf(up_shadow + 0.0f, 0.0f, 1.0f), 0.0f, 1.0f);
-                v3 indirect = sh_to_irradiance(up.sh, up.cocg, n);
+                v3 indirect = sh_to_irradiance(up.sh, up.cocg, nh);   // IndirectN = NormalMapped (:834-840)
                 const float vb = 0.00125f;
                 if (vxao && uv.x > vb && uv.x < 1.0f - vb && uv.y > vb && uv.y < 1.0f - vb) {
                     float ao = up.ao;
@@ -1283,42 +1310,41 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
                     ao = dm_pow(ao, 2.2f);
                     indirect = muls(indirect, clampf(ao, 0.05f, 1.0f));
                 }
-                float sampled_ao = dm_pow(1.0f, 1.25f);
-                v3 sun_direct = directional_light(viewer, wp, sun, sun_color, sun_color, albedo, n, m.rough, m.metal, rt_shadow);
-                v3 moon_direct = directional_light(viewer, wp, moon, moon_color, moon_color, albedo, n, m.rough, m.metal, rt_shadow);
+                float sampled_ao = dm_pow(tex_ao, 1.25f);
+                v3 sun_direct = directional_light(viewer, wp, sun, sun_color, sun_color, albedo, nh, rough, metal, rt_shadow);
+                v3 moon_direct = directional_light(viewer, wp, moon, moon_color, moon_color, albedo, nh, rough, metal, rt_shadow);
                 v3 direct = vmixv(sun_direct, moon_direct, mk3(sun_vis * 1.0f, sun_vis * 1.0f, sun_vis * 1.0f));
                 direct = muls(direct, (!(emissivity > 0.05f)) ? 1.0f : 0.0f);
                 direct = vmax(direct, 0.000001f);
-                float rough = m.rough;
                 v3 diffuse_indirect = mul(indirect, albedo);
                 v3 I = normalize(sub(wp, viewer));
-                float idn = dot(n, I);
-                v3 R = sub(I, muls(n, 2.0f * idn));
+                float idn = dot(nh, I);
+                v3 R = sub(I, muls(nh, 2.0f * idn));
                 // SpecularIndirect (:901-909): the upscaled reflection times
                 // clamp(max(n.n, 1e-8)^2 * 1.5, 0.1, 1) inside the 0.0035 border
                 v3 spec_ind = mk3(0, 0, 0);
                 const float sb = 0.0035f;
                 if (spec && uv.x > sb && uv.x < 1.0f - sb && uv.y > sb && uv.y < 1.0f - sb) {
-                    const float att = clampf(dm_pow(fmaxg(dot(n, n), 0.00000001f), 2.0f) * 1.5f, 0.1f, 1.0f);
+                    const float att = clampf(dm_pow(fmaxg(dot(n, nh), 0.00000001f), 2.0f) * 1.5f, 0.1f, 1.0f);
                     spec_ind = muls(mk3(up.spec[0], up.spec[1], up.spec[2]), att);
                 }
                 spec_ind = vmax(spec_ind, 0.0001f);
                 v3 Lo = normalize(sub(viewer, wp));
-                v3 F0 = vmix(mk3(0.04f, 0.04f, 0.04f), albedo, m.metal);
+                v3 F0 = vmix(mk3(0.04f, 0.04f, 0.04f), albedo, metal);
                 diffuse_indirect = muls(diffuse_indirect, clampf(sampled_ao, 0.2f, 1.01f));
-                float nov = clampf(dot(n, Lo), 0.0000000001f, 1.0f);
-                // ComputeSpecularAO (:742-745), pbr.w (G-buffer AO) = 1 for flat materials
-                float spec_ao = clampf(dm_pow(nov + 1.0f, dm_exp2(-16.0f * rough - 1.0f)) - 1.0f + 1.0f, 0.0f, 1.0f);
+                float nov = clampf(dot(nh, Lo), 0.0000000001f, 1.0f);
+                // ComputeSpecularAO (:742-745) of the texture AO (1 for flat materials)
+                float spec_ao = clampf(dm_pow(nov + tex_ao, dm_exp2(-16.0f * rough - 1.0f)) - 1.0f + tex_ao, 0.0f, 1.0f);
                 spec_ao = dm_pow(spec_ao, 1.5f);
-                float horizon = fming(1.0f + dot(R, n), 1.0f);
+                float horizon = fming(1.0f + dot(R, nh), 1.0f);
                 horizon = (horizon * horizon) * horizon;
-                if (m.metal >= 0.1f) spec_ind = muls(spec_ind, 1.3f);
+                if (metal >= 0.1f) spec_ind = muls(spec_ind, 1.3f);
                 spec_ind = muls(spec_ind, spec_ao);
                 spec_ind = muls(spec_ind, horizon);
-                v3 F = vclamp(fresnel_schlick_roughness(Lo, n, F0, rough), 0.0f, 1.0f);
+                v3 F = vclamp(fresnel_schlick_roughness(Lo, nh, F0, rough), 0.0f, 1.0f);
                 v3 kD = sub(mk3(1, 1, 1), F);
-                kD = muls(kD, 1.0f - m.metal);
-                float ex = clampf(fmaxg(dot(neg(I), n), 0.000001f), 0.0f, 1.0f);
+                kD = muls(kD, 1.0f - metal);
+                float ex = clampf(fmaxg(dot(neg(I), nh), 0.000001f), 0.0f, 1.0f);
                 float ey = clampf(rough, 0.0f, 1.0f);
                 v2 env = karis_env_brdf(ex, ey);
                 v3 ind_spec = mul(spec_ind, mk3(F.x * env.x + env.y, F.y * env.x + env.y, F.z * env.x + env.y));
@@ -1333,6 +1359,23 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
             rgb[px * 3 + 2] = storage(color.z, fp16);
         }
     }
+}
+
+void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* p,
+                const vpto_frame* f, const float* t, const uint8_t* face, const uint8_t* block,
+                const uint8_t* shadow, const float* sh, const float* cocg, const float* aosky,
+                const float* spec, int row0, int row1, float* rgb) {
+    shade_impl(w, cam, p, f, t, face, block, shadow, sh, cocg, aosky, spec, row0, row1, rgb, nullptr, nullptr, nullptr,
+               nullptr);
+}
+
+void vpto_shade_textured(const vpto_world* w, const vpto_camera* cam, const vpto_params* p, const vpto_frame* f,
+                         const float* t, const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
+                         const float* sh, const float* cocg, const float* aosky, const float* spec, int row0, int row1,
+                         float* rgb, const float* gb_albedo, const float* gb_normal, const float* gb_pbr,
+                         const float* gb_ao) {
+    shade_impl(w, cam, p, f, t, face, block, shadow, sh, cocg, aosky, spec, row0, row1, rgb, gb_albedo, gb_normal,
+               gb_pbr, gb_ao);
 }
 
 // ------------------------------------------------------------ reflections --

@@ -207,6 +207,14 @@ void vpto_shade(const vpto_world* w, const vpto_camera* cam, const vpto_params* 
                 const uint8_t* shadow, const float* sh, const float* cocg, const float* aosky,
                 const float* spec, int row0, int row1, float* rgb);
 
+/* The colour pass with block textures: albedo (3), normal-mapped normal (3),
+ * PBR (4) and texture AO (1) from the textured G-buffer (W*H each). */
+void vpto_shade_textured(const vpto_world* w, const vpto_camera* cam, const vpto_params* p, const vpto_frame* f,
+                         const float* t, const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
+                         const float* sh, const float* cocg, const float* aosky, const float* spec, int row0, int row1,
+                         float* rgb, const float* gb_albedo, const float* gb_normal, const float* gb_pbr,
+                         const float* gb_ao);
+
 /* The non-SVGF denoiser path (USE_SVGF off, Core/Pipeline.cpp:2618-2786):
  * TemporalFilter.glsl (diffuse mode), SampleVarianceCompute.glsl and one
  * AtrousSpatialFilter.glsl iteration. */

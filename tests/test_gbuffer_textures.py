@@ -162,3 +162,83 @@ def test_gbuffer_needs_textures_and_a_gbuffer(vpt, oracle, gpu):
         ctx.set_block_textures(None)
         with pytest.raises(vpt.VPTError):
             ctx.generate_gbuffer()
+
+
+# ------------------------------------------------ colour pass with textures --
+def test_oracle_textured_colour_pass(vpt, oracle):
+    """The colour pass reads the textured G-buffer: sky unchanged, a brighter
+    albedo texture brightens the lit pixels, and an emissive texel over 0.05
+    switches the direct light off."""
+    vox, blocks, world, cams = scene(vpt, oracle)
+    cfg = vpt.default_config(width=W, height=H, primary_max_steps=256)
+    frame = vpt.default_frame(frame_index=0, seed=9)
+    prev_g, hist = oracle.empty_history(H, W)
+    flat = oracle.render_frame(world, cams[0], cams[0], cfg, frame, prev_g, hist)
+    dark, bright = constant_textures(vpt), constant_textures(vpt)
+    dark["emissive_id"][:] = -1
+    bright["emissive_id"][:] = -1
+    dark["albedo"][..., :3] = 60
+    bright["albedo"][..., :3] = 200
+    fd = oracle.render_frame(world, cams[0], cams[0], cfg, frame, prev_g, hist, textures=dark)
+    fb = oracle.render_frame(world, cams[0], cams[0], cfg, frame, prev_g, hist, textures=bright)
+    sky, hit = flat["g"]["t"] < 0, flat["g"]["t"] > 0
+    assert (fd["rgb"][sky] == flat["rgb"][sky]).all() and (fb["rgb"][sky] == flat["rgb"][sky]).all()
+    assert fb["rgb"][hit].mean() > 1.5 * fd["rgb"][hit].mean()
+    glow, plain = constant_textures(vpt), constant_textures(vpt)
+    glow["emissive_id"][:] = 0
+    plain["emissive_id"][:] = -1
+    fg = oracle.render_frame(world, cams[0], cams[0], cfg, frame, prev_g, hist, textures=glow)
+    fp = oracle.render_frame(world, cams[0], cams[0], cfg, frame, prev_g, hist, textures=plain)
+    lit = hit & (fg["gbt"]["pbr"][..., 3] > 0.05)
+    assert lit.any() and (fg["rgb"][lit] <= fp["rgb"][lit]).all() and fg["rgb"][lit].mean() < fp["rgb"][lit].mean()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage,d,rspp", [(0, 1, 0), (1, 1, 0), (0, 2, 2), (1, 1, 2)],
+                         ids=["f32", "f16", "f32-d2-reflections", "f16-reflections"])
+def test_textured_frames_bit_exact(vpt, oracle, storage, d, rspp, gpu):
+    """Whole frames through vpt_render_frame with block textures: the
+    textured G-buffer, the colour pass over it (with the GI upscale and the
+    reflection gather) and the history across frames equal the oracle's."""
+    vox, blocks, world, cams = scene(vpt, oracle, seed=3)
+    tex = vpt.generate_block_textures(16, 9, seed=7, grass_block=int(np.bincount(vox[vox > 0]).argmax()))
+    X, Z = DIMS[0], DIMS[2]
+    yaw, pitch = vpt.seeded_pose(3)
+    poses = [cams[0], vpt.camera_from_pose((X / 2 + 0.6, 58.1, Z / 2 - 0.3), yaw + 2.0, pitch + 1.0, 90.0, W / H)]
+    with vpt.Context(width=W, height=H, primary_max_steps=256, storage=storage, gi_divisor=d,
+                     reflection_spp=rspp) as ctx:
+        ctx.upload_world(vox)
+        ctx.set_block_table(blocks)
+        ctx.build_df()
+        ctx.set_block_textures(tex)
+        cfg = ctx.config
+        prev_g, hist = oracle.empty_history(H, W, d)
+        prev_refl, prev_cam = None, poses[0]
+        for k, cam in enumerate(poses):
+            frame = vpt.default_frame(frame_index=k, seed=5, time=0.3 + 0.2 * k)
+            rgb = ctx.render_frame(cam, frame)
+            ref = oracle.render_frame(world, cam, prev_cam, cfg, frame, prev_g, hist, prev_refl, textures=tex)
+            assert_same(rgb, ref["rgb"], f"frame {k} colour")
+            prev_g = {n: ref["g"][n] for n in ("t", "face", "block")}
+            hist = ref["svgf"]["temporal"]
+            prev_refl = ref["refl"]
+            prev_cam = cam
+
+
+@pytest.mark.gpu
+def test_textured_shade_needs_this_frames_gbuffer(vpt, oracle, gpu):
+    vox, blocks, world, cams = scene(vpt, oracle)
+    frame = vpt.default_frame(frame_index=0, seed=1)
+    with vpt.Context(width=W, height=H) as ctx:
+        ctx.upload_world(vox)
+        ctx.set_block_table(blocks)
+        ctx.build_df()
+        ctx.set_block_textures(vpt.generate_block_textures(8, 3))
+        ctx.trace_primary(cams[0])
+        ctx.trace_shadow(frame)
+        ctx.trace_diffuse(frame)
+        ctx.svgf(None, frame)
+        with pytest.raises(vpt.VPTError):
+            ctx.shade(frame)
+        ctx.generate_gbuffer()
+        ctx.shade(frame)

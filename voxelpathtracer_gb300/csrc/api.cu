@@ -145,6 +145,7 @@ struct vpt_ctx {
     int tex_grass[10] = {};
     bool textured = false;
     void* gbt[4] = {};
+    bool gbt_valid = false;   // the textured planes belong to this frame's G-buffer
 };
 
 namespace {
@@ -602,6 +603,7 @@ vpt_status vpt_set_block_textures(vpt_ctx* c, const vpt_block_textures* t) {
     dfree(c, (void**)&c->tex_ids);
     dfree(c, (void**)&c->srgb);
     c->textured = false;
+    c->gbt_valid = false;
     if (!t) return VPT_OK;
     const int S = t->size;
     if (S < 1 || S > 1024 || (S & (S - 1)))
@@ -684,6 +686,7 @@ vpt_status vpt_generate_gbuffer(vpt_ctx* c) {
                            c->gbt[0], c->gbt[1], c->gbt[2], c->gbt[3], c->stream));
     pass_end(c, VPT_PASS_GBUFFER);
     c->launches += 1;
+    c->gbt_valid = true;
     return VPT_OK;
 }
 
@@ -748,6 +751,7 @@ vpt_status vpt_trace_primary(vpt_ctx* c, const vpt_camera* cam) {
     cudaSetDevice(c->dev);
     c->cam = *cam;
     c->have_cam = true;
+    c->gbt_valid = false;
     GBufferOut g;
     g.t = c->gbuf[c->cur][GB_T];
     g.face = (uint8_t*)c->gbuf[c->cur][GB_FACE];
@@ -810,6 +814,7 @@ vpt_status vpt_trace_frame(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f
     cudaSetDevice(c->dev);
     c->cam = *cam;
     c->have_cam = true;
+    c->gbt_valid = false;
     const int W = c->cfg.width, H = c->cfg.height;
     FrameTraceArgs a;
     a.w = world_view(c);
@@ -1170,6 +1175,17 @@ vpt_status shade_run(vpt_ctx* c, const vpt_frame* f, int source, void* out = nul
         cocg = c->gi[GI_COCG];
         ao = c->gi[GI_AOSKY];
     }
+    // the plain frame with block textures reads the textured G-buffer; the
+    // learned path's inputs (sources 1 and 2) keep the block table's flat
+    // materials its network was trained on
+    if (c->textured && source == 0) {
+        if (!c->gbt_valid)
+            return fail(c, VPT_ERR_STATE, "block textures are set: run vpt_generate_gbuffer after the primary trace");
+        a.gb_albedo = c->gbt[0];
+        a.gb_normal = c->gbt[1];
+        a.gb_pbr = c->gbt[2];
+        a.gb_ao = c->gbt[3];
+    }
     pass_begin(c, VPT_PASS_SHADE);
     CK(c, shade(world_view(c), cam_view(c->cam), c->cfg.width, c->cfg.height, c->fp16, a, c->gbuf[c->cur][GB_T],
                 (const uint8_t*)c->gbuf[c->cur][GB_FACE], (const uint8_t*)c->gbuf[c->cur][GB_BLOCK], c->shadow, sh, cocg,
@@ -1323,6 +1339,7 @@ vpt_status vpt_render_frame(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* 
     vpt_status s;
     const vpt_camera prev = c->have_prev ? c->prev_cam : *cam;
     if ((s = trace_all(c, cam, f)) != VPT_OK) return s;
+    if (c->textured && (s = vpt_generate_gbuffer(c)) != VPT_OK) return s;
     if ((s = vpt_svgf(c, &prev, f)) != VPT_OK) return s;
     if (c->cfg.reflection_spp > 0 && (s = reflection_run(c, f)) != VPT_OK) return s;
     if ((s = vpt_shade(c, f)) != VPT_OK) return s;

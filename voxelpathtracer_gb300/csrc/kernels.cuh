@@ -288,6 +288,12 @@ struct ShadeArgs {
     float sun_vis;             // 1 - clamp(dot(sun, up) + 0.05, 0, 0.1) * 12
     int vxao;                  // u_DoVXAO && u_SVGFEnabled: the GI AO darkens the indirect term
     int gi_div;                // the GI planes are (W / gi_div) x (H / gi_div)
+    // the textured G-buffer (albedo 3, normal 3, PBR 4, AO 1 channels in the
+    // storage type), or all NULL: flat materials from the block table
+    const void* gb_albedo = nullptr;
+    const void* gb_normal = nullptr;
+    const void* gb_pbr = nullptr;
+    const void* gb_ao = nullptr;
 };
 // spec: the resolved reflection on the GI grid (4 ch), or NULL without a
 // reflection pass.

@@ -81,13 +81,16 @@ struct UpscaledGI {
 // (12 |roughness - base roughness| + 1) * max(n.n', 0)^8 (:595-603; the
 // G-buffer roughness and normal are the block's and the face's). All loads of
 // a tap are issued before its weights are formed; taps in x-outer, y-inner
-// order keep the sums' rounding identical to the shader's loop.
-template <typename S, bool kScaled, bool kSpec>
+// order keep the sums' rounding identical to the shader's loop. With block
+// textures (kTex) the specular gather reads the tap's roughness and
+// normal-mapped normal from the textured G-buffer (u_GBufferPBR,
+// u_GBufferNormals, :596-599) and compares with the base pixel's (base_hf).
+template <typename S, bool kScaled, bool kSpec, bool kTex>
 __device__ __forceinline__ UpscaledGI upscale_gi(const WorldView& w, int W, int H, int d, int i, int j, v2 uv,
                                                  const S* t, const uint8_t* face, const uint8_t* block,
                                                  const uint8_t* shadow, const S* sh_p, const S* cocg_p,
                                                  const S* ao_p, const S* spec_p, int base_face, float base_d,
-                                                 float base_rough) {
+                                                 float base_rough, const S* gb_normal, const S* gb_pbr, v3 base_hf) {
     UpscaledGI u;
     // the normal weights for a clamped dot product of the decoded face
     // normals of 0, 1 or 3 (face_cos): max(n.n', 1e-6)^16 floored at 1e-4,
@@ -126,7 +129,7 @@ __device__ __forceinline__ UpscaledGI upscale_gi(const WorldView& w, int W, int 
                 a0 = ld(ao_p + q * 2);
                 if (kSpec) sp4 = ld4(spec_p + q * 4);
             }
-            const int tap_block = kSpec ? (int)__ldg(block + q) : 0;
+            const int tap_block = (kSpec && !kTex) ? (int)__ldg(block + q) : 0;
             const bool cross = x == 0 || y == 0;
             const float sv = (filter_shadows && cross) ? (float)__ldg(shadow + q) : 0.0f;
             const float lda = 1.0f / (1.0f / tt);
@@ -137,8 +140,16 @@ __device__ __forceinline__ UpscaledGI upscale_gi(const WorldView& w, int W, int 
             const float kwt = (x == 0 ? 1.0f : 2.0f / 3.0f) * (y == 0 ? 1.0f : 2.0f / 3.0f);   // AtrousWeights
             float wgt = clampf((nw * dw) * kwt, 0.0f, 1.0f);
             if (kSpec) {
-                const float ra = pbr_rough(w, tap_block);
-                float spw = (wgt / ((fabsf(ra - base_rough) * 12.0f) + 1.0f)) * (fc == 0 ? 0.0f : (fc == 1 ? sw1 : sw3));
+                float ra, nsp;
+                if (kTex) {
+                    ra = ld(gb_pbr + q * 4);
+                    const v3 hf = mk3(ld(gb_normal + q * 3), ld(gb_normal + q * 3 + 1), ld(gb_normal + q * 3 + 2));
+                    nsp = dpow(fmaxf(dot(hf, base_hf), 0.0f), 8.0f);
+                } else {
+                    ra = pbr_rough(w, tap_block);
+                    nsp = fc == 0 ? 0.0f : (fc == 1 ? sw1 : sw3);
+                }
+                float spw = (wgt / ((fabsf(ra - base_rough) * 12.0f) + 1.0f)) * nsp;
                 spw = fmaxf(spw, 0.00000001f);
                 tsp.x += sp4.x * spw;
                 tsp.y += sp4.y * spw;
@@ -181,7 +192,11 @@ __device__ __forceinline__ UpscaledGI upscale_gi(const WorldView& w, int W, int 
     return u;
 }
 
-template <typename S, bool kScaled, bool kSpec>
+// kTex: albedo, normal-mapped normal, roughness / metalness / emissivity and
+// texture AO from the textured G-buffer (u_GBufferAlbedos, u_GBufferNormals,
+// u_GBufferPBR, u_GBufferAO, :797-803) instead of the block table and the
+// face normal; the face normal stays where the shader reads u_NormalTexture.
+template <typename S, bool kScaled, bool kSpec, bool kTex>
 __global__ void __launch_bounds__(256, 4) k_shade(WorldView w, CamView cam, int W, int H, ShadeArgs a, const S* t,
                                                const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
                                                const S* sh_p, const S* cocg_p, const S* ao_p, const S* spec_p,
@@ -200,16 +215,29 @@ __global__ void __launch_bounds__(256, 4) k_shade(WorldView w, CamView cam, int 
     v3 color;
     if (dist > 0.0f) {
         int bid = min(max((int)__ldg(block + px), 0), 127);
-        Material m = material(w, bid);
-        v3 albedo = basic_saturation(m.albedo, 1.0f - 0.1f);
-        if (m.metal >= 0.1f - 0.01f) albedo = basic_saturation(albedo, 0.9f);
-        float emissivity = (float)m.emissive;
-        const UpscaledGI up = upscale_gi<S, kScaled, kSpec>(w, W, H, a.gi_div, i, j, uv, t, face, block, shadow,
-                                                            sh_p, cocg_p, ao_p, spec_p, (int)__ldg(face + px), dist,
-                                                            m.rough);
+        const Material m = material(w, bid);
+        v3 base_albedo = m.albedo, nh = n;
+        float rough = m.rough, metal = m.metal, emissivity = (float)m.emissive, tex_ao = 1.0f;
+        const S* gb_normal = (const S*)a.gb_normal;
+        const S* gb_pbr = (const S*)a.gb_pbr;
+        if (kTex) {
+            const S* ga = (const S*)a.gb_albedo;
+            base_albedo = mk3(ld(ga + px * 3), ld(ga + px * 3 + 1), ld(ga + px * 3 + 2));
+            nh = mk3(ld(gb_normal + px * 3), ld(gb_normal + px * 3 + 1), ld(gb_normal + px * 3 + 2));
+            rough = ld(gb_pbr + px * 4);
+            metal = ld(gb_pbr + px * 4 + 1);
+            emissivity = ld(gb_pbr + px * 4 + 3);
+            tex_ao = ld((const S*)a.gb_ao + px);
+        }
+        v3 albedo = basic_saturation(base_albedo, 1.0f - 0.1f);
+        if (metal >= 0.1f - 0.01f) albedo = basic_saturation(albedo, 0.9f);
+        const UpscaledGI up = upscale_gi<S, kScaled, kSpec, kTex>(w, W, H, a.gi_div, i, j, uv, t, face, block,
+                                                                  shadow, sh_p, cocg_p, ao_p, spec_p,
+                                                                  (int)__ldg(face + px), dist, rough, gb_normal,
+                                                                  gb_pbr, nh);
         float up_shadow = clampf(up.shadow, 0.0f, 1.0f);
         float rt_shadow = clampf(clampf(up_shadow + 0.0f, 0.0f, 1.0f), 0.0f, 1.0f);
-        v3 indirect = sh_to_irradiance(up.sh, up.cocg, n);
+        v3 indirect = sh_to_irradiance(up.sh, up.cocg, nh);   // IndirectN = NormalMapped (:834-840)
         const float vb = 0.00125f;
         if (a.vxao && uv.x > vb && uv.x < 1.0f - vb && uv.y > vb && uv.y < 1.0f - vb) {
             float ao = up.ao;
@@ -219,46 +247,45 @@ __global__ void __launch_bounds__(256, 4) k_shade(WorldView w, CamView cam, int 
             ao = dpow(ao, 2.2f);
             indirect = muls(indirect, clampf(ao, 0.05f, 1.0f));
         }
-        float sampled_ao = dpow(1.0f, 1.25f);
+        float sampled_ao = dpow(tex_ao, 1.25f);
         v3 sun = mk3(a.sun[0], a.sun[1], a.sun[2]);
         v3 moon = mk3(a.moon[0], a.moon[1], a.moon[2]);
         v3 sun_color = mk3(a.sun_color[0], a.sun_color[1], a.sun_color[2]);
         v3 moon_color = mk3(a.moon_color[0], a.moon_color[1], a.moon_color[2]);
-        v3 sun_direct = directional_light(viewer, wp, sun, sun_color, sun_color, albedo, n, m.rough, m.metal, rt_shadow);
-        v3 moon_direct = directional_light(viewer, wp, moon, moon_color, moon_color, albedo, n, m.rough, m.metal, rt_shadow);
+        v3 sun_direct = directional_light(viewer, wp, sun, sun_color, sun_color, albedo, nh, rough, metal, rt_shadow);
+        v3 moon_direct = directional_light(viewer, wp, moon, moon_color, moon_color, albedo, nh, rough, metal, rt_shadow);
         v3 direct = vmixv(sun_direct, moon_direct, mk3(a.sun_vis * 1.0f, a.sun_vis * 1.0f, a.sun_vis * 1.0f));
         direct = muls(direct, (!(emissivity > 0.05f)) ? 1.0f : 0.0f);
         direct = vmax(direct, 0.000001f);
-        float rough = m.rough;
         v3 diffuse_indirect = mul(indirect, albedo);
         v3 I = normalize(sub(wp, viewer));
-        float idn = dot(n, I);
-        v3 R = sub(I, muls(n, 2.0f * idn));
+        float idn = dot(nh, I);
+        v3 R = sub(I, muls(nh, 2.0f * idn));
         // SpecularIndirect (:901-909): the upscaled reflection times
         // clamp(max(n.n, 1e-8)^2 * 1.5, 0.1, 1) inside the 0.0035 border
         v3 spec_ind = mk3(0.0f, 0.0f, 0.0f);
         const float sb = 0.0035f;
         if (kSpec && uv.x > sb && uv.x < 1.0f - sb && uv.y > sb && uv.y < 1.0f - sb) {
-            const float att = clampf(dpow(fmaxf(dot(n, n), 0.00000001f), 2.0f) * 1.5f, 0.1f, 1.0f);
+            const float att = clampf(dpow(fmaxf(dot(n, nh), 0.00000001f), 2.0f) * 1.5f, 0.1f, 1.0f);
             spec_ind = muls(mk3(up.spec[0], up.spec[1], up.spec[2]), att);
         }
         spec_ind = vmax(spec_ind, 0.0001f);
         v3 Lo = normalize(sub(viewer, wp));
-        v3 F0 = vmix(mk3(0.04f, 0.04f, 0.04f), albedo, m.metal);
+        v3 F0 = vmix(mk3(0.04f, 0.04f, 0.04f), albedo, metal);
         diffuse_indirect = muls(diffuse_indirect, clampf(sampled_ao, 0.2f, 1.01f));
-        float nov = clampf(dot(n, Lo), 0.0000000001f, 1.0f);
-        // ComputeSpecularAO (:742-745) with the flat G-buffer AO of 1
-        float spec_ao = clampf(dpow(nov + 1.0f, dexp2(-16.0f * rough - 1.0f)) - 1.0f + 1.0f, 0.0f, 1.0f);
+        float nov = clampf(dot(nh, Lo), 0.0000000001f, 1.0f);
+        // ComputeSpecularAO (:742-745) of the texture AO (1 without textures)
+        float spec_ao = clampf(dpow(nov + tex_ao, dexp2(-16.0f * rough - 1.0f)) - 1.0f + tex_ao, 0.0f, 1.0f);
         spec_ao = dpow(spec_ao, 1.5f);
-        float horizon = fminf(1.0f + dot(R, n), 1.0f);
+        float horizon = fminf(1.0f + dot(R, nh), 1.0f);
         horizon = (horizon * horizon) * horizon;
-        if (m.metal >= 0.1f) spec_ind = muls(spec_ind, 1.3f);
+        if (metal >= 0.1f) spec_ind = muls(spec_ind, 1.3f);
         spec_ind = muls(spec_ind, spec_ao);
         spec_ind = muls(spec_ind, horizon);
-        v3 F = vclamp(fresnel_schlick_roughness(Lo, n, F0, rough), 0.0f, 1.0f);
+        v3 F = vclamp(fresnel_schlick_roughness(Lo, nh, F0, rough), 0.0f, 1.0f);
         v3 kD = sub(mk3(1.0f, 1.0f, 1.0f), F);
-        kD = muls(kD, 1.0f - m.metal);
-        float ex = clampf(fmaxf(dot(neg(I), n), 0.000001f), 0.0f, 1.0f);
+        kD = muls(kD, 1.0f - metal);
+        float ex = clampf(fmaxf(dot(neg(I), nh), 0.000001f), 0.0f, 1.0f);
         float ey = clampf(rough, 0.0f, 1.0f);
         v2 env = karis_env_brdf(ex, ey);
         v3 ind_spec = mul(spec_ind, mk3(F.x * env.x + env.y, F.y * env.x + env.y, F.z * env.x + env.y));
@@ -273,6 +300,21 @@ __global__ void __launch_bounds__(256, 4) k_shade(WorldView w, CamView cam, int 
     st(rgb + px * 3 + 2, color.z);
 }
 
+template <typename S>
+void launch_shade(bool scaled, bool sp, bool tx, dim3 grid, dim3 blk, cudaStream_t s, const WorldView& w,
+                  const CamView& cam, int W, int H, const ShadeArgs& a, const void* t, const uint8_t* face,
+                  const uint8_t* block, const uint8_t* shadow, const void* sh, const void* cocg, const void* aosky,
+                  const void* spec, void* rgb) {
+    using K = void (*)(WorldView, CamView, int, int, ShadeArgs, const S*, const uint8_t*, const uint8_t*,
+                       const uint8_t*, const S*, const S*, const S*, const S*, S*);
+    const K table[8] = {k_shade<S, false, false, false>, k_shade<S, false, false, true>, k_shade<S, false, true, false>,
+                        k_shade<S, false, true, true>,   k_shade<S, true, false, false>,  k_shade<S, true, false, true>,
+                        k_shade<S, true, true, false>,   k_shade<S, true, true, true>};
+    const K k = table[(scaled ? 4 : 0) + (sp ? 2 : 0) + (tx ? 1 : 0)];
+    k<<<grid, blk, 0, s>>>(w, cam, W, H, a, (const S*)t, face, block, shadow, (const S*)sh, (const S*)cocg,
+                           (const S*)aosky, (const S*)spec, (S*)rgb);
+}
+
 }  // namespace
 
 cudaError_t shade(const WorldView& w, const CamView& cam, int W, int H, int fp16, const ShadeArgs& a,
@@ -280,17 +322,13 @@ cudaError_t shade(const WorldView& w, const CamView& cam, int W, int H, int fp16
                   const void* sh, const void* cocg, const void* aosky, const void* spec, void* rgb, cudaStream_t s) {
     dim3 grid((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8));
     dim3 blk(32, 8);
-    const bool scaled = a.gi_div > 1, sp = spec != nullptr;
+    const bool scaled = a.gi_div > 1, sp = spec != nullptr, tx = a.gb_albedo != nullptr;
     if (fp16) {
-        auto k = scaled ? (sp ? k_shade<__half, true, true> : k_shade<__half, true, false>)
-                        : (sp ? k_shade<__half, false, true> : k_shade<__half, false, false>);
-        k<<<grid, blk, 0, s>>>(w, cam, W, H, a, (const __half*)t, face, block, shadow, (const __half*)sh,
-                               (const __half*)cocg, (const __half*)aosky, (const __half*)spec, (__half*)rgb);
+        launch_shade<__half>(scaled, sp, tx, grid, blk, s, w, cam, W, H, a, t, face, block, shadow, sh, cocg, aosky, spec,
+                             rgb);
     } else {
-        auto k = scaled ? (sp ? k_shade<float, true, true> : k_shade<float, true, false>)
-                        : (sp ? k_shade<float, false, true> : k_shade<float, false, false>);
-        k<<<grid, blk, 0, s>>>(w, cam, W, H, a, (const float*)t, face, block, shadow, (const float*)sh,
-                               (const float*)cocg, (const float*)aosky, (const float*)spec, (float*)rgb);
+        launch_shade<float>(scaled, sp, tx, grid, blk, s, w, cam, W, H, a, t, face, block, shadow, sh, cocg, aosky, spec,
+                            rgb);
     }
     return cudaGetLastError();
 }
