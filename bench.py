@@ -272,11 +272,13 @@ def run_ours(args):
     # 4) variants on the same frames (device-resident timing): FP16 storage, and
     # the reference's default GI grid (DiffuseTraceResolution 1/4: diffuse rays
     # and SVGF on 480x270, joint-bilateral upscale in the colour pass)
-    def run_variant(**cfg):
+    def run_variant(textures=None, **cfg):
         vc = vpt.Context(width=W, height=H, device=local, **cfg)
         vc.upload_world(vox)
         vc.set_block_table(blocks)
         vc.build_df()
+        if textures is not None:
+            vc.set_block_textures(textures)
         vc.set_stats(True)
         vrays = 0
         for s in range(total):
@@ -314,7 +316,13 @@ def run_ours(args):
         vr, _ = run_variant(reflection_spp=2)
         vrq, _ = run_variant(gi_divisor=4, reflection_spp=2)
         vrq["gi_grid"] = [W // 4, H // 4]
-        variant = {"fp16_storage": v16, "gi_quarter": vq, "reflections": vr, "gi_quarter_reflections": vrq}
+        # with block textures (GenerateGBuffer + the colour pass over it):
+        # 24 seeded 512 x 512 layers per array, as the reference's block PNGs
+        tex = vpt.generate_block_textures(512, 24, seed=0, grass_block=1)
+        vt, _ = run_variant(textures=tex)
+        vt["textures"] = {"size": 512, "layers": 24}
+        variant = {"fp16_storage": v16, "gi_quarter": vq, "reflections": vr, "gi_quarter_reflections": vrq,
+                   "block_textures": vt}
 
     # 5) error against the FP64 ground truth of the last frame on the centre crop
     quality_out = None

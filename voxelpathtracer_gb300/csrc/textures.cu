@@ -61,9 +61,23 @@ __device__ void bilinear_level(const TexArray& a, int level, int layer, float u,
     const uint8_t* p10 = base + ((long long)j0 * sl + i1) * a.channels;
     const uint8_t* p01 = base + ((long long)j1 * sl + i0) * a.channels;
     const uint8_t* p11 = base + ((long long)j1 * sl + i1) * a.channels;
+    // a texel's channels in one load (RGBA8 texels are 4-byte aligned)
+    uint32_t w00, w10, w01, w11;
+    if (a.channels == 4) {
+        w00 = __ldg(reinterpret_cast<const uint32_t*>(p00));
+        w10 = __ldg(reinterpret_cast<const uint32_t*>(p10));
+        w01 = __ldg(reinterpret_cast<const uint32_t*>(p01));
+        w11 = __ldg(reinterpret_cast<const uint32_t*>(p11));
+    } else {
+        w00 = __ldg(p00);
+        w10 = __ldg(p10);
+        w01 = __ldg(p01);
+        w11 = __ldg(p11);
+    }
     for (int c = 0; c < nch; c++) {
-        const float v00 = texel_value(__ldg(p00 + c), srgb), v10 = texel_value(__ldg(p10 + c), srgb);
-        const float v01 = texel_value(__ldg(p01 + c), srgb), v11 = texel_value(__ldg(p11 + c), srgb);
+        const int sh = 8 * c;
+        const float v00 = texel_value((uint8_t)(w00 >> sh), srgb), v10 = texel_value((uint8_t)(w10 >> sh), srgb);
+        const float v01 = texel_value((uint8_t)(w01 >> sh), srgb), v11 = texel_value((uint8_t)(w11 >> sh), srgb);
         const float lo = v00 * bx + v10 * ax;
         const float hi = v01 * bx + v11 * ax;
         out[c] = lo * by + hi * ay;
