@@ -102,6 +102,7 @@ def lib() -> C.CDLL:
         L.vpto_ground_truth.argtypes = [P, P, P, P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                         C.c_uint32, P, P]
         L.vpto_generate_gbuffer.argtypes = [P, P, P, P, P, P, P, P, P, P]
+        L.vpto_set_block_textures.argtypes = [P]
         L.vpto_shade_textured.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, C.c_int, C.c_int, P, P, P, P, P]
         _lib = L
     return _lib
@@ -227,8 +228,9 @@ def _f32(d, keys):
     return {k: np.ascontiguousarray(d[k], dtype=np.float32) for k in keys if d.get(k) is not None}
 
 
-def trace_diffuse(world: World, cam, config, frame, t, face, rows=None) -> dict:
-    """Diffuse GI on the GI grid; t and face are the G-buffer's GI-grid view."""
+def trace_diffuse(world: World, cam, config, frame, t, face, rows=None, textures=None) -> dict:
+    """Diffuse GI on the GI grid; t and face are the G-buffer's GI-grid view;
+    textures (a block-texture dict) textures the bounce hits."""
     p = params(config)
     H, W = gi_dims(p)
     out = _planes(H, W, GI_SPEC)
@@ -236,8 +238,13 @@ def trace_diffuse(world: World, cam, config, frame, t, face, rows=None) -> dict:
     face = np.ascontiguousarray(face, dtype=np.uint8)
     r0, r1 = rows if rows else (0, H)
     s = _struct4(out, ["sh", "cocg", "luma", "aosky"])
-    lib().vpto_trace_diffuse(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)),
-                             _p(t), _p(face), r0, r1, C.byref(s))
+    keep = _set_textures(textures)
+    try:
+        lib().vpto_trace_diffuse(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p),
+                                 C.byref(_as(OFrame, frame)), _p(t), _p(face), r0, r1, C.byref(s))
+    finally:
+        lib().vpto_set_block_textures(None)
+    del keep
     return out
 
 
@@ -306,12 +313,8 @@ class OBlockTextures(C.Structure):   # vpto_block_textures
                 ("emissive_id", C.c_int32 * 128), ("grass", C.c_int32 * 10)]
 
 
-def generate_gbuffer(cam, config, textures: dict, t, face, block) -> dict:
-    """The textured G-buffer pass (GenerateGBuffer.glsl main) over the
-    G-buffer t / face / block with the block textures (a dict as
-    generate_block_textures makes): albedo (3), normal (3), pbr (4), ao."""
-    p = params(config)
-    H, W = p.height, p.width
+def _block_textures(textures: dict):
+    """(vpto_block_textures, the arrays it points into) for a texture dict."""
     keep = {k: np.ascontiguousarray(textures[k], np.uint8) for k in ("albedo", "normal", "pbr")}
     if textures.get("emissive") is not None:
         keep["emissive"] = np.ascontiguousarray(textures["emissive"], np.uint8)
@@ -323,6 +326,26 @@ def generate_gbuffer(cam, config, textures: dict, t, face, block) -> dict:
     for k in ("albedo_id", "normal_id", "pbr_id", "emissive_id"):
         getattr(bt, k)[:] = [int(v) for v in np.asarray(textures[k], np.int64)[:128]]
     bt.grass[:] = [int(v) for v in np.asarray(textures["grass"], np.int64)[:10]]
+    return bt, keep
+
+
+def _set_textures(textures):
+    """Sets (or clears, for None) the oracle's bounce-hit textures; returns what must stay alive."""
+    if textures is None:
+        lib().vpto_set_block_textures(None)
+        return None
+    bt, keep = _block_textures(textures)
+    lib().vpto_set_block_textures(C.byref(bt))   # copies the texels
+    return keep
+
+
+def generate_gbuffer(cam, config, textures: dict, t, face, block) -> dict:
+    """The textured G-buffer pass (GenerateGBuffer.glsl main) over the
+    G-buffer t / face / block with the block textures (a dict as
+    generate_block_textures makes): albedo (3), normal (3), pbr (4), ao."""
+    p = params(config)
+    H, W = p.height, p.width
+    bt, keep = _block_textures(textures)
     out = {"albedo": np.zeros((H, W, 3), np.float32), "normal": np.zeros((H, W, 3), np.float32),
            "pbr": np.zeros((H, W, 4), np.float32), "ao": np.zeros((H, W), np.float32)}
     ts, fs, bs = (np.ascontiguousarray(a, dtype=dt) for a, dt in ((t, np.float32), (face, np.uint8),
@@ -496,7 +519,7 @@ def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist:
     g = trace_primary(world, cam, p)
     shadow = trace_shadow(world, cam, p, frame, g["t"], g["face"])
     v = gi_view(p, g["t"], g["face"], g["block"])
-    gi = trace_diffuse(world, cam, p, frame, v["t"], v["face"])
+    gi = trace_diffuse(world, cam, p, frame, v["t"], v["face"], textures=textures)
     if p.denoiser == 1:
         sv = plain_denoise(cam, prev_cam, p, g, prev_g, gi, hist)
         last = sv["atrous"][-1] if sv["atrous"] else sv["temporal"]

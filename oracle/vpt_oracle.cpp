@@ -395,6 +395,13 @@ Lighting frame_lighting(const vpto_frame* f) {
     return L;
 }
 
+// The block textures' material at a bounce hit (set by vpto_set_block_textures;
+// false without textures): textureLod of the albedo array at level 3 and of
+// the PBR array at level 2 at the block's albedo layer (DiffuseRayTraceFrag.glsl
+// :569-584), at CalculateUV's coordinates (:1235-1273), and the emissive
+// texel at level 0 (has_emis false when the block has no emissive layer).
+bool tex_bounce_material(int bid, v3 ip, v3 hn, v3* albedo, float* rough, float* emis, bool* has_emis);
+
 // CalculateDiffuse (DiffuseRayTraceFrag.glsl:535-664) with `bounces` = MAX_BOUNCE_LIMIT.
 v4 calculate_diffuse(const vpto_world* w, const vpto_params* p, const vpto_frame* f, const Lighting& L,
                      v3 initial_origin, v3 input_normal, uint32_t* rng, v3* odir, bool* skyhit, RowCount* cnt) {
@@ -413,10 +420,20 @@ v4 calculate_diffuse(const vpto_world* w, const vpto_params* p, const vpto_frame
         bool intersect = T > 0.0f;
         v3 ip = add(ro, muls(rd, T));
         if (intersect && tr.block > 0) {
-            Material m = material(w, std::min(std::max(tr.block, 0), 127));
+            const int bid = std::min(std::max(tr.block, 0), 127);
+            Material m = material(w, bid);
             v3 hn = tr.normal;
             float emissivity = 0.0f;
-            if (m.emissive) emissivity = 1.0f * L.emissivity_multiplier * f->diffuse_light_intensity;
+            v3 t_albedo;
+            float t_rough, t_emis;
+            bool t_has;
+            if (tex_bounce_material(bid, ip, hn, &t_albedo, &t_rough, &t_emis, &t_has)) {
+                m.albedo = t_albedo;
+                m.rough = t_rough;
+                if (t_has) emissivity = t_emis * L.emissivity_multiplier * f->diffuse_light_intensity;
+            } else if (m.emissive) {
+                emissivity = 1.0f * L.emissivity_multiplier * f->diffuse_light_intensity;
+            }
             float ndl = fmaxg(dot(hn, L.light_dir), 0.0f);
             v3 bias_shadow = muls(hn, 0.045f);
             float shadow_at;
@@ -2461,3 +2478,56 @@ extern "C" void vpto_generate_gbuffer(const vpto_camera* cam, const vpto_params*
         }
     }
 }
+
+// Block textures of the diffuse bounce hits (test state of the oracle).
+namespace {
+struct OTexState {
+    bool on = false, has_e = false;
+    OTexArray A, P, E;
+    std::vector<int> albedo_id, emissive_id;
+    float srgb[256];
+};
+OTexState g_tex;
+}  // namespace
+
+extern "C" void vpto_set_block_textures(const vpto_block_textures* tx) {
+    g_tex = OTexState{};
+    if (!tx) return;
+    g_tex.A = build_tex_array(tx->albedo, tx->albedo_layers, 4, tx->size);
+    g_tex.P = build_tex_array(tx->pbr, tx->pbr_layers, 4, tx->size);
+    g_tex.has_e = tx->emissive != nullptr;
+    if (g_tex.has_e) g_tex.E = build_tex_array(tx->emissive, tx->emissive_layers, 1, tx->size);
+    g_tex.albedo_id.assign(tx->albedo_id, tx->albedo_id + 128);
+    g_tex.emissive_id.assign(tx->emissive_id, tx->emissive_id + 128);
+    for (int v = 0; v < 256; v++) {
+        const float x = (float)v / 255.0f;
+        g_tex.srgb[v] = x <= 0.04045f ? x / 12.92f : dm_pow((x + 0.055f) / 1.055f, 2.4f);
+    }
+    g_tex.on = true;
+}
+
+namespace {
+bool tex_bounce_material(int bid, v3 ip, v3 hn, v3* albedo, float* rough, float* emis, bool* has_emis) {
+    if (!g_tex.on) return false;
+    const v2 P = face_coords(ip, normal_id(hn));
+    const float u = fract(P.x), v = fract(P.y);
+    const int layer = g_tex.albedo_id[bid], el = g_tex.emissive_id[bid];
+    auto level = [&](const OTexArray& a, int id, int lv, int nch, const float* srgb, float* out) {
+        const int l = std::min(std::max(id, 0), a.layers - 1);
+        tex_bilinear(a, std::min(lv, a.levels - 1), l, u, v, nch, srgb, out);
+    };
+    float al[4], pb[4];
+    level(g_tex.A, layer, 3, 3, g_tex.srgb, al);
+    level(g_tex.P, layer, 2, 3, nullptr, pb);
+    *albedo = mk3(al[0], al[1], al[2]);
+    *rough = pb[0];
+    *has_emis = g_tex.has_e && el >= 0;
+    *emis = 0.0f;
+    if (*has_emis) {
+        float e[4];
+        level(g_tex.E, el, 0, 1, nullptr, e);
+        *emis = e[0];
+    }
+    return true;
+}
+}  // namespace

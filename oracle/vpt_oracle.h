@@ -251,6 +251,10 @@ typedef struct vpto_block_textures {
     int32_t grass[10];
 } vpto_block_textures;
 
+/* Block textures for the diffuse bounce hits of vpto_trace_diffuse (and the
+ * ground truth); NULL returns to the block table's flat materials. */
+void vpto_set_block_textures(const vpto_block_textures* tx);
+
 /* GenerateGBuffer.glsl main (parallax off, no lava): albedo (3), normal (3),
  * PBR (4) and texture AO (1) per pixel of the W x H G-buffer. */
 void vpto_generate_gbuffer(const vpto_camera* cam, const vpto_params* p, const vpto_block_textures* tx,

@@ -184,13 +184,18 @@ def test_oracle_textured_colour_pass(vpt, oracle):
     sky, hit = flat["g"]["t"] < 0, flat["g"]["t"] > 0
     assert (fd["rgb"][sky] == flat["rgb"][sky]).all() and (fb["rgb"][sky] == flat["rgb"][sky]).all()
     assert fb["rgb"][hit].mean() > 1.5 * fd["rgb"][hit].mean()
-    glow, plain = constant_textures(vpt), constant_textures(vpt)
-    glow["emissive_id"][:] = 0
-    plain["emissive_id"][:] = -1
-    fg = oracle.render_frame(world, cams[0], cams[0], cfg, frame, prev_g, hist, textures=glow)
-    fp = oracle.render_frame(world, cams[0], cams[0], cfg, frame, prev_g, hist, textures=plain)
-    lit = hit & (fg["gbt"]["pbr"][..., 3] > 0.05)
-    assert lit.any() and (fg["rgb"][lit] <= fp["rgb"][lit]).all() and fg["rgb"][lit].mean() < fp["rgb"][lit].mean()
+    # the bounce hits read the textures too: brighter texels, more bounced light
+    assert fb["gi"]["luma"][hit].mean() > fd["gi"]["luma"][hit].mean()
+    assert not np.array_equal(fd["gi"]["sh"], flat["gi"]["sh"])
+    # the same colour pass inputs but an emissive G-buffer texel: no direct light there
+    g, sv = fd["g"], fd["svgf"]["atrous"][-1]
+    glow = {k: v.copy() for k, v in fd["gbt"].items()}
+    glow["pbr"][..., 3] = np.where(hit, 1.0, 0.0)
+    args = (world, cams[0], cfg, frame, g["t"], g["face"], g["block"], fd["shadow"], sv["sh"], sv["cocg"], sv["aosky"])
+    lit = oracle.shade(*args, gbt=fd["gbt"])
+    dark = oracle.shade(*args, gbt=glow)
+    assert (lit == fd["rgb"]).all()
+    assert (dark[hit] <= lit[hit]).all() and dark[hit].mean() < lit[hit].mean() and (dark[sky] == lit[sky]).all()
 
 
 @pytest.mark.gpu
@@ -218,6 +223,9 @@ def test_textured_frames_bit_exact(vpt, oracle, storage, d, rspp, gpu):
             frame = vpt.default_frame(frame_index=k, seed=5, time=0.3 + 0.2 * k)
             rgb = ctx.render_frame(cam, frame)
             ref = oracle.render_frame(world, cam, prev_cam, cfg, frame, prev_g, hist, prev_refl, textures=tex)
+            for name, key in (("GI_SH", "sh"), ("GI_COCG", "cocg"), ("GI_LUMA", "luma"), ("GI_AOSKY", "aosky")):
+                got = ctx.read_plane(name)
+                assert_same(got[..., 0] if key == "luma" else got, ref["gi"][key], f"frame {k} {name}")
             assert_same(rgb, ref["rgb"], f"frame {k} colour")
             prev_g = {n: ref["g"][n] for n in ("t", "face", "block")}
             hist = ref["svgf"]["temporal"]

@@ -583,6 +583,18 @@ vpt_status vpt_set_block_table(vpt_ctx* c, const vpt_block* table, int32_t n) {
 }
 
 namespace {
+BlockTexView tex_view(const vpt_ctx* c) {
+    BlockTexView tv;
+    tv.albedo = c->tex_arr[0];
+    tv.normal = c->tex_arr[1];
+    tv.pbr = c->tex_arr[2];
+    tv.emissive = c->tex_arr[3];
+    tv.ids = c->tex_ids;
+    for (int k = 0; k < 10; k++) tv.grass[k] = c->tex_grass[k];
+    tv.srgb = c->srgb;
+    return tv;
+}
+
 void dfree(vpt_ctx* c, void** p) {
     if (!*p) return;
     for (size_t k = 0; k < c->allocs.size(); k++)
@@ -672,14 +684,7 @@ vpt_status vpt_generate_gbuffer(vpt_ctx* c) {
     if (!c->textured) return fail(c, VPT_ERR_STATE, "no block textures set (vpt_set_block_textures)");
     if (!c->have_cam) return fail(c, VPT_ERR_STATE, "no G-buffer yet (call vpt_trace_primary)");
     cudaSetDevice(c->dev);
-    BlockTexView tv;
-    tv.albedo = c->tex_arr[0];
-    tv.normal = c->tex_arr[1];
-    tv.pbr = c->tex_arr[2];
-    tv.emissive = c->tex_arr[3];
-    tv.ids = c->tex_ids;
-    for (int k = 0; k < 10; k++) tv.grass[k] = c->tex_grass[k];
-    tv.srgb = c->srgb;
+    const BlockTexView tv = tex_view(c);
     pass_begin(c, VPT_PASS_GBUFFER);
     CK(c, gbuffer_textured(cam_view(c->cam), c->cfg.width, c->cfg.height, c->fp16, c->gbuf[c->cur][GB_T],
                            (const uint8_t*)c->gbuf[c->cur][GB_FACE], (const uint8_t*)c->gbuf[c->cur][GB_BLOCK], tv,
@@ -795,6 +800,10 @@ vpt_status vpt_trace_diffuse(vpt_ctx* c, const vpt_frame* f) {
     a.frame_index = f->frame_index;
     a.seed = f->seed;
     a.lighting = gi_lighting(f);
+    if (c->textured) {
+        a.textured = 1;
+        a.tex = tex_view(c);
+    }
     GIOut o{c->gi[GI_SH], c->gi[GI_COCG], c->gi[GI_LUMA], c->gi[GI_AOSKY]};
     pass_begin(c, VPT_PASS_DIFFUSE);
     if ((s = refresh_view(c)) != VPT_OK) return s;
@@ -811,6 +820,7 @@ vpt_status vpt_trace_frame(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f
     vpt_status s = check_world(c);
     if (s != VPT_OK) return s;
     if (c->gd != 1) return fail(c, VPT_ERR_STATE, "the fused trace needs the GI on the G-buffer's grid");
+    if (c->textured) return fail(c, VPT_ERR_STATE, "the fused trace samples no block textures");
     cudaSetDevice(c->dev);
     c->cam = *cam;
     c->have_cam = true;
@@ -1197,7 +1207,7 @@ vpt_status shade_run(vpt_ctx* c, const vpt_frame* f, int source, void* out = nul
 
 vpt_status trace_all(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f) {
     vpt_status s;
-    if (c->tuning.fused_trace && c->gd == 1) return vpt_trace_frame(c, cam, f);
+    if (c->tuning.fused_trace && c->gd == 1 && !c->textured) return vpt_trace_frame(c, cam, f);
     if ((s = vpt_trace_primary(c, cam)) != VPT_OK) return s;
     if ((s = vpt_trace_shadow(c, f)) != VPT_OK) return s;
     return vpt_trace_diffuse(c, f);

@@ -4,6 +4,7 @@
 #pragma once
 #include "dda.cuh"
 #include "kernels.cuh"
+#include "textures.cuh"
 
 namespace vpt {
 
@@ -11,8 +12,14 @@ struct GICount {
     unsigned diffuse_rays, diffuse_steps, shadow_rays, shadow_steps;
 };
 
-// CalculateDiffuse (DiffuseRayTraceFrag.glsl:535-664); B is the distance-field layout.
-template <int B = 0>
+// CalculateDiffuse (DiffuseRayTraceFrag.glsl:535-664); B is the distance-field
+// layout. kTex: the bounce hit's albedo, roughness and emission come from the
+// block textures (:569-584): textureLod of the albedo array at level 3 and of
+// the PBR array at level 2, both at the block's albedo layer as the shader
+// indexes them, at CalculateUV's coordinates; the emissive texture (texture(),
+// whose implicit derivatives across a pixel quad's unrelated bounce hits are
+// taken as zero) at level 0.
+template <int B = 0, bool kTex = false>
 __device__ __forceinline__ v4 calculate_diffuse(const WorldView& w, const DiffuseArgs& a, v3 initial_origin,
                                                 v3 input_normal, uint32_t* rng, v3* odir, bool* skyhit,
                                                 GICount* cnt) {
@@ -35,10 +42,28 @@ __device__ __forceinline__ v4 calculate_diffuse(const WorldView& w, const Diffus
         bool intersect = T > 0.0f;
         v3 ip = add(ro, muls(rd, T));
         if (intersect && tr.block > 0) {
-            Material m = material(w, min(max(tr.block, 0), 127));
+            const int bid = min(max(tr.block, 0), 127);
+            Material m = material(w, bid);
             v3 hn = tr.normal;
             float emissivity = 0.0f;
-            if (m.emissive) emissivity = 1.0f * L.emissivity_multiplier * L.diffuse_light_intensity;
+            if (kTex) {
+                const BlockTexView& tv = a.tex;
+                const v2 P = face_coords(ip, normal_id(hn));
+                const float u = P.x - floorf(P.x), v = P.y - floorf(P.y);
+                const int layer = __ldg(tv.ids + bid), el = __ldg(tv.ids + 384 + bid);
+                float alb[4], pbr[4];
+                sample_level(tv.albedo, layer, u, v, 3, 3, tv.srgb, alb);
+                sample_level(tv.pbr, layer, u, v, 2, 3, nullptr, pbr);
+                m.albedo = mk3(alb[0], alb[1], alb[2]);
+                m.rough = pbr[0];
+                if (tv.emissive.texels && el >= 0) {
+                    float e[4];
+                    sample_level(tv.emissive, el, u, v, 0, 1, nullptr, e);
+                    emissivity = e[0] * L.emissivity_multiplier * L.diffuse_light_intensity;
+                }
+            } else if (m.emissive) {
+                emissivity = 1.0f * L.emissivity_multiplier * L.diffuse_light_intensity;
+            }
             float ndl = fmaxf(dot(hn, light_dir), 0.0f);
             v3 bias_shadow = muls(hn, 0.045f);
             float shadow_at;

@@ -58,6 +58,23 @@ struct GBufferOut {
     int32_t* hit;       // 3 per pixel
     uint16_t* steps;
 };
+// One block texture array on the device: `layers` layers of `size`^2 texels
+// of `channels` 8-bit channels per mip level, levels stored one after the
+// other (level l: layers x (size >> l)^2 texels from element offset
+// level_off[l] * channels).
+struct TexArray {
+    const uint8_t* texels;
+    int layers, channels, size, levels;
+    long long level_off[11];
+};
+// The arrays, the per-block layer ids [albedo 128 | normal 128 | PBR 128 |
+// emissive 128], the grass override and the sRGB decode table (256 entries).
+struct BlockTexView {
+    TexArray albedo, normal, pbr, emissive;   // emissive.texels NULL: none
+    const int* ids;
+    int grass[10];
+    const float* srgb;
+};
 struct DiffuseArgs {
     int diffuse_max_steps;
     int bounce_shadow_max_steps;
@@ -66,6 +83,9 @@ struct DiffuseArgs {
     uint32_t frame_index;
     uint32_t seed;
     GILighting lighting;
+    // block textures for the bounce hits (textured = 0: the block table)
+    int textured = 0;
+    BlockTexView tex{};
 };
 struct GIOut {
     void* sh;           // 4 ch
@@ -311,23 +331,6 @@ cudaError_t learned_features(int W, int H, int x0, int y0, int w, int h, int fp1
 cudaError_t learned_unpack(int W, int H, int fp16, const float* net_out, void* color, cudaStream_t s);
 
 // ---------------------------------------------------------- textures.cu --
-// One block texture array on the device: `layers` layers of `size`^2 texels
-// of `channels` 8-bit channels per mip level, levels stored one after the
-// other (level l: layers x (size >> l)^2 texels from element offset
-// level_off[l] * channels).
-struct TexArray {
-    const uint8_t* texels;
-    int layers, channels, size, levels;
-    long long level_off[11];
-};
-// The arrays, the per-block layer ids [albedo 128 | normal 128 | PBR 128 |
-// emissive 128], the grass override and the sRGB decode table (256 entries).
-struct BlockTexView {
-    TexArray albedo, normal, pbr, emissive;   // emissive.texels NULL: none
-    const int* ids;
-    int grass[10];
-    const float* srgb;
-};
 // Level l + 1 of every layer from level l (rounded 2 x 2 mean per channel).
 cudaError_t tex_build_mip(const TexArray& a, int level, uint8_t* texels, cudaStream_t s);
 // GenerateGBuffer.glsl main over the W x H G-buffer: albedo (3), normal (3),

@@ -64,7 +64,7 @@ __device__ __forceinline__ uint8_t shadow_pixel(const WorldView& w, const CamVie
 // kOneSample: the caller guarantees one sample (spp <= 1, sun stronger than
 // the moon), so nothing of the per-texel sums stays live across the traversal;
 // the arithmetic is the same.
-template <int B, typename S, bool kOneSample = false>
+template <int B, typename S, bool kOneSample = false, bool kTex = false>
 __device__ __forceinline__ void diffuse_pixel(const WorldView& w, const CamView& cam, int W, int H, int i, int j,
                                               const DiffuseArgs& a, size_t px, float d, int face, S* o_sh,
                                               S* o_cocg, S* o_luma, S* o_aosky, GICount* cnt) {
@@ -91,7 +91,7 @@ __device__ __forceinline__ void diffuse_pixel(const WorldView& w, const CamView&
     for (int s = 0; s < spp; s++) {
         v3 odir = mk3(0.0f, 0.0f, 0.0f);
         bool ss = false;
-        const v4 x = calculate_diffuse<B>(w, a, pos, n, &rng, &odir, &ss, cnt);
+        const v4 x = calculate_diffuse<B, kTex>(w, a, pos, n, &rng, &odir, &ss, cnt);
         const v3 xc = vclamp(mk3(x.x, x.y, x.z), 0.0f, 8.0f);
         radiance = add(radiance, xc);
         acc_ao += x.w;

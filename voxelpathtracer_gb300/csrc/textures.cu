@@ -20,7 +20,7 @@
 //     with the quad partner's world position reconstructed from its own depth
 //     and projected onto this pixel's face axes; a partner outside the image
 //     gives a zero derivative.
-#include "kernels.cuh"
+#include "textures.cuh"
 
 namespace vpt {
 
@@ -37,88 +37,6 @@ __global__ void k_mip(const uint8_t* src, uint8_t* dst, int layers, int s2, int 
         for (int c = 0; c < ch; c++)
             dst[q * ch + c] = (uint8_t)(((int)r0[c] + (int)r0[ch + c] + (int)r1[c] + (int)r1[ch + c] + 2) >> 2);
     }
-}
-
-__device__ __forceinline__ float fract_f(float x) { return x - floorf(x); }
-
-// texel channel value: byte / 255, or the sRGB decode of the byte
-__device__ __forceinline__ float texel_value(uint8_t v, const float* srgb) {
-    return srgb ? __ldg(srgb + v) : (float)v / 255.0f;
-}
-
-// texture() at one mip level: bilinear with REPEAT wrap and fp32 weights,
-// channels [0, nch)
-__device__ void bilinear_level(const TexArray& a, int level, int layer, float u, float v, int nch, const float* srgb,
-                               float* out) {
-    const int sl = a.size >> level;
-    const float x = u * (float)sl - 0.5f, y = v * (float)sl - 0.5f;
-    const float x0 = floorf(x), y0 = floorf(y);
-    const float ax = x - x0, ay = y - y0, bx = 1.0f - ax, by = 1.0f - ay;
-    const int i0 = wrapi(f2i(x0), sl), j0 = wrapi(f2i(y0), sl);
-    const int i1 = i0 + 1 == sl ? 0 : i0 + 1, j1 = j0 + 1 == sl ? 0 : j0 + 1;
-    const uint8_t* base = a.texels + (a.level_off[level] + (long long)layer * sl * sl) * a.channels;
-    const uint8_t* p00 = base + ((long long)j0 * sl + i0) * a.channels;
-    const uint8_t* p10 = base + ((long long)j0 * sl + i1) * a.channels;
-    const uint8_t* p01 = base + ((long long)j1 * sl + i0) * a.channels;
-    const uint8_t* p11 = base + ((long long)j1 * sl + i1) * a.channels;
-    // a texel's channels in one load (RGBA8 texels are 4-byte aligned)
-    uint32_t w00, w10, w01, w11;
-    if (a.channels == 4) {
-        w00 = __ldg(reinterpret_cast<const uint32_t*>(p00));
-        w10 = __ldg(reinterpret_cast<const uint32_t*>(p10));
-        w01 = __ldg(reinterpret_cast<const uint32_t*>(p01));
-        w11 = __ldg(reinterpret_cast<const uint32_t*>(p11));
-    } else {
-        w00 = __ldg(p00);
-        w10 = __ldg(p10);
-        w01 = __ldg(p01);
-        w11 = __ldg(p11);
-    }
-    for (int c = 0; c < nch; c++) {
-        const int sh = 8 * c;
-        const float v00 = texel_value((uint8_t)(w00 >> sh), srgb), v10 = texel_value((uint8_t)(w10 >> sh), srgb);
-        const float v01 = texel_value((uint8_t)(w01 >> sh), srgb), v11 = texel_value((uint8_t)(w11 >> sh), srgb);
-        const float lo = v00 * bx + v10 * ax;
-        const float hi = v01 * bx + v11 * ax;
-        out[c] = lo * by + hi * ay;
-    }
-}
-
-// level of detail of textureGrad(dPdx, dPdy) on a size x size array
-__device__ __forceinline__ float lod_of(int size, float dxu, float dxv, float dyu, float dyv) {
-    const float s = (float)size;
-    const float ax = dxu * s, ay = dxv * s, bx = dyu * s, by = dyv * s;
-    const float rx = sqrtf(ax * ax + ay * ay), ry = sqrtf(bx * bx + by * by);
-    return dlog2(fmaxf(rx, ry));
-}
-
-// LINEAR magnification / LINEAR_MIPMAP_LINEAR minification at level of detail lam
-__device__ void sample_lod(const TexArray& a, int layer_id, float u, float v, float lam, int nch, const float* srgb,
-                           float* out) {
-    const int layer = min(max(layer_id, 0), a.layers - 1);
-    const int q = a.levels - 1;
-    if (!(lam > 0.0f)) {
-        bilinear_level(a, 0, layer, u, v, nch, srgb, out);
-        return;
-    }
-    if (lam >= (float)q) {
-        bilinear_level(a, q, layer, u, v, nch, srgb, out);
-        return;
-    }
-    const float d1f = floorf(lam);
-    const int d1 = (int)d1f;
-    const float f = lam - d1f;
-    float t1[4], t2[4];
-    bilinear_level(a, d1, layer, u, v, nch, srgb, t1);
-    bilinear_level(a, d1 + 1, layer, u, v, nch, srgb, t2);
-    for (int c = 0; c < nch; c++) out[c] = (1.0f - f) * t1[c] + f * t2[c];
-}
-
-// the two face coordinates CalculateVectors takes for face id f: (x, y) for
-// +-Z, (x, z) for +-Y, (z, y) for +-X
-__device__ __forceinline__ v2 face_coords(v3 p, int f) {
-    const int axis = f >> 1;
-    return axis == 0 ? mk2(p.x, p.y) : (axis == 1 ? mk2(p.x, p.z) : mk2(p.z, p.y));
 }
 
 // world position of G-buffer texel (i, j): GetPositionAt (GenerateGBuffer.glsl:114-119)

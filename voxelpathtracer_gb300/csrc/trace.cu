@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(256) k_trace_shadow(WorldView w, CamView cam, 
 }
 
 // DiffuseRayTraceFrag.glsl main (:822-935)
-template <typename S, bool kOneSample>
+template <typename S, bool kOneSample, bool kTex>
 __global__ void __launch_bounds__(256, 8) k_trace_diffuse(WorldView w, CamView cam, int W, int H, DiffuseArgs a,
                                                        const S* t, const uint8_t* face, S* o_sh, S* o_cocg,
                                                        S* o_luma, S* o_aosky, Counters* stats) {
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(256, 8) k_trace_diffuse(WorldView w, CamView c
     GICount cnt = {0u, 0u, 0u, 0u};
     if (i < W && j < H) {
         const size_t px = (size_t)j * W + i;
-        diffuse_pixel<0, S, kOneSample>(w, cam, W, H, i, j, a, px, ld(t + px), __ldg(face + px), o_sh, o_cocg, o_luma, o_aosky,
+        diffuse_pixel<0, S, kOneSample, kTex>(w, cam, W, H, i, j, a, px, ld(t + px), __ldg(face + px), o_sh, o_cocg, o_luma, o_aosky,
                          &cnt);
     }
     if (stats) {
@@ -70,6 +70,16 @@ __global__ void __launch_bounds__(256, 8) k_trace_diffuse(WorldView w, CamView c
 }
 
 inline dim3 tile_grid(int W, int H) { return dim3((unsigned)((W + 15) / 16), (unsigned)((H + 15) / 16)); }
+
+template <typename S>
+void launch_diffuse(bool one, bool tex, dim3 grid, cudaStream_t s, const WorldView& w, const CamView& cam, int W,
+                    int H, const DiffuseArgs& a, const void* t, const uint8_t* face, GIOut out, Counters* stats) {
+    using K = void (*)(WorldView, CamView, int, int, DiffuseArgs, const S*, const uint8_t*, S*, S*, S*, S*, Counters*);
+    const K table[4] = {k_trace_diffuse<S, false, false>, k_trace_diffuse<S, false, true>,
+                        k_trace_diffuse<S, true, false>, k_trace_diffuse<S, true, true>};
+    table[(one ? 2 : 0) + (tex ? 1 : 0)]<<<grid, 256, 0, s>>>(w, cam, W, H, a, (const S*)t, face, (S*)out.sh,
+                                                               (S*)out.cocg, (S*)out.luma, (S*)out.aosky, stats);
+}
 
 }  // namespace
 
@@ -98,15 +108,11 @@ cudaError_t trace_shadow(const WorldView& w, const CamView& cam, int W, int H, i
 
 cudaError_t trace_diffuse(const WorldView& w, const CamView& cam, int W, int H, const DiffuseArgs& a, int fp16,
                           const void* t, const uint8_t* face, GIOut out, Counters* stats, cudaStream_t s) {
-    const bool one = a.spp <= 1 && !a.lighting.moon_stronger;
+    const bool one = a.spp <= 1 && !a.lighting.moon_stronger, tex = a.textured != 0;
     if (fp16)
-        (one ? k_trace_diffuse<__half, true> : k_trace_diffuse<__half, false>)<<<tile_grid(W, H), 256, 0, s>>>(
-            w, cam, W, H, a, (const __half*)t, face, (__half*)out.sh, (__half*)out.cocg, (__half*)out.luma,
-            (__half*)out.aosky, stats);
+        launch_diffuse<__half>(one, tex, tile_grid(W, H), s, w, cam, W, H, a, t, face, out, stats);
     else
-        (one ? k_trace_diffuse<float, true> : k_trace_diffuse<float, false>)<<<tile_grid(W, H), 256, 0, s>>>(
-            w, cam, W, H, a, (const float*)t, face, (float*)out.sh, (float*)out.cocg, (float*)out.luma,
-            (float*)out.aosky, stats);
+        launch_diffuse<float>(one, tex, tile_grid(W, H), s, w, cam, W, H, a, t, face, out, stats);
     return cudaGetLastError();
 }
 
