@@ -141,7 +141,7 @@ struct vpt_ctx {
     uint8_t* tex[4] = {};
     TexArray tex_arr[4] = {};
     int* tex_ids = nullptr;
-    float* srgb = nullptr;
+    float* srgb = nullptr;    // 256 sRGB decodes, then 256 values byte / 255
     int tex_grass[10] = {};
     bool textured = false;
     void* gbt[4] = {};
@@ -592,6 +592,7 @@ BlockTexView tex_view(const vpt_ctx* c) {
     tv.ids = c->tex_ids;
     for (int k = 0; k < 10; k++) tv.grass[k] = c->tex_grass[k];
     tv.srgb = c->srgb;
+    tv.unorm = c->srgb ? c->srgb + 256 : nullptr;
     return tv;
 }
 
@@ -660,10 +661,11 @@ vpt_status vpt_set_block_textures(vpt_ctx* c, const vpt_block_textures* t) {
         ids[256 + b] = t->pbr_id[b];
         ids[384 + b] = t->emissive_id[b];
     }
-    std::vector<float> lut(256);
+    std::vector<float> lut(512);
     for (int v = 0; v < 256; v++) {
         const float x = (float)v / 255.0f;
         lut[v] = x <= 0.04045f ? x / 12.92f : dpow((x + 0.055f) / 1.055f, 2.4f);
+        lut[256 + v] = x;
     }
     if ((st = dalloc(c, (void**)&c->tex_ids, ids.size() * sizeof(int))) != VPT_OK) return st;
     if ((st = dalloc(c, (void**)&c->srgb, lut.size() * sizeof(float))) != VPT_OK) return st;

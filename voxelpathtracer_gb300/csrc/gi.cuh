@@ -53,12 +53,12 @@ __device__ __forceinline__ v4 calculate_diffuse(const WorldView& w, const Diffus
                 const int layer = __ldg(tv.ids + bid), el = __ldg(tv.ids + 384 + bid);
                 float alb[4], pbr[4];
                 sample_level(tv.albedo, layer, u, v, 3, 3, tv.srgb, alb);
-                sample_level(tv.pbr, layer, u, v, 2, 3, nullptr, pbr);
+                sample_level(tv.pbr, layer, u, v, 2, 3, tv.unorm, pbr);
                 m.albedo = mk3(alb[0], alb[1], alb[2]);
                 m.rough = pbr[0];
                 if (tv.emissive.texels && el >= 0) {
                     float e[4];
-                    sample_level(tv.emissive, el, u, v, 0, 1, nullptr, e);
+                    sample_level(tv.emissive, el, u, v, 0, 1, tv.unorm, e);
                     emissivity = e[0] * L.emissivity_multiplier * L.diffuse_light_intensity;
                 }
             } else if (m.emissive) {

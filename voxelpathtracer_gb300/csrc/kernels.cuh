@@ -68,12 +68,14 @@ struct TexArray {
     long long level_off[11];
 };
 // The arrays, the per-block layer ids [albedo 128 | normal 128 | PBR 128 |
-// emissive 128], the grass override and the sRGB decode table (256 entries).
+// emissive 128], the grass override and the byte -> value tables (256
+// entries each: sRGB decode for albedo, byte / 255 for the others).
 struct BlockTexView {
     TexArray albedo, normal, pbr, emissive;   // emissive.texels NULL: none
     const int* ids;
     int grass[10];
     const float* srgb;
+    const float* unorm;   // byte / 255 (256 entries)
 };
 struct DiffuseArgs {
     int diffuse_max_steps;

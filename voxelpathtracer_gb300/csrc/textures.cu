@@ -118,12 +118,12 @@ __global__ void __launch_bounds__(256) k_gbuffer_tex(CamView cam, int W, int H, 
     const v3 B = f < 2 ? mk3(0.0f, 1.0f, 0.0f) : (f < 4 ? mk3(0.0f, 0.0f, 1.0f) : mk3(0.0f, -1.0f, 0.0f));
     const v3 N = normal_from_id(f, 1.0f);
     float nm[4], pbr[4], alb[4];
-    sample_lod(tv.normal, in_, uv.x, uv.y, lam, 3, nullptr, nm);
+    sample_lod(tv.normal, in_, uv.x, uv.y, lam, 3, tv.unorm, nm);
     for (int c = 0; c < 3; c++) nm[c] = nm[c] * 2.0f - 1.0f;
     // tbn * NormalMapped, columns tangent, bitangent, normal
     const v3 nmap = mk3((T.x * nm[0] + B.x * nm[1]) + N.x * nm[2], (T.y * nm[0] + B.y * nm[1]) + N.y * nm[2],
                         (T.z * nm[0] + B.z * nm[1]) + N.z * nm[2]);
-    sample_lod(tv.pbr, ip, uv.x, uv.y, lam, 4, nullptr, pbr);
+    sample_lod(tv.pbr, ip, uv.x, uv.y, lam, 4, tv.unorm, pbr);
     float emis = 0.0f;
     if (ie > -1) {
         // texture() with the implicit derivatives of UV itself
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(256) k_gbuffer_tex(CamView cam, int W, int H, 
         const float lam_e = lod_of(tv.emissive.size, quad_diff(ox, uv.x, ux.x), quad_diff(ox, uv.y, ux.y),
                                    quad_diff(oy, uv.x, uy.x), quad_diff(oy, uv.y, uy.y));
         float e[4];
-        sample_lod(tv.emissive, ie, uv.x, uv.y, lam_e, 1, nullptr, e);
+        sample_lod(tv.emissive, ie, uv.x, uv.y, lam_e, 1, tv.unorm, e);
         emis = e[0];
     }
     sample_lod(tv.albedo, ia, uv.x, uv.y, lam, 3, tv.srgb, alb);

@@ -1,6 +1,7 @@
 // Sampling of the block texture arrays as the CUDA path defines GL's fetches
 // (textures.cu has the full statement of the choices): REPEAT wrap, fp32
-// bilinear weights, texel = byte / 255 (sRGB-decoded through `srgb`), and
+// bilinear weights, texel = a 256-entry table of the byte (byte / 255, or its
+// sRGB decode for the albedo array), and
 // LINEAR / LINEAR_MIPMAP_LINEAR selection by level of detail. Shared by the
 // textured G-buffer pass and the diffuse trace's bounce hits.
 #pragma once
@@ -10,14 +11,13 @@ namespace vpt {
 
 __device__ __forceinline__ float fract_f(float x) { return x - floorf(x); }
 
-// texel channel value: byte / 255, or the sRGB decode of the byte
-__device__ __forceinline__ float texel_value(uint8_t v, const float* srgb) {
-    return srgb ? __ldg(srgb + v) : (float)v / 255.0f;
-}
+// texel channel value: the byte through the array's table (byte / 255 or the
+// sRGB decode, computed once on the host: a table load instead of a division)
+__device__ __forceinline__ float texel_value(uint8_t v, const float* lut) { return __ldg(lut + v); }
 
 // texture() at one mip level: bilinear with REPEAT wrap and fp32 weights,
 // channels [0, nch)
-__device__ inline void bilinear_level(const TexArray& a, int level, int layer, float u, float v, int nch, const float* srgb,
+__device__ inline void bilinear_level(const TexArray& a, int level, int layer, float u, float v, int nch, const float* lut,
                                float* out) {
     const int sl = a.size >> level;
     const float x = u * (float)sl - 0.5f, y = v * (float)sl - 0.5f;
@@ -45,8 +45,8 @@ __device__ inline void bilinear_level(const TexArray& a, int level, int layer, f
     }
     for (int c = 0; c < nch; c++) {
         const int sh = 8 * c;
-        const float v00 = texel_value((uint8_t)(w00 >> sh), srgb), v10 = texel_value((uint8_t)(w10 >> sh), srgb);
-        const float v01 = texel_value((uint8_t)(w01 >> sh), srgb), v11 = texel_value((uint8_t)(w11 >> sh), srgb);
+        const float v00 = texel_value((uint8_t)(w00 >> sh), lut), v10 = texel_value((uint8_t)(w10 >> sh), lut);
+        const float v01 = texel_value((uint8_t)(w01 >> sh), lut), v11 = texel_value((uint8_t)(w11 >> sh), lut);
         const float lo = v00 * bx + v10 * ax;
         const float hi = v01 * bx + v11 * ax;
         out[c] = lo * by + hi * ay;
@@ -62,24 +62,24 @@ __device__ __forceinline__ float lod_of(int size, float dxu, float dxv, float dy
 }
 
 // LINEAR magnification / LINEAR_MIPMAP_LINEAR minification at level of detail lam
-__device__ inline void sample_lod(const TexArray& a, int layer_id, float u, float v, float lam, int nch, const float* srgb,
+__device__ inline void sample_lod(const TexArray& a, int layer_id, float u, float v, float lam, int nch, const float* lut,
                            float* out) {
     const int layer = min(max(layer_id, 0), a.layers - 1);
     const int q = a.levels - 1;
     if (!(lam > 0.0f)) {
-        bilinear_level(a, 0, layer, u, v, nch, srgb, out);
+        bilinear_level(a, 0, layer, u, v, nch, lut, out);
         return;
     }
     if (lam >= (float)q) {
-        bilinear_level(a, q, layer, u, v, nch, srgb, out);
+        bilinear_level(a, q, layer, u, v, nch, lut, out);
         return;
     }
     const float d1f = floorf(lam);
     const int d1 = (int)d1f;
     const float f = lam - d1f;
     float t1[4], t2[4];
-    bilinear_level(a, d1, layer, u, v, nch, srgb, t1);
-    bilinear_level(a, d1 + 1, layer, u, v, nch, srgb, t2);
+    bilinear_level(a, d1, layer, u, v, nch, lut, t1);
+    bilinear_level(a, d1 + 1, layer, u, v, nch, lut, t2);
     for (int c = 0; c < nch; c++) out[c] = (1.0f - f) * t1[c] + f * t2[c];
 }
 
@@ -94,9 +94,9 @@ __device__ __forceinline__ v2 face_coords(v3 p, int f) {
 // textureLod at an integer level: the level's bilinear sample (the last
 // level from q on)
 __device__ __forceinline__ void sample_level(const TexArray& a, int layer_id, float u, float v, int level, int nch,
-                                             const float* srgb, float* out) {
+                                             const float* lut, float* out) {
     const int layer = min(max(layer_id, 0), a.layers - 1);
-    bilinear_level(a, min(level, a.levels - 1), layer, u, v, nch, srgb, out);
+    bilinear_level(a, min(level, a.levels - 1), layer, u, v, nch, lut, out);
 }
 
 }  // namespace vpt
