@@ -252,22 +252,26 @@ def run_ours(args):
     if traffic is None and args.storage == 0 and args.gi_divisor == 1 and args.reflection_spp == 0:
         traffic, traffic_source = profile_traffic(KERNEL_NAMES[dom])
 
-    # 3) end-to-end through the C ABI with host buffers (pinned)
+    # 3) end-to-end through the C ABI with host buffers (pinned): every frame's
+    # image is copied to host memory by vpt_render_frame_async, double
+    # buffered (the copy of frame k runs while frame k + 1 computes); the
+    # timed region ends when the last image is in host memory
     ctx.reset_history()
-    out = torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True)
-    out_np = out.numpy()
+    outs = [torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
     for s in range(args.warmup):
-        ctx.render_frame(camera_at(vpt, yaw, pitch, s), frame_at(vpt, s), out=out_np)
+        ctx.render_frame_async(camera_at(vpt, yaw, pitch, s), frame_at(vpt, s), outs[s % 2])
+    ctx.readback_wait()
     dist.barrier()
     t0 = time.perf_counter()
     for s in range(args.warmup, total):
         cam = camera_at(vpt, yaw, pitch, s)
         fr = frame_at(vpt, s)
-        ctx.render_frame(cam, fr, out=out_np)
+        ctx.render_frame_async(cam, fr, outs[s % 2])
+    ctx.readback_wait()
     e2e_t = dist.max(time.perf_counter() - t0)
     e2e_value = rays_total / e2e_t
     h2d = len(bytes(memoryview(vpt.Camera()))) + len(bytes(memoryview(vpt.Frame())))
-    last_rgb = {"fp32": out_np.copy()}
+    last_rgb = {"fp32": outs[(total - 1) % 2].copy()}
 
     # 4) variants on the same frames (device-resident timing): FP16 storage, and
     # the reference's default GI grid (DiffuseTraceResolution 1/4: diffuse rays
@@ -389,7 +393,7 @@ def run_ours(args):
                    "l2": "flushed (512 MiB write) between timed steps"},
         "e2e": {"value": e2e_value, "unit": "rays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": W * H * 3 * 4, "ms_per_step": e2e_t * 1e3 / args.steps,
-                "api": "vpt_render_frame -> pinned host RGB"},
+                "api": "vpt_render_frame_async -> pinned host RGB, double-buffered readback"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom],
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -337,6 +337,15 @@ vpt_status vpt_reset_history(vpt_ctx* ctx);
  * (W*H*3 floats) and the call waits for it. prev_cam may be NULL on the
  * first frame (the camera of the previous call is used otherwise). */
 vpt_status vpt_render_frame(vpt_ctx* ctx, const vpt_camera* cam, const vpt_frame* frame, float* rgb_out);
+/* The same frame with a double-buffered readback: the COLOR plane is copied
+ * to rgb_out (float32 RGB, W*H*3; page-locked host memory lets the copy run
+ * asynchronously) on a copy stream while the next call's frame is computed.
+ * The call returns once the PREVIOUS call's image is complete, so one frame
+ * is in flight; vpt_readback_wait completes the last one. rgb_out must stay
+ * valid until then. */
+vpt_status vpt_render_frame_async(vpt_ctx* ctx, const vpt_camera* cam, const vpt_frame* frame, float* rgb_out);
+/* Waits for the readback of the last vpt_render_frame_async call. */
+vpt_status vpt_readback_wait(vpt_ctx* ctx);
 
 /* The colour pass from the denoised GI (source 0, as vpt_shade), from the
  * temporally accumulated GI before any spatial filter (source 1) or from

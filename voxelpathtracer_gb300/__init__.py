@@ -177,6 +177,8 @@ def _load() -> C.CDLL:
         "vpt_end_frame": ([P], C.c_int),
         "vpt_reset_history": ([P], C.c_int),
         "vpt_render_frame": ([P, C.POINTER(Camera), C.POINTER(Frame), P], C.c_int),
+        "vpt_render_frame_async": ([P, C.POINTER(Camera), C.POINTER(Frame), P], C.c_int),
+        "vpt_readback_wait": ([P], C.c_int),
         "vpt_plane_info": ([P, i32, C.POINTER(sz), C.POINTER(i32), C.POINTER(i32)], C.c_int),
         "vpt_plane_dims": ([P, i32, C.POINTER(i32), C.POINTER(i32)], C.c_int),
         "vpt_read_plane": ([P, i32, P, sz], C.c_int),
@@ -601,6 +603,20 @@ class Context:
         ptr = _ptr(out) if readback else None
         self._ck(lib.vpt_render_frame(self._h, C.byref(cam), C.byref(frame), ptr), "vpt_render_frame")
         return out
+
+    def render_frame_async(self, cam: Camera, frame: Frame, out: np.ndarray):
+        """vpt_render_frame_async: the image lands in `out` (float32 H x W x 3,
+        ideally page-locked) while the next frame computes; returns once the
+        previous call's image is complete. readback_wait() finishes the last."""
+        if out.dtype != np.float32 or out.shape != (self.height, self.width, 3) or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float32 (H, W, 3) array")
+        self._ck(lib.vpt_render_frame_async(self._h, C.byref(cam), C.byref(frame), _ptr(out)),
+                 "vpt_render_frame_async")
+        self._async_out = getattr(self, "_async_out", [])[-1:] + [out]   # keep the in-flight buffers alive
+
+    def readback_wait(self):
+        self._ck(lib.vpt_readback_wait(self._h), "vpt_readback_wait")
+        self._async_out = []
 
     # planes
     def plane_info(self, plane):

@@ -146,6 +146,12 @@ struct vpt_ctx {
     bool textured = false;
     void* gbt[4] = {};
     bool gbt_valid = false;   // the textured planes belong to this frame's G-buffer
+    // double-buffered readback (vpt_render_frame_async): copy stream, the
+    // copy's completion event, and an fp32 staging plane for fp16 storage
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_color = nullptr, ev_copy = nullptr;
+    bool copy_pending = false;
+    void* color_stage = nullptr;
 };
 
 namespace {
@@ -528,6 +534,10 @@ vpt_status vpt_destroy(vpt_ctx* c) {
             if (c->ev[p][k]) cudaEventDestroy(c->ev[p][k]);
     for (int k = 0; k < 2; k++)
         if (c->ev_net[k]) cudaEventDestroy(c->ev_net[k]);
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+    if (c->ev_color) cudaEventDestroy(c->ev_color);
+    if (c->ev_copy) cudaEventDestroy(c->ev_copy);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return VPT_OK;
@@ -1198,6 +1208,8 @@ vpt_status shade_run(vpt_ctx* c, const vpt_frame* f, int source, void* out = nul
         a.gb_pbr = c->gbt[2];
         a.gb_ao = c->gbt[3];
     }
+    // an asynchronous readback of the colour plane must finish before it is rewritten
+    if (!out && c->copy_pending) CK(c, cudaStreamWaitEvent(c->stream, c->ev_copy, 0));
     pass_begin(c, VPT_PASS_SHADE);
     CK(c, shade(world_view(c), cam_view(c->cam), c->cfg.width, c->cfg.height, c->fp16, a, c->gbuf[c->cur][GB_T],
                 (const uint8_t*)c->gbuf[c->cur][GB_FACE], (const uint8_t*)c->gbuf[c->cur][GB_BLOCK], c->shadow, sh, cocg,
@@ -1319,6 +1331,7 @@ vpt_status vpt_render_frame_learned(vpt_ctx* c, vpt_unet* net, const vpt_camera*
         vpt_unet_output(net, &out);
         CK(c, cudaEventRecord(c->ev_net[1], (cudaStream_t)ns));
         CK(c, cudaStreamWaitEvent(c->stream, c->ev_net[1], 0));
+        if (c->copy_pending) CK(c, cudaStreamWaitEvent(c->stream, c->ev_copy, 0));
         CK(c, learned_unpack(W, H, c->fp16, out, c->color, c->stream));
         pass_end(c, VPT_PASS_LEARNED);
         c->launches += 2;
@@ -1357,6 +1370,59 @@ vpt_status vpt_render_frame(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* 
     if ((s = vpt_shade(c, f)) != VPT_OK) return s;
     if (rgb_out && (s = read_color(c, rgb_out)) != VPT_OK) return s;
     return vpt_end_frame(c);
+}
+
+namespace {
+__global__ void k_half_to_float(const __half* in, float* out, long long n) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        out[k] = __half2float(in[k]);
+}
+}  // namespace
+
+vpt_status vpt_render_frame_async(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f, float* rgb_out) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    if (!cam || !f || !rgb_out) return fail(c, VPT_ERR_INVALID_ARG, "camera, frame and rgb_out are required");
+    cudaSetDevice(c->dev);
+    if (!c->copy_stream) {
+        CK(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        CK(c, cudaEventCreateWithFlags(&c->ev_color, cudaEventDisableTiming));
+        CK(c, cudaEventCreateWithFlags(&c->ev_copy, cudaEventDisableTiming));
+    }
+    vpt_status s;
+    const vpt_camera prev = c->have_prev ? c->prev_cam : *cam;
+    if ((s = trace_all(c, cam, f)) != VPT_OK) return s;
+    if (c->textured && (s = vpt_generate_gbuffer(c)) != VPT_OK) return s;
+    if ((s = vpt_svgf(c, &prev, f)) != VPT_OK) return s;
+    if (c->cfg.reflection_spp > 0 && (s = reflection_run(c, f)) != VPT_OK) return s;
+    if ((s = vpt_shade(c, f)) != VPT_OK) return s;   // waits for the previous readback on the device
+    // this frame is queued: the previous image is complete once its copy is
+    if (c->copy_pending) CK(c, cudaEventSynchronize(c->ev_copy));
+    const size_t n = c->npx * 3;
+    const void* src = c->color;
+    if (c->fp16) {
+        if (!c->color_stage && (s = dalloc(c, &c->color_stage, n * 4)) != VPT_OK) return s;
+        const long long blocks = ((long long)n + 255) / 256;
+        k_half_to_float<<<(unsigned)(blocks < 65535 ? blocks : 65535), 256, 0, c->stream>>>((const __half*)c->color,
+                                                                                       (float*)c->color_stage,
+                                                                                       (long long)n);
+        CK(c, cudaGetLastError());
+        c->launches += 1;
+        src = c->color_stage;
+    }
+    CK(c, cudaEventRecord(c->ev_color, c->stream));
+    CK(c, cudaStreamWaitEvent(c->copy_stream, c->ev_color, 0));
+    CK(c, cudaMemcpyAsync(rgb_out, src, n * 4, cudaMemcpyDeviceToHost, c->copy_stream));
+    CK(c, cudaEventRecord(c->ev_copy, c->copy_stream));
+    c->copy_pending = true;
+    return vpt_end_frame(c);
+}
+
+vpt_status vpt_readback_wait(vpt_ctx* c) {
+    if (!c) return VPT_ERR_INVALID_ARG;
+    cudaSetDevice(c->dev);
+    if (c->copy_pending) CK(c, cudaEventSynchronize(c->ev_copy));
+    c->copy_pending = false;
+    return VPT_OK;
 }
 
 vpt_status vpt_plane_info(const vpt_ctx* c, int32_t plane, size_t* bytes, int32_t* channels, int32_t* dtype) {
