@@ -197,7 +197,7 @@ typedef struct vpt_tuning {
 /* ------------------------------------------------------------- lifetime -- */
 const char* vpt_status_string(vpt_status s);
 int vpt_abi_version(void);
-/* Defaults of the reference's frame loop at BASELINE sizes (1920x1080, 1 spp, 1 bounce). */
+/* Defaults of the reference's frame loop for a 1920x1080 frame with 1 spp and 1 bounce. */
 vpt_status vpt_default_config(vpt_config* cfg);
 vpt_status vpt_default_frame(vpt_frame* frame);
 /* Replaces MainPipeline::StartPipeline's FBO creation (Core/Pipeline.cpp:1094-1158, :1690-1735). */
