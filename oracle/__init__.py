@@ -103,6 +103,7 @@ def lib() -> C.CDLL:
                                         C.c_uint32, P, P]
         L.vpto_generate_gbuffer.argtypes = [P, P, P, P, P, P, P, P, P, P]
         L.vpto_set_block_textures.argtypes = [P]
+        L.vpto_set_textured_gbuffer.argtypes = [P, P, C.c_int, C.c_int]
         L.vpto_shade_textured.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, C.c_int, C.c_int, P, P, P, P, P]
         _lib = L
     return _lib
@@ -531,19 +532,31 @@ def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist:
             sh, cocg, ao = last["sh"], last["cocg"], last["aosky"]
         else:
             sh, cocg, ao = sv["variance"]["sh"], sv["variance"]["cocg"], sv["temporal"]["aosky"]
+    gbt = None if textures is None else generate_gbuffer(cam, p, textures, g["t"], g["face"], g["block"])
     refl = None
     if p.reflection_spp > 0:
-        refl = trace_reflection(world, cam, p, frame, g, shadow, {"sh": sh, "cocg": cocg, "aosky": ao})
-        refl["raw_hit"] = refl["hit"]
-        refl["hit"] = spec_hit_blur(p, g, refl["raw_hit"])
-        prev_refl = prev_refl if prev_refl is not None else empty_reflection_history(p)
-        refl.update(spec_temporal(world, cam, prev_cam, p, g, prev_g, refl, prev_refl))
-        if p.reflection_denoise:
-            hd = refl["stable"] if p.reflection_temporal else refl["hit"]
-            refl["den1"] = spec_denoise(world, cam, p, g, refl["out"], hd, refl["acc"], 1)
-            refl["den"] = spec_denoise(world, cam, p, g, refl["den1"], hd, refl["acc"], 0)
+        # with block textures the reflection passes read the textured G-buffer
+        # and sample the textures at their hits
+        keep = _set_textures(textures)
+        if gbt is not None:
+            gbn = np.ascontiguousarray(gbt["normal"], np.float32)
+            gbp = np.ascontiguousarray(gbt["pbr"], np.float32)
+            lib().vpto_set_textured_gbuffer(_p(gbn), _p(gbp), p.width, p.height)
+        try:
+            refl = trace_reflection(world, cam, p, frame, g, shadow, {"sh": sh, "cocg": cocg, "aosky": ao})
+            refl["raw_hit"] = refl["hit"]
+            refl["hit"] = spec_hit_blur(p, g, refl["raw_hit"])
+            prev_refl = prev_refl if prev_refl is not None else empty_reflection_history(p)
+            refl.update(spec_temporal(world, cam, prev_cam, p, g, prev_g, refl, prev_refl))
+            if p.reflection_denoise:
+                hd = refl["stable"] if p.reflection_temporal else refl["hit"]
+                refl["den1"] = spec_denoise(world, cam, p, g, refl["out"], hd, refl["acc"], 1)
+                refl["den"] = spec_denoise(world, cam, p, g, refl["den1"], hd, refl["acc"], 0)
+        finally:
+            lib().vpto_set_textured_gbuffer(None, None, 0, 0)
+            lib().vpto_set_block_textures(None)
+        del keep
     spec = None if refl is None else (refl["den"] if p.reflection_denoise else refl["out"])
-    gbt = None if textures is None else generate_gbuffer(cam, p, textures, g["t"], g["face"], g["block"])
     rgb = shade(world, cam, p, frame, g["t"], g["face"], g["block"], shadow, sh, cocg, ao, spec=spec, gbt=gbt)
     return {"g": g, "shadow": shadow, "gi": gi, "svgf": sv, "refl": refl, "rgb": rgb, "gbt": gbt}
 

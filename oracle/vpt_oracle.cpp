@@ -1481,6 +1481,39 @@ inline v3 reflection_directional_light(v3 viewer, v3 wp, v3 light_dir, v3 radian
 
 // The face UV of CalculateVectors (ReflectionTraceFrag.glsl:1388-1446) with
 // the shader's UV.y = 1 - UV.y (:848).
+// The textured G-buffer the reflection passes read with block textures
+// (vpto_set_textured_gbuffer; off: the block table and the face normals):
+// PBR nearest and the normal-mapped normal bilinear at uv, as GL samples them.
+struct GbtState {
+    const float* normal = nullptr;
+    const float* pbr = nullptr;
+    int W = 0, H = 0;
+};
+GbtState g_gbt;
+inline float gbt_pbr(v2 uv, int c) {
+    const Plane P{g_gbt.pbr, g_gbt.W, g_gbt.H, 4};
+    return P.at(f2i(std::floor(uv.x * (float)g_gbt.W)), f2i(std::floor(uv.y * (float)g_gbt.H)), c);
+}
+inline v3 gbt_normal(v2 uv) {
+    const Plane P{g_gbt.normal, g_gbt.W, g_gbt.H, 3};
+    float n[3];
+    P.linear(uv, n);
+    return mk3(n[0], n[1], n[2]);
+}
+inline v3 gbt_normal_at(size_t px) {
+    return mk3(g_gbt.normal[px * 3], g_gbt.normal[px * 3 + 1], g_gbt.normal[px * 3 + 2]);
+}
+
+// The block textures at a reflection hit (ReflectionTraceFrag.glsl :887-1007):
+// albedo, PBR (level 0), the normal map at level 3 through the face's tangent
+// basis and the emissive texel at level 2 (-1 without one); false without
+// textures.
+struct TexHit {
+    v3 albedo, nmap;
+    float rough, metal, ao, emis;
+};
+bool tex_reflection_hit(int rid, v3 hp, v3 hn, TexHit* out);
+
 inline v2 face_uv(v3 p, v3 n) {
     v2 uv;
     if (n.z != 0.0f) uv = v2{fract(p.x), fract(p.y)};
@@ -1520,8 +1553,14 @@ void reflection_texel(const vpto_world* w, const vpto_camera* cam, const vpto_pa
     const v3 N = normal_from_id(in.FV.at(i, j), 1.0f);
     // NormalMappedInitial (:794): the linear normal G-buffer at the texel
     // centre, the face normal itself on the G-buffer's grid
-    const v3 NM = gi_div(p) == 1 ? N : gnormal_linear(in.F, uv);
+    v3 NM = gi_div(p) == 1 ? N : gnormal_linear(in.F, uv);
     const Material base = material(w, std::min(std::max(in.BV.at(i, j), 0), 127));
+    float base_rough = base.rough, base_metal = base.metal;
+    if (g_gbt.normal) {
+        base_rough = gbt_pbr(uv, 0);
+        base_metal = gbt_pbr(uv, 1);
+        NM = gi_div(p) == 1 ? gbt_normal_at(q) : gbt_normal(uv);
+    }
     const v3 I = normalize(sub(mk3(P.x, P.y, P.z), viewer));
     P.x += N.x * 0.035f;
     P.y += N.y * 0.035f;
@@ -1543,7 +1582,7 @@ void reflection_texel(const vpto_world* w, const vpto_camera* cam, const vpto_pa
     float avg_hit = 0.001f, meaningful = 0.0f, emask = 0.0f, computed_shadow = 0.0f;
     int shadow_itr = 0, total_hits = 0;
     for (int s = 0; s < spp; s++) {
-        const v3 rn = reflection_normal(NM, clampf(base.rough * rbias, 0.01f, 1.0f), &rng);
+        const v3 rn = reflection_normal(NM, clampf(base_rough * rbias, 0.01f, 1.0f), &rng);
         const v3 R = reflect3(I, rn);
         const TraceResult tr = traverse(w, pos, R, p->reflection_max_steps);
         cnt->add(4, tr.steps);
@@ -1573,9 +1612,19 @@ void reflection_texel(const vpto_world* w, const vpto_camera* cam, const vpto_pa
                 const float vxao = dm_pow(rao[0], 0.75f);
                 if (pa.w > 0.0f && length(sub(mk3(pa.x, pa.y, pa.z), cam_pos)) < 40.0f) ambient = muls(ambient, vxao);
             }
-            const Material m = material(w, rid);
+            Material m = material(w, rid);
             const v3 radiance = muls(mixed, 0.6f);
-            const float ao = dm_pow(1.0f, 2.0f);
+            float ao = dm_pow(1.0f, 2.0f);
+            v3 nmap = hn;
+            TexHit th;
+            const bool textured = tex_reflection_hit(rid, hp, hn, &th);
+            if (textured) {
+                m.albedo = th.albedo;
+                m.rough = th.rough;
+                m.metal = th.metal;
+                ao = th.ao;
+                nmap = th.nmap;
+            }
             if (shadow_itr < std::max(spp / 4, 1)) {   // (:929-953)
                 if (success && in_ss) {
                     computed_shadow = in.S.linearf(rc);
@@ -1588,10 +1637,11 @@ void reflection_texel(const vpto_world* w, const vpto_camera* cam, const vpto_pa
                 shadow_itr++;
             }
             ambient = mul(muls(muls(ambient, 1.0f), clampf(ao, 0.1f, 1.0f)), m.albedo);
-            v3 direct = add(ambient, reflection_directional_light(viewer, hp, L.light_dir, radiance, m.albedo, hn,
+            v3 direct = add(ambient, reflection_directional_light(viewer, hp, L.light_dir, radiance, m.albedo, nmap,
                                                                   m.rough, m.metal, computed_shadow));
-            if (m.emissive) {   // (:988-1007), Emissivity = 1 for a flat emissive block
-                float emissivity = 1.0f;
+            // (:988-1007), Emissivity = 1 for a flat emissive block
+            if (textured ? th.emis > 0.1f : m.emissive != 0) {
+                float emissivity = textured ? th.emis : 1.0f;
                 const v2 fuv = face_uv(hp, hn);
                 const float bx = 0.02501f, by = 0.03001f;
                 emissivity *= (fuv.x > bx && fuv.x < 1.0f - bx && fuv.y > by && fuv.y < 1.0f - by) ? 1.0f : 0.0f;
@@ -1602,7 +1652,7 @@ void reflection_texel(const vpto_world* w, const vpto_camera* cam, const vpto_pa
             avg_hit += T;
             meaningful += 1.0f;
         } else {
-            computed = muls(sky_radiance(normalize(R)), mixf(1.0f, 1.175f, base.metal > 0.05f ? 1.0f : 0.0f));
+            computed = muls(sky_radiance(normalize(R)), mixf(1.0f, 1.175f, base_metal > 0.05f ? 1.0f : 0.0f));
         }
         total[0] += computed.x;
         total[1] += computed.y;
@@ -1755,7 +1805,8 @@ void vpto_spec_temporal(const vpto_world* w, const vpto_camera* cam, const vpto_
             if (P.w > 0.0f && temporal) {
                 const bool sky = hc < 0.0f;
                 const Material mt = material(w, std::min(std::max(BV.at(i, j), 0), 127));
-                const float rough = mixf(0.095f, mt.rough, 1.0f), metal = mt.metal;
+                const float pr = g_gbt.pbr ? gbt_pbr(uv, 0) : mt.rough;
+                const float rough = mixf(0.095f, pr, 1.0f), metal = g_gbt.pbr ? gbt_pbr(uv, 1) : mt.metal;
                 bool less_valid = false;
                 v2 rep = v2{0.0f, 0.0f};
                 if (hc > 0.0f && !sky && rough <= 0.875f + 0.01f) {
@@ -1913,11 +1964,13 @@ void vpto_spec_denoise(const vpto_world* w, const vpto_camera* cam, const vpto_p
             for (int c = 0; c < 4; c++) bc[c] = IN.at(i, j, c);
             const float base_lum = dot(mk3(bc[0], bc[1], bc[2]), mk3(0.299f, 0.587f, 0.114f));
             const int bblock = BV.at(i, j);
-            const float pbr_x = pbr_rough(w, bblock), pbr_y = pbr_metal(w, bblock);
+            const bool gbt = g_gbt.pbr != nullptr;
+            const float pbr_x = gbt ? gbt_pbr(uv, 0) : pbr_rough(w, bblock);
+            const float pbr_y = gbt ? gbt_pbr(uv, 1) : pbr_metal(w, bblock);
             float br = pbr_x + 0.001f;
             const float raw_rough = br;
             br *= mixf(1.0f, 0.91f, 1.0f);
-            const v3 nm_base = d == 1 ? bn : gnormal_linear(F, uv);
+            const v3 nm_base = gbt ? (d == 1 ? gbt_normal_at(q) : gbt_normal(uv)) : (d == 1 ? bn : gnormal_linear(F, uv));
             float hd = hit_data[q] + 0.0001f;
             if (hd < 0.001f) hd = 1.75f;
             else hd = dm_pow(hd, 1.0f / 1.3f);
@@ -1994,7 +2047,7 @@ void vpto_spec_denoise(const vpto_world* w, const vpto_camera* cam, const vpto_p
                     sface = F.nearest(sc);
                     sblock = B.nearest(sc);
                     IN.linear(sc, sd);
-                    nm_at = gnormal_linear(F, sc);
+                    nm_at = gbt ? gbt_normal(sc) : gnormal_linear(F, sc);
                 }
                 const bool sample_sky = sdepth < 0.0f;
                 if (sample_sky != base_sky) continue;
@@ -2003,7 +2056,7 @@ void vpto_spec_denoise(const vpto_world* w, const vpto_camera* cam, const vpto_p
                 const v3 sn = normal_from_id(sface, 1.0f);
                 const float nw = dm_pow(fmaxg(dot(bn, sn), 0.00000000001f), 32.0f);
                 float lw = 1.0f;
-                const float srough = pbr_rough(w, sblock);
+                const float srough = gbt ? (s == 0 ? pbr_x : gbt_pbr(sc, 0)) : pbr_rough(w, sblock);
                 const bool too_rough = srough >= 0.89f;
                 if (!too_rough) {
                     const float luma = dot(mk3(sd[0], sd[1], sd[2]), mk3(0.299f, 0.587f, 0.114f));
@@ -2483,8 +2536,9 @@ extern "C" void vpto_generate_gbuffer(const vpto_camera* cam, const vpto_params*
 namespace {
 struct OTexState {
     bool on = false, has_e = false;
-    OTexArray A, P, E;
-    std::vector<int> albedo_id, emissive_id;
+    OTexArray A, N, P, E;
+    std::vector<int> albedo_id, normal_id, pbr_id, emissive_id;
+    int grass[10];
     float srgb[256];
 };
 OTexState g_tex;
@@ -2494,7 +2548,11 @@ extern "C" void vpto_set_block_textures(const vpto_block_textures* tx) {
     g_tex = OTexState{};
     if (!tx) return;
     g_tex.A = build_tex_array(tx->albedo, tx->albedo_layers, 4, tx->size);
+    g_tex.N = build_tex_array(tx->normal, tx->normal_layers, 4, tx->size);
     g_tex.P = build_tex_array(tx->pbr, tx->pbr_layers, 4, tx->size);
+    g_tex.normal_id.assign(tx->normal_id, tx->normal_id + 128);
+    g_tex.pbr_id.assign(tx->pbr_id, tx->pbr_id + 128);
+    for (int k = 0; k < 10; k++) g_tex.grass[k] = tx->grass[k];
     g_tex.has_e = tx->emissive != nullptr;
     if (g_tex.has_e) g_tex.E = build_tex_array(tx->emissive, tx->emissive_layers, 1, tx->size);
     g_tex.albedo_id.assign(tx->albedo_id, tx->albedo_id + 128);
@@ -2531,3 +2589,50 @@ bool tex_bounce_material(int bid, v3 ip, v3 hn, v3* albedo, float* rough, float*
     return true;
 }
 }  // namespace
+
+bool tex_reflection_hit(int rid, v3 hp, v3 hn, TexHit* out) {
+    if (!g_tex.on) return false;
+    const int f = normal_id(hn);
+    int ia = g_tex.albedo_id[rid], in_ = g_tex.normal_id[rid], ip = g_tex.pbr_id[rid];
+    const int ie = g_tex.has_e ? g_tex.emissive_id[rid] : -1;
+    if (rid == g_tex.grass[0]) {
+        const int k = f == 2 ? 1 : (f == 3 ? 7 : 4);
+        ia = g_tex.grass[k];
+        in_ = g_tex.grass[k + 1];
+        ip = g_tex.grass[k + 2];
+    }
+    const v2 fuv = face_uv(hp, hn);
+    auto level = [&](const OTexArray& a, int id, int lv, int nch, const float* srgb, float* o) {
+        const int l = std::min(std::max(id, 0), a.layers - 1);
+        tex_bilinear(a, std::min(lv, a.levels - 1), l, fuv.x, fuv.y, nch, srgb, o);
+    };
+    float al[4], pb[4], nm[4];
+    level(g_tex.A, ia, 0, 3, g_tex.srgb, al);
+    level(g_tex.P, ip, 0, 4, nullptr, pb);
+    level(g_tex.N, in_, 3, 3, nullptr, nm);
+    out->albedo = mk3(al[0], al[1], al[2]);
+    out->rough = pb[0];
+    out->metal = pb[1];
+    out->ao = dm_pow(pb[3], 2.0f);
+    for (int c = 0; c < 3; c++) nm[c] = nm[c] * 2.0f - 1.0f;
+    const v3 T = f < 4 ? mk3(1.0f, 0.0f, 0.0f) : mk3(0.0f, 0.0f, -1.0f);
+    const v3 B = f < 2 ? mk3(0.0f, 1.0f, 0.0f) : (f < 4 ? mk3(0.0f, 0.0f, 1.0f) : mk3(0.0f, -1.0f, 0.0f));
+    out->nmap = mk3((T.x * nm[0] + B.x * nm[1]) + hn.x * nm[2], (T.y * nm[0] + B.y * nm[1]) + hn.y * nm[2],
+                    (T.z * nm[0] + B.z * nm[1]) + hn.z * nm[2]);
+    out->emis = -1.0f;
+    if (ie > -1) {
+        float e[4];
+        level(g_tex.E, ie, 2, 1, nullptr, e);
+        out->emis = e[0];
+    }
+    return true;
+}
+
+extern "C" void vpto_set_textured_gbuffer(const float* normal, const float* pbr, int W, int H) {
+    g_gbt = GbtState{};
+    if (!normal || !pbr) return;
+    g_gbt.normal = normal;
+    g_gbt.pbr = pbr;
+    g_gbt.W = W;
+    g_gbt.H = H;
+}

@@ -255,6 +255,11 @@ typedef struct vpto_block_textures {
  * ground truth); NULL returns to the block table's flat materials. */
 void vpto_set_block_textures(const vpto_block_textures* tx);
 
+/* The textured G-buffer (normal 3 ch, PBR 4 ch, W*H) the reflection passes
+ * read instead of the block table and the face normals; NULLs turn it off.
+ * The pointers must stay valid while the passes run. */
+void vpto_set_textured_gbuffer(const float* normal, const float* pbr, int W, int H);
+
 /* GenerateGBuffer.glsl main (parallax off, no lava): albedo (3), normal (3),
  * PBR (4) and texture AO (1) per pixel of the W x H G-buffer. */
 void vpto_generate_gbuffer(const vpto_camera* cam, const vpto_params* p, const vpto_block_textures* tx,

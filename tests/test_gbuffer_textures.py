@@ -250,3 +250,25 @@ def test_textured_shade_needs_this_frames_gbuffer(vpt, oracle, gpu):
             ctx.shade(frame)
         ctx.generate_gbuffer()
         ctx.shade(frame)
+
+
+def test_oracle_textured_reflections_read_the_textures(vpt, oracle):
+    """With block textures the reflection pass reads the textured G-buffer
+    and samples the textures at its hits: brighter albedo texels, brighter
+    reflections; sky texels reflect nothing either way."""
+    vox, blocks, world, cams = scene(vpt, oracle)
+    cfg = vpt.default_config(width=W, height=H, primary_max_steps=256, reflection_spp=2, reflection_temporal=0)
+    frame = vpt.default_frame(frame_index=0, seed=9)
+    prev_g, hist = oracle.empty_history(H, W)
+    dark, bright = constant_textures(vpt), constant_textures(vpt)
+    for t in (dark, bright):
+        t["emissive_id"][:] = -1
+        t["pbr"][..., 0] = 40          # smooth enough to reflect
+    dark["albedo"][..., :3] = 60
+    bright["albedo"][..., :3] = 200
+    fd = oracle.render_frame(world, cams[0], cams[0], cfg, frame, prev_g, hist, textures=dark)
+    fb = oracle.render_frame(world, cams[0], cams[0], cfg, frame, prev_g, hist, textures=bright)
+    sky = fd["g"]["t"] < 0
+    hits = (fd["refl"]["hit"] > 0) & ~sky
+    assert hits.any() and (fd["refl"]["spec"][sky] == 0).all()
+    assert fb["refl"]["spec"][hits][:, :3].mean() > 1.2 * fd["refl"]["spec"][hits][:, :3].mean()

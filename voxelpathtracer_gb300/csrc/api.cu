@@ -1103,6 +1103,16 @@ vpt_status reflection_run(vpt_ctx* c, const vpt_frame* f) {
     a.mixed[0] = mixed.x;
     a.mixed[1] = mixed.y;
     a.mixed[2] = mixed.z;
+    // with block textures the passes read the textured G-buffer of this frame
+    const bool tex = c->textured;
+    if (tex) {
+        if (!c->gbt_valid)
+            return fail(c, VPT_ERR_STATE, "block textures are set: run vpt_generate_gbuffer after the primary trace");
+        a.gb_normal = c->gbt[1];
+        a.gb_pbr = c->gbt[2];
+        a.textured = 1;
+        a.tex = tex_view(c);
+    }
     const void *sh, *cocg, *ao;
     denoised_gi(c, &sh, &cocg, &ao);
     const int cur = c->cur, prv = 1 - c->cur;
@@ -1119,6 +1129,7 @@ vpt_status reflection_run(vpt_ctx* c, const vpt_frame* f) {
         ta.prev_pos[k] = pc.position[k];
     }
     ta.temporal = c->cfg.reflection_temporal ? 1 : 0;
+    if (tex) ta.gb_pbr = c->gbt[2];
     pass_begin(c, VPT_PASS_REFLECTION);
     CK(c, trace_reflection(world_view(c), cam_view(cm), c->cfg.width, c->cfg.height, c->gw, c->gh, c->fp16, a,
                            c->gbuf[cur][GB_T], (const uint8_t*)c->gbuf[cur][GB_FACE], c->shadow, c->view[0],
@@ -1139,6 +1150,10 @@ vpt_status reflection_run(vpt_ctx* c, const vpt_frame* f) {
         // ReflectionDenoiserNew, x then y (:3312-3440); the hit distance is the
         // stabilised one with the temporal filter on, else the blurred trace's
         SpecDenoiseArgs da;
+        if (tex) {
+            da.gb_normal = c->gbt[1];
+            da.gb_pbr = c->gbt[2];
+        }
         memcpy(da.view, cm.view, sizeof da.view);
         da.res_scale = 1.0f / (float)c->gd;
         da.temporal_weight = ta.temporal;

@@ -272,6 +272,13 @@ struct ReflectionArgs {
     float light_dir[3];         // u_StrongerLightDirection
     float mixed[3];             // SAMPLED_COLOR_MIXED: sun / moon radiance by sun visibility
     float viewer[3];            // u_ViewerPosition
+    // with block textures: the textured G-buffer's normal-mapped normal (3 ch)
+    // and PBR (4 ch) at W x H for the base pixel, and the arrays for the hits;
+    // NULL / 0: the block table and the face normals
+    const void* gb_normal = nullptr;
+    const void* gb_pbr = nullptr;
+    int textured = 0;
+    BlockTexView tex{};
 };
 // W x H: the G-buffer (t, face, shadow); Wg x Hg: the GI grid (views, denoised
 // GI, outputs spec 4 ch, hit, mask).
@@ -286,12 +293,15 @@ struct SpecTemporalArgs {
     float prev_view_proj[16];   // u_PrevProjection * u_PrevView
     float cur_pos[3], prev_pos[3];
     int temporal;               // TEMPORAL_SPEC
+    const void* gb_pbr = nullptr;   // textured G-buffer PBR (4 ch, W x H), or NULL: the block table
 };
 struct SpecDenoiseArgs {
     float view[16];             // u_View
     float res_scale;            // u_ResolutionScale (ReflectionSuperSampleResolution) = 1 / gi_divisor
     int dir;                    // u_Dir: 1 = x, 0 = y
     int temporal_weight;        // u_TemporalWeight && TEMPORAL_SPEC
+    const void* gb_normal = nullptr;   // textured G-buffer normal (3 ch) and PBR (4 ch) at W x H,
+    const void* gb_pbr = nullptr;      // or NULL: face normals and the block table
 };
 cudaError_t spec_denoise(const WorldView& w, const CamView& cam, const SpecDenoiseArgs& a, int W, int H, int Wg,
                          int Hg, int fp16, const void* t, const uint8_t* face, const uint8_t* block, const void* tv,

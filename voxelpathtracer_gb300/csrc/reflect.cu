@@ -101,6 +101,21 @@ __device__ __forceinline__ v3 reflection_directional_light(v3 viewer, v3 wp, v3 
 }
 
 // The face UV of CalculateVectors (:1388-1446), UV.y = 1 - UV.y (:848).
+// the textured G-buffer read as its GL samplers would: PBR nearest,
+// normal-mapped normal bilinear (REPEAT), on the W x H plane at uv
+template <typename S>
+__device__ __forceinline__ float gb_pbr_at(const S* p, int W, int H, v2 uv, int c) {
+    const int x = wrapi(f2i_floor(uv.x * (float)W), W), y = wrapi(f2i_floor(uv.y * (float)H), H);
+    return ld(p + ((size_t)y * W + x) * 4 + c);
+}
+template <typename S>
+__device__ __forceinline__ v3 gb_normal_at(const S* p, int W, int H, v2 uv) {
+    const Plane<S, 3> P{p, W, H};
+    float n[3];
+    P.linear(uv, n);
+    return mk3(n[0], n[1], n[2]);
+}
+
 __device__ __forceinline__ v2 face_uv(v3 p, v3 n) {
     v2 uv;
     if (n.z != 0.0f) uv = mk2(fract(p.x), fract(p.y));
@@ -141,8 +156,16 @@ __global__ void __launch_bounds__(256, 8) k_trace_reflection(WorldView w, CamVie
             const v3 N = normal_from_id(__ldg(fv + q), 1.0f);
             // NormalMappedInitial (:794): the linear normal G-buffer at the
             // texel centre, the face normal itself on the G-buffer's grid
-            const v3 NM = (W == Wg && H == Hg) ? N : gnormal_linear(face, W, H, uv);
+            v3 NM = (W == Wg && H == Hg) ? N : gnormal_linear(face, W, H, uv);
             const Material base = material(w, min(max((int)__ldg(bv + q), 0), 127));
+            float base_rough = base.rough, base_metal = base.metal;
+            if (a.gb_normal) {   // the textured G-buffer (u_GBufferPBR, u_GBufferNormals, :777-789)
+                const S* gn = (const S*)a.gb_normal;
+                base_rough = gb_pbr_at((const S*)a.gb_pbr, W, H, uv, 0);
+                base_metal = gb_pbr_at((const S*)a.gb_pbr, W, H, uv, 1);
+                NM = (W == Wg && H == Hg) ? mk3(ld(gn + q * 3), ld(gn + q * 3 + 1), ld(gn + q * 3 + 2))
+                                          : gb_normal_at(gn, W, H, uv);
+            }
             const v3 I = normalize(sub(mk3(P.x, P.y, P.z), viewer));
             P.x += N.x * 0.035f;
             P.y += N.y * 0.035f;
@@ -161,7 +184,7 @@ __global__ void __launch_bounds__(256, 8) k_trace_reflection(WorldView w, CamVie
             int shadow_itr = 0, total_hits = 0;
 #pragma unroll 1
             for (int s = 0; s < spp; s++) {
-                const v3 rn = reflection_normal(NM, clampf(base.rough * rbias, 0.01f, 1.0f), &rng);
+                const v3 rn = reflection_normal(NM, clampf(base_rough * rbias, 0.01f, 1.0f), &rng);
                 const v3 R = reflect3(I, rn);
                 const TraceResult tr = traverse<0>(w, pos, R, a.max_steps);
                 nr += 1;
@@ -189,8 +212,45 @@ __global__ void __launch_bounds__(256, 8) k_trace_reflection(WorldView w, CamVie
                         if (pa.w > 0.0f && length(sub(mk3(pa.x, pa.y, pa.z), cam_pos)) < 40.0f)
                             ambient = muls(ambient, vxao);
                     }
-                    const Material m = material(w, rid);
-                    const float ao = dpow(1.0f, 2.0f);
+                    Material m = material(w, rid);
+                    float ao = dpow(1.0f, 2.0f);
+                    v3 nmap = hn;
+                    float emis_tex = -1.0f;   // the emissive texel, -1: none
+                    if (a.textured) {
+                        // the hit's textures (:887-960): ids with the grass override,
+                        // albedo and PBR by texture() (taken at level 0), the normal
+                        // map at level 3 through the face's tangent basis, the
+                        // emissive texture at level 2
+                        const BlockTexView& tx = a.tex;
+                        const int f = normal_id(hn);
+                        int ia = __ldg(tx.ids + rid), in_ = __ldg(tx.ids + 128 + rid), ip = __ldg(tx.ids + 256 + rid);
+                        const int ie = tx.emissive.texels ? __ldg(tx.ids + 384 + rid) : -1;
+                        if (rid == tx.grass[0]) {
+                            const int k = f == 2 ? 1 : (f == 3 ? 7 : 4);
+                            ia = tx.grass[k];
+                            in_ = tx.grass[k + 1];
+                            ip = tx.grass[k + 2];
+                        }
+                        const v2 fuv = face_uv(hp, hn);
+                        float alb[4], pb[4], nm[4];
+                        sample_level(tx.albedo, ia, fuv.x, fuv.y, 0, 3, tx.srgb, alb);
+                        sample_level(tx.pbr, ip, fuv.x, fuv.y, 0, 4, tx.unorm, pb);
+                        sample_level(tx.normal, in_, fuv.x, fuv.y, 3, 3, tx.unorm, nm);
+                        m.albedo = mk3(alb[0], alb[1], alb[2]);
+                        m.rough = pb[0];
+                        m.metal = pb[1];
+                        ao = dpow(pb[3], 2.0f);
+                        for (int c = 0; c < 3; c++) nm[c] = nm[c] * 2.0f - 1.0f;
+                        const v3 Tt = f < 4 ? mk3(1.0f, 0.0f, 0.0f) : mk3(0.0f, 0.0f, -1.0f);
+                        const v3 Bt = f < 2 ? mk3(0.0f, 1.0f, 0.0f) : (f < 4 ? mk3(0.0f, 0.0f, 1.0f) : mk3(0.0f, -1.0f, 0.0f));
+                        nmap = mk3((Tt.x * nm[0] + Bt.x * nm[1]) + hn.x * nm[2], (Tt.y * nm[0] + Bt.y * nm[1]) + hn.y * nm[2],
+                                   (Tt.z * nm[0] + Bt.z * nm[1]) + hn.z * nm[2]);
+                        if (ie > -1) {
+                            float e[4];
+                            sample_level(tx.emissive, ie, fuv.x, fuv.y, 2, 1, tx.unorm, e);
+                            emis_tex = e[0];
+                        }
+                    }
                     if (shadow_itr < max(spp / 4, 1)) {
                         if (success && in_ss) {
                             computed_shadow = bl_u8(shadow, bilin(rc, W, H));
@@ -205,9 +265,9 @@ __global__ void __launch_bounds__(256, 8) k_trace_reflection(WorldView w, CamVie
                     }
                     ambient = mul(muls(muls(ambient, 1.0f), clampf(ao, 0.1f, 1.0f)), m.albedo);
                     v3 direct = add(ambient, reflection_directional_light(viewer, hp, light_dir, radiance, m.albedo,
-                                                                          hn, m.rough, m.metal, computed_shadow));
-                    if (m.emissive) {
-                        float emissivity = 1.0f;
+                                                                          nmap, m.rough, m.metal, computed_shadow));
+                    if (a.textured ? emis_tex > 0.1f : m.emissive != 0) {
+                        float emissivity = a.textured ? emis_tex : 1.0f;
                         const v2 fuv = face_uv(hp, hn);
                         const float bx = 0.02501f, by = 0.03001f;
                         emissivity *= (fuv.x > bx && fuv.x < 1.0f - bx && fuv.y > by && fuv.y < 1.0f - by) ? 1.0f
@@ -219,7 +279,7 @@ __global__ void __launch_bounds__(256, 8) k_trace_reflection(WorldView w, CamVie
                     avg_hit += Tt;
                     meaningful += 1.0f;
                 } else {
-                    computed = muls(sky_radiance(normalize(R)), mixf(1.0f, 1.175f, base.metal > 0.05f ? 1.0f : 0.0f));
+                    computed = muls(sky_radiance(normalize(R)), mixf(1.0f, 1.175f, base_metal > 0.05f ? 1.0f : 0.0f));
                 }
                 total[0] += computed.x;
                 total[1] += computed.y;
@@ -334,7 +394,8 @@ __global__ void __launch_bounds__(256, 6) k_spec_temporal(WorldView w, CamView c
     if (P.w > 0.0f && a.temporal) {
         const bool sky = hc < 0.0f;
         const Material mt = material(w, min(max((int)__ldg(bv + q), 0), 127));
-        const float rough = mixf(0.095f, mt.rough, 1.0f), metal = mt.metal;
+        const float pr = a.gb_pbr ? gb_pbr_at((const S*)a.gb_pbr, W, H, uv, 0) : mt.rough;
+        const float rough = mixf(0.095f, pr, 1.0f), metal = a.gb_pbr ? gb_pbr_at((const S*)a.gb_pbr, W, H, uv, 1) : mt.metal;
         const v3 cur_pos = mk3(a.cur_pos[0], a.cur_pos[1], a.cur_pos[2]);
         const v3 prev_pos = mk3(a.prev_pos[0], a.prev_pos[1], a.prev_pos[2]);
         const v3 ro = ray_origin(cam);
@@ -486,12 +547,17 @@ __global__ void __launch_bounds__(256, 6) k_spec_denoise(WorldView w, CamView ca
     const float4 bc = ld4(in + 4 * q);
     const float base_lum = dot(mk3(bc.x, bc.y, bc.z), mk3(0.299f, 0.587f, 0.114f));
     const int bblock = __ldg(bv + q);
-    const float pbr_x = pbr_rough(w, bblock), pbr_y = pbr_metal(w, bblock);
+    const S* gbp = (const S*)a.gb_pbr;
+    const S* gbn = (const S*)a.gb_normal;
+    const float pbr_x = gbp ? gb_pbr_at(gbp, W, H, uv, 0) : pbr_rough(w, bblock);
+    const float pbr_y = gbp ? gb_pbr_at(gbp, W, H, uv, 1) : pbr_metal(w, bblock);
     float br = pbr_x + 0.001f;
     const float raw_rough = br;
     br *= mixf(1.0f, 0.91f, 1.0f);
     const bool same_grid = W == Wg && H == Hg;
-    const v3 nm_base = same_grid ? bn : gnormal_linear(face, W, H, uv);
+    const v3 nm_base = gbn ? (same_grid ? mk3(ld(gbn + q * 3), ld(gbn + q * 3 + 1), ld(gbn + q * 3 + 2))
+                                        : gb_normal_at(gbn, W, H, uv))
+                           : (same_grid ? bn : gnormal_linear(face, W, H, uv));
     float hd = ld(hit_data + q) + 0.0001f;
     if (hd < 0.001f) hd = 1.75f;
     else hd = dpow(hd, 1.0f / 1.3f);
@@ -572,7 +638,7 @@ __global__ void __launch_bounds__(256, 6) k_spec_denoise(WorldView w, CamView ca
             sface = F.nearest(sc);
             sblock = B.nearest(sc);
             sd = bl4(in, bilin(sc, Wg, Hg));
-            nm_at = gnormal_linear(face, W, H, sc);
+            nm_at = gbn ? gb_normal_at(gbn, W, H, sc) : gnormal_linear(face, W, H, sc);
         }
         const bool sample_sky = sdepth < 0.0f;
         if (sample_sky != base_sky) continue;
@@ -582,7 +648,7 @@ __global__ void __launch_bounds__(256, 6) k_spec_denoise(WorldView w, CamView ca
         const int ncls = face_cos(bf, sface);
         const float nw = ncls == 0 ? nw0 : (ncls == 1 ? dpow(1.0f, 32.0f) : nw3);
         float lw = 1.0f;
-        const float srough = pbr_rough(w, sblock);
+        const float srough = gbp ? (s == 0 ? pbr_x : gb_pbr_at(gbp, W, H, sc, 0)) : pbr_rough(w, sblock);
         const bool too_rough = srough >= 0.89f;
         if (!too_rough) {
             const float luma = dot(mk3(sd.x, sd.y, sd.z), mk3(0.299f, 0.587f, 0.114f));
