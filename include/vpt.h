@@ -74,7 +74,10 @@ typedef struct vpt_config {
                                         SpecularTemporalFilter's reprojection and accumulation */
     int32_t reflection_denoise;      /* DenoiseReflections (:105): 1 (default) runs the two separable
                                         passes of ReflectionDenoiserNew.glsl before the colour pass */
-    int32_t reserved[3];
+    int32_t alpha_test;              /* u_ShouldAlphaTest (Core/Pipeline.cpp:141, off by default): with block
+                                        textures the primary trace passes through texels of transparent
+                                        blocks whose albedo alpha is at most 0.975 */
+    int32_t reserved[2];
 } vpt_config;
 
 typedef enum vpt_denoiser {
@@ -239,6 +242,7 @@ typedef struct vpt_block_textures {
     int32_t emissive_id[128];        /* BlockEmissiveData; -1 = none */
     int32_t grass[10];               /* grass block id, then albedo / normal / PBR layers of
                                         its top (1-3), sides (4-6) and bottom (7-9); id -1 = none */
+    int32_t transparent[128];        /* BlockTransparentData: 1 for blocks the alpha test looks through */
 } vpt_block_textures;
 /* Uploads the arrays and builds their mip chains; NULL removes them (flat
  * materials from the block table). Allocates the G-buffer texture planes. */

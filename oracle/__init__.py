@@ -43,7 +43,7 @@ class OParams(C.Structure):
                 ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
                 ("gi_divisor", C.c_int32), ("reflection_spp", C.c_int32), ("reflection_max_steps", C.c_int32),
                 ("reflection_shadow_max_steps", C.c_int32), ("reflection_temporal", C.c_int32),
-                ("reflection_denoise", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("reflection_denoise", C.c_int32), ("alpha_test", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 class OWorld(C.Structure):
@@ -193,14 +193,21 @@ def _planes(H, W, spec):
     return {k: np.zeros((H, W, c) if c > 1 else (H, W), dtype=dt) for k, (c, dt) in spec.items()}
 
 
-def trace_primary(world: World, cam, config, rows=None) -> dict:
+def trace_primary(world: World, cam, config, rows=None, textures=None) -> dict:
+    """The primary G-buffer; with config.alpha_test and block textures, the
+    alpha-tested traversal."""
     p = params(config)
     H, W = p.height, p.width
     g = _planes(H, W, {"t": (1, np.float32), "face": (1, np.uint8), "block": (1, np.uint8),
                        "hit": (3, np.int32), "steps": (1, np.uint16)})
     r0, r1 = rows if rows else (0, H)
     gb = OGBuffer(_p(g["t"]), _p(g["face"]), _p(g["block"]), _p(g["hit"]), _p(g["steps"]))
-    lib().vpto_trace_primary(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), r0, r1, C.byref(gb))
+    keep = _set_textures(textures)
+    try:
+        lib().vpto_trace_primary(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), r0, r1, C.byref(gb))
+    finally:
+        lib().vpto_set_block_textures(None)
+    del keep
     return g
 
 
@@ -311,7 +318,7 @@ class OBlockTextures(C.Structure):   # vpto_block_textures
                 ("normal", C.c_void_p), ("normal_layers", C.c_int32), ("pbr", C.c_void_p),
                 ("pbr_layers", C.c_int32), ("emissive", C.c_void_p), ("emissive_layers", C.c_int32),
                 ("albedo_id", C.c_int32 * 128), ("normal_id", C.c_int32 * 128), ("pbr_id", C.c_int32 * 128),
-                ("emissive_id", C.c_int32 * 128), ("grass", C.c_int32 * 10)]
+                ("emissive_id", C.c_int32 * 128), ("grass", C.c_int32 * 10), ("transparent", C.c_int32 * 128)]
 
 
 def _block_textures(textures: dict):
@@ -327,6 +334,8 @@ def _block_textures(textures: dict):
     for k in ("albedo_id", "normal_id", "pbr_id", "emissive_id"):
         getattr(bt, k)[:] = [int(v) for v in np.asarray(textures[k], np.int64)[:128]]
     bt.grass[:] = [int(v) for v in np.asarray(textures["grass"], np.int64)[:10]]
+    if textures.get("transparent") is not None:
+        bt.transparent[:] = [int(v) for v in np.asarray(textures["transparent"], np.int64)[:128]]
     return bt, keep
 
 
@@ -517,7 +526,7 @@ def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist:
     """One whole frame in the order of vpt_render_frame; prev_refl is last
     frame's "refl" (zero planes when None)."""
     p = params(config)
-    g = trace_primary(world, cam, p)
+    g = trace_primary(world, cam, p, textures=textures)
     shadow = trace_shadow(world, cam, p, frame, g["t"], g["face"])
     v = gi_view(p, g["t"], g["face"], g["block"])
     gi = trace_diffuse(world, cam, p, frame, v["t"], v["face"], textures=textures)

@@ -149,6 +149,100 @@ TraceResult traverse(const vpto_world* w, v3 origin, v3 direction, int max_steps
     return r;
 }
 
+int normal_id(v3 n);
+bool alpha_active(const vpto_params* p);
+
+// K of StopRay (InitialRayTraceFrag.glsl:421): 1 / (2 tan(fov / (2 W))),
+// the vertical fov 2 atan(1 / proj[1][1]), in double precision.
+inline float alpha_k(float proj11, int width) {
+    const double fov = 2.0 * std::atan(1.0 / (double)proj11);
+    return (float)(1.0 / (std::tan(fov / (2.0 * (double)width)) * 2.0));
+}
+
+// StopRay (InitialRayTraceFrag.glsl:189-202) with the block textures set by
+// vpto_set_block_textures (true for every block without them).
+bool alpha_stop(v3 p, v3 n, int type, v3 cam, float k);
+
+// VoxelTraversalDF_AlphaTest (InitialRayTraceFrag.glsl:204-305): at a solid
+// voxel (E == 0) StopRay decides; if the ray goes on, up to four exact face
+// steps look for a voxel that stops it, then the loop continues from one
+// direction length back (origin += (E - 1) * direction).
+TraceResult traverse_alpha(const vpto_world* w, v3 origin, v3 direction, int max_steps, v3 cam, float k) {
+    const v3 initial = origin;
+    bool intersection = false;
+    int min_idx = 0;
+    const int sgn[3] = {isign(direction.x), isign(direction.y), isign(direction.z)};
+    const int half[3] = {(1 + sgn[0]) >> 1, (1 + sgn[1]) >> 1, (1 + sgn[2]) >> 1};
+    const v3 inv = mk3(1.0f / direction.x, 1.0f / direction.y, 1.0f / direction.z);
+    auto face_step = [&]() {
+        int g[3] = {f2i(origin.x), f2i(origin.y), f2i(origin.z)};
+        v3 wv = mk3(origin.x - (float)g[0], origin.y - (float)g[1], origin.z - (float)g[2]);
+        v3 df = mk3(((float)half[0] - wv.x) * inv.x, ((float)half[1] - wv.y) * inv.y, ((float)half[2] - wv.z) * inv.z);
+        min_idx = (df.x < df.y && sgn[0] != 0) ? ((df.x < df.z || sgn[2] == 0) ? 0 : 2)
+                                               : ((df.y < df.z || sgn[2] == 0) ? 1 : 2);
+        g[min_idx] += sgn[min_idx];
+        float dm = comp(df, min_idx);
+        wv = mk3(wv.x + direction.x * dm, wv.y + direction.y * dm, wv.z + direction.z * dm);
+        set_comp(&wv, min_idx, (float)(1 - half[min_idx]));
+        origin = mk3((float)g[0] + wv.x, (float)g[1] + wv.y, (float)g[2] + wv.z);
+        set_comp(&origin, min_idx, comp(origin, min_idx) + (float)sgn[min_idx] * 0.0001f);
+    };
+    auto step_normal = [&]() {
+        v3 n = mk3(0.0f, 0.0f, 0.0f);
+        set_comp(&n, min_idx, (float)(-sgn[min_idx]));
+        return n;
+    };
+    int itr = 0;
+    for (itr = 0; itr < max_steps; itr++) {
+        int lx = f2i(std::floor(origin.x)), ly = f2i(std::floor(origin.y)), lz = f2i(std::floor(origin.z));
+        if (!in_volume(w, lx, ly, lz)) {
+            intersection = false;
+            break;
+        }
+        int e = euclid_steps((int)w->df[vidx(w, lx, ly, lz)]);
+        if (e == 0) {
+            if (alpha_stop(origin, step_normal(), get_voxel(w, lx, ly, lz), cam, k)) break;
+            for (int s = 0; s < 4; s++) {
+                face_step();
+                const int cx = f2i(std::floor(origin.x)), cy = f2i(std::floor(origin.y)), cz = f2i(std::floor(origin.z));
+                const int bt = get_voxel(w, cx, cy, cz);
+                if (bt > 0 && alpha_stop(origin, step_normal(), bt, cam, k)) {
+                    TraceResult r;
+                    r.cell[0] = cx;
+                    r.cell[1] = cy;
+                    r.cell[2] = cz;
+                    r.steps = itr;
+                    r.normal = step_normal();
+                    r.block = bt;
+                    r.t = length(sub(origin, initial));
+                    return r;
+                }
+            }
+        }
+        if (e == 1) {
+            face_step();
+            intersection = true;
+        } else {
+            float kk = (float)(e - 1);
+            origin = mk3(origin.x + kk * direction.x, origin.y + kk * direction.y, origin.z + kk * direction.z);
+        }
+    }
+    TraceResult r;
+    r.cell[0] = f2i(std::floor(origin.x));
+    r.cell[1] = f2i(std::floor(origin.y));
+    r.cell[2] = f2i(std::floor(origin.z));
+    r.steps = itr;
+    r.normal = mk3(0.0f, 0.0f, 0.0f);
+    r.block = 0;
+    r.t = -1.0f;
+    if (intersection) {
+        set_comp(&r.normal, min_idx, (float)(-sgn[min_idx]));
+        r.block = get_voxel(w, r.cell[0], r.cell[1], r.cell[2]);
+        r.t = r.block > 0 ? length(sub(origin, initial)) : -1.0f;
+    }
+    return r;
+}
+
 // GetNormalID (InitialRayTraceFrag.glsl:143-185): exact compares, 0 when none match.
 int normal_id(v3 n) {
     static const v3 N[6] = {{0, 0, 1}, {0, 0, -1}, {0, 1, 0}, {0, -1, 0}, {-1, 0, 0}, {1, 0, 0}};
@@ -602,7 +696,8 @@ void vpto_trace_primary(const vpto_world* w, const vpto_camera* cam, const vpto_
         for (int i = 0; i < W; i++) {
             size_t px = (size_t)j * W + i;
             v3 dir = normalize(ray_dir_at(cam, texcoord(i, j, W, H)));
-            TraceResult r = traverse(w, r0, dir, p->primary_max_steps);
+            TraceResult r = alpha_active(p) ? traverse_alpha(w, r0, dir, p->primary_max_steps, r0, alpha_k(cam->proj[5], W))
+                                           : traverse(w, r0, dir, p->primary_max_steps);
             cnt.add(0, r.steps);
             bool intersect = r.t > 0.0f && r.block > 0;
             out->t[px] = storage(r.t, p->storage);
@@ -2539,6 +2634,7 @@ struct OTexState {
     OTexArray A, N, P, E;
     std::vector<int> albedo_id, normal_id, pbr_id, emissive_id;
     int grass[10];
+    int transparent[128];
     float srgb[256];
 };
 OTexState g_tex;
@@ -2553,6 +2649,7 @@ extern "C" void vpto_set_block_textures(const vpto_block_textures* tx) {
     g_tex.normal_id.assign(tx->normal_id, tx->normal_id + 128);
     g_tex.pbr_id.assign(tx->pbr_id, tx->pbr_id + 128);
     for (int k = 0; k < 10; k++) g_tex.grass[k] = tx->grass[k];
+    for (int b = 0; b < 128; b++) g_tex.transparent[b] = tx->transparent[b] ? 1 : 0;
     g_tex.has_e = tx->emissive != nullptr;
     if (g_tex.has_e) g_tex.E = build_tex_array(tx->emissive, tx->emissive_layers, 1, tx->size);
     g_tex.albedo_id.assign(tx->albedo_id, tx->albedo_id + 128);
@@ -2636,3 +2733,21 @@ extern "C" void vpto_set_textured_gbuffer(const float* normal, const float* pbr,
     g_gbt.W = W;
     g_gbt.H = H;
 }
+
+namespace {
+bool alpha_active(const vpto_params* p) { return p->alpha_test != 0 && g_tex.on; }
+
+bool alpha_stop(v3 p, v3 n, int type, v3 cam, float k) {
+    const int id = std::min(std::max(type, 0), 127);
+    if (!g_tex.on || !g_tex.transparent[id]) return true;
+    const v2 fc = face_coords(p, normal_id(n));
+    const float u = 1.0f - fract(fc.x), v = 1.0f - fract(fc.y);
+    const float D = length(sub(p, cam));
+    const int lod = std::min(std::max(f2i(dm_log2((float)g_tex.A.size / ((1.0f / D) * k))), 0), 8);
+    const OTexArray& a = g_tex.A;
+    const int layer = std::min(std::max(g_tex.albedo_id[id], 0), a.layers - 1);
+    float o[4];
+    tex_bilinear(a, std::min(lod, a.levels - 1), layer, u, v, 4, nullptr, o);
+    return o[3] > 0.975f;
+}
+}  // namespace

@@ -71,7 +71,8 @@ typedef struct vpto_params {
     int32_t reflection_shadow_max_steps;
     int32_t reflection_temporal;  /* TEMPORAL_SPEC */
     int32_t reflection_denoise;   /* DenoiseReflections */
-    int32_t reserved[3];
+    int32_t alpha_test;           /* u_ShouldAlphaTest */
+    int32_t reserved[2];
 } vpto_params;
 
 typedef struct vpto_world {
@@ -249,6 +250,7 @@ typedef struct vpto_block_textures {
     int32_t pbr_id[128];
     int32_t emissive_id[128];
     int32_t grass[10];
+    int32_t transparent[128];
 } vpto_block_textures;
 
 /* Block textures for the diffuse bounce hits of vpto_trace_diffuse (and the

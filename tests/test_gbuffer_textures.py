@@ -272,3 +272,48 @@ def test_oracle_textured_reflections_read_the_textures(vpt, oracle):
     hits = (fd["refl"]["hit"] > 0) & ~sky
     assert hits.any() and (fd["refl"]["spec"][sky] == 0).all()
     assert fb["refl"]["spec"][hits][:, :3].mean() > 1.2 * fd["refl"]["spec"][hits][:, :3].mean()
+
+
+# ------------------------------------------------ alpha-tested traversal --
+def test_oracle_alpha_test(vpt, oracle):
+    """u_ShouldAlphaTest: with every block transparent to it, rays pass the
+    cut-out texels and end farther; with none transparent, or without the
+    flag, the G-buffer is the plain traversal's."""
+    vox, blocks, world, cams = scene(vpt, oracle)
+    tex = vpt.generate_block_textures(16, 6, seed=1)
+    plain = oracle.trace_primary(world, cams[0], vpt.default_config(width=W, height=H, primary_max_steps=256))
+    cfg = vpt.default_config(width=W, height=H, primary_max_steps=256, alpha_test=1)
+    tex["transparent"][:] = 0
+    opaque = oracle.trace_primary(world, cams[0], cfg, textures=tex)
+    for k in ("t", "face", "block", "hit", "steps"):
+        assert np.array_equal(opaque[k], plain[k]), k
+    tex["transparent"][:] = 1
+    cut = oracle.trace_primary(world, cams[0], cfg, textures=tex)
+    hit = plain["t"] > 0
+    assert (cut["t"][hit] > plain["t"][hit] + 0.5).mean() > 0.2
+    assert (cut["t"][~hit] == plain["t"][~hit]).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage,frac", [(0, 1.0), (1, 0.5), (0, 0.0)], ids=["f32-all", "f16-half", "f32-none"])
+def test_alpha_tested_gbuffer_bit_exact(vpt, oracle, storage, frac, gpu):
+    vox, blocks, world, cams = scene(vpt, oracle, seed=2)
+    tex = vpt.generate_block_textures(32, 5, seed=4)
+    tex["transparent"][:] = (np.random.default_rng(1).random(128) < frac).astype(np.int32)
+    with vpt.Context(width=W, height=H, primary_max_steps=256, storage=storage, alpha_test=1) as ctx:
+        ctx.upload_world(vox)
+        ctx.set_block_table(blocks)
+        ctx.build_df()
+        ctx.set_block_textures(tex)
+        cfg = ctx.config
+        for k, cam in enumerate(cams):
+            ctx.set_stats(True)
+            ctx.trace_primary(cam)
+            stats = ctx.read_stats()
+            with oracle.Counting() as cnt:
+                ref = oracle.trace_primary(world, cam, cfg, textures=tex)
+            for name, key in (("T", "t"), ("FACE", "face"), ("BLOCK", "block"), ("HIT", "hit"), ("STEPS", "steps")):
+                got = ctx.read_plane(name)
+                assert_same(got[..., 0] if got.ndim == 3 and key != "hit" else got, ref[key], f"cam {k} {name}")
+            assert stats["steps"]["primary"] == cnt.steps["primary"]
+            ctx.end_frame()

@@ -60,7 +60,7 @@ class Config(C.Structure):
                 ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
                 ("gi_divisor", C.c_int32), ("reflection_spp", C.c_int32), ("reflection_max_steps", C.c_int32),
                 ("reflection_shadow_max_steps", C.c_int32), ("reflection_temporal", C.c_int32),
-                ("reflection_denoise", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("reflection_denoise", C.c_int32), ("alpha_test", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 class Camera(C.Structure):
@@ -74,7 +74,7 @@ class BlockTextures(C.Structure):
                 ("normal", C.c_void_p), ("normal_layers", C.c_int32), ("pbr", C.c_void_p),
                 ("pbr_layers", C.c_int32), ("emissive", C.c_void_p), ("emissive_layers", C.c_int32),
                 ("albedo_id", C.c_int32 * 128), ("normal_id", C.c_int32 * 128), ("pbr_id", C.c_int32 * 128),
-                ("emissive_id", C.c_int32 * 128), ("grass", C.c_int32 * 10)]
+                ("emissive_id", C.c_int32 * 128), ("grass", C.c_int32 * 10), ("transparent", C.c_int32 * 128)]
 
 
 class Block(C.Structure):
@@ -357,8 +357,14 @@ def generate_block_textures(size: int = 32, layers: int = 12, n_blocks: int = 10
     if grass_block >= 0:
         grass[0] = grass_block
         grass[1:] = rng.integers(0, layers, size=9)
+    # cut-out alpha (about a third of the texels see-through) and one block in
+    # six transparent to the alpha test
+    for l in range(layers):
+        alb[l, ..., 3] = np.where(pattern(l) < 0.4, 0, 255).astype(np.uint8)
+    transparent = (rng.random(128) < 1 / 6).astype(np.int32)
     return {"size": size, "albedo": alb, "normal": nrm, "pbr": pbr, "emissive": emi, "albedo_id": ids[0],
-            "normal_id": ids[1], "pbr_id": ids[2], "emissive_id": ids[3], "grass": grass}
+            "normal_id": ids[1], "pbr_id": ids[2], "emissive_id": ids[3], "grass": grass,
+            "transparent": transparent}
 
 
 def block_textures_struct(t: dict):
@@ -375,6 +381,8 @@ def block_textures_struct(t: dict):
     for k in ("albedo_id", "normal_id", "pbr_id", "emissive_id"):
         getattr(bt, k)[:] = [int(v) for v in np.asarray(t[k], np.int64)[:128]]
     bt.grass[:] = [int(v) for v in np.asarray(t["grass"], np.int64)[:10]]
+    if t.get("transparent") is not None:
+        bt.transparent[:] = [int(v) for v in np.asarray(t["transparent"], np.int64)[:128]]
     return bt, keep
 
 

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "kernels.cuh"
+#include "textures.cuh"
 #include "vpt.h"
 
 using namespace vpt;
@@ -593,6 +594,13 @@ vpt_status vpt_set_block_table(vpt_ctx* c, const vpt_block* table, int32_t n) {
 }
 
 namespace {
+// K of StopRay (InitialRayTraceFrag.glsl:421): 1 / (2 tan(fov / (2 W))) with the
+// vertical fov 2 atan(1 / proj[1][1]), in double precision
+float alpha_k(float proj11, int width) {
+    const double fov = 2.0 * std::atan(1.0 / (double)proj11);
+    return (float)(1.0 / (std::tan(fov / (2.0 * (double)width)) * 2.0));
+}
+
 BlockTexView tex_view(const vpt_ctx* c) {
     BlockTexView tv;
     tv.albedo = c->tex_arr[0];
@@ -664,12 +672,13 @@ vpt_status vpt_set_block_textures(vpt_ctx* c, const vpt_block_textures* t) {
     }
     // layer ids [albedo | normal | PBR | emissive] and the sRGB decode of a byte
     // (IEC 61966-2-1: c / 12.92 up to 0.04045, else ((c + 0.055) / 1.055)^2.4)
-    std::vector<int> ids(512);
+    std::vector<int> ids(640);
     for (int b = 0; b < 128; b++) {
         ids[b] = t->albedo_id[b];
         ids[128 + b] = t->normal_id[b];
         ids[256 + b] = t->pbr_id[b];
         ids[384 + b] = t->emissive_id[b];
+        ids[512 + b] = t->transparent[b] ? 1 : 0;
     }
     std::vector<float> lut(512);
     for (int v = 0; v < 256; v++) {
@@ -775,9 +784,18 @@ vpt_status vpt_trace_primary(vpt_ctx* c, const vpt_camera* cam) {
     g.block = (uint8_t*)c->gbuf[c->cur][GB_BLOCK];
     g.hit = (int32_t*)c->gbuf[c->cur][GB_HIT];
     g.steps = (uint16_t*)c->gbuf[c->cur][GB_STEPS];
+    // the alpha-tested traversal with block textures (u_ShouldAlphaTest);
+    // K = 1 / (2 tan(fov / (2 W))), the vertical field of view from the projection
+    AlphaStop stop;
+    const bool alpha = c->cfg.alpha_test && c->textured;
+    if (alpha) {
+        stop.tv = tex_view(c);
+        stop.cam = mk3(cam->inv_view[12], cam->inv_view[13], cam->inv_view[14]);
+        stop.k = alpha_k(cam->proj[5], c->cfg.width);
+    }
     pass_begin(c, VPT_PASS_PRIMARY);
     CK(c, trace_primary(world_view(c), cam_view(*cam), c->cfg.width, c->cfg.height, c->cfg.primary_max_steps, c->fp16,
-                        g, c->stats ? c->counters : nullptr, c->stream));
+                        g, c->stats ? c->counters : nullptr, c->stream, alpha ? &stop : nullptr));
     pass_end(c, VPT_PASS_PRIMARY);
     c->launches += 1;
     return VPT_OK;

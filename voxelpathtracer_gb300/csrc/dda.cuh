@@ -50,6 +50,33 @@ __device__ __forceinline__ void ray_start(RayState& r, v3 origin, v3 dir, int ma
     r.inter = 0;
 }
 
+// One exact DDA face step (:341-356), the E == 1 branch's body; updates the
+// origin and MinIdx.
+__device__ __forceinline__ void dda_face_step(RayState& r) {
+    const int sx = isign(r.d.x), sy = isign(r.d.y), sz = isign(r.d.z);
+    const int hx = (1 + sx) >> 1, hy = (1 + sy) >> 1, hz = (1 + sz) >> 1;
+    int gx = f2i(r.o.x), gy = f2i(r.o.y), gz = f2i(r.o.z);
+    float wx = r.o.x - (float)gx, wy = r.o.y - (float)gy, wz = r.o.z - (float)gz;
+    const float dfx = ((float)hx - wx) * r.ix;
+    const float dfy = ((float)hy - wy) * r.iy;
+    const float dfz = ((float)hz - wz) * r.iz;
+    const int m = (dfx < dfy && sx != 0) ? ((dfx < dfz || sz == 0) ? 0 : 2) : ((dfy < dfz || sz == 0) ? 1 : 2);
+    const float dm = m == 0 ? dfx : (m == 1 ? dfy : dfz);
+    wx = wx + r.d.x * dm;
+    wy = wy + r.d.y * dm;
+    wz = wz + r.d.z * dm;
+    if (m == 0) { gx += sx; wx = (float)(1 - hx); }
+    else if (m == 1) { gy += sy; wy = (float)(1 - hy); }
+    else { gz += sz; wz = (float)(1 - hz); }
+    r.o.x = (float)gx + wx;
+    r.o.y = (float)gy + wy;
+    r.o.z = (float)gz + wz;
+    if (m == 0) r.o.x = r.o.x + (float)sx * 0.0001f;
+    else if (m == 1) r.o.y = r.o.y + (float)sy * 0.0001f;
+    else r.o.z = r.o.z + (float)sz * 0.0001f;
+    r.min_idx = m;
+}
+
 // One iteration of the traversal loop; returns true once the loop is over.
 // B is the distance-field layout (df_index).
 template <int B = 0>
@@ -65,29 +92,7 @@ __device__ __forceinline__ bool dda_step(const WorldView& w, RayState& r) {
     const int e = euclid_steps((int)__ldg(w.df + df_index<B>(w, lx, ly, lz)));
     if (e == 0) return true;
     if (e == 1) {
-        // one exact DDA face step (:341-356)
-        const int sx = isign(r.d.x), sy = isign(r.d.y), sz = isign(r.d.z);
-        const int hx = (1 + sx) >> 1, hy = (1 + sy) >> 1, hz = (1 + sz) >> 1;
-        int gx = f2i(r.o.x), gy = f2i(r.o.y), gz = f2i(r.o.z);
-        float wx = r.o.x - (float)gx, wy = r.o.y - (float)gy, wz = r.o.z - (float)gz;
-        const float dfx = ((float)hx - wx) * r.ix;
-        const float dfy = ((float)hy - wy) * r.iy;
-        const float dfz = ((float)hz - wz) * r.iz;
-        const int m = (dfx < dfy && sx != 0) ? ((dfx < dfz || sz == 0) ? 0 : 2) : ((dfy < dfz || sz == 0) ? 1 : 2);
-        const float dm = m == 0 ? dfx : (m == 1 ? dfy : dfz);
-        wx = wx + r.d.x * dm;
-        wy = wy + r.d.y * dm;
-        wz = wz + r.d.z * dm;
-        if (m == 0) { gx += sx; wx = (float)(1 - hx); }
-        else if (m == 1) { gy += sy; wy = (float)(1 - hy); }
-        else { gz += sz; wz = (float)(1 - hz); }
-        r.o.x = (float)gx + wx;
-        r.o.y = (float)gy + wy;
-        r.o.z = (float)gz + wz;
-        if (m == 0) r.o.x = r.o.x + (float)sx * 0.0001f;
-        else if (m == 1) r.o.y = r.o.y + (float)sy * 0.0001f;
-        else r.o.z = r.o.z + (float)sz * 0.0001f;
-        r.min_idx = m;
+        dda_face_step(r);
         r.inter = 1;
     } else {
         // jump by the conservative Euclidean radius (:361)
@@ -127,6 +132,66 @@ __device__ __forceinline__ TraceResult traverse(const WorldView& w, v3 origin, v
     ray_start(r, origin, direction, max_steps);
     while (!dda_step<B>(w, r)) {
     }
+    return ray_finish(w, r);
+}
+
+// The normal of the last face step: normal[MinIdx] = -sign(direction[MinIdx]).
+__device__ __forceinline__ v3 step_normal(const RayState& r) {
+    const int m = r.min_idx;
+    const int s = m == 0 ? isign(r.d.x) : (m == 1 ? isign(r.d.y) : isign(r.d.z));
+    v3 n = mk3(0.0f, 0.0f, 0.0f);
+    if (m == 0) n.x = (float)(-s); else if (m == 1) n.y = (float)(-s); else n.z = (float)(-s);
+    return n;
+}
+
+// VoxelTraversalDF_AlphaTest (InitialRayTraceFrag.glsl:204-305): as the DF
+// traversal, but at a solid voxel (E == 0) `stop(origin, normal, block)`
+// (StopRay, :189-202) decides whether the ray ends there; if not, up to four
+// exact face steps look for a voxel that stops it, after which the loop goes
+// on from one direction length back (origin += (E - 1) * direction, E = 0).
+template <int B, typename Stop>
+__device__ __forceinline__ TraceResult traverse_alpha(const WorldView& w, v3 origin, v3 direction, int max_steps,
+                                                      const Stop& stop) {
+    RayState r;
+    ray_start(r, origin, direction, max_steps);
+    bool inter = false;
+    for (r.itr = 0; r.itr < max_steps; r.itr++) {
+        const int lx = f2i_floor(r.o.x), ly = f2i_floor(r.o.y), lz = f2i_floor(r.o.z);
+        if (!in_volume(w, lx, ly, lz)) {
+            inter = false;
+            break;
+        }
+        const int e = euclid_steps((int)__ldg(w.df + df_index<B>(w, lx, ly, lz)));
+        if (e == 0) {
+            if (stop(r.o, step_normal(r), get_voxel(w, lx, ly, lz))) break;
+            for (int k = 0; k < 4; k++) {
+                dda_face_step(r);
+                const int cx = f2i_floor(r.o.x), cy = f2i_floor(r.o.y), cz = f2i_floor(r.o.z);
+                const int bt = get_voxel(w, cx, cy, cz);
+                if (bt > 0 && stop(r.o, step_normal(r), bt)) {
+                    TraceResult t;
+                    t.cell[0] = cx;
+                    t.cell[1] = cy;
+                    t.cell[2] = cz;
+                    t.steps = r.itr;
+                    t.normal = step_normal(r);
+                    t.block = bt;
+                    t.t = length(sub(r.o, r.init));
+                    return t;
+                }
+            }
+        }
+        if (e == 1) {
+            dda_face_step(r);
+            inter = true;
+        } else {
+            const float k = (float)(e - 1);
+            r.o.x = r.o.x + k * r.d.x;
+            r.o.y = r.o.y + k * r.d.y;
+            r.o.z = r.o.z + k * r.d.z;
+        }
+    }
+    r.inter = inter ? 1 : 0;
     return ray_finish(w, r);
 }
 

@@ -68,7 +68,7 @@ struct TexArray {
     long long level_off[11];
 };
 // The arrays, the per-block layer ids [albedo 128 | normal 128 | PBR 128 |
-// emissive 128], the grass override and the byte -> value tables (256
+// emissive 128 | transparent flag 128], the grass override and the byte -> value tables (256
 // entries each: sRGB decode for albedo, byte / 255 for the others).
 struct BlockTexView {
     TexArray albedo, normal, pbr, emissive;   // emissive.texels NULL: none
@@ -96,8 +96,10 @@ struct GIOut {
     void* aosky;        // 2 ch
 };
 
+struct AlphaStop;   // textures.cuh: StopRay of the alpha-tested traversal
+// alpha: the alpha-tested traversal (u_ShouldAlphaTest), or NULL
 cudaError_t trace_primary(const WorldView& w, const CamView& cam, int W, int H, int max_steps, int fp16,
-                          GBufferOut out, Counters* stats, cudaStream_t s);
+                          GBufferOut out, Counters* stats, cudaStream_t s, const AlphaStop* alpha = nullptr);
 cudaError_t trace_shadow(const WorldView& w, const CamView& cam, int W, int H, int max_steps, const float sun[3],
                          int fp16, const void* t, const uint8_t* face, uint8_t* shadow, Counters* stats,
                          cudaStream_t s);

@@ -15,14 +15,15 @@ __device__ __forceinline__ float stored_value(float v, const __half*) { return _
 // InitialRayTraceFrag.glsl main (:417-468). Writes the G-buffer texel `px`;
 // returns the step count and, for the passes that follow, the hit distance as
 // stored and the face id.
-template <int B, typename S>
+// kAlpha: the alpha-tested traversal (u_ShouldAlphaTest) with `stop`.
+template <int B, typename S, bool kAlpha = false>
 __device__ __forceinline__ unsigned primary_pixel(const WorldView& w, const CamView& cam, int W, int H, int i, int j,
                                                   int max_steps, size_t px, S* out_t, uint8_t* out_face,
                                                   uint8_t* out_block, int32_t* out_hit, uint16_t* out_steps,
-                                                  float* t_stored, int* face_id) {
+                                                  float* t_stored, int* face_id, const AlphaStop* stop = nullptr) {
     const v3 r0 = ray_origin(cam);
     const v3 dir = normalize(ray_dir_at(cam, texcoord(i, j, W, H)));
-    const TraceResult r = traverse<B>(w, r0, dir, max_steps);
+    const TraceResult r = kAlpha ? traverse_alpha<B>(w, r0, dir, max_steps, *stop) : traverse<B>(w, r0, dir, max_steps);
     const bool intersect = r.t > 0.0f && r.block > 0;
     const int face = intersect ? normal_id(r.normal) : kFaceMiss;
     st(out_t + px, r.t);

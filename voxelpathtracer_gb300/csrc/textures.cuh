@@ -5,6 +5,7 @@
 // LINEAR / LINEAR_MIPMAP_LINEAR selection by level of detail. Shared by the
 // textured G-buffer pass and the diffuse trace's bounce hits.
 #pragma once
+#include "dda.cuh"
 #include "kernels.cuh"
 
 namespace vpt {
@@ -98,5 +99,34 @@ __device__ __forceinline__ void sample_level(const TexArray& a, int layer_id, fl
     const int layer = min(max(layer_id, 0), a.layers - 1);
     bilinear_level(a, min(level, a.levels - 1), layer, u, v, nch, lut, out);
 }
+
+// channel c alone of a textureLod at an integer level
+__device__ __forceinline__ float sample_channel_level(const TexArray& a, int layer_id, float u, float v, int level,
+                                                      int c, const float* lut) {
+    float out[4];
+    sample_level(a, layer_id, u, v, level, c + 1, lut, out);
+    return out[c];
+}
+
+// StopRay (InitialRayTraceFrag.glsl:189-202): an opaque block stops the ray;
+// a transparent one (BlockTransparentData) only where the albedo alpha,
+// sampled at the face UV (CalculateUV, both coordinates flipped) at level
+// int(log2(size / ((1 / D) * K))) clamped to 0..8 (D the distance to the
+// camera, K = 1 / (2 tan(fov / (2 W))) in pixels per radian; the reference
+// writes its 512-texel size as a constant), exceeds 0.975.
+struct AlphaStop {
+    BlockTexView tv;
+    v3 cam;
+    float k;
+    __device__ __forceinline__ bool operator()(v3 p, v3 n, int type) const {
+        const int id = min(max(type, 0), 127);
+        if (__ldg(tv.ids + 512 + id) == 0) return true;
+        const v2 fc = face_coords(p, normal_id(n));
+        const float u = 1.0f - fract_f(fc.x), v = 1.0f - fract_f(fc.y);
+        const float D = length(sub(p, cam));
+        const int lod = min(max(f2i(dlog2((float)tv.albedo.size / ((1.0f / D) * k))), 0), 8);
+        return sample_channel_level(tv.albedo, __ldg(tv.ids + id), u, v, lod, 3, tv.unorm) > 0.975f;
+    }
+};
 
 }  // namespace vpt

@@ -17,10 +17,11 @@ __device__ __forceinline__ void tile_pixel(int* i, int* j) {
 }
 
 // InitialRayTraceFrag.glsl main (:417-468)
-template <typename S>
+template <typename S, bool kAlpha>
 __global__ void __launch_bounds__(256) k_trace_primary(WorldView w, CamView cam, int W, int H, int max_steps,
                                                        S* out_t, uint8_t* out_face, uint8_t* out_block,
-                                                       int32_t* out_hit, uint16_t* out_steps, Counters* stats) {
+                                                       int32_t* out_hit, uint16_t* out_steps, Counters* stats,
+                                                       AlphaStop stop) {
     int i, j;
     tile_pixel(&i, &j);
     const bool valid = i < W && j < H;
@@ -28,8 +29,8 @@ __global__ void __launch_bounds__(256) k_trace_primary(WorldView w, CamView cam,
     if (valid) {
         float d;
         int face;
-        nsteps = primary_pixel<0>(w, cam, W, H, i, j, max_steps, (size_t)j * W + i, out_t, out_face, out_block,
-                                  out_hit, out_steps, &d, &face);
+        nsteps = primary_pixel<0, S, kAlpha>(w, cam, W, H, i, j, max_steps, (size_t)j * W + i, out_t, out_face,
+                                             out_block, out_hit, out_steps, &d, &face, &stop);
     }
     if (stats) count_rays(stats, kRayPrimary, valid ? 1u : 0u, nsteps);
 }
@@ -84,13 +85,14 @@ void launch_diffuse(bool one, bool tex, dim3 grid, cudaStream_t s, const WorldVi
 }  // namespace
 
 cudaError_t trace_primary(const WorldView& w, const CamView& cam, int W, int H, int max_steps, int fp16,
-                          GBufferOut out, Counters* stats, cudaStream_t s) {
+                          GBufferOut out, Counters* stats, cudaStream_t s, const AlphaStop* alpha) {
+    const AlphaStop st = alpha ? *alpha : AlphaStop{};
     if (fp16)
-        k_trace_primary<__half><<<tile_grid(W, H), 256, 0, s>>>(w, cam, W, H, max_steps, (__half*)out.t, out.face,
-                                                                out.block, out.hit, out.steps, stats);
+        (alpha ? k_trace_primary<__half, true> : k_trace_primary<__half, false>)<<<tile_grid(W, H), 256, 0, s>>>(
+            w, cam, W, H, max_steps, (__half*)out.t, out.face, out.block, out.hit, out.steps, stats, st);
     else
-        k_trace_primary<float><<<tile_grid(W, H), 256, 0, s>>>(w, cam, W, H, max_steps, (float*)out.t, out.face,
-                                                               out.block, out.hit, out.steps, stats);
+        (alpha ? k_trace_primary<float, true> : k_trace_primary<float, false>)<<<tile_grid(W, H), 256, 0, s>>>(
+            w, cam, W, H, max_steps, (float*)out.t, out.face, out.block, out.hit, out.steps, stats, st);
     return cudaGetLastError();
 }
 
