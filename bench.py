@@ -323,7 +323,7 @@ def run_ours(args):
         # with block textures (GenerateGBuffer + the colour pass over it):
         # 24 seeded 512 x 512 layers per array, as the reference's block PNGs
         tex = vpt.generate_block_textures(512, 24, seed=0, grass_block=1)
-        vt, _ = run_variant(textures=tex)
+        vt, last_rgb["textured"] = run_variant(textures=tex)
         vt["textures"] = {"size": 512, "layers": 24}
         variant = {"fp16_storage": v16, "gi_quarter": vq, "reflections": vr, "gi_quarter_reflections": vrq,
                    "block_textures": vt}
@@ -342,6 +342,12 @@ def run_ours(args):
                        "gt_seconds": gt_s, "gt_luma_sh_stderr_mean": float(np.mean(se)),
                        "frame": total - 1, "rmse": {}}
         for k, img in last_rgb.items():
+            if k == "textured":   # against the ground truth of the textured frame
+                with quality.make_gt_context(W, H, vox, blocks, textures=tex) as g:
+                    gt_t, _ = quality.ground_truth_color(g, camera_at(vpt, yaw, pitch, total - 1),
+                                                         frame_at(vpt, total - 1), crop, spp=args.gt_spp, chunk=256)
+                quality_out["rmse"]["textured_svgf"] = quality.rmse(img[y0:y0 + ch, x0:x0 + cw], gt_t)
+                continue
             quality_out["rmse"][f"{k}_svgf"] = quality.rmse(img[y0:y0 + ch, x0:x0 + cw], gt)
 
     batched = None

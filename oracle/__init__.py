@@ -444,16 +444,23 @@ def spec_temporal(world: World, cam, prev_cam, config, g: dict, prev_g: dict, re
     return out
 
 
-def ground_truth(world: World, cam, config, frame, t, face, crop, spp, chunk, seed=0x5eed):
-    """FP64 Welford mean and M2 (h, w, 7) of the diffuse GI over crop = (x0, y0, w, h)."""
+def ground_truth(world: World, cam, config, frame, t, face, crop, spp, chunk, seed=0x5eed, textures=None):
+    """FP64 Welford mean and M2 (h, w, 7) of the diffuse GI over crop = (x0, y0, w, h);
+    textures (a block-texture dict) textures the bounce hits."""
     p = params(config)
     x0, y0, w, h = crop
     mean = np.empty((h, w, 7), np.float64)
     m2 = np.empty((h, w, 7), np.float64)
     t = np.ascontiguousarray(t, dtype=np.float32)
     face = np.ascontiguousarray(face, dtype=np.uint8)
-    lib().vpto_ground_truth(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)),
-                            _p(t), _p(face), x0, y0, w, h, spp, chunk, seed, _p(mean), _p(m2))
+    keep = _set_textures(textures)
+    try:
+        lib().vpto_ground_truth(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p),
+                                C.byref(_as(OFrame, frame)), _p(t), _p(face), x0, y0, w, h, spp, chunk, seed,
+                                _p(mean), _p(m2))
+    finally:
+        lib().vpto_set_block_textures(None)
+    del keep
     return mean, m2
 
 

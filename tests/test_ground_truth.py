@@ -51,19 +51,29 @@ def test_oracle_ground_truth_converges(oracle, small):
 
 
 @pytest.mark.gpu
-def test_gpu_ground_truth_bit_exact(vpt, oracle, small, gpu):
+@pytest.mark.parametrize("textured", [False, True], ids=["flat", "block-textures"])
+def test_gpu_ground_truth_bit_exact(vpt, oracle, small, textured, gpu):
+    """FP64 means and M2 equal the oracle's to the bit, with flat materials
+    and with the bounce hits sampling block textures."""
     s = small
     crop = (6, 4, 30, 20)
+    tex = vpt.generate_block_textures(16, 6, seed=3) if textured else None
     with vpt.Context(s["cfg"]) as ctx:
         ctx.upload_world(s["vox"])
         ctx.set_block_table(s["blocks"])
         ctx.build_df()
+        if tex is not None:
+            ctx.set_block_textures(tex)
         ctx.trace_primary(s["cam"])
         mean, m2 = ctx.ground_truth(s["frame"], crop, spp=40, chunk=16, seed=77)
     r_mean, r_m2 = oracle.ground_truth(s["world"], s["cam"], s["cfg"], s["frame"], s["g"]["t"], s["g"]["face"],
-                                       crop, spp=40, chunk=16, seed=77)
+                                       crop, spp=40, chunk=16, seed=77, textures=tex)
     assert np.array_equal(mean.view(np.uint64), r_mean.view(np.uint64))
     assert np.array_equal(m2.view(np.uint64), r_m2.view(np.uint64))
+    if textured:   # the textures change the converged GI
+        f_mean, _ = oracle.ground_truth(s["world"], s["cam"], s["cfg"], s["frame"], s["g"]["t"], s["g"]["face"],
+                                        crop, spp=40, chunk=16, seed=77)
+        assert not np.array_equal(f_mean, r_mean)
 
 
 @pytest.mark.gpu

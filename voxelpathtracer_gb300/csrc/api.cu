@@ -920,6 +920,10 @@ vpt_status vpt_ground_truth(vpt_ctx* c, const vpt_frame* f, int32_t x0, int32_t 
     a.d.frame_index = f->frame_index;
     a.d.seed = f->seed;
     a.d.lighting = gi_lighting(f);
+    if (c->textured) {   // the bounce hits read the block textures, as the diffuse trace's
+        a.d.textured = 1;
+        a.d.tex = tex_view(c);
+    }
     a.t = (const float*)c->gbuf[c->cur][GB_T];
     a.face = (const uint8_t*)c->gbuf[c->cur][GB_FACE];
     a.x0 = x0;

@@ -21,6 +21,8 @@ __device__ __forceinline__ uint32_t gt_stream(uint32_t px, uint32_t k, uint32_t 
     return pcg_hash(px + pcg_hash(k + pcg_hash(seed ^ 0x9E3779B9u)));
 }
 
+// kTex: the bounce hits sample the block textures (a.d.textured)
+template <bool kTex>
 __global__ void __launch_bounds__(128) k_gt_partial(GroundTruthArgs a) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     const int npx = a.cw * a.ch;
@@ -46,7 +48,7 @@ __global__ void __launch_bounds__(128) k_gt_partial(GroundTruthArgs a) {
             uint32_t rng = gt_stream((uint32_t)px, (uint32_t)k, a.seed);
             v3 odir = mk3(0.0f, 0.0f, 0.0f);
             bool sky = false;
-            const v4 x = calculate_diffuse(a.w, a.d, pos, nrm, &rng, &odir, &sky, &cnt);
+            const v4 x = calculate_diffuse<0, kTex>(a.w, a.d, pos, nrm, &rng, &odir, &sky, &cnt);
             irradiance_to_sh(vclamp(mk3(x.x, x.y, x.z), 0.0f, 8.0f), odir, sh, cocg);
             v[6] = x.w;
         }
@@ -103,7 +105,7 @@ __global__ void __launch_bounds__(128) k_gt_merge(GroundTruthArgs a) {
 
 cudaError_t ground_truth(const GroundTruthArgs& a, cudaStream_t s) {
     const int parts = a.cw * a.ch * a.nchunks;
-    k_gt_partial<<<(parts + 127) / 128, 128, 0, s>>>(a);
+    (a.d.textured ? k_gt_partial<true> : k_gt_partial<false>)<<<(parts + 127) / 128, 128, 0, s>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_gt_merge<<<(a.cw * a.ch + 127) / 128, 128, 0, s>>>(a);

@@ -24,6 +24,8 @@ def ground_truth_color(ctx: Context, cam: Camera, frame: Frame, crop, spp: int =
     least one a-trous iteration and the world loaded."""
     x0, y0, w, h = crop
     ctx.trace_primary(cam)
+    if getattr(ctx, "_textures", None) is not None:   # block textures: the textured G-buffer
+        ctx.generate_gbuffer()
     ctx.trace_shadow(frame)
     mean, m2 = ctx.ground_truth(frame, crop, spp=spp, chunk=chunk, seed=seed)
     H, W = ctx.height, ctx.width
@@ -48,11 +50,13 @@ def rmse(a: np.ndarray, b: np.ndarray) -> float:
     return float(np.sqrt(np.mean(d * d)))
 
 
-def make_gt_context(width: int, height: int, vox, blocks, **cfg) -> Context:
+def make_gt_context(width: int, height: int, vox, blocks, textures=None, **cfg) -> Context:
     c = default_config(width=width, height=height, **cfg)
     c.storage = 0
     ctx = Context(c)
     ctx.upload_world(vox)
     ctx.set_block_table(blocks)
     ctx.build_df()
+    if textures is not None:
+        ctx.set_block_textures(textures)
     return ctx
