@@ -77,7 +77,9 @@ typedef struct vpt_config {
     int32_t alpha_test;              /* u_ShouldAlphaTest (Core/Pipeline.cpp:141, off by default): with block
                                         textures the primary trace passes through texels of transparent
                                         blocks whose albedo alpha is at most 0.975 */
-    int32_t reserved[2];
+    int32_t alpha_test_shadows;      /* ShouldAlphaTestShadows (Core/Pipeline.cpp:142, off by default): the
+                                        same for the sun-shadow rays */
+    int32_t reserved[1];
 } vpt_config;
 
 typedef enum vpt_denoiser {

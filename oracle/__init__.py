@@ -43,7 +43,8 @@ class OParams(C.Structure):
                 ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
                 ("gi_divisor", C.c_int32), ("reflection_spp", C.c_int32), ("reflection_max_steps", C.c_int32),
                 ("reflection_shadow_max_steps", C.c_int32), ("reflection_temporal", C.c_int32),
-                ("reflection_denoise", C.c_int32), ("alpha_test", C.c_int32), ("reserved", C.c_int32 * 2)]
+                ("reflection_denoise", C.c_int32), ("alpha_test", C.c_int32), ("alpha_test_shadows", C.c_int32),
+                ("reserved", C.c_int32 * 1)]
 
 
 class OWorld(C.Structure):
@@ -211,15 +212,21 @@ def trace_primary(world: World, cam, config, rows=None, textures=None) -> dict:
     return g
 
 
-def trace_shadow(world: World, cam, config, frame, t, face, rows=None) -> np.ndarray:
+def trace_shadow(world: World, cam, config, frame, t, face, rows=None, textures=None) -> np.ndarray:
+    """Sun shadow; with config.alpha_test_shadows and block textures, alpha-tested rays."""
     p = params(config)
     H, W = p.height, p.width
     out = np.zeros((H, W), dtype=np.uint8)
     t = np.ascontiguousarray(t, dtype=np.float32)
     face = np.ascontiguousarray(face, dtype=np.uint8)
     r0, r1 = rows if rows else (0, H)
-    lib().vpto_trace_shadow(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p), C.byref(_as(OFrame, frame)),
-                            _p(t), _p(face), r0, r1, _p(out))
+    keep = _set_textures(textures)
+    try:
+        lib().vpto_trace_shadow(C.byref(world.s), C.byref(_as(OCamera, cam)), C.byref(p),
+                                C.byref(_as(OFrame, frame)), _p(t), _p(face), r0, r1, _p(out))
+    finally:
+        lib().vpto_set_block_textures(None)
+    del keep
     return out
 
 
@@ -534,7 +541,7 @@ def render_frame(world: World, cam, prev_cam, config, frame, prev_g: dict, hist:
     frame's "refl" (zero planes when None)."""
     p = params(config)
     g = trace_primary(world, cam, p, textures=textures)
-    shadow = trace_shadow(world, cam, p, frame, g["t"], g["face"])
+    shadow = trace_shadow(world, cam, p, frame, g["t"], g["face"], textures=textures)
     v = gi_view(p, g["t"], g["face"], g["block"])
     gi = trace_diffuse(world, cam, p, frame, v["t"], v["face"], textures=textures)
     if p.denoiser == 1:

@@ -151,6 +151,7 @@ TraceResult traverse(const vpto_world* w, v3 origin, v3 direction, int max_steps
 
 int normal_id(v3 n);
 bool alpha_active(const vpto_params* p);
+bool alpha_active_shadows(const vpto_params* p);
 
 // K of StopRay (InitialRayTraceFrag.glsl:421): 1 / (2 tan(fov / (2 W))),
 // the vertical fov 2 atan(1 / proj[1][1]), in double precision.
@@ -161,13 +162,16 @@ inline float alpha_k(float proj11, int width) {
 
 // StopRay (InitialRayTraceFrag.glsl:189-202) with the block textures set by
 // vpto_set_block_textures (true for every block without them).
-bool alpha_stop(v3 p, v3 n, int type, v3 cam, float k);
+// flip_x / lod_bias: 1 / 0 for the primary rays, 0 / -2 for the shadow rays
+// (ShadowRayTraceFrag.glsl:105-117).
+bool alpha_stop(v3 p, v3 n, int type, v3 cam, float k, int flip_x, int lod_bias);
 
 // VoxelTraversalDF_AlphaTest (InitialRayTraceFrag.glsl:204-305): at a solid
 // voxel (E == 0) StopRay decides; if the ray goes on, up to four exact face
 // steps look for a voxel that stops it, then the loop continues from one
 // direction length back (origin += (E - 1) * direction).
-TraceResult traverse_alpha(const vpto_world* w, v3 origin, v3 direction, int max_steps, v3 cam, float k) {
+TraceResult traverse_alpha(const vpto_world* w, v3 origin, v3 direction, int max_steps, v3 cam, float k,
+                           int flip_x = 1, int lod_bias = 0) {
     const v3 initial = origin;
     bool intersection = false;
     int min_idx = 0;
@@ -201,12 +205,12 @@ TraceResult traverse_alpha(const vpto_world* w, v3 origin, v3 direction, int max
         }
         int e = euclid_steps((int)w->df[vidx(w, lx, ly, lz)]);
         if (e == 0) {
-            if (alpha_stop(origin, step_normal(), get_voxel(w, lx, ly, lz), cam, k)) break;
+            if (alpha_stop(origin, step_normal(), get_voxel(w, lx, ly, lz), cam, k, flip_x, lod_bias)) break;
             for (int s = 0; s < 4; s++) {
                 face_step();
                 const int cx = f2i(std::floor(origin.x)), cy = f2i(std::floor(origin.y)), cz = f2i(std::floor(origin.z));
                 const int bt = get_voxel(w, cx, cy, cz);
-                if (bt > 0 && alpha_stop(origin, step_normal(), bt, cam, k)) {
+                if (bt > 0 && alpha_stop(origin, step_normal(), bt, cam, k, flip_x, lod_bias)) {
                     TraceResult r;
                     r.cell[0] = cx;
                     r.cell[1] = cy;
@@ -734,7 +738,10 @@ void vpto_trace_shadow(const vpto_world* w, const vpto_camera* cam, const vpto_p
             int block_at = get_voxel(w, f2i(std::floor(o.x)), f2i(std::floor(o.y)), f2i(std::floor(o.z)));
             float T = -1.0f;
             if (d > 0.0f) {
-                TraceResult r = traverse(w, o, L, p->shadow_max_steps);
+                TraceResult r = alpha_active_shadows(p)
+                                    ? traverse_alpha(w, o, L, p->shadow_max_steps, ray_origin(cam),
+                                                     alpha_k(cam->proj[5], W), 0, -2)
+                                    : traverse(w, o, L, p->shadow_max_steps);
                 cnt.add(1, r.steps);
                 T = r.t;
             }
@@ -2736,14 +2743,15 @@ extern "C" void vpto_set_textured_gbuffer(const float* normal, const float* pbr,
 
 namespace {
 bool alpha_active(const vpto_params* p) { return p->alpha_test != 0 && g_tex.on; }
+bool alpha_active_shadows(const vpto_params* p) { return p->alpha_test_shadows != 0 && g_tex.on; }
 
-bool alpha_stop(v3 p, v3 n, int type, v3 cam, float k) {
+bool alpha_stop(v3 p, v3 n, int type, v3 cam, float k, int flip_x, int lod_bias) {
     const int id = std::min(std::max(type, 0), 127);
     if (!g_tex.on || !g_tex.transparent[id]) return true;
     const v2 fc = face_coords(p, normal_id(n));
-    const float u = 1.0f - fract(fc.x), v = 1.0f - fract(fc.y);
+    const float u = flip_x ? 1.0f - fract(fc.x) : fract(fc.x), v = 1.0f - fract(fc.y);
     const float D = length(sub(p, cam));
-    const int lod = std::min(std::max(f2i(dm_log2((float)g_tex.A.size / ((1.0f / D) * k))), 0), 8);
+    const int lod = std::min(std::max(f2i(dm_log2((float)g_tex.A.size / ((1.0f / D) * k))) + lod_bias, 0), 8);
     const OTexArray& a = g_tex.A;
     const int layer = std::min(std::max(g_tex.albedo_id[id], 0), a.layers - 1);
     float o[4];

@@ -72,7 +72,8 @@ typedef struct vpto_params {
     int32_t reflection_temporal;  /* TEMPORAL_SPEC */
     int32_t reflection_denoise;   /* DenoiseReflections */
     int32_t alpha_test;           /* u_ShouldAlphaTest */
-    int32_t reserved[2];
+    int32_t alpha_test_shadows;   /* ShouldAlphaTestShadows */
+    int32_t reserved[1];
 } vpto_params;
 
 typedef struct vpto_world {

@@ -317,3 +317,45 @@ def test_alpha_tested_gbuffer_bit_exact(vpt, oracle, storage, frac, gpu):
                 assert_same(got[..., 0] if got.ndim == 3 and key != "hit" else got, ref[key], f"cam {k} {name}")
             assert stats["steps"]["primary"] == cnt.steps["primary"]
             ctx.end_frame()
+
+
+def test_oracle_alpha_tested_shadows(vpt, oracle):
+    """ShouldAlphaTestShadows: sun rays pass the cut-out texels of transparent
+    blocks, so fewer texels are shadowed; with no transparent block the
+    shadow plane is the plain one."""
+    vox, blocks, world, cams = scene(vpt, oracle)
+    tex = vpt.generate_block_textures(16, 6, seed=1)
+    frame = vpt.default_frame(frame_index=0, seed=3)
+    base = vpt.default_config(width=W, height=H, primary_max_steps=256)
+    g = oracle.trace_primary(world, cams[1], base)
+    plain = oracle.trace_shadow(world, cams[1], base, frame, g["t"], g["face"])
+    cfg = vpt.default_config(width=W, height=H, primary_max_steps=256, alpha_test_shadows=1)
+    tex["transparent"][:] = 0
+    assert np.array_equal(oracle.trace_shadow(world, cams[1], cfg, frame, g["t"], g["face"], textures=tex), plain)
+    tex["transparent"][:] = 1
+    cut = oracle.trace_shadow(world, cams[1], cfg, frame, g["t"], g["face"], textures=tex)
+    assert cut.sum() < plain.sum() and (cut <= plain).mean() > 0.9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", [0, 1], ids=["f32", "f16"])
+def test_alpha_tested_shadows_bit_exact(vpt, oracle, storage, gpu):
+    vox, blocks, world, cams = scene(vpt, oracle, seed=2)
+    tex = vpt.generate_block_textures(32, 5, seed=4)
+    tex["transparent"][:] = (np.random.default_rng(2).random(128) < 0.6).astype(np.int32)
+    frame = vpt.default_frame(frame_index=0, seed=3)
+    with vpt.Context(width=W, height=H, primary_max_steps=256, storage=storage, alpha_test=1,
+                     alpha_test_shadows=1) as ctx:
+        ctx.upload_world(vox)
+        ctx.set_block_table(blocks)
+        ctx.build_df()
+        ctx.set_block_textures(tex)
+        cfg = ctx.config
+        for k, cam in enumerate(cams):
+            ctx.trace_primary(cam)
+            ctx.trace_shadow(frame)
+            g = oracle.trace_primary(world, cam, cfg, textures=tex)
+            ref = oracle.trace_shadow(world, cam, cfg, frame, g["t"], g["face"], textures=tex)
+            assert_same(ctx.read_plane("SHADOW")[..., 0] if ctx.read_plane("SHADOW").ndim == 3
+                        else ctx.read_plane("SHADOW"), ref, f"cam {k} shadow")
+            ctx.end_frame()

@@ -60,7 +60,8 @@ class Config(C.Structure):
                 ("color_phi_bias", C.c_float), ("device", C.c_int32), ("denoiser", C.c_int32),
                 ("gi_divisor", C.c_int32), ("reflection_spp", C.c_int32), ("reflection_max_steps", C.c_int32),
                 ("reflection_shadow_max_steps", C.c_int32), ("reflection_temporal", C.c_int32),
-                ("reflection_denoise", C.c_int32), ("alpha_test", C.c_int32), ("reserved", C.c_int32 * 2)]
+                ("reflection_denoise", C.c_int32), ("alpha_test", C.c_int32), ("alpha_test_shadows", C.c_int32),
+                ("reserved", C.c_int32 * 1)]
 
 
 class Camera(C.Structure):

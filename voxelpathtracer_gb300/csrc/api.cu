@@ -808,9 +808,19 @@ vpt_status vpt_trace_shadow(vpt_ctx* c, const vpt_frame* f) {
     if ((s = check_frame(c, f)) != VPT_OK) return s;
     cudaSetDevice(c->dev);
     pass_begin(c, VPT_PASS_SHADOW);
+    // the alpha-tested shadow rays with block textures (ShouldAlphaTestShadows)
+    AlphaStop stop;
+    const bool alpha = c->cfg.alpha_test_shadows && c->textured;
+    if (alpha) {
+        stop.tv = tex_view(c);
+        stop.cam = mk3(c->cam.inv_view[12], c->cam.inv_view[13], c->cam.inv_view[14]);
+        stop.k = alpha_k(c->cam.proj[5], c->cfg.width);
+        stop.flip_x = 0;
+        stop.lod_bias = -2;
+    }
     CK(c, trace_shadow(world_view(c), cam_view(c->cam), c->cfg.width, c->cfg.height, c->cfg.shadow_max_steps,
                        f->sun_dir, c->fp16, c->gbuf[c->cur][GB_T], (const uint8_t*)c->gbuf[c->cur][GB_FACE],
-                       c->shadow, c->stats ? c->counters : nullptr, c->stream));
+                       c->shadow, c->stats ? c->counters : nullptr, c->stream, alpha ? &stop : nullptr));
     pass_end(c, VPT_PASS_SHADOW);
     c->launches += 1;
     return VPT_OK;

@@ -102,7 +102,7 @@ cudaError_t trace_primary(const WorldView& w, const CamView& cam, int W, int H, 
                           GBufferOut out, Counters* stats, cudaStream_t s, const AlphaStop* alpha = nullptr);
 cudaError_t trace_shadow(const WorldView& w, const CamView& cam, int W, int H, int max_steps, const float sun[3],
                          int fp16, const void* t, const uint8_t* face, uint8_t* shadow, Counters* stats,
-                         cudaStream_t s);
+                         cudaStream_t s, const AlphaStop* alpha = nullptr);
 cudaError_t trace_diffuse(const WorldView& w, const CamView& cam, int W, int H, const DiffuseArgs& a, int fp16,
                           const void* t, const uint8_t* face, GIOut out, Counters* stats, cudaStream_t s);
 

@@ -40,10 +40,11 @@ __device__ __forceinline__ unsigned primary_pixel(const WorldView& w, const CamV
 
 // ShadowRayTraceFrag.glsl main (:414-513): one hard shadow ray towards the sun
 // from the G-buffer texel with hit distance d and face id `face`.
-template <int B>
+// kAlpha: the alpha-tested traversal (u_ShouldAlphaTest = ShouldAlphaTestShadows) with `stop`.
+template <int B, bool kAlpha = false>
 __device__ __forceinline__ uint8_t shadow_pixel(const WorldView& w, const CamView& cam, int W, int H, int i, int j,
                                                 int max_steps, v3 L, float d, int face, unsigned* nrays,
-                                                unsigned* nsteps) {
+                                                unsigned* nsteps, const AlphaStop* stop = nullptr) {
     if (d < 0.0f) return 0;
     const v3 pos = add(ray_origin(cam), muls(normalize(ray_dir_at(cam, texcoord(i, j, W, H))), d));
     const v3 n = normal_from_id(face, 1.0f);
@@ -53,7 +54,7 @@ __device__ __forceinline__ uint8_t shadow_pixel(const WorldView& w, const CamVie
     const int block_at = get_voxel(w, f2i_floor(o.x), f2i_floor(o.y), f2i_floor(o.z));
     float T = -1.0f;
     if (d > 0.0f) {
-        const TraceResult r = traverse<B>(w, o, L, max_steps);
+        const TraceResult r = kAlpha ? traverse_alpha<B>(w, o, L, max_steps, *stop) : traverse<B>(w, o, L, max_steps);
         T = r.t;
         *nrays += 1;
         *nsteps += (unsigned)r.steps;

@@ -114,17 +114,20 @@ __device__ __forceinline__ float sample_channel_level(const TexArray& a, int lay
 // int(log2(size / ((1 / D) * K))) clamped to 0..8 (D the distance to the
 // camera, K = 1 / (2 tan(fov / (2 W))) in pixels per radian; the reference
 // writes its 512-texel size as a constant), exceeds 0.975.
+// The shadow pass's StopRay (ShadowRayTraceFrag.glsl:105-117) flips only the
+// v coordinate and samples two levels finer (flip_x = 0, lod_bias = -2).
 struct AlphaStop {
     BlockTexView tv;
     v3 cam;
     float k;
+    int flip_x = 1, lod_bias = 0;
     __device__ __forceinline__ bool operator()(v3 p, v3 n, int type) const {
         const int id = min(max(type, 0), 127);
         if (__ldg(tv.ids + 512 + id) == 0) return true;
         const v2 fc = face_coords(p, normal_id(n));
-        const float u = 1.0f - fract_f(fc.x), v = 1.0f - fract_f(fc.y);
+        const float u = flip_x ? 1.0f - fract_f(fc.x) : fract_f(fc.x), v = 1.0f - fract_f(fc.y);
         const float D = length(sub(p, cam));
-        const int lod = min(max(f2i(dlog2((float)tv.albedo.size / ((1.0f / D) * k))), 0), 8);
+        const int lod = min(max(f2i(dlog2((float)tv.albedo.size / ((1.0f / D) * k))) + lod_bias, 0), 8);
         return sample_channel_level(tv.albedo, __ldg(tv.ids + id), u, v, lod, 3, tv.unorm) > 0.975f;
     }
 };

@@ -36,17 +36,18 @@ __global__ void __launch_bounds__(256) k_trace_primary(WorldView w, CamView cam,
 }
 
 // ShadowRayTraceFrag.glsl main (:414-513): one hard shadow ray towards the sun.
-template <typename S>
+template <typename S, bool kAlpha>
 __global__ void __launch_bounds__(256) k_trace_shadow(WorldView w, CamView cam, int W, int H, int max_steps,
                                                       float lx, float ly, float lz, const S* t,
-                                                      const uint8_t* face, uint8_t* shadow, Counters* stats) {
+                                                      const uint8_t* face, uint8_t* shadow, Counters* stats,
+                                                      AlphaStop stop) {
     int i, j;
     tile_pixel(&i, &j);
     unsigned nrays = 0, nsteps = 0;
     if (i < W && j < H) {
         const size_t px = (size_t)j * W + i;
-        shadow[px] = shadow_pixel<0>(w, cam, W, H, i, j, max_steps, mk3(lx, ly, lz), ld(t + px), __ldg(face + px),
-                                     &nrays, &nsteps);
+        shadow[px] = shadow_pixel<0, kAlpha>(w, cam, W, H, i, j, max_steps, mk3(lx, ly, lz), ld(t + px),
+                                             __ldg(face + px), &nrays, &nsteps, &stop);
     }
     if (stats) count_rays(stats, kRayShadow, nrays, nsteps);
 }
@@ -98,13 +99,14 @@ cudaError_t trace_primary(const WorldView& w, const CamView& cam, int W, int H, 
 
 cudaError_t trace_shadow(const WorldView& w, const CamView& cam, int W, int H, int max_steps, const float sun[3],
                          int fp16, const void* t, const uint8_t* face, uint8_t* shadow, Counters* stats,
-                         cudaStream_t s) {
+                         cudaStream_t s, const AlphaStop* alpha) {
+    const AlphaStop st = alpha ? *alpha : AlphaStop{};
     if (fp16)
-        k_trace_shadow<__half><<<tile_grid(W, H), 256, 0, s>>>(w, cam, W, H, max_steps, sun[0], sun[1], sun[2],
-                                                               (const __half*)t, face, shadow, stats);
+        (alpha ? k_trace_shadow<__half, true> : k_trace_shadow<__half, false>)<<<tile_grid(W, H), 256, 0, s>>>(
+            w, cam, W, H, max_steps, sun[0], sun[1], sun[2], (const __half*)t, face, shadow, stats, st);
     else
-        k_trace_shadow<float><<<tile_grid(W, H), 256, 0, s>>>(w, cam, W, H, max_steps, sun[0], sun[1], sun[2],
-                                                              (const float*)t, face, shadow, stats);
+        (alpha ? k_trace_shadow<float, true> : k_trace_shadow<float, false>)<<<tile_grid(W, H), 256, 0, s>>>(
+            w, cam, W, H, max_steps, sun[0], sun[1], sun[2], (const float*)t, face, shadow, stats, st);
     return cudaGetLastError();
 }
 
