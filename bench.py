@@ -11,13 +11,15 @@ little every frame so the temporal pass reprojects real motion.
 `value` is DF-DDA rays per second over the whole denoised frame (trace +
 SVGF + shade inside the timed region, inputs resident in HBM); `frame_ms` is
 the denoised frame time. `e2e` is the same metric through the public C ABI
-call vpt_render_frame with the image copied to pinned host memory every step.
-The L2 is flushed (a 512 MiB write) between timed steps.
+call vpt_render_frame_async, every frame's image copied to pinned host memory
+(double-buffered readback). The L2 is flushed (a 512 MiB write) between timed
+steps.
 
 --impl reference times the reference's algorithm on the host cores: the CPU
-restatement of the shaders (the reference itself is GLSL and cannot run
-without an OpenGL context), OpenMP over all host threads, on a bounded band
-of rows of the same frame.
+restatement of the shaders (oracle/; the reference itself is GLSL and cannot
+run without an OpenGL context), OpenMP over all host threads, rendering the
+same whole frames (traces, SVGF and colour pass) from inputs generated by
+oracle.inputs, so that arm never loads libvpt.
 """
 from __future__ import annotations
 
@@ -144,15 +146,27 @@ def workload_inputs(vpt, seed=0):
     return vox, blocks, yaw, pitch
 
 
-def camera_at(vpt, yaw, pitch, step):
-    # a slow pan: 0.25 degree of yaw and 0.05 voxel of travel per frame
+def camera_at(gen, yaw, pitch, step):
+    """Camera of frame `step`: a slow pan, 0.25 degree of yaw and 0.05 voxel of
+    travel per frame. gen is libvpt's package or oracle.inputs (same matrices)."""
     W, H = RES
     pos = (CAM_POS[0] + 0.05 * step, CAM_POS[1], CAM_POS[2])
-    return vpt.camera_from_pose(pos, yaw + 0.25 * step, pitch, 90.0, W / H)
+    return gen.camera_from_pose(pos, yaw + 0.25 * step, pitch, 90.0, W / H)
 
 
-def frame_at(vpt, step):
-    return vpt.default_frame(frame_index=step, seed=0, time=1.0 + step / 60.0)
+def frame_at(gen, step):
+    return gen.default_frame(frame_index=step, seed=0, time=1.0 + step / 60.0)
+
+
+def workload_config(args, world):
+    """The `config` object of both arms' lines."""
+    return {"workload": "full frame 1920x1080, 256^3 world (seed 0), 1 spp + sun shadow + 1 bounce "
+                        "(+ bounce shadow), SVGF temporal + variance + 5 a-trous, colour pass",
+            "world": list(WORLD), "resolution": list(RES), "spp": 1, "bounces": 1,
+            "storage": "fp32" if args.storage == 0 else "fp16",
+            "gi_divisor": args.gi_divisor, "reflection_spp": args.reflection_spp,
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "l2": "flushed (512 MiB write) between timed steps"}
 
 
 # ------------------------------------------------------------- our arm --
@@ -350,6 +364,28 @@ def run_ours(args):
                 continue
             quality_out["rmse"][f"{k}_svgf"] = quality.rmse(img[y0:y0 + ch, x0:x0 + cw], gt)
 
+    if args.error_curve and rank == 0:
+        # RMSE against the FP64 ground truth as the history grows, for a static
+        # and for the benchmark's panning camera: the SVGF output, its temporal
+        # input before any spatial filter and this frame's raw 1-spp GI
+        from voxelpathtracer_gb300 import quality
+        sample_at = (0, 1, 2, 4, 8, 16, 32)
+        frames = [frame_at(vpt, s) for s in range(max(sample_at) + 1)]
+        curves = {}
+        with quality.make_gt_context(W, H, vox, blocks) as g:
+            for name, cams in (("static", [camera_at(vpt, yaw, pitch, 0)] * len(frames)),
+                               ("pan", [camera_at(vpt, yaw, pitch, s) for s in range(len(frames))])):
+                with vpt.Context(width=W, height=H, device=local) as c2:
+                    c2.upload_world(vox)
+                    c2.set_block_table(blocks)
+                    c2.build_df()
+                    curves[name] = quality.error_by_history(c2, g, cams, frames, quality.DEFAULT_CROP_1080P,
+                                                            sample_at, spp=args.gt_spp)
+        if quality_out is None:
+            quality_out = {}
+        quality_out["error_by_history"] = {"crop": list(quality.DEFAULT_CROP_1080P), "gt_spp": args.gt_spp,
+                                           "rmse_by_frame": curves}
+
     batched = None
     if not args.no_batch:
         batched = batched_section(vpt, torch, args, local, flush)
@@ -366,7 +402,7 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(vpt, args, vox, blocks, yaw, pitch, sample_rows=args.cpu_rows)
+        cpu = cpu_baseline(args, vox, blocks, yaw, pitch)
     ctx.close()
     dist.close()
     if rank != 0:
@@ -390,13 +426,7 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f32" if args.storage == 0 else "f16-storage/f32",
         "data": "synthetic",
-        "config": {"workload": "full frame 1920x1080, 256^3 world (seed 0), 1 spp + sun shadow + 1 bounce "
-                               "(+ bounce shadow), SVGF temporal + variance + 5 a-trous, colour pass",
-                   "world": list(WORLD), "resolution": list(RES), "spp": 1, "bounces": 1,
-                   "storage": "fp32" if args.storage == 0 else "fp16",
-                   "gi_divisor": args.gi_divisor, "reflection_spp": args.reflection_spp,
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "flushed (512 MiB write) between timed steps"},
+        "config": workload_config(args, world),
         "e2e": {"value": e2e_value, "unit": "rays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": W * H * 3 * 4, "ms_per_step": e2e_t * 1e3 / args.steps,
                 "api": "vpt_render_frame_async -> pinned host RGB, double-buffered readback"},
@@ -521,6 +551,9 @@ def learned_section(vpt, torch, args, local, flush, vox, blocks, yaw, pitch, pea
     W, H = RES
     out = {"weights": {k: meta[k] for k in ("pairs", "crop", "spp", "steps", "holdout_rmse_noisy",
                                              "holdout_rmse_net") if k in meta}}
+    out["weights"]["deviation"] = ("trained on random crops of 1920x1080 frames (the crop size above), not on "
+                                   "whole 1080p pairs: the same per-pixel statistics at a fraction of the "
+                                   "1024-spp ground-truth cost")
     with vpt.UNet(1, H, W, device=local) as net, vpt.Context(width=W, height=H, device=local) as ctx:
         net.set_params(params)
         ctx.upload_world(vox)
@@ -688,67 +721,83 @@ def large_section(vpt, torch, args, local):
 
 
 # ------------------------------------------------------- CPU (oracle) arm --
-def cpu_band_frame(vpt, oracle, wobj, yaw, pitch, step, rows):
-    """Primary + sun shadow + diffuse traces of rows [r0, r1) of frame `step`
-    on the host cores. Returns (seconds, DF-DDA rays traced)."""
-    W, H = RES
-    cfg = vpt.default_config(width=W, height=H)
-    cam = camera_at(vpt, yaw, pitch, step)
-    fr = frame_at(vpt, step)
-    with oracle.Counting() as cnt:
-        t0 = time.perf_counter()
-        g = oracle.trace_primary(wobj, cam, cfg, rows=rows)
-        oracle.trace_shadow(wobj, cam, cfg, fr, g["t"], g["face"], rows=rows)
-        oracle.trace_diffuse(wobj, cam, cfg, fr, g["t"], g["face"], rows=rows)
-        dt = time.perf_counter() - t0
-    return dt, sum(cnt.rays.values())
+class OracleFrames:
+    """Whole frames of the workload rendered by the CPU restatement (oracle/):
+    primary, sun-shadow and diffuse traces, SVGF (pre-temporal 3x3, temporal,
+    variance, 5 a-trous iterations) and the colour pass, the history carried
+    from frame to frame as libvpt carries it. gen makes the cameras and frame
+    constants (oracle.inputs for the reference arm)."""
+
+    def __init__(self, oracle, gen, vox, blocks, yaw, pitch, storage=0, gi_divisor=1, reflection_spp=0):
+        W, H = RES
+        self.oracle, self.gen, self.yaw, self.pitch = oracle, gen, yaw, pitch
+        from oracle import inputs
+        self.cfg = inputs.default_config(width=W, height=H, storage=storage, gi_divisor=gi_divisor,
+                                         reflection_spp=reflection_spp)
+        self.world = oracle.World(vox, oracle.build_df(vox), blocks)
+        self.prev_g, self.hist = oracle.empty_history(H, W, gi_divisor)
+        self.prev_refl = None
+        self.prev_cam = None
+
+    def render(self, step):
+        """Frame `step`; returns (seconds, DF-DDA rays traced)."""
+        o = self.oracle
+        cam = camera_at(self.gen, self.yaw, self.pitch, step)
+        fr = frame_at(self.gen, step)
+        prev_cam = self.prev_cam if self.prev_cam is not None else cam
+        with o.Counting() as cnt:
+            t0 = time.perf_counter()
+            r = o.render_frame(self.world, cam, prev_cam, self.cfg, fr, self.prev_g, self.hist, self.prev_refl)
+            dt = time.perf_counter() - t0
+        self.prev_g = {k: r["g"][k] for k in ("t", "face", "block")}
+        self.hist = r["svgf"]["temporal"]
+        if r["refl"] is not None:
+            self.prev_refl = {"out": r["refl"]["out"], "hit": r["refl"]["hit"], "stable": r["refl"]["stable"]}
+        self.prev_cam = cam
+        return dt, sum(cnt.rays.values())
 
 
-def band_rows(n):
-    W, H = RES
-    r0 = H // 2 - n // 2
-    return (r0, r0 + n)
-
-
-def cpu_baseline(vpt, args, vox, blocks, yaw, pitch, sample_rows=None):
-    """Whole frames of the workload traced by the CPU restatement on all host
+def cpu_baseline(args, vox, blocks, yaw, pitch):
+    """Whole frames of the workload rendered by the CPU restatement on all host
     threads, repeated until args.cpu_seconds of CPU work have accumulated."""
     import oracle
-    W, H = RES
-    rows = band_rows(sample_rows) if sample_rows else (0, H)
-    wobj = oracle.World(vox, oracle.build_df(vox), blocks)
-    cpu_band_frame(vpt, oracle, wobj, yaw, pitch, 0, (H // 2, H // 2 + 4))   # thread pool warm-up
+    from oracle import inputs
+    of = OracleFrames(oracle, inputs, vox, blocks, yaw, pitch, args.storage, args.gi_divisor, args.reflection_spp)
     t_sum, rays_sum, frames = 0.0, 0, 0
     while t_sum < args.cpu_seconds:
-        dt, rays = cpu_band_frame(vpt, oracle, wobj, yaw, pitch, frames, rows)
+        dt, rays = of.render(frames)
         t_sum += dt
         rays_sum += rays
         frames += 1
-    what = "whole frames" if rows == (0, H) else f"rows {rows[0]}..{rows[1] - 1} of frames"
     return {"value": rays_sum / t_sum, "unit": "rays/s", "cores": oracle.omp_threads(), "kind": "port",
-            "sample": f"{what} 0..{frames - 1} of the workload (primary, sun-shadow, diffuse and bounce-shadow "
-                      f"rays of the CPU restatement): {rays_sum} rays in {t_sum:.1f} s"}
+            "ms_per_frame": 1e3 * t_sum / frames,
+            "sample": f"whole frames 0..{frames - 1} of the workload (traces, SVGF and colour pass of the CPU "
+                      f"restatement): {rays_sum} rays in {t_sum:.1f} s"}
 
 
 def run_reference(args):
+    """The reference's algorithm on the host cores: the CPU restatement renders
+    the same whole frames as the GPU arm. Nothing of libvpt is loaded."""
     rank, world, local = dist_env()
     if rank != 0:
         return
     import oracle
-    import voxelpathtracer_gb300 as vpt
-    W, H = RES
-    vox, blocks, yaw, pitch = workload_inputs(vpt, seed=0)
-    rows = band_rows(args.cpu_rows) if args.cpu_rows else (0, H)
-    wobj = oracle.World(vox, oracle.build_df(vox), blocks)
+    from oracle import inputs
+    X, Y, Z = WORLD
+    vox = inputs.generate_world(X, Y, Z, seed=0)
+    blocks = inputs.generate_block_table(100, seed=0)
+    yaw, pitch = inputs.seeded_pose(0)
+    of = OracleFrames(oracle, inputs, vox, blocks, yaw, pitch, args.storage, args.gi_divisor, args.reflection_spp)
     times, rays = [], []
     for s in range(args.warmup + args.steps):
-        dt, n = cpu_band_frame(vpt, oracle, wobj, yaw, pitch, s, rows)
+        dt, n = of.render(s)
         if s >= args.warmup:
             times.append(dt)
             rays.append(n)
     value = sum(rays) / sum(times)
-    what = "each whole 1920x1080 frame" if rows == (0, H) else f"rows {rows[0]}..{rows[1] - 1} of each frame"
-    sample = f"{what}: primary, sun-shadow, diffuse and bounce-shadow rays of the CPU restatement"
+    sample = (f"whole frames {args.warmup}..{args.warmup + args.steps - 1} of the workload after {args.warmup} "
+              f"warm-up frames: traces, SVGF and colour pass of the CPU restatement, {sum(rays)} rays in "
+              f"{sum(times):.1f} s")
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -758,19 +807,19 @@ def run_reference(args):
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": 1e3 * sum(times) / len(times),
+        "frame_ms": 1e3 * sum(times) / len(times),
+        "rays_per_frame": float(np.mean(rays)),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": "f32" if args.storage == 0 else "f16-storage/f32",
         "data": "synthetic",
-        "config": {"workload": "full frame 1920x1080, 256^3 world (seed 0), 1 spp + sun shadow + 1 bounce "
-                               "(+ bounce shadow); a bounded band of rows per step",
-                   "world": list(WORLD), "resolution": list(RES)},
+        "config": workload_config(args, world),
         "cpu_baseline": {"value": value, "unit": "rays/s", "cores": oracle.omp_threads(), "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference implements this path in GLSL behind OpenGL, which cannot run here; its CPU "
-                "restatement (oracle/) is timed on the host cores instead",
+                "restatement (oracle/, OpenMP) renders the same frames on the host cores instead",
     }
     print(json.dumps(line), flush=True)
 
@@ -786,9 +835,7 @@ def main():
                     help="GI grid = frame / this (the reference's DiffuseTraceResolution is 1/4)")
     ap.add_argument("--reflection-spp", type=int, default=0,
                     help="reflection rays per GI texel in the timed frame (0: no reflection pass)")
-    ap.add_argument("--cpu-rows", type=int, default=0,
-                    help="trace only a band of this many rows on the CPU (0 = whole frames)")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="CPU work accumulated by the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the FP16-storage variant")
@@ -797,6 +844,8 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-denoiser measurements")
     ap.add_argument("--no-large", action="store_true", help="skip the 512^3 / 3840x2160 combined run")
     ap.add_argument("--gt-spp", type=int, default=4096, help="samples per pixel of the FP64 ground truth")
+    ap.add_argument("--error-curve", action="store_true",
+                    help="also measure the RMSE against the ground truth over 33 frames, static and panning camera")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the dominant kernel from an ncu capture")
     args = ap.parse_args()

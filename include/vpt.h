@@ -296,7 +296,9 @@ vpt_status vpt_shade(vpt_ctx* ctx, const vpt_frame* frame);
  * vpt_trace_shadow and vpt_trace_diffuse would. Stores `cam` as this frame's
  * camera. */
 vpt_status vpt_trace_frame(vpt_ctx* ctx, const vpt_camera* cam, const vpt_frame* frame);
-/* Device buffers of one frame trace, owned by the caller. Layouts as the
+/* Device buffers of one frame trace, owned by the caller. Every plane, the
+ * GI planes included, holds cfg->width x cfg->height pixels (the fused trace
+ * has no coarser GI grid: cfg->gi_divisor must be 0 or 1). Layouts as the
  * planes of vpt_plane_info: t and gi_* in cfg->storage's type (fp32 or fp16),
  * hit 3 x int32 per pixel, gi_sh 4, gi_cocg 2, gi_luma 1, gi_aosky 2 channels. */
 typedef struct vpt_trace_buffers {
@@ -325,7 +327,10 @@ typedef struct vpt_trace_buffers {
  * only scratch, its work-queue counter, sits in a 256-byte static device
  * array of libvpt that every GPU using the library holds until the process
  * exits. The first call on a device looks that array's address up (with the
- * device current). Images are limited to 16384 x 16384. All calls share the
+ * device current) and keeps it, so a device that was reset with
+ * cudaDeviceReset must not be used with this call again in that process.
+ * Images are limited to 16384 x 16384 and gi_divisor > 1 is rejected
+ * (VPT_ERR_INVALID_ARG). All calls share the
  * array, which is reset at the start of each call: calls that overlap on the
  * GPU race, so issue them on one stream (or otherwise order them). The
  * current device and `stream` (a cudaStream_t, 0 = legacy default) are the

@@ -83,6 +83,7 @@ def lib() -> C.CDLL:
         L.vpto_spatial_initial.argtypes = [P, P, P, P, P, P]
         L.vpto_temporal.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, P]
         L.vpto_variance.argtypes = [P, P, P, P, P, P]
+        L.vpto_reproject.argtypes = [P, P, C.c_int, C.c_int, P, P, P]
         L.vpto_atrous.argtypes = [P, P, P, C.c_int, P, P, P, P, P, P, P, P]
         L.vpto_gi_view.argtypes = [P, P, P, P, P, P, P]
         L.vpto_shade.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, C.c_int, C.c_int, P]
@@ -288,6 +289,17 @@ def temporal(cam, prev_cam, config, frame, t, face, block, prev_t, prev_face, pr
     lib().vpto_temporal(C.byref(_as(OCamera, cam)), C.byref(_as(OCamera, prev_cam)), C.byref(p),
                         C.byref(_as(OFrame, frame)), *[_p(a) for a in arrs], C.byref(sc), C.byref(sh_), C.byref(so))
     return out
+
+
+def reproject(cam, prev_cam, t) -> tuple:
+    """(world position (H, W, 3), previous texture coordinate (H, W, 2)) of every
+    texel of the hit-distance plane t, as the temporal pass computes them."""
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    H, W = t.shape
+    pos = np.zeros((H, W, 3), np.float32)
+    uv = np.zeros((H, W, 2), np.float32)
+    lib().vpto_reproject(C.byref(_as(OCamera, cam)), C.byref(_as(OCamera, prev_cam)), W, H, _p(t), _p(pos), _p(uv))
+    return pos, uv
 
 
 def variance(cam, config, t, face, temporal_out: dict) -> dict:

@@ -4,6 +4,10 @@ reference tree) with the driver oracle/enkimi_ref.c. TEST INFRASTRUCTURE; a
 no-op when the reference tree is absent (the tests that need the library
 skip then).
 
+The reference tree is taken from the environment variable VPT_REFERENCE_DIR,
+else from the directory `reference` beside this repository's own directory
+(`<repo>/../reference`).
+
     python oracle/build_ref.py
 """
 from __future__ import annotations
@@ -14,7 +18,7 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REFERENCE = Path(os.environ.get("VPT_REFERENCE_DIR", "/root/reference"))
+REFERENCE = Path(os.environ.get("VPT_REFERENCE_DIR") or HERE.parent.parent / "reference")
 ENKI = REFERENCE / "Dependencies" / "enkiMI"
 OUT = HERE / "_ref" / "libenkimi_ref.so"
 

@@ -914,6 +914,44 @@ void vpto_spatial_initial(const vpto_camera* cam, const vpto_params* p,
     }
 }
 
+// u_PrevProjection * u_PrevView (SVGF/TemporalFilter.glsl:61-68), a 4x4
+// product evaluated left to right.
+static void prev_view_proj(const vpto_camera* prev_cam, float* m) {
+    for (int c = 0; c < 4; c++)
+        for (int r = 0; r < 4; r++)
+            m[c * 4 + r] = ((prev_cam->proj[0 * 4 + r] * prev_cam->view[c * 4 + 0] +
+                             prev_cam->proj[1 * 4 + r] * prev_cam->view[c * 4 + 1]) +
+                            prev_cam->proj[2 * 4 + r] * prev_cam->view[c * 4 + 2]) +
+                           prev_cam->proj[3 * 4 + r] * prev_cam->view[c * 4 + 3];
+}
+
+// Reprojection(ProjectPositionPrevious(pos)) (SVGF/TemporalFilter.glsl:61-73):
+// the previous frame's texture coordinate of world position pos.
+static inline v2 reproject(const float* m, v4 pos) {
+    v4 pr = mat_mul4(m, pos.x, pos.y, pos.z, 1.0f);
+    return v2{(pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f};
+}
+
+// The world position GetPositionAt gives each texel of the hit-distance plane
+// t and its reprojected coordinate, as the temporal pass computes them.
+void vpto_reproject(const vpto_camera* cam, const vpto_camera* prev_cam, int W, int H, const float* t, float* pos,
+                    float* uv_prev) {
+    const Plane T{t, W, H, 1};
+    float m[16];
+    prev_view_proj(prev_cam, m);
+    for (int j = 0; j < H; j++)
+        for (int i = 0; i < W; i++) {
+            const size_t px = (size_t)j * W + i;
+            const v4 bp = position_fetch(cam, T, i, j, texcoord(i, j, W, H));
+            const v2 rc = reproject(m, bp);
+            pos[px * 3 + 0] = bp.x;
+            pos[px * 3 + 1] = bp.y;
+            pos[px * 3 + 2] = bp.z;
+            uv_prev[px * 2 + 0] = rc.x;
+            uv_prev[px * 2 + 1] = rc.y;
+        }
+}
+
 // SVGF/TemporalFilter.glsl main (:132-360)
 void vpto_temporal(const vpto_camera* cam, const vpto_camera* prev_cam, const vpto_params* p,
                    const vpto_frame* f,
@@ -926,14 +964,8 @@ void vpto_temporal(const vpto_camera* cam, const vpto_camera* prev_cam, const vp
     const Plane8 F{face, W, H}, B{block, W, H}, PF{prev_face, p->width, p->height}, PB{prev_block, p->width, p->height};
     const Plane PSH{prev->sh, W, H, 4}, PCC{prev->cocg, W, H, 2}, PU{prev->util, W, H, 4}, PAO{prev->aosky, W, H, 2};
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
-    // u_PrevProjection * u_PrevView, a 4x4 product evaluated left to right.
     float m[16];
-    for (int c = 0; c < 4; c++)
-        for (int r = 0; r < 4; r++)
-            m[c * 4 + r] = ((prev_cam->proj[0 * 4 + r] * prev_cam->view[c * 4 + 0] +
-                             prev_cam->proj[1 * 4 + r] * prev_cam->view[c * 4 + 1]) +
-                            prev_cam->proj[2 * 4 + r] * prev_cam->view[c * 4 + 2]) +
-                           prev_cam->proj[3 * 4 + r] * prev_cam->view[c * 4 + 3];
+    prev_view_proj(prev_cam, m);
     const float weights[5] = {3.0f / 32.0f, 3.0f / 32.0f, 9.0f / 64.0f, 3.0f / 32.0f, 3.0f / 32.0f};
     const int offs[5][2] = {{1, 0}, {0, 1}, {0, 0}, {-1, 0}, {0, -1}};
     const bool be_useful = f->temporal != 0;
@@ -948,8 +980,7 @@ void vpto_temporal(const vpto_camera* cam, const vpto_camera* prev_cam, const vp
             float bsh[4], bcc[2], bao[2];
             for (int c = 0; c < 4; c++) bsh[c] = cur->sh[px * 4 + c];
             for (int c = 0; c < 2; c++) { bcc[c] = cur->cocg[px * 2 + c]; bao[c] = cur->aosky[px * 2 + c]; }
-            v4 pr = mat_mul4(m, bp.x, bp.y, bp.z, 1.0f);
-            v2 rc = v2{(pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f};
+            v2 rc = reproject(m, bp);
             float base_lum = cur->luma[px];
             int base_block = std::min(std::max((int)B.at(i, j), 0), 127);
             float tol = 0.75f;

@@ -155,6 +155,12 @@ void vpto_spatial_initial(const vpto_camera* cam, const vpto_params* p,
                           const float* t, const uint8_t* face, const vpto_gi* in, vpto_gi* out);
 
 /* SVGF/TemporalFilter.glsl */
+/* ProjectPositionPrevious / Reprojection (SVGF/TemporalFilter.glsl:61-73) of
+ * every texel of the W x H hit-distance plane t, as the temporal pass computes
+ * them: the world position (3 floats per texel) and the previous frame's
+ * texture coordinate (2 floats per texel). */
+void vpto_reproject(const vpto_camera* cam, const vpto_camera* prev_cam, int W, int H, const float* t, float* pos,
+                    float* uv_prev);
 void vpto_temporal(const vpto_camera* cam, const vpto_camera* prev_cam, const vpto_params* p,
                    const vpto_frame* f,
                    const float* t, const uint8_t* face, const uint8_t* block,

@@ -352,17 +352,31 @@ __global__ void __launch_bounds__(128) k_trace_frame(FrameTraceArgs a) {
     }
 }
 
+// Resident-grid size (SMs x resident blocks of 128 threads) of one kernel
+// instantiation, looked up once per device: devices of different models get
+// their own grid, and concurrent first calls are serialised by the mutex.
+constexpr int kMaxGridDevices = 64;
+
 template <typename S, bool STATS>
 cudaError_t launch_frame(const FrameTraceArgs& a, int blocks_hint, cudaStream_t s) {
-    static int blocks_per_sm = 0, sms = 0;
-    if (blocks_per_sm == 0) {
+    static int grid[kMaxGridDevices];
+    static std::mutex mu;
+    int blocks = blocks_hint;
+    if (blocks <= 0) {
         int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace_frame<S, STATS>, 128, 0);
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        if (dev < 0 || dev >= kMaxGridDevices) return cudaErrorInvalidDevice;
+        std::lock_guard<std::mutex> lock(mu);
+        if (grid[dev] == 0) {
+            int sms = 0, per_sm = 0;
+            e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_frame<S, STATS>, 128, 0);
+            if (e != cudaSuccess) return e;
+            grid[dev] = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+        }
+        blocks = grid[dev];
     }
-    int blocks = blocks_hint > 0 ? blocks_hint : sms * blocks_per_sm;
     k_trace_frame<S, STATS><<<blocks, 128, 0, s>>>(a);
     return cudaGetLastError();
 }
@@ -395,7 +409,10 @@ std::mutex g_noalloc_mu;
 
 // Device address of the scratch array on the current device. Host code may
 // not use &g_noalloc_scratch (that is a host-side stand-in), so the address is
-// looked up once per device, with that device current.
+// looked up once per device, with that device current, and kept for the life
+// of the process: after a cudaDeviceReset of that device the module and its
+// array are reloaded elsewhere, so the library must not be called on a
+// device that was reset.
 vpt_status noalloc_scratch(int** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -431,6 +448,9 @@ extern "C" vpt_status vpt_trace_frame_noalloc(const vpt_trace_buffers* b, const 
         return VPT_ERR_INVALID_ARG;
     // the work-queue counter indexes 8x4-pixel tiles * 32 entries in an int
     if (cfg->width <= 0 || cfg->height <= 0 || cfg->width > 16384 || cfg->height > 16384) return VPT_ERR_INVALID_ARG;
+    // every plane, the GI ones included, is width x height: the coarser GI
+    // grid of gi_divisor > 1 is not traced by the fused kernel
+    if (cfg->gi_divisor > 1) return VPT_ERR_INVALID_ARG;
     if ((cfg->storage != VPT_STORAGE_F32 && cfg->storage != VPT_STORAGE_F16) || cfg->spp < 1 || cfg->spp > 32 ||
         cfg->bounces < 0 || cfg->bounces > 8 || cfg->primary_max_steps < 0 || cfg->shadow_max_steps < 0 ||
         cfg->diffuse_max_steps < 0 || cfg->bounce_shadow_max_steps < 0)

@@ -60,3 +60,34 @@ def make_gt_context(width: int, height: int, vox, blocks, textures=None, **cfg) 
     if textures is not None:
         ctx.set_block_textures(textures)
     return ctx
+
+
+def error_by_history(ctx: Context, gt_ctx: Context, cameras, frames, crop, sample_at, spp: int = 1024) -> dict:
+    """RMSE against the FP64 ground truth as the temporal history grows.
+
+    Renders frame k = 0, 1, ... with cameras[k] / frames[k] through ctx (its
+    history carried) and, at every k in sample_at, compares on `crop` the
+    denoised colour (SVGF or the plain a-trous path), the colour shaded from the
+    temporally accumulated GI before any spatial filter, and the colour shaded
+    from this frame's raw 1-spp GI with the ground-truth colour of that frame
+    (gt_ctx, an fp32 context of the same world). Returns {k: {denoised,
+    temporal, raw}}."""
+    x0, y0, w, h = crop
+    out = {}
+    for k in range(max(sample_at) + 1):
+        cam, frame = cameras[k], frames[k]
+        ctx.trace_primary(cam)
+        ctx.trace_shadow(frame)
+        ctx.trace_diffuse(frame)
+        ctx.svgf(cameras[k - 1] if k > 0 else cam, frame)
+        if k in sample_at:
+            row = {}
+            for name, source in (("temporal", 1), ("raw", 2), ("denoised", 0)):
+                ctx.shade_from(frame, source)
+                row[name] = ctx.read_plane("COLOR")[y0:y0 + h, x0:x0 + w].astype(np.float64)
+            gt, _ = ground_truth_color(gt_ctx, cam, frame, crop, spp=spp)
+            out[k] = {name: rmse(img, gt) for name, img in row.items()}
+        else:
+            ctx.shade(frame)
+        ctx.end_frame()
+    return out
