@@ -386,6 +386,8 @@ def run_ours(args):
         quality_out["error_by_history"] = {"crop": list(quality.DEFAULT_CROP_1080P), "gt_spp": args.gt_spp,
                                            "rmse_by_frame": curves}
 
+    df_out = df_section(vpt, torch, local, flush, peak) if not args.no_df else None
+
     batched = None
     if not args.no_batch:
         batched = batched_section(vpt, torch, args, local, flush)
@@ -438,6 +440,7 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": per_launch_bytes,
                      "kernels": {KERNEL_NAMES[k]: v for k, v in kernels.items()}},
         "clocks": clk,
+        "distance_field": df_out,
         "variants": variant,
         "quality": quality_out,
         "batched": batched,
@@ -446,6 +449,41 @@ def run_ours(args):
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------- distance field --
+def df_section(vpt, torch, local, flush, peak):
+    """The distance-field build (x, y and z sweeps) of the 256^3 and 512^3
+    worlds through vpt_df_build_device: median of 10 builds, L2 flushed
+    between them. Algorithmic bytes: 1 read + 1 write per voxel per sweep."""
+    import ctypes as C
+    out = {}
+    stream = torch.cuda.Stream(device=local)
+    for edge in (256, 512):
+        vox = vpt.generate_world(edge, edge, edge, seed=0)
+        d_vox = torch.from_numpy(vox.reshape(-1)).to(f"cuda:{local}")
+        d_df = torch.empty_like(d_vox)
+        ms = []
+        with torch.cuda.stream(stream):
+            for k in range(13):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                st = vpt.lib.vpt_df_build_device(C.c_void_p(d_vox.data_ptr()), C.c_void_p(d_df.data_ptr()), edge,
+                                                 edge, edge, C.c_void_p(stream.cuda_stream))
+                e1.record(stream)
+                e1.synchronize()
+                if st != vpt.OK:
+                    raise RuntimeError(f"vpt_df_build_device failed: {st}")
+                if k >= 3:
+                    ms.append(e0.elapsed_time(e1))
+        med = float(statistics.median(ms))
+        alg = 3 * 2 * edge ** 3
+        gbs = alg / (med * 1e-3) / 1e9
+        out[f"{edge}^3"] = {"ms": med, "launches": 3, "algorithmic_bytes": alg, "achieved_gbs": gbs,
+                            "frac": gbs / peak}
+        del d_vox, d_df
+    return out
 
 
 # ------------------------------------------------------- batched worlds --
@@ -841,6 +879,7 @@ def main():
     ap.add_argument("--no-variants", action="store_true", help="skip the FP16-storage variant")
     ap.add_argument("--no-quality", action="store_true", help="skip the ground-truth error measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-world batched comparison")
+    ap.add_argument("--no-df", action="store_true", help="skip the distance-field build timing")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-denoiser measurements")
     ap.add_argument("--no-large", action="store_true", help="skip the 512^3 / 3840x2160 combined run")
     ap.add_argument("--gt-spp", type=int, default=4096, help="samples per pixel of the FP64 ground truth")

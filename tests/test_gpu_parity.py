@@ -70,7 +70,13 @@ def test_distance_field_bit_exact(vpt, oracle, scene, gpu):
         assert_same(ctx.read_df(), scene["df"], "distance field")
 
 
-@pytest.mark.parametrize("dims", [(16, 16, 16), (37, 21, 50), (200, 40, 9), (1, 1, 1), (64, 1, 3)])
+# shapes for both paths of the build: the 128-bit one (X % 16 == 0, X <= 1024:
+# one to 32 rows per warp, lanes without a segment, two segments per lane,
+# lines along y / z from 1 to 1536 voxels, tiles narrower than 64 bytes) and
+# the generic one (other X, lines over 1536)
+@pytest.mark.parametrize("dims", [(16, 16, 16), (37, 21, 50), (200, 40, 9), (1, 1, 1), (64, 1, 3), (48, 20, 30),
+                                  (1024, 8, 6), (528, 5, 7), (80, 33, 17), (16, 1536, 2), (32, 3, 800),
+                                  (2048, 2, 2), (96, 1537, 1), (272, 12, 12)])
 def test_distance_field_shapes(vpt, oracle, dims, gpu):
     X, Y, Z = dims
     rng = np.random.default_rng(sum(dims))

@@ -1,9 +1,10 @@
 """Bit-exact parity of whole frames at the benchmark's own sizes.
 
 The other parity tests run small images; these render the two measured
-configurations at full size through the frame call the benchmark times
-(vpt_render_frame) and compare every plane the frame writes against the
-oracle's restatement of the same frame (Core/Pipeline.cpp:1959-3821):
+configurations at full size, pass by pass in the order vpt_render_frame runs
+them (primary, shadow and diffuse traces, SVGF, colour pass, end of frame),
+and compare every plane each frame writes against the oracle's restatement
+of the same frame (Core/Pipeline.cpp:1959-3821):
 
 * the full-frame workload: the 256^3 world of seed 0, 1920x1080, 1 spp,
   sun shadow, one diffuse bounce with its shadow ray, SVGF (pre-temporal 3x3,
@@ -26,29 +27,26 @@ from test_gpu_parity import assert_same
 pytestmark = pytest.mark.gpu
 
 
-def compare_frame(ctx, ref, rgb, what):
-    """Every plane of a rendered frame (after its end_frame swap) against the
+def compare_frame(ctx, ref, what):
+    """Every plane of a rendered frame (before its end_frame swap) against the
     oracle's frame dict."""
     g = ref["g"]
-    for name, plane in (("t", "PREV_T"), ("face", "PREV_FACE"), ("block", "PREV_BLOCK")):
+    for name, plane in (("t", "T"), ("face", "FACE"), ("block", "BLOCK"), ("hit", "HIT"), ("steps", "STEPS")):
         assert_same(ctx.read_plane(plane), g[name], f"{what}: G-buffer {name}")
-    assert_same(ctx.read_plane("HIT"), g["hit"], f"{what}: hit voxel")
-    assert_same(ctx.read_plane("STEPS"), g["steps"], f"{what}: step count")
     assert_same(ctx.read_plane("SHADOW"), ref["shadow"], f"{what}: sun shadow")
     for k in ("sh", "cocg", "luma", "aosky"):
         assert_same(ctx.read_plane("GI_" + k.upper()), ref["gi"][k], f"{what}: diffuse GI {k}")
     sv = ref["svgf"]
     for k in ("sh", "cocg", "luma", "aosky"):
         assert_same(ctx.read_plane("PRE_" + k.upper()), sv["pre"][k], f"{what}: pre-temporal {k}")
-    for k in ("sh", "cocg", "util", "aosky"):   # this frame's temporal output is the history after the swap
-        assert_same(ctx.read_plane("HIST_" + k.upper()), sv["temporal"][k], f"{what}: temporal {k}")
+    for k in ("sh", "cocg", "util", "aosky"):
+        assert_same(ctx.read_plane("TEMP_" + k.upper()), sv["temporal"][k], f"{what}: temporal {k}")
     for k in ("sh", "cocg", "variance"):
         assert_same(ctx.read_plane("VAR_" + k.upper()), sv["variance"][k], f"{what}: variance {k}")
     last = sv["atrous"][-1]
     for k in ("sh", "cocg", "variance", "aosky"):
         assert_same(ctx.read_plane("DEN_" + k.upper()), last[k], f"{what}: a-trous {k}")
-    assert_same(ctx.read_plane("COLOR"), ref["rgb"], f"{what}: colour plane")
-    assert_same(rgb, ref["rgb"], f"{what}: image read back")
+    assert_same(ctx.read_plane("COLOR"), ref["rgb"], f"{what}: colour")
 
 
 def render_and_compare(vpt, oracle, vox, blocks, cams, frames, what, **cfg):
@@ -64,9 +62,14 @@ def render_and_compare(vpt, oracle, vox, blocks, cams, frames, what, **cfg):
         prev_cam = cams[0]
         hits = []
         for fi, (cam, frame) in enumerate(zip(cams, frames)):
-            rgb = ctx.render_frame(cam, frame)
+            ctx.trace_primary(cam)
+            ctx.trace_shadow(frame)
+            ctx.trace_diffuse(frame)
+            ctx.svgf(prev_cam, frame)
+            ctx.shade(frame)
             ref = oracle.render_frame(world, cam, prev_cam, c, frame, prev_g, hist)
-            compare_frame(ctx, ref, rgb, f"{what} frame {fi}")
+            compare_frame(ctx, ref, f"{what} frame {fi}")
+            ctx.end_frame()
             hits.append(float((ref["g"]["t"] > 0).mean()))
             prev_g = {k: ref["g"][k] for k in ("t", "face", "block")}
             hist = ref["svgf"]["temporal"]

@@ -3,13 +3,23 @@
 //
 // The reference runs three dependent sweeps with one thread per row/column and
 // image load/store. Its result is min(min(254, X+Y+Z), L1 distance to the
-// nearest non-air voxel); these kernels produce the same bytes:
-//   x: one warp per row, segmented nearest-solid search with warp shuffles;
-//   y, z: one thread per column, forward/backward min(d, d_prev + 1) sweeps
-//         with the running value in a register; a warp covers 32 consecutive
-//         x, so every row access is one coalesced 32-byte sector.
-// The x sweep reads the volume and writes the field once; the y and z sweeps
-// read the field twice and write it at most twice (L2-resident for <= 256^3).
+// nearest non-air voxel); these kernels produce the same bytes.
+//
+// Vectorised path (X a multiple of 16 up to 1024, lines along y and z up to
+// 1536 voxels, both volumes 16-byte aligned: every benchmark world):
+//   x: k_df_x16 -- each lane owns one 16-byte segment of a row (one 128-bit
+//      load), finds the nearest solid voxel left and right of each byte from
+//      its own segment and a shuffle scan over the row's lanes, and writes the
+//      16 distances with one 128-bit store: one read and one write per voxel;
+//   y, z: k_df_sweep_tile -- a CTA stages a tile of 16..64 consecutive x by
+//      the whole line along y (or z) in shared memory with 128-bit loads,
+//      sweeps it forward and backward there (4 columns per thread, two 16-bit
+//      lanes per register, min(d_prev + 1, d) as one DPX add-min per lane
+//      pair), and writes the tile back with 128-bit stores: one read and one
+//      write per voxel per sweep, all global accesses independent of one
+//      another.
+// Generic path (any X, any alignment): one warp per row with warp shuffles
+// for x; one thread per column with the running value in a register for y, z.
 #include <algorithm>
 
 #include "kernels.cuh"
@@ -106,6 +116,132 @@ __global__ void __launch_bounds__(128) k_df_z(uint8_t* df, int X, int Y, int Z) 
     sweep(df + (size_t)y * X + x, (size_t)X * Y, Z);
 }
 
+// ------------------------------------------------- vectorised full build --
+// x sweep, X % 16 == 0 and X <= 1024. A row of X bytes is S = X / 16
+// segments; L lanes (a power of two >= S, at most 32) work on one row, each on
+// kSegs = ceil(S / L) consecutive segments held in registers, so a warp holds
+// 32 / L rows.
+template <int kSegs>
+__global__ void __launch_bounds__(256) k_df_x16(const uint4* __restrict__ vox, uint4* __restrict__ df, int S,
+                                                int L, int rows, int maxd) {
+    const int lane = threadIdx.x & 31;
+    const int rows_per_warp = 32 / L;
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int sub = lane / L, l = lane % L;                 // row within the warp, lane within the row
+    const int row = warp * rows_per_warp + sub;
+    const bool live = row < rows;
+    // segments [s0, s0 + kSegs) of the row belong to this lane
+    const int s0 = l * kSegs;
+    uint4 v[kSegs];
+#pragma unroll
+    for (int k = 0; k < kSegs; k++)
+        v[k] = (live && s0 + k < S) ? __ldg(vox + (size_t)row * S + s0 + k) : make_uint4(0u, 0u, 0u, 0u);
+    const int NEG = -(1 << 24), POS = 1 << 24;
+    // nearest solid at or left of / at or right of each byte, first within the lane
+    int first = POS, last = NEG;
+#pragma unroll
+    for (int k = kSegs - 1; k >= 0; k--) {
+        const unsigned w[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+#pragma unroll
+        for (int b = 15; b >= 0; b--)
+            if ((w[b >> 2] >> (8 * (b & 3))) & 0xffu) first = (s0 + k) * 16 + b;
+    }
+#pragma unroll
+    for (int k = 0; k < kSegs; k++) {
+        const unsigned w[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+#pragma unroll
+        for (int b = 0; b < 16; b++)
+            if ((w[b >> 2] >> (8 * (b & 3))) & 0xffu) last = (s0 + k) * 16 + b;
+    }
+    // inclusive max-scan of `last` towards the right, min-scan of `first` towards the left, within the row
+    int incl = last, incr = first;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        if (off >= L) break;
+        const int a = __shfl_up_sync(kFull, incl, off, L);   // every lane of the warp gets here
+        const int b = __shfl_down_sync(kFull, incr, off, L);
+        if (l >= off) incl = max(incl, a);
+        if (l + off < L) incr = min(incr, b);
+    }
+    int left = __shfl_up_sync(kFull, incl, 1, L);
+    int right = __shfl_down_sync(kFull, incr, 1, L);
+    if (l == 0) left = NEG;
+    if (l == L - 1) right = POS;
+    // right-to-left pass: distance to the nearest solid at or right of x
+    unsigned char dr[kSegs * 16];
+#pragma unroll
+    for (int k = kSegs - 1; k >= 0; k--) {
+        const unsigned w[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+#pragma unroll
+        for (int b = 15; b >= 0; b--) {
+            const int x = (s0 + k) * 16 + b;
+            if ((w[b >> 2] >> (8 * (b & 3))) & 0xffu) right = x;
+            dr[k * 16 + b] = (unsigned char)min(maxd, right - x);
+        }
+    }
+    // left-to-right pass, combined and packed
+#pragma unroll
+    for (int k = 0; k < kSegs; k++) {
+        const unsigned w[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+        unsigned o[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+        for (int b = 0; b < 16; b++) {
+            const int x = (s0 + k) * 16 + b;
+            if ((w[b >> 2] >> (8 * (b & 3))) & 0xffu) left = x;
+            const unsigned d = (unsigned)min((int)dr[k * 16 + b], min(maxd, x - left));
+            o[b >> 2] |= d << (8 * (b & 3));
+        }
+        if (live && s0 + k < S) df[(size_t)row * S + s0 + k] = make_uint4(o[0], o[1], o[2], o[3]);
+    }
+}
+
+// y or z sweep over a tile: x in [x0, x0 + w) (w a multiple of 16, at most
+// kTile) and the whole line of n samples `stride` bytes apart, starting at
+// byte base = blockIdx.y * outer + x0. The tile sits in shared memory, row r
+// at r * w; thread t < w / 4 sweeps columns 4t..4t+3.
+constexpr int kTile = 64;
+
+__global__ void __launch_bounds__(128) k_df_sweep_tile(uint8_t* __restrict__ df, int X, int n, size_t stride,
+                                                       size_t outer) {
+    extern __shared__ __align__(16) uint8_t tile[];
+    const int x0 = blockIdx.x * kTile;
+    const int w = min(kTile, X - x0);
+    const int q = w >> 4;   // 16-byte words per row
+    uint8_t* base = df + (size_t)blockIdx.y * outer + x0;
+    for (int k = threadIdx.x; k < n * q; k += blockDim.x) {
+        const int r = k / q, c = k - r * q;
+        reinterpret_cast<uint4*>(tile + (size_t)r * w)[c] =
+            *reinterpret_cast<const uint4*>(base + (size_t)r * stride + 16 * c);
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < (w >> 2)) {
+        unsigned* col = reinterpret_cast<unsigned*>(tile) + threadIdx.x;
+        const int pitch = w >> 2;   // words per row
+        const unsigned one = 0x00010001u;
+        // bytes b0..b3 of a word as 16-bit lanes (b0, b1) and (b2, b3), and back
+        unsigned w0 = col[0];
+        unsigned lo = __byte_perm(w0, 0u, 0x4140), hi = __byte_perm(w0, 0u, 0x4342);
+        for (int r = 1; r < n; r++) {   // ManhattanDistanceY.comp:105-109: d = min(d, d_prev + 1)
+            const unsigned cw = col[(size_t)r * pitch];
+            lo = __viaddmin_u16x2(lo, one, __byte_perm(cw, 0u, 0x4140));
+            hi = __viaddmin_u16x2(hi, one, __byte_perm(cw, 0u, 0x4342));
+            col[(size_t)r * pitch] = __byte_perm(lo, hi, 0x6420);
+        }
+        for (int r = n - 2; r >= 0; r--) {
+            const unsigned cw = col[(size_t)r * pitch];
+            lo = __viaddmin_u16x2(lo, one, __byte_perm(cw, 0u, 0x4140));
+            hi = __viaddmin_u16x2(hi, one, __byte_perm(cw, 0u, 0x4342));
+            col[(size_t)r * pitch] = __byte_perm(lo, hi, 0x6420);
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n * q; k += blockDim.x) {
+        const int r = k / q, c = k - r * q;
+        *reinterpret_cast<uint4*>(base + (size_t)r * stride + 16 * c) =
+            reinterpret_cast<const uint4*>(tile + (size_t)r * w)[c];
+    }
+}
+
 // ------------------------------------------------------ incremental update --
 // An edit of the voxels in box E changes the field only within L1 distance
 // maxd of E, inside the box O = E grown by maxd on every side. Over the sweep
@@ -176,9 +312,49 @@ cudaError_t df_update(const uint8_t* vox, uint8_t* df, int X, int Y, int Z, int 
     return cudaSuccess;
 }
 
+namespace {
+
+constexpr int kSweepSmemMax = 96 * 1024;   // shared memory of one sweep tile: lines of up to 1536 voxels
+
+template <int kSegs>
+cudaError_t launch_x16(const uint8_t* vox, uint8_t* df, int X, int rows, int maxd, cudaStream_t s) {
+    const int S = X / 16;
+    int L = 1;
+    while (L < S && L < 32) L <<= 1;
+    const long long threads = (long long)(rows + 32 / L - 1) / (32 / L) * 32;
+    k_df_x16<kSegs><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+        reinterpret_cast<const uint4*>(vox), reinterpret_cast<uint4*>(df), S, L, rows, maxd);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sweep_tile(uint8_t* df, int X, int n, size_t stride, size_t outer, int lines, cudaStream_t s) {
+    const size_t smem = (size_t)n * kTile;
+    cudaError_t e = cudaSuccess;
+    if (smem > 48 * 1024) {   // lines longer than 768 voxels: opt in to more shared memory (current device)
+        e = cudaFuncSetAttribute(k_df_sweep_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, kSweepSmemMax);
+        if (e != cudaSuccess) return e;
+    }
+    k_df_sweep_tile<<<dim3((unsigned)((X + kTile - 1) / kTile), (unsigned)lines), 128, smem, s>>>(df, X, n, stride,
+                                                                                                  outer);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
 cudaError_t df_build(const uint8_t* vox, uint8_t* df, int X, int Y, int Z, cudaStream_t s, int* launches) {
     const int maxd = min(254, X + Y + Z);   // ManhattanDistanceX.comp:51
     const int rows = Y * Z;
+    const bool vec = X % 16 == 0 && X <= 16 * 32 * 2 && ((uintptr_t)vox & 15u) == 0 && ((uintptr_t)df & 15u) == 0 &&
+                     (size_t)std::max(Y, Z) * kTile <= (size_t)kSweepSmemMax;
+    if (vec) {
+        cudaError_t e = X <= 16 * 32 ? launch_x16<1>(vox, df, X, rows, maxd, s) : launch_x16<2>(vox, df, X, rows, maxd, s);
+        if (e != cudaSuccess) return e;
+        // y lines: for each z, X * Y bytes; z lines: for each y, stride X * Y
+        if ((e = launch_sweep_tile(df, X, Y, (size_t)X, (size_t)X * Y, Z, s)) != cudaSuccess) return e;
+        if ((e = launch_sweep_tile(df, X, Z, (size_t)X * Y, (size_t)X, Y, s)) != cudaSuccess) return e;
+        if (launches) *launches += 3;
+        return cudaSuccess;
+    }
     k_df_x<<<(unsigned)((rows + 7) / 8), 256, 0, s>>>(vox, df, X, rows, maxd);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
