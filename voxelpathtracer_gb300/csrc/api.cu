@@ -971,8 +971,9 @@ vpt_status vpt_ground_truth(vpt_ctx* c, const vpt_frame* f, int32_t x0, int32_t 
 vpt_status vpt_set_tuning(vpt_ctx* c, const vpt_tuning* t) {
     if (!c || !t) return VPT_ERR_INVALID_ARG;
     if (t->refill_threshold < 1 || t->refill_threshold > 32 || t->trace_blocks < 0 || t->trace_blocks > 65535 ||
-        t->fused_trace < 0 || t->fused_trace > 1)
-        return fail(c, VPT_ERR_INVALID_ARG, "refill_threshold must be 1..32, trace_blocks 0..65535, fused_trace 0/1");
+        t->fused_trace < 0 || t->fused_trace > 1 || t->split_prefilter < 0 || t->split_prefilter > 1)
+        return fail(c, VPT_ERR_INVALID_ARG,
+                    "refill_threshold must be 1..32, trace_blocks 0..65535, fused_trace and split_prefilter 0/1");
     c->tuning = *t;
     return VPT_OK;
 }
@@ -1033,12 +1034,15 @@ vpt_status svgf_run(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f, 
         c->launches += 2 + (uint64_t)io.iterations;
         return VPT_OK;
     }
-    // Spatial3x3Initial (Core/Pipeline.cpp:2288-2330)
-    pass_begin(c, VPT_PASS_SPATIAL_INITIAL);
-    CK(c, svgf_spatial_initial(cv, W, H, c->fp16, t, face, GIIn{c->gi[GI_SH], c->gi[GI_COCG], c->gi[GI_LUMA], c->gi[GI_AOSKY]},
-                               GIOut{c->pre[GI_SH], c->pre[GI_COCG], c->pre[GI_LUMA], c->pre[GI_AOSKY]}, c->stream));
-    pass_end(c, VPT_PASS_SPATIAL_INITIAL);
-    // temporal (:2334-2436)
+    // Spatial3x3Initial (Core/Pipeline.cpp:2288-2330) and temporal (:2334-2436)
+    const GIIn gin{c->gi[GI_SH], c->gi[GI_COCG], c->gi[GI_LUMA], c->gi[GI_AOSKY]};
+    const GIOut pre{c->pre[GI_SH], c->pre[GI_COCG], c->pre[GI_LUMA], c->pre[GI_AOSKY]};
+    if (c->tuning.split_prefilter) {
+        pass_begin(c, VPT_PASS_SPATIAL_INITIAL);
+        CK(c, svgf_spatial_initial(cv, W, H, c->fp16, t, face, gin, pre, c->stream));
+        pass_end(c, VPT_PASS_SPATIAL_INITIAL);
+        c->launches += 1;
+    }
     TemporalArgs ta;
     for (int col = 0; col < 4; col++)
         for (int r = 0; r < 4; r++)
@@ -1050,17 +1054,22 @@ vpt_status svgf_run(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f, 
     HistIO hout{c->hist[cur][HI_SH], c->hist[cur][HI_COCG], c->hist[cur][HI_UTIL], c->hist[cur][HI_AOSKY]};
     HistIO hprev{c->hist[prv][HI_SH], c->hist[prv][HI_COCG], c->hist[prv][HI_UTIL], c->hist[prv][HI_AOSKY]};
     pass_begin(c, VPT_PASS_TEMPORAL);
-    CK(c, svgf_temporal(cv, W, H, Wf, Hf, c->fp16, ta, t, face, block, c->gbuf[prv][GB_T],
-                        (const uint8_t*)c->gbuf[prv][GB_FACE], (const uint8_t*)c->gbuf[prv][GB_BLOCK],
-                        GIIn{c->pre[GI_SH], c->pre[GI_COCG], c->pre[GI_LUMA], c->pre[GI_AOSKY]}, hprev, hout,
-                        c->stream));
+    if (c->tuning.split_prefilter)
+        CK(c, svgf_temporal(cv, W, H, Wf, Hf, c->fp16, ta, t, face, block, c->gbuf[prv][GB_T],
+                            (const uint8_t*)c->gbuf[prv][GB_FACE], (const uint8_t*)c->gbuf[prv][GB_BLOCK],
+                            GIIn{c->pre[GI_SH], c->pre[GI_COCG], c->pre[GI_LUMA], c->pre[GI_AOSKY]}, hprev, hout,
+                            c->stream));
+    else   // the pre-filter fused into the temporal kernel
+        CK(c, svgf_pre_temporal(cv, W, H, Wf, Hf, c->fp16, ta, t, face, block, c->gbuf[prv][GB_T],
+                                (const uint8_t*)c->gbuf[prv][GB_FACE], (const uint8_t*)c->gbuf[prv][GB_BLOCK], gin,
+                                pre, hprev, hout, c->stream));
     pass_end(c, VPT_PASS_TEMPORAL);
     // variance (:2438-2475)
     pass_begin(c, VPT_PASS_VARIANCE);
     CK(c, svgf_variance(cv, W, H, c->fp16, t, face, hout, FiltIO{c->var[FI_SH], c->var[FI_COCG], c->var[FI_VAR], nullptr},
                         c->stream));
     pass_end(c, VPT_PASS_VARIANCE);
-    c->launches += 3;
+    c->launches += 2;
     if (!atrous) return VPT_OK;
     // a-trous iterations with steps 16, 8, 4, 2, 1 (:2481-2610)
     const float tmod = f->time * 100.493850275f;

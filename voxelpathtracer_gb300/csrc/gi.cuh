@@ -12,6 +12,21 @@ struct GICount {
     unsigned diffuse_rays, diffuse_steps, shadow_rays, shadow_steps;
 };
 
+// How calculate_diffuse gets its traversals. kLive: it traces the bounce and
+// shadow rays itself. The staged one-bounce kernel splits a sample in three:
+// kBounceOnly traces the first bounce ray, reports its hit (StagedBounce) and
+// whether a sun-shadow ray is needed from where, and stops; the shadow rays
+// are traced separately; kGiven then runs the whole sample again with that
+// bounce hit and shadow result supplied instead of tracing, so every value
+// comes out of the same arithmetic as in kLive.
+enum DiffuseMode { kDiffuseLive = 0, kDiffuseBounceOnly = 1, kDiffuseGiven = 2 };
+
+struct StagedBounce {
+    float t;        // hit distance of the first bounce ray (-1: miss)
+    int face;       // normal_id of its hit normal
+    int block;      // block id at the hit (0: miss)
+};
+
 // CalculateDiffuse (DiffuseRayTraceFrag.glsl:535-664); B is the distance-field
 // layout. kTex: the bounce hit's albedo, roughness and emission come from the
 // block textures (:569-584): textureLod of the albedo array at level 3 and of
@@ -19,10 +34,16 @@ struct GICount {
 // indexes them, at CalculateUV's coordinates; the emissive texture (texture(),
 // whose implicit derivatives across a pixel quad's unrelated bounce hits are
 // taken as zero) at level 0.
-template <int B = 0, bool kTex = false>
+//
+// kMode (DiffuseMode), for one bounce only: kDiffuseBounceOnly fills *staged,
+// *need_shadow and *shadow_origin and returns; kDiffuseGiven takes *staged
+// and given_shadow (the shadow ray's verdict, 1 = occluded) instead of tracing.
+template <int B = 0, bool kTex = false, int kMode = kDiffuseLive>
 __device__ __forceinline__ v4 calculate_diffuse(const WorldView& w, const DiffuseArgs& a, v3 initial_origin,
                                                 v3 input_normal, uint32_t* rng, v3* odir, bool* skyhit,
-                                                GICount* cnt) {
+                                                GICount* cnt, StagedBounce* staged = nullptr,
+                                                bool* need_shadow = nullptr, v3* shadow_origin = nullptr,
+                                                float given_shadow = 0.0f) {
     const GILighting& L = a.lighting;
     const v3 light_dir = mk3(L.light_dir[0], L.light_dir[1], L.light_dir[2]);
     const v3 light_color = mk3(L.light_color[0], L.light_color[1], L.light_color[2]);
@@ -33,14 +54,31 @@ __device__ __forceinline__ v4 calculate_diffuse(const WorldView& w, const Diffus
     float ao = 1.0f;
     v3 contribution = mk3(0.0f, 0.0f, 0.0f);
     v3 throughput = mk3(1.0f, 1.0f, 1.0f);
-    for (int i = 0; i < a.bounces; i++) {
+    const int bounces = kMode == kDiffuseLive ? a.bounces : 1;
+    for (int i = 0; i < bounces; i++) {
         if (i == 0) *odir = rd;
-        TraceResult tr = traverse<B>(w, ro, rd, a.diffuse_max_steps);
-        cnt->diffuse_rays += 1;
-        cnt->diffuse_steps += (unsigned)tr.steps;
+        TraceResult tr;
+        if (kMode == kDiffuseGiven) {
+            tr.t = staged->t;
+            tr.block = staged->block;
+            tr.normal = staged->block > 0 ? normal_from_id(staged->face, 1.0f) : mk3(0.0f, 0.0f, 0.0f);
+        } else {
+            tr = traverse<B>(w, ro, rd, a.diffuse_max_steps);
+            cnt->diffuse_rays += 1;
+            cnt->diffuse_steps += (unsigned)tr.steps;
+        }
         float T = tr.t;
         bool intersect = T > 0.0f;
         v3 ip = add(ro, muls(rd, T));
+        if (kMode == kDiffuseBounceOnly) {
+            const bool hit = intersect && tr.block > 0;
+            staged->t = T;
+            staged->block = hit ? tr.block : 0;
+            staged->face = hit ? normal_id(tr.normal) : 0;
+            *need_shadow = hit && !L.moon_stronger && !(fmaxf(dot(tr.normal, light_dir), 0.0f) < 0.001f);
+            *shadow_origin = add(ip, muls(tr.normal, 0.045f));
+            return v4{};
+        }
         if (intersect && tr.block > 0) {
             const int bid = min(max(tr.block, 0), 127);
             Material m = material(w, bid);
@@ -71,6 +109,8 @@ __device__ __forceinline__ v4 calculate_diffuse(const WorldView& w, const Diffus
                 shadow_at = 1.0f;
             } else if (ndl < 0.001f) {
                 shadow_at = 0.0f;
+            } else if (kMode == kDiffuseGiven) {
+                shadow_at = given_shadow;
             } else {
                 // GetShadowAt (:1202-1222)
                 TraceResult sr = traverse<B>(w, add(ip, bias_shadow), light_dir, a.bounce_shadow_max_steps);

@@ -235,6 +235,12 @@ cudaError_t svgf_temporal(const CamView& cam, int W, int H, int Wf, int Hf, int 
                           const void* t, const uint8_t* face, const uint8_t* block,
                           const void* prev_t, const uint8_t* prev_face, const uint8_t* prev_block,
                           GIIn cur, HistIO prev, HistIO out, cudaStream_t s);
+// Spatial3x3Initial and the temporal pass fused (one launch; the
+// pre-filtered planes `pre` are written as svgf_spatial_initial writes them).
+cudaError_t svgf_pre_temporal(const CamView& cam, int W, int H, int Wf, int Hf, int fp16, const TemporalArgs& a,
+                              const void* t, const uint8_t* face, const uint8_t* block, const void* prev_t,
+                              const uint8_t* prev_face, const uint8_t* prev_block, GIIn gi, GIOut pre, HistIO prev,
+                              HistIO out, cudaStream_t s);
 cudaError_t svgf_variance(const CamView& cam, int W, int H, int fp16, const void* t, const uint8_t* face,
                           HistIO in, FiltIO out, cudaStream_t s);
 cudaError_t svgf_atrous(const CamView& cam, int W, int H, int Wf, int Hf, int fp16, const AtrousArgs& a,

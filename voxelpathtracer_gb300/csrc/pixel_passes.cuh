@@ -66,15 +66,24 @@ __device__ __forceinline__ uint8_t shadow_pixel(const WorldView& w, const CamVie
 // kOneSample: the caller guarantees one sample (spp <= 1, sun stronger than
 // the moon), so nothing of the per-texel sums stays live across the traversal;
 // the arithmetic is the same.
-template <int B, typename S, bool kOneSample = false, bool kTex = false>
+//
+// kMode (DiffuseMode, gi.cuh) splits a one-sample, one-bounce texel for the
+// staged kernel: kDiffuseBounceOnly traces its bounce ray into *staged (and
+// the shadow-ray request) and writes nothing; kDiffuseGiven finishes it from
+// *staged and given_shadow and writes the outputs. Sky texels (d < 0) are
+// written by kDiffuseLive only.
+template <int B, typename S, bool kOneSample = false, bool kTex = false, int kMode = kDiffuseLive>
 __device__ __forceinline__ void diffuse_pixel(const WorldView& w, const CamView& cam, int W, int H, int i, int j,
                                               const DiffuseArgs& a, size_t px, float d, int face, S* o_sh,
-                                              S* o_cocg, S* o_luma, S* o_aosky, GICount* cnt) {
+                                              S* o_cocg, S* o_luma, S* o_aosky, GICount* cnt,
+                                              StagedBounce* staged = nullptr, bool* need_shadow = nullptr,
+                                              v3* shadow_origin = nullptr, float given_shadow = 0.0f) {
+    static_assert(kMode == kDiffuseLive || kOneSample, "the staged modes run one sample");
     const v3 dir = normalize(ray_dir_at(cam, texcoord(i, j, W, H)));
     const v3 pos = add(ray_origin(cam), muls(dir, d));
     const v3 n = normal_from_id(face, 0.5f);
     float sh[4], cocg[2];
-    if (d < 0.0f) {
+    if (kMode == kDiffuseLive && d < 0.0f) {
         irradiance_to_sh(muls(sky_radiance(dir), 2.66f), n, sh, cocg);
         for (int c = 0; c < 4; c++) st(o_sh + px * 4 + c, sh[c]);
         st(o_cocg + px * 2 + 0, cocg[0]);
@@ -93,7 +102,9 @@ __device__ __forceinline__ void diffuse_pixel(const WorldView& w, const CamView&
     for (int s = 0; s < spp; s++) {
         v3 odir = mk3(0.0f, 0.0f, 0.0f);
         bool ss = false;
-        const v4 x = calculate_diffuse<B, kTex>(w, a, pos, n, &rng, &odir, &ss, cnt);
+        const v4 x = calculate_diffuse<B, kTex, kMode>(w, a, pos, n, &rng, &odir, &ss, cnt, staged, need_shadow,
+                                                        shadow_origin, given_shadow);
+        if (kMode == kDiffuseBounceOnly) return;
         const v3 xc = vclamp(mk3(x.x, x.y, x.z), 0.0f, 8.0f);
         radiance = add(radiance, xc);
         acc_ao += x.w;

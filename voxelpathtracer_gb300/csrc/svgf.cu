@@ -20,19 +20,21 @@ __device__ __forceinline__ bool pixel_of(int W, int H, int* i, int* j) {
     return *i < W && *j < H;
 }
 
-// Spatial3x3Initial.glsl main (:96-176)
+// A value as a plane of storage type S holds it (fp16 planes round to half).
+__device__ __forceinline__ float as_stored(float v, const float*) { return v; }
+__device__ __forceinline__ float as_stored(float v, const __half*) { return __half2float(__float2half_rn(v)); }
+
+// Spatial3x3Initial.glsl main (:96-176) for texel (i, j) with texture
+// coordinate uv and reconstructed position bp; out: SH (4), CoCg (2), AO/sky
+// (2) and the luminance passed through.
 template <typename S>
-__global__ void __launch_bounds__(256) k_spatial_initial(CamView cam, int W, int H, const S* t, const uint8_t* face,
-                                                         const S* sh, const S* cocg, const S* luma, const S* aosky,
-                                                         S* o_sh, S* o_cocg, S* o_luma, S* o_aosky) {
-    int i, j;
-    if (!pixel_of(W, H, &i, &j)) return;
-    const Plane<S, 1> T{t, W, H};
+__device__ __forceinline__ void pre_filter_texel(const CamView& cam, int W, int H, const Plane<S, 1>& T,
+                                                 const uint8_t* face, const S* sh, const S* cocg, const S* luma,
+                                                 const S* aosky, int i, int j, v2 uv, v4 bp, float* o_sh,
+                                                 float* o_cc, float* o_ao, float* o_luma) {
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
     const float aw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
     const size_t px = (size_t)j * W + i;
-    const v2 uv = texcoord(i, j, W, H);
-    const v4 bp = position_fetch(cam, T, i, j, uv);
     const int bf = __ldg(face + px);
     const float nw3 = dpow(3.0f, 16.0f);   // the normal weight of two misses
     const float4 bsh = ld4(sh + 4 * px);
@@ -84,11 +86,31 @@ __global__ void __launch_bounds__(256) k_spatial_initial(CamView cam, int W, int
         }
     }
     tw = fmaxf(tw, 0.01f);
-    st4(o_sh + 4 * px, tsh[0] / tw, tsh[1] / tw, tsh[2] / tw, tsh[3] / tw);
-    st2(o_cocg + 2 * px, tcc[0] / tw, tcc[1] / tw);
+    for (int c = 0; c < 4; c++) o_sh[c] = tsh[c] / tw;
+    o_cc[0] = tcc[0] / tw;
+    o_cc[1] = tcc[1] / tw;
     const float awt = fmaxf(taow, 0.01f);
-    st2(o_aosky + 2 * px, tao[0] / awt, tao[1] / awt);
-    st(o_luma + px, butil);
+    o_ao[0] = tao[0] / awt;
+    o_ao[1] = tao[1] / awt;
+    *o_luma = butil;
+}
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_spatial_initial(CamView cam, int W, int H, const S* t, const uint8_t* face,
+                                                         const S* sh, const S* cocg, const S* luma, const S* aosky,
+                                                         S* o_sh, S* o_cocg, S* o_luma, S* o_aosky) {
+    int i, j;
+    if (!pixel_of(W, H, &i, &j)) return;
+    const Plane<S, 1> T{t, W, H};
+    const size_t px = (size_t)j * W + i;
+    const v2 uv = texcoord(i, j, W, H);
+    const v4 bp = position_fetch(cam, T, i, j, uv);
+    float psh[4], pcc[2], pao[2], pl;
+    pre_filter_texel<S>(cam, W, H, T, face, sh, cocg, luma, aosky, i, j, uv, bp, psh, pcc, pao, &pl);
+    st4(o_sh + 4 * px, psh[0], psh[1], psh[2], psh[3]);
+    st2(o_cocg + 2 * px, pcc[0], pcc[1]);
+    st2(o_aosky + 2 * px, pao[0], pao[1]);
+    st(o_luma + px, pl);
 }
 
 // SVGF/TemporalFilter.glsl main (:132-360). t / face / block: this frame's
@@ -96,30 +118,25 @@ __global__ void __launch_bounds__(256) k_spatial_initial(CamView cam, int W, int
 // G-buffer at its own Wf x Hf, sampled at the reprojected points (kScaled
 // when that grid is finer than the GI grid, so the two need separate
 // bilinear footprints).
+// The temporal pass for texel (i, j) with texture coordinate uv, position bp
+// and this frame's (pre-filtered) SH bsh, CoCg bcc, AO/sky bao and luminance
+// base_lum, as the planes hold them.
 template <typename S, bool kScaled>
-__global__ void __launch_bounds__(256, 4) k_temporal(CamView cam, int W, int H, int Wf, int Hf, TemporalArgs a, const S* t,
-                                                  const uint8_t* face, const uint8_t* block, const S* prev_t,
-                                                  const uint8_t* prev_face, const uint8_t* prev_block,
-                                                  const S* c_sh, const S* c_cocg, const S* c_luma, const S* c_aosky,
-                                                  const S* p_sh, const S* p_cocg, const S* p_util, const S* p_aosky,
-                                                  S* o_sh, S* o_cocg, S* o_util, S* o_aosky) {
-    int i, j;
-    if (!pixel_of(W, H, &i, &j)) return;
-    const Plane<S, 1> T{t, W, H};
+__device__ __forceinline__ void temporal_texel(const CamView& cam, int W, int H, int Wf, int Hf, const TemporalArgs& a,
+                                               const uint8_t* face, const uint8_t* block, const S* prev_t,
+                                               const uint8_t* prev_face, const uint8_t* prev_block, int i, int j,
+                                               v2 uv, v4 bp, float4 bsh, float2 bcc, float2 bao, float base_lum,
+                                               const S* p_sh, const S* p_cocg, const S* p_util, const S* p_aosky,
+                                               S* o_sh, S* o_cocg, S* o_util, S* o_aosky) {
     const Plane8 PF{prev_face, Wf, Hf}, PB{prev_block, Wf, Hf};
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
     const float weights[5] = {3.0f / 32.0f, 3.0f / 32.0f, 9.0f / 64.0f, 3.0f / 32.0f, 3.0f / 32.0f};
     const int offx[5] = {1, 0, 0, -1, 0};
     const int offy[5] = {0, 1, 0, 0, -1};
     const size_t px = (size_t)j * W + i;
-    const v2 uv = texcoord(i, j, W, H);
-    const v4 bp = position_fetch(cam, T, i, j, uv);
     const v3 bn = normal_from_id(__ldg(face + px), 1.0f);
-    const float4 bsh = ld4(c_sh + 4 * px);
-    const float2 bcc = ld2(c_cocg + 2 * px), bao = ld2(c_aosky + 2 * px);
     const v4 pr = mat_mul4(a.prev_view_proj, bp.x, bp.y, bp.z, 1.0f);
     const v2 rc = mk2((pr.x / pr.w) * 0.5f + 0.5f, (pr.y / pr.w) * 0.5f + 0.5f);
-    const float base_lum = ld(c_luma + px);
     const int base_block = min(max((int)__ldg(block + px), 0), 127);
     float tol = 0.75f;
     bool do_block = true, do_normal = true;
@@ -219,6 +236,60 @@ __global__ void __launch_bounds__(256, 4) k_temporal(CamView cam, int W, int H, 
         clampf(store_luma, -150.0f, 150.0f), 0.0f);
 }
 
+template <typename S, bool kScaled>
+__global__ void __launch_bounds__(256, 4) k_temporal(CamView cam, int W, int H, int Wf, int Hf, TemporalArgs a, const S* t,
+                                                  const uint8_t* face, const uint8_t* block, const S* prev_t,
+                                                  const uint8_t* prev_face, const uint8_t* prev_block,
+                                                  const S* c_sh, const S* c_cocg, const S* c_luma, const S* c_aosky,
+                                                  const S* p_sh, const S* p_cocg, const S* p_util, const S* p_aosky,
+                                                  S* o_sh, S* o_cocg, S* o_util, S* o_aosky) {
+    int i, j;
+    if (!pixel_of(W, H, &i, &j)) return;
+    const Plane<S, 1> T{t, W, H};
+    const size_t px = (size_t)j * W + i;
+    const v2 uv = texcoord(i, j, W, H);
+    const v4 bp = position_fetch(cam, T, i, j, uv);
+    temporal_texel<S, kScaled>(cam, W, H, Wf, Hf, a, face, block, prev_t, prev_face, prev_block, i, j, uv, bp,
+                               ld4(c_sh + 4 * px), ld2(c_cocg + 2 * px), ld2(c_aosky + 2 * px), ld(c_luma + px), p_sh,
+                               p_cocg, p_util, p_aosky, o_sh, o_cocg, o_util, o_aosky);
+}
+
+// Spatial3x3Initial and the temporal pass in one kernel: the temporal pass
+// reads the pre-filtered planes only at its own texel, so each thread filters
+// its texel and goes on with the result, rounded as the planes would store
+// it. The pre-filtered planes are still written (kWritePre) for callers that
+// read them.
+template <typename S, bool kScaled, bool kWritePre>
+__global__ void __launch_bounds__(256, 4) k_pre_temporal(CamView cam, int W, int H, int Wf, int Hf, TemporalArgs a,
+                                                      const S* t, const uint8_t* face, const uint8_t* block,
+                                                      const S* prev_t, const uint8_t* prev_face,
+                                                      const uint8_t* prev_block, const S* g_sh, const S* g_cocg,
+                                                      const S* g_luma, const S* g_aosky, S* c_sh, S* c_cocg,
+                                                      S* c_luma, S* c_aosky, const S* p_sh, const S* p_cocg,
+                                                      const S* p_util, const S* p_aosky, S* o_sh, S* o_cocg,
+                                                      S* o_util, S* o_aosky) {
+    int i, j;
+    if (!pixel_of(W, H, &i, &j)) return;
+    const Plane<S, 1> T{t, W, H};
+    const size_t px = (size_t)j * W + i;
+    const v2 uv = texcoord(i, j, W, H);
+    const v4 bp = position_fetch(cam, T, i, j, uv);
+    float psh[4], pcc[2], pao[2], pl;
+    pre_filter_texel<S>(cam, W, H, T, face, g_sh, g_cocg, g_luma, g_aosky, i, j, uv, bp, psh, pcc, pao, &pl);
+    if (kWritePre) {
+        st4(c_sh + 4 * px, psh[0], psh[1], psh[2], psh[3]);
+        st2(c_cocg + 2 * px, pcc[0], pcc[1]);
+        st2(c_aosky + 2 * px, pao[0], pao[1]);
+        st(c_luma + px, pl);
+    }
+    const S* q = nullptr;
+    temporal_texel<S, kScaled>(
+        cam, W, H, Wf, Hf, a, face, block, prev_t, prev_face, prev_block, i, j, uv, bp,
+        make_float4(as_stored(psh[0], q), as_stored(psh[1], q), as_stored(psh[2], q), as_stored(psh[3], q)),
+        make_float2(as_stored(pcc[0], q), as_stored(pcc[1], q)), make_float2(as_stored(pao[0], q), as_stored(pao[1], q)),
+        as_stored(pl, q), p_sh, p_cocg, p_util, p_aosky, o_sh, o_cocg, o_util, o_aosky);
+}
+
 // SVGF/VarianceEstimate.glsl main (:73-193) with DO_SPATIAL and
 // AGGRESSIVE_DISOCCLUSION_HANDLING on. Only the hit distance of the taps'
 // reconstructed positions is used (the depth weight), so no ray is rebuilt.
@@ -260,11 +331,17 @@ __global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, cons
                 const float2 s2 = ld2(i_cocg + 2 * sp_);
                 const float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
                 const float sl = sh_to_y(ssh);
-                const float nw = fc == 0 ? 0.0f : (fc == 1 ? 1.0f : nw3);
-                const float de = dexp(-fabsf(sd - bd));
-                const float dw = de * de;   // pow(e, 2) for e in [0, 1]
-                const float lw = fabsf(sl - bl) / phi;
-                float wgt = (dexp(-lw) * nw) * dw;
+                // (exp(-lw) * nw) * dw with nw = 0 is 0 (or NaN for a NaN
+                // input), and either becomes the 1.5e-8 floor below: taps
+                // across a face edge skip both exponentials
+                float wgt = 0.0f;
+                if (fc != 0) {
+                    const float nw = fc == 1 ? 1.0f : nw3;
+                    const float de = dexp(-fabsf(sd - bd));
+                    const float dw = de * de;   // pow(e, 2) for e in [0, 1]
+                    const float lw = fabsf(sl - bl) / phi;
+                    wgt = (dexp(-lw) * nw) * dw;
+                }
                 float wgt2 = wgt;
                 wgt = fmaxf(wgt, 0.000000015f);
                 wgt2 = fmaxf(wgt2, 0.0000000015f);
@@ -460,6 +537,19 @@ cudaError_t launch_temporal(const CamView& cam, int W, int H, int Wf, int Hf, co
     return cudaGetLastError();
 }
 
+template <typename S, bool kScaled>
+cudaError_t launch_pre_temporal(const CamView& cam, int W, int H, int Wf, int Hf, const TemporalArgs& a, const void* t,
+                                const uint8_t* face, const uint8_t* block, const void* prev_t,
+                                const uint8_t* prev_face, const uint8_t* prev_block, GIIn gi, GIOut pre, HistIO prev,
+                                HistIO out, cudaStream_t s) {
+    k_pre_temporal<S, kScaled, true><<<grid2(W, H), kBlock2, 0, s>>>(
+        cam, W, H, Wf, Hf, a, (const S*)t, face, block, (const S*)prev_t, prev_face, prev_block, (const S*)gi.sh,
+        (const S*)gi.cocg, (const S*)gi.luma, (const S*)gi.aosky, (S*)pre.sh, (S*)pre.cocg, (S*)pre.luma,
+        (S*)pre.aosky, (const S*)prev.sh, (const S*)prev.cocg, (const S*)prev.util, (const S*)prev.aosky, (S*)out.sh,
+        (S*)out.cocg, (S*)out.util, (S*)out.aosky);
+    return cudaGetLastError();
+}
+
 template <typename S>
 cudaError_t launch_variance(int W, int H, const void* t, const uint8_t* face, HistIO in, FiltIO out, cudaStream_t s) {
     k_variance<S><<<grid2(W, H), kBlock2, 0, s>>>(W, H, (const S*)t, face, (const S*)in.sh, (const S*)in.cocg,
@@ -500,6 +590,22 @@ cudaError_t svgf_temporal(const CamView& cam, int W, int H, int Wf, int Hf, int 
                                                  cur, prev, out, s)
                   : launch_temporal<float, false>(cam, W, H, Wf, Hf, a, t, face, block, prev_t, prev_face, prev_block,
                                                   cur, prev, out, s);
+}
+
+cudaError_t svgf_pre_temporal(const CamView& cam, int W, int H, int Wf, int Hf, int fp16, const TemporalArgs& a,
+                              const void* t, const uint8_t* face, const uint8_t* block, const void* prev_t,
+                              const uint8_t* prev_face, const uint8_t* prev_block, GIIn gi, GIOut pre, HistIO prev,
+                              HistIO out, cudaStream_t s) {
+    const bool scaled = Wf != W || Hf != H;
+    if (fp16)
+        return scaled ? launch_pre_temporal<__half, true>(cam, W, H, Wf, Hf, a, t, face, block, prev_t, prev_face,
+                                                          prev_block, gi, pre, prev, out, s)
+                      : launch_pre_temporal<__half, false>(cam, W, H, Wf, Hf, a, t, face, block, prev_t, prev_face,
+                                                           prev_block, gi, pre, prev, out, s);
+    return scaled ? launch_pre_temporal<float, true>(cam, W, H, Wf, Hf, a, t, face, block, prev_t, prev_face,
+                                                     prev_block, gi, pre, prev, out, s)
+                  : launch_pre_temporal<float, false>(cam, W, H, Wf, Hf, a, t, face, block, prev_t, prev_face,
+                                                      prev_block, gi, pre, prev, out, s);
 }
 
 cudaError_t svgf_variance(const CamView& cam, int W, int H, int fp16, const void* t, const uint8_t* face,

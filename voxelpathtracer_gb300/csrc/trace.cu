@@ -71,6 +71,104 @@ __global__ void __launch_bounds__(256, 8) k_trace_diffuse(WorldView w, CamView c
     }
 }
 
+// The same pass for one sample and one bounce, staged inside the CTA so that
+// rays of one kind fill whole warps (DiffuseRayTraceFrag.glsl main :822-935,
+// CalculateDiffuse :535-664 with one bounce):
+//   0. sky texels (no G-buffer hit) are written at once; texels with a hit are
+//      appended to a list in shared memory (ballot + one atomic per warp, so
+//      each warp's 8x4 patch stays together);
+//   1. one thread per listed texel traces its bounce ray and records the hit
+//      and, when the hit faces the sun, a sun-shadow ray request;
+//   2. one thread per request traces the shadow ray (about one bounce in
+//      eight needs one: without this stage nearly every warp would wait for a
+//      few lanes' shadow rays);
+//   3. one thread per listed texel finishes the sample from the recorded hit
+//      and shadow verdict and writes the GI planes.
+// Outputs and ray counts are those of k_trace_diffuse.
+template <typename S, bool kTex>
+__global__ void __launch_bounds__(256, 6) k_trace_diffuse_staged(WorldView w, CamView cam, int W, int H,
+                                                                  DiffuseArgs a, const S* t, const uint8_t* face,
+                                                                  S* o_sh, S* o_cocg, S* o_luma, S* o_aosky,
+                                                                  Counters* stats) {
+    __shared__ uint32_t s_pix[256];         // listed texels: i | j << 16
+    __shared__ float s_bt[256];             // their bounce hit distance
+    __shared__ uint8_t s_bface[256], s_bblock[256], s_shadow[256];
+    __shared__ float4 s_ray[256];           // shadow ray origin xyz, w = listed texel
+    __shared__ int s_n[2];                  // listed texels, shadow requests
+    const int tid = threadIdx.x, lane = tid & 31;
+    if (tid < 2) s_n[tid] = 0;
+    __syncthreads();
+    GICount cnt = {0u, 0u, 0u, 0u};
+    {
+        int i, j;
+        tile_pixel(&i, &j);
+        bool hit = false;
+        if (i < W && j < H) {
+            const size_t px = (size_t)j * W + i;
+            const float d = ld(t + px);
+            if (d < 0.0f)
+                diffuse_pixel<0, S, true, kTex>(w, cam, W, H, i, j, a, px, d, __ldg(face + px), o_sh, o_cocg, o_luma,
+                                                o_aosky, &cnt);
+            else
+                hit = true;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        int base = 0;
+        if (lane == 0 && m) base = atomicAdd(&s_n[0], __popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (hit) s_pix[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i | ((uint32_t)j << 16);
+    }
+    __syncthreads();
+    const int n_hit = s_n[0];
+    const unsigned part = __ballot_sync(0xffffffffu, tid < n_hit);   // this warp's lanes with a listed texel
+    if (tid < n_hit) {
+        const int i = (int)(s_pix[tid] & 0xffffu), j = (int)(s_pix[tid] >> 16);
+        const size_t px = (size_t)j * W + i;
+        StagedBounce sb;
+        bool need = false;
+        v3 so;
+        diffuse_pixel<0, S, true, kTex, kDiffuseBounceOnly>(w, cam, W, H, i, j, a, px, ld(t + px), __ldg(face + px),
+                                                            o_sh, o_cocg, o_luma, o_aosky, &cnt, &sb, &need, &so);
+        s_bt[tid] = sb.t;
+        s_bface[tid] = (uint8_t)sb.face;
+        s_bblock[tid] = (uint8_t)sb.block;
+        s_shadow[tid] = 0;
+        const unsigned m = __ballot_sync(part, need);
+        if (m) {   // the same for every lane of `part`
+            const int leader = __ffs(m) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(&s_n[1], __popc(m));
+            base = __shfl_sync(part, base, leader);
+            if (need)
+                s_ray[base + __popc(m & ((1u << lane) - 1u))] = make_float4(so.x, so.y, so.z, __int_as_float(tid));
+        }
+    }
+    __syncthreads();
+    if (tid < s_n[1]) {
+        // GetShadowAt (DiffuseRayTraceFrag.glsl:1202-1222)
+        const float4 r = s_ray[tid];
+        const GILighting& L = a.lighting;
+        const TraceResult sr = traverse<0>(w, mk3(r.x, r.y, r.z), mk3(L.light_dir[0], L.light_dir[1], L.light_dir[2]),
+                                           a.bounce_shadow_max_steps);
+        cnt.shadow_rays += 1;
+        cnt.shadow_steps += (unsigned)sr.steps;
+        s_shadow[__float_as_int(r.w)] = sr.t > 0.0f ? 1 : 0;
+    }
+    __syncthreads();
+    if (tid < n_hit) {
+        const int i = (int)(s_pix[tid] & 0xffffu), j = (int)(s_pix[tid] >> 16);
+        const size_t px = (size_t)j * W + i;
+        StagedBounce sb{s_bt[tid], (int)s_bface[tid], (int)s_bblock[tid]};
+        diffuse_pixel<0, S, true, kTex, kDiffuseGiven>(w, cam, W, H, i, j, a, px, ld(t + px), __ldg(face + px), o_sh,
+                                                       o_cocg, o_luma, o_aosky, &cnt, &sb, nullptr, nullptr,
+                                                       s_shadow[tid] ? 1.0f : 0.0f);
+    }
+    if (stats) {
+        count_rays(stats, kRayDiffuse, cnt.diffuse_rays, cnt.diffuse_steps);
+        count_rays(stats, kRayBounceShadow, cnt.shadow_rays, cnt.shadow_steps);
+    }
+}
+
 inline dim3 tile_grid(int W, int H) { return dim3((unsigned)((W + 15) / 16), (unsigned)((H + 15) / 16)); }
 
 template <typename S>
@@ -113,6 +211,18 @@ cudaError_t trace_shadow(const WorldView& w, const CamView& cam, int W, int H, i
 cudaError_t trace_diffuse(const WorldView& w, const CamView& cam, int W, int H, const DiffuseArgs& a, int fp16,
                           const void* t, const uint8_t* face, GIOut out, Counters* stats, cudaStream_t s) {
     const bool one = a.spp <= 1 && !a.lighting.moon_stronger, tex = a.textured != 0;
+    if (one && a.bounces == 1 && W < 65536 && H < 65536) {
+        const dim3 g = tile_grid(W, H);
+        if (fp16)
+            (tex ? k_trace_diffuse_staged<__half, true> : k_trace_diffuse_staged<__half, false>)<<<g, 256, 0, s>>>(
+                w, cam, W, H, a, (const __half*)t, face, (__half*)out.sh, (__half*)out.cocg, (__half*)out.luma,
+                (__half*)out.aosky, stats);
+        else
+            (tex ? k_trace_diffuse_staged<float, true> : k_trace_diffuse_staged<float, false>)<<<g, 256, 0, s>>>(
+                w, cam, W, H, a, (const float*)t, face, (float*)out.sh, (float*)out.cocg, (float*)out.luma,
+                (float*)out.aosky, stats);
+        return cudaGetLastError();
+    }
     if (fp16)
         launch_diffuse<__half>(one, tex, tile_grid(W, H), s, w, cam, W, H, a, t, face, out, stats);
     else
