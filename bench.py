@@ -42,8 +42,6 @@ METRIC = "rays/s DF-DDA + denoised 1080p frame ms, batched/learned vs plain at s
 WORLD = (256, 256, 256)
 RES = (1920, 1080)
 CAM_POS = (128.0, 90.0, 128.0)
-ALG_BYTES_PER_STEP = 32     # one 32-byte sector per DF gather
-ALG_BYTES_PER_RAY = 16      # ray output
 PEAKS_FILE = REPO / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
 TRACE_KINDS = {"primary": ["primary"], "shadow": ["shadow"], "diffuse": ["diffuse", "bounce_shadow"],
@@ -54,14 +52,18 @@ TRACE_KINDS = {"primary": ["primary"], "shadow": ["shadow"], "diffuse": ["diffus
 # planes written once), fp32 / fp16 storage.
 FILTER_BYTES_PER_PX = {
     "spatial_initial": (77, 39),   # t, face, SH, CoCg, luma, AO in; SH, CoCg, luma, AO out
-    "temporal": (144, 74),         # current G-buffer + pre-temporal planes, previous G-buffer + history; history out
+    "temporal": (180, 92),         # fused with the pre-filter: its inputs and outputs (77 / 39) + previous
+                                   # G-buffer, current block, history in and out (less the pre-filtered planes
+                                   # and the t / face it no longer reads twice)
+    "temporal_split": (144, 74),   # the temporal pass alone: current G-buffer + pre-filtered planes, previous
+                                   # G-buffer + history; history out
     "variance": (65, 33),          # t, face, SH, CoCg, util.xy in; SH, CoCg, variance out
     "atrous": (81, 41),            # t, face, util.x, SH, CoCg, variance, AO in; SH, CoCg, variance, AO out
     "shade": (47, 25),             # t, face, block, shadow, SH, CoCg, AO.x in; RGB out
 }
-KERNEL_NAMES = {"primary": "k_trace_primary", "shadow": "k_trace_shadow", "diffuse": "k_trace_diffuse",
+KERNEL_NAMES = {"primary": "k_trace_primary", "shadow": "k_trace_shadow", "diffuse": "k_trace_diffuse_staged",
                 "trace_frame": "k_trace_frame",
-                "spatial_initial": "k_spatial_initial", "temporal": "k_temporal", "variance": "k_variance",
+                "spatial_initial": "k_spatial_initial", "temporal": "k_pre_temporal", "variance": "k_variance",
                 "atrous": "k_atrous", "shade": "k_shade",
                 "reflection": "k_trace_reflection (+ hit blur, temporal and denoiser kernels)"}
 
@@ -245,21 +247,28 @@ def run_ours(args):
     iters = ctx.config.atrous_iterations
     kernels = {}
     mean_pass = {p: ms for p, ms in mean_pass.items() if ms > 0}   # passes this frame path ran
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    l2_gbs = l2_read_roof(torch, local)
     for p, ms in mean_pass.items():
         launches_per_frame = iters if p == "atrous" else 1
-        if p in TRACE_KINDS:
-            b = float(np.mean([sum(st[k] for k in TRACE_KINDS[p]) * ALG_BYTES_PER_STEP +
-                               sum(r[k] for k in TRACE_KINDS[p]) * ALG_BYTES_PER_RAY
-                               for st, r in zip(steps[timed], rays[timed])]))
-        else:
-            b = float(FILTER_BYTES_PER_PX[p][args.storage] * W * H)
-            if p != "shade":   # the GI-side filters run on the GI grid
-                b /= float(args.gi_divisor * args.gi_divisor)
         per_launch_ms = ms / launches_per_frame
+        if p in TRACE_KINDS:
+            # the DDA is bound by instruction issue on L2-resident gathers, not
+            # by HBM: its roof comes from the kernel's ncu summary
+            st_ = float(np.mean([sum(st[k] for k in TRACE_KINDS[p]) for st in steps[timed]]))
+            ry = float(np.mean([sum(r[k] for k in TRACE_KINDS[p]) for r in rays[timed]]))
+            kernels[p] = dict(trace_roofline(KERNEL_NAMES[p], per_launch_ms, st_, ry, sm_count, clk.get("sm_mhz"),
+                                             l2_gbs), launches_per_frame=launches_per_frame,
+                              ms_per_launch=per_launch_ms)
+            continue
+        key = "temporal_split" if p == "temporal" and "spatial_initial" in mean_pass else p
+        b = float(FILTER_BYTES_PER_PX[key][args.storage] * W * H)
+        if p != "shade":   # the GI-side filters run on the GI grid
+            b /= float(args.gi_divisor * args.gi_divisor)
         gbs = b / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
-        kernels[p] = {"launches_per_frame": launches_per_frame, "ms_per_launch": per_launch_ms,
+        kernels[p] = {"bound": "hbm", "launches_per_frame": launches_per_frame, "ms_per_launch": per_launch_ms,
                       "algorithmic_bytes_per_launch": b, "achieved_gbs": gbs, "frac": gbs / peak}
-    dom = max(mean_pass, key=mean_pass.get)
+    dom = max((p for p in mean_pass if p not in TRACE_KINDS), key=mean_pass.get)
     per_launch_bytes = kernels[dom]["algorithmic_bytes_per_launch"]
     achieved = kernels[dom]["achieved_gbs"]
     traffic, traffic_source = args.traffic, "--traffic" if args.traffic is not None else None
@@ -438,6 +447,7 @@ def run_ours(args):
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback", "traffic": traffic, "traffic_source": traffic_source,
                      "algorithmic_bytes_per_launch": per_launch_bytes,
+                     "l2_read_roof_gbs": l2_gbs,
                      "kernels": {KERNEL_NAMES[k]: v for k, v in kernels.items()}},
         "clocks": clk,
         "distance_field": df_out,
@@ -651,6 +661,68 @@ def learned_section(vpt, torch, args, local, flush, vox, blocks, yaw, pitch, pea
 def quality_crop():
     from voxelpathtracer_gb300 import quality
     return quality.DEFAULT_CROP_1080P
+
+
+def profile_metrics(kernel):
+    """Rows of the committed ncu summary profiles/<kernel>_1080p.md, as
+    {metric: value in base units}; {} when there is none."""
+    import re
+    path = Path(__file__).resolve().parent / "profiles" / f"{kernel}_1080p.md"
+    if not path.exists():
+        return {}
+    units = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "inst": 1.0, "us": 1e-6, "ms": 1e-3,
+             "ns": 1e-9, "": 1.0, "%": 1.0}
+    out = {}
+    for m in re.finditer(r"^\| ([^|]+?) \| ([0-9.eE+-]+) \| ([^|]*?) \|$", path.read_text(), re.M):
+        name, val, unit = m.group(1).strip(), m.group(2), m.group(3).strip()
+        if unit in units:
+            out[name] = float(val) * units[unit]
+    out["_source"] = f"profiles/{path.name}"
+    return out
+
+
+def l2_read_roof(torch, local):
+    """Achievable L2 read bandwidth: a sum over a 64 MiB fp32 tensor that stays
+    in the 126 MB L2, median of 20 reductions after warm-up (GB/s)."""
+    x = torch.ones(16 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")
+    for _ in range(5):
+        x.sum()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(20):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        x.sum()
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return x.numel() * 4 / (statistics.median(ms) * 1e-3) / 1e9
+
+
+def trace_roofline(kernel, ms_per_launch, steps, rays, sm_count, sm_mhz, l2_gbs):
+    """The DDA kernels' roofs from their committed ncu summary: instruction
+    issue (warp instructions / event time against SMs x 4 schedulers x the
+    sampled SM clock), L2 -> L1 bytes per DDA step and their rate against the
+    measured L2 read roof, and SIMD efficiency (threads per instruction / 32)."""
+    m = profile_metrics(kernel)
+    if "instructions (warp)" not in m or not sm_mhz:
+        return {"bound": "issue", "frac": None, "note": "no ncu summary for this kernel"}
+    t = ms_per_launch * 1e-3
+    issue = m["instructions (warp)"] / t
+    issue_peak = sm_count * 4 * sm_mhz * 1e6
+    l2l1 = m.get("L2 -> L1 read bytes")
+    out = {"bound": "issue", "unit": "warp instructions/s", "achieved": issue, "peak": issue_peak,
+           "frac": issue / issue_peak, "warp_instructions_per_launch": m["instructions (warp)"],
+           "simd_efficiency": m.get("threads per instruction (of 32)", 0.0) / 32.0,
+           "dda_steps_per_launch": steps, "rays_per_launch": rays, "source": m["_source"]}
+    if l2l1 is not None:
+        out["l2_to_l1_bytes_per_launch"] = l2l1
+        out["l2_to_l1_bytes_per_step"] = l2l1 / max(steps, 1.0)
+        out["l2_to_l1_gbs"] = l2l1 / t / 1e9
+        if l2_gbs:
+            out["l2_roof_gbs"] = l2_gbs
+            out["l2_frac"] = l2l1 / t / 1e9 / l2_gbs
+    return out
 
 
 def profile_traffic(kernel):

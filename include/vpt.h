@@ -442,10 +442,13 @@ typedef struct vpt_batch_config {
 /* Launch shape of the persistent batch kernel (vpt_batch_autotune picks it). */
 typedef struct vpt_batch_tuning {
     int32_t block_threads;           /* 64..512, a multiple of 32 */
-    int32_t tiles_per_grab;          /* 8x4-pixel tiles a warp takes per queue access, 1..16 (rays per warp = 32 x this) */
+    int32_t tiles_per_grab;          /* 8x4-pixel tile pairs (rays_per_lane 2) or tiles a warp takes per queue
+                                        access, 1..16 */
     int32_t df_brick;                /* distance-field layout traced: 0 x-fastest, 4 or 8 = B^3-voxel bricks */
     int32_t blocks;                  /* persistent blocks; 0 = every SM filled to its occupancy limit */
-    int32_t reserved[4];
+    int32_t rays_per_lane;           /* 1: a warp traces 32 pixels at a time; 2: 64 (two tiles of one world), each
+                                        lane's two primary and two shadow traversals interleaved */
+    int32_t reserved[3];
 } vpt_batch_tuning;
 
 typedef struct vpt_batch_tune_record {
@@ -482,8 +485,9 @@ vpt_status vpt_batch_set_tuning(vpt_batch* batch, const vpt_batch_tuning* tuning
 vpt_status vpt_batch_get_tuning(const vpt_batch* batch, vpt_batch_tuning* tuning);
 /* Traces every world with its camera. Stream-ordered; returns without waiting. */
 vpt_status vpt_batch_trace(vpt_batch* batch, const vpt_frame* frame, int32_t mode);
-/* Times every candidate launch shape (block_threads 128/256/512 x
- * tiles_per_grab 1/2/4 x df_brick 0/4/8) on the batch as it stands, `reps`
+/* Times every candidate launch shape (rays_per_lane 1/2 x block_threads
+ * 128/256/512 x tiles_per_grab 1/2/4 x df_brick 0/4/8, 54 in all) on the
+ * batch as it stands, `reps`
  * timed launches each after one warm-up, keeps the fastest as the batch's
  * tuning and writes up to max_records records (all candidates, in the order
  * tried). Synchronises. */

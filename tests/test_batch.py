@@ -68,11 +68,15 @@ def test_batch_distance_fields(vpt, scenes, gpu):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("rays", [1, 2], ids=["1ray", "2rays"])
 @pytest.mark.parametrize("mode", [0, 1, 2], ids=["graph", "persistent", "per_world"])
 @pytest.mark.parametrize("brick", [0, 4, 8])
-def test_batch_bit_exact(vpt, scenes, mode, brick, gpu):
+def test_batch_bit_exact(vpt, scenes, mode, brick, rays, gpu):
+    """Every world's planes equal the oracle's; with two rays per lane a warp's
+    grab of 3 tile pairs crosses world boundaries, so single tiles and pairs
+    both run."""
     with make_batch(vpt, scenes) as b:
-        b.set_tuning(df_brick=brick, tiles_per_grab=3, block_threads=128)
+        b.set_tuning(df_brick=brick, tiles_per_grab=3, block_threads=128, rays_per_lane=rays)
         b.set_stats(True)
         b.trace(scenes[0]["frame"], mode)
         b.synchronize()
@@ -104,12 +108,13 @@ def test_batch_graph_replay_follows_frame_and_camera(vpt, oracle, scenes, gpu):
 def test_batch_autotune(vpt, scenes, gpu):
     with make_batch(vpt, scenes) as b:
         recs = b.autotune(scenes[0]["frame"], reps=2)
-        assert len(recs) == 27
+        assert len(recs) == 54
+        assert {r["rays_per_lane"] for r in recs} == {1, 2}
         assert all(r["ms"] > 0 for r in recs)
         best = min(recs, key=lambda r: r["ms"])
         t = b.tuning().as_dict()
-        assert (t["block_threads"], t["tiles_per_grab"], t["df_brick"]) == (
-            best["block_threads"], best["tiles_per_grab"], best["df_brick"])
+        assert (t["block_threads"], t["tiles_per_grab"], t["df_brick"], t["rays_per_lane"]) == (
+            best["block_threads"], best["tiles_per_grab"], best["df_brick"], best["rays_per_lane"])
         b.trace(scenes[0]["frame"], vpt.BATCH_GRAPH)
         b.synchronize()
         check_all(b, scenes, "after autotune")

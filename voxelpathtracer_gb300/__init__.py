@@ -116,11 +116,12 @@ class BatchConfig(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("block_threads", C.c_int32), ("tiles_per_grab", C.c_int32), ("df_brick", C.c_int32),
-                ("blocks", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("blocks", C.c_int32), ("rays_per_lane", C.c_int32), ("reserved", C.c_int32 * 3)]
 
     def as_dict(self) -> dict:
         return {"block_threads": self.block_threads, "tiles_per_grab": self.tiles_per_grab,
-                "rays_per_warp": 32 * self.tiles_per_grab, "df_brick": self.df_brick, "blocks": self.blocks}
+                "rays_per_lane": self.rays_per_lane, "rays_per_warp": 32 * self.rays_per_lane,
+                "df_brick": self.df_brick, "blocks": self.blocks}
 
 
 class BatchTuneRecord(C.Structure):
@@ -782,10 +783,10 @@ class Batch:
         self._ck(lib.vpt_batch_read_df(self._h, world, _ptr(out), out.nbytes), "vpt_batch_read_df")
         return out
 
-    def set_tuning(self, block_threads=None, tiles_per_grab=None, df_brick=None, blocks=None):
+    def set_tuning(self, block_threads=None, tiles_per_grab=None, df_brick=None, blocks=None, rays_per_lane=None):
         t = self.tuning()
         for k, v in (("block_threads", block_threads), ("tiles_per_grab", tiles_per_grab), ("df_brick", df_brick),
-                     ("blocks", blocks)):
+                     ("blocks", blocks), ("rays_per_lane", rays_per_lane)):
             if v is not None:
                 setattr(t, k, int(v))
         self._ck(lib.vpt_batch_set_tuning(self._h, C.byref(t)), "vpt_batch_set_tuning")

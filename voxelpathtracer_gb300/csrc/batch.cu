@@ -17,51 +17,110 @@ namespace vpt {
 
 namespace {
 
+// Last world whose first tile is <= tile (worlds with no tiles are skipped over).
+__device__ __forceinline__ int world_of(const int* s_begin, int n_worlds, int tile) {
+    int lo = 0, hi = n_worlds - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_begin[mid] <= tile) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Primary, sun-shadow and diffuse passes of one 8x4 tile, one pixel per lane.
 template <int B>
+__device__ __forceinline__ void batch_tile(const BatchLaunch& a, const BatchFrame& fr, const BatchWorld& bw,
+                                           int local, int lane) {
+    const int i = (local % bw.tiles_x) * 8 + (lane & 7);
+    const int j = (local / bw.tiles_x) * 4 + (lane >> 3);
+    const bool valid = i < bw.W && j < bw.H;
+    unsigned psteps = 0, srays = 0, ssteps = 0;
+    GICount cnt = {0u, 0u, 0u, 0u};
+    if (valid) {
+        const WorldView w = bw.w;
+        const CamView& cam = bw.cam;
+        const size_t px = (size_t)j * bw.W + i;
+        float d;
+        int face;
+        psteps = primary_pixel<B>(w, cam, bw.W, bw.H, i, j, fr.primary_max_steps, px, bw.t, bw.face, bw.block, bw.hit,
+                                  bw.steps, &d, &face);
+        bw.shadow[px] = shadow_pixel<B>(w, cam, bw.W, bw.H, i, j, fr.shadow_max_steps,
+                                        mk3(fr.sun[0], fr.sun[1], fr.sun[2]), d, face, &srays, &ssteps);
+        diffuse_pixel<B>(w, cam, bw.W, bw.H, i, j, fr.d, px, d, face, bw.sh, bw.cocg, bw.luma, bw.aosky, &cnt);
+    }
+    if (a.stats) {
+        count_rays(a.stats, kRayPrimary, valid ? 1u : 0u, psteps);
+        count_rays(a.stats, kRayShadow, srays, ssteps);
+        count_rays(a.stats, kRayDiffuse, cnt.diffuse_rays, cnt.diffuse_steps);
+        count_rays(a.stats, kRayBounceShadow, cnt.shadow_rays, cnt.shadow_steps);
+    }
+}
+
+// Two tiles of one world, two pixels per lane: the primary rays and then the
+// sun-shadow rays of both pixels are traced interleaved (two gathers in
+// flight per lane), the diffuse samples one pixel after the other. The same
+// bits as two batch_tile calls.
+template <int B>
+__device__ __forceinline__ void batch_tile_pair(const BatchLaunch& a, const BatchFrame& fr, const BatchWorld& bw,
+                                                int local0, int lane) {
+    int i[2], j[2];
+    bool valid[2];
+    for (int k = 0; k < 2; k++) {
+        const int local = local0 + k;
+        i[k] = (local % bw.tiles_x) * 8 + (lane & 7);
+        j[k] = (local / bw.tiles_x) * 4 + (lane >> 3);
+        valid[k] = i[k] < bw.W && j[k] < bw.H;
+    }
+    const WorldView w = bw.w;
+    const CamView& cam = bw.cam;
+    float d[2] = {-1.0f, -1.0f};
+    int face[2] = {kFaceMiss, kFaceMiss};
+    unsigned psteps[2] = {0u, 0u}, srays = 0, ssteps = 0;
+    GICount cnt = {0u, 0u, 0u, 0u};
+    primary_pixel2<B>(w, cam, bw.W, bw.H, i, j, valid, fr.primary_max_steps, bw.t, bw.face, bw.block, bw.hit, bw.steps,
+                      d, face, psteps);
+    uint8_t sh[2];
+    shadow_pixel2<B>(w, cam, bw.W, bw.H, i, j, valid, fr.shadow_max_steps, mk3(fr.sun[0], fr.sun[1], fr.sun[2]), d,
+                     face, sh, &srays, &ssteps);
+    for (int k = 0; k < 2; k++) {
+        if (!valid[k]) continue;
+        const size_t px = (size_t)j[k] * bw.W + i[k];
+        bw.shadow[px] = sh[k];
+        diffuse_pixel<B>(w, cam, bw.W, bw.H, i[k], j[k], fr.d, px, d[k], face[k], bw.sh, bw.cocg, bw.luma, bw.aosky,
+                         &cnt);
+    }
+    if (a.stats) {
+        count_rays(a.stats, kRayPrimary, (valid[0] ? 1u : 0u) + (valid[1] ? 1u : 0u), psteps[0] + psteps[1]);
+        count_rays(a.stats, kRayShadow, srays, ssteps);
+        count_rays(a.stats, kRayDiffuse, cnt.diffuse_rays, cnt.diffuse_steps);
+        count_rays(a.stats, kRayBounceShadow, cnt.shadow_rays, cnt.shadow_steps);
+    }
+}
+
+// kRays: pixels (rays of a pass) per lane, 1 or 2; a warp takes
+// tiles_per_grab * kRays tiles per queue access.
+template <int B, int kRays>
 __global__ void __launch_bounds__(512, 3) k_batch_trace(BatchLaunch a) {
     __shared__ int s_begin[kBatchMaxWorlds + 1];
     for (int k = threadIdx.x; k <= a.n_worlds; k += blockDim.x) s_begin[k] = a.tile_begin[k];
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const BatchFrame& fr = *a.frame;
+    const int grab = a.tiles_per_grab * kRays;
     for (;;) {
         int base = 0;
-        if (lane == 0) base = atomicAdd(a.queue, a.tiles_per_grab);
+        if (lane == 0) base = atomicAdd(a.queue, grab);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= a.n_tiles) break;
-        const int end = min(base + a.tiles_per_grab, a.n_tiles);
-        for (int tile = base; tile < end; tile++) {
-            // last world whose first tile is <= tile (worlds with no tiles are skipped over)
-            int lo = 0, hi = a.n_worlds - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (s_begin[mid] <= tile) lo = mid; else hi = mid - 1;
-            }
-            const BatchWorld& bw = a.worlds[lo];
-            const int local = tile - s_begin[lo];
-            const int i = (local % bw.tiles_x) * 8 + (lane & 7);
-            const int j = (local / bw.tiles_x) * 4 + (lane >> 3);
-            const bool valid = i < bw.W && j < bw.H;
-            unsigned psteps = 0, srays = 0, ssteps = 0;
-            GICount cnt = {0u, 0u, 0u, 0u};
-            if (valid) {
-                const WorldView w = bw.w;
-                const CamView& cam = bw.cam;
-                const size_t px = (size_t)j * bw.W + i;
-                float d;
-                int face;
-                psteps = primary_pixel<B>(w, cam, bw.W, bw.H, i, j, fr.primary_max_steps, px, bw.t, bw.face,
-                                          bw.block, bw.hit, bw.steps, &d, &face);
-                bw.shadow[px] = shadow_pixel<B>(w, cam, bw.W, bw.H, i, j, fr.shadow_max_steps,
-                                                mk3(fr.sun[0], fr.sun[1], fr.sun[2]), d, face, &srays, &ssteps);
-                diffuse_pixel<B>(w, cam, bw.W, bw.H, i, j, fr.d, px, d, face, bw.sh, bw.cocg, bw.luma, bw.aosky,
-                                 &cnt);
-            }
-            if (a.stats) {
-                count_rays(a.stats, kRayPrimary, valid ? 1u : 0u, psteps);
-                count_rays(a.stats, kRayShadow, srays, ssteps);
-                count_rays(a.stats, kRayDiffuse, cnt.diffuse_rays, cnt.diffuse_steps);
-                count_rays(a.stats, kRayBounceShadow, cnt.shadow_rays, cnt.shadow_steps);
+        const int end = min(base + grab, a.n_tiles);
+        for (int tile = base; tile < end;) {
+            const int lo = world_of(s_begin, a.n_worlds, tile);
+            if (kRays == 2 && tile + 1 < end && world_of(s_begin, a.n_worlds, tile + 1) == lo) {
+                batch_tile_pair<B>(a, fr, a.worlds[lo], tile - s_begin[lo], lane);
+                tile += 2;
+            } else {
+                batch_tile<B>(a, fr, a.worlds[lo], tile - s_begin[lo], lane);
+                tile += 1;
             }
         }
     }
@@ -82,10 +141,10 @@ __global__ void __launch_bounds__(256) k_df_bricks(const uint8_t* __restrict__ d
     out[o] = (x < X && y < Y && z < Z) ? df[(size_t)x + (size_t)X * ((size_t)y + (size_t)Y * z)] : 0;
 }
 
-template <int B>
+template <int B, int kRays>
 int max_blocks_for(int block_threads) {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_trace<B>, block_threads, 0) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_trace<B, kRays>, block_threads, 0) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
@@ -94,27 +153,30 @@ int max_blocks_for(int block_threads) {
 
 }  // namespace
 
-int batch_max_blocks(int df_brick, int block_threads, int device) {
+int batch_max_blocks(int df_brick, int block_threads, int rays_per_lane, int device) {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
-    const int per_sm = df_brick == 4 ? max_blocks_for<4>(block_threads)
-                       : df_brick == 8 ? max_blocks_for<8>(block_threads)
-                                       : max_blocks_for<0>(block_threads);
+    const bool two = rays_per_lane == 2;
+    const int per_sm = df_brick == 4 ? (two ? max_blocks_for<4, 2>(block_threads) : max_blocks_for<4, 1>(block_threads))
+                       : df_brick == 8 ? (two ? max_blocks_for<8, 2>(block_threads) : max_blocks_for<8, 1>(block_threads))
+                                       : (two ? max_blocks_for<0, 2>(block_threads) : max_blocks_for<0, 1>(block_threads));
     return per_sm * sms;
 }
 
-cudaError_t batch_trace(const BatchLaunch& a, int df_brick, int block_threads, int blocks, cudaStream_t s) {
+cudaError_t batch_trace(const BatchLaunch& a, int df_brick, int block_threads, int rays_per_lane, int blocks,
+                        cudaStream_t s) {
     if (a.n_worlds < 1 || a.n_worlds > kBatchMaxWorlds || block_threads < 32 || block_threads > 512 ||
-        (block_threads & 31) || a.tiles_per_grab < 1)
+        (block_threads & 31) || a.tiles_per_grab < 1 || (rays_per_lane != 1 && rays_per_lane != 2))
         return cudaErrorInvalidValue;
     int dev = 0;
     cudaGetDevice(&dev);
-    if (blocks <= 0) blocks = batch_max_blocks(df_brick, block_threads, dev);
+    if (blocks <= 0) blocks = batch_max_blocks(df_brick, block_threads, rays_per_lane, dev);
     if (blocks <= 0) return cudaErrorInvalidConfiguration;
+    const bool two = rays_per_lane == 2;
     switch (df_brick) {
-        case 0: k_batch_trace<0><<<blocks, block_threads, 0, s>>>(a); break;
-        case 4: k_batch_trace<4><<<blocks, block_threads, 0, s>>>(a); break;
-        case 8: k_batch_trace<8><<<blocks, block_threads, 0, s>>>(a); break;
+        case 0: (two ? k_batch_trace<0, 2> : k_batch_trace<0, 1>)<<<blocks, block_threads, 0, s>>>(a); break;
+        case 4: (two ? k_batch_trace<4, 2> : k_batch_trace<4, 1>)<<<blocks, block_threads, 0, s>>>(a); break;
+        case 8: (two ? k_batch_trace<8, 2> : k_batch_trace<8, 1>)<<<blocks, block_threads, 0, s>>>(a); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

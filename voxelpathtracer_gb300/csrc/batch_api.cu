@@ -237,7 +237,8 @@ BatchLaunch launch_args(vpt_batch* b) {
 
 vpt_status launch_persistent(vpt_batch* b) {
     BCK(b, cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream));
-    BCK(b, batch_trace(launch_args(b), b->tuning.df_brick, b->tuning.block_threads, b->tuning.blocks, b->stream));
+    BCK(b, batch_trace(launch_args(b), b->tuning.df_brick, b->tuning.block_threads, b->tuning.rays_per_lane,
+                       b->tuning.blocks, b->stream));
     b->launches += 1;
     return VPT_OK;
 }
@@ -251,7 +252,8 @@ vpt_status launch_graph(vpt_batch* b) {
         cudaGraph_t g = nullptr;
         BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
         cudaError_t e1 = cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream);
-        cudaError_t e2 = batch_trace(launch_args(b), b->tuning.df_brick, b->tuning.block_threads, b->tuning.blocks,
+        cudaError_t e2 = batch_trace(launch_args(b), b->tuning.df_brick, b->tuning.block_threads, b->tuning.rays_per_lane,
+                                     b->tuning.blocks,
                                      b->stream);
         cudaError_t e3 = cudaStreamEndCapture(b->stream, &g);
         if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
@@ -300,7 +302,8 @@ vpt_status launch_per_world(vpt_batch* b, const vpt_frame* f) {
 
 bool valid_tuning(const vpt_batch_tuning& t) {
     return t.block_threads >= 64 && t.block_threads <= 512 && (t.block_threads & 31) == 0 && t.tiles_per_grab >= 1 &&
-           t.tiles_per_grab <= 16 && (t.df_brick == 0 || t.df_brick == 4 || t.df_brick == 8) && t.blocks >= 0;
+           t.tiles_per_grab <= 16 && (t.df_brick == 0 || t.df_brick == 4 || t.df_brick == 8) && t.blocks >= 0 &&
+           (t.rays_per_lane == 1 || t.rays_per_lane == 2);
 }
 
 }  // namespace
@@ -342,6 +345,7 @@ vpt_status vpt_batch_create(vpt_batch** out, const vpt_batch_config* cfg) {
     b->tuning.tiles_per_grab = 1;
     b->tuning.df_brick = 0;
     b->tuning.blocks = 0;
+    b->tuning.rays_per_lane = 1;
     vpt_status s = VPT_OK;
     if (cudaSetDevice(b->dev) != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->frame_copied, cudaEventDisableTiming) != cudaSuccess ||
@@ -512,7 +516,8 @@ vpt_status vpt_batch_autotune(vpt_batch* b, const vpt_frame* f, int32_t reps, vp
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     BCK(b, cudaEventCreate(&e0));
     BCK(b, cudaEventCreate(&e1));
-    const int threads[3] = {128, 256, 512}, grabs[3] = {1, 2, 4}, bricks[3] = {0, 4, 8};
+    const int threads[3] = {128, 256, 512}, grabs[3] = {1, 2, 4}, bricks[3] = {0, 4, 8}, rays[2] = {1, 2};
+    for (int ri = 0; ri < 2 && s == VPT_OK; ri++)
     for (int bi = 0; bi < 3 && s == VPT_OK; bi++) {
         for (int ti = 0; ti < 3 && s == VPT_OK; ti++) {
             for (int gi = 0; gi < 3 && s == VPT_OK; gi++) {
@@ -520,6 +525,7 @@ vpt_status vpt_batch_autotune(vpt_batch* b, const vpt_frame* f, int32_t reps, vp
                 t.df_brick = bricks[bi];
                 t.block_threads = threads[ti];
                 t.tiles_per_grab = grabs[gi];
+                t.rays_per_lane = rays[ri];
                 t.blocks = 0;
                 b->tuning = t;
                 b->graph_valid = false;

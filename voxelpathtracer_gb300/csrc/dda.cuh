@@ -77,10 +77,13 @@ __device__ __forceinline__ void dda_face_step(RayState& r) {
     r.min_idx = m;
 }
 
-// One iteration of the traversal loop; returns true once the loop is over.
-// B is the distance-field layout (df_index).
+// One iteration of the traversal loop in two halves around its one memory
+// access: dda_fetch returns true if the loop ends before the distance-field
+// gather (step cap, or the ray left the volume), else the gather's address;
+// dda_apply takes the gathered distance and returns true once the loop is
+// over. B is the distance-field layout (df_index).
 template <int B = 0>
-__device__ __forceinline__ bool dda_step(const WorldView& w, RayState& r) {
+__device__ __forceinline__ bool dda_fetch(const WorldView& w, RayState& r, int* addr) {
     if (r.itr >= r.max_steps) return true;
     const int lx = f2i_floor(r.o.x);
     const int ly = f2i_floor(r.o.y);
@@ -89,7 +92,12 @@ __device__ __forceinline__ bool dda_step(const WorldView& w, RayState& r) {
         r.inter = 0;
         return true;
     }
-    const int e = euclid_steps((int)__ldg(w.df + df_index<B>(w, lx, ly, lz)));
+    *addr = df_index<B>(w, lx, ly, lz);
+    return false;
+}
+
+__device__ __forceinline__ bool dda_apply(RayState& r, int dist) {
+    const int e = euclid_steps(dist);
     if (e == 0) return true;
     if (e == 1) {
         dda_face_step(r);
@@ -103,6 +111,14 @@ __device__ __forceinline__ bool dda_step(const WorldView& w, RayState& r) {
     }
     r.itr++;
     return r.itr >= r.max_steps;
+}
+
+// One iteration of the traversal loop; returns true once the loop is over.
+template <int B = 0>
+__device__ __forceinline__ bool dda_step(const WorldView& w, RayState& r) {
+    int addr = 0;
+    if (dda_fetch<B>(w, r, &addr)) return true;
+    return dda_apply(r, (int)__ldg(w.df + addr));
 }
 
 // The code after the loop (:365-373).
@@ -133,6 +149,30 @@ __device__ __forceinline__ TraceResult traverse(const WorldView& w, v3 origin, v
     while (!dda_step<B>(w, r)) {
     }
     return ray_finish(w, r);
+}
+
+// Two rays traversed together by one thread, their DDA steps interleaved so
+// that both distance-field gathers of an iteration are in flight at once (the
+// gather latency is what bounds a lone ray). Each ray's state evolves exactly
+// as in traverse; a ray with live == false is not traced.
+template <int B = 0>
+__device__ __forceinline__ void traverse2(const WorldView& w, v3 o0, v3 d0, int n0, bool live0, v3 o1, v3 d1, int n1,
+                                          bool live1, TraceResult* r0, TraceResult* r1) {
+    RayState a, b;
+    ray_start(a, o0, d0, n0);
+    ray_start(b, o1, d1, n1);
+    bool fa = !live0, fb = !live1;
+    while (!(fa && fb)) {
+        int ia = 0, ib = 0;
+        const bool ea = fa || dda_fetch<B>(w, a, &ia);
+        const bool eb = fb || dda_fetch<B>(w, b, &ib);
+        const int va = ea ? 0 : (int)__ldg(w.df + ia);
+        const int vb = eb ? 0 : (int)__ldg(w.df + ib);
+        fa = ea || dda_apply(a, va);
+        fb = eb || dda_apply(b, vb);
+    }
+    if (live0) *r0 = ray_finish(w, a);
+    if (live1) *r1 = ray_finish(w, b);
 }
 
 // The normal of the last face step: normal[MinIdx] = -sign(direction[MinIdx]).

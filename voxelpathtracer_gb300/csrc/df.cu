@@ -13,11 +13,12 @@
 //      16 distances with one 128-bit store: one read and one write per voxel;
 //   y, z: k_df_sweep_tile -- a CTA stages a tile of 16..64 consecutive x by
 //      the whole line along y (or z) in shared memory with 128-bit loads,
-//      sweeps it forward and backward there (4 columns per thread, two 16-bit
-//      lanes per register, min(d_prev + 1, d) as one DPX add-min per lane
-//      pair), and writes the tile back with 128-bit stores: one read and one
-//      write per voxel per sweep, all global accesses independent of one
-//      another.
+//      computes the line transform there with all its threads (4 columns per
+//      thread as two 16-bit lanes per register, each line split into
+//      segments joined by their end values; min(d_prev + 1, d) is one DPX
+//      add-min per lane pair), and writes the tile back with 128-bit stores:
+//      one read and one write per voxel per sweep, all global accesses
+//      independent of one another.
 // Generic path (any X, any alignment): one warp per row with warp shuffles
 // for x; one thread per column with the running value in a register for y, z.
 #include <algorithm>
@@ -120,22 +121,14 @@ __global__ void __launch_bounds__(128) k_df_z(uint8_t* df, int X, int Y, int Z) 
 // x sweep, X % 16 == 0 and X <= 1024. A row of X bytes is S = X / 16
 // segments; L lanes (a power of two >= S, at most 32) work on one row, each on
 // kSegs = ceil(S / L) consecutive segments held in registers, so a warp holds
-// 32 / L rows.
+// 32 / L rows. Each warp does two such row groups, with the loads of both
+// issued before either is processed (twice the bytes in flight).
+
+// The distances of one row group's segments v (row `row`, this lane's
+// segments from s0); every lane of the warp calls it.
 template <int kSegs>
-__global__ void __launch_bounds__(256) k_df_x16(const uint4* __restrict__ vox, uint4* __restrict__ df, int S,
-                                                int L, int rows, int maxd) {
-    const int lane = threadIdx.x & 31;
-    const int rows_per_warp = 32 / L;
-    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int sub = lane / L, l = lane % L;                 // row within the warp, lane within the row
-    const int row = warp * rows_per_warp + sub;
-    const bool live = row < rows;
-    // segments [s0, s0 + kSegs) of the row belong to this lane
-    const int s0 = l * kSegs;
-    uint4 v[kSegs];
-#pragma unroll
-    for (int k = 0; k < kSegs; k++)
-        v[k] = (live && s0 + k < S) ? __ldg(vox + (size_t)row * S + s0 + k) : make_uint4(0u, 0u, 0u, 0u);
+__device__ __forceinline__ void x_row(const uint4 (&v)[kSegs], uint4* __restrict__ df, int S, int L, int l, int s0,
+                                      int row, bool live, int maxd) {
     const int NEG = -(1 << 24), POS = 1 << 24;
     // nearest solid at or left of / at or right of each byte, first within the lane
     int first = POS, last = NEG;
@@ -195,15 +188,54 @@ __global__ void __launch_bounds__(256) k_df_x16(const uint4* __restrict__ vox, u
     }
 }
 
+template <int kSegs>
+__global__ void __launch_bounds__(256) k_df_x16(const uint4* __restrict__ vox, uint4* __restrict__ df, int S,
+                                                int L, int rows, int maxd) {
+    const int lane = threadIdx.x & 31;
+    const int rows_per_warp = 32 / L;
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int sub = lane / L, l = lane % L;                 // row within the group, lane within the row
+    const int row0 = (2 * warp) * rows_per_warp + sub, row1 = row0 + rows_per_warp;
+    const bool live0 = row0 < rows, live1 = row1 < rows;
+    // segments [s0, s0 + kSegs) of a row belong to this lane
+    const int s0 = l * kSegs;
+    uint4 v0[kSegs], v1[kSegs];
+#pragma unroll
+    for (int k = 0; k < kSegs; k++) {
+        v0[k] = (live0 && s0 + k < S) ? __ldg(vox + (size_t)row0 * S + s0 + k) : make_uint4(0u, 0u, 0u, 0u);
+        v1[k] = (live1 && s0 + k < S) ? __ldg(vox + (size_t)row1 * S + s0 + k) : make_uint4(0u, 0u, 0u, 0u);
+    }
+    x_row<kSegs>(v0, df, S, L, l, s0, row0, live0, maxd);
+    x_row<kSegs>(v1, df, S, L, l, s0, row1, live1, maxd);
+}
+
 // y or z sweep over a tile: x in [x0, x0 + w) (w a multiple of 16, at most
 // kTile) and the whole line of n samples `stride` bytes apart, starting at
 // byte base = blockIdx.y * outer + x0. The tile sits in shared memory, row r
-// at r * w; thread t < w / 4 sweeps columns 4t..4t+3.
+// at r * w. The line's result is min over j of d[j] + |r - j| (the forward
+// then backward min(d, d_prev + 1) sweeps of ManhattanDistanceY/Z.comp), so
+// the 128 threads split it: G = w / 4 column groups (4 columns per thread, as
+// two 16-bit lanes per register) times P = 128 / G segments of m rows each
+// (m odd, so the segments of one warp fall in different shared-memory
+// banks). Each thread
+//   1. reduces its segment to the distance it passes on at either end
+//      (min of d[j] + distance to the segment's last / first row);
+//   2. chains those over the segments before / after it into the forward
+//      value just before its segment and the backward value just after it;
+//   3. runs the forward sweep over its segment seeded with the first and the
+//      backward sweep over the forward values seeded with the second, which
+//      leaves the exact line result in its rows.
 constexpr int kTile = 64;
+constexpr unsigned kInf2 = 0x3fff3fffu;   // "no voxel yet" in both 16-bit lanes; + 1536 cannot overflow
+
+__device__ __forceinline__ unsigned lo_pair(unsigned w) { return __byte_perm(w, 0u, 0x4140); }   // bytes 0, 1
+__device__ __forceinline__ unsigned hi_pair(unsigned w) { return __byte_perm(w, 0u, 0x4342); }   // bytes 2, 3
+__device__ __forceinline__ unsigned pack_pairs(unsigned lo, unsigned hi) { return __byte_perm(lo, hi, 0x6420); }
 
 __global__ void __launch_bounds__(128) k_df_sweep_tile(uint8_t* __restrict__ df, int X, int n, size_t stride,
                                                        size_t outer) {
     extern __shared__ __align__(16) uint8_t tile[];
+    __shared__ unsigned s_carry[4][128];   // per thread: forward-end lo / hi, backward-start lo / hi
     const int x0 = blockIdx.x * kTile;
     const int w = min(kTile, X - x0);
     const int q = w >> 4;   // 16-byte words per row
@@ -214,25 +246,54 @@ __global__ void __launch_bounds__(128) k_df_sweep_tile(uint8_t* __restrict__ df,
             *reinterpret_cast<const uint4*>(base + (size_t)r * stride + 16 * c);
     }
     __syncthreads();
-    if ((int)threadIdx.x < (w >> 2)) {
-        unsigned* col = reinterpret_cast<unsigned*>(tile) + threadIdx.x;
-        const int pitch = w >> 2;   // words per row
-        const unsigned one = 0x00010001u;
-        // bytes b0..b3 of a word as 16-bit lanes (b0, b1) and (b2, b3), and back
-        unsigned w0 = col[0];
-        unsigned lo = __byte_perm(w0, 0u, 0x4140), hi = __byte_perm(w0, 0u, 0x4342);
-        for (int r = 1; r < n; r++) {   // ManhattanDistanceY.comp:105-109: d = min(d, d_prev + 1)
-            const unsigned cw = col[(size_t)r * pitch];
-            lo = __viaddmin_u16x2(lo, one, __byte_perm(cw, 0u, 0x4140));
-            hi = __viaddmin_u16x2(hi, one, __byte_perm(cw, 0u, 0x4342));
-            col[(size_t)r * pitch] = __byte_perm(lo, hi, 0x6420);
-        }
-        for (int r = n - 2; r >= 0; r--) {
-            const unsigned cw = col[(size_t)r * pitch];
-            lo = __viaddmin_u16x2(lo, one, __byte_perm(cw, 0u, 0x4140));
-            hi = __viaddmin_u16x2(hi, one, __byte_perm(cw, 0u, 0x4342));
-            col[(size_t)r * pitch] = __byte_perm(lo, hi, 0x6420);
-        }
+    const int G = w >> 2;                   // column groups (words per row)
+    const int P = blockDim.x / G;           // segments
+    const int g = threadIdx.x % G, sg = threadIdx.x / G;
+    const int m = ((n + P - 1) / P) | 1;
+    const int a = min(n, sg * m), b = min(n, a + m);
+    unsigned* col = reinterpret_cast<unsigned*>(tile) + g;
+    // 1. the segment's own contribution at its ends
+    unsigned fl = kInf2, fh = kInf2, bl = kInf2, bh = kInf2;
+    for (int r = a; r < b; r++) {
+        const unsigned cw = col[(size_t)r * G];
+        const unsigned to_end = (unsigned)(b - 1 - r) * 0x00010001u, to_start = (unsigned)(r - a) * 0x00010001u;
+        fl = __viaddmin_u16x2(lo_pair(cw), to_end, fl);
+        fh = __viaddmin_u16x2(hi_pair(cw), to_end, fh);
+        bl = __viaddmin_u16x2(lo_pair(cw), to_start, bl);
+        bh = __viaddmin_u16x2(hi_pair(cw), to_start, bh);
+    }
+    s_carry[0][threadIdx.x] = fl;
+    s_carry[1][threadIdx.x] = fh;
+    s_carry[2][threadIdx.x] = bl;
+    s_carry[3][threadIdx.x] = bh;
+    __syncthreads();
+    // 2. forward value before row a, backward value after row b - 1
+    unsigned Fl = kInf2, Fh = kInf2, Bl = kInf2, Bh = kInf2;
+    for (int k = 0; k < sg; k++) {
+        const int ka = min(n, k * m);
+        const unsigned len = (unsigned)(min(n, ka + m) - ka) * 0x00010001u;
+        Fl = __viaddmin_u16x2(Fl, len, s_carry[0][k * G + g]);
+        Fh = __viaddmin_u16x2(Fh, len, s_carry[1][k * G + g]);
+    }
+    for (int k = P - 1; k > sg; k--) {
+        const int ka = min(n, k * m);
+        const unsigned len = (unsigned)(min(n, ka + m) - ka) * 0x00010001u;
+        Bl = __viaddmin_u16x2(Bl, len, s_carry[2][k * G + g]);
+        Bh = __viaddmin_u16x2(Bh, len, s_carry[3][k * G + g]);
+    }
+    // 3. the seeded sweeps (ManhattanDistanceY.comp:105-109: d = min(d, d_prev + 1))
+    const unsigned one = 0x00010001u;
+    for (int r = a; r < b; r++) {
+        const unsigned cw = col[(size_t)r * G];
+        Fl = __viaddmin_u16x2(Fl, one, lo_pair(cw));
+        Fh = __viaddmin_u16x2(Fh, one, hi_pair(cw));
+        col[(size_t)r * G] = pack_pairs(Fl, Fh);
+    }
+    for (int r = b - 1; r >= a; r--) {
+        const unsigned cw = col[(size_t)r * G];
+        Bl = __viaddmin_u16x2(Bl, one, lo_pair(cw));
+        Bh = __viaddmin_u16x2(Bh, one, hi_pair(cw));
+        col[(size_t)r * G] = pack_pairs(Bl, Bh);
     }
     __syncthreads();
     for (int k = threadIdx.x; k < n * q; k += blockDim.x) {
@@ -321,7 +382,8 @@ cudaError_t launch_x16(const uint8_t* vox, uint8_t* df, int X, int rows, int max
     const int S = X / 16;
     int L = 1;
     while (L < S && L < 32) L <<= 1;
-    const long long threads = (long long)(rows + 32 / L - 1) / (32 / L) * 32;
+    const int rows_per_warp = 2 * (32 / L);
+    const long long threads = (long long)(rows + rows_per_warp - 1) / rows_per_warp * 32;
     k_df_x16<kSegs><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
         reinterpret_cast<const uint4*>(vox), reinterpret_cast<uint4*>(df), S, L, rows, maxd);
     return cudaGetLastError();

@@ -175,8 +175,9 @@ struct BatchLaunch {
 };
 constexpr int kBatchMaxWorlds = 1024;
 // df_brick: 0, 4 or 8; blocks <= 0 fills every SM to its occupancy limit.
-cudaError_t batch_trace(const BatchLaunch& a, int df_brick, int block_threads, int blocks, cudaStream_t s);
-int batch_max_blocks(int df_brick, int block_threads, int device);
+cudaError_t batch_trace(const BatchLaunch& a, int df_brick, int block_threads, int rays_per_lane, int blocks,
+                        cudaStream_t s);
+int batch_max_blocks(int df_brick, int block_threads, int rays_per_lane, int device);
 // Copies an x-fastest distance field into the BxBxB brick layout of df_index.
 cudaError_t df_to_bricks(const uint8_t* df, uint8_t* out, int X, int Y, int Z, int brick, cudaStream_t s);
 

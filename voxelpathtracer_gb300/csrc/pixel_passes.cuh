@@ -12,6 +12,11 @@ namespace vpt {
 __device__ __forceinline__ float stored_value(float v, const float*) { return v; }
 __device__ __forceinline__ float stored_value(float v, const __half*) { return __half2float(__float2half_rn(v)); }
 
+template <typename S>
+__device__ __forceinline__ unsigned primary_store(const TraceResult& r, size_t px, S* out_t, uint8_t* out_face,
+                                                  uint8_t* out_block, int32_t* out_hit, uint16_t* out_steps,
+                                                  float* t_stored, int* face_id);
+
 // InitialRayTraceFrag.glsl main (:417-468). Writes the G-buffer texel `px`;
 // returns the step count and, for the passes that follow, the hit distance as
 // stored and the face id.
@@ -24,6 +29,14 @@ __device__ __forceinline__ unsigned primary_pixel(const WorldView& w, const CamV
     const v3 r0 = ray_origin(cam);
     const v3 dir = normalize(ray_dir_at(cam, texcoord(i, j, W, H)));
     const TraceResult r = kAlpha ? traverse_alpha<B>(w, r0, dir, max_steps, *stop) : traverse<B>(w, r0, dir, max_steps);
+    return primary_store(r, px, out_t, out_face, out_block, out_hit, out_steps, t_stored, face_id);
+}
+
+// The G-buffer texel `px` of a traced primary ray (InitialRayTraceFrag.glsl:438-468).
+template <typename S>
+__device__ __forceinline__ unsigned primary_store(const TraceResult& r, size_t px, S* out_t, uint8_t* out_face,
+                                                  uint8_t* out_block, int32_t* out_hit, uint16_t* out_steps,
+                                                  float* t_stored, int* face_id) {
     const bool intersect = r.t > 0.0f && r.block > 0;
     const int face = intersect ? normal_id(r.normal) : kFaceMiss;
     st(out_t + px, r.t);
@@ -36,6 +49,27 @@ __device__ __forceinline__ unsigned primary_pixel(const WorldView& w, const CamV
     *t_stored = stored_value(r.t, out_t);
     *face_id = face;
     return (unsigned)r.steps;
+}
+
+// Two primary rays of one thread, their traversals interleaved (traverse2);
+// the same G-buffer texels as two primary_pixel calls.
+template <int B, typename S>
+__device__ __forceinline__ void primary_pixel2(const WorldView& w, const CamView& cam, int W, int H, const int (&i)[2],
+                                               const int (&j)[2], const bool (&live)[2], int max_steps, S* out_t,
+                                               uint8_t* out_face, uint8_t* out_block, int32_t* out_hit,
+                                               uint16_t* out_steps, float (&t_stored)[2], int (&face_id)[2],
+                                               unsigned (&steps)[2]) {
+    const v3 r0 = ray_origin(cam);
+    v3 dir[2];
+    for (int k = 0; k < 2; k++) dir[k] = live[k] ? normalize(ray_dir_at(cam, texcoord(i[k], j[k], W, H))) : r0;
+    TraceResult r[2];
+    traverse2<B>(w, r0, dir[0], max_steps, live[0], r0, dir[1], max_steps, live[1], &r[0], &r[1]);
+    for (int k = 0; k < 2; k++) {
+        steps[k] = 0;
+        if (live[k])
+            steps[k] = primary_store(r[k], (size_t)j[k] * W + i[k], out_t, out_face, out_block, out_hit, out_steps,
+                                     &t_stored[k], &face_id[k]);
+    }
 }
 
 // ShadowRayTraceFrag.glsl main (:414-513): one hard shadow ray towards the sun
@@ -60,6 +94,43 @@ __device__ __forceinline__ uint8_t shadow_pixel(const WorldView& w, const CamVie
         *nsteps += (unsigned)r.steps;
     }
     return (T > 0.0f || block_at > 0) ? 1 : 0;
+}
+
+// Two sun-shadow rays of one thread (texels k = 0, 1 with hit distances d[k]
+// and faces face[k]), the traversals interleaved; the same bytes as
+// shadow_pixel without alpha testing.
+template <int B>
+__device__ __forceinline__ void shadow_pixel2(const WorldView& w, const CamView& cam, int W, int H, const int (&i)[2],
+                                              const int (&j)[2], const bool (&live)[2], int max_steps, v3 L,
+                                              const float (&d)[2], const int (&face)[2], uint8_t (&out)[2],
+                                              unsigned* nrays, unsigned* nsteps) {
+    v3 o[2];
+    int block_at[2] = {0, 0};
+    bool trace[2] = {false, false};
+    for (int k = 0; k < 2; k++) {
+        out[k] = 0;
+        o[k] = mk3(0.0f, 0.0f, 0.0f);
+        if (!live[k] || d[k] < 0.0f) continue;
+        const v3 pos = add(ray_origin(cam), muls(normalize(ray_dir_at(cam, texcoord(i[k], j[k], W, H))), d[k]));
+        const v3 n = normal_from_id(face[k], 1.0f);
+        const float ndl = dot(n, L);
+        if (ndl <= 0.01f) {
+            out[k] = 1;
+            continue;
+        }
+        o[k] = add(pos, mul(n, mk3(0.06f, 0.06f, 0.06f)));
+        block_at[k] = get_voxel(w, f2i_floor(o[k].x), f2i_floor(o[k].y), f2i_floor(o[k].z));
+        trace[k] = d[k] > 0.0f;
+        if (!trace[k]) out[k] = block_at[k] > 0 ? 1 : 0;
+    }
+    TraceResult r[2];
+    traverse2<B>(w, o[0], L, max_steps, trace[0], o[1], L, max_steps, trace[1], &r[0], &r[1]);
+    for (int k = 0; k < 2; k++) {
+        if (!trace[k]) continue;
+        *nrays += 1;
+        *nsteps += (unsigned)r[k].steps;
+        out[k] = (r[k].t > 0.0f || block_at[k] > 0) ? 1 : 0;
+    }
 }
 
 // DiffuseRayTraceFrag.glsl main (:822-935): `spp` GI samples of the texel.
