@@ -52,18 +52,18 @@ TRACE_KINDS = {"primary": ["primary"], "shadow": ["shadow"], "diffuse": ["diffus
 # planes written once), fp32 / fp16 storage.
 FILTER_BYTES_PER_PX = {
     "spatial_initial": (77, 39),   # t, face, SH, CoCg, luma, AO in; SH, CoCg, luma, AO out
-    "temporal": (180, 92),         # fused with the pre-filter: its inputs and outputs (77 / 39) + previous
-                                   # G-buffer, current block, history in and out (less the pre-filtered planes
-                                   # and the t / face it no longer reads twice)
-    "temporal_split": (144, 74),   # the temporal pass alone: current G-buffer + pre-filtered planes, previous
-                                   # G-buffer + history; history out
+    "temporal": (144, 74),         # current G-buffer + pre-filtered planes, previous G-buffer + history;
+                                   # history out
+    "temporal_fused": (180, 92),   # k_pre_temporal (vpt_tuning.fused_prefilter): the pre-filter's inputs and
+                                   # outputs (77 / 39) + the temporal pass's, less the pre-filtered planes and
+                                   # the t / face it does not read twice
     "variance": (65, 33),          # t, face, SH, CoCg, util.xy in; SH, CoCg, variance out
     "atrous": (81, 41),            # t, face, util.x, SH, CoCg, variance, AO in; SH, CoCg, variance, AO out
     "shade": (47, 25),             # t, face, block, shadow, SH, CoCg, AO.x in; RGB out
 }
 KERNEL_NAMES = {"primary": "k_trace_primary", "shadow": "k_trace_shadow", "diffuse": "k_trace_diffuse_staged",
                 "trace_frame": "k_trace_frame",
-                "spatial_initial": "k_spatial_initial", "temporal": "k_pre_temporal", "variance": "k_variance",
+                "spatial_initial": "k_spatial_initial", "temporal": "k_temporal", "variance": "k_variance",
                 "atrous": "k_atrous", "shade": "k_shade",
                 "reflection": "k_trace_reflection (+ hit blur, temporal and denoiser kernels)"}
 
@@ -261,13 +261,16 @@ def run_ours(args):
                                              l2_gbs), launches_per_frame=launches_per_frame,
                               ms_per_launch=per_launch_ms)
             continue
-        key = "temporal_split" if p == "temporal" and "spatial_initial" in mean_pass else p
+        fused_pre = p == "temporal" and "spatial_initial" not in mean_pass
+        key = "temporal_fused" if fused_pre else p
         b = float(FILTER_BYTES_PER_PX[key][args.storage] * W * H)
         if p != "shade":   # the GI-side filters run on the GI grid
             b /= float(args.gi_divisor * args.gi_divisor)
         gbs = b / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
         kernels[p] = {"bound": "hbm", "launches_per_frame": launches_per_frame, "ms_per_launch": per_launch_ms,
                       "algorithmic_bytes_per_launch": b, "achieved_gbs": gbs, "frac": gbs / peak}
+        if fused_pre:
+            kernels[p]["kernel"] = "k_pre_temporal"
     dom = max((p for p in mean_pass if p not in TRACE_KINDS), key=mean_pass.get)
     per_launch_bytes = kernels[dom]["algorithmic_bytes_per_launch"]
     achieved = kernels[dom]["achieved_gbs"]

@@ -196,8 +196,8 @@ typedef struct vpt_tuning {
     int32_t refill_threshold;        /* waiting lanes that trigger a warp refill, 1..32 (default 16) */
     int32_t trace_blocks;            /* persistent blocks of 128 threads; 0 = fill every SM once */
     int32_t fused_trace;             /* vpt_render_frame traces with vpt_trace_frame (1) or the three passes (0, default) */
-    int32_t split_prefilter;         /* SVGF runs Spatial3x3Initial and the temporal pass as two launches (1) or as
-                                        one fused kernel (0, default); the same planes either way */
+    int32_t fused_prefilter;         /* SVGF runs Spatial3x3Initial inside the temporal kernel (1) or as its own
+                                        launch before it (0, default: measured faster); the same planes either way */
     int32_t reserved[4];
 } vpt_tuning;
 

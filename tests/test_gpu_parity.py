@@ -100,12 +100,12 @@ def test_distance_field_empty_and_full(vpt, oracle, gpu):
         assert (got == (0 if fill else min(254, 90))).all()
 
 
-@pytest.mark.parametrize("split", [False, True], ids=["fused_prefilter", "split_prefilter"])
+@pytest.mark.parametrize("fused", [False, True], ids=["split_prefilter", "fused_prefilter"])
 @pytest.mark.parametrize("storage", [0, 1], ids=["f32", "f16"])
-def test_passes_bit_exact_two_frames(vpt, oracle, scene, storage, split, gpu):
+def test_passes_bit_exact_two_frames(vpt, oracle, scene, storage, fused, gpu):
     world = scene["world"]
     ctx = make_ctx(vpt, scene, storage)
-    ctx.set_tuning(split_prefilter=split)
+    ctx.set_tuning(fused_prefilter=fused)
     cfg = ctx.config
     prev_g, hist = oracle.empty_history(H, W)
     prev_cam = scene["cams"][0]

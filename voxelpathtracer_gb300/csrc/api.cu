@@ -971,9 +971,9 @@ vpt_status vpt_ground_truth(vpt_ctx* c, const vpt_frame* f, int32_t x0, int32_t 
 vpt_status vpt_set_tuning(vpt_ctx* c, const vpt_tuning* t) {
     if (!c || !t) return VPT_ERR_INVALID_ARG;
     if (t->refill_threshold < 1 || t->refill_threshold > 32 || t->trace_blocks < 0 || t->trace_blocks > 65535 ||
-        t->fused_trace < 0 || t->fused_trace > 1 || t->split_prefilter < 0 || t->split_prefilter > 1)
+        t->fused_trace < 0 || t->fused_trace > 1 || t->fused_prefilter < 0 || t->fused_prefilter > 1)
         return fail(c, VPT_ERR_INVALID_ARG,
-                    "refill_threshold must be 1..32, trace_blocks 0..65535, fused_trace and split_prefilter 0/1");
+                    "refill_threshold must be 1..32, trace_blocks 0..65535, fused_trace and fused_prefilter 0/1");
     c->tuning = *t;
     return VPT_OK;
 }
@@ -1037,7 +1037,7 @@ vpt_status svgf_run(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f, 
     // Spatial3x3Initial (Core/Pipeline.cpp:2288-2330) and temporal (:2334-2436)
     const GIIn gin{c->gi[GI_SH], c->gi[GI_COCG], c->gi[GI_LUMA], c->gi[GI_AOSKY]};
     const GIOut pre{c->pre[GI_SH], c->pre[GI_COCG], c->pre[GI_LUMA], c->pre[GI_AOSKY]};
-    if (c->tuning.split_prefilter) {
+    if (!c->tuning.fused_prefilter) {
         pass_begin(c, VPT_PASS_SPATIAL_INITIAL);
         CK(c, svgf_spatial_initial(cv, W, H, c->fp16, t, face, gin, pre, c->stream));
         pass_end(c, VPT_PASS_SPATIAL_INITIAL);
@@ -1054,7 +1054,7 @@ vpt_status svgf_run(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f, 
     HistIO hout{c->hist[cur][HI_SH], c->hist[cur][HI_COCG], c->hist[cur][HI_UTIL], c->hist[cur][HI_AOSKY]};
     HistIO hprev{c->hist[prv][HI_SH], c->hist[prv][HI_COCG], c->hist[prv][HI_UTIL], c->hist[prv][HI_AOSKY]};
     pass_begin(c, VPT_PASS_TEMPORAL);
-    if (c->tuning.split_prefilter)
+    if (!c->tuning.fused_prefilter)
         CK(c, svgf_temporal(cv, W, H, Wf, Hf, c->fp16, ta, t, face, block, c->gbuf[prv][GB_T],
                             (const uint8_t*)c->gbuf[prv][GB_FACE], (const uint8_t*)c->gbuf[prv][GB_BLOCK],
                             GIIn{c->pre[GI_SH], c->pre[GI_COCG], c->pre[GI_LUMA], c->pre[GI_AOSKY]}, hprev, hout,
