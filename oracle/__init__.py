@@ -84,6 +84,7 @@ def lib() -> C.CDLL:
         L.vpto_temporal.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, P]
         L.vpto_variance.argtypes = [P, P, P, P, P, P]
         L.vpto_reproject.argtypes = [P, P, C.c_int, C.c_int, P, P, P]
+        L.vpto_vecmath.argtypes = [C.c_int, P, P, P, P, C.c_int]
         L.vpto_atrous.argtypes = [P, P, P, C.c_int, P, P, P, P, P, P, P, P]
         L.vpto_gi_view.argtypes = [P, P, P, P, P, P, P]
         L.vpto_shade.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, C.c_int, C.c_int, P]
@@ -288,6 +289,18 @@ def temporal(cam, prev_cam, config, frame, t, face, block, prev_t, prev_face, pr
                    _struct4(out, ["sh", "cocg", "util", "aosky"]))
     lib().vpto_temporal(C.byref(_as(OCamera, cam)), C.byref(_as(OCamera, prev_cam)), C.byref(p),
                         C.byref(_as(OFrame, frame)), *[_p(a) for a in arrs], C.byref(sc), C.byref(sh_), C.byref(so))
+    return out
+
+
+def vecmath(op: int, a, b, c) -> np.ndarray:
+    """The oracle's dot / cross / length / normalize / mix / mat4*vec4 (op 0..5)
+    over arrays of inputs (n x 3, or n x 16 and n x 4 for op 5)."""
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    c = np.ascontiguousarray(c, np.float32)
+    n = a.shape[0]
+    out = np.zeros((n, 4 if op == 5 else 3), np.float32)
+    lib().vpto_vecmath(op, _p(a), _p(b), _p(c), _p(out), n)
     return out
 
 

@@ -914,6 +914,34 @@ void vpto_spatial_initial(const vpto_camera* cam, const vpto_params* p,
     }
 }
 
+// The oracle's vector builtins over n inputs, for the comparison with glm:
+// op 0 dot, 1 cross, 2 length, 3 normalize, 4 mix (scalar), 5 mat4 * vec4.
+void vpto_vecmath(int op, const float* a, const float* b, const float* c, float* out, int n) {
+    for (int k = 0; k < n; k++) {
+        if (op == 5) {
+            const v4 r = mat_mul4(a + 16 * k, b[4 * k], b[4 * k + 1], b[4 * k + 2], b[4 * k + 3]);
+            out[4 * k] = r.x;
+            out[4 * k + 1] = r.y;
+            out[4 * k + 2] = r.z;
+            out[4 * k + 3] = r.w;
+            continue;
+        }
+        const v3 x = mk3(a[3 * k], a[3 * k + 1], a[3 * k + 2]), y = mk3(b[3 * k], b[3 * k + 1], b[3 * k + 2]);
+        v3 r = mk3(0.0f, 0.0f, 0.0f);
+        switch (op) {
+            case 0: r.x = dot(x, y); break;
+            case 1: r = cross(x, y); break;
+            case 2: r.x = length(x); break;
+            case 3: r = normalize(x); break;
+            case 4: r.x = mixf(x.x, y.x, c[3 * k]); break;
+            default: break;
+        }
+        out[3 * k] = r.x;
+        out[3 * k + 1] = r.y;
+        out[3 * k + 2] = r.z;
+    }
+}
+
 // u_PrevProjection * u_PrevView (SVGF/TemporalFilter.glsl:61-68), a 4x4
 // product evaluated left to right.
 static void prev_view_proj(const vpto_camera* prev_cam, float* m) {

@@ -155,6 +155,9 @@ void vpto_spatial_initial(const vpto_camera* cam, const vpto_params* p,
                           const float* t, const uint8_t* face, const vpto_gi* in, vpto_gi* out);
 
 /* SVGF/TemporalFilter.glsl */
+/* The oracle's vector builtins (dot, cross, length, normalize, mix, mat4 *
+ * vec4) over n inputs, for the comparison with the reference's glm. */
+void vpto_vecmath(int op, const float* a, const float* b, const float* c, float* out, int n);
 /* ProjectPositionPrevious / Reprojection (SVGF/TemporalFilter.glsl:61-73) of
  * every texel of the W x H hit-distance plane t, as the temporal pass computes
  * them: the world position (3 floats per texel) and the previous frame's

@@ -93,7 +93,8 @@ def build_libvpt(verbose: bool = False, jobs: int | None = None) -> Path:
 def build_oracle(verbose: bool = False) -> Path:
     out_dir = ORACLE_LIB.parent
     out_dir.mkdir(exist_ok=True)
-    sources = sorted(ORACLE_DIR.glob("*.cpp"))
+    # *_ref.* files are compiled against the reference tree (oracle/build_ref.py)
+    sources = sorted(p for p in ORACLE_DIR.glob("*.cpp") if not p.stem.endswith("_ref"))
     deps = sources + list(ORACLE_DIR.glob("*.h")) + [Path(__file__)]
     if _newer(ORACLE_LIB, deps):
         cxx = os.environ.get("CXX", "g++")
