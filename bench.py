@@ -248,7 +248,7 @@ def run_ours(args):
     kernels = {}
     mean_pass = {p: ms for p, ms in mean_pass.items() if ms > 0}   # passes this frame path ran
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
-    l2_gbs = l2_read_roof(torch, local)
+    l2_gbs = l2_read_roof(vpt, local)
     for p, ms in mean_pass.items():
         launches_per_frame = iters if p == "atrous" else 1
         per_launch_ms = ms / launches_per_frame
@@ -684,22 +684,14 @@ def profile_metrics(kernel):
     return out
 
 
-def l2_read_roof(torch, local):
-    """Achievable L2 read bandwidth: a sum over a 64 MiB fp32 tensor that stays
-    in the 126 MB L2, median of 20 reductions after warm-up (GB/s)."""
-    x = torch.ones(16 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")
-    for _ in range(5):
-        x.sum()
-    torch.cuda.synchronize()
-    ms = []
-    for _ in range(20):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        x.sum()
-        e1.record()
-        e1.synchronize()
-        ms.append(e0.elapsed_time(e1))
-    return x.numel() * 4 / (statistics.median(ms) * 1e-3) / 1e9
+def l2_read_roof(vpt, local):
+    """Achievable L2 read bandwidth: 128-bit reads of a 32 MiB buffer that
+    stays in L2 (vpt_measure_l2_read), median of 20 reads (GB/s)."""
+    import ctypes as C
+    g = C.c_float()
+    if vpt.lib.vpt_measure_l2_read(local, 32 * 1024 * 1024, 20, C.byref(g)) != vpt.OK:
+        return None
+    return float(g.value)
 
 
 def trace_roofline(kernel, ms_per_launch, steps, rays, sm_count, sm_mhz, l2_gbs):

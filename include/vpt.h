@@ -485,6 +485,13 @@ vpt_status vpt_batch_set_tuning(vpt_batch* batch, const vpt_batch_tuning* tuning
 vpt_status vpt_batch_get_tuning(const vpt_batch* batch, vpt_batch_tuning* tuning);
 /* Traces every world with its camera. Stream-ordered; returns without waiting. */
 vpt_status vpt_batch_trace(vpt_batch* batch, const vpt_frame* frame, int32_t mode);
+/* No counterpart in the reference: the read bandwidth (GB/s, median of
+ * `reps` reads after two warm-ups) of a `bytes`-long device buffer (1 MiB ..
+ * 4 GiB) that stays in L2 when it fits, read with 128-bit L2-cached loads on
+ * `device` - the memory roof of the trace kernels, whose distance-field
+ * gathers hit an L2-resident volume. Allocates and frees its buffer. */
+vpt_status vpt_measure_l2_read(int32_t device, uint64_t bytes, int32_t reps, float* gbs);
+
 /* Times every candidate launch shape (rays_per_lane 1/2 x block_threads
  * 128/256/512 x tiles_per_grab 1/2/4 x df_brick 0/4/8, 54 in all) on the
  * batch as it stands, `reps`

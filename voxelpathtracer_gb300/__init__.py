@@ -164,6 +164,7 @@ def _load() -> C.CDLL:
         "vpt_build_df": ([P], C.c_int),
         "vpt_read_df": ([P, P, sz], C.c_int),
         "vpt_df_build_device": ([P, P, i32, i32, i32, P], C.c_int),
+        "vpt_measure_l2_read": ([i32, C.c_uint64, i32, C.POINTER(C.c_float)], C.c_int),
         "vpt_trace_primary": ([P, C.POINTER(Camera)], C.c_int),
         "vpt_trace_shadow": ([P, C.POINTER(Frame)], C.c_int),
         "vpt_trace_diffuse": ([P, C.POINTER(Frame)], C.c_int),
