@@ -296,11 +296,19 @@ __global__ void __launch_bounds__(256, 4) k_pre_temporal(CamView cam, int W, int
 // SVGF/VarianceEstimate.glsl main (:73-193) with DO_SPATIAL and
 // AGGRESSIVE_DISOCCLUSION_HANDLING on. Only the hit distance of the taps'
 // reconstructed positions is used (the depth weight), so no ray is rebuilt.
-template <typename S>
-__global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, const uint8_t* face, const S* i_sh,
-                                                  const S* i_cocg, const S* i_util, S* o_sh, S* o_cocg, S* o_var) {
-    int i, j;
-    if (!pixel_of(W, H, &i, &j)) return;
+//
+// A texel with fewer than 12 accumulated frames takes the 81-tap estimate,
+// every other one the temporal moments. Once a history has grown, the young
+// texels are the few the camera's motion disoccluded, spread over many warps,
+// each of which would run the 81-tap loop for a lane or two; so every thread
+// first finishes its texel if it is old, and the block's young texels are
+// then listed in shared memory and estimated by consecutive threads (the
+// same per-texel arithmetic, only the thread that runs it changes).
+// kYoung: the texel's history is younger than 12 frames (the caller tested it).
+template <typename S, bool kYoung>
+__device__ __forceinline__ void variance_texel(int W, int H, int i, int j, const S* t, const uint8_t* face,
+                                               const S* i_sh, const S* i_cocg, const S* i_util, S* o_sh, S* o_cocg,
+                                               S* o_var) {
     const float thresh = 4.0f + 4.0f + 4.0f;
     const size_t px = (size_t)j * W + i;
     const float4 bsh = ld4(i_sh + 4 * px);
@@ -311,7 +319,7 @@ __global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, cons
     const float acc = bu.x;
     const float bm = bu.y;
     float osh[4], occ[2], var;
-    if (acc < thresh) {
+    if (kYoung) {   // acc < thresh
         const float bd = ld(t + px);
         const int bf = __ldg(face + px);
         // normal weight pow(max(dot(n, n'), 0), 16) for a clamped dot of 0, 1, 3
@@ -378,6 +386,35 @@ __global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, cons
         clampf(osh[2], -100.0f, 100.0f), clampf(osh[3], -100.0f, 100.0f));
     st2(o_cocg + 2 * px, clampf(occ[0], -10.0f, 100.0f), clampf(occ[1], -10.0f, 100.0f));
     st(o_var + px, clampf(var, -1.0f, 50.0f));
+}
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, const uint8_t* face, const S* i_sh,
+                                                  const S* i_cocg, const S* i_util, S* o_sh, S* o_cocg, S* o_var) {
+    __shared__ uint32_t s_young[256];   // young texels of the block: i | j << 16
+    __shared__ int s_n;
+    if (threadIdx.x == 0 && threadIdx.y == 0) s_n = 0;
+    __syncthreads();
+    int i, j;
+    const bool in = pixel_of(W, H, &i, &j);
+    bool young = false;
+    if (in) {
+        young = ld4(i_util + 4 * ((size_t)j * W + i)).x < 4.0f + 4.0f + 4.0f;
+        if (!young) variance_texel<S, false>(W, H, i, j, t, face, i_sh, i_cocg, i_util, o_sh, o_cocg, o_var);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, young);
+    const int lane = threadIdx.x & 31;   // blocks are 32 x 8: a warp is one row of the block
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(&s_n, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (young) s_young[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i | ((uint32_t)j << 16);
+    __syncthreads();
+    const int k = threadIdx.y * blockDim.x + threadIdx.x;
+    if (k < s_n) {
+        const uint32_t q = s_young[k];
+        variance_texel<S, true>(W, H, (int)(q & 0xffffu), (int)(q >> 16), t, face, i_sh, i_cocg, i_util, o_sh,
+                                o_cocg, o_var);
+    }
 }
 
 // SVGF/SpatialFilter.glsl main (:175-355), 3x3 taps (u_LargeKernel off).
