@@ -12,13 +12,14 @@ struct GICount {
     unsigned diffuse_rays, diffuse_steps, shadow_rays, shadow_steps;
 };
 
-// How calculate_diffuse gets its traversals. kDiffuseLive: it traces the
-// bounce and shadow rays itself. kDiffuseGiven (one bounce): the pooled
-// diffuse kernel has traced the first bounce ray (diffuse_bounce_ray,
-// staged_record) and the sun-shadow ray from its hit separately, and runs the
-// whole sample again with that hit and shadow verdict supplied instead of
-// tracing, so every value comes out of the same arithmetic as in kLive.
-enum DiffuseMode { kDiffuseLive = 0, kDiffuseGiven = 2 };
+// How calculate_diffuse gets its traversals. kLive: it traces the bounce and
+// shadow rays itself. The staged one-bounce kernel splits a sample in three:
+// kBounceOnly traces the first bounce ray, reports its hit (StagedBounce) and
+// whether a sun-shadow ray is needed from where, and stops; the shadow rays
+// are traced separately; kGiven then runs the whole sample again with that
+// bounce hit and shadow result supplied instead of tracing, so every value
+// comes out of the same arithmetic as in kLive.
+enum DiffuseMode { kDiffuseLive = 0, kDiffuseBounceOnly = 1, kDiffuseGiven = 2 };
 
 struct StagedBounce {
     float t;        // hit distance of the first bounce ray (-1: miss)
@@ -34,46 +35,22 @@ struct StagedBounce {
 // whose implicit derivatives across a pixel quad's unrelated bounce hits are
 // taken as zero) at level 0.
 //
-// kMode (DiffuseMode): kDiffuseGiven (one bounce) takes *staged and
-// given_shadow (the shadow ray's verdict, 1 = occluded) instead of tracing.
-// The first bounce ray of a sample (CalculateDiffuse :538-541): the origin
-// biased off the surface, the cosine-weighted direction from the sample's
-// random stream.
-__device__ __forceinline__ void diffuse_bounce_ray(v3 initial_origin, v3 input_normal, uint32_t* rng, v3* ro, v3* rd) {
-    const float bias = 0.06f;
-    *ro = add(initial_origin, muls(input_normal, bias));
-    *rd = cos_hemisphere(input_normal, rng);
-}
-
-// What the rest of a one-bounce sample needs from its bounce ray `tr`
-// (traced from ro along rd): the hit (StagedBounce), whether a sun-shadow ray
-// is traced from it (GetShadowAt is skipped for a stronger moon or a face
-// turned from the sun, :590-597) and that ray's origin.
-__device__ __forceinline__ void staged_record(const TraceResult& tr, v3 ro, v3 rd, const GILighting& L,
-                                              StagedBounce* sb, bool* need_shadow, v3* shadow_origin) {
-    const v3 light_dir = mk3(L.light_dir[0], L.light_dir[1], L.light_dir[2]);
-    const float T = tr.t;
-    const v3 ip = add(ro, muls(rd, T));
-    const bool hit = T > 0.0f && tr.block > 0;
-    sb->t = T;
-    sb->block = hit ? tr.block : 0;
-    sb->face = hit ? normal_id(tr.normal) : 0;
-    *need_shadow = hit && !L.moon_stronger && !(fmaxf(dot(tr.normal, light_dir), 0.0f) < 0.001f);
-    *shadow_origin = add(ip, muls(tr.normal, 0.045f));
-}
-
+// kMode (DiffuseMode), for one bounce only: kDiffuseBounceOnly fills *staged,
+// *need_shadow and *shadow_origin and returns; kDiffuseGiven takes *staged
+// and given_shadow (the shadow ray's verdict, 1 = occluded) instead of tracing.
 template <int B = 0, bool kTex = false, int kMode = kDiffuseLive>
 __device__ __forceinline__ v4 calculate_diffuse(const WorldView& w, const DiffuseArgs& a, v3 initial_origin,
                                                 v3 input_normal, uint32_t* rng, v3* odir, bool* skyhit,
-                                                GICount* cnt, const StagedBounce* staged = nullptr,
+                                                GICount* cnt, StagedBounce* staged = nullptr,
+                                                bool* need_shadow = nullptr, v3* shadow_origin = nullptr,
                                                 float given_shadow = 0.0f) {
     const GILighting& L = a.lighting;
     const v3 light_dir = mk3(L.light_dir[0], L.light_dir[1], L.light_dir[2]);
     const v3 light_color = mk3(L.light_color[0], L.light_color[1], L.light_color[2]);
     *skyhit = false;
     const float bias = 0.06f;
-    v3 ro, rd;
-    diffuse_bounce_ray(initial_origin, input_normal, rng, &ro, &rd);
+    v3 ro = add(initial_origin, muls(input_normal, bias));
+    v3 rd = cos_hemisphere(input_normal, rng);
     float ao = 1.0f;
     v3 contribution = mk3(0.0f, 0.0f, 0.0f);
     v3 throughput = mk3(1.0f, 1.0f, 1.0f);
@@ -93,6 +70,15 @@ __device__ __forceinline__ v4 calculate_diffuse(const WorldView& w, const Diffus
         float T = tr.t;
         bool intersect = T > 0.0f;
         v3 ip = add(ro, muls(rd, T));
+        if (kMode == kDiffuseBounceOnly) {
+            const bool hit = intersect && tr.block > 0;
+            staged->t = T;
+            staged->block = hit ? tr.block : 0;
+            staged->face = hit ? normal_id(tr.normal) : 0;
+            *need_shadow = hit && !L.moon_stronger && !(fmaxf(dot(tr.normal, light_dir), 0.0f) < 0.001f);
+            *shadow_origin = add(ip, muls(tr.normal, 0.045f));
+            return v4{};
+        }
         if (intersect && tr.block > 0) {
             const int bid = min(max(tr.block, 0), 127);
             Material m = material(w, bid);

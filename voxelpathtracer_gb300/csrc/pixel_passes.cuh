@@ -133,35 +133,26 @@ __device__ __forceinline__ void shadow_pixel2(const WorldView& w, const CamView&
     }
 }
 
-// The surface point, normal and random stream of a G-buffer texel's GI
-// samples (DiffuseRayTraceFrag.glsl main :822-858).
-__device__ __forceinline__ void diffuse_texel_setup(const CamView& cam, int W, int H, int i, int j,
-                                                    const DiffuseArgs& a, size_t px, float d, int face, v3* dir,
-                                                    v3* pos, v3* n, uint32_t* rng) {
-    *dir = normalize(ray_dir_at(cam, texcoord(i, j, W, H)));
-    *pos = add(ray_origin(cam), muls(*dir, d));
-    *n = normal_from_id(face, 0.5f);
-    *rng = pcg_hash((uint32_t)px + pcg_hash(a.frame_index + pcg_hash(a.seed)));
-}
-
 // DiffuseRayTraceFrag.glsl main (:822-935): `spp` GI samples of the texel.
 // kOneSample: the caller guarantees one sample (spp <= 1, sun stronger than
 // the moon), so nothing of the per-texel sums stays live across the traversal;
 // the arithmetic is the same.
 //
-// kMode (DiffuseMode, gi.cuh): kDiffuseGiven finishes a one-sample,
-// one-bounce texel from *staged and given_shadow (traced by the pooled
-// kernel) and writes the outputs. Sky texels (d < 0) are written by
-// kDiffuseLive only.
+// kMode (DiffuseMode, gi.cuh) splits a one-sample, one-bounce texel for the
+// staged kernel: kDiffuseBounceOnly traces its bounce ray into *staged (and
+// the shadow-ray request) and writes nothing; kDiffuseGiven finishes it from
+// *staged and given_shadow and writes the outputs. Sky texels (d < 0) are
+// written by kDiffuseLive only.
 template <int B, typename S, bool kOneSample = false, bool kTex = false, int kMode = kDiffuseLive>
 __device__ __forceinline__ void diffuse_pixel(const WorldView& w, const CamView& cam, int W, int H, int i, int j,
                                               const DiffuseArgs& a, size_t px, float d, int face, S* o_sh,
                                               S* o_cocg, S* o_luma, S* o_aosky, GICount* cnt,
-                                              const StagedBounce* staged = nullptr, float given_shadow = 0.0f) {
-    static_assert(kMode == kDiffuseLive || kOneSample, "the staged mode runs one sample");
-    v3 dir, pos, n;
-    uint32_t rng;
-    diffuse_texel_setup(cam, W, H, i, j, a, px, d, face, &dir, &pos, &n, &rng);
+                                              StagedBounce* staged = nullptr, bool* need_shadow = nullptr,
+                                              v3* shadow_origin = nullptr, float given_shadow = 0.0f) {
+    static_assert(kMode == kDiffuseLive || kOneSample, "the staged modes run one sample");
+    const v3 dir = normalize(ray_dir_at(cam, texcoord(i, j, W, H)));
+    const v3 pos = add(ray_origin(cam), muls(dir, d));
+    const v3 n = normal_from_id(face, 0.5f);
     float sh[4], cocg[2];
     if (kMode == kDiffuseLive && d < 0.0f) {
         irradiance_to_sh(muls(sky_radiance(dir), 2.66f), n, sh, cocg);
@@ -173,6 +164,7 @@ __device__ __forceinline__ void diffuse_pixel(const WorldView& w, const CamView&
         st(o_aosky + px * 2 + 1, 0.0f);
         return;
     }
+    uint32_t rng = pcg_hash((uint32_t)px + pcg_hash(a.frame_index + pcg_hash(a.seed)));
     int spp = kOneSample ? 1 : min(max(a.spp, 1), 32);
     if (!kOneSample && a.lighting.moon_stronger) spp *= 2;
     float tsh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, tcc[2] = {0.0f, 0.0f};
@@ -181,7 +173,9 @@ __device__ __forceinline__ void diffuse_pixel(const WorldView& w, const CamView&
     for (int s = 0; s < spp; s++) {
         v3 odir = mk3(0.0f, 0.0f, 0.0f);
         bool ss = false;
-        const v4 x = calculate_diffuse<B, kTex, kMode>(w, a, pos, n, &rng, &odir, &ss, cnt, staged, given_shadow);
+        const v4 x = calculate_diffuse<B, kTex, kMode>(w, a, pos, n, &rng, &odir, &ss, cnt, staged, need_shadow,
+                                                        shadow_origin, given_shadow);
+        if (kMode == kDiffuseBounceOnly) return;
         const v3 xc = vclamp(mk3(x.x, x.y, x.z), 0.0f, 8.0f);
         radiance = add(radiance, xc);
         acc_ao += x.w;

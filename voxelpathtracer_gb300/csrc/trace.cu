@@ -71,53 +71,37 @@ __global__ void __launch_bounds__(256, 8) k_trace_diffuse(WorldView w, CamView c
     }
 }
 
-// The same pass for one sample and one bounce, reorganised so that rays of
-// one kind fill whole warps (DiffuseRayTraceFrag.glsl main :822-935,
-// CalculateDiffuse :535-664 with one bounce). A CTA of 128 threads owns a
-// 32x16-pixel tile (16 patches of 8x4 pixels):
-//   0. sky texels (no G-buffer hit) are written at once; the texels with a hit
-//      are listed in shared memory, patch by patch;
-//   1. each listed texel's bounce ray is set up (origin, cosine-weighted
-//      direction) by one thread per texel;
-//   2. the bounce rays are traversed from a pool: every warp keeps its lanes
-//      busy by taking the next listed ray whenever at least kRefill lanes have
-//      finished theirs, so a warp no longer waits for its slowest of 32 fixed
-//      rays; a finished ray leaves only its final DDA state behind;
-//   3. one thread per texel turns that state into the hit (ray_finish) and the
-//      sun-shadow request (about one hit in eight faces the sun);
-//   4. the shadow requests, compacted, are traced by consecutive threads;
-//   5. one thread per texel finishes the sample (calculate_diffuse replayed
-//      with the recorded hit and shadow verdict) and writes the GI planes.
+// The same pass for one sample and one bounce, staged inside the CTA so that
+// rays of one kind fill whole warps (DiffuseRayTraceFrag.glsl main :822-935,
+// CalculateDiffuse :535-664 with one bounce):
+//   0. sky texels (no G-buffer hit) are written at once; texels with a hit are
+//      appended to a list in shared memory (ballot + one atomic per warp, so
+//      each warp's 8x4 patch stays together);
+//   1. one thread per listed texel traces its bounce ray and records the hit
+//      and, when the hit faces the sun, a sun-shadow ray request;
+//   2. one thread per request traces the shadow ray (about one bounce in
+//      eight needs one: without this stage nearly every warp would wait for a
+//      few lanes' shadow rays);
+//   3. one thread per listed texel finishes the sample from the recorded hit
+//      and shadow verdict and writes the GI planes.
 // Outputs and ray counts are those of k_trace_diffuse.
-constexpr int kPoolTileW = 32, kPoolTileH = 16, kPoolTexels = kPoolTileW * kPoolTileH, kPoolThreads = 128;
-constexpr int kRefill = 8;   // idle lanes that make a warp take new rays
-
 template <typename S, bool kTex>
-__global__ void __launch_bounds__(kPoolThreads, 6) k_trace_diffuse_staged(WorldView w, CamView cam, int W, int H,
-                                                                           DiffuseArgs a, const S* t,
-                                                                           const uint8_t* face, S* o_sh, S* o_cocg,
-                                                                           S* o_luma, S* o_aosky, Counters* stats) {
-    __shared__ uint32_t s_pix[kPoolTexels];          // listed texels: i | j << 16
-    __shared__ float s_ro[kPoolTexels][3];           // bounce ray origin
-    __shared__ float s_rd[kPoolTexels][3];           // and direction
-    __shared__ float4 s_end[kPoolTexels];            // final DDA position, step count; then the shadow ray origin
-    __shared__ uint8_t s_meta[kPoolTexels];          // final MinIdx | Intersection << 2
-    __shared__ float s_bt[kPoolTexels];              // bounce hit distance
-    __shared__ uint8_t s_bface[kPoolTexels], s_bblock[kPoolTexels], s_need[kPoolTexels], s_shadow[kPoolTexels];
-    __shared__ uint16_t s_slist[kPoolTexels];        // texels with a shadow request
-    __shared__ int s_n[3];                           // listed texels, pool position, shadow requests
+__global__ void __launch_bounds__(256, 6) k_trace_diffuse_staged(WorldView w, CamView cam, int W, int H,
+                                                                  DiffuseArgs a, const S* t, const uint8_t* face,
+                                                                  S* o_sh, S* o_cocg, S* o_luma, S* o_aosky,
+                                                                  Counters* stats) {
+    __shared__ uint32_t s_pix[256];         // listed texels: i | j << 16
+    __shared__ float s_bt[256];             // their bounce hit distance
+    __shared__ uint8_t s_bface[256], s_bblock[256], s_shadow[256];
+    __shared__ float4 s_ray[256];           // shadow ray origin xyz, w = listed texel
+    __shared__ int s_n[2];                  // listed texels, shadow requests
     const int tid = threadIdx.x, lane = tid & 31;
-    const unsigned full = 0xffffffffu;
-    if (tid < 3) s_n[tid] = 0;
+    if (tid < 2) s_n[tid] = 0;
     __syncthreads();
     GICount cnt = {0u, 0u, 0u, 0u};
-    const GILighting& L = a.lighting;
-
-    // 0. sky texels now, hit texels listed (a warp takes one 8x4 patch per pass)
-    for (int p = tid; p < kPoolTexels; p += kPoolThreads) {
-        const int patch = p >> 5;
-        const int i = blockIdx.x * kPoolTileW + (patch & 3) * 8 + (lane & 7);
-        const int j = blockIdx.y * kPoolTileH + (patch >> 2) * 4 + (lane >> 3);
+    {
+        int i, j;
+        tile_pixel(&i, &j);
         bool hit = false;
         if (i < W && j < H) {
             const size_t px = (size_t)j * W + i;
@@ -128,124 +112,56 @@ __global__ void __launch_bounds__(kPoolThreads, 6) k_trace_diffuse_staged(WorldV
             else
                 hit = true;
         }
-        const unsigned m = __ballot_sync(full, hit);
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
         int base = 0;
         if (lane == 0 && m) base = atomicAdd(&s_n[0], __popc(m));
-        base = __shfl_sync(full, base, 0);
+        base = __shfl_sync(0xffffffffu, base, 0);
         if (hit) s_pix[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i | ((uint32_t)j << 16);
     }
     __syncthreads();
     const int n_hit = s_n[0];
-
-    // 1. bounce rays
-    for (int k = tid; k < n_hit; k += kPoolThreads) {
-        const int i = (int)(s_pix[k] & 0xffffu), j = (int)(s_pix[k] >> 16);
+    const unsigned part = __ballot_sync(0xffffffffu, tid < n_hit);   // this warp's lanes with a listed texel
+    if (tid < n_hit) {
+        const int i = (int)(s_pix[tid] & 0xffffu), j = (int)(s_pix[tid] >> 16);
         const size_t px = (size_t)j * W + i;
-        v3 dir, pos, n, ro, rd;
-        uint32_t rng;
-        diffuse_texel_setup(cam, W, H, i, j, a, px, ld(t + px), __ldg(face + px), &dir, &pos, &n, &rng);
-        diffuse_bounce_ray(pos, n, &rng, &ro, &rd);
-        s_ro[k][0] = ro.x; s_ro[k][1] = ro.y; s_ro[k][2] = ro.z;
-        s_rd[k][0] = rd.x; s_rd[k][1] = rd.y; s_rd[k][2] = rd.z;
-    }
-    __syncthreads();
-
-    // 2. the pool: lanes take rays as they become free
-    {
-        RayState r;
-        bool active = false, drained = false;   // drained is the same on every lane of the warp
-        int item = 0;
-        for (;;) {
-            if (!drained) {
-                const unsigned idle = __ballot_sync(full, !active);
-                const int n_idle = __popc(idle);
-                if (n_idle >= kRefill || idle == full) {
-                    const int leader = __ffs(idle) - 1;
-                    int base = 0;
-                    if (lane == leader) base = atomicAdd(&s_n[1], n_idle);
-                    base = __shfl_sync(full, base, leader);
-                    if (base + n_idle >= n_hit) drained = true;
-                    if (!active) {
-                        const int q = base + __popc(idle & ((1u << lane) - 1u));
-                        if (q < n_hit) {
-                            ray_start(r, mk3(s_ro[q][0], s_ro[q][1], s_ro[q][2]),
-                                      mk3(s_rd[q][0], s_rd[q][1], s_rd[q][2]), a.diffuse_max_steps);
-                            item = q;
-                            active = true;
-                        }
-                    }
-                }
-            }
-            if (!__any_sync(full, active)) {
-                if (drained) break;
-                continue;
-            }
-            if (active && dda_step<0>(w, r)) {
-                s_end[item] = make_float4(r.o.x, r.o.y, r.o.z, __int_as_float(r.itr));
-                s_meta[item] = (uint8_t)(r.min_idx | (r.inter << 2));
-                cnt.diffuse_rays += 1;
-                cnt.diffuse_steps += (unsigned)r.itr;
-                active = false;
-            }
-        }
-    }
-    __syncthreads();
-
-    // 3. hits and shadow requests
-    for (int k = tid; k < n_hit; k += kPoolThreads) {
-        RayState r;
-        const v3 ro = mk3(s_ro[k][0], s_ro[k][1], s_ro[k][2]);
-        ray_start(r, ro, mk3(s_rd[k][0], s_rd[k][1], s_rd[k][2]), a.diffuse_max_steps);
-        const float4 e = s_end[k];
-        r.o = mk3(e.x, e.y, e.z);
-        r.itr = __float_as_int(e.w);
-        r.min_idx = s_meta[k] & 3;
-        r.inter = s_meta[k] >> 2;
-        const TraceResult tr = ray_finish(w, r);
         StagedBounce sb;
         bool need = false;
         v3 so;
-        staged_record(tr, ro, r.d, L, &sb, &need, &so);
-        s_bt[k] = sb.t;
-        s_bface[k] = (uint8_t)sb.face;
-        s_bblock[k] = (uint8_t)sb.block;
-        s_need[k] = need ? 1 : 0;
-        s_shadow[k] = 0;
-        s_end[k] = make_float4(so.x, so.y, so.z, 0.0f);
+        diffuse_pixel<0, S, true, kTex, kDiffuseBounceOnly>(w, cam, W, H, i, j, a, px, ld(t + px), __ldg(face + px),
+                                                            o_sh, o_cocg, o_luma, o_aosky, &cnt, &sb, &need, &so);
+        s_bt[tid] = sb.t;
+        s_bface[tid] = (uint8_t)sb.face;
+        s_bblock[tid] = (uint8_t)sb.block;
+        s_shadow[tid] = 0;
+        const unsigned m = __ballot_sync(part, need);
+        if (m) {   // the same for every lane of `part`
+            const int leader = __ffs(m) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(&s_n[1], __popc(m));
+            base = __shfl_sync(part, base, leader);
+            if (need)
+                s_ray[base + __popc(m & ((1u << lane) - 1u))] = make_float4(so.x, so.y, so.z, __int_as_float(tid));
+        }
     }
     __syncthreads();
-    for (int k0 = 0; k0 < n_hit; k0 += kPoolThreads) {   // compaction, in texel order
-        const int k = k0 + tid;
-        const bool need = k < n_hit && s_need[k];
-        const unsigned m = __ballot_sync(full, need);
-        int base = 0;
-        if (lane == 0 && m) base = atomicAdd(&s_n[2], __popc(m));
-        base = __shfl_sync(full, base, 0);
-        if (need) s_slist[base + __popc(m & ((1u << lane) - 1u))] = (uint16_t)k;
-    }
-    __syncthreads();
-
-    // 4. GetShadowAt (DiffuseRayTraceFrag.glsl:1202-1222) for the requests
-    const int n_sh = s_n[2];
-    const v3 light_dir = mk3(L.light_dir[0], L.light_dir[1], L.light_dir[2]);
-    for (int k = tid; k < n_sh; k += kPoolThreads) {
-        const int item = s_slist[k];
-        const float4 o = s_end[item];
-        const TraceResult sr = traverse<0>(w, mk3(o.x, o.y, o.z), light_dir, a.bounce_shadow_max_steps);
+    if (tid < s_n[1]) {
+        // GetShadowAt (DiffuseRayTraceFrag.glsl:1202-1222)
+        const float4 r = s_ray[tid];
+        const GILighting& L = a.lighting;
+        const TraceResult sr = traverse<0>(w, mk3(r.x, r.y, r.z), mk3(L.light_dir[0], L.light_dir[1], L.light_dir[2]),
+                                           a.bounce_shadow_max_steps);
         cnt.shadow_rays += 1;
         cnt.shadow_steps += (unsigned)sr.steps;
-        s_shadow[item] = sr.t > 0.0f ? 1 : 0;
+        s_shadow[__float_as_int(r.w)] = sr.t > 0.0f ? 1 : 0;
     }
     __syncthreads();
-
-    // 5. the samples, finished
-    for (int k = tid; k < n_hit; k += kPoolThreads) {
-        const int i = (int)(s_pix[k] & 0xffffu), j = (int)(s_pix[k] >> 16);
+    if (tid < n_hit) {
+        const int i = (int)(s_pix[tid] & 0xffffu), j = (int)(s_pix[tid] >> 16);
         const size_t px = (size_t)j * W + i;
-        const StagedBounce sb{s_bt[k], (int)s_bface[k], (int)s_bblock[k]};
+        StagedBounce sb{s_bt[tid], (int)s_bface[tid], (int)s_bblock[tid]};
         diffuse_pixel<0, S, true, kTex, kDiffuseGiven>(w, cam, W, H, i, j, a, px, ld(t + px), __ldg(face + px), o_sh,
-                                                       o_cocg, o_luma, o_aosky, &cnt, &sb,
-                                                       s_shadow[k] ? 1.0f : 0.0f);
+                                                       o_cocg, o_luma, o_aosky, &cnt, &sb, nullptr, nullptr,
+                                                       s_shadow[tid] ? 1.0f : 0.0f);
     }
     if (stats) {
         count_rays(stats, kRayDiffuse, cnt.diffuse_rays, cnt.diffuse_steps);
@@ -296,13 +212,13 @@ cudaError_t trace_diffuse(const WorldView& w, const CamView& cam, int W, int H, 
                           const void* t, const uint8_t* face, GIOut out, Counters* stats, cudaStream_t s) {
     const bool one = a.spp <= 1 && !a.lighting.moon_stronger, tex = a.textured != 0;
     if (one && a.bounces == 1 && W < 65536 && H < 65536) {
-        const dim3 g((unsigned)((W + kPoolTileW - 1) / kPoolTileW), (unsigned)((H + kPoolTileH - 1) / kPoolTileH));
+        const dim3 g = tile_grid(W, H);
         if (fp16)
-            (tex ? k_trace_diffuse_staged<__half, true> : k_trace_diffuse_staged<__half, false>)<<<g, kPoolThreads, 0, s>>>(
+            (tex ? k_trace_diffuse_staged<__half, true> : k_trace_diffuse_staged<__half, false>)<<<g, 256, 0, s>>>(
                 w, cam, W, H, a, (const __half*)t, face, (__half*)out.sh, (__half*)out.cocg, (__half*)out.luma,
                 (__half*)out.aosky, stats);
         else
-            (tex ? k_trace_diffuse_staged<float, true> : k_trace_diffuse_staged<float, false>)<<<g, kPoolThreads, 0, s>>>(
+            (tex ? k_trace_diffuse_staged<float, true> : k_trace_diffuse_staged<float, false>)<<<g, 256, 0, s>>>(
                 w, cam, W, H, a, (const float*)t, face, (float*)out.sh, (float*)out.cocg, (float*)out.luma,
                 (float*)out.aosky, stats);
         return cudaGetLastError();
