@@ -268,7 +268,8 @@ def run_ours(args):
             b /= float(args.gi_divisor * args.gi_divisor)
         gbs = b / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
         kernels[p] = {"bound": "hbm", "launches_per_frame": launches_per_frame, "ms_per_launch": per_launch_ms,
-                      "algorithmic_bytes_per_launch": b, "achieved_gbs": gbs, "frac": gbs / peak}
+                      "algorithmic_bytes_per_launch": b, "achieved_gbs": gbs, "frac": gbs / peak,
+                      "issue_frac": issue_roof(KERNEL_NAMES[p], per_launch_ms, sm_count, clk.get("sm_mhz"))}
         if fused_pre:
             kernels[p]["kernel"] = "k_pre_temporal"
     dom = max((p for p in mean_pass if p not in TRACE_KINDS), key=mean_pass.get)
@@ -679,9 +680,20 @@ def profile_metrics(kernel):
     for m in re.finditer(r"^\| ([^|]+?) \| ([0-9.eE+-]+) \| ([^|]*?) \|$", path.read_text(), re.M):
         name, val, unit = m.group(1).strip(), m.group(2), m.group(3).strip()
         if unit in units:
-            out[name] = float(val) * units[unit]
-    out["_source"] = f"profiles/{path.name}"
-    return out
+            out.setdefault(name, []).append(float(val) * units[unit])   # one value per captured launch
+    return {k: float(np.mean(v)) for k, v in out.items()} | {"_source": f"profiles/{path.name}",
+                                                             "_launches": max(map(len, out.values()), default=0)}
+
+
+def issue_roof(kernel, ms_per_launch, sm_count, sm_mhz):
+    """Fraction of the instruction-issue roof (SMs x 4 schedulers x the sampled
+    SM clock, one warp instruction per scheduler and cycle) a kernel reaches:
+    its warp instructions per launch (committed ncu summary, mean over the
+    captured launches) over its event-timed duration."""
+    m = profile_metrics(kernel)
+    if "instructions (warp)" not in m or not sm_mhz or ms_per_launch <= 0:
+        return None
+    return m["instructions (warp)"] / (ms_per_launch * 1e-3) / (sm_count * 4 * sm_mhz * 1e6)
 
 
 def l2_read_roof(vpt, local):
