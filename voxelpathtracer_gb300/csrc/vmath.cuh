@@ -74,6 +74,10 @@ VPT_HD float pow2i(int n) { return f_from_bits((uint32_t)(n + 127) << 23); }
 // p * 2^k in two exact steps, so a subnormal result is rounded once (either
 // split of k gives the same bits while p * 2^k1 stays normal)
 VPT_HD float scale2(float p, int k) {
+    // p is in [0.70, 1.42] (exp_poly of |r| <= ln2 / 2): for -125 <= k <= 127
+    // 2^k is a normal float and the product stays normal, so one exact
+    // multiply gives the same bits as the two steps
+    if (k >= -125 && k <= 127) return p * pow2i(k);
     int k1 = k >> 1;
     int k2 = k - k1;
     return (p * pow2i(k1)) * pow2i(k2);
