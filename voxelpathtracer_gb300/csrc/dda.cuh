@@ -51,34 +51,29 @@ __device__ __forceinline__ void ray_start(RayState& r, v3 origin, v3 dir, int ma
 }
 
 // One exact DDA face step (:341-356), the E == 1 branch's body; updates the
-// origin and MinIdx. With s = sign(direction) and h = (1 + s) / 2, the values
-// the shader builds from them are selected directly from the direction's
-// signs: float(h) is 1 for a positive component and 0 otherwise, float(1 - h)
-// the opposite, float(s) * 0.0001 is +-0.0001 or 0 - the same floats, fewer
-// integer steps.
+// origin and MinIdx.
 __device__ __forceinline__ void dda_face_step(RayState& r) {
-    const bool px = r.d.x > 0.0f, py = r.d.y > 0.0f, pz = r.d.z > 0.0f;
-    const bool nx = r.d.x < 0.0f, ny = r.d.y < 0.0f, nz = r.d.z < 0.0f;
+    const int sx = isign(r.d.x), sy = isign(r.d.y), sz = isign(r.d.z);
+    const int hx = (1 + sx) >> 1, hy = (1 + sy) >> 1, hz = (1 + sz) >> 1;
     int gx = f2i(r.o.x), gy = f2i(r.o.y), gz = f2i(r.o.z);
     float wx = r.o.x - (float)gx, wy = r.o.y - (float)gy, wz = r.o.z - (float)gz;
-    const float dfx = ((px ? 1.0f : 0.0f) - wx) * r.ix;
-    const float dfy = ((py ? 1.0f : 0.0f) - wy) * r.iy;
-    const float dfz = ((pz ? 1.0f : 0.0f) - wz) * r.iz;
-    const bool sx0 = !(px || nx), sz0 = !(pz || nz);   // sign 0
-    const int m = (dfx < dfy && !sx0) ? ((dfx < dfz || sz0) ? 0 : 2) : ((dfy < dfz || sz0) ? 1 : 2);
+    const float dfx = ((float)hx - wx) * r.ix;
+    const float dfy = ((float)hy - wy) * r.iy;
+    const float dfz = ((float)hz - wz) * r.iz;
+    const int m = (dfx < dfy && sx != 0) ? ((dfx < dfz || sz == 0) ? 0 : 2) : ((dfy < dfz || sz == 0) ? 1 : 2);
     const float dm = m == 0 ? dfx : (m == 1 ? dfy : dfz);
     wx = wx + r.d.x * dm;
     wy = wy + r.d.y * dm;
     wz = wz + r.d.z * dm;
-    if (m == 0) { gx += px ? 1 : (nx ? -1 : 0); wx = px ? 0.0f : 1.0f; }
-    else if (m == 1) { gy += py ? 1 : (ny ? -1 : 0); wy = py ? 0.0f : 1.0f; }
-    else { gz += pz ? 1 : (nz ? -1 : 0); wz = pz ? 0.0f : 1.0f; }
+    if (m == 0) { gx += sx; wx = (float)(1 - hx); }
+    else if (m == 1) { gy += sy; wy = (float)(1 - hy); }
+    else { gz += sz; wz = (float)(1 - hz); }
     r.o.x = (float)gx + wx;
     r.o.y = (float)gy + wy;
     r.o.z = (float)gz + wz;
-    if (m == 0) r.o.x = r.o.x + (px ? 0.0001f : (nx ? -0.0001f : 0.0f));
-    else if (m == 1) r.o.y = r.o.y + (py ? 0.0001f : (ny ? -0.0001f : 0.0f));
-    else r.o.z = r.o.z + (pz ? 0.0001f : (nz ? -0.0001f : 0.0f));
+    if (m == 0) r.o.x = r.o.x + (float)sx * 0.0001f;
+    else if (m == 1) r.o.y = r.o.y + (float)sy * 0.0001f;
+    else r.o.z = r.o.z + (float)sz * 0.0001f;
     r.min_idx = m;
 }
 
