@@ -98,9 +98,12 @@ __device__ __forceinline__ void batch_tile_pair(const BatchLaunch& a, const Batc
 }
 
 // kRays: pixels (rays of a pass) per lane, 1 or 2; a warp takes
-// tiles_per_grab * kRays tiles per queue access.
-template <int B, int kRays>
-__global__ void __launch_bounds__(512, 3) k_batch_trace(BatchLaunch a) {
+// tiles_per_grab * kRays tiles per queue access. kWide: blocks of up to 512
+// threads, three per SM (40 registers a thread); otherwise up to 256
+// threads, four per SM (64 registers, far fewer spills of the diffuse path's
+// state).
+template <int B, int kRays, bool kWide>
+__global__ void __launch_bounds__(kWide ? 512 : 256, kWide ? 3 : 4) k_batch_trace(BatchLaunch a) {
     __shared__ int s_begin[kBatchMaxWorlds + 1];
     for (int k = threadIdx.x; k <= a.n_worlds; k += blockDim.x) s_begin[k] = a.tile_begin[k];
     __syncthreads();
@@ -144,7 +147,12 @@ __global__ void __launch_bounds__(256) k_df_bricks(const uint8_t* __restrict__ d
 template <int B, int kRays>
 int max_blocks_for(int block_threads) {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_trace<B, kRays>, block_threads, 0) != cudaSuccess) {
+    const cudaError_t e = block_threads > 256
+                              ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_trace<B, kRays, true>,
+                                                                              block_threads, 0)
+                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_trace<B, kRays, false>,
+                                                                              block_threads, 0);
+    if (e != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
@@ -173,12 +181,15 @@ cudaError_t batch_trace(const BatchLaunch& a, int df_brick, int block_threads, i
     if (blocks <= 0) blocks = batch_max_blocks(df_brick, block_threads, rays_per_lane, dev);
     if (blocks <= 0) return cudaErrorInvalidConfiguration;
     const bool two = rays_per_lane == 2;
-    switch (df_brick) {
-        case 0: (two ? k_batch_trace<0, 2> : k_batch_trace<0, 1>)<<<blocks, block_threads, 0, s>>>(a); break;
-        case 4: (two ? k_batch_trace<4, 2> : k_batch_trace<4, 1>)<<<blocks, block_threads, 0, s>>>(a); break;
-        case 8: (two ? k_batch_trace<8, 2> : k_batch_trace<8, 1>)<<<blocks, block_threads, 0, s>>>(a); break;
-        default: return cudaErrorInvalidValue;
-    }
+    using K = void (*)(BatchLaunch);
+    // [brick 0 / 4 / 8][one / two rays][narrow / wide blocks]
+    const K table[3][2][2] = {
+        {{k_batch_trace<0, 1, false>, k_batch_trace<0, 1, true>}, {k_batch_trace<0, 2, false>, k_batch_trace<0, 2, true>}},
+        {{k_batch_trace<4, 1, false>, k_batch_trace<4, 1, true>}, {k_batch_trace<4, 2, false>, k_batch_trace<4, 2, true>}},
+        {{k_batch_trace<8, 1, false>, k_batch_trace<8, 1, true>}, {k_batch_trace<8, 2, false>, k_batch_trace<8, 2, true>}}};
+    const int bi = df_brick == 0 ? 0 : (df_brick == 4 ? 1 : (df_brick == 8 ? 2 : -1));
+    if (bi < 0) return cudaErrorInvalidValue;
+    table[bi][two ? 1 : 0][block_threads > 256 ? 1 : 0]<<<blocks, block_threads, 0, s>>>(a);
     return cudaGetLastError();
 }
 
