@@ -509,10 +509,15 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf,
                 const float sl = sh_to_y(ssh);
                 // clamp(pow(max(dot(n, n'), 0), 32), 0.001, 1) for a clamped dot of 0, 1 or 3
                 const float nw = face_cos(bf, sface) > 0 ? 1.0f : 0.001f;
-                const float lw = fabsf(sl - bl) / phi;
                 const float de = dexp(-fmaxf(dd, 0.00001f));
                 const float dw = clampf(de * de, 0.0001f, 1.0f);   // pow(e, 2) for e in [0, 1)
-                float wgt = strong ? nw * dw : (dexp(-lw) * nw) * dw;
+                float wgt;
+                if (strong) {   // young histories: no luminance weight (nor its division and exponential)
+                    wgt = nw * dw;
+                } else {
+                    const float lw = fabsf(sl - bl) / phi;
+                    wgt = (dexp(-lw) * nw) * dw;
+                }
                 wgt = clampf(wgt, 0.001f, 1.0f);
                 const float xw = aw[x < 0 ? -x : x], yw = aw[y < 0 ? -y : y];
                 wgt = (xw * yw) * wgt;
