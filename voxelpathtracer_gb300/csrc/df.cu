@@ -121,8 +121,9 @@ __global__ void __launch_bounds__(128) k_df_z(uint8_t* df, int X, int Y, int Z) 
 // x sweep, X % 16 == 0 and X <= 1024. A row of X bytes is S = X / 16
 // segments; L lanes (a power of two >= S, at most 32) work on one row, each on
 // kSegs = ceil(S / L) consecutive segments held in registers, so a warp holds
-// 32 / L rows. Each warp does two such row groups, with the loads of both
-// issued before either is processed (twice the bytes in flight).
+// 32 / L rows. Each warp does kGroups such row groups, with the loads of all
+// of them issued before any is processed (more bytes in flight).
+constexpr int kGroups = 4;
 
 // The distances of one row group's segments v (row `row`, this lane's
 // segments from s0); every lane of the warp calls it.
@@ -195,18 +196,21 @@ __global__ void __launch_bounds__(256) k_df_x16(const uint4* __restrict__ vox, u
     const int rows_per_warp = 32 / L;
     const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int sub = lane / L, l = lane % L;                 // row within the group, lane within the row
-    const int row0 = (2 * warp) * rows_per_warp + sub, row1 = row0 + rows_per_warp;
-    const bool live0 = row0 < rows, live1 = row1 < rows;
     // segments [s0, s0 + kSegs) of a row belong to this lane
     const int s0 = l * kSegs;
-    uint4 v0[kSegs], v1[kSegs];
+    int row[kGroups];
+    bool live[kGroups];
+    uint4 v[kGroups][kSegs];
 #pragma unroll
-    for (int k = 0; k < kSegs; k++) {
-        v0[k] = (live0 && s0 + k < S) ? __ldg(vox + (size_t)row0 * S + s0 + k) : make_uint4(0u, 0u, 0u, 0u);
-        v1[k] = (live1 && s0 + k < S) ? __ldg(vox + (size_t)row1 * S + s0 + k) : make_uint4(0u, 0u, 0u, 0u);
+    for (int g = 0; g < kGroups; g++) {
+        row[g] = (kGroups * warp + g) * rows_per_warp + sub;
+        live[g] = row[g] < rows;
+#pragma unroll
+        for (int k = 0; k < kSegs; k++)
+            v[g][k] = (live[g] && s0 + k < S) ? __ldg(vox + (size_t)row[g] * S + s0 + k) : make_uint4(0u, 0u, 0u, 0u);
     }
-    x_row<kSegs>(v0, df, S, L, l, s0, row0, live0, maxd);
-    x_row<kSegs>(v1, df, S, L, l, s0, row1, live1, maxd);
+#pragma unroll
+    for (int g = 0; g < kGroups; g++) x_row<kSegs>(v[g], df, S, L, l, s0, row[g], live[g], maxd);
 }
 
 // y or z sweep over a tile: x in [x0, x0 + w) (w a multiple of 16, at most
@@ -240,10 +244,26 @@ __global__ void __launch_bounds__(128) k_df_sweep_tile(uint8_t* __restrict__ df,
     const int w = min(kTile, X - x0);
     const int q = w >> 4;   // 16-byte words per row
     uint8_t* base = df + (size_t)blockIdx.y * outer + x0;
-    for (int k = threadIdx.x; k < n * q; k += blockDim.x) {
-        const int r = k / q, c = k - r * q;
-        reinterpret_cast<uint4*>(tile + (size_t)r * w)[c] =
-            *reinterpret_cast<const uint4*>(base + (size_t)r * stride + 16 * c);
+    // four independent 128-bit loads in flight per thread before they are stored
+    const int nq = n * q;
+    for (int k0 = threadIdx.x; k0 < nq; k0 += 4 * blockDim.x) {
+        uint4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int k = k0 + u * blockDim.x;
+            if (k < nq) {
+                const int r = k / q, c = k - r * q;
+                v[u] = *reinterpret_cast<const uint4*>(base + (size_t)r * stride + 16 * c);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int k = k0 + u * blockDim.x;
+            if (k < nq) {
+                const int r = k / q, c = k - r * q;
+                reinterpret_cast<uint4*>(tile + (size_t)r * w)[c] = v[u];
+            }
+        }
     }
     __syncthreads();
     const int G = w >> 2;                   // column groups (words per row)
@@ -296,7 +316,7 @@ __global__ void __launch_bounds__(128) k_df_sweep_tile(uint8_t* __restrict__ df,
         col[(size_t)r * G] = pack_pairs(Bl, Bh);
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < n * q; k += blockDim.x) {
+    for (int k = threadIdx.x; k < nq; k += blockDim.x) {
         const int r = k / q, c = k - r * q;
         *reinterpret_cast<uint4*>(base + (size_t)r * stride + 16 * c) =
             reinterpret_cast<const uint4*>(tile + (size_t)r * w)[c];
@@ -382,7 +402,7 @@ cudaError_t launch_x16(const uint8_t* vox, uint8_t* df, int X, int rows, int max
     const int S = X / 16;
     int L = 1;
     while (L < S && L < 32) L <<= 1;
-    const int rows_per_warp = 2 * (32 / L);
+    const int rows_per_warp = kGroups * (32 / L);
     const long long threads = (long long)(rows + rows_per_warp - 1) / rows_per_warp * 32;
     k_df_x16<kSegs><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
         reinterpret_cast<const uint4*>(vox), reinterpret_cast<uint4*>(df), S, L, rows, maxd);
