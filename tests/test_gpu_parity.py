@@ -178,11 +178,11 @@ def test_fused_trace_frame_bit_exact(vpt, oracle, scene, storage, threshold, blo
             ctx.end_frame()
 
 
-@pytest.mark.parametrize("fused", [False, True], ids=["passes", "fused"])
-def test_render_frame_matches_oracle(vpt, oracle, scene, fused, gpu):
+@pytest.mark.parametrize("mode", ["passes", "fused", "overlap_shadow"])
+def test_render_frame_matches_oracle(vpt, oracle, scene, mode, gpu):
     world = scene["world"]
     ctx = make_ctx(vpt, scene, vpt.STORAGE_F32)
-    ctx.set_tuning(fused_trace=fused)
+    ctx.set_tuning(fused_trace=mode == "fused", overlap_shadow=mode == "overlap_shadow")
     prev_g, hist = oracle.empty_history(H, W)
     prev_cam = scene["cams"][0]
     for fi, cam in enumerate(scene["cams"]):

@@ -104,7 +104,7 @@ class TraceBuffers(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("refill_threshold", C.c_int32), ("trace_blocks", C.c_int32), ("fused_trace", C.c_int32),
-                ("fused_prefilter", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("fused_prefilter", C.c_int32), ("overlap_shadow", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class BatchConfig(C.Structure):
@@ -576,7 +576,8 @@ class Context:
         self._ck(lib.vpt_trace_frame(self._h, C.byref(cam), C.byref(frame)), "vpt_trace_frame")
 
     def set_tuning(self, refill_threshold: int | None = None, trace_blocks: int | None = None,
-                   fused_trace: bool | None = None, fused_prefilter: bool | None = None):
+                   fused_trace: bool | None = None, fused_prefilter: bool | None = None,
+                   overlap_shadow: bool | None = None):
         t = self.tuning()
         if refill_threshold is not None:
             t.refill_threshold = refill_threshold
@@ -586,6 +587,8 @@ class Context:
             t.fused_trace = 1 if fused_trace else 0
         if fused_prefilter is not None:
             t.fused_prefilter = 1 if fused_prefilter else 0
+        if overlap_shadow is not None:
+            t.overlap_shadow = 1 if overlap_shadow else 0
         self._ck(lib.vpt_set_tuning(self._h, C.byref(t)), "vpt_set_tuning")
 
     def tuning(self) -> Tuning:

@@ -153,6 +153,12 @@ struct vpt_ctx {
     cudaEvent_t ev_color = nullptr, ev_copy = nullptr;
     bool copy_pending = false;
     void* color_stage = nullptr;
+    // the sun-shadow pass overlapped with the diffuse trace and SVGF
+    // (vpt_tuning.overlap_shadow): its stream, the fork and join events, and
+    // whether a forked shadow pass has not been joined yet
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool shadow_forked = false;
 };
 
 namespace {
@@ -360,14 +366,28 @@ vpt_status clear_history(vpt_ctx* c) {
     return VPT_OK;
 }
 
-void pass_begin(vpt_ctx* c, int pass) {
+void pass_begin(vpt_ctx* c, int pass, cudaStream_t st = nullptr) {
     if (c->profiling) {
-        cudaEventRecord(c->ev[pass][0], c->stream);
+        cudaEventRecord(c->ev[pass][0], st ? st : c->stream);
         c->ev_used[pass] = true;
     }
 }
-void pass_end(vpt_ctx* c, int pass) {
-    if (c->profiling) cudaEventRecord(c->ev[pass][1], c->stream);
+void pass_end(vpt_ctx* c, int pass, cudaStream_t st = nullptr) {
+    if (c->profiling) cudaEventRecord(c->ev[pass][1], st ? st : c->stream);
+}
+
+vpt_status shadow_run(vpt_ctx* c, const vpt_frame* f, cudaStream_t st);
+
+// Makes the context stream wait for a sun-shadow pass forked onto the side
+// stream (before anything that reads the shadow plane).
+vpt_status join_shadow(vpt_ctx* c) {
+    if (!c->shadow_forked) return VPT_OK;
+    c->shadow_forked = false;
+    if (cudaStreamWaitEvent(c->stream, c->ev_join, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return VPT_ERR_CUDA;
+    }
+    return VPT_OK;
 }
 
 vpt_status check_world(vpt_ctx* c) {
@@ -539,6 +559,10 @@ vpt_status vpt_destroy(vpt_ctx* c) {
     if (c->ev_color) cudaEventDestroy(c->ev_color);
     if (c->ev_copy) cudaEventDestroy(c->ev_copy);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    if (c->side_stream) cudaStreamSynchronize(c->side_stream);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side_stream) cudaStreamDestroy(c->side_stream);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return VPT_OK;
@@ -803,11 +827,23 @@ vpt_status vpt_trace_primary(vpt_ctx* c, const vpt_camera* cam) {
 
 vpt_status vpt_trace_shadow(vpt_ctx* c, const vpt_frame* f) {
     if (!c) return VPT_ERR_INVALID_ARG;
+    vpt_status s = join_shadow(c);
+    if (s != VPT_OK) return fail(c, s, "joining the previous shadow pass failed");
+    return shadow_run(c, f, c->stream);
+}
+
+}  // extern "C"
+
+namespace {
+
+// The sun-shadow pass on stream `st` (the context stream, or the side stream
+// when it overlaps the diffuse trace and SVGF).
+vpt_status shadow_run(vpt_ctx* c, const vpt_frame* f, cudaStream_t st) {
     vpt_status s = check_world(c);
     if (s != VPT_OK) return s;
     if ((s = check_frame(c, f)) != VPT_OK) return s;
     cudaSetDevice(c->dev);
-    pass_begin(c, VPT_PASS_SHADOW);
+    pass_begin(c, VPT_PASS_SHADOW, st);
     // the alpha-tested shadow rays with block textures (ShouldAlphaTestShadows)
     AlphaStop stop;
     const bool alpha = c->cfg.alpha_test_shadows && c->textured;
@@ -820,11 +856,15 @@ vpt_status vpt_trace_shadow(vpt_ctx* c, const vpt_frame* f) {
     }
     CK(c, trace_shadow(world_view(c), cam_view(c->cam), c->cfg.width, c->cfg.height, c->cfg.shadow_max_steps,
                        f->sun_dir, c->fp16, c->gbuf[c->cur][GB_T], (const uint8_t*)c->gbuf[c->cur][GB_FACE],
-                       c->shadow, c->stats ? c->counters : nullptr, c->stream, alpha ? &stop : nullptr));
-    pass_end(c, VPT_PASS_SHADOW);
+                       c->shadow, c->stats ? c->counters : nullptr, st, alpha ? &stop : nullptr));
+    pass_end(c, VPT_PASS_SHADOW, st);
     c->launches += 1;
     return VPT_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 vpt_status vpt_trace_diffuse(vpt_ctx* c, const vpt_frame* f) {
     if (!c) return VPT_ERR_INVALID_ARG;
@@ -971,9 +1011,10 @@ vpt_status vpt_ground_truth(vpt_ctx* c, const vpt_frame* f, int32_t x0, int32_t 
 vpt_status vpt_set_tuning(vpt_ctx* c, const vpt_tuning* t) {
     if (!c || !t) return VPT_ERR_INVALID_ARG;
     if (t->refill_threshold < 1 || t->refill_threshold > 32 || t->trace_blocks < 0 || t->trace_blocks > 65535 ||
-        t->fused_trace < 0 || t->fused_trace > 1 || t->fused_prefilter < 0 || t->fused_prefilter > 1)
-        return fail(c, VPT_ERR_INVALID_ARG,
-                    "refill_threshold must be 1..32, trace_blocks 0..65535, fused_trace and fused_prefilter 0/1");
+        t->fused_trace < 0 || t->fused_trace > 1 || t->fused_prefilter < 0 || t->fused_prefilter > 1 ||
+        t->overlap_shadow < 0 || t->overlap_shadow > 1)
+        return fail(c, VPT_ERR_INVALID_ARG, "refill_threshold must be 1..32, trace_blocks 0..65535, fused_trace, "
+                                            "fused_prefilter and overlap_shadow 0/1");
     c->tuning = *t;
     return VPT_OK;
 }
@@ -1118,6 +1159,7 @@ void denoised_gi(vpt_ctx* c, const void** sh, const void** cocg, const void** ao
 vpt_status reflection_run(vpt_ctx* c, const vpt_frame* f) {
     vpt_status s = check_world(c);
     if (s != VPT_OK) return s;
+    if ((s = join_shadow(c)) != VPT_OK) return fail(c, s, "joining the shadow pass failed");
     if ((s = check_frame(c, f)) != VPT_OK) return s;
     if (c->cfg.reflection_spp <= 0) return fail(c, VPT_ERR_STATE, "reflections are off (reflection_spp = 0)");
     cudaSetDevice(c->dev);
@@ -1221,6 +1263,7 @@ vpt_status reflection_run(vpt_ctx* c, const vpt_frame* f) {
 vpt_status shade_run(vpt_ctx* c, const vpt_frame* f, int source, void* out = nullptr) {
     vpt_status s = check_world(c);
     if (s != VPT_OK) return s;
+    if ((s = join_shadow(c)) != VPT_OK) return fail(c, s, "joining the shadow pass failed");
     if ((s = check_frame(c, f)) != VPT_OK) return s;
     cudaSetDevice(c->dev);
     ShadeArgs a;
@@ -1279,7 +1322,24 @@ vpt_status trace_all(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f) {
     vpt_status s;
     if (c->tuning.fused_trace && c->gd == 1 && !c->textured) return vpt_trace_frame(c, cam, f);
     if ((s = vpt_trace_primary(c, cam)) != VPT_OK) return s;
-    if ((s = vpt_trace_shadow(c, f)) != VPT_OK) return s;
+    if (c->tuning.overlap_shadow) {
+        // the shadow pass reads only this frame's G-buffer and writes only the
+        // shadow plane, which nothing reads before the reflection and colour
+        // passes: it runs on the side stream beside the diffuse trace and SVGF
+        if (!c->side_stream) {
+            CK(c, cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking));
+            CK(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+            CK(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+        }
+        if ((s = join_shadow(c)) != VPT_OK) return fail(c, s, "joining the previous shadow pass failed");
+        CK(c, cudaEventRecord(c->ev_fork, c->stream));
+        CK(c, cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
+        if ((s = shadow_run(c, f, c->side_stream)) != VPT_OK) return s;
+        CK(c, cudaEventRecord(c->ev_join, c->side_stream));
+        c->shadow_forked = true;
+    } else if ((s = vpt_trace_shadow(c, f)) != VPT_OK) {
+        return s;
+    }
     return vpt_trace_diffuse(c, f);
 }
 
@@ -1399,6 +1459,7 @@ vpt_status vpt_render_frame_learned(vpt_ctx* c, vpt_unet* net, const vpt_camera*
 
 vpt_status vpt_end_frame(vpt_ctx* c) {
     if (!c) return VPT_ERR_INVALID_ARG;
+    if (join_shadow(c) != VPT_OK) return fail(c, VPT_ERR_CUDA, "joining the shadow pass failed");
     if (c->have_cam) {
         c->prev_cam = c->cam;
         c->have_prev = true;

@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(128) k_df_sweep_tile(uint8_t* __restrict__ df,
 // segmented scheme of k_df_sweep_tile over the slice's full width, and the
 // slice is written once: one read and one write per voxel for two sweeps.
 constexpr int kSliceSmemMax = 96 * 1024;
-constexpr int kSliceThreads = 256;
+constexpr int kSliceThreads = 1024;
 
 __global__ void __launch_bounds__(kSliceThreads) k_df_xy_slice(const uint8_t* __restrict__ vox,
                                                                uint8_t* __restrict__ df, int X, int Y, int maxd) {
