@@ -184,8 +184,8 @@ def run_ours(args):
     vox, blocks, yaw, pitch = workload_inputs(vpt, seed=rank)
     ctx = vpt.Context(width=W, height=H, device=local, storage=args.storage, gi_divisor=args.gi_divisor,
                       reflection_spp=args.reflection_spp)
-    if args.overlap_shadow:
-        ctx.set_tuning(overlap_shadow=True)
+    if args.inline_shadow:
+        ctx.set_tuning(overlap_shadow=False)
     ctx.upload_world(vox)
     ctx.set_block_table(blocks)
     ctx.build_df()
@@ -974,8 +974,9 @@ def main():
     ap.add_argument("--no-quality", action="store_true", help="skip the ground-truth error measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-world batched comparison")
     ap.add_argument("--no-df", action="store_true", help="skip the distance-field build timing")
-    ap.add_argument("--overlap-shadow", action="store_true",
-                    help="run the main frame's sun-shadow pass on a second stream (vpt_tuning.overlap_shadow)")
+    ap.add_argument("--inline-shadow", action="store_true",
+                    help="run the main frame's sun-shadow pass in line on the context stream instead of on a second "
+                         "stream beside the diffuse trace and SVGF (vpt_tuning.overlap_shadow = 0)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-denoiser measurements")
     ap.add_argument("--no-large", action="store_true", help="skip the 512^3 / 3840x2160 combined run")
     ap.add_argument("--gt-spp", type=int, default=4096, help="samples per pixel of the FP64 ground truth")

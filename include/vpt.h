@@ -199,8 +199,8 @@ typedef struct vpt_tuning {
     int32_t fused_prefilter;         /* SVGF runs Spatial3x3Initial inside the temporal kernel (1) or as its own
                                         launch before it (0, default: measured faster); the same planes either way */
     int32_t overlap_shadow;          /* vpt_render_frame* run the sun-shadow pass on a second stream beside the
-                                        diffuse trace and SVGF, joined before the reflection and colour passes (1),
-                                        or in line (0, default) */
+                                        diffuse trace and SVGF, joined before the reflection and colour passes (1,
+                                        default: 1.878 against 1.916 ms per 1080p frame), or in line (0) */
     int32_t reserved[3];
 } vpt_tuning;
 

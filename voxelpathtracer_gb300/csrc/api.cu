@@ -517,6 +517,7 @@ vpt_status vpt_create(vpt_ctx** out, const vpt_config* cfg) {
     c->dev = cfg->device;
     c->tuning.refill_threshold = 16;
     c->tuning.trace_blocks = 0;
+    c->tuning.overlap_shadow = 1;
     c->fp16 = cfg->storage == VPT_STORAGE_F16;
     c->npx = (size_t)cfg->width * (size_t)cfg->height;
     c->gd = gd;

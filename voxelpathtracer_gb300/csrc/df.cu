@@ -6,9 +6,7 @@
 // nearest non-air voxel); these kernels produce the same bytes.
 //
 // Vectorised path (X a multiple of 16 up to 1024, lines along y and z up to
-// 1536 voxels, both volumes 16-byte aligned: every benchmark world). Where an
-// XY slice fits in shared memory (256^3 and smaller worlds), k_df_xy_slice
-// does the x and y sweeps of a slice in one pass; otherwise:
+// 1536 voxels, both volumes 16-byte aligned: every benchmark world):
 //   x: k_df_x16 -- each lane owns one 16-byte segment of a row (one 128-bit
 //      load), finds the nearest solid voxel left and right of each byte from
 //      its own segment and a shuffle scan over the row's lanes, and writes the
@@ -325,105 +323,6 @@ __global__ void __launch_bounds__(128) k_df_sweep_tile(uint8_t* __restrict__ df,
     }
 }
 
-// The x and y sweeps of one z slice in one kernel, for slices that fit in
-// shared memory (X % 16 == 0, X <= 512, X * Y <= kSliceSmemMax): the slice is
-// read once with 128-bit loads, each row's x transform is done in place
-// (x_row, a row group per warp), then each column's y transform with the
-// segmented scheme of k_df_sweep_tile over the slice's full width, and the
-// slice is written once: one read and one write per voxel for two sweeps.
-constexpr int kSliceSmemMax = 96 * 1024;
-constexpr int kSliceThreads = 1024;
-
-__global__ void __launch_bounds__(kSliceThreads) k_df_xy_slice(const uint8_t* __restrict__ vox,
-                                                               uint8_t* __restrict__ df, int X, int Y, int maxd) {
-    extern __shared__ __align__(16) uint8_t slice[];
-    __shared__ unsigned s_carry[4][kSliceThreads];
-    const size_t base = (size_t)blockIdx.x * X * Y;
-    const int nq = X * Y / 16;
-    for (int k0 = threadIdx.x; k0 < nq; k0 += 4 * kSliceThreads) {
-        uint4 v[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int k = k0 + u * kSliceThreads;
-            if (k < nq) v[u] = __ldg(reinterpret_cast<const uint4*>(vox + base) + k);
-        }
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int k = k0 + u * kSliceThreads;
-            if (k < nq) reinterpret_cast<uint4*>(slice)[k] = v[u];
-        }
-    }
-    __syncthreads();
-    // x: row groups of 32 / L rows per warp, in place
-    {
-        const int S = X / 16;
-        int L = 1;
-        while (L < S) L <<= 1;
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, rows_per_warp = 32 / L;
-        const int sub = lane / L, l = lane % L;
-        for (int r0 = warp * rows_per_warp; r0 < Y; r0 += (kSliceThreads / 32) * rows_per_warp) {
-            const int row = r0 + sub;
-            const bool live = row < Y;
-            uint4 v[1];
-            v[0] = (live && l < S) ? reinterpret_cast<const uint4*>(slice)[(size_t)row * S + l]
-                                   : make_uint4(0u, 0u, 0u, 0u);
-            x_row<1>(v, reinterpret_cast<uint4*>(slice), S, L, l, l, row, live, maxd);
-        }
-    }
-    __syncthreads();
-    // y: the segmented line transform of every 4-byte column group
-    const int n = Y;
-    const int G = X >> 2;
-    const int P = kSliceThreads / G;
-    const int g = threadIdx.x % G, sg = threadIdx.x / G;
-    const int m = ((n + P - 1) / P) | 1;
-    const int a = min(n, sg * m), b = min(n, a + m);
-    unsigned* col = reinterpret_cast<unsigned*>(slice) + g;
-    unsigned fl = kInf2, fh = kInf2, bl = kInf2, bh = kInf2;
-    for (int r = a; r < b; r++) {
-        const unsigned cw = col[(size_t)r * G];
-        const unsigned to_end = (unsigned)(b - 1 - r) * 0x00010001u, to_start = (unsigned)(r - a) * 0x00010001u;
-        fl = __viaddmin_u16x2(lo_pair(cw), to_end, fl);
-        fh = __viaddmin_u16x2(hi_pair(cw), to_end, fh);
-        bl = __viaddmin_u16x2(lo_pair(cw), to_start, bl);
-        bh = __viaddmin_u16x2(hi_pair(cw), to_start, bh);
-    }
-    s_carry[0][threadIdx.x] = fl;
-    s_carry[1][threadIdx.x] = fh;
-    s_carry[2][threadIdx.x] = bl;
-    s_carry[3][threadIdx.x] = bh;
-    __syncthreads();
-    unsigned Fl = kInf2, Fh = kInf2, Bl = kInf2, Bh = kInf2;
-    for (int k = 0; k < sg; k++) {
-        const int ka = min(n, k * m);
-        const unsigned len = (unsigned)(min(n, ka + m) - ka) * 0x00010001u;
-        Fl = __viaddmin_u16x2(Fl, len, s_carry[0][k * G + g]);
-        Fh = __viaddmin_u16x2(Fh, len, s_carry[1][k * G + g]);
-    }
-    for (int k = P - 1; k > sg; k--) {
-        const int ka = min(n, k * m);
-        const unsigned len = (unsigned)(min(n, ka + m) - ka) * 0x00010001u;
-        Bl = __viaddmin_u16x2(Bl, len, s_carry[2][k * G + g]);
-        Bh = __viaddmin_u16x2(Bh, len, s_carry[3][k * G + g]);
-    }
-    const unsigned one = 0x00010001u;
-    for (int r = a; r < b; r++) {
-        const unsigned cw = col[(size_t)r * G];
-        Fl = __viaddmin_u16x2(Fl, one, lo_pair(cw));
-        Fh = __viaddmin_u16x2(Fh, one, hi_pair(cw));
-        col[(size_t)r * G] = pack_pairs(Fl, Fh);
-    }
-    for (int r = b - 1; r >= a; r--) {
-        const unsigned cw = col[(size_t)r * G];
-        Bl = __viaddmin_u16x2(Bl, one, lo_pair(cw));
-        Bh = __viaddmin_u16x2(Bh, one, hi_pair(cw));
-        col[(size_t)r * G] = pack_pairs(Bl, Bh);
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < nq; k += kSliceThreads)
-        reinterpret_cast<uint4*>(df + base)[k] = reinterpret_cast<const uint4*>(slice)[k];
-}
-
 // ------------------------------------------------------ incremental update --
 // An edit of the voxels in box E changes the field only within L1 distance
 // maxd of E, inside the box O = E grown by maxd on every side. Over the sweep
@@ -530,21 +429,8 @@ cudaError_t df_build(const uint8_t* vox, uint8_t* df, int X, int Y, int Z, cudaS
     const bool vec = X % 16 == 0 && X <= 16 * 32 * 2 && ((uintptr_t)vox & 15u) == 0 && ((uintptr_t)df & 15u) == 0 &&
                      (size_t)std::max(Y, Z) * kTile <= (size_t)kSweepSmemMax;
     if (vec) {
-        cudaError_t e = cudaSuccess;
-        const size_t slice = (size_t)X * Y;
-        if (X <= 512 && slice <= (size_t)kSliceSmemMax) {
-            // x and y together, one z slice per CTA
-            if (slice > 48 * 1024 &&
-                (e = cudaFuncSetAttribute(k_df_xy_slice, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          kSliceSmemMax)) != cudaSuccess)
-                return e;
-            k_df_xy_slice<<<(unsigned)Z, kSliceThreads, slice, s>>>(vox, df, X, Y, maxd);
-            if ((e = cudaGetLastError()) != cudaSuccess) return e;
-            if ((e = launch_sweep_tile(df, X, Z, (size_t)X * Y, (size_t)X, Y, s)) != cudaSuccess) return e;
-            if (launches) *launches += 2;
-            return cudaSuccess;
-        }
-        e = X <= 16 * 32 ? launch_x16<1>(vox, df, X, rows, maxd, s) : launch_x16<2>(vox, df, X, rows, maxd, s);
+        cudaError_t e =
+            X <= 16 * 32 ? launch_x16<1>(vox, df, X, rows, maxd, s) : launch_x16<2>(vox, df, X, rows, maxd, s);
         if (e != cudaSuccess) return e;
         // y lines: for each z, X * Y bytes; z lines: for each y, stride X * Y
         if ((e = launch_sweep_tile(df, X, Y, (size_t)X, (size_t)X * Y, Z, s)) != cudaSuccess) return e;
