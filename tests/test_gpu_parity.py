@@ -259,6 +259,34 @@ def test_detmath_device_equals_host(vpt, gpu):
         assert_same(dev, host, f"detmath op {op}")
 
 
+def test_packed_pairs_device_equals_host(vpt, gpu):
+    """The filters' packed fp32 pairs (two adds or multiplies per
+    instruction) round every lane as the scalar operation does."""
+    rng = np.random.default_rng(11)
+    n = 50000
+
+    def wide():
+        return (rng.uniform(-1, 1, n) * np.exp2(rng.integers(-30, 30, n))).astype(np.float32)
+
+    x, y = wide(), wide()
+    for op, want in ((6, x * y), (7, x * y), (8, x + y), (9, x + y)):
+        dev = vpt.detmath(op, x, y, on_device=True)
+        assert_same(dev, want, f"packed op {op}")
+        assert_same(vpt.detmath(op, x, y, on_device=False), want, f"host op {op}")
+    e = rng.uniform(-110, 90, n).astype(np.float32)
+    f = rng.uniform(-20, 0, n).astype(np.float32)
+    f[::7] = e[::7]   # some pairs with a lane outside the polynomial's range
+    for op in (10, 11):
+        assert_same(vpt.detmath(op, e, f, on_device=True), vpt.detmath(0, e, on_device=False), f"packed exp op {op}")
+    w = rng.uniform(0, 8, n).astype(np.float32)
+    bad = []
+    for op, b in ((12, y), (13, w), (14, w)):
+        d, h = vpt.detmath(op, x, b, on_device=True), vpt.detmath(op, x, b, on_device=False)
+        if not same_bits(d, h).all():
+            bad.append((op, int((~same_bits(d, h)).sum())))
+    assert not bad, f"packed ops differing from the scalar operations (op, count): {bad}"
+
+
 def test_stats_count_rays(vpt, oracle, scene, gpu):
     with make_ctx(vpt, scene, vpt.STORAGE_F32) as ctx:
         ctx.set_stats(True)

@@ -175,22 +175,96 @@ __device__ __forceinline__ float blend(const Bilin& b, float v00, float v10, flo
     float hi = v01 * b.bx + v11 * b.ax;
     return lo * b.by + hi * b.ay;
 }
+
+// Packed fp32 pairs: sm_100-family GPUs issue two fp32 adds or multiplies as
+// one instruction, each lane the same round-to-nearest operation as the
+// scalar code, so the bits are unchanged and the filters, which are bound by
+// instruction issue, spend fewer issue slots on their blends and sums.
+// A packed product must never feed a packed sum directly: the code generator
+// contracts that pair into a packed fused multiply-add (one rounding instead
+// of two) even with --fmad=false and explicit .rn, as a device test of these
+// helpers showed. So products are packed and the sums that take them are
+// scalar (the scalar pair is not contracted); padd only adds values that are
+// not packed products.
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "mul.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 padd(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "add.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
+// a + b lane by lane as two scalar adds (for sums of packed products)
+__device__ __forceinline__ float2 sadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+// acc + v * w for two channels with one weight (the filters' weighted sums)
+__device__ __forceinline__ float2 pacc(float2 acc, float2 v, float w) { return sadd(acc, pmul(v, splat(w))); }
+
+// dexp of two arguments with packed products and polynomial steps: lane by
+// lane the operations of dexp (vmath.cuh), so the same bits; arguments
+// outside its polynomial range take the scalar function.
+__device__ __forceinline__ float2 dexp_pair(float a, float b) {
+    const float lo = -103.97208404541016f, hi = 88.72283935546875f;
+    if (!(a >= lo && a <= hi && b >= lo && b <= hi)) return make_float2(dexp(a), dexp(b));
+    const float2 x = make_float2(a, b);
+    const float2 t = sadd(pmul(x, splat(1.44269502162933350f)), splat(0.5f));
+    const float2 kf = make_float2(floorf(t.x), floorf(t.y));
+    // (x - kf * ln2_hi) - kf * ln2_lo, each subtraction an addition of the negated product
+    const float2 r = sadd(sadd(x, pmul(kf, splat(-0.693145751953125f))), pmul(kf, splat(-1.428606765330187e-06f)));
+    float2 q = splat(1.0f / 40320.0f);
+    q = __ffma2_rn(q, r, splat(1.0f / 5040.0f));
+    q = __ffma2_rn(q, r, splat(1.0f / 720.0f));
+    q = __ffma2_rn(q, r, splat(1.0f / 120.0f));
+    q = __ffma2_rn(q, r, splat(1.0f / 24.0f));
+    q = __ffma2_rn(q, r, splat(1.0f / 6.0f));
+    q = __ffma2_rn(q, r, splat(0.5f));
+    q = __ffma2_rn(q, r, splat(1.0f));
+    q = __ffma2_rn(q, r, splat(1.0f));
+    const int k0 = (int)kf.x, k1 = (int)kf.y;
+    if (k0 >= -125 && k0 <= 127 && k1 >= -125 && k1 <= 127) return pmul(q, make_float2(pow2i(k0), pow2i(k1)));
+    return make_float2(scale2(q.x, k0), scale2(q.y, k1));
+}
+
+// blend of two channels at once
+__device__ __forceinline__ float2 blend2(const Bilin& b, float2 v00, float2 v10, float2 v01, float2 v11) {
+    const float2 bx = splat(b.bx), ax = splat(b.ax);
+    const float2 lo = sadd(pmul(v00, bx), pmul(v10, ax));
+    const float2 hi = sadd(pmul(v01, bx), pmul(v11, ax));
+    return sadd(pmul(lo, splat(b.by)), pmul(hi, splat(b.ay)));
+}
+// blend of one channel, its two rows at once
+__device__ __forceinline__ float blend1(const Bilin& b, float v00, float v10, float v01, float v11) {
+    const float2 r = sadd(pmul(make_float2(v00, v01), splat(b.bx)), pmul(make_float2(v10, v11), splat(b.ax)));
+    const float2 q = pmul(r, make_float2(b.by, b.ay));
+    return q.x + q.y;
+}
 template <typename S>
 __device__ __forceinline__ float bl1(const S* p, const Bilin& b) {
-    return blend(b, ld(p + b.o00), ld(p + b.o10), ld(p + b.o01), ld(p + b.o11));
+    return blend1(b, ld(p + b.o00), ld(p + b.o10), ld(p + b.o01), ld(p + b.o11));
 }
 template <typename S>
 __device__ __forceinline__ float2 bl2(const S* p, const Bilin& b) {
     float2 a = ld2(p + 2 * (size_t)b.o00), c = ld2(p + 2 * (size_t)b.o10);
     float2 d = ld2(p + 2 * (size_t)b.o01), e = ld2(p + 2 * (size_t)b.o11);
-    return make_float2(blend(b, a.x, c.x, d.x, e.x), blend(b, a.y, c.y, d.y, e.y));
+    return blend2(b, a, c, d, e);
 }
 template <typename S>
 __device__ __forceinline__ float4 bl4(const S* p, const Bilin& b) {
     float4 a = ld4(p + 4 * (size_t)b.o00), c = ld4(p + 4 * (size_t)b.o10);
     float4 d = ld4(p + 4 * (size_t)b.o01), e = ld4(p + 4 * (size_t)b.o11);
-    return make_float4(blend(b, a.x, c.x, d.x, e.x), blend(b, a.y, c.y, d.y, e.y), blend(b, a.z, c.z, d.z, e.z),
-                       blend(b, a.w, c.w, d.w, e.w));
+    const float2 xy = blend2(b, make_float2(a.x, a.y), make_float2(c.x, c.y), make_float2(d.x, d.y),
+                             make_float2(e.x, e.y));
+    const float2 zw = blend2(b, make_float2(a.z, a.w), make_float2(c.z, c.w), make_float2(d.z, d.w),
+                             make_float2(e.z, e.w));
+    return make_float4(xy.x, xy.y, zw.x, zw.y);
 }
 
 // A W x H plane with C interleaved channels of storage type S.

@@ -345,7 +345,27 @@ __global__ void k_detmath(int op, const float* x, const float* y, float* out, in
         case 2: r = dlog2(a); break;
         case 3: r = dpow(a, y[k]); break;
         case 4: r = dsin(a); break;
-        default: r = dcos(a); break;
+        case 5: r = dcos(a); break;
+        // packed pairs, each lane against its scalar operation
+        case 6: r = pmul(make_float2(a, y[k]), make_float2(y[k], a)).x; break;
+        case 7: r = pmul(make_float2(y[k], a), make_float2(a, y[k])).y; break;
+        case 8: r = padd(make_float2(a, y[k]), make_float2(y[k], a)).x; break;
+        case 9: r = padd(make_float2(y[k], a), make_float2(a, y[k])).y; break;
+        case 10: r = dexp_pair(a, y[k]).x; break;
+        case 11: r = dexp_pair(y[k], a).y; break;
+        case 12: r = pacc(make_float2(y[k], a), make_float2(a, y[k]), a).y; break;   // a + y * a
+        default: {   // bilinear blend of (a, 2a, -a, y) at weights (frac(y), frac(2y))
+            Bilin b;
+            b.ax = y[k] - floorf(y[k]);
+            b.ay = 2.0f * y[k] - floorf(2.0f * y[k]);
+            b.bx = 1.0f - b.ax;
+            b.by = 1.0f - b.ay;
+            const float v00 = a, v10 = 2.0f * a, v01 = -a, v11 = y[k];
+            r = op == 13 ? blend1(b, v00, v10, v01, v11)
+                         : blend2(b, make_float2(0.0f, v00), make_float2(0.0f, v10), make_float2(0.0f, v01),
+                                  make_float2(0.0f, v11)).y;
+            break;
+        }
     }
     out[k] = r;
 }

@@ -42,8 +42,9 @@ __device__ __forceinline__ void pre_filter_texel(const CamView& cam, int W, int 
     float bshv[4] = {bsh.x, bsh.y, bsh.z, bsh.w};
     const float bl = sh_to_y(bshv);
     const float butil = ld(luma + px);
-    float tsh[4] = {bsh.x, bsh.y, bsh.z, bsh.w}, tcc[2] = {bcc.x, bcc.y}, tao[2] = {bao.x, bao.y};
-    float tw = 1.0f, taow = 1.0f;
+    // packed sums: SH (2 pairs), CoCg, AO/sky, (weight, AO/sky weight)
+    float2 t01 = make_float2(bsh.x, bsh.y), t23 = make_float2(bsh.z, bsh.w), tcc2 = bcc, tao2 = bao;
+    float2 tww = make_float2(1.0f, 1.0f);
     const float phi = 4.0f;
 #pragma unroll
     for (int x = -1; x <= 1; x++) {
@@ -71,27 +72,25 @@ __device__ __forceinline__ void pre_filter_texel(const CamView& cam, int W, int 
                 wgt = (aw[x < 0 ? -x : x] * aw[y < 0 ? -y : y]) * wgt;
                 wgt = fmaxf(wgt, 0.01f);
                 wgt = clampf(wgt, 0.0f, 1.0f);
-                tsh[0] += ssh[0] * wgt;
-                tsh[1] += ssh[1] * wgt;
-                tsh[2] += ssh[2] * wgt;
-                tsh[3] += ssh[3] * wgt;
-                tcc[0] += s2.x * wgt;
-                tcc[1] += s2.y * wgt;
-                tw += wgt;
-                float2 a2 = ld2(aosky + 2 * sp_);
-                tao[0] += a2.x * wgt;
-                tao[1] += a2.y * wgt;
-                taow += wgt;
+                t01 = pacc(t01, make_float2(s4.x, s4.y), wgt);
+                t23 = pacc(t23, make_float2(s4.z, s4.w), wgt);
+                tcc2 = pacc(tcc2, s2, wgt);
+                const float2 a2 = ld2(aosky + 2 * sp_);
+                tao2 = pacc(tao2, a2, wgt);
+                tww = padd(tww, splat(wgt));
             }
         }
     }
-    tw = fmaxf(tw, 0.01f);
-    for (int c = 0; c < 4; c++) o_sh[c] = tsh[c] / tw;
-    o_cc[0] = tcc[0] / tw;
-    o_cc[1] = tcc[1] / tw;
-    const float awt = fmaxf(taow, 0.01f);
-    o_ao[0] = tao[0] / awt;
-    o_ao[1] = tao[1] / awt;
+    const float tw = fmaxf(tww.x, 0.01f);
+    o_sh[0] = t01.x / tw;
+    o_sh[1] = t01.y / tw;
+    o_sh[2] = t23.x / tw;
+    o_sh[3] = t23.y / tw;
+    o_cc[0] = tcc2.x / tw;
+    o_cc[1] = tcc2.y / tw;
+    const float awt = fmaxf(tww.y, 0.01f);
+    o_ao[0] = tao2.x / awt;
+    o_ao[1] = tao2.y / awt;
     *o_luma = butil;
 }
 
@@ -151,8 +150,9 @@ __device__ __forceinline__ void temporal_texel(const CamView& cam, int W, int H,
     else if (dp < 96.0f) { tol = 6.25f; do_block = false; do_normal = false; }
     else if (dp < 128.0f) { tol = 9.0f; do_block = false; do_normal = false; }
     else if (dp < 200.0f) { tol = 14.0f; do_block = false; do_normal = false; }
-    float tw = 0.0f, ssh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, scc[2] = {0.0f, 0.0f}, sao[2] = {0.0f, 0.0f};
-    float slum = 0.0f, sspp = 0.0f, smom = 0.0f;
+    // packed sums: SH (2 pairs), CoCg, AO/sky, (spp, moment), (luminance, weight)
+    float2 p_sh01 = make_float2(0.0f, 0.0f), p_sh23 = p_sh01, p_cc = p_sh01, p_ao = p_sh01, p_sm = p_sh01,
+           p_lw = p_sh01;
     int successful = 0;
 #pragma unroll
     for (int k = 0; k < 5; k++) {
@@ -179,21 +179,18 @@ __device__ __forceinline__ void temporal_texel(const CamView& cam, int W, int H,
         if (valid) {
             float4 pu = bl4(p_util, fp), psh = bl4(p_sh, fp);
             float2 pcc = bl2(p_cocg, fp), pao = bl2(p_aosky, fp);
-            ssh[0] += psh.x * cw;
-            ssh[1] += psh.y * cw;
-            ssh[2] += psh.z * cw;
-            ssh[3] += psh.w * cw;
-            scc[0] += pcc.x * cw;
-            scc[1] += pcc.y * cw;
-            sspp += pu.x * cw;
-            smom += pu.y * cw;
-            slum += pu.z * cw;
-            sao[0] += pao.x * cw;
-            sao[1] += pao.y * cw;
-            tw += cw;
+            p_sh01 = pacc(p_sh01, make_float2(psh.x, psh.y), cw);
+            p_sh23 = pacc(p_sh23, make_float2(psh.z, psh.w), cw);
+            p_cc = pacc(p_cc, pcc, cw);
+            p_sm = pacc(p_sm, make_float2(pu.x, pu.y), cw);
+            p_lw = sadd(p_lw, pmul(make_float2(pu.z, cw), make_float2(cw, 1.0f)));   // (lum * cw, cw * 1 == cw)
+            p_ao = pacc(p_ao, pao, cw);
             successful++;
         }
     }
+    float ssh[4] = {p_sh01.x, p_sh01.y, p_sh23.x, p_sh23.y}, scc[2] = {p_cc.x, p_cc.y}, sao[2] = {p_ao.x, p_ao.y};
+    float sspp = p_sm.x, smom = p_sm.y, slum = p_lw.x;
+    const float tw = p_lw.y;
     if (tw > 0.001f) {
         for (int c = 0; c < 4; c++) ssh[c] /= tw;
         scc[0] /= tw;
@@ -325,8 +322,9 @@ __device__ __forceinline__ void variance_texel(int W, int H, int i, int j, const
         // normal weight pow(max(dot(n, n'), 0), 16) for a clamped dot of 0, 1, 3
         const float nw3 = dpow(3.0f, 16.0f);
         const float phi = 5.0f;
-        float tw = 0.0f, tm = 0.0f, tl = 0.0f, tw2 = 0.0f;
-        float tsh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, tcc[2] = {0.0f, 0.0f};
+        // (tw, tw2), (tm, tl), SH and CoCg sums as packed pairs
+        float2 tww = make_float2(0.0f, 0.0f), tml = make_float2(0.0f, 0.0f);
+        float2 tsh01 = make_float2(0.0f, 0.0f), tsh23 = make_float2(0.0f, 0.0f), tcc = make_float2(0.0f, 0.0f);
         for (int x = -4; x <= 4; x++) {
             const int si = i + x;
             if (si < 0 || si >= W) continue;
@@ -343,35 +341,32 @@ __device__ __forceinline__ void variance_texel(int W, int H, int i, int j, const
                 const float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
                 const float sl = sh_to_y(ssh);
                 const float nw = fc == 0 ? 0.0f : (fc == 1 ? 1.0f : nw3);
-                const float de = dexp(-fabsf(sd - bd));
-                const float dw = de * de;   // pow(e, 2) for e in [0, 1]
                 const float lw = fabsf(sl - bl) / phi;
-                float wgt = (dexp(-lw) * nw) * dw;
+                const float2 e = dexp_pair(-fabsf(sd - bd), -lw);
+                const float dw = e.x * e.x;   // pow(e, 2) for e in [0, 1]
+                float wgt = (e.y * nw) * dw;
                 float wgt2 = wgt;
                 wgt = fmaxf(wgt, 0.000000015f);
                 wgt2 = fmaxf(wgt2, 0.0000000015f);
-                tw += wgt;
-                tm += smom * wgt2;
-                tsh[0] += ssh[0] * wgt;
-                tsh[1] += ssh[1] * wgt;
-                tsh[2] += ssh[2] * wgt;
-                tsh[3] += ssh[3] * wgt;
-                tcc[0] += s2.x * wgt;
-                tcc[1] += s2.y * wgt;
-                tl += sl * wgt2;
-                tw2 += wgt2;
+                tww = padd(tww, make_float2(wgt, wgt2));
+                tml = pacc(tml, make_float2(smom, sl), wgt2);
+                tsh01 = pacc(tsh01, make_float2(s4.x, s4.y), wgt);
+                tsh23 = pacc(tsh23, make_float2(s4.z, s4.w), wgt);
+                tcc = pacc(tcc, s2, wgt);
             }
         }
+        const float tw = tww.x, tw2 = tww.y;
+        float tm = tml.x, tl = tml.y;
+        osh[0] = tsh01.x; osh[1] = tsh01.y; osh[2] = tsh23.x; osh[3] = tsh23.y;
+        occ[0] = tcc.x;
+        occ[1] = tcc.y;
         if (tw > 0.0f) {
             tm /= tw2;
             tl /= tw2;
-            tcc[0] /= tw;
-            tcc[1] /= tw;
-            for (int c = 0; c < 4; c++) tsh[c] /= tw;
+            occ[0] /= tw;
+            occ[1] /= tw;
+            for (int c = 0; c < 4; c++) osh[c] /= tw;
         }
-        for (int c = 0; c < 4; c++) osh[c] = tsh[c];
-        occ[0] = tcc[0];
-        occ[1] = tcc[1];
         const float al = tl * tl;
         var = tm - al;
         var *= 3.0f;
@@ -456,8 +451,8 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf,
             tk += kv;
         }
     }
-    float tsh[4] = {bsh.x, bsh.y, bsh.z, bsh.w}, tcc[2] = {bcc.x, bcc.y};
-    float tw = 1.0f, tvar = bvar, tao[2] = {bao.x, bao.y}, taow = 1.0f;
+    float2 tsh01 = make_float2(bsh.x, bsh.y), tsh23 = make_float2(bsh.z, bsh.w), tcc = bcc, tao = bao;
+    float tw = 1.0f, tvar = bvar, taow = 1.0f;
     if (!(bd < 0.0f)) {
         const v2 uv = texcoord(i, j, W, H);
         // GradientNoise (:160-165)
@@ -509,48 +504,46 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf,
                 const float sl = sh_to_y(ssh);
                 // clamp(pow(max(dot(n, n'), 0), 32), 0.001, 1) for a clamped dot of 0, 1 or 3
                 const float nw = face_cos(bf, sface) > 0 ? 1.0f : 0.001f;
-                const float de = dexp(-fmaxf(dd, 0.00001f));
-                const float dw = clampf(de * de, 0.0001f, 1.0f);   // pow(e, 2) for e in [0, 1)
-                float wgt;
+                float wgt, dw;
                 if (strong) {   // young histories: no luminance weight (nor its division and exponential)
+                    const float de = dexp(-fmaxf(dd, 0.00001f));
+                    dw = clampf(de * de, 0.0001f, 1.0f);   // pow(e, 2) for e in [0, 1)
                     wgt = nw * dw;
                 } else {
                     const float lw = fabsf(sl - bl) / phi;
-                    wgt = (dexp(-lw) * nw) * dw;
+                    const float2 e = dexp_pair(-fmaxf(dd, 0.00001f), -lw);
+                    dw = clampf(e.x * e.x, 0.0001f, 1.0f);
+                    wgt = (e.y * nw) * dw;
                 }
                 wgt = clampf(wgt, 0.001f, 1.0f);
                 const float xw = aw[x < 0 ? -x : x], yw = aw[y < 0 ? -y : y];
                 wgt = (xw * yw) * wgt;
                 wgt = fmaxf(wgt, 0.00000001f);
-                tsh[0] += ssh[0] * wgt;
-                tsh[1] += ssh[1] * wgt;
-                tsh[2] += ssh[2] * wgt;
-                tsh[3] += ssh[3] * wgt;
-                tcc[0] += s2.x * wgt;
-                tcc[1] += s2.y * wgt;
+                tsh01 = pacc(tsh01, make_float2(s4.x, s4.y), wgt);
+                tsh23 = pacc(tsh23, make_float2(s4.z, s4.w), wgt);
+                tcc = pacc(tcc, s2, wgt);
                 tvar += (wgt * wgt) * sv;
                 tw += wgt;
                 if (filter_sky || filter_ao) {
                     const float awt = clampf(((xw * yw) * nw) * dw, 0.000001f, 1.0f);
-                    tao[0] += sao.x * awt;
-                    tao[1] += sao.y * awt;
+                    tao = pacc(tao, sao, awt);
                     taow += awt;
                 }
             }
         }
     }
-    for (int c = 0; c < 4; c++) tsh[c] /= tw;
-    tcc[0] /= tw;
-    tcc[1] /= tw;
+    const float osh[4] = {tsh01.x / tw, tsh01.y / tw, tsh23.x / tw, tsh23.y / tw};
+    tcc.x /= tw;
+    tcc.y /= tw;
     tvar /= (tw * tw);
-    tao[0] /= taow;
-    tao[1] /= taow;
-    if (!filter_ao) tao[0] = bao.x;
-    st4(o_sh + 4 * px, clampf(tsh[0], -100.0f, 100.0f), clampf(tsh[1], -100.0f, 100.0f),
-        clampf(tsh[2], -100.0f, 100.0f), clampf(tsh[3], -100.0f, 100.0f));
-    st2(o_cocg + 2 * px, clampf(tcc[0], -10.0f, 100.0f), clampf(tcc[1], -10.0f, 100.0f));
+    tao.x /= taow;
+    tao.y /= taow;
+    if (!filter_ao) tao.x = bao.x;
+    st4(o_sh + 4 * px, clampf(osh[0], -100.0f, 100.0f), clampf(osh[1], -100.0f, 100.0f),
+        clampf(osh[2], -100.0f, 100.0f), clampf(osh[3], -100.0f, 100.0f));
+    st2(o_cocg + 2 * px, clampf(tcc.x, -10.0f, 100.0f), clampf(tcc.y, -10.0f, 100.0f));
     st(o_var + px, clampf(tvar, -1.0f, 50.0f));
-    st2(o_aosky + 2 * px, clampf(tao[0], 0.0f, 1.0f), clampf(tao[1], 0.0f, 1.0f));
+    st2(o_aosky + 2 * px, clampf(tao.x, 0.0f, 1.0f), clampf(tao.y, 0.0f, 1.0f));
 }
 
 inline dim3 grid2(int W, int H) { return dim3((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8)); }
