@@ -421,7 +421,7 @@ vpt_status vpt_get_stream(const vpt_ctx* ctx, void** stream);
  * lanes 0 and 1), x + y (8, 9), exp(x) from the packed exponential (10, 11),
  * the weighted sum x + y * x (12) and the bilinear blends of one and two
  * channels (13, 14) of the values (x, 2x, -x, y) at weights (fract(y),
- * fract(2y)). */
+ * fract(2y)), and x / 5 in the variance estimate's three-operation form (15). */
 vpt_status vpt_detmath(int32_t op, const float* x, const float* y, float* out, int32_t n, int32_t on_device);
 
 /* -------------------------------------------------------- batched worlds --

@@ -85,6 +85,8 @@ def lib() -> C.CDLL:
         L.vpto_variance.argtypes = [P, P, P, P, P, P]
         L.vpto_reproject.argtypes = [P, P, C.c_int, C.c_int, P, P, P]
         L.vpto_vecmath.argtypes = [C.c_int, P, P, P, P, C.c_int]
+        L.vpto_check_div_const.argtypes = [C.c_float, C.c_uint32, C.c_uint32]
+        L.vpto_check_div_const.restype = C.c_uint64
         L.vpto_atrous.argtypes = [P, P, P, C.c_int, P, P, P, P, P, P, P, P]
         L.vpto_gi_view.argtypes = [P, P, P, P, P, P, P]
         L.vpto_shade.argtypes = [P, P, P, P, P, P, P, P, P, P, P, P, C.c_int, C.c_int, P]

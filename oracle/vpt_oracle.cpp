@@ -914,6 +914,33 @@ void vpto_spatial_initial(const vpto_camera* cam, const vpto_params* p,
     }
 }
 
+// How many x with bit patterns in [lo, hi) give a division x / c different
+// from the three-operation form the device uses for a constant divisor:
+// q = x * RN(1/c), then one correction with the exact remainder,
+// q + fma(-q, c, x) * RN(1/c) (P. Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
+// 1990). An exhaustive run over every non-negative finite float is what
+// allows the form for a given c.
+uint64_t vpto_check_div_const(float c, uint32_t lo, uint32_t hi) {
+    const float y = 1.0f / c;
+    uint64_t bad = 0;
+#pragma omp parallel for reduction(+ : bad) schedule(static)
+    for (int64_t u = (int64_t)lo; u < (int64_t)hi; u++) {
+        uint32_t b = (uint32_t)u;
+        float x;
+        std::memcpy(&x, &b, 4);
+        const float q = x * y;
+        const float r = std::fma(-q, c, x);
+        const float d = std::fma(r, y, q);
+        const float e = x / c;
+        uint32_t bd, be;
+        std::memcpy(&bd, &d, 4);
+        std::memcpy(&be, &e, 4);
+        bad += bd != be;
+    }
+    return bad;
+}
+
 // The oracle's vector builtins over n inputs, for the comparison with glm:
 // op 0 dot, 1 cross, 2 length, 3 normalize, 4 mix (scalar), 5 mat4 * vec4.
 void vpto_vecmath(int op, const float* a, const float* b, const float* c, float* out, int n) {

@@ -158,6 +158,9 @@ void vpto_spatial_initial(const vpto_camera* cam, const vpto_params* p,
 /* The oracle's vector builtins (dot, cross, length, normalize, mix, mat4 *
  * vec4) over n inputs, for the comparison with the reference's glm. */
 void vpto_vecmath(int op, const float* a, const float* b, const float* c, float* out, int n);
+/* Inputs x (bit patterns in [lo, hi)) for which q = x * RN(1/c) corrected once
+   by the exact remainder, fma(fma(-q, c, x), RN(1/c), q), differs from x / c. */
+uint64_t vpto_check_div_const(float c, uint32_t lo, uint32_t hi);
 /* ProjectPositionPrevious / Reprojection (SVGF/TemporalFilter.glsl:61-73) of
  * every texel of the W x H hit-distance plane t, as the temporal pass computes
  * them: the world position (3 floats per texel) and the previous frame's

@@ -280,7 +280,7 @@ def test_packed_pairs_device_equals_host(vpt, gpu):
         assert_same(vpt.detmath(op, e, f, on_device=True), vpt.detmath(0, e, on_device=False), f"packed exp op {op}")
     w = rng.uniform(0, 8, n).astype(np.float32)
     bad = []
-    for op, b in ((12, y), (13, w), (14, w)):
+    for op, b in ((12, y), (13, w), (14, w), (15, y)):
         d, h = vpt.detmath(op, x, b, on_device=True), vpt.detmath(op, x, b, on_device=False)
         if not same_bits(d, h).all():
             bad.append((op, int((~same_bits(d, h)).sum())))

@@ -92,3 +92,12 @@ def test_libvpt_host_math_is_bit_identical_to_oracle(vpt, L):
     a = vpt.detmath(3, x, y, on_device=False)
     b = oracle_vec(L.vpto_pow, x, y)
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_division_by_five_in_three_operations_is_exact(L):
+    """The device's x / 5 (one product, one remainder correction) equals
+    IEEE division for every non-negative finite float; the form is odd in
+    x, so for every finite float."""
+    assert L.vpto_check_div_const(5.0, 0, 0x7F800000) == 0
+    # the check does see a difference: infinity, which the form turns into NaN
+    assert L.vpto_check_div_const(5.0, 0x7F800000, 0x7F800001) == 1

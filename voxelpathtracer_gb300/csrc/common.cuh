@@ -233,6 +233,19 @@ __device__ __forceinline__ float2 dexp_pair(float a, float b) {
     return make_float2(scale2(q.x, k0), scale2(q.y, k1));
 }
 
+// x / 5 for finite x in three operations: q = x * RN(1/5), then one
+// correction with the exact remainder, q + fma(-q, 5, x) * RN(1/5)
+// (P. Markstein, IBM J. Res. Dev. 34(1), 1990). For the divisor 5 this is
+// IEEE division's result for every finite x, which the oracle's exhaustive
+// check over all 2^31 non-negative finite floats establishes (the form is
+// odd in x); the device division instead takes a reciprocal estimate,
+// refinement steps and a range check.
+__device__ __forceinline__ float div5(float x) {
+    const float y = 0.2f;   // RN(1/5)
+    const float q = __fmul_rn(x, y);
+    return __fmaf_rn(__fmaf_rn(-q, 5.0f, x), y, q);
+}
+
 // blend of two channels at once
 __device__ __forceinline__ float2 blend2(const Bilin& b, float2 v00, float2 v10, float2 v01, float2 v11) {
     const float2 bx = splat(b.bx), ax = splat(b.ax);
@@ -245,6 +258,25 @@ __device__ __forceinline__ float blend1(const Bilin& b, float v00, float v10, fl
     const float2 r = sadd(pmul(make_float2(v00, v01), splat(b.bx)), pmul(make_float2(v10, v11), splat(b.ax)));
     const float2 q = pmul(r, make_float2(b.by, b.ay));
     return q.x + q.y;
+}
+// Scalar blends of 1 / 2 / 4 channels: the a-trous iteration, whose register
+// budget the packed pairs' operand copies strain, measured faster with these.
+template <typename S>
+__device__ __forceinline__ float bl1s(const S* p, const Bilin& b) {
+    return blend(b, ld(p + b.o00), ld(p + b.o10), ld(p + b.o01), ld(p + b.o11));
+}
+template <typename S>
+__device__ __forceinline__ float2 bl2s(const S* p, const Bilin& b) {
+    float2 a = ld2(p + 2 * (size_t)b.o00), c = ld2(p + 2 * (size_t)b.o10);
+    float2 d = ld2(p + 2 * (size_t)b.o01), e = ld2(p + 2 * (size_t)b.o11);
+    return make_float2(blend(b, a.x, c.x, d.x, e.x), blend(b, a.y, c.y, d.y, e.y));
+}
+template <typename S>
+__device__ __forceinline__ float4 bl4s(const S* p, const Bilin& b) {
+    float4 a = ld4(p + 4 * (size_t)b.o00), c = ld4(p + 4 * (size_t)b.o10);
+    float4 d = ld4(p + 4 * (size_t)b.o01), e = ld4(p + 4 * (size_t)b.o11);
+    return make_float4(blend(b, a.x, c.x, d.x, e.x), blend(b, a.y, c.y, d.y, e.y), blend(b, a.z, c.z, d.z, e.z),
+                       blend(b, a.w, c.w, d.w, e.w));
 }
 template <typename S>
 __device__ __forceinline__ float bl1(const S* p, const Bilin& b) {

@@ -354,6 +354,7 @@ __global__ void k_detmath(int op, const float* x, const float* y, float* out, in
         case 10: r = dexp_pair(a, y[k]).x; break;
         case 11: r = dexp_pair(y[k], a).y; break;
         case 12: r = pacc(make_float2(y[k], a), make_float2(a, y[k]), a).y; break;   // a + y * a
+        case 15: r = div5(a); break;
         default: {   // bilinear blend of (a, 2a, -a, y) at weights (frac(y), frac(2y))
             Bilin b;
             b.ax = y[k] - floorf(y[k]);
@@ -361,6 +362,7 @@ __global__ void k_detmath(int op, const float* x, const float* y, float* out, in
             b.bx = 1.0f - b.ax;
             b.by = 1.0f - b.ay;
             const float v00 = a, v10 = 2.0f * a, v01 = -a, v11 = y[k];
+            if (op != 13 && op != 14) { r = 0.0f; break; }
             r = op == 13 ? blend1(b, v00, v10, v01, v11)
                          : blend2(b, make_float2(0.0f, v00), make_float2(0.0f, v10), make_float2(0.0f, v01),
                                   make_float2(0.0f, v11)).y;

@@ -321,7 +321,6 @@ __device__ __forceinline__ void variance_texel(int W, int H, int i, int j, const
         const int bf = __ldg(face + px);
         // normal weight pow(max(dot(n, n'), 0), 16) for a clamped dot of 0, 1, 3
         const float nw3 = dpow(3.0f, 16.0f);
-        const float phi = 5.0f;
         // (tw, tw2), (tm, tl), SH and CoCg sums as packed pairs
         float2 tww = make_float2(0.0f, 0.0f), tml = make_float2(0.0f, 0.0f);
         float2 tsh01 = make_float2(0.0f, 0.0f), tsh23 = make_float2(0.0f, 0.0f), tcc = make_float2(0.0f, 0.0f);
@@ -341,7 +340,7 @@ __device__ __forceinline__ void variance_texel(int W, int H, int i, int j, const
                 const float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
                 const float sl = sh_to_y(ssh);
                 const float nw = fc == 0 ? 0.0f : (fc == 1 ? 1.0f : nw3);
-                const float lw = fabsf(sl - bl) / phi;
+                const float lw = div5(fabsf(sl - bl));   // / phi, phi = 5
                 const float2 e = dexp_pair(-fabsf(sd - bd), -lw);
                 const float dw = e.x * e.x;   // pow(e, 2) for e in [0, 1]
                 float wgt = (e.y * nw) * dw;
@@ -451,8 +450,8 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf,
             tk += kv;
         }
     }
-    float2 tsh01 = make_float2(bsh.x, bsh.y), tsh23 = make_float2(bsh.z, bsh.w), tcc = bcc, tao = bao;
-    float tw = 1.0f, tvar = bvar, taow = 1.0f;
+    float tsh[4] = {bsh.x, bsh.y, bsh.z, bsh.w}, tcc[2] = {bcc.x, bcc.y};
+    float tw = 1.0f, tvar = bvar, tao[2] = {bao.x, bao.y}, taow = 1.0f;
     if (!(bd < 0.0f)) {
         const v2 uv = texcoord(i, j, W, H);
         // GradientNoise (:160-165)
@@ -492,58 +491,60 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf,
                 // so the unrolled taps' loads can all be in flight together
                 const Bilin fp = bilin(sc, W, H);
                 const Bilin fq = kScaled ? bilin(sc, Wf, Hf) : fp;
-                const float sd = bl1(tf, fq);
+                const float sd = bl1s(tf, fq);
                 const int sface = F.nearest(sc);
-                const float4 s4 = bl4(i_sh, fp);
-                const float2 s2 = bl2(i_cocg, fp);
-                const float sv = bl1(i_var, fp);
-                const float2 sao = (filter_sky || filter_ao) ? bl2(i_aosky, fp) : make_float2(0.0f, 0.0f);
+                const float4 s4 = bl4s(i_sh, fp);
+                const float2 s2 = bl2s(i_cocg, fp);
+                const float sv = bl1s(i_var, fp);
+                const float2 sao = (filter_sky || filter_ao) ? bl2s(i_aosky, fp) : make_float2(0.0f, 0.0f);
                 if (!(sc.x > 0.0f && sc.x < 1.0f && sc.y > 0.0f && sc.y < 1.0f)) continue;
                 const float dd = fabsf(sd - bd);
                 const float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
                 const float sl = sh_to_y(ssh);
                 // clamp(pow(max(dot(n, n'), 0), 32), 0.001, 1) for a clamped dot of 0, 1 or 3
                 const float nw = face_cos(bf, sface) > 0 ? 1.0f : 0.001f;
-                float wgt, dw;
+                const float de = dexp(-fmaxf(dd, 0.00001f));
+                const float dw = clampf(de * de, 0.0001f, 1.0f);   // pow(e, 2) for e in [0, 1)
+                float wgt;
                 if (strong) {   // young histories: no luminance weight (nor its division and exponential)
-                    const float de = dexp(-fmaxf(dd, 0.00001f));
-                    dw = clampf(de * de, 0.0001f, 1.0f);   // pow(e, 2) for e in [0, 1)
                     wgt = nw * dw;
                 } else {
                     const float lw = fabsf(sl - bl) / phi;
-                    const float2 e = dexp_pair(-fmaxf(dd, 0.00001f), -lw);
-                    dw = clampf(e.x * e.x, 0.0001f, 1.0f);
-                    wgt = (e.y * nw) * dw;
+                    wgt = (dexp(-lw) * nw) * dw;
                 }
                 wgt = clampf(wgt, 0.001f, 1.0f);
                 const float xw = aw[x < 0 ? -x : x], yw = aw[y < 0 ? -y : y];
                 wgt = (xw * yw) * wgt;
                 wgt = fmaxf(wgt, 0.00000001f);
-                tsh01 = pacc(tsh01, make_float2(s4.x, s4.y), wgt);
-                tsh23 = pacc(tsh23, make_float2(s4.z, s4.w), wgt);
-                tcc = pacc(tcc, s2, wgt);
+                tsh[0] += ssh[0] * wgt;
+                tsh[1] += ssh[1] * wgt;
+                tsh[2] += ssh[2] * wgt;
+                tsh[3] += ssh[3] * wgt;
+                tcc[0] += s2.x * wgt;
+                tcc[1] += s2.y * wgt;
                 tvar += (wgt * wgt) * sv;
                 tw += wgt;
                 if (filter_sky || filter_ao) {
                     const float awt = clampf(((xw * yw) * nw) * dw, 0.000001f, 1.0f);
-                    tao = pacc(tao, sao, awt);
+                    tao[0] += sao.x * awt;
+                    tao[1] += sao.y * awt;
                     taow += awt;
                 }
             }
         }
     }
-    const float osh[4] = {tsh01.x / tw, tsh01.y / tw, tsh23.x / tw, tsh23.y / tw};
-    tcc.x /= tw;
-    tcc.y /= tw;
+    for (int c = 0; c < 4; c++) tsh[c] /= tw;
+    tcc[0] /= tw;
+    tcc[1] /= tw;
     tvar /= (tw * tw);
-    tao.x /= taow;
-    tao.y /= taow;
-    if (!filter_ao) tao.x = bao.x;
-    st4(o_sh + 4 * px, clampf(osh[0], -100.0f, 100.0f), clampf(osh[1], -100.0f, 100.0f),
-        clampf(osh[2], -100.0f, 100.0f), clampf(osh[3], -100.0f, 100.0f));
-    st2(o_cocg + 2 * px, clampf(tcc.x, -10.0f, 100.0f), clampf(tcc.y, -10.0f, 100.0f));
+    tao[0] /= taow;
+    tao[1] /= taow;
+    if (!filter_ao) tao[0] = bao.x;
+    st4(o_sh + 4 * px, clampf(tsh[0], -100.0f, 100.0f), clampf(tsh[1], -100.0f, 100.0f),
+        clampf(tsh[2], -100.0f, 100.0f), clampf(tsh[3], -100.0f, 100.0f));
+    st2(o_cocg + 2 * px, clampf(tcc[0], -10.0f, 100.0f), clampf(tcc[1], -10.0f, 100.0f));
     st(o_var + px, clampf(tvar, -1.0f, 50.0f));
-    st2(o_aosky + 2 * px, clampf(tao.x, 0.0f, 1.0f), clampf(tao.y, 0.0f, 1.0f));
+    st2(o_aosky + 2 * px, clampf(tao[0], 0.0f, 1.0f), clampf(tao[1], 0.0f, 1.0f));
 }
 
 inline dim3 grid2(int W, int H) { return dim3((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8)); }
