@@ -7,6 +7,34 @@
 
 namespace vpt {
 
+// Programmatic dependent launch for the frame's kernel chain. A kernel
+// launched by pdl_launch may be scheduled onto the SMs its predecessor on the
+// stream frees while that predecessor's last blocks still run; pdl_enter,
+// the first statement of such a kernel, waits for the predecessor grid to
+// complete (its writes visible) before any global access and then lets the
+// kernel's own successor be scheduled early in turn. The wait is the
+// hardware's grid dependency, not a spin, and the successor can only be
+// scheduled once every block of this grid has started, so it never holds
+// SM room this grid still needs. Without the launch attribute both are no-ops.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+template <typename... KArgs, typename... Args>
+cudaError_t pdl_launch(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 // Device counters filled when statistics are on (layout of vpt_stats).
 struct Counters {
     unsigned long long rays[6];

@@ -201,6 +201,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(WorldView w, CamView cam, int 
                                                const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
                                                const S* sh_p, const S* cocg_p, const S* ao_p, const S* spec_p,
                                                S* rgb) {
+    pdl_enter();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= W || j >= H) return;
@@ -311,8 +312,8 @@ void launch_shade(bool scaled, bool sp, bool tx, dim3 grid, dim3 blk, cudaStream
                         k_shade<S, false, true, true>,   k_shade<S, true, false, false>,  k_shade<S, true, false, true>,
                         k_shade<S, true, true, false>,   k_shade<S, true, true, true>};
     const K k = table[(scaled ? 4 : 0) + (sp ? 2 : 0) + (tx ? 1 : 0)];
-    k<<<grid, blk, 0, s>>>(w, cam, W, H, a, (const S*)t, face, block, shadow, (const S*)sh, (const S*)cocg,
-                           (const S*)aosky, (const S*)spec, (S*)rgb);
+    pdl_launch(k, grid, blk, 0, s, w, cam, W, H, a, (const S*)t, face, block, shadow, (const S*)sh, (const S*)cocg,
+               (const S*)aosky, (const S*)spec, (S*)rgb);
 }
 
 }  // namespace

@@ -98,6 +98,7 @@ template <typename S>
 __global__ void __launch_bounds__(256) k_spatial_initial(CamView cam, int W, int H, const S* t, const uint8_t* face,
                                                          const S* sh, const S* cocg, const S* luma, const S* aosky,
                                                          S* o_sh, S* o_cocg, S* o_luma, S* o_aosky) {
+    pdl_enter();
     int i, j;
     if (!pixel_of(W, H, &i, &j)) return;
     const Plane<S, 1> T{t, W, H};
@@ -240,6 +241,7 @@ __global__ void __launch_bounds__(256, 4) k_temporal(CamView cam, int W, int H, 
                                                   const S* c_sh, const S* c_cocg, const S* c_luma, const S* c_aosky,
                                                   const S* p_sh, const S* p_cocg, const S* p_util, const S* p_aosky,
                                                   S* o_sh, S* o_cocg, S* o_util, S* o_aosky) {
+    pdl_enter();
     int i, j;
     if (!pixel_of(W, H, &i, &j)) return;
     const Plane<S, 1> T{t, W, H};
@@ -268,6 +270,7 @@ __global__ void __launch_bounds__(256, 4) k_pre_temporal(CamView cam, int W, int
                                                       S* c_luma, S* c_aosky, const S* p_sh, const S* p_cocg,
                                                       const S* p_util, const S* p_aosky, S* o_sh, S* o_cocg,
                                                       S* o_util, S* o_aosky) {
+    pdl_enter();
     int i, j;
     if (!pixel_of(W, H, &i, &j)) return;
     const Plane<S, 1> T{t, W, H};
@@ -385,6 +388,7 @@ __device__ __forceinline__ void variance_texel(int W, int H, int i, int j, const
 template <typename S>
 __global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, const uint8_t* face, const S* i_sh,
                                                   const S* i_cocg, const S* i_util, S* o_sh, S* o_cocg, S* o_var) {
+    pdl_enter();
     __shared__ uint32_t s_young[256];   // young texels of the block: i | j << 16
     __shared__ int s_n;
     if (threadIdx.x == 0 && threadIdx.y == 0) s_n = 0;
@@ -422,6 +426,7 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf,
                                                 const uint8_t* face, const S* tf, const uint8_t* ff,
                                                 const S* t_util, const S* i_sh, const S* i_cocg, const S* i_var,
                                                 const S* i_aosky, S* o_sh, S* o_cocg, S* o_var, S* o_aosky) {
+    pdl_enter();
     int i, j;
     if (!pixel_of(W, H, &i, &j)) return;
     const Plane8 F{ff, Wf, Hf};
@@ -553,9 +558,9 @@ const dim3 kBlock2(32, 8);
 template <typename S>
 cudaError_t launch_all_spatial_initial(const CamView& cam, int W, int H, const void* t, const uint8_t* face, GIIn in,
                                        GIOut out, cudaStream_t s) {
-    k_spatial_initial<S><<<grid2(W, H), kBlock2, 0, s>>>(cam, W, H, (const S*)t, face, (const S*)in.sh,
-                                                         (const S*)in.cocg, (const S*)in.luma, (const S*)in.aosky,
-                                                         (S*)out.sh, (S*)out.cocg, (S*)out.luma, (S*)out.aosky);
+    pdl_launch(k_spatial_initial<S>, grid2(W, H), kBlock2, 0, s, cam, W, H, (const S*)t, face, (const S*)in.sh,
+               (const S*)in.cocg, (const S*)in.luma, (const S*)in.aosky, (S*)out.sh, (S*)out.cocg, (S*)out.luma,
+               (S*)out.aosky);
     return cudaGetLastError();
 }
 
@@ -563,7 +568,7 @@ template <typename S, bool kScaled>
 cudaError_t launch_temporal(const CamView& cam, int W, int H, int Wf, int Hf, const TemporalArgs& a, const void* t,
                             const uint8_t* face, const uint8_t* block, const void* prev_t, const uint8_t* prev_face,
                             const uint8_t* prev_block, GIIn cur, HistIO prev, HistIO out, cudaStream_t s) {
-    k_temporal<S, kScaled><<<grid2(W, H), kBlock2, 0, s>>>(
+    pdl_launch(k_temporal<S, kScaled>, grid2(W, H), kBlock2, 0, s,
         cam, W, H, Wf, Hf, a, (const S*)t, face, block, (const S*)prev_t, prev_face, prev_block, (const S*)cur.sh,
         (const S*)cur.cocg, (const S*)cur.luma, (const S*)cur.aosky, (const S*)prev.sh, (const S*)prev.cocg,
         (const S*)prev.util, (const S*)prev.aosky, (S*)out.sh, (S*)out.cocg, (S*)out.util, (S*)out.aosky);
@@ -575,7 +580,7 @@ cudaError_t launch_pre_temporal(const CamView& cam, int W, int H, int Wf, int Hf
                                 const uint8_t* face, const uint8_t* block, const void* prev_t,
                                 const uint8_t* prev_face, const uint8_t* prev_block, GIIn gi, GIOut pre, HistIO prev,
                                 HistIO out, cudaStream_t s) {
-    k_pre_temporal<S, kScaled, true><<<grid2(W, H), kBlock2, 0, s>>>(
+    pdl_launch(k_pre_temporal<S, kScaled, true>, grid2(W, H), kBlock2, 0, s,
         cam, W, H, Wf, Hf, a, (const S*)t, face, block, (const S*)prev_t, prev_face, prev_block, (const S*)gi.sh,
         (const S*)gi.cocg, (const S*)gi.luma, (const S*)gi.aosky, (S*)pre.sh, (S*)pre.cocg, (S*)pre.luma,
         (S*)pre.aosky, (const S*)prev.sh, (const S*)prev.cocg, (const S*)prev.util, (const S*)prev.aosky, (S*)out.sh,
@@ -585,8 +590,8 @@ cudaError_t launch_pre_temporal(const CamView& cam, int W, int H, int Wf, int Hf
 
 template <typename S>
 cudaError_t launch_variance(int W, int H, const void* t, const uint8_t* face, HistIO in, FiltIO out, cudaStream_t s) {
-    k_variance<S><<<grid2(W, H), kBlock2, 0, s>>>(W, H, (const S*)t, face, (const S*)in.sh, (const S*)in.cocg,
-                                                  (const S*)in.util, (S*)out.sh, (S*)out.cocg, (S*)out.variance);
+    pdl_launch(k_variance<S>, grid2(W, H), kBlock2, 0, s, W, H, (const S*)t, face, (const S*)in.sh, (const S*)in.cocg,
+               (const S*)in.util, (S*)out.sh, (S*)out.cocg, (S*)out.variance);
     return cudaGetLastError();
 }
 
@@ -594,10 +599,9 @@ template <typename S, bool kScaled>
 cudaError_t launch_atrous(int W, int H, int Wf, int Hf, const AtrousArgs& a, const void* t, const uint8_t* face,
                           const void* tf, const uint8_t* ff, const void* temporal_util, FiltIO in,
                           const void* in_aosky, FiltIO out, cudaStream_t s) {
-    k_atrous<S, kScaled><<<grid2(W, H), kBlock2, 0, s>>>(W, H, Wf, Hf, a, (const S*)t, face, (const S*)tf, ff,
-                                                         (const S*)temporal_util, (const S*)in.sh,
-                                                (const S*)in.cocg, (const S*)in.variance, (const S*)in_aosky,
-                                                (S*)out.sh, (S*)out.cocg, (S*)out.variance, (S*)out.aosky);
+    pdl_launch(k_atrous<S, kScaled>, grid2(W, H), kBlock2, 0, s, W, H, Wf, Hf, a, (const S*)t, face, (const S*)tf, ff,
+               (const S*)temporal_util, (const S*)in.sh, (const S*)in.cocg, (const S*)in.variance,
+               (const S*)in_aosky, (S*)out.sh, (S*)out.cocg, (S*)out.variance, (S*)out.aosky);
     return cudaGetLastError();
 }
 

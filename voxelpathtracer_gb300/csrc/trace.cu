@@ -22,6 +22,7 @@ __global__ void __launch_bounds__(256) k_trace_primary(WorldView w, CamView cam,
                                                        S* out_t, uint8_t* out_face, uint8_t* out_block,
                                                        int32_t* out_hit, uint16_t* out_steps, Counters* stats,
                                                        AlphaStop stop) {
+    pdl_enter();
     int i, j;
     tile_pixel(&i, &j);
     const bool valid = i < W && j < H;
@@ -41,6 +42,7 @@ __global__ void __launch_bounds__(256) k_trace_shadow(WorldView w, CamView cam, 
                                                       float lx, float ly, float lz, const S* t,
                                                       const uint8_t* face, uint8_t* shadow, Counters* stats,
                                                       AlphaStop stop) {
+    pdl_enter();
     int i, j;
     tile_pixel(&i, &j);
     unsigned nrays = 0, nsteps = 0;
@@ -57,6 +59,7 @@ template <typename S, bool kOneSample, bool kTex>
 __global__ void __launch_bounds__(256, 8) k_trace_diffuse(WorldView w, CamView cam, int W, int H, DiffuseArgs a,
                                                        const S* t, const uint8_t* face, S* o_sh, S* o_cocg,
                                                        S* o_luma, S* o_aosky, Counters* stats) {
+    pdl_enter();
     int i, j;
     tile_pixel(&i, &j);
     GICount cnt = {0u, 0u, 0u, 0u};
@@ -90,6 +93,7 @@ __global__ void __launch_bounds__(256, 6) k_trace_diffuse_staged(WorldView w, Ca
                                                                   DiffuseArgs a, const S* t, const uint8_t* face,
                                                                   S* o_sh, S* o_cocg, S* o_luma, S* o_aosky,
                                                                   Counters* stats) {
+    pdl_enter();
     __shared__ uint32_t s_pix[256];         // listed texels: i | j << 16
     __shared__ float s_bt[256];             // their bounce hit distance
     __shared__ uint8_t s_bface[256], s_bblock[256], s_shadow[256];
@@ -177,8 +181,8 @@ void launch_diffuse(bool one, bool tex, dim3 grid, cudaStream_t s, const WorldVi
     using K = void (*)(WorldView, CamView, int, int, DiffuseArgs, const S*, const uint8_t*, S*, S*, S*, S*, Counters*);
     const K table[4] = {k_trace_diffuse<S, false, false>, k_trace_diffuse<S, false, true>,
                         k_trace_diffuse<S, true, false>, k_trace_diffuse<S, true, true>};
-    table[(one ? 2 : 0) + (tex ? 1 : 0)]<<<grid, 256, 0, s>>>(w, cam, W, H, a, (const S*)t, face, (S*)out.sh,
-                                                               (S*)out.cocg, (S*)out.luma, (S*)out.aosky, stats);
+    pdl_launch(table[(one ? 2 : 0) + (tex ? 1 : 0)], grid, 256, 0, s, w, cam, W, H, a, (const S*)t, face, (S*)out.sh,
+               (S*)out.cocg, (S*)out.luma, (S*)out.aosky, stats);
 }
 
 }  // namespace
@@ -187,10 +191,10 @@ cudaError_t trace_primary(const WorldView& w, const CamView& cam, int W, int H, 
                           GBufferOut out, Counters* stats, cudaStream_t s, const AlphaStop* alpha) {
     const AlphaStop st = alpha ? *alpha : AlphaStop{};
     if (fp16)
-        (alpha ? k_trace_primary<__half, true> : k_trace_primary<__half, false>)<<<tile_grid(W, H), 256, 0, s>>>(
+        pdl_launch((alpha ? k_trace_primary<__half, true> : k_trace_primary<__half, false>), tile_grid(W, H), 256, 0, s,
             w, cam, W, H, max_steps, (__half*)out.t, out.face, out.block, out.hit, out.steps, stats, st);
     else
-        (alpha ? k_trace_primary<float, true> : k_trace_primary<float, false>)<<<tile_grid(W, H), 256, 0, s>>>(
+        pdl_launch((alpha ? k_trace_primary<float, true> : k_trace_primary<float, false>), tile_grid(W, H), 256, 0, s,
             w, cam, W, H, max_steps, (float*)out.t, out.face, out.block, out.hit, out.steps, stats, st);
     return cudaGetLastError();
 }
@@ -200,10 +204,10 @@ cudaError_t trace_shadow(const WorldView& w, const CamView& cam, int W, int H, i
                          cudaStream_t s, const AlphaStop* alpha) {
     const AlphaStop st = alpha ? *alpha : AlphaStop{};
     if (fp16)
-        (alpha ? k_trace_shadow<__half, true> : k_trace_shadow<__half, false>)<<<tile_grid(W, H), 256, 0, s>>>(
+        pdl_launch((alpha ? k_trace_shadow<__half, true> : k_trace_shadow<__half, false>), tile_grid(W, H), 256, 0, s,
             w, cam, W, H, max_steps, sun[0], sun[1], sun[2], (const __half*)t, face, shadow, stats, st);
     else
-        (alpha ? k_trace_shadow<float, true> : k_trace_shadow<float, false>)<<<tile_grid(W, H), 256, 0, s>>>(
+        pdl_launch((alpha ? k_trace_shadow<float, true> : k_trace_shadow<float, false>), tile_grid(W, H), 256, 0, s,
             w, cam, W, H, max_steps, sun[0], sun[1], sun[2], (const float*)t, face, shadow, stats, st);
     return cudaGetLastError();
 }
@@ -214,11 +218,11 @@ cudaError_t trace_diffuse(const WorldView& w, const CamView& cam, int W, int H, 
     if (one && a.bounces == 1 && W < 65536 && H < 65536) {
         const dim3 g = tile_grid(W, H);
         if (fp16)
-            (tex ? k_trace_diffuse_staged<__half, true> : k_trace_diffuse_staged<__half, false>)<<<g, 256, 0, s>>>(
+            pdl_launch((tex ? k_trace_diffuse_staged<__half, true> : k_trace_diffuse_staged<__half, false>), g, 256, 0, s,
                 w, cam, W, H, a, (const __half*)t, face, (__half*)out.sh, (__half*)out.cocg, (__half*)out.luma,
                 (__half*)out.aosky, stats);
         else
-            (tex ? k_trace_diffuse_staged<float, true> : k_trace_diffuse_staged<float, false>)<<<g, 256, 0, s>>>(
+            pdl_launch((tex ? k_trace_diffuse_staged<float, true> : k_trace_diffuse_staged<float, false>), g, 256, 0, s,
                 w, cam, W, H, a, (const float*)t, face, (float*)out.sh, (float*)out.cocg, (float*)out.luma,
                 (float*)out.aosky, stats);
         return cudaGetLastError();
