@@ -415,21 +415,96 @@ __global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, cons
     }
 }
 
-// SVGF/SpatialFilter.glsl main (:175-355), 3x3 taps (u_LargeKernel off).
-// A tap contributes only when (BaseDepth < 0) == (DepthDiff < 0), i.e. when
-// the centre is not sky (DepthDiff = abs(...) >= 0); sky centres keep their
-// own values, so their tap loop is skipped. t / face: the G-buffer on the GI
-// grid (the centre); tf / ff: the G-buffer at its own Wf x Hf, sampled at the
-// taps (kScaled when that grid is finer than the GI grid).
+// The texel fetches of one a-trous tap at texture coordinate sc: depth
+// (bilinear, on the G-buffer's own grid), nearest face, and the bilinear SH,
+// CoCg, variance and AO/sky of the filter's input planes. Gathered from
+// global memory (each tap's wrapped footprint is a valid address, so every
+// load of the unrolled taps can be in flight together).
 template <typename S, bool kScaled>
-__global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf, AtrousArgs a, const S* t,
-                                                const uint8_t* face, const S* tf, const uint8_t* ff,
-                                                const S* t_util, const S* i_sh, const S* i_cocg, const S* i_var,
-                                                const S* i_aosky, S* o_sh, S* o_cocg, S* o_var, S* o_aosky) {
-    pdl_enter();
-    int i, j;
-    if (!pixel_of(W, H, &i, &j)) return;
-    const Plane8 F{ff, Wf, Hf};
+struct AtrousGlobal {
+    int W, H, Wf, Hf;
+    const S* tf;
+    const uint8_t* ff;
+    const S *sh, *cocg, *var, *ao;
+    __device__ __forceinline__ float var_at(int si, int sj) const { return ld(var + (size_t)sj * W + si); }
+    __device__ __forceinline__ void tap(v2 sc, bool need_ao, float* sd, int* sface, float4* s4, float2* s2,
+                                        float* sv, float2* sao) const {
+        const Plane8 F{ff, Wf, Hf};
+        const Bilin fp = bilin(sc, W, H);
+        const Bilin fq = kScaled ? bilin(sc, Wf, Hf) : fp;
+        *sd = bl1s(tf, fq);
+        *sface = F.nearest(sc);
+        *s4 = bl4s(sh, fp);
+        *s2 = bl2s(cocg, fp);
+        *sv = bl1s(var, fp);
+        *sao = need_ao ? bl2s(ao, fp) : make_float2(0.0f, 0.0f);
+    }
+};
+
+// The same fetches from a shared-memory tile of the block's neighbourhood
+// (kHalo texels around the 32 x 8 block; the G-buffer on the planes' grid),
+// three float4 per texel: (SH), (CoCg, variance, AO), (sky, depth, face).
+// The footprint and weights are computed with bilin's operations, so a tap
+// blends the same values with the same weights; a tap whose footprint leaves
+// the tile takes the global fetch.
+template <typename S, int kHalo>
+struct AtrousTile {
+    static constexpr int TW = 32 + 2 * kHalo, TH = 8 + 2 * kHalo;
+    const float4* A;
+    const float4* B;
+    const float4* C;
+    int tx0, ty0;
+    AtrousGlobal<S, false> g;
+    __device__ __forceinline__ float var_at(int si, int sj) const { return B[(sj - ty0) * TW + (si - tx0)].z; }
+    __device__ __forceinline__ void tap(v2 sc, bool need_ao, float* sd, int* sface, float4* s4, float2* s2,
+                                        float* sv, float2* sao) const {
+        const float x = sc.x * (float)g.W - 0.5f;
+        const float y = sc.y * (float)g.H - 0.5f;
+        const float x0 = floorf(x), y0 = floorf(y);
+        Bilin b;
+        b.ax = x - x0;
+        b.ay = y - y0;
+        b.bx = 1.0f - b.ax;
+        b.by = 1.0f - b.ay;
+        const int li = f2i(x0) - tx0, lj = f2i(y0) - ty0;
+        const int ni = f2i_floor(sc.x * (float)g.W) - tx0, nj = f2i_floor(sc.y * (float)g.H) - ty0;
+        if (!((unsigned)li < (unsigned)(TW - 1) && (unsigned)lj < (unsigned)(TH - 1) && (unsigned)ni < (unsigned)TW &&
+              (unsigned)nj < (unsigned)TH)) {
+            g.tap(sc, need_ao, sd, sface, s4, s2, sv, sao);
+            return;
+        }
+        const int k00 = lj * TW + li, k10 = k00 + 1, k01 = k00 + TW, k11 = k01 + 1;
+        const float4 a00 = A[k00], a10 = A[k10], a01 = A[k01], a11 = A[k11];
+        const float4 b00 = B[k00], b10 = B[k10], b01 = B[k01], b11 = B[k11];
+        const float2 c00 = *reinterpret_cast<const float2*>(C + k00), c10 = *reinterpret_cast<const float2*>(C + k10);
+        const float2 c01 = *reinterpret_cast<const float2*>(C + k01), c11 = *reinterpret_cast<const float2*>(C + k11);
+        // the tile's float4 texels blend as packed pairs: (SH x, y), (SH z, w), (CoCg), (variance, AO), (sky, depth)
+        const float2 sxy = blend2(b, xy(a00), xy(a10), xy(a01), xy(a11));
+        const float2 szw = blend2(b, zw(a00), zw(a10), zw(a01), zw(a11));
+        *s2 = blend2(b, xy(b00), xy(b10), xy(b01), xy(b11));
+        const float2 va = blend2(b, zw(b00), zw(b10), zw(b01), zw(b11));
+        const float2 sk = blend2(b, c00, c10, c01, c11);
+        *s4 = make_float4(sxy.x, sxy.y, szw.x, szw.y);
+        *sv = va.x;
+        *sd = sk.y;
+        *sface = __float_as_int(C[nj * TW + ni].z);
+        *sao = need_ao ? make_float2(va.y, sk.x) : make_float2(0.0f, 0.0f);
+    }
+    static __device__ __forceinline__ float2 xy(float4 v) { return make_float2(v.x, v.y); }
+    static __device__ __forceinline__ float2 zw(float4 v) { return make_float2(v.z, v.w); }
+};
+
+// SVGF/SpatialFilter.glsl main (:175-355), 3x3 taps (u_LargeKernel off), for
+// texel (i, j). A tap contributes only when (BaseDepth < 0) == (DepthDiff <
+// 0), i.e. when the centre is not sky (DepthDiff = abs(...) >= 0); sky
+// centres keep their own values, so their tap loop is skipped. t / face: the
+// G-buffer on the GI grid (the centre); the taps read the G-buffer on its own
+// grid through `fe`.
+template <typename S, class Fetch>
+__device__ __forceinline__ void atrous_texel(int W, int H, const AtrousArgs& a, int i, int j, const S* t,
+                                             const uint8_t* face, const S* t_util, const S* i_sh, const S* i_cocg,
+                                             const S* i_aosky, S* o_sh, S* o_cocg, S* o_var, S* o_aosky,
+                                             const Fetch& fe) {
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
     const float aw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
     const float gauss[2] = {0.60283f, 0.198585f};
@@ -449,7 +524,7 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf,
             const int si = i + x, sj = j + y;
             if (si < 0 || si >= W || sj < 0 || sj >= H) continue;
             const float kv = gauss[x < 0 ? -x : x] * gauss[y < 0 ? -y : y];
-            const float v = ld(i_var + (size_t)sj * W + si);
+            const float v = fe.var_at(si, sj);
             if (x == 0 && y == 0) bvar = v;
             vsum += v * kv;
             tk += kv;
@@ -477,9 +552,9 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf,
         else if (vest < 0.1f) curve = 70.0f;
         float tweaked = vest;
         if (vest < 0.1f) {   // TweakVariance (:167-173)
-            const float fe = clampf(vest, 0.0f, 1.0f);
-            const float tt = 1.0f - fe;
-            tweaked = fe * dpow(tt, curve + 6.0f);
+            const float fe_ = clampf(vest, 0.0f, 1.0f);
+            const float tt = 1.0f - fe_;
+            tweaked = fe_ * dpow(tt, curve + 6.0f);
         }
         float phi = sqrtf(fmaxf(0.0f, 0.000001f + tweaked));
         phi /= a.phi_bias;
@@ -492,16 +567,11 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf,
                 const float ox = ((float)x * (float)step) * a.add_scale + jo;
                 const float oy = ((float)y * (float)step) * a.add_scale + jo;
                 const v2 sc = mk2(uv.x + ox * texel_x, uv.y + oy * texel_y);
-                // loads first (the wrapped footprint is always a valid address),
-                // so the unrolled taps' loads can all be in flight together
-                const Bilin fp = bilin(sc, W, H);
-                const Bilin fq = kScaled ? bilin(sc, Wf, Hf) : fp;
-                const float sd = bl1s(tf, fq);
-                const int sface = F.nearest(sc);
-                const float4 s4 = bl4s(i_sh, fp);
-                const float2 s2 = bl2s(i_cocg, fp);
-                const float sv = bl1s(i_var, fp);
-                const float2 sao = (filter_sky || filter_ao) ? bl2s(i_aosky, fp) : make_float2(0.0f, 0.0f);
+                float sd, sv;
+                int sface;
+                float4 s4;
+                float2 s2, sao;
+                fe.tap(sc, filter_sky || filter_ao, &sd, &sface, &s4, &s2, &sv, &sao);
                 if (!(sc.x > 0.0f && sc.x < 1.0f && sc.y > 0.0f && sc.y < 1.0f)) continue;
                 const float dd = fabsf(sd - bd);
                 const float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
@@ -552,6 +622,61 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf,
     st2(o_aosky + 2 * px, clampf(tao[0], 0.0f, 1.0f), clampf(tao[1], 0.0f, 1.0f));
 }
 
+// One a-trous iteration gathering its taps from the planes (kScaled when the
+// G-buffer's grid Wf x Hf is finer than the GI grid W x H).
+template <typename S, bool kScaled>
+__global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf, AtrousArgs a, const S* t,
+                                                const uint8_t* face, const S* tf, const uint8_t* ff,
+                                                const S* t_util, const S* i_sh, const S* i_cocg, const S* i_var,
+                                                const S* i_aosky, S* o_sh, S* o_cocg, S* o_var, S* o_aosky) {
+    pdl_enter();
+    int i, j;
+    if (!pixel_of(W, H, &i, &j)) return;
+    const AtrousGlobal<S, kScaled> fe{W, H, Wf, Hf, tf, ff, i_sh, i_cocg, i_var, i_aosky};
+    atrous_texel<S>(W, H, a, i, j, t, face, t_util, i_sh, i_cocg, i_aosky, o_sh, o_cocg, o_var, o_aosky, fe);
+}
+
+// One a-trous iteration of a small step (1 or 2: no jitter, every tap's
+// footprint within kHalo texels of the centre): a block whose neighbourhood
+// lies inside the image first stages it in shared memory with coalesced
+// loads (each texel read once per block instead of once per tap that
+// touches it, fp16 planes converted once), then every tap reads the tile.
+// Blocks at the image border gather from the planes as k_atrous does.
+template <typename S, int kHalo>
+__global__ void __launch_bounds__(256, 4) k_atrous_tile(int W, int H, AtrousArgs a, const S* t, const uint8_t* face,
+                                                     const S* tf, const uint8_t* ff, const S* t_util,
+                                                     const S* i_sh, const S* i_cocg, const S* i_var,
+                                                     const S* i_aosky, S* o_sh, S* o_cocg, S* o_var,
+                                                     S* o_aosky) {
+    using Tile = AtrousTile<S, kHalo>;
+    constexpr int TW = Tile::TW, TH = Tile::TH, N = TW * TH;
+    __shared__ float4 s_tile[3 * N];
+    pdl_enter();
+    const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+    const bool in = i < W && j < H;
+    const int tx0 = (int)blockIdx.x * 32 - kHalo, ty0 = (int)blockIdx.y * 8 - kHalo;
+    const AtrousGlobal<S, false> g{W, H, W, H, tf, ff, i_sh, i_cocg, i_var, i_aosky};
+    if (!(tx0 >= 0 && ty0 >= 0 && tx0 + TW <= W && ty0 + TH <= H)) {   // border block (uniform)
+        if (in) atrous_texel<S>(W, H, a, i, j, t, face, t_util, i_sh, i_cocg, i_aosky, o_sh, o_cocg, o_var, o_aosky, g);
+        return;
+    }
+    for (int k = threadIdx.y * 32 + threadIdx.x; k < N; k += 256) {
+        const int ly = k / TW, lx = k - ly * TW;
+        const size_t q = (size_t)(ty0 + ly) * W + (tx0 + lx);
+        const float4 sh = ld4(i_sh + 4 * q);
+        const float2 cc = ld2(i_cocg + 2 * q), ao = ld2(i_aosky + 2 * q);
+        const float v = ld(i_var + q), d = ld(tf + q);
+        const int f = __ldg(ff + q);
+        s_tile[k] = sh;
+        s_tile[N + k] = make_float4(cc.x, cc.y, v, ao.x);
+        s_tile[2 * N + k] = make_float4(ao.y, d, __int_as_float(f), 0.0f);
+    }
+    __syncthreads();
+    if (!in) return;
+    const Tile fe{s_tile, s_tile + N, s_tile + 2 * N, tx0, ty0, g};
+    atrous_texel<S>(W, H, a, i, j, t, face, t_util, i_sh, i_cocg, i_aosky, o_sh, o_cocg, o_var, o_aosky, fe);
+}
+
 inline dim3 grid2(int W, int H) { return dim3((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8)); }
 const dim3 kBlock2(32, 8);
 
@@ -595,10 +720,28 @@ cudaError_t launch_variance(int W, int H, const void* t, const uint8_t* face, Hi
     return cudaGetLastError();
 }
 
+// The halo a shared-memory tile needs for the taps of a jitter-free step
+// (1 or 2): |offset| <= step * add_scale, plus the bilinear footprint's second
+// texel and a margin for the rounding of the texture coordinates; 0 when the
+// step is tiled by no kernel.
+inline int atrous_tile_halo(const AtrousArgs& a) {
+    if (a.step > 2 || !(a.add_scale >= 0.0f)) return 0;
+    const int need = (int)floorf((float)a.step * a.add_scale + 0.01f) + 1;
+    return need <= 3 ? 3 : (need <= 5 ? 5 : 0);
+}
+
 template <typename S, bool kScaled>
 cudaError_t launch_atrous(int W, int H, int Wf, int Hf, const AtrousArgs& a, const void* t, const uint8_t* face,
                           const void* tf, const uint8_t* ff, const void* temporal_util, FiltIO in,
                           const void* in_aosky, FiltIO out, cudaStream_t s) {
+    const int halo = kScaled ? 0 : atrous_tile_halo(a);
+    if (halo) {
+        pdl_launch(halo == 3 ? k_atrous_tile<S, 3> : k_atrous_tile<S, 5>, grid2(W, H), kBlock2, 0, s, W, H, a,
+                   (const S*)t, face, (const S*)tf, ff, (const S*)temporal_util, (const S*)in.sh, (const S*)in.cocg,
+                   (const S*)in.variance, (const S*)in_aosky, (S*)out.sh, (S*)out.cocg, (S*)out.variance,
+                   (S*)out.aosky);
+        return cudaGetLastError();
+    }
     pdl_launch(k_atrous<S, kScaled>, grid2(W, H), kBlock2, 0, s, W, H, Wf, Hf, a, (const S*)t, face, (const S*)tf, ff,
                (const S*)temporal_util, (const S*)in.sh, (const S*)in.cocg, (const S*)in.variance,
                (const S*)in_aosky, (S*)out.sh, (S*)out.cocg, (S*)out.variance, (S*)out.aosky);
