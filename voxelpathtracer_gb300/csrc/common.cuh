@@ -259,24 +259,12 @@ __device__ __forceinline__ float blend1(const Bilin& b, float v00, float v10, fl
     const float2 q = pmul(r, make_float2(b.by, b.ay));
     return q.x + q.y;
 }
-// Scalar blends of 1 / 2 / 4 channels: the a-trous iteration, whose register
-// budget the packed pairs' operand copies strain, measured faster with these.
+// Scalar blend of one channel: the a-trous iteration's single-channel taps
+// (depth, variance), whose packed form needs operand copies its register
+// budget cannot spare, measured faster with it.
 template <typename S>
 __device__ __forceinline__ float bl1s(const S* p, const Bilin& b) {
     return blend(b, ld(p + b.o00), ld(p + b.o10), ld(p + b.o01), ld(p + b.o11));
-}
-template <typename S>
-__device__ __forceinline__ float2 bl2s(const S* p, const Bilin& b) {
-    float2 a = ld2(p + 2 * (size_t)b.o00), c = ld2(p + 2 * (size_t)b.o10);
-    float2 d = ld2(p + 2 * (size_t)b.o01), e = ld2(p + 2 * (size_t)b.o11);
-    return make_float2(blend(b, a.x, c.x, d.x, e.x), blend(b, a.y, c.y, d.y, e.y));
-}
-template <typename S>
-__device__ __forceinline__ float4 bl4s(const S* p, const Bilin& b) {
-    float4 a = ld4(p + 4 * (size_t)b.o00), c = ld4(p + 4 * (size_t)b.o10);
-    float4 d = ld4(p + 4 * (size_t)b.o01), e = ld4(p + 4 * (size_t)b.o11);
-    return make_float4(blend(b, a.x, c.x, d.x, e.x), blend(b, a.y, c.y, d.y, e.y), blend(b, a.z, c.z, d.z, e.z),
-                       blend(b, a.w, c.w, d.w, e.w));
 }
 template <typename S>
 __device__ __forceinline__ float bl1(const S* p, const Bilin& b) {

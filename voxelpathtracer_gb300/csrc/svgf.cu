@@ -434,10 +434,10 @@ struct AtrousGlobal {
         const Bilin fq = kScaled ? bilin(sc, Wf, Hf) : fp;
         *sd = bl1s(tf, fq);
         *sface = F.nearest(sc);
-        *s4 = bl4s(sh, fp);
-        *s2 = bl2s(cocg, fp);
+        *s4 = bl4(sh, fp);
+        *s2 = bl2(cocg, fp);
         *sv = bl1s(var, fp);
-        *sao = need_ao ? bl2s(ao, fp) : make_float2(0.0f, 0.0f);
+        *sao = need_ao ? bl2(ao, fp) : make_float2(0.0f, 0.0f);
     }
 };
 
