@@ -105,10 +105,12 @@ __device__ __forceinline__ UpscaledGI upscale_gi(const WorldView& w, int W, int 
     const int Wg = W / d, Hg = H / d;
     const float texel_x = 1.0f / (float)Wg, texel_y = 1.0f / (float)Hg;
     const bool inner = i >= d && j >= d && i < W - d && j < H - d;
-#pragma unroll
+    // rolled: the nine unrolled taps (each with its exponential and power)
+    // overflow the instruction cache
+#pragma unroll 1
     for (int x = -1; x <= 1; x++) {
         const int si = inner ? i + d * x : wrapi(i + d * x, W);
-#pragma unroll
+#pragma unroll 1
         for (int y = -1; y <= 1; y++) {
             const int sj = inner ? j + d * y : wrapi(j + d * y, H);
             const size_t q = (size_t)sj * W + si;

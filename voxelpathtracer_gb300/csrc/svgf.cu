@@ -46,7 +46,9 @@ __device__ __forceinline__ void pre_filter_texel(const CamView& cam, int W, int 
     float2 t01 = make_float2(bsh.x, bsh.y), t23 = make_float2(bsh.z, bsh.w), tcc2 = bcc, tao2 = bao;
     float2 tww = make_float2(1.0f, 1.0f);
     const float phi = 4.0f;
-#pragma unroll
+    // the tap loops stay rolled where the kernel's unrolled body overflows the
+    // instruction cache (measured: warps stalled on instruction fetch)
+#pragma unroll 1
     for (int x = -1; x <= 1; x++) {
 #pragma unroll
         for (int y = -1; y <= 1; y++) {
@@ -69,7 +71,7 @@ __device__ __forceinline__ void pre_filter_texel(const CamView& cam, int W, int 
                 float lw = fabsf(sl - bl) / phi;
                 float wgt = dexp(-lw - nw);
                 wgt = fmaxf(wgt, 0.01f);
-                wgt = (aw[x < 0 ? -x : x] * aw[y < 0 ? -y : y]) * wgt;
+                wgt = ((x == 0 ? aw[0] : aw[1]) * aw[y < 0 ? -y : y]) * wgt;
                 wgt = fmaxf(wgt, 0.01f);
                 wgt = clampf(wgt, 0.0f, 1.0f);
                 t01 = pacc(t01, make_float2(s4.x, s4.y), wgt);
@@ -130,9 +132,7 @@ __device__ __forceinline__ void temporal_texel(const CamView& cam, int W, int H,
                                                S* o_sh, S* o_cocg, S* o_util, S* o_aosky) {
     const Plane8 PF{prev_face, Wf, Hf}, PB{prev_block, Wf, Hf};
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
-    const float weights[5] = {3.0f / 32.0f, 3.0f / 32.0f, 9.0f / 64.0f, 3.0f / 32.0f, 3.0f / 32.0f};
-    const int offx[5] = {1, 0, 0, -1, 0};
-    const int offy[5] = {0, 1, 0, 0, -1};
+    // taps k = 0..4 at (1, 0), (0, 1), (0, 0), (-1, 0), (0, -1), weights 3/32 and 9/64 at the centre
     const size_t px = (size_t)j * W + i;
     const v3 bn = normal_from_id(__ldg(face + px), 1.0f);
     const v4 pr = mat_mul4(a.prev_view_proj, bp.x, bp.y, bp.z, 1.0f);
@@ -155,10 +155,11 @@ __device__ __forceinline__ void temporal_texel(const CamView& cam, int W, int H,
     float2 p_sh01 = make_float2(0.0f, 0.0f), p_sh23 = p_sh01, p_cc = p_sh01, p_ao = p_sh01, p_sm = p_sh01,
            p_lw = p_sh01;
     int successful = 0;
-#pragma unroll
+#pragma unroll 1   // rolled: the unrolled body overflows the instruction cache
     for (int k = 0; k < 5; k++) {
+        const int offx = k == 0 ? 1 : (k == 3 ? -1 : 0), offy = k == 1 ? 1 : (k == 4 ? -1 : 0);
         // Jitter is ivec2((noise - 0.5) * 1.0) == 0 for every pixel (:165)
-        v2 sc = mk2(rc.x + ((float)offx[k] + 0.0f) * texel_x, rc.y + ((float)offy[k] + 0.0f) * texel_y);
+        v2 sc = mk2(rc.x + ((float)offx + 0.0f) * texel_x, rc.y + ((float)offy + 0.0f) * texel_y);
         const float b = 0.0035f;
         if (!(sc.x < 1.0f - b && sc.x > b && sc.y < 1.0f - b && sc.y > b)) continue;
         const Bilin fp = bilin(sc, W, H);
@@ -169,7 +170,7 @@ __device__ __forceinline__ void temporal_texel(const CamView& cam, int W, int H,
         v3 pn = normal_from_id(PF.nearest(sc), 1.0f);
         v3 pd = mk3(fabsf(bp.x - pp.x), fabsf(bp.y - pp.y), fabsf(bp.z - pp.z));
         float perr = dot(pd, pd);
-        float cw = weights[k];
+        const float cw = k == 2 ? 9.0f / 64.0f : 3.0f / 32.0f;
         int sblock = min(max(PB.nearest(sc), 0), 127);
         bool valid = false;
         if (perr < tol && ((pt < 0.0f) == (bp.w < 0.0f))) {
@@ -559,9 +560,10 @@ __device__ __forceinline__ void atrous_texel(int W, int H, const AtrousArgs& a, 
         float phi = sqrtf(fmaxf(0.0f, 0.000001f + tweaked));
         phi /= a.phi_bias;
         const float jo = (float)jit * 0.5f;
-#pragma unroll
+        // rolled: the eight unrolled taps overflow the instruction cache
+#pragma unroll 1
         for (int x = -1; x <= 1; x++) {
-#pragma unroll
+#pragma unroll 1
             for (int y = -1; y <= 1; y++) {
                 if (x == 0 && y == 0) continue;
                 const float ox = ((float)x * (float)step) * a.add_scale + jo;
@@ -588,7 +590,7 @@ __device__ __forceinline__ void atrous_texel(int W, int H, const AtrousArgs& a, 
                     wgt = (dexp(-lw) * nw) * dw;
                 }
                 wgt = clampf(wgt, 0.001f, 1.0f);
-                const float xw = aw[x < 0 ? -x : x], yw = aw[y < 0 ? -y : y];
+                const float xw = x == 0 ? aw[0] : aw[1], yw = y == 0 ? aw[0] : aw[1];
                 wgt = (xw * yw) * wgt;
                 wgt = fmaxf(wgt, 0.00000001f);
                 tsh[0] += ssh[0] * wgt;
