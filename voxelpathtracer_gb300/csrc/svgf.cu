@@ -443,14 +443,14 @@ struct AtrousGlobal {
 };
 
 // The same fetches from a shared-memory tile of the block's neighbourhood
-// (kHalo texels around the 32 x 8 block; the G-buffer on the planes' grid),
+// (kHalo texels around the 32 x kRows block; the G-buffer on the planes' grid),
 // three float4 per texel: (SH), (CoCg, variance, AO), (sky, depth, face).
 // The footprint and weights are computed with bilin's operations, so a tap
 // blends the same values with the same weights; a tap whose footprint leaves
 // the tile takes the global fetch.
-template <typename S, int kHalo>
+template <typename S, int kHalo, int kRows>
 struct AtrousTile {
-    static constexpr int TW = 32 + 2 * kHalo, TH = 8 + 2 * kHalo;
+    static constexpr int TW = 32 + 2 * kHalo, TH = kRows + 2 * kHalo;
     const float4* A;
     const float4* B;
     const float4* C;
@@ -638,31 +638,30 @@ __global__ void __launch_bounds__(256, 4) k_atrous(int W, int H, int Wf, int Hf,
     atrous_texel<S>(W, H, a, i, j, t, face, t_util, i_sh, i_cocg, i_aosky, o_sh, o_cocg, o_var, o_aosky, fe);
 }
 
-// One a-trous iteration of a small step (1 or 2: no jitter, every tap's
-// footprint within kHalo texels of the centre): a block whose neighbourhood
-// lies inside the image first stages it in shared memory with coalesced
-// loads (each texel read once per block instead of once per tap that
-// touches it, fp16 planes converted once), then every tap reads the tile.
-// Blocks at the image border gather from the planes as k_atrous does.
-template <typename S, int kHalo>
-__global__ void __launch_bounds__(256, 4) k_atrous_tile(int W, int H, AtrousArgs a, const S* t, const uint8_t* face,
-                                                     const S* tf, const uint8_t* ff, const S* t_util,
-                                                     const S* i_sh, const S* i_cocg, const S* i_var,
-                                                     const S* i_aosky, S* o_sh, S* o_cocg, S* o_var,
-                                                     S* o_aosky) {
-    using Tile = AtrousTile<S, kHalo>;
-    constexpr int TW = Tile::TW, TH = Tile::TH, N = TW * TH;
-    __shared__ float4 s_tile[3 * N];
+// One a-trous iteration of a small step (every tap's footprint within kHalo
+// texels of the centre) by 32 x kRows blocks: a block whose neighbourhood
+// lies inside the image first stages it in shared memory (dynamic, 48 bytes
+// per texel) with coalesced loads (each texel read once per block instead of
+// once per tap that touches it, fp16 planes converted once), then every tap
+// reads the tile. Blocks at the image border gather from the planes as
+// k_atrous does.
+template <typename S, int kHalo, int kRows>
+__global__ void __launch_bounds__(32 * kRows, 1024 / (32 * kRows)) k_atrous_tile(
+    int W, int H, AtrousArgs a, const S* t, const uint8_t* face, const S* tf, const uint8_t* ff, const S* t_util,
+    const S* i_sh, const S* i_cocg, const S* i_var, const S* i_aosky, S* o_sh, S* o_cocg, S* o_var, S* o_aosky) {
+    using Tile = AtrousTile<S, kHalo, kRows>;
+    constexpr int TW = Tile::TW, TH = Tile::TH, N = TW * TH, kThreads = 32 * kRows;
+    extern __shared__ float4 s_tile[];   // 3 * N
     pdl_enter();
-    const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+    const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * kRows + threadIdx.y;
     const bool in = i < W && j < H;
-    const int tx0 = (int)blockIdx.x * 32 - kHalo, ty0 = (int)blockIdx.y * 8 - kHalo;
+    const int tx0 = (int)blockIdx.x * 32 - kHalo, ty0 = (int)blockIdx.y * kRows - kHalo;
     const AtrousGlobal<S, false> g{W, H, W, H, tf, ff, i_sh, i_cocg, i_var, i_aosky};
     if (!(tx0 >= 0 && ty0 >= 0 && tx0 + TW <= W && ty0 + TH <= H)) {   // border block (uniform)
         if (in) atrous_texel<S>(W, H, a, i, j, t, face, t_util, i_sh, i_cocg, i_aosky, o_sh, o_cocg, o_var, o_aosky, g);
         return;
     }
-    for (int k = threadIdx.y * 32 + threadIdx.x; k < N; k += 256) {
+    for (int k = threadIdx.y * 32 + threadIdx.x; k < N; k += kThreads) {
         const int ly = k / TW, lx = k - ly * TW;
         const size_t q = (size_t)(ty0 + ly) * W + (tx0 + lx);
         const float4 sh = ld4(i_sh + 4 * q);
@@ -722,27 +721,44 @@ cudaError_t launch_variance(int W, int H, const void* t, const uint8_t* face, Hi
     return cudaGetLastError();
 }
 
-// The halo a shared-memory tile needs for the taps of a jitter-free step
-// (1 or 2): |offset| <= step * add_scale, plus the bilinear footprint's second
-// texel and a margin for the rounding of the texture coordinates; 0 when the
-// step is tiled by no kernel.
-inline int atrous_tile_halo(const AtrousArgs& a) {
-    if (a.step > 2 || !(a.add_scale >= 0.0f)) return 0;
-    const int need = (int)floorf((float)a.step * a.add_scale + 0.01f) + 1;
-    return need <= 3 ? 3 : (need <= 5 ? 5 : 0);
+// The halo a shared-memory tile needs for an iteration's taps: |offset| <=
+// step * add_scale + |jitter| / 2, the jitter f2i((noise - 0.5) * 0.8 step)
+// at most 0.4 step in magnitude; plus the bilinear footprint's second texel
+// and a margin for the rounding of the texture coordinates.
+inline int atrous_tile_need(const AtrousArgs& a) {
+    if (!(a.add_scale >= 0.0f) || a.step > 64) return 1 << 20;
+    const float jit = floorf(0.4f * (float)a.step);
+    return (int)floorf((float)a.step * a.add_scale + 0.5f * jit + 0.01f) + 1;
+}
+
+template <typename S, int kHalo, int kRows>
+cudaError_t launch_atrous_tile(int W, int H, const AtrousArgs& a, const void* t, const uint8_t* face, const void* tf,
+                               const uint8_t* ff, const void* temporal_util, FiltIO in, const void* in_aosky,
+                               FiltIO out, cudaStream_t s) {
+    using Tile = AtrousTile<S, kHalo, kRows>;
+    const size_t smem = (size_t)3 * Tile::TW * Tile::TH * sizeof(float4);
+    auto k = k_atrous_tile<S, kHalo, kRows>;
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    pdl_launch(k, dim3((unsigned)((W + 31) / 32), (unsigned)((H + kRows - 1) / kRows)), dim3(32, kRows), smem, s, W,
+               H, a, (const S*)t, face, (const S*)tf, ff, (const S*)temporal_util, (const S*)in.sh,
+               (const S*)in.cocg, (const S*)in.variance, (const S*)in_aosky, (S*)out.sh, (S*)out.cocg,
+               (S*)out.variance, (S*)out.aosky);
+    return cudaGetLastError();
 }
 
 template <typename S, bool kScaled>
 cudaError_t launch_atrous(int W, int H, int Wf, int Hf, const AtrousArgs& a, const void* t, const uint8_t* face,
                           const void* tf, const uint8_t* ff, const void* temporal_util, FiltIO in,
                           const void* in_aosky, FiltIO out, cudaStream_t s) {
-    const int halo = kScaled ? 0 : atrous_tile_halo(a);
-    if (halo) {
-        pdl_launch(halo == 3 ? k_atrous_tile<S, 3> : k_atrous_tile<S, 5>, grid2(W, H), kBlock2, 0, s, W, H, a,
-                   (const S*)t, face, (const S*)tf, ff, (const S*)temporal_util, (const S*)in.sh, (const S*)in.cocg,
-                   (const S*)in.variance, (const S*)in_aosky, (S*)out.sh, (S*)out.cocg, (S*)out.variance,
-                   (S*)out.aosky);
-        return cudaGetLastError();
+    if (!kScaled) {   // the steps whose neighbourhood fits a shared-memory tile
+        const int need = atrous_tile_need(a);
+        if (need <= 3) return launch_atrous_tile<S, 3, 8>(W, H, a, t, face, tf, ff, temporal_util, in, in_aosky, out, s);
+        if (need <= 5) return launch_atrous_tile<S, 5, 8>(W, H, a, t, face, tf, ff, temporal_util, in, in_aosky, out, s);
+        // step 4 (halo 11) measured slower tiled (32 x 16 blocks, two per SM: 0.670 against 0.666 ms per frame
+        // for the five iterations), steps 8 and 16 need halos of 21 and 41
     }
     pdl_launch(k_atrous<S, kScaled>, grid2(W, H), kBlock2, 0, s, W, H, Wf, Hf, a, (const S*)t, face, (const S*)tf, ff,
                (const S*)temporal_util, (const S*)in.sh, (const S*)in.cocg, (const S*)in.variance,
