@@ -586,9 +586,10 @@ def batched_section(vpt, torch, args, local, flush):
                 e1.record(stream)
                 e1.synchronize()
                 ms.append(e0.elapsed_time(e1))
-            host_launches = (b.launch_count() - l0) / steps
+            kernels = (b.launch_count() - l0) / steps
             med = float(statistics.median(ms))
-            out[name] = {"ms": med, "rays_per_s": rays / (med * 1e-3), "host_launch_calls_per_step": host_launches}
+            out[name] = {"ms": med, "rays_per_s": rays / (med * 1e-3), "kernels_per_step": kernels,
+                         "host_calls_per_step": 1 if mode == vpt.BATCH_GRAPH else kernels}
     tiles = [sp["tile"] for sp in specs]
     res = {
         "worlds": len(specs),

@@ -456,7 +456,10 @@ typedef struct vpt_batch_tuning {
     int32_t blocks;                  /* persistent blocks; 0 = every SM filled to its occupancy limit */
     int32_t rays_per_lane;           /* 1: a warp traces 32 pixels at a time; 2: 64 (two tiles of one world), each
                                         lane's two primary and two shadow traversals interleaved */
-    int32_t reserved[3];
+    int32_t phased;                  /* 0: one persistent kernel runs the primary, shadow and diffuse passes of a
+                                        tile; 1 (rays_per_lane 1): three persistent kernels, one per pass, each
+                                        pass's code alone on the SMs */
+    int32_t reserved[2];
 } vpt_batch_tuning;
 
 typedef struct vpt_batch_tune_record {
@@ -500,9 +503,9 @@ vpt_status vpt_batch_trace(vpt_batch* batch, const vpt_frame* frame, int32_t mod
  * gathers hit an L2-resident volume. Allocates and frees its buffer. */
 vpt_status vpt_measure_l2_read(int32_t device, uint64_t bytes, int32_t reps, float* gbs);
 
-/* Times every candidate launch shape (rays_per_lane 1/2 x block_threads
- * 128/256/512 x tiles_per_grab 1/2/4 x df_brick 0/4/8, 54 in all) on the
- * batch as it stands, `reps`
+/* Times every candidate launch shape (one kernel with rays_per_lane 1 or 2, or
+ * the phased launch; x block_threads 128/256/512 x tiles_per_grab 1/2/4 x
+ * df_brick 0/4/8: 81 in all) on the batch as it stands, `reps`
  * timed launches each after one warm-up, keeps the fastest as the batch's
  * tuning and writes up to max_records records (all candidates, in the order
  * tried). Synchronises. */

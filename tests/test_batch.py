@@ -68,15 +68,17 @@ def test_batch_distance_fields(vpt, scenes, gpu):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("rays", [1, 2], ids=["1ray", "2rays"])
+@pytest.mark.parametrize("rays", [1, 2, "phased"], ids=["1ray", "2rays", "phased"])
 @pytest.mark.parametrize("mode", [0, 1, 2], ids=["graph", "persistent", "per_world"])
 @pytest.mark.parametrize("brick", [0, 4, 8])
 def test_batch_bit_exact(vpt, scenes, mode, brick, rays, gpu):
     """Every world's planes equal the oracle's; with two rays per lane a warp's
     grab of 3 tile pairs crosses world boundaries, so single tiles and pairs
-    both run."""
+    both run; the phased launch runs the three passes as kernels of their own."""
     with make_batch(vpt, scenes) as b:
-        b.set_tuning(df_brick=brick, tiles_per_grab=3, block_threads=128, rays_per_lane=rays)
+        phased = rays == "phased"
+        b.set_tuning(df_brick=brick, tiles_per_grab=3, block_threads=128, rays_per_lane=1 if phased else rays,
+                     phased=phased)
         b.set_stats(True)
         b.trace(scenes[0]["frame"], mode)
         b.synchronize()
@@ -108,13 +110,14 @@ def test_batch_graph_replay_follows_frame_and_camera(vpt, oracle, scenes, gpu):
 def test_batch_autotune(vpt, scenes, gpu):
     with make_batch(vpt, scenes) as b:
         recs = b.autotune(scenes[0]["frame"], reps=2)
-        assert len(recs) == 54
+        assert len(recs) == 81
         assert {r["rays_per_lane"] for r in recs} == {1, 2}
+        assert sum(r["phased"] for r in recs) == 27 and all(r["rays_per_lane"] == 1 for r in recs if r["phased"])
         assert all(r["ms"] > 0 for r in recs)
         best = min(recs, key=lambda r: r["ms"])
         t = b.tuning().as_dict()
-        assert (t["block_threads"], t["tiles_per_grab"], t["df_brick"], t["rays_per_lane"]) == (
-            best["block_threads"], best["tiles_per_grab"], best["df_brick"], best["rays_per_lane"])
+        assert (t["block_threads"], t["tiles_per_grab"], t["df_brick"], t["rays_per_lane"], t["phased"]) == (
+            best["block_threads"], best["tiles_per_grab"], best["df_brick"], best["rays_per_lane"], best["phased"])
         b.trace(scenes[0]["frame"], vpt.BATCH_GRAPH)
         b.synchronize()
         check_all(b, scenes, "after autotune")

@@ -116,12 +116,13 @@ class BatchConfig(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("block_threads", C.c_int32), ("tiles_per_grab", C.c_int32), ("df_brick", C.c_int32),
-                ("blocks", C.c_int32), ("rays_per_lane", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("blocks", C.c_int32), ("rays_per_lane", C.c_int32), ("phased", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
     def as_dict(self) -> dict:
         return {"block_threads": self.block_threads, "tiles_per_grab": self.tiles_per_grab,
                 "rays_per_lane": self.rays_per_lane, "rays_per_warp": 32 * self.rays_per_lane,
-                "df_brick": self.df_brick, "blocks": self.blocks}
+                "df_brick": self.df_brick, "blocks": self.blocks, "phased": self.phased}
 
 
 class BatchTuneRecord(C.Structure):
@@ -787,10 +788,11 @@ class Batch:
         self._ck(lib.vpt_batch_read_df(self._h, world, _ptr(out), out.nbytes), "vpt_batch_read_df")
         return out
 
-    def set_tuning(self, block_threads=None, tiles_per_grab=None, df_brick=None, blocks=None, rays_per_lane=None):
+    def set_tuning(self, block_threads=None, tiles_per_grab=None, df_brick=None, blocks=None, rays_per_lane=None,
+                   phased=None):
         t = self.tuning()
         for k, v in (("block_threads", block_threads), ("tiles_per_grab", tiles_per_grab), ("df_brick", df_brick),
-                     ("blocks", blocks), ("rays_per_lane", rays_per_lane)):
+                     ("blocks", blocks), ("rays_per_lane", rays_per_lane), ("phased", phased)):
             if v is not None:
                 setattr(t, k, int(v))
         self._ck(lib.vpt_batch_set_tuning(self._h, C.byref(t)), "vpt_batch_set_tuning")
@@ -804,9 +806,9 @@ class Batch:
         self._ck(lib.vpt_batch_trace(self._h, C.byref(frame), mode), "vpt_batch_trace")
 
     def autotune(self, frame: Frame, reps: int = 3) -> list:
-        recs = (BatchTuneRecord * 64)()
+        recs = (BatchTuneRecord * 128)()
         n = C.c_int32()
-        self._ck(lib.vpt_batch_autotune(self._h, C.byref(frame), reps, recs, 64, C.byref(n)), "vpt_batch_autotune")
+        self._ck(lib.vpt_batch_autotune(self._h, C.byref(frame), reps, recs, 128, C.byref(n)), "vpt_batch_autotune")
         return [dict(recs[k].tuning.as_dict(), ms=float(recs[k].ms)) for k in range(n.value)]
 
     def read_plane(self, world: int, plane) -> np.ndarray:

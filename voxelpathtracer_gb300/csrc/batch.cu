@@ -129,6 +129,69 @@ __global__ void __launch_bounds__(kWide ? 512 : 256, kWide ? 3 : 4) k_batch_trac
     }
 }
 
+// One pass of the tile queue for the phased launch: kPass 0 primary, 1 sun
+// shadow, 2 diffuse, each pass a persistent kernel of its own (the three
+// passes' code never competes for one SM's instruction cache). The shadow
+// and diffuse passes read the hit distance and face the primary pass stored,
+// as the per-pass kernels do; outputs and ray counts are batch_tile's.
+template <int B, int kPass>
+__device__ __forceinline__ void batch_pass_tile(const BatchLaunch& a, const BatchFrame& fr, const BatchWorld& bw,
+                                                int local, int lane) {
+    const int i = (local % bw.tiles_x) * 8 + (lane & 7);
+    const int j = (local / bw.tiles_x) * 4 + (lane >> 3);
+    const bool valid = i < bw.W && j < bw.H;
+    unsigned n0 = 0, s0 = 0;
+    GICount cnt = {0u, 0u, 0u, 0u};
+    if (valid) {
+        const WorldView w = bw.w;
+        const CamView& cam = bw.cam;
+        const size_t px = (size_t)j * bw.W + i;
+        if (kPass == 0) {
+            float d;
+            int face;
+            s0 = primary_pixel<B>(w, cam, bw.W, bw.H, i, j, fr.primary_max_steps, px, bw.t, bw.face, bw.block, bw.hit,
+                                  bw.steps, &d, &face);
+            n0 = 1;
+        } else if (kPass == 1) {
+            bw.shadow[px] = shadow_pixel<B>(w, cam, bw.W, bw.H, i, j, fr.shadow_max_steps,
+                                            mk3(fr.sun[0], fr.sun[1], fr.sun[2]), __ldg(bw.t + px),
+                                            __ldg(bw.face + px), &n0, &s0);
+        } else {
+            diffuse_pixel<B>(w, cam, bw.W, bw.H, i, j, fr.d, px, __ldg(bw.t + px), __ldg(bw.face + px), bw.sh, bw.cocg,
+                             bw.luma, bw.aosky, &cnt);
+        }
+    }
+    if (a.stats) {
+        if (kPass == 0) count_rays(a.stats, kRayPrimary, n0, s0);
+        if (kPass == 1) count_rays(a.stats, kRayShadow, n0, s0);
+        if (kPass == 2) {
+            count_rays(a.stats, kRayDiffuse, cnt.diffuse_rays, cnt.diffuse_steps);
+            count_rays(a.stats, kRayBounceShadow, cnt.shadow_rays, cnt.shadow_steps);
+        }
+    }
+}
+
+template <int B, int kPass, bool kWide>
+__global__ void __launch_bounds__(kWide ? 512 : 256, kWide ? 3 : 4) k_batch_pass(BatchLaunch a) {
+    __shared__ int s_begin[kBatchMaxWorlds + 1];
+    for (int k = threadIdx.x; k <= a.n_worlds; k += blockDim.x) s_begin[k] = a.tile_begin[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const BatchFrame& fr = *a.frame;
+    int* queue = a.queue + kPass;
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(queue, a.tiles_per_grab);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= a.n_tiles) break;
+        const int end = min(base + a.tiles_per_grab, a.n_tiles);
+        for (int tile = base; tile < end; tile++) {
+            const int lo = world_of(s_begin, a.n_worlds, tile);
+            batch_pass_tile<B, kPass>(a, fr, a.worlds[lo], tile - s_begin[lo], lane);
+        }
+    }
+}
+
 template <int B>
 __global__ void __launch_bounds__(256) k_df_bricks(const uint8_t* __restrict__ df, uint8_t* __restrict__ out, int X,
                                                    int Y, int Z, int bx, int by, size_t total) {
@@ -159,6 +222,30 @@ int max_blocks_for(int block_threads) {
     return n;
 }
 
+// The three pass kernels of the phased launch, each with the grid that fills
+// every SM to its own occupancy limit (or `blocks`).
+template <int B, bool kWide>
+cudaError_t launch_passes(const BatchLaunch& a, int block_threads, int blocks, int sms, cudaStream_t s) {
+    using K = void (*)(BatchLaunch);
+    const K ks[3] = {k_batch_pass<B, 0, kWide>, k_batch_pass<B, 1, kWide>, k_batch_pass<B, 2, kWide>};
+    for (int p = 0; p < 3; p++) {
+        int g = blocks;
+        if (g <= 0) {
+            int n = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ks[p], block_threads, 0) != cudaSuccess) {
+                cudaGetLastError();
+                return cudaErrorInvalidConfiguration;
+            }
+            g = n * sms;
+        }
+        if (g <= 0) return cudaErrorInvalidConfiguration;
+        ks[p]<<<g, block_threads, 0, s>>>(a);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 }  // namespace
 
 int batch_max_blocks(int df_brick, int block_threads, int rays_per_lane, int device) {
@@ -172,12 +259,27 @@ int batch_max_blocks(int df_brick, int block_threads, int rays_per_lane, int dev
 }
 
 cudaError_t batch_trace(const BatchLaunch& a, int df_brick, int block_threads, int rays_per_lane, int blocks,
-                        cudaStream_t s) {
+                        int phased, cudaStream_t s) {
     if (a.n_worlds < 1 || a.n_worlds > kBatchMaxWorlds || block_threads < 32 || block_threads > 512 ||
-        (block_threads & 31) || a.tiles_per_grab < 1 || (rays_per_lane != 1 && rays_per_lane != 2))
+        (block_threads & 31) || a.tiles_per_grab < 1 || (rays_per_lane != 1 && rays_per_lane != 2) ||
+        (phased && rays_per_lane != 1))
         return cudaErrorInvalidValue;
     int dev = 0;
     cudaGetDevice(&dev);
+    if (phased) {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return cudaErrorInvalidValue;
+        const bool wide = block_threads > 256;
+        switch (df_brick) {
+            case 0: return wide ? launch_passes<0, true>(a, block_threads, blocks, sms, s)
+                                : launch_passes<0, false>(a, block_threads, blocks, sms, s);
+            case 4: return wide ? launch_passes<4, true>(a, block_threads, blocks, sms, s)
+                                : launch_passes<4, false>(a, block_threads, blocks, sms, s);
+            case 8: return wide ? launch_passes<8, true>(a, block_threads, blocks, sms, s)
+                                : launch_passes<8, false>(a, block_threads, blocks, sms, s);
+            default: return cudaErrorInvalidValue;
+        }
+    }
     if (blocks <= 0) blocks = batch_max_blocks(df_brick, block_threads, rays_per_lane, dev);
     if (blocks <= 0) return cudaErrorInvalidConfiguration;
     const bool two = rays_per_lane == 2;

@@ -236,10 +236,10 @@ BatchLaunch launch_args(vpt_batch* b) {
 }
 
 vpt_status launch_persistent(vpt_batch* b) {
-    BCK(b, cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream));
+    BCK(b, cudaMemsetAsync(b->d_queue, 0, 3 * sizeof(int), b->stream));
     BCK(b, batch_trace(launch_args(b), b->tuning.df_brick, b->tuning.block_threads, b->tuning.rays_per_lane,
-                       b->tuning.blocks, b->stream));
-    b->launches += 1;
+                       b->tuning.blocks, b->tuning.phased, b->stream));
+    b->launches += b->tuning.phased ? 3 : 1;
     return VPT_OK;
 }
 
@@ -251,10 +251,9 @@ vpt_status launch_graph(vpt_batch* b) {
         }
         cudaGraph_t g = nullptr;
         BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e1 = cudaMemsetAsync(b->d_queue, 0, sizeof(int), b->stream);
+        cudaError_t e1 = cudaMemsetAsync(b->d_queue, 0, 3 * sizeof(int), b->stream);
         cudaError_t e2 = batch_trace(launch_args(b), b->tuning.df_brick, b->tuning.block_threads, b->tuning.rays_per_lane,
-                                     b->tuning.blocks,
-                                     b->stream);
+                                     b->tuning.blocks, b->tuning.phased, b->stream);
         cudaError_t e3 = cudaStreamEndCapture(b->stream, &g);
         if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -272,7 +271,7 @@ vpt_status launch_graph(vpt_batch* b) {
         b->graph_stats = b->stats;
     }
     BCK(b, cudaGraphLaunch(b->graph, b->stream));
-    b->launches += 1;
+    b->launches += b->tuning.phased ? 3 : 1;
     return VPT_OK;
 }
 
@@ -303,7 +302,7 @@ vpt_status launch_per_world(vpt_batch* b, const vpt_frame* f) {
 bool valid_tuning(const vpt_batch_tuning& t) {
     return t.block_threads >= 64 && t.block_threads <= 512 && (t.block_threads & 31) == 0 && t.tiles_per_grab >= 1 &&
            t.tiles_per_grab <= 16 && (t.df_brick == 0 || t.df_brick == 4 || t.df_brick == 8) && t.blocks >= 0 &&
-           (t.rays_per_lane == 1 || t.rays_per_lane == 2);
+           (t.rays_per_lane == 1 || t.rays_per_lane == 2) && (t.phased == 0 || (t.phased == 1 && t.rays_per_lane == 1));
 }
 
 }  // namespace
@@ -517,7 +516,8 @@ vpt_status vpt_batch_autotune(vpt_batch* b, const vpt_frame* f, int32_t reps, vp
     BCK(b, cudaEventCreate(&e0));
     BCK(b, cudaEventCreate(&e1));
     const int threads[3] = {128, 256, 512}, grabs[3] = {1, 2, 4}, bricks[3] = {0, 4, 8}, rays[2] = {1, 2};
-    for (int ri = 0; ri < 2 && s == VPT_OK; ri++)
+    // one or two rays per lane in the one-kernel launch, and the phased launch (one ray per lane)
+    for (int ri = 0; ri < 3 && s == VPT_OK; ri++)
     for (int bi = 0; bi < 3 && s == VPT_OK; bi++) {
         for (int ti = 0; ti < 3 && s == VPT_OK; ti++) {
             for (int gi = 0; gi < 3 && s == VPT_OK; gi++) {
@@ -525,7 +525,8 @@ vpt_status vpt_batch_autotune(vpt_batch* b, const vpt_frame* f, int32_t reps, vp
                 t.df_brick = bricks[bi];
                 t.block_threads = threads[ti];
                 t.tiles_per_grab = grabs[gi];
-                t.rays_per_lane = rays[ri];
+                t.rays_per_lane = ri < 2 ? rays[ri] : 1;
+                t.phased = ri == 2 ? 1 : 0;
                 t.blocks = 0;
                 b->tuning = t;
                 b->graph_valid = false;

@@ -198,13 +198,15 @@ struct BatchLaunch {
     int n_worlds;
     int n_tiles;
     int tiles_per_grab;       // queue entries a warp takes at once
-    int* queue;               // zero at launch
+    int* queue;               // zero at launch (the phased launch: one counter per pass, queue[0..2])
     Counters* stats;
 };
 constexpr int kBatchMaxWorlds = 1024;
-// df_brick: 0, 4 or 8; blocks <= 0 fills every SM to its occupancy limit.
+// df_brick: 0, 4 or 8; blocks <= 0 fills every SM to its occupancy limit;
+// phased: the primary, shadow and diffuse passes as three persistent kernels
+// (rays_per_lane 1) instead of one.
 cudaError_t batch_trace(const BatchLaunch& a, int df_brick, int block_threads, int rays_per_lane, int blocks,
-                        cudaStream_t s);
+                        int phased, cudaStream_t s);
 int batch_max_blocks(int df_brick, int block_threads, int rays_per_lane, int device);
 // Copies an x-fastest distance field into the BxBxB brick layout of df_index.
 cudaError_t df_to_bricks(const uint8_t* df, uint8_t* out, int X, int Y, int Z, int brick, cudaStream_t s);
