@@ -87,25 +87,31 @@ __global__ void __launch_bounds__(256, 8) k_trace_diffuse(WorldView w, CamView c
 //      few lanes' shadow rays);
 //   3. one thread per listed texel finishes the sample from the recorded hit
 //      and shadow verdict and writes the GI planes.
-// Outputs and ray counts are those of k_trace_diffuse.
-template <typename S, bool kTex>
+// Outputs and ray counts are those of k_trace_diffuse. A block covers kR
+// 16x16 tiles stacked in y (a thread lists kR texels and works through the
+// listed ones kR at a time): with two, each lane's work is the sum of two
+// bounce rays' step counts, which differ less from lane to lane than single
+// ones, and a block's shadow-request stage fills more of its warps.
+template <typename S, bool kTex, int kR>
 __global__ void __launch_bounds__(256, 6) k_trace_diffuse_staged(WorldView w, CamView cam, int W, int H,
                                                                   DiffuseArgs a, const S* t, const uint8_t* face,
                                                                   S* o_sh, S* o_cocg, S* o_luma, S* o_aosky,
                                                                   Counters* stats) {
+    constexpr int N = 256 * kR;             // texels of the block: a 16 x 16kR tile
     pdl_enter();
-    __shared__ uint32_t s_pix[256];         // listed texels: i | j << 16
-    __shared__ float s_bt[256];             // their bounce hit distance
-    __shared__ uint8_t s_bface[256], s_bblock[256], s_shadow[256];
-    __shared__ float4 s_ray[256];           // shadow ray origin xyz, w = listed texel
+    __shared__ uint32_t s_pix[N];           // listed texels: i | j << 16
+    __shared__ float s_bt[N];               // their bounce hit distance
+    __shared__ uint8_t s_bface[N], s_bblock[N], s_shadow[N];
+    __shared__ float4 s_ray[N];             // shadow ray origin xyz, w = listed texel
     __shared__ int s_n[2];                  // listed texels, shadow requests
-    const int tid = threadIdx.x, lane = tid & 31;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid < 2) s_n[tid] = 0;
     __syncthreads();
     GICount cnt = {0u, 0u, 0u, 0u};
-    {
-        int i, j;
-        tile_pixel(&i, &j);
+#pragma unroll 1
+    for (int r = 0; r < kR; r++) {
+        const int i = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+        const int j = blockIdx.y * 16 * kR + r * 16 + (warp >> 1) * 4 + (lane >> 3);
         bool hit = false;
         if (i < W && j < H) {
             const size_t px = (size_t)j * W + i;
@@ -124,33 +130,38 @@ __global__ void __launch_bounds__(256, 6) k_trace_diffuse_staged(WorldView w, Ca
     }
     __syncthreads();
     const int n_hit = s_n[0];
-    const unsigned part = __ballot_sync(0xffffffffu, tid < n_hit);   // this warp's lanes with a listed texel
-    if (tid < n_hit) {
-        const int i = (int)(s_pix[tid] & 0xffffu), j = (int)(s_pix[tid] >> 16);
-        const size_t px = (size_t)j * W + i;
-        StagedBounce sb;
+#pragma unroll 1
+    for (int k0 = 0; k0 < n_hit; k0 += 256) {   // uniform rounds; lane k = k0 + tid
+        const int k = k0 + tid;
         bool need = false;
         v3 so;
-        diffuse_pixel<0, S, true, kTex, kDiffuseBounceOnly>(w, cam, W, H, i, j, a, px, ld(t + px), __ldg(face + px),
-                                                            o_sh, o_cocg, o_luma, o_aosky, &cnt, &sb, &need, &so);
-        s_bt[tid] = sb.t;
-        s_bface[tid] = (uint8_t)sb.face;
-        s_bblock[tid] = (uint8_t)sb.block;
-        s_shadow[tid] = 0;
-        const unsigned m = __ballot_sync(part, need);
-        if (m) {   // the same for every lane of `part`
+        if (k < n_hit) {
+            const int i = (int)(s_pix[k] & 0xffffu), j = (int)(s_pix[k] >> 16);
+            const size_t px = (size_t)j * W + i;
+            StagedBounce sb;
+            diffuse_pixel<0, S, true, kTex, kDiffuseBounceOnly>(w, cam, W, H, i, j, a, px, ld(t + px),
+                                                                __ldg(face + px), o_sh, o_cocg, o_luma, o_aosky, &cnt,
+                                                                &sb, &need, &so);
+            s_bt[k] = sb.t;
+            s_bface[k] = (uint8_t)sb.face;
+            s_bblock[k] = (uint8_t)sb.block;
+            s_shadow[k] = 0;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        if (m) {
             const int leader = __ffs(m) - 1;
             int base = 0;
             if (lane == leader) base = atomicAdd(&s_n[1], __popc(m));
-            base = __shfl_sync(part, base, leader);
-            if (need)
-                s_ray[base + __popc(m & ((1u << lane) - 1u))] = make_float4(so.x, so.y, so.z, __int_as_float(tid));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) s_ray[base + __popc(m & ((1u << lane) - 1u))] = make_float4(so.x, so.y, so.z, __int_as_float(k));
         }
     }
     __syncthreads();
-    if (tid < s_n[1]) {
+    const int n_sh = s_n[1];
+#pragma unroll 1
+    for (int k = tid; k < n_sh; k += 256) {
         // GetShadowAt (DiffuseRayTraceFrag.glsl:1202-1222)
-        const float4 r = s_ray[tid];
+        const float4 r = s_ray[k];
         const GILighting& L = a.lighting;
         const TraceResult sr = traverse<0>(w, mk3(r.x, r.y, r.z), mk3(L.light_dir[0], L.light_dir[1], L.light_dir[2]),
                                            a.bounce_shadow_max_steps);
@@ -159,13 +170,14 @@ __global__ void __launch_bounds__(256, 6) k_trace_diffuse_staged(WorldView w, Ca
         s_shadow[__float_as_int(r.w)] = sr.t > 0.0f ? 1 : 0;
     }
     __syncthreads();
-    if (tid < n_hit) {
-        const int i = (int)(s_pix[tid] & 0xffffu), j = (int)(s_pix[tid] >> 16);
+#pragma unroll 1
+    for (int k = tid; k < n_hit; k += 256) {
+        const int i = (int)(s_pix[k] & 0xffffu), j = (int)(s_pix[k] >> 16);
         const size_t px = (size_t)j * W + i;
-        StagedBounce sb{s_bt[tid], (int)s_bface[tid], (int)s_bblock[tid]};
+        StagedBounce sb{s_bt[k], (int)s_bface[k], (int)s_bblock[k]};
         diffuse_pixel<0, S, true, kTex, kDiffuseGiven>(w, cam, W, H, i, j, a, px, ld(t + px), __ldg(face + px), o_sh,
                                                        o_cocg, o_luma, o_aosky, &cnt, &sb, nullptr, nullptr,
-                                                       s_shadow[tid] ? 1.0f : 0.0f);
+                                                       s_shadow[k] ? 1.0f : 0.0f);
     }
     if (stats) {
         count_rays(stats, kRayDiffuse, cnt.diffuse_rays, cnt.diffuse_steps);
@@ -216,13 +228,14 @@ cudaError_t trace_diffuse(const WorldView& w, const CamView& cam, int W, int H, 
                           const void* t, const uint8_t* face, GIOut out, Counters* stats, cudaStream_t s) {
     const bool one = a.spp <= 1 && !a.lighting.moon_stronger, tex = a.textured != 0;
     if (one && a.bounces == 1 && W < 65536 && H < 65536) {
-        const dim3 g = tile_grid(W, H);
+        constexpr int kR = 2;   // 16x32 texels per block (measured: 1 and 4 slower in the frame)
+        const dim3 g((unsigned)((W + 15) / 16), (unsigned)((H + 16 * kR - 1) / (16 * kR)));
         if (fp16)
-            pdl_launch((tex ? k_trace_diffuse_staged<__half, true> : k_trace_diffuse_staged<__half, false>), g, 256, 0, s,
+            pdl_launch((tex ? k_trace_diffuse_staged<__half, true, kR> : k_trace_diffuse_staged<__half, false, kR>), g, 256, 0, s,
                 w, cam, W, H, a, (const __half*)t, face, (__half*)out.sh, (__half*)out.cocg, (__half*)out.luma,
                 (__half*)out.aosky, stats);
         else
-            pdl_launch((tex ? k_trace_diffuse_staged<float, true> : k_trace_diffuse_staged<float, false>), g, 256, 0, s,
+            pdl_launch((tex ? k_trace_diffuse_staged<float, true, kR> : k_trace_diffuse_staged<float, false, kR>), g, 256, 0, s,
                 w, cam, W, H, a, (const float*)t, face, (float*)out.sh, (float*)out.cocg, (float*)out.luma,
                 (float*)out.aosky, stats);
         return cudaGetLastError();
