@@ -306,10 +306,51 @@ __global__ void __launch_bounds__(256, 4) k_pre_temporal(CamView cam, int W, int
 // then listed in shared memory and estimated by consecutive threads (the
 // same per-texel arithmetic, only the thread that runs it changes).
 // kYoung: the texel's history is younger than 12 frames (the caller tested it).
-template <typename S, bool kYoung>
+// The 81-tap branch's texel fetches: depth, face, second moment, SH, CoCg
+// and the SH's luminance at an in-image texel (si, sj), from the planes or
+// from a shared-memory tile of the block's 9x9 neighbourhoods (kVarHalo = 4
+// around the 32 x 8 block, three float4 per texel: SH; CoCg, moment,
+// luminance; depth, face).
+template <typename S>
+struct VarGlobal {
+    int W;
+    const S* t;
+    const uint8_t* face;
+    const S *sh, *cocg, *util;
+    __device__ __forceinline__ void tap(int si, int sj, float* sd, int* sf, float* smom, float4* s4, float2* s2,
+                                        float* sl) const {
+        const size_t q = (size_t)sj * W + si;
+        *sd = ld(t + q);
+        *sf = __ldg(face + q);
+        *smom = ld(util + 4 * q + 1);
+        *s4 = ld4(sh + 4 * q);
+        *s2 = ld2(cocg + 2 * q);
+        const float ssh[4] = {s4->x, s4->y, s4->z, s4->w};
+        *sl = sh_to_y(ssh);
+    }
+};
+constexpr int kVarHalo = 4, kVarTW = 32 + 2 * kVarHalo, kVarTH = 8 + 2 * kVarHalo, kVarN = kVarTW * kVarTH;
+struct VarTile {
+    const float4* T;   // 3 * kVarN
+    int tx0, ty0;
+    __device__ __forceinline__ void tap(int si, int sj, float* sd, int* sf, float* smom, float4* s4, float2* s2,
+                                        float* sl) const {
+        const int k = (sj - ty0) * kVarTW + (si - tx0);
+        *s4 = T[k];
+        const float4 b = T[kVarN + k];
+        const float2 c = *reinterpret_cast<const float2*>(T + 2 * kVarN + k);
+        *s2 = make_float2(b.x, b.y);
+        *smom = b.z;
+        *sl = b.w;
+        *sd = c.x;
+        *sf = __float_as_int(c.y);
+    }
+};
+
+template <typename S, bool kYoung, class VF = VarGlobal<S>>
 __device__ __forceinline__ void variance_texel(int W, int H, int i, int j, const S* t, const uint8_t* face,
                                                const S* i_sh, const S* i_cocg, const S* i_util, S* o_sh, S* o_cocg,
-                                               S* o_var) {
+                                               S* o_var, const VF* vf = nullptr) {
     const float thresh = 4.0f + 4.0f + 4.0f;
     const size_t px = (size_t)j * W + i;
     const float4 bsh = ld4(i_sh + 4 * px);
@@ -335,14 +376,12 @@ __device__ __forceinline__ void variance_texel(int W, int H, int i, int j, const
             for (int y = -4; y <= 4; y++) {
                 const int sj = j + y;
                 if (sj < 0 || sj >= H) continue;
-                const size_t sp_ = (size_t)sj * W + si;
-                const float sd = ld(t + sp_);
-                const int fc = face_cos(bf, __ldg(face + sp_));
-                const float smom = ld(i_util + 4 * sp_ + 1);
-                const float4 s4 = ld4(i_sh + 4 * sp_);
-                const float2 s2 = ld2(i_cocg + 2 * sp_);
-                const float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
-                const float sl = sh_to_y(ssh);
+                float sd, smom, sl;
+                int sf;
+                float4 s4;
+                float2 s2;
+                vf->tap(si, sj, &sd, &sf, &smom, &s4, &s2, &sl);
+                const int fc = face_cos(bf, sf);
                 const float nw = fc == 0 ? 0.0f : (fc == 1 ? 1.0f : nw3);
                 const float lw = div5(fabsf(sl - bl));   // / phi, phi = 5
                 const float2 e = dexp_pair(-fabsf(sd - bd), -lw);
@@ -392,6 +431,7 @@ __global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, cons
     pdl_enter();
     __shared__ uint32_t s_young[256];   // young texels of the block: i | j << 16
     __shared__ int s_n;
+    __shared__ float4 s_vt[3 * kVarN];
     if (threadIdx.x == 0 && threadIdx.y == 0) s_n = 0;
     __syncthreads();
     int i, j;
@@ -409,10 +449,44 @@ __global__ void __launch_bounds__(256) k_variance(int W, int H, const S* t, cons
     if (young) s_young[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i | ((uint32_t)j << 16);
     __syncthreads();
     const int k = threadIdx.y * blockDim.x + threadIdx.x;
-    if (k < s_n) {
+    const int n = s_n;
+    const int tx0 = (int)blockIdx.x * 32 - kVarHalo, ty0 = (int)blockIdx.y * 8 - kVarHalo;
+    // A block with a warp's worth of young texels or more (every block while
+    // the history is young) stages their neighbourhoods in shared memory
+    // once: 640 texels instead of 81 gathers per young texel, the luminance
+    // computed once per texel (uniform per block).
+    if (n >= 32) {
+        for (int q = k; q < kVarN; q += 256) {
+            const int ly = q / kVarTW, lx = q - ly * kVarTW;
+            const int si = tx0 + lx, sj = ty0 + ly;
+            float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f), B = A, Cc = A;
+            if (si >= 0 && si < W && sj >= 0 && sj < H) {   // texels outside the image are never read
+                float sd, smom, sl;
+                int sf;
+                float4 s4;
+                float2 s2;
+                const VarGlobal<S> g{W, t, face, i_sh, i_cocg, i_util};
+                g.tap(si, sj, &sd, &sf, &smom, &s4, &s2, &sl);
+                A = s4;
+                B = make_float4(s2.x, s2.y, smom, sl);
+                Cc = make_float4(sd, __int_as_float(sf), 0.0f, 0.0f);
+            }
+            s_vt[q] = A;
+            s_vt[kVarN + q] = B;
+            s_vt[2 * kVarN + q] = Cc;
+        }
+        __syncthreads();
+        if (k < n) {
+            const uint32_t q = s_young[k];
+            const VarTile vt{s_vt, tx0, ty0};
+            variance_texel<S, true, VarTile>(W, H, (int)(q & 0xffffu), (int)(q >> 16), t, face, i_sh, i_cocg, i_util,
+                                             o_sh, o_cocg, o_var, &vt);
+        }
+    } else if (k < n) {
         const uint32_t q = s_young[k];
+        const VarGlobal<S> g{W, t, face, i_sh, i_cocg, i_util};
         variance_texel<S, true>(W, H, (int)(q & 0xffffu), (int)(q >> 16), t, face, i_sh, i_cocg, i_util, o_sh,
-                                o_cocg, o_var);
+                                o_cocg, o_var, &g);
     }
 }
 
