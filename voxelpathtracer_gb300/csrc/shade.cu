@@ -85,12 +85,25 @@ struct UpscaledGI {
 // textures (kTex) the specular gather reads the tap's roughness and
 // normal-mapped normal from the textured G-buffer (u_GBufferPBR,
 // u_GBufferNormals, :596-599) and compares with the base pixel's (base_hf).
+// The GI planes and G-buffer around a 32 x 8 block of the colour pass on the
+// GI's own grid (halo 1, REPEAT-wrapped as the taps are): per texel the SH;
+// CoCg, AO and the depth as the taps use it, 1 / (1 / t); face | shadow << 8.
+constexpr int kShadeTW = 34, kShadeTH = 10, kShadeN = kShadeTW * kShadeTH;
+struct ShadeTile {
+    const float4* A;
+    const float4* B;
+    const int* C;
+    int lx, ly;   // this pixel's tile position
+};
+
 template <typename S, bool kScaled, bool kSpec, bool kTex>
 __device__ __forceinline__ UpscaledGI upscale_gi(const WorldView& w, int W, int H, int d, int i, int j, v2 uv,
                                                  const S* t, const uint8_t* face, const uint8_t* block,
                                                  const uint8_t* shadow, const S* sh_p, const S* cocg_p,
                                                  const S* ao_p, const S* spec_p, int base_face, float base_d,
-                                                 float base_rough, const S* gb_normal, const S* gb_pbr, v3 base_hf) {
+                                                 float base_rough, const S* gb_normal, const S* gb_pbr, v3 base_hf,
+                                                 const ShadeTile* tile) {
+    constexpr bool kTile = !kScaled && !kSpec;
     UpscaledGI u;
     // the normal weights for a clamped dot product of the decoded face
     // normals of 0, 1 or 3 (face_cos): max(n.n', 1e-6)^16 floored at 1e-4,
@@ -114,12 +127,28 @@ __device__ __forceinline__ UpscaledGI upscale_gi(const WorldView& w, int W, int 
         for (int y = -1; y <= 1; y++) {
             const int sj = inner ? j + d * y : wrapi(j + d * y, H);
             const size_t q = (size_t)sj * W + si;
-            const float tt = ld(t + q);
-            const int fid = __ldg(face + q);
             float4 s4, sp4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             float2 c2;
-            float a0;
-            if (kScaled) {
+            float a0, lda, sv;
+            int fid;
+            const bool cross = x == 0 || y == 0;
+            if (kTile) {
+                const int k = (tile->ly + y) * kShadeTW + tile->lx + x;
+                s4 = tile->A[k];
+                const float4 b = tile->B[k];
+                const int c = tile->C[k];
+                c2 = make_float2(b.x, b.y);
+                a0 = b.z;
+                lda = b.w;
+                fid = c & 255;
+                sv = (filter_shadows && cross) ? (float)(c >> 8) : 0.0f;
+            } else {
+                lda = 1.0f / (1.0f / ld(t + q));
+                fid = __ldg(face + q);
+                sv = (filter_shadows && cross) ? (float)__ldg(shadow + q) : 0.0f;
+            }
+            if (kTile) {
+            } else if (kScaled) {
                 const Bilin fg = bilin(mk2(uv.x + (float)x * texel_x, uv.y + (float)y * texel_y), Wg, Hg);
                 s4 = bl4(sh_p, fg);
                 c2 = bl2(cocg_p, fg);
@@ -132,9 +161,6 @@ __device__ __forceinline__ UpscaledGI upscale_gi(const WorldView& w, int W, int 
                 if (kSpec) sp4 = ld4(spec_p + q * 4);
             }
             const int tap_block = (kSpec && !kTex) ? (int)__ldg(block + q) : 0;
-            const bool cross = x == 0 || y == 0;
-            const float sv = (filter_shadows && cross) ? (float)__ldg(shadow + q) : 0.0f;
-            const float lda = 1.0f / (1.0f / tt);
             const float ed = dexp(-(fabsf(lda - base_d) * 2.0f));
             const float dw = dpow(ed, 5.25f);
             const int fc = face_cos(base_face, fid);
@@ -203,10 +229,27 @@ __global__ void __launch_bounds__(256, 4) k_shade(WorldView w, CamView cam, int 
                                                const uint8_t* face, const uint8_t* block, const uint8_t* shadow,
                                                const S* sh_p, const S* cocg_p, const S* ao_p, const S* spec_p,
                                                S* rgb) {
+    constexpr bool kTile = !kScaled && !kSpec;
+    __shared__ float4 s_ta[kTile ? kShadeN : 1], s_tb[kTile ? kShadeN : 1];
+    __shared__ int s_tc[kTile ? kShadeN : 1];
     pdl_enter();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (kTile) {   // the 3x3 gather's texels, loaded once per block (GI grid = G-buffer grid)
+        for (int q = threadIdx.y * 32 + threadIdx.x; q < kShadeN; q += 256) {
+            const int ly = q / kShadeTW, lx = q - ly * kShadeTW;
+            const int gi = wrapi((int)blockIdx.x * 32 - 1 + lx, W), gj = wrapi((int)blockIdx.y * 8 - 1 + ly, H);
+            const size_t g = (size_t)gj * W + gi;
+            const float4 sh = ld4(sh_p + 4 * g);
+            const float2 cc = ld2(cocg_p + 2 * g);
+            s_ta[q] = sh;
+            s_tb[q] = make_float4(cc.x, cc.y, ld(ao_p + 2 * g), 1.0f / (1.0f / ld(t + g)));
+            s_tc[q] = (int)__ldg(face + g) | ((int)__ldg(shadow + g) << 8);
+        }
+        __syncthreads();
+    }
     if (i >= W || j >= H) return;
+    const ShadeTile tile{s_ta, s_tb, s_tc, (int)threadIdx.x + 1, (int)threadIdx.y + 1};
     size_t px = (size_t)j * W + i;
     const v3 viewer = mk3(cam.pos[0], cam.pos[1], cam.pos[2]);
     v2 uv = texcoord(i, j, W, H);
@@ -237,7 +280,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(WorldView w, CamView cam, int 
         const UpscaledGI up = upscale_gi<S, kScaled, kSpec, kTex>(w, W, H, a.gi_div, i, j, uv, t, face, block,
                                                                   shadow, sh_p, cocg_p, ao_p, spec_p,
                                                                   (int)__ldg(face + px), dist, rough, gb_normal,
-                                                                  gb_pbr, nh);
+                                                                  gb_pbr, nh, &tile);
         float up_shadow = clampf(up.shadow, 0.0f, 1.0f);
         float rt_shadow = clampf(clampf(up_shadow + 0.0f, 0.0f, 1.0f), 0.0f, 1.0f);
         v3 indirect = sh_to_irradiance(up.sh, up.cocg, nh);   // IndirectN = NormalMapped (:834-840)
