@@ -228,16 +228,30 @@ cudaError_t trace_diffuse(const WorldView& w, const CamView& cam, int W, int H, 
                           const void* t, const uint8_t* face, GIOut out, Counters* stats, cudaStream_t s) {
     const bool one = a.spp <= 1 && !a.lighting.moon_stronger, tex = a.textured != 0;
     if (one && a.bounces == 1 && W < 65536 && H < 65536) {
-        constexpr int kR = 2;   // 16x32 texels per block (measured: 1 and 4 slower in the frame)
-        const dim3 g((unsigned)((W + 15) / 16), (unsigned)((H + 16 * kR - 1) / (16 * kR)));
-        if (fp16)
-            pdl_launch((tex ? k_trace_diffuse_staged<__half, true, kR> : k_trace_diffuse_staged<__half, false, kR>), g, 256, 0, s,
-                w, cam, W, H, a, (const __half*)t, face, (__half*)out.sh, (__half*)out.cocg, (__half*)out.luma,
-                (__half*)out.aosky, stats);
-        else
-            pdl_launch((tex ? k_trace_diffuse_staged<float, true, kR> : k_trace_diffuse_staged<float, false, kR>), g, 256, 0, s,
-                w, cam, W, H, a, (const float*)t, face, (float*)out.sh, (float*)out.cocg, (float*)out.luma,
-                (float*)out.aosky, stats);
+        // 16x32 texels per block where that still gives every SM two waves
+        // of its six resident blocks (the 1080p frame: 1.668 -> 1.658 ms),
+        // else 16x16 (a 480x270 GI grid has too few blocks for two waves)
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const unsigned gx = (unsigned)((W + 15) / 16), gy2 = (unsigned)((H + 31) / 32);
+        const bool two = (long long)gx * gy2 >= 2LL * 6 * (sms > 0 ? sms : 1);
+        const dim3 g(gx, two ? gy2 : (unsigned)((H + 15) / 16));
+        if (fp16) {
+            using K = void (*)(WorldView, CamView, int, int, DiffuseArgs, const __half*, const uint8_t*, __half*,
+                               __half*, __half*, __half*, Counters*);
+            const K k = two ? (tex ? k_trace_diffuse_staged<__half, true, 2> : k_trace_diffuse_staged<__half, false, 2>)
+                            : (tex ? k_trace_diffuse_staged<__half, true, 1> : k_trace_diffuse_staged<__half, false, 1>);
+            pdl_launch(k, g, 256, 0, s, w, cam, W, H, a, (const __half*)t, face, (__half*)out.sh, (__half*)out.cocg,
+                       (__half*)out.luma, (__half*)out.aosky, stats);
+        } else {
+            using K = void (*)(WorldView, CamView, int, int, DiffuseArgs, const float*, const uint8_t*, float*, float*,
+                               float*, float*, Counters*);
+            const K k = two ? (tex ? k_trace_diffuse_staged<float, true, 2> : k_trace_diffuse_staged<float, false, 2>)
+                            : (tex ? k_trace_diffuse_staged<float, true, 1> : k_trace_diffuse_staged<float, false, 1>);
+            pdl_launch(k, g, 256, 0, s, w, cam, W, H, a, (const float*)t, face, (float*)out.sh, (float*)out.cocg,
+                       (float*)out.luma, (float*)out.aosky, stats);
+        }
         return cudaGetLastError();
     }
     if (fp16)
