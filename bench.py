@@ -186,6 +186,8 @@ def run_ours(args):
                       reflection_spp=args.reflection_spp)
     if args.inline_shadow:
         ctx.set_tuning(overlap_shadow=False)
+    if args.split_temporal:
+        ctx.set_tuning(split_temporal=True)
     ctx.upload_world(vox)
     ctx.set_block_table(blocks)
     ctx.build_df()
@@ -992,6 +994,9 @@ def main():
     ap.add_argument("--no-quality", action="store_true", help="skip the ground-truth error measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-world batched comparison")
     ap.add_argument("--no-df", action="store_true", help="skip the distance-field build timing")
+    ap.add_argument("--split-temporal", action="store_true",
+                    help="run the temporal pass's history gather on the second stream beside the diffuse trace and "
+                         "only its blend after the pre-filter (vpt_tuning.split_temporal = 1)")
     ap.add_argument("--inline-shadow", action="store_true",
                     help="run the main frame's sun-shadow pass in line on the context stream instead of on a second "
                          "stream beside the diffuse trace and SVGF (vpt_tuning.overlap_shadow = 0)")

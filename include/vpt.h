@@ -201,7 +201,13 @@ typedef struct vpt_tuning {
     int32_t overlap_shadow;          /* vpt_render_frame* run the sun-shadow pass on a second stream beside the
                                         diffuse trace and SVGF, joined before the reflection and colour passes (1,
                                         default: 1.878 against 1.916 ms per 1080p frame), or in line (0) */
-    int32_t reserved[3];
+    int32_t split_temporal;          /* with overlap_shadow, GI on the G-buffer's grid, no block textures and the
+                                        pre-filter unfused: the temporal pass's history gather runs on the second
+                                        stream too, ahead of the shadow pass, and only its blend with the
+                                        pre-filtered planes after the pre-filter (1), or the pass in one kernel (0,
+                                        default: 1.620 against 1.647 ms per 1080p frame, the gather competing with
+                                        the diffuse trace for the SMs and adding 64 bytes a texel each way) */
+    int32_t reserved[2];
 } vpt_tuning;
 
 /* ------------------------------------------------------------- lifetime -- */

@@ -178,11 +178,15 @@ def test_fused_trace_frame_bit_exact(vpt, oracle, scene, storage, threshold, blo
             ctx.end_frame()
 
 
-@pytest.mark.parametrize("mode", ["passes", "fused", "overlap_shadow"])
+@pytest.mark.parametrize("mode", ["passes", "fused", "overlap_shadow", "overlap_unsplit"])
 def test_render_frame_matches_oracle(vpt, oracle, scene, mode, gpu):
+    """Whole frames through vpt_render_frame: passes in line, the fused
+    trace, the sun-shadow trace and the temporal history gather on the second
+    stream (split_temporal), and the shadow alone there (the default)."""
     world = scene["world"]
     ctx = make_ctx(vpt, scene, vpt.STORAGE_F32)
-    ctx.set_tuning(fused_trace=mode == "fused", overlap_shadow=mode == "overlap_shadow")
+    ctx.set_tuning(fused_trace=mode == "fused", overlap_shadow=mode.startswith("overlap"),
+                   split_temporal=mode == "overlap_shadow")
     prev_g, hist = oracle.empty_history(H, W)
     prev_cam = scene["cams"][0]
     for fi, cam in enumerate(scene["cams"]):

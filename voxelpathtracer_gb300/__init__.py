@@ -104,7 +104,8 @@ class TraceBuffers(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("refill_threshold", C.c_int32), ("trace_blocks", C.c_int32), ("fused_trace", C.c_int32),
-                ("fused_prefilter", C.c_int32), ("overlap_shadow", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("fused_prefilter", C.c_int32), ("overlap_shadow", C.c_int32), ("split_temporal", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class BatchConfig(C.Structure):
@@ -578,7 +579,7 @@ class Context:
 
     def set_tuning(self, refill_threshold: int | None = None, trace_blocks: int | None = None,
                    fused_trace: bool | None = None, fused_prefilter: bool | None = None,
-                   overlap_shadow: bool | None = None):
+                   overlap_shadow: bool | None = None, split_temporal: bool | None = None):
         t = self.tuning()
         if refill_threshold is not None:
             t.refill_threshold = refill_threshold
@@ -590,6 +591,8 @@ class Context:
             t.fused_prefilter = 1 if fused_prefilter else 0
         if overlap_shadow is not None:
             t.overlap_shadow = 1 if overlap_shadow else 0
+        if split_temporal is not None:
+            t.split_temporal = 1 if split_temporal else 0
         self._ck(lib.vpt_set_tuning(self._h, C.byref(t)), "vpt_set_tuning")
 
     def tuning(self) -> Tuning:

@@ -159,6 +159,12 @@ struct vpt_ctx {
     cudaStream_t side_stream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool shadow_forked = false;
+    // the temporal pass's history gather queued on the side stream by
+    // trace_all (split_temporal), with the arguments it used
+    void* tsum = nullptr;
+    cudaEvent_t ev_tgather = nullptr;
+    bool tgather_pending = false;
+    TemporalArgs tgather_args;
 };
 
 namespace {
@@ -518,6 +524,7 @@ vpt_status vpt_create(vpt_ctx** out, const vpt_config* cfg) {
     c->tuning.refill_threshold = 16;
     c->tuning.trace_blocks = 0;
     c->tuning.overlap_shadow = 1;
+    c->tuning.split_temporal = 0;
     c->fp16 = cfg->storage == VPT_STORAGE_F16;
     c->npx = (size_t)cfg->width * (size_t)cfg->height;
     c->gd = gd;
@@ -563,6 +570,7 @@ vpt_status vpt_destroy(vpt_ctx* c) {
     if (c->side_stream) cudaStreamSynchronize(c->side_stream);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->ev_tgather) cudaEventDestroy(c->ev_tgather);
     if (c->side_stream) cudaStreamDestroy(c->side_stream);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1013,9 +1021,9 @@ vpt_status vpt_set_tuning(vpt_ctx* c, const vpt_tuning* t) {
     if (!c || !t) return VPT_ERR_INVALID_ARG;
     if (t->refill_threshold < 1 || t->refill_threshold > 32 || t->trace_blocks < 0 || t->trace_blocks > 65535 ||
         t->fused_trace < 0 || t->fused_trace > 1 || t->fused_prefilter < 0 || t->fused_prefilter > 1 ||
-        t->overlap_shadow < 0 || t->overlap_shadow > 1)
+        t->overlap_shadow < 0 || t->overlap_shadow > 1 || t->split_temporal < 0 || t->split_temporal > 1)
         return fail(c, VPT_ERR_INVALID_ARG, "refill_threshold must be 1..32, trace_blocks 0..65535, fused_trace, "
-                                            "fused_prefilter and overlap_shadow 0/1");
+                                            "fused_prefilter, overlap_shadow and split_temporal 0/1");
     c->tuning = *t;
     return VPT_OK;
 }
@@ -1029,6 +1037,21 @@ vpt_status vpt_get_tuning(const vpt_ctx* c, vpt_tuning* t) {
 }  // extern "C"
 
 namespace {
+
+// The temporal pass's arguments for the previous camera pc
+// (ProjectPositionPrevious's u_PrevProjection * u_PrevView, in the shader's
+// operation order) and frame f.
+TemporalArgs temporal_args(const vpt_camera& pc, const vpt_frame* f) {
+    TemporalArgs ta;
+    for (int col = 0; col < 4; col++)
+        for (int r = 0; r < 4; r++)
+            ta.prev_view_proj[col * 4 + r] = ((pc.proj[0 * 4 + r] * pc.view[col * 4 + 0] +
+                                               pc.proj[1 * 4 + r] * pc.view[col * 4 + 1]) +
+                                              pc.proj[2 * 4 + r] * pc.view[col * 4 + 2]) +
+                                             pc.proj[3 * 4 + r] * pc.view[col * 4 + 3];
+    ta.be_useful = f->temporal ? 1 : 0;
+    return ta;
+}
 
 // The denoiser passes of one frame; `atrous` false stops after the SVGF
 // variance pass (the learned path reads the temporal output instead).
@@ -1085,18 +1108,20 @@ vpt_status svgf_run(vpt_ctx* c, const vpt_camera* prev_cam, const vpt_frame* f, 
         pass_end(c, VPT_PASS_SPATIAL_INITIAL);
         c->launches += 1;
     }
-    TemporalArgs ta;
-    for (int col = 0; col < 4; col++)
-        for (int r = 0; r < 4; r++)
-            ta.prev_view_proj[col * 4 + r] = ((pc.proj[0 * 4 + r] * pc.view[col * 4 + 0] +
-                                               pc.proj[1 * 4 + r] * pc.view[col * 4 + 1]) +
-                                              pc.proj[2 * 4 + r] * pc.view[col * 4 + 2]) +
-                                             pc.proj[3 * 4 + r] * pc.view[col * 4 + 3];
-    ta.be_useful = f->temporal ? 1 : 0;
+    const TemporalArgs ta = temporal_args(pc, f);
     HistIO hout{c->hist[cur][HI_SH], c->hist[cur][HI_COCG], c->hist[cur][HI_UTIL], c->hist[cur][HI_AOSKY]};
     HistIO hprev{c->hist[prv][HI_SH], c->hist[prv][HI_COCG], c->hist[prv][HI_UTIL], c->hist[prv][HI_AOSKY]};
+    // the history gather queued by trace_all for this frame, if it used these arguments
+    const bool gathered = c->tgather_pending && !c->tuning.fused_prefilter && W == Wf && H == Hf &&
+                          std::memcmp(&ta, &c->tgather_args, sizeof ta) == 0;
+    c->tgather_pending = false;
     pass_begin(c, VPT_PASS_TEMPORAL);
-    if (!c->tuning.fused_prefilter)
+    if (gathered) {
+        CK(c, cudaStreamWaitEvent(c->stream, c->ev_tgather, 0));
+        CK(c, svgf_temporal_blend(W, H, c->fp16, ta, c->tsum,
+                                  GIIn{c->pre[GI_SH], c->pre[GI_COCG], c->pre[GI_LUMA], c->pre[GI_AOSKY]}, hout,
+                                  c->stream));
+    } else if (!c->tuning.fused_prefilter)
         CK(c, svgf_temporal(cv, W, H, Wf, Hf, c->fp16, ta, t, face, block, c->gbuf[prv][GB_T],
                             (const uint8_t*)c->gbuf[prv][GB_FACE], (const uint8_t*)c->gbuf[prv][GB_BLOCK],
                             GIIn{c->pre[GI_SH], c->pre[GI_COCG], c->pre[GI_LUMA], c->pre[GI_AOSKY]}, hprev, hout,
@@ -1335,8 +1360,32 @@ vpt_status trace_all(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f) {
         if ((s = join_shadow(c)) != VPT_OK) return fail(c, s, "joining the previous shadow pass failed");
         CK(c, cudaEventRecord(c->ev_fork, c->stream));
         CK(c, cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
+        c->tgather_pending = false;
+        if (c->tuning.split_temporal && c->cfg.denoiser == VPT_DENOISER_SVGF && !c->tuning.fused_prefilter &&
+            c->gd == 1 && !c->textured) {
+            // the temporal pass's history gather reads only this frame's
+            // G-buffer and the previous frame's planes: it runs here, ahead
+            // of the shadow pass, and svgf_run blends its sums (the previous
+            // camera as the frame calls pass it to svgf_run)
+            if (!c->tsum && (s = dalloc(c, &c->tsum, c->npx * 64)) != VPT_OK) return s;
+            if (!c->ev_tgather) CK(c, cudaEventCreateWithFlags(&c->ev_tgather, cudaEventDisableTiming));
+            const vpt_camera prev = c->have_prev ? c->prev_cam : *cam;
+            const TemporalArgs ta = temporal_args(prev, f);
+            const int cur = c->cur, prv = 1 - c->cur;
+            CK(c, svgf_temporal_gather(cam_view(c->cam), c->cfg.width, c->cfg.height, c->fp16, ta,
+                                       c->gbuf[cur][GB_T], (const uint8_t*)c->gbuf[cur][GB_FACE],
+                                       (const uint8_t*)c->gbuf[cur][GB_BLOCK], c->gbuf[prv][GB_T],
+                                       (const uint8_t*)c->gbuf[prv][GB_FACE], (const uint8_t*)c->gbuf[prv][GB_BLOCK],
+                                       HistIO{c->hist[prv][HI_SH], c->hist[prv][HI_COCG], c->hist[prv][HI_UTIL],
+                                              c->hist[prv][HI_AOSKY]},
+                                       c->tsum, c->side_stream));
+            CK(c, cudaEventRecord(c->ev_tgather, c->side_stream));
+            c->launches += 1;
+            c->tgather_args = ta;
+            c->tgather_pending = true;
+        }
         if ((s = shadow_run(c, f, c->side_stream)) != VPT_OK) return s;
-        CK(c, cudaEventRecord(c->ev_join, c->side_stream));
+        CK(c, cudaEventRecord(c->ev_join, c->side_stream));   // after both: joining it joins the gather too
         c->shadow_forked = true;
     } else if ((s = vpt_trace_shadow(c, f)) != VPT_OK) {
         return s;

@@ -268,6 +268,15 @@ cudaError_t svgf_temporal(const CamView& cam, int W, int H, int Wf, int Hf, int 
                           GIIn cur, HistIO prev, HistIO out, cudaStream_t s);
 // Spatial3x3Initial and the temporal pass fused (one launch; the
 // pre-filtered planes `pre` are written as svgf_spatial_initial writes them).
+// The temporal pass split in two (GI on the G-buffer's grid): the history
+// taps' sums into `sums` (64 bytes a texel), then their blend with the
+// pre-filtered planes; together bit-identical to svgf_temporal.
+cudaError_t svgf_temporal_gather(const CamView& cam, int W, int H, int fp16, const TemporalArgs& a, const void* t,
+                                 const uint8_t* face, const uint8_t* block, const void* prev_t,
+                                 const uint8_t* prev_face, const uint8_t* prev_block, HistIO prev, void* sums,
+                                 cudaStream_t s);
+cudaError_t svgf_temporal_blend(int W, int H, int fp16, const TemporalArgs& a, const void* sums, GIIn cur,
+                                HistIO out, cudaStream_t s);
 cudaError_t svgf_pre_temporal(const CamView& cam, int W, int H, int Wf, int Hf, int fp16, const TemporalArgs& a,
                               const void* t, const uint8_t* face, const uint8_t* block, const void* prev_t,
                               const uint8_t* prev_face, const uint8_t* prev_block, GIIn gi, GIOut pre, HistIO prev,

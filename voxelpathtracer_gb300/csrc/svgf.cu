@@ -123,13 +123,20 @@ __global__ void __launch_bounds__(256) k_spatial_initial(CamView cam, int W, int
 // The temporal pass for texel (i, j) with texture coordinate uv, position bp
 // and this frame's (pre-filtered) SH bsh, CoCg bcc, AO/sky bao and luminance
 // base_lum, as the planes hold them.
+// The history taps' weighted sums of the temporal pass (the loop of
+// TemporalFilter.glsl main over the five reprojected taps): the part that
+// reads only the G-buffers and the previous frame's history.
+struct TemporalSums {
+    float2 sh01, sh23, cc, ao, sm, lw;   // lw = (luminance sum, weight sum)
+    int successful;
+};
 template <typename S, bool kScaled>
-__device__ __forceinline__ void temporal_texel(const CamView& cam, int W, int H, int Wf, int Hf, const TemporalArgs& a,
-                                               const uint8_t* face, const uint8_t* block, const S* prev_t,
-                                               const uint8_t* prev_face, const uint8_t* prev_block, int i, int j,
-                                               v2 uv, v4 bp, float4 bsh, float2 bcc, float2 bao, float base_lum,
-                                               const S* p_sh, const S* p_cocg, const S* p_util, const S* p_aosky,
-                                               S* o_sh, S* o_cocg, S* o_util, S* o_aosky) {
+__device__ __forceinline__ TemporalSums temporal_gather(const CamView& cam, int W, int H, int Wf, int Hf,
+                                                        const TemporalArgs& a, const uint8_t* face,
+                                                        const uint8_t* block, const S* prev_t,
+                                                        const uint8_t* prev_face, const uint8_t* prev_block, int i,
+                                                        int j, v4 bp, const S* p_sh, const S* p_cocg,
+                                                        const S* p_util, const S* p_aosky) {
     const Plane8 PF{prev_face, Wf, Hf}, PB{prev_block, Wf, Hf};
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
     // taps k = 0..4 at (1, 0), (0, 1), (0, 0), (-1, 0), (0, -1), weights 3/32 and 9/64 at the centre
@@ -190,6 +197,18 @@ __device__ __forceinline__ void temporal_texel(const CamView& cam, int W, int H,
             successful++;
         }
     }
+    return TemporalSums{p_sh01, p_sh23, p_cc, p_ao, p_sm, p_lw, successful};
+}
+
+// The rest of the pass for texel px: the sums blended with this frame's
+// (pre-filtered) SH bsh, CoCg bcc, AO/sky bao and luminance base_lum as the
+// planes hold them, and the history written.
+template <typename S>
+__device__ __forceinline__ void temporal_blend(const TemporalArgs& a, size_t px, const TemporalSums& ts, float4 bsh,
+                                               float2 bcc, float2 bao, float base_lum, S* o_sh, S* o_cocg,
+                                               S* o_util, S* o_aosky) {
+    const float2 p_sh01 = ts.sh01, p_sh23 = ts.sh23, p_cc = ts.cc, p_ao = ts.ao, p_sm = ts.sm, p_lw = ts.lw;
+    int successful = ts.successful;
     float ssh[4] = {p_sh01.x, p_sh01.y, p_sh23.x, p_sh23.y}, scc[2] = {p_cc.x, p_cc.y}, sao[2] = {p_ao.x, p_ao.y};
     float sspp = p_sm.x, smom = p_sm.y, slum = p_lw.x;
     const float tw = p_lw.y;
@@ -235,6 +254,20 @@ __device__ __forceinline__ void temporal_texel(const CamView& cam, int W, int H,
         clampf(store_luma, -150.0f, 150.0f), 0.0f);
 }
 
+// The whole temporal pass for texel (i, j) with position bp.
+template <typename S, bool kScaled>
+__device__ __forceinline__ void temporal_texel(const CamView& cam, int W, int H, int Wf, int Hf, const TemporalArgs& a,
+                                               const uint8_t* face, const uint8_t* block, const S* prev_t,
+                                               const uint8_t* prev_face, const uint8_t* prev_block, int i, int j,
+                                               v2 uv, v4 bp, float4 bsh, float2 bcc, float2 bao, float base_lum,
+                                               const S* p_sh, const S* p_cocg, const S* p_util, const S* p_aosky,
+                                               S* o_sh, S* o_cocg, S* o_util, S* o_aosky) {
+    (void)uv;
+    const TemporalSums ts = temporal_gather<S, kScaled>(cam, W, H, Wf, Hf, a, face, block, prev_t, prev_face,
+                                                        prev_block, i, j, bp, p_sh, p_cocg, p_util, p_aosky);
+    temporal_blend<S>(a, (size_t)j * W + i, ts, bsh, bcc, bao, base_lum, o_sh, o_cocg, o_util, o_aosky);
+}
+
 template <typename S, bool kScaled>
 __global__ void __launch_bounds__(256, 4) k_temporal(CamView cam, int W, int H, int Wf, int Hf, TemporalArgs a, const S* t,
                                                   const uint8_t* face, const uint8_t* block, const S* prev_t,
@@ -252,6 +285,50 @@ __global__ void __launch_bounds__(256, 4) k_temporal(CamView cam, int W, int H, 
     temporal_texel<S, kScaled>(cam, W, H, Wf, Hf, a, face, block, prev_t, prev_face, prev_block, i, j, uv, bp,
                                ld4(c_sh + 4 * px), ld2(c_cocg + 2 * px), ld2(c_aosky + 2 * px), ld(c_luma + px), p_sh,
                                p_cocg, p_util, p_aosky, o_sh, o_cocg, o_util, o_aosky);
+}
+
+// The temporal pass in two launches, so that its history gather (all but
+// the final blend) can run beside the diffuse trace and the pre-filter:
+// k_temporal_gather stores each texel's sums (four float4: SH; CoCg, AO/sky;
+// moments, luminance and weight; taps accepted), k_temporal_blend blends them
+// with the pre-filtered planes once those exist. GI and G-buffer on one grid.
+template <typename S>
+__global__ void __launch_bounds__(256, 4) k_temporal_gather(CamView cam, int W, int H, TemporalArgs a, const S* t,
+                                                         const uint8_t* face, const uint8_t* block, const S* prev_t,
+                                                         const uint8_t* prev_face, const uint8_t* prev_block,
+                                                         const S* p_sh, const S* p_cocg, const S* p_util,
+                                                         const S* p_aosky, float4* sums) {
+    pdl_enter();
+    int i, j;
+    if (!pixel_of(W, H, &i, &j)) return;
+    const Plane<S, 1> T{t, W, H};
+    const size_t px = (size_t)j * W + i;
+    const v4 bp = position_fetch(cam, T, i, j, texcoord(i, j, W, H));
+    const TemporalSums ts = temporal_gather<S, false>(cam, W, H, W, H, a, face, block, prev_t, prev_face, prev_block,
+                                                      i, j, bp, p_sh, p_cocg, p_util, p_aosky);
+    float4* o = sums + 4 * px;
+    o[0] = make_float4(ts.sh01.x, ts.sh01.y, ts.sh23.x, ts.sh23.y);
+    o[1] = make_float4(ts.cc.x, ts.cc.y, ts.ao.x, ts.ao.y);
+    o[2] = make_float4(ts.sm.x, ts.sm.y, ts.lw.x, ts.lw.y);
+    o[3] = make_float4(__int_as_float(ts.successful), 0.0f, 0.0f, 0.0f);
+}
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_temporal_blend(int W, int H, TemporalArgs a, const float4* sums,
+                                                        const S* c_sh, const S* c_cocg, const S* c_luma,
+                                                        const S* c_aosky, S* o_sh, S* o_cocg, S* o_util,
+                                                        S* o_aosky) {
+    pdl_enter();
+    int i, j;
+    if (!pixel_of(W, H, &i, &j)) return;
+    const size_t px = (size_t)j * W + i;
+    const float4* q = sums + 4 * px;
+    const float4 s0 = q[0], s1 = q[1], s2 = q[2], s3 = q[3];
+    const TemporalSums ts{make_float2(s0.x, s0.y), make_float2(s0.z, s0.w), make_float2(s1.x, s1.y),
+                          make_float2(s1.z, s1.w), make_float2(s2.x, s2.y), make_float2(s2.z, s2.w),
+                          __float_as_int(s3.x)};
+    temporal_blend<S>(a, px, ts, ld4(c_sh + 4 * px), ld2(c_cocg + 2 * px), ld2(c_aosky + 2 * px), ld(c_luma + px),
+                      o_sh, o_cocg, o_util, o_aosky);
 }
 
 // Spatial3x3Initial and the temporal pass in one kernel: the temporal pass
@@ -775,6 +852,26 @@ cudaError_t launch_temporal(const CamView& cam, int W, int H, int Wf, int Hf, co
     return cudaGetLastError();
 }
 
+template <typename S>
+cudaError_t launch_temporal_gather(const CamView& cam, int W, int H, const TemporalArgs& a, const void* t,
+                                   const uint8_t* face, const uint8_t* block, const void* prev_t,
+                                   const uint8_t* prev_face, const uint8_t* prev_block, HistIO prev, void* sums,
+                                   cudaStream_t s) {
+    pdl_launch(k_temporal_gather<S>, grid2(W, H), kBlock2, 0, s, cam, W, H, a, (const S*)t, face, block,
+               (const S*)prev_t, prev_face, prev_block, (const S*)prev.sh, (const S*)prev.cocg, (const S*)prev.util,
+               (const S*)prev.aosky, (float4*)sums);
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t launch_temporal_blend(int W, int H, const TemporalArgs& a, const void* sums, GIIn cur, HistIO out,
+                                  cudaStream_t s) {
+    pdl_launch(k_temporal_blend<S>, grid2(W, H), kBlock2, 0, s, W, H, a, (const float4*)sums, (const S*)cur.sh,
+               (const S*)cur.cocg, (const S*)cur.luma, (const S*)cur.aosky, (S*)out.sh, (S*)out.cocg, (S*)out.util,
+               (S*)out.aosky);
+    return cudaGetLastError();
+}
+
 template <typename S, bool kScaled>
 cudaError_t launch_pre_temporal(const CamView& cam, int W, int H, int Wf, int Hf, const TemporalArgs& a, const void* t,
                                 const uint8_t* face, const uint8_t* block, const void* prev_t,
@@ -862,6 +959,22 @@ cudaError_t svgf_temporal(const CamView& cam, int W, int H, int Wf, int Hf, int 
                                                  cur, prev, out, s)
                   : launch_temporal<float, false>(cam, W, H, Wf, Hf, a, t, face, block, prev_t, prev_face, prev_block,
                                                   cur, prev, out, s);
+}
+
+cudaError_t svgf_temporal_gather(const CamView& cam, int W, int H, int fp16, const TemporalArgs& a, const void* t,
+                                 const uint8_t* face, const uint8_t* block, const void* prev_t,
+                                 const uint8_t* prev_face, const uint8_t* prev_block, HistIO prev, void* sums,
+                                 cudaStream_t s) {
+    return fp16 ? launch_temporal_gather<__half>(cam, W, H, a, t, face, block, prev_t, prev_face, prev_block, prev,
+                                                 sums, s)
+                : launch_temporal_gather<float>(cam, W, H, a, t, face, block, prev_t, prev_face, prev_block, prev,
+                                                sums, s);
+}
+
+cudaError_t svgf_temporal_blend(int W, int H, int fp16, const TemporalArgs& a, const void* sums, GIIn cur,
+                                HistIO out, cudaStream_t s) {
+    return fp16 ? launch_temporal_blend<__half>(W, H, a, sums, cur, out, s)
+                : launch_temporal_blend<float>(W, H, a, sums, cur, out, s);
 }
 
 cudaError_t svgf_pre_temporal(const CamView& cam, int W, int H, int Wf, int Hf, int fp16, const TemporalArgs& a,
