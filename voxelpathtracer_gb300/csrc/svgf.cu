@@ -24,14 +24,48 @@ __device__ __forceinline__ bool pixel_of(int W, int H, int* i, int* j) {
 __device__ __forceinline__ float as_stored(float v, const float*) { return v; }
 __device__ __forceinline__ float as_stored(float v, const __half*) { return __half2float(__float2half_rn(v)); }
 
+// The pre-filter's tap fetches at an in-image texel (si, sj): the depth, and
+// the SH, CoCg, face and AO/sky; from the planes, or from a shared-memory
+// tile of the 34 x 10 texels around a 32 x 8 block.
+template <typename S>
+struct PreGlobal {
+    int W;
+    const S *t, *sh, *cocg, *aosky;
+    const uint8_t* face;
+    __device__ __forceinline__ float depth(int si, int sj) const { return ld(t + (size_t)sj * W + si); }
+    __device__ __forceinline__ void tap(int si, int sj, float4* s4, float2* s2, int* f, float2* a2) const {
+        const size_t q = (size_t)sj * W + si;
+        *s4 = ld4(sh + 4 * q);
+        *s2 = ld2(cocg + 2 * q);
+        *f = __ldg(face + q);
+        *a2 = ld2(aosky + 2 * q);
+    }
+};
+constexpr int kPreTW = 34, kPreTH = 10, kPreN = kPreTW * kPreTH;
+struct PreTile {
+    const float4 *A, *B;
+    const float2* C;   // (depth, face)
+    int tx0, ty0;
+    __device__ __forceinline__ float depth(int si, int sj) const { return C[(sj - ty0) * kPreTW + si - tx0].x; }
+    __device__ __forceinline__ void tap(int si, int sj, float4* s4, float2* s2, int* f, float2* a2) const {
+        const int k = (sj - ty0) * kPreTW + si - tx0;
+        *s4 = A[k];
+        const float4 b = B[k];
+        *s2 = make_float2(b.x, b.y);
+        *a2 = make_float2(b.z, b.w);
+        *f = __float_as_int(C[k].y);
+    }
+};
+
 // Spatial3x3Initial.glsl main (:96-176) for texel (i, j) with texture
 // coordinate uv and reconstructed position bp; out: SH (4), CoCg (2), AO/sky
 // (2) and the luminance passed through.
-template <typename S>
+template <typename S, class PF = PreGlobal<S>>
 __device__ __forceinline__ void pre_filter_texel(const CamView& cam, int W, int H, const Plane<S, 1>& T,
                                                  const uint8_t* face, const S* sh, const S* cocg, const S* luma,
                                                  const S* aosky, int i, int j, v2 uv, v4 bp, float* o_sh,
-                                                 float* o_cc, float* o_ao, float* o_luma) {
+                                                 float* o_cc, float* o_ao, float* o_luma, const PF* pf = nullptr) {
+    const PreGlobal<S> pg{W, T.p, sh, cocg, aosky, face};
     const float texel_x = 1.0f / (float)W, texel_y = 1.0f / (float)H;
     const float aw[3] = {1.0f, 2.0f / 3.0f, 1.0f / 6.0f};
     const size_t px = (size_t)j * W + i;
@@ -55,16 +89,20 @@ __device__ __forceinline__ void pre_filter_texel(const CamView& cam, int W, int 
             if (x == 0 && y == 0) continue;
             const int si = i + x, sj = j + y;
             if (si < 0 || si >= W || sj < 0 || sj >= H) continue;
-            const size_t sp_ = (size_t)sj * W + si;
             v2 sc = mk2(uv.x + (float)x * texel_x, uv.y + (float)y * texel_y);
-            v4 sp = position_fetch(cam, T, si, sj, sc);
-            v3 pd = mk3(fabsf(sp.x - bp.x), fabsf(sp.y - bp.y), fabsf(sp.z - bp.z));
+            // GetPositionAt: position_fetch's operations on the tap's depth
+            const float sd = pf ? pf->depth(si, sj) : pg.depth(si, sj);
+            const v3 spp = add(ray_origin(cam), muls(normalize(ray_dir_at(cam, sc)), sd));
+            v3 pd = mk3(fabsf(spp.x - bp.x), fabsf(spp.y - bp.y), fabsf(spp.z - bp.z));
             float dist_sqr = dot(pd, pd);
             if (dist_sqr < 1.0f) {
-                float4 s4 = ld4(sh + 4 * sp_);
-                float2 s2 = ld2(cocg + 2 * sp_);
+                float4 s4;
+                float2 s2, a2;
+                int sf;
+                if (pf) pf->tap(si, sj, &s4, &s2, &sf, &a2);
+                else pg.tap(si, sj, &s4, &s2, &sf, &a2);
                 float ssh[4] = {s4.x, s4.y, s4.z, s4.w};
-                const int fc = face_cos(bf, __ldg(face + sp_));
+                const int fc = face_cos(bf, sf);
                 float sl = sh_to_y(ssh);
                 // pow(max(dot(n, n'), 0), 16) for a clamped dot of 0, 1 or 3
                 float nw = fc == 0 ? 0.0f : (fc == 1 ? 1.0f : nw3);
@@ -77,7 +115,6 @@ __device__ __forceinline__ void pre_filter_texel(const CamView& cam, int W, int 
                 t01 = pacc(t01, make_float2(s4.x, s4.y), wgt);
                 t23 = pacc(t23, make_float2(s4.z, s4.w), wgt);
                 tcc2 = pacc(tcc2, s2, wgt);
-                const float2 a2 = ld2(aosky + 2 * sp_);
                 tao2 = pacc(tao2, a2, wgt);
                 tww = padd(tww, splat(wgt));
             }
@@ -100,7 +137,23 @@ template <typename S>
 __global__ void __launch_bounds__(256) k_spatial_initial(CamView cam, int W, int H, const S* t, const uint8_t* face,
                                                          const S* sh, const S* cocg, const S* luma, const S* aosky,
                                                          S* o_sh, S* o_cocg, S* o_luma, S* o_aosky) {
+    __shared__ float4 s_a[kPreN], s_b[kPreN];
+    __shared__ float2 s_c[kPreN];
     pdl_enter();
+    // the block's 3x3 neighbourhoods, loaded once (taps outside the image are
+    // skipped by the filter and never read)
+    const int tx0 = (int)blockIdx.x * 32 - 1, ty0 = (int)blockIdx.y * 8 - 1;
+    for (int q = threadIdx.y * 32 + threadIdx.x; q < kPreN; q += 256) {
+        const int ly = q / kPreTW, lx = q - ly * kPreTW;
+        const int si = tx0 + lx, sj = ty0 + ly;
+        if (si < 0 || si >= W || sj < 0 || sj >= H) continue;
+        const size_t g = (size_t)sj * W + si;
+        const float2 cc = ld2(cocg + 2 * g), ao = ld2(aosky + 2 * g);
+        s_a[q] = ld4(sh + 4 * g);
+        s_b[q] = make_float4(cc.x, cc.y, ao.x, ao.y);
+        s_c[q] = make_float2(ld(t + g), __int_as_float((int)__ldg(face + g)));
+    }
+    __syncthreads();
     int i, j;
     if (!pixel_of(W, H, &i, &j)) return;
     const Plane<S, 1> T{t, W, H};
@@ -108,7 +161,8 @@ __global__ void __launch_bounds__(256) k_spatial_initial(CamView cam, int W, int
     const v2 uv = texcoord(i, j, W, H);
     const v4 bp = position_fetch(cam, T, i, j, uv);
     float psh[4], pcc[2], pao[2], pl;
-    pre_filter_texel<S>(cam, W, H, T, face, sh, cocg, luma, aosky, i, j, uv, bp, psh, pcc, pao, &pl);
+    const PreTile tile{s_a, s_b, s_c, tx0, ty0};
+    pre_filter_texel<S, PreTile>(cam, W, H, T, face, sh, cocg, luma, aosky, i, j, uv, bp, psh, pcc, pao, &pl, &tile);
     st4(o_sh + 4 * px, psh[0], psh[1], psh[2], psh[3]);
     st2(o_cocg + 2 * px, pcc[0], pcc[1]);
     st2(o_aosky + 2 * px, pao[0], pao[1]);
