@@ -178,6 +178,34 @@ def test_fused_trace_frame_bit_exact(vpt, oracle, scene, storage, threshold, blo
             ctx.end_frame()
 
 
+@pytest.mark.parametrize("storage,bounces", [(0, 1), (0, 2), (1, 2)])
+def test_diffuse_pass_bit_exact(vpt, oracle, scene, storage, bounces, gpu):
+    """The diffuse pass at one sample (the staged kernel for one bounce, the
+    per-texel kernel for two) writes the oracle's GI planes and counts its
+    rays and steps."""
+    world = scene["world"]
+    with vpt.Context(width=W, height=H, primary_max_steps=256, storage=storage, bounces=bounces) as ctx:
+        ctx.upload_world(scene["vox"])
+        ctx.set_block_table(scene["blocks"])
+        ctx.build_df()
+        for fi, cam in enumerate(scene["cams"]):
+            frame = vpt.default_frame(frame_index=fi, seed=29)
+            ctx.trace_primary(cam)
+            ctx.set_stats(True)
+            ctx.trace_diffuse(frame)
+            stats = ctx.read_stats()
+            ctx.set_stats(False)
+            cfg = ctx.config
+            g = oracle.trace_primary(world, cam, cfg)
+            with oracle.Counting() as cnt:
+                gi = oracle.trace_diffuse(world, cam, cfg, frame, g["t"], g["face"])
+            for k in GI_PLANES:
+                assert_same(ctx.read_plane("GI_" + k.upper()), gi[k], f"bounces {bounces} GI {k} frame {fi}")
+            for kind in ("diffuse", "bounce_shadow"):
+                assert stats["rays"][kind] == cnt.rays[kind] and stats["steps"][kind] == cnt.steps[kind], kind
+            ctx.end_frame()
+
+
 @pytest.mark.parametrize("mode", ["passes", "fused", "overlap_shadow", "overlap_unsplit"])
 def test_render_frame_matches_oracle(vpt, oracle, scene, mode, gpu):
     """Whole frames through vpt_render_frame: passes in line, the fused
