@@ -101,3 +101,27 @@ def test_division_by_five_in_three_operations_is_exact(L):
     assert L.vpto_check_div_const(5.0, 0, 0x7F800000) == 0
     # the check does see a difference: infinity, which the form turns into NaN
     assert L.vpto_check_div_const(5.0, 0x7F800000, 0x7F800001) == 1
+
+
+def test_libvpt_host_references_of_the_packed_checks(vpt):
+    """The host side of detmath's packed-pair checks (ops 6..15), the values
+    the device's packed forms are compared with: IEEE products, sums, x + y x,
+    the two-row bilinear blend and x / 5, as numpy's float32 gives them."""
+    rng = np.random.default_rng(12)
+    n = 4000
+    x = (rng.uniform(-1, 1, n) * np.exp2(rng.integers(-20, 20, n))).astype(np.float32)
+    y = (rng.uniform(-1, 1, n) * np.exp2(rng.integers(-20, 20, n))).astype(np.float32)
+    with np.errstate(over="ignore", invalid="ignore"):
+        for op, want in ((6, x * y), (7, x * y), (8, x + y), (9, x + y), (12, x + y * x), (15, x / np.float32(5))):
+            got = vpt.detmath(op, x, y, on_device=False)
+            assert np.array_equal(got.view(np.uint32), want.astype(np.float32).view(np.uint32)), op
+        w = rng.uniform(0, 8, n).astype(np.float32)
+        ax = w - np.floor(w)
+        ay = np.float32(2) * w - np.floor(np.float32(2) * w)
+        bx, by = np.float32(1) - ax, np.float32(1) - ay
+        lo = x * bx + (np.float32(2) * x) * ax
+        hi = (-x) * bx + w * ax
+        want = lo * by + hi * ay
+        for op in (13, 14):
+            got = vpt.detmath(op, x, w, on_device=False)
+            assert np.array_equal(got.view(np.uint32), want.astype(np.float32).view(np.uint32)), op
