@@ -225,10 +225,17 @@ int max_blocks_for(int block_threads) {
 // The three pass kernels of the phased launch, each with the grid that fills
 // every SM to its own occupancy limit (or `blocks`).
 template <int B, bool kWide>
-cudaError_t launch_passes(const BatchLaunch& a, int block_threads, int blocks, int sms, cudaStream_t s) {
+cudaError_t launch_passes(const BatchLaunch& a, int block_threads, int blocks, int sms, cudaStream_t s,
+                          const BatchSide* side) {
     using K = void (*)(BatchLaunch);
     const K ks[3] = {k_batch_pass<B, 0, kWide>, k_batch_pass<B, 1, kWide>, k_batch_pass<B, 2, kWide>};
     for (int p = 0; p < 3; p++) {
+        cudaStream_t st = s;
+        if (side && p == 1) {   // the shadow pass on the side stream, beside the diffuse pass
+            if (cudaEventRecord(side->fork, s) != cudaSuccess || cudaStreamWaitEvent(side->side, side->fork, 0) != cudaSuccess)
+                return cudaErrorInvalidValue;
+            st = side->side;
+        }
         int g = blocks;
         if (g <= 0) {
             int n = 0;
@@ -239,10 +246,12 @@ cudaError_t launch_passes(const BatchLaunch& a, int block_threads, int blocks, i
             g = n * sms;
         }
         if (g <= 0) return cudaErrorInvalidConfiguration;
-        ks[p]<<<g, block_threads, 0, s>>>(a);
+        ks[p]<<<g, block_threads, 0, st>>>(a);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
+        if (side && p == 1 && cudaEventRecord(side->join, side->side) != cudaSuccess) return cudaErrorInvalidValue;
     }
+    if (side && cudaStreamWaitEvent(s, side->join, 0) != cudaSuccess) return cudaErrorInvalidValue;
     return cudaSuccess;
 }
 
@@ -259,7 +268,7 @@ int batch_max_blocks(int df_brick, int block_threads, int rays_per_lane, int dev
 }
 
 cudaError_t batch_trace(const BatchLaunch& a, int df_brick, int block_threads, int rays_per_lane, int blocks,
-                        int phased, cudaStream_t s) {
+                        int phased, cudaStream_t s, const BatchSide* side) {
     if (a.n_worlds < 1 || a.n_worlds > kBatchMaxWorlds || block_threads < 32 || block_threads > 512 ||
         (block_threads & 31) || a.tiles_per_grab < 1 || (rays_per_lane != 1 && rays_per_lane != 2) ||
         (phased && rays_per_lane != 1))
@@ -271,12 +280,12 @@ cudaError_t batch_trace(const BatchLaunch& a, int df_brick, int block_threads, i
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return cudaErrorInvalidValue;
         const bool wide = block_threads > 256;
         switch (df_brick) {
-            case 0: return wide ? launch_passes<0, true>(a, block_threads, blocks, sms, s)
-                                : launch_passes<0, false>(a, block_threads, blocks, sms, s);
-            case 4: return wide ? launch_passes<4, true>(a, block_threads, blocks, sms, s)
-                                : launch_passes<4, false>(a, block_threads, blocks, sms, s);
-            case 8: return wide ? launch_passes<8, true>(a, block_threads, blocks, sms, s)
-                                : launch_passes<8, false>(a, block_threads, blocks, sms, s);
+            case 0: return wide ? launch_passes<0, true>(a, block_threads, blocks, sms, s, side)
+                                : launch_passes<0, false>(a, block_threads, blocks, sms, s, side);
+            case 4: return wide ? launch_passes<4, true>(a, block_threads, blocks, sms, s, side)
+                                : launch_passes<4, false>(a, block_threads, blocks, sms, s, side);
+            case 8: return wide ? launch_passes<8, true>(a, block_threads, blocks, sms, s, side)
+                                : launch_passes<8, false>(a, block_threads, blocks, sms, s, side);
             default: return cudaErrorInvalidValue;
         }
     }

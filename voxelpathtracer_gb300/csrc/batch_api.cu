@@ -47,6 +47,7 @@ struct vpt_batch {
     vpt_batch_config cfg{};
     int dev = 0;
     cudaStream_t stream = nullptr;
+    BatchSide side{nullptr, nullptr, nullptr};   // the phased launch's shadow stream
     std::string err;
     std::vector<HostWorld> worlds;
     bool df_valid = false;
@@ -235,10 +236,24 @@ BatchLaunch launch_args(vpt_batch* b) {
     return a;
 }
 
+vpt_status ensure_side(vpt_batch* b) {
+    if (b->side.side) return VPT_OK;
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    BCK(b, cudaStreamCreateWithPriority(&b->side.side, cudaStreamNonBlocking, hi));
+    BCK(b, cudaEventCreateWithFlags(&b->side.fork, cudaEventDisableTiming));
+    BCK(b, cudaEventCreateWithFlags(&b->side.join, cudaEventDisableTiming));
+    return VPT_OK;
+}
+
 vpt_status launch_persistent(vpt_batch* b) {
     BCK(b, cudaMemsetAsync(b->d_queue, 0, 3 * sizeof(int), b->stream));
+    if (b->tuning.phased) {
+        const vpt_status st = ensure_side(b);
+        if (st != VPT_OK) return st;
+    }
     BCK(b, batch_trace(launch_args(b), b->tuning.df_brick, b->tuning.block_threads, b->tuning.rays_per_lane,
-                       b->tuning.blocks, b->tuning.phased, b->stream));
+                       b->tuning.blocks, b->tuning.phased, b->stream, b->tuning.phased ? &b->side : nullptr));
     b->launches += b->tuning.phased ? 3 : 1;
     return VPT_OK;
 }
@@ -250,10 +265,15 @@ vpt_status launch_graph(vpt_batch* b) {
             b->graph = nullptr;
         }
         cudaGraph_t g = nullptr;
+        if (b->tuning.phased) {
+            const vpt_status st = ensure_side(b);
+            if (st != VPT_OK) return st;
+        }
         BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
         cudaError_t e1 = cudaMemsetAsync(b->d_queue, 0, 3 * sizeof(int), b->stream);
         cudaError_t e2 = batch_trace(launch_args(b), b->tuning.df_brick, b->tuning.block_threads, b->tuning.rays_per_lane,
-                                     b->tuning.blocks, b->tuning.phased, b->stream);
+                                     b->tuning.blocks, b->tuning.phased, b->stream,
+                                     b->tuning.phased ? &b->side : nullptr);
         cudaError_t e3 = cudaStreamEndCapture(b->stream, &g);
         if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -370,6 +390,10 @@ vpt_status vpt_batch_destroy(vpt_batch* b) {
     cudaSetDevice(b->dev);
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->side.side) cudaStreamSynchronize(b->side.side);
+    if (b->side.fork) cudaEventDestroy(b->side.fork);
+    if (b->side.join) cudaEventDestroy(b->side.join);
+    if (b->side.side) cudaStreamDestroy(b->side.side);
     for (void* p : b->allocs) cudaFree(p);
     if (b->h_frame) cudaFreeHost(b->h_frame);
     if (b->frame_copied) cudaEventDestroy(b->frame_copied);

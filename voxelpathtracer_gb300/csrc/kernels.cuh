@@ -205,8 +205,14 @@ constexpr int kBatchMaxWorlds = 1024;
 // df_brick: 0, 4 or 8; blocks <= 0 fills every SM to its occupancy limit;
 // phased: the primary, shadow and diffuse passes as three persistent kernels
 // (rays_per_lane 1) instead of one.
+// The phased launch's shadow pass may run on `side` beside the diffuse pass
+// (forked after the primary pass with `fork`, joined with `join`).
+struct BatchSide {
+    cudaStream_t side;
+    cudaEvent_t fork, join;
+};
 cudaError_t batch_trace(const BatchLaunch& a, int df_brick, int block_threads, int rays_per_lane, int blocks,
-                        int phased, cudaStream_t s);
+                        int phased, cudaStream_t s, const BatchSide* side = nullptr);
 int batch_max_blocks(int df_brick, int block_threads, int rays_per_lane, int device);
 // Copies an x-fastest distance field into the BxBxB brick layout of df_index.
 cudaError_t df_to_bricks(const uint8_t* df, uint8_t* out, int X, int Y, int Z, int brick, cudaStream_t s);
