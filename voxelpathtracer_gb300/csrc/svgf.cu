@@ -827,15 +827,19 @@ __device__ __forceinline__ void atrous_texels(int W, int H, const AtrousArgs& a,
                     const float sl = sh_to_y(ssh);
                     // clamp(pow(max(dot(n, n'), 0), 32), 0.001, 1) for a clamped dot of 0, 1 or 3
                     const float nw = face_cos(q.bf, sface[p]) > 0 ? 1.0f : 0.001f;
-                    const float de = dexp(-fmaxf(dd, 0.00001f));
-                    const float dw = clampf(de * de, 0.0001f, 1.0f);   // pow(e, 2) for e in [0, 1)
-                    float wgt;
-                    if (q.strong) {   // young histories: no luminance weight (nor its division and exponential)
-                        wgt = nw * dw;
+                    // young histories: no luminance weight (nor its division and exponential); otherwise the
+                    // depth and luminance exponentials as one packed polynomial
+                    const float dn = -fmaxf(dd, 0.00001f);
+                    float de, le = 0.0f;
+                    if (q.strong) {
+                        de = dexp(dn);
                     } else {
-                        const float lw = fabsf(sl - q.bl) / q.phi;
-                        wgt = (dexp(-lw) * nw) * dw;
+                        const float2 e = dexp_pair(dn, -(fabsf(sl - q.bl) / q.phi));
+                        de = e.x;
+                        le = e.y;
                     }
+                    const float dw = clampf(de * de, 0.0001f, 1.0f);   // pow(e, 2) for e in [0, 1)
+                    float wgt = q.strong ? nw * dw : (le * nw) * dw;
                     wgt = clampf(wgt, 0.001f, 1.0f);
                     const float xw = x == 0 ? aw[0] : aw[1], yw = y == 0 ? aw[0] : aw[1];
                     wgt = (xw * yw) * wgt;
