@@ -1352,11 +1352,10 @@ vpt_status trace_all(vpt_ctx* c, const vpt_camera* cam, const vpt_frame* f) {
         // the shadow pass reads only this frame's G-buffer and writes only the
         // shadow plane, which nothing reads before the reflection and colour
         // passes: it runs on the side stream beside the diffuse trace and SVGF
-        if (!c->side_stream) {
-            CK(c, cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking));
-            CK(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
-            CK(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
-        }
+        // each handle created once (a call after a failed creation retries the missing ones)
+        if (!c->side_stream) CK(c, cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking));
+        if (!c->ev_fork) CK(c, cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+        if (!c->ev_join) CK(c, cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
         if ((s = join_shadow(c)) != VPT_OK) return fail(c, s, "joining the previous shadow pass failed");
         CK(c, cudaEventRecord(c->ev_fork, c->stream));
         CK(c, cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0));
@@ -1550,11 +1549,9 @@ vpt_status vpt_render_frame_async(vpt_ctx* c, const vpt_camera* cam, const vpt_f
     if (!c) return VPT_ERR_INVALID_ARG;
     if (!cam || !f || !rgb_out) return fail(c, VPT_ERR_INVALID_ARG, "camera, frame and rgb_out are required");
     cudaSetDevice(c->dev);
-    if (!c->copy_stream) {
-        CK(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-        CK(c, cudaEventCreateWithFlags(&c->ev_color, cudaEventDisableTiming));
-        CK(c, cudaEventCreateWithFlags(&c->ev_copy, cudaEventDisableTiming));
-    }
+    if (!c->copy_stream) CK(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    if (!c->ev_color) CK(c, cudaEventCreateWithFlags(&c->ev_color, cudaEventDisableTiming));
+    if (!c->ev_copy) CK(c, cudaEventCreateWithFlags(&c->ev_copy, cudaEventDisableTiming));
     vpt_status s;
     const vpt_camera prev = c->have_prev ? c->prev_cam : *cam;
     if ((s = trace_all(c, cam, f)) != VPT_OK) return s;

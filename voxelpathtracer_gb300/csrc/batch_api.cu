@@ -237,12 +237,14 @@ BatchLaunch launch_args(vpt_batch* b) {
 }
 
 vpt_status ensure_side(vpt_batch* b) {
-    if (b->side.side) return VPT_OK;
-    int lo = 0, hi = 0;
-    cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    BCK(b, cudaStreamCreateWithPriority(&b->side.side, cudaStreamNonBlocking, hi));
-    BCK(b, cudaEventCreateWithFlags(&b->side.fork, cudaEventDisableTiming));
-    BCK(b, cudaEventCreateWithFlags(&b->side.join, cudaEventDisableTiming));
+    // each handle created once; a call after a failed creation retries the missing ones
+    if (!b->side.side) {
+        int lo = 0, hi = 0;
+        cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        BCK(b, cudaStreamCreateWithPriority(&b->side.side, cudaStreamNonBlocking, hi));
+    }
+    if (!b->side.fork) BCK(b, cudaEventCreateWithFlags(&b->side.fork, cudaEventDisableTiming));
+    if (!b->side.join) BCK(b, cudaEventCreateWithFlags(&b->side.join, cudaEventDisableTiming));
     return VPT_OK;
 }
 
