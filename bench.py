@@ -340,8 +340,10 @@ def run_ours(args):
         vrays = 0
         for s in range(total):
             vc.render_frame(camera_at(vpt, yaw, pitch, s), frame_at(vpt, s), readback=False)
+            # read (and reset) every frame, so the warm-up frames' rays are not counted
+            st = vc.read_stats()
             if s >= args.warmup:
-                vrays += sum(vc.read_stats()["rays"].values())
+                vrays += sum(st["rays"].values())
         vc.set_stats(False)
         vc.reset_history()
         vs = torch.cuda.ExternalStream(vc.stream(), device=local)
