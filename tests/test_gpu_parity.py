@@ -100,16 +100,20 @@ def test_distance_field_empty_and_full(vpt, oracle, gpu):
         assert (got == (0 if fill else min(254, 90))).all()
 
 
-@pytest.mark.parametrize("fused", [False, True], ids=["split_prefilter", "fused_prefilter"])
-@pytest.mark.parametrize("storage", [0, 1], ids=["f32", "f16"])
-def test_passes_bit_exact_two_frames(vpt, oracle, scene, storage, fused, gpu):
+def check_passes_two_frames(vpt, oracle, scene, storage, fused, w=W, h=H, cams=None):
+    """Every plane of every pass over two frames (the second reprojects the
+    first), pass by pass against the oracle, at a w x h image."""
     world = scene["world"]
-    ctx = make_ctx(vpt, scene, storage)
+    cams = cams or scene["cams"]
+    ctx = vpt.Context(width=w, height=h, primary_max_steps=256, storage=storage)
+    ctx.upload_world(scene["vox"])
+    ctx.set_block_table(scene["blocks"])
+    ctx.build_df()
     ctx.set_tuning(fused_prefilter=fused)
     cfg = ctx.config
-    prev_g, hist = oracle.empty_history(H, W)
-    prev_cam = scene["cams"][0]
-    for fi, cam in enumerate(scene["cams"]):
+    prev_g, hist = oracle.empty_history(h, w)
+    prev_cam = cams[0]
+    for fi, cam in enumerate(cams):
         frame = vpt.default_frame(frame_index=fi, seed=11, time=1.3 + 0.37 * fi)
         ctx.trace_primary(cam)
         g = oracle.trace_primary(world, cam, cfg)
@@ -142,6 +146,27 @@ def test_passes_bit_exact_two_frames(vpt, oracle, scene, storage, fused, gpu):
         hist = sv["temporal"]
         prev_cam = cam
     ctx.close()
+
+
+@pytest.mark.parametrize("fused", [False, True], ids=["split_prefilter", "fused_prefilter"])
+@pytest.mark.parametrize("storage", [0, 1], ids=["f32", "f16"])
+def test_passes_bit_exact_two_frames(vpt, oracle, scene, storage, fused, gpu):
+    check_passes_two_frames(vpt, oracle, scene, storage, fused)
+
+
+@pytest.mark.parametrize("size", [(101, 67), (45, 13), (7, 5), (1, 1)], ids=lambda s: f"{s[0]}x{s[1]}")
+@pytest.mark.parametrize("storage", [0, 1], ids=["f32", "f16"])
+def test_passes_bit_exact_ragged_sizes(vpt, oracle, scene, storage, size, gpu):
+    """Images whose sides are no multiple of any block shape (the 16x16 trace
+    tiles, the 16x32 staged diffuse blocks, the 32x8 filter blocks and their
+    shared-memory neighbourhoods), down to a single texel: the border blocks'
+    fallbacks and every image-edge test, pass by pass."""
+    w, h = size
+    X, Y, Z = DIMS
+    yaw, pitch = vpt.seeded_pose(1)
+    cams = [vpt.camera_from_pose((X / 2, 58.0, Z / 2), yaw, pitch, 90.0, w / h),
+            vpt.camera_from_pose((X / 2 + 0.7, 58.2, Z / 2 - 0.4), yaw + 2.0, pitch + 1.0, 90.0, w / h)]
+    check_passes_two_frames(vpt, oracle, scene, storage, False, w, h, cams)
 
 
 TRACE_PLANES = [("t", "T"), ("face", "FACE"), ("block", "BLOCK"), ("hit", "HIT"), ("steps", "STEPS")]
@@ -226,6 +251,31 @@ def test_render_frame_matches_oracle(vpt, oracle, scene, mode, gpu):
         hist = ref["svgf"]["temporal"]
         prev_cam = cam
     ctx.close()
+
+
+def test_render_frame_ragged_size(vpt, oracle, scene, gpu):
+    """Whole frames at 101 x 67 with the default tuning (sun shadow on the
+    second stream, staged diffuse trace, tiled filter steps)."""
+    w, h = 101, 67
+    X, Y, Z = DIMS
+    yaw, pitch = vpt.seeded_pose(1)
+    cams = [vpt.camera_from_pose((X / 2, 58.0, Z / 2), yaw, pitch, 90.0, w / h),
+            vpt.camera_from_pose((X / 2 + 0.7, 58.2, Z / 2 - 0.4), yaw + 2.0, pitch + 1.0, 90.0, w / h)]
+    world = scene["world"]
+    with vpt.Context(width=w, height=h, primary_max_steps=256) as ctx:
+        ctx.upload_world(scene["vox"])
+        ctx.set_block_table(scene["blocks"])
+        ctx.build_df()
+        prev_g, hist = oracle.empty_history(h, w)
+        prev_cam = cams[0]
+        for fi, cam in enumerate(cams):
+            frame = vpt.default_frame(frame_index=fi, seed=3, time=0.5 * fi)
+            rgb = ctx.render_frame(cam, frame)
+            ref = oracle.render_frame(world, cam, prev_cam, ctx.config, frame, prev_g, hist)
+            assert_same(rgb, ref["rgb"], f"render_frame {fi}")
+            prev_g = {k: ref["g"][k] for k in ("t", "face", "block")}
+            hist = ref["svgf"]["temporal"]
+            prev_cam = cam
 
 
 @pytest.mark.parametrize("storage", [0, 1], ids=["f32", "f16"])
