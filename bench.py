@@ -162,9 +162,10 @@ def frame_at(gen, step):
 
 def workload_config(args, world):
     """The `config` object of both arms' lines."""
-    return {"workload": "full frame 1920x1080, 256^3 world (seed 0), 1 spp + sun shadow + 1 bounce "
+    nb = f"{args.bounces} bounce" + ("s" if args.bounces > 1 else "")
+    return {"workload": f"full frame 1920x1080, 256^3 world (seed 0), 1 spp + sun shadow + {nb} "
                         "(+ bounce shadow), SVGF temporal + variance + 5 a-trous, colour pass",
-            "world": list(WORLD), "resolution": list(RES), "spp": 1, "bounces": 1,
+            "world": list(WORLD), "resolution": list(RES), "spp": 1, "bounces": args.bounces,
             "storage": "fp32" if args.storage == 0 else "fp16",
             "gi_divisor": args.gi_divisor, "reflection_spp": args.reflection_spp,
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
@@ -181,9 +182,11 @@ def run_ours(args):
     from voxelpathtracer_gb300.replicas import Replicas
     dist = Replicas(world)
     W, H = RES
+    if args.bounces > 1:   # two bounces take the per-texel diffuse kernel
+        KERNEL_NAMES["diffuse"] = "k_trace_diffuse"
     vox, blocks, yaw, pitch = workload_inputs(vpt, seed=rank)
     ctx = vpt.Context(width=W, height=H, device=local, storage=args.storage, gi_divisor=args.gi_divisor,
-                      reflection_spp=args.reflection_spp)
+                      reflection_spp=args.reflection_spp, bounces=args.bounces)
     if args.inline_shadow:
         ctx.set_tuning(overlap_shadow=False)
     if args.split_temporal:
@@ -330,7 +333,7 @@ def run_ours(args):
     # the reference's default GI grid (DiffuseTraceResolution 1/4: diffuse rays
     # and SVGF on 480x270, joint-bilateral upscale in the colour pass)
     def run_variant(textures=None, **cfg):
-        vc = vpt.Context(width=W, height=H, device=local, **cfg)
+        vc = vpt.Context(width=W, height=H, device=local, bounces=args.bounces, **cfg)
         vc.upload_world(vox)
         vc.set_block_table(blocks)
         vc.build_df()
@@ -882,12 +885,12 @@ class OracleFrames:
     from frame to frame as libvpt carries it. gen makes the cameras and frame
     constants (oracle.inputs for the reference arm)."""
 
-    def __init__(self, oracle, gen, vox, blocks, yaw, pitch, storage=0, gi_divisor=1, reflection_spp=0):
+    def __init__(self, oracle, gen, vox, blocks, yaw, pitch, storage=0, gi_divisor=1, reflection_spp=0, bounces=1):
         W, H = RES
         self.oracle, self.gen, self.yaw, self.pitch = oracle, gen, yaw, pitch
         from oracle import inputs
         self.cfg = inputs.default_config(width=W, height=H, storage=storage, gi_divisor=gi_divisor,
-                                         reflection_spp=reflection_spp)
+                                         reflection_spp=reflection_spp, bounces=bounces)
         self.world = oracle.World(vox, oracle.build_df(vox), blocks)
         self.prev_g, self.hist = oracle.empty_history(H, W, gi_divisor)
         self.prev_refl = None
@@ -916,7 +919,8 @@ def cpu_baseline(args, vox, blocks, yaw, pitch):
     threads, repeated until args.cpu_seconds of CPU work have accumulated."""
     import oracle
     from oracle import inputs
-    of = OracleFrames(oracle, inputs, vox, blocks, yaw, pitch, args.storage, args.gi_divisor, args.reflection_spp)
+    of = OracleFrames(oracle, inputs, vox, blocks, yaw, pitch, args.storage, args.gi_divisor, args.reflection_spp,
+                      args.bounces)
     t_sum, rays_sum, frames = 0.0, 0, 0
     while t_sum < args.cpu_seconds:
         dt, rays = of.render(frames)
@@ -941,7 +945,8 @@ def run_reference(args):
     vox = inputs.generate_world(X, Y, Z, seed=0)
     blocks = inputs.generate_block_table(100, seed=0)
     yaw, pitch = inputs.seeded_pose(0)
-    of = OracleFrames(oracle, inputs, vox, blocks, yaw, pitch, args.storage, args.gi_divisor, args.reflection_spp)
+    of = OracleFrames(oracle, inputs, vox, blocks, yaw, pitch, args.storage, args.gi_divisor, args.reflection_spp,
+                      args.bounces)
     times, rays = [], []
     for s in range(args.warmup + args.steps):
         dt, n = of.render(s)
@@ -987,6 +992,8 @@ def main():
     ap.add_argument("--storage", type=int, default=0, help="0 = fp32 planes, 1 = fp16 planes")
     ap.add_argument("--gi-divisor", type=int, default=1,
                     help="GI grid = frame / this (the reference's DiffuseTraceResolution is 1/4)")
+    ap.add_argument("--bounces", type=int, default=1, choices=[1, 2],
+                    help="diffuse bounces in the timed frame (2 takes the per-texel diffuse kernel)")
     ap.add_argument("--reflection-spp", type=int, default=0,
                     help="reflection rays per GI texel in the timed frame (0: no reflection pass)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
