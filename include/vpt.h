@@ -422,12 +422,14 @@ vpt_status vpt_get_stream(const vpt_ctx* ctx, void** stream);
 
 /* Deterministic math used by every kernel (exp, exp2, log2, pow, sin, cos as
  * op 0..5), evaluated on the device (on_device = 1) or on the host; lets a
- * caller check that both give identical bits. y is read for pow and ops 6..11.
+ * caller check that both give identical bits. y is read for pow and ops 6..17.
  * Ops 6..14 check the filters' packed fp32 pairs lane by lane: x * y (6, 7:
  * lanes 0 and 1), x + y (8, 9), exp(x) from the packed exponential (10, 11),
  * the weighted sum x + y * x (12) and the bilinear blends of one and two
  * channels (13, 14) of the values (x, 2x, -x, y) at weights (fract(y),
- * fract(2y)), and x / 5 in the variance estimate's three-operation form (15). */
+ * fract(2y)), x / 5 in the variance estimate's three-operation form (15),
+ * and exp(x) from the packed exponential for non-positive arguments (16, 17;
+ * x and y must be <= 0 or NaN). */
 vpt_status vpt_detmath(int32_t op, const float* x, const float* y, float* out, int32_t n, int32_t on_device);
 
 /* -------------------------------------------------------- batched worlds --

@@ -360,6 +360,16 @@ def test_packed_pairs_device_equals_host(vpt, gpu):
     f[::7] = e[::7]   # some pairs with a lane outside the polynomial's range
     for op in (10, 11):
         assert_same(vpt.detmath(op, e, f, on_device=True), vpt.detmath(0, e, on_device=False), f"packed exp op {op}")
+    # the form for non-positive arguments (the filters' negated distances),
+    # down to and beyond the polynomial's range, zeros of both signs and NaN
+    en = -np.abs(e) * np.float32(1.2)
+    fn = -np.abs(f)
+    fn[::7] = en[::7]
+    en[:4] = [0.0, -0.0, np.nan, -1e-40]
+    fn[:4] = [-0.0, np.nan, -3.0, -104.5]
+    for op in (16, 17):
+        assert_same(vpt.detmath(op, en, fn, on_device=True), vpt.detmath(0, en, on_device=False),
+                    f"packed non-positive exp op {op}")
     w = rng.uniform(0, 8, n).astype(np.float32)
     bad = []
     for op, b in ((12, y), (13, w), (14, w), (15, y)):

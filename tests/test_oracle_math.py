@@ -104,7 +104,7 @@ def test_division_by_five_in_three_operations_is_exact(L):
 
 
 def test_libvpt_host_references_of_the_packed_checks(vpt):
-    """The host side of detmath's packed-pair checks (ops 6..15), the values
+    """The host side of detmath's packed-pair checks (ops 6..17), the values
     the device's packed forms are compared with: IEEE products, sums, x + y x,
     the two-row bilinear blend and x / 5, as numpy's float32 gives them."""
     rng = np.random.default_rng(12)
@@ -125,3 +125,8 @@ def test_libvpt_host_references_of_the_packed_checks(vpt):
         for op in (13, 14):
             got = vpt.detmath(op, x, w, on_device=False)
             assert np.array_equal(got.view(np.uint32), want.astype(np.float32).view(np.uint32)), op
+        # ops 16 and 17 (the packed exponential for non-positive arguments): exp(x) itself
+        xn = -np.abs(x)
+        for op in (16, 17):
+            got = vpt.detmath(op, xn, -np.abs(y), on_device=False)
+            assert np.array_equal(got.view(np.uint32), vpt.detmath(0, xn, on_device=False).view(np.uint32)), op

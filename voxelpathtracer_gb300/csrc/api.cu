@@ -1700,7 +1700,7 @@ vpt_status vpt_get_stream(const vpt_ctx* c, void** stream) {
 // frame API): evaluates op over n host inputs on the device, or on the host
 // when on_device is 0.
 vpt_status vpt_detmath(int32_t op, const float* x, const float* y, float* out, int32_t n, int32_t on_device) {
-    if (!x || !out || n < 0 || op < 0 || op > 15 || ((op == 3 || op >= 6) && !y)) return VPT_ERR_INVALID_ARG;
+    if (!x || !out || n < 0 || op < 0 || op > 17 || ((op == 3 || op >= 6) && !y)) return VPT_ERR_INVALID_ARG;
     if (!on_device) {
         for (int k = 0; k < n; k++) {
             float a = x[k], r;
@@ -1713,7 +1713,7 @@ vpt_status vpt_detmath(int32_t op, const float* x, const float* y, float* out, i
                 case 5: r = dcos(a); break;
                 case 6: case 7: r = a * y[k]; break;
                 case 8: case 9: r = a + y[k]; break;
-                case 10: case 11: r = dexp(a); break;
+                case 10: case 11: case 16: case 17: r = dexp(a); break;
                 case 12: r = a + y[k] * a; break;
                 case 15: r = a / 5.0f; break;
                 default: {

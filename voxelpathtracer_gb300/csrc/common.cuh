@@ -233,6 +233,32 @@ __device__ __forceinline__ float2 dexp_pair(float a, float b) {
     return make_float2(scale2(q.x, k0), scale2(q.y, k1));
 }
 
+// dexp_pair for arguments that are never positive (the filters' negated
+// distances and differences; the caller guarantees a <= 0 and b <= 0 unless
+// NaN): the same operations, without the range tests a positive argument
+// needs (kf = floor(x log2(e) + 1/2) <= 0 here, so k <= 127 always). NaN and
+// arguments below the polynomial's range take the scalar function.
+__device__ __forceinline__ float2 dexp_pair_np(float a, float b) {
+    const float lo = -103.97208404541016f;
+    if (!(a >= lo && b >= lo)) return make_float2(dexp(a), dexp(b));
+    const float2 x = make_float2(a, b);
+    const float2 t = sadd(pmul(x, splat(1.44269502162933350f)), splat(0.5f));
+    const float2 kf = make_float2(floorf(t.x), floorf(t.y));
+    const float2 r = sadd(sadd(x, pmul(kf, splat(-0.693145751953125f))), pmul(kf, splat(-1.428606765330187e-06f)));
+    float2 q = splat(1.0f / 40320.0f);
+    q = __ffma2_rn(q, r, splat(1.0f / 5040.0f));
+    q = __ffma2_rn(q, r, splat(1.0f / 720.0f));
+    q = __ffma2_rn(q, r, splat(1.0f / 120.0f));
+    q = __ffma2_rn(q, r, splat(1.0f / 24.0f));
+    q = __ffma2_rn(q, r, splat(1.0f / 6.0f));
+    q = __ffma2_rn(q, r, splat(0.5f));
+    q = __ffma2_rn(q, r, splat(1.0f));
+    q = __ffma2_rn(q, r, splat(1.0f));
+    const int k0 = (int)kf.x, k1 = (int)kf.y;
+    if (k0 >= -125 && k1 >= -125) return pmul(q, make_float2(pow2i(k0), pow2i(k1)));
+    return make_float2(scale2(q.x, k0), scale2(q.y, k1));
+}
+
 // x / 5 for finite x in three operations: q = x * RN(1/5), then one
 // correction with the exact remainder, q + fma(-q, 5, x) * RN(1/5)
 // (P. Markstein, IBM J. Res. Dev. 34(1), 1990). For the divisor 5 this is

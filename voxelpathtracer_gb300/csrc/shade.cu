@@ -401,6 +401,8 @@ __global__ void k_detmath(int op, const float* x, const float* y, float* out, in
         case 11: r = dexp_pair(y[k], a).y; break;
         case 12: r = pacc(make_float2(y[k], a), make_float2(a, y[k]), a).y; break;   // a + y * a
         case 15: r = div5(a); break;
+        case 16: r = dexp_pair_np(a, y[k]).x; break;
+        case 17: r = dexp_pair_np(y[k], a).y; break;
         default: {   // bilinear blend of (a, 2a, -a, y) at weights (frac(y), frac(2y))
             Bilin b;
             b.ax = y[k] - floorf(y[k]);

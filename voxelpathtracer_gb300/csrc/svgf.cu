@@ -515,7 +515,7 @@ __device__ __forceinline__ void variance_texel(int W, int H, int i, int j, const
                 const int fc = face_cos(bf, sf);
                 const float nw = fc == 0 ? 0.0f : (fc == 1 ? 1.0f : nw3);
                 const float lw = div5(fabsf(sl - bl));   // / phi, phi = 5
-                const float2 e = dexp_pair(-fabsf(sd - bd), -lw);
+                const float2 e = dexp_pair_np(-fabsf(sd - bd), -lw);
                 const float dw = e.x * e.x;   // pow(e, 2) for e in [0, 1]
                 float wgt = (e.y * nw) * dw;
                 float wgt2 = wgt;
@@ -834,7 +834,7 @@ __device__ __forceinline__ void atrous_texels(int W, int H, const AtrousArgs& a,
                     if (q.strong) {
                         de = dexp(dn);
                     } else {
-                        const float2 e = dexp_pair(dn, -(fabsf(sl - q.bl) / q.phi));
+                        const float2 e = dexp_pair_np(dn, -(fabsf(sl - q.bl) / q.phi));   // both <= 0
                         de = e.x;
                         le = e.y;
                     }
