@@ -253,6 +253,32 @@ def test_render_frame_matches_oracle(vpt, oracle, scene, mode, gpu):
     ctx.close()
 
 
+@pytest.mark.parametrize("iterations", [0, 1, 2, 3, 5])
+def test_atrous_iteration_counts(vpt, oracle, scene, iterations, gpu):
+    """Whole frames with 0 to 5 a-trous iterations (each count ends on a
+    different step and ping-pong buffer): the final planes and the colour
+    equal the oracle's."""
+    world = scene["world"]
+    with vpt.Context(width=W, height=H, primary_max_steps=256, atrous_iterations=iterations) as ctx:
+        ctx.upload_world(scene["vox"])
+        ctx.set_block_table(scene["blocks"])
+        ctx.build_df()
+        prev_g, hist = oracle.empty_history(H, W)
+        prev_cam = scene["cams"][0]
+        for fi, cam in enumerate(scene["cams"]):
+            frame = vpt.default_frame(frame_index=fi, seed=7, time=0.25 * fi)
+            rgb = ctx.render_frame(cam, frame)
+            ref = oracle.render_frame(world, cam, prev_cam, ctx.config, frame, prev_g, hist)
+            if iterations:
+                last = ref["svgf"]["atrous"][-1]
+                for k in ("sh", "cocg", "variance", "aosky"):
+                    assert_same(ctx.read_plane("DEN_" + k.upper()), last[k], f"frame {fi} a-trous {k}")
+            assert_same(rgb, ref["rgb"], f"frame {fi} colour")
+            prev_g = {k: ref["g"][k] for k in ("t", "face", "block")}
+            hist = ref["svgf"]["temporal"]
+            prev_cam = cam
+
+
 def test_render_frame_ragged_size(vpt, oracle, scene, gpu):
     """Whole frames at 101 x 67 with the default tuning (sun shadow on the
     second stream, staged diffuse trace, tiled filter steps)."""
