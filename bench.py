@@ -129,7 +129,96 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi, 200 ms period"}
+
+
+class NvmlClockSampler:
+    """SM clock and clock-event reasons read through NVML (read-only queries)
+    every millisecond on a background thread, so a timed region of a few tens
+    of milliseconds still gets many samples. The GPU is found by its PCI
+    address when torch reports it. start() returns False where NVML cannot be
+    loaded or the device not found; the caller then takes ClockSampler."""
+
+    # nvmlClocksEventReasons bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, torch, index: int):
+        import ctypes
+        self.C = ctypes
+        self.index = index
+        self.torch = torch
+        self.lib = None
+        self.handle = None
+        self.samples = []
+        self.stop_flag = threading.Event()
+        self.thread = None
+
+    def start(self) -> bool:
+        C = self.C
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return False
+            h = C.c_void_p()
+            props = self.torch.cuda.get_device_properties(self.index)
+            bus = getattr(props, "pci_bus_id", None)
+            ok = False
+            if bus is not None:
+                addr = (f"{getattr(props, 'pci_domain_id', 0):08x}:{bus:02x}:"
+                        f"{getattr(props, 'pci_device_id', 0):02x}.0").encode()
+                ok = lib.nvmlDeviceGetHandleByPciBusId_v2(C.c_char_p(addr), C.byref(h)) == 0
+            if not ok:
+                n = C.c_uint()
+                if lib.nvmlDeviceGetCount_v2(C.byref(n)) != 0 or n.value != 1:
+                    lib.nvmlShutdown()
+                    return False   # several GPUs and no PCI address to tell them apart
+                ok = lib.nvmlDeviceGetHandleByIndex_v2(0, C.byref(h)) == 0
+            if not ok:
+                lib.nvmlShutdown()
+                return False
+            self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        except (OSError, AttributeError):
+            return False
+        self.lib, self.handle = lib, h
+        mx = C.c_uint()
+        self.max_mhz = float(mx.value) if lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0 else None
+        self.thread = threading.Thread(target=self._poll, daemon=True)
+        self.thread.start()
+        return True
+
+    def _poll(self):
+        C = self.C
+        mhz, reasons = C.c_uint(), C.c_ulonglong()
+        while not self.stop_flag.is_set():
+            if self.lib.nvmlDeviceGetClockInfo(self.handle, 1, C.byref(mhz)) == 0 and \
+                    self.reasons_fn(self.handle, C.byref(reasons)) == 0:
+                self.samples.append((float(mhz.value), int(reasons.value)))
+            time.sleep(0.001)
+
+    def stop(self):
+        self.stop_flag.set()
+        if self.thread is not None:
+            self.thread.join(timeout=5)
+        if self.lib is not None:
+            self.lib.nvmlShutdown()
+        sm = [m for m, _ in self.samples]
+        bits = 0
+        for _, r in self.samples:
+            bits |= r
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(n for b, n in self.REASONS.items() if bits & b), "samples": len(sm),
+                "source": "NVML, 1 ms period, during the timed frames"}
+
+
+def start_clock_sampler(torch, local):
+    """NVML sampler where NVML answers, else the nvidia-smi one."""
+    s = NvmlClockSampler(torch, local)
+    if s.start():
+        return s
+    s = ClockSampler(local)
+    s.start()
+    return s
 
 
 def peak_hbm():
@@ -218,8 +307,7 @@ def run_ours(args):
             ctx.render_frame(camera_at(vpt, yaw, pitch, s), frame_at(vpt, s), readback=False)
         torch.cuda.synchronize()
         dist.barrier()
-        clocks = ClockSampler(local)
-        clocks.start()
+        clocks = start_clock_sampler(torch, local)
         launches0 = ctx.launch_count()
         for s in range(args.warmup, total):
             flush.zero_()
