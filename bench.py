@@ -159,6 +159,9 @@ class NvmlClockSampler:
             lib = C.CDLL("libnvidia-ml.so.1")
             if lib.nvmlInit_v2() != 0:
                 return False
+        except (OSError, AttributeError):
+            return False
+        try:
             h = C.c_void_p()
             props = self.torch.cuda.get_device_properties(self.index)
             bus = getattr(props, "pci_bus_id", None)
@@ -178,7 +181,8 @@ class NvmlClockSampler:
                 return False
             self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
                 getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
-        except (OSError, AttributeError):
+        except (OSError, AttributeError, RuntimeError):
+            lib.nvmlShutdown()
             return False
         self.lib, self.handle = lib, h
         mx = C.c_uint()
