@@ -1,8 +1,9 @@
 """Builds the parts of the reference that compile standalone into oracle/_ref/:
 libenkimi_ref.so, the reference's own Minecraft region / NBT reader (enkiMI
 and miniz, compiled from the sources where they lie in the reference tree)
-with the driver oracle/enkimi_ref.c, and libglm_ref.so, the reference's
-vendored glm (header-only) behind oracle/glm_ref.cpp. TEST INFRASTRUCTURE; a
+with the driver oracle/enkimi_ref.c, libglm_ref.so, the reference's
+vendored glm (header-only) behind oracle/glm_ref.cpp, and libglsl_ref.so, the
+reference's own shaders compiled as C++ (oracle/build_glsl_ref.py). TEST INFRASTRUCTURE; a
 no-op when the reference tree is absent (the tests that need the libraries
 skip then).
 
@@ -55,6 +56,12 @@ def build_glm(verbose: bool = False) -> Path | None:
 
 def build(verbose: bool = False) -> Path | None:
     build_glm(verbose)
+    # the reference's shaders compiled as C++ (oracle/build_glsl_ref.py)
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("vpt_build_glsl_ref", HERE / "build_glsl_ref.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.build(verbose)
     sources = [ENKI / "enkimi.c", ENKI / "miniz.c", HERE / "enkimi_ref.c"]
     if not all(p.exists() for p in sources[:2]):
         return None

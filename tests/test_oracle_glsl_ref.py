@@ -1,0 +1,93 @@
+"""The oracle against the reference's own shader code, compiled as C++.
+
+oracle/build_glsl_ref.py takes ManhattanDistance{X,Y,Z}.comp and
+InitialRayTraceFrag.glsl from the reference tree, rewrites only GLSL syntax
+(qualifiers, swizzles, literals, interface variables) and compiles them with
+GLSL's types and built-ins from oracle/glsl_compat.h into
+oracle/_ref/libglsl_ref.so; oracle/glsl_ref.cpp runs them as the
+reference's dispatches and draws do. Where they and the oracle take the same
+inputs, every output must be bit-identical: the distance field of every
+world, and the primary G-buffer (hit distance, face id, block id) of every
+texel. That pins the oracle's restatement of those passes to the reference's
+own code; the built-ins (normalize, texel fetch of R8 data, matrix times
+vector) are the conventions the oracle fixes for them. Skipped where the
+reference tree is absent (the GPU machines).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import build_glsl_ref, inputs
+
+
+@pytest.fixture(scope="module")
+def ref():
+    if build_glsl_ref.build() is None or not build_glsl_ref.OUT.exists():
+        pytest.skip("the reference tree (its shaders) is not present")
+    L = C.CDLL(str(build_glsl_ref.OUT))
+    P = C.c_void_p
+    L.glslref_build_df.argtypes = [P, C.c_int, C.c_int, C.c_int, P]
+    L.glslref_trace_primary.argtypes = [P, P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_int, C.c_int,
+                                        C.c_float, P, P, P]
+    return L
+
+
+def ref_df(L, vox):
+    vox = np.ascontiguousarray(vox, np.uint8)
+    Z, Y, X = vox.shape
+    out = np.zeros_like(vox)
+    L.glslref_build_df(vox.ctypes.data, X, Y, Z, out.ctypes.data)
+    return out
+
+
+def ref_primary(L, vox, df, cam, W, H, steps):
+    Z, Y, X = vox.shape
+    iv = np.ascontiguousarray(np.asarray(cam.inv_view, np.float32))
+    ip = np.ascontiguousarray(np.asarray(cam.inv_proj, np.float32))
+    t, n, b = (np.zeros((H, W), np.float32) for _ in range(3))
+    L.glslref_trace_primary(vox.ctypes.data, df.ctypes.data, X, Y, Z, iv.ctypes.data, ip.ctypes.data, W, H, steps,
+                            90.0, t.ctypes.data, n.ctypes.data, b.ctypes.data)
+    return t, n, b
+
+
+@pytest.mark.parametrize("dims", [(32, 32, 32), (64, 32, 96), (33, 17, 5), (1, 1, 1), (200, 3, 7)])
+@pytest.mark.parametrize("fill", [0.0, 0.02, 0.3, 1.0])
+def test_distance_field_equals_the_reference_shaders(ref, dims, fill):
+    X, Y, Z = dims
+    rng = np.random.default_rng(X * 131 + Y * 7 + Z + int(fill * 100))
+    vox = ((rng.random((Z, Y, X)) < fill) * rng.integers(1, 128, (Z, Y, X))).astype(np.uint8)
+    assert np.array_equal(ref_df(ref, vox), oracle.build_df(vox))
+
+
+def test_distance_field_of_generated_worlds(ref):
+    for seed, dims in ((0, (128, 64, 96)), (3, (64, 64, 64))):
+        vox = inputs.generate_world(*dims, seed=seed)
+        assert np.array_equal(ref_df(ref, vox), oracle.build_df(vox)), seed
+
+
+@pytest.mark.parametrize("case", [
+    # (world dims, seed, camera position, yaw / pitch offsets, W, H, step cap, rays that hit)
+    ((64, 64, 64), 1, (32.0, 58.0, 32.0), (0.0, 0.0), 96, 64, 256, True),
+    ((64, 64, 64), 1, (32.7, 58.2, 31.6), (2.0, 1.0), 80, 48, 256, True),
+    ((128, 64, 96), 5, (40.5, 60.0, 50.25), (-35.0, -20.0), 72, 40, 350, True),
+    ((64, 64, 64), 2, (10.5, 5.5, 10.5), (30.0, 10.0), 48, 32, 256, False),   # camera inside the terrain
+    ((64, 64, 64), 1, (32.0, 58.0, 32.0), (0.0, 0.0), 64, 40, 3, False),      # step cap before any hit
+])
+def test_primary_gbuffer_equals_the_reference_shader(ref, case):
+    dims, seed, pos, (dyaw, dpitch), W, H, steps, hits = case
+    X, Y, Z = dims
+    vox = inputs.generate_world(X, Y, Z, seed=seed)
+    blocks = inputs.generate_block_table(100, seed=seed)
+    df = oracle.build_df(vox)
+    yaw, pitch = inputs.seeded_pose(seed)
+    cam = inputs.camera_from_pose(pos, yaw + dyaw, pitch + dpitch, 90.0, W / H)
+    cfg = inputs.default_config(width=W, height=H, primary_max_steps=steps)
+    g = oracle.trace_primary(oracle.World(vox, df, blocks), cam, cfg)
+    t, n, b = ref_primary(ref, vox, df, cam, W, H, steps)
+    assert np.array_equal(t.view(np.uint32), g["t"].view(np.uint32)) or np.array_equal(t, g["t"])
+    # o_Normal holds the face id / 10 (1.0 for a miss, the oracle's 10), o_BlockID the R8 block id / 255
+    assert np.array_equal(np.rint(n * np.float32(10)).astype(np.int32), g["face"].astype(np.int32))
+    assert np.array_equal(np.rint(b * np.float32(255)).astype(np.int32), g["block"].astype(np.int32))
+    assert (t > 0).any() == hits
