@@ -45,6 +45,7 @@ UNITS = [
     ("df_y", "ManhattanDistanceY.comp", "main", ()),
     ("df_z", "ManhattanDistanceZ.comp", "main", ()),
     ("primary", "InitialRayTraceFrag.glsl", "main", ("VoxelTraversalDF_AlphaTest",)),
+    ("shadow", "ShadowRayTraceFrag.glsl", "main", ("VoxelTraversalDF_AlphaTest",)),
 ]
 WORLD_DEFINES = ("WORLD_SIZE_X", "WORLD_SIZE_Y", "WORLD_SIZE_Z")
 KEYWORDS = {"if", "else", "for", "while", "return", "const", "void", "float", "int", "bool", "true", "false",
@@ -143,8 +144,8 @@ def rewrite_array_ctors(text: str) -> str:
 
 def rewrite_expr(text: str) -> str:
     text = rewrite_array_ctors(text)
-    swz = {"xyz": "xyz", "rgb": "xyz", "xy": "xy", "rg": "xy"}
-    text = re.sub(r"\.(xyz|rgb|xy|rg)\b(?!\s*\()", lambda m: f".{swz[m.group(1)]}()", text)
+    swz = {"xyzw": "xyzw", "rgba": "xyzw", "xyz": "xyz", "rgb": "xyz", "xy": "xy", "rg": "xy"}
+    text = re.sub(r"\.(xyzw|rgba|xyz|rgb|xy|rg)\b(?!\s*\()", lambda m: f".{swz[m.group(1)]}()", text)
     comp = {"r": "x", "g": "y", "b": "z", "a": "w"}
     text = re.sub(r"(?<=[\w\)\]])\.([rgba])\b(?!\s*\()", lambda m: "." + comp[m.group(1)], text)
     text = re.sub(r"(?<![\w.])(\d+\.\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])",
@@ -193,7 +194,7 @@ def translate(ns: str, path: Path, entry: str, stubs) -> str:
                 if ident in by_name:
                     work.append(ident)
     out = [f"namespace {ns} {{", "int WORLD_SIZE_X = 0, WORLD_SIZE_Y = 0, WORLD_SIZE_Z = 0;",
-           "uvec3 gl_GlobalInvocationID;"]
+           "uvec3 gl_GlobalInvocationID;", "vec4 gl_FragCoord;"]
     for k, item in enumerate(items):
         kind, names = cls[k]
         if kind == "pp":
@@ -223,7 +224,8 @@ def build(verbose: bool = False) -> Path | None:
         gen.append(translate(ns, SHADERS / f, entry, set(stubs)))
     GEN.write_text("\n".join(gen))
     tmp = OUT.with_suffix(".so.tmp")
-    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
+    # -fwrapv: GLSL's integer arithmetic wraps (the shaders' hash seeds overflow)
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fwrapv", "-fPIC",
            "-shared", "-w", f"-I{HERE}", f"-I{GEN.parent}", str(HERE / "glsl_ref.cpp"), "-o", str(tmp)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

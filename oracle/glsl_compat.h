@@ -63,6 +63,7 @@ struct vec4 {
     float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
     vec2 xy() const { return vec2(x, y); }
     vec3 xyz() const { return vec3(x, y, z); }
+    vec4 xyzw() const { return *this; }
 };
 
 inline vec2::vec2(const vec3& v) : x(v.x), y(v.y) {}
@@ -87,6 +88,29 @@ struct ivec3 {
     ivec3 xyz() const { return *this; }
 };
 
+
+struct ivec2 {
+    int x = 0, y = 0;
+    ivec2() = default;
+    ivec2(int a, int b) : x(a), y(b) {}
+    explicit ivec2(const vec2& v) : x((int)v.x), y((int)v.y) {}
+    int& operator[](int i) { return i == 0 ? x : y; }
+    int operator[](int i) const { return i == 0 ? x : y; }
+    operator vec2() const { return vec2((float)x, (float)y); }   // GLSL's implicit int -> float
+};
+inline ivec2 operator+(const ivec2& a, const ivec2& b) { return ivec2(a.x + b.x, a.y + b.y); }
+inline ivec2 operator%(const ivec2& a, const ivec2& b) { return ivec2(a.x % b.x, a.y % b.y); }
+
+// mat3: three columns, m * v summed column by column
+struct mat3 {
+    vec3 c[3];
+    mat3(const vec3& a, const vec3& b, const vec3& d) : c{a, b, d} {}
+};
+inline vec3 operator*(const mat3& m, const vec3& v) {
+    vec3 r;
+    for (int i = 0; i < 3; i++) r[i] = (m.c[0][i] * v.x + m.c[1][i] * v.y) + m.c[2][i] * v.z;
+    return r;
+}
 
 // mat4: four columns; m[c] is column c, m * v sums the columns left to right
 struct mat4 {
@@ -169,6 +193,8 @@ inline float mix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
 
 // ---- vector built-ins ----
 inline vec3 floor(const vec3& v) { return vec3(floor(v.x), floor(v.y), floor(v.z)); }
+inline vec2 floor(const vec2& v) { return vec2(floor(v.x), floor(v.y)); }
+inline float round(float x) { return std::nearbyint(x); }
 inline vec3 sign(const vec3& v) { return vec3(sign(v.x), sign(v.y), sign(v.z)); }
 inline vec3 abs(const vec3& v) { return vec3(abs(v.x), abs(v.y), abs(v.z)); }
 inline vec2 fract(const vec2& v) { return vec2(fract(v.x), fract(v.y)); }
@@ -193,6 +219,38 @@ inline vec4 texelFetch(const sampler3D& s, const ivec3& p, int lod) {
     const uint8_t v = s.data[((size_t)p.z * s.Y + p.y) * s.X + p.x];
     return vec4((float)v / 255.0f, 0.0f, 0.0f, 1.0f);
 }
+// One-channel float 2-D texture (a G-buffer plane), rows from the bottom.
+// texture() follows the oracle's sampling convention: at a texel centre (the
+// texel-space coordinate within 2^-9 of an integer, what the hardware's
+// fixed-point addressing snaps) it returns that texel, elsewhere it blends
+// the four texels with fp32 weights, REPEAT wrap.
+struct sampler2D {
+    const float* data = nullptr;
+    int W = 0, H = 0;
+};
+inline float texel2d(const sampler2D& s, int i, int j) {
+    i %= s.W; if (i < 0) i += s.W;
+    j %= s.H; if (j < 0) j += s.H;
+    return s.data[(size_t)j * s.W + i];
+}
+inline vec4 texture(const sampler2D& s, const vec2& uv) {
+    const float x = uv.x * (float)s.W - 0.5f, y = uv.y * (float)s.H - 0.5f;
+    const float rx = std::nearbyint(x), ry = std::nearbyint(y);
+    if (std::fabs(x - rx) < 0.001953125f && std::fabs(y - ry) < 0.001953125f)
+        return vec4(texel2d(s, (int)rx, (int)ry), 0.0f, 0.0f, 1.0f);
+    const float x0 = std::floor(x), y0 = std::floor(y), ax = x - x0, ay = y - y0;
+    const int i0 = (int)x0, j0 = (int)y0;
+    const float lo = texel2d(s, i0, j0) * (1.0f - ax) + texel2d(s, i0 + 1, j0) * ax;
+    const float hi = texel2d(s, i0, j0 + 1) * (1.0f - ax) + texel2d(s, i0 + 1, j0 + 1) * ax;
+    return vec4(lo * (1.0f - ay) + hi * ay, 0.0f, 0.0f, 1.0f);
+}
+inline vec4 texelFetch(const sampler2D& s, const ivec2& p, int lod) {
+    (void)lod;
+    if (p.x < 0 || p.y < 0 || p.x >= s.W || p.y >= s.H) std::abort();
+    return vec4(s.data[(size_t)p.y * s.W + p.x], 0.0f, 0.0f, 1.0f);
+}
+inline ivec2 textureSize(const sampler2D& s, int lod) { (void)lod; return ivec2(s.W, s.H); }
+
 struct image3D {
     uint8_t* data = nullptr;
     int X = 0, Y = 0, Z = 0;

@@ -85,4 +85,41 @@ void glslref_trace_primary(const uint8_t* vox, const uint8_t* df, int X, int Y, 
         }
 }
 
+// The sun-shadow trace (Core/Pipeline.cpp:2796-2830, ShadowRayTraceFrag.glsl
+// main) over a W x H target at full resolution (no Halton offset), hard
+// shadows (no contact-hardening cone), no alpha test. hit_t: the G-buffer's
+// hit distance plane (u_PositionTexture); normal: its face plane as the
+// initial trace writes it (u_NormalTexture, face id / 10). v_RayOrigin is the
+// camera position the vertex stage passes, gl_FragCoord the texel centre.
+// Out: o_Shadow per texel.
+void glslref_trace_shadow(const uint8_t* vox, const uint8_t* df, int X, int Y, int Z, const float* inv_view,
+                          const float* inv_proj, int W, int H, const float* hit_t, const float* normal,
+                          const float* light_dir, float* o_shadow) {
+    static const float no_noise[1] = {0.0f};
+    shadow::WORLD_SIZE_X = X; shadow::WORLD_SIZE_Y = Y; shadow::WORLD_SIZE_Z = Z;
+    shadow::u_VoxelData = sampler3D{vox, X, Y, Z};
+    shadow::u_DistanceFieldTexture = sampler3D{df, X, Y, Z};
+    shadow::u_PositionTexture = sampler2D{hit_t, W, H};
+    shadow::u_NormalTexture = sampler2D{normal, W, H};
+    shadow::u_BlueNoiseTexture = sampler2D{no_noise, 1, 1};
+    shadow::u_InverseView = mat_from(inv_view);
+    shadow::u_InverseProjection = mat_from(inv_proj);
+    shadow::u_Dimensions = vec2((float)W, (float)H);
+    shadow::u_Halton = vec2(0.0f, 0.0f);
+    shadow::u_LightDirection = vec3(light_dir[0], light_dir[1], light_dir[2]);
+    shadow::u_ContactHardeningShadows = false;
+    shadow::u_ShouldAlphaTest = false;
+    shadow::u_FOV = 90.0f;
+    shadow::u_Time = 0.0f;
+    shadow::u_CurrentFrame = 0;
+    shadow::v_RayOrigin = vec3(inv_view[12], inv_view[13], inv_view[14]);
+    for (int j = 0; j < H; j++)
+        for (int i = 0; i < W; i++) {
+            shadow::v_TexCoords = vec2(((float)i + 0.5f) / (float)W, ((float)j + 0.5f) / (float)H);
+            shadow::gl_FragCoord = vec4((float)i + 0.5f, (float)j + 0.5f, 0.0f, 1.0f);
+            shadow::main();
+            o_shadow[(size_t)j * W + i] = shadow::o_Shadow;
+        }
+}
+
 }  // extern "C"

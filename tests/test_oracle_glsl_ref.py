@@ -1,14 +1,14 @@
 """The oracle against the reference's own shader code, compiled as C++.
 
-oracle/build_glsl_ref.py takes ManhattanDistance{X,Y,Z}.comp and
-InitialRayTraceFrag.glsl from the reference tree, rewrites only GLSL syntax
+oracle/build_glsl_ref.py takes ManhattanDistance{X,Y,Z}.comp,
+InitialRayTraceFrag.glsl and ShadowRayTraceFrag.glsl from the reference tree, rewrites only GLSL syntax
 (qualifiers, swizzles, literals, interface variables) and compiles them with
 GLSL's types and built-ins from oracle/glsl_compat.h into
 oracle/_ref/libglsl_ref.so; oracle/glsl_ref.cpp runs them as the
 reference's dispatches and draws do. Where they and the oracle take the same
 inputs, every output must be bit-identical: the distance field of every
-world, and the primary G-buffer (hit distance, face id, block id) of every
-texel. That pins the oracle's restatement of those passes to the reference's
+world, the primary G-buffer (hit distance, face id, block id) and the sun
+shadow of every texel. That pins the oracle's restatement of those passes to the reference's
 own code; the built-ins (normalize, texel fetch of R8 data, matrix times
 vector) are the conventions the oracle fixes for them. Skipped where the
 reference tree is absent (the GPU machines).
@@ -31,6 +31,7 @@ def ref():
     L.glslref_build_df.argtypes = [P, C.c_int, C.c_int, C.c_int, P]
     L.glslref_trace_primary.argtypes = [P, P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_int, C.c_int,
                                         C.c_float, P, P, P]
+    L.glslref_trace_shadow.argtypes = [P, P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P]
     return L
 
 
@@ -91,3 +92,34 @@ def test_primary_gbuffer_equals_the_reference_shader(ref, case):
     assert np.array_equal(np.rint(n * np.float32(10)).astype(np.int32), g["face"].astype(np.int32))
     assert np.array_equal(np.rint(b * np.float32(255)).astype(np.int32), g["block"].astype(np.int32))
     assert (t > 0).any() == hits
+
+
+@pytest.mark.parametrize("sun", [(0.3, 0.8, 0.5), (0.9, 0.15, 0.3), (-0.5, 0.6, -0.6), (0.05, 0.99, -0.1)])
+@pytest.mark.parametrize("seed", [1, 5])
+def test_sun_shadow_equals_the_reference_shader(ref, sun, seed):
+    """The reference's shadow pass reads the G-buffer its initial trace wrote
+    (here the reference's own, equal to the oracle's by the test above)."""
+    X, Y, Z = 64, 64, 64
+    W, H = 80, 48
+    vox = inputs.generate_world(X, Y, Z, seed=seed)
+    blocks = inputs.generate_block_table(100, seed=seed)
+    df = oracle.build_df(vox)
+    yaw, pitch = inputs.seeded_pose(seed)
+    cam = inputs.camera_from_pose((X / 2 + 0.3, 58.0, Z / 2 - 0.2), yaw, pitch, 90.0, W / H)
+    cfg = inputs.default_config(width=W, height=H, primary_max_steps=256)
+    frame = inputs.default_frame(frame_index=0, seed=3)
+    s = np.asarray(sun, np.float64)
+    frame.sun_dir[:] = [float(v) for v in (s / np.linalg.norm(s)).astype(np.float32)]
+    world = oracle.World(vox, df, blocks)
+    g = oracle.trace_primary(world, cam, cfg)
+    t, n, _ = ref_primary(ref, vox, df, cam, W, H, 256)
+    iv = np.ascontiguousarray(np.asarray(cam.inv_view, np.float32))
+    ip = np.ascontiguousarray(np.asarray(cam.inv_proj, np.float32))
+    light = np.ascontiguousarray(np.asarray(frame.sun_dir, np.float32))
+    out = np.zeros((H, W), np.float32)
+    ref.glslref_trace_shadow(vox.ctypes.data, df.ctypes.data, X, Y, Z, iv.ctypes.data, ip.ctypes.data, W, H,
+                             t.ctypes.data, n.ctypes.data, light.ctypes.data, out.ctypes.data)
+    want = oracle.trace_shadow(world, cam, cfg, frame, g["t"], g["face"])
+    assert set(np.unique(out).tolist()) <= {0.0, 1.0}
+    assert np.array_equal(out.astype(np.uint8), want)
+    assert (want[g["t"] > 0] == 1).any()
