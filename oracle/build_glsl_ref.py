@@ -46,6 +46,8 @@ UNITS = [
     ("df_z", "ManhattanDistanceZ.comp", "main", ()),
     ("primary", "InitialRayTraceFrag.glsl", "main", ("VoxelTraversalDF_AlphaTest",)),
     ("shadow", "ShadowRayTraceFrag.glsl", "main", ("VoxelTraversalDF_AlphaTest",)),
+    ("pre3x3", "Spatial3x3Initial.glsl", "main", ()),
+    ("variance", "SVGF/VarianceEstimate.glsl", "main", ()),
 ]
 WORLD_DEFINES = ("WORLD_SIZE_X", "WORLD_SIZE_Y", "WORLD_SIZE_Z")
 KEYWORDS = {"if", "else", "for", "while", "return", "const", "void", "float", "int", "bool", "true", "false",

@@ -94,6 +94,7 @@ struct ivec2 {
     ivec2() = default;
     ivec2(int a, int b) : x(a), y(b) {}
     explicit ivec2(const vec2& v) : x((int)v.x), y((int)v.y) {}
+    explicit ivec2(float f) : x((int)f), y((int)f) {}
     int& operator[](int i) { return i == 0 ? x : y; }
     int operator[](int i) const { return i == 0 ? x : y; }
     operator vec2() const { return vec2((float)x, (float)y); }   // GLSL's implicit int -> float
@@ -190,6 +191,7 @@ inline float cos(float x) { return vpto::dm_cos(x); }
 inline float tan(float x) { return vpto::dm_sin(x) / vpto::dm_cos(x); }
 inline float radians(float d) { return d * 0.01745329251994329577f; }
 inline float mix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+inline float mod(float x, float y) { return x - y * floor(x / y); }
 
 // ---- vector built-ins ----
 inline vec3 floor(const vec3& v) { return vec3(floor(v.x), floor(v.y), floor(v.z)); }
@@ -198,6 +200,10 @@ inline float round(float x) { return std::nearbyint(x); }
 inline vec3 sign(const vec3& v) { return vec3(sign(v.x), sign(v.y), sign(v.z)); }
 inline vec3 abs(const vec3& v) { return vec3(abs(v.x), abs(v.y), abs(v.z)); }
 inline vec2 fract(const vec2& v) { return vec2(fract(v.x), fract(v.y)); }
+inline vec2 clamp(const vec2& v, float lo, float hi) { return vec2(clamp(v.x, lo, hi), clamp(v.y, lo, hi)); }
+inline vec4 clamp(const vec4& v, float lo, float hi) {
+    return vec4(clamp(v.x, lo, hi), clamp(v.y, lo, hi), clamp(v.z, lo, hi), clamp(v.w, lo, hi));
+}
 inline vec2 sin(const vec2& v) { return vec2(sin(v.x), sin(v.y)); }
 inline float dot(const vec2& a, const vec2& b) { return a.x * b.x + a.y * b.y; }
 inline float dot(const vec3& a, const vec3& b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
@@ -219,35 +225,45 @@ inline vec4 texelFetch(const sampler3D& s, const ivec3& p, int lod) {
     const uint8_t v = s.data[((size_t)p.z * s.Y + p.y) * s.X + p.x];
     return vec4((float)v / 255.0f, 0.0f, 0.0f, 1.0f);
 }
-// One-channel float 2-D texture (a G-buffer plane), rows from the bottom.
-// texture() follows the oracle's sampling convention: at a texel centre (the
-// texel-space coordinate within 2^-9 of an integer, what the hardware's
-// fixed-point addressing snaps) it returns that texel, elsewhere it blends
-// the four texels with fp32 weights, REPEAT wrap.
+// Float 2-D texture of C interleaved channels (a G-buffer or filter plane),
+// rows from the bottom; a fetch fills (r, g, b, a) from the C channels and
+// (0, 0, 0, 1) after them. texture() follows the oracle's sampling
+// convention: at a texel centre (the texel-space coordinate within 2^-9 of an
+// integer, what the hardware's fixed-point addressing snaps) it returns that
+// texel, elsewhere it blends the four texels with fp32 weights, REPEAT wrap.
 struct sampler2D {
     const float* data = nullptr;
-    int W = 0, H = 0;
+    int W = 0, H = 0, C = 1;
 };
-inline float texel2d(const sampler2D& s, int i, int j) {
+inline float texel2d(const sampler2D& s, int i, int j, int c) {
     i %= s.W; if (i < 0) i += s.W;
     j %= s.H; if (j < 0) j += s.H;
-    return s.data[(size_t)j * s.W + i];
+    return s.data[((size_t)j * s.W + i) * s.C + c];
+}
+inline vec4 texel_vec(const sampler2D& s, int i, int j) {
+    vec4 r(0.0f, 0.0f, 0.0f, 1.0f);
+    for (int c = 0; c < s.C && c < 4; c++) r[c] = texel2d(s, i, j, c);
+    return r;
 }
 inline vec4 texture(const sampler2D& s, const vec2& uv) {
     const float x = uv.x * (float)s.W - 0.5f, y = uv.y * (float)s.H - 0.5f;
     const float rx = std::nearbyint(x), ry = std::nearbyint(y);
     if (std::fabs(x - rx) < 0.001953125f && std::fabs(y - ry) < 0.001953125f)
-        return vec4(texel2d(s, (int)rx, (int)ry), 0.0f, 0.0f, 1.0f);
+        return texel_vec(s, (int)rx, (int)ry);
     const float x0 = std::floor(x), y0 = std::floor(y), ax = x - x0, ay = y - y0;
     const int i0 = (int)x0, j0 = (int)y0;
-    const float lo = texel2d(s, i0, j0) * (1.0f - ax) + texel2d(s, i0 + 1, j0) * ax;
-    const float hi = texel2d(s, i0, j0 + 1) * (1.0f - ax) + texel2d(s, i0 + 1, j0 + 1) * ax;
-    return vec4(lo * (1.0f - ay) + hi * ay, 0.0f, 0.0f, 1.0f);
+    vec4 r(0.0f, 0.0f, 0.0f, 1.0f);
+    for (int c = 0; c < s.C && c < 4; c++) {
+        const float lo = texel2d(s, i0, j0, c) * (1.0f - ax) + texel2d(s, i0 + 1, j0, c) * ax;
+        const float hi = texel2d(s, i0, j0 + 1, c) * (1.0f - ax) + texel2d(s, i0 + 1, j0 + 1, c) * ax;
+        r[c] = lo * (1.0f - ay) + hi * ay;
+    }
+    return r;
 }
 inline vec4 texelFetch(const sampler2D& s, const ivec2& p, int lod) {
     (void)lod;
     if (p.x < 0 || p.y < 0 || p.x >= s.W || p.y >= s.H) std::abort();
-    return vec4(s.data[(size_t)p.y * s.W + p.x], 0.0f, 0.0f, 1.0f);
+    return texel_vec(s, p.x, p.y);
 }
 inline ivec2 textureSize(const sampler2D& s, int lod) { (void)lod; return ivec2(s.W, s.H); }
 

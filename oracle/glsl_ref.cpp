@@ -122,4 +122,65 @@ void glslref_trace_shadow(const uint8_t* vox, const uint8_t* df, int X, int Y, i
         }
 }
 
+// The pre-temporal 3x3 filter (Core/Pipeline.cpp:2288-2330,
+// Spatial3x3Initial.glsl main) over a W x H grid. t: hit distance, normal:
+// face id / 10; sh (4 channels), cocg (2), aosky (2), luma (1): the diffuse
+// trace's planes. Out: o_SH, o_CoCg, o_AOSky, o_Utility per texel.
+void glslref_spatial_initial(const float* inv_view, const float* inv_proj, int W, int H, const float* t,
+                             const float* normal, const float* sh, const float* cocg, const float* aosky,
+                             const float* luma, float* o_sh, float* o_cocg, float* o_aosky, float* o_luma) {
+    pre3x3::u_PositionTexture = sampler2D{t, W, H, 1};
+    pre3x3::u_NormalTexture = sampler2D{normal, W, H, 1};
+    pre3x3::u_SH = sampler2D{sh, W, H, 4};
+    pre3x3::u_CoCg = sampler2D{cocg, W, H, 2};
+    pre3x3::u_AO = sampler2D{aosky, W, H, 2};
+    pre3x3::u_Utility = sampler2D{luma, W, H, 1};
+    pre3x3::u_InverseView = mat_from(inv_view);
+    pre3x3::u_InverseProjection = mat_from(inv_proj);
+    pre3x3::u_Dimensions = vec2((float)W, (float)H);
+    pre3x3::u_Time = 0.0f;
+    pre3x3::v_RayOrigin = vec3(inv_view[12], inv_view[13], inv_view[14]);
+    for (int j = 0; j < H; j++)
+        for (int i = 0; i < W; i++) {
+            pre3x3::v_TexCoords = vec2(((float)i + 0.5f) / (float)W, ((float)j + 0.5f) / (float)H);
+            pre3x3::gl_FragCoord = vec4((float)i + 0.5f, (float)j + 0.5f, 0.0f, 1.0f);
+            pre3x3::main();
+            const size_t px = (size_t)j * W + i;
+            for (int c = 0; c < 4; c++) o_sh[px * 4 + c] = pre3x3::o_SH[c];
+            o_cocg[px * 2] = pre3x3::o_CoCg.x;
+            o_cocg[px * 2 + 1] = pre3x3::o_CoCg.y;
+            o_aosky[px * 2] = pre3x3::o_AOSky.x;
+            o_aosky[px * 2 + 1] = pre3x3::o_AOSky.y;
+            o_luma[px] = pre3x3::o_Utility;
+        }
+}
+
+// The SVGF variance estimate (Core/Pipeline.cpp:2440-2475,
+// SVGF/VarianceEstimate.glsl main) over a W x H grid. t / normal as above;
+// sh (4 channels), cocg (2), util (4: accumulated frames, moment, luminance):
+// the temporal pass's planes. Out: o_SH, o_CoCg, o_Variance per texel.
+void glslref_variance(const float* inv_view, const float* inv_proj, int W, int H, const float* t,
+                      const float* normal, const float* sh, const float* cocg, const float* util, float* o_sh,
+                      float* o_cocg, float* o_var) {
+    variance::u_PositionTexture = sampler2D{t, W, H, 1};
+    variance::u_NormalTexture = sampler2D{normal, W, H, 1};
+    variance::u_SH = sampler2D{sh, W, H, 4};
+    variance::u_CoCg = sampler2D{cocg, W, H, 2};
+    variance::u_Utility = sampler2D{util, W, H, 4};
+    variance::u_InverseView = mat_from(inv_view);
+    variance::u_InverseProjection = mat_from(inv_proj);
+    variance::v_RayOrigin = vec3(inv_view[12], inv_view[13], inv_view[14]);
+    for (int j = 0; j < H; j++)
+        for (int i = 0; i < W; i++) {
+            variance::v_TexCoords = vec2(((float)i + 0.5f) / (float)W, ((float)j + 0.5f) / (float)H);
+            variance::gl_FragCoord = vec4((float)i + 0.5f, (float)j + 0.5f, 0.0f, 1.0f);
+            variance::main();
+            const size_t px = (size_t)j * W + i;
+            for (int c = 0; c < 4; c++) o_sh[px * 4 + c] = variance::o_SH[c];
+            o_cocg[px * 2] = variance::o_CoCg.x;
+            o_cocg[px * 2 + 1] = variance::o_CoCg.y;
+            o_var[px] = variance::o_Variance;
+        }
+}
+
 }  // extern "C"

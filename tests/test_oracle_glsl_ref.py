@@ -1,14 +1,15 @@
 """The oracle against the reference's own shader code, compiled as C++.
 
 oracle/build_glsl_ref.py takes ManhattanDistance{X,Y,Z}.comp,
-InitialRayTraceFrag.glsl and ShadowRayTraceFrag.glsl from the reference tree, rewrites only GLSL syntax
+InitialRayTraceFrag.glsl, ShadowRayTraceFrag.glsl, Spatial3x3Initial.glsl and
+SVGF/VarianceEstimate.glsl from the reference tree, rewrites only GLSL syntax
 (qualifiers, swizzles, literals, interface variables) and compiles them with
 GLSL's types and built-ins from oracle/glsl_compat.h into
 oracle/_ref/libglsl_ref.so; oracle/glsl_ref.cpp runs them as the
 reference's dispatches and draws do. Where they and the oracle take the same
 inputs, every output must be bit-identical: the distance field of every
-world, the primary G-buffer (hit distance, face id, block id) and the sun
-shadow of every texel. That pins the oracle's restatement of those passes to the reference's
+world, the primary G-buffer (hit distance, face id, block id), the sun
+shadow, the pre-temporal 3x3 filter and the variance estimate of every texel. That pins the oracle's restatement of those passes to the reference's
 own code; the built-ins (normalize, texel fetch of R8 data, matrix times
 vector) are the conventions the oracle fixes for them. Skipped where the
 reference tree is absent (the GPU machines).
@@ -32,6 +33,8 @@ def ref():
     L.glslref_trace_primary.argtypes = [P, P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_int, C.c_int,
                                         C.c_float, P, P, P]
     L.glslref_trace_shadow.argtypes = [P, P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P]
+    L.glslref_spatial_initial.argtypes = [P, P, C.c_int, C.c_int] + [P] * 10
+    L.glslref_variance.argtypes = [P, P, C.c_int, C.c_int] + [P] * 8
     return L
 
 
@@ -123,3 +126,69 @@ def test_sun_shadow_equals_the_reference_shader(ref, sun, seed):
     assert set(np.unique(out).tolist()) <= {0.0, 1.0}
     assert np.array_equal(out.astype(np.uint8), want)
     assert (want[g["t"] > 0] == 1).any()
+
+
+def f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def same(a, b):
+    a, b = f32(a), f32(b)
+    eq = (a.view(np.uint32) == b.view(np.uint32)) | ((a == 0) & (b == 0)) | (np.isnan(a) & np.isnan(b))
+    return bool(eq.all())
+
+
+@pytest.fixture(scope="module", params=[1, 5])
+def gi_frame(request):
+    """A traced frame (G-buffer and diffuse GI) and its SVGF intermediates."""
+    seed = request.param
+    X, Y, Z = 64, 64, 64
+    W, H = 96, 64
+    vox = inputs.generate_world(X, Y, Z, seed=seed)
+    blocks = inputs.generate_block_table(100, seed=seed)
+    df = oracle.build_df(vox)
+    world = oracle.World(vox, df, blocks)
+    yaw, pitch = inputs.seeded_pose(seed)
+    cam = inputs.camera_from_pose((X / 2, 58.0, Z / 2), yaw, pitch, 90.0, W / H)
+    cfg = inputs.default_config(width=W, height=H, primary_max_steps=256)
+    frame = inputs.default_frame(frame_index=0, seed=11, time=1.3)
+    g = oracle.trace_primary(world, cam, cfg)
+    gi = oracle.trace_diffuse(world, cam, cfg, frame, g["t"], g["face"])
+    prev_g, hist = oracle.empty_history(H, W)
+    sv = oracle.svgf(cam, cam, cfg, frame, g, prev_g, gi, hist)
+    # the face plane as the initial trace writes it (GetNormalID: k / 10, 1.0 for a miss)
+    normal = np.array([np.float32(k) / np.float32(10) for k in range(11)], np.float32)[g["face"]]
+    return dict(W=W, H=H, cam=cam, cfg=cfg, frame=frame, g=g, gi=gi, sv=sv, normal=normal,
+                iv=f32(cam.inv_view), ip=f32(cam.inv_proj))
+
+
+def test_pre_temporal_filter_equals_the_reference_shader(ref, gi_frame):
+    F = gi_frame
+    W, H, gi = F["W"], F["H"], F["gi"]
+    want = oracle.spatial_initial(F["cam"], F["cfg"], F["g"]["t"], F["g"]["face"], gi)
+    o = {"sh": np.zeros((H, W, 4), np.float32), "cocg": np.zeros((H, W, 2), np.float32),
+         "aosky": np.zeros((H, W, 2), np.float32), "luma": np.zeros((H, W), np.float32)}
+    ins = [f32(F["g"]["t"]), F["normal"], f32(gi["sh"]), f32(gi["cocg"]), f32(gi["aosky"]), f32(gi["luma"])]
+    ref.glslref_spatial_initial(F["iv"].ctypes.data, F["ip"].ctypes.data, W, H, *[a.ctypes.data for a in ins],
+                                *[o[k].ctypes.data for k in ("sh", "cocg", "aosky", "luma")])
+    for k in o:
+        assert same(o[k], want[k]), k
+
+
+def test_variance_estimate_equals_the_reference_shader(ref, gi_frame):
+    """Both branches: the accumulated-frame count of every texel drawn from
+    young (< 12, the 81-tap estimate) and old histories."""
+    F = gi_frame
+    W, H = F["W"], F["H"]
+    tmp = F["sv"]["temporal"]
+    util = f32(tmp["util"]).copy()
+    rng = np.random.default_rng(W + H)
+    util[..., 0] = rng.choice(np.array([1, 2, 5, 11, 11.5, 12, 13, 30], np.float32), size=(H, W))
+    want = oracle.variance(F["cam"], F["cfg"], F["g"]["t"], F["g"]["face"], dict(tmp, util=util))
+    o = {"sh": np.zeros((H, W, 4), np.float32), "cocg": np.zeros((H, W, 2), np.float32),
+         "variance": np.zeros((H, W), np.float32)}
+    ins = [f32(F["g"]["t"]), F["normal"], f32(tmp["sh"]), f32(tmp["cocg"]), util]
+    ref.glslref_variance(F["iv"].ctypes.data, F["ip"].ctypes.data, W, H, *[a.ctypes.data for a in ins],
+                         *[o[k].ctypes.data for k in ("sh", "cocg", "variance")])
+    for k in o:
+        assert same(o[k], want[k]), k
