@@ -48,6 +48,7 @@ UNITS = [
     ("shadow", "ShadowRayTraceFrag.glsl", "main", ("VoxelTraversalDF_AlphaTest",)),
     ("pre3x3", "Spatial3x3Initial.glsl", "main", ()),
     ("variance", "SVGF/VarianceEstimate.glsl", "main", ()),
+    ("atrous", "SVGF/SpatialFilter.glsl", "main", ()),
 ]
 WORLD_DEFINES = ("WORLD_SIZE_X", "WORLD_SIZE_Y", "WORLD_SIZE_Z")
 KEYWORDS = {"if", "else", "for", "while", "return", "const", "void", "float", "int", "bool", "true", "false",

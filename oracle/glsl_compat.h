@@ -227,13 +227,15 @@ inline vec4 texelFetch(const sampler3D& s, const ivec3& p, int lod) {
 }
 // Float 2-D texture of C interleaved channels (a G-buffer or filter plane),
 // rows from the bottom; a fetch fills (r, g, b, a) from the C channels and
-// (0, 0, 0, 1) after them. texture() follows the oracle's sampling
+// (0, 0, 0, 1) after them. texture() of a GL_NEAREST texture returns the
+// texel the coordinate falls in; otherwise it follows the oracle's sampling
 // convention: at a texel centre (the texel-space coordinate within 2^-9 of an
 // integer, what the hardware's fixed-point addressing snaps) it returns that
 // texel, elsewhere it blends the four texels with fp32 weights, REPEAT wrap.
 struct sampler2D {
     const float* data = nullptr;
     int W = 0, H = 0, C = 1;
+    bool nearest = false;   // GL_NEAREST (the G-buffer's face and block planes)
 };
 inline float texel2d(const sampler2D& s, int i, int j, int c) {
     i %= s.W; if (i < 0) i += s.W;
@@ -246,6 +248,7 @@ inline vec4 texel_vec(const sampler2D& s, int i, int j) {
     return r;
 }
 inline vec4 texture(const sampler2D& s, const vec2& uv) {
+    if (s.nearest) return texel_vec(s, (int)std::floor(uv.x * (float)s.W), (int)std::floor(uv.y * (float)s.H));
     const float x = uv.x * (float)s.W - 0.5f, y = uv.y * (float)s.H - 0.5f;
     const float rx = std::nearbyint(x), ry = std::nearbyint(y);
     if (std::fabs(x - rx) < 0.001953125f && std::fabs(y - ry) < 0.001953125f)

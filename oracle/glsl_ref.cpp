@@ -89,7 +89,8 @@ void glslref_trace_primary(const uint8_t* vox, const uint8_t* df, int X, int Y, 
 // main) over a W x H target at full resolution (no Halton offset), hard
 // shadows (no contact-hardening cone), no alpha test. hit_t: the G-buffer's
 // hit distance plane (u_PositionTexture); normal: its face plane as the
-// initial trace writes it (u_NormalTexture, face id / 10). v_RayOrigin is the
+// initial trace writes it (u_NormalTexture, face id / 10, GL_NEAREST as the
+// G-buffer's face plane is, Core/Pipeline.cpp:1094). v_RayOrigin is the
 // camera position the vertex stage passes, gl_FragCoord the texel centre.
 // Out: o_Shadow per texel.
 void glslref_trace_shadow(const uint8_t* vox, const uint8_t* df, int X, int Y, int Z, const float* inv_view,
@@ -100,7 +101,7 @@ void glslref_trace_shadow(const uint8_t* vox, const uint8_t* df, int X, int Y, i
     shadow::u_VoxelData = sampler3D{vox, X, Y, Z};
     shadow::u_DistanceFieldTexture = sampler3D{df, X, Y, Z};
     shadow::u_PositionTexture = sampler2D{hit_t, W, H};
-    shadow::u_NormalTexture = sampler2D{normal, W, H};
+    shadow::u_NormalTexture = sampler2D{normal, W, H, 1, true};
     shadow::u_BlueNoiseTexture = sampler2D{no_noise, 1, 1};
     shadow::u_InverseView = mat_from(inv_view);
     shadow::u_InverseProjection = mat_from(inv_proj);
@@ -130,7 +131,7 @@ void glslref_spatial_initial(const float* inv_view, const float* inv_proj, int W
                              const float* normal, const float* sh, const float* cocg, const float* aosky,
                              const float* luma, float* o_sh, float* o_cocg, float* o_aosky, float* o_luma) {
     pre3x3::u_PositionTexture = sampler2D{t, W, H, 1};
-    pre3x3::u_NormalTexture = sampler2D{normal, W, H, 1};
+    pre3x3::u_NormalTexture = sampler2D{normal, W, H, 1, true};
     pre3x3::u_SH = sampler2D{sh, W, H, 4};
     pre3x3::u_CoCg = sampler2D{cocg, W, H, 2};
     pre3x3::u_AO = sampler2D{aosky, W, H, 2};
@@ -163,7 +164,7 @@ void glslref_variance(const float* inv_view, const float* inv_proj, int W, int H
                       const float* normal, const float* sh, const float* cocg, const float* util, float* o_sh,
                       float* o_cocg, float* o_var) {
     variance::u_PositionTexture = sampler2D{t, W, H, 1};
-    variance::u_NormalTexture = sampler2D{normal, W, H, 1};
+    variance::u_NormalTexture = sampler2D{normal, W, H, 1, true};
     variance::u_SH = sampler2D{sh, W, H, 4};
     variance::u_CoCg = sampler2D{cocg, W, H, 2};
     variance::u_Utility = sampler2D{util, W, H, 4};
@@ -180,6 +181,47 @@ void glslref_variance(const float* inv_view, const float* inv_proj, int W, int H
             o_cocg[px * 2] = variance::o_CoCg.x;
             o_cocg[px * 2 + 1] = variance::o_CoCg.y;
             o_var[px] = variance::o_Variance;
+        }
+}
+
+// One SVGF a-trous iteration (Core/Pipeline.cpp:2481-2610,
+// SVGF/SpatialFilter.glsl main) of step `step` over a W x H grid, with the
+// pipeline's settings (3x3 taps, aggressive disocclusion handling, spatial
+// filter on). sh (4 channels), cocg (2), variance (1), aosky (2): the
+// iteration's input planes; util (4): the temporal pass's (accumulated
+// frames first). Out: o_SH, o_CoCg, o_Variance, o_AOAndSkylighting.
+void glslref_atrous(int W, int H, int step, float resolution_scale,
+                    float color_phi_bias, float time, const float* t, const float* normal, const float* util,
+                    const float* sh, const float* cocg, const float* var, const float* aosky, float* o_sh,
+                    float* o_cocg, float* o_var, float* o_aosky) {
+    atrous::u_PositionTexture = sampler2D{t, W, H, 1};
+    atrous::u_NormalTexture = sampler2D{normal, W, H, 1, true};
+    atrous::u_Utility = sampler2D{util, W, H, 4};
+    atrous::u_TemporalMoment = sampler2D{util, W, H, 4};
+    atrous::u_SH = sampler2D{sh, W, H, 4};
+    atrous::u_CoCg = sampler2D{cocg, W, H, 2};
+    atrous::u_VarianceTexture = sampler2D{var, W, H, 1};
+    atrous::u_AO = sampler2D{aosky, W, H, 2};
+    atrous::u_Dimensions = vec2((float)W, (float)H);
+    atrous::u_Step = step;
+    atrous::u_LargeKernel = false;
+    atrous::AGGRESSIVE_DISOCCLUSION_HANDLING = true;
+    atrous::DO_SPATIAL = true;
+    atrous::u_ColorPhiBias = color_phi_bias;
+    atrous::u_ResolutionScale = resolution_scale;
+    atrous::u_Time = time;
+    for (int j = 0; j < H; j++)
+        for (int i = 0; i < W; i++) {
+            atrous::v_TexCoords = vec2(((float)i + 0.5f) / (float)W, ((float)j + 0.5f) / (float)H);
+            atrous::gl_FragCoord = vec4((float)i + 0.5f, (float)j + 0.5f, 0.0f, 1.0f);
+            atrous::main();
+            const size_t px = (size_t)j * W + i;
+            for (int c = 0; c < 4; c++) o_sh[px * 4 + c] = atrous::o_SH[c];
+            o_cocg[px * 2] = atrous::o_CoCg.x;
+            o_cocg[px * 2 + 1] = atrous::o_CoCg.y;
+            o_var[px] = atrous::o_Variance;
+            o_aosky[px * 2] = atrous::o_AOAndSkylighting.x;
+            o_aosky[px * 2 + 1] = atrous::o_AOAndSkylighting.y;
         }
 }
 

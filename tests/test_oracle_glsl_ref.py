@@ -1,15 +1,16 @@
 """The oracle against the reference's own shader code, compiled as C++.
 
 oracle/build_glsl_ref.py takes ManhattanDistance{X,Y,Z}.comp,
-InitialRayTraceFrag.glsl, ShadowRayTraceFrag.glsl, Spatial3x3Initial.glsl and
-SVGF/VarianceEstimate.glsl from the reference tree, rewrites only GLSL syntax
+InitialRayTraceFrag.glsl, ShadowRayTraceFrag.glsl, Spatial3x3Initial.glsl,
+SVGF/VarianceEstimate.glsl and SVGF/SpatialFilter.glsl from the reference tree, rewrites only GLSL syntax
 (qualifiers, swizzles, literals, interface variables) and compiles them with
 GLSL's types and built-ins from oracle/glsl_compat.h into
 oracle/_ref/libglsl_ref.so; oracle/glsl_ref.cpp runs them as the
 reference's dispatches and draws do. Where they and the oracle take the same
 inputs, every output must be bit-identical: the distance field of every
 world, the primary G-buffer (hit distance, face id, block id), the sun
-shadow, the pre-temporal 3x3 filter and the variance estimate of every texel. That pins the oracle's restatement of those passes to the reference's
+shadow, the pre-temporal 3x3 filter, the variance estimate and the five
+a-trous iterations of every texel. That pins the oracle's restatement of those passes to the reference's
 own code; the built-ins (normalize, texel fetch of R8 data, matrix times
 vector) are the conventions the oracle fixes for them. Skipped where the
 reference tree is absent (the GPU machines).
@@ -35,6 +36,7 @@ def ref():
     L.glslref_trace_shadow.argtypes = [P, P, C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P]
     L.glslref_spatial_initial.argtypes = [P, P, C.c_int, C.c_int] + [P] * 10
     L.glslref_variance.argtypes = [P, P, C.c_int, C.c_int] + [P] * 8
+    L.glslref_atrous.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float] + [P] * 11
     return L
 
 
@@ -192,3 +194,29 @@ def test_variance_estimate_equals_the_reference_shader(ref, gi_frame):
                          *[o[k].ctypes.data for k in ("sh", "cocg", "variance")])
     for k in o:
         assert same(o[k], want[k]), k
+
+
+@pytest.mark.parametrize("history", ["young", "old"])
+def test_atrous_iterations_equal_the_reference_shader(ref, gi_frame, history):
+    """The five iterations (steps 16, 8, 4, 2, 1: gathered taps at fractional
+    offsets, jittered, with and without the AO / sky filter), each from the
+    oracle's previous output; young histories take the strong spatial branch
+    at steps <= 8, old ones the luminance weight at every step."""
+    F = gi_frame
+    W, H, sv = F["W"], F["H"], F["sv"]
+    p = oracle.params(F["cfg"])
+    util = f32(sv["temporal"]["util"]).copy()
+    if history == "old":
+        util[..., 0] = 30.0
+    cur, ao = sv["variance"], sv["temporal"]["aosky"]
+    for it in range(p.atrous_iterations):
+        step = max(16 >> it, 1)
+        want = oracle.atrous(F["cam"], F["cfg"], F["frame"], step, F["g"]["t"], F["g"]["face"], util, cur, ao)
+        o = {"sh": np.zeros((H, W, 4), np.float32), "cocg": np.zeros((H, W, 2), np.float32),
+             "variance": np.zeros((H, W), np.float32), "aosky": np.zeros((H, W, 2), np.float32)}
+        ins = [f32(F["g"]["t"]), F["normal"], util, f32(cur["sh"]), f32(cur["cocg"]), f32(cur["variance"]), f32(ao)]
+        ref.glslref_atrous(W, H, step, p.resolution_scale, p.color_phi_bias, F["frame"].time,
+                           *[a.ctypes.data for a in ins], *[o[k].ctypes.data for k in ("sh", "cocg", "variance", "aosky")])
+        for k in o:
+            assert same(o[k], want[k]), (step, k)
+        cur, ao = want, want["aosky"]
