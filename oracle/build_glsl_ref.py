@@ -18,8 +18,9 @@ The rewrites keep the shader's own arithmetic and operation order:
     a `buffer` block -> its members; `layout(...) in;` is dropped;
   * the WORLD_SIZE_* #defines -> variables the drivers set (the shaders hard
     code the reference's 384 x 128 x 384 world);
-  * swizzles `.xyz` / `.xy` (and `.rgb` / `.rg`) -> member calls, single
-    colour components `.r .g .b .a` -> `.x .y .z .w`;
+  * swizzles `.xyzw` / `.xyz` / `.xy` (and `.rgba` / `.rgb` / `.rg`) -> member
+    calls, single colour components `.r .g .b .a` -> `.x .y .z .w`, and
+    `v.xyz /= s;` -> the three component divisions;
   * array constructors `T[](a, b, ...)` -> brace lists;
   * floating literals without a suffix -> float literals (GLSL's float).
 
@@ -49,6 +50,7 @@ UNITS = [
     ("pre3x3", "Spatial3x3Initial.glsl", "main", ()),
     ("variance", "SVGF/VarianceEstimate.glsl", "main", ()),
     ("atrous", "SVGF/SpatialFilter.glsl", "main", ()),
+    ("temporal", "SVGF/TemporalFilter.glsl", "main", ()),
 ]
 WORLD_DEFINES = ("WORLD_SIZE_X", "WORLD_SIZE_Y", "WORLD_SIZE_Z")
 KEYWORDS = {"if", "else", "for", "while", "return", "const", "void", "float", "int", "bool", "true", "false",
@@ -147,6 +149,10 @@ def rewrite_array_ctors(text: str) -> str:
 
 def rewrite_expr(text: str) -> str:
     text = rewrite_array_ctors(text)
+    # a swizzle assigned through `/=`: each component divided by the value read once
+    text = re.sub(r"\b(\w+)\.xyz\s*/=\s*([^;]+);",
+                  lambda m: (f"{{ const float d_ = {m.group(2)}; {m.group(1)}.x /= d_; {m.group(1)}.y /= d_; "
+                             f"{m.group(1)}.z /= d_; }}"), text)
     swz = {"xyzw": "xyzw", "rgba": "xyzw", "xyz": "xyz", "rgb": "xyz", "xy": "xy", "rg": "xy"}
     text = re.sub(r"\.(xyzw|rgba|xyz|rgb|xy|rg)\b(?!\s*\()", lambda m: f".{swz[m.group(1)]}()", text)
     comp = {"r": "x", "g": "y", "b": "z", "a": "w"}

@@ -124,6 +124,12 @@ inline vec4 operator*(const mat4& m, const vec4& v) {
     for (int i = 0; i < 4; i++) r[i] = ((m.c[0][i] * v.x + m.c[1][i] * v.y) + m.c[2][i] * v.z) + m.c[3][i] * v.w;
     return r;
 }
+// a * b: column c of the product is a * (column c of b)
+inline mat4 operator*(const mat4& a, const mat4& b) {
+    mat4 r;
+    for (int c = 0; c < 4; c++) r.c[c] = a * b.c[c];
+    return r;
+}
 
 // ---- float vector operators (component-wise) ----
 #define GLSL_VEC_OPS(V, N)                                                                         \
@@ -201,6 +207,13 @@ inline vec3 sign(const vec3& v) { return vec3(sign(v.x), sign(v.y), sign(v.z)); 
 inline vec3 abs(const vec3& v) { return vec3(abs(v.x), abs(v.y), abs(v.z)); }
 inline vec2 fract(const vec2& v) { return vec2(fract(v.x), fract(v.y)); }
 inline vec2 clamp(const vec2& v, float lo, float hi) { return vec2(clamp(v.x, lo, hi), clamp(v.y, lo, hi)); }
+inline vec3 clamp(const vec3& v, float lo, float hi) {
+    return vec3(clamp(v.x, lo, hi), clamp(v.y, lo, hi), clamp(v.z, lo, hi));
+}
+inline vec2 mix(const vec2& a, const vec2& b, float t) { return vec2(mix(a.x, b.x, t), mix(a.y, b.y, t)); }
+inline vec4 mix(const vec4& a, const vec4& b, float t) {
+    return vec4(mix(a.x, b.x, t), mix(a.y, b.y, t), mix(a.z, b.z, t), mix(a.w, b.w, t));
+}
 inline vec4 clamp(const vec4& v, float lo, float hi) {
     return vec4(clamp(v.x, lo, hi), clamp(v.y, lo, hi), clamp(v.z, lo, hi), clamp(v.w, lo, hi));
 }
@@ -236,6 +249,7 @@ struct sampler2D {
     const float* data = nullptr;
     int W = 0, H = 0, C = 1;
     bool nearest = false;   // GL_NEAREST (the G-buffer's face and block planes)
+    bool snap = true;       // texel centres return the texel (off: always the fp32 blend)
 };
 inline float texel2d(const sampler2D& s, int i, int j, int c) {
     i %= s.W; if (i < 0) i += s.W;
@@ -251,7 +265,7 @@ inline vec4 texture(const sampler2D& s, const vec2& uv) {
     if (s.nearest) return texel_vec(s, (int)std::floor(uv.x * (float)s.W), (int)std::floor(uv.y * (float)s.H));
     const float x = uv.x * (float)s.W - 0.5f, y = uv.y * (float)s.H - 0.5f;
     const float rx = std::nearbyint(x), ry = std::nearbyint(y);
-    if (std::fabs(x - rx) < 0.001953125f && std::fabs(y - ry) < 0.001953125f)
+    if (s.snap && std::fabs(x - rx) < 0.001953125f && std::fabs(y - ry) < 0.001953125f)
         return texel_vec(s, (int)rx, (int)ry);
     const float x0 = std::floor(x), y0 = std::floor(y), ax = x - x0, ay = y - y0;
     const int i0 = (int)x0, j0 = (int)y0;

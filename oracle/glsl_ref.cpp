@@ -225,4 +225,54 @@ void glslref_atrous(int W, int H, int step, float resolution_scale,
         }
 }
 
+// The SVGF temporal pass (Core/Pipeline.cpp:2336-2436,
+// SVGF/TemporalFilter.glsl main) over a W x H grid. The current frame: t,
+// normal (face id / 10), block (id / 255), the pre-filtered sh (4 channels),
+// cocg (2), luma (1) and aosky (2); the previous frame: its G-buffer (prev_t,
+// prev_normal, prev_block) and history (prev_sh, prev_cocg, prev_util (4),
+// prev_aosky), sampled at the reprojected coordinates (bilinear, the face and
+// block planes nearest). view / proj: the previous camera's. Out: o_SH,
+// o_CoCg, o_Utility (3), o_AOAndSkyLighting.
+void glslref_temporal(const float* inv_view, const float* inv_proj, const float* prev_view, const float* prev_proj,
+                      int W, int H, int be_useful, const float* t, const float* normal, const float* block,
+                      const float* sh, const float* cocg, const float* luma, const float* aosky, const float* prev_t,
+                      const float* prev_normal, const float* prev_block, const float* prev_sh,
+                      const float* prev_cocg, const float* prev_util, const float* prev_aosky, float* o_sh,
+                      float* o_cocg, float* o_util, float* o_aosky) {
+    temporal::u_CurrentPositionTexture = sampler2D{t, W, H, 1};
+    temporal::u_CurrentNormalTexture = sampler2D{normal, W, H, 1, true};
+    temporal::u_CurrentBlockIDTexture = sampler2D{block, W, H, 1, true};
+    temporal::u_CurrentSH = sampler2D{sh, W, H, 4};
+    temporal::u_CurrentCoCg = sampler2D{cocg, W, H, 2};
+    temporal::u_NoisyLuminosity = sampler2D{luma, W, H, 1};
+    temporal::u_CurrentAO = sampler2D{aosky, W, H, 2};
+    temporal::u_PreviousPositionTexture = sampler2D{prev_t, W, H, 1, false, false};
+    temporal::u_PreviousNormalTexture = sampler2D{prev_normal, W, H, 1, true};
+    temporal::u_PrevBlockIDTexture = sampler2D{prev_block, W, H, 1, true};
+    temporal::u_PreviousSH = sampler2D{prev_sh, W, H, 4, false, false};
+    temporal::u_PrevCoCg = sampler2D{prev_cocg, W, H, 2, false, false};
+    temporal::u_PreviousUtility = sampler2D{prev_util, W, H, 4, false, false};
+    temporal::u_PreviousAO = sampler2D{prev_aosky, W, H, 2, false, false};
+    temporal::u_InverseView = mat_from(inv_view);
+    temporal::u_InverseProjection = mat_from(inv_proj);
+    temporal::u_PrevView = mat_from(prev_view);
+    temporal::u_PrevProjection = mat_from(prev_proj);
+    temporal::u_BeUseful = be_useful != 0;
+    temporal::u_Time = 0.0f;
+    temporal::v_RayOrigin = vec3(inv_view[12], inv_view[13], inv_view[14]);
+    for (int j = 0; j < H; j++)
+        for (int i = 0; i < W; i++) {
+            temporal::v_TexCoords = vec2(((float)i + 0.5f) / (float)W, ((float)j + 0.5f) / (float)H);
+            temporal::gl_FragCoord = vec4((float)i + 0.5f, (float)j + 0.5f, 0.0f, 1.0f);
+            temporal::main();
+            const size_t px = (size_t)j * W + i;
+            for (int c = 0; c < 4; c++) o_sh[px * 4 + c] = temporal::o_SH[c];
+            o_cocg[px * 2] = temporal::o_CoCg.x;
+            o_cocg[px * 2 + 1] = temporal::o_CoCg.y;
+            for (int c = 0; c < 3; c++) o_util[px * 3 + c] = temporal::o_Utility[c];
+            o_aosky[px * 2] = temporal::o_AOAndSkyLighting.x;
+            o_aosky[px * 2 + 1] = temporal::o_AOAndSkyLighting.y;
+        }
+}
+
 }  // extern "C"

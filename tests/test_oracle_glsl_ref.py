@@ -1,16 +1,16 @@
 """The oracle against the reference's own shader code, compiled as C++.
 
 oracle/build_glsl_ref.py takes ManhattanDistance{X,Y,Z}.comp,
-InitialRayTraceFrag.glsl, ShadowRayTraceFrag.glsl, Spatial3x3Initial.glsl,
-SVGF/VarianceEstimate.glsl and SVGF/SpatialFilter.glsl from the reference tree, rewrites only GLSL syntax
+InitialRayTraceFrag.glsl, ShadowRayTraceFrag.glsl, Spatial3x3Initial.glsl and
+SVGF/{TemporalFilter,VarianceEstimate,SpatialFilter}.glsl from the reference tree, rewrites only GLSL syntax
 (qualifiers, swizzles, literals, interface variables) and compiles them with
 GLSL's types and built-ins from oracle/glsl_compat.h into
 oracle/_ref/libglsl_ref.so; oracle/glsl_ref.cpp runs them as the
 reference's dispatches and draws do. Where they and the oracle take the same
 inputs, every output must be bit-identical: the distance field of every
 world, the primary G-buffer (hit distance, face id, block id), the sun
-shadow, the pre-temporal 3x3 filter, the variance estimate and the five
-a-trous iterations of every texel. That pins the oracle's restatement of those passes to the reference's
+shadow, the pre-temporal 3x3 filter, the temporal pass over a moving camera,
+the variance estimate and the five a-trous iterations of every texel. That pins the oracle's restatement of those passes to the reference's
 own code; the built-ins (normalize, texel fetch of R8 data, matrix times
 vector) are the conventions the oracle fixes for them. Skipped where the
 reference tree is absent (the GPU machines).
@@ -37,6 +37,7 @@ def ref():
     L.glslref_spatial_initial.argtypes = [P, P, C.c_int, C.c_int] + [P] * 10
     L.glslref_variance.argtypes = [P, P, C.c_int, C.c_int] + [P] * 8
     L.glslref_atrous.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float] + [P] * 11
+    L.glslref_temporal.argtypes = [P] * 4 + [C.c_int] * 3 + [P] * 18
     return L
 
 
@@ -220,3 +221,43 @@ def test_atrous_iterations_equal_the_reference_shader(ref, gi_frame, history):
         for k in o:
             assert same(o[k], want[k]), (step, k)
         cur, ao = want, want["aosky"]
+
+
+@pytest.mark.parametrize("seed", [1, 5])
+def test_temporal_pass_equals_the_reference_shader(ref, seed):
+    """Three frames: an empty history, a moved and turned camera (the history
+    reprojected through the previous view-projection and sampled between
+    texels), then the same camera again (reprojection onto the texel centres)."""
+    X, Y, Z = 64, 64, 64
+    W, H = 96, 64
+    vox = inputs.generate_world(X, Y, Z, seed=seed)
+    blocks = inputs.generate_block_table(100, seed=seed)
+    world = oracle.World(vox, oracle.build_df(vox), blocks)
+    yaw, pitch = inputs.seeded_pose(seed)
+    cams = [inputs.camera_from_pose((X / 2, 58.0, Z / 2), yaw, pitch, 90.0, W / H),
+            inputs.camera_from_pose((X / 2 + 0.7, 58.2, Z / 2 - 0.4), yaw + 2.0, pitch + 1.0, 90.0, W / H)]
+    cfg = inputs.default_config(width=W, height=H, primary_max_steps=256)
+    ids = np.array([np.float32(k) / np.float32(10) for k in range(11)], np.float32)
+    prev_g, hist = oracle.empty_history(H, W)
+    prev_cam = cams[0]
+    reprojected = 0
+    for fi, cam in enumerate(cams + [cams[1]]):
+        frame = inputs.default_frame(frame_index=fi, seed=11, time=1.3 + 0.37 * fi)
+        g = oracle.trace_primary(world, cam, cfg)
+        gi = oracle.trace_diffuse(world, cam, cfg, frame, g["t"], g["face"])
+        sv = oracle.svgf(cam, prev_cam, cfg, frame, g, prev_g, gi, hist)
+        pre, want = sv["pre"], sv["temporal"]
+        blk, pblk = (f32(b.astype(np.float32) / np.float32(255)) for b in (g["block"], prev_g["block"]))
+        ins = [f32(g["t"]), ids[g["face"]], blk, f32(pre["sh"]), f32(pre["cocg"]), f32(pre["luma"]),
+               f32(pre["aosky"]), f32(prev_g["t"]), ids[prev_g["face"]], pblk, f32(hist["sh"]), f32(hist["cocg"]),
+               f32(hist["util"]), f32(hist["aosky"])]
+        o = {"sh": np.zeros((H, W, 4), np.float32), "cocg": np.zeros((H, W, 2), np.float32),
+             "util": np.zeros((H, W, 3), np.float32), "aosky": np.zeros((H, W, 2), np.float32)}
+        mats = [f32(cam.inv_view), f32(cam.inv_proj), f32(prev_cam.view), f32(prev_cam.proj)]
+        ref.glslref_temporal(*[m.ctypes.data for m in mats], W, H, int(frame.temporal), *[a.ctypes.data for a in ins],
+                             *[o[k].ctypes.data for k in ("sh", "cocg", "util", "aosky")])
+        assert same(o["sh"], want["sh"]) and same(o["cocg"], want["cocg"]), fi
+        assert same(o["util"], f32(want["util"])[..., :3]) and same(o["aosky"], want["aosky"]), fi
+        reprojected += int((f32(want["util"])[..., 0] > 1).sum())
+        prev_g, hist, prev_cam = {k: g[k] for k in ("t", "face", "block")}, want, cam
+    assert reprojected > 1000
