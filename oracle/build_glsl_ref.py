@@ -21,7 +21,7 @@ The rewrites keep the shader's own arithmetic and operation order:
   * swizzles `.xyzw` / `.xyz` / `.xy` (and `.rgba` / `.rgb` / `.rg`) -> member
     calls, single colour components `.r .g .b .a` -> `.x .y .z .w`, and
     `v.xyz /= s;` -> the three component divisions;
-  * array constructors `T[](a, b, ...)` -> brace lists;
+  * array constructors `T[](a, b, ...)` -> brace lists, `T[n] name` -> `T name[n]`;
   * floating literals without a suffix -> float literals (GLSL's float).
 
     python oracle/build_glsl_ref.py
@@ -51,6 +51,7 @@ UNITS = [
     ("variance", "SVGF/VarianceEstimate.glsl", "main", ()),
     ("atrous", "SVGF/SpatialFilter.glsl", "main", ()),
     ("temporal", "SVGF/TemporalFilter.glsl", "main", ()),
+    ("plain_atrous", "AtrousSpatialFilter.glsl", "main", ()),
 ]
 WORLD_DEFINES = ("WORLD_SIZE_X", "WORLD_SIZE_Y", "WORLD_SIZE_Z")
 KEYWORDS = {"if", "else", "for", "while", "return", "const", "void", "float", "int", "bool", "true", "false",
@@ -148,6 +149,8 @@ def rewrite_array_ctors(text: str) -> str:
 
 
 def rewrite_expr(text: str) -> str:
+    # GLSL's `T[n] name = ...` array declarations -> `T name[n] = ...`
+    text = re.sub(r"\b(\w+)\s*\[\s*(\d+)\s*\]\s+(\w+)\s*=", r"\1 \3[\2] =", text)
     text = rewrite_array_ctors(text)
     # a swizzle assigned through `/=`: each component divided by the value read once
     text = re.sub(r"\b(\w+)\.xyz\s*/=\s*([^;]+);",

@@ -275,4 +275,35 @@ void glslref_temporal(const float* inv_view, const float* inv_proj, const float*
         }
 }
 
+// One a-trous iteration of the non-SVGF denoiser (Core/Pipeline.cpp:2720-2786,
+// AtrousSpatialFilter.glsl main) of step `step` over a W x H grid. t,
+// normal (face id / 10), block (id / 255), var: the G-buffer and the
+// variance estimate; sh (4 channels) and cocg (2): the iteration's input.
+// Out: o_SpatialResult (SH) and o_SpatialResult2 (CoCg) per texel.
+void glslref_plain_atrous(const float* inv_view, const float* inv_proj, int W, int H, int step, const float* t,
+                          const float* normal, const float* block, const float* var, const float* sh,
+                          const float* cocg, float* o_sh, float* o_cocg) {
+    plain_atrous::u_PositionTexture = sampler2D{t, W, H, 1};
+    plain_atrous::u_NormalTexture = sampler2D{normal, W, H, 1, true};
+    plain_atrous::u_BlockIDTexture = sampler2D{block, W, H, 1, true};
+    plain_atrous::u_VarianceTexture = sampler2D{var, W, H, 1};
+    plain_atrous::u_InputTexture = sampler2D{sh, W, H, 4};
+    plain_atrous::u_InputTexture2 = sampler2D{cocg, W, H, 2};
+    plain_atrous::u_InverseView = mat_from(inv_view);
+    plain_atrous::u_InverseProjection = mat_from(inv_proj);
+    plain_atrous::u_Dimensions = vec2((float)W, (float)H);
+    plain_atrous::u_Step = step;
+    plain_atrous::v_RayOrigin = vec3(inv_view[12], inv_view[13], inv_view[14]);
+    for (int j = 0; j < H; j++)
+        for (int i = 0; i < W; i++) {
+            plain_atrous::v_TexCoords = vec2(((float)i + 0.5f) / (float)W, ((float)j + 0.5f) / (float)H);
+            plain_atrous::gl_FragCoord = vec4((float)i + 0.5f, (float)j + 0.5f, 0.0f, 1.0f);
+            plain_atrous::main();
+            const size_t px = (size_t)j * W + i;
+            for (int c = 0; c < 4; c++) o_sh[px * 4 + c] = plain_atrous::o_SpatialResult[c];
+            o_cocg[px * 2] = plain_atrous::o_SpatialResult2.x;
+            o_cocg[px * 2 + 1] = plain_atrous::o_SpatialResult2.y;
+        }
+}
+
 }  // extern "C"

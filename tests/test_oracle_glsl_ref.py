@@ -2,7 +2,8 @@
 
 oracle/build_glsl_ref.py takes ManhattanDistance{X,Y,Z}.comp,
 InitialRayTraceFrag.glsl, ShadowRayTraceFrag.glsl, Spatial3x3Initial.glsl and
-SVGF/{TemporalFilter,VarianceEstimate,SpatialFilter}.glsl from the reference tree, rewrites only GLSL syntax
+SVGF/{TemporalFilter,VarianceEstimate,SpatialFilter}.glsl and
+AtrousSpatialFilter.glsl from the reference tree, rewrites only GLSL syntax
 (qualifiers, swizzles, literals, interface variables) and compiles them with
 GLSL's types and built-ins from oracle/glsl_compat.h into
 oracle/_ref/libglsl_ref.so; oracle/glsl_ref.cpp runs them as the
@@ -10,7 +11,8 @@ reference's dispatches and draws do. Where they and the oracle take the same
 inputs, every output must be bit-identical: the distance field of every
 world, the primary G-buffer (hit distance, face id, block id), the sun
 shadow, the pre-temporal 3x3 filter, the temporal pass over a moving camera,
-the variance estimate and the five a-trous iterations of every texel. That pins the oracle's restatement of those passes to the reference's
+the variance estimate and the five a-trous iterations of every texel, and
+the five iterations of the non-SVGF denoiser's a-trous filter. That pins the oracle's restatement of those passes to the reference's
 own code; the built-ins (normalize, texel fetch of R8 data, matrix times
 vector) are the conventions the oracle fixes for them. Skipped where the
 reference tree is absent (the GPU machines).
@@ -38,6 +40,7 @@ def ref():
     L.glslref_variance.argtypes = [P, P, C.c_int, C.c_int] + [P] * 8
     L.glslref_atrous.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float] + [P] * 11
     L.glslref_temporal.argtypes = [P] * 4 + [C.c_int] * 3 + [P] * 18
+    L.glslref_plain_atrous.argtypes = [P] * 2 + [C.c_int] * 3 + [P] * 8
     return L
 
 
@@ -261,3 +264,32 @@ def test_temporal_pass_equals_the_reference_shader(ref, seed):
         reprojected += int((f32(want["util"])[..., 0] > 1).sum())
         prev_g, hist, prev_cam = {k: g[k] for k in ("t", "face", "block")}, want, cam
     assert reprojected > 1000
+
+
+@pytest.mark.parametrize("seed", [1, 5])
+def test_plain_atrous_iterations_equal_the_reference_shader(ref, seed):
+    """The non-SVGF denoiser's five a-trous iterations (steps 12, 8, 4, 2, 1,
+    5 x 5 taps), each from the oracle's previous output."""
+    X, Y, Z = 64, 64, 64
+    W, H = 96, 64
+    vox = inputs.generate_world(X, Y, Z, seed=seed)
+    world = oracle.World(vox, oracle.build_df(vox), inputs.generate_block_table(100, seed=seed))
+    yaw, pitch = inputs.seeded_pose(seed)
+    cam = inputs.camera_from_pose((X / 2, 58.0, Z / 2), yaw, pitch, 90.0, W / H)
+    cfg = inputs.default_config(width=W, height=H, primary_max_steps=256, denoiser=1)
+    frame = inputs.default_frame(frame_index=0, seed=5)
+    g = oracle.trace_primary(world, cam, cfg)
+    gi = oracle.trace_diffuse(world, cam, cfg, frame, g["t"], g["face"])
+    prev_g, hist = oracle.empty_history(H, W)
+    out = oracle.plain_denoise(cam, cam, cfg, g, prev_g, gi, hist)
+    ids = np.array([np.float32(k) / np.float32(10) for k in range(11)], np.float32)
+    blk = f32(g["block"].astype(np.float32) / np.float32(255))
+    iv, ip = f32(cam.inv_view), f32(cam.inv_proj)   # kept alive across the calls
+    sh, cocg = out["temporal"]["sh"], out["temporal"]["cocg"]
+    for it, want in enumerate(out["atrous"]):
+        o_sh, o_cc = np.zeros((H, W, 4), np.float32), np.zeros((H, W, 2), np.float32)
+        ins = [f32(g["t"]), ids[g["face"]], blk, f32(out["variance"]), f32(sh), f32(cocg)]
+        ref.glslref_plain_atrous(iv.ctypes.data, ip.ctypes.data, W, H, (12, 8, 4, 2, 1)[it],
+                                 *[a.ctypes.data for a in ins], o_sh.ctypes.data, o_cc.ctypes.data)
+        assert same(o_sh, want["sh"]) and same(o_cc, want["cocg"]), it
+        sh, cocg = want["sh"], want["cocg"]
