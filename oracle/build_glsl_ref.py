@@ -11,7 +11,8 @@ reference tree is absent; the tests that use the library skip then.
 For each shader the top-level items (preprocessor lines, declarations,
 structs, interface blocks, functions) are split, the functions reachable from
 the entry point are kept, and functions on paths the drivers never take (the
-alpha-tested traversal with its texture sampling) become stubs that abort.
+alpha-tested traversal with its texture sampling, the shadow-temporal
+helpers of the temporal filter) become stubs that abort.
 The rewrites keep the shader's own arithmetic and operation order:
   * parameter qualifiers: `in T x` -> `T x`, `out T x` / `inout T x` -> `T& x`;
   * `uniform`, `in`, `out` and `layout(...)` globals -> namespace variables,
@@ -52,6 +53,7 @@ UNITS = [
     ("atrous", "SVGF/SpatialFilter.glsl", "main", ()),
     ("temporal", "SVGF/TemporalFilter.glsl", "main", ()),
     ("plain_atrous", "AtrousSpatialFilter.glsl", "main", ()),
+    ("plain_temporal", "TemporalFilter.glsl", "main", ("GetShadowSpatial", "ClipShadow")),
 ]
 WORLD_DEFINES = ("WORLD_SIZE_X", "WORLD_SIZE_Y", "WORLD_SIZE_Z")
 KEYWORDS = {"if", "else", "for", "while", "return", "const", "void", "float", "int", "bool", "true", "false",

@@ -37,6 +37,7 @@ struct vec2 {
     explicit vec2(const vec4& v);
     float& operator[](int i) { return i == 0 ? x : y; }
     float operator[](int i) const { return i == 0 ? x : y; }
+    vec2 xy() const { return *this; }
 };
 
 struct vec3 {
@@ -98,6 +99,7 @@ struct ivec2 {
     int& operator[](int i) { return i == 0 ? x : y; }
     int operator[](int i) const { return i == 0 ? x : y; }
     operator vec2() const { return vec2((float)x, (float)y); }   // GLSL's implicit int -> float
+    ivec2 xy() const { return *this; }
 };
 inline ivec2 operator+(const ivec2& a, const ivec2& b) { return ivec2(a.x + b.x, a.y + b.y); }
 inline ivec2 operator%(const ivec2& a, const ivec2& b) { return ivec2(a.x % b.x, a.y % b.y); }
@@ -219,6 +221,7 @@ inline vec4 clamp(const vec4& v, float lo, float hi) {
 }
 inline vec2 sin(const vec2& v) { return vec2(sin(v.x), sin(v.y)); }
 inline float dot(const vec2& a, const vec2& b) { return a.x * b.x + a.y * b.y; }
+inline float length(const vec2& a) { return sqrt(dot(a, a)); }
 inline float dot(const vec3& a, const vec3& b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
 inline float length(const vec3& a) { return sqrt(dot(a, a)); }
 inline float distance(const vec3& a, const vec3& b) { return length(a - b); }

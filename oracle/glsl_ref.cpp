@@ -306,4 +306,44 @@ void glslref_plain_atrous(const float* inv_view, const float* inv_proj, int W, i
         }
 }
 
+// The non-SVGF temporal pass (Core/Pipeline.cpp:2618-2680, TemporalFilter.glsl
+// main in its diffuse mode: u_DiffuseTemporal on, u_ShadowTemporal off,
+// u_MinimumMix 0, u_MaximumMix 0.96) over a W x H grid. t / prev_t: the
+// current and previous hit distances; sh (4 channels) / cocg (2): this
+// frame's GI, prev_sh / prev_cocg the previous output, sampled at the
+// reprojected coordinates. Out: o_Color (SH) and o_CoCg per texel.
+void glslref_plain_temporal(const float* inv_view, const float* inv_proj, const float* prev_view,
+                            const float* prev_proj, int W, int H, const float* t, const float* prev_t,
+                            const float* sh, const float* cocg, const float* prev_sh, const float* prev_cocg,
+                            float* o_sh, float* o_cocg) {
+    static const float zero[1] = {0.0f};
+    plain_temporal::u_CurrentColorTexture = sampler2D{sh, W, H, 4};
+    plain_temporal::u_CurrentPositionTexture = sampler2D{t, W, H, 1};
+    plain_temporal::u_PreviousColorTexture = sampler2D{prev_sh, W, H, 4, false, false};
+    plain_temporal::u_PreviousFramePositionTexture = sampler2D{prev_t, W, H, 1, false, false};
+    plain_temporal::u_CurrentSH = sampler2D{cocg, W, H, 2};
+    plain_temporal::u_PreviousSH = sampler2D{prev_cocg, W, H, 2, false, false};
+    plain_temporal::u_ShadowTransversals = sampler2D{zero, 1, 1, 1};
+    plain_temporal::u_InverseView = mat_from(inv_view);
+    plain_temporal::u_InverseProjection = mat_from(inv_proj);
+    plain_temporal::u_PrevView = mat_from(prev_view);
+    plain_temporal::u_PrevProjection = mat_from(prev_proj);
+    plain_temporal::u_MinimumMix = 0.0f;
+    plain_temporal::u_MaximumMix = 0.96f;
+    plain_temporal::u_DiffuseTemporal = true;
+    plain_temporal::u_ShadowTemporal = false;
+    plain_temporal::u_ShouldFilterShadows = false;
+    plain_temporal::v_RayOrigin = vec3(inv_view[12], inv_view[13], inv_view[14]);
+    for (int j = 0; j < H; j++)
+        for (int i = 0; i < W; i++) {
+            plain_temporal::v_TexCoords = vec2(((float)i + 0.5f) / (float)W, ((float)j + 0.5f) / (float)H);
+            plain_temporal::gl_FragCoord = vec4((float)i + 0.5f, (float)j + 0.5f, 0.0f, 1.0f);
+            plain_temporal::main();
+            const size_t px = (size_t)j * W + i;
+            for (int c = 0; c < 4; c++) o_sh[px * 4 + c] = plain_temporal::o_Color[c];
+            o_cocg[px * 2] = plain_temporal::o_CoCg.x;
+            o_cocg[px * 2 + 1] = plain_temporal::o_CoCg.y;
+        }
+}
+
 }  // extern "C"

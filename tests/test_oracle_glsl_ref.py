@@ -2,8 +2,8 @@
 
 oracle/build_glsl_ref.py takes ManhattanDistance{X,Y,Z}.comp,
 InitialRayTraceFrag.glsl, ShadowRayTraceFrag.glsl, Spatial3x3Initial.glsl and
-SVGF/{TemporalFilter,VarianceEstimate,SpatialFilter}.glsl and
-AtrousSpatialFilter.glsl from the reference tree, rewrites only GLSL syntax
+SVGF/{TemporalFilter,VarianceEstimate,SpatialFilter}.glsl, TemporalFilter.glsl
+and AtrousSpatialFilter.glsl from the reference tree, rewrites only GLSL syntax
 (qualifiers, swizzles, literals, interface variables) and compiles them with
 GLSL's types and built-ins from oracle/glsl_compat.h into
 oracle/_ref/libglsl_ref.so; oracle/glsl_ref.cpp runs them as the
@@ -12,7 +12,7 @@ inputs, every output must be bit-identical: the distance field of every
 world, the primary G-buffer (hit distance, face id, block id), the sun
 shadow, the pre-temporal 3x3 filter, the temporal pass over a moving camera,
 the variance estimate and the five a-trous iterations of every texel, and
-the five iterations of the non-SVGF denoiser's a-trous filter. That pins the oracle's restatement of those passes to the reference's
+the non-SVGF denoiser's temporal pass and five a-trous iterations. That pins the oracle's restatement of those passes to the reference's
 own code; the built-ins (normalize, texel fetch of R8 data, matrix times
 vector) are the conventions the oracle fixes for them. Skipped where the
 reference tree is absent (the GPU machines).
@@ -41,6 +41,7 @@ def ref():
     L.glslref_atrous.argtypes = [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float] + [P] * 11
     L.glslref_temporal.argtypes = [P] * 4 + [C.c_int] * 3 + [P] * 18
     L.glslref_plain_atrous.argtypes = [P] * 2 + [C.c_int] * 3 + [P] * 8
+    L.glslref_plain_temporal.argtypes = [P] * 4 + [C.c_int] * 2 + [P] * 8
     return L
 
 
@@ -293,3 +294,34 @@ def test_plain_atrous_iterations_equal_the_reference_shader(ref, seed):
                                  *[a.ctypes.data for a in ins], o_sh.ctypes.data, o_cc.ctypes.data)
         assert same(o_sh, want["sh"]) and same(o_cc, want["cocg"]), it
         sh, cocg = want["sh"], want["cocg"]
+
+
+@pytest.mark.parametrize("seed", [1, 5])
+def test_plain_temporal_pass_equals_the_reference_shader(ref, seed):
+    """The non-SVGF temporal pass (TemporalFilter.glsl in its diffuse mode)
+    over an empty history, a moved camera and a repeated one."""
+    X, Y, Z = 64, 64, 64
+    W, H = 96, 64
+    vox = inputs.generate_world(X, Y, Z, seed=seed)
+    world = oracle.World(vox, oracle.build_df(vox), inputs.generate_block_table(100, seed=seed))
+    yaw, pitch = inputs.seeded_pose(seed)
+    cams = [inputs.camera_from_pose((X / 2, 58.0, Z / 2), yaw, pitch, 90.0, W / H),
+            inputs.camera_from_pose((X / 2 + 0.7, 58.2, Z / 2 - 0.4), yaw + 2.0, pitch + 1.0, 90.0, W / H)]
+    cfg = inputs.default_config(width=W, height=H, primary_max_steps=256, denoiser=1)
+    prev_g, hist = oracle.empty_history(H, W)
+    prev_cam = cams[0]
+    blended = 0
+    for fi, cam in enumerate(cams + [cams[1]]):
+        frame = inputs.default_frame(frame_index=fi, seed=5)
+        g = oracle.trace_primary(world, cam, cfg)
+        gi = oracle.trace_diffuse(world, cam, cfg, frame, g["t"], g["face"])
+        want = oracle.plain_denoise(cam, prev_cam, cfg, g, prev_g, gi, hist)["temporal"]
+        o_sh, o_cc = np.zeros((H, W, 4), np.float32), np.zeros((H, W, 2), np.float32)
+        mats = [f32(cam.inv_view), f32(cam.inv_proj), f32(prev_cam.view), f32(prev_cam.proj)]
+        ins = [f32(g["t"]), f32(prev_g["t"]), f32(gi["sh"]), f32(gi["cocg"]), f32(hist["sh"]), f32(hist["cocg"])]
+        ref.glslref_plain_temporal(*[m.ctypes.data for m in mats], W, H, *[a.ctypes.data for a in ins],
+                                   o_sh.ctypes.data, o_cc.ctypes.data)
+        assert same(o_sh, want["sh"]) and same(o_cc, want["cocg"]), fi
+        blended += int((np.abs(f32(want["sh"]) - f32(gi["sh"])).sum(-1) > 0).sum())
+        prev_g, hist, prev_cam = {k: g[k] for k in ("t", "face", "block")}, want, cam
+    assert blended > 1000
