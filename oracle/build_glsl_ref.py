@@ -22,7 +22,8 @@ The rewrites keep the shader's own arithmetic and operation order:
   * swizzles `.xyzw` / `.xyz` / `.xy` (and `.rgba` / `.rgb` / `.rg`) -> member
     calls, single colour components `.r .g .b .a` -> `.x .y .z .w`, and
     `v.xyz /= s;` -> the three component divisions;
-  * array constructors `T[](a, b, ...)` -> brace lists, `T[n] name` -> `T name[n]`;
+  * array constructors `T[](a, b, ...)` -> brace lists, `T[n] name` -> `T name[n]`,
+    a function returning `float[6]` -> the compat header's array type;
   * floating literals without a suffix -> float literals (GLSL's float).
 
     python oracle/build_glsl_ref.py
@@ -54,6 +55,9 @@ UNITS = [
     ("temporal", "SVGF/TemporalFilter.glsl", "main", ()),
     ("plain_atrous", "AtrousSpatialFilter.glsl", "main", ()),
     ("plain_temporal", "TemporalFilter.glsl", "main", ("GetShadowSpatial", "ClipShadow")),
+    # the SH / YCoCg encoding of the diffuse trace and its decoding in the colour pass
+    ("sh_encode", "DiffuseRayTraceFrag.glsl", "IrridianceToSH", ()),
+    ("sh_decode", "ColorPassFrag.glsl", "SHToIrridiance", ()),
 ]
 WORLD_DEFINES = ("WORLD_SIZE_X", "WORLD_SIZE_Y", "WORLD_SIZE_Z")
 KEYWORDS = {"if", "else", "for", "while", "return", "const", "void", "float", "int", "bool", "true", "false",
@@ -188,7 +192,9 @@ def rewrite_item(kind: str, item: str, stub: bool = False) -> str:
 
 
 def translate(ns: str, path: Path, entry: str, stubs) -> str:
-    items = split_items(strip_comments(path.read_text()))
+    # functions returning arrays (`float[6] F(...)`) return the compat header's array type
+    items = [re.sub(r"^(\w+)\s*\[(\d+)\]\s+(\w+\s*\()", r"arr_\1_\2 \3", t)
+             for t in split_items(strip_comments(path.read_text()))]
     cls = [classify(t) for t in items]
     by_name = {}
     for k, (kind, names) in enumerate(cls):

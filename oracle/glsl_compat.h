@@ -230,6 +230,14 @@ inline vec3 cross(const vec3& a, const vec3& b) {
     return vec3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 
+// A function's `float[6]` return value (GLSL returns arrays by value).
+struct arr_float_6 {
+    float v[6];
+    arr_float_6(const float* p) { for (int i = 0; i < 6; i++) v[i] = p[i]; }   // NOLINT: GLSL's array copy
+    float operator[](int i) const { return v[i]; }
+};
+inline vec3 max(const vec3& a, const vec3& b) { return vec3(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z)); }
+
 // ---- textures and images (unsigned normalised bytes, x fastest) ----
 struct sampler3D {
     const uint8_t* data = nullptr;

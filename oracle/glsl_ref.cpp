@@ -346,4 +346,25 @@ void glslref_plain_temporal(const float* inv_view, const float* inv_proj, const 
         }
 }
 
+// The diffuse trace's IrridianceToSH (DiffuseRayTraceFrag.glsl:766-784) and
+// the colour pass's SHToIrridiance (ColorPassFrag.glsl:357-368) over n items.
+// op 0: in = radiance (3) and direction (3) per item, out = SH (4) and CoCg
+// (2); op 1: in = SH (4), CoCg (2) and normal (3), out = irradiance (3).
+void glslref_sh_codec(int op, int n, const float* in, float* out) {
+    for (int k = 0; k < n; k++) {
+        if (op == 0) {
+            const float* a = in + 6 * k;
+            const arr_float_6 r = sh_encode::IrridianceToSH(vec3(a[0], a[1], a[2]), vec3(a[3], a[4], a[5]));
+            for (int i = 0; i < 6; i++) out[6 * k + i] = r[i];
+        } else {
+            const float* a = in + 9 * k;
+            const vec3 r = sh_decode::SHToIrridiance(vec4(a[0], a[1], a[2], a[3]), vec2(a[4], a[5]),
+                                                     vec3(a[6], a[7], a[8]));
+            out[3 * k] = r.x;
+            out[3 * k + 1] = r.y;
+            out[3 * k + 2] = r.z;
+        }
+    }
+}
+
 }  // extern "C"

@@ -2845,3 +2845,19 @@ bool alpha_stop(v3 p, v3 n, int type, v3 cam, float k, int flip_x, int lod_bias)
     return o[3] > 0.975f;
 }
 }  // namespace
+
+// Test hook: irradiance_to_sh / sh_to_irradiance over n items (vpt_oracle.h).
+extern "C" void vpto_sh_codec(int op, int n, const float* in, float* out) {
+    for (int k = 0; k < n; k++) {
+        if (op == 0) {
+            const float* a = in + 6 * k;
+            irradiance_to_sh(mk3(a[0], a[1], a[2]), mk3(a[3], a[4], a[5]), out + 6 * k, out + 6 * k + 4);
+        } else {
+            const float* a = in + 9 * k;
+            const v3 r = sh_to_irradiance(a, a + 4, mk3(a[6], a[7], a[8]));
+            out[3 * k] = r.x;
+            out[3 * k + 1] = r.y;
+            out[3 * k + 2] = r.z;
+        }
+    }
+}

@@ -158,6 +158,11 @@ void vpto_spatial_initial(const vpto_camera* cam, const vpto_params* p,
 /* The oracle's vector builtins (dot, cross, length, normalize, mix, mat4 *
  * vec4) over n inputs, for the comparison with the reference's glm. */
 void vpto_vecmath(int op, const float* a, const float* b, const float* c, float* out, int n);
+/* The SH / YCoCg encoding of a diffuse sample (op 0: radiance (3) and
+ * direction (3) per item in, SH (4) and CoCg (2) out) and its decoding for a
+ * normal (op 1: SH (4), CoCg (2) and normal (3) in, irradiance (3) out), over
+ * n items, for the comparison with the reference's shader functions. */
+void vpto_sh_codec(int op, int n, const float* in, float* out);
 /* Inputs x (bit patterns in [lo, hi)) for which q = x * RN(1/c) corrected once
    by the exact remainder, fma(fma(-q, c, x), RN(1/c), q), differs from x / c. */
 uint64_t vpto_check_div_const(float c, uint32_t lo, uint32_t hi);

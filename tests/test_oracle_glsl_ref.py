@@ -12,7 +12,9 @@ inputs, every output must be bit-identical: the distance field of every
 world, the primary G-buffer (hit distance, face id, block id), the sun
 shadow, the pre-temporal 3x3 filter, the temporal pass over a moving camera,
 the variance estimate and the five a-trous iterations of every texel, and
-the non-SVGF denoiser's temporal pass and five a-trous iterations. That pins the oracle's restatement of those passes to the reference's
+the non-SVGF denoiser's temporal pass and five a-trous iterations; and the
+SH / YCoCg encoding of a diffuse sample (DiffuseRayTraceFrag.glsl) and its
+decoding in the colour pass (ColorPassFrag.glsl), function by function. That pins the oracle's restatement of those passes to the reference's
 own code; the built-ins (normalize, texel fetch of R8 data, matrix times
 vector) are the conventions the oracle fixes for them. Skipped where the
 reference tree is absent (the GPU machines).
@@ -42,6 +44,7 @@ def ref():
     L.glslref_temporal.argtypes = [P] * 4 + [C.c_int] * 3 + [P] * 18
     L.glslref_plain_atrous.argtypes = [P] * 2 + [C.c_int] * 3 + [P] * 8
     L.glslref_plain_temporal.argtypes = [P] * 4 + [C.c_int] * 2 + [P] * 8
+    L.glslref_sh_codec.argtypes = [C.c_int, C.c_int, P, P]
     return L
 
 
@@ -325,3 +328,25 @@ def test_plain_temporal_pass_equals_the_reference_shader(ref, seed):
         blended += int((np.abs(f32(want["sh"]) - f32(gi["sh"])).sum(-1) > 0).sum())
         prev_g, hist, prev_cam = {k: g[k] for k in ("t", "face", "block")}, want, cam
     assert blended > 1000
+
+
+def test_sh_encoding_and_decoding_equal_the_reference_shaders(ref):
+    """IrridianceToSH and SHToIrridiance on 200,000 random radiances (four
+    decades), unit directions and normals, against the oracle's own."""
+    lib = oracle.lib()
+    lib.vpto_sh_codec.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    rng = np.random.default_rng(4)
+    n = 200000
+    rad = rng.random((n, 3)) * rng.choice([0.01, 1.0, 8.0, 100.0], (n, 1))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    enc_in = f32(np.concatenate([rad, d], 1))
+    got, want = np.zeros((n, 6), np.float32), np.zeros((n, 6), np.float32)
+    ref.glslref_sh_codec(0, n, enc_in.ctypes.data, got.ctypes.data)
+    lib.vpto_sh_codec(0, n, enc_in.ctypes.data, want.ctypes.data)
+    assert same(got, want)
+    dec_in = f32(np.concatenate([want, rng.normal(size=(n, 3))], 1))
+    got3, want3 = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
+    ref.glslref_sh_codec(1, n, dec_in.ctypes.data, got3.ctypes.data)
+    lib.vpto_sh_codec(1, n, dec_in.ctypes.data, want3.ctypes.data)
+    assert same(got3, want3)
