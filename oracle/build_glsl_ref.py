@@ -58,6 +58,8 @@ UNITS = [
     # the SH / YCoCg encoding of the diffuse trace and its decoding in the colour pass
     ("sh_encode", "DiffuseRayTraceFrag.glsl", "IrridianceToSH", ()),
     ("sh_decode", "ColorPassFrag.glsl", "SHToIrridiance", ()),
+    # the Hammon diffuse BRDF of the bounce rays
+    ("brdf", "DiffuseRayTraceFrag.glsl", "DiffuseRayBRDF", ()),
 ]
 WORLD_DEFINES = ("WORLD_SIZE_X", "WORLD_SIZE_Y", "WORLD_SIZE_Z")
 KEYWORDS = {"if", "else", "for", "while", "return", "const", "void", "float", "int", "bool", "true", "false",
@@ -222,7 +224,7 @@ def translate(ns: str, path: Path, entry: str, stubs) -> str:
                 continue
             if any(re.match(rf"#define\s+{d}\b", item) for d in WORLD_DEFINES):
                 continue
-            out.append(item)
+            out.append(rewrite_expr(item) if item.startswith("#define") else item)
         elif k in keep and kind != "drop":
             out.append(rewrite_item(kind, item, stub=kind == "func" and names[0] in stubs))
     out.append(f"}}  // namespace {ns}")

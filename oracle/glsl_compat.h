@@ -198,6 +198,7 @@ inline float sin(float x) { return vpto::dm_sin(x); }
 inline float cos(float x) { return vpto::dm_cos(x); }
 inline float tan(float x) { return vpto::dm_sin(x) / vpto::dm_cos(x); }
 inline float radians(float d) { return d * 0.01745329251994329577f; }
+inline float rcp(float x) { return 1.0f / x; }   // accepted by the reference's GLSL compiler; 1 / x
 inline float mix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
 inline float mod(float x, float y) { return x - y * floor(x / y); }
 

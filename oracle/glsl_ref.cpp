@@ -367,4 +367,14 @@ void glslref_sh_codec(int op, int n, const float* in, float* out) {
     }
 }
 
+// DiffuseRayBRDF (DiffuseRayTraceFrag.glsl:527-531, DiffuseHammon :1311-1332)
+// over n items: in = normal (3), incident (3), direction (3), roughness per
+// item; out = the BRDF's first component.
+void glslref_diffuse_brdf(int n, const float* in, float* out) {
+    for (int k = 0; k < n; k++) {
+        const float* a = in + 10 * k;
+        out[k] = brdf::DiffuseRayBRDF(vec3(a[0], a[1], a[2]), vec3(a[3], a[4], a[5]), vec3(a[6], a[7], a[8]), a[9]).x;
+    }
+}
+
 }  // extern "C"

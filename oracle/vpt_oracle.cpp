@@ -2861,3 +2861,11 @@ extern "C" void vpto_sh_codec(int op, int n, const float* in, float* out) {
         }
     }
 }
+
+// Test hook: DiffuseRayBRDF = diffuse_hammon(n, -incident, d, roughness) over n items.
+extern "C" void vpto_diffuse_brdf(int n, const float* in, float* out) {
+    for (int k = 0; k < n; k++) {
+        const float* a = in + 10 * k;
+        out[k] = diffuse_hammon(mk3(a[0], a[1], a[2]), neg(mk3(a[3], a[4], a[5])), mk3(a[6], a[7], a[8]), a[9]);
+    }
+}

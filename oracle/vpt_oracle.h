@@ -163,6 +163,9 @@ void vpto_vecmath(int op, const float* a, const float* b, const float* c, float*
  * normal (op 1: SH (4), CoCg (2) and normal (3) in, irradiance (3) out), over
  * n items, for the comparison with the reference's shader functions. */
 void vpto_sh_codec(int op, int n, const float* in, float* out);
+/* The Hammon diffuse BRDF of a bounce ray over n items (normal (3), incident
+ * direction (3), new direction (3), roughness in; DiffuseRayBRDF's value out). */
+void vpto_diffuse_brdf(int n, const float* in, float* out);
 /* Inputs x (bit patterns in [lo, hi)) for which q = x * RN(1/c) corrected once
    by the exact remainder, fma(fma(-q, c, x), RN(1/c), q), differs from x / c. */
 uint64_t vpto_check_div_const(float c, uint32_t lo, uint32_t hi);

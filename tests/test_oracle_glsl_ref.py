@@ -13,8 +13,9 @@ world, the primary G-buffer (hit distance, face id, block id), the sun
 shadow, the pre-temporal 3x3 filter, the temporal pass over a moving camera,
 the variance estimate and the five a-trous iterations of every texel, and
 the non-SVGF denoiser's temporal pass and five a-trous iterations; and the
-SH / YCoCg encoding of a diffuse sample (DiffuseRayTraceFrag.glsl) and its
-decoding in the colour pass (ColorPassFrag.glsl), function by function. That pins the oracle's restatement of those passes to the reference's
+SH / YCoCg encoding of a diffuse sample and the bounce rays' Hammon BRDF
+(DiffuseRayTraceFrag.glsl) and the decoding in the colour pass
+(ColorPassFrag.glsl), function by function. That pins the oracle's restatement of those passes to the reference's
 own code; the built-ins (normalize, texel fetch of R8 data, matrix times
 vector) are the conventions the oracle fixes for them. Skipped where the
 reference tree is absent (the GPU machines).
@@ -45,6 +46,7 @@ def ref():
     L.glslref_plain_atrous.argtypes = [P] * 2 + [C.c_int] * 3 + [P] * 8
     L.glslref_plain_temporal.argtypes = [P] * 4 + [C.c_int] * 2 + [P] * 8
     L.glslref_sh_codec.argtypes = [C.c_int, C.c_int, P, P]
+    L.glslref_diffuse_brdf.argtypes = [C.c_int, P, P]
     return L
 
 
@@ -350,3 +352,25 @@ def test_sh_encoding_and_decoding_equal_the_reference_shaders(ref):
     ref.glslref_sh_codec(1, n, dec_in.ctypes.data, got3.ctypes.data)
     lib.vpto_sh_codec(1, n, dec_in.ctypes.data, want3.ctypes.data)
     assert same(got3, want3)
+
+
+def test_bounce_brdf_equals_the_reference_shader(ref):
+    """DiffuseRayBRDF / DiffuseHammon on 200,000 random normals, incident and
+    new directions and roughnesses (0 and 1 included), against the oracle's."""
+    lib = oracle.lib()
+    lib.vpto_diffuse_brdf.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+    rng = np.random.default_rng(6)
+    n = 200000
+
+    def unit():
+        v = rng.normal(size=(n, 3))
+        return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+    inp = np.concatenate([unit(), unit(), unit(), rng.random((n, 1))], 1).astype(np.float32)
+    inp[::5, 9], inp[1::5, 9] = 0.0, 1.0
+    inp = f32(inp)
+    got, want = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    ref.glslref_diffuse_brdf(n, inp.ctypes.data, got.ctypes.data)
+    lib.vpto_diffuse_brdf(n, inp.ctypes.data, want.ctypes.data)
+    assert same(got, want)
+    assert (want > 0).sum() > n // 4
